@@ -1,0 +1,61 @@
+"""ctypes binding of libflexigpu.so (C ABI in include/flexi_gpu.h)."""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libflexigpu.so")
+_lib = None
+
+
+class FgConfig(ctypes.Structure):
+    _fields_ = [("N", ctypes.c_int), ("NodeType", ctypes.c_int), ("Riemann", ctypes.c_int), ("RiemannBC", ctypes.c_int),
+                ("Lifting", ctypes.c_int), ("doWeakLifting", ctypes.c_int), ("doConservativeLifting", ctypes.c_int),
+                ("SplitDG", ctypes.c_int), ("etaBR2", ctypes.c_double), ("etaBR2_wall", ctypes.c_double), ("kappa", ctypes.c_double),
+                ("R", ctypes.c_double), ("Pr", ctypes.c_double), ("mu0", ctypes.c_double), ("CFLScale", ctypes.c_double),
+                ("DFLScale", ctypes.c_double), ("doTCSource", ctypes.c_int), ("dpdx", ctypes.c_double), ("TimeDiscMethod", ctypes.c_int)]
+
+
+EXPORTS = ["fg_config_default", "fg_config_from_ini", "fg_create", "fg_destroy", "fg_last_error", "fg_build_mesh", "fg_set_mesh",
+           "fg_set_instance_mu0", "fg_get_elem_xgp", "fg_get_sizes", "fg_get_mesh_array", "fg_get_side_to_elem", "fg_set_state",
+           "fg_get_state", "fg_state_device_ptr", "fg_time_derivative", "fg_calc_timestep", "fg_timestep_lserkw2", "fg_run",
+           "fg_get_gradients", "fg_get_stream", "fg_launch_count", "fg_probe_fp64"]
+
+
+def load(path=None):
+    """Loads the library; raises if it has not been built (there is no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError(f"libflexigpu.so not found at {path}; run __graft_entry__.build() (no CPU fallback exists)")
+    L = ctypes.CDLL(path)
+    P, I, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    PI = ctypes.POINTER(ctypes.c_int)
+    L.fg_config_default.argtypes = [ctypes.POINTER(FgConfig)]
+    L.fg_config_from_ini.argtypes = [ctypes.c_char_p, ctypes.POINTER(FgConfig)]
+    L.fg_create.argtypes = [ctypes.POINTER(FgConfig), ctypes.POINTER(P)]
+    L.fg_destroy.argtypes = [P]
+    L.fg_last_error.argtypes = [P]
+    L.fg_last_error.restype = ctypes.c_char_p
+    L.fg_build_mesh.argtypes = [P, I, I, P, P, I, P, I, P, P]
+    L.fg_set_mesh.argtypes = [P, I, I, I, P, P, P, I, P, I, P, P, P, P, P, P, P, P, P]
+    L.fg_set_instance_mu0.argtypes = [P, I, P]
+    L.fg_get_elem_xgp.argtypes = [P, P]
+    L.fg_get_sizes.argtypes = [P, P]
+    L.fg_get_mesh_array.argtypes = [P, I, P]
+    L.fg_get_side_to_elem.argtypes = [P, P]
+    L.fg_set_state.argtypes = [P, P]
+    L.fg_get_state.argtypes = [P, P]
+    L.fg_state_device_ptr.argtypes = [P, ctypes.POINTER(P)]
+    L.fg_time_derivative.argtypes = [P, D, P]
+    L.fg_calc_timestep.argtypes = [P, P, PI]
+    L.fg_timestep_lserkw2.argtypes = [P, ctypes.POINTER(D), D]
+    L.fg_run.argtypes = [P, I, P]
+    L.fg_get_gradients.argtypes = [P, P, P, P]
+    L.fg_get_stream.argtypes = [P, ctypes.POINTER(P)]
+    L.fg_launch_count.argtypes = [P]
+    L.fg_launch_count.restype = ctypes.c_longlong
+    L.fg_probe_fp64.argtypes = [ctypes.POINTER(D)]
+    _lib = L
+    return L

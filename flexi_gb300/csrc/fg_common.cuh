@@ -1,0 +1,305 @@
+// flexi_gb300 -- device data layout and point-wise physics of the DGSEM Navier-Stokes operator.
+//
+// Everything is FP64. GB300's FP64 pipe (measured 0.50 T instr/s, 1.0 TFLOP/s FMA) is ~70x slower than
+// its FP32 pipe and ~30x below what this operator needs to be HBM-bound, so the kernels are organised to
+// minimise FP64 instructions: reciprocals are formed once and reused, constant factors are folded, face
+// values are computed once per side and read by both neighbours, and integer/shared-memory work (which
+// is essentially free next to FP64) replaces recomputation wherever possible.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define FG_MAXN 10  // maximum number of nodes per direction (N <= 9)
+
+namespace fg {
+
+// local side ids of FLEXI (src/flexi.h:90-95)
+enum { ZETA_MINUS = 1, ETA_MINUS = 2, XI_PLUS = 3, ETA_PLUS = 4, XI_MINUS = 5, ZETA_PLUS = 6 };
+enum { RIEMANN_LF = 1, RIEMANN_HLLC = 2, RIEMANN_ROE = 3, RIEMANN_ROEENTROPYFIX = 33 };
+enum { NODE_GAUSS = 1, NODE_GL = 2 };
+
+// face state fields, stored [side][field][p + n*q] for the master and for the slave (in master orientation)
+enum { FS_RHO = 0, FS_E, FS_U, FS_V, FS_W, FS_P, FS_T, FS_SRHO, FS_NF };
+// volume primitive fields, stored [elem][field][node]
+enum { VP_SRHO = 0, VP_U, VP_V, VP_W, VP_P, VP_T, VP_NF };
+// face geometry, stored [side][field][p + n*q]
+enum { FG_NX = 0, FG_NY, FG_NZ, FG_T1X, FG_T1Y, FG_T1Z, FG_T2X, FG_T2Y, FG_T2Z, FG_SURF, FG_NF };
+
+// Operator constants passed by value (they live in the kernel-parameter constant bank).
+struct Basis {
+  int N, n, nodeType, splitDG;
+  int riemann, riemannBC, lifting, weakLifting;
+  double D_T[FG_MAXN * FG_MAXN];     // D_T[l*n+i] = D(i,l)
+  double Dhat_T[FG_MAXN * FG_MAXN];  // Dhat_T[l*n+i] = D_Hat_T(l,i)
+  double DVS[FG_MAXN * FG_MAXN];     // DVS[l*n+i] = DVolSurf(l,i)
+  double Lm[FG_MAXN], Lp[FG_MAXN], LhM[FG_MAXN], LhP[FG_MAXN];
+  double kappa, kappaM1, sKappaM1, Rgas, sR, lambdaFac, etaBR2, etaBR2_wall;
+  double kappaFac, sKappaP1;
+};
+
+// Device arrays of one solver handle (all sizes in units of doubles / ints).
+struct Dev {
+  int nElems, nSides, nBCSides, nInst;
+  // elements
+  double* U;       // [e][5][n3]
+  double* Ut;      // [e][5][n3] time derivative (RK register source)
+  double* Ut_tmp;  // [e][5][n3] LSERK register
+  double* prim;    // [e][VP_NF][n3]
+  double* grad;    // [e][12][n3]: index 4*dir + var, var = (u,v,w,T)
+  double* metr;    // [e][9][n3]: Metrics_fTilde(3), Metrics_gTilde(3), Metrics_hTilde(3)
+  double* sJ;      // [e][n3]
+  int* elemSide;   // [e][6]: 8*sideID + flip (flip 0 => this element is the master)
+  int* elemInst;   // [e]
+  // sides
+  double* faceM;   // [s][FS_NF][n2]
+  double* faceS;   // [s][FS_NF][n2]
+  double* gradM;   // [s][12][n2]
+  double* gradS;   // [s][12][n2]
+  double* geo;     // [s][FG_NF][n2]
+  double* flux;    // [s][5][n2] numerical flux times SurfElem, master orientation
+  int* sideElem;   // [s][4]: master elem, master locSide, slave elem (-1: BC side), 8*slave locSide + flip
+  int* sideInst;   // [s]
+  int* bcType;     // [nBCSides]
+  double* bcTwall; // [nBCSides]
+  // per instance
+  double* mu0;     // [nInst]
+  double* dt;      // [nInst]
+  double* bulkVel; // [nInst]
+  double* dpdx;    // [nInst] (0 when no body force)
+  int* err;        // [1] sticky error word
+};
+
+// ------------------------------------------------------------------------------------------------------
+// orientation maps (mappings.f90: Flip_S2M, CGNS_SideToVol2) -- integer work, free next to FP64
+// ------------------------------------------------------------------------------------------------------
+__host__ __device__ inline void flip_s2m(int N, int p, int q, int flip, int& a, int& b) {
+  switch (flip) {
+    case 0: a = p; b = q; break;
+    case 1: a = q; b = p; break;
+    case 2: a = N - p; b = q; break;
+    case 3: a = N - q; b = N - p; break;
+    default: a = p; b = N - q; break;
+  }
+}
+__host__ __device__ inline void side_to_vol2(int N, int p, int q, int flip, int ls, int& a, int& b) {
+  int x, y;
+  flip_s2m(N, p, q, flip, x, y);
+  switch (ls) {
+    case XI_MINUS: a = y; b = x; break;
+    case XI_PLUS: a = x; b = y; break;
+    case ETA_MINUS: a = x; b = y; break;
+    case ETA_PLUS: a = N - x; b = y; break;
+    case ZETA_MINUS: a = y; b = x; break;
+    default: a = x; b = y; break;
+  }
+}
+// node index of face coordinate (a,b) at normal distance l counted in volume index order
+__host__ __device__ inline int face_node(int ls, int a, int b, int l, int n) {
+  switch (ls) {
+    case XI_MINUS: case XI_PLUS: return l + n * (a + n * b);
+    case ETA_MINUS: case ETA_PLUS: return a + n * (l + n * b);
+    default: return a + n * (b + n * l);
+  }
+}
+__host__ __device__ inline bool side_is_minus(int ls) { return ls == XI_MINUS || ls == ETA_MINUS || ls == ZETA_MINUS; }
+__host__ __device__ inline int side_dir(int ls) {  // 0 xi, 1 eta, 2 zeta
+  return (ls == XI_MINUS || ls == XI_PLUS) ? 0 : ((ls == ETA_MINUS || ls == ETA_PLUS) ? 1 : 2);
+}
+
+// ------------------------------------------------------------------------------------------------------
+// point-wise physics
+// ------------------------------------------------------------------------------------------------------
+// Viscous flux (flux.f90:EvalDiffFlux3D_Point, stored with the minus sign), contracted with a direction
+// vector m: F = m1*f + m2*g + m3*h. g[4*d+v] = d/dx_d of (u,v,w,T). Returns F[1..4] (F[0] = 0).
+__device__ __forceinline__ void visc_flux_dir(double mu, double lam, double u, double v, double w, const double* g,
+                                              double m1, double m2, double m3, double* F) {
+  // tau terms (s43 = 4/3, s23 = 2/3): tau_xx = mu*(4/3 ux - 2/3 (vy + wz)) = mu*(2 ux - 2/3 div)
+  const double div = g[0] + g[5] + g[10];
+  const double mdiv = (2.0 / 3.0) * div;
+  const double txx = mu * (2.0 * g[0] - mdiv);
+  const double tyy = mu * (2.0 * g[5] - mdiv);
+  const double tzz = mu * (2.0 * g[10] - mdiv);
+  const double txy = mu * (g[4] + g[1]);
+  const double txz = mu * (g[8] + g[2]);
+  const double tyz = mu * (g[9] + g[6]);
+  // row of tau contracted with m
+  const double a1 = txx * m1 + txy * m2 + txz * m3;
+  const double a2 = txy * m1 + tyy * m2 + tyz * m3;
+  const double a3 = txz * m1 + tyz * m2 + tzz * m3;
+  const double qn = g[3] * m1 + g[7] * m2 + g[11] * m3;
+  F[1] = -a1;
+  F[2] = -a2;
+  F[3] = -a3;
+  F[4] = -(a1 * u + a2 * v + a3 * w) - lam * qn;
+}
+
+// Rotated extended state (riemann.f90:Riemann_Point): rho, srho, E, p, vn, vt1, vt2.
+struct RotState {
+  double rho, srho, E, p, v1, v2, v3;
+};
+
+// Central split surface flux (splitflux.f90:SplitSurfaceFluxPI / SD) on rotated states.
+__device__ __forceinline__ void split_surface_flux(int splitDG, const RotState& L, const RotState& R, double HL, double HR, double* F) {
+  if (splitDG == 4) {
+    const double rs = L.rho + R.rho, us = L.v1 + R.v1;
+    const double a = rs * us;
+    const double b = 0.125 * a;
+    F[0] = 0.25 * a;
+    F[1] = b * us + 0.5 * (L.p + R.p);
+    F[2] = b * (L.v2 + R.v2);
+    F[3] = b * (L.v3 + R.v3);
+    F[4] = b * (HL + HR);
+  } else {  // SD: 0.5*(F_L+F_R)
+    const double mL = L.rho * L.v1, mR = R.rho * R.v1;
+    F[0] = 0.5 * (mL + mR);
+    F[1] = 0.5 * (mL * L.v1 + L.p + mR * R.v1 + R.p);
+    F[2] = 0.5 * (mL * L.v2 + mR * R.v2);
+    F[3] = 0.5 * (mL * L.v3 + mR * R.v3);
+    F[4] = 0.5 * ((L.E + L.p) * L.v1 + (R.E + R.p) * R.v1);
+  }
+}
+
+__device__ __forceinline__ void euler_flux_1d(const RotState& S, double* F) {
+  const double m = S.rho * S.v1;
+  F[0] = m;
+  F[1] = m * S.v1 + S.p;
+  F[2] = m * S.v2;
+  F[3] = m * S.v3;
+  F[4] = (S.E + S.p) * S.v1;
+}
+
+// Riemann solvers of riemann.f90 (LF :558, HLLC :594, Roe :668, RoeEntropyFix :748) on rotated states.
+// split != 0: central part from the split surface flux (SPLIT_DG builds), as the reference does.
+__device__ __forceinline__ void riemann_rotated(int solver, int splitDG, const Basis& B, const RotState& L, const RotState& R, double* F) {
+  const bool split = splitDG >= 0;
+  const double HL = (L.E + L.p) * L.srho, HR = (R.E + R.p) * R.srho;
+  if (solver == RIEMANN_LF) {
+    const double cL = sqrt(B.kappa * L.p * L.srho), cR = sqrt(B.kappa * R.p * R.srho);
+    const double lmax = fmax(fabs(R.v1), fabs(L.v1)) + fmax(cL, cR);
+    const double dU[5] = {R.rho - L.rho, R.rho * R.v1 - L.rho * L.v1, R.rho * R.v2 - L.rho * L.v2, R.rho * R.v3 - L.rho * L.v3, R.E - L.E};
+    if (!split) {
+      double FL[5], FR[5];
+      euler_flux_1d(L, FL); euler_flux_1d(R, FR);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) F[v] = 0.5 * ((FL[v] + FR[v]) - lmax * dU[v]);
+    } else {
+      split_surface_flux(splitDG, L, R, HL, HR, F);
+      const double h = 0.5 * lmax;
+#pragma unroll
+      for (int v = 0; v < 5; ++v) F[v] = F[v] - h * dU[v];
+    }
+    return;
+  }
+  const double sqL = sqrt(L.rho), sqR = sqrt(R.rho);
+  const double ssq = 1.0 / (sqL + sqR);
+  const double r1v = (sqR * R.v1 + sqL * L.v1) * ssq;
+  const double r2v = (sqR * R.v2 + sqL * L.v2) * ssq;
+  const double r3v = (sqR * R.v3 + sqL * L.v3) * ssq;
+  const double rH = (sqR * HR + sqL * HL) * ssq;
+  const double absVel = r1v * r1v + r2v * r2v + r3v * r3v;
+  const double rc = sqrt(B.kappaM1 * (rH - 0.5 * absVel));
+  if (solver == RIEMANN_HLLC) {
+    double FL[5], FR[5];
+    euler_flux_1d(L, FL); euler_flux_1d(R, FR);
+    const double Ssl = r1v - rc, Ssr = r1v + rc;
+    if (Ssl >= 0.0) {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) F[v] = FL[v];
+    } else if (Ssr <= 0.0) {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) F[v] = FR[v];
+    } else {
+      const double sMuL = Ssl - L.v1, sMuR = Ssr - R.v1;
+      const double mL = L.rho * L.v1, mR = R.rho * R.v1;
+      const double SStar = (R.p - L.p + mL * sMuL - mR * sMuR) / (L.rho * sMuL - R.rho * sMuR);
+      if (Ssl <= 0.0 && SStar >= 0.0) {
+        const double EStar = L.E * L.srho + (SStar - L.v1) * (SStar + L.p * L.srho / sMuL);
+        const double fac = L.rho * sMuL / (Ssl - SStar);
+        const double Us[5] = {fac, fac * SStar, fac * L.v2, fac * L.v3, fac * EStar};
+        const double Uc[5] = {L.rho, mL, L.rho * L.v2, L.rho * L.v3, L.E};
+#pragma unroll
+        for (int v = 0; v < 5; ++v) F[v] = FL[v] + Ssl * (Us[v] - Uc[v]);
+      } else {
+        const double EStar = R.E * R.srho + (SStar - R.v1) * (SStar + R.p * R.srho / sMuR);
+        const double fac = R.rho * sMuR / (Ssr - SStar);
+        const double Us[5] = {fac, fac * SStar, fac * R.v2, fac * R.v3, fac * EStar};
+        const double Uc[5] = {R.rho, mR, R.rho * R.v2, R.rho * R.v3, R.E};
+#pragma unroll
+        for (int v = 0; v < 5; ++v) F[v] = FR[v] + Ssr * (Us[v] - Uc[v]);
+      }
+    }
+    return;
+  }
+  // Roe-type: eigenvalues a, strengths Alpha, eigenvectors r1..r5
+  double a0 = r1v - rc, a1 = r1v, a4 = r1v + rc;
+  double A0, A1, A2, A3, A4;
+  double e0, e1, e4;  // |a| after the optional entropy fix (a1 = a2 = a3)
+  if (solver == RIEMANN_ROE) {
+    const double d0 = R.rho - L.rho;
+    const double d1 = R.rho * R.v1 - L.rho * L.v1;
+    const double d2 = R.rho * R.v2 - L.rho * L.v2;
+    const double d3 = R.rho * R.v3 - L.rho * L.v3;
+    const double d4 = R.E - L.E;
+    A2 = d2 - r2v * d0;
+    A3 = d3 - r3v * d0;
+    const double d5 = d4 - A2 * r2v - A3 * r3v;
+    const double src = 1.0 / rc;
+    A1 = B.kappaM1 * (src * src) * (d0 * (rH - r1v * r1v) - d5 + r1v * d1);
+    A0 = 0.5 * src * (d0 * (r1v + rc) - d1 - rc * A1);
+    A4 = d0 - A0 - A1;
+    e0 = fabs(a0); e1 = fabs(a1); e4 = fabs(a4);
+  } else {  // RoeEntropyFix
+    const double cL = sqrt(B.kappa * L.p * L.srho), cR = sqrt(B.kappa * R.p * R.srho);
+    const double RoeDens = sqL * sqR;
+    const double dr = R.rho - L.rho, du = R.v1 - L.v1, dv = R.v2 - L.v2, dw = R.v3 - L.v3, dp = R.p - L.p;
+    const double tmp = 0.5 / (rc * rc);
+    const double rdc = RoeDens * rc * du;
+    A0 = tmp * (dp - rdc);
+    A1 = dr - dp * (2.0 * tmp);
+    A2 = RoeDens * dv;
+    A3 = RoeDens * dw;
+    A4 = tmp * (dp + rdc);
+    // Harten-Hyman entropy fix
+    auto fix = [](double a, double al, double ar) {
+      const double da = fmax(0.0, fmax(a - al, ar - a));
+      const double aa = fabs(a);
+      return (aa < da) ? 0.5 * (a * a / da + da) : aa;
+    };
+    e0 = fix(a0, L.v1 - cL, R.v1 - cR);
+    e1 = fix(a1, L.v1, R.v1);
+    e4 = fix(a4, L.v1 + cL, R.v1 + cR);
+  }
+  // dissipation D = sum_k Alpha_k |a_k| r_k
+  const double w0 = A0 * e0, w1 = A1 * e1, w2 = A2 * e1, w3 = A3 * e1, w4 = A4 * e4;
+  double D[5];
+  D[0] = w0 + w1 + w4;
+  D[1] = w0 * a0 + w1 * r1v + w4 * a4;
+  D[2] = (w0 + w1 + w4) * r2v + w2;
+  D[3] = (w0 + w1 + w4) * r3v + w3;
+  D[4] = w0 * (rH - r1v * rc) + w1 * (0.5 * absVel) + w2 * r2v + w3 * r3v + w4 * (rH + r1v * rc);
+  if (!split) {
+    double FL[5], FR[5];
+    euler_flux_1d(L, FL); euler_flux_1d(R, FR);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) F[v] = 0.5 * ((FL[v] + FR[v]) - D[v]);
+  } else {
+    split_surface_flux(splitDG, L, R, HL, HR, F);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) F[v] = F[v] - 0.5 * D[v];
+  }
+}
+
+// eos.f90:PRESSURE_RIEMANN on the rotated boundary state (v1 = normal velocity)
+__device__ __forceinline__ double pressure_riemann(const Basis& B, double rho, double vn, double p) {
+  if (vn <= 0.0) {
+    const double base = fmax(0.0001, 1.0 + 0.5 * B.kappaM1 * vn / sqrt(B.kappa * p / rho));
+    return p * pow(base, B.kappaFac);
+  }
+  const double ar = 2.0 * B.sKappaP1 / rho;
+  const double br = B.kappaM1 * B.sKappaP1 * p;
+  return p + vn / ar * 0.5 * (vn + sqrt(vn * vn + 4.0 * ar * (p + br)));
+}
+
+__device__ __forceinline__ void set_error(int* err, int code) { atomicCAS(err, 0, code); }
+
+}  // namespace fg

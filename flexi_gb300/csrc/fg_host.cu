@@ -1,0 +1,665 @@
+// flexi_gb300 -- host runtime and C ABI (include/flexi_gpu.h).
+//
+// One fg_handle owns all device memory of one solver (one or many ensemble instances), one CUDA stream
+// and, after the first fg_run, one captured CUDA graph of a whole time step. The per-stage sequence is
+//   k_prep -> k_lift -> k_flux -> k_vol (fused LSERK update)
+// and a step is  k_reset -> k_dt (CALCTIMESTEP + bulk velocity partial sums) -> k_finish_dt -> 5 stages.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cctype>
+#include <cmath>
+#include <cstring>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/flexi_gpu.h"
+#include "fg_common.cuh"
+#include "fg_launch.cuh"
+#include "fg_mesh.hpp"
+
+namespace fg {
+KernelSet kernel_set_n2(bool);
+KernelSet kernel_set_n3(bool);
+KernelSet kernel_set_n4(bool);
+KernelSet kernel_set_n5(bool);
+KernelSet kernel_set_n6(bool);
+KernelSet kernel_set_n7(bool);
+KernelSet kernel_set_n8(bool);
+KernelSet get_kernel_set(int n, bool gl) {
+  switch (n) {
+    case 2: return kernel_set_n2(gl);
+    case 3: return kernel_set_n3(gl);
+    case 4: return kernel_set_n4(gl);
+    case 5: return kernel_set_n5(gl);
+    case 6: return kernel_set_n6(gl);
+    case 7: return kernel_set_n7(gl);
+    case 8: return kernel_set_n8(gl);
+    default: return KernelSet{};
+  }
+}
+
+// ---- small helper kernels ----
+__global__ void k_fill(double* a, double v, int cnt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < cnt) a[i] = v;
+}
+// per-instance reductions of the step set-up: bulk velocity = sum(bulkPart of the instance)/Vol,
+// and the per-instance time counter. One thread per instance, elements of an instance are contiguous
+// in [instStart[i], instStart[i+1]).
+__global__ void k_finish_step(Dev d, const double* bulkPart, const int* instStart, const double* instVol, double* tInst, int doBulk,
+                              int checkDt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.nInst) return;
+  if (doBulk) {
+    double s = 0.;
+    for (int e = instStart[i]; e < instStart[i + 1]; ++e) s += bulkPart[e];
+    d.bulkVel[i] = s / instVol[i];
+  }
+  if (!checkDt) return;
+  const double dt = d.dt[i];
+  if (!(dt > 0.) || dt > 1e300) set_error(d.err, 2);
+  if (tInst) tInst[i] += dt;
+}
+// layout conversion between FLEXI's U(v,i,j,k,e) and [e][v][ijk]
+__global__ void k_fortran_to_dev(const double* __restrict__ f, double* __restrict__ d, int nv, int n3, long long total) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  const int v = (int)(t % nv);
+  const long long r = t / nv;
+  const int x = (int)(r % n3);
+  const long long e = r / n3;
+  d[(e * nv + v) * n3 + x] = f[t];
+}
+__global__ void k_dev_to_fortran(const double* __restrict__ d, double* __restrict__ f, int nvDev, int v0, int nv, int n3, long long total) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  const int v = (int)(t % nv);
+  const long long r = t / nv;
+  const int x = (int)(r % n3);
+  const long long e = r / n3;
+  f[t] = d[(e * nvDev + v0 + v) * n3 + x];
+}
+// FP64 FMA throughput probe
+__global__ void k_probe_dfma(double* out, double a, double b, int iters) {
+  double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+}  // namespace fg
+
+using namespace fg;
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+struct fg_handle {
+  fg_config cfg{};
+  Basis B{};
+  KernelSet K{};
+  fgh::HostMesh M;
+  Dev d{};
+  bool haveMesh = false;
+  cudaStream_t st = nullptr;
+  std::vector<DevBuf> bufs;
+  double* dMetAdv = nullptr;
+  double* dMetVisc = nullptr;
+  double* dWVol = nullptr;
+  double* dBulkPart = nullptr;
+  int* dInstStart = nullptr;
+  double* dInstVol = nullptr;
+  double* dTime = nullptr;
+  double* dStage = nullptr;  // staging for layout conversion (size nElems*5*n3)
+  double RKA[6]{}, RKb[6]{}, RKc[6]{};
+  double cflEff = 0., dflEff = 0.;
+  cudaGraphExec_t graph = nullptr;
+  long long launches = 0;
+  std::string err;
+  std::vector<double> instMu0;
+};
+
+namespace {
+
+thread_local std::string g_err;  // errors without a handle (fg_create, fg_probe_fp64)
+
+int fail(fg_handle* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  else g_err = msg;
+  return code;
+}
+#define CUDA_TRY(x)                                                                                   \
+  do {                                                                                                \
+    cudaError_t e_ = (x);                                                                             \
+    if (e_ != cudaSuccess) return fail(h, FG_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T>
+int dalloc(fg_handle* h, T*& ptr, size_t count) {
+  void* p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+  if (e != cudaSuccess) return fail(h, FG_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  h->bufs.push_back({p, count * sizeof(T)});
+  ptr = (T*)p;
+  return 0;
+}
+template <class T>
+int upload(fg_handle* h, T*& ptr, const std::vector<T>& v) {
+  if (int r = dalloc(h, ptr, v.size())) return r;
+  if (!v.empty()) {
+    cudaError_t e = cudaMemcpy(ptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail(h, FG_ERR_CUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+  }
+  return 0;
+}
+void free_device(fg_handle* h) {
+  if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+  for (auto& b : h->bufs) cudaFree(b.p);
+  h->bufs.clear();
+  h->haveMesh = false;
+}
+
+void init_basis(fg_handle* h) {
+  const fg_config& c = h->cfg;
+  Basis& B = h->B;
+  std::memset(&B, 0, sizeof(B));
+  const int N = c.N, n = N + 1;
+  B.N = N; B.n = n; B.nodeType = c.NodeType; B.splitDG = c.SplitDG;
+  B.riemann = c.Riemann; B.riemannBC = c.RiemannBC < 0 ? c.Riemann : c.RiemannBC;
+  B.lifting = c.Lifting; B.weakLifting = c.doWeakLifting;
+  fgh::Vec x, w;
+  fgh::nodes(N, c.NodeType == FG_NODE_GAUSS_LOBATTO ? fgh::LOBATTO : fgh::GAUSS, x, w);
+  const fgh::Mat D = fgh::diff_matrix(x);
+  const fgh::Vec wb = fgh::bary_weights(x);
+  const fgh::Vec Lm = fgh::lagrange_at(-1., x, wb), Lp = fgh::lagrange_at(1., x, wb);
+  for (int i = 0; i < n; ++i)
+    for (int l = 0; l < n; ++l) {
+      B.D_T[l * n + i] = D(i, l);                        // D_T(l,i) = D(i,l)
+      B.Dhat_T[l * n + i] = -(1. / w[i]) * D(l, i) * w[l];  // D_Hat_T(l,i) = D_Hat(i,l) = -w_i^-1 D(l,i) w_l
+    }
+  // DVolSurf (dg.f90:180-203): GL: D^T with the corner corrections; Gauss: transpose of D - 1/2 M^-1 Vf^T B Vf
+  for (int l = 0; l < n; ++l)
+    for (int i = 0; i < n; ++i) {
+      double v;
+      if (c.NodeType == FG_NODE_GAUSS_LOBATTO) {
+        v = D(i, l);  // DVolSurf(l,i) = D_T(l,i) = D(i,l)
+        if (l == 0 && i == 0) v += 1.0 / (2.0 * w[0]);
+        if (l == N && i == N) v -= 1.0 / (2.0 * w[N]);
+      } else {
+        v = D(i, l) - 0.5 * (1. / w[i]) * (-Lm[i] * Lm[l] + Lp[i] * Lp[l]);  // DVolSurf(l,i) = S(i,l)
+      }
+      B.DVS[l * n + i] = v;
+    }
+  for (int i = 0; i < n; ++i) { B.Lm[i] = Lm[i]; B.Lp[i] = Lp[i]; B.LhM[i] = Lm[i] / w[i]; B.LhP[i] = Lp[i] / w[i]; }
+  B.kappa = c.kappa; B.kappaM1 = c.kappa - 1.; B.sKappaM1 = 1. / (c.kappa - 1.);
+  B.Rgas = c.R; B.sR = 1. / c.R;
+  const double cp = c.R * c.kappa / (c.kappa - 1.);
+  B.lambdaFac = cp / c.Pr;
+  B.etaBR2 = c.etaBR2; B.etaBR2_wall = (c.etaBR2_wall == -1.) ? c.etaBR2 : c.etaBR2_wall;
+  B.kappaFac = 2. * c.kappa / (c.kappa - 1.);
+  B.sKappaP1 = 1. / (c.kappa + 1.);
+  // Carpenter-Kennedy RK4-5, timedisc_vars.f90:199-214
+  double* A = h->RKA; double* b = h->RKb; double* cc = h->RKc;
+  A[2] = 567301805773.0 / 1357537059087.0; A[3] = 2404267990393.0 / 2016746695238.0;
+  A[4] = 3550918686646.0 / 2091501179385.0; A[5] = 1275806237668.0 / 842570457699.0;
+  b[1] = 1432997174477.0 / 9575080441755.0; b[2] = 5161836677717.0 / 13612068292357.0;
+  b[3] = 1720146321549.0 / 2090206949498.0; b[4] = 3134564353537.0 / 4481467310338.0;
+  b[5] = 2277821191437.0 / 14882151754819.0;
+  cc[2] = 1432997174477.0 / 9575080441755.0; cc[3] = 2526269341429.0 / 6820363962896.0;
+  cc[4] = 2006345519317.0 / 3224310063776.0; cc[5] = 2802321613138.0 / 2924317926251.0;
+  // FillCFL_DFL (timedisc_func.f90:463-527)
+  static const double cflG[15] = {2.0351, 1.7595, 1.5401, 1.3702, 1.2375, 1.1318, 1.0440, 0.9709, 0.9079, 0.8539, 0.8066, 0.7650, 0.7290, 0.6952, 0.6660};
+  static const double cflGL[15] = {4.7497, 3.4144, 2.8451, 2.4739, 2.2027, 1.9912, 1.8225, 1.6830, 1.5682, 1.4692, 1.3849, 1.3106, 1.2454, 1.1880, 1.1362};
+  static const double dflG[10] = {1.12, 0.76, 0.55, 0.41, 0.32, 0.25, 0.20, 0.17, 0.14, 0.12};
+  static const double dflGL[10] = {4.50, 1.95, 1.18, 0.79, 0.56, 0.42, 0.32, 0.25, 0.20, 0.17};
+  const bool gl = c.NodeType == FG_NODE_GAUSS_LOBATTO;
+  h->cflEff = c.CFLScale * (gl ? cflGL : cflG)[std::min(15, N) - 1] / (2. * N + 1.);
+  h->dflEff = c.DFLScale * (gl ? dflGL : dflG)[std::min(10, N) - 1] * 1.853 / ((2. * N + 1.) * (2. * N + 1.));
+}
+
+int upload_mesh(fg_handle* h) {
+  fgh::HostMesh& M = h->M;
+  fgh::finish_mesh(M, h->cfg.kappa, h->cfg.Pr);
+  free_device(h);
+  const int n = M.n, n2 = n * n, n3 = n2 * n, nE = M.nElems, nS = M.nSides;
+  Dev& d = h->d;
+  d = Dev{};
+  d.nElems = nE; d.nSides = nS; d.nBCSides = M.nBCSides; d.nInst = M.nInst;
+  int r = 0;
+  if ((r = dalloc(h, d.U, (size_t)nE * 5 * n3))) return r;
+  if ((r = dalloc(h, d.Ut, (size_t)nE * 5 * n3))) return r;
+  if ((r = dalloc(h, d.Ut_tmp, (size_t)nE * 5 * n3))) return r;
+  if ((r = dalloc(h, d.prim, (size_t)nE * VP_NF * n3))) return r;
+  if ((r = dalloc(h, d.grad, (size_t)nE * 12 * n3))) return r;
+  if ((r = upload(h, d.metr, M.metr))) return r;
+  if ((r = upload(h, d.sJ, M.sJ))) return r;
+  if ((r = upload(h, d.elemSide, M.elemSide))) return r;
+  if ((r = upload(h, d.elemInst, M.elemInst))) return r;
+  if ((r = dalloc(h, d.faceM, (size_t)nS * FS_NF * n2))) return r;
+  if ((r = dalloc(h, d.faceS, (size_t)nS * FS_NF * n2))) return r;
+  if ((r = dalloc(h, d.gradM, (size_t)nS * 12 * n2))) return r;
+  if ((r = dalloc(h, d.gradS, (size_t)nS * 12 * n2))) return r;
+  if ((r = upload(h, d.geo, M.geo))) return r;
+  if ((r = dalloc(h, d.flux, (size_t)nS * 5 * n2))) return r;
+  if ((r = upload(h, d.sideElem, M.sideElem))) return r;
+  if ((r = upload(h, d.sideInst, M.sideInst))) return r;
+  if ((r = upload(h, d.bcType, M.bcType))) return r;
+  if ((r = upload(h, d.bcTwall, M.bcTwall))) return r;
+  std::vector<double> mu(M.nInst, h->cfg.mu0), zero(M.nInst, 0.), dp(M.nInst, h->cfg.doTCSource ? h->cfg.dpdx : 0.);
+  if (h->instMu0.size() == (size_t)M.nInst) mu = h->instMu0;
+  if ((r = upload(h, d.mu0, mu))) return r;
+  if ((r = upload(h, d.dt, zero))) return r;
+  if ((r = upload(h, d.bulkVel, zero))) return r;
+  if ((r = upload(h, d.dpdx, dp))) return r;
+  if ((r = upload(h, d.err, std::vector<int>(1, 0)))) return r;
+  if ((r = upload(h, h->dMetAdv, M.metAdv))) return r;
+  if ((r = upload(h, h->dMetVisc, M.metVisc))) return r;
+  if ((r = upload(h, h->dWVol, M.wVol))) return r;
+  if ((r = dalloc(h, h->dBulkPart, (size_t)nE))) return r;
+  // instances must be contiguous element ranges
+  std::vector<int> start(M.nInst + 1, 0);
+  for (int e = 0; e < nE; ++e) {
+    if (e > 0 && M.elemInst[e] < M.elemInst[e - 1]) return fail(h, FG_ERR_MESH, "ensemble instances must be contiguous element ranges");
+    start[M.elemInst[e] + 1] = e + 1;
+  }
+  for (int i = 1; i <= M.nInst; ++i) start[i] = std::max(start[i], start[i - 1]);
+  if ((r = upload(h, h->dInstStart, start))) return r;
+  if ((r = upload(h, h->dInstVol, M.instVol))) return r;
+  if ((r = upload(h, h->dTime, zero))) return r;
+  if ((r = dalloc(h, h->dStage, (size_t)nE * 12 * n3))) return r;
+  h->haveMesh = true;
+  return 0;
+}
+
+// state sequence of one right-hand side evaluation plus the RK register update
+void launch_rhs(fg_handle* h, int mode, double rkA, double rkB) {
+  const Dev& d = h->d;
+  h->K.prep(d, h->B, h->st);
+  h->K.lift(d, h->B, h->st);
+  h->K.flux(d, h->B, h->st);
+  if (h->cfg.SplitDG >= 0) h->K.vol_split(d, h->B, mode, rkA, rkB, h->st);
+  else h->K.vol_weak(d, h->B, mode, rkA, rkB, h->st);
+  h->launches += 4;
+}
+// step set-up: mode 0 = CALCTIMESTEP, 1 = fixed dt, 2 = bulk velocity only (plain right-hand side)
+void launch_step_setup(fg_handle* h, int mode, double fixedDt, bool advanceTime) {
+  const Dev& d = h->d;
+  const int nI = d.nInst;
+  const bool doBulk = h->cfg.doTCSource != 0;
+  const bool computeDt = mode == 0;
+  if (mode == 2) {
+    if (!doBulk) return;
+    h->K.dt(d, h->B, h->dMetAdv, h->dMetVisc, h->cflEff, h->dflEff, h->dBulkPart, h->dWVol, h->st);
+    k_finish_step<<<(nI + 127) / 128, 128, 0, h->st>>>(d, h->dBulkPart, h->dInstStart, h->dInstVol, nullptr, 1, 0);
+    h->launches += 2;
+    return;
+  }
+  if (computeDt) {
+    k_fill<<<(nI + 127) / 128, 128, 0, h->st>>>(d.dt, INFINITY, nI);
+    h->K.dt(d, h->B, h->dMetAdv, h->dMetVisc, h->cflEff, h->dflEff, h->dBulkPart, h->dWVol, h->st);
+    h->launches += 2;
+  } else {
+    k_fill<<<(nI + 127) / 128, 128, 0, h->st>>>(d.dt, fixedDt, nI);
+    h->launches += 1;
+    if (doBulk) {
+      h->K.dt(d, h->B, h->dMetAdv, h->dMetVisc, h->cflEff, h->dflEff, h->dBulkPart, h->dWVol, h->st);
+      k_fill<<<(nI + 127) / 128, 128, 0, h->st>>>(d.dt, fixedDt, nI);
+      h->launches += 2;
+    }
+  }
+  k_finish_step<<<(nI + 127) / 128, 128, 0, h->st>>>(d, h->dBulkPart, h->dInstStart, h->dInstVol, advanceTime ? h->dTime : nullptr, doBulk, 1);
+  h->launches += 1;
+}
+void launch_lserk(fg_handle* h) {
+  for (int s = 1; s <= 5; ++s) launch_rhs(h, s == 1 ? 1 : 2, s == 1 ? 0. : h->RKA[s], h->RKb[s]);
+}
+int check_err(fg_handle* h) {
+  int e = 0;
+  CUDA_TRY(cudaMemcpyAsync(&e, h->d.err, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CUDA_TRY(cudaStreamSynchronize(h->st));
+  if (e == 1) return fail(h, FG_ERR_NAN, "NaN density found");
+  if (e) return fail(h, FG_ERR_DT, "non-finite or non-positive time step");
+  return 0;
+}
+
+std::string lower(std::string s) {
+  for (char& c : s) c = (char)std::tolower((unsigned char)c);
+  return s;
+}
+std::string trim(const std::string& s) {
+  size_t a = s.find_first_not_of(" \t\r\n"), b = s.find_last_not_of(" \t\r\n");
+  return a == std::string::npos ? "" : s.substr(a, b - a + 1);
+}
+
+}  // namespace
+
+extern "C" {
+
+int fg_config_default(fg_config* c) {
+  if (!c) return FG_ERR_CONFIG;
+  std::memset(c, 0, sizeof(*c));
+  c->N = 3; c->NodeType = FG_NODE_GAUSS; c->Riemann = FG_RIEMANN_ROEENTROPYFIX; c->RiemannBC = FG_RIEMANN_SAME;
+  c->Lifting = 1; c->doWeakLifting = 0; c->doConservativeLifting = 0; c->SplitDG = FG_SPLIT_PI;
+  c->etaBR2 = 2.; c->etaBR2_wall = -1.; c->kappa = 1.4; c->R = 287.058; c->Pr = 0.72; c->mu0 = 0.;
+  c->CFLScale = 0.9; c->DFLScale = 0.9; c->doTCSource = 0; c->dpdx = -1.; c->TimeDiscMethod = 0;
+  return FG_OK;
+}
+
+int fg_config_from_ini(const char* text, fg_config* c) {
+  if (!text || !c) return FG_ERR_CONFIG;
+  std::istringstream in(text);
+  std::string line;
+  while (std::getline(in, line)) {
+    const size_t bang = line.find('!');
+    if (bang != std::string::npos) line = line.substr(0, bang);
+    const size_t eq = line.find('=');
+    if (eq == std::string::npos) continue;
+    const std::string key = lower(trim(line.substr(0, eq))), val = trim(line.substr(eq + 1)), lv = lower(val);
+    try {
+      if (key == "n") c->N = std::stoi(val);
+      else if (key == "nodetype") c->NodeType = (lv == "gauss-lobatto" || lv == "2") ? FG_NODE_GAUSS_LOBATTO : FG_NODE_GAUSS;
+      else if (key == "riemann" || key == "riemannbc") {
+        int id;
+        if (lv == "lf") id = FG_RIEMANN_LF;
+        else if (lv == "hllc") id = FG_RIEMANN_HLLC;
+        else if (lv == "roe") id = FG_RIEMANN_ROE;
+        else if (lv == "roeentropyfix") id = FG_RIEMANN_ROEENTROPYFIX;
+        else if (lv == "same") id = FG_RIEMANN_SAME;
+        else id = std::stoi(val);
+        (key == "riemann" ? c->Riemann : c->RiemannBC) = id;
+      } else if (key == "splitdg") {
+        if (lv == "sd") c->SplitDG = FG_SPLIT_SD;
+        else if (lv == "pi") c->SplitDG = FG_SPLIT_PI;
+        else if (lv == "none" || lv == "off") c->SplitDG = FG_SPLIT_NONE;
+        else c->SplitDG = std::stoi(val);
+      } else if (key == "lifting") c->Lifting = (lv == "br2" || lv == "2") ? 2 : 1;
+      else if (key == "doweaklifting") c->doWeakLifting = (lv == "t" || lv == ".true." || lv == "true" || lv == "1");
+      else if (key == "doconservativelifting") c->doConservativeLifting = (lv == "t" || lv == ".true." || lv == "true" || lv == "1");
+      else if (key == "etabr2") c->etaBR2 = std::stod(val);
+      else if (key == "etabr2_wall") c->etaBR2_wall = std::stod(val);
+      else if (key == "kappa") c->kappa = std::stod(val);
+      else if (key == "r") c->R = std::stod(val);
+      else if (key == "pr") c->Pr = std::stod(val);
+      else if (key == "mu0") c->mu0 = std::stod(val);
+      else if (key == "cflscale") c->CFLScale = std::stod(val);
+      else if (key == "dflscale") c->DFLScale = std::stod(val);
+      else if (key == "timediscmethod") c->TimeDiscMethod = (lv == "carpenterrk4-5") ? 0 : -1;
+    } catch (...) {
+      return FG_ERR_CONFIG;
+    }
+  }
+  return FG_OK;
+}
+
+int fg_create(const fg_config* cfg, fg_handle** out) {
+  if (!cfg || !out) return FG_ERR_CONFIG;
+  *out = nullptr;
+  fg_handle* h = new fg_handle();
+  h->cfg = *cfg;
+  const fg_config& c = h->cfg;
+  std::string why;
+  if (c.N < 1 || c.N > 7) why = "N must be in 1..7";
+  else if (c.NodeType != FG_NODE_GAUSS && c.NodeType != FG_NODE_GAUSS_LOBATTO) why = "NodeType must be 1 (Gauss) or 2 (Gauss-Lobatto)";
+  else if (c.Riemann != FG_RIEMANN_LF && c.Riemann != FG_RIEMANN_HLLC && c.Riemann != FG_RIEMANN_ROE && c.Riemann != FG_RIEMANN_ROEENTROPYFIX)
+    why = "Riemann must be LF, HLLC, Roe or RoeEntropyFix";
+  else if (c.Lifting != 1 && c.Lifting != 2) why = "Lifting must be 1 (BR1) or 2 (BR2)";
+  else if (c.doConservativeLifting) why = "doConservativeLifting is not supported";
+  else if (c.Lifting == 2 && c.doWeakLifting) why = "BR2 lifting is strong only";
+  else if (c.SplitDG != FG_SPLIT_NONE && c.SplitDG != FG_SPLIT_SD && c.SplitDG != FG_SPLIT_PI) why = "SplitDG must be -1 (weak), 0 (SD) or 4 (PI)";
+  else if (c.SplitDG != FG_SPLIT_NONE && c.NodeType != FG_NODE_GAUSS_LOBATTO) why = "the split form is supported with Gauss-Lobatto nodes";
+  else if (c.SplitDG != FG_SPLIT_NONE && c.N != 1 && c.N != 3 && c.N != 7) why = "the split form supports N = 1, 3, 7";
+  else if (c.TimeDiscMethod != 0) why = "TimeDiscMethod must be CarpenterRK4-5";
+  if (!why.empty()) { delete h; return fail(nullptr, FG_ERR_CONFIG, why); }
+  h->K = get_kernel_set(c.N + 1, c.NodeType == FG_NODE_GAUSS_LOBATTO);
+  if (h->K.n == 0) { delete h; return fail(nullptr, FG_ERR_CONFIG, "no kernels for this N"); }
+  init_basis(h);
+  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) { delete h; return FG_ERR_CUDA; }
+  *out = h;
+  return FG_OK;
+}
+
+int fg_destroy(fg_handle* h) {
+  if (!h) return FG_OK;
+  free_device(h);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+  return FG_OK;
+}
+
+const char* fg_last_error(const fg_handle* h) { return h ? h->err.c_str() : g_err.c_str(); }
+
+int fg_build_mesh(fg_handle* h, int nElems, int NGeo, const double* NodeCoords, const int* ElemNb, int nBCs, const int* BoundaryType,
+                  int nRefStates, const double* RefStatePrim, const int* ElemInst) {
+  if (!h) return FG_ERR_STATE;
+  if (nElems <= 0 || NGeo < 1 || !NodeCoords || !ElemNb) return fail(h, FG_ERR_MESH, "invalid mesh arguments");
+  try {
+    fgh::RawMesh R;
+    R.nElems = nElems; R.NGeo = NGeo; R.nodeCoords = NodeCoords; R.elemNb = ElemNb; R.nBCs = nBCs; R.boundaryType = BoundaryType;
+    R.nRefStates = nRefStates; R.refStatePrim = RefStatePrim; R.elemInst = ElemInst;
+    fgh::build_from_raw(R, h->cfg.N, h->cfg.NodeType == FG_NODE_GAUSS_LOBATTO ? fgh::LOBATTO : fgh::GAUSS, h->M);
+  } catch (std::exception& e) {
+    return fail(h, FG_ERR_MESH, e.what());
+  }
+  return upload_mesh(h);
+}
+
+int fg_set_mesh(fg_handle* h, int nElems, int nSides, int nBCSides, const int* SideToElem, const int* ElemToSide, const int* BC, int nBCs,
+                const int* BoundaryType, int nRefStates, const double* RefStatePrim, const double* Mf, const double* Mg, const double* Mh,
+                const double* sJ, const double* NormVec, const double* TangVec1, const double* TangVec2, const double* SurfElem) {
+  if (!h) return FG_ERR_STATE;
+  try {
+    fgh::build_from_flexi(h->cfg.N, h->cfg.NodeType == FG_NODE_GAUSS_LOBATTO ? fgh::LOBATTO : fgh::GAUSS, nElems, nSides, nBCSides,
+                          SideToElem, ElemToSide, BC, nBCs, BoundaryType, nRefStates, RefStatePrim, Mf, Mg, Mh, sJ, NormVec, TangVec1,
+                          TangVec2, SurfElem, h->M);
+  } catch (std::exception& e) {
+    return fail(h, FG_ERR_MESH, e.what());
+  }
+  return upload_mesh(h);
+}
+
+int fg_set_instance_mu0(fg_handle* h, int nInst, const double* mu0) {
+  if (!h || !mu0 || nInst <= 0) return FG_ERR_CONFIG;
+  h->instMu0.assign(mu0, mu0 + nInst);
+  if (h->haveMesh) {
+    if (nInst != h->d.nInst) return fail(h, FG_ERR_CONFIG, "instance count mismatch");
+    CUDA_TRY(cudaMemcpy(h->d.mu0, mu0, sizeof(double) * nInst, cudaMemcpyHostToDevice));
+  }
+  return FG_OK;
+}
+
+int fg_get_sizes(const fg_handle* h, int* out) {
+  if (!h || !out) return FG_ERR_STATE;
+  out[0] = h->M.nElems; out[1] = h->M.nSides; out[2] = h->M.nBCSides; out[3] = h->cfg.N; out[4] = h->M.nInst;
+  return FG_OK;
+}
+
+int fg_get_elem_xgp(fg_handle* h, double* X) {
+  if (!h || !h->haveMesh || h->M.elemX.empty()) return fail(h, FG_ERR_STATE, "no solution coordinates (mesh not built from nodes)");
+  const int n3 = h->M.n * h->M.n * h->M.n;
+  for (int e = 0; e < h->M.nElems; ++e)
+    for (int x = 0; x < n3; ++x)
+      for (int c = 0; c < 3; ++c) X[((size_t)e * n3 + x) * 3 + c] = h->M.elemX[((size_t)e * 3 + c) * n3 + x];
+  return FG_OK;
+}
+
+int fg_get_mesh_array(fg_handle* h, int which, double* out) {
+  if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
+  const fgh::HostMesh& M = h->M;
+  const int n = M.n, n2 = n * n, n3 = n2 * n;
+  if (which >= 0 && which <= 2) {
+    for (int e = 0; e < M.nElems; ++e) for (int x = 0; x < n3; ++x) for (int c = 0; c < 3; ++c)
+      out[((size_t)e * n3 + x) * 3 + c] = M.metr[((size_t)e * 9 + 3 * which + c) * n3 + x];
+  } else if (which == 3) {
+    std::copy(M.sJ.begin(), M.sJ.end(), out);
+  } else if (which >= 4 && which <= 6) {
+    for (int s = 0; s < M.nSides; ++s) for (int pq = 0; pq < n2; ++pq) for (int c = 0; c < 3; ++c)
+      out[((size_t)s * n2 + pq) * 3 + c] = M.geo[((size_t)s * 10 + 3 * (which - 4) + c) * n2 + pq];
+  } else if (which == 7) {
+    for (int s = 0; s < M.nSides; ++s) for (int pq = 0; pq < n2; ++pq) out[(size_t)s * n2 + pq] = M.geo[((size_t)s * 10 + 9) * n2 + pq];
+  } else return fail(h, FG_ERR_CONFIG, "unknown mesh array");
+  return FG_OK;
+}
+
+int fg_get_side_to_elem(fg_handle* h, int* out) {
+  if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
+  for (int s = 0; s < h->M.nSides; ++s) {
+    const int* r = &h->M.sideElem[s * 4];
+    out[s * 5 + 0] = r[0] + 1; out[s * 5 + 2] = r[1];
+    out[s * 5 + 1] = r[2] >= 0 ? r[2] + 1 : -1;
+    out[s * 5 + 3] = r[2] >= 0 ? r[3] >> 3 : -1;
+    out[s * 5 + 4] = r[2] >= 0 ? r[3] & 7 : 0;
+  }
+  return FG_OK;
+}
+
+int fg_set_state(fg_handle* h, const double* U) {
+  if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
+  const int n3 = h->M.n * h->M.n * h->M.n;
+  const long long total = (long long)h->M.nElems * 5 * n3;
+  CUDA_TRY(cudaMemcpyAsync(h->dStage, U, total * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  k_fortran_to_dev<<<(unsigned)((total + 255) / 256), 256, 0, h->st>>>(h->dStage, h->d.U, 5, n3, total);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(h->st));
+  return FG_OK;
+}
+
+static int export_field(fg_handle* h, const double* dsrc, int nvDev, int v0, int nv, double* out) {
+  const int n3 = h->M.n * h->M.n * h->M.n;
+  const long long total = (long long)h->M.nElems * nv * n3;
+  k_dev_to_fortran<<<(unsigned)((total + 255) / 256), 256, 0, h->st>>>(dsrc, h->dStage, nvDev, v0, nv, n3, total);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(out, h->dStage, total * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CUDA_TRY(cudaStreamSynchronize(h->st));
+  return FG_OK;
+}
+
+int fg_get_state(fg_handle* h, double* U) {
+  if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
+  return export_field(h, h->d.U, 5, 0, 5, U);
+}
+
+int fg_state_device_ptr(fg_handle* h, double** p) {
+  if (!h || !h->haveMesh || !p) return fail(h, FG_ERR_STATE, "no mesh");
+  *p = h->d.U;
+  return FG_OK;
+}
+
+int fg_time_derivative(fg_handle* h, double t, double* Ut) {
+  (void)t;  // no time-dependent source or boundary condition on this path
+  if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
+  h->launches = 0;
+  launch_step_setup(h, 2, 0., false);
+  launch_rhs(h, 0, 0., 0.);
+  CUDA_TRY(cudaGetLastError());
+  if (Ut) return export_field(h, h->d.Ut, 5, 0, 5, Ut);
+  CUDA_TRY(cudaStreamSynchronize(h->st));
+  return FG_OK;
+}
+
+int fg_calc_timestep(fg_handle* h, double* dt, int* errType) {
+  if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
+  CUDA_TRY(cudaMemsetAsync(h->d.err, 0, sizeof(int), h->st));
+  const int nI = h->d.nInst;
+  k_fill<<<(nI + 127) / 128, 128, 0, h->st>>>(h->d.dt, INFINITY, nI);
+  h->K.dt(h->d, h->B, h->dMetAdv, h->dMetVisc, h->cflEff, h->dflEff, nullptr, h->dWVol, h->st);
+  CUDA_TRY(cudaGetLastError());
+  std::vector<double> v(nI);
+  int e = 0;
+  CUDA_TRY(cudaMemcpyAsync(v.data(), h->d.dt, sizeof(double) * nI, cudaMemcpyDeviceToHost, h->st));
+  CUDA_TRY(cudaMemcpyAsync(&e, h->d.err, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CUDA_TRY(cudaStreamSynchronize(h->st));
+  if (dt) std::copy(v.begin(), v.end(), dt);
+  if (errType) *errType = e;
+  return FG_OK;
+}
+
+int fg_timestep_lserkw2(fg_handle* h, double* t, double dt) {
+  if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
+  h->launches = 0;
+  CUDA_TRY(cudaMemsetAsync(h->d.err, 0, sizeof(int), h->st));
+  launch_step_setup(h, 1, dt, false);
+  launch_lserk(h);
+  CUDA_TRY(cudaGetLastError());
+  if (int r = check_err(h)) return r;
+  if (t) *t += dt;
+  return FG_OK;
+}
+
+int fg_run(fg_handle* h, int nSteps, double* t) {
+  if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
+  if (nSteps < 0) return fail(h, FG_ERR_CONFIG, "nSteps < 0");
+  CUDA_TRY(cudaMemsetAsync(h->d.err, 0, sizeof(int), h->st));
+  if (!h->graph) {
+    cudaGraph_t g;
+    const long long before = h->launches;
+    CUDA_TRY(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+    launch_step_setup(h, 0, 0., true);
+    launch_lserk(h);
+    CUDA_TRY(cudaStreamEndCapture(h->st, &g));
+    CUDA_TRY(cudaGraphInstantiate(&h->graph, g, 0));
+    cudaGraphDestroy(g);
+    h->launches = h->launches - before;  // launches per step
+  }
+  const long long perStep = h->launches;
+  for (int s = 0; s < nSteps; ++s) CUDA_TRY(cudaGraphLaunch(h->graph, h->st));
+  CUDA_TRY(cudaGetLastError());
+  if (int r = check_err(h)) return r;
+  if (t) CUDA_TRY(cudaMemcpy(t, h->dTime, sizeof(double) * h->d.nInst, cudaMemcpyDeviceToHost));
+  h->launches = perStep;
+  (void)perStep;
+  return FG_OK;
+}
+
+int fg_get_gradients(fg_handle* h, double* gx, double* gy, double* gz) {
+  if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
+  double* outs[3] = {gx, gy, gz};
+  for (int dd = 0; dd < 3; ++dd)
+    if (outs[dd])
+      if (int r = export_field(h, h->d.grad, 12, 4 * dd, 4, outs[dd])) return r;
+  return FG_OK;
+}
+
+int fg_get_stream(fg_handle* h, void** s) {
+  if (!h || !s) return FG_ERR_STATE;
+  *s = (void*)h->st;
+  return FG_OK;
+}
+
+long long fg_launch_count(const fg_handle* h) { return h ? h->launches : 0; }
+
+int fg_probe_fp64(double* tflops) {
+  fg_handle* h = nullptr;
+  int dev = 0;
+  cudaDeviceProp p;
+  CUDA_TRY(cudaGetDevice(&dev));
+  CUDA_TRY(cudaGetDeviceProperties(&p, dev));
+  const int blocks = p.multiProcessorCount * 8, threads = 256, iters = 4096;
+  double* out = nullptr;
+  CUDA_TRY(cudaMalloc(&out, sizeof(double) * blocks * threads));
+  cudaEvent_t a, b;
+  cudaEventCreate(&a); cudaEventCreate(&b);
+  k_probe_dfma<<<blocks, threads>>>(out, 0.999, 1e-3, 256);
+  float best = 1e30f;
+  for (int r = 0; r < 3; ++r) {
+    cudaEventRecord(a);
+    k_probe_dfma<<<blocks, threads>>>(out, 0.999, 1e-3, iters);
+    cudaEventRecord(b);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    best = std::min(best, ms);
+  }
+  cudaEventDestroy(a); cudaEventDestroy(b);
+  cudaFree(out);
+  CUDA_TRY(cudaGetLastError());
+  *tflops = (double)blocks * threads * iters * 8 * 2 / (best * 1e-3) / 1e12;
+  return FG_OK;
+}
+
+}  // extern "C"

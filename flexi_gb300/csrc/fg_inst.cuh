@@ -1,0 +1,61 @@
+// flexi_gb300 -- launch wrappers for one (n, node type) instantiation; included by fg_inst_n*.cu
+#pragma once
+#include "fg_kernels.cuh"
+#include "fg_launch.cuh"
+
+namespace fg {
+
+template <int n, bool GL>
+struct Inst {
+  using S = Shape<n>;
+  static int blocks(const Dev& d) { return (d.nElems + S::EPB - 1) / S::EPB; }
+  static size_t smem_prep() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * (5 + VP_NF) * S::n3); }
+  static size_t smem_lift() {
+    return sizeof(double) * (SBasis<n>::SIZE + S::EPB * (4 * S::n3 + 6 * S::n2 * 7 + 12 * S::n3 + S::n3));
+  }
+  static size_t smem_weak() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * (15 * S::n3 + 6 * S::n2 * 5)); }
+  static size_t smem_split() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * (32 * S::n3 + 6 * S::n2 * 5)); }
+  template <class K>
+  static void set_smem(K kern, size_t bytes) {
+    static bool done = false;
+    if (!done) {
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+      done = true;
+    }
+  }
+  static void prep(const Dev& d, const Basis& B, cudaStream_t st) {
+    set_smem(k_prep<n, GL>, smem_prep());
+    k_prep<n, GL><<<blocks(d), S::THREADS, smem_prep(), st>>>(d, B);
+  }
+  static void lift(const Dev& d, const Basis& B, cudaStream_t st) {
+    set_smem(k_lift<n, GL>, smem_lift());
+    k_lift<n, GL><<<blocks(d), S::THREADS, smem_lift(), st>>>(d, B);
+  }
+  static void flux(const Dev& d, const Basis& B, cudaStream_t st) {
+    const long long pts = (long long)d.nSides * S::n2;
+    k_flux<n><<<(unsigned)((pts + 127) / 128), 128, 0, st>>>(d, B);
+  }
+  static void vol_weak(const Dev& d, const Basis& B, int mode, double rkA, double rkB, cudaStream_t st) {
+    set_smem(k_vol_weak<n, GL>, smem_weak());
+    k_vol_weak<n, GL><<<blocks(d), S::THREADS, smem_weak(), st>>>(d, B, Stage{mode, rkA, rkB});
+  }
+  static void vol_split(const Dev& d, const Basis& B, int mode, double rkA, double rkB, cudaStream_t st) {
+    if constexpr (GL && (n == 2 || n == 4 || n == 8)) {
+      set_smem(k_vol_split<n>, smem_split());
+      k_vol_split<n><<<blocks(d), S::THREADS, smem_split(), st>>>(d, B, Stage{mode, rkA, rkB});
+    }
+  }
+  static void dt(const Dev& d, const Basis& B, const double* ma, const double* mv, double cfl, double dfl, double* bulk, const double* wv,
+                 cudaStream_t st) {
+    k_dt<n><<<blocks(d), S::THREADS, 0, st>>>(d, B, ma, mv, cfl, dfl, bulk, wv);
+  }
+  static KernelSet make() {
+    KernelSet k;
+    k.n = n; k.gl = GL;
+    k.prep = &prep; k.lift = &lift; k.flux = &flux; k.vol_weak = &vol_weak; k.dt = &dt;
+    if (GL && (n == 2 || n == 4 || n == 8)) k.vol_split = &vol_split;
+    return k;
+  }
+};
+
+}  // namespace fg

@@ -1,0 +1,788 @@
+// flexi_gb300 -- element and side kernels of one DGSEM right-hand-side evaluation (FLEXI's
+// DGTimeDerivative_weakForm, src/dg/dg.f90:221-678) and the fused low-storage RK stage update
+// (src/timedisc/timestep.f90:82-152).
+//
+// Per RK stage four launches:
+//   k_prep  (element)  ConsToPrim of the volume, ProlongToFace of U, ConsToPrim of the face values
+//   k_lift  (element)  BR1/BR2 lifting: volume gradient (D sweeps + metrics), surface lifting terms,
+//                      Jacobian, ProlongToFaceLifting (+ the BR2 face penalty)
+//   k_flux  (side)     Riemann solver + viscous flux (+ wall BCs), times SurfElem
+//   k_vol   (element)  volume integral (weak or split form), surface integral, -Ut*sJ, source,
+//                      and the LSERK register update -- or plain Ut output for fg_time_derivative
+// One CTA processes EPB elements with one thread per volume node; all face work is done by the
+// element that owns the data, reading its neighbour's face values from global memory.
+#pragma once
+#include "fg_common.cuh"
+
+namespace fg {
+
+template <int n> struct Shape {
+  static constexpr int N = n - 1, n2 = n * n, n3 = n * n * n;
+  // elements per CTA: fill at least ~128 threads for small n
+  static constexpr int EPB = (n3 >= 128) ? 1 : (128 + n3 - 1) / n3;
+  static constexpr int THREADS = ((EPB * n3 + 31) / 32) * 32;
+};
+
+// copies the basis matrices a kernel indexes with thread-dependent indices into shared memory
+template <int n>
+__device__ __forceinline__ void load_basis_smem(const Basis& B, double* sD) {
+  for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+    sD[t] = B.D_T[t];
+    sD[n * n + t] = B.Dhat_T[t];
+    sD[2 * n * n + t] = B.DVS[t];
+  }
+  for (int t = threadIdx.x; t < n; t += blockDim.x) {
+    sD[3 * n * n + t] = B.Lm[t];
+    sD[3 * n * n + n + t] = B.Lp[t];
+    sD[3 * n * n + 2 * n + t] = B.LhM[t];
+    sD[3 * n * n + 3 * n + t] = B.LhP[t];
+  }
+}
+template <int n> struct SBasis {
+  static constexpr int SIZE = 3 * n * n + 4 * n;
+  const double* s;
+  __device__ double DT(int l, int i) const { return s[l * n + i]; }
+  __device__ double DhT(int l, int i) const { return s[n * n + l * n + i]; }
+  __device__ double DVS(int l, int i) const { return s[2 * n * n + l * n + i]; }
+  __device__ double Lm(int l) const { return s[3 * n * n + l]; }
+  __device__ double Lp(int l) const { return s[3 * n * n + n + l]; }
+  __device__ double LhM(int l) const { return s[3 * n * n + 2 * n + l]; }
+  __device__ double LhP(int l) const { return s[3 * n * n + 3 * n + l]; }
+};
+
+// =====================================================================================================
+// k_prep: eos.f90:ConsToPrim (volume), prolongtoface.t90:ProlongToFace, equation.f90:GetPrimitiveStateSurface
+// =====================================================================================================
+template <int n, bool GL>
+__global__ void __launch_bounds__(Shape<n>::THREADS) k_prep(Dev d, Basis B) {
+  using S = Shape<n>;
+  constexpr int n2 = S::n2, n3 = S::n3, EPB = S::EPB, N = S::N;
+  extern __shared__ double smem[];
+  double* sD = smem;
+  double* sU = smem + SBasis<n>::SIZE;         // [EPB][5][n3]
+  double* sP = sU + EPB * 5 * n3;              // [EPB][VP_NF][n3]
+  load_basis_smem<n>(B, sD);
+  SBasis<n> Bs{sD};
+  const int e0 = blockIdx.x * EPB;
+  for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
+    const int es = t / n3, x = t - es * n3, e = e0 + es;
+    if (e >= d.nElems) continue;
+    double u[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) u[v] = d.U[((size_t)e * 5 + v) * n3 + x];
+    const double srho = 1.0 / u[0];
+    const double vx = u[1] * srho, vy = u[2] * srho, vz = u[3] * srho;
+    const double p = B.kappaM1 * (u[4] - 0.5 * (u[1] * vx + u[2] * vy + u[3] * vz));
+    const double T = p * srho * B.sR;
+    const double pr[VP_NF] = {srho, vx, vy, vz, p, T};
+#pragma unroll
+    for (int f = 0; f < VP_NF; ++f) {
+      d.prim[((size_t)e * VP_NF + f) * n3 + x] = pr[f];
+      sP[(es * VP_NF + f) * n3 + x] = pr[f];
+    }
+#pragma unroll
+    for (int v = 0; v < 5; ++v) sU[(es * 5 + v) * n3 + x] = u[v];
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < EPB * 6 * n2; t += blockDim.x) {
+    const int es = t / (6 * n2), r = t - es * 6 * n2, lsi = r / n2, pq = r - lsi * n2;
+    const int e = e0 + es;
+    if (e >= d.nElems) continue;
+    const int ls = lsi + 1, p = pq % n, q = pq / n;
+    const int code = d.elemSide[e * 6 + lsi], s = code >> 3, flip = code & 7;
+    int a, b;
+    side_to_vol2(N, p, q, flip, ls, a, b);
+    double fs[FS_NF];
+    if (GL) {
+      const int x = face_node(ls, a, b, side_is_minus(ls) ? 0 : N, n);
+      fs[FS_RHO] = sU[(es * 5 + 0) * n3 + x];
+      fs[FS_E] = sU[(es * 5 + 4) * n3 + x];
+      fs[FS_SRHO] = sP[(es * VP_NF + VP_SRHO) * n3 + x];
+      fs[FS_U] = sP[(es * VP_NF + VP_U) * n3 + x];
+      fs[FS_V] = sP[(es * VP_NF + VP_V) * n3 + x];
+      fs[FS_W] = sP[(es * VP_NF + VP_W) * n3 + x];
+      fs[FS_P] = sP[(es * VP_NF + VP_P) * n3 + x];
+      fs[FS_T] = sP[(es * VP_NF + VP_T) * n3 + x];
+    } else {
+      const bool minus = side_is_minus(ls);
+      double c[5] = {0., 0., 0., 0., 0.};
+#pragma unroll
+      for (int l = 0; l < n; ++l) {
+        const int x = face_node(ls, a, b, l, n);
+        const double L = minus ? Bs.Lm(l) : Bs.Lp(l);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) c[v] = fma(sU[(es * 5 + v) * n3 + x], L, c[v]);
+      }
+      const double srho = 1.0 / c[0];
+      const double vx = c[1] * srho, vy = c[2] * srho, vz = c[3] * srho;
+      const double pp = B.kappaM1 * (c[4] - 0.5 * (c[1] * vx + c[2] * vy + c[3] * vz));
+      fs[FS_RHO] = c[0]; fs[FS_E] = c[4]; fs[FS_SRHO] = srho;
+      fs[FS_U] = vx; fs[FS_V] = vy; fs[FS_W] = vz; fs[FS_P] = pp; fs[FS_T] = pp * srho * B.sR;
+    }
+    double* dst = (flip == 0 ? d.faceM : d.faceS) + (size_t)s * FS_NF * n2 + pq;
+#pragma unroll
+    for (int f = 0; f < FS_NF; ++f) dst[f * n2] = fs[f];
+  }
+}
+
+// =====================================================================================================
+// k_lift: lifting_br1.t90 / lifting_br2.t90 (strong or weak BR1, BR2), non-conservative volume part
+// (lifting_volint.t90:Lifting_VolInt_Nonconservative), surface part, ApplyJacobianLifting,
+// ProlongToFaceLifting.
+// =====================================================================================================
+template <int n, bool GL>
+__global__ void __launch_bounds__(Shape<n>::THREADS) k_lift(Dev d, Basis B) {
+  using S = Shape<n>;
+  constexpr int n2 = S::n2, n3 = S::n3, EPB = S::EPB, N = S::N;
+  extern __shared__ double smem[];
+  double* sD = smem;
+  double* sL = smem + SBasis<n>::SIZE;   // [EPB][4][n3] lifting variables u,v,w,T
+  double* sF = sL + EPB * 4 * n3;        // [EPB][6][n2][4] surface lifting flux (times SurfElem), local face order
+  double* sN = sF + EPB * 6 * n2 * 4;    // [EPB][6][n2][3] face normal of the side point mapped to local face order
+  double* sG = sN + EPB * 6 * n2 * 3;    // [EPB][12][n3] gradients for the prolongation
+  double* sJs = sG + EPB * 12 * n3;      // [EPB][n3]
+  load_basis_smem<n>(B, sD);
+  SBasis<n> Bs{sD};
+  const int e0 = blockIdx.x * EPB;
+  const bool br2 = B.lifting == 2;
+  for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
+    const int es = t / n3, x = t - es * n3, e = e0 + es;
+    if (e >= d.nElems) continue;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) sL[(es * 4 + v) * n3 + x] = d.prim[((size_t)e * VP_NF + VP_U + v) * n3 + x];
+    sJs[es * n3 + x] = d.sJ[(size_t)e * n3 + x];
+  }
+  // surface lifting fluxes of the six sides (lifting_fillflux.t90), stored in this element's face order
+  const double sig = B.weakLifting ? 1.0 : -1.0;
+  for (int t = threadIdx.x; t < EPB * 6 * n2; t += blockDim.x) {
+    const int es = t / (6 * n2), r = t - es * 6 * n2, lsi = r / n2, pq = r - lsi * n2;
+    const int e = e0 + es;
+    if (e >= d.nElems) continue;
+    const int ls = lsi + 1, p = pq % n, q = pq / n;
+    const int code = d.elemSide[e * 6 + lsi], s = code >> 3, flip = code & 7;
+    int a, b;
+    side_to_vol2(N, p, q, flip, ls, a, b);
+    const double* gm = d.geo + (size_t)s * FG_NF * n2 + pq;
+    const double se = gm[FG_SURF * n2];
+    const double* fm = d.faceM + (size_t)s * FS_NF * n2 + pq;
+    double F[4];
+    if (s < d.nBCSides) {
+      // getboundaryflux.f90:Lifting_GetBoundaryFlux, no-slip walls (BC 3/4)
+      const int bt = d.bcType[s];
+      const double Tb = (bt == 4) ? d.bcTwall[s] : fm[FS_T * n2];
+      const double bval[4] = {0., 0., 0., Tb};
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const double um = fm[(FS_U + (v < 3 ? v : 3)) * n2];
+        const double f = B.weakLifting ? bval[v] : bval[v] - um;
+        F[v] = f * se;
+      }
+    } else {
+      const double* fsl = d.faceS + (size_t)s * FS_NF * n2 + pq;
+      const double hs = 0.5 * se;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const int f = FS_U + (v < 3 ? v : 3);
+        F[v] = (sig * fm[f * n2] + fsl[f * n2]) * hs;
+      }
+      // slave side of a weak lifting integrates -Flux
+      if (flip != 0 && B.weakLifting) for (int v = 0; v < 4; ++v) F[v] = -F[v];
+    }
+    const int o = ((es * 6 + lsi) * n2 + a + n * b);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) sF[o * 4 + v] = F[v];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) sN[o * 3 + c] = gm[(FG_NX + c) * n2];
+  }
+  __syncthreads();
+  // volume gradient: d/dxi via D_T sweeps, contravariant -> Cartesian with the metrics
+  for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
+    const int es = t / n3, x = t - es * n3, e = e0 + es;
+    if (e >= d.nElems) continue;
+    const int i = x % n, j = (x / n) % n, k = x / n2;
+    const double* L = sL + es * 4 * n3;
+    double gx[4], ge[4], gz[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) { gx[v] = 0.; ge[v] = 0.; gz[v] = 0.; }
+#pragma unroll
+    for (int l = 0; l < n; ++l) {
+      const double dxi = Bs.DT(l, i), deta = Bs.DT(l, j), dzeta = Bs.DT(l, k);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        gx[v] = fma(dxi, L[v * n3 + l + n * (j + n * k)], gx[v]);
+        ge[v] = fma(deta, L[v * n3 + i + n * (l + n * k)], ge[v]);
+        gz[v] = fma(dzeta, L[v * n3 + i + n * (j + n * l)], gz[v]);
+      }
+    }
+    double m[9];
+#pragma unroll
+    for (int c = 0; c < 9; ++c) m[c] = d.metr[((size_t)e * 9 + c) * n3 + x];
+    double g[12];
+#pragma unroll
+    for (int dd = 0; dd < 3; ++dd)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) g[4 * dd + v] = m[dd] * gx[v] + m[3 + dd] * ge[v] + m[6 + dd] * gz[v];
+    const double sj = sJs[es * n3 + x];
+    // surface contributions along the three normal lines through this node (DoSurfIntLifting)
+    double sg[12];
+#pragma unroll
+    for (int c = 0; c < 12; ++c) sg[c] = 0.;
+    const int idx3[3] = {i, j, k};
+#pragma unroll
+    for (int dir = 0; dir < 3; ++dir) {
+      const int lsM = dir == 0 ? XI_MINUS : (dir == 1 ? ETA_MINUS : ZETA_MINUS);
+      const int lsP = dir == 0 ? XI_PLUS : (dir == 1 ? ETA_PLUS : ZETA_PLUS);
+      const int a = dir == 0 ? j : i, b = dir == 2 ? j : k;
+      const int l = idx3[dir];
+      double wM, wP;
+      if (GL) { wM = (l == 0) ? Bs.LhM(0) : 0.; wP = (l == N) ? Bs.LhP(N) : 0.; }
+      else { wM = Bs.LhM(l); wP = Bs.LhP(l); }
+      if (wM != 0.) {
+        const int o = (es * 6 + lsM - 1) * n2 + a + n * b;
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          const double f = sF[o * 4 + v] * wM;
+#pragma unroll
+          for (int c = 0; c < 3; ++c) sg[4 * c + v] = fma(f, sN[o * 3 + c], sg[4 * c + v]);
+        }
+      }
+      if (wP != 0.) {
+        const int o = (es * 6 + lsP - 1) * n2 + a + n * b;
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          const double f = sF[o * 4 + v] * wP;
+#pragma unroll
+          for (int c = 0; c < 3; ++c) sg[4 * c + v] = fma(f, sN[o * 3 + c], sg[4 * c + v]);
+        }
+      }
+    }
+    // BR1: face gradients are prolonged from the full gradient; BR2: from the volume part only
+#pragma unroll
+    for (int c = 0; c < 12; ++c) {
+      const double full = (g[c] + sg[c]) * sj;
+      d.grad[((size_t)e * 12 + c) * n3 + x] = full;
+      sG[(es * 12 + c) * n3 + x] = br2 ? g[c] * sj : full;
+    }
+  }
+  __syncthreads();
+  // ProlongToFaceLifting (+ BR2: eta * lifting contribution of this face, lifting_br2.t90:Lifting_SurfInt_BR2)
+  for (int t = threadIdx.x; t < EPB * 6 * n2; t += blockDim.x) {
+    const int es = t / (6 * n2), r = t - es * 6 * n2, lsi = r / n2, pq = r - lsi * n2;
+    const int e = e0 + es;
+    if (e >= d.nElems) continue;
+    const int ls = lsi + 1, p = pq % n, q = pq / n;
+    const int code = d.elemSide[e * 6 + lsi], s = code >> 3, flip = code & 7;
+    int a, b;
+    side_to_vol2(N, p, q, flip, ls, a, b);
+    const bool minus = side_is_minus(ls);
+    double gf[12];
+    if (GL) {
+      const int x = face_node(ls, a, b, minus ? 0 : N, n);
+#pragma unroll
+      for (int c = 0; c < 12; ++c) gf[c] = sG[(es * 12 + c) * n3 + x];
+    } else {
+#pragma unroll
+      for (int c = 0; c < 12; ++c) gf[c] = 0.;
+#pragma unroll
+      for (int l = 0; l < n; ++l) {
+        const int x = face_node(ls, a, b, l, n);
+        const double L = minus ? Bs.Lm(l) : Bs.Lp(l);
+#pragma unroll
+        for (int c = 0; c < 12; ++c) gf[c] = fma(sG[(es * 12 + c) * n3 + x], L, gf[c]);
+      }
+    }
+    if (br2) {
+      double eta = B.etaBR2;
+      if (s < d.nBCSides && (d.bcType[s] == 3 || d.bcType[s] == 4)) eta = B.etaBR2_wall;
+      // sum_l L_Minus(l) * L_HatMinus(l) * sJ(node at distance l from this face)
+      double wsum = 0.;
+      if (GL) {
+        wsum = Bs.Lm(0) * Bs.LhM(0) * sJs[es * n3 + face_node(ls, a, b, minus ? 0 : N, n)];
+      } else {
+#pragma unroll
+        for (int l = 0; l < n; ++l) wsum = fma(Bs.Lm(l) * Bs.LhM(l), sJs[es * n3 + face_node(ls, a, b, minus ? l : N - l, n)], wsum);
+      }
+      const int o = (es * 6 + lsi) * n2 + a + n * b;
+      const double ew = eta * wsum;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const double f = sF[o * 4 + v] * ew;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) gf[4 * c + v] = fma(f, sN[o * 3 + c], gf[4 * c + v]);
+      }
+    }
+    double* dst = (flip == 0 ? d.gradM : d.gradS) + (size_t)s * 12 * n2 + pq;
+#pragma unroll
+    for (int c = 0; c < 12; ++c) dst[c * n2] = gf[c];
+  }
+}
+
+// =====================================================================================================
+// k_flux: fillflux.f90:FillFlux -- riemann.f90:Riemann_Side + ViscousFlux_Side on inner sides,
+// getboundaryflux.f90:GetBoundaryFlux (no-slip walls) on BC sides, times SurfElem.
+// =====================================================================================================
+template <int n>
+__global__ void __launch_bounds__(128) k_flux(Dev d, Basis B) {
+  constexpr int n2 = n * n;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = idx / n2, pq = idx - s * n2;
+  if (s >= d.nSides) return;
+  const double* gm = d.geo + (size_t)s * FG_NF * n2 + pq;
+  double nv[3], t1[3], t2[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) { nv[c] = gm[(FG_NX + c) * n2]; t1[c] = gm[(FG_T1X + c) * n2]; t2[c] = gm[(FG_T2X + c) * n2]; }
+  const double se = gm[FG_SURF * n2];
+  const double mu = d.mu0[d.sideInst[s]];
+  const double lam = mu * B.lambdaFac;
+  const double* fm = d.faceM + (size_t)s * FS_NF * n2 + pq;
+  double gL[12];
+#pragma unroll
+  for (int c = 0; c < 12; ++c) gL[c] = d.gradM[((size_t)s * 12 + c) * n2 + pq];
+  double F[5];
+  if (s < d.nBCSides) {
+    const int bt = d.bcType[s];
+    const double rho = fm[FS_RHO * n2], p = fm[FS_P * n2];
+    const double vn = fm[FS_U * n2] * nv[0] + fm[FS_V * n2] * nv[1] + fm[FS_W * n2] * nv[2];
+    const double pb = pressure_riemann(B, rho, vn, p);
+    F[0] = 0.;
+    F[1] = pb * nv[0]; F[2] = pb * nv[1]; F[3] = pb * nv[2];
+    F[4] = 0.;
+    double Fv[5];
+    visc_flux_dir(mu, lam, 0., 0., 0., gL, nv[0], nv[1], nv[2], Fv);
+    F[1] += Fv[1]; F[2] += Fv[2]; F[3] += Fv[3];
+    if (bt != 3) F[4] += Fv[4];
+  } else {
+    const double* fs = d.faceS + (size_t)s * FS_NF * n2 + pq;
+    RotState L, R;
+    const double uL = fm[FS_U * n2], vL = fm[FS_V * n2], wL = fm[FS_W * n2];
+    const double uR = fs[FS_U * n2], vR = fs[FS_V * n2], wR = fs[FS_W * n2];
+    L.rho = fm[FS_RHO * n2]; L.srho = fm[FS_SRHO * n2]; L.E = fm[FS_E * n2]; L.p = fm[FS_P * n2];
+    R.rho = fs[FS_RHO * n2]; R.srho = fs[FS_SRHO * n2]; R.E = fs[FS_E * n2]; R.p = fs[FS_P * n2];
+    L.v1 = uL * nv[0] + vL * nv[1] + wL * nv[2];
+    L.v2 = uL * t1[0] + vL * t1[1] + wL * t1[2];
+    L.v3 = uL * t2[0] + vL * t2[1] + wL * t2[2];
+    R.v1 = uR * nv[0] + vR * nv[1] + wR * nv[2];
+    R.v2 = uR * t1[0] + vR * t1[1] + wR * t1[2];
+    R.v3 = uR * t2[0] + vR * t2[1] + wR * t2[2];
+    double Fr[5];
+    riemann_rotated(B.riemann, B.splitDG, B, L, R, Fr);
+    F[0] = Fr[0];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) F[1 + c] = nv[c] * Fr[1] + t1[c] * Fr[2] + t2[c] * Fr[3];
+    F[4] = Fr[4];
+    double gR[12];
+#pragma unroll
+    for (int c = 0; c < 12; ++c) gR[c] = d.gradS[((size_t)s * 12 + c) * n2 + pq];
+    double FvL[5], FvR[5];
+    visc_flux_dir(mu, lam, uL, vL, wL, gL, nv[0], nv[1], nv[2], FvL);
+    visc_flux_dir(mu, lam, uR, vR, wR, gR, nv[0], nv[1], nv[2], FvR);
+#pragma unroll
+    for (int v = 1; v < 5; ++v) F[v] += 0.5 * (FvL[v] + FvR[v]);
+  }
+#pragma unroll
+  for (int v = 0; v < 5; ++v) d.flux[((size_t)s * 5 + v) * n2 + pq] = F[v] * se;
+}
+
+// stage parameters of the fused LSERK update
+struct Stage {
+  int mode;        // 0: write Ut only (fg_time_derivative); 1: first RK stage; 2: later RK stage
+  double rkA;      // RKA(stage) (stage >= 2)
+  double rkB;      // RKb(stage)
+};
+
+// surface integral + Jacobian + source + RK update for the node owned by this thread
+template <int n, bool GL>
+__device__ __forceinline__ void finish_node(const Dev& d, const SBasis<n>& Bs, const Stage& st, const double* sFl, int es, int e, int x,
+                                            double* ut) {
+  constexpr int n2 = n * n, n3 = n * n * n, N = n - 1;
+  const int i = x % n, j = (x / n) % n, k = x / n2;
+  const int idx3[3] = {i, j, k};
+#pragma unroll
+  for (int dir = 0; dir < 3; ++dir) {
+    const int lsM = dir == 0 ? XI_MINUS : (dir == 1 ? ETA_MINUS : ZETA_MINUS);
+    const int lsP = dir == 0 ? XI_PLUS : (dir == 1 ? ETA_PLUS : ZETA_PLUS);
+    const int a = dir == 0 ? j : i, b = dir == 2 ? j : k;
+    const int l = idx3[dir];
+    double wM, wP;
+    if (GL) { wM = (l == 0) ? Bs.LhM(0) : 0.; wP = (l == N) ? Bs.LhP(N) : 0.; }
+    else { wM = Bs.LhM(l); wP = Bs.LhP(l); }
+    if (wM != 0.) {
+      const int o = (es * 6 + lsM - 1) * n2 + a + n * b;
+#pragma unroll
+      for (int v = 0; v < 5; ++v) ut[v] = fma(sFl[o * 5 + v], wM, ut[v]);
+    }
+    if (wP != 0.) {
+      const int o = (es * 6 + lsP - 1) * n2 + a + n * b;
+#pragma unroll
+      for (int v = 0; v < 5; ++v) ut[v] = fma(sFl[o * 5 + v], wP, ut[v]);
+    }
+  }
+  const double sj = d.sJ[(size_t)e * n3 + x];
+  const int inst = d.elemInst[e];
+  const double dpdx = d.dpdx[inst];
+  const double msj = -sj;
+#pragma unroll
+  for (int v = 0; v < 5; ++v) ut[v] *= msj;
+  if (dpdx != 0.) {  // channel testcase.f90:TestcaseSource, applied before ApplyJacobian
+    ut[1] -= dpdx;
+    ut[4] -= dpdx * d.bulkVel[inst];
+  }
+  if (st.mode == 0) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) d.Ut[((size_t)e * 5 + v) * n3 + x] = ut[v];
+    return;
+  }
+  const double bdt = st.rkB * d.dt[inst];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    const size_t o = ((size_t)e * 5 + v) * n3 + x;
+    double r = ut[v];
+    if (st.mode == 2) r = fma(-st.rkA, d.Ut_tmp[o], r);
+    d.Ut_tmp[o] = r;
+    d.U[o] = fma(bdt, r, d.U[o]);
+  }
+}
+
+// loads the six sides' numerical fluxes into shared memory in this element's face order,
+// with the sign of the slave side (surfint.t90: -Flux_slave)
+template <int n>
+__device__ __forceinline__ void load_face_fluxes(const Dev& d, double* sFl, int e0) {
+  constexpr int n2 = n * n, EPB = Shape<n>::EPB, N = n - 1;
+  for (int t = threadIdx.x; t < EPB * 6 * n2; t += blockDim.x) {
+    const int es = t / (6 * n2), r = t - es * 6 * n2, lsi = r / n2, pq = r - lsi * n2;
+    const int e = e0 + es;
+    if (e >= d.nElems) continue;
+    const int ls = lsi + 1, p = pq % n, q = pq / n;
+    const int code = d.elemSide[e * 6 + lsi], s = code >> 3, flip = code & 7;
+    int a, b;
+    side_to_vol2(N, p, q, flip, ls, a, b);
+    const int o = (es * 6 + lsi) * n2 + a + n * b;
+    const double sg = flip == 0 ? 1.0 : -1.0;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) sFl[o * 5 + v] = sg * d.flux[((size_t)s * 5 + v) * n2 + pq];
+  }
+}
+
+// =====================================================================================================
+// k_vol_weak: volint.f90:VolInt_weakForm (advective + viscous fluxes, VolInt_Metrics, D_Hat^T sweeps),
+// surfint.t90:SurfInt, Ut=-Ut, ApplyJacobian, and the LSERK stage update.
+// =====================================================================================================
+template <int n, bool GL>
+__global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_weak(Dev d, Basis B, Stage st) {
+  using S = Shape<n>;
+  constexpr int n2 = S::n2, n3 = S::n3, EPB = S::EPB;
+  extern __shared__ double smem[];
+  double* sD = smem;
+  double* sT = smem + SBasis<n>::SIZE;   // [EPB][15][n3] transformed fluxes f~(5) g~(5) h~(5)
+  double* sFl = sT + EPB * 15 * n3;      // [EPB][6][n2][5]
+  load_basis_smem<n>(B, sD);
+  SBasis<n> Bs{sD};
+  const int e0 = blockIdx.x * EPB;
+  load_face_fluxes<n>(d, sFl, e0);
+  for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
+    const int es = t / n3, x = t - es * n3, e = e0 + es;
+    if (e >= d.nElems) continue;
+    double u[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) u[v] = d.U[((size_t)e * 5 + v) * n3 + x];
+    const double vx = d.prim[((size_t)e * VP_NF + VP_U) * n3 + x];
+    const double vy = d.prim[((size_t)e * VP_NF + VP_V) * n3 + x];
+    const double vz = d.prim[((size_t)e * VP_NF + VP_W) * n3 + x];
+    const double p = d.prim[((size_t)e * VP_NF + VP_P) * n3 + x];
+    double g[12];
+#pragma unroll
+    for (int c = 0; c < 12; ++c) g[c] = d.grad[((size_t)e * 12 + c) * n3 + x];
+    const double mu = d.mu0[d.elemInst[e]];
+    const double lam = mu * B.lambdaFac;
+    // physical flux (advective + viscous, flux.f90:EvalFlux3D_Point + EvalDiffFlux3D_Point)
+    const double div = g[0] + g[5] + g[10];
+    const double mdiv = (2.0 / 3.0) * div;
+    const double txx = mu * (2.0 * g[0] - mdiv), tyy = mu * (2.0 * g[5] - mdiv), tzz = mu * (2.0 * g[10] - mdiv);
+    const double txy = mu * (g[4] + g[1]), txz = mu * (g[8] + g[2]), tyz = mu * (g[9] + g[6]);
+    const double Ep = u[4] + p;
+    double f[5], gg[5], h[5];
+    f[0] = u[1];
+    f[1] = fma(u[1], vx, p) - txx;
+    f[2] = u[1] * vy - txy;
+    f[3] = u[1] * vz - txz;
+    f[4] = Ep * vx - (txx * vx + txy * vy + txz * vz) - lam * g[3];
+    gg[0] = u[2];
+    gg[1] = u[2] * vx - txy;
+    gg[2] = fma(u[2], vy, p) - tyy;
+    gg[3] = u[2] * vz - tyz;
+    gg[4] = Ep * vy - (txy * vx + tyy * vy + tyz * vz) - lam * g[7];
+    h[0] = u[3];
+    h[1] = u[3] * vx - txz;
+    h[2] = u[3] * vy - tyz;
+    h[3] = fma(u[3], vz, p) - tzz;
+    h[4] = Ep * vz - (txz * vx + tyz * vy + tzz * vz) - lam * g[11];
+    // VolInt_Metrics
+#pragma unroll
+    for (int dd = 0; dd < 3; ++dd) {
+      const double m1 = d.metr[((size_t)e * 9 + 3 * dd + 0) * n3 + x];
+      const double m2 = d.metr[((size_t)e * 9 + 3 * dd + 1) * n3 + x];
+      const double m3 = d.metr[((size_t)e * 9 + 3 * dd + 2) * n3 + x];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) sT[(es * 15 + 5 * dd + v) * n3 + x] = f[v] * m1 + gg[v] * m2 + h[v] * m3;
+    }
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
+    const int es = t / n3, x = t - es * n3, e = e0 + es;
+    if (e >= d.nElems) continue;
+    const int i = x % n, j = (x / n) % n, k = x / n2;
+    const double* T = sT + es * 15 * n3;
+    double ut[5] = {0., 0., 0., 0., 0.};
+#pragma unroll
+    for (int l = 0; l < n; ++l) {
+      const double ci = Bs.DhT(l, i), cj = Bs.DhT(l, j), ck = Bs.DhT(l, k);
+      const int xi = l + n * (j + n * k), xj = i + n * (l + n * k), xk = i + n * (j + n * l);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        ut[v] = fma(ci, T[v * n3 + xi], ut[v]);
+        ut[v] = fma(cj, T[(5 + v) * n3 + xj], ut[v]);
+        ut[v] = fma(ck, T[(10 + v) * n3 + xk], ut[v]);
+      }
+    }
+    finish_node<n, GL>(d, Bs, st, sFl, es, e, x, ut);
+  }
+}
+
+// =====================================================================================================
+// k_vol_split: volint.f90:VolInt_splitForm with SplitVolumeFluxPI / SD (Gauss-Lobatto nodes, 8 nodes
+// per line handled by an 8-lane segment of a warp), viscous part in weak form, surface integral,
+// Jacobian, LSERK update. Each two-point flux of a line is evaluated once: lane a evaluates the pair
+// (a, a+dd mod n) for dd = 1..n/2-1, keeps its own share and hands the partner's share over with a
+// warp shuffle; the pairs at distance n/2 are evaluated by both lanes.
+// =====================================================================================================
+template <int n>
+__global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_split(Dev d, Basis B, Stage st) {
+  using S = Shape<n>;
+  constexpr int n2 = S::n2, n3 = S::n3, EPB = S::EPB;
+  static_assert(n == 8 || n == 4 || n == 2, "split kernel expects 2, 4 or 8 nodes per line");
+  extern __shared__ double smem[];
+  double* sD = smem;
+  double* sV = smem + SBasis<n>::SIZE;  // [EPB][12][n3] transformed viscous fluxes (mom1..3, ener) x 3 directions
+  double* sQ = sV + EPB * 12 * n3;      // [EPB][6][n3] rho, u, v, w, 4p, H
+  double* sM = sQ + EPB * 6 * n3;       // [EPB][9][n3] metrics
+  double* sA = sM + EPB * 9 * n3;       // [EPB][5][n3] accumulated split-flux divergence
+  double* sFl = sA + EPB * 5 * n3;      // [EPB][6][n2][5]
+  load_basis_smem<n>(B, sD);
+  SBasis<n> Bs{sD};
+  const int e0 = blockIdx.x * EPB;
+  load_face_fluxes<n>(d, sFl, e0);
+  const bool pi = B.splitDG == 4;
+  for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
+    const int es = t / n3, x = t - es * n3, e = e0 + es;
+    if (e >= d.nElems) continue;
+    double u[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) u[v] = d.U[((size_t)e * 5 + v) * n3 + x];
+    const double srho = d.prim[((size_t)e * VP_NF + VP_SRHO) * n3 + x];
+    const double vx = d.prim[((size_t)e * VP_NF + VP_U) * n3 + x];
+    const double vy = d.prim[((size_t)e * VP_NF + VP_V) * n3 + x];
+    const double vz = d.prim[((size_t)e * VP_NF + VP_W) * n3 + x];
+    const double p = d.prim[((size_t)e * VP_NF + VP_P) * n3 + x];
+    double m[9];
+#pragma unroll
+    for (int c = 0; c < 9; ++c) { m[c] = d.metr[((size_t)e * 9 + c) * n3 + x]; sM[(es * 9 + c) * n3 + x] = m[c]; }
+    sQ[(es * 6 + 0) * n3 + x] = u[0];
+    sQ[(es * 6 + 1) * n3 + x] = vx;
+    sQ[(es * 6 + 2) * n3 + x] = vy;
+    sQ[(es * 6 + 3) * n3 + x] = vz;
+    if (pi) {
+      sQ[(es * 6 + 4) * n3 + x] = 4.0 * p;
+      sQ[(es * 6 + 5) * n3 + x] = (u[4] + p) * srho;
+    } else {
+      sQ[(es * 6 + 4) * n3 + x] = p;
+      sQ[(es * 6 + 5) * n3 + x] = u[4] + p;
+    }
+    double g[12];
+#pragma unroll
+    for (int c = 0; c < 12; ++c) g[c] = d.grad[((size_t)e * 12 + c) * n3 + x];
+    const double mu = d.mu0[d.elemInst[e]];
+    const double lam = mu * B.lambdaFac;
+#pragma unroll
+    for (int dd = 0; dd < 3; ++dd) {
+      double Fv[5];
+      visc_flux_dir(mu, lam, vx, vy, vz, g, m[3 * dd], m[3 * dd + 1], m[3 * dd + 2], Fv);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) sV[(es * 12 + 4 * dd + v) * n3 + x] = Fv[1 + v];
+    }
+#pragma unroll
+    for (int v = 0; v < 5; ++v) sA[(es * 5 + v) * n3 + x] = 0.;
+  }
+  __syncthreads();
+  // split-flux divergence, one direction at a time
+  const int lane = threadIdx.x & 31;
+  const int segBase = lane & ~(n - 1);
+#pragma unroll 1
+  for (int dir = 0; dir < 3; ++dir) {
+    for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
+      const int es = t / n3, r = t - es * n3;
+      const int e = e0 + es;
+      const bool valid = e < d.nElems;
+      const int a = r % n, c1 = (r / n) % n, c2 = r / n2;  // a = index along the line
+      int xa;
+      if (dir == 0) xa = a + n * (c1 + n * c2);
+      else if (dir == 1) xa = c1 + n * (a + n * c2);
+      else xa = c1 + n * (c2 + n * a);
+      const int stride = dir == 0 ? 1 : (dir == 1 ? n : n2);
+      const int xline = xa - a * stride;
+      const double* Q = sQ + es * 6 * n3;
+      const double* Mm = sM + (es * 9 + 3 * dir) * n3;
+      const double ra = Q[xa], ua = Q[n3 + xa], va = Q[2 * n3 + xa], wa = Q[3 * n3 + xa], pa = Q[4 * n3 + xa], ha = Q[5 * n3 + xa];
+      const double ma0 = Mm[xa], ma1 = Mm[n3 + xa], ma2 = Mm[2 * n3 + xa];
+      double acc[5] = {0., 0., 0., 0., 0.};
+#pragma unroll
+      for (int dd = 1; dd <= n / 2; ++dd) {
+        const int bI = (a + dd) & (n - 1);
+        const int xb = xline + bI * stride;
+        const double rb = Q[xb], ub = Q[n3 + xb], vb = Q[2 * n3 + xb], wb = Q[3 * n3 + xb], pb = Q[4 * n3 + xb], hb = Q[5 * n3 + xb];
+        const double ms0 = ma0 + Mm[xb], ms1 = ma1 + Mm[n3 + xb], ms2 = ma2 + Mm[2 * n3 + xb];
+        double G[5];
+        double c0, c1o;  // scale factors of the density / other components
+        if (pi) {
+          // SplitVolumeFluxPI in contravariant form: F = 1/4 A (dens), 1/8 (A u_s + 4 p_s m_s), 1/8 A H_s
+          const double rs = ra + rb, us = ua + ub, vs = va + vb, ws = wa + wb, ps4 = pa + pb, hs = ha + hb;
+          const double qs = us * ms0 + vs * ms1 + ws * ms2;
+          const double A = rs * qs;
+          G[0] = A;
+          G[1] = fma(A, us, ps4 * ms0);
+          G[2] = fma(A, vs, ps4 * ms1);
+          G[3] = fma(A, ws, ps4 * ms2);
+          G[4] = A * hs;
+          c0 = 0.25; c1o = 0.125;
+        } else {
+          // SplitVolumeFluxSD: F = 1/2 m_s . (F(a) + F(b)); here sQ holds p and rho*E+p
+          const double qa = ua * ms0 + va * ms1 + wa * ms2, qb = ub * ms0 + vb * ms1 + wb * ms2;
+          const double mqa = ra * qa, mqb = rb * qb;
+          G[0] = mqa + mqb;
+          G[1] = fma(mqa, ua, mqb * ub) + (pa + pb) * ms0;
+          G[2] = fma(mqa, va, mqb * vb) + (pa + pb) * ms1;
+          G[3] = fma(mqa, wa, mqb * wb) + (pa + pb) * ms2;
+          G[4] = fma(ha, qa, hb * qb);
+          c0 = 0.5; c1o = 0.5;
+        }
+        const double cOwn = Bs.DVS(bI, a), cPart = Bs.DVS(a, bI);
+        const double o0 = cOwn * c0, o1 = cOwn * c1o;
+        acc[0] = fma(o0, G[0], acc[0]);
+#pragma unroll
+        for (int v = 1; v < 5; ++v) acc[v] = fma(o1, G[v], acc[v]);
+        if (dd < n / 2) {
+          const double p0 = cPart * c0, p1 = cPart * c1o;
+          const int src = segBase | ((a - dd) & (n - 1));
+          double recv[5];
+          recv[0] = __shfl_sync(0xffffffffu, p0 * G[0], src);
+#pragma unroll
+          for (int v = 1; v < 5; ++v) recv[v] = __shfl_sync(0xffffffffu, p1 * G[v], src);
+#pragma unroll
+          for (int v = 0; v < 5; ++v) acc[v] += recv[v];
+        }
+      }
+      if (valid) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) sA[(es * 5 + v) * n3 + xa] += acc[v];
+      }
+    }
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
+    const int es = t / n3, x = t - es * n3, e = e0 + es;
+    if (e >= d.nElems) continue;
+    const int i = x % n, j = (x / n) % n, k = x / n2;
+    double ut[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) ut[v] = sA[(es * 5 + v) * n3 + x];
+    const double* V = sV + es * 12 * n3;
+#pragma unroll
+    for (int l = 0; l < n; ++l) {
+      const double ci = Bs.DhT(l, i), cj = Bs.DhT(l, j), ck = Bs.DhT(l, k);
+      const int xi = l + n * (j + n * k), xj = i + n * (l + n * k), xk = i + n * (j + n * l);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        ut[1 + v] = fma(ci, V[v * n3 + xi], ut[1 + v]);
+        ut[1 + v] = fma(cj, V[(4 + v) * n3 + xj], ut[1 + v]);
+        ut[1 + v] = fma(ck, V[(8 + v) * n3 + xk], ut[1 + v]);
+      }
+    }
+    finish_node<n, true>(d, Bs, st, sFl, es, e, x, ut);
+  }
+}
+
+// =====================================================================================================
+// k_dt: calctimestep.f90:CALCTIMESTEP per element (convective and viscous eigenvalue bounds with the
+// precomputed MetricsAdv / MetricsVisc), reduced per instance with an atomic minimum on the bit pattern
+// of the (positive) time step; plus the channel bulk velocity partial sums (testcase.f90:CalcForcing).
+// =====================================================================================================
+__device__ __forceinline__ void atomic_min_pos_double(double* addr, double v) {
+  // positive doubles order like their bit patterns
+  atomicMin((unsigned long long*)addr, (unsigned long long)__double_as_longlong(v));
+}
+template <int n>
+__global__ void __launch_bounds__(Shape<n>::THREADS) k_dt(Dev d, Basis B, const double* metAdv, const double* metVisc, double cfl, double dfl,
+                                                          double* bulkPart /* [nElems] or null */, const double* wVol) {
+  using S = Shape<n>;
+  constexpr int n3 = S::n3, EPB = S::EPB;
+  __shared__ double red[S::THREADS / 32][4];
+  const int e0 = blockIdx.x * EPB;
+  const int t = threadIdx.x;
+  const int es = t / n3, x = t - es * n3, e = e0 + es;
+  double lc[3] = {0., 0., 0.}, lv = 0., bp = 0.;
+  bool nanFlag = false;
+  if (es < EPB && e < d.nElems) {
+    double u[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) u[v] = d.U[((size_t)e * 5 + v) * n3 + x];
+    const double srho = 1.0 / u[0];
+    const double vx = u[1] * srho, vy = u[2] * srho, vz = u[3] * srho;
+    const double p = B.kappaM1 * (u[4] - 0.5 * (vx * u[1] + vy * u[2] + vz * u[3]));
+    if (u[0] != u[0]) nanFlag = true;
+    const double c = sqrt(B.kappa * p * srho);
+    const double sj = d.sJ[(size_t)e * n3 + x];
+    const double vs[3] = {vx * sj, vy * sj, vz * sj};
+    double mvs = 0.;
+#pragma unroll
+    for (int dd = 0; dd < 3; ++dd) {
+      const double* mm = d.metr + ((size_t)e * 9 + 3 * dd) * n3 + x;
+      const double q = mm[0] * vs[0] + mm[n3] * vs[1] + mm[2 * n3] * vs[2];
+      lc[dd] = fabs(q) + c * metAdv[((size_t)e * 3 + dd) * n3 + x];
+      mvs += metVisc[((size_t)e * 3 + dd) * n3 + x];
+    }
+    lv = d.mu0[d.elemInst[e]] * srho;
+    // max over nodes of mu*srho*MetricsVisc(d) per direction is taken below; keep the three separately
+    bp = bulkPart ? vx * wVol[x] / sj : 0.;
+    // pack: lc[0..2] convective, viscous per direction via separate loads in the reduction below
+    (void)mvs;
+  }
+  // per-direction maxima over the element's nodes; viscous bounds need per-direction maxima as well
+  double lvd[3] = {0., 0., 0.};
+  if (es < EPB && e < d.nElems) {
+#pragma unroll
+    for (int dd = 0; dd < 3; ++dd) lvd[dd] = lv * metVisc[((size_t)e * 3 + dd) * n3 + x];
+  }
+  if (nanFlag) set_error(d.err, 1);
+  // reduce within the element: EPB elements per block, each of n3 threads; use shared atomics-free
+  // two-level reduction over the element's threads
+  __shared__ double sred[S::THREADS][7];
+  sred[t][0] = lc[0]; sred[t][1] = lc[1]; sred[t][2] = lc[2];
+  sred[t][3] = lvd[0]; sred[t][4] = lvd[1]; sred[t][5] = lvd[2]; sred[t][6] = bp;
+  __syncthreads();
+  if (es < EPB && x == 0 && e < d.nElems) {
+    double m[6] = {0., 0., 0., 0., 0., 0.}, bs = 0.;
+    for (int y = 0; y < n3; ++y) {
+#pragma unroll
+      for (int c = 0; c < 6; ++c) m[c] = fmax(m[c], sred[t + y][c]);
+      bs += sred[t + y][6];
+    }
+    double dtE = cfl * 2.0 / (m[0] + m[1] + m[2]);
+    const double sv = m[3] + m[4] + m[5];
+    if (sv > 0.) dtE = fmin(dtE, dfl * 4.0 / sv);
+    if (!(dtE == dtE)) set_error(d.err, 2);
+    else atomic_min_pos_double(&d.dt[d.elemInst[e]], dtE);
+    if (bulkPart) bulkPart[e] = bs;
+  }
+  (void)red;
+}
+
+}  // namespace fg

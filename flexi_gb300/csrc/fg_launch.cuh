@@ -1,0 +1,21 @@
+// flexi_gb300 -- kernel sets per (nodes per direction, node type); instantiated in fg_inst_*.cu
+#pragma once
+#include "fg_common.cuh"
+
+namespace fg {
+
+struct KernelSet {
+  int n = 0;
+  bool gl = false;
+  void (*prep)(const Dev&, const Basis&, cudaStream_t) = nullptr;
+  void (*lift)(const Dev&, const Basis&, cudaStream_t) = nullptr;
+  void (*flux)(const Dev&, const Basis&, cudaStream_t) = nullptr;
+  void (*vol_weak)(const Dev&, const Basis&, int, double, double, cudaStream_t) = nullptr;
+  void (*vol_split)(const Dev&, const Basis&, int, double, double, cudaStream_t) = nullptr;  // null if unsupported
+  void (*dt)(const Dev&, const Basis&, const double*, const double*, double, double, double*, const double*, cudaStream_t) = nullptr;
+};
+
+// returns the kernel set for n nodes per direction (2..8) and the node type; n == 0 if unsupported
+KernelSet get_kernel_set(int n, bool gl);
+
+}  // namespace fg

@@ -1,0 +1,218 @@
+"""Host-side mirror of FLEXI's module interface for the DGSEM right-hand side and the LSERK stepper.
+
+The methods keep the reference's names and meaning:
+    DGTimeDerivative_weakForm(t)   src/dg/dg.f90:221
+    TimeStepByLSERKW2(t, dt)       src/timedisc/timestep.f90:82 (CarpenterRK4-5, timedisc_vars.f90:199)
+    CalcTimeStep()                 src/equations/navierstokes/calctimestep.f90:89
+    TimeDisc(nSteps)               loop body of src/timedisc/timedisc.f90:190-212 (UpdateTimeStep, CalcForcing, TimeStep)
+Arrays use FLEXI's Fortran layouts, held in numpy with reversed axes: U(1:5,0:N,0:N,0:N,1:nElems) is
+an array of shape (nElems, N+1, N+1, N+1, 5). All work runs in libflexigpu.so on the GPU; a missing
+library or GPU raises instead of falling back to anything else.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .mesh import BoxMesh
+
+NODE_TYPES = {"gauss": 1, "gauss-lobatto": 2}
+RIEMANN = {"lf": 1, "hllc": 2, "roe": 3, "roeentropyfix": 33, "same": -1}
+SPLIT = {"none": -1, "weak": -1, "sd": 0, "pi": 4}
+
+
+class FlexiError(RuntimeError):
+    pass
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def make_config(**kw) -> _lib.FgConfig:
+    """fg_config with the reference defaults, overridden by keyword arguments (ini key names;
+    string values accepted for NodeType, Riemann, RiemannBC, SplitDG, Lifting)."""
+    L = _lib.load()
+    c = _lib.FgConfig()
+    L.fg_config_default(ctypes.byref(c))
+    for k, v in kw.items():
+        if k == "NodeType" and isinstance(v, str):
+            v = NODE_TYPES[v.lower()]
+        elif k in ("Riemann", "RiemannBC") and isinstance(v, str):
+            v = RIEMANN[v.lower()]
+        elif k == "SplitDG" and isinstance(v, str):
+            v = SPLIT[v.lower()]
+        elif k == "Lifting" and isinstance(v, str):
+            v = {"br1": 1, "br2": 2}[v.lower()]
+        if not hasattr(c, k):
+            raise KeyError(k)
+        setattr(c, k, type(getattr(c, k))(v))
+    return c
+
+
+def config_from_ini(text: str) -> _lib.FgConfig:
+    L = _lib.load()
+    c = _lib.FgConfig()
+    L.fg_config_default(ctypes.byref(c))
+    if L.fg_config_from_ini(text.encode(), ctypes.byref(c)) != 0:
+        raise FlexiError("invalid parameter file")
+    return c
+
+
+def config_dict(c: _lib.FgConfig) -> dict:
+    return {name: getattr(c, name) for name, _ in _lib.FgConfig._fields_}
+
+
+class Flexi:
+    """One GPU solver: configuration + mesh + state (an ensemble when the mesh has several instances)."""
+
+    def __init__(self, cfg: _lib.FgConfig, mesh: BoxMesh = None):
+        self.L = _lib.load()
+        self.cfg = cfg
+        h = ctypes.c_void_p()
+        rc = self.L.fg_create(ctypes.byref(cfg), ctypes.byref(h))
+        if rc != 0:
+            raise FlexiError(f"fg_create failed ({rc}): {self.L.fg_last_error(None).decode()}")
+        self.h = h
+        self.N = cfg.N
+        self.n = cfg.N + 1
+        if mesh is not None:
+            self.build_mesh(mesh)
+
+    def _check(self, rc, what):
+        if rc != 0:
+            raise FlexiError(f"{what} failed ({rc}): {self.L.fg_last_error(self.h).decode()}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.fg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---------------------------------------------------------------- mesh
+    def build_mesh(self, m: BoxMesh):
+        nc = np.ascontiguousarray(m.node_coords, np.float64)
+        nb = np.ascontiguousarray(m.elem_nb, np.int32)
+        bt = np.ascontiguousarray(m.boundary_type, np.int32).reshape(-1)
+        rs = np.ascontiguousarray(m.ref_state_prim, np.float64).reshape(-1)
+        inst = None if m.elem_inst is None else np.ascontiguousarray(m.elem_inst, np.int32)
+        self._check(self.L.fg_build_mesh(self.h, m.n_elems, m.ngeo, _p(nc), _p(nb), len(bt) // 2, _p(bt) if len(bt) else None,
+                                         len(rs) // 6, _p(rs) if len(rs) else None, _p(inst) if inst is not None else None),
+                    "fg_build_mesh")
+        self._sizes()
+
+    def set_mesh(self, side_to_elem, elem_to_side, bc, boundary_type, ref_state_prim, Mf, Mg, Mh, sJ, NormVec, TangVec1, TangVec2, SurfElem):
+        """Drop-in path: FLEXI's own processed mesh arrays (MOD_Mesh_Vars)."""
+        a = [np.ascontiguousarray(x) for x in (Mf, Mg, Mh, sJ, NormVec, TangVec1, TangVec2, SurfElem)]
+        s2e = np.ascontiguousarray(side_to_elem, np.int32)
+        e2s = np.ascontiguousarray(elem_to_side, np.int32)
+        bcv = np.ascontiguousarray(bc, np.int32)
+        bt = np.ascontiguousarray(boundary_type, np.int32).reshape(-1)
+        rs = np.ascontiguousarray(ref_state_prim, np.float64).reshape(-1)
+        n_elems = a[3].shape[0]
+        n_sides = s2e.shape[0]
+        self._check(self.L.fg_set_mesh(self.h, n_elems, n_sides, len(bcv), _p(s2e), _p(e2s), _p(bcv) if len(bcv) else None,
+                                       len(bt) // 2, _p(bt) if len(bt) else None, len(rs) // 6, _p(rs) if len(rs) else None,
+                                       *[_p(x) for x in a]), "fg_set_mesh")
+        self._sizes()
+
+    def _sizes(self):
+        s = np.zeros(5, np.int32)
+        self._check(self.L.fg_get_sizes(self.h, _p(s)), "fg_get_sizes")
+        self.n_elems, self.n_sides, self.n_bc_sides, _, self.n_inst = (int(v) for v in s)
+
+    def set_instance_mu0(self, mu0):
+        mu0 = np.ascontiguousarray(mu0, np.float64)
+        self._check(self.L.fg_set_instance_mu0(self.h, len(mu0), _p(mu0)), "fg_set_instance_mu0")
+
+    @property
+    def ushape(self):
+        return (self.n_elems, self.n, self.n, self.n, 5)
+
+    def elem_xgp(self):
+        x = np.empty((self.n_elems, self.n, self.n, self.n, 3))
+        self._check(self.L.fg_get_elem_xgp(self.h, _p(x)), "fg_get_elem_xgp")
+        return x
+
+    def mesh_array(self, name):
+        w = {"Mf": 0, "Mg": 1, "Mh": 2, "sJ": 3, "NormVec": 4, "TangVec1": 5, "TangVec2": 6, "SurfElem": 7}[name]
+        n = self.n
+        shape = {0: (self.n_elems, n, n, n, 3), 1: (self.n_elems, n, n, n, 3), 2: (self.n_elems, n, n, n, 3), 3: (self.n_elems, n, n, n),
+                 4: (self.n_sides, n, n, 3), 5: (self.n_sides, n, n, 3), 6: (self.n_sides, n, n, 3), 7: (self.n_sides, n, n)}[w]
+        out = np.empty(shape)
+        self._check(self.L.fg_get_mesh_array(self.h, w, _p(out)), "fg_get_mesh_array")
+        return out
+
+    def side_to_elem(self):
+        out = np.empty((self.n_sides, 5), np.int32)
+        self._check(self.L.fg_get_side_to_elem(self.h, _p(out)), "fg_get_side_to_elem")
+        return out
+
+    # ---------------------------------------------------------------- state
+    @property
+    def U(self):
+        out = np.empty(self.ushape)
+        self._check(self.L.fg_get_state(self.h, _p(out)), "fg_get_state")
+        return out
+
+    @U.setter
+    def U(self, value):
+        v = np.ascontiguousarray(value, np.float64).reshape(self.ushape)
+        self._check(self.L.fg_set_state(self.h, _p(v)), "fg_set_state")
+
+    def set_state_ptr(self, host_ptr):
+        """U from a raw host pointer (e.g. pinned memory); Fortran layout."""
+        self._check(self.L.fg_set_state(self.h, ctypes.c_void_p(host_ptr)), "fg_set_state")
+
+    def get_state_ptr(self, host_ptr):
+        self._check(self.L.fg_get_state(self.h, ctypes.c_void_p(host_ptr)), "fg_get_state")
+
+    # ---------------------------------------------------------------- operator and stepper
+    def DGTimeDerivative_weakForm(self, t=0.0, out=None):
+        Ut = np.empty(self.ushape) if out is None else out
+        self._check(self.L.fg_time_derivative(self.h, float(t), _p(Ut)), "fg_time_derivative")
+        return Ut
+
+    def CalcTimeStep(self):
+        dt = np.zeros(max(1, getattr(self, "n_inst", 1)))
+        err = ctypes.c_int(0)
+        self._check(self.L.fg_calc_timestep(self.h, _p(dt), ctypes.byref(err)), "fg_calc_timestep")
+        return (float(dt[0]) if len(dt) == 1 else dt), err.value
+
+    def TimeStepByLSERKW2(self, t, dt):
+        tt = ctypes.c_double(t)
+        self._check(self.L.fg_timestep_lserkw2(self.h, ctypes.byref(tt), float(dt)), "fg_timestep_lserkw2")
+        return tt.value
+
+    def TimeDisc(self, n_steps):
+        """n_steps of the TimeDisc loop (dt from CALCTIMESTEP each step, per instance); returns times."""
+        t = np.zeros(self.n_inst)
+        self._check(self.L.fg_run(self.h, int(n_steps), _p(t)), "fg_run")
+        return t
+
+    def gradients(self):
+        n = self.n
+        g = [np.empty((self.n_elems, n, n, n, 4)) for _ in range(3)]
+        self._check(self.L.fg_get_gradients(self.h, _p(g[0]), _p(g[1]), _p(g[2])), "fg_get_gradients")
+        return g
+
+    def stream(self):
+        s = ctypes.c_void_p()
+        self._check(self.L.fg_get_stream(self.h, ctypes.byref(s)), "fg_get_stream")
+        return s.value
+
+    def launch_count(self):
+        return int(self.L.fg_launch_count(self.h))
+
+
+def probe_fp64_tflops():
+    L = _lib.load()
+    v = ctypes.c_double(0.0)
+    if L.fg_probe_fp64(ctypes.byref(v)) != 0:
+        raise FlexiError("fg_probe_fp64 failed: " + L.fg_last_error(None).decode())
+    return v.value

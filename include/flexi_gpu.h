@@ -1,0 +1,162 @@
+/*
+ * flexi_gpu.h -- C ABI of libflexigpu.so, a GB300 (sm_103a) implementation of FLEXI's DGSEM
+ * right-hand side and low-storage Runge-Kutta stepper for the compressible Navier-Stokes equations.
+ *
+ * FLEXI (v25.10) has no C interface for this path; its entry points are Fortran module procedures
+ * operating on module arrays. Each function below names the reference procedure it replaces
+ * (path:line inside the FLEXI source tree). Arrays crossing this interface use FLEXI's Fortran
+ * layouts, e.g. U(1:5,0:N,0:N,0:N,1:nElems), and are host pointers borrowed for the duration of the
+ * call unless stated otherwise. The library copies them into its own device-resident layouts.
+ *
+ * Every function returns 0 on success or a positive FG_ERR_* code; fg_last_error() gives a message.
+ * Device-side failures (NaN density, non-finite time step) are recorded in a sticky error word that
+ * the host reads after each step; nothing traps or aborts.
+ */
+#ifndef FLEXI_GPU_H
+#define FLEXI_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FG_OK 0
+#define FG_ERR_CONFIG 1    /* invalid or unsupported configuration */
+#define FG_ERR_MESH 2      /* mesh could not be processed */
+#define FG_ERR_CUDA 3      /* CUDA runtime error */
+#define FG_ERR_STATE 4     /* call order violated (e.g. no mesh yet) */
+#define FG_ERR_NAN 5       /* NaN density found (calctimestep.f90 errType 1) */
+#define FG_ERR_DT 6        /* non-finite time step (errType 2/3) */
+
+/* Riemann solver ids: the integer values of riemann.f90:44-58 */
+#define FG_RIEMANN_SAME (-1)
+#define FG_RIEMANN_LF 1
+#define FG_RIEMANN_HLLC 2
+#define FG_RIEMANN_ROE 3
+#define FG_RIEMANN_ROEENTROPYFIX 33
+/* SplitDG ids: splitflux.f90:63-69; -1 selects the weak (non-split) form */
+#define FG_SPLIT_NONE (-1)
+#define FG_SPLIT_SD 0
+#define FG_SPLIT_PI 4
+#define FG_NODE_GAUSS 1
+#define FG_NODE_GAUSS_LOBATTO 2
+
+/* Parameters of parameter_flexi.ini for this path (same meaning and defaults as the reference):
+ *   N (interpolation.f90:59), NodeType (CMake FLEXI_NODETYPE), Riemann/RiemannBC (riemann.f90:91-115),
+ *   Lifting 1=BR1 / 2=BR2 (CMake FLEXI_LIFTING), doWeakLifting, doConservativeLifting, etaBR2,
+ *   etaBR2_wall (lifting.f90:61-83), SplitDG (splitflux.f90:77), kappa, R, Pr, mu0 (eos.f90:84-90),
+ *   CFLScale, DFLScale (timedisc_func.f90:463-527), TimeDiscMethod (0 = CarpenterRK4-5),
+ *   and the channel body force of testcase/channel (doTCSource, dpdx). */
+typedef struct fg_config {
+  int N;
+  int NodeType;
+  int Riemann;
+  int RiemannBC;
+  int Lifting;
+  int doWeakLifting;
+  int doConservativeLifting;
+  int SplitDG;
+  double etaBR2;
+  double etaBR2_wall;
+  double kappa;
+  double R;
+  double Pr;
+  double mu0;
+  double CFLScale;
+  double DFLScale;
+  int doTCSource;
+  double dpdx;
+  int TimeDiscMethod;
+} fg_config;
+
+typedef struct fg_handle fg_handle;
+
+/* Defaults of the reference (Riemann=RoeEntropyFix, SplitDG=PI, Lifting=BR1, etaBR2=2, kappa=1.4,
+ * R=287.058, Pr=0.72, mu0=0, CFLScale=DFLScale=0.9, CarpenterRK4-5). */
+int fg_config_default(fg_config* cfg);
+
+/* Parses the keys above from parameter_flexi.ini text (readintools.f90:read_options syntax:
+ * "key = value", "!" comments, case-insensitive keys, string values for Riemann/SplitDG/NodeType/
+ * TimeDiscMethod). Unknown keys are ignored. */
+int fg_config_from_ini(const char* ini_text, fg_config* cfg);
+
+/* Creates a solver on the current CUDA device. Replaces InitDG/InitLifting/InitTimeDisc
+ * (dg.f90:InitDG, lifting.f90:InitLifting, timedisc_func.f90:InitTimeDisc). */
+int fg_create(const fg_config* cfg, fg_handle** out);
+int fg_destroy(fg_handle* h);
+const char* fg_last_error(const fg_handle* h);
+
+/* Mesh from raw element data -- what InitMesh (mesh.f90:82) builds from a HOPR mesh file:
+ * NodeCoords(3,0:NGeo,0:NGeo,0:NGeo,nElems) on equidistant points (mesh_readin.f90:ReadMesh),
+ * ElemNb(3,6,nElems) = (neighbour element 1-based or 0, neighbour local side, BC index) per local side
+ * in FLEXI's local side numbering (flexi.h:90-95), BoundaryType(2,nBCs) = (type, state),
+ * RefStatePrim(6,nRefStates). ElemInst(nElems) (nullable) assigns elements to independent ensemble
+ * instances (0-based). Sides, orientation flips and curl-form metrics are computed here
+ * (prepare_mesh.f90, mappings.f90, metrics.f90:CalcMetrics/CalcSurfMetrics). */
+int fg_build_mesh(fg_handle* h, int nElems, int NGeo, const double* NodeCoords, const int* ElemNb, int nBCs, const int* BoundaryType,
+                  int nRefStates, const double* RefStatePrim, const int* ElemInst);
+
+/* Drop-in mesh: the arrays of MOD_Mesh_Vars (mesh_vars.f90:34-160) after FLEXI's own InitMesh,
+ * SideToElem(5,nSides), ElemToSide(2,6,nElems), BC(nBCSides), Metrics_fTilde/gTilde/hTilde
+ * (3,0:N,0:N,0:N,nElems), sJ(0:N,0:N,0:N,nElems), NormVec/TangVec1/TangVec2(3,0:N,0:N,nSides),
+ * SurfElem(0:N,0:N,nSides). Single rank: no MPI or mortar sides. */
+int fg_set_mesh(fg_handle* h, int nElems, int nSides, int nBCSides, const int* SideToElem, const int* ElemToSide, const int* BC, int nBCs,
+                const int* BoundaryType, int nRefStates, const double* RefStatePrim, const double* Metrics_fTilde,
+                const double* Metrics_gTilde, const double* Metrics_hTilde, const double* sJ, const double* NormVec,
+                const double* TangVec1, const double* TangVec2, const double* SurfElem);
+
+/* Per-instance viscosity (ensembles); default: cfg.mu0 for every instance. */
+int fg_set_instance_mu0(fg_handle* h, int nInst, const double* mu0);
+
+/* Solution coordinates Elem_xGP(3,0:N,0:N,0:N,nElems) (metrics.f90:BuildCoords), fg_build_mesh only. */
+int fg_get_elem_xgp(fg_handle* h, double* Elem_xGP);
+/* Sizes: out[0]=nElems, out[1]=nSides, out[2]=nBCSides, out[3]=N, out[4]=nInstances. */
+int fg_get_sizes(const fg_handle* h, int* out);
+/* Processed metrics in FLEXI layouts, for comparison with FLEXI's own arrays:
+ * which 0..2 = Metrics_f/g/hTilde, 3 = sJ, 4..6 = NormVec/TangVec1/TangVec2 of the master sides,
+ * 7 = SurfElem (side order of this library, see fg_get_side_to_elem). */
+int fg_get_mesh_array(fg_handle* h, int which, double* out);
+/* SideToElem(5,nSides) of this library's side numbering (FLEXI conventions, 1-based). */
+int fg_get_side_to_elem(fg_handle* h, int* out);
+
+/* Solution U(1:5,0:N,0:N,0:N,1:nElems), Fortran layout. */
+int fg_set_state(fg_handle* h, const double* U);
+int fg_get_state(fg_handle* h, double* U);
+/* Device pointer of the state in this library's layout [elem][var][k][j][i] (zero-copy access). */
+int fg_state_device_ptr(fg_handle* h, double** dptr);
+
+/* DGTimeDerivative_weakForm(t) (dg.f90:221): Ut(1:5,0:N,0:N,0:N,1:nElems) of the current state.
+ * Ut may be NULL (result stays on the device). */
+int fg_time_derivative(fg_handle* h, double t, double* Ut);
+
+/* CALCTIMESTEP (calctimestep.f90:89): dt = min over elements of the convective and viscous limits,
+ * per instance; dt[0] is instance 0. errType as in the reference (0 ok, 1 NaN density, 2/3 NaN dt). */
+int fg_calc_timestep(fg_handle* h, double* dt, int* errType);
+
+/* TimeStepByLSERKW2 (timestep.f90:82) with CarpenterRK4-5 (timedisc_vars.f90:199-214): advances the
+ * state by dt (all instances use the same dt here); t is advanced by dt. Includes CalcForcing
+ * (testcase/channel/testcase.f90:262) when the channel body force is active. */
+int fg_timestep_lserkw2(fg_handle* h, double* t, double dt);
+
+/* TimeDisc loop body (timedisc.f90:190-212) for nSteps steps without host synchronisation:
+ * UpdateTimeStep (dt from CALCTIMESTEP, per instance), CalcForcing, TimeStepByLSERKW2; the step
+ * sequence is captured once into a CUDA graph and replayed. t[inst] (nullable) receives the
+ * per-instance times, which start at 0 on the first call and continue on later calls. */
+int fg_run(fg_handle* h, int nSteps, double* t);
+
+/* Lifted gradients of the last right-hand side, gradUx/gradUy/gradUz(4,0:N,0:N,0:N,nElems) of the
+ * lifting variables (v1,v2,v3,T) (lifting_vars.f90, PP_OPTLIFT layout). */
+int fg_get_gradients(fg_handle* h, double* gx, double* gy, double* gz);
+
+/* CUDA stream the handle launches on (cudaStream_t as void*). */
+int fg_get_stream(fg_handle* h, void** stream);
+
+/* Number of kernel launches issued by the last fg_run / fg_timestep_lserkw2 / fg_time_derivative call. */
+long long fg_launch_count(const fg_handle* h);
+
+/* FP64 FMA throughput probe (TFLOP/s, 2 flop per FMA) of the current device, used for the roofline. */
+int fg_probe_fp64(double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FLEXI_GPU_H */

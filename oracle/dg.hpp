@@ -1,0 +1,836 @@
+// TEST INFRASTRUCTURE ONLY -- part of the CPU oracle (restatement of FLEXI v25.10); see basis.hpp.
+//
+// The DGSEM right-hand side for the compressible Navier-Stokes equations, DGTimeDerivative_weakForm
+// (src/dg/dg.f90:221-678), and the low-storage Runge-Kutta stepper TimeStepByLSERKW2
+// (src/timedisc/timestep.f90:82-152). Templated on the scalar type so that a flop-counting scalar can
+// measure the algorithmic flops per DOF and stage. All arrays use FLEXI's Fortran layouts.
+#pragma once
+#include "mesh.hpp"
+#include <atomic>
+#include <type_traits>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace orc {
+
+// ---------------------------------------------------------------------------------------------
+// flop-counting scalar (every +,-,*,/,sqrt counts 1; a*b+c therefore counts 2)
+// ---------------------------------------------------------------------------------------------
+inline long long& flop_counter() { static long long c = 0; return c; }
+struct FD {
+  double v;
+  FD() : v(0.) {}
+  FD(double x) : v(x) {}
+  explicit operator double() const { return v; }
+};
+inline FD operator+(FD a, FD b) { ++flop_counter(); return FD(a.v + b.v); }
+inline FD operator-(FD a, FD b) { ++flop_counter(); return FD(a.v - b.v); }
+inline FD operator*(FD a, FD b) { ++flop_counter(); return FD(a.v * b.v); }
+inline FD operator/(FD a, FD b) { ++flop_counter(); return FD(a.v / b.v); }
+inline FD operator-(FD a) { return FD(-a.v); }
+inline FD& operator+=(FD& a, FD b) { a = a + b; return a; }
+inline FD& operator-=(FD& a, FD b) { a = a - b; return a; }
+inline FD& operator*=(FD& a, FD b) { a = a * b; return a; }
+inline bool operator<(FD a, FD b) { return a.v < b.v; }
+inline bool operator>(FD a, FD b) { return a.v > b.v; }
+inline bool operator<=(FD a, FD b) { return a.v <= b.v; }
+inline bool operator>=(FD a, FD b) { return a.v >= b.v; }
+inline FD sqrt(FD a) { ++flop_counter(); return FD(std::sqrt(a.v)); }
+inline FD fabs(FD a) { return FD(std::fabs(a.v)); }
+inline FD pow(FD a, FD b) { ++flop_counter(); return FD(std::pow(a.v, b.v)); }
+inline double sqrt(double a) { return std::sqrt(a); }
+inline double fabs(double a) { return std::fabs(a); }
+inline double pow(double a, double b) { return std::pow(a, b); }
+inline double val(double x) { return x; }
+inline double val(FD x) { return x.v; }
+template <class R> inline R rmax(R a, R b) { return a < b ? b : a; }
+template <class R> inline R rmin(R a, R b) { return a < b ? a : b; }
+
+// ---------------------------------------------------------------------------------------------
+// configuration (ini keys of parameter_flexi.ini; integer codes as in the reference)
+// ---------------------------------------------------------------------------------------------
+enum { RIEMANN_LF = 1, RIEMANN_HLLC = 2, RIEMANN_ROE = 3, RIEMANN_ROEENTROPYFIX = 33, RIEMANN_SAME = -1 };
+enum { SPLIT_NONE = -1, SPLIT_SD = 0, SPLIT_PI = 4 };
+struct Config {
+  int N = 3, nodeType = NT_GAUSS;
+  int riemann = RIEMANN_ROEENTROPYFIX, riemannBC = RIEMANN_SAME;
+  int lifting = 1;  // 1 BR1, 2 BR2
+  int weakLifting = 0, consLifting = 0;
+  double etaBR2 = 2., etaBR2_wall = -1.;
+  int splitDG = SPLIT_NONE;
+  double kappa = 1.4, R = 287.058, Pr = 0.72, mu0 = 0.;
+  double CFLScale = 0.9, DFLScale = 0.9;
+  int doTCSource = 0;  // channel body force
+  double dpdx = -1.;
+};
+
+// lifting variables (PP_OPTLIFT=1 set): velocity and temperature. The lifted density gradient of the
+// default build never enters Ut for a constant viscosity, so Ut is identical.
+static const int NLIFT = 4;
+static const int PRIM_LIFT[4] = {1, 2, 3, 5};  // 0-based prim indices: v1,v2,v3,T
+
+template <class R>
+struct DG {
+  Config C;
+  DGBasis B;
+  Mesh M;
+  int N = 0, n = 0, nE = 0, nS = 0;
+  R kappa, kappaM1, sKappaM1, Rgas, cp, cv, Pr, mu0, lambdaFac, s23, s43;
+  std::vector<R> U, Ut, UPrim, U_master, U_slave, UPrim_master, UPrim_slave;
+  std::vector<R> gradUx, gradUy, gradUz, gradUx_m, gradUy_m, gradUz_m, gradUx_s, gradUy_s, gradUz_s;
+  std::vector<R> LiftFlux, FluxX, FluxY, FluxZ;  // lifting side fluxes
+  std::vector<R> Flux_master, Flux_slave;
+  std::vector<R> Ut_tmp;
+  double BulkVel = 0.;
+  // time discretisation (timedisc_vars.f90:175-216, CarpenterRK4-5)
+  double RKA[6], RKb[6], RKc[6];
+  int nRKStages = 5;
+  double CFLScaleEff = 0., DFLScaleEff = 0.;
+  std::vector<double> MetricsAdv, MetricsVisc;
+
+  size_t vi(int v, int i, int j, int k, int e, int nv) const { return ((((size_t)e * n + k) * n + j) * n + i) * nv + v; }
+  size_t si(int v, int p, int q, int s, int nv) const { return (((size_t)s * n + q) * n + p) * nv + v; }
+  int s2e(int c, int s) const { return M.SideToElem[(size_t)s * 5 + c]; }
+
+  void init(const Config& cfg, const MeshInput& mi) {
+    C = cfg; N = C.N; n = N + 1;
+    B.init(N, C.nodeType);
+    build_mesh(mi, N, C.nodeType, M);
+    nE = M.nElems; nS = M.nSides;
+    kappa = C.kappa; kappaM1 = C.kappa - 1.; sKappaM1 = 1. / (C.kappa - 1.); Rgas = C.R;
+    cp = C.R * C.kappa / (C.kappa - 1.); cv = C.R / (C.kappa - 1.); Pr = C.Pr; mu0 = C.mu0;
+    lambdaFac = val(cp) / C.Pr;  // THERMAL_CONDUCTIVITY_H(mu) = mu*cp/Pr
+    s23 = 2. / 3.; s43 = 4. / 3.;
+    if (C.etaBR2_wall == -1.) C.etaBR2_wall = C.etaBR2;
+    const size_t nv3 = (size_t)n * n * n, ns2 = (size_t)n * n;
+    U.assign(5 * nv3 * nE, R(0.)); Ut = U; Ut_tmp = U;
+    UPrim.assign(6 * nv3 * nE, R(0.));
+    U_master.assign(5 * ns2 * nS, R(0.)); U_slave = U_master;
+    UPrim_master.assign(6 * ns2 * nS, R(0.)); UPrim_slave = UPrim_master;
+    gradUx.assign(NLIFT * nv3 * nE, R(0.)); gradUy = gradUx; gradUz = gradUx;
+    gradUx_m.assign(NLIFT * ns2 * nS, R(0.)); gradUy_m = gradUx_m; gradUz_m = gradUx_m;
+    gradUx_s = gradUx_m; gradUy_s = gradUx_m; gradUz_s = gradUx_m;
+    LiftFlux = gradUx_m; FluxX = gradUx_m; FluxY = gradUx_m; FluxZ = gradUx_m;
+    Flux_master.assign(5 * ns2 * nS, R(0.)); Flux_slave = Flux_master;
+    // Carpenter-Kennedy RK4-5 (timedisc_vars.f90:199-214), 1-based stage index
+    RKA[2] = 567301805773.0 / 1357537059087.0; RKA[3] = 2404267990393.0 / 2016746695238.0;
+    RKA[4] = 3550918686646.0 / 2091501179385.0; RKA[5] = 1275806237668.0 / 842570457699.0;
+    RKb[1] = 1432997174477.0 / 9575080441755.0; RKb[2] = 5161836677717.0 / 13612068292357.0;
+    RKb[3] = 1720146321549.0 / 2090206949498.0; RKb[4] = 3134564353537.0 / 4481467310338.0;
+    RKb[5] = 2277821191437.0 / 14882151754819.0;
+    RKc[2] = 1432997174477.0 / 9575080441755.0; RKc[3] = 2526269341429.0 / 6820363962896.0;
+    RKc[4] = 2006345519317.0 / 3224310063776.0; RKc[5] = 2802321613138.0 / 2924317926251.0;
+    // FillCFL_DFL (timedisc_func.f90:463-527) with CFLScaleAlpha/DFLScaleAlpha tables (timedisc_vars.f90)
+    static const double cflG[15] = {2.0351, 1.7595, 1.5401, 1.3702, 1.2375, 1.1318, 1.0440, 0.9709, 0.9079, 0.8539, 0.8066, 0.7650, 0.7290, 0.6952, 0.6660};
+    static const double cflGL[15] = {4.7497, 3.4144, 2.8451, 2.4739, 2.2027, 1.9912, 1.8225, 1.6830, 1.5682, 1.4692, 1.3849, 1.3106, 1.2454, 1.1880, 1.1362};
+    static const double dflG[10] = {1.12, 0.76, 0.55, 0.41, 0.32, 0.25, 0.20, 0.17, 0.14, 0.12};
+    static const double dflGL[10] = {4.50, 1.95, 1.18, 0.79, 0.56, 0.42, 0.32, 0.25, 0.20, 0.17};
+    const double* ct = C.nodeType == NT_GL ? cflGL : cflG;
+    const double* dtab = C.nodeType == NT_GL ? dflGL : dflG;
+    double alpha = ct[std::min(15, N) - 1];
+    CFLScaleEff = C.CFLScale * alpha / (2. * N + 1.);
+    double RelativeDFL = 1.853;
+    alpha = dtab[std::min(10, N) - 1] * RelativeDFL;
+    DFLScaleEff = C.DFLScale * alpha / ((2. * N + 1.) * (2. * N + 1.));
+    // InitCalctimestep (calctimestep.f90:42-83)
+    MetricsAdv.assign(3 * nv3 * nE, 0.); MetricsVisc.assign(3 * nv3 * nE, 0.);
+    double KappasPr_max = std::max(4. / 3., C.kappa / C.Pr);
+    for (int e = 0; e < nE; ++e) for (size_t x = 0; x < nv3; ++x) {
+      double sj = M.sJ[(size_t)e * nv3 + x];
+      const double* mm[3] = {&M.Mf[((size_t)e * nv3 + x) * 3], &M.Mg[((size_t)e * nv3 + x) * 3], &M.Mh[((size_t)e * nv3 + x) * 3]};
+      for (int d = 0; d < 3; ++d) {
+        double nrm = std::sqrt(mm[d][0] * mm[d][0] + mm[d][1] * mm[d][1] + mm[d][2] * mm[d][2]);
+        MetricsAdv[((size_t)e * nv3 + x) * 3 + d] = sj * nrm;
+        double s2 = (mm[d][0] * sj) * (mm[d][0] * sj) + (mm[d][1] * sj) * (mm[d][1] * sj) + (mm[d][2] * sj) * (mm[d][2] * sj);
+        MetricsVisc[((size_t)e * nv3 + x) * 3 + d] = KappasPr_max * s2;
+      }
+    }
+  }
+
+  // ---------------- eos.f90:ConsToPrim ----------------
+  void cons_to_prim(const R* c, R* p) const {
+    R sRho = R(1.) / c[0];
+    p[0] = c[0];
+    p[1] = c[1] * sRho; p[2] = c[2] * sRho; p[3] = c[3] * sRho;
+    p[4] = kappaM1 * (c[4] - R(0.5) * (c[1] * p[1] + c[2] * p[2] + c[3] * p[3]));
+    p[5] = p[4] * sRho / Rgas;
+  }
+  // eos.f90:PrimToCons
+  void prim_to_cons(const R* p, R* c) const {
+    c[0] = p[0];
+    c[1] = p[1] * p[0]; c[2] = p[2] * p[0]; c[3] = p[3] * p[0];
+    c[4] = sKappaM1 * p[4] + R(0.5) * (c[1] * p[1] + c[2] * p[2] + c[3] * p[3]);
+  }
+
+  // ---------------- prolongtoface.t90:ProlongToFace ----------------
+  template <int NV>
+  void prolong_to_face(const std::vector<R>& Uvol, std::vector<R>& Um, std::vector<R>& Us) const {
+    const int nodeT = C.nodeType;
+    auto eval_face = [&](int e, int ls, std::vector<R>& Uface) {
+      // Uface(v,a,b) in volume order
+      for (int b = 0; b < n; ++b) for (int a = 0; a < n; ++a) {
+        R acc[NV];
+        int i, j, k;
+        if (nodeT == NT_GL) {
+          int l = (ls == XI_MINUS || ls == ETA_MINUS || ls == ZETA_MINUS) ? 0 : N;
+          face_vol_index(ls, a, b, l, N, i, j, k);
+          for (int v = 0; v < NV; ++v) acc[v] = Uvol[vi(v, i, j, k, e, NV)];
+        } else {
+          const std::vector<double>& Lf = (ls == XI_MINUS || ls == ETA_MINUS || ls == ZETA_MINUS) ? B.Lm : B.Lp;
+          face_vol_index(ls, a, b, 0, N, i, j, k);
+          for (int v = 0; v < NV; ++v) acc[v] = Uvol[vi(v, i, j, k, e, NV)] * R(Lf[0]);
+          for (int l = 1; l <= N; ++l) {
+            face_vol_index(ls, a, b, l, N, i, j, k);
+            for (int v = 0; v < NV; ++v) acc[v] = acc[v] + Uvol[vi(v, i, j, k, e, NV)] * R(Lf[l]);
+          }
+        }
+        for (int v = 0; v < NV; ++v) Uface[((size_t)b * n + a) * NV + v] = acc[v];
+      }
+    };
+#pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
+    for (int s = 0; s < nS; ++s) {
+      std::vector<R> Uface((size_t)n * n * NV);
+      int e = s2e(0, s), ne = s2e(1, s);
+      if (e > 0) {
+        int ls = s2e(2, s);
+        eval_face(e - 1, ls, Uface);
+        for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
+          auto ab = side_to_vol2(N, p, q, 0, ls);
+          for (int v = 0; v < NV; ++v) Um[si(v, p, q, s, NV)] = Uface[((size_t)ab[1] * n + ab[0]) * NV + v];
+        }
+      }
+      if (ne > 0) {
+        int nls = s2e(3, s), flip = s2e(4, s);
+        eval_face(ne - 1, nls, Uface);
+        for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
+          auto ab = side_to_vol2(N, p, q, flip, nls);
+          for (int v = 0; v < NV; ++v) Us[si(v, p, q, s, NV)] = Uface[((size_t)ab[1] * n + ab[0]) * NV + v];
+        }
+      }
+    }
+  }
+
+  // ---------------- surfint.t90:DoSurfInt (Gauss: all nodes on the normal line; GL: face node only) --------
+  template <int NV>
+  void do_surf_int(const R* FluxTmp /*(NV,a,b) volume order*/, int ls, std::vector<R>& Uout, int e) const {
+    bool minus = (ls == XI_MINUS || ls == ETA_MINUS || ls == ZETA_MINUS);
+    for (int b = 0; b < n; ++b) for (int a = 0; a < n; ++a) {
+      if (C.nodeType == NT_GL) {
+        int l = minus ? 0 : N; double Lh = minus ? B.LhatM[0] : B.LhatP[N];
+        int i, j, k; face_vol_index(ls, a, b, l, N, i, j, k);
+        for (int v = 0; v < NV; ++v) Uout[vi(v, i, j, k, e, NV)] += FluxTmp[((size_t)b * n + a) * NV + v] * R(Lh);
+      } else {
+        const std::vector<double>& Lh = minus ? B.LhatM : B.LhatP;
+        for (int l = 0; l <= N; ++l) {
+          int i, j, k; face_vol_index(ls, a, b, l, N, i, j, k);
+          for (int v = 0; v < NV; ++v) Uout[vi(v, i, j, k, e, NV)] += FluxTmp[((size_t)b * n + a) * NV + v] * R(Lh[l]);
+        }
+      }
+    }
+  }
+  // surfint.t90:SurfInt (side loop restated as an element loop over the element's six sides)
+  // slaveSign: -1 for the conservative flux, +1/-1 for strong/weak lifting
+  template <int NV>
+  void surf_int(const std::vector<R>& Fm, const std::vector<R>& Fs, std::vector<R>& Uout, R slaveSign) const {
+#pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
+    for (int e = 0; e < nE; ++e) {
+      std::vector<R> FluxTmp((size_t)n * n * NV);
+      for (int ls = 1; ls <= 6; ++ls) {
+        int s = M.ElemToSide[((size_t)e * 6 + ls - 1) * 2 + 0] - 1;
+        int flip = M.ElemToSide[((size_t)e * 6 + ls - 1) * 2 + 1];
+        bool master = (s2e(0, s) == e + 1 && s2e(2, s) == ls);
+        for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
+          auto ab = side_to_vol2(N, p, q, master ? 0 : flip, ls);
+          for (int v = 0; v < NV; ++v)
+            FluxTmp[((size_t)ab[1] * n + ab[0]) * NV + v] = master ? Fm[si(v, p, q, s, NV)] : slaveSign * Fs[si(v, p, q, s, NV)];
+        }
+        do_surf_int<NV>(FluxTmp.data(), ls, Uout, e);
+      }
+    }
+  }
+
+  // ---------------- eos.f90:PRESSURE_RIEMANN (uses rotated prim: VEL1 = normal velocity) ----------------
+  R pressure_riemann(const R* up) const {
+    R kappaFac = R(2.) * kappa * sKappaM1;
+    R P;
+    if (up[1] <= R(0.)) {
+      R base = rmax(R(0.0001), R(1.) + R(0.5) * kappaM1 * up[1] / sqrt(kappa * up[4] / up[0]));
+      P = up[4] * pow(base, kappaFac);
+    } else {
+      R ar = R(2.) * (R(1.) / (kappa + R(1.))) / up[0];
+      R br = kappaM1 * (R(1.) / (kappa + R(1.))) * up[4];
+      P = up[4] + up[1] / ar * R(0.5) * (up[1] + sqrt(up[1] * up[1] + R(4.) * ar * (up[4] + br)));
+    }
+    return P;
+  }
+  // getboundaryflux.f90:GetBoundaryState for wall BCs 3 (adiabatic) and 4 (isothermal)
+  void wall_boundary_state(int bcType, int bcState, const R* um, const double* nv, const double* t1, const double* t2, R* ub) const {
+    ub[0] = um[0];
+    ub[1] = um[1] * R(nv[0]) + um[2] * R(nv[1]) + um[3] * R(nv[2]);
+    ub[2] = um[1] * R(t1[0]) + um[2] * R(t1[1]) + um[3] * R(t1[2]);
+    ub[3] = um[1] * R(t2[0]) + um[2] * R(t2[1]) + um[3] * R(t2[2]);
+    ub[4] = um[4]; ub[5] = um[5];
+    ub[4] = pressure_riemann(ub);
+    ub[1] = R(0.); ub[2] = R(0.); ub[3] = R(0.);
+    if (bcType == 4) ub[5] = R(M.RefStatePrim[(size_t)(bcState - 1) * 6 + 5]);
+    else ub[5] = um[5];
+    ub[0] = ub[4] / (ub[5] * Rgas);
+  }
+  int bc_type(int s) const { return M.BoundaryType[(size_t)(M.BC[s] - 1) * 2 + 0]; }
+  int bc_state(int s) const { return M.BoundaryType[(size_t)(M.BC[s] - 1) * 2 + 1]; }
+
+  // ---------------- lifting ----------------
+  void lifting() {
+    const size_t nv3 = (size_t)n * n * n;
+    const bool br2 = C.lifting == 2;
+    // volume part: lifting_volint.t90
+    if (C.weakLifting || C.consLifting) {
+      const std::vector<double>& DMat = C.weakLifting ? B.Dhat_T : B.D_T;
+      for (int dir = 0; dir < 3; ++dir) {
+        std::vector<R>& g = dir == 0 ? gradUx : (dir == 1 ? gradUy : gradUz);
+#pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
+        for (int e = 0; e < nE; ++e) {
+          std::vector<R> Ef(NLIFT * nv3), Eg(NLIFT * nv3), Eh(NLIFT * nv3);
+          for (size_t x = 0; x < nv3; ++x) for (int v = 0; v < NLIFT; ++v) {
+            R u = UPrim[((size_t)e * nv3 + x) * 6 + PRIM_LIFT[v]];
+            Ef[x * NLIFT + v] = R(M.Mf[((size_t)e * nv3 + x) * 3 + dir]) * u;
+            Eg[x * NLIFT + v] = R(M.Mg[((size_t)e * nv3 + x) * 3 + dir]) * u;
+            Eh[x * NLIFT + v] = R(M.Mh[((size_t)e * nv3 + x) * 3 + dir]) * u;
+          }
+          for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i)
+            for (int v = 0; v < NLIFT; ++v) {
+              R a = R(DMat[0 * n + i]) * Ef[(((size_t)k * n + j) * n + 0) * NLIFT + v] + R(DMat[0 * n + k]) * Eh[(((size_t)0 * n + j) * n + i) * NLIFT + v] +
+                    R(DMat[0 * n + j]) * Eg[(((size_t)k * n + 0) * n + i) * NLIFT + v];
+              for (int l = 1; l <= N; ++l)
+                a = a + R(DMat[l * n + i]) * Ef[(((size_t)k * n + j) * n + l) * NLIFT + v] + R(DMat[l * n + k]) * Eh[(((size_t)l * n + j) * n + i) * NLIFT + v] +
+                    R(DMat[l * n + j]) * Eg[(((size_t)k * n + l) * n + i) * NLIFT + v];
+              g[vi(v, i, j, k, e, NLIFT)] = a;
+            }
+        }
+      }
+    } else {
+#pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
+      for (int e = 0; e < nE; ++e)
+        for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
+          R gxi[NLIFT], geta[NLIFT], gzeta[NLIFT];
+          for (int v = 0; v < NLIFT; ++v) {
+            int pv = PRIM_LIFT[v];
+            gxi[v] = R(B.D_T[0 * n + i]) * UPrim[vi(pv, 0, j, k, e, 6)];
+            geta[v] = R(B.D_T[0 * n + j]) * UPrim[vi(pv, i, 0, k, e, 6)];
+            gzeta[v] = R(B.D_T[0 * n + k]) * UPrim[vi(pv, i, j, 0, e, 6)];
+            for (int l = 1; l <= N; ++l) {
+              gxi[v] = gxi[v] + R(B.D_T[l * n + i]) * UPrim[vi(pv, l, j, k, e, 6)];
+              geta[v] = geta[v] + R(B.D_T[l * n + j]) * UPrim[vi(pv, i, l, k, e, 6)];
+              gzeta[v] = gzeta[v] + R(B.D_T[l * n + k]) * UPrim[vi(pv, i, j, l, e, 6)];
+            }
+          }
+          size_t x = (((size_t)e * n + k) * n + j) * n + i;
+          const double* mf = &M.Mf[x * 3]; const double* mg = &M.Mg[x * 3]; const double* mh = &M.Mh[x * 3];
+          for (int v = 0; v < NLIFT; ++v) {
+            gradUx[vi(v, i, j, k, e, NLIFT)] = R(mf[0]) * gxi[v] + R(mg[0]) * geta[v] + R(mh[0]) * gzeta[v];
+            gradUy[vi(v, i, j, k, e, NLIFT)] = R(mf[1]) * gxi[v] + R(mg[1]) * geta[v] + R(mh[1]) * gzeta[v];
+            gradUz[vi(v, i, j, k, e, NLIFT)] = R(mf[2]) * gxi[v] + R(mg[2]) * geta[v] + R(mh[2]) * gzeta[v];
+          }
+        }
+    }
+    // boundary lifting flux: lifting_fillflux.t90:Lifting_FillFlux_BC -> getboundaryflux.f90:Lifting_GetBoundaryFlux
+    for (int s = 0; s < M.nBCSides; ++s) {
+      int bt = bc_type(s);
+      for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
+        const R* um = &UPrim_master[si(0, p, q, s, 6)];
+        size_t sx = M.sidx(p, q, s);
+        R F[NLIFT];
+        if (bt == 3 || bt == 4) {
+          R ub[6];
+          wall_boundary_state(bt, bc_state(s), um, &M.NormVec[sx * 3], &M.TangVec1[sx * 3], &M.TangVec2[sx * 3], ub);
+          F[0] = R(0.); F[1] = R(0.); F[2] = R(0.); F[3] = ub[5];
+        } else throw std::runtime_error("unsupported BC type in oracle");
+        if (!C.weakLifting) for (int v = 0; v < NLIFT; ++v) F[v] = F[v] - um[PRIM_LIFT[v]];
+        for (int v = 0; v < NLIFT; ++v) {
+          R f = F[v] * R(M.SurfElem[sx]);
+          LiftFlux[si(v, p, q, s, NLIFT)] = f;
+          if (br2) {
+            FluxX[si(v, p, q, s, NLIFT)] = f * R(M.NormVec[sx * 3 + 0]);
+            FluxY[si(v, p, q, s, NLIFT)] = f * R(M.NormVec[sx * 3 + 1]);
+            FluxZ[si(v, p, q, s, NLIFT)] = f * R(M.NormVec[sx * 3 + 2]);
+          }
+        }
+      }
+    }
+    // inner sides: Lifting_FillFlux
+    R sig = C.weakLifting ? R(1.) : R(-1.);  // sig = MERGE(1,-1,doWeakLifting)
+    for (int s = M.nBCSides; s < nS; ++s)
+      for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
+        size_t sx = M.sidx(p, q, s);
+        for (int v = 0; v < NLIFT; ++v) {
+          R f = sig * UPrim_master[si(PRIM_LIFT[v], p, q, s, 6)] + UPrim_slave[si(PRIM_LIFT[v], p, q, s, 6)];
+          if (!br2) LiftFlux[si(v, p, q, s, NLIFT)] = R(0.5) * f * R(M.SurfElem[sx]);
+          else {
+            FluxX[si(v, p, q, s, NLIFT)] = R(0.5) * f * R(M.NormVec[sx * 3 + 0]) * R(M.SurfElem[sx]);
+            FluxY[si(v, p, q, s, NLIFT)] = R(0.5) * f * R(M.NormVec[sx * 3 + 1]) * R(M.SurfElem[sx]);
+            FluxZ[si(v, p, q, s, NLIFT)] = R(0.5) * f * R(M.NormVec[sx * 3 + 2]) * R(M.SurfElem[sx]);
+          }
+        }
+      }
+    if (!br2) {
+      // Lifting_FillFlux_NormVec into gradU*_master, then Lifting_SurfInt_BR1, ApplyJacobianLifting, ProlongToFaceLifting
+      for (int s = 0; s < nS; ++s) for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
+        size_t sx = M.sidx(p, q, s);
+        for (int v = 0; v < NLIFT; ++v) {
+          R f = LiftFlux[si(v, p, q, s, NLIFT)];
+          gradUx_m[si(v, p, q, s, NLIFT)] = f * R(M.NormVec[sx * 3 + 0]);
+          gradUy_m[si(v, p, q, s, NLIFT)] = f * R(M.NormVec[sx * 3 + 1]);
+          gradUz_m[si(v, p, q, s, NLIFT)] = f * R(M.NormVec[sx * 3 + 2]);
+        }
+      }
+      R slaveSign = C.weakLifting ? R(-1.) : R(1.);
+      surf_int<NLIFT>(gradUx_m, gradUx_m, gradUx, slaveSign);
+      surf_int<NLIFT>(gradUy_m, gradUy_m, gradUy, slaveSign);
+      surf_int<NLIFT>(gradUz_m, gradUz_m, gradUz, slaveSign);
+      apply_jacobian_lift();
+      prolong_to_face<NLIFT>(gradUx, gradUx_m, gradUx_s);
+      prolong_to_face<NLIFT>(gradUy, gradUy_m, gradUy_s);
+      prolong_to_face<NLIFT>(gradUz, gradUz_m, gradUz_s);
+    } else {
+      apply_jacobian_lift();
+      prolong_to_face<NLIFT>(gradUx, gradUx_m, gradUx_s);
+      prolong_to_face<NLIFT>(gradUy, gradUy_m, gradUy_s);
+      prolong_to_face<NLIFT>(gradUz, gradUz_m, gradUz_s);
+      surf_int_br2(FluxX, gradUx, gradUx_m, gradUx_s);
+      surf_int_br2(FluxY, gradUy, gradUy_m, gradUy_s);
+      surf_int_br2(FluxZ, gradUz, gradUz_m, gradUz_s);
+    }
+  }
+  void apply_jacobian_lift() {
+    const size_t nv3 = (size_t)n * n * n;
+    for (int e = 0; e < nE; ++e) for (size_t x = 0; x < nv3; ++x) {
+      R sj = R(M.sJ[(size_t)e * nv3 + x]);
+      for (int v = 0; v < NLIFT; ++v) {
+        gradUx[((size_t)e * nv3 + x) * NLIFT + v] = gradUx[((size_t)e * nv3 + x) * NLIFT + v] * sj;
+        gradUy[((size_t)e * nv3 + x) * NLIFT + v] = gradUy[((size_t)e * nv3 + x) * NLIFT + v] * sj;
+        gradUz[((size_t)e * nv3 + x) * NLIFT + v] = gradUz[((size_t)e * nv3 + x) * NLIFT + v] * sj;
+      }
+    }
+  }
+  // lifting_br2.t90:Lifting_SurfInt_BR2 (slave part for inner sides, then master part incl. BC sides)
+  void surf_int_br2(const std::vector<R>& Flux, std::vector<R>& g, std::vector<R>& gm, std::vector<R>& gs) {
+    const int lmax = C.nodeType == NT_GL ? 0 : N;
+    for (int s = M.nBCSides; s < nS; ++s) {
+      int ne = s2e(1, s);
+      if (ne <= 0) continue;
+      int nls = s2e(3, s), flip = s2e(4, s);
+      for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) for (int l = 0; l <= lmax; ++l) {
+        auto ijk = side_to_vol(N, l, p, q, flip, nls);
+        R sj = R(M.sJ[M.vidx(ijk[0], ijk[1], ijk[2], ne - 1)]);
+        for (int v = 0; v < NLIFT; ++v) {
+          R F = sj * Flux[si(v, p, q, s, NLIFT)] * R(B.LhatM[l]);
+          g[vi(v, ijk[0], ijk[1], ijk[2], ne - 1, NLIFT)] += F;
+          gs[si(v, p, q, s, NLIFT)] += R(C.etaBR2) * R(B.Lm[l]) * F;
+        }
+      }
+    }
+    for (int s = 0; s < nS; ++s) {
+      double eta = C.etaBR2;
+      if (s < M.nBCSides && (bc_type(s) == 4 || bc_type(s) == 3)) eta = C.etaBR2_wall;
+      int e = s2e(0, s);
+      if (e <= 0) continue;
+      int ls = s2e(2, s);
+      for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) for (int l = 0; l <= lmax; ++l) {
+        auto ijk = side_to_vol(N, l, p, q, 0, ls);
+        R sj = R(M.sJ[M.vidx(ijk[0], ijk[1], ijk[2], e - 1)]);
+        for (int v = 0; v < NLIFT; ++v) {
+          R F = sj * Flux[si(v, p, q, s, NLIFT)] * R(B.LhatM[l]);
+          g[vi(v, ijk[0], ijk[1], ijk[2], e - 1, NLIFT)] += F;
+          gm[si(v, p, q, s, NLIFT)] += R(eta) * R(B.Lm[l]) * F;
+        }
+      }
+    }
+  }
+
+  // ---------------- flux.f90:EvalDiffFlux3D_Point (viscous flux, stored with the minus sign) ----------------
+  void diff_flux(const R* up, const R* gx, const R* gy, const R* gz, R* f, R* g, R* h) const {
+    R muS = mu0;
+    R lambda = muS * R(lambdaFac);
+    R txx = muS * (s43 * gx[0] - s23 * gy[1] - s23 * gz[2]);
+    R tyy = muS * (-s23 * gx[0] + s43 * gy[1] - s23 * gz[2]);
+    R tzz = muS * (-s23 * gx[0] - s23 * gy[1] + s43 * gz[2]);
+    R txy = muS * (gy[0] + gx[1]);
+    R txz = muS * (gz[0] + gx[2]);
+    R tyz = muS * (gz[1] + gy[2]);
+    R v1 = up[1], v2 = up[2], v3 = up[3];
+    f[0] = R(0.); f[1] = -txx; f[2] = -txy; f[3] = -txz; f[4] = -txx * v1 - txy * v2 - txz * v3 - lambda * gx[3];
+    g[0] = R(0.); g[1] = -txy; g[2] = -tyy; g[3] = -tyz; g[4] = -txy * v1 - tyy * v2 - tyz * v3 - lambda * gy[3];
+    h[0] = R(0.); h[1] = -txz; h[2] = -tyz; h[3] = -tzz; h[4] = -txz * v1 - tyz * v2 - tzz * v3 - lambda * gz[3];
+  }
+  // flux.f90:EvalFlux3D_Point
+  void euler_flux(const R* u, const R* up, R* f, R* g, R* h) const {
+    R Ep = u[4] + up[4];
+    f[0] = u[1]; f[1] = u[1] * up[1] + up[4]; f[2] = u[1] * up[2]; f[3] = u[1] * up[3]; f[4] = Ep * up[1];
+    g[0] = u[2]; g[1] = f[2]; g[2] = u[2] * up[2] + up[4]; g[3] = u[2] * up[3]; g[4] = Ep * up[2];
+    h[0] = u[3]; h[1] = f[3]; h[2] = g[3]; h[3] = u[3] * up[3] + up[4]; h[4] = Ep * up[3];
+  }
+  // splitflux.f90:SplitVolumeFluxPI / SplitVolumeFluxSD (factor 2 of the split form included)
+  void split_volume_flux(const R* uR, const R* pR, const R* u, const R* p, const R* mR, const R* m, R* F) const {
+    R ft[5], gt[5], ht[5];
+    if (C.splitDG == SPLIT_PI) {
+      R HR = (uR[4] + pR[4]) / uR[0], H = (u[4] + p[4]) / u[0];
+      R rs = uR[0] + u[0], us = pR[1] + p[1], vs = pR[2] + p[2], ws = pR[3] + p[3], ps = pR[4] + p[4], Hs = HR + H;
+      ft[0] = R(0.5) * rs * us; ft[1] = R(0.25) * rs * us * us + ps; ft[2] = R(0.25) * rs * us * vs; ft[3] = R(0.25) * rs * us * ws; ft[4] = R(0.25) * rs * us * Hs;
+      gt[0] = R(0.5) * rs * vs; gt[1] = ft[2]; gt[2] = R(0.25) * rs * vs * vs + ps; gt[3] = R(0.25) * rs * vs * ws; gt[4] = R(0.25) * rs * vs * Hs;
+      ht[0] = R(0.5) * rs * ws; ht[1] = ft[3]; ht[2] = gt[3]; ht[3] = R(0.25) * rs * ws * ws + ps; ht[4] = R(0.25) * rs * ws * Hs;
+    } else {  // SD
+      R eR = uR[4] + pR[4], e = u[4] + p[4];
+      ft[0] = uR[1] + u[1]; ft[1] = uR[1] * pR[1] + pR[4] + u[1] * p[1] + p[4]; ft[2] = uR[1] * pR[2] + u[1] * p[2]; ft[3] = uR[1] * pR[3] + u[1] * p[3]; ft[4] = eR * pR[1] + e * p[1];
+      gt[0] = uR[2] + u[2]; gt[1] = uR[1] * pR[2] + u[1] * p[2]; gt[2] = uR[2] * pR[2] + pR[4] + u[2] * p[2] + p[4]; gt[3] = uR[2] * pR[3] + u[2] * p[3]; gt[4] = eR * pR[2] + e * p[2];
+      ht[0] = uR[3] + u[3]; ht[1] = uR[1] * pR[3] + u[1] * p[3]; ht[2] = uR[2] * pR[3] + u[2] * p[3]; ht[3] = uR[3] * pR[3] + pR[4] + u[3] * p[3] + p[4]; ht[4] = eR * pR[3] + e * p[3];
+    }
+    R m1 = R(0.5) * (mR[0] + m[0]), m2 = R(0.5) * (mR[1] + m[1]), m3 = R(0.5) * (mR[2] + m[2]);
+    for (int v = 0; v < 5; ++v) F[v] = m1 * ft[v] + m3 * ht[v] + m2 * gt[v];
+  }
+  // splitflux.f90:SplitSurfaceFluxPI / SD on rotated extended states UE(11): 0..4 cons, 5 srho, 6..8 vel, 9 p, 10 T
+  void split_surface_flux(const R* L, const R* Rr, R* F) const {
+    if (C.splitDG == SPLIT_PI) {
+      R HL = (L[4] + L[9]) / L[0], HR = (Rr[4] + Rr[9]) / Rr[0];
+      R rs = L[0] + Rr[0], us = L[6] + Rr[6];
+      F[0] = R(0.25) * rs * us;
+      F[1] = R(0.125) * rs * us * us + R(0.5) * (L[9] + Rr[9]);
+      F[2] = R(0.125) * rs * us * (L[7] + Rr[7]);
+      F[3] = R(0.125) * rs * us * (L[8] + Rr[8]);
+      F[4] = R(0.125) * rs * (HL + HR) * us;
+    } else {  // SplitSurfaceFluxSD: 0.5*(F_L+F_R)
+      R eL = L[4] + L[9], eR = Rr[4] + Rr[9];
+      F[0] = R(0.5) * (L[1] + Rr[1]);
+      F[1] = R(0.5) * (L[1] * L[6] + L[9] + Rr[1] * Rr[6] + Rr[9]);
+      F[2] = R(0.5) * (L[1] * L[7] + Rr[1] * Rr[7]);
+      F[3] = R(0.5) * (L[1] * L[8] + Rr[1] * Rr[8]);
+      F[4] = R(0.5) * (eL * L[6] + eR * Rr[6]);
+    }
+  }
+  // flux.f90:EvalEulerFlux1D_fast
+  void euler_flux_1d(const R* U, R* F) const {
+    F[0] = U[1]; F[1] = U[1] * U[6] + U[9]; F[2] = U[1] * U[7]; F[3] = U[1] * U[8]; F[4] = (U[4] + U[9]) * U[6];
+  }
+  // riemann.f90: Riemann_LF/HLLC/Roe/RoeEntropyFix
+  void riemann_point(int solver, const R* L, const R* Rr, R* F) const {
+    const bool split = C.splitDG != SPLIT_NONE;
+    R FL[5], FR[5];
+    if (!split || solver == RIEMANN_HLLC) { euler_flux_1d(L, FL); euler_flux_1d(Rr, FR); }
+    if (solver == RIEMANN_LF) {
+      R cL = sqrt(kappa * L[9] * L[5]), cR = sqrt(kappa * Rr[9] * Rr[5]);
+      R lmax = rmax(fabs(Rr[6]), fabs(L[6])) + rmax(cL, cR);
+      if (!split) for (int v = 0; v < 5; ++v) F[v] = R(0.5) * ((FL[v] + FR[v]) - lmax * (Rr[v] - L[v]));
+      else { split_surface_flux(L, Rr, F); for (int v = 0; v < 5; ++v) F[v] = F[v] - R(0.5) * lmax * (Rr[v] - L[v]); }
+      return;
+    }
+    R HL = (L[4] + L[9]) * L[5], HR = (Rr[4] + Rr[9]) * Rr[5];
+    R sqL = sqrt(L[0]), sqR = sqrt(Rr[0]);
+    R ssq = R(1.) / (sqL + sqR);
+    R rv[3] = {(sqR * Rr[6] + sqL * L[6]) * ssq, (sqR * Rr[7] + sqL * L[7]) * ssq, (sqR * Rr[8] + sqL * L[8]) * ssq};
+    R rH = (sqR * HR + sqL * HL) * ssq;
+    R absVel = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
+    if (solver == RIEMANN_HLLC) {
+      R rc = sqrt(kappaM1 * (rH - R(0.5) * absVel));
+      R Ssl = rv[0] - rc, Ssr = rv[0] + rc;
+      if (Ssl >= R(0.)) { for (int v = 0; v < 5; ++v) F[v] = FL[v]; }
+      else if (Ssr <= R(0.)) { for (int v = 0; v < 5; ++v) F[v] = FR[v]; }
+      else {
+        R sMuL = Ssl - L[6], sMuR = Ssr - Rr[6];
+        R SStar = (Rr[9] - L[9] + L[1] * sMuL - Rr[1] * sMuR) / (L[0] * sMuL - Rr[0] * sMuR);
+        if (Ssl <= R(0.) && SStar >= R(0.)) {
+          R EStar = L[4] * L[5] + (SStar - L[6]) * (SStar + L[9] * L[5] / sMuL);
+          R fac = L[0] * sMuL / (Ssl - SStar);
+          R Us[5] = {fac, fac * SStar, fac * L[7], fac * L[8], fac * EStar};
+          for (int v = 0; v < 5; ++v) F[v] = FL[v] + Ssl * (Us[v] - L[v]);
+        } else {
+          R EStar = Rr[4] * Rr[5] + (SStar - Rr[6]) * (SStar + Rr[9] * Rr[5] / sMuR);
+          R fac = Rr[0] * sMuR / (Ssr - SStar);
+          R Us[5] = {fac, fac * SStar, fac * Rr[7], fac * Rr[8], fac * EStar};
+          for (int v = 0; v < 5; ++v) F[v] = FR[v] + Ssr * (Us[v] - Rr[v]);
+        }
+      }
+      return;
+    }
+    R rc = sqrt(kappaM1 * (rH - R(0.5) * absVel));  // ROEC_RIEMANN_H
+    R a[5] = {rv[0] - rc, rv[0], rv[0], rv[0], rv[0] + rc};
+    R r1[5] = {R(1.), a[0], rv[1], rv[2], rH - rv[0] * rc};
+    R r2[5] = {R(1.), rv[0], rv[1], rv[2], R(0.5) * absVel};
+    R r3[5] = {R(0.), R(0.), R(1.), R(0.), rv[1]};
+    R r4[5] = {R(0.), R(0.), R(0.), R(1.), rv[2]};
+    R r5[5] = {R(1.), a[4], rv[1], rv[2], rH + rv[0] * rc};
+    R Alpha[5];
+    if (solver == RIEMANN_ROE) {
+      R dU[6];
+      for (int v = 0; v < 5; ++v) dU[v] = Rr[v] - L[v];
+      dU[5] = dU[4] - (dU[2] - rv[1] * dU[0]) * rv[1] - (dU[3] - rv[2] * dU[0]) * rv[2];
+      Alpha[2] = dU[2] - rv[1] * dU[0];
+      Alpha[3] = dU[3] - rv[2] * dU[0];
+      Alpha[1] = kappaM1 / (rc * rc) * (dU[0] * (rH - rv[0] * rv[0]) - dU[5] + rv[0] * dU[1]);
+      Alpha[0] = R(0.5) / rc * (dU[0] * (rv[0] + rc) - dU[1] - rc * Alpha[1]);
+      Alpha[4] = dU[0] - Alpha[0] - Alpha[1];
+      for (int v = 0; v < 5; ++v) a[v] = fabs(a[v]);
+    } else {  // RoeEntropyFix
+      R cL = sqrt(kappa * L[9] * L[5]), cR = sqrt(kappa * Rr[9] * Rr[5]);
+      R RoeDens = sqrt(L[0] * Rr[0]);
+      R dU[5] = {Rr[0] - L[0], Rr[6] - L[6], Rr[7] - L[7], Rr[8] - L[8], Rr[9] - L[9]};
+      R tmp = R(0.5) / (rc * rc);
+      Alpha[0] = tmp * (dU[4] - RoeDens * rc * dU[1]);
+      Alpha[1] = dU[0] - dU[4] * R(2.) * tmp;
+      Alpha[2] = RoeDens * dU[2];
+      Alpha[3] = RoeDens * dU[3];
+      Alpha[4] = tmp * (dU[4] + RoeDens * rc * dU[1]);
+      R al[5] = {L[6] - cL, L[6], L[6], L[6], L[6] + cL};
+      R ar[5] = {Rr[6] - cR, Rr[6], Rr[6], Rr[6], Rr[6] + cR};
+      for (int v = 0; v < 5; ++v) {
+        R da = rmax(R(0.), rmax(a[v] - al[v], ar[v] - a[v]));
+        if (fabs(a[v]) < da) a[v] = R(0.5) * (a[v] * a[v] / da + da);
+        else a[v] = fabs(a[v]);
+      }
+    }
+    if (!split) {
+      for (int v = 0; v < 5; ++v)
+        F[v] = R(0.5) * ((FL[v] + FR[v]) - Alpha[0] * a[0] * r1[v] - Alpha[1] * a[1] * r2[v] - Alpha[2] * a[2] * r3[v] - Alpha[3] * a[3] * r4[v] - Alpha[4] * a[4] * r5[v]);
+    } else {
+      split_surface_flux(L, Rr, F);
+      for (int v = 0; v < 5; ++v)
+        F[v] = F[v] - R(0.5) * (Alpha[0] * a[0] * r1[v] + Alpha[1] * a[1] * r2[v] + Alpha[2] * a[2] * r3[v] + Alpha[3] * a[3] * r4[v] + Alpha[4] * a[4] * r5[v]);
+    }
+  }
+  // riemann.f90:Riemann_Point -- rotate into (n,t1,t2), solve, rotate back
+  void riemann_rot(int solver, const R* uL, const R* pL, const R* uR, const R* pR, const double* nv, const double* t1, const double* t2, R* Fout) const {
+    R L[11], Rr[11];
+    auto ext = [&](const R* u, const R* p, R* E) {
+      E[0] = u[0]; E[5] = R(1.) / E[0]; E[4] = u[4]; E[9] = p[4];
+      E[6] = p[1] * R(nv[0]) + p[2] * R(nv[1]) + p[3] * R(nv[2]);
+      E[7] = p[1] * R(t1[0]) + p[2] * R(t1[1]) + p[3] * R(t1[2]);
+      E[1] = E[0] * E[6]; E[2] = E[0] * E[7];
+      E[8] = p[1] * R(t2[0]) + p[2] * R(t2[1]) + p[3] * R(t2[2]);
+      E[3] = E[0] * E[8];
+      E[10] = p[5];
+    };
+    ext(uL, pL, L); ext(uR, pR, Rr);
+    R F[5];
+    riemann_point(solver, L, Rr, F);
+    Fout[0] = F[0];
+    for (int d = 0; d < 3; ++d) Fout[1 + d] = R(nv[d]) * F[1] + R(t1[d]) * F[2] + R(t2[d]) * F[3];
+    Fout[4] = F[4];
+  }
+
+  // ---------------- fillflux.f90:FillFlux ----------------
+  void fill_flux(double t) {
+    (void)t;
+#pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
+    for (int s = M.nBCSides; s < nS; ++s)
+      for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
+        size_t sx = M.sidx(p, q, s);
+        R F[5];
+        riemann_rot(C.riemann, &U_master[si(0, p, q, s, 5)], &UPrim_master[si(0, p, q, s, 6)], &U_slave[si(0, p, q, s, 5)],
+                    &UPrim_slave[si(0, p, q, s, 6)], &M.NormVec[sx * 3], &M.TangVec1[sx * 3], &M.TangVec2[sx * 3], F);
+        // riemann.f90:ViscousFlux_Point
+        R fL[5], gL[5], hL[5], fR[5], gR[5], hR[5];
+        diff_flux(&UPrim_master[si(0, p, q, s, 6)], &gradUx_m[si(0, p, q, s, NLIFT)], &gradUy_m[si(0, p, q, s, NLIFT)], &gradUz_m[si(0, p, q, s, NLIFT)], fL, gL, hL);
+        diff_flux(&UPrim_slave[si(0, p, q, s, 6)], &gradUx_s[si(0, p, q, s, NLIFT)], &gradUy_s[si(0, p, q, s, NLIFT)], &gradUz_s[si(0, p, q, s, NLIFT)], fR, gR, hR);
+        const double* nv = &M.NormVec[sx * 3];
+        for (int v = 0; v < 5; ++v) {
+          R FV = R(0.5) * (R(nv[0]) * (fL[v] + fR[v]) + R(nv[1]) * (gL[v] + gR[v]) + R(nv[2]) * (hL[v] + hR[v]));
+          Flux_master[si(v, p, q, s, 5)] = F[v] + FV;
+        }
+      }
+    // boundary sides: getboundaryflux.f90:GetBoundaryFlux (walls 3/4)
+    for (int s = 0; s < M.nBCSides; ++s) {
+      int bt = bc_type(s);
+      if (bt != 3 && bt != 4) throw std::runtime_error("unsupported BC type in oracle");
+      for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
+        size_t sx = M.sidx(p, q, s);
+        const R* um = &UPrim_master[si(0, p, q, s, 6)];
+        R ub[6];
+        wall_boundary_state(bt, bc_state(s), um, &M.NormVec[sx * 3], &M.TangVec1[sx * 3], &M.TangVec2[sx * 3], ub);
+        const double* nv = &M.NormVec[sx * 3];
+        R Fl[5] = {R(0.), ub[4] * R(nv[0]), ub[4] * R(nv[1]), ub[4] * R(nv[2]), R(0.)};
+        R fd[5], gd[5], hd[5];
+        diff_flux(ub, &gradUx_m[si(0, p, q, s, NLIFT)], &gradUy_m[si(0, p, q, s, NLIFT)], &gradUz_m[si(0, p, q, s, NLIFT)], fd, gd, hd);
+        if (bt == 3) { fd[4] = R(0.); gd[4] = R(0.); hd[4] = R(0.); }
+        for (int v = 1; v < 5; ++v) Fl[v] = Fl[v] + R(nv[0]) * fd[v] + R(nv[1]) * gd[v] + R(nv[2]) * hd[v];
+        for (int v = 0; v < 5; ++v) Flux_master[si(v, p, q, s, 5)] = Fl[v];
+      }
+    }
+    for (int s = 0; s < nS; ++s) for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
+      R se = R(M.SurfElem[M.sidx(p, q, s)]);
+      for (int v = 0; v < 5; ++v) { Flux_master[si(v, p, q, s, 5)] = Flux_master[si(v, p, q, s, 5)] * se; Flux_slave[si(v, p, q, s, 5)] = Flux_master[si(v, p, q, s, 5)]; }
+    }
+  }
+
+  // ---------------- volint.f90 ----------------
+  void vol_int() {
+    const size_t nv3 = (size_t)n * n * n;
+    const bool split = C.splitDG != SPLIT_NONE;
+#pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
+    for (int e = 0; e < nE; ++e) {
+      std::vector<R> f(5 * nv3), g(5 * nv3), h(5 * nv3);
+      // viscous fluxes fv,gv,hv (EvalDiffFlux3D) and, for the weak form, advective fluxes
+      for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
+        size_t x = ((size_t)k * n + j) * n + i;
+        R fv[5], gv[5], hv[5];
+        diff_flux(&UPrim[vi(0, i, j, k, e, 6)], &gradUx[vi(0, i, j, k, e, NLIFT)], &gradUy[vi(0, i, j, k, e, NLIFT)], &gradUz[vi(0, i, j, k, e, NLIFT)], fv, gv, hv);
+        R fa[5], ga[5], ha[5];
+        if (!split) {
+          euler_flux(&U[vi(0, i, j, k, e, 5)], &UPrim[vi(0, i, j, k, e, 6)], fa, ga, ha);
+          for (int v = 0; v < 5; ++v) { fa[v] = fa[v] + fv[v]; ga[v] = ga[v] + gv[v]; ha[v] = ha[v] + hv[v]; }
+        } else for (int v = 0; v < 5; ++v) { fa[v] = fv[v]; ga[v] = gv[v]; ha[v] = hv[v]; }
+        // VolInt_Metrics
+        size_t gx = (size_t)e * nv3 + x;
+        const double* mf = &M.Mf[gx * 3]; const double* mg = &M.Mg[gx * 3]; const double* mh = &M.Mh[gx * 3];
+        for (int v = 0; v < 5; ++v) {
+          f[x * 5 + v] = fa[v] * R(mf[0]) + ga[v] * R(mf[1]) + ha[v] * R(mf[2]);
+          g[x * 5 + v] = fa[v] * R(mg[0]) + ga[v] * R(mg[1]) + ha[v] * R(mg[2]);
+          h[x * 5 + v] = fa[v] * R(mh[0]) + ga[v] * R(mh[1]) + ha[v] * R(mh[2]);
+        }
+      }
+      auto F = [&](std::vector<R>& a, int v, int i, int j, int k) -> R& { return a[(((size_t)k * n + j) * n + i) * 5 + v]; };
+      if (!split) {
+        for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i)
+          for (int v = 0; v < 5; ++v) {
+            R a = R(B.Dhat_T[0 * n + i]) * F(f, v, 0, j, k) + R(B.Dhat_T[0 * n + k]) * F(h, v, i, j, 0) + R(B.Dhat_T[0 * n + j]) * F(g, v, i, 0, k);
+            for (int l = 1; l <= N; ++l)
+              a = a + R(B.Dhat_T[l * n + i]) * F(f, v, l, j, k) + R(B.Dhat_T[l * n + k]) * F(h, v, i, j, l) + R(B.Dhat_T[l * n + j]) * F(g, v, i, l, k);
+            Ut[vi(v, i, j, k, e, 5)] = a;
+          }
+      } else {
+        for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i)
+          for (int v = 0; v < 5; ++v)
+            Ut[vi(v, i, j, k, e, 5)] = R(B.Dhat_T[i * n + i]) * F(f, v, i, j, k) + R(B.Dhat_T[j * n + j]) * F(g, v, i, j, k) + R(B.Dhat_T[k * n + k]) * F(h, v, i, j, k);
+        auto Ue = [&](int i, int j, int k) { return &U[vi(0, i, j, k, e, 5)]; };
+        auto Pe = [&](int i, int j, int k) { return &UPrim[vi(0, i, j, k, e, 6)]; };
+        auto Mv = [&](const std::vector<double>& Mx, int i, int j, int k) {
+          size_t gx = (size_t)e * nv3 + ((size_t)k * n + j) * n + i; return &Mx[gx * 3]; };
+        for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
+          R Fl[5];
+          for (int l = i + 1; l <= N; ++l) {
+            R m1[3], m2[3];
+            for (int c = 0; c < 3; ++c) { m1[c] = R(Mv(M.Mf, i, j, k)[c]); m2[c] = R(Mv(M.Mf, l, j, k)[c]); }
+            split_volume_flux(Ue(i, j, k), Pe(i, j, k), Ue(l, j, k), Pe(l, j, k), m1, m2, Fl);
+            for (int v = 0; v < 5; ++v) {
+              Ut[vi(v, i, j, k, e, 5)] += R(B.DVolSurf[l * n + i]) * Fl[v];
+              Ut[vi(v, l, j, k, e, 5)] += R(B.DVolSurf[i * n + l]) * Fl[v];
+              Ut[vi(v, i, j, k, e, 5)] += R(B.Dhat_T[l * n + i]) * F(f, v, l, j, k);
+              Ut[vi(v, l, j, k, e, 5)] += R(B.Dhat_T[i * n + l]) * F(f, v, i, j, k);
+            }
+          }
+          for (int l = j + 1; l <= N; ++l) {
+            R m1[3], m2[3];
+            for (int c = 0; c < 3; ++c) { m1[c] = R(Mv(M.Mg, i, j, k)[c]); m2[c] = R(Mv(M.Mg, i, l, k)[c]); }
+            split_volume_flux(Ue(i, j, k), Pe(i, j, k), Ue(i, l, k), Pe(i, l, k), m1, m2, Fl);
+            for (int v = 0; v < 5; ++v) {
+              Ut[vi(v, i, j, k, e, 5)] += R(B.DVolSurf[l * n + j]) * Fl[v];
+              Ut[vi(v, i, l, k, e, 5)] += R(B.DVolSurf[j * n + l]) * Fl[v];
+              Ut[vi(v, i, j, k, e, 5)] += R(B.Dhat_T[l * n + j]) * F(g, v, i, l, k);
+              Ut[vi(v, i, l, k, e, 5)] += R(B.Dhat_T[j * n + l]) * F(g, v, i, j, k);
+            }
+          }
+          for (int l = k + 1; l <= N; ++l) {
+            R m1[3], m2[3];
+            for (int c = 0; c < 3; ++c) { m1[c] = R(Mv(M.Mh, i, j, k)[c]); m2[c] = R(Mv(M.Mh, i, j, l)[c]); }
+            split_volume_flux(Ue(i, j, k), Pe(i, j, k), Ue(i, j, l), Pe(i, j, l), m1, m2, Fl);
+            for (int v = 0; v < 5; ++v) {
+              Ut[vi(v, i, j, k, e, 5)] += R(B.DVolSurf[l * n + k]) * Fl[v];
+              Ut[vi(v, i, j, l, e, 5)] += R(B.DVolSurf[k * n + l]) * Fl[v];
+              Ut[vi(v, i, j, k, e, 5)] += R(B.Dhat_T[l * n + k]) * F(h, v, i, j, l);
+              Ut[vi(v, i, j, l, e, 5)] += R(B.Dhat_T[k * n + l]) * F(h, v, i, j, k);
+            }
+          }
+        }
+      }
+    }
+  }
+
+  // ---------------- dg.f90:DGTimeDerivative_weakForm ----------------
+  void time_derivative(double t) {
+    const size_t nv3 = (size_t)n * n * n;
+    if (C.splitDG != SPLIT_NONE && C.nodeType != NT_GL)
+      throw std::runtime_error("split form with Gauss nodes needs the split-Gauss surface correction (not restated)");
+#pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
+    for (int e = 0; e < nE; ++e) for (size_t x = 0; x < nv3; ++x) cons_to_prim(&U[((size_t)e * nv3 + x) * 5], &UPrim[((size_t)e * nv3 + x) * 6]);
+    prolong_to_face<5>(U, U_master, U_slave);
+    // equation.f90:GetPrimitiveStateSurface
+    for (int s = 0; s < nS; ++s) for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
+      cons_to_prim(&U_master[si(0, p, q, s, 5)], &UPrim_master[si(0, p, q, s, 6)]);
+      if (s >= M.nBCSides) cons_to_prim(&U_slave[si(0, p, q, s, 5)], &UPrim_slave[si(0, p, q, s, 6)]);
+    }
+    lifting();
+    vol_int();
+    fill_flux(t);
+    surf_int<5>(Flux_master, Flux_slave, Ut, R(-1.));
+    // Ut = -Ut ; TestcaseSource (channel) ; ApplyJacobianCons
+#pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
+    for (int e = 0; e < nE; ++e) for (size_t x = 0; x < nv3; ++x) {
+      double sj = M.sJ[(size_t)e * nv3 + x];
+      R* ut = &Ut[((size_t)e * nv3 + x) * 5];
+      for (int v = 0; v < 5; ++v) ut[v] = -ut[v];
+      if (C.doTCSource) {
+        ut[1] = ut[1] - R(C.dpdx) / R(sj);
+        ut[4] = ut[4] - R(C.dpdx) / R(sj) * R(BulkVel);
+      }
+      for (int v = 0; v < 5; ++v) ut[v] = ut[v] * R(sj);
+    }
+  }
+
+  // channel testcase.f90:CalcForcing -- bulk velocity (done once per time step before the RK stages)
+  void calc_forcing() {
+    const size_t nv3 = (size_t)n * n * n;
+    double bv = 0.;
+    for (int e = 0; e < nE; ++e) for (size_t x = 0; x < nv3; ++x) {
+      size_t g = (size_t)e * nv3 + x;
+      bv += val(U[g * 5 + 1]) / val(U[g * 5 + 0]) * M.wGPVol[x] / M.sJ[g];
+    }
+    BulkVel = bv / M.Vol;
+  }
+
+  // timestep.f90:TimeStepByLSERKW2
+  void timestep_lserkw2(double& t, double dt) {
+    const size_t nTot = U.size();
+    for (int s = 1; s <= nRKStages; ++s) {
+      double tStage = (s == 1) ? t : t + RKc[s] * dt;
+      time_derivative(tStage);
+      if (s == 1) { for (size_t x = 0; x < nTot; ++x) Ut_tmp[x] = Ut[x]; }
+      else { R a = R(-RKA[s]); for (size_t x = 0; x < nTot; ++x) Ut_tmp[x] = Ut[x] + Ut_tmp[x] * a; }
+      R bdt = R(RKb[s] * dt);
+      for (size_t x = 0; x < nTot; ++x) U[x] = U[x] + Ut_tmp[x] * bdt;
+    }
+    t += dt;
+  }
+
+  // calctimestep.f90:CALCTIMESTEP
+  double calc_timestep(int& errType) {
+    const size_t nv3 = (size_t)n * n * n;
+    errType = 0;
+    double tsConv = HUGE_VAL, tsVisc = HUGE_VAL;
+    for (int e = 0; e < nE; ++e) {
+      double ml[3] = {0., 0., 0.}, mlv[3] = {0., 0., 0.};
+      for (size_t x = 0; x < nv3; ++x) {
+        size_t g = (size_t)e * nv3 + x;
+        double u[5]; for (int v = 0; v < 5; ++v) u[v] = val(U[g * 5 + v]);
+        double srho = 1. / u[0];
+        double vel[3] = {u[1] * srho, u[2] * srho, u[3] * srho};
+        double p = val(kappaM1) * (u[4] - 0.5 * (vel[0] * u[1] + vel[1] * u[2] + vel[2] * u[3]));
+        if (std::isnan(u[0])) errType = 1;
+        double c = std::sqrt(val(kappa) * p * srho);
+        double sj = M.sJ[g];
+        double vsJ[3] = {vel[0] * sj, vel[1] * sj, vel[2] * sj};
+        const double* mm[3] = {&M.Mf[g * 3], &M.Mg[g * 3], &M.Mh[g * 3]};
+        for (int d = 0; d < 3; ++d)
+          ml[d] = std::max(ml[d], std::fabs(mm[d][0] * vsJ[0] + mm[d][1] * vsJ[1] + mm[d][2] * vsJ[2]) + c * MetricsAdv[g * 3 + d]);
+        double mu = val(mu0);
+        for (int d = 0; d < 3; ++d) mlv[d] = std::max(mlv[d], mu * srho * MetricsVisc[g * 3 + d]);
+      }
+      double dtE = CFLScaleEff * 2. / (ml[0] + ml[1] + ml[2]);
+      tsConv = std::min(tsConv, dtE);
+      if (std::isnan(tsConv)) errType = 2;
+      double slv = mlv[0] + mlv[1] + mlv[2];
+      if (slv > 0.) tsVisc = std::min(tsVisc, DFLScaleEff * 4. / slv);
+      if (std::isnan(tsVisc)) errType = 3;
+    }
+    return std::min(tsConv, tsVisc);
+  }
+};
+
+}  // namespace orc

@@ -1,0 +1,354 @@
+// TEST INFRASTRUCTURE ONLY -- part of the CPU oracle (restatement of FLEXI v25.10); see basis.hpp.
+//
+// Face orientation maps (src/mesh/mappings.f90), side numbering and SideToElem/ElemToSide
+// (src/mesh/prepare_mesh.f90:fillMeshInfo, src/mesh/mesh_readin.f90 flips), curl-form volume metrics,
+// Jacobian and surface metrics (src/mesh/metrics.f90:CalcMetrics/CalcSurfMetrics/SurfMetricsFromJa),
+// and solution-point coordinates (metrics.f90:BuildCoords).
+#pragma once
+#include "basis.hpp"
+#include <array>
+#include <algorithm>
+
+namespace orc {
+
+// local side ids, src/flexi.h:90-95
+enum { ZETA_MINUS = 1, ETA_MINUS = 2, XI_PLUS = 3, ETA_PLUS = 4, XI_MINUS = 5, ZETA_PLUS = 6 };
+// src/mesh/mesh_vars.f90:105-111
+static const int NormalDirs[7] = {0, 3, 2, 1, 2, 1, 3};
+static const int TangDirs[7] = {0, 1, 3, 2, 3, 2, 1};
+static const double NormalSigns[7] = {0., -1., -1., 1., 1., -1., 1.};
+
+// mappings.f90:Flip_S2M (3D)
+inline std::array<int, 2> flip_s2m(int N, int p, int q, int flip) {
+  switch (flip) {
+    case 0: return {p, q};
+    case 1: return {q, p};
+    case 2: return {N - p, q};
+    case 3: return {N - q, N - p};
+    default: return {p, N - q};
+  }
+}
+// mappings.f90:CGNS_SideToVol2 (3D)
+inline std::array<int, 2> cgns_side_to_vol2(int N, int p, int q, int locSide) {
+  switch (locSide) {
+    case XI_MINUS: return {q, p};
+    case XI_PLUS: return {p, q};
+    case ETA_MINUS: return {p, q};
+    case ETA_PLUS: return {N - p, q};
+    case ZETA_MINUS: return {q, p};
+    default: return {p, q};  // ZETA_PLUS
+  }
+}
+// mappings.f90:CGNS_SideToVol (3D)
+inline std::array<int, 3> cgns_side_to_vol(int N, int l, int p, int q, int locSide) {
+  switch (locSide) {
+    case XI_MINUS: return {l, q, p};
+    case XI_PLUS: return {N - l, p, q};
+    case ETA_MINUS: return {p, l, q};
+    case ETA_PLUS: return {N - p, N - l, q};
+    case ZETA_MINUS: return {q, p, l};
+    default: return {p, q, N - l};  // ZETA_PLUS
+  }
+}
+// mappings.f90:SideToVol2 / SideToVol
+inline std::array<int, 2> side_to_vol2(int N, int p, int q, int flip, int locSide) {
+  auto pq = flip_s2m(N, p, q, flip);
+  return cgns_side_to_vol2(N, pq[0], pq[1], locSide);
+}
+inline std::array<int, 3> side_to_vol(int N, int l, int p, int q, int flip, int locSide) {
+  auto pq = flip_s2m(N, p, q, flip);
+  return cgns_side_to_vol(N, l, pq[0], pq[1], locSide);
+}
+
+// Face nodes of a volume array: for a local side, face array index (a,b) in "volume order" as used by
+// prolongtoface.t90:EvalElemFaceG/GL (XI sides -> (j,k), ETA -> (i,k), ZETA -> (i,j)) and the normal index.
+inline void face_vol_index(int locSide, int a, int b, int l, int N, int& i, int& j, int& k) {
+  // l = index along the normal direction counted in the volume (0..N)
+  switch (locSide) {
+    case XI_MINUS: case XI_PLUS: i = l; j = a; k = b; break;
+    case ETA_MINUS: case ETA_PLUS: i = a; j = l; k = b; break;
+    default: i = a; j = b; k = l; break;
+  }
+  (void)N;
+}
+
+struct MeshInput {
+  int nElems = 0, NGeo = 1;
+  std::vector<double> NodeCoords;  // Fortran (3,0:NGeo,0:NGeo,0:NGeo,nElems)
+  std::vector<int> ElemNb;         // (3,6,nElems): nbElem(1-based,0=none), nbLocSide, BCIndex(1-based,0=none)
+  int nBCs = 0;
+  std::vector<int> BoundaryType;   // (2,nBCs): type, state
+  std::vector<double> RefStatePrim;  // (6,nRefStates)
+};
+
+// Processed mesh: everything MOD_Mesh_Vars provides to the DG operator.
+struct Mesh {
+  int N = 0, n = 0, NGeo = 1, nElems = 0, nSides = 0, nBCSides = 0, nInnerSides = 0;
+  int firstInnerSide = 0, lastInnerSide = 0;
+  std::vector<int> SideToElem;  // (5,nSides) 1-based entries as in FLEXI, -1 if none
+  std::vector<int> ElemToSide;  // (2,6,nElems)
+  std::vector<int> BC;          // (nBCSides) -> BC index (1-based)
+  std::vector<int> BoundaryType;  // (2,nBCs)
+  std::vector<double> RefStatePrim;
+  std::vector<double> Mf, Mg, Mh;  // Metrics_f/g/hTilde (3,0:N,0:N,0:N,nElems)
+  std::vector<double> sJ;          // (0:N,0:N,0:N,nElems)
+  std::vector<double> NormVec, TangVec1, TangVec2, Face_xGP;  // (3,0:N,0:N,nSides)
+  std::vector<double> SurfElem;    // (0:N,0:N,nSides)
+  std::vector<double> Elem_xGP;    // (3,0:N,0:N,0:N,nElems)
+  double Vol = 0.;
+  std::vector<double> wGPVol;
+  size_t vidx(int i, int j, int k, int e) const { return (((size_t)e * n + k) * n + j) * n + i; }
+  size_t sidx(int p, int q, int s) const { return ((size_t)s * n + q) * n + p; }
+};
+
+// ChangeBasis3D: Xout(nv, 0:No^3) = Vdm (No+1 x Ni+1) applied in all three directions to Xin(nv, 0:Ni^3)
+inline void change_basis_3d(int nv, int Ni, int No, const std::vector<double>& V, const double* Xin, double* Xout) {
+  const int ni = Ni + 1, no = No + 1;
+  std::vector<double> t1((size_t)nv * no * ni * ni, 0.), t2((size_t)nv * no * no * ni, 0.);
+  for (int k = 0; k < ni; ++k) for (int j = 0; j < ni; ++j) for (int a = 0; a < no; ++a)
+    for (int i = 0; i < ni; ++i) { double v = V[a * ni + i];
+      for (int c = 0; c < nv; ++c) t1[(((size_t)k * ni + j) * no + a) * nv + c] += v * Xin[(((size_t)k * ni + j) * ni + i) * nv + c]; }
+  for (int k = 0; k < ni; ++k) for (int b = 0; b < no; ++b) for (int j = 0; j < ni; ++j) { double v = V[b * ni + j];
+    for (int a = 0; a < no; ++a) for (int c = 0; c < nv; ++c)
+      t2[(((size_t)k * no + b) * no + a) * nv + c] += v * t1[(((size_t)k * ni + j) * no + a) * nv + c]; }
+  for (size_t x = 0; x < (size_t)nv * no * no * no; ++x) Xout[x] = 0.;
+  for (int cc = 0; cc < no; ++cc) for (int k = 0; k < ni; ++k) { double v = V[cc * ni + k];
+    for (int b = 0; b < no; ++b) for (int a = 0; a < no; ++a) for (int c = 0; c < nv; ++c)
+      Xout[(((size_t)cc * no + b) * no + a) * nv + c] += v * t2[(((size_t)k * no + b) * no + a) * nv + c]; }
+}
+// ChangeBasisSurf: 2D version
+inline void change_basis_2d(int nv, int Ni, int No, const std::vector<double>& V, const double* Xin, double* Xout) {
+  const int ni = Ni + 1, no = No + 1;
+  std::vector<double> t1((size_t)nv * no * ni, 0.);
+  for (int j = 0; j < ni; ++j) for (int a = 0; a < no; ++a) for (int i = 0; i < ni; ++i) { double v = V[a * ni + i];
+    for (int c = 0; c < nv; ++c) t1[((size_t)j * no + a) * nv + c] += v * Xin[((size_t)j * ni + i) * nv + c]; }
+  for (size_t x = 0; x < (size_t)nv * no * no; ++x) Xout[x] = 0.;
+  for (int b = 0; b < no; ++b) for (int j = 0; j < ni; ++j) { double v = V[b * ni + j];
+    for (int a = 0; a < no; ++a) for (int c = 0; c < nv; ++c) Xout[((size_t)b * no + a) * nv + c] += v * t1[((size_t)j * no + a) * nv + c]; }
+}
+
+// Builds sides, orientation flips, metrics. N: polynomial degree, nodeType: NT_GAUSS / NT_GL.
+inline void build_mesh(const MeshInput& in, int N, int nodeType, Mesh& M) {
+  M.N = N; M.n = N + 1; M.NGeo = in.NGeo; M.nElems = in.nElems;
+  M.BoundaryType = in.BoundaryType; M.RefStatePrim = in.RefStatePrim;
+  const int nE = in.nElems, NG = in.NGeo, ng = NG + 1, n = N + 1;
+  auto nc = [&](int d, int i, int j, int k, int e) { return in.NodeCoords[((((size_t)e * ng + k) * ng + j) * ng + i) * 3 + d]; };
+  auto nb = [&](int c, int ls, int e) { return in.ElemNb[((size_t)e * 6 + (ls - 1)) * 3 + c]; };
+
+  // ---- sides: BC sides first, then inner sides (prepare_mesh.f90: setLocalSideIDs ordering, no MPI sides) ----
+  std::vector<int> sideOf(6 * nE, -1), flipOf(6 * nE, 0);
+  struct S { int e, ls, nbe, nbls, bc; };
+  std::vector<S> bcs, inner;
+  for (int e = 0; e < nE; ++e)
+    for (int ls = 1; ls <= 6; ++ls) {
+      int ne = nb(0, ls, e), nls = nb(1, ls, e), bci = nb(2, ls, e);
+      if (ne == 0) { bcs.push_back({e, ls, -1, -1, bci}); continue; }
+      int oe = ne - 1;
+      // master = element with smaller id (same element: smaller local side id)
+      bool iAmMaster = (e < oe) || (e == oe && ls < nls);
+      if (iAmMaster) inner.push_back({e, ls, oe, nls, 0});
+    }
+  M.nBCSides = (int)bcs.size(); M.nInnerSides = (int)inner.size();
+  M.nSides = M.nBCSides + M.nInnerSides;
+  M.firstInnerSide = M.nBCSides + 1; M.lastInnerSide = M.nSides;
+  M.SideToElem.assign(5 * M.nSides, -1);
+  M.ElemToSide.assign(2 * 6 * nE, 0);
+  M.BC.assign(M.nBCSides, 0);
+  auto s2e = [&](int c, int s) -> int& { return M.SideToElem[(size_t)s * 5 + c]; };
+  auto e2s = [&](int c, int ls, int e) -> int& { return M.ElemToSide[((size_t)e * 6 + (ls - 1)) * 2 + c]; };
+  for (int s = 0; s < M.nBCSides; ++s) {
+    const S& b = bcs[s];
+    s2e(0, s) = b.e + 1; s2e(1, s) = -1; s2e(2, s) = b.ls; s2e(3, s) = -1; s2e(4, s) = 0;
+    e2s(0, b.ls, b.e) = s + 1; e2s(1, b.ls, b.e) = 0;
+    M.BC[s] = b.bc;
+  }
+  // geometric flip: corner nodes of the master face must coincide (up to one constant periodic shift) with the slave's
+  auto face_node = [&](int e, int ls, int p, int q, double* x) {
+    // node (p,q) of the side in CGNS side coordinates at degree NGeo, flip 0
+    auto ij = cgns_side_to_vol2(NG, p, q, ls);
+    int i, j, k; int l = (ls == XI_MINUS || ls == ETA_MINUS || ls == ZETA_MINUS) ? 0 : NG;
+    face_vol_index(ls, ij[0], ij[1], l, NG, i, j, k);
+    for (int d = 0; d < 3; ++d) x[d] = nc(d, i, j, k, e);
+  };
+  for (int t = 0; t < M.nInnerSides; ++t) {
+    const S& si = inner[t];
+    int s = M.nBCSides + t;
+    int best = -1;
+    for (int f = 0; f <= 4 && best < 0; ++f) {
+      double shift[3]; bool ok = true; bool first = true;
+      for (int q = 0; q <= NG && ok; q += NG) for (int p = 0; p <= NG && ok; p += NG) {
+        double xm[3], xs[3];
+        face_node(si.e, si.ls, p, q, xm);
+        // slave node that pairs with master (p,q): slave side coords Flip_M2S(p,q,f)
+        auto ab = flip_s2m(NG, p, q, f);
+        face_node(si.nbe, si.nbls, ab[0], ab[1], xs);
+        double d[3] = {xs[0] - xm[0], xs[1] - xm[1], xs[2] - xm[2]};
+        if (first) { for (int c = 0; c < 3; ++c) shift[c] = d[c]; first = false; }
+        else for (int c = 0; c < 3; ++c) if (std::fabs(d[c] - shift[c]) > 1e-9 * (1. + std::fabs(shift[c]))) ok = false;
+      }
+      if (ok && f > 0) best = f;  // flip 0 is reserved for master sides
+    }
+    if (best < 0) throw std::runtime_error("could not determine side flip");
+    s2e(0, s) = si.e + 1; s2e(1, s) = si.nbe + 1; s2e(2, s) = si.ls; s2e(3, s) = si.nbls; s2e(4, s) = best;
+    e2s(0, si.ls, si.e) = s + 1; e2s(1, si.ls, si.e) = 0;
+    e2s(0, si.nbls, si.nbe) = s + 1; e2s(1, si.nbls, si.nbe) = best;
+  }
+
+  // ---- metrics: metrics.f90:CalcMetrics (curl form, no tree) ----
+  const int NGeoRef = 3 * NG;
+  auto V_EQ_CL = get_vandermonde(NG, NT_VISU, NG, NT_CL, false);
+  auto V_CLNG_CLN = get_vandermonde(NG, NT_CL, N, NT_CL, false);
+  auto DCL_NG = get_derivative_matrix(NG, NT_CL);
+  auto V_CLNG_Ref = get_vandermonde(NG, NT_CL, NGeoRef, nodeType, false);
+  auto V_Ref_N = get_vandermonde(NGeoRef, nodeType, N, nodeType, true);
+  auto DCL_N = get_derivative_matrix(N, NT_CL);
+  auto V_CLN_N = get_vandermonde(N, NT_CL, N, nodeType, false);
+  // Elem_xGP via BuildCoords: Vdm = Vdm_CLN_N * Vdm_EQNGeo_CLN
+  auto V_EQ_CLN = get_vandermonde(NG, NT_VISU, N, NT_CL, false);
+  std::vector<double> V_EQ_N((size_t)n * ng, 0.);
+  for (int a = 0; a < n; ++a) for (int b = 0; b < ng; ++b) { double s = 0.; for (int m = 0; m < n; ++m) s += V_CLN_N[a * n + m] * V_EQ_CLN[m * ng + b]; V_EQ_N[a * ng + b] = s; }
+
+  const size_t nv3 = (size_t)n * n * n;
+  M.Mf.assign(3 * nv3 * nE, 0.); M.Mg.assign(3 * nv3 * nE, 0.); M.Mh.assign(3 * nv3 * nE, 0.);
+  M.sJ.assign(nv3 * nE, 0.); M.Elem_xGP.assign(3 * nv3 * nE, 0.);
+  const size_t nsp = (size_t)n * n;
+  M.NormVec.assign(3 * nsp * M.nSides, 0.); M.TangVec1 = M.NormVec; M.TangVec2 = M.NormVec; M.Face_xGP = M.NormVec;
+  M.SurfElem.assign(nsp * M.nSides, 0.);
+  const int nr = NGeoRef + 1;
+
+  for (int e = 0; e < nE; ++e) {
+    const double* NC = &in.NodeCoords[(size_t)e * ng * ng * ng * 3];
+    std::vector<double> XCL_NG((size_t)ng * ng * ng * 3), XCL_N(nv3 * 3);
+    change_basis_3d(3, NG, NG, V_EQ_CL, NC, XCL_NG.data());
+    change_basis_3d(3, NG, N, V_CLNG_CLN, XCL_NG.data(), XCL_N.data());
+    change_basis_3d(3, NG, N, V_EQ_N, NC, &M.Elem_xGP[(size_t)e * nv3 * 3]);
+    // dXCL_NGeo(dir, comp, i,j,k): stored as [(k,j,i)][dir*3+comp]
+    std::vector<double> dX_NG((size_t)ng * ng * ng * 9, 0.);
+    for (int k = 0; k < ng; ++k) for (int j = 0; j < ng; ++j) for (int i = 0; i < ng; ++i) {
+      double* o = &dX_NG[(((size_t)k * ng + j) * ng + i) * 9];
+      for (int ll = 0; ll < ng; ++ll) for (int c = 0; c < 3; ++c) {
+        o[0 * 3 + c] += DCL_NG[i * ng + ll] * XCL_NG[(((size_t)k * ng + j) * ng + ll) * 3 + c];
+        o[1 * 3 + c] += DCL_NG[j * ng + ll] * XCL_NG[(((size_t)k * ng + ll) * ng + i) * 3 + c];
+        o[2 * 3 + c] += DCL_NG[k * ng + ll] * XCL_NG[(((size_t)ll * ng + j) * ng + i) * 3 + c];
+      }
+    }
+    // dX_NGeoRef = ChangeBasis(dXCL_NGeo), detJac on NGeoRef
+    std::vector<double> dX_Ref((size_t)nr * nr * nr * 9);
+    change_basis_3d(9, NG, NGeoRef, V_CLNG_Ref, dX_NG.data(), dX_Ref.data());
+    std::vector<double> detRef((size_t)nr * nr * nr), detN(nv3);
+    for (size_t x = 0; x < (size_t)nr * nr * nr; ++x) {
+      const double* d = &dX_Ref[x * 9];
+      auto dd = [&](int a, int b) { return d[(a - 1) * 3 + (b - 1)]; };
+      detRef[x] = dd(1, 1) * (dd(2, 2) * dd(3, 3) - dd(3, 2) * dd(2, 3)) + dd(2, 1) * (dd(3, 2) * dd(1, 3) - dd(1, 2) * dd(3, 3)) +
+                  dd(3, 1) * (dd(1, 2) * dd(2, 3) - dd(2, 2) * dd(1, 3));
+    }
+    change_basis_3d(1, NGeoRef, N, V_Ref_N, detRef.data(), detN.data());
+    for (size_t x = 0; x < nv3; ++x) M.sJ[(size_t)e * nv3 + x] = 1. / detN[x];
+    // dXCL_N
+    std::vector<double> dX_N(nv3 * 9, 0.);
+    if (N >= NG) change_basis_3d(9, NG, N, V_CLNG_CLN, dX_NG.data(), dX_N.data());
+    else {
+      for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
+        double* o = &dX_N[(((size_t)k * n + j) * n + i) * 9];
+        for (int ll = 0; ll < n; ++ll) for (int c = 0; c < 3; ++c) {
+          o[0 * 3 + c] += DCL_N[i * n + ll] * XCL_N[(((size_t)k * n + j) * n + ll) * 3 + c];
+          o[1 * 3 + c] += DCL_N[j * n + ll] * XCL_N[(((size_t)k * n + ll) * n + i) * 3 + c];
+          o[2 * 3 + c] += DCL_N[k * n + ll] * XCL_N[(((size_t)ll * n + j) * n + i) * 3 + c];
+        }
+      }
+    }
+    // curl metrics: R_CL_N(dir, comp), JaCL_N(dd, comp)
+    std::vector<double> R(nv3 * 9), Ja(nv3 * 9, 0.);
+    for (size_t x = 0; x < nv3; ++x) {
+      const double* X = &XCL_N[x * 3]; const double* d = &dX_N[x * 9];
+      for (int dir = 0; dir < 3; ++dir) {
+        R[x * 9 + dir * 3 + 0] = 0.5 * (X[2] * d[dir * 3 + 1] - X[1] * d[dir * 3 + 2]);
+        R[x * 9 + dir * 3 + 1] = 0.5 * (X[0] * d[dir * 3 + 2] - X[2] * d[dir * 3 + 0]);
+        R[x * 9 + dir * 3 + 2] = 0.5 * (X[1] * d[dir * 3 + 0] - X[0] * d[dir * 3 + 1]);
+      }
+    }
+    auto Rv = [&](int dir, int comp, int i, int j, int k) { return R[(((size_t)k * n + j) * n + i) * 9 + dir * 3 + comp]; };
+    for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
+      double* J = &Ja[(((size_t)k * n + j) * n + i) * 9];
+      for (int c = 0; c < 3; ++c) {
+        for (int q = 0; q < n; ++q) {
+          J[0 * 3 + c] -= DCL_N[j * n + q] * Rv(2, c, i, q, k);
+          J[1 * 3 + c] -= DCL_N[k * n + q] * Rv(0, c, i, j, q);
+          J[2 * 3 + c] -= DCL_N[i * n + q] * Rv(1, c, q, j, k);
+        }
+        for (int q = 0; q < n; ++q) {
+          J[0 * 3 + c] += DCL_N[k * n + q] * Rv(1, c, i, j, q);
+          J[1 * 3 + c] += DCL_N[i * n + q] * Rv(2, c, q, j, k);
+          J[2 * 3 + c] += DCL_N[j * n + q] * Rv(0, c, i, q, k);
+        }
+      }
+    }
+    // volume metrics: ChangeBasis(Vdm_CLN_N, JaCL_N(dd,:))
+    for (int dd = 0; dd < 3; ++dd) {
+      std::vector<double> tin(nv3 * 3), tout(nv3 * 3);
+      for (size_t x = 0; x < nv3; ++x) for (int c = 0; c < 3; ++c) tin[x * 3 + c] = Ja[x * 9 + dd * 3 + c];
+      change_basis_3d(3, N, N, V_CLN_N, tin.data(), tout.data());
+      std::vector<double>& Mx = dd == 0 ? M.Mf : (dd == 1 ? M.Mg : M.Mh);
+      std::copy(tout.begin(), tout.end(), Mx.begin() + (size_t)e * nv3 * 3);
+    }
+    // surface metrics: CalcSurfMetrics (only for flip==0 sides: master/BC)
+    for (int ls = 1; ls <= 6; ++ls) {
+      int flip = e2s(1, ls, e), SideID = e2s(0, ls, e) - 1;
+      int lface = (ls == XI_MINUS || ls == ETA_MINUS || ls == ZETA_MINUS) ? 0 : N;
+      if (flip == 0) {
+        std::vector<double> tmp(nsp * 3), tmp2(nsp * 3);
+        for (int b = 0; b < n; ++b) for (int a = 0; a < n; ++a) {
+          int i, j, k; face_vol_index(ls, a, b, lface, N, i, j, k);
+          for (int c = 0; c < 3; ++c) tmp[((size_t)b * n + a) * 3 + c] = XCL_N[(((size_t)k * n + j) * n + i) * 3 + c];
+        }
+        change_basis_2d(3, N, N, V_CLN_N, tmp.data(), tmp2.data());
+        for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
+          auto pq = side_to_vol2(N, p, q, 0, ls);
+          for (int c = 0; c < 3; ++c) M.Face_xGP[M.sidx(p, q, SideID) * 3 + c] = tmp2[((size_t)pq[1] * n + pq[0]) * 3 + c];
+        }
+      }
+      if (flip != 0) continue;
+      std::vector<double> JaF(nsp * 9);
+      for (int dd = 0; dd < 3; ++dd) {
+        std::vector<double> tmp(nsp * 3), tmp2(nsp * 3);
+        for (int b = 0; b < n; ++b) for (int a = 0; a < n; ++a) {
+          int i, j, k; face_vol_index(ls, a, b, lface, N, i, j, k);
+          for (int c = 0; c < 3; ++c) tmp[((size_t)b * n + a) * 3 + c] = Ja[(((size_t)k * n + j) * n + i) * 9 + dd * 3 + c];
+        }
+        change_basis_2d(3, N, N, V_CLN_N, tmp.data(), tmp2.data());
+        for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
+          auto pq = side_to_vol2(N, p, q, flip, ls);
+          for (int c = 0; c < 3; ++c) JaF[((size_t)q * n + p) * 9 + dd * 3 + c] = tmp2[((size_t)pq[1] * n + pq[0]) * 3 + c];
+        }
+      }
+      // SurfMetricsFromJa
+      int nd = NormalDirs[ls] - 1, td = TangDirs[ls] - 1; double ns = NormalSigns[ls];
+      for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
+        const double* J = &JaF[((size_t)q * n + p) * 9];
+        size_t si = M.sidx(p, q, SideID);
+        double se = std::sqrt(J[nd * 3 + 0] * J[nd * 3 + 0] + J[nd * 3 + 1] * J[nd * 3 + 1] + J[nd * 3 + 2] * J[nd * 3 + 2]);
+        M.SurfElem[si] = se;
+        double nv[3], t1[3], t2[3];
+        for (int c = 0; c < 3; ++c) nv[c] = ns * J[nd * 3 + c] / se;
+        double dt = J[td * 3 + 0] * nv[0] + J[td * 3 + 1] * nv[1] + J[td * 3 + 2] * nv[2];
+        for (int c = 0; c < 3; ++c) t1[c] = J[td * 3 + c] - dt * nv[c];
+        double tl = std::sqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
+        for (int c = 0; c < 3; ++c) t1[c] /= tl;
+        t2[0] = nv[1] * t1[2] - nv[2] * t1[1];
+        t2[1] = nv[2] * t1[0] - nv[0] * t1[2];
+        t2[2] = nv[0] * t1[1] - nv[1] * t1[0];
+        for (int c = 0; c < 3; ++c) { M.NormVec[si * 3 + c] = nv[c]; M.TangVec1[si * 3 + c] = t1[c]; M.TangVec2[si * 3 + c] = t2[c]; }
+      }
+    }
+  }
+  // analyze.f90:InitAnalyze -- wGPVol and domain volume
+  DGBasis B; B.init(N, nodeType);
+  M.wGPVol.resize(nv3);
+  for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i)
+    M.wGPVol[((size_t)k * n + j) * n + i] = B.wGP[i] * B.wGP[j] * B.wGP[k];
+  double vol = 0.;
+  for (int e = 0; e < nE; ++e) for (size_t x = 0; x < nv3; ++x) vol += M.wGPVol[x] / M.sJ[(size_t)e * nv3 + x];
+  M.Vol = vol;
+}
+
+}  // namespace orc

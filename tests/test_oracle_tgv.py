@@ -1,0 +1,62 @@
+"""End-to-end pin of the CPU oracle: FLEXI's Taylor-Green regression reference
+(regressioncheck/checks/tgv/split: GL N=7, split PI, RoeEntropyFix, BR1, 8^3 periodic, CFL=DFL=0.8,
+Re=1600, Ma=0.1, R=71.42857), whose TGVAnalysis CSV rows are written every 10 steps and compared by
+the reference at 1e-4 relative (analyze.ini). Checks the t=0 row and the first rows after stepping
+with the reference's time-step control (UpdateTimeStep/CALCTIMESTEP), including the time column."""
+import numpy as np
+import pytest
+
+from flexi_gb300 import mesh as fmesh
+from oracle import oracle as orc
+
+TGV_CFG = dict(N=7, nodeType=orc.NT_GL, riemann=33, riemannBC=-1, lifting=1, weakLifting=0, consLifting=0, splitDG=4,
+               etaBR2=2.0, etaBR2_wall=-1.0, kappa=1.4, R=71.42857, Pr=0.72, mu0=6.25e-4, CFLScale=0.8, DFLScale=0.8,
+               doTCSource=0, dpdx=-1.0)
+REL = 1e-4
+
+
+def tgv_oracle(n=8, cfg=TGV_CFG):
+    m = fmesh.tgv_box(n, ngeo=1)
+    o = orc.Oracle(cfg, m)
+    x = o.mesh_array("Elem_xGP")
+    o.set_state(orc.tgv_exact(x, mach=0.1, kappa=cfg["kappa"], R=cfg["R"]))
+    return o
+
+
+def analysis(o, cfg=TGV_CFG):
+    return orc.tgv_analysis(cfg["N"], cfg["nodeType"], o.mesh_array("sJ"), o.get_state(), o.gradients(), 10, cfg["kappa"], cfg["R"],
+                            cfg["mu0"])
+
+
+def compare_row(row, ref, scale):
+    # relative 1e-4 on every column; columns at round-off level (|ref| < 1e-12 of the column scale) in absolute terms
+    for c in range(len(ref)):
+        if abs(ref[c]) > 1e-12 * scale[c]:
+            assert abs(row[c] - ref[c]) <= REL * abs(ref[c]), (c, row[c], ref[c])
+        else:
+            assert abs(row[c]) <= 1e-9 * scale[c], (c, row[c], ref[c])
+
+
+def test_tgv_t0_row(tgv_reference):
+    _, rows = tgv_reference
+    o = tgv_oracle()
+    o.time_derivative(0.0)
+    a = analysis(o)
+    scale = np.abs(rows[:, 1:]).max(axis=0)
+    compare_row(a, rows[0, 1:], scale)
+
+
+@pytest.mark.timeout(900)
+def test_tgv_first_rows(tgv_reference):
+    _, rows = tgv_reference
+    o = tgv_oracle()
+    scale = np.abs(rows[:, 1:]).max(axis=0)
+    t = 0.0
+    o.time_derivative(0.0)
+    for r in (1, 2):
+        for _ in range(10):
+            dt, err = o.calc_timestep()
+            assert err == 0
+            t = o.timestep(t, dt)
+        assert abs(t - rows[r, 0]) <= 1e-10 * rows[r, 0], (t, rows[r, 0])
+        compare_row(analysis(o), rows[r, 1:], scale)
