@@ -1,0 +1,316 @@
+"""Benchmark: FP64 DOF*stage/s of FLEXI's DGSEM Navier-Stokes RHS + LSERK stepper on GB300.
+
+Workload (default): Taylor-Green vortex on a curved periodic 32^3 hexahedral mesh, N=7 Gauss-Lobatto,
+split form with the Pirozzoli flux, BR2 lifting, RoeEntropyFix surface flux (the reference's split-form
+solver; it rejects HLLC with the split form), Re=1600, Ma=0.1, FP64, CarpenterRK4-5 with CFL/DFL time
+step control at CFLScale=DFLScale=0.8 (the setting of the reference's own split-form TGV regression; 0.9
+is at the stability edge of this discretisation). 16.8 M DOF x 5 variables; the state alone (671 MB) exceeds L2 (129 MB), so no L2 flush is
+needed between steps. Synthetic data: mesh and initial state are generated (no external dataset).
+
+value  : DOF*stage/s on the device, inputs resident in HBM, K steps bracketed by CUDA events on the
+         solver's stream (barrier + synchronize on both sides, max over ranks).
+e2e    : the same metric through the public C ABI with the state in pinned host memory: each step
+         uploads U (fg_set_state), advances one step (fg_run), downloads U (fg_get_state).
+--impl reference : the CPU implementation of the path (the C++ restatement of FLEXI's Fortran solver,
+         FLEXI itself cannot be built here: Fortran/MPI/HDF5) on all host threads, bounded sample per step.
+Multi-GPU: the path does not shard on this setup (no halo exchange is built); N ranks run N replicas.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "FP64 DOF*stage/s (N=7 TGV)"
+UNIT = "DOF*stage/s"
+# algorithmic flops per DOF and RK stage of the reference algorithm (counted with the oracle's
+# flop-counting scalar on this configuration; pinned by tests/test_bench_constants.py)
+FLOPS_PER_DOF_STAGE = {"prep": 24.5, "lift": 322.5, "flux": 145.5, "vol": 1408.9}
+# compulsory HBM traffic per DOF and stage: U read+write, Ut_tmp read+write, 9 metric terms + sJ
+BYTES_ALG_PER_DOF_STAGE = 240.0
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--elems", type=int, default=32, help="elements per direction")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def workload_config(n):
+    return {"workload": f"TGV {n}^3 curved (perturbation 0.05, NGeo=3), N=7 Gauss-Lobatto, split PI, BR2, RoeEntropyFix, FP64",
+            "n_elems": n ** 3, "N": 7, "dof": n ** 3 * 512, "Re": 1600, "Ma": 0.1, "CFLScale": 0.8, "DFLScale": 0.8,
+            "time_integration": "CarpenterRK4-5, 5 stages/step, CFL/DFL dt each step",
+            "l2": "inputs larger than L2 (state 671 MB at 32^3)", "parallelism": "replicas"}
+
+
+def solver_config():
+    from flexi_gb300.solver import make_config
+    return make_config(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roeentropyfix", Lifting="br2", kappa=1.4, R=71.42857,
+                       Pr=0.72, mu0=6.25e-4, CFLScale=0.8, DFLScale=0.8)
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                                          "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"), f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def ncu_traffic():
+    try:
+        return json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
+    except Exception:
+        return {}
+
+
+def cpu_baseline_sample(n_elems_dir=8, budget_s=12.0):
+    """Oracle (C++ restatement of FLEXI's operator) on all host threads: TGV sample of the same
+    discretisation, timed RK steps until the budget is used. Returns (DOF*stage/s, threads, sample)."""
+    import numpy as np
+    from flexi_gb300 import mesh as fmesh, testcases
+    from oracle import oracle as orc
+    orc.set_threads(os.cpu_count() or 1)
+    cfg = dict(N=7, nodeType=2, riemann=33, riemannBC=-1, lifting=2, weakLifting=0, consLifting=0, splitDG=4, etaBR2=2.0, etaBR2_wall=-1.0,
+               kappa=1.4, R=71.42857, Pr=0.72, mu0=6.25e-4, CFLScale=0.8, DFLScale=0.8, doTCSource=0, dpdx=-1.0)
+    m = fmesh.tgv_box(n_elems_dir, ngeo=3, perturb=0.05, seed=0)
+    o = orc.Oracle(cfg, m)
+    o.set_state(testcases.tgv_state(o.mesh_array("Elem_xGP"), mach=0.1, kappa=1.4, R=71.42857))
+    dof = m.n_elems * 512
+    t = 0.0
+    dt, _ = o.calc_timestep()
+    t = o.timestep(t, dt)  # warm-up
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        dt, _ = o.calc_timestep()
+        t = o.timestep(t, dt)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or steps >= 200:
+            break
+    rate = dof * 5 * steps / el
+    return rate, orc.max_threads(), f"TGV {n_elems_dir}^3 same discretisation ({dof} DOF), {steps} RK steps with dt control, {el:.1f} s"
+
+
+def run_reference(args):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return
+    import numpy as np
+    from flexi_gb300 import mesh as fmesh, testcases
+    from oracle import oracle as orc
+    threads = os.cpu_count() or 1
+    orc.set_threads(threads)
+    cfg = dict(N=7, nodeType=2, riemann=33, riemannBC=-1, lifting=2, weakLifting=0, consLifting=0, splitDG=4, etaBR2=2.0, etaBR2_wall=-1.0,
+               kappa=1.4, R=71.42857, Pr=0.72, mu0=6.25e-4, CFLScale=0.8, DFLScale=0.8, doTCSource=0, dpdx=-1.0)
+    ns = 6  # bounded sample: 6^3 elements of the same discretisation per step
+    m = fmesh.tgv_box(ns, ngeo=3, perturb=0.05, seed=0)
+    o = orc.Oracle(cfg, m)
+    o.set_state(testcases.tgv_state(o.mesh_array("Elem_xGP"), mach=0.1, kappa=1.4, R=71.42857))
+    dof = m.n_elems * 512
+    t = 0.0
+    for _ in range(args.warmup):
+        dt, _ = o.calc_timestep()
+        t = o.timestep(t, dt)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        dt, _ = o.calc_timestep()
+        t = o.timestep(t, dt)
+    el = time.perf_counter() - t0
+    value = dof * 5 * args.steps / el
+    sample = f"TGV {ns}^3 of the workload's discretisation ({dof} DOF) per step, {args.steps} RK steps, {el:.2f} s"
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(args.elems),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "C++ restatement of FLEXI's Fortran path (FLEXI needs Fortran, MPI and HDF5, absent here)"}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args):
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    ws, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from flexi_gb300 import mesh as fmesh, testcases
+    from flexi_gb300.solver import Flexi, probe_fp64_tflops
+
+    n = args.elems
+    cfgd = workload_config(n)
+    c = solver_config()
+    m = fmesh.tgv_box(n, ngeo=3, perturb=0.05, seed=rank)
+    f = Flexi(c, m)
+    U0 = testcases.tgv_state(f.elem_xgp(), mach=0.1, kappa=1.4, R=71.42857)
+    f.U = U0
+    dof = f.n_elems * f.n ** 3
+    stream = torch.cuda.ExternalStream(f.stream())
+    fp64_peak = probe_fp64_tflops()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+
+    # warm-up (graph capture happens here)
+    f.TimeDisc(args.warmup)
+    # timed region: K steps, per-kernel events on the solver stream
+    f.profile(True)
+    f.profile_read()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    f.TimeDisc(args.steps)
+    e1.record(stream)
+    barrier()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    prof = f.profile_read()
+    launches_per_step = f.launch_count()
+    f.profile(False)
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = dof * 5 * args.steps * ws / (ms * 1e-3)
+
+    # e2e through the public API, state in pinned host memory
+    e2e = None
+    if not args.no_e2e:
+        nbytes = dof * 5 * 8
+        hin = torch.empty(dof * 5, dtype=torch.float64).pin_memory()
+        hout = torch.empty(dof * 5, dtype=torch.float64).pin_memory()
+        f.get_state_ptr(hin.data_ptr())
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            f.set_state_ptr(hin.data_ptr())
+            f.TimeDisc(1)
+            f.get_state_ptr(hout.data_ptr())
+            hin, hout = hout, hin
+        barrier()
+        el = time.perf_counter() - t0
+        if ws > 1:
+            t = torch.tensor([el], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            el = float(t.item())
+        e2e = {"value": dof * 5 * args.steps * ws / el, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+               "ms_per_step": el / args.steps * 1e3}
+
+    if rank != 0:
+        f.close()
+        return
+    # roofline of the dominant kernel class
+    dom = max(("prep", "lift", "flux", "vol"), key=lambda k: prof[k][0])
+    dom_ms, dom_cnt = prof[dom]
+    avg_ms = dom_ms / max(dom_cnt, 1)
+    achieved = FLOPS_PER_DOF_STAGE[dom] * dof / (avg_ms * 1e-3) / 1e12
+    peaks = measured_peaks()
+    traffic = ncu_traffic().get(dom)
+    roofline = {"bound": "fp64", "kernel": {"vol": "k_vol_split<8>", "lift": "k_lift<8,GL>", "flux": "k_flux<8>", "prep": "k_prep<8,GL>"}[dom],
+                "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved / fp64_peak,
+                "peak_source": "own DFMA probe (fg_probe_fp64), MEASURED_PEAKS.json has no FP64 figure",
+                "traffic": (traffic * dof / 1e6 if traffic is not None else None),
+                "traffic_unit": "bytes per launch (ncu dram read+write, scaled per DOF)" if traffic is not None else None,
+                "algorithmic_flops_per_dof": FLOPS_PER_DOF_STAGE[dom], "avg_launch_ms": avg_ms,
+                "hbm_alg_gbs": value / ws * BYTES_ALG_PER_DOF_STAGE / 1e9,
+                "hbm_peak_gbs": peaks.get("hbm_gbs"),
+                "frac_hbm": (value / ws * BYTES_ALG_PER_DOF_STAGE / 1e9 / peaks["hbm_gbs"]) if peaks.get("hbm_gbs") else None,
+                "kernel_ms_per_step": {k: prof[k][0] / args.steps for k in prof}}
+    try:
+        cpu_val, cores, sample = cpu_baseline_sample()
+        cpu = {"value": cpu_val, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+    except Exception as ex:  # reported, never substituted for the GPU path
+        cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port", "sample": f"failed: {ex}"}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": cfgd, "e2e": e2e, "gpu_launches": launches_per_step * args.steps, "clocks": clk,
+            "roofline": roofline, "cpu_baseline": cpu}
+    print(json.dumps(line), flush=True)
+    f.close()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -17,8 +17,8 @@ class FgConfig(ctypes.Structure):
 
 EXPORTS = ["fg_config_default", "fg_config_from_ini", "fg_create", "fg_destroy", "fg_last_error", "fg_build_mesh", "fg_set_mesh",
            "fg_set_instance_mu0", "fg_get_elem_xgp", "fg_get_sizes", "fg_get_mesh_array", "fg_get_side_to_elem", "fg_set_state",
-           "fg_get_state", "fg_state_device_ptr", "fg_time_derivative", "fg_calc_timestep", "fg_timestep_lserkw2", "fg_run",
-           "fg_get_gradients", "fg_get_stream", "fg_launch_count", "fg_probe_fp64"]
+           "fg_get_state", "fg_state_device_ptr", "fg_time_derivative", "fg_calc_timestep", "fg_get_dt_elem", "fg_timestep_lserkw2", "fg_run",
+           "fg_get_gradients", "fg_get_stream", "fg_launch_count", "fg_debug_array", "fg_profile_enable", "fg_profile_read", "fg_probe_fp64"]
 
 
 def load(path=None):
@@ -50,12 +50,16 @@ def load(path=None):
     L.fg_state_device_ptr.argtypes = [P, ctypes.POINTER(P)]
     L.fg_time_derivative.argtypes = [P, D, P]
     L.fg_calc_timestep.argtypes = [P, P, PI]
+    L.fg_get_dt_elem.argtypes = [P, P, P]
     L.fg_timestep_lserkw2.argtypes = [P, ctypes.POINTER(D), D]
     L.fg_run.argtypes = [P, I, P]
     L.fg_get_gradients.argtypes = [P, P, P, P]
     L.fg_get_stream.argtypes = [P, ctypes.POINTER(P)]
     L.fg_launch_count.argtypes = [P]
     L.fg_launch_count.restype = ctypes.c_longlong
+    L.fg_debug_array.argtypes = [P, ctypes.c_char_p, P, ctypes.POINTER(ctypes.c_longlong)]
+    L.fg_profile_enable.argtypes = [P, I]
+    L.fg_profile_read.argtypes = [P, P, P]
     L.fg_probe_fp64.argtypes = [ctypes.POINTER(D)]
     _lib = L
     return L

@@ -67,6 +67,7 @@ struct Dev {
   double* bulkVel; // [nInst]
   double* dpdx;    // [nInst] (0 when no body force)
   int* err;        // [1] sticky error word
+  double* dtElem;  // [2][nElems] convective and viscous element time-step limits of the last CALCTIMESTEP
 };
 
 // ------------------------------------------------------------------------------------------------------

@@ -105,7 +105,8 @@ struct fg_handle {
   KernelSet K{};
   fgh::HostMesh M;
   Dev d{};
-  bool haveMesh = false;
+  bool haveMesh = false;      // device arrays ready
+  bool haveHostMesh = false;  // host-side mesh ready (set-up can be inspected without a GPU)
   cudaStream_t st = nullptr;
   std::vector<DevBuf> bufs;
   double* dMetAdv = nullptr;
@@ -122,6 +123,11 @@ struct fg_handle {
   long long launches = 0;
   std::string err;
   std::vector<double> instMu0;
+  // per-kernel event timing (fg_profile_enable)
+  bool profiling = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> evPool;
+  std::vector<int> evClass;
+  size_t evUsed = 0;
 };
 
 namespace {
@@ -160,6 +166,8 @@ int upload(fg_handle* h, T*& ptr, const std::vector<T>& v) {
 }
 void free_device(fg_handle* h) {
   if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+  for (auto& e : h->evPool) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+  h->evPool.clear(); h->evClass.clear(); h->evUsed = 0;
   for (auto& b : h->bufs) cudaFree(b.p);
   h->bufs.clear();
   h->haveMesh = false;
@@ -219,14 +227,23 @@ void init_basis(fg_handle* h) {
   static const double dflG[10] = {1.12, 0.76, 0.55, 0.41, 0.32, 0.25, 0.20, 0.17, 0.14, 0.12};
   static const double dflGL[10] = {4.50, 1.95, 1.18, 0.79, 0.56, 0.42, 0.32, 0.25, 0.20, 0.17};
   const bool gl = c.NodeType == FG_NODE_GAUSS_LOBATTO;
-  h->cflEff = c.CFLScale * (gl ? cflGL : cflG)[std::min(15, N) - 1] / (2. * N + 1.);
-  h->dflEff = c.DFLScale * (gl ? dflGL : dflG)[std::min(10, N) - 1] * 1.853 / ((2. * N + 1.) * (2. * N + 1.));
+  // table lookups through plain pointers: indexing a conditional expression of two arrays with a
+  // non-literal subscript mis-compiles with the host compiler in use here (g++ 13 returns 0)
+  const double* cflTab = gl ? cflGL : cflG;
+  const double* dflTab = gl ? dflGL : dflG;
+  const int iC = (N < 15 ? N : 15) - 1, iD = (N < 10 ? N : 10) - 1;
+  h->cflEff = c.CFLScale * cflTab[iC] / (2. * N + 1.);
+  h->dflEff = c.DFLScale * dflTab[iD] * 1.853 / ((2. * N + 1.) * (2. * N + 1.));
 }
 
 int upload_mesh(fg_handle* h) {
   fgh::HostMesh& M = h->M;
   fgh::finish_mesh(M, h->cfg.kappa, h->cfg.Pr);
+  h->haveHostMesh = true;
   free_device(h);
+  if (!h->st) CUDA_TRY(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+  h->K.prepare();
+  CUDA_TRY(cudaGetLastError());
   const int n = M.n, n2 = n * n, n3 = n2 * n, nE = M.nElems, nS = M.nSides;
   Dev& d = h->d;
   d = Dev{};
@@ -258,6 +275,7 @@ int upload_mesh(fg_handle* h) {
   if ((r = upload(h, d.bulkVel, zero))) return r;
   if ((r = upload(h, d.dpdx, dp))) return r;
   if ((r = upload(h, d.err, std::vector<int>(1, 0)))) return r;
+  if ((r = dalloc(h, d.dtElem, (size_t)2 * nE))) return r;
   if ((r = upload(h, h->dMetAdv, M.metAdv))) return r;
   if ((r = upload(h, h->dMetVisc, M.metVisc))) return r;
   if ((r = upload(h, h->dWVol, M.wVol))) return r;
@@ -273,18 +291,45 @@ int upload_mesh(fg_handle* h) {
   if ((r = upload(h, h->dInstVol, M.instVol))) return r;
   if ((r = upload(h, h->dTime, zero))) return r;
   if ((r = dalloc(h, h->dStage, (size_t)nE * 12 * n3))) return r;
+  // the uploads above run on the legacy default stream, which the solver's non-blocking stream does not
+  // order against: finish them before any kernel can read the arrays
+  CUDA_TRY(cudaDeviceSynchronize());
   h->haveMesh = true;
   return 0;
 }
 
+// event pair around one launch of kernel class cls (profiling mode only)
+struct ProfScope {
+  fg_handle* h;
+  size_t slot = (size_t)-1;
+  ProfScope(fg_handle* h_, int cls) : h(h_) {
+    if (!h->profiling) return;
+    if (h->evUsed == h->evPool.size()) {
+      cudaEvent_t a, b;
+      cudaEventCreate(&a); cudaEventCreate(&b);
+      h->evPool.push_back({a, b});
+      h->evClass.push_back(0);
+    }
+    slot = h->evUsed++;
+    h->evClass[slot] = cls;
+    cudaEventRecord(h->evPool[slot].first, h->st);
+  }
+  ~ProfScope() {
+    if (slot != (size_t)-1) cudaEventRecord(h->evPool[slot].second, h->st);
+  }
+};
+
 // state sequence of one right-hand side evaluation plus the RK register update
 void launch_rhs(fg_handle* h, int mode, double rkA, double rkB) {
   const Dev& d = h->d;
-  h->K.prep(d, h->B, h->st);
-  h->K.lift(d, h->B, h->st);
-  h->K.flux(d, h->B, h->st);
-  if (h->cfg.SplitDG >= 0) h->K.vol_split(d, h->B, mode, rkA, rkB, h->st);
-  else h->K.vol_weak(d, h->B, mode, rkA, rkB, h->st);
+  { ProfScope p(h, 0); h->K.prep(d, h->B, h->st); }
+  { ProfScope p(h, 1); h->K.lift(d, h->B, h->st); }
+  { ProfScope p(h, 2); h->K.flux(d, h->B, h->st); }
+  {
+    ProfScope p(h, 3);
+    if (h->cfg.SplitDG >= 0) h->K.vol_split(d, h->B, mode, rkA, rkB, h->st);
+    else h->K.vol_weak(d, h->B, mode, rkA, rkB, h->st);
+  }
   h->launches += 4;
 }
 // step set-up: mode 0 = CALCTIMESTEP, 1 = fixed dt, 2 = bulk velocity only (plain right-hand side)
@@ -302,7 +347,7 @@ void launch_step_setup(fg_handle* h, int mode, double fixedDt, bool advanceTime)
   }
   if (computeDt) {
     k_fill<<<(nI + 127) / 128, 128, 0, h->st>>>(d.dt, INFINITY, nI);
-    h->K.dt(d, h->B, h->dMetAdv, h->dMetVisc, h->cflEff, h->dflEff, h->dBulkPart, h->dWVol, h->st);
+    { ProfScope p(h, 4); h->K.dt(d, h->B, h->dMetAdv, h->dMetVisc, h->cflEff, h->dflEff, h->dBulkPart, h->dWVol, h->st); }
     h->launches += 2;
   } else {
     k_fill<<<(nI + 127) / 128, 128, 0, h->st>>>(d.dt, fixedDt, nI);
@@ -410,7 +455,7 @@ int fg_create(const fg_config* cfg, fg_handle** out) {
     why = "Riemann must be LF, HLLC, Roe or RoeEntropyFix";
   else if (c.Lifting != 1 && c.Lifting != 2) why = "Lifting must be 1 (BR1) or 2 (BR2)";
   else if (c.doConservativeLifting) why = "doConservativeLifting is not supported";
-  else if (c.Lifting == 2 && c.doWeakLifting) why = "BR2 lifting is strong only";
+  else if (c.doWeakLifting) why = "doWeakLifting is not supported (the volume part needs the conservative form)";
   else if (c.SplitDG != FG_SPLIT_NONE && c.SplitDG != FG_SPLIT_SD && c.SplitDG != FG_SPLIT_PI) why = "SplitDG must be -1 (weak), 0 (SD) or 4 (PI)";
   else if (c.SplitDG != FG_SPLIT_NONE && c.NodeType != FG_NODE_GAUSS_LOBATTO) why = "the split form is supported with Gauss-Lobatto nodes";
   else if (c.SplitDG != FG_SPLIT_NONE && c.N != 1 && c.N != 3 && c.N != 7) why = "the split form supports N = 1, 3, 7";
@@ -419,7 +464,6 @@ int fg_create(const fg_config* cfg, fg_handle** out) {
   h->K = get_kernel_set(c.N + 1, c.NodeType == FG_NODE_GAUSS_LOBATTO);
   if (h->K.n == 0) { delete h; return fail(nullptr, FG_ERR_CONFIG, "no kernels for this N"); }
   init_basis(h);
-  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) { delete h; return FG_ERR_CUDA; }
   *out = h;
   return FG_OK;
 }
@@ -480,7 +524,7 @@ int fg_get_sizes(const fg_handle* h, int* out) {
 }
 
 int fg_get_elem_xgp(fg_handle* h, double* X) {
-  if (!h || !h->haveMesh || h->M.elemX.empty()) return fail(h, FG_ERR_STATE, "no solution coordinates (mesh not built from nodes)");
+  if (!h || !h->haveHostMesh || h->M.elemX.empty()) return fail(h, FG_ERR_STATE, "no solution coordinates (mesh not built from nodes)");
   const int n3 = h->M.n * h->M.n * h->M.n;
   for (int e = 0; e < h->M.nElems; ++e)
     for (int x = 0; x < n3; ++x)
@@ -489,7 +533,7 @@ int fg_get_elem_xgp(fg_handle* h, double* X) {
 }
 
 int fg_get_mesh_array(fg_handle* h, int which, double* out) {
-  if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
+  if (!h || !h->haveHostMesh) return fail(h, FG_ERR_STATE, "no mesh");
   const fgh::HostMesh& M = h->M;
   const int n = M.n, n2 = n * n, n3 = n2 * n;
   if (which >= 0 && which <= 2) {
@@ -507,7 +551,7 @@ int fg_get_mesh_array(fg_handle* h, int which, double* out) {
 }
 
 int fg_get_side_to_elem(fg_handle* h, int* out) {
-  if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
+  if (!h || !h->haveHostMesh) return fail(h, FG_ERR_STATE, "no mesh");
   for (int s = 0; s < h->M.nSides; ++s) {
     const int* r = &h->M.sideElem[s * 4];
     out[s * 5 + 0] = r[0] + 1; out[s * 5 + 2] = r[1];
@@ -579,6 +623,15 @@ int fg_calc_timestep(fg_handle* h, double* dt, int* errType) {
   return FG_OK;
 }
 
+int fg_get_dt_elem(fg_handle* h, double* dtConv, double* dtVisc) {
+  if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
+  const int nE = h->d.nElems;
+  if (dtConv) CUDA_TRY(cudaMemcpyAsync(dtConv, h->d.dtElem, sizeof(double) * nE, cudaMemcpyDeviceToHost, h->st));
+  if (dtVisc) CUDA_TRY(cudaMemcpyAsync(dtVisc, h->d.dtElem + nE, sizeof(double) * nE, cudaMemcpyDeviceToHost, h->st));
+  CUDA_TRY(cudaStreamSynchronize(h->st));
+  return FG_OK;
+}
+
 int fg_timestep_lserkw2(fg_handle* h, double* t, double dt) {
   if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
   h->launches = 0;
@@ -595,6 +648,18 @@ int fg_run(fg_handle* h, int nSteps, double* t) {
   if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
   if (nSteps < 0) return fail(h, FG_ERR_CONFIG, "nSteps < 0");
   CUDA_TRY(cudaMemsetAsync(h->d.err, 0, sizeof(int), h->st));
+  if (h->profiling) {  // direct launches with per-kernel events
+    h->launches = 0;
+    for (int s = 0; s < nSteps; ++s) {
+      launch_step_setup(h, 0, 0., true);
+      launch_lserk(h);
+    }
+    CUDA_TRY(cudaGetLastError());
+    if (int r = check_err(h)) return r;
+    if (t) CUDA_TRY(cudaMemcpy(t, h->dTime, sizeof(double) * h->d.nInst, cudaMemcpyDeviceToHost));
+    if (nSteps > 0) h->launches /= nSteps;
+    return FG_OK;
+  }
   if (!h->graph) {
     cudaGraph_t g;
     const long long before = h->launches;
@@ -632,6 +697,58 @@ int fg_get_stream(fg_handle* h, void** s) {
 }
 
 long long fg_launch_count(const fg_handle* h) { return h ? h->launches : 0; }
+
+int fg_debug_array(fg_handle* h, const char* name, void* out, long long* count) {
+  if (!h || !h->haveMesh || !name || !count) return fail(h, FG_ERR_STATE, "no mesh");
+  const long long n3 = (long long)h->M.n * h->M.n * h->M.n, nE = h->d.nElems, nS = h->d.nSides;
+  const std::string k = name;
+  const void* src = nullptr;
+  long long cnt = 0;
+  size_t esz = sizeof(double);
+  if (k == "U") { src = h->d.U; cnt = nE * 5 * n3; }
+  else if (k == "Ut") { src = h->d.Ut; cnt = nE * 5 * n3; }
+  else if (k == "prim") { src = h->d.prim; cnt = nE * VP_NF * n3; }
+  else if (k == "grad") { src = h->d.grad; cnt = nE * 12 * n3; }
+  else if (k == "metr") { src = h->d.metr; cnt = nE * 9 * n3; }
+  else if (k == "sJ") { src = h->d.sJ; cnt = nE * n3; }
+  else if (k == "metAdv") { src = h->dMetAdv; cnt = nE * 3 * n3; }
+  else if (k == "metVisc") { src = h->dMetVisc; cnt = nE * 3 * n3; }
+  else if (k == "mu0") { src = h->d.mu0; cnt = h->d.nInst; }
+  else if (k == "dt") { src = h->d.dt; cnt = h->d.nInst; }
+  else if (k == "dtElem") { src = h->d.dtElem; cnt = 2 * nE; }
+  else if (k == "elemInst") { src = h->d.elemInst; cnt = nE; esz = sizeof(int); }
+  else if (k == "elemSide") { src = h->d.elemSide; cnt = nE * 6; esz = sizeof(int); }
+  else if (k == "sideElem") { src = h->d.sideElem; cnt = nS * 4; esz = sizeof(int); }
+  else return fail(h, FG_ERR_CONFIG, "unknown array " + k);
+  *count = cnt;
+  if (out) {
+    CUDA_TRY(cudaStreamSynchronize(h->st));
+    CUDA_TRY(cudaMemcpy(out, src, cnt * esz, cudaMemcpyDeviceToHost));
+  }
+  return FG_OK;
+}
+
+int fg_profile_enable(fg_handle* h, int on) {
+  if (!h) return FG_ERR_STATE;
+  h->profiling = on != 0;
+  h->evUsed = 0;
+  return FG_OK;
+}
+
+int fg_profile_read(fg_handle* h, double* ms, long long* counts) {
+  if (!h) return FG_ERR_STATE;
+  for (int c = 0; c < 6; ++c) { if (ms) ms[c] = 0.; if (counts) counts[c] = 0; }
+  if (h->st) CUDA_TRY(cudaStreamSynchronize(h->st));
+  for (size_t i = 0; i < h->evUsed; ++i) {
+    float t = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&t, h->evPool[i].first, h->evPool[i].second));
+    const int c = h->evClass[i];
+    if (ms) ms[c] += t;
+    if (counts) counts[c] += 1;
+  }
+  h->evUsed = 0;
+  return FG_OK;
+}
 
 int fg_probe_fp64(double* tflops) {
   fg_handle* h = nullptr;

@@ -17,18 +17,18 @@ struct Inst {
   static size_t smem_split() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * (32 * S::n3 + 6 * S::n2 * 5)); }
   template <class K>
   static void set_smem(K kern, size_t bytes) {
-    static bool done = false;
-    if (!done) {
-      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-      done = true;
-    }
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  }
+  static void prepare() {
+    set_smem(k_prep<n, GL>, smem_prep());
+    set_smem(k_lift<n, GL>, smem_lift());
+    set_smem(k_vol_weak<n, GL>, smem_weak());
+    if constexpr (GL && (n == 2 || n == 4 || n == 8)) set_smem(k_vol_split<n>, smem_split());
   }
   static void prep(const Dev& d, const Basis& B, cudaStream_t st) {
-    set_smem(k_prep<n, GL>, smem_prep());
     k_prep<n, GL><<<blocks(d), S::THREADS, smem_prep(), st>>>(d, B);
   }
   static void lift(const Dev& d, const Basis& B, cudaStream_t st) {
-    set_smem(k_lift<n, GL>, smem_lift());
     k_lift<n, GL><<<blocks(d), S::THREADS, smem_lift(), st>>>(d, B);
   }
   static void flux(const Dev& d, const Basis& B, cudaStream_t st) {
@@ -36,12 +36,10 @@ struct Inst {
     k_flux<n><<<(unsigned)((pts + 127) / 128), 128, 0, st>>>(d, B);
   }
   static void vol_weak(const Dev& d, const Basis& B, int mode, double rkA, double rkB, cudaStream_t st) {
-    set_smem(k_vol_weak<n, GL>, smem_weak());
     k_vol_weak<n, GL><<<blocks(d), S::THREADS, smem_weak(), st>>>(d, B, Stage{mode, rkA, rkB});
   }
   static void vol_split(const Dev& d, const Basis& B, int mode, double rkA, double rkB, cudaStream_t st) {
     if constexpr (GL && (n == 2 || n == 4 || n == 8)) {
-      set_smem(k_vol_split<n>, smem_split());
       k_vol_split<n><<<blocks(d), S::THREADS, smem_split(), st>>>(d, B, Stage{mode, rkA, rkB});
     }
   }
@@ -52,6 +50,7 @@ struct Inst {
   static KernelSet make() {
     KernelSet k;
     k.n = n; k.gl = GL;
+    k.prepare = &prepare;
     k.prep = &prep; k.lift = &lift; k.flux = &flux; k.vol_weak = &vol_weak; k.dt = &dt;
     if (GL && (n == 2 || n == 4 || n == 8)) k.vol_split = &vol_split;
     return k;

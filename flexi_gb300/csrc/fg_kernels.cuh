@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_lift(Dev d, Basis B) {
     const int es = t / n3, x = t - es * n3, e = e0 + es;
     if (e >= d.nElems) continue;
 #pragma unroll
-    for (int v = 0; v < 4; ++v) sL[(es * 4 + v) * n3 + x] = d.prim[((size_t)e * VP_NF + VP_U + v) * n3 + x];
+    for (int v = 0; v < 4; ++v) sL[(es * 4 + v) * n3 + x] = d.prim[((size_t)e * VP_NF + (v < 3 ? VP_U + v : VP_T)) * n3 + x];
     sJs[es * n3 + x] = d.sJ[(size_t)e * n3 + x];
   }
   // surface lifting fluxes of the six sides (lifting_fillflux.t90), stored in this element's face order
@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_lift(Dev d, Basis B) {
       const double bval[4] = {0., 0., 0., Tb};
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
-        const double um = fm[(FS_U + (v < 3 ? v : 3)) * n2];
+        const double um = fm[(v < 3 ? FS_U + v : FS_T) * n2];
         const double f = B.weakLifting ? bval[v] : bval[v] - um;
         F[v] = f * se;
       }
@@ -182,7 +182,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_lift(Dev d, Basis B) {
       const double hs = 0.5 * se;
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
-        const int f = FS_U + (v < 3 ? v : 3);
+        const int f = v < 3 ? FS_U + v : FS_T;
         F[v] = (sig * fm[f * n2] + fsl[f * n2]) * hs;
       }
       // slave side of a weak lifting integrates -Flux
@@ -724,65 +724,58 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_dt(Dev d, Basis B, const 
                                                           double* bulkPart /* [nElems] or null */, const double* wVol) {
   using S = Shape<n>;
   constexpr int n3 = S::n3, EPB = S::EPB;
-  __shared__ double red[S::THREADS / 32][4];
+  // per-thread values: convective bound per direction (3), viscous bound per direction (3), bulk-velocity part
+  __shared__ double sred[7][S::THREADS];
   const int e0 = blockIdx.x * EPB;
   const int t = threadIdx.x;
   const int es = t / n3, x = t - es * n3, e = e0 + es;
-  double lc[3] = {0., 0., 0.}, lv = 0., bp = 0.;
-  bool nanFlag = false;
-  if (es < EPB && e < d.nElems) {
+  const bool active = es < EPB && e < d.nElems;
+  double v7[7] = {0., 0., 0., 0., 0., 0., 0.};
+  if (active) {
     double u[5];
 #pragma unroll
     for (int v = 0; v < 5; ++v) u[v] = d.U[((size_t)e * 5 + v) * n3 + x];
+    if (u[0] != u[0]) set_error(d.err, 1);
     const double srho = 1.0 / u[0];
     const double vx = u[1] * srho, vy = u[2] * srho, vz = u[3] * srho;
     const double p = B.kappaM1 * (u[4] - 0.5 * (vx * u[1] + vy * u[2] + vz * u[3]));
-    if (u[0] != u[0]) nanFlag = true;
     const double c = sqrt(B.kappa * p * srho);
     const double sj = d.sJ[(size_t)e * n3 + x];
-    const double vs[3] = {vx * sj, vy * sj, vz * sj};
-    double mvs = 0.;
+    const double lv = d.mu0[d.elemInst[e]] * srho;
 #pragma unroll
     for (int dd = 0; dd < 3; ++dd) {
       const double* mm = d.metr + ((size_t)e * 9 + 3 * dd) * n3 + x;
-      const double q = mm[0] * vs[0] + mm[n3] * vs[1] + mm[2 * n3] * vs[2];
-      lc[dd] = fabs(q) + c * metAdv[((size_t)e * 3 + dd) * n3 + x];
-      mvs += metVisc[((size_t)e * 3 + dd) * n3 + x];
+      const double q = (mm[0] * vx + mm[n3] * vy + mm[2 * n3] * vz) * sj;
+      v7[dd] = fabs(q) + c * metAdv[((size_t)e * 3 + dd) * n3 + x];
+      v7[3 + dd] = lv * metVisc[((size_t)e * 3 + dd) * n3 + x];
     }
-    lv = d.mu0[d.elemInst[e]] * srho;
-    // max over nodes of mu*srho*MetricsVisc(d) per direction is taken below; keep the three separately
-    bp = bulkPart ? vx * wVol[x] / sj : 0.;
-    // pack: lc[0..2] convective, viscous per direction via separate loads in the reduction below
-    (void)mvs;
+    if (bulkPart) v7[6] = vx * wVol[x] / sj;
   }
-  // per-direction maxima over the element's nodes; viscous bounds need per-direction maxima as well
-  double lvd[3] = {0., 0., 0.};
-  if (es < EPB && e < d.nElems) {
 #pragma unroll
-    for (int dd = 0; dd < 3; ++dd) lvd[dd] = lv * metVisc[((size_t)e * 3 + dd) * n3 + x];
-  }
-  if (nanFlag) set_error(d.err, 1);
-  // reduce within the element: EPB elements per block, each of n3 threads; use shared atomics-free
-  // two-level reduction over the element's threads
-  __shared__ double sred[S::THREADS][7];
-  sred[t][0] = lc[0]; sred[t][1] = lc[1]; sred[t][2] = lc[2];
-  sred[t][3] = lvd[0]; sred[t][4] = lvd[1]; sred[t][5] = lvd[2]; sred[t][6] = bp;
+  for (int c = 0; c < 7; ++c) sred[c][t] = v7[c];
   __syncthreads();
-  if (es < EPB && x == 0 && e < d.nElems) {
-    double m[6] = {0., 0., 0., 0., 0., 0.}, bs = 0.;
-    for (int y = 0; y < n3; ++y) {
+  // tree reduction inside each element's thread range [es*n3, es*n3+n3): max for the bounds, sum for the bulk part
+  constexpr int P2 = (n3 <= 1) ? 1 : (1 << (32 - __builtin_clz(n3 - 1)));
+#pragma unroll 1
+  for (int st = P2 / 2; st > 0; st >>= 1) {
+    if (es < EPB && x < st && x + st < n3) {
 #pragma unroll
-      for (int c = 0; c < 6; ++c) m[c] = fmax(m[c], sred[t + y][c]);
-      bs += sred[t + y][6];
+      for (int c = 0; c < 6; ++c) sred[c][t] = fmax(sred[c][t], sred[c][t + st]);
+      sred[6][t] += sred[6][t + st];
     }
-    double dtE = cfl * 2.0 / (m[0] + m[1] + m[2]);
-    const double sv = m[3] + m[4] + m[5];
-    if (sv > 0.) dtE = fmin(dtE, dfl * 4.0 / sv);
-    if (!(dtE == dtE)) set_error(d.err, 2);
-    else atomic_min_pos_double(&d.dt[d.elemInst[e]], dtE);
-    if (bulkPart) bulkPart[e] = bs;
+    __syncthreads();
   }
-  (void)red;
+  if (active && x == 0) {
+    const double dtC = cfl * 2.0 / (sred[0][t] + sred[1][t] + sred[2][t]);
+    const double sv = sred[3][t] + sred[4][t] + sred[5][t];
+    const double dtV = sv > 0. ? dfl * 4.0 / sv : INFINITY;
+    d.dtElem[e] = dtC;
+    d.dtElem[d.nElems + e] = dtV;
+    const double dtE = fmin(dtC, dtV);
+    if (!(dtE == dtE) || !(dtE > 0.)) set_error(d.err, 2);
+    else atomic_min_pos_double(&d.dt[d.elemInst[e]], dtE);
+    if (bulkPart) bulkPart[e] = sred[6][t];
+  }
 }
 
 }  // namespace fg

@@ -13,6 +13,8 @@ struct KernelSet {
   void (*vol_weak)(const Dev&, const Basis&, int, double, double, cudaStream_t) = nullptr;
   void (*vol_split)(const Dev&, const Basis&, int, double, double, cudaStream_t) = nullptr;  // null if unsupported
   void (*dt)(const Dev&, const Basis&, const double*, const double*, double, double, double*, const double*, cudaStream_t) = nullptr;
+  // sets the dynamic shared-memory limits of all kernels; must run before any stream capture
+  void (*prepare)() = nullptr;
 };
 
 // returns the kernel set for n nodes per direction (2..8) and the node type; n == 0 if unsupported

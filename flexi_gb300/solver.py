@@ -95,15 +95,18 @@ class Flexi:
             pass
 
     # ---------------------------------------------------------------- mesh
-    def build_mesh(self, m: BoxMesh):
+    def build_mesh(self, m: BoxMesh, host_only_ok=False):
+        """fg_build_mesh. host_only_ok: accept a failed device upload (no GPU) once the host-side
+        preparation succeeded, so that the set-up can be inspected on a machine without a GPU."""
         nc = np.ascontiguousarray(m.node_coords, np.float64)
         nb = np.ascontiguousarray(m.elem_nb, np.int32)
         bt = np.ascontiguousarray(m.boundary_type, np.int32).reshape(-1)
         rs = np.ascontiguousarray(m.ref_state_prim, np.float64).reshape(-1)
         inst = None if m.elem_inst is None else np.ascontiguousarray(m.elem_inst, np.int32)
-        self._check(self.L.fg_build_mesh(self.h, m.n_elems, m.ngeo, _p(nc), _p(nb), len(bt) // 2, _p(bt) if len(bt) else None,
-                                         len(rs) // 6, _p(rs) if len(rs) else None, _p(inst) if inst is not None else None),
-                    "fg_build_mesh")
+        rc = self.L.fg_build_mesh(self.h, m.n_elems, m.ngeo, _p(nc), _p(nb), len(bt) // 2, _p(bt) if len(bt) else None,
+                                  len(rs) // 6, _p(rs) if len(rs) else None, _p(inst) if inst is not None else None)
+        if not (host_only_ok and rc == 3):  # FG_ERR_CUDA after a complete host-side set-up
+            self._check(rc, "fg_build_mesh")
         self._sizes()
 
     def set_mesh(self, side_to_elem, elem_to_side, bc, boundary_type, ref_state_prim, Mf, Mg, Mh, sJ, NormVec, TangVec1, TangVec2, SurfElem):
@@ -184,6 +187,12 @@ class Flexi:
         self._check(self.L.fg_calc_timestep(self.h, _p(dt), ctypes.byref(err)), "fg_calc_timestep")
         return (float(dt[0]) if len(dt) == 1 else dt), err.value
 
+    def dt_elem(self):
+        """Per-element convective and viscous time-step limits of the last CalcTimeStep."""
+        a, b = np.empty(self.n_elems), np.empty(self.n_elems)
+        self._check(self.L.fg_get_dt_elem(self.h, _p(a), _p(b)), "fg_get_dt_elem")
+        return a, b
+
     def TimeStepByLSERKW2(self, t, dt):
         tt = ctypes.c_double(t)
         self._check(self.L.fg_timestep_lserkw2(self.h, ctypes.byref(tt), float(dt)), "fg_timestep_lserkw2")
@@ -208,6 +217,26 @@ class Flexi:
 
     def launch_count(self):
         return int(self.L.fg_launch_count(self.h))
+
+    def debug_array(self, name):
+        """Copy of a device array in the device layout (inspection only)."""
+        cnt = ctypes.c_longlong(0)
+        self._check(self.L.fg_debug_array(self.h, name.encode(), None, ctypes.byref(cnt)), "fg_debug_array")
+        dtype = np.int32 if name in ("elemInst", "elemSide", "sideElem") else np.float64
+        out = np.empty(cnt.value, dtype)
+        self._check(self.L.fg_debug_array(self.h, name.encode(), _p(out), ctypes.byref(cnt)), "fg_debug_array")
+        return out
+
+    KERNEL_CLASSES = ("prep", "lift", "flux", "vol", "dt", "other")
+
+    def profile(self, on=True):
+        self._check(self.L.fg_profile_enable(self.h, int(on)), "fg_profile_enable")
+
+    def profile_read(self):
+        ms = np.zeros(6)
+        cnt = np.zeros(6, np.int64)
+        self._check(self.L.fg_profile_read(self.h, _p(ms), _p(cnt)), "fg_profile_read")
+        return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(self.KERNEL_CLASSES)}
 
 
 def probe_fp64_tflops():

@@ -132,6 +132,10 @@ int fg_time_derivative(fg_handle* h, double t, double* Ut);
  * per instance; dt[0] is instance 0. errType as in the reference (0 ok, 1 NaN density, 2/3 NaN dt). */
 int fg_calc_timestep(fg_handle* h, double* dt, int* errType);
 
+/* Per-element time-step limits of the last CALCTIMESTEP (calctimestep.f90:dtElem): convective limit
+ * CFL*2/sum(lambda_conv) and viscous limit DFL*4/sum(lambda_visc) (+inf when mu0 = 0), nElems each. */
+int fg_get_dt_elem(fg_handle* h, double* dtConv, double* dtVisc);
+
 /* TimeStepByLSERKW2 (timestep.f90:82) with CarpenterRK4-5 (timedisc_vars.f90:199-214): advances the
  * state by dt (all instances use the same dt here); t is advanced by dt. Includes CalcForcing
  * (testcase/channel/testcase.f90:262) when the channel body force is active. */
@@ -152,6 +156,18 @@ int fg_get_stream(fg_handle* h, void** stream);
 
 /* Number of kernel launches issued by the last fg_run / fg_timestep_lserkw2 / fg_time_derivative call. */
 long long fg_launch_count(const fg_handle* h);
+
+/* Copies one of the handle's device arrays to host memory for inspection, in the device layout:
+ * "U","Ut","prim","grad","metr","sJ","metAdv","metVisc","mu0","dt","dtElem" (double), "elemInst",
+ * "elemSide","sideElem" (int). *count receives the number of elements; out may be NULL to query it. */
+int fg_debug_array(fg_handle* h, const char* name, void* out, long long* count);
+
+/* Per-kernel CUDA-event timing of later launches on the handle's stream; while enabled, fg_run issues
+ * the kernels directly instead of replaying the captured graph. fg_profile_read returns, per kernel
+ * class (0 prep, 1 lift, 2 flux, 3 volume+update, 4 time step, 5 other), the summed milliseconds and
+ * the launch counts since the previous read, and resets them. */
+int fg_profile_enable(fg_handle* h, int on);
+int fg_profile_read(fg_handle* h, double* ms, long long* counts);
 
 /* FP64 FMA throughput probe (TFLOP/s, 2 flop per FMA) of the current device, used for the roofline. */
 int fg_probe_fp64(double* tflops);

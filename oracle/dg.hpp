@@ -748,6 +748,8 @@ struct DG {
     const size_t nv3 = (size_t)n * n * n;
     if (C.splitDG != SPLIT_NONE && C.nodeType != NT_GL)
       throw std::runtime_error("split form with Gauss nodes needs the split-Gauss surface correction (not restated)");
+    long long& fc = flop_counter();
+    phase[0] = fc;
 #pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
     for (int e = 0; e < nE; ++e) for (size_t x = 0; x < nv3; ++x) cons_to_prim(&U[((size_t)e * nv3 + x) * 5], &UPrim[((size_t)e * nv3 + x) * 6]);
     prolong_to_face<5>(U, U_master, U_slave);
@@ -756,9 +758,13 @@ struct DG {
       cons_to_prim(&U_master[si(0, p, q, s, 5)], &UPrim_master[si(0, p, q, s, 6)]);
       if (s >= M.nBCSides) cons_to_prim(&U_slave[si(0, p, q, s, 5)], &UPrim_slave[si(0, p, q, s, 6)]);
     }
+    phase[1] = fc;
     lifting();
+    phase[2] = fc;
     vol_int();
+    phase[3] = fc;
     fill_flux(t);
+    phase[4] = fc;
     surf_int<5>(Flux_master, Flux_slave, Ut, R(-1.));
     // Ut = -Ut ; TestcaseSource (channel) ; ApplyJacobianCons
 #pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
@@ -772,7 +778,12 @@ struct DG {
       }
       for (int v = 0; v < 5; ++v) ut[v] = ut[v] * R(sj);
     }
+    phase[5] = fc;
   }
+  // flop counter at the phase boundaries of the last time_derivative (flop-counting scalar only):
+  // [0] start, [1] after ConsToPrim+ProlongToFace, [2] after lifting, [3] after the volume integral,
+  // [4] after FillFlux, [5] after surface integral, sign, source and Jacobian
+  long long phase[6] = {0, 0, 0, 0, 0, 0};
 
   // channel testcase.f90:CalcForcing -- bulk velocity (done once per time step before the RK stages)
   void calc_forcing() {

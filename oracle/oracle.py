@@ -53,6 +53,7 @@ def lib():
         _lib.orc_get_gradients.argtypes = [P, ctypes.c_int, P]
         _lib.orc_flops_per_dof_stage.argtypes = [P]
         _lib.orc_flops_per_dof_stage.restype = ctypes.c_double
+        _lib.orc_flops_breakdown.argtypes = [P, P]
         _lib.orc_set_threads.argtypes = [ctypes.c_int]
         _lib.orc_max_threads.restype = ctypes.c_int
         _lib.orc_nodes_and_weights.argtypes = [ctypes.c_int, ctypes.c_int, P, P, P]
@@ -180,6 +181,13 @@ class Oracle:
 
     def flops_per_dof_stage(self):
         return lib().orc_flops_per_dof_stage(self.h)
+
+    def flops_breakdown(self):
+        """Algorithmic flops per DOF of one LSERK stage by kernel class: prep, lift, flux, vol (incl. the
+        register update), total."""
+        out = np.zeros(5)
+        lib().orc_flops_breakdown(self.h, _p(out))
+        return dict(zip(("prep", "lift", "flux", "vol", "total"), out.tolist()))
 
 
 def set_threads(n):

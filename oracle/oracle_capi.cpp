@@ -136,6 +136,25 @@ double orc_flops_per_dof_stage(void* hp) {
   return (double)rhs / ndof + 4. * 5.;
 }
 
+// algorithmic flops per DOF of one stage, split like the GPU kernel classes:
+// out[0] ConsToPrim+ProlongToFace(+face ConsToPrim), out[1] lifting, out[2] FillFlux (Riemann+viscous+BC),
+// out[3] volume integral + surface integral + sign/source/Jacobian + LSERK register update, out[4] total
+void orc_flops_breakdown(void* hp, double* out) {
+  auto* h = (OrcHandle*)hp;
+  DG<FD> f;
+  f.init(h->dg.C, h->mi);
+  for (size_t x = 0; x < f.U.size(); ++x) f.U[x] = FD(h->dg.U[x]);
+  f.BulkVel = h->dg.BulkVel;
+  f.time_derivative(0.);
+  const double ndof = (double)f.nE * f.n * f.n * f.n;
+  const long long* p = f.phase;
+  out[0] = (p[1] - p[0]) / ndof;
+  out[1] = (p[2] - p[1]) / ndof;
+  out[2] = (p[4] - p[3]) / ndof;
+  out[3] = ((p[3] - p[2]) + (p[5] - p[4])) / ndof + 4. * 5.;
+  out[4] = out[0] + out[1] + out[2] + out[3];
+}
+
 // --------------------------------------------------------------------------------------------
 // unit-test level restatements (unitTests/ProlongToFace.f90, unitTests/SurfInt.f90)
 // --------------------------------------------------------------------------------------------

@@ -1,0 +1,96 @@
+"""CPU tests of the product library's host side: C ABI exports, configuration, ini parsing, and the
+mesh preparation (sides, flips, curl-form metrics, surface metrics) against the oracle's restatement
+of FLEXI's InitMesh/CalcMetrics. No GPU work is issued here."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from flexi_gb300 import _lib, mesh as fmesh
+from flexi_gb300.solver import Flexi, FlexiError, make_config, config_from_ini, config_dict
+from oracle import oracle as orc
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from flexi_gb300 import build
+    build.build()
+    return _lib.load()
+
+
+def test_exports_every_declared_symbol(lib):
+    header = open(os.path.join(ROOT, "include", "flexi_gpu.h")).read()
+    declared = set(re.findall(r"^\s*(?:int|const char\*|long long)\s+(fg_\w+)\s*\(", header, re.M))
+    assert len(declared) >= 20
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert declared == set(_lib.EXPORTS)
+
+
+def test_config_defaults_and_validation(lib):
+    c = make_config()
+    d = config_dict(c)
+    assert d["Riemann"] == 33 and d["SplitDG"] == 4 and d["Lifting"] == 1 and d["kappa"] == 1.4 and d["R"] == 287.058
+    assert d["CFLScale"] == 0.9 and d["etaBR2"] == 2.0 and d["Pr"] == 0.72
+    with pytest.raises(FlexiError):
+        Flexi(make_config(N=12))
+    with pytest.raises(FlexiError):
+        Flexi(make_config(N=5, NodeType="gauss", SplitDG="pi"))  # split form needs Gauss-Lobatto nodes
+    with pytest.raises(FlexiError):
+        Flexi(make_config(N=3, doConservativeLifting=1))
+
+
+def test_ini_parser(lib):
+    # keys as written in regressioncheck/checks/tgv/split/parameter.ini
+    text = """
+    N             = 7 ! Polynomial degree
+    Riemann               =  RoeEntropyFix ! Riemann solver
+    SplitDG               = PI
+    Mu0           = 6.25E-04    ! viscosity set to 1/Re
+    R             = 71.42857
+    CFLscale   = 0.8  ! Scaling of theoretical CFL number
+    DFLscale   = 0.8
+    NodeType = Gauss-Lobatto
+    Lifting = br2
+    etaBR2 = 3.
+    """
+    d = config_dict(config_from_ini(text))
+    assert d["N"] == 7 and d["Riemann"] == 33 and d["SplitDG"] == 4 and d["mu0"] == 6.25e-4 and d["R"] == 71.42857
+    assert d["CFLScale"] == 0.8 and d["DFLScale"] == 0.8 and d["NodeType"] == 2 and d["Lifting"] == 2 and d["etaBR2"] == 3.0
+
+
+def _oracle_cfg(N, node_type):
+    return dict(N=N, nodeType=node_type, riemann=33, riemannBC=-1, lifting=1, weakLifting=0, consLifting=0, splitDG=-1, etaBR2=2.0,
+                etaBR2_wall=-1.0, kappa=1.4, R=71.42857, Pr=0.72, mu0=1e-3, CFLScale=0.9, DFLScale=0.9, doTCSource=0, dpdx=-1.0)
+
+
+MESHES = {
+    "cartesian": lambda: fmesh.tgv_box(3, ngeo=1),
+    "curved": lambda: fmesh.tgv_box(3, ngeo=3, perturb=0.3, seed=1),
+    "channel": lambda: fmesh.channel_box((3, 4, 2), beta=1.5, ngeo=2),
+}
+
+
+@pytest.mark.parametrize("mesh_name", list(MESHES))
+@pytest.mark.parametrize("N,node_type", [(3, 1), (4, 2), (7, 2)])
+def test_mesh_preparation_matches_oracle(lib, mesh_name, N, node_type):
+    m = MESHES[mesh_name]()
+    o = orc.Oracle(_oracle_cfg(N, node_type), m)
+    f = Flexi(make_config(N=N, NodeType=node_type, SplitDG=-1))
+    f.build_mesh(m, host_only_ok=True)
+    assert (f.n_elems, f.n_sides, f.n_bc_sides) == (o.n_elems, o.n_sides, o.n_bc_sides)
+    assert np.array_equal(f.side_to_elem(), o.mesh_iarray("SideToElem"))
+    for name in ("Mf", "Mg", "Mh"):
+        a, b = f.mesh_array(name), o.mesh_array(name)
+        assert np.abs(a - b).max() <= 1e-13 * max(1.0, np.abs(b).max()), name
+    assert np.abs(f.mesh_array("sJ") / o.mesh_array("sJ") - 1).max() < 1e-13
+    np.testing.assert_allclose(f.elem_xgp(), o.mesh_array("Elem_xGP"), rtol=0, atol=1e-13)
+    # face metrics: master sides are stored by both in the same side numbering
+    for name in ("NormVec", "TangVec1", "TangVec2", "SurfElem"):
+        a, b = f.mesh_array(name), o.mesh_array(name)
+        assert np.abs(a - b).max() <= 1e-13 * max(1.0, np.abs(b).max()), name
+    f.close()
