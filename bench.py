@@ -44,6 +44,7 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--elems", type=int, default=32, help="elements per direction")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline leg (profiling runs)")
     return p.parse_args()
 
 
@@ -292,6 +293,8 @@ def run_gb300(args):
                 "frac_hbm": (value / ws * BYTES_ALG_PER_DOF_STAGE / 1e9 / peaks["hbm_gbs"]) if peaks.get("hbm_gbs") else None,
                 "kernel_ms_per_step": {k: prof[k][0] / args.steps for k in prof}}
     try:
+        if args.no_cpu_baseline:
+            raise RuntimeError("skipped (--no-cpu-baseline)")
         cpu_val, cores, sample = cpu_baseline_sample()
         cpu = {"value": cpu_val, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
     except Exception as ex:  # reported, never substituted for the GPU path
