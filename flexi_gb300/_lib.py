@@ -18,7 +18,15 @@ class FgConfig(ctypes.Structure):
 EXPORTS = ["fg_config_default", "fg_config_from_ini", "fg_create", "fg_destroy", "fg_last_error", "fg_build_mesh", "fg_set_mesh",
            "fg_set_instance_mu0", "fg_get_elem_xgp", "fg_get_sizes", "fg_get_mesh_array", "fg_get_side_to_elem", "fg_set_state",
            "fg_get_state", "fg_state_device_ptr", "fg_time_derivative", "fg_calc_timestep", "fg_get_dt_elem", "fg_timestep_lserkw2", "fg_run",
-           "fg_get_gradients", "fg_get_stream", "fg_launch_count", "fg_debug_array", "fg_profile_enable", "fg_profile_read", "fg_probe_fp64"]
+           "fg_get_gradients", "fg_get_stream", "fg_launch_count", "fg_debug_array", "fg_profile_enable", "fg_profile_read", "fg_probe_fp64",
+           "fg_time_derivative_noalloc"]
+
+
+class FgDeviceMesh(ctypes.Structure):
+    """fg_device_mesh: caller-owned device arrays for fg_time_derivative_noalloc (pointers as integers)."""
+    _fields_ = [("nElems", ctypes.c_int), ("nSides", ctypes.c_int), ("nBCSides", ctypes.c_int),
+                ("elemSide", ctypes.c_void_p), ("sideElem", ctypes.c_void_p), ("metr", ctypes.c_void_p), ("sJ", ctypes.c_void_p),
+                ("geo", ctypes.c_void_p), ("bcType", ctypes.c_void_p), ("bcTwall", ctypes.c_void_p)]
 
 
 def load(path=None):
@@ -61,5 +69,6 @@ def load(path=None):
     L.fg_profile_enable.argtypes = [P, I]
     L.fg_profile_read.argtypes = [P, P, P]
     L.fg_probe_fp64.argtypes = [ctypes.POINTER(D)]
+    L.fg_time_derivative_noalloc.argtypes = [ctypes.POINTER(FgConfig), ctypes.POINTER(FgDeviceMesh), P, P, P]
     _lib = L
     return L

@@ -384,6 +384,10 @@ std::string trim(const std::string& s) {
 
 }  // namespace
 
+namespace fg {
+void set_error_without_handle(const char* msg) { g_err = msg; }
+}  // namespace fg
+
 extern "C" {
 
 int fg_config_default(fg_config* c) {

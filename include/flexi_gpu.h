@@ -172,6 +172,40 @@ int fg_profile_read(fg_handle* h, double* ms, long long* counts);
 /* FP64 FMA throughput probe (TFLOP/s, 2 flop per FMA) of the current device, used for the roofline. */
 int fg_probe_fp64(double* tflops);
 
+/* ---- Allocation-free right-hand side (no counterpart in the reference) ----------------------------
+ * For callers that cannot allocate device memory: host codes whose device memory all comes from their
+ * own pool or caching allocator, and time loops that must not allocate once they run. Everything is
+ * caller-owned DEVICE memory in the library's device layouts (n = N+1 nodes per direction, n2 = n*n,
+ * n3 = n*n*n); the layouts are those fg_debug_array returns for "U", "metr", "sJ", "elemSide",
+ * "sideElem". BC sides are sides 0..nBCSides-1, as in FLEXI. */
+typedef struct fg_device_mesh {
+  int nElems, nSides, nBCSides;
+  const int* elemSide;    /* [nElems][6]: 8*sideID + flip per local side ZETA-,ETA-,XI+,ETA+,XI-,ZETA+ (flip 0: master) */
+  const int* sideElem;    /* [nSides][4]: master elem, master local side, slave elem (-1 on BC sides), 8*slave local side + flip */
+  const double* metr;     /* [nElems][9][n3]: Metrics_fTilde(1:3), Metrics_gTilde(1:3), Metrics_hTilde(1:3) */
+  const double* sJ;       /* [nElems][n3]: 1/J */
+  const double* geo;      /* [nSides][10][n2]: NormVec(3), TangVec1(3), TangVec2(3), SurfElem */
+  const int* bcType;      /* [nBCSides]: FLEXI BC type of each BC side (3 adiabatic, 4 isothermal wall) */
+  const double* bcTwall;  /* [nBCSides]: wall temperature of each BC side (isothermal walls) */
+} fg_device_mesh;
+
+/* Largest scratch the allocation-free call can use: 64 MiB of static device memory, held by every
+ * device that loads the library (e.g. 343 elements at N=7, ~2500 elements at N=3). */
+#define FG_NOALLOC_SCRATCH_BYTES (64ull << 20)
+
+/* Ut = DGTimeDerivative_weakForm(U) for one instance with viscosity cfg->mu0, like fg_time_derivative
+ * but handle-free and allocation-free: U and Ut are DEVICE arrays [nElems][5][n3], the launches are
+ * asynchronous on `stream` (cudaStream_t as void*, NULL = legacy default stream). All intermediate
+ * arrays live in one static __device__ scratch array of FG_NOALLOC_SCRATCH_BYTES; the call clears what
+ * must start at zero (sticky error word, instance ids) itself on the stream. The first call on each
+ * device, with that device current, looks up the scratch address and sets the kernels' shared-memory
+ * limits: make it before any stream capture. Calls that overlap on the GPU (other streams, or host
+ * threads without ordering) race on the shared scratch. Meshes needing more scratch, and configurations
+ * the kernels do not cover (N > 7, weak or conservative lifting, body force, split form off
+ * Gauss-Lobatto nodes or with N not in {1,3,7}), are rejected before any launch, with the reason in
+ * fg_last_error(NULL). No cudaMalloc, cudaFree or other device allocation is made. */
+int fg_time_derivative_noalloc(const fg_config* cfg, const fg_device_mesh* mesh, const double* U, double* Ut, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
