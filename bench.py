@@ -285,7 +285,7 @@ def run_gb300(args):
     roofline = {"bound": "fp64", "kernel": {"vol": "k_vol_split<8>", "lift": "k_lift<8,GL>", "flux": "k_flux<8>", "prep": "k_prep<8,GL>"}[dom],
                 "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved / fp64_peak,
                 "peak_source": "own DFMA probe (fg_probe_fp64), MEASURED_PEAKS.json has no FP64 figure",
-                "traffic": (traffic * dof / 1e6 if traffic is not None else None),
+                "traffic": (traffic * dof if traffic is not None else None),
                 "traffic_unit": "bytes per launch (ncu dram read+write, scaled per DOF)" if traffic is not None else None,
                 "algorithmic_flops_per_dof": FLOPS_PER_DOF_STAGE[dom], "avg_launch_ms": avg_ms,
                 "hbm_alg_gbs": value / ws * BYTES_ALG_PER_DOF_STAGE / 1e9,

@@ -47,6 +47,7 @@ struct Dev {
   double* prim;    // [e][VP_NF][n3]
   double* grad;    // [e][12][n3]: index 4*dir + var, var = (u,v,w,T)
   double* metr;    // [e][9][n3]: Metrics_fTilde(3), Metrics_gTilde(3), Metrics_hTilde(3)
+  double* metrJ;   // [e][9][n3]: metr times sJ (null: the kernels form the products)
   double* sJ;      // [e][n3]
   int* elemSide;   // [e][6]: 8*sideID + flip (flip 0 => this element is the master)
   int* elemInst;   // [e]

@@ -256,6 +256,13 @@ int upload_mesh(fg_handle* h) {
   if ((r = dalloc(h, d.grad, (size_t)nE * 12 * n3))) return r;
   if ((r = upload(h, d.metr, M.metr))) return r;
   if ((r = upload(h, d.sJ, M.sJ))) return r;
+  {
+    std::vector<double> mJ(M.metr.size());
+    for (size_t e = 0; e < (size_t)nE; ++e)
+      for (int c = 0; c < 9; ++c)
+        for (int x = 0; x < n3; ++x) mJ[(e * 9 + c) * n3 + x] = M.metr[(e * 9 + c) * n3 + x] * M.sJ[e * n3 + x];
+    if ((r = upload(h, d.metrJ, mJ))) return r;
+  }
   if ((r = upload(h, d.elemSide, M.elemSide))) return r;
   if ((r = upload(h, d.elemInst, M.elemInst))) return r;
   if ((r = dalloc(h, d.faceM, (size_t)nS * FS_NF * n2))) return r;

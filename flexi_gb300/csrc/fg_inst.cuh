@@ -14,7 +14,7 @@ struct Inst {
     return sizeof(double) * (SBasis<n>::SIZE + S::EPB * (4 * S::n3 + 6 * S::n2 * 7 + 12 * S::n3 + S::n3));
   }
   static size_t smem_weak() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * (15 * S::n3 + 6 * S::n2 * 5)); }
-  static size_t smem_split() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * (32 * S::n3 + 6 * S::n2 * 5)); }
+  static size_t smem_split() { return sizeof(double) * (SBasis<n>::SIZE + 2 * S::n2 + S::EPB * (20 * S::n3 + 6 * S::n2 * 5)); }
   template <class K>
   static void set_smem(K kern, size_t bytes) {
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);

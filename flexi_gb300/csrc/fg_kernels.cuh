@@ -125,13 +125,73 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_prep(Dev d, Basis B) {
   }
 }
 
+// ProlongToFaceLifting of the gradients in sG (+ BR2: eta * lifting contribution of this face,
+// lifting_br2.t90:Lifting_SurfInt_BR2) for the six faces of the CTA's elements
+template <int n, bool GL>
+__device__ __forceinline__ void lift_prolong_faces(const Dev& d, const Basis& B, const SBasis<n>& Bs, const double* sG, const double* sF,
+                                                   const double* sN, const double* sJs, int e0, bool br2) {
+  constexpr int n2 = n * n, n3 = n2 * n, EPB = Shape<n>::EPB, N = n - 1;
+  for (int t = threadIdx.x; t < EPB * 6 * n2; t += blockDim.x) {
+    const int es = t / (6 * n2), r = t - es * 6 * n2, lsi = r / n2, pq = r - lsi * n2;
+    const int e = e0 + es;
+    if (e >= d.nElems) continue;
+    const int ls = lsi + 1, p = pq % n, q = pq / n;
+    const int code = d.elemSide[e * 6 + lsi], s = code >> 3, flip = code & 7;
+    int a, b;
+    side_to_vol2(N, p, q, flip, ls, a, b);
+    const bool minus = side_is_minus(ls);
+    double gf[12];
+    if (GL) {
+      const int x = face_node(ls, a, b, minus ? 0 : N, n);
+#pragma unroll
+      for (int c = 0; c < 12; ++c) gf[c] = sG[(es * 12 + c) * n3 + x];
+    } else {
+#pragma unroll
+      for (int c = 0; c < 12; ++c) gf[c] = 0.;
+#pragma unroll
+      for (int l = 0; l < n; ++l) {
+        const int x = face_node(ls, a, b, l, n);
+        const double L = minus ? Bs.Lm(l) : Bs.Lp(l);
+#pragma unroll
+        for (int c = 0; c < 12; ++c) gf[c] = fma(sG[(es * 12 + c) * n3 + x], L, gf[c]);
+      }
+    }
+    if (br2) {
+      double eta = B.etaBR2;
+      if (s < d.nBCSides && (d.bcType[s] == 3 || d.bcType[s] == 4)) eta = B.etaBR2_wall;
+      // sum_l L_Minus(l) * L_HatMinus(l) * sJ(node at distance l from this face)
+      double wsum = 0.;
+      if (GL) {
+        wsum = Bs.Lm(0) * Bs.LhM(0) * sJs[es * n3 + face_node(ls, a, b, minus ? 0 : N, n)];
+      } else {
+#pragma unroll
+        for (int l = 0; l < n; ++l) wsum = fma(Bs.Lm(l) * Bs.LhM(l), sJs[es * n3 + face_node(ls, a, b, minus ? l : N - l, n)], wsum);
+      }
+      const int o = (es * 6 + lsi) * n2 + a + n * b;
+      const double ew = eta * wsum;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const double f = sF[o * 4 + v] * ew;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) gf[4 * c + v] = fma(f, sN[o * 3 + c], gf[4 * c + v]);
+      }
+    }
+    double* dst = (flip == 0 ? d.gradM : d.gradS) + (size_t)s * 12 * n2 + pq;
+#pragma unroll
+    for (int c = 0; c < 12; ++c) dst[c * n2] = gf[c];
+  }
+}
+
 // =====================================================================================================
 // k_lift: lifting_br1.t90 / lifting_br2.t90 (strong or weak BR1, BR2), non-conservative volume part
 // (lifting_volint.t90:Lifting_VolInt_Nonconservative), surface part, ApplyJacobianLifting,
-// ProlongToFaceLifting.
+// ProlongToFaceLifting. The volume part uses the metrics pre-multiplied by sJ when the mesh provides
+// them (Dev::metrJ), else forms the products itself. On Gauss-Lobatto nodes the surface part reaches
+// only the face nodes: it is added face-parallel, one direction (two opposite faces, disjoint node
+// sets) at a time, so that no warp runs it for interior nodes.
 // =====================================================================================================
 template <int n, bool GL>
-__global__ void __launch_bounds__(Shape<n>::THREADS) k_lift(Dev d, Basis B) {
+__global__ void __launch_bounds__(Shape<n>::THREADS, (n == 8 && GL ? 2 : 1)) k_lift(Dev d, Basis B) {
   using S = Shape<n>;
   constexpr int n2 = S::n2, n3 = S::n3, EPB = S::EPB, N = S::N;
   extern __shared__ double smem[];
@@ -139,7 +199,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_lift(Dev d, Basis B) {
   double* sL = smem + SBasis<n>::SIZE;   // [EPB][4][n3] lifting variables u,v,w,T
   double* sF = sL + EPB * 4 * n3;        // [EPB][6][n2][4] surface lifting flux (times SurfElem), local face order
   double* sN = sF + EPB * 6 * n2 * 4;    // [EPB][6][n2][3] face normal of the side point mapped to local face order
-  double* sG = sN + EPB * 6 * n2 * 3;    // [EPB][12][n3] gradients for the prolongation
+  double* sG = sN + EPB * 6 * n2 * 3;    // [EPB][12][n3] gradients
   double* sJs = sG + EPB * 12 * n3;      // [EPB][n3]
   load_basis_smem<n>(B, sD);
   SBasis<n> Bs{sD};
@@ -195,7 +255,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_lift(Dev d, Basis B) {
     for (int c = 0; c < 3; ++c) sN[o * 3 + c] = gm[(FG_NX + c) * n2];
   }
   __syncthreads();
-  // volume gradient: d/dxi via D_T sweeps, contravariant -> Cartesian with the metrics
+  // volume gradient: d/dxi via D_T sweeps, contravariant -> Cartesian with the metrics times sJ
   for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
     const int es = t / n3, x = t - es * n3, e = e0 + es;
     if (e >= d.nElems) continue;
@@ -214,106 +274,94 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_lift(Dev d, Basis B) {
         gz[v] = fma(dzeta, L[v * n3 + i + n * (j + n * l)], gz[v]);
       }
     }
-    double m[9];
+    double mJ[9];
+    if (d.metrJ) {
 #pragma unroll
-    for (int c = 0; c < 9; ++c) m[c] = d.metr[((size_t)e * 9 + c) * n3 + x];
+      for (int c = 0; c < 9; ++c) mJ[c] = d.metrJ[((size_t)e * 9 + c) * n3 + x];
+    } else {
+      const double sj = sJs[es * n3 + x];
+#pragma unroll
+      for (int c = 0; c < 9; ++c) mJ[c] = d.metr[((size_t)e * 9 + c) * n3 + x] * sj;
+    }
     double g[12];
 #pragma unroll
     for (int dd = 0; dd < 3; ++dd)
 #pragma unroll
-      for (int v = 0; v < 4; ++v) g[4 * dd + v] = m[dd] * gx[v] + m[3 + dd] * ge[v] + m[6 + dd] * gz[v];
-    const double sj = sJs[es * n3 + x];
-    // surface contributions along the three normal lines through this node (DoSurfIntLifting)
-    double sg[12];
+      for (int v = 0; v < 4; ++v) g[4 * dd + v] = mJ[dd] * gx[v] + mJ[3 + dd] * ge[v] + mJ[6 + dd] * gz[v];
+    if constexpr (GL) {
 #pragma unroll
-    for (int c = 0; c < 12; ++c) sg[c] = 0.;
-    const int idx3[3] = {i, j, k};
+      for (int c = 0; c < 12; ++c) sG[(es * 12 + c) * n3 + x] = g[c];
+    } else {
+      // Gauss nodes: the surface part reaches every node of the normal lines (DoSurfIntLifting)
+      const double sj = sJs[es * n3 + x];
+      double sg[12];
 #pragma unroll
-    for (int dir = 0; dir < 3; ++dir) {
-      const int lsM = dir == 0 ? XI_MINUS : (dir == 1 ? ETA_MINUS : ZETA_MINUS);
-      const int lsP = dir == 0 ? XI_PLUS : (dir == 1 ? ETA_PLUS : ZETA_PLUS);
-      const int a = dir == 0 ? j : i, b = dir == 2 ? j : k;
-      const int l = idx3[dir];
-      double wM, wP;
-      if (GL) { wM = (l == 0) ? Bs.LhM(0) : 0.; wP = (l == N) ? Bs.LhP(N) : 0.; }
-      else { wM = Bs.LhM(l); wP = Bs.LhP(l); }
-      if (wM != 0.) {
-        const int o = (es * 6 + lsM - 1) * n2 + a + n * b;
+      for (int c = 0; c < 12; ++c) sg[c] = 0.;
+      const int idx3[3] = {i, j, k};
 #pragma unroll
-        for (int v = 0; v < 4; ++v) {
-          const double f = sF[o * 4 + v] * wM;
-#pragma unroll
-          for (int c = 0; c < 3; ++c) sg[4 * c + v] = fma(f, sN[o * 3 + c], sg[4 * c + v]);
-        }
-      }
-      if (wP != 0.) {
-        const int o = (es * 6 + lsP - 1) * n2 + a + n * b;
+      for (int dir = 0; dir < 3; ++dir) {
+        const int lsM = dir == 0 ? XI_MINUS : (dir == 1 ? ETA_MINUS : ZETA_MINUS);
+        const int lsP = dir == 0 ? XI_PLUS : (dir == 1 ? ETA_PLUS : ZETA_PLUS);
+        const int a = dir == 0 ? j : i, b = dir == 2 ? j : k;
+        const int l = idx3[dir];
+        const double wM = Bs.LhM(l), wP = Bs.LhP(l);
+        const int oM = (es * 6 + lsM - 1) * n2 + a + n * b, oP = (es * 6 + lsP - 1) * n2 + a + n * b;
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
-          const double f = sF[o * 4 + v] * wP;
+          const double fM = sF[oM * 4 + v] * wM, fP = sF[oP * 4 + v] * wP;
 #pragma unroll
-          for (int c = 0; c < 3; ++c) sg[4 * c + v] = fma(f, sN[o * 3 + c], sg[4 * c + v]);
+          for (int c = 0; c < 3; ++c) sg[4 * c + v] = fma(fP, sN[oP * 3 + c], fma(fM, sN[oM * 3 + c], sg[4 * c + v]));
         }
       }
-    }
-    // BR1: face gradients are prolonged from the full gradient; BR2: from the volume part only
+      // BR1: face gradients are prolonged from the full gradient; BR2: from the volume part only
 #pragma unroll
-    for (int c = 0; c < 12; ++c) {
-      const double full = (g[c] + sg[c]) * sj;
-      d.grad[((size_t)e * 12 + c) * n3 + x] = full;
-      sG[(es * 12 + c) * n3 + x] = br2 ? g[c] * sj : full;
+      for (int c = 0; c < 12; ++c) {
+        const double full = fma(sg[c], sj, g[c]);
+        d.grad[((size_t)e * 12 + c) * n3 + x] = full;
+        sG[(es * 12 + c) * n3 + x] = br2 ? g[c] : full;
+      }
     }
   }
   __syncthreads();
-  // ProlongToFaceLifting (+ BR2: eta * lifting contribution of this face, lifting_br2.t90:Lifting_SurfInt_BR2)
-  for (int t = threadIdx.x; t < EPB * 6 * n2; t += blockDim.x) {
-    const int es = t / (6 * n2), r = t - es * 6 * n2, lsi = r / n2, pq = r - lsi * n2;
-    const int e = e0 + es;
-    if (e >= d.nElems) continue;
-    const int ls = lsi + 1, p = pq % n, q = pq / n;
-    const int code = d.elemSide[e * 6 + lsi], s = code >> 3, flip = code & 7;
-    int a, b;
-    side_to_vol2(N, p, q, flip, ls, a, b);
-    const bool minus = side_is_minus(ls);
-    double gf[12];
-    if (GL) {
-      const int x = face_node(ls, a, b, minus ? 0 : N, n);
-#pragma unroll
-      for (int c = 0; c < 12; ++c) gf[c] = sG[(es * 12 + c) * n3 + x];
-    } else {
-#pragma unroll
-      for (int c = 0; c < 12; ++c) gf[c] = 0.;
-#pragma unroll
-      for (int l = 0; l < n; ++l) {
-        const int x = face_node(ls, a, b, l, n);
-        const double L = minus ? Bs.Lm(l) : Bs.Lp(l);
-#pragma unroll
-        for (int c = 0; c < 12; ++c) gf[c] = fma(sG[(es * 12 + c) * n3 + x], L, gf[c]);
-      }
-    }
+  if constexpr (GL) {
+    // BR2 prolongs the volume part, before the surface part is added
     if (br2) {
-      double eta = B.etaBR2;
-      if (s < d.nBCSides && (d.bcType[s] == 3 || d.bcType[s] == 4)) eta = B.etaBR2_wall;
-      // sum_l L_Minus(l) * L_HatMinus(l) * sJ(node at distance l from this face)
-      double wsum = 0.;
-      if (GL) {
-        wsum = Bs.Lm(0) * Bs.LhM(0) * sJs[es * n3 + face_node(ls, a, b, minus ? 0 : N, n)];
-      } else {
-#pragma unroll
-        for (int l = 0; l < n; ++l) wsum = fma(Bs.Lm(l) * Bs.LhM(l), sJs[es * n3 + face_node(ls, a, b, minus ? l : N - l, n)], wsum);
-      }
-      const int o = (es * 6 + lsi) * n2 + a + n * b;
-      const double ew = eta * wsum;
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        const double f = sF[o * 4 + v] * ew;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) gf[4 * c + v] = fma(f, sN[o * 3 + c], gf[4 * c + v]);
-      }
+      lift_prolong_faces<n, GL>(d, B, Bs, sG, sF, sN, sJs, e0, true);
+      __syncthreads();
     }
-    double* dst = (flip == 0 ? d.gradM : d.gradS) + (size_t)s * 12 * n2 + pq;
+    // surface part (DoSurfIntLifting) on the face nodes l = 0 and l = N of one direction at a time
+#pragma unroll 1
+    for (int dir = 0; dir < 3; ++dir) {
+      for (int t = threadIdx.x; t < EPB * 2 * n2; t += blockDim.x) {
+        const int es = t / (2 * n2), r = t - es * 2 * n2, plus = r / n2, ab = r - plus * n2;
+        const int e = e0 + es;
+        if (e >= d.nElems) continue;
+        const int a = ab % n, b = ab / n, l = plus ? N : 0;
+        const int ls = plus ? (dir == 0 ? XI_PLUS : (dir == 1 ? ETA_PLUS : ZETA_PLUS))
+                            : (dir == 0 ? XI_MINUS : (dir == 1 ? ETA_MINUS : ZETA_MINUS));
+        const int x = dir == 0 ? l + n * (a + n * b) : (dir == 1 ? a + n * (l + n * b) : a + n * (b + n * l));
+        const double w = (plus ? Bs.LhP(N) : Bs.LhM(0)) * sJs[es * n3 + x];
+        const int o = (es * 6 + ls - 1) * n2 + a + n * b;
+        double* G = sG + es * 12 * n3 + x;
 #pragma unroll
-    for (int c = 0; c < 12; ++c) dst[c * n2] = gf[c];
+        for (int v = 0; v < 4; ++v) {
+          const double f = sF[o * 4 + v] * w;
+#pragma unroll
+          for (int c = 0; c < 3; ++c) G[(4 * c + v) * n3] = fma(f, sN[o * 3 + c], G[(4 * c + v) * n3]);
+        }
+      }
+      __syncthreads();
+    }
+    // BR1 prolongs the full gradient
+    if (!br2) lift_prolong_faces<n, GL>(d, B, Bs, sG, sF, sN, sJs, e0, false);
+    for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
+      const int es = t / n3, x = t - es * n3, e = e0 + es;
+      if (e >= d.nElems) continue;
+#pragma unroll
+      for (int c = 0; c < 12; ++c) d.grad[((size_t)e * 12 + c) * n3 + x] = sG[(es * 12 + c) * n3 + x];
+    }
+  } else {
+    lift_prolong_faces<n, GL>(d, B, Bs, sG, sF, sN, sJs, e0, br2);
   }
 }
 
@@ -549,71 +597,60 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_weak(Dev d, Basis B, 
 }
 
 // =====================================================================================================
-// k_vol_split: volint.f90:VolInt_splitForm with SplitVolumeFluxPI / SD (Gauss-Lobatto nodes, 8 nodes
-// per line handled by an 8-lane segment of a warp), viscous part in weak form, surface integral,
+// k_vol_split: volint.f90:VolInt_splitForm with SplitVolumeFluxPI / SD (Gauss-Lobatto nodes, n nodes
+// per line handled by an n-lane segment of a warp), viscous part in weak form, surface integral,
 // Jacobian, LSERK update. Each two-point flux of a line is evaluated once: lane a evaluates the pair
-// (a, a+dd mod n) for dd = 1..n/2-1, keeps its own share and hands the partner's share over with a
-// warp shuffle; the pairs at distance n/2 are evaluated by both lanes.
+// (a, a+dd mod n) for dd = 1..n/2-1, applies its own coefficient, and hands the unscaled flux to lane
+// a+dd with a warp shuffle, which applies its coefficient with one FMA per component; the pairs at
+// distance n/2 are evaluated by both lanes. The coefficients DVolSurf(l,i) are pre-scaled in shared
+// memory by the split flux's constant factors (exact: powers of two).
+// Shared memory: one region holds the split-flux inputs (rho, u, v, w, p-term, H-term and the metrics)
+// and afterwards the transformed viscous fluxes, so that two CTAs of 8^3 nodes fit on one SM.
 // =====================================================================================================
 template <int n>
-__global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_split(Dev d, Basis B, Stage st) {
+__global__ void __launch_bounds__(Shape<n>::THREADS, (n == 8 ? 2 : 1)) k_vol_split(Dev d, Basis B, Stage st) {
   using S = Shape<n>;
   constexpr int n2 = S::n2, n3 = S::n3, EPB = S::EPB;
   static_assert(n == 8 || n == 4 || n == 2, "split kernel expects 2, 4 or 8 nodes per line");
   extern __shared__ double smem[];
   double* sD = smem;
-  double* sV = smem + SBasis<n>::SIZE;  // [EPB][12][n3] transformed viscous fluxes (mom1..3, ener) x 3 directions
-  double* sQ = sV + EPB * 12 * n3;      // [EPB][6][n3] rho, u, v, w, 4p, H
-  double* sM = sQ + EPB * 6 * n3;       // [EPB][9][n3] metrics
-  double* sA = sM + EPB * 9 * n3;       // [EPB][5][n3] accumulated split-flux divergence
-  double* sFl = sA + EPB * 5 * n3;      // [EPB][6][n2][5]
+  double* sC = sD + SBasis<n>::SIZE;   // [2][n2]: DVolSurf(l,i) x density factor, x factor of the other components
+  double* sR = sC + 2 * n2;            // [EPB][15][n3]: rho, u, v, w, p-term, H-term, metrics(9); later viscous fluxes(12)
+  double* sA = sR + EPB * 15 * n3;     // [EPB][5][n3] split-flux divergence
+  double* sFl = sA + EPB * 5 * n3;     // [EPB][6][n2][5]
   load_basis_smem<n>(B, sD);
   SBasis<n> Bs{sD};
+  const bool pi = B.splitDG == 4;
+  {
+    // SplitVolumeFluxPI: 1/4 (density), 1/8 (others) of the contravariant sums below; SD: 1/2
+    const double f0 = pi ? 0.25 : 0.5, f1 = pi ? 0.125 : 0.5;
+    for (int t = threadIdx.x; t < n2; t += blockDim.x) { sC[t] = B.DVS[t] * f0; sC[n2 + t] = B.DVS[t] * f1; }
+  }
   const int e0 = blockIdx.x * EPB;
   load_face_fluxes<n>(d, sFl, e0);
-  const bool pi = B.splitDG == 4;
   for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
     const int es = t / n3, x = t - es * n3, e = e0 + es;
     if (e >= d.nElems) continue;
-    double u[5];
-#pragma unroll
-    for (int v = 0; v < 5; ++v) u[v] = d.U[((size_t)e * 5 + v) * n3 + x];
+    double* Q = sR + es * 15 * n3;
+    const double u0 = d.U[((size_t)e * 5 + 0) * n3 + x], u4 = d.U[((size_t)e * 5 + 4) * n3 + x];
     const double srho = d.prim[((size_t)e * VP_NF + VP_SRHO) * n3 + x];
-    const double vx = d.prim[((size_t)e * VP_NF + VP_U) * n3 + x];
-    const double vy = d.prim[((size_t)e * VP_NF + VP_V) * n3 + x];
-    const double vz = d.prim[((size_t)e * VP_NF + VP_W) * n3 + x];
     const double p = d.prim[((size_t)e * VP_NF + VP_P) * n3 + x];
-    double m[9];
-#pragma unroll
-    for (int c = 0; c < 9; ++c) { m[c] = d.metr[((size_t)e * 9 + c) * n3 + x]; sM[(es * 9 + c) * n3 + x] = m[c]; }
-    sQ[(es * 6 + 0) * n3 + x] = u[0];
-    sQ[(es * 6 + 1) * n3 + x] = vx;
-    sQ[(es * 6 + 2) * n3 + x] = vy;
-    sQ[(es * 6 + 3) * n3 + x] = vz;
+    Q[x] = u0;
+    Q[n3 + x] = d.prim[((size_t)e * VP_NF + VP_U) * n3 + x];
+    Q[2 * n3 + x] = d.prim[((size_t)e * VP_NF + VP_V) * n3 + x];
+    Q[3 * n3 + x] = d.prim[((size_t)e * VP_NF + VP_W) * n3 + x];
     if (pi) {
-      sQ[(es * 6 + 4) * n3 + x] = 4.0 * p;
-      sQ[(es * 6 + 5) * n3 + x] = (u[4] + p) * srho;
+      Q[4 * n3 + x] = 4.0 * p;
+      Q[5 * n3 + x] = (u4 + p) * srho;
     } else {
-      sQ[(es * 6 + 4) * n3 + x] = p;
-      sQ[(es * 6 + 5) * n3 + x] = u[4] + p;
-    }
-    double g[12];
-#pragma unroll
-    for (int c = 0; c < 12; ++c) g[c] = d.grad[((size_t)e * 12 + c) * n3 + x];
-    const double mu = d.mu0[d.elemInst[e]];
-    const double lam = mu * B.lambdaFac;
-#pragma unroll
-    for (int dd = 0; dd < 3; ++dd) {
-      double Fv[5];
-      visc_flux_dir(mu, lam, vx, vy, vz, g, m[3 * dd], m[3 * dd + 1], m[3 * dd + 2], Fv);
-#pragma unroll
-      for (int v = 0; v < 4; ++v) sV[(es * 12 + 4 * dd + v) * n3 + x] = Fv[1 + v];
+      Q[4 * n3 + x] = p;
+      Q[5 * n3 + x] = u4 + p;
     }
 #pragma unroll
-    for (int v = 0; v < 5; ++v) sA[(es * 5 + v) * n3 + x] = 0.;
+    for (int c = 0; c < 9; ++c) Q[(6 + c) * n3 + x] = d.metr[((size_t)e * 9 + c) * n3 + x];
   }
   __syncthreads();
-  // split-flux divergence, one direction at a time
+  // split-flux divergence, one direction at a time; the sum carries over from the previous direction
   const int lane = threadIdx.x & 31;
   const int segBase = lane & ~(n - 1);
 #pragma unroll 1
@@ -629,11 +666,13 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_split(Dev d, Basis B,
       else xa = c1 + n * (c2 + n * a);
       const int stride = dir == 0 ? 1 : (dir == 1 ? n : n2);
       const int xline = xa - a * stride;
-      const double* Q = sQ + es * 6 * n3;
-      const double* Mm = sM + (es * 9 + 3 * dir) * n3;
+      const double* Q = sR + es * 15 * n3;
+      const double* Mm = Q + (6 + 3 * dir) * n3;
       const double ra = Q[xa], ua = Q[n3 + xa], va = Q[2 * n3 + xa], wa = Q[3 * n3 + xa], pa = Q[4 * n3 + xa], ha = Q[5 * n3 + xa];
       const double ma0 = Mm[xa], ma1 = Mm[n3 + xa], ma2 = Mm[2 * n3 + xa];
-      double acc[5] = {0., 0., 0., 0., 0.};
+      double acc[5];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) acc[v] = (dir == 0) ? 0. : sA[(es * 5 + v) * n3 + xa];
 #pragma unroll
       for (int dd = 1; dd <= n / 2; ++dd) {
         const int bI = (a + dd) & (n - 1);
@@ -641,9 +680,8 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_split(Dev d, Basis B,
         const double rb = Q[xb], ub = Q[n3 + xb], vb = Q[2 * n3 + xb], wb = Q[3 * n3 + xb], pb = Q[4 * n3 + xb], hb = Q[5 * n3 + xb];
         const double ms0 = ma0 + Mm[xb], ms1 = ma1 + Mm[n3 + xb], ms2 = ma2 + Mm[2 * n3 + xb];
         double G[5];
-        double c0, c1o;  // scale factors of the density / other components
         if (pi) {
-          // SplitVolumeFluxPI in contravariant form: F = 1/4 A (dens), 1/8 (A u_s + 4 p_s m_s), 1/8 A H_s
+          // SplitVolumeFluxPI in contravariant form (factors in sC): A = rho_s q_s; A u_s + 4 p_s m_s; A H_s
           const double rs = ra + rb, us = ua + ub, vs = va + vb, ws = wa + wb, ps4 = pa + pb, hs = ha + hb;
           const double qs = us * ms0 + vs * ms1 + ws * ms2;
           const double A = rs * qs;
@@ -652,9 +690,8 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_split(Dev d, Basis B,
           G[2] = fma(A, vs, ps4 * ms1);
           G[3] = fma(A, ws, ps4 * ms2);
           G[4] = A * hs;
-          c0 = 0.25; c1o = 0.125;
         } else {
-          // SplitVolumeFluxSD: F = 1/2 m_s . (F(a) + F(b)); here sQ holds p and rho*E+p
+          // SplitVolumeFluxSD: m_s . (F(a) + F(b)) (factor 1/2 in sC); Q holds p and rho*E+p
           const double qa = ua * ms0 + va * ms1 + wa * ms2, qb = ub * ms0 + vb * ms1 + wb * ms2;
           const double mqa = ra * qa, mqb = rb * qb;
           G[0] = mqa + mqb;
@@ -662,31 +699,65 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_split(Dev d, Basis B,
           G[2] = fma(mqa, va, mqb * vb) + (pa + pb) * ms1;
           G[3] = fma(mqa, wa, mqb * wb) + (pa + pb) * ms2;
           G[4] = fma(ha, qa, hb * qb);
-          c0 = 0.5; c1o = 0.5;
         }
-        const double cOwn = Bs.DVS(bI, a), cPart = Bs.DVS(a, bI);
-        const double o0 = cOwn * c0, o1 = cOwn * c1o;
+        // contribution to node i from its partner l: DVolSurf(l, i)
+        const double o0 = sC[bI * n + a], o1 = sC[n2 + bI * n + a];
         acc[0] = fma(o0, G[0], acc[0]);
 #pragma unroll
         for (int v = 1; v < 5; ++v) acc[v] = fma(o1, G[v], acc[v]);
         if (dd < n / 2) {
-          const double p0 = cPart * c0, p1 = cPart * c1o;
-          const int src = segBase | ((a - dd) & (n - 1));
-          double recv[5];
-          recv[0] = __shfl_sync(0xffffffffu, p0 * G[0], src);
+          // receive the flux of the pair (a-dd, a) from lane a-dd
+          const int aS = (a - dd) & (n - 1);
+          const int src = segBase | aS;
+          const double r0 = sC[aS * n + a], r1 = sC[n2 + aS * n + a];
+          const double g0 = __shfl_sync(0xffffffffu, G[0], src);
+          acc[0] = fma(r0, g0, acc[0]);
 #pragma unroll
-          for (int v = 1; v < 5; ++v) recv[v] = __shfl_sync(0xffffffffu, p1 * G[v], src);
-#pragma unroll
-          for (int v = 0; v < 5; ++v) acc[v] += recv[v];
+          for (int v = 1; v < 5; ++v) {
+            const double gv = __shfl_sync(0xffffffffu, G[v], src);
+            acc[v] = fma(r1, gv, acc[v]);
+          }
         }
       }
       if (valid) {
 #pragma unroll
-        for (int v = 0; v < 5; ++v) sA[(es * 5 + v) * n3 + xa] += acc[v];
+        for (int v = 0; v < 5; ++v) sA[(es * 5 + v) * n3 + xa] = acc[v];
       }
     }
     __syncthreads();
   }
+  // viscous fluxes (weak form): transformed fluxes of this node from the metrics still in sR, written
+  // over sR once every thread has finished reading it (one node per thread: EPB * n3 == THREADS)
+  static_assert(EPB * n3 == S::THREADS, "one node per thread");
+  {
+    const int t = threadIdx.x;
+    const int es = t / n3, x = t - es * n3, e = e0 + es;
+    double Fv[12];
+    if (e < d.nElems) {
+      const double* Q = sR + es * 15 * n3;
+      const double vx = Q[n3 + x], vy = Q[2 * n3 + x], vz = Q[3 * n3 + x];
+      double m[9], g[12];
+#pragma unroll
+      for (int c = 0; c < 9; ++c) m[c] = Q[(6 + c) * n3 + x];
+#pragma unroll
+      for (int c = 0; c < 12; ++c) g[c] = d.grad[((size_t)e * 12 + c) * n3 + x];
+      const double mu = d.mu0[d.elemInst[e]];
+      const double lam = mu * B.lambdaFac;
+#pragma unroll
+      for (int dd = 0; dd < 3; ++dd) {
+        double F[5];
+        visc_flux_dir(mu, lam, vx, vy, vz, g, m[3 * dd], m[3 * dd + 1], m[3 * dd + 2], F);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) Fv[4 * dd + v] = F[1 + v];
+      }
+    }
+    __syncthreads();
+    if (e < d.nElems) {
+#pragma unroll
+      for (int c = 0; c < 12; ++c) sR[(es * 15 + c) * n3 + x] = Fv[c];
+    }
+  }
+  __syncthreads();
   for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
     const int es = t / n3, x = t - es * n3, e = e0 + es;
     if (e >= d.nElems) continue;
@@ -694,7 +765,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_split(Dev d, Basis B,
     double ut[5];
 #pragma unroll
     for (int v = 0; v < 5; ++v) ut[v] = sA[(es * 5 + v) * n3 + x];
-    const double* V = sV + es * 12 * n3;
+    const double* V = sR + es * 15 * n3;
 #pragma unroll
     for (int l = 0; l < n; ++l) {
       const double ci = Bs.DhT(l, i), cj = Bs.DhT(l, j), ck = Bs.DhT(l, k);
