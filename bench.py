@@ -1,10 +1,11 @@
 """Benchmark: FP64 DOF*stage/s of FLEXI's DGSEM Navier-Stokes RHS + LSERK stepper on GB300.
 
 Workload (default): Taylor-Green vortex on a curved periodic 32^3 hexahedral mesh, N=7 Gauss-Lobatto,
-split form with the Pirozzoli flux, BR2 lifting, RoeEntropyFix surface flux (the reference's split-form
-solver; it rejects HLLC with the split form), Re=1600, Ma=0.1, FP64, CarpenterRK4-5 with CFL/DFL time
-step control at CFLScale=DFLScale=0.8 (the setting of the reference's own split-form TGV regression; 0.9
-is at the stability edge of this discretisation). 16.8 M DOF x 5 variables; the state alone (671 MB) exceeds L2 (129 MB), so no L2 flush is
+split form with the Pirozzoli flux, BR2 lifting, HLLC surface flux (--riemann roeentropyfix selects the
+surface flux of the reference's own split-form TGV regression; the reference rejects HLLC with the split
+form, the CPU restatement and these kernels do not), Re=1600, Ma=0.1, FP64, CarpenterRK4-5 with CFL/DFL
+time step control at CFLScale=DFLScale=0.8 (the setting of the reference's split-form TGV regression;
+0.9 is at the stability edge of this discretisation). 16.8 M DOF x 5 variables; the state alone (671 MB) exceeds L2 (129 MB), so no L2 flush is
 needed between steps. Synthetic data: mesh and initial state are generated (no external dataset).
 
 value  : DOF*stage/s on the device, inputs resident in HBM, K steps bracketed by CUDA events on the
@@ -31,7 +32,14 @@ METRIC = "FP64 DOF*stage/s (N=7 TGV)"
 UNIT = "DOF*stage/s"
 # algorithmic flops per DOF and RK stage of the reference algorithm (counted with the oracle's
 # flop-counting scalar on this configuration; pinned by tests/test_bench_constants.py)
-FLOPS_PER_DOF_STAGE = {"prep": 24.5, "lift": 322.5, "flux": 145.5, "vol": 1408.9}
+FLOPS_PER_DOF_STAGE = {"prep": 24.5, "lift": 322.5, "vol": 1408.9}
+FLUX_FLOPS_PER_DOF_STAGE = {"hllc": 107.6, "roeentropyfix": 145.5}
+RIEMANN_IDS = {"hllc": 2, "roeentropyfix": 33}
+RIEMANN_NAMES = {"hllc": "HLLC", "roeentropyfix": "RoeEntropyFix"}
+
+
+def flops_per_dof_stage(riemann):
+    return dict(FLOPS_PER_DOF_STAGE, flux=FLUX_FLOPS_PER_DOF_STAGE[riemann])
 # compulsory HBM traffic per DOF and stage: U read+write, Ut_tmp read+write, 9 metric terms + sJ
 BYTES_ALG_PER_DOF_STAGE = 240.0
 
@@ -43,22 +51,32 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--elems", type=int, default=32, help="elements per direction")
+    p.add_argument("--riemann", default="hllc", choices=sorted(RIEMANN_IDS), help="surface Riemann solver")
+    p.add_argument("--workload", default="tgv", choices=["tgv", "ensemble"],
+                   help="tgv: the single-case N=7 TGV; ensemble: 256 independent TGV/vortex instances at N=5 against a loop over instances")
+    p.add_argument("--instances", type=int, default=256, help="ensemble size")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline leg (profiling runs)")
     return p.parse_args()
 
 
-def workload_config(n):
-    return {"workload": f"TGV {n}^3 curved (perturbation 0.05, NGeo=3), N=7 Gauss-Lobatto, split PI, BR2, RoeEntropyFix, FP64",
+def workload_config(n, riemann):
+    return {"workload": f"TGV {n}^3 curved (perturbation 0.05, NGeo=3), N=7 Gauss-Lobatto, split PI, BR2, {RIEMANN_NAMES[riemann]}, FP64",
             "n_elems": n ** 3, "N": 7, "dof": n ** 3 * 512, "Re": 1600, "Ma": 0.1, "CFLScale": 0.8, "DFLScale": 0.8,
             "time_integration": "CarpenterRK4-5, 5 stages/step, CFL/DFL dt each step",
             "l2": "inputs larger than L2 (state 671 MB at 32^3)", "parallelism": "replicas"}
 
 
-def solver_config():
+def solver_config(riemann):
     from flexi_gb300.solver import make_config
-    return make_config(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roeentropyfix", Lifting="br2", kappa=1.4, R=71.42857,
+    return make_config(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann=riemann, Lifting="br2", kappa=1.4, R=71.42857,
                        Pr=0.72, mu0=6.25e-4, CFLScale=0.8, DFLScale=0.8)
+
+
+def oracle_config(riemann):
+    """The same discretisation for the CPU restatement."""
+    return dict(N=7, nodeType=2, riemann=RIEMANN_IDS[riemann], riemannBC=-1, lifting=2, weakLifting=0, consLifting=0, splitDG=4, etaBR2=2.0,
+                etaBR2_wall=-1.0, kappa=1.4, R=71.42857, Pr=0.72, mu0=6.25e-4, CFLScale=0.8, DFLScale=0.8, doTCSource=0, dpdx=-1.0)
 
 
 def dist_info():
@@ -131,15 +149,14 @@ def ncu_traffic():
         return {}
 
 
-def cpu_baseline_sample(n_elems_dir=8, budget_s=12.0):
+def cpu_baseline_sample(riemann, n_elems_dir=8, budget_s=12.0):
     """Oracle (C++ restatement of FLEXI's operator) on all host threads: TGV sample of the same
     discretisation, timed RK steps until the budget is used. Returns (DOF*stage/s, threads, sample)."""
     import numpy as np
     from flexi_gb300 import mesh as fmesh, testcases
     from oracle import oracle as orc
     orc.set_threads(os.cpu_count() or 1)
-    cfg = dict(N=7, nodeType=2, riemann=33, riemannBC=-1, lifting=2, weakLifting=0, consLifting=0, splitDG=4, etaBR2=2.0, etaBR2_wall=-1.0,
-               kappa=1.4, R=71.42857, Pr=0.72, mu0=6.25e-4, CFLScale=0.8, DFLScale=0.8, doTCSource=0, dpdx=-1.0)
+    cfg = oracle_config(riemann)
     m = fmesh.tgv_box(n_elems_dir, ngeo=3, perturb=0.05, seed=0)
     o = orc.Oracle(cfg, m)
     o.set_state(testcases.tgv_state(o.mesh_array("Elem_xGP"), mach=0.1, kappa=1.4, R=71.42857))
@@ -168,8 +185,7 @@ def run_reference(args):
     from oracle import oracle as orc
     threads = os.cpu_count() or 1
     orc.set_threads(threads)
-    cfg = dict(N=7, nodeType=2, riemann=33, riemannBC=-1, lifting=2, weakLifting=0, consLifting=0, splitDG=4, etaBR2=2.0, etaBR2_wall=-1.0,
-               kappa=1.4, R=71.42857, Pr=0.72, mu0=6.25e-4, CFLScale=0.8, DFLScale=0.8, doTCSource=0, dpdx=-1.0)
+    cfg = oracle_config(args.riemann)
     ns = 6  # bounded sample: 6^3 elements of the same discretisation per step
     m = fmesh.tgv_box(ns, ngeo=3, perturb=0.05, seed=0)
     o = orc.Oracle(cfg, m)
@@ -188,7 +204,7 @@ def run_reference(args):
     sample = f"TGV {ns}^3 of the workload's discretisation ({dof} DOF) per step, {args.steps} RK steps, {el:.2f} s"
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(args.elems),
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(args.elems, args.riemann),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "C++ restatement of FLEXI's Fortran path (FLEXI needs Fortran, MPI and HDF5, absent here)"}
@@ -210,8 +226,8 @@ def run_gb300(args):
     from flexi_gb300.solver import Flexi, probe_fp64_tflops
 
     n = args.elems
-    cfgd = workload_config(n)
-    c = solver_config()
+    cfgd = workload_config(n, args.riemann)
+    c = solver_config(args.riemann)
     m = fmesh.tgv_box(n, ngeo=3, perturb=0.05, seed=rank)
     f = Flexi(c, m)
     U0 = testcases.tgv_state(f.elem_xgp(), mach=0.1, kappa=1.4, R=71.42857)
@@ -279,7 +295,8 @@ def run_gb300(args):
     dom = max(("prep", "lift", "flux", "vol"), key=lambda k: prof[k][0])
     dom_ms, dom_cnt = prof[dom]
     avg_ms = dom_ms / max(dom_cnt, 1)
-    achieved = FLOPS_PER_DOF_STAGE[dom] * dof / (avg_ms * 1e-3) / 1e12
+    flops = flops_per_dof_stage(args.riemann)
+    achieved = flops[dom] * dof / (avg_ms * 1e-3) / 1e12
     peaks = measured_peaks()
     traffic = ncu_traffic().get(dom)
     roofline = {"bound": "fp64", "kernel": {"vol": "k_vol_split<8>", "lift": "k_lift<8,GL>", "flux": "k_flux<8>", "prep": "k_prep<8,GL>"}[dom],
@@ -287,7 +304,7 @@ def run_gb300(args):
                 "peak_source": "own DFMA probe (fg_probe_fp64), MEASURED_PEAKS.json has no FP64 figure",
                 "traffic": (traffic * dof if traffic is not None else None),
                 "traffic_unit": "bytes per launch (ncu dram read+write, scaled per DOF)" if traffic is not None else None,
-                "algorithmic_flops_per_dof": FLOPS_PER_DOF_STAGE[dom], "avg_launch_ms": avg_ms,
+                "algorithmic_flops_per_dof": flops[dom], "avg_launch_ms": avg_ms,
                 "hbm_alg_gbs": value / ws * BYTES_ALG_PER_DOF_STAGE / 1e9,
                 "hbm_peak_gbs": peaks.get("hbm_gbs"),
                 "frac_hbm": (value / ws * BYTES_ALG_PER_DOF_STAGE / 1e9 / peaks["hbm_gbs"]) if peaks.get("hbm_gbs") else None,
@@ -295,7 +312,7 @@ def run_gb300(args):
     try:
         if args.no_cpu_baseline:
             raise RuntimeError("skipped (--no-cpu-baseline)")
-        cpu_val, cores, sample = cpu_baseline_sample()
+        cpu_val, cores, sample = cpu_baseline_sample(args.riemann)
         cpu = {"value": cpu_val, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
     except Exception as ex:  # reported, never substituted for the GPU path
         cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port", "sample": f"failed: {ex}"}
@@ -307,10 +324,208 @@ def run_gb300(args):
     f.close()
 
 
+# ---------------------------------------------------------------------------------------------------------
+# Ensemble workload: independent periodic instances of uneven size and flow parameters in one solver
+# ---------------------------------------------------------------------------------------------------------
+ENSEMBLE_SIZES = (4, 6, 8, 12, 16)
+# oracle flop counts per DOF and stage of the ensemble discretisation (N=5 Gauss, weak form, RoeEntropyFix, BR1)
+ENSEMBLE_FLOPS = {"prep": 83.0, "lift": 500.0, "flux": 191.0, "vol": 411.5}
+ENSEMBLE_METRIC = "ensemble instance-steps/s (256 TGV/vortex instances, N=5 Gauss)"
+
+
+def ensemble_spec(n_inst, seed=0):
+    """Seeded instance parameters: elements per direction, Mach number U[0.05,0.3], Reynolds number
+    logU[400,3200], kind (0 Taylor-Green vortex, 1 isentropic vortex)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    sizes = rng.choice(ENSEMBLE_SIZES, size=n_inst)
+    mach = rng.uniform(0.05, 0.3, n_inst)
+    re = np.exp(rng.uniform(np.log(400.0), np.log(3200.0), n_inst))
+    kind = rng.integers(0, 2, n_inst)
+    return sizes, mach, re, kind
+
+
+def ensemble_solver_config():
+    from flexi_gb300.solver import make_config
+    return make_config(N=5, NodeType="gauss", SplitDG="weak", Riemann="roeentropyfix", Lifting="br1", kappa=1.4, R=71.42857, Pr=0.72,
+                       mu0=1.0 / 1600.0, CFLScale=0.9, DFLScale=0.9)
+
+
+def ensemble_oracle_config():
+    return dict(N=5, nodeType=1, riemann=33, riemannBC=-1, lifting=1, weakLifting=0, consLifting=0, splitDG=-1, etaBR2=2.0, etaBR2_wall=-1.0,
+                kappa=1.4, R=71.42857, Pr=0.72, mu0=1.0 / 1600.0, CFLScale=0.9, DFLScale=0.9, doTCSource=0, dpdx=-1.0)
+
+
+def instance_state(xgp, kind, mach):
+    from flexi_gb300 import testcases
+    if kind == 0:
+        return testcases.tgv_state(xgp, mach=mach, kappa=1.4, R=71.42857)
+    return testcases.shu_vortex_state(xgp, mach=mach, kappa=1.4)
+
+
+def ensemble_config(sizes, n_dof):
+    return {"workload": f"ensemble of {len(sizes)} periodic TGV / isentropic-vortex instances, elements per instance drawn from "
+                        f"{{4,6,8,12,16}}^3, Ma U[0.05,0.3], Re logU[400,3200] (seeded), N=5 Gauss, weak form, RoeEntropyFix, BR1, FP64",
+            "instances": len(sizes), "n_elems": int(sum(int(k) ** 3 for k in sizes)), "N": 5, "dof": n_dof, "CFLScale": 0.9, "DFLScale": 0.9,
+            "time_integration": "CarpenterRK4-5, per-instance CFL/DFL dt each step, one graph-replayed launch sequence for all instances",
+            "l2": f"inputs larger than L2 (state {n_dof * 40 / 1e9:.1f} GB)", "parallelism": "replicas"}
+
+
+def run_ensemble(args):
+    import numpy as np
+    import torch
+
+    ws, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from flexi_gb300 import mesh as fmesh
+    from flexi_gb300.solver import Flexi, probe_fp64_tflops
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+
+    sizes, mach, re, kind = ensemble_spec(args.instances, seed=rank)
+    c = ensemble_solver_config()
+    boxes = {int(k): fmesh.tgv_box(int(k)) for k in set(sizes.tolist())}
+    m = fmesh.concatenate([boxes[int(k)] for k in sizes])
+    f = Flexi(c, m)
+    xgp = f.elem_xgp()
+    starts = np.concatenate([[0], np.cumsum(sizes.astype(np.int64) ** 3)])
+    U0 = np.concatenate([instance_state(xgp[starts[i]:starts[i + 1]], int(kind[i]), float(mach[i])) for i in range(len(sizes))])
+    mu = 1.0 / re
+    f.U = U0
+    f.set_instance_mu0(mu)
+    dof = f.n_elems * f.n ** 3
+    stream = torch.cuda.ExternalStream(f.stream())
+    fp64_peak = probe_fp64_tflops()
+
+    f.TimeDisc(args.warmup)
+    f.profile(True)
+    f.profile_read()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    f.TimeDisc(args.steps)
+    e1.record(stream)
+    barrier()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    prof = f.profile_read()
+    launches_per_step = f.launch_count()
+    f.profile(False)
+    U_ens = f.U
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = len(sizes) * args.steps * ws / (ms * 1e-3)
+
+    # e2e through the public API: host state in, one step for all instances, host state out
+    e2e = None
+    if not args.no_e2e:
+        f.U = U0
+        nbytes = dof * 5 * 8
+        hin = torch.from_numpy(np.ascontiguousarray(U0).reshape(-1)).pin_memory()
+        hout = torch.empty(dof * 5, dtype=torch.float64).pin_memory()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            f.set_state_ptr(hin.data_ptr())
+            f.TimeDisc(1)
+            f.get_state_ptr(hout.data_ptr())
+            hin, hout = hout, hin
+        barrier()
+        el = time.perf_counter() - t0
+        e2e = {"value": len(sizes) * args.steps * ws / el, "unit": "instance-steps/s", "h2d_bytes_per_step": nbytes,
+               "d2h_bytes_per_step": nbytes, "ms_per_step": el / args.steps * 1e3}
+    f.close()
+
+    # the same instances, one plain solver after another (same kernels, same steps, graph-replayed per instance)
+    loop_ms, max_diff = 0.0, 0.0
+    for i in range(len(sizes)):
+        g = Flexi(c, boxes[int(sizes[i])])
+        g.U = U0[starts[i]:starts[i + 1]]
+        g.set_instance_mu0(np.array([mu[i]]))
+        g.TimeDisc(args.warmup)
+        gs = torch.cuda.ExternalStream(g.stream())
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(gs)
+        g.TimeDisc(args.steps)
+        b.record(gs)
+        torch.cuda.synchronize()
+        loop_ms += a.elapsed_time(b)
+        ref = U_ens[starts[i]:starts[i + 1]]
+        max_diff = max(max_diff, float(np.abs(g.U - ref).max() / np.abs(ref).max()))
+        g.close()
+    loop_value = len(sizes) * args.steps / (loop_ms * 1e-3)
+
+    if rank != 0:
+        return
+    dom = max(("prep", "lift", "flux", "vol"), key=lambda k: prof[k][0])
+    avg_ms = prof[dom][0] / max(prof[dom][1], 1)
+    achieved = ENSEMBLE_FLOPS[dom] * dof / (avg_ms * 1e-3) / 1e12
+    roofline = {"bound": "fp64", "kernel": {"vol": "k_vol_weak<6,Gauss>", "lift": "k_lift<6,Gauss>", "flux": "k_flux<6>", "prep": "k_prep<6,Gauss>"}[dom],
+                "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved / fp64_peak,
+                "peak_source": "own DFMA probe (fg_probe_fp64), MEASURED_PEAKS.json has no FP64 figure", "traffic": None,
+                "algorithmic_flops_per_dof": ENSEMBLE_FLOPS[dom], "avg_launch_ms": avg_ms,
+                "kernel_ms_per_step": {k: prof[k][0] / args.steps for k in prof}}
+    try:
+        if args.no_cpu_baseline:
+            raise RuntimeError("skipped (--no-cpu-baseline)")
+        cpu = ensemble_cpu_baseline()
+    except Exception as ex:
+        cpu = {"value": None, "unit": "instance-steps/s", "cores": None, "kind": "port", "sample": f"failed: {ex}"}
+    line = {"metric": ENSEMBLE_METRIC, "value": value, "unit": "instance-steps/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "config": ensemble_config(sizes, dof), "e2e": e2e,
+            "gpu_launches": launches_per_step * args.steps, "clocks": clk, "roofline": roofline, "cpu_baseline": cpu,
+            "dof_stage_per_s": dof * 5 * args.steps * ws / (ms * 1e-3),
+            "loop_baseline": {"value": loop_value, "unit": "instance-steps/s", "ms_per_step": loop_ms / args.steps,
+                              "what": "the same instances advanced one after another by the plain solver (one handle per instance)"},
+            "speedup_vs_loop": value / ws / loop_value, "max_rel_state_diff_vs_loop": max_diff}
+    print(json.dumps(line), flush=True)
+
+
+def ensemble_cpu_baseline(budget_s=10.0):
+    """Oracle on all host threads, instance by instance over the first instances of the ensemble."""
+    import numpy as np
+    from flexi_gb300 import mesh as fmesh
+    from oracle import oracle as orc
+    orc.set_threads(os.cpu_count() or 1)
+    sizes, mach, re, kind = ensemble_spec(8)
+    done, el = 0, 0.0
+    for i in range(len(sizes)):
+        cfg = dict(ensemble_oracle_config(), mu0=float(1.0 / re[i]))
+        m = fmesh.tgv_box(int(sizes[i]))
+        o = orc.Oracle(cfg, m)
+        o.set_state(instance_state(o.mesh_array("Elem_xGP"), int(kind[i]), float(mach[i])))
+        t = 0.0
+        t0 = time.perf_counter()
+        for _ in range(2):
+            dt, _ = o.calc_timestep()
+            t = o.timestep(t, dt)
+            done += 1
+        el += time.perf_counter() - t0
+        if el > budget_s:
+            break
+    return {"value": done / el, "unit": "instance-steps/s", "cores": orc.max_threads(), "kind": "port",
+            "sample": f"first {i + 1} instances of the same seeded ensemble (sizes {sizes[:i + 1].tolist()}), 2 RK steps each, "
+                      f"{el:.1f} s of stepping"}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "ensemble":
+        run_ensemble(args)
     else:
         run_gb300(args)
 

@@ -18,13 +18,12 @@ def _bench():
     return mod
 
 
-def test_flops_per_dof_stage_match_oracle_count():
+@pytest.mark.parametrize("riemann", ["hllc", "roeentropyfix"])
+def test_flops_per_dof_stage_match_oracle_count(riemann):
     bench = _bench()
-    cfg = dict(N=7, nodeType=2, riemann=33, riemannBC=-1, lifting=2, weakLifting=0, consLifting=0, splitDG=4, etaBR2=2.0, etaBR2_wall=-1.0,
-               kappa=1.4, R=71.42857, Pr=0.72, mu0=6.25e-4, CFLScale=0.8, DFLScale=0.8, doTCSource=0, dpdx=-1.0)
     m = fmesh.tgv_box(4, ngeo=3, perturb=0.05)
-    o = orc.Oracle(cfg, m)
+    o = orc.Oracle(bench.oracle_config(riemann), m)
     o.set_state(testcases.tgv_state(o.mesh_array("Elem_xGP"), mach=0.1, kappa=1.4, R=71.42857))
     counted = o.flops_breakdown()
-    for k, v in bench.FLOPS_PER_DOF_STAGE.items():
+    for k, v in bench.flops_per_dof_stage(riemann).items():
         assert v == pytest.approx(counted[k], rel=2e-3), (k, v, counted[k])
