@@ -17,7 +17,10 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU = ["fg_host.cu", "fg_noalloc.cu"] + [f"fg_inst_n{n}.cu" for n in range(2, 9)]
 CPP = ["fg_mesh.cpp"]
-HEADERS = ["fg_common.cuh", "fg_kernels.cuh", "fg_launch.cuh", "fg_inst.cuh", "fg_basis.hpp", "fg_mesh.hpp"]
+HEADERS = ["fg_common.cuh", "fg_kernels.cuh", "fg_launch.cuh", "fg_inst.cuh", "fg_basis.hpp", "fg_mesh.hpp", "fg_adjoint_point.cuh"]
+# host-only harness of the point-wise physics and its adjoints, for the CPU tests
+POINT_SRC = "fg_point_test.cu"
+POINT_LIB = os.path.join(OUT, "libfgpoint.so")
 
 
 def _nvcc():
@@ -67,7 +70,21 @@ def build(force: bool = False, jobs: int = 0) -> str:
         if r.returncode != 0:
             raise RuntimeError(f"link failed\n{r.stdout}\n{r.stderr}")
         os.replace(LIB + ".tmp", LIB)
+    build_point_harness()
     return LIB
+
+
+def build_point_harness() -> str:
+    """libfgpoint.so: the point-wise functions compiled as host code (no device code, no GPU needed)."""
+    os.makedirs(OUT, exist_ok=True)
+    src = os.path.join(CSRC, POINT_SRC)
+    if _stale(POINT_LIB, src):
+        cmd = [_nvcc(), "-O2", "-std=c++17", "-shared", "-Xcompiler", "-fPIC", "-I", INCLUDE, src, "-o", POINT_LIB + ".tmp"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"compile failed: {POINT_SRC}\n{r.stdout}\n{r.stderr}")
+        os.replace(POINT_LIB + ".tmp", POINT_LIB)
+    return POINT_LIB
 
 
 if __name__ == "__main__":

@@ -1,0 +1,392 @@
+// flexi_gb300 -- reverse-mode (vector-Jacobian) counterparts of the point-wise physics of fg_common.cuh.
+//
+// Each *_adj function takes the inputs of its forward function and the cotangent of its outputs and
+// ADDS the cotangent of every input to the caller's accumulators (x_bar += J^T y_bar). They retrace the
+// forward function's own operations, so that they are the exact transposed Jacobians of the code that
+// runs forward, including its branch choices (entropy fix, max/abs, pressure clamp). At a tie of a max
+// the forward's choice (the first argument of fmax when both are equal) gets the derivative.
+#pragma once
+#include "fg_common.cuh"
+
+namespace fg {
+
+#define FG_HD __host__ __device__ __forceinline__
+
+FG_HD double sgn1(double x) { return x >= 0.0 ? 1.0 : -1.0; }
+
+// eos.f90:ConsToPrim: (rho, m, E) -> (1/rho, v, p, T). Given the bars of 1/rho, v (3), p, T and direct bars
+// of rho and E (face states store both), accumulates the conservative bars into Ub[5].
+FG_HD void cons_to_prim_adj(const Basis& B, const double* U, double sb, double ub, double vb, double wb, double pb, double Tb,
+                            double rhob, double Eb, double* Ub) {
+  const double srho = 1.0 / U[0];
+  const double vx = U[1] * srho, vy = U[2] * srho, vz = U[3] * srho;
+  const double p = B.kappaM1 * (U[4] - 0.5 * (U[1] * vx + U[2] * vy + U[3] * vz));
+  // T = p * srho * sR
+  pb += Tb * srho * B.sR;
+  sb += Tb * p * B.sR;
+  // p = kappaM1 * (E - 1/2 (m . v))
+  const double kp = B.kappaM1 * pb;
+  Eb += kp;
+  double mb1 = -0.5 * kp * vx, mb2 = -0.5 * kp * vy, mb3 = -0.5 * kp * vz;
+  ub -= 0.5 * kp * U[1];
+  vb -= 0.5 * kp * U[2];
+  wb -= 0.5 * kp * U[3];
+  // v = m * srho
+  mb1 += ub * srho; mb2 += vb * srho; mb3 += wb * srho;
+  sb += ub * U[1] + vb * U[2] + wb * U[3];
+  // srho = 1 / rho
+  rhob -= sb * srho * srho;
+  Ub[0] += rhob; Ub[1] += mb1; Ub[2] += mb2; Ub[3] += mb3; Ub[4] += Eb;
+}
+
+// visc_flux_dir: F[1..4] of the viscous flux contracted with (m1, m2, m3). Fb[1..4] given; adds to the
+// velocity bars (ub, vb, wb), the gradient bars gb[12] and the viscosity bar mub (lam = mu * lamFac).
+FG_HD void visc_flux_dir_adj(double mu, double lamFac, double u, double v, double w, const double* g, double m1, double m2, double m3,
+                             const double* Fb, double& ub, double& vb, double& wb, double* gb, double& mub) {
+  const double lam = mu * lamFac;
+  const double div = g[0] + g[5] + g[10];
+  const double mdiv = (2.0 / 3.0) * div;
+  const double sxx = 2.0 * g[0] - mdiv, syy = 2.0 * g[5] - mdiv, szz = 2.0 * g[10] - mdiv;
+  const double sxy = g[4] + g[1], sxz = g[8] + g[2], syz = g[9] + g[6];
+  const double txx = mu * sxx, tyy = mu * syy, tzz = mu * szz, txy = mu * sxy, txz = mu * sxz, tyz = mu * syz;
+  const double a1 = txx * m1 + txy * m2 + txz * m3;
+  const double a2 = txy * m1 + tyy * m2 + tyz * m3;
+  const double a3 = txz * m1 + tyz * m2 + tzz * m3;
+  const double qn = g[3] * m1 + g[7] * m2 + g[11] * m3;
+  // F1 = -a1, F2 = -a2, F3 = -a3, F4 = -(a1 u + a2 v + a3 w) - lam qn
+  const double a1b = -Fb[1] - Fb[4] * u, a2b = -Fb[2] - Fb[4] * v, a3b = -Fb[3] - Fb[4] * w;
+  ub -= Fb[4] * a1; vb -= Fb[4] * a2; wb -= Fb[4] * a3;
+  const double lamb = -Fb[4] * qn, qnb = -Fb[4] * lam;
+  gb[3] += qnb * m1; gb[7] += qnb * m2; gb[11] += qnb * m3;
+  const double txxb = a1b * m1, tyyb = a2b * m2, tzzb = a3b * m3;
+  const double txyb = a1b * m2 + a2b * m1, txzb = a1b * m3 + a3b * m1, tyzb = a2b * m3 + a3b * m2;
+  mub += txxb * sxx + tyyb * syy + tzzb * szz + txyb * sxy + txzb * sxz + tyzb * syz + lamb * lamFac;
+  const double sxxb = mu * txxb, syyb = mu * tyyb, szzb = mu * tzzb;
+  const double divb = -(2.0 / 3.0) * (sxxb + syyb + szzb);
+  gb[0] += 2.0 * sxxb + divb; gb[5] += 2.0 * syyb + divb; gb[10] += 2.0 * szzb + divb;
+  gb[4] += mu * txyb; gb[1] += mu * txyb;
+  gb[8] += mu * txzb; gb[2] += mu * txzb;
+  gb[9] += mu * tyzb; gb[6] += mu * tyzb;
+}
+
+FG_HD void rot_zero(RotState& S) { S.rho = S.srho = S.E = S.p = S.v1 = S.v2 = S.v3 = 0.0; }
+
+FG_HD void euler_flux_1d_adj(const RotState& S, const double* Fb, RotState& Sb) {
+  const double m = S.rho * S.v1;
+  const double mb = Fb[0] + Fb[1] * S.v1 + Fb[2] * S.v2 + Fb[3] * S.v3;
+  Sb.v1 += Fb[1] * m + Fb[4] * (S.E + S.p) + mb * S.rho;
+  Sb.p += Fb[1] + Fb[4] * S.v1;
+  Sb.v2 += Fb[2] * m;
+  Sb.v3 += Fb[3] * m;
+  Sb.E += Fb[4] * S.v1;
+  Sb.rho += mb * S.v1;
+}
+
+// H = (E + p) * srho
+FG_HD void enthalpy_adj(const RotState& S, double Hb, RotState& Sb) {
+  Sb.E += Hb * S.srho;
+  Sb.p += Hb * S.srho;
+  Sb.srho += Hb * (S.E + S.p);
+}
+
+FG_HD void split_surface_flux_adj(int splitDG, const RotState& L, const RotState& R, double HL, double HR, const double* Fb, RotState& Lb,
+                                  RotState& Rb, double& HLb, double& HRb) {
+  if (splitDG == 4) {
+    const double rs = L.rho + R.rho, us = L.v1 + R.v1;
+    const double a = rs * us;
+    const double b = 0.125 * a;
+    const double v2s = L.v2 + R.v2, v3s = L.v3 + R.v3, Hs = HL + HR;
+    const double bb = Fb[1] * us + Fb[2] * v2s + Fb[3] * v3s + Fb[4] * Hs;
+    const double ab = 0.25 * Fb[0] + 0.125 * bb;
+    const double usb = Fb[1] * b + ab * rs;
+    const double rsb = ab * us;
+    Lb.rho += rsb; Rb.rho += rsb;
+    Lb.v1 += usb; Rb.v1 += usb;
+    Lb.p += 0.5 * Fb[1]; Rb.p += 0.5 * Fb[1];
+    Lb.v2 += Fb[2] * b; Rb.v2 += Fb[2] * b;
+    Lb.v3 += Fb[3] * b; Rb.v3 += Fb[3] * b;
+    HLb += Fb[4] * b; HRb += Fb[4] * b;
+  } else {  // SD
+    const double mL = L.rho * L.v1, mR = R.rho * R.v1;
+    // F0 = (mL+mR)/2; F1 = (mL vL + pL + mR vR + pR)/2; F2 = (mL v2L + mR v2R)/2; F3 ...; F4 = ((EL+pL) v1L + (ER+pR) v1R)/2
+    const double mLb = 0.5 * (Fb[0] + Fb[1] * L.v1 + Fb[2] * L.v2 + Fb[3] * L.v3);
+    const double mRb = 0.5 * (Fb[0] + Fb[1] * R.v1 + Fb[2] * R.v2 + Fb[3] * R.v3);
+    Lb.v1 += 0.5 * Fb[1] * mL + 0.5 * Fb[4] * (L.E + L.p) + mLb * L.rho;
+    Rb.v1 += 0.5 * Fb[1] * mR + 0.5 * Fb[4] * (R.E + R.p) + mRb * R.rho;
+    Lb.p += 0.5 * Fb[1] + 0.5 * Fb[4] * L.v1;
+    Rb.p += 0.5 * Fb[1] + 0.5 * Fb[4] * R.v1;
+    Lb.v2 += 0.5 * Fb[2] * mL; Rb.v2 += 0.5 * Fb[2] * mR;
+    Lb.v3 += 0.5 * Fb[3] * mL; Rb.v3 += 0.5 * Fb[3] * mR;
+    Lb.E += 0.5 * Fb[4] * L.v1; Rb.E += 0.5 * Fb[4] * R.v1;
+    Lb.rho += mLb * L.v1; Rb.rho += mRb * R.v1;
+  }
+}
+
+// Harten-Hyman entropy fix of RoeEntropyFix: e = fix(a, al, ar); adds the bars of a, al, ar.
+FG_HD void entropy_fix_adj(double a, double al, double ar, double eb, double& abar, double& alb, double& arb) {
+  const double x = a - al, y = ar - a;
+  const double da = fmax(0.0, fmax(x, y));
+  const double aa = fabs(a);
+  double dab = 0.0;
+  if (aa < da) {
+    abar += eb * (a / da);
+    dab = eb * 0.5 * (1.0 - (a * a) / (da * da));
+  } else {
+    abar += eb * sgn1(a);
+  }
+  if (dab != 0.0 && da > 0.0) {
+    if (x >= y) { abar += dab; alb -= dab; }
+    else { arb += dab; abar -= dab; }
+  }
+}
+
+// Transposed Jacobian of riemann_rotated (LF, Roe, RoeEntropyFix; split or not): Fb[5] given, adds to the
+// bars of both rotated states (all seven fields of each are independent inputs).
+FG_HD void riemann_rotated_adj(int solver, int splitDG, const Basis& B, const RotState& L, const RotState& R, const double* Fb, RotState& Lb,
+                               RotState& Rb) {
+  const bool split = splitDG >= 0;
+  const double HL = (L.E + L.p) * L.srho, HR = (R.E + R.p) * R.srho;
+  double HLb = 0.0, HRb = 0.0;
+  double Db[5];  // bar of the dissipation term (F = central - 1/2 D, or -1/2 lmax dU)
+  if (!split) {
+    double Fh[5];
+    for (int v = 0; v < 5; ++v) Fh[v] = 0.5 * Fb[v];
+    euler_flux_1d_adj(L, Fh, Lb);
+    euler_flux_1d_adj(R, Fh, Rb);
+  } else {
+    split_surface_flux_adj(splitDG, L, R, HL, HR, Fb, Lb, Rb, HLb, HRb);
+  }
+  for (int v = 0; v < 5; ++v) Db[v] = -0.5 * Fb[v];
+  if (solver == RIEMANN_LF) {
+    const double cL = sqrt(B.kappa * L.p * L.srho), cR = sqrt(B.kappa * R.p * R.srho);
+    const double aL = fabs(L.v1), aR = fabs(R.v1);
+    const double lmax = fmax(aR, aL) + fmax(cL, cR);
+    const double dU[5] = {R.rho - L.rho, R.rho * R.v1 - L.rho * L.v1, R.rho * R.v2 - L.rho * L.v2, R.rho * R.v3 - L.rho * L.v3, R.E - L.E};
+    double lb = 0.0;
+    for (int v = 0; v < 5; ++v) lb += Db[v] * dU[v];
+    double dUb[5];
+    for (int v = 0; v < 5; ++v) dUb[v] = Db[v] * lmax;
+    if (aR >= aL) Rb.v1 += lb * sgn1(R.v1); else Lb.v1 += lb * sgn1(L.v1);
+    if (cL >= cR) {
+      Lb.p += lb * B.kappa * L.srho / (2.0 * cL);
+      Lb.srho += lb * B.kappa * L.p / (2.0 * cL);
+    } else {
+      Rb.p += lb * B.kappa * R.srho / (2.0 * cR);
+      Rb.srho += lb * B.kappa * R.p / (2.0 * cR);
+    }
+    Rb.rho += dUb[0] + dUb[1] * R.v1 + dUb[2] * R.v2 + dUb[3] * R.v3;
+    Lb.rho -= dUb[0] + dUb[1] * L.v1 + dUb[2] * L.v2 + dUb[3] * L.v3;
+    Rb.v1 += dUb[1] * R.rho; Lb.v1 -= dUb[1] * L.rho;
+    Rb.v2 += dUb[2] * R.rho; Lb.v2 -= dUb[2] * L.rho;
+    Rb.v3 += dUb[3] * R.rho; Lb.v3 -= dUb[3] * L.rho;
+    Rb.E += dUb[4]; Lb.E -= dUb[4];
+    enthalpy_adj(L, HLb, Lb);
+    enthalpy_adj(R, HRb, Rb);
+    return;
+  }
+  // Roe averages
+  const double sqL = sqrt(L.rho), sqR = sqrt(R.rho);
+  const double ssq = 1.0 / (sqL + sqR);
+  const double r1v = (sqR * R.v1 + sqL * L.v1) * ssq;
+  const double r2v = (sqR * R.v2 + sqL * L.v2) * ssq;
+  const double r3v = (sqR * R.v3 + sqL * L.v3) * ssq;
+  const double rH = (sqR * HR + sqL * HL) * ssq;
+  const double absVel = r1v * r1v + r2v * r2v + r3v * r3v;
+  const double rc = sqrt(B.kappaM1 * (rH - 0.5 * absVel));
+  const double a0 = r1v - rc, a1 = r1v, a4 = r1v + rc;
+  // forward: strengths and |eigenvalues|
+  double A0, A1, A2, A3, A4, e0, e1, e4;
+  // Roe intermediates
+  double d0 = 0, d1 = 0, d2 = 0, d3 = 0, d4 = 0, d5 = 0, src = 0;
+  // RoeEntropyFix intermediates
+  double cL = 0, cR = 0, RoeDens = 0, dr = 0, du = 0, dv = 0, dw = 0, dp = 0, tmp = 0, rdc = 0;
+  if (solver == RIEMANN_ROE) {
+    d0 = R.rho - L.rho;
+    d1 = R.rho * R.v1 - L.rho * L.v1;
+    d2 = R.rho * R.v2 - L.rho * L.v2;
+    d3 = R.rho * R.v3 - L.rho * L.v3;
+    d4 = R.E - L.E;
+    A2 = d2 - r2v * d0;
+    A3 = d3 - r3v * d0;
+    d5 = d4 - A2 * r2v - A3 * r3v;
+    src = 1.0 / rc;
+    A1 = B.kappaM1 * (src * src) * (d0 * (rH - r1v * r1v) - d5 + r1v * d1);
+    A0 = 0.5 * src * (d0 * (r1v + rc) - d1 - rc * A1);
+    A4 = d0 - A0 - A1;
+    e0 = fabs(a0); e1 = fabs(a1); e4 = fabs(a4);
+  } else {
+    cL = sqrt(B.kappa * L.p * L.srho); cR = sqrt(B.kappa * R.p * R.srho);
+    RoeDens = sqL * sqR;
+    dr = R.rho - L.rho; du = R.v1 - L.v1; dv = R.v2 - L.v2; dw = R.v3 - L.v3; dp = R.p - L.p;
+    tmp = 0.5 / (rc * rc);
+    rdc = RoeDens * rc * du;
+    A0 = tmp * (dp - rdc);
+    A1 = dr - dp * (2.0 * tmp);
+    A2 = RoeDens * dv;
+    A3 = RoeDens * dw;
+    A4 = tmp * (dp + rdc);
+    auto fix = [](double a, double al, double ar) {
+      const double da = fmax(0.0, fmax(a - al, ar - a));
+      const double aa = fabs(a);
+      return (aa < da) ? 0.5 * (a * a / da + da) : aa;
+    };
+    e0 = fix(a0, L.v1 - cL, R.v1 - cR);
+    e1 = fix(a1, L.v1, R.v1);
+    e4 = fix(a4, L.v1 + cL, R.v1 + cR);
+  }
+  const double w0 = A0 * e0, w1 = A1 * e1, w2 = A2 * e1, w3 = A3 * e1, w4 = A4 * e4;
+  const double Ssum = w0 + w1 + w4;
+  // reverse of D
+  double w0b = 0, w1b = 0, w2b = 0, w3b = 0, w4b = 0, a0b = 0, a1b = 0, a4b = 0, r1vb = 0, r2vb = 0, r3vb = 0, rHb = 0, rcb = 0, absb = 0;
+  double Sb = Db[0];
+  w0b += Db[1] * a0; a0b += Db[1] * w0; w1b += Db[1] * r1v; r1vb += Db[1] * w1; w4b += Db[1] * a4; a4b += Db[1] * w4;
+  Sb += Db[2] * r2v; r2vb += Db[2] * Ssum; w2b += Db[2];
+  Sb += Db[3] * r3v; r3vb += Db[3] * Ssum; w3b += Db[3];
+  w0b += Db[4] * (rH - r1v * rc); rHb += Db[4] * (w0 + w4); r1vb += Db[4] * rc * (w4 - w0); rcb += Db[4] * r1v * (w4 - w0);
+  w1b += Db[4] * (0.5 * absVel); absb += Db[4] * 0.5 * w1;
+  w2b += Db[4] * r2v; r2vb += Db[4] * w2; w3b += Db[4] * r3v; r3vb += Db[4] * w3;
+  w4b += Db[4] * (rH + r1v * rc);
+  w0b += Sb; w1b += Sb; w4b += Sb;
+  double A0b = w0b * e0, A1b = w1b * e1, A2b = w2b * e1, A3b = w3b * e1, A4b = w4b * e4;
+  const double e0b = w0b * A0, e1b = w1b * A1 + w2b * A2 + w3b * A3, e4b = w4b * A4;
+  if (solver == RIEMANN_ROE) {
+    a0b += e0b * sgn1(a0); a1b += e1b * sgn1(a1); a4b += e4b * sgn1(a4);
+    double d0b = 0, d1b = 0, d2b = 0, d3b = 0, d4b = 0, d5b = 0, srcb = 0;
+    // A4 = d0 - A0 - A1
+    d0b += A4b; A0b -= A4b; A1b -= A4b;
+    // A0 = 1/2 src X, X = d0 (r1v + rc) - d1 - rc A1
+    const double X = d0 * (r1v + rc) - d1 - rc * A1;
+    srcb += A0b * 0.5 * X;
+    const double Xb = A0b * 0.5 * src;
+    d0b += Xb * (r1v + rc); r1vb += Xb * d0; rcb += Xb * (d0 - A1); d1b -= Xb; A1b -= Xb * rc;
+    // A1 = kappaM1 src^2 Y, Y = d0 (rH - r1v^2) - d5 + r1v d1
+    const double Y = d0 * (rH - r1v * r1v) - d5 + r1v * d1;
+    srcb += A1b * B.kappaM1 * 2.0 * src * Y;
+    const double Yb = A1b * B.kappaM1 * src * src;
+    d0b += Yb * (rH - r1v * r1v); rHb += Yb * d0; r1vb += Yb * (d1 - 2.0 * r1v * d0); d5b -= Yb; d1b += Yb * r1v;
+    rcb -= srcb * src * src;
+    // d5 = d4 - A2 r2v - A3 r3v
+    d4b += d5b; A2b -= d5b * r2v; r2vb -= d5b * A2; A3b -= d5b * r3v; r3vb -= d5b * A3;
+    // A2 = d2 - r2v d0, A3 = d3 - r3v d0
+    d2b += A2b; r2vb -= A2b * d0; d0b -= A2b * r2v;
+    d3b += A3b; r3vb -= A3b * d0; d0b -= A3b * r3v;
+    // differences
+    Rb.rho += d0b + d1b * R.v1 + d2b * R.v2 + d3b * R.v3;
+    Lb.rho -= d0b + d1b * L.v1 + d2b * L.v2 + d3b * L.v3;
+    Rb.v1 += d1b * R.rho; Lb.v1 -= d1b * L.rho;
+    Rb.v2 += d2b * R.rho; Lb.v2 -= d2b * L.rho;
+    Rb.v3 += d3b * R.rho; Lb.v3 -= d3b * L.rho;
+    Rb.E += d4b; Lb.E -= d4b;
+  } else {
+    double alb = 0, arb = 0;
+    double cLb = 0, cRb = 0;
+    entropy_fix_adj(a0, L.v1 - cL, R.v1 - cR, e0b, a0b, alb, arb);
+    Lb.v1 += alb; cLb -= alb; Rb.v1 += arb; cRb -= arb;
+    alb = arb = 0;
+    entropy_fix_adj(a1, L.v1, R.v1, e1b, a1b, alb, arb);
+    Lb.v1 += alb; Rb.v1 += arb;
+    alb = arb = 0;
+    entropy_fix_adj(a4, L.v1 + cL, R.v1 + cR, e4b, a4b, alb, arb);
+    Lb.v1 += alb; cLb += alb; Rb.v1 += arb; cRb += arb;
+    // strengths
+    const double tmpb = A0b * (dp - rdc) - 2.0 * A1b * dp + A4b * (dp + rdc);
+    const double dpb = (A0b - 2.0 * A1b + A4b) * tmp;
+    const double rdcb = (A4b - A0b) * tmp;
+    const double drb = A1b;
+    const double RoeDensb = A2b * dv + A3b * dw + rdcb * rc * du;
+    const double dvb = A2b * RoeDens, dwb = A3b * RoeDens;
+    rcb += rdcb * RoeDens * du - tmpb / (rc * rc * rc);
+    const double dub = rdcb * RoeDens * rc;
+    Rb.rho += drb; Lb.rho -= drb;
+    Rb.v1 += dub; Lb.v1 -= dub;
+    Rb.v2 += dvb; Lb.v2 -= dvb;
+    Rb.v3 += dwb; Lb.v3 -= dwb;
+    Rb.p += dpb; Lb.p -= dpb;
+    // RoeDens = sqL sqR handled with the Roe averages below through sqLb/sqRb
+    // c = sqrt(kappa p srho)
+    Lb.p += cLb * B.kappa * L.srho / (2.0 * cL); Lb.srho += cLb * B.kappa * L.p / (2.0 * cL);
+    Rb.p += cRb * B.kappa * R.srho / (2.0 * cR); Rb.srho += cRb * B.kappa * R.p / (2.0 * cR);
+    // stash RoeDens bar into the square-root bars
+    // (applied below)
+    HLb += 0.0;
+    // eigenvalue bars
+    r1vb += a0b + a1b + a4b;
+    rcb += a4b - a0b;
+    // Roe averages reverse (shared with Roe), plus RoeDens
+    double ssqb = 0, sqLb = RoeDensb * sqR, sqRb = RoeDensb * sqL;
+    const double Zb = rcb / (2.0 * rc);
+    rHb += B.kappaM1 * Zb;
+    absb -= 0.5 * B.kappaM1 * Zb;
+    r1vb += 2.0 * r1v * absb; r2vb += 2.0 * r2v * absb; r3vb += 2.0 * r3v * absb;
+    ssqb += rHb * (sqR * HR + sqL * HL) + r1vb * (sqR * R.v1 + sqL * L.v1) + r2vb * (sqR * R.v2 + sqL * L.v2) + r3vb * (sqR * R.v3 + sqL * L.v3);
+    sqRb += (rHb * HR + r1vb * R.v1 + r2vb * R.v2 + r3vb * R.v3) * ssq;
+    sqLb += (rHb * HL + r1vb * L.v1 + r2vb * L.v2 + r3vb * L.v3) * ssq;
+    HRb += rHb * sqR * ssq; HLb += rHb * sqL * ssq;
+    Rb.v1 += r1vb * sqR * ssq; Lb.v1 += r1vb * sqL * ssq;
+    Rb.v2 += r2vb * sqR * ssq; Lb.v2 += r2vb * sqL * ssq;
+    Rb.v3 += r3vb * sqR * ssq; Lb.v3 += r3vb * sqL * ssq;
+    sqLb -= ssqb * ssq * ssq; sqRb -= ssqb * ssq * ssq;
+    Lb.rho += sqLb / (2.0 * sqL); Rb.rho += sqRb / (2.0 * sqR);
+    enthalpy_adj(L, HLb, Lb);
+    enthalpy_adj(R, HRb, Rb);
+    return;
+  }
+  // Roe: eigenvalue bars and Roe averages reverse
+  r1vb += a0b + a1b + a4b;
+  rcb += a4b - a0b;
+  double ssqb = 0, sqLb = 0, sqRb = 0;
+  const double Zb = rcb / (2.0 * rc);
+  rHb += B.kappaM1 * Zb;
+  absb -= 0.5 * B.kappaM1 * Zb;
+  r1vb += 2.0 * r1v * absb; r2vb += 2.0 * r2v * absb; r3vb += 2.0 * r3v * absb;
+  ssqb += rHb * (sqR * HR + sqL * HL) + r1vb * (sqR * R.v1 + sqL * L.v1) + r2vb * (sqR * R.v2 + sqL * L.v2) + r3vb * (sqR * R.v3 + sqL * L.v3);
+  sqRb += (rHb * HR + r1vb * R.v1 + r2vb * R.v2 + r3vb * R.v3) * ssq;
+  sqLb += (rHb * HL + r1vb * L.v1 + r2vb * L.v2 + r3vb * L.v3) * ssq;
+  HRb += rHb * sqR * ssq; HLb += rHb * sqL * ssq;
+  Rb.v1 += r1vb * sqR * ssq; Lb.v1 += r1vb * sqL * ssq;
+  Rb.v2 += r2vb * sqR * ssq; Lb.v2 += r2vb * sqL * ssq;
+  Rb.v3 += r3vb * sqR * ssq; Lb.v3 += r3vb * sqL * ssq;
+  sqLb -= ssqb * ssq * ssq; sqRb -= ssqb * ssq * ssq;
+  Lb.rho += sqLb / (2.0 * sqL); Rb.rho += sqRb / (2.0 * sqR);
+  enthalpy_adj(L, HLb, Lb);
+  enthalpy_adj(R, HRb, Rb);
+}
+
+// eos.f90:PRESSURE_RIEMANN: adds the bars of rho, vn, p for the bar of the boundary pressure
+FG_HD void pressure_riemann_adj(const Basis& B, double rho, double vn, double p, double pbb, double& rhob, double& vnb, double& pb) {
+  if (vn <= 0.0) {
+    const double c = sqrt(B.kappa * p / rho);
+    const double raw = 1.0 + 0.5 * B.kappaM1 * vn / c;
+    const double base = fmax(0.0001, raw);
+    pb += pbb * pow(base, B.kappaFac);
+    const double baseb = pbb * p * B.kappaFac * pow(base, B.kappaFac - 1.0);
+    if (raw >= 0.0001) {
+      vnb += baseb * 0.5 * B.kappaM1 / c;
+      const double cb = -baseb * 0.5 * B.kappaM1 * vn / (c * c);
+      pb += cb * B.kappa / (2.0 * c * rho);
+      rhob -= cb * B.kappa * p / (2.0 * c * rho * rho);
+    }
+    return;
+  }
+  const double ar = 2.0 * B.sKappaP1 / rho;
+  const double br = B.kappaM1 * B.sKappaP1 * p;
+  const double Z = vn * vn + 4.0 * ar * (p + br);
+  const double Q = sqrt(Z);
+  // pb = p + vn / ar * 0.5 * (vn + Q)
+  const double K = vn / ar * 0.5;
+  pb += pbb;
+  const double Kb = pbb * (vn + Q);
+  vnb += pbb * K;
+  const double Qb = pbb * K;
+  vnb += Kb * 0.5 / ar;
+  double arb = -Kb * 0.5 * vn / (ar * ar);
+  const double Zb = Qb / (2.0 * Q);
+  vnb += 2.0 * vn * Zb;
+  arb += 4.0 * (p + br) * Zb;
+  pb += 4.0 * ar * Zb;
+  const double brb = 4.0 * ar * Zb;
+  pb += brb * B.kappaM1 * B.sKappaP1;
+  rhob -= arb * 2.0 * B.sKappaP1 / (rho * rho);
+}
+
+}  // namespace fg

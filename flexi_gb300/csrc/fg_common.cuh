@@ -113,7 +113,7 @@ __host__ __device__ inline int side_dir(int ls) {  // 0 xi, 1 eta, 2 zeta
 // ------------------------------------------------------------------------------------------------------
 // Viscous flux (flux.f90:EvalDiffFlux3D_Point, stored with the minus sign), contracted with a direction
 // vector m: F = m1*f + m2*g + m3*h. g[4*d+v] = d/dx_d of (u,v,w,T). Returns F[1..4] (F[0] = 0).
-__device__ __forceinline__ void visc_flux_dir(double mu, double lam, double u, double v, double w, const double* g,
+__host__ __device__ __forceinline__ void visc_flux_dir(double mu, double lam, double u, double v, double w, const double* g,
                                               double m1, double m2, double m3, double* F) {
   // tau terms (s43 = 4/3, s23 = 2/3): tau_xx = mu*(4/3 ux - 2/3 (vy + wz)) = mu*(2 ux - 2/3 div)
   const double div = g[0] + g[5] + g[10];
@@ -141,7 +141,7 @@ struct RotState {
 };
 
 // Central split surface flux (splitflux.f90:SplitSurfaceFluxPI / SD) on rotated states.
-__device__ __forceinline__ void split_surface_flux(int splitDG, const RotState& L, const RotState& R, double HL, double HR, double* F) {
+__host__ __device__ __forceinline__ void split_surface_flux(int splitDG, const RotState& L, const RotState& R, double HL, double HR, double* F) {
   if (splitDG == 4) {
     const double rs = L.rho + R.rho, us = L.v1 + R.v1;
     const double a = rs * us;
@@ -161,7 +161,7 @@ __device__ __forceinline__ void split_surface_flux(int splitDG, const RotState& 
   }
 }
 
-__device__ __forceinline__ void euler_flux_1d(const RotState& S, double* F) {
+__host__ __device__ __forceinline__ void euler_flux_1d(const RotState& S, double* F) {
   const double m = S.rho * S.v1;
   F[0] = m;
   F[1] = m * S.v1 + S.p;
@@ -172,7 +172,7 @@ __device__ __forceinline__ void euler_flux_1d(const RotState& S, double* F) {
 
 // Riemann solvers of riemann.f90 (LF :558, HLLC :594, Roe :668, RoeEntropyFix :748) on rotated states.
 // split != 0: central part from the split surface flux (SPLIT_DG builds), as the reference does.
-__device__ __forceinline__ void riemann_rotated(int solver, int splitDG, const Basis& B, const RotState& L, const RotState& R, double* F) {
+__host__ __device__ __forceinline__ void riemann_rotated(int solver, int splitDG, const Basis& B, const RotState& L, const RotState& R, double* F) {
   const bool split = splitDG >= 0;
   const double HL = (L.E + L.p) * L.srho, HR = (R.E + R.p) * R.srho;
   if (solver == RIEMANN_LF) {
@@ -292,7 +292,7 @@ __device__ __forceinline__ void riemann_rotated(int solver, int splitDG, const B
 }
 
 // eos.f90:PRESSURE_RIEMANN on the rotated boundary state (v1 = normal velocity)
-__device__ __forceinline__ double pressure_riemann(const Basis& B, double rho, double vn, double p) {
+__host__ __device__ __forceinline__ double pressure_riemann(const Basis& B, double rho, double vn, double p) {
   if (vn <= 0.0) {
     const double base = fmax(0.0001, 1.0 + 0.5 * B.kappaM1 * vn / sqrt(B.kappa * p / rho));
     return p * pow(base, B.kappaFac);

@@ -1,0 +1,76 @@
+// flexi_gb300 -- host-side harness for the point-wise physics and its adjoints (built as libfgpoint.so).
+//
+// Exposes the __host__ __device__ functions of fg_common.cuh and fg_adjoint_point.cuh through plain C
+// entry points so that the CPU test suite can check every transposed Jacobian against central finite
+// differences of the very same forward code. Not part of the solver library.
+#include "fg_adjoint_point.cuh"
+
+using namespace fg;
+
+namespace {
+Basis gas(double kappa, double R) {
+  Basis B{};
+  B.kappa = kappa; B.kappaM1 = kappa - 1.0; B.sKappaM1 = 1.0 / (kappa - 1.0);
+  B.Rgas = R; B.sR = 1.0 / R;
+  B.kappaFac = 2.0 * kappa / (kappa - 1.0);
+  B.sKappaP1 = 1.0 / (kappa + 1.0);
+  return B;
+}
+RotState rs(const double* a) { RotState S; S.rho = a[0]; S.srho = a[1]; S.E = a[2]; S.p = a[3]; S.v1 = a[4]; S.v2 = a[5]; S.v3 = a[6]; return S; }
+void rs_out(const RotState& S, double* a) { a[0] = S.rho; a[1] = S.srho; a[2] = S.E; a[3] = S.p; a[4] = S.v1; a[5] = S.v2; a[6] = S.v3; }
+}  // namespace
+
+extern "C" {
+
+// U[5] -> (srho, u, v, w, p, T)
+void fgpt_cons_to_prim(double kappa, double R, const double* U, double* out) {
+  const Basis B = gas(kappa, R);
+  const double srho = 1.0 / U[0];
+  const double vx = U[1] * srho, vy = U[2] * srho, vz = U[3] * srho;
+  const double p = B.kappaM1 * (U[4] - 0.5 * (U[1] * vx + U[2] * vy + U[3] * vz));
+  out[0] = srho; out[1] = vx; out[2] = vy; out[3] = vz; out[4] = p; out[5] = p * srho * B.sR;
+}
+// bar[8] = bars of (srho, u, v, w, p, T, rho_direct, E_direct) -> Ub[5]
+void fgpt_cons_to_prim_adj(double kappa, double R, const double* U, const double* bar, double* Ub) {
+  const Basis B = gas(kappa, R);
+  for (int v = 0; v < 5; ++v) Ub[v] = 0.0;
+  cons_to_prim_adj(B, U, bar[0], bar[1], bar[2], bar[3], bar[4], bar[5], bar[6], bar[7], Ub);
+}
+
+// x = (u, v, w, g[12], mu), m[3]: F[1..4] -> out[4]
+void fgpt_visc(double lamFac, const double* x, const double* m, double* out) {
+  double F[5];
+  visc_flux_dir(x[15], x[15] * lamFac, x[0], x[1], x[2], x + 3, m[0], m[1], m[2], F);
+  for (int v = 0; v < 4; ++v) out[v] = F[1 + v];
+}
+void fgpt_visc_adj(double lamFac, const double* x, const double* m, const double* Fb4, double* xb) {
+  double Fb[5] = {0.0, Fb4[0], Fb4[1], Fb4[2], Fb4[3]};
+  for (int c = 0; c < 16; ++c) xb[c] = 0.0;
+  visc_flux_dir_adj(x[15], lamFac, x[0], x[1], x[2], x + 3, m[0], m[1], m[2], Fb, xb[0], xb[1], xb[2], xb + 3, xb[15]);
+}
+
+// L[7], R[7] = (rho, srho, E, p, v1, v2, v3) -> F[5]
+void fgpt_riemann(int solver, int splitDG, double kappa, double R, const double* L, const double* Rr, double* F) {
+  const Basis B = gas(kappa, R);
+  riemann_rotated(solver, splitDG, B, rs(L), rs(Rr), F);
+}
+void fgpt_riemann_adj(int solver, int splitDG, double kappa, double R, const double* L, const double* Rr, const double* Fb, double* Lb, double* Rb) {
+  const Basis B = gas(kappa, R);
+  RotState lb, rb;
+  rot_zero(lb); rot_zero(rb);
+  riemann_rotated_adj(solver, splitDG, B, rs(L), rs(Rr), Fb, lb, rb);
+  rs_out(lb, Lb); rs_out(rb, Rb);
+}
+
+// x = (rho, vn, p) -> boundary pressure
+double fgpt_pressure_riemann(double kappa, double R, const double* x) {
+  const Basis B = gas(kappa, R);
+  return pressure_riemann(B, x[0], x[1], x[2]);
+}
+void fgpt_pressure_riemann_adj(double kappa, double R, const double* x, double pbb, double* xb) {
+  const Basis B = gas(kappa, R);
+  xb[0] = xb[1] = xb[2] = 0.0;
+  pressure_riemann_adj(B, x[0], x[1], x[2], pbb, xb[0], xb[1], xb[2]);
+}
+
+}  // extern "C"

@@ -1,0 +1,159 @@
+"""Point-wise adjoints (fg_adjoint_point.cuh) against central finite differences of the same forward code.
+
+Runs on the CPU through libfgpoint.so, the point-wise functions compiled as host code. For random
+physical states x, random output cotangents yb and random directions dx, the adjoint gives xb = J^T yb
+and the test compares <xb, dx> with <yb, (f(x + h dx) - f(x - h dx)) / 2h>, Richardson-extrapolated
+from h and 2h. Samples whose finite
+difference straddles a branch of the forward function (entropy fix, max, abs, pressure clamp) are
+recognised by two step sizes disagreeing and skipped; the test asserts that most samples are kept."""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+from flexi_gb300 import build as fbuild
+
+KAPPA, RGAS = 1.4, 287.058
+TOL = 2e-7
+
+
+@pytest.fixture(scope="module")
+def pt():
+    path = fbuild.build_point_harness()
+    L = ctypes.CDLL(path)
+    D, I, P = ctypes.c_double, ctypes.c_int, ctypes.c_void_p
+    L.fgpt_cons_to_prim.argtypes = [D, D, P, P]
+    L.fgpt_cons_to_prim_adj.argtypes = [D, D, P, P, P]
+    L.fgpt_visc.argtypes = [D, P, P, P]
+    L.fgpt_visc_adj.argtypes = [D, P, P, P, P]
+    L.fgpt_riemann.argtypes = [I, I, D, D, P, P, P]
+    L.fgpt_riemann_adj.argtypes = [I, I, D, D, P, P, P, P, P]
+    L.fgpt_pressure_riemann.argtypes = [D, D, P]
+    L.fgpt_pressure_riemann.restype = D
+    L.fgpt_pressure_riemann_adj.argtypes = [D, D, P, D, P]
+    return L
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _check(f, fadj, x, nout, rng, n_dirs=3):
+    """Returns the worst relative mismatch over a few directions, or None if a branch was crossed."""
+    worst = 0.0
+    for _ in range(n_dirs):
+        yb = rng.standard_normal(nout)
+        dx = rng.standard_normal(x.size) * np.maximum(np.abs(x), 1e-3)
+        xb = fadj(x, yb)
+        lhs = float(xb @ dx)
+        fd = []
+        for h in (1e-5, 2e-5):
+            fd.append(float(yb @ (f(x + h * dx) - f(x - h * dx)) / (2 * h)))
+        rich = (4.0 * fd[0] - fd[1]) / 3.0  # Richardson: O(h^4)
+        scale = max(abs(lhs), abs(rich), 1e-8 * (np.abs(xb).sum() * np.abs(dx).max() + 1e-300))
+        if abs(fd[0] - fd[1]) > 1e-4 * scale:
+            return None
+        worst = max(worst, abs(lhs - rich) / scale)
+    return worst
+
+
+def _state(rng, vmax=1.0):
+    rho = rng.uniform(0.5, 2.0)
+    v = rng.uniform(-vmax, vmax, 3)
+    p = rng.uniform(0.5, 3.0)
+    E = p / (KAPPA - 1) + 0.5 * rho * (v @ v)
+    return np.array([rho, 1.0 / rho, E, p, v[0], v[1], v[2]])
+
+
+def test_cons_to_prim_adjoint(pt):
+    rng = np.random.default_rng(1)
+
+    def f(U):
+        out = np.empty(6)
+        pt.fgpt_cons_to_prim(KAPPA, RGAS, _p(U), _p(out))
+        return np.concatenate([out, [U[0], U[4]]])  # face states also carry rho and E directly
+
+    def fadj(U, yb):
+        Ub = np.empty(5)
+        pt.fgpt_cons_to_prim_adj(KAPPA, RGAS, _p(U), _p(np.ascontiguousarray(yb)), _p(Ub))
+        return Ub
+
+    for _ in range(50):
+        s = _state(rng)
+        U = np.array([s[0], s[0] * s[4], s[0] * s[5], s[0] * s[6], s[2]])
+        err = _check(f, fadj, U, 8, rng)
+        assert err is not None and err < TOL, err
+
+
+def test_viscous_flux_adjoint(pt):
+    rng = np.random.default_rng(2)
+    lamfac = RGAS * KAPPA / (KAPPA - 1) / 0.72
+    for _ in range(50):
+        x = np.concatenate([rng.uniform(-1, 1, 3), rng.standard_normal(12), [rng.uniform(1e-4, 1e-2)]])
+        m = rng.standard_normal(3)
+
+        def f(x):
+            out = np.empty(4)
+            pt.fgpt_visc(lamfac, _p(x), _p(m), _p(out))
+            return out
+
+        def fadj(x, yb):
+            xb = np.empty(16)
+            pt.fgpt_visc_adj(lamfac, _p(x), _p(m), _p(np.ascontiguousarray(yb)), _p(xb))
+            return xb
+
+        err = _check(f, fadj, x, 4, rng)
+        assert err is not None and err < TOL, err
+
+
+@pytest.mark.parametrize("solver", [1, 3, 33])
+@pytest.mark.parametrize("split", [-1, 4, 0])
+def test_riemann_adjoint(pt, solver, split):
+    rng = np.random.default_rng(10 * solver + split + 5)
+    kept, n = 0, 120
+    for it in range(n):
+        L, R = _state(rng, vmax=1.6), _state(rng, vmax=1.6)
+        x = np.concatenate([L, R])
+
+        def f(x):
+            F = np.empty(5)
+            pt.fgpt_riemann(solver, split, KAPPA, RGAS, _p(np.ascontiguousarray(x[:7])), _p(np.ascontiguousarray(x[7:])), _p(F))
+            return F
+
+        def fadj(x, yb):
+            Lb, Rb = np.empty(7), np.empty(7)
+            pt.fgpt_riemann_adj(solver, split, KAPPA, RGAS, _p(np.ascontiguousarray(x[:7])), _p(np.ascontiguousarray(x[7:])),
+                                _p(np.ascontiguousarray(yb)), _p(Lb), _p(Rb))
+            return np.concatenate([Lb, Rb])
+
+        err = _check(f, fadj, x, 5, rng)
+        if err is None:
+            continue
+        kept += 1
+        assert err < TOL, (it, err)
+    assert kept >= 0.8 * n
+
+
+def test_pressure_riemann_adjoint(pt):
+    rng = np.random.default_rng(3)
+    kept = 0
+    for it in range(100):
+        rho, p = rng.uniform(0.5, 2.0), rng.uniform(0.5, 3.0)
+        vn = rng.uniform(-1.5, 1.5)
+        x = np.array([rho, vn, p])
+
+        def f(x):
+            return np.array([pt.fgpt_pressure_riemann(KAPPA, RGAS, _p(np.ascontiguousarray(x)))])
+
+        def fadj(x, yb):
+            xb = np.empty(3)
+            pt.fgpt_pressure_riemann_adj(KAPPA, RGAS, _p(np.ascontiguousarray(x)), float(yb[0]), _p(xb))
+            return xb
+
+        err = _check(f, fadj, x, 1, rng)
+        if err is None:
+            continue
+        kept += 1
+        assert err < TOL, (it, err)
+    assert kept >= 90
