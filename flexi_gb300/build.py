@@ -17,7 +17,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU = ["fg_host.cu", "fg_noalloc.cu"] + [f"fg_inst_n{n}.cu" for n in range(2, 9)]
 CPP = ["fg_mesh.cpp"]
-HEADERS = ["fg_common.cuh", "fg_kernels.cuh", "fg_launch.cuh", "fg_inst.cuh", "fg_basis.hpp", "fg_mesh.hpp", "fg_adjoint_point.cuh"]
+HEADERS = ["fg_common.cuh", "fg_kernels.cuh", "fg_launch.cuh", "fg_inst.cuh", "fg_basis.hpp", "fg_mesh.hpp", "fg_adjoint_point.cuh", "fg_adjoint.cuh"]
 # host-only harness of the point-wise physics and its adjoints, for the CPU tests
 POINT_SRC = "fg_point_test.cu"
 POINT_LIB = os.path.join(OUT, "libfgpoint.so")

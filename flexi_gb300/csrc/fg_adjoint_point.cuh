@@ -69,6 +69,38 @@ FG_HD void visc_flux_dir_adj(double mu, double lamFac, double u, double v, doubl
   gb[9] += mu * tyzb; gb[6] += mu * tyzb;
 }
 
+// Physical viscous fluxes f, g, h (flux.f90:EvalDiffFlux3D_Point, components 1..4 of each, with the minus
+// sign) at one node: given their bars fb, gb_, hb (index 1..4 used), adds the velocity bars, the gradient
+// bars and the viscosity bar (lam = mu * lamFac).
+FG_HD void visc_flux_phys_adj(double mu, double lamFac, double u, double v, double w, const double* g, const double* fb, const double* gyb,
+                              const double* hb, double& ub, double& vb, double& wb, double* gb, double& mub) {
+  const double lam = mu * lamFac;
+  const double div = g[0] + g[5] + g[10];
+  const double mdiv = (2.0 / 3.0) * div;
+  const double sxx = 2.0 * g[0] - mdiv, syy = 2.0 * g[5] - mdiv, szz = 2.0 * g[10] - mdiv;
+  const double sxy = g[4] + g[1], sxz = g[8] + g[2], syz = g[9] + g[6];
+  const double txx = mu * sxx, tyy = mu * syy, tzz = mu * szz, txy = mu * sxy, txz = mu * sxz, tyz = mu * syz;
+  // f = (-txx, -txy, -txz, -(txx u + txy v + txz w) - lam Tx), g = (-txy, -tyy, -tyz, ...), h = (-txz, -tyz, -tzz, ...)
+  const double txxb = -fb[1] - fb[4] * u;
+  const double tyyb = -gyb[2] - gyb[4] * v;
+  const double tzzb = -hb[3] - hb[4] * w;
+  const double txyb = -fb[2] - gyb[1] - fb[4] * v - gyb[4] * u;
+  const double txzb = -fb[3] - hb[1] - fb[4] * w - hb[4] * u;
+  const double tyzb = -gyb[3] - hb[2] - gyb[4] * w - hb[4] * v;
+  ub -= fb[4] * txx + gyb[4] * txy + hb[4] * txz;
+  vb -= fb[4] * txy + gyb[4] * tyy + hb[4] * tyz;
+  wb -= fb[4] * txz + gyb[4] * tyz + hb[4] * tzz;
+  const double lamb = -(fb[4] * g[3] + gyb[4] * g[7] + hb[4] * g[11]);
+  gb[3] -= fb[4] * lam; gb[7] -= gyb[4] * lam; gb[11] -= hb[4] * lam;
+  mub += txxb * sxx + tyyb * syy + tzzb * szz + txyb * sxy + txzb * sxz + tyzb * syz + lamb * lamFac;
+  const double sxxb = mu * txxb, syyb = mu * tyyb, szzb = mu * tzzb;
+  const double divb = -(2.0 / 3.0) * (sxxb + syyb + szzb);
+  gb[0] += 2.0 * sxxb + divb; gb[5] += 2.0 * syyb + divb; gb[10] += 2.0 * szzb + divb;
+  gb[4] += mu * txyb; gb[1] += mu * txyb;
+  gb[8] += mu * txzb; gb[2] += mu * txzb;
+  gb[9] += mu * tyzb; gb[6] += mu * tyzb;
+}
+
 FG_HD void rot_zero(RotState& S) { S.rho = S.srho = S.E = S.p = S.v1 = S.v2 = S.v3 = 0.0; }
 
 FG_HD void euler_flux_1d_adj(const RotState& S, const double* Fb, RotState& Sb) {

@@ -67,9 +67,16 @@ struct Dev {
   double* dt;      // [nInst]
   double* bulkVel; // [nInst]
   double* dpdx;    // [nInst] (0 when no body force)
+  double* muScale; // [nElems] viscosity multiplier of each element (null: 1)
   int* err;        // [1] sticky error word
   double* dtElem;  // [2][nElems] convective and viscous element time-step limits of the last CALCTIMESTEP
 };
+
+// viscosity of element e: its instance's mu0 times its multiplier
+__host__ __device__ inline double elem_mu(const Dev& d, int e) {
+  const double m = d.mu0[d.elemInst[e]];
+  return d.muScale ? m * d.muScale[e] : m;
+}
 
 // ------------------------------------------------------------------------------------------------------
 // orientation maps (mappings.f90: Flip_S2M, CGNS_SideToVol2) -- integer work, free next to FP64

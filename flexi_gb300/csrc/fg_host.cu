@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../../include/flexi_gpu.h"
+#include "fg_adjoint.cuh"
 #include "fg_common.cuh"
 #include "fg_launch.cuh"
 #include "fg_mesh.hpp"
@@ -123,6 +124,9 @@ struct fg_handle {
   long long launches = 0;
   std::string err;
   std::vector<double> instMu0;
+  // adjoint buffers (allocated on the first fg_rhs_vjp)
+  AdjDev a{};
+  bool haveAdj = false;
   // per-kernel event timing (fg_profile_enable)
   bool profiling = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> evPool;
@@ -171,6 +175,8 @@ void free_device(fg_handle* h) {
   for (auto& b : h->bufs) cudaFree(b.p);
   h->bufs.clear();
   h->haveMesh = false;
+  h->haveAdj = false;
+  h->a = AdjDev{};
 }
 
 void init_basis(fg_handle* h) {
@@ -282,6 +288,7 @@ int upload_mesh(fg_handle* h) {
   if ((r = upload(h, d.bulkVel, zero))) return r;
   if ((r = upload(h, d.dpdx, dp))) return r;
   if ((r = upload(h, d.err, std::vector<int>(1, 0)))) return r;
+  if ((r = upload(h, d.muScale, std::vector<double>(nE, 1.0)))) return r;
   if ((r = dalloc(h, d.dtElem, (size_t)2 * nE))) return r;
   if ((r = upload(h, h->dMetAdv, M.metAdv))) return r;
   if ((r = upload(h, h->dMetVisc, M.metVisc))) return r;
@@ -394,6 +401,59 @@ std::string trim(const std::string& s) {
 namespace fg {
 void set_error_without_handle(const char* msg) { g_err = msg; }
 }  // namespace fg
+
+namespace {
+
+// the adjoint kernels cover: weak form and split form PI, LF/Roe/RoeEntropyFix, BR1/BR2
+const char* adjoint_unsupported(const fg_config& c) {
+  if (c.SplitDG != FG_SPLIT_NONE && c.SplitDG != FG_SPLIT_PI) return "the adjoint supports the weak form and the split form PI";
+  if (c.Riemann != FG_RIEMANN_LF && c.Riemann != FG_RIEMANN_ROE && c.Riemann != FG_RIEMANN_ROEENTROPYFIX)
+    return "the adjoint supports the LF, Roe and RoeEntropyFix surface fluxes";
+  return nullptr;
+}
+
+int ensure_adjoint(fg_handle* h) {
+  if (h->haveAdj) return 0;
+  const int n = h->M.n, n2 = n * n, n3 = n2 * n, nE = h->M.nElems, nS = h->M.nSides;
+  AdjDev& a = h->a;
+  double* W = nullptr;
+  int r = 0;
+  if ((r = dalloc(h, W, (size_t)nE * 5 * n3))) return r;
+  a.W = W;
+  if ((r = dalloc(h, a.Ub, (size_t)nE * 5 * n3))) return r;
+  if ((r = dalloc(h, a.gb, (size_t)nE * 12 * n3))) return r;
+  if ((r = dalloc(h, a.fluxb, (size_t)nS * 2 * 5 * n2))) return r;
+  if ((r = dalloc(h, a.faceMb, (size_t)nS * FS_NF * n2))) return r;
+  if ((r = dalloc(h, a.faceSb, (size_t)nS * FS_NF * n2))) return r;
+  if ((r = dalloc(h, a.gradMb, (size_t)nS * 12 * n2))) return r;
+  if ((r = dalloc(h, a.gradSb, (size_t)nS * 12 * n2))) return r;
+  if ((r = dalloc(h, a.liftb, (size_t)nS * 2 * 4 * n2))) return r;
+  if ((r = dalloc(h, a.muSideb, (size_t)nS * 2 * n2))) return r;
+  if ((r = dalloc(h, a.muElemb, (size_t)nE))) return r;
+  // entries no kernel writes (slave slots of boundary sides) stay zero
+  CUDA_TRY(cudaMemset(a.faceSb, 0, sizeof(double) * nS * FS_NF * n2));
+  CUDA_TRY(cudaMemset(a.gradSb, 0, sizeof(double) * nS * 12 * n2));
+  CUDA_TRY(cudaMemset(a.liftb, 0, sizeof(double) * nS * 2 * 4 * n2));
+  CUDA_TRY(cudaMemset(a.fluxb, 0, sizeof(double) * nS * 2 * 5 * n2));
+  CUDA_TRY(cudaMemset(a.muSideb, 0, sizeof(double) * nS * 2 * n2));
+  h->haveAdj = true;
+  return 0;
+}
+
+// V = (dUt/dU)^T W at d.U, W already in h->a.W; leaves V in h->a.Ub and the viscosity-multiplier
+// cotangent in h->a.muElemb
+void launch_vjp(fg_handle* h) {
+  const Dev& d = h->d;
+  h->K.prep(d, h->B, h->st);
+  h->K.lift(d, h->B, h->st);
+  h->K.vol_adj(d, h->a, h->B, h->st);
+  h->K.flux_adj(d, h->a, h->B, h->st);
+  h->K.lift_adj(d, h->a, h->B, h->st);
+  h->K.prep_adj(d, h->a, h->B, h->st);
+  h->launches += 6;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -613,6 +673,37 @@ int fg_time_derivative(fg_handle* h, double t, double* Ut) {
   launch_rhs(h, 0, 0., 0.);
   CUDA_TRY(cudaGetLastError());
   if (Ut) return export_field(h, h->d.Ut, 5, 0, 5, Ut);
+  CUDA_TRY(cudaStreamSynchronize(h->st));
+  return FG_OK;
+}
+
+int fg_set_elem_mu_scale(fg_handle* h, const double* scale) {
+  if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
+  const int nE = h->M.nElems;
+  if (scale) {
+    CUDA_TRY(cudaMemcpy(h->d.muScale, scale, sizeof(double) * nE, cudaMemcpyHostToDevice));
+  } else {
+    k_fill<<<(nE + 127) / 128, 128, 0, h->st>>>(h->d.muScale, 1.0, nE);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(h->st));
+  }
+  return FG_OK;
+}
+
+int fg_rhs_vjp(fg_handle* h, const double* W, double* V, double* muScaleBar) {
+  if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
+  if (!W) return fail(h, FG_ERR_CONFIG, "null cotangent");
+  if (const char* why = adjoint_unsupported(h->cfg)) return fail(h, FG_ERR_CONFIG, why);
+  if (int r = ensure_adjoint(h)) return r;
+  const int n3 = h->M.n * h->M.n * h->M.n;
+  const long long total = (long long)h->M.nElems * 5 * n3;
+  h->launches = 0;
+  CUDA_TRY(cudaMemcpyAsync(h->dStage, W, total * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  k_fortran_to_dev<<<(unsigned)((total + 255) / 256), 256, 0, h->st>>>(h->dStage, const_cast<double*>(h->a.W), 5, n3, total);
+  launch_vjp(h);
+  CUDA_TRY(cudaGetLastError());
+  if (V) { if (int r = export_field(h, h->a.Ub, 5, 0, 5, V)) return r; }
+  if (muScaleBar) CUDA_TRY(cudaMemcpyAsync(muScaleBar, h->a.muElemb, sizeof(double) * h->M.nElems, cudaMemcpyDeviceToHost, h->st));
   CUDA_TRY(cudaStreamSynchronize(h->st));
   return FG_OK;
 }

@@ -1,5 +1,6 @@
 // flexi_gb300 -- launch wrappers for one (n, node type) instantiation; included by fg_inst_n*.cu
 #pragma once
+#include "fg_adjoint.cuh"
 #include "fg_kernels.cuh"
 #include "fg_launch.cuh"
 
@@ -15,6 +16,10 @@ struct Inst {
   }
   static size_t smem_weak() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * (15 * S::n3 + 6 * S::n2 * 5)); }
   static size_t smem_split() { return sizeof(double) * (SBasis<n>::SIZE + 2 * S::n2 + S::EPB * (20 * S::n3 + 6 * S::n2 * 5)); }
+  static size_t smem_weak_adj() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * 5 * S::n3 + S::THREADS); }
+  static size_t smem_split_adj() { return sizeof(double) * (SBasis<n>::SIZE + 2 * S::n2 + S::EPB * 26 * S::n3 + S::THREADS); }
+  static size_t smem_lift_adj() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * (13 * S::n3 + 6 * S::n2 * 19)); }
+  static size_t smem_prep_adj() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * (10 * S::n3 + 6 * S::n2 * 6)); }
   template <class K>
   static void set_smem(K kern, size_t bytes) {
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
@@ -24,6 +29,29 @@ struct Inst {
     set_smem(k_lift<n, GL>, smem_lift());
     set_smem(k_vol_weak<n, GL>, smem_weak());
     if constexpr (GL && (n == 2 || n == 4 || n == 8)) set_smem(k_vol_split<n>, smem_split());
+    set_smem(k_vol_weak_adj<n, GL>, smem_weak_adj());
+    set_smem(k_lift_adj<n, GL>, smem_lift_adj());
+    set_smem(k_prep_adj<n, GL>, smem_prep_adj());
+    if constexpr (GL && (n == 2 || n == 4 || n == 8)) set_smem(k_vol_split_adj<n>, smem_split_adj());
+  }
+  static void vol_adj(const Dev& d, const AdjDev& a, const Basis& B, cudaStream_t st) {
+    if constexpr (GL && (n == 2 || n == 4 || n == 8)) {
+      if (B.splitDG >= 0) {
+        k_vol_split_adj<n><<<blocks(d), S::THREADS, smem_split_adj(), st>>>(d, a, B);
+        return;
+      }
+    }
+    k_vol_weak_adj<n, GL><<<blocks(d), S::THREADS, smem_weak_adj(), st>>>(d, a, B);
+  }
+  static void flux_adj(const Dev& d, const AdjDev& a, const Basis& B, cudaStream_t st) {
+    const long long pts = (long long)d.nSides * S::n2;
+    k_flux_adj<n><<<(unsigned)((pts + 127) / 128), 128, 0, st>>>(d, a, B);
+  }
+  static void lift_adj(const Dev& d, const AdjDev& a, const Basis& B, cudaStream_t st) {
+    k_lift_adj<n, GL><<<blocks(d), S::THREADS, smem_lift_adj(), st>>>(d, a, B);
+  }
+  static void prep_adj(const Dev& d, const AdjDev& a, const Basis& B, cudaStream_t st) {
+    k_prep_adj<n, GL><<<blocks(d), S::THREADS, smem_prep_adj(), st>>>(d, a, B);
   }
   static void prep(const Dev& d, const Basis& B, cudaStream_t st) {
     k_prep<n, GL><<<blocks(d), S::THREADS, smem_prep(), st>>>(d, B);
@@ -53,6 +81,7 @@ struct Inst {
     k.prepare = &prepare;
     k.prep = &prep; k.lift = &lift; k.flux = &flux; k.vol_weak = &vol_weak; k.dt = &dt;
     if (GL && (n == 2 || n == 4 || n == 8)) k.vol_split = &vol_split;
+    k.vol_adj = &vol_adj; k.flux_adj = &flux_adj; k.lift_adj = &lift_adj; k.prep_adj = &prep_adj;
     return k;
   }
 };

@@ -380,7 +380,9 @@ __global__ void __launch_bounds__(128) k_flux(Dev d, Basis B) {
 #pragma unroll
   for (int c = 0; c < 3; ++c) { nv[c] = gm[(FG_NX + c) * n2]; t1[c] = gm[(FG_T1X + c) * n2]; t2[c] = gm[(FG_T2X + c) * n2]; }
   const double se = gm[FG_SURF * n2];
-  const double mu = d.mu0[d.sideInst[s]];
+  // viscosity of each neighbour (its own instance viscosity times its element multiplier)
+  const double mu0s = d.mu0[d.sideInst[s]];
+  const double mu = d.muScale ? mu0s * d.muScale[d.sideElem[s * 4 + 0]] : mu0s;
   const double lam = mu * B.lambdaFac;
   const double* fm = d.faceM + (size_t)s * FS_NF * n2 + pq;
   double gL[12];
@@ -422,8 +424,9 @@ __global__ void __launch_bounds__(128) k_flux(Dev d, Basis B) {
 #pragma unroll
     for (int c = 0; c < 12; ++c) gR[c] = d.gradS[((size_t)s * 12 + c) * n2 + pq];
     double FvL[5], FvR[5];
+    const double muR = d.muScale ? mu0s * d.muScale[d.sideElem[s * 4 + 2]] : mu0s;
     visc_flux_dir(mu, lam, uL, vL, wL, gL, nv[0], nv[1], nv[2], FvL);
-    visc_flux_dir(mu, lam, uR, vR, wR, gR, nv[0], nv[1], nv[2], FvR);
+    visc_flux_dir(muR, muR * B.lambdaFac, uR, vR, wR, gR, nv[0], nv[1], nv[2], FvR);
 #pragma unroll
     for (int v = 1; v < 5; ++v) F[v] += 0.5 * (FvL[v] + FvR[v]);
   }
@@ -540,7 +543,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_weak(Dev d, Basis B, 
     double g[12];
 #pragma unroll
     for (int c = 0; c < 12; ++c) g[c] = d.grad[((size_t)e * 12 + c) * n3 + x];
-    const double mu = d.mu0[d.elemInst[e]];
+    const double mu = elem_mu(d, e);
     const double lam = mu * B.lambdaFac;
     // physical flux (advective + viscous, flux.f90:EvalFlux3D_Point + EvalDiffFlux3D_Point)
     const double div = g[0] + g[5] + g[10];
@@ -741,7 +744,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS, (n == 8 ? 2 : 1)) k_vol_spl
       for (int c = 0; c < 9; ++c) m[c] = Q[(6 + c) * n3 + x];
 #pragma unroll
       for (int c = 0; c < 12; ++c) g[c] = d.grad[((size_t)e * 12 + c) * n3 + x];
-      const double mu = d.mu0[d.elemInst[e]];
+      const double mu = elem_mu(d, e);
       const double lam = mu * B.lambdaFac;
 #pragma unroll
       for (int dd = 0; dd < 3; ++dd) {
@@ -812,7 +815,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_dt(Dev d, Basis B, const 
     const double p = B.kappaM1 * (u[4] - 0.5 * (vx * u[1] + vy * u[2] + vz * u[3]));
     const double c = sqrt(B.kappa * p * srho);
     const double sj = d.sJ[(size_t)e * n3 + x];
-    const double lv = d.mu0[d.elemInst[e]] * srho;
+    const double lv = elem_mu(d, e) * srho;
 #pragma unroll
     for (int dd = 0; dd < 3; ++dd) {
       const double* mm = d.metr + ((size_t)e * 9 + 3 * dd) * n3 + x;

@@ -4,6 +4,8 @@
 
 namespace fg {
 
+struct AdjDev;
+
 struct KernelSet {
   int n = 0;
   bool gl = false;
@@ -13,6 +15,11 @@ struct KernelSet {
   void (*vol_weak)(const Dev&, const Basis&, int, double, double, cudaStream_t) = nullptr;
   void (*vol_split)(const Dev&, const Basis&, int, double, double, cudaStream_t) = nullptr;  // null if unsupported
   void (*dt)(const Dev&, const Basis&, const double*, const double*, double, double, double*, const double*, cudaStream_t) = nullptr;
+  // adjoint (vector-Jacobian product) of the right-hand side; vol_adj is null where unsupported
+  void (*vol_adj)(const Dev&, const AdjDev&, const Basis&, cudaStream_t) = nullptr;
+  void (*flux_adj)(const Dev&, const AdjDev&, const Basis&, cudaStream_t) = nullptr;
+  void (*lift_adj)(const Dev&, const AdjDev&, const Basis&, cudaStream_t) = nullptr;
+  void (*prep_adj)(const Dev&, const AdjDev&, const Basis&, cudaStream_t) = nullptr;
   // sets the dynamic shared-memory limits of all kernels; must run before any stream capture
   void (*prepare)() = nullptr;
 };

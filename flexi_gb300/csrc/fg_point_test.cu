@@ -49,6 +49,21 @@ void fgpt_visc_adj(double lamFac, const double* x, const double* m, const double
   visc_flux_dir_adj(x[15], lamFac, x[0], x[1], x[2], x + 3, m[0], m[1], m[2], Fb, xb[0], xb[1], xb[2], xb + 3, xb[15]);
 }
 
+// x = (u, v, w, g[12], mu): physical viscous fluxes f, g, h components 1..4 -> out[12]
+void fgpt_visc_phys(double lamFac, const double* x, double* out) {
+  const double e[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  for (int d = 0; d < 3; ++d) {
+    double F[5];
+    visc_flux_dir(x[15], x[15] * lamFac, x[0], x[1], x[2], x + 3, e[d][0], e[d][1], e[d][2], F);
+    for (int v = 0; v < 4; ++v) out[4 * d + v] = F[1 + v];
+  }
+}
+void fgpt_visc_phys_adj(double lamFac, const double* x, const double* yb, double* xb) {
+  double fb[5] = {0, yb[0], yb[1], yb[2], yb[3]}, gyb[5] = {0, yb[4], yb[5], yb[6], yb[7]}, hb[5] = {0, yb[8], yb[9], yb[10], yb[11]};
+  for (int c = 0; c < 16; ++c) xb[c] = 0.0;
+  visc_flux_phys_adj(x[15], lamFac, x[0], x[1], x[2], x + 3, fb, gyb, hb, xb[0], xb[1], xb[2], xb + 3, xb[15]);
+}
+
 // L[7], R[7] = (rho, srho, E, p, v1, v2, v3) -> F[5]
 void fgpt_riemann(int solver, int splitDG, double kappa, double R, const double* L, const double* Rr, double* F) {
   const Basis B = gas(kappa, R);

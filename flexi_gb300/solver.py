@@ -210,6 +210,23 @@ class Flexi:
         self._check(self.L.fg_get_gradients(self.h, _p(g[0]), _p(g[1]), _p(g[2])), "fg_get_gradients")
         return g
 
+    # ---------------------------------------------------------------- differentiation
+    def set_elem_mu_scale(self, scale):
+        """Per-element viscosity multiplier (None: all ones)."""
+        if scale is None:
+            self._check(self.L.fg_set_elem_mu_scale(self.h, None), "fg_set_elem_mu_scale")
+            return
+        s = np.ascontiguousarray(scale, np.float64).reshape(self.n_elems)
+        self._check(self.L.fg_set_elem_mu_scale(self.h, _p(s)), "fg_set_elem_mu_scale")
+
+    def rhs_vjp(self, W):
+        """(V, mu_bar): V = (dUt/dU)^T W at the current state, mu_bar = d<W, Ut>/d(viscosity multipliers)."""
+        W = np.ascontiguousarray(W, np.float64).reshape(self.ushape)
+        V = np.empty(self.ushape)
+        mub = np.empty(self.n_elems)
+        self._check(self.L.fg_rhs_vjp(self.h, _p(W), _p(V), _p(mub)), "fg_rhs_vjp")
+        return V, mub
+
     def stream(self):
         s = ctypes.c_void_p()
         self._check(self.L.fg_get_stream(self.h, ctypes.byref(s)), "fg_get_stream")

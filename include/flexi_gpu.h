@@ -169,6 +169,19 @@ int fg_debug_array(fg_handle* h, const char* name, void* out, long long* count);
 int fg_profile_enable(fg_handle* h, int on);
 int fg_profile_read(fg_handle* h, double* ms, long long* counts);
 
+/* ---- Differentiation ---------------------------------------------------------------------------------
+ * Per-element viscosity multiplier: element e uses mu0 (of its instance) x scale[e] in its volume viscous
+ * flux, its own half of the viscous side fluxes and its viscous time-step limit; NULL resets all to 1.
+ * No counterpart in the reference (the parameter of a gradient study). */
+int fg_set_elem_mu_scale(fg_handle* h, const double* scale);
+
+/* Adjoint of DGTimeDerivative_weakForm (dg.f90:221) at the current state: V = (dUt/dU)^T W, with W and V
+ * in the layout of U (host arrays), and optionally muScaleBar[nElems] = d<W, Ut>/d(scale). The transposed
+ * Jacobian is that of the discrete operator the GPU evaluates (the reference's implicit solver only forms
+ * J V by finite differences, implicit.f90:MatrixVector). The bulk velocity of a channel body force is
+ * held fixed. Supported: weak form and split form PI, LF/Roe/RoeEntropyFix, BR1/BR2, walls 3/4. */
+int fg_rhs_vjp(fg_handle* h, const double* W, double* V, double* muScaleBar);
+
 /* FP64 FMA throughput probe (TFLOP/s, 2 flop per FMA) of the current device, used for the roofline. */
 int fg_probe_fp64(double* tflops);
 

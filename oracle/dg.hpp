@@ -44,6 +44,34 @@ inline double fabs(double a) { return std::fabs(a); }
 inline double pow(double a, double b) { return std::pow(a, b); }
 inline double val(double x) { return x; }
 inline double val(FD x) { return x.v; }
+// forward-mode dual number (value, directional derivative): instantiating the solver with it gives the
+// exact Jacobian-vector product of the restated algorithm, used to check the GPU adjoint
+struct DD {
+  double v, d;
+  DD() : v(0.), d(0.) {}
+  DD(double x) : v(x), d(0.) {}
+  DD(double x, double y) : v(x), d(y) {}
+  explicit operator double() const { return v; }
+};
+inline DD operator+(DD a, DD b) { return DD(a.v + b.v, a.d + b.d); }
+inline DD operator-(DD a, DD b) { return DD(a.v - b.v, a.d - b.d); }
+inline DD operator*(DD a, DD b) { return DD(a.v * b.v, a.d * b.v + a.v * b.d); }
+inline DD operator/(DD a, DD b) { const double q = a.v / b.v; return DD(q, (a.d - q * b.d) / b.v); }
+inline DD operator-(DD a) { return DD(-a.v, -a.d); }
+inline DD& operator+=(DD& a, DD b) { a = a + b; return a; }
+inline DD& operator-=(DD& a, DD b) { a = a - b; return a; }
+inline DD& operator*=(DD& a, DD b) { a = a * b; return a; }
+inline bool operator<(DD a, DD b) { return a.v < b.v; }
+inline bool operator>(DD a, DD b) { return a.v > b.v; }
+inline bool operator<=(DD a, DD b) { return a.v <= b.v; }
+inline bool operator>=(DD a, DD b) { return a.v >= b.v; }
+inline DD sqrt(DD a) { const double r = std::sqrt(a.v); return DD(r, a.d / (2. * r)); }
+inline DD fabs(DD a) { return a.v >= 0. ? a : -a; }
+inline DD pow(DD a, DD b) {
+  const double r = std::pow(a.v, b.v);
+  return DD(r, r * (b.v * a.d / a.v) + (b.d != 0. ? r * b.d * std::log(a.v) : 0.));
+}
+inline double val(DD x) { return x.v; }
 template <class R> inline R rmax(R a, R b) { return a < b ? b : a; }
 template <class R> inline R rmin(R a, R b) { return a < b ? a : b; }
 
@@ -83,6 +111,8 @@ struct DG {
   std::vector<R> Flux_master, Flux_slave;
   std::vector<R> Ut_tmp;
   double BulkVel = 0.;
+  // per-element viscosity multiplier (an extension for the differentiation study; empty = 1)
+  std::vector<double> muScale;
   // time discretisation (timedisc_vars.f90:175-216, CarpenterRK4-5)
   double RKA[6], RKb[6], RKc[6];
   int nRKStages = 5;
@@ -449,8 +479,10 @@ struct DG {
   }
 
   // ---------------- flux.f90:EvalDiffFlux3D_Point (viscous flux, stored with the minus sign) ----------------
-  void diff_flux(const R* up, const R* gx, const R* gy, const R* gz, R* f, R* g, R* h) const {
-    R muS = mu0;
+  // viscosity of element e (0-based): mu0 times the element's multiplier (1 unless set)
+  double elem_mu_scale(int e) const { return muScale.empty() ? 1.0 : muScale[e]; }
+  void diff_flux(const R* up, const R* gx, const R* gy, const R* gz, R* f, R* g, R* h, double scale = 1.0) const {
+    R muS = scale == 1.0 ? mu0 : mu0 * R(scale);
     R lambda = muS * R(lambdaFac);
     R txx = muS * (s43 * gx[0] - s23 * gy[1] - s23 * gz[2]);
     R tyy = muS * (-s23 * gx[0] + s43 * gy[1] - s23 * gz[2]);
@@ -628,8 +660,10 @@ struct DG {
                     &UPrim_slave[si(0, p, q, s, 6)], &M.NormVec[sx * 3], &M.TangVec1[sx * 3], &M.TangVec2[sx * 3], F);
         // riemann.f90:ViscousFlux_Point
         R fL[5], gL[5], hL[5], fR[5], gR[5], hR[5];
-        diff_flux(&UPrim_master[si(0, p, q, s, 6)], &gradUx_m[si(0, p, q, s, NLIFT)], &gradUy_m[si(0, p, q, s, NLIFT)], &gradUz_m[si(0, p, q, s, NLIFT)], fL, gL, hL);
-        diff_flux(&UPrim_slave[si(0, p, q, s, 6)], &gradUx_s[si(0, p, q, s, NLIFT)], &gradUy_s[si(0, p, q, s, NLIFT)], &gradUz_s[si(0, p, q, s, NLIFT)], fR, gR, hR);
+        diff_flux(&UPrim_master[si(0, p, q, s, 6)], &gradUx_m[si(0, p, q, s, NLIFT)], &gradUy_m[si(0, p, q, s, NLIFT)], &gradUz_m[si(0, p, q, s, NLIFT)], fL, gL, hL,
+                  elem_mu_scale(s2e(0, s) - 1));
+        diff_flux(&UPrim_slave[si(0, p, q, s, 6)], &gradUx_s[si(0, p, q, s, NLIFT)], &gradUy_s[si(0, p, q, s, NLIFT)], &gradUz_s[si(0, p, q, s, NLIFT)], fR, gR, hR,
+                  elem_mu_scale(s2e(1, s) - 1));
         const double* nv = &M.NormVec[sx * 3];
         for (int v = 0; v < 5; ++v) {
           R FV = R(0.5) * (R(nv[0]) * (fL[v] + fR[v]) + R(nv[1]) * (gL[v] + gR[v]) + R(nv[2]) * (hL[v] + hR[v]));
@@ -648,7 +682,8 @@ struct DG {
         const double* nv = &M.NormVec[sx * 3];
         R Fl[5] = {R(0.), ub[4] * R(nv[0]), ub[4] * R(nv[1]), ub[4] * R(nv[2]), R(0.)};
         R fd[5], gd[5], hd[5];
-        diff_flux(ub, &gradUx_m[si(0, p, q, s, NLIFT)], &gradUy_m[si(0, p, q, s, NLIFT)], &gradUz_m[si(0, p, q, s, NLIFT)], fd, gd, hd);
+        diff_flux(ub, &gradUx_m[si(0, p, q, s, NLIFT)], &gradUy_m[si(0, p, q, s, NLIFT)], &gradUz_m[si(0, p, q, s, NLIFT)], fd, gd, hd,
+                  elem_mu_scale(s2e(0, s) - 1));
         if (bt == 3) { fd[4] = R(0.); gd[4] = R(0.); hd[4] = R(0.); }
         for (int v = 1; v < 5; ++v) Fl[v] = Fl[v] + R(nv[0]) * fd[v] + R(nv[1]) * gd[v] + R(nv[2]) * hd[v];
         for (int v = 0; v < 5; ++v) Flux_master[si(v, p, q, s, 5)] = Fl[v];
@@ -671,7 +706,8 @@ struct DG {
       for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
         size_t x = ((size_t)k * n + j) * n + i;
         R fv[5], gv[5], hv[5];
-        diff_flux(&UPrim[vi(0, i, j, k, e, 6)], &gradUx[vi(0, i, j, k, e, NLIFT)], &gradUy[vi(0, i, j, k, e, NLIFT)], &gradUz[vi(0, i, j, k, e, NLIFT)], fv, gv, hv);
+        diff_flux(&UPrim[vi(0, i, j, k, e, 6)], &gradUx[vi(0, i, j, k, e, NLIFT)], &gradUy[vi(0, i, j, k, e, NLIFT)], &gradUz[vi(0, i, j, k, e, NLIFT)], fv, gv, hv,
+                  elem_mu_scale(e));
         R fa[5], ga[5], ha[5];
         if (!split) {
           euler_flux(&U[vi(0, i, j, k, e, 5)], &UPrim[vi(0, i, j, k, e, 6)], fa, ga, ha);
@@ -830,7 +866,7 @@ struct DG {
         const double* mm[3] = {&M.Mf[g * 3], &M.Mg[g * 3], &M.Mh[g * 3]};
         for (int d = 0; d < 3; ++d)
           ml[d] = std::max(ml[d], std::fabs(mm[d][0] * vsJ[0] + mm[d][1] * vsJ[1] + mm[d][2] * vsJ[2]) + c * MetricsAdv[g * 3 + d]);
-        double mu = val(mu0);
+        double mu = val(mu0) * elem_mu_scale(e);
         for (int d = 0; d < 3; ++d) mlv[d] = std::max(mlv[d], mu * srho * MetricsVisc[g * 3 + d]);
       }
       double dtE = CFLScaleEff * 2. / (ml[0] + ml[1] + ml[2]);

@@ -45,6 +45,9 @@ def lib():
         _lib.orc_bulk_velocity.argtypes = [P]
         _lib.orc_bulk_velocity.restype = ctypes.c_double
         _lib.orc_set_bulk_velocity.argtypes = [P, ctypes.c_double]
+        _lib.orc_set_mu_scale.argtypes = [P, P]
+        _lib.orc_jvp.argtypes = [P, P, P]
+        _lib.orc_fd_jvp.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_double, P]
         _lib.orc_sizes.argtypes = [P, P]
         _lib.orc_mesh_array.argtypes = [P, ctypes.c_int, P]
         _lib.orc_mesh_array.restype = ctypes.c_longlong
@@ -128,6 +131,31 @@ class Oracle:
         if lib().orc_timestep(self.h, ctypes.byref(tt), dt) != 0:
             raise RuntimeError("oracle: " + lib().orc_last_error().decode())
         return tt.value
+
+    def set_mu_scale(self, scale):
+        """Per-element viscosity multiplier (None: all ones)."""
+        if scale is None:
+            lib().orc_set_mu_scale(self.h, None)
+            return
+        self._mu_scale = np.ascontiguousarray(scale, dtype=np.float64).reshape(self.n_elems)
+        lib().orc_set_mu_scale(self.h, _p(self._mu_scale))
+
+    def jvp(self, V):
+        """Exact J V of the time derivative at the current state (dual-number instantiation)."""
+        V = np.ascontiguousarray(V, dtype=np.float64).reshape(self.ushape)
+        JV = np.empty(self.ushape)
+        if lib().orc_jvp(self.h, _p(V), _p(JV)) != 0:
+            raise RuntimeError("oracle: " + lib().orc_last_error().decode())
+        return JV
+
+    def fd_jvp(self, V, fd_order=2, eps_method=1, scaleps=1.0):
+        """Matrix-free finite-difference J V as the reference's implicit solver forms it
+        (src/implicit/implicit.f90:MatrixVector with the step size of InitImplicit)."""
+        V = np.ascontiguousarray(V, dtype=np.float64).reshape(self.ushape)
+        JV = np.empty(self.ushape)
+        if lib().orc_fd_jvp(self.h, _p(V), fd_order, eps_method, scaleps, _p(JV)) != 0:
+            raise RuntimeError("oracle: " + lib().orc_last_error().decode())
+        return JV
 
     def calc_timestep(self):
         err = ctypes.c_int(0)

@@ -3,6 +3,7 @@
 // checker and as the timed CPU baseline. Never linked into, or called by, the product library.
 #include "dg.hpp"
 #include <cstring>
+#include <limits>
 #include <memory>
 
 using namespace orc;
@@ -28,6 +29,8 @@ static Config to_cfg(const orc_config* c) {
 struct OrcHandle {
   DG<double> dg;
   MeshInput mi;
+  Config cfg;
+  std::unique_ptr<DG<DD>> dgd;  // dual-number instance for exact Jacobian-vector products (built on first use)
   std::string err;
 };
 
@@ -45,7 +48,8 @@ void* orc_create(const orc_config* cfg, int nElems, int NGeo, const double* Node
     mi.ElemNb.assign(ElemNb, ElemNb + (size_t)18 * nElems);
     if (nBCs > 0) mi.BoundaryType.assign(BoundaryType, BoundaryType + 2 * nBCs);
     if (nRefStates > 0) mi.RefStatePrim.assign(RefStatePrim, RefStatePrim + 6 * nRefStates);
-    h->dg.init(to_cfg(cfg), mi);
+    h->cfg = to_cfg(cfg);
+    h->dg.init(h->cfg, mi);
     return h;
   } catch (std::exception& e) { g_err = e.what(); return nullptr; }
 }
@@ -88,6 +92,60 @@ int orc_timestep(void* hp, double* t, double dt) {
   return 0;
 }
 double orc_calc_timestep(void* hp, int* err) { return ((OrcHandle*)hp)->dg.calc_timestep(*err); }
+
+// per-element viscosity multiplier (NULL: all ones)
+void orc_set_mu_scale(void* hp, const double* s) {
+  auto& d = ((OrcHandle*)hp)->dg;
+  if (s) d.muScale.assign(s, s + d.nE); else d.muScale.clear();
+}
+
+// exact J V of DGTimeDerivative_weakForm at the current state, by the dual-number instantiation
+int orc_jvp(void* hp, const double* V, double* JV) {
+  auto* h = (OrcHandle*)hp;
+  try {
+    if (!h->dgd) { h->dgd.reset(new DG<DD>()); h->dgd->init(h->cfg, h->mi); }
+    DG<DD>& dd = *h->dgd;
+    const DG<double>& d = h->dg;
+    dd.muScale = d.muScale;
+    dd.BulkVel = d.BulkVel;
+    for (size_t i = 0; i < d.U.size(); ++i) dd.U[i] = DD(d.U[i], V[i]);
+    dd.time_derivative(0.);
+    for (size_t i = 0; i < d.U.size(); ++i) JV[i] = dd.Ut[i].d;
+    return 0;
+  } catch (std::exception& e) { g_err = e.what(); return 1; }
+}
+
+// matrix-free finite-difference J V as the reference's implicit solver forms it (implicit.f90:MatrixVector,
+// step size of InitImplicit): FD_Order 1 or 2, Eps_Method 1 (Qin, Ludlow, Shaw) or 2 (Knoll, Keyes)
+int orc_fd_jvp(void* hp, const double* V, int fdOrder, int epsMethod, double scaleps, double* JV) {
+  auto* h = (OrcHandle*)hp;
+  DG<double>& d = h->dg;
+  try {
+    const size_t nTot = d.U.size();
+    const std::vector<double> Xk = d.U;
+    double Vabs = 0., normXk = 0.;
+    for (size_t i = 0; i < nTot; ++i) Vabs += V[i] * V[i];
+    if (epsMethod == 2) { for (size_t i = 0; i < nTot; ++i) normXk += Xk[i] * Xk[i]; normXk = std::sqrt(normXk); }
+    const double mach = std::numeric_limits<double>::epsilon();
+    const double rEps0 = fdOrder == 1 ? scaleps * std::sqrt(mach) : std::pow(scaleps * scaleps * 0.5 * mach, 1. / 3.);
+    double eps = rEps0 / std::sqrt(Vabs);
+    if (epsMethod == 2) eps *= std::sqrt(1. + normXk);
+    d.time_derivative(0.);
+    const std::vector<double> R0 = d.Ut;
+    for (size_t i = 0; i < nTot; ++i) d.U[i] = Xk[i] + eps * V[i];
+    d.time_derivative(0.);
+    if (fdOrder == 1) {
+      for (size_t i = 0; i < nTot; ++i) JV[i] = (d.Ut[i] - R0[i]) / eps;
+    } else {
+      const std::vector<double> Rp = d.Ut;
+      for (size_t i = 0; i < nTot; ++i) d.U[i] = Xk[i] - eps * V[i];
+      d.time_derivative(0.);
+      for (size_t i = 0; i < nTot; ++i) JV[i] = (Rp[i] - d.Ut[i]) / (2. * eps);
+    }
+    d.U = Xk;
+    return 0;
+  } catch (std::exception& e) { g_err = e.what(); return 1; }
+}
 double orc_bulk_velocity(void* hp) { auto& d = ((OrcHandle*)hp)->dg; d.calc_forcing(); return d.BulkVel; }
 void orc_set_bulk_velocity(void* hp, double bv) { ((OrcHandle*)hp)->dg.BulkVel = bv; }
 

@@ -1,0 +1,115 @@
+"""Adjoint of the right-hand side (fg_rhs_vjp) against the oracle's Jacobian-vector products.
+
+Dot-product test <J V, W> = <V, J^T W>: J V comes from the oracle, exactly by its dual-number
+instantiation of the restated algorithm and approximately by the matrix-free finite difference of the
+reference's implicit solver (src/implicit/implicit.f90:MatrixVector, FD_Order 2); J^T W comes from the
+GPU adjoint kernels. Bars: exact JVP within 1e-11 of the sum of |JV_i W_i| (round-off only), FD JVP
+within 1e-8 relative. The viscosity-multiplier cotangent is checked against a central difference of
+<W, Ut> in a random direction of the multipliers (1e-7 relative), and the forward with random
+multipliers against the oracle (1e-12, as all forward parity tests)."""
+import numpy as np
+import pytest
+
+from _cases import oracle_cfg, perturb_state, rel_err
+from flexi_gb300 import mesh as fmesh, testcases
+from flexi_gb300.solver import Flexi, make_config
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    "gauss3_weak_roeef_br1": (dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="roeentropyfix", Lifting="br1"), "tgv"),
+    "gauss5_weak_roe_br2": (dict(N=5, NodeType="gauss", SplitDG="weak", Riemann="roe", Lifting="br2", etaBR2=2.5), "tgv"),
+    "gl3_weak_lf_br1": (dict(N=3, NodeType="gauss-lobatto", SplitDG="weak", Riemann="lf", Lifting="br1"), "tgv"),
+    "gl7_split_pi_roe_br1": (dict(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roe", Lifting="br1"), "tgv"),
+    "gl7_split_pi_roeef_br2": (dict(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roeentropyfix", Lifting="br2"), "tgv"),
+    "gl3_split_pi_lf_br2": (dict(N=3, NodeType="gauss-lobatto", SplitDG="pi", Riemann="lf", Lifting="br2"), "tgv"),
+    "channel_gauss3_weak_roe_br1": (dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="roe", Lifting="br1"), "channel"),
+    "channel_gl7_split_pi_roe_br1": (dict(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roe", Lifting="br1"), "channel"),
+    "channel_gl3_split_pi_roeef_br2_adiabatic": (dict(N=3, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roeentropyfix", Lifting="br2"),
+                                                 "adiabatic"),
+}
+
+
+def _setup(name, seed=0):
+    kw, kind = CASES[name]
+    c = make_config(mu0=5e-3, R=1.0 if kind != "tgv" else 71.42857, **kw)
+    if kind == "tgv":
+        m = fmesh.tgv_box(3, ngeo=2, perturb=0.05, seed=seed)
+    elif kind == "channel":
+        m = fmesh.channel_box((3, 4, 2), beta=1.5, ngeo=2, t_wall=1.0)
+    else:
+        m = fmesh.cartesian_box((3, 3, 2), (0.0, -1.0, 0.0), (2.0, 1.0, 1.0), ngeo=1, periodic=(True, False, True), wall_bc=(3, 1),
+                                ref_state_prim=np.array([[1.0, 0.0, 0.0, 0.0, 1.0, 1.0]]))
+    f = Flexi(c, m)
+    o = orc.Oracle(oracle_cfg(c), m)
+    x = f.elem_xgp()
+    if kind == "tgv":
+        U = testcases.tgv_state(x, mach=0.3, kappa=c.kappa, R=c.R)
+    else:
+        U = testcases.channel_state(x, mach=0.3, kappa=c.kappa, R=c.R, t_wall=1.0, noise=0.0, seed=seed)
+    U = perturb_state(U, seed=seed + 7, amp=0.05)
+    rng = np.random.default_rng(seed + 100)
+    scale = rng.uniform(0.8, 1.2, f.n_elems)
+    f.U = U
+    f.set_elem_mu_scale(scale)
+    o.set_state(U)
+    o.set_mu_scale(scale)
+    return f, o, U, scale, rng
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_forward_with_viscosity_multipliers(name):
+    f, o, U, scale, rng = _setup(name)
+    assert rel_err(f.DGTimeDerivative_weakForm(0.0), o.time_derivative()) <= 1e-12
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_dot_product_against_exact_jvp(name):
+    f, o, U, scale, rng = _setup(name)
+    for k in range(2):
+        V = rng.standard_normal(U.shape) * np.abs(U).max(axis=(0, 1, 2, 3))
+        W = rng.standard_normal(U.shape)
+        JV = o.jvp(V)
+        JTW, _ = f.rhs_vjp(W)
+        lhs = float((JV * W).sum())
+        rhs = float((V * JTW).sum())
+        scale_ = float(np.abs(JV * W).sum())
+        assert abs(lhs - rhs) <= 1e-11 * scale_, (k, lhs, rhs, abs(lhs - rhs) / scale_)
+
+
+@pytest.mark.parametrize("name", ["gauss3_weak_roeef_br1", "gl7_split_pi_roe_br1", "channel_gl7_split_pi_roe_br1"])
+def test_dot_product_against_reference_fd_jvp(name):
+    f, o, U, scale, rng = _setup(name, seed=1)
+    V = rng.standard_normal(U.shape) * np.abs(U).max(axis=(0, 1, 2, 3))
+    W = rng.standard_normal(U.shape)
+    JV = o.fd_jvp(V, fd_order=2, eps_method=1)
+    JTW, _ = f.rhs_vjp(W)
+    lhs, rhs = float((JV * W).sum()), float((V * JTW).sum())
+    assert abs(lhs - rhs) <= 1e-8 * float(np.abs(JV * W).sum()), (lhs, rhs)
+
+
+@pytest.mark.parametrize("name", ["gauss3_weak_roeef_br1", "gl7_split_pi_roeef_br2", "channel_gauss3_weak_roe_br1"])
+def test_viscosity_multiplier_cotangent(name):
+    f, o, U, scale, rng = _setup(name, seed=2)
+    W = rng.standard_normal(U.shape)
+    _, mub = f.rhs_vjp(W)
+    ds = rng.standard_normal(f.n_elems)
+    h = 1e-5
+
+    def J(s):
+        f.set_elem_mu_scale(s)
+        return float((f.DGTimeDerivative_weakForm(0.0) * W).sum())
+
+    fd = (J(scale + h * ds) - J(scale - h * ds)) / (2 * h)
+    fd2 = (J(scale + 2 * h * ds) - J(scale - 2 * h * ds)) / (4 * h)
+    rich = (4 * fd - fd2) / 3
+    assert abs(float(mub @ ds) - rich) <= 1e-7 * abs(rich), (float(mub @ ds), rich)
+
+
+def test_vjp_rejects_unsupported():
+    c = make_config(N=3, NodeType="gauss-lobatto", SplitDG="pi", Riemann="hllc")
+    f = Flexi(c, fmesh.tgv_box(2))
+    f.U = testcases.tgv_state(f.elem_xgp(), mach=0.1)
+    with pytest.raises(Exception, match="LF, Roe and RoeEntropyFix"):
+        f.rhs_vjp(np.zeros(f.ushape))
