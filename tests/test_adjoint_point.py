@@ -27,6 +27,8 @@ def pt():
     L.fgpt_cons_to_prim_adj.argtypes = [D, D, P, P, P]
     L.fgpt_visc.argtypes = [D, P, P, P]
     L.fgpt_visc_adj.argtypes = [D, P, P, P, P]
+    L.fgpt_visc_phys.argtypes = [D, P, P]
+    L.fgpt_visc_phys_adj.argtypes = [D, P, P, P]
     L.fgpt_riemann.argtypes = [I, I, D, D, P, P, P]
     L.fgpt_riemann_adj.argtypes = [I, I, D, D, P, P, P, P, P]
     L.fgpt_pressure_riemann.argtypes = [D, D, P]
@@ -104,6 +106,26 @@ def test_viscous_flux_adjoint(pt):
             return xb
 
         err = _check(f, fadj, x, 4, rng)
+        assert err is not None and err < TOL, err
+
+
+def test_physical_viscous_flux_adjoint(pt):
+    rng = np.random.default_rng(4)
+    lamfac = RGAS * KAPPA / (KAPPA - 1) / 0.72
+    for _ in range(50):
+        x = np.concatenate([rng.uniform(-1, 1, 3), rng.standard_normal(12), [rng.uniform(1e-4, 1e-2)]])
+
+        def f(x):
+            out = np.empty(12)
+            pt.fgpt_visc_phys(lamfac, _p(x), _p(out))
+            return out
+
+        def fadj(x, yb):
+            xb = np.empty(16)
+            pt.fgpt_visc_phys_adj(lamfac, _p(x), _p(np.ascontiguousarray(yb)), _p(xb))
+            return xb
+
+        err = _check(f, fadj, x, 12, rng)
         assert err is not None and err < TOL, err
 
 
