@@ -35,6 +35,7 @@ struct AdjDev {
   double* liftb;    // [s][2][4][n2] cotangent of the lifting surface flux, from the master (0) / slave (1) element
   double* muSideb;  // [s][2][n2] cotangent of the master / slave viscosity multiplier per side point
   double* muElemb;  // [e] cotangent of the element's viscosity multiplier
+  int accumulate;   // 1: add V to Ub and the multiplier cotangent to muElemb instead of overwriting them
 };
 
 // -----------------------------------------------------------------------------------------------------
@@ -86,7 +87,7 @@ __device__ __forceinline__ void adj_load_ubar_and_surface(const Dev& d, const Ad
 
 // per-element sum of one value per node of the CTA (blockDim.x threads, EPB elements): sRed has THREADS slots
 template <int n>
-__device__ __forceinline__ void adj_element_sum(double val, double* sRed, double* out, int e0, int nElems) {
+__device__ __forceinline__ void adj_element_sum(double val, double* sRed, double* out, int e0, int nElems, int accumulate) {
   constexpr int n3 = n * n * n, EPB = Shape<n>::EPB;
   sRed[threadIdx.x] = val;
   __syncthreads();
@@ -95,7 +96,7 @@ __device__ __forceinline__ void adj_element_sum(double val, double* sRed, double
     if (e < nElems) {
       double s = 0.;
       for (int x = 0; x < n3; ++x) s += sRed[threadIdx.x * n3 + x];
-      out[e] = s;
+      out[e] = accumulate ? out[e] + s : s;
     }
   }
 }
@@ -179,11 +180,14 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_weak_adj(Dev d, AdjDe
     mub *= d.mu0[d.elemInst[e]];
     cons_to_prim_adj(B, u, 0., vxb, vyb, vzb, pb, 0., 0., 0., ub);
 #pragma unroll
-    for (int v = 0; v < 5; ++v) a.Ub[((size_t)e * 5 + v) * n3 + x] = ub[v];
+    for (int v = 0; v < 5; ++v) {
+      double* o = a.Ub + ((size_t)e * 5 + v) * n3 + x;
+      *o = a.accumulate ? *o + ub[v] : ub[v];
+    }
 #pragma unroll
     for (int c = 0; c < 12; ++c) a.gb[((size_t)e * 12 + c) * n3 + x] = gb[c];
   }
-  adj_element_sum<n>(mub, sRed, a.muElemb, e0, d.nElems);
+  adj_element_sum<n>(mub, sRed, a.muElemb, e0, d.nElems, a.accumulate);
 }
 
 // -----------------------------------------------------------------------------------------------------
@@ -343,11 +347,14 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_split_adj(Dev d, AdjD
     double ubar[5] = {0., 0., 0., 0., 0.};
     cons_to_prim_adj(B, u, sb, vxb, vyb, vzb, pb, 0., sQb[(es * 6 + 0) * n3 + x], Eb, ubar);
 #pragma unroll
-    for (int v = 0; v < 5; ++v) a.Ub[((size_t)e * 5 + v) * n3 + x] = ubar[v];
+    for (int v = 0; v < 5; ++v) {
+      double* o = a.Ub + ((size_t)e * 5 + v) * n3 + x;
+      *o = a.accumulate ? *o + ubar[v] : ubar[v];
+    }
 #pragma unroll
     for (int c = 0; c < 12; ++c) a.gb[((size_t)e * 12 + c) * n3 + x] = gb[c];
   }
-  adj_element_sum<n>(mub, sRed, a.muElemb, e0, d.nElems);
+  adj_element_sum<n>(mub, sRed, a.muElemb, e0, d.nElems, a.accumulate);
 }
 
 // -----------------------------------------------------------------------------------------------------

@@ -63,6 +63,12 @@ __global__ void k_finish_step(Dev d, const double* bulkPart, const int* instStar
   if (!(dt > 0.) || dt > 1e300) set_error(d.err, 2);
   if (tInst) tInst[i] += dt;
 }
+// LSERK adjoint stage update: G = alpha G + beta U (cotangents of the RK register and of the state);
+// alpha = 0 starts G afresh without reading it
+__global__ void k_adj_axpby(double* __restrict__ G, const double* __restrict__ U, double alpha, double beta, long long count) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) G[i] = alpha == 0.0 ? beta * U[i] : fma(alpha, G[i], beta * U[i]);
+}
 // layout conversion between FLEXI's U(v,i,j,k,e) and [e][v][ijk]
 __global__ void k_fortran_to_dev(const double* __restrict__ f, double* __restrict__ d, int nv, int n3, long long total) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -127,6 +133,15 @@ struct fg_handle {
   // adjoint buffers (allocated on the first fg_rhs_vjp)
   AdjDev a{};
   bool haveAdj = false;
+  // LSERK adjoint: U checkpoints of the last fg_adjoint_forward, stage states of one segment, the
+  // running cotangents, and the final forward state (restored after the reverse sweep)
+  std::vector<void*> adjStore;
+  std::vector<double*> adjCkpt, adjStage;
+  double* adjGbar = nullptr;
+  double* adjUbar = nullptr;
+  double* adjUfinal = nullptr;
+  int adjSteps = 0, adjEvery = 0;
+  double adjDt = 0.;
   // per-kernel event timing (fg_profile_enable)
   bool profiling = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> evPool;
@@ -168,7 +183,16 @@ int upload(fg_handle* h, T*& ptr, const std::vector<T>& v) {
   }
   return 0;
 }
+void free_adjoint_store(fg_handle* h) {
+  for (void* p : h->adjStore) cudaFree(p);
+  h->adjStore.clear();
+  h->adjCkpt.clear();
+  h->adjStage.clear();
+  h->adjGbar = h->adjUbar = h->adjUfinal = nullptr;
+  h->adjSteps = h->adjEvery = 0;
+}
 void free_device(fg_handle* h) {
+  free_adjoint_store(h);
   if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
   for (auto& e : h->evPool) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
   h->evPool.clear(); h->evClass.clear(); h->evUsed = 0;
@@ -440,17 +464,25 @@ int ensure_adjoint(fg_handle* h) {
   return 0;
 }
 
-// V = (dUt/dU)^T W at d.U, W already in h->a.W; leaves V in h->a.Ub and the viscosity-multiplier
-// cotangent in h->a.muElemb
-void launch_vjp(fg_handle* h) {
-  const Dev& d = h->d;
+// V = (dUt/dU)^T W at the state d.U, W in a.W; leaves V in a.Ub and the viscosity-multiplier
+// cotangent in a.muElemb (added to them when a.accumulate)
+void launch_vjp(fg_handle* h, const Dev& d, const AdjDev& a) {
   h->K.prep(d, h->B, h->st);
   h->K.lift(d, h->B, h->st);
-  h->K.vol_adj(d, h->a, h->B, h->st);
-  h->K.flux_adj(d, h->a, h->B, h->st);
-  h->K.lift_adj(d, h->a, h->B, h->st);
-  h->K.prep_adj(d, h->a, h->B, h->st);
+  h->K.vol_adj(d, a, h->B, h->st);
+  h->K.flux_adj(d, a, h->B, h->st);
+  h->K.lift_adj(d, a, h->B, h->st);
+  h->K.prep_adj(d, a, h->B, h->st);
   h->launches += 6;
+}
+
+int adj_alloc(fg_handle* h, double*& p, size_t count) {
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, count * sizeof(double));
+  if (e != cudaSuccess) return fail(h, FG_ERR_CUDA, std::string("cudaMalloc (adjoint checkpoints): ") + cudaGetErrorString(e));
+  h->adjStore.push_back(q);
+  p = (double*)q;
+  return 0;
 }
 
 }  // namespace
@@ -700,9 +732,90 @@ int fg_rhs_vjp(fg_handle* h, const double* W, double* V, double* muScaleBar) {
   h->launches = 0;
   CUDA_TRY(cudaMemcpyAsync(h->dStage, W, total * sizeof(double), cudaMemcpyHostToDevice, h->st));
   k_fortran_to_dev<<<(unsigned)((total + 255) / 256), 256, 0, h->st>>>(h->dStage, const_cast<double*>(h->a.W), 5, n3, total);
-  launch_vjp(h);
+  AdjDev a = h->a;
+  a.accumulate = 0;
+  launch_vjp(h, h->d, a);
   CUDA_TRY(cudaGetLastError());
   if (V) { if (int r = export_field(h, h->a.Ub, 5, 0, 5, V)) return r; }
+  if (muScaleBar) CUDA_TRY(cudaMemcpyAsync(muScaleBar, h->a.muElemb, sizeof(double) * h->M.nElems, cudaMemcpyDeviceToHost, h->st));
+  CUDA_TRY(cudaStreamSynchronize(h->st));
+  return FG_OK;
+}
+
+int fg_adjoint_forward(fg_handle* h, int nSteps, double dt, int ckptEvery) {
+  if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
+  if (const char* why = adjoint_unsupported(h->cfg)) return fail(h, FG_ERR_CONFIG, why);
+  if (h->cfg.doTCSource) return fail(h, FG_ERR_CONFIG, "the time-stepping adjoint does not cover the channel body force");
+  if (nSteps < 1 || ckptEvery < 1 || !(dt > 0.) || !std::isfinite(dt)) return fail(h, FG_ERR_CONFIG, "nSteps, ckptEvery >= 1 and dt > 0 required");
+  if (int r = ensure_adjoint(h)) return r;
+  free_adjoint_store(h);
+  const int n3 = h->M.n * h->M.n * h->M.n;
+  const size_t cnt = (size_t)h->M.nElems * 5 * n3, bytes = cnt * sizeof(double);
+  const int nCk = (nSteps + ckptEvery - 1) / ckptEvery;
+  h->adjCkpt.assign(nCk, nullptr);
+  h->adjStage.assign((size_t)ckptEvery * 5, nullptr);
+  for (auto& p : h->adjCkpt) if (int r = adj_alloc(h, p, cnt)) { free_adjoint_store(h); return r; }
+  for (auto& p : h->adjStage) if (int r = adj_alloc(h, p, cnt)) { free_adjoint_store(h); return r; }
+  if (int r = adj_alloc(h, h->adjGbar, cnt)) { free_adjoint_store(h); return r; }
+  if (int r = adj_alloc(h, h->adjUbar, cnt)) { free_adjoint_store(h); return r; }
+  if (int r = adj_alloc(h, h->adjUfinal, cnt)) { free_adjoint_store(h); return r; }
+  h->launches = 0;
+  for (int step = 0; step < nSteps; ++step) {
+    if (step % ckptEvery == 0) CUDA_TRY(cudaMemcpyAsync(h->adjCkpt[step / ckptEvery], h->d.U, bytes, cudaMemcpyDeviceToDevice, h->st));
+    launch_step_setup(h, 1, dt, true);
+    launch_lserk(h);
+  }
+  CUDA_TRY(cudaMemcpyAsync(h->adjUfinal, h->d.U, bytes, cudaMemcpyDeviceToDevice, h->st));
+  CUDA_TRY(cudaGetLastError());
+  if (int r = check_err(h)) { free_adjoint_store(h); return r; }
+  h->adjSteps = nSteps; h->adjEvery = ckptEvery; h->adjDt = dt;
+  return FG_OK;
+}
+
+int fg_adjoint_reverse(fg_handle* h, const double* UbarT, double* Ubar0, double* muScaleBar) {
+  if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
+  if (h->adjSteps < 1) return fail(h, FG_ERR_STATE, "no fg_adjoint_forward run to reverse");
+  if (!UbarT) return fail(h, FG_ERR_CONFIG, "null cotangent");
+  const int n3 = h->M.n * h->M.n * h->M.n;
+  const long long cnt = (long long)h->M.nElems * 5 * n3;
+  const size_t bytes = (size_t)cnt * sizeof(double);
+  const unsigned gridAx = (unsigned)((cnt + 255) / 256);
+  const double dt = h->adjDt;
+  h->launches = 0;
+  CUDA_TRY(cudaMemcpyAsync(h->dStage, UbarT, bytes, cudaMemcpyHostToDevice, h->st));
+  k_fortran_to_dev<<<gridAx, 256, 0, h->st>>>(h->dStage, h->adjUbar, 5, n3, cnt);
+  CUDA_TRY(cudaMemsetAsync(h->a.muElemb, 0, sizeof(double) * h->M.nElems, h->st));
+  AdjDev a = h->a;
+  a.accumulate = 1;
+  a.Ub = h->adjUbar;
+  a.W = h->adjGbar;
+  const int nCk = (int)h->adjCkpt.size();
+  for (int seg = nCk - 1; seg >= 0; --seg) {
+    const int s0 = seg * h->adjEvery, ns = std::min(h->adjEvery, h->adjSteps - s0);
+    // recompute the segment's stage states from its checkpoint
+    CUDA_TRY(cudaMemcpyAsync(h->d.U, h->adjCkpt[seg], bytes, cudaMemcpyDeviceToDevice, h->st));
+    for (int s = 0; s < ns; ++s) {
+      launch_step_setup(h, 1, dt, false);
+      for (int k = 1; k <= 5; ++k) {
+        CUDA_TRY(cudaMemcpyAsync(h->adjStage[(size_t)s * 5 + k - 1], h->d.U, bytes, cudaMemcpyDeviceToDevice, h->st));
+        launch_rhs(h, k == 1 ? 1 : 2, k == 1 ? 0. : h->RKA[k], h->RKb[k]);
+      }
+    }
+    // reverse the segment: Gbar_k = -A_{k+1} Gbar_{k+1} + b_k dt Ubar; Ubar += J(U_{k-1})^T Gbar_k
+    for (int s = ns - 1; s >= 0; --s) {
+      for (int k = 5; k >= 1; --k) {
+        k_adj_axpby<<<gridAx, 256, 0, h->st>>>(h->adjGbar, h->adjUbar, k == 5 ? 0. : -h->RKA[k + 1], h->RKb[k] * dt, cnt);
+        Dev dv = h->d;
+        dv.U = h->adjStage[(size_t)s * 5 + k - 1];
+        launch_vjp(h, dv, a);
+        h->launches += 1;
+      }
+    }
+  }
+  CUDA_TRY(cudaGetLastError());
+  // leave the handle at the final forward state
+  CUDA_TRY(cudaMemcpyAsync(h->d.U, h->adjUfinal, bytes, cudaMemcpyDeviceToDevice, h->st));
+  if (Ubar0) { if (int r = export_field(h, h->adjUbar, 5, 0, 5, Ubar0)) return r; }
   if (muScaleBar) CUDA_TRY(cudaMemcpyAsync(muScaleBar, h->a.muElemb, sizeof(double) * h->M.nElems, cudaMemcpyDeviceToHost, h->st));
   CUDA_TRY(cudaStreamSynchronize(h->st));
   return FG_OK;

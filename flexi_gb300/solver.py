@@ -227,6 +227,18 @@ class Flexi:
         self._check(self.L.fg_rhs_vjp(self.h, _p(W), _p(V), _p(mub)), "fg_rhs_vjp")
         return V, mub
 
+    def adjoint_forward(self, n_steps, dt, ckpt_every):
+        """Advances n_steps LSERK steps of fixed dt, keeping a checkpoint every ckpt_every steps."""
+        self._check(self.L.fg_adjoint_forward(self.h, int(n_steps), float(dt), int(ckpt_every)), "fg_adjoint_forward")
+
+    def adjoint_reverse(self, UbarT):
+        """(Ubar0, mu_bar) for the cotangent UbarT of the final state of the last adjoint_forward."""
+        UbarT = np.ascontiguousarray(UbarT, np.float64).reshape(self.ushape)
+        Ub0 = np.empty(self.ushape)
+        mub = np.empty(self.n_elems)
+        self._check(self.L.fg_adjoint_reverse(self.h, _p(UbarT), _p(Ub0), _p(mub)), "fg_adjoint_reverse")
+        return Ub0, mub
+
     def stream(self):
         s = ctypes.c_void_p()
         self._check(self.L.fg_get_stream(self.h, ctypes.byref(s)), "fg_get_stream")

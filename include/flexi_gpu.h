@@ -182,6 +182,16 @@ int fg_set_elem_mu_scale(fg_handle* h, const double* scale);
  * held fixed. Supported: weak form and split form PI, LF/Roe/RoeEntropyFix, BR1/BR2, walls 3/4. */
 int fg_rhs_vjp(fg_handle* h, const double* W, double* V, double* muScaleBar);
 
+/* Adjoint of TimeStepByLSERKW2 (timestep.f90:82) over nSteps steps of fixed dt (the time step is not
+ * differentiated), in two calls. fg_adjoint_forward advances the state by nSteps steps and keeps a device
+ * checkpoint of U every ckptEvery steps. fg_adjoint_reverse takes UbarT = dL/dU(t_end) (layout of U) and
+ * returns Ubar0 = dL/dU(t_0) and muScaleBar[nElems] = dL/d(viscosity multipliers), both optional: per
+ * segment it recomputes the stage states from the checkpoint and runs the transposed stages in reverse.
+ * Device memory: (nSteps/ckptEvery + 5 ckptEvery + 3) states. The state is left at t_end. No counterpart
+ * in the reference. The channel body force is not covered. */
+int fg_adjoint_forward(fg_handle* h, int nSteps, double dt, int ckptEvery);
+int fg_adjoint_reverse(fg_handle* h, const double* UbarT, double* Ubar0, double* muScaleBar);
+
 /* FP64 FMA throughput probe (TFLOP/s, 2 flop per FMA) of the current device, used for the roofline. */
 int fg_probe_fp64(double* tflops);
 

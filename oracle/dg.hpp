@@ -113,6 +113,7 @@ struct DG {
   double BulkVel = 0.;
   // per-element viscosity multiplier (an extension for the differentiation study; empty = 1)
   std::vector<double> muScale;
+  std::vector<R> muScaleR;
   // time discretisation (timedisc_vars.f90:175-216, CarpenterRK4-5)
   double RKA[6], RKb[6], RKc[6];
   int nRKStages = 5;
@@ -479,10 +480,13 @@ struct DG {
   }
 
   // ---------------- flux.f90:EvalDiffFlux3D_Point (viscous flux, stored with the minus sign) ----------------
-  // viscosity of element e (0-based): mu0 times the element's multiplier (1 unless set)
-  double elem_mu_scale(int e) const { return muScale.empty() ? 1.0 : muScale[e]; }
-  void diff_flux(const R* up, const R* gx, const R* gy, const R* gz, R* f, R* g, R* h, double scale = 1.0) const {
-    R muS = scale == 1.0 ? mu0 : mu0 * R(scale);
+  // viscosity of element e (0-based): mu0 times the element's multiplier (1 unless set; the scalar-typed
+  // muScaleR, when set, carries a derivative direction for the dual-number instance)
+  R elem_mu_scale(int e) const { return !muScaleR.empty() ? muScaleR[e] : (muScale.empty() ? R(1.0) : R(muScale[e])); }
+  void diff_flux(const R* up, const R* gx, const R* gy, const R* gz, R* f, R* g, R* h, R scale = R(1.0)) const {
+    R muS;
+    if constexpr (std::is_same<R, FD>::value) muS = val(scale) == 1.0 ? mu0 : mu0 * scale;  // reference flop count
+    else muS = mu0 * scale;
     R lambda = muS * R(lambdaFac);
     R txx = muS * (s43 * gx[0] - s23 * gy[1] - s23 * gz[2]);
     R tyy = muS * (-s23 * gx[0] + s43 * gy[1] - s23 * gz[2]);
@@ -866,7 +870,7 @@ struct DG {
         const double* mm[3] = {&M.Mf[g * 3], &M.Mg[g * 3], &M.Mh[g * 3]};
         for (int d = 0; d < 3; ++d)
           ml[d] = std::max(ml[d], std::fabs(mm[d][0] * vsJ[0] + mm[d][1] * vsJ[1] + mm[d][2] * vsJ[2]) + c * MetricsAdv[g * 3 + d]);
-        double mu = val(mu0) * elem_mu_scale(e);
+        double mu = val(mu0) * val(elem_mu_scale(e));
         for (int d = 0; d < 3; ++d) mlv[d] = std::max(mlv[d], mu * srho * MetricsVisc[g * 3 + d]);
       }
       double dtE = CFLScaleEff * 2. / (ml[0] + ml[1] + ml[2]);

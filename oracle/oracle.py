@@ -47,6 +47,7 @@ def lib():
         _lib.orc_set_bulk_velocity.argtypes = [P, ctypes.c_double]
         _lib.orc_set_mu_scale.argtypes = [P, P]
         _lib.orc_jvp.argtypes = [P, P, P]
+        _lib.orc_jvp_solve.argtypes = [P, P, P, ctypes.c_int, ctypes.c_double, P]
         _lib.orc_fd_jvp.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_double, P]
         _lib.orc_sizes.argtypes = [P, P]
         _lib.orc_mesh_array.argtypes = [P, ctypes.c_int, P]
@@ -145,6 +146,16 @@ class Oracle:
         V = np.ascontiguousarray(V, dtype=np.float64).reshape(self.ushape)
         JV = np.empty(self.ushape)
         if lib().orc_jvp(self.h, _p(V), _p(JV)) != 0:
+            raise RuntimeError("oracle: " + lib().orc_last_error().decode())
+        return JV
+
+    def jvp_solve(self, V, n_steps, dt, d_scale=None):
+        """Exact tangent of n_steps LSERK steps of fixed dt (dual numbers): dU(t_end)/dU(t_0) V plus
+        dU(t_end)/d(viscosity multipliers) d_scale (V or d_scale may be None)."""
+        Vp = None if V is None else np.ascontiguousarray(V, dtype=np.float64).reshape(self.ushape)
+        Sp = None if d_scale is None else np.ascontiguousarray(d_scale, dtype=np.float64).reshape(self.n_elems)
+        JV = np.empty(self.ushape)
+        if lib().orc_jvp_solve(self.h, None if Vp is None else _p(Vp), None if Sp is None else _p(Sp), int(n_steps), float(dt), _p(JV)) != 0:
             raise RuntimeError("oracle: " + lib().orc_last_error().decode())
         return JV
 

@@ -115,6 +115,29 @@ int orc_jvp(void* hp, const double* V, double* JV) {
   } catch (std::exception& e) { g_err = e.what(); return 1; }
 }
 
+// exact tangent of nSteps LSERK steps of fixed dt from the current state (dual numbers):
+// JV = dU(t_end)/dU(t_0) V + dU(t_end)/d(viscosity multipliers) dScale (either direction may be NULL);
+// the state of the double instance is not changed
+int orc_jvp_solve(void* hp, const double* V, const double* dScale, int nSteps, double dt, double* JV) {
+  auto* h = (OrcHandle*)hp;
+  try {
+    if (!h->dgd) { h->dgd.reset(new DG<DD>()); h->dgd->init(h->cfg, h->mi); }
+    DG<DD>& dd = *h->dgd;
+    const DG<double>& d = h->dg;
+    dd.muScale = d.muScale;
+    dd.muScaleR.clear();
+    if (dScale)
+      for (int e = 0; e < d.nE; ++e) dd.muScaleR.push_back(DD(d.muScale.empty() ? 1.0 : d.muScale[e], dScale[e]));
+    dd.BulkVel = d.BulkVel;
+    for (size_t i = 0; i < d.U.size(); ++i) dd.U[i] = DD(d.U[i], V ? V[i] : 0.);
+    double t = 0.;
+    for (int s = 0; s < nSteps; ++s) dd.timestep_lserkw2(t, dt);
+    for (size_t i = 0; i < d.U.size(); ++i) JV[i] = dd.U[i].d;
+    dd.muScaleR.clear();
+    return 0;
+  } catch (std::exception& e) { g_err = e.what(); return 1; }
+}
+
 // matrix-free finite-difference J V as the reference's implicit solver forms it (implicit.f90:MatrixVector,
 // step size of InitImplicit): FD_Order 1 or 2, Eps_Method 1 (Qin, Ludlow, Shaw) or 2 (Knoll, Keyes)
 int orc_fd_jvp(void* hp, const double* V, int fdOrder, int epsMethod, double scaleps, double* JV) {
