@@ -52,8 +52,11 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--elems", type=int, default=32, help="elements per direction")
     p.add_argument("--riemann", default="hllc", choices=sorted(RIEMANN_IDS), help="surface Riemann solver")
-    p.add_argument("--workload", default="tgv", choices=["tgv", "ensemble"],
-                   help="tgv: the single-case N=7 TGV; ensemble: 256 independent TGV/vortex instances at N=5 against a loop over instances")
+    p.add_argument("--workload", default="tgv", choices=["tgv", "ensemble", "adjoint"],
+                   help="tgv: the single-case N=7 TGV; ensemble: 256 independent TGV/vortex instances at N=5 against a loop over "
+                        "instances; adjoint: gradient of a kinetic-energy loss over a 200-step TGV solve (16^3, N=5)")
+    p.add_argument("--ckpt", type=int, default=20, help="adjoint: checkpoint interval in steps")
+    p.add_argument("--fd-dirs", type=int, default=20, help="adjoint: random directions of the finite-difference check")
     p.add_argument("--instances", type=int, default=256, help="ensemble size")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline leg (profiling runs)")
@@ -520,12 +523,147 @@ def ensemble_cpu_baseline(budget_s=10.0):
                       f"{el:.1f} s of stepping"}
 
 
+# ---------------------------------------------------------------------------------------------------------
+# Differentiation workload: adjoint of a checkpointed fixed-dt solve
+# ---------------------------------------------------------------------------------------------------------
+ADJOINT_METRIC = "adjoint/forward cost ratio (TGV 16^3, N=5 Gauss, 200 LSERK steps)"
+
+
+def run_adjoint(args):
+    import numpy as np
+    import torch
+
+    ws, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    from flexi_gb300 import mesh as fmesh, testcases
+    from flexi_gb300.solver import Flexi, make_config
+    from oracle import oracle as orc
+
+    n_el, n_steps = 16, 200 if args.steps == 20 else args.steps
+    c = make_config(N=5, NodeType="gauss", SplitDG="weak", Riemann="roeentropyfix", Lifting="br1", kappa=1.4, R=71.42857, Pr=0.72,
+                    mu0=1.0 / 1600.0, CFLScale=0.9, DFLScale=0.9)
+    m = fmesh.tgv_box(n_el)
+    f = Flexi(c, m)
+    rng = np.random.default_rng(1234 + rank)
+    U0 = testcases.tgv_state(f.elem_xgp(), mach=0.1, kappa=1.4, R=71.42857)
+    scale = rng.uniform(0.8, 1.2, f.n_elems)
+    f.U = U0
+    f.set_elem_mu_scale(scale)
+    dt = float(np.atleast_1d(f.CalcTimeStep()[0])[0])
+    dof = f.n_elems * f.n ** 3
+    _, w1, _ = orc.nodes_and_weights(5, 1)
+    wq = np.einsum("k,j,i->kji", w1, w1, w1)[None] / f.mesh_array("sJ")  # quadrature weight x Jacobian
+
+    def kinetic(U):
+        return float((0.5 * (U[..., 1] ** 2 + U[..., 2] ** 2 + U[..., 3] ** 2) / U[..., 0] * wq).sum())
+
+    target = kinetic(U0) * rng.uniform(0.9, 0.95)
+
+    def loss(U0_, s_):
+        # the same fixed-dt solve through the reference-facing step entry (TimeStepByLSERKW2)
+        f.U = U0_
+        f.set_elem_mu_scale(s_)
+        t = 0.0
+        for _ in range(n_steps):
+            t = f.TimeStepByLSERKW2(t, dt)
+        return 0.5 * (kinetic(f.U) - target) ** 2
+
+    stream = torch.cuda.ExternalStream(f.stream())
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        out = fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return out, a.elapsed_time(b)
+
+    # warm-up (kernel loading, buffer allocation)
+    f.U = U0
+    f.adjoint_forward(args.warmup, dt, args.ckpt)
+    f.adjoint_reverse(np.zeros(f.ushape))
+    # plain forward: the solver's own time loop (graph-replayed, dt from CALCTIMESTEP each step)
+    f.U = U0
+    f.set_elem_mu_scale(scale)
+    f.TimeDisc(2)
+    f.U = U0
+    _, ms_plain = timed(lambda: f.TimeDisc(n_steps))
+    # forward with checkpoints, then the reverse sweep
+    f.U = U0
+    f.adjoint_forward(1, dt, 1)  # release the warm-up store before measuring the footprint
+    free0 = torch.cuda.mem_get_info()[0]
+    clocks = ClockSampler(local)
+    clocks.start()
+    _, ms_fwd = timed(lambda: f.adjoint_forward(n_steps, dt, args.ckpt))
+    adj_bytes = free0 - torch.cuda.mem_get_info()[0]
+    UT = f.U
+    KE = kinetic(UT)
+    UbarT = np.zeros(f.ushape)
+    rho = UT[..., 0]
+    UbarT[..., 0] = -0.5 * (UT[..., 1] ** 2 + UT[..., 2] ** 2 + UT[..., 3] ** 2) / rho ** 2 * wq
+    for c_ in (1, 2, 3):
+        UbarT[..., c_] = UT[..., c_] / rho * wq
+    UbarT *= KE - target
+    (Ub0, mub), ms_rev = timed(lambda: f.adjoint_reverse(UbarT))
+    clk = clocks.stop()
+    L0 = 0.5 * (KE - target) ** 2
+    # central finite differences (eps = 1e-6) of the loss in seeded random directions of (U0, multipliers)
+    errs = []
+    for k in range(args.fd_dirs):
+        dU = rng.standard_normal(U0.shape) * np.abs(U0).max(axis=(0, 1, 2, 3))
+        ds = rng.standard_normal(f.n_elems)
+        eps = 1e-6
+        fd = (loss(U0 + eps * dU, scale + eps * ds) - loss(U0 - eps * dU, scale - eps * ds)) / (2 * eps)
+        ad = float((Ub0 * dU).sum() + mub @ ds)
+        errs.append(abs(ad - fd) / max(abs(fd), 1e-300))
+    # dot-product test at t_end against the reference's matrix-free FD JVP (FD_Order 2) on the oracle
+    o = orc.Oracle(dict(N=5, nodeType=1, riemann=33, riemannBC=-1, lifting=1, weakLifting=0, consLifting=0, splitDG=-1, etaBR2=2.0,
+                        etaBR2_wall=-1.0, kappa=1.4, R=71.42857, Pr=0.72, mu0=1.0 / 1600.0, CFLScale=0.9, DFLScale=0.9, doTCSource=0,
+                        dpdx=-1.0), m)
+    o.set_state(UT)
+    o.set_mu_scale(scale)
+    V = rng.standard_normal(UT.shape) * np.abs(UT).max(axis=(0, 1, 2, 3))
+    W = rng.standard_normal(UT.shape)
+    JV = o.fd_jvp(V, fd_order=2, eps_method=1)
+    f.U = UT
+    f.set_elem_mu_scale(scale)
+    JTW, _ = f.rhs_vjp(W)
+    dot_err = abs(float((JV * W).sum()) - float((V * JTW).sum())) / float(np.abs(JV * W).sum())
+    nck = (n_steps + args.ckpt - 1) // args.ckpt
+    mem_states_gb = (nck + 5 * args.ckpt + 3) * dof * 5 * 8 / 1e9
+    if rank != 0:
+        return
+    line = {"metric": ADJOINT_METRIC, "value": ms_rev / ms_plain, "unit": "reverse time / forward time", "n_gpus": ws,
+            "steps": n_steps, "warmup": args.warmup, "ms_per_step": ms_rev / n_steps, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"TGV {n_el}^3 Cartesian, N=5 Gauss, weak form, RoeEntropyFix, BR1, Re=1600, Ma=0.1, FP64, {n_steps} "
+                                   f"LSERK steps of fixed dt, checkpoint every {args.ckpt} steps; loss 1/2 (KE(t_end) - target)^2; "
+                                   "gradient w.r.t. U0 and per-element viscosity multipliers U[0.8,1.2]",
+                       "n_elems": f.n_elems, "N": 5, "dof": dof, "dt": dt, "l2": "inputs larger than L2 (state 35 MB, stage states 3.5 GB)"},
+            "forward_ms_per_step": ms_plain / n_steps, "forward": "the plain solver's graph-replayed time loop (fg_run)",
+            "forward_with_checkpoints_ms_per_step": ms_fwd / n_steps,
+            "reverse_ms_per_step": ms_rev / n_steps,
+            "reverse_includes": "recomputation of every segment's stage states from its checkpoint + 5 adjoint right-hand sides per step",
+            "adjoint_device_memory_gb": adj_bytes / 1e9, "checkpoint_and_stage_states_gb": mem_states_gb,
+            "stage_intermediates_kept": adj_bytes / 1e9 > 1.5 * mem_states_gb, "loss": L0,
+            "fd_check": {"directions": args.fd_dirs, "eps": 1e-6, "max_rel_err": max(errs) if errs else None,
+                         "median_rel_err": float(np.median(errs)) if errs else None},
+            "dot_product_vs_reference_fd_jvp": {"rel_err": dot_err, "fd": "implicit.f90:MatrixVector FD_Order 2, Eps_Method 1, on the oracle"},
+            "e2e": {"value": ms_rev / ms_plain, "unit": "reverse time / forward time", "h2d_bytes_per_step": dof * 5 * 8 / n_steps,
+                    "d2h_bytes_per_step": (dof * 5 * 8 + f.n_elems * 8) / n_steps},
+            "gpu_launches": None, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "ensemble":
         run_ensemble(args)
+    elif args.workload == "adjoint":
+        run_adjoint(args)
     else:
         run_gb300(args)
 

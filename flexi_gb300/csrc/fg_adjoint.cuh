@@ -85,6 +85,39 @@ __device__ __forceinline__ void adj_load_ubar_and_surface(const Dev& d, const Ad
   }
 }
 
+// transposed prolongation gathered by the volume node that owns the result: node (i,j,k) collects, per
+// direction, the cotangents (NC components, element face order) of the two face points on its normal
+// line, weighted by L_minus(l) and L_plus(l) (Gauss) or taken at l = 0 / N (Gauss-Lobatto)
+template <int n, bool GL, int NC>
+__device__ __forceinline__ void prolong_gather_node(const SBasis<n>& Bs, const double* sFace, int es, int x, double* acc) {
+  constexpr int n2 = n * n, N = n - 1;
+  const int i = x % n, j = (x / n) % n, k = x / n2;
+  const int idx3[3] = {i, j, k};
+#pragma unroll
+  for (int dir = 0; dir < 3; ++dir) {
+    const int lsM = dir == 0 ? XI_MINUS : (dir == 1 ? ETA_MINUS : ZETA_MINUS);
+    const int lsP = dir == 0 ? XI_PLUS : (dir == 1 ? ETA_PLUS : ZETA_PLUS);
+    const int ab = (dir == 0 ? j : i) + n * (dir == 2 ? j : k);
+    const int l = idx3[dir];
+    const double* fM = sFace + ((es * 6 + lsM - 1) * n2 + ab) * NC;
+    const double* fP = sFace + ((es * 6 + lsP - 1) * n2 + ab) * NC;
+    if (GL) {
+      if (l == 0) {
+#pragma unroll
+        for (int c = 0; c < NC; ++c) acc[c] += fM[c];
+      }
+      if (l == N) {
+#pragma unroll
+        for (int c = 0; c < NC; ++c) acc[c] += fP[c];
+      }
+    } else {
+      const double LM = Bs.Lm(l), LP = Bs.Lp(l);
+#pragma unroll
+      for (int c = 0; c < NC; ++c) acc[c] = fma(LM, fM[c], fma(LP, fP[c], acc[c]));
+    }
+  }
+}
+
 // per-element sum of one value per node of the CTA (blockDim.x threads, EPB elements): sRed has THREADS slots
 template <int n>
 __device__ __forceinline__ void adj_element_sum(double val, double* sRed, double* out, int e0, int nElems, int accumulate) {
@@ -527,36 +560,18 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_lift_adj(Dev d, AdjDev a,
   // transposed prolongation of the face gradients into sGb, one direction (two opposite faces) at a time.
   // BR1 prolongs the full gradient (added before the surface part is transposed), BR2 the volume part (after).
   auto prolong_adj = [&]() {
-#pragma unroll 1
-    for (int dir = 0; dir < 3; ++dir) {
-      for (int t = threadIdx.x; t < EPB * n2; t += blockDim.x) {
-        const int es = t / n2, ab = t - es * n2;
-        const int e = e0 + es;
-        if (e >= d.nElems) continue;
-        const int aa = ab % n, bb = ab / n;
-        const int lsM = dir == 0 ? XI_MINUS : (dir == 1 ? ETA_MINUS : ZETA_MINUS);
-        const int lsP = dir == 0 ? XI_PLUS : (dir == 1 ? ETA_PLUS : ZETA_PLUS);
-        const int oM = (es * 6 + lsM - 1) * n2 + ab, oP = (es * 6 + lsP - 1) * n2 + ab;
-        double* G = sGb + es * 12 * n3;
-        if (GL) {
-          const int xM = face_node(lsM, aa, bb, 0, n), xP = face_node(lsP, aa, bb, N, n);
+    for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
+      const int es = t / n3, x = t - es * n3, e = e0 + es;
+      if (e >= d.nElems) continue;
+      double acc[12];
 #pragma unroll
-          for (int c = 0; c < 12; ++c) {
-            G[c * n3 + xM] += sGf[oM * 12 + c];
-            G[c * n3 + xP] += sGf[oP * 12 + c];
-          }
-        } else {
+      for (int c = 0; c < 12; ++c) acc[c] = 0.;
+      prolong_gather_node<n, GL, 12>(Bs, sGf, es, x, acc);
+      double* G = sGb + es * 12 * n3;
 #pragma unroll
-          for (int l = 0; l < n; ++l) {
-            const int x = face_node(lsM, aa, bb, l, n);  // same line for the plus face
-            const double LM = Bs.Lm(l), LP = Bs.Lp(l);
-#pragma unroll
-            for (int c = 0; c < 12; ++c) G[c * n3 + x] += LM * sGf[oM * 12 + c] + LP * sGf[oP * 12 + c];
-          }
-        }
-      }
-      __syncthreads();
+      for (int c = 0; c < 12; ++c) G[c * n3 + x] += acc[c];
     }
+    __syncthreads();
   };
   __syncthreads();
   if (!br2) prolong_adj();
@@ -671,8 +686,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_prep_adj(Dev d, AdjDev a,
   extern __shared__ double smem[];
   double* sD = smem;
   double* sU = sD + SBasis<n>::SIZE;   // [EPB][5][n3] state
-  double* sUb = sU + EPB * 5 * n3;     // [EPB][5][n3] face parts of U bar
-  double* sCb = sUb + EPB * 5 * n3;    // [EPB][6][n2][5] cotangents of the prolonged face states, element face order
+  double* sCb = sU + EPB * 5 * n3;     // [EPB][6][n2][5] cotangents of the prolonged face states, element face order
   double* sMub = sCb + EPB * 6 * n2 * 5;  // [EPB][6][n2] viscosity-multiplier cotangent of each face point
   load_basis_smem<n>(B, sD);
   SBasis<n> Bs{sD};
@@ -681,7 +695,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_prep_adj(Dev d, AdjDev a,
     const int es = t / n3, x = t - es * n3, e = e0 + es;
     if (e >= d.nElems) continue;
 #pragma unroll
-    for (int v = 0; v < 5; ++v) { sU[(es * 5 + v) * n3 + x] = d.U[((size_t)e * 5 + v) * n3 + x]; sUb[(es * 5 + v) * n3 + x] = 0.; }
+    for (int v = 0; v < 5; ++v) sU[(es * 5 + v) * n3 + x] = d.U[((size_t)e * 5 + v) * n3 + x];
   }
   __syncthreads();
   const double sig = B.weakLifting ? 1.0 : -1.0;
@@ -739,39 +753,14 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_prep_adj(Dev d, AdjDev a,
     for (int v = 0; v < 5; ++v) sCb[o * 5 + v] = cb[v];
   }
   __syncthreads();
-  // transposed prolongation, one direction (two opposite faces) at a time
-#pragma unroll 1
-  for (int dir = 0; dir < 3; ++dir) {
-    for (int t = threadIdx.x; t < EPB * n2; t += blockDim.x) {
-      const int es = t / n2, ab = t - es * n2;
-      const int e = e0 + es;
-      if (e >= d.nElems) continue;
-      const int aa = ab % n, bb = ab / n;
-      const int lsM = dir == 0 ? XI_MINUS : (dir == 1 ? ETA_MINUS : ZETA_MINUS);
-      const int lsP = dir == 0 ? XI_PLUS : (dir == 1 ? ETA_PLUS : ZETA_PLUS);
-      const int oM = (es * 6 + lsM - 1) * n2 + ab, oP = (es * 6 + lsP - 1) * n2 + ab;
-      double* Ubs = sUb + es * 5 * n3;
-      if (GL) {
-        const int xM = face_node(lsM, aa, bb, 0, n), xP = face_node(lsP, aa, bb, N, n);
-#pragma unroll
-        for (int v = 0; v < 5; ++v) { Ubs[v * n3 + xM] += sCb[oM * 5 + v]; Ubs[v * n3 + xP] += sCb[oP * 5 + v]; }
-      } else {
-#pragma unroll
-        for (int l = 0; l < n; ++l) {
-          const int x = face_node(lsM, aa, bb, l, n);
-          const double LM = Bs.Lm(l), LP = Bs.Lp(l);
-#pragma unroll
-          for (int v = 0; v < 5; ++v) Ubs[v * n3 + x] += LM * sCb[oM * 5 + v] + LP * sCb[oP * 5 + v];
-        }
-      }
-    }
-    __syncthreads();
-  }
+  // transposed prolongation, gathered per volume node
   for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
     const int es = t / n3, x = t - es * n3, e = e0 + es;
     if (e >= d.nElems) continue;
+    double acc[5] = {0., 0., 0., 0., 0.};
+    prolong_gather_node<n, GL, 5>(Bs, sCb, es, x, acc);
 #pragma unroll
-    for (int v = 0; v < 5; ++v) a.Ub[((size_t)e * 5 + v) * n3 + x] += sUb[(es * 5 + v) * n3 + x];
+    for (int v = 0; v < 5; ++v) a.Ub[((size_t)e * 5 + v) * n3 + x] += acc[v];
   }
   // mu bar of the element: volume part (k_vol_*_adj) + its sides' viscous fluxes
   if (threadIdx.x < EPB) {

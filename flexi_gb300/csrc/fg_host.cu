@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cctype>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <sstream>
 #include <string>
@@ -137,6 +138,11 @@ struct fg_handle {
   // running cotangents, and the final forward state (restored after the reverse sweep)
   std::vector<void*> adjStore;
   std::vector<double*> adjCkpt, adjStage;
+  // with enough device memory, the forward intermediates of every stage of the segment being reversed
+  // (primitive variables, lifted gradients, face states and face gradients), so that the adjoint right-hand
+  // sides need not recompute them
+  bool adjKeepInter = false;
+  std::vector<Dev> adjInter;
   double* adjGbar = nullptr;
   double* adjUbar = nullptr;
   double* adjUfinal = nullptr;
@@ -188,6 +194,8 @@ void free_adjoint_store(fg_handle* h) {
   h->adjStore.clear();
   h->adjCkpt.clear();
   h->adjStage.clear();
+  h->adjInter.clear();
+  h->adjKeepInter = false;
   h->adjGbar = h->adjUbar = h->adjUfinal = nullptr;
   h->adjSteps = h->adjEvery = 0;
 }
@@ -358,8 +366,7 @@ struct ProfScope {
 };
 
 // state sequence of one right-hand side evaluation plus the RK register update
-void launch_rhs(fg_handle* h, int mode, double rkA, double rkB) {
-  const Dev& d = h->d;
+void launch_rhs_dev(fg_handle* h, const Dev& d, int mode, double rkA, double rkB) {
   { ProfScope p(h, 0); h->K.prep(d, h->B, h->st); }
   { ProfScope p(h, 1); h->K.lift(d, h->B, h->st); }
   { ProfScope p(h, 2); h->K.flux(d, h->B, h->st); }
@@ -370,6 +377,7 @@ void launch_rhs(fg_handle* h, int mode, double rkA, double rkB) {
   }
   h->launches += 4;
 }
+void launch_rhs(fg_handle* h, int mode, double rkA, double rkB) { launch_rhs_dev(h, h->d, mode, rkA, rkB); }
 // step set-up: mode 0 = CALCTIMESTEP, 1 = fixed dt, 2 = bulk velocity only (plain right-hand side)
 void launch_step_setup(fg_handle* h, int mode, double fixedDt, bool advanceTime) {
   const Dev& d = h->d;
@@ -474,6 +482,15 @@ void launch_vjp(fg_handle* h, const Dev& d, const AdjDev& a) {
   h->K.lift_adj(d, a, h->B, h->st);
   h->K.prep_adj(d, a, h->B, h->st);
   h->launches += 6;
+}
+
+// adjoint right-hand side on forward intermediates the caller kept (no prep/lift recomputation)
+void launch_vjp_kept(fg_handle* h, const Dev& d, const AdjDev& a) {
+  h->K.vol_adj(d, a, h->B, h->st);
+  h->K.flux_adj(d, a, h->B, h->st);
+  h->K.lift_adj(d, a, h->B, h->st);
+  h->K.prep_adj(d, a, h->B, h->st);
+  h->launches += 4;
 }
 
 int adj_alloc(fg_handle* h, double*& p, size_t count) {
@@ -756,6 +773,30 @@ int fg_adjoint_forward(fg_handle* h, int nSteps, double dt, int ckptEvery) {
   h->adjStage.assign((size_t)ckptEvery * 5, nullptr);
   for (auto& p : h->adjCkpt) if (int r = adj_alloc(h, p, cnt)) { free_adjoint_store(h); return r; }
   for (auto& p : h->adjStage) if (int r = adj_alloc(h, p, cnt)) { free_adjoint_store(h); return r; }
+  {
+    // keep the stage intermediates of a segment when they take at most half of the free device memory
+    const int n2 = h->M.n * h->M.n;
+    const size_t perStage = (size_t)h->M.nElems * (VP_NF + 12) * n3 + (size_t)h->M.nSides * (2 * FS_NF + 24) * n2;
+    size_t freeB = 0, totalB = 0;
+    cudaMemGetInfo(&freeB, &totalB);
+    const char* env = std::getenv("FLEXI_GB300_ADJOINT_RECOMPUTE");
+    const bool forceRecompute = env && env[0] == '1';
+    if (!forceRecompute && perStage * sizeof(double) * h->adjStage.size() < freeB / 2) {
+      h->adjKeepInter = true;
+      h->adjInter.assign(h->adjStage.size(), h->d);
+      for (size_t i = 0; i < h->adjStage.size(); ++i) {
+        Dev& v = h->adjInter[i];
+        v.U = h->adjStage[i];
+        int r = 0;
+        if ((r = adj_alloc(h, v.prim, (size_t)h->M.nElems * VP_NF * n3)) || (r = adj_alloc(h, v.grad, (size_t)h->M.nElems * 12 * n3)) ||
+            (r = adj_alloc(h, v.faceM, (size_t)h->M.nSides * FS_NF * n2)) || (r = adj_alloc(h, v.faceS, (size_t)h->M.nSides * FS_NF * n2)) ||
+            (r = adj_alloc(h, v.gradM, (size_t)h->M.nSides * 12 * n2)) || (r = adj_alloc(h, v.gradS, (size_t)h->M.nSides * 12 * n2))) {
+          free_adjoint_store(h);
+          return r;
+        }
+      }
+    }
+  }
   if (int r = adj_alloc(h, h->adjGbar, cnt)) { free_adjoint_store(h); return r; }
   if (int r = adj_alloc(h, h->adjUbar, cnt)) { free_adjoint_store(h); return r; }
   if (int r = adj_alloc(h, h->adjUfinal, cnt)) { free_adjoint_store(h); return r; }
@@ -797,17 +838,30 @@ int fg_adjoint_reverse(fg_handle* h, const double* UbarT, double* Ubar0, double*
     for (int s = 0; s < ns; ++s) {
       launch_step_setup(h, 1, dt, false);
       for (int k = 1; k <= 5; ++k) {
-        CUDA_TRY(cudaMemcpyAsync(h->adjStage[(size_t)s * 5 + k - 1], h->d.U, bytes, cudaMemcpyDeviceToDevice, h->st));
-        launch_rhs(h, k == 1 ? 1 : 2, k == 1 ? 0. : h->RKA[k], h->RKb[k]);
+        const size_t slot = (size_t)s * 5 + k - 1;
+        CUDA_TRY(cudaMemcpyAsync(h->adjStage[slot], h->d.U, bytes, cudaMemcpyDeviceToDevice, h->st));
+        if (h->adjKeepInter) {
+          // the stage writes its intermediates into the slot; the state is updated in place as usual
+          Dev dv = h->adjInter[slot];
+          dv.U = h->d.U;
+          launch_rhs_dev(h, dv, k == 1 ? 1 : 2, k == 1 ? 0. : h->RKA[k], h->RKb[k]);
+        } else {
+          launch_rhs(h, k == 1 ? 1 : 2, k == 1 ? 0. : h->RKA[k], h->RKb[k]);
+        }
       }
     }
     // reverse the segment: Gbar_k = -A_{k+1} Gbar_{k+1} + b_k dt Ubar; Ubar += J(U_{k-1})^T Gbar_k
     for (int s = ns - 1; s >= 0; --s) {
       for (int k = 5; k >= 1; --k) {
         k_adj_axpby<<<gridAx, 256, 0, h->st>>>(h->adjGbar, h->adjUbar, k == 5 ? 0. : -h->RKA[k + 1], h->RKb[k] * dt, cnt);
-        Dev dv = h->d;
-        dv.U = h->adjStage[(size_t)s * 5 + k - 1];
-        launch_vjp(h, dv, a);
+        const size_t slot = (size_t)s * 5 + k - 1;
+        if (h->adjKeepInter) {
+          launch_vjp_kept(h, h->adjInter[slot], a);
+        } else {
+          Dev dv = h->d;
+          dv.U = h->adjStage[slot];
+          launch_vjp(h, dv, a);
+        }
         h->launches += 1;
       }
     }

@@ -19,7 +19,7 @@ struct Inst {
   static size_t smem_weak_adj() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * 5 * S::n3 + S::THREADS); }
   static size_t smem_split_adj() { return sizeof(double) * (SBasis<n>::SIZE + 2 * S::n2 + S::EPB * 26 * S::n3 + S::THREADS); }
   static size_t smem_lift_adj() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * (13 * S::n3 + 6 * S::n2 * 19)); }
-  static size_t smem_prep_adj() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * (10 * S::n3 + 6 * S::n2 * 6)); }
+  static size_t smem_prep_adj() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * (5 * S::n3 + 6 * S::n2 * 6)); }
   template <class K>
   static void set_smem(K kern, size_t bytes) {
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);

@@ -187,7 +187,10 @@ int fg_rhs_vjp(fg_handle* h, const double* W, double* V, double* muScaleBar);
  * checkpoint of U every ckptEvery steps. fg_adjoint_reverse takes UbarT = dL/dU(t_end) (layout of U) and
  * returns Ubar0 = dL/dU(t_0) and muScaleBar[nElems] = dL/d(viscosity multipliers), both optional: per
  * segment it recomputes the stage states from the checkpoint and runs the transposed stages in reverse.
- * Device memory: (nSteps/ckptEvery + 5 ckptEvery + 3) states. The state is left at t_end. No counterpart
+ * Device memory: (nSteps/ckptEvery + 5 ckptEvery + 3) states; when it takes at most half of the free
+ * device memory, the forward intermediates of the 5 ckptEvery stages of a segment are kept as well (about
+ * 8 states per stage), so that the adjoint right-hand sides skip their recomputation (environment variable
+ * FLEXI_GB300_ADJOINT_RECOMPUTE=1 forces the recomputing path). The state is left at t_end. No counterpart
  * in the reference. The channel body force is not covered. */
 int fg_adjoint_forward(fg_handle* h, int nSteps, double dt, int ckptEvery);
 int fg_adjoint_reverse(fg_handle* h, const double* UbarT, double* Ubar0, double* muScaleBar);

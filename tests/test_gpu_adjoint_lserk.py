@@ -78,7 +78,11 @@ def test_lserk_adjoint_against_exact_tangent_and_finite_differences(name):
         assert abs(float(mub @ ds) - fds) <= 1e-7 * abs(fds), (float(mub @ ds), fds)
 
 
-def test_checkpoint_interval_does_not_change_the_gradient():
+@pytest.mark.parametrize("recompute", ["0", "1"])
+def test_checkpoint_interval_does_not_change_the_gradient(recompute, monkeypatch):
+    """Both reverse paths (kept stage intermediates / recomputed ones) and every checkpoint interval give
+    the same gradient."""
+    monkeypatch.setenv("FLEXI_GB300_ADJOINT_RECOMPUTE", recompute)
     f, U0, scale, dt, rng = _setup("gauss3_weak_roeef_br1", seed=4)
     w = rng.standard_normal(U0.shape)
     ref = None
