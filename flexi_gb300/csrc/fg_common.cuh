@@ -68,6 +68,7 @@ struct Dev {
   double* bulkVel; // [nInst]
   double* dpdx;    // [nInst] (0 when no body force)
   double* muScale; // [nElems] viscosity multiplier of each element (null: 1)
+  double* forceField;  // [e][n3] additional x-momentum body force per node, energy source F * bulkVel (null: none)
   int* err;        // [1] sticky error word
   double* dtElem;  // [2][nElems] convective and viscous element time-step limits of the last CALCTIMESTEP
 };

@@ -70,6 +70,75 @@ __global__ void k_adj_axpby(double* __restrict__ G, const double* __restrict__ U
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < count) G[i] = alpha == 0.0 ? beta * U[i] : fma(alpha, G[i], beta * U[i]);
 }
+// body-force adjoint of one RK stage, one CTA per element: Fbar += G_mom1 + bulkVel G_ener (cotangent of the
+// additional body force at each node) and partial[e] += sum_x G_ener (body force at x) (the stage's share of
+// the bulk-velocity cotangent; uniform body force -dpdx plus the field)
+__global__ void k_adj_source(const Dev d, const double* __restrict__ G, double* __restrict__ Fbar, double* __restrict__ partial,
+                             const double* __restrict__ bulkVel, int n3) {
+  __shared__ double red[128];
+  const int e = blockIdx.x;
+  const int inst = d.elemInst[e];
+  const double bv = bulkVel[inst], mdp = -d.dpdx[inst];
+  double s = 0.;
+  for (int x = threadIdx.x; x < n3; x += blockDim.x) {
+    const double g1 = G[((size_t)e * 5 + 1) * n3 + x], g4 = G[((size_t)e * 5 + 4) * n3 + x];
+    if (Fbar) Fbar[(size_t)e * n3 + x] += fma(bv, g4, g1);
+    s = fma(g4, mdp + (d.forceField ? d.forceField[(size_t)e * n3 + x] : 0.), s);
+  }
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[e] += red[0];
+}
+// per-instance bulk-velocity cotangent from the element partials (elements of an instance are contiguous)
+__global__ void k_adj_bulk_reduce(int nInst, const int* instStart, double* partial, double* bulkBar) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nInst) return;
+  double s = 0.;
+  for (int e = instStart[i]; e < instStart[i + 1]; ++e) { s += partial[e]; partial[e] = 0.; }
+  bulkBar[i] = s;
+}
+// Ubar += bulkBar dBulkVel/dU at the step-start state U (testcase.f90:CalcForcing: sum of m1/rho w J / Vol)
+__global__ void k_adj_bulk_apply(const Dev d, double* __restrict__ Ubar, const double* __restrict__ U, const double* __restrict__ bulkBar,
+                                 const double* __restrict__ wVol, const double* __restrict__ instVol, int n3) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)d.nElems * n3) return;
+  const int e = (int)(t / n3), x = (int)(t - (long long)e * n3);
+  const int inst = d.elemInst[e];
+  const double c = bulkBar[inst] * wVol[x] / (d.sJ[(size_t)e * n3 + x] * instVol[inst]);
+  const double rho = U[((size_t)e * 5 + 0) * n3 + x], m1 = U[((size_t)e * 5 + 1) * n3 + x];
+  const double srho = 1.0 / rho;
+  Ubar[((size_t)e * 5 + 0) * n3 + x] -= c * m1 * srho * srho;
+  Ubar[((size_t)e * 5 + 1) * n3 + x] += c * srho;
+}
+// mean wall shear: per wall side point the x-momentum viscous flux through the wall x SurfElem (the shear the
+// fluid exerts on the wall) and SurfElem; with seed != 0 also the cotangent of the master face gradients
+// for the seed's weight (cotangent of the mean)
+__global__ void k_wall_shear(const Dev d, const Basis B, int n2, double* terms, double* areas, double seed, double* gradMb) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= d.nBCSides * n2) return;
+  const int s = t / n2, pq = t - s * n2;
+  const double* gm = d.geo + (size_t)s * FG_NF * n2 + pq;
+  const double nv[3] = {gm[FG_NX * n2], gm[FG_NY * n2], gm[FG_NZ * n2]};
+  const double se = gm[FG_SURF * n2];
+  const double mu = elem_mu(d, d.sideElem[s * 4 + 0]);
+  double g[12];
+  for (int c = 0; c < 12; ++c) g[c] = d.gradM[((size_t)s * 12 + c) * n2 + pq];
+  double F[5];
+  visc_flux_dir(mu, mu * B.lambdaFac, 0., 0., 0., g, nv[0], nv[1], nv[2], F);
+  terms[t] = F[1] * se;
+  areas[t] = se;
+  if (gradMb) {
+    const double Fb[5] = {0., seed * se, 0., 0., 0.};
+    double gb[12] = {0., 0., 0., 0., 0., 0., 0., 0., 0., 0., 0., 0.};
+    double zu = 0., zv = 0., zw = 0., mub = 0.;
+    visc_flux_dir_adj(mu, B.lambdaFac, 0., 0., 0., g, nv[0], nv[1], nv[2], Fb, zu, zv, zw, gb, mub);
+    for (int c = 0; c < 12; ++c) gradMb[((size_t)s * 12 + c) * n2 + pq] = gb[c];
+  }
+}
 // layout conversion between FLEXI's U(v,i,j,k,e) and [e][v][ijk]
 __global__ void k_fortran_to_dev(const double* __restrict__ f, double* __restrict__ d, int nv, int n3, long long total) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -146,6 +215,10 @@ struct fg_handle {
   double* adjGbar = nullptr;
   double* adjUbar = nullptr;
   double* adjUfinal = nullptr;
+  double* adjBulkHist = nullptr;  // [ckptEvery][nInst] bulk velocity of each step of the segment being reversed
+  double* adjPartial = nullptr;   // [nElems] element shares of the bulk-velocity cotangent of the current step
+  double* adjBulkBar = nullptr;   // [nInst]
+  double* adjFbar = nullptr;      // [e][n3] cotangent of the body-force field
   int adjSteps = 0, adjEvery = 0;
   double adjDt = 0.;
   // per-kernel event timing (fg_profile_enable)
@@ -197,6 +270,7 @@ void free_adjoint_store(fg_handle* h) {
   h->adjInter.clear();
   h->adjKeepInter = false;
   h->adjGbar = h->adjUbar = h->adjUfinal = nullptr;
+  h->adjBulkHist = h->adjPartial = h->adjBulkBar = h->adjFbar = nullptr;
   h->adjSteps = h->adjEvery = 0;
 }
 void free_device(fg_handle* h) {
@@ -762,7 +836,6 @@ int fg_rhs_vjp(fg_handle* h, const double* W, double* V, double* muScaleBar) {
 int fg_adjoint_forward(fg_handle* h, int nSteps, double dt, int ckptEvery) {
   if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
   if (const char* why = adjoint_unsupported(h->cfg)) return fail(h, FG_ERR_CONFIG, why);
-  if (h->cfg.doTCSource) return fail(h, FG_ERR_CONFIG, "the time-stepping adjoint does not cover the channel body force");
   if (nSteps < 1 || ckptEvery < 1 || !(dt > 0.) || !std::isfinite(dt)) return fail(h, FG_ERR_CONFIG, "nSteps, ckptEvery >= 1 and dt > 0 required");
   if (int r = ensure_adjoint(h)) return r;
   free_adjoint_store(h);
@@ -800,6 +873,10 @@ int fg_adjoint_forward(fg_handle* h, int nSteps, double dt, int ckptEvery) {
   if (int r = adj_alloc(h, h->adjGbar, cnt)) { free_adjoint_store(h); return r; }
   if (int r = adj_alloc(h, h->adjUbar, cnt)) { free_adjoint_store(h); return r; }
   if (int r = adj_alloc(h, h->adjUfinal, cnt)) { free_adjoint_store(h); return r; }
+  if (int r = adj_alloc(h, h->adjBulkHist, (size_t)ckptEvery * h->d.nInst)) { free_adjoint_store(h); return r; }
+  if (int r = adj_alloc(h, h->adjPartial, (size_t)h->M.nElems)) { free_adjoint_store(h); return r; }
+  if (int r = adj_alloc(h, h->adjBulkBar, (size_t)h->d.nInst)) { free_adjoint_store(h); return r; }
+  if (int r = adj_alloc(h, h->adjFbar, (size_t)h->M.nElems * n3)) { free_adjoint_store(h); return r; }
   h->launches = 0;
   for (int step = 0; step < nSteps; ++step) {
     if (step % ckptEvery == 0) CUDA_TRY(cudaMemcpyAsync(h->adjCkpt[step / ckptEvery], h->d.U, bytes, cudaMemcpyDeviceToDevice, h->st));
@@ -813,7 +890,7 @@ int fg_adjoint_forward(fg_handle* h, int nSteps, double dt, int ckptEvery) {
   return FG_OK;
 }
 
-int fg_adjoint_reverse(fg_handle* h, const double* UbarT, double* Ubar0, double* muScaleBar) {
+int fg_adjoint_reverse(fg_handle* h, const double* UbarT, double* Ubar0, double* muScaleBar, double* forceBar) {
   if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
   if (h->adjSteps < 1) return fail(h, FG_ERR_STATE, "no fg_adjoint_forward run to reverse");
   if (!UbarT) return fail(h, FG_ERR_CONFIG, "null cotangent");
@@ -826,6 +903,12 @@ int fg_adjoint_reverse(fg_handle* h, const double* UbarT, double* Ubar0, double*
   CUDA_TRY(cudaMemcpyAsync(h->dStage, UbarT, bytes, cudaMemcpyHostToDevice, h->st));
   k_fortran_to_dev<<<gridAx, 256, 0, h->st>>>(h->dStage, h->adjUbar, 5, n3, cnt);
   CUDA_TRY(cudaMemsetAsync(h->a.muElemb, 0, sizeof(double) * h->M.nElems, h->st));
+  CUDA_TRY(cudaMemsetAsync(h->adjPartial, 0, sizeof(double) * h->M.nElems, h->st));
+  CUDA_TRY(cudaMemsetAsync(h->adjFbar, 0, sizeof(double) * h->M.nElems * n3, h->st));
+  // with the channel forcing, each step's bulk velocity is a function of its start state, and the energy
+  // source of the body force (uniform and/or field) couples to it
+  const bool bulkAdj = h->cfg.doTCSource != 0;
+  const int nI = h->d.nInst;
   AdjDev a = h->a;
   a.accumulate = 1;
   a.Ub = h->adjUbar;
@@ -837,6 +920,7 @@ int fg_adjoint_reverse(fg_handle* h, const double* UbarT, double* Ubar0, double*
     CUDA_TRY(cudaMemcpyAsync(h->d.U, h->adjCkpt[seg], bytes, cudaMemcpyDeviceToDevice, h->st));
     for (int s = 0; s < ns; ++s) {
       launch_step_setup(h, 1, dt, false);
+      CUDA_TRY(cudaMemcpyAsync(h->adjBulkHist + (size_t)s * nI, h->d.bulkVel, sizeof(double) * nI, cudaMemcpyDeviceToDevice, h->st));
       for (int k = 1; k <= 5; ++k) {
         const size_t slot = (size_t)s * 5 + k - 1;
         CUDA_TRY(cudaMemcpyAsync(h->adjStage[slot], h->d.U, bytes, cudaMemcpyDeviceToDevice, h->st));
@@ -854,6 +938,8 @@ int fg_adjoint_reverse(fg_handle* h, const double* UbarT, double* Ubar0, double*
     for (int s = ns - 1; s >= 0; --s) {
       for (int k = 5; k >= 1; --k) {
         k_adj_axpby<<<gridAx, 256, 0, h->st>>>(h->adjGbar, h->adjUbar, k == 5 ? 0. : -h->RKA[k + 1], h->RKb[k] * dt, cnt);
+        k_adj_source<<<h->M.nElems, 128, 0, h->st>>>(h->d, h->adjGbar, h->adjFbar, h->adjPartial, h->adjBulkHist + (size_t)s * nI, n3);
+        h->launches += 1;
         const size_t slot = (size_t)s * 5 + k - 1;
         if (h->adjKeepInter) {
           launch_vjp_kept(h, h->adjInter[slot], a);
@@ -864,6 +950,12 @@ int fg_adjoint_reverse(fg_handle* h, const double* UbarT, double* Ubar0, double*
         }
         h->launches += 1;
       }
+      if (bulkAdj) {
+        // the step's bulk velocity depends on its start state (stage 1 input)
+        k_adj_bulk_reduce<<<(nI + 127) / 128, 128, 0, h->st>>>(nI, h->dInstStart, h->adjPartial, h->adjBulkBar);
+        k_adj_bulk_apply<<<gridAx, 256, 0, h->st>>>(h->d, h->adjUbar, h->adjStage[(size_t)s * 5], h->adjBulkBar, h->dWVol, h->dInstVol, n3);
+        h->launches += 2;
+      }
     }
   }
   CUDA_TRY(cudaGetLastError());
@@ -871,8 +963,73 @@ int fg_adjoint_reverse(fg_handle* h, const double* UbarT, double* Ubar0, double*
   CUDA_TRY(cudaMemcpyAsync(h->d.U, h->adjUfinal, bytes, cudaMemcpyDeviceToDevice, h->st));
   if (Ubar0) { if (int r = export_field(h, h->adjUbar, 5, 0, 5, Ubar0)) return r; }
   if (muScaleBar) CUDA_TRY(cudaMemcpyAsync(muScaleBar, h->a.muElemb, sizeof(double) * h->M.nElems, cudaMemcpyDeviceToHost, h->st));
+  if (forceBar) { if (int r = export_field(h, h->adjFbar, 1, 0, 1, forceBar)) return r; }
   CUDA_TRY(cudaStreamSynchronize(h->st));
   return FG_OK;
+}
+
+int fg_set_body_force_field(fg_handle* h, const double* F) {
+  if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
+  const int n3 = h->M.n * h->M.n * h->M.n;
+  const long long total = (long long)h->M.nElems * n3;
+  if (!h->d.forceField) {
+    if (!F) return FG_OK;
+    if (int r = dalloc(h, h->d.forceField, (size_t)total)) return r;
+    // the captured time loop holds the device pointers by value: capture it again with the field
+    if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+  }
+  if (F) {
+    CUDA_TRY(cudaMemcpyAsync(h->dStage, F, total * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    k_fortran_to_dev<<<(unsigned)((total + 255) / 256), 256, 0, h->st>>>(h->dStage, h->d.forceField, 1, n3, total);
+  } else {
+    k_fill<<<(unsigned)((total + 255) / 256), 256, 0, h->st>>>(h->d.forceField, 0., (int)total);
+  }
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(h->st));
+  return FG_OK;
+}
+
+int fg_wall_shear(fg_handle* h, double* J, double* dJdU) {
+  if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
+  if (h->M.nBCSides == 0) return fail(h, FG_ERR_MESH, "the mesh has no wall sides");
+  if (dJdU) {
+    if (const char* why = adjoint_unsupported(h->cfg)) return fail(h, FG_ERR_CONFIG, why);
+    if (int r = ensure_adjoint(h)) return r;
+  }
+  const int n = h->M.n, n2 = n * n, n3 = n2 * n, nE = h->M.nElems, nS = h->M.nSides, nBC = h->M.nBCSides;
+  h->launches = 0;
+  const Dev& d = h->d;
+  h->K.prep(d, h->B, h->st);
+  h->K.lift(d, h->B, h->st);
+  // per-point terms in the (otherwise unused) staging buffer: [0, nBC n2) terms, [nBC n2, 2 nBC n2) areas
+  double* terms = h->dStage;
+  double* areas = h->dStage + (size_t)nBC * n2;
+  const int pts = nBC * n2;
+  k_wall_shear<<<(pts + 127) / 128, 128, 0, h->st>>>(d, h->B, n2, terms, areas, 0., nullptr);
+  std::vector<double> tv(pts), av(pts);
+  CUDA_TRY(cudaMemcpyAsync(tv.data(), terms, sizeof(double) * pts, cudaMemcpyDeviceToHost, h->st));
+  CUDA_TRY(cudaMemcpyAsync(av.data(), areas, sizeof(double) * pts, cudaMemcpyDeviceToHost, h->st));
+  CUDA_TRY(cudaStreamSynchronize(h->st));
+  double T = 0., A = 0.;
+  for (int i = 0; i < pts; ++i) { T += tv[i]; A += av[i]; }
+  if (J) *J = T / A;
+  if (!dJdU) return FG_OK;
+  AdjDev a = h->a;
+  a.accumulate = 0;
+  CUDA_TRY(cudaMemsetAsync(a.Ub, 0, sizeof(double) * nE * 5 * n3, h->st));
+  CUDA_TRY(cudaMemsetAsync(a.gb, 0, sizeof(double) * nE * 12 * n3, h->st));
+  CUDA_TRY(cudaMemsetAsync(a.gradMb, 0, sizeof(double) * nS * 12 * n2, h->st));
+  CUDA_TRY(cudaMemsetAsync(a.gradSb, 0, sizeof(double) * nS * 12 * n2, h->st));
+  CUDA_TRY(cudaMemsetAsync(a.faceMb, 0, sizeof(double) * nS * FS_NF * n2, h->st));
+  CUDA_TRY(cudaMemsetAsync(a.faceSb, 0, sizeof(double) * nS * FS_NF * n2, h->st));
+  CUDA_TRY(cudaMemsetAsync(a.muSideb, 0, sizeof(double) * nS * 2 * n2, h->st));
+  CUDA_TRY(cudaMemsetAsync(a.muElemb, 0, sizeof(double) * nE, h->st));
+  k_wall_shear<<<(pts + 127) / 128, 128, 0, h->st>>>(d, h->B, n2, terms, areas, 1.0 / A, a.gradMb);
+  h->K.lift_adj(d, a, h->B, h->st);
+  h->K.prep_adj(d, a, h->B, h->st);
+  h->launches += 6;
+  CUDA_TRY(cudaGetLastError());
+  return export_field(h, a.Ub, 5, 0, 5, dJdU);
 }
 
 int fg_calc_timestep(fg_handle* h, double* dt, int* errType) {

@@ -478,6 +478,11 @@ __device__ __forceinline__ void finish_node(const Dev& d, const SBasis<n>& Bs, c
     ut[1] -= dpdx;
     ut[4] -= dpdx * d.bulkVel[inst];
   }
+  if (d.forceField) {  // additional per-node body force of the same form
+    const double F = d.forceField[(size_t)e * n3 + x];
+    ut[1] += F;
+    ut[4] += F * d.bulkVel[inst];
+  }
   if (st.mode == 0) {
 #pragma unroll
     for (int v = 0; v < 5; ++v) d.Ut[((size_t)e * 5 + v) * n3 + x] = ut[v];

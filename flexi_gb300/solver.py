@@ -231,13 +231,29 @@ class Flexi:
         """Advances n_steps LSERK steps of fixed dt, keeping a checkpoint every ckpt_every steps."""
         self._check(self.L.fg_adjoint_forward(self.h, int(n_steps), float(dt), int(ckpt_every)), "fg_adjoint_forward")
 
-    def adjoint_reverse(self, UbarT):
-        """(Ubar0, mu_bar) for the cotangent UbarT of the final state of the last adjoint_forward."""
+    def adjoint_reverse(self, UbarT, force_bar=False):
+        """(Ubar0, mu_bar[, force_bar]) for the cotangent UbarT of the final state of the last adjoint_forward."""
         UbarT = np.ascontiguousarray(UbarT, np.float64).reshape(self.ushape)
         Ub0 = np.empty(self.ushape)
         mub = np.empty(self.n_elems)
-        self._check(self.L.fg_adjoint_reverse(self.h, _p(UbarT), _p(Ub0), _p(mub)), "fg_adjoint_reverse")
-        return Ub0, mub
+        fb = np.empty(self.ushape[:-1]) if force_bar else None
+        self._check(self.L.fg_adjoint_reverse(self.h, _p(UbarT), _p(Ub0), _p(mub), _p(fb) if force_bar else None), "fg_adjoint_reverse")
+        return (Ub0, mub, fb) if force_bar else (Ub0, mub)
+
+    def set_body_force_field(self, F):
+        """Additional per-node x-momentum body force, shape (nElems, n, n, n) (None: zero)."""
+        if F is None:
+            self._check(self.L.fg_set_body_force_field(self.h, None), "fg_set_body_force_field")
+            return
+        F = np.ascontiguousarray(F, np.float64).reshape(self.ushape[:-1])
+        self._check(self.L.fg_set_body_force_field(self.h, _p(F)), "fg_set_body_force_field")
+
+    def wall_shear(self, grad=False):
+        """Mean wall shear J of the current state (and dJ/dU with grad=True)."""
+        J = ctypes.c_double(0.0)
+        g = np.empty(self.ushape) if grad else None
+        self._check(self.L.fg_wall_shear(self.h, ctypes.byref(J), _p(g) if grad else None), "fg_wall_shear")
+        return (J.value, g) if grad else J.value
 
     def stream(self):
         s = ctypes.c_void_p()

@@ -191,9 +191,23 @@ int fg_rhs_vjp(fg_handle* h, const double* W, double* V, double* muScaleBar);
  * device memory, the forward intermediates of the 5 ckptEvery stages of a segment are kept as well (about
  * 8 states per stage), so that the adjoint right-hand sides skip their recomputation (environment variable
  * FLEXI_GB300_ADJOINT_RECOMPUTE=1 forces the recomputing path). The state is left at t_end. No counterpart
- * in the reference. The channel body force is not covered. */
+ * in the reference. */
 int fg_adjoint_forward(fg_handle* h, int nSteps, double dt, int ckptEvery);
-int fg_adjoint_reverse(fg_handle* h, const double* UbarT, double* Ubar0, double* muScaleBar);
+/* forceBar(0:N,0:N,0:N,nElems) (optional) = dL/d(body-force field of fg_set_body_force_field). With the channel
+ * body force or a body-force field, the dependence of each step's bulk velocity on its start state is
+ * included. */
+int fg_adjoint_reverse(fg_handle* h, const double* UbarT, double* Ubar0, double* muScaleBar, double* forceBar);
+
+/* Additional x-momentum body-force field F(0:N,0:N,0:N,nElems) with the form of the channel forcing
+ * (testcase/channel/testcase.f90:361-362): Ut(MOM1) += F, Ut(ENER) += F * BulkVel (after the Jacobian);
+ * NULL sets it to zero. No counterpart in the reference (the parameter of a gradient study). */
+int fg_set_body_force_field(fg_handle* h, const double* F);
+
+/* Mean wall shear of the current state: J = sum over wall side points of the x-momentum viscous flux through
+ * the wall times SurfElem, divided by the wall area (the lifted face gradients of the master side, as in
+ * GetBoundaryFlux). dJdU (optional, layout of U) = dJ/dU through the lifting. No counterpart in the
+ * reference. */
+int fg_wall_shear(fg_handle* h, double* J, double* dJdU);
 
 /* FP64 FMA throughput probe (TFLOP/s, 2 flop per FMA) of the current device, used for the roofline. */
 int fg_probe_fp64(double* tflops);

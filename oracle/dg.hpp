@@ -110,7 +110,10 @@ struct DG {
   std::vector<R> LiftFlux, FluxX, FluxY, FluxZ;  // lifting side fluxes
   std::vector<R> Flux_master, Flux_slave;
   std::vector<R> Ut_tmp;
-  double BulkVel = 0.;
+  R BulkVel = R(0.);
+  // additional per-node x-momentum body force (an extension of the channel source for the differentiation
+  // study: energy source F * BulkVel as for the uniform one; empty = none)
+  std::vector<R> forceField;
   // per-element viscosity multiplier (an extension for the differentiation study; empty = 1)
   std::vector<double> muScale;
   std::vector<R> muScaleR;
@@ -814,7 +817,12 @@ struct DG {
       for (int v = 0; v < 5; ++v) ut[v] = -ut[v];
       if (C.doTCSource) {
         ut[1] = ut[1] - R(C.dpdx) / R(sj);
-        ut[4] = ut[4] - R(C.dpdx) / R(sj) * R(BulkVel);
+        ut[4] = ut[4] - R(C.dpdx) / R(sj) * BulkVel;
+      }
+      if (!forceField.empty()) {
+        const R F = forceField[(size_t)e * nv3 + x];
+        ut[1] = ut[1] + F / R(sj);
+        ut[4] = ut[4] + F / R(sj) * BulkVel;
       }
       for (int v = 0; v < 5; ++v) ut[v] = ut[v] * R(sj);
     }
@@ -828,12 +836,12 @@ struct DG {
   // channel testcase.f90:CalcForcing -- bulk velocity (done once per time step before the RK stages)
   void calc_forcing() {
     const size_t nv3 = (size_t)n * n * n;
-    double bv = 0.;
+    R bv = R(0.);
     for (int e = 0; e < nE; ++e) for (size_t x = 0; x < nv3; ++x) {
       size_t g = (size_t)e * nv3 + x;
-      bv += val(U[g * 5 + 1]) / val(U[g * 5 + 0]) * M.wGPVol[x] / M.sJ[g];
+      bv = bv + U[g * 5 + 1] / U[g * 5 + 0] * R(M.wGPVol[x] / M.sJ[g]);
     }
-    BulkVel = bv / M.Vol;
+    BulkVel = bv / R(M.Vol);
   }
 
   // timestep.f90:TimeStepByLSERKW2

@@ -47,7 +47,8 @@ def lib():
         _lib.orc_set_bulk_velocity.argtypes = [P, ctypes.c_double]
         _lib.orc_set_mu_scale.argtypes = [P, P]
         _lib.orc_jvp.argtypes = [P, P, P]
-        _lib.orc_jvp_solve.argtypes = [P, P, P, ctypes.c_int, ctypes.c_double, P]
+        _lib.orc_jvp_solve.argtypes = [P, P, P, P, ctypes.c_int, ctypes.c_double, P]
+        _lib.orc_set_force_field.argtypes = [P, P]
         _lib.orc_fd_jvp.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_double, P]
         _lib.orc_sizes.argtypes = [P, P]
         _lib.orc_mesh_array.argtypes = [P, ctypes.c_int, P]
@@ -149,13 +150,24 @@ class Oracle:
             raise RuntimeError("oracle: " + lib().orc_last_error().decode())
         return JV
 
-    def jvp_solve(self, V, n_steps, dt, d_scale=None):
-        """Exact tangent of n_steps LSERK steps of fixed dt (dual numbers): dU(t_end)/dU(t_0) V plus
-        dU(t_end)/d(viscosity multipliers) d_scale (V or d_scale may be None)."""
+    def set_force_field(self, F):
+        """Additional per-node x-momentum body force, shape (nElems, n, n, n) (None: none)."""
+        if F is None:
+            lib().orc_set_force_field(self.h, None)
+            return
+        self._force = np.ascontiguousarray(F, dtype=np.float64).reshape(self.ushape[:-1])
+        lib().orc_set_force_field(self.h, _p(self._force))
+
+    def jvp_solve(self, V, n_steps, dt, d_scale=None, d_force=None):
+        """Exact tangent of n_steps LSERK steps of fixed dt (dual numbers, bulk velocity included): the
+        directional derivative of U(t_end) along V (initial state), d_scale (viscosity multipliers) and
+        d_force (body-force field); any of them may be None."""
         Vp = None if V is None else np.ascontiguousarray(V, dtype=np.float64).reshape(self.ushape)
         Sp = None if d_scale is None else np.ascontiguousarray(d_scale, dtype=np.float64).reshape(self.n_elems)
+        Fp = None if d_force is None else np.ascontiguousarray(d_force, dtype=np.float64).reshape(self.ushape[:-1])
         JV = np.empty(self.ushape)
-        if lib().orc_jvp_solve(self.h, None if Vp is None else _p(Vp), None if Sp is None else _p(Sp), int(n_steps), float(dt), _p(JV)) != 0:
+        if lib().orc_jvp_solve(self.h, None if Vp is None else _p(Vp), None if Sp is None else _p(Sp), None if Fp is None else _p(Fp),
+                               int(n_steps), float(dt), _p(JV)) != 0:
             raise RuntimeError("oracle: " + lib().orc_last_error().decode())
         return JV
 

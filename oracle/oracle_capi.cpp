@@ -93,6 +93,12 @@ int orc_timestep(void* hp, double* t, double dt) {
 }
 double orc_calc_timestep(void* hp, int* err) { return ((OrcHandle*)hp)->dg.calc_timestep(*err); }
 
+// additional per-node x-momentum body force, layout of U without the variable index (NULL: none)
+void orc_set_force_field(void* hp, const double* F) {
+  auto& d = ((OrcHandle*)hp)->dg;
+  if (F) d.forceField.assign(F, F + d.U.size() / 5); else d.forceField.clear();
+}
+
 // per-element viscosity multiplier (NULL: all ones)
 void orc_set_mu_scale(void* hp, const double* s) {
   auto& d = ((OrcHandle*)hp)->dg;
@@ -108,6 +114,7 @@ int orc_jvp(void* hp, const double* V, double* JV) {
     const DG<double>& d = h->dg;
     dd.muScale = d.muScale;
     dd.BulkVel = d.BulkVel;
+    dd.forceField.assign(d.forceField.begin(), d.forceField.end());
     for (size_t i = 0; i < d.U.size(); ++i) dd.U[i] = DD(d.U[i], V[i]);
     dd.time_derivative(0.);
     for (size_t i = 0; i < d.U.size(); ++i) JV[i] = dd.Ut[i].d;
@@ -118,7 +125,7 @@ int orc_jvp(void* hp, const double* V, double* JV) {
 // exact tangent of nSteps LSERK steps of fixed dt from the current state (dual numbers):
 // JV = dU(t_end)/dU(t_0) V + dU(t_end)/d(viscosity multipliers) dScale (either direction may be NULL);
 // the state of the double instance is not changed
-int orc_jvp_solve(void* hp, const double* V, const double* dScale, int nSteps, double dt, double* JV) {
+int orc_jvp_solve(void* hp, const double* V, const double* dScale, const double* dForce, int nSteps, double dt, double* JV) {
   auto* h = (OrcHandle*)hp;
   try {
     if (!h->dgd) { h->dgd.reset(new DG<DD>()); h->dgd->init(h->cfg, h->mi); }
@@ -129,11 +136,18 @@ int orc_jvp_solve(void* hp, const double* V, const double* dScale, int nSteps, d
     if (dScale)
       for (int e = 0; e < d.nE; ++e) dd.muScaleR.push_back(DD(d.muScale.empty() ? 1.0 : d.muScale[e], dScale[e]));
     dd.BulkVel = d.BulkVel;
+    dd.forceField.clear();
+    if (dForce || !d.forceField.empty())
+      for (size_t i = 0; i < d.U.size() / 5; ++i) dd.forceField.push_back(DD(d.forceField.empty() ? 0. : d.forceField[i], dForce ? dForce[i] : 0.));
     for (size_t i = 0; i < d.U.size(); ++i) dd.U[i] = DD(d.U[i], V ? V[i] : 0.);
     double t = 0.;
-    for (int s = 0; s < nSteps; ++s) dd.timestep_lserkw2(t, dt);
+    for (int s = 0; s < nSteps; ++s) {
+      if (dd.C.doTCSource) dd.calc_forcing();
+      dd.timestep_lserkw2(t, dt);
+    }
     for (size_t i = 0; i < d.U.size(); ++i) JV[i] = dd.U[i].d;
     dd.muScaleR.clear();
+    dd.forceField.clear();
     return 0;
   } catch (std::exception& e) { g_err = e.what(); return 1; }
 }
@@ -169,7 +183,7 @@ int orc_fd_jvp(void* hp, const double* V, int fdOrder, int epsMethod, double sca
     return 0;
   } catch (std::exception& e) { g_err = e.what(); return 1; }
 }
-double orc_bulk_velocity(void* hp) { auto& d = ((OrcHandle*)hp)->dg; d.calc_forcing(); return d.BulkVel; }
+double orc_bulk_velocity(void* hp) { auto& d = ((OrcHandle*)hp)->dg; d.calc_forcing(); return val(d.BulkVel); }
 void orc_set_bulk_velocity(void* hp, double bv) { ((OrcHandle*)hp)->dg.BulkVel = bv; }
 
 // mesh arrays for comparison and for the drop-in (fg_set_mesh) path
