@@ -52,7 +52,7 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--elems", type=int, default=32, help="elements per direction")
     p.add_argument("--riemann", default="hllc", choices=sorted(RIEMANN_IDS), help="surface Riemann solver")
-    p.add_argument("--workload", default="tgv", choices=["tgv", "ensemble", "adjoint"],
+    p.add_argument("--workload", default="tgv", choices=["tgv", "ensemble", "adjoint", "adjoint-channel"],
                    help="tgv: the single-case N=7 TGV; ensemble: 256 independent TGV/vortex instances at N=5 against a loop over "
                         "instances; adjoint: gradient of a kinetic-energy loss over a 200-step TGV solve (16^3, N=5)")
     p.add_argument("--ckpt", type=int, default=20, help="adjoint: checkpoint interval in steps")
@@ -657,6 +657,97 @@ def run_adjoint(args):
     print(json.dumps(line), flush=True)
 
 
+ADJOINT_CHANNEL_METRIC = "adjoint/forward cost ratio (channel 24x12x12, N=7 GL split PI, 500 LSERK steps)"
+
+
+def run_adjoint_channel(args):
+    """Gradient of the mean wall shear after a forward channel solve with respect to the body-force field."""
+    import numpy as np
+    import torch
+
+    ws, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    from flexi_gb300 import mesh as fmesh, testcases
+    from flexi_gb300.solver import Flexi, make_config
+
+    n_steps = 500 if args.steps == 20 else args.steps
+    mu0 = 1.0 / 2800.0  # Re_b = rho_b U_b h / mu = 2800 with rho_b = U_b = h = 1
+    dpdx = -3.0 * mu0   # the body force that balances the wall shear of the laminar profile
+    c = make_config(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roe", Lifting="br1", kappa=1.4, R=1.0, Pr=0.72, mu0=mu0,
+                    CFLScale=0.8, DFLScale=0.8, doTCSource=1, dpdx=dpdx)
+    m = fmesh.channel_box((24, 12, 12), beta=1.5, t_wall=1.0)
+    f = Flexi(c, m)
+    xgp = f.elem_xgp()
+    U0 = testcases.channel_state(xgp, mach=0.1, kappa=1.4, R=1.0, t_wall=1.0, noise=0.05, seed=rank)
+    f.U = U0
+    dt = float(np.atleast_1d(f.CalcTimeStep()[0])[0])
+    dof = f.n_elems * f.n ** 3
+    stream = torch.cuda.ExternalStream(f.stream())
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        out = fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return out, a.elapsed_time(b)
+
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    f.adjoint_forward(args.warmup, dt, args.ckpt)
+    f.adjoint_reverse(np.zeros(f.ushape))
+    f.U = U0
+    f.TimeDisc(2)
+    f.U = U0
+    _, ms_plain = timed(lambda: f.TimeDisc(n_steps))
+    f.U = U0
+    clocks = ClockSampler(local)
+    clocks.start()
+    _, ms_fwd = timed(lambda: f.adjoint_forward(n_steps, dt, args.ckpt))
+    adj_bytes = free0 - torch.cuda.mem_get_info()[0]
+    (J, dJdU), ms_seed = timed(lambda: f.wall_shear(grad=True))
+    (Ub0, mub, Fbar), ms_rev = timed(lambda: f.adjoint_reverse(dJdU, force_bar=True))
+    clk = clocks.stop()
+    # directional check along one smooth body-force mode with a Richardson-extrapolated central difference
+    # of the same fixed-dt solve (approximate: the Roe flux has kinks a difference quotient can straddle)
+    dF = 0.1 * abs(dpdx) * np.cos(xgp[..., 0]) * (1.0 - xgp[..., 1] ** 2)
+
+    def J_of(h):
+        f.set_body_force_field(h * dF)
+        f.U = U0
+        t = 0.0
+        for _ in range(n_steps):
+            t = f.TimeStepByLSERKW2(t, dt)
+        return f.wall_shear()
+
+    d1 = (J_of(1.0) - J_of(-1.0)) / 2.0
+    d2 = (J_of(2.0) - J_of(-2.0)) / 4.0
+    f.set_body_force_field(None)
+    fd = (4.0 * d1 - d2) / 3.0
+    ad = float((Fbar * dF).sum())
+    if rank != 0:
+        return
+    line = {"metric": ADJOINT_CHANNEL_METRIC, "value": ms_rev / ms_plain, "unit": "reverse time / forward time", "n_gpus": ws,
+            "steps": n_steps, "warmup": args.warmup, "ms_per_step": ms_rev / n_steps, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"channel [0,2pi]x[-1,1]x[0,pi], 24x12x12 elements tanh-stretched (beta=1.5), isothermal walls, "
+                                   f"N=7 Gauss-Lobatto, split PI, Roe, BR1, body force dpdx=-3 mu, Ma=0.1, Re_b=2800, laminar profile + 5% "
+                                   f"seeded noise, FP64, {n_steps} LSERK steps of fixed dt, checkpoint every {args.ckpt} steps; gradient of the "
+                                   "mean wall shear at t_end w.r.t. the body-force field",
+                       "n_elems": f.n_elems, "N": 7, "dof": dof, "dt": dt, "l2": "inputs larger than L2 (state 71 MB)"},
+            "forward_ms_per_step": ms_plain / n_steps, "forward": "the plain solver's graph-replayed time loop (fg_run)",
+            "forward_with_checkpoints_ms_per_step": ms_fwd / n_steps, "reverse_ms_per_step": ms_rev / n_steps,
+            "wall_shear_gradient_ms": ms_seed, "adjoint_device_memory_gb": adj_bytes / 1e9, "mean_wall_shear": J,
+            "body_force_gradient_norm": float(np.sqrt((Fbar ** 2).sum())),
+            "fd_check": {"direction": "0.1 |dpdx| cos(x) (1 - y^2)", "adjoint": ad, "fd_richardson": fd,
+                         "rel_err": abs(ad - fd) / max(abs(fd), 1e-300)},
+            "e2e": {"value": ms_rev / ms_plain, "unit": "reverse time / forward time", "h2d_bytes_per_step": dof * 5 * 8 / n_steps,
+                    "d2h_bytes_per_step": dof * 6 * 8 / n_steps},
+            "gpu_launches": None, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -665,6 +756,8 @@ def main():
         run_ensemble(args)
     elif args.workload == "adjoint":
         run_adjoint(args)
+    elif args.workload == "adjoint-channel":
+        run_adjoint_channel(args)
     else:
         run_gb300(args)
 
