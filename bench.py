@@ -629,7 +629,7 @@ def run_adjoint(args):
     JV = o.fd_jvp(V, fd_order=2, eps_method=1)
     f.U = UT
     f.set_elem_mu_scale(scale)
-    JTW, _ = f.rhs_vjp(W)
+    JTW, _ = f.vjp_time_derivative(W)
     dot_err = abs(float((JV * W).sum()) - float((V * JTW).sum())) / float(np.abs(JV * W).sum())
     nck = (n_steps + args.ckpt - 1) // args.ckpt
     mem_states_gb = (nck + 5 * args.ckpt + 3) * dof * 5 * 8 / 1e9

@@ -19,8 +19,8 @@ EXPORTS = ["fg_config_default", "fg_config_from_ini", "fg_create", "fg_destroy",
            "fg_set_instance_mu0", "fg_get_elem_xgp", "fg_get_sizes", "fg_get_mesh_array", "fg_get_side_to_elem", "fg_set_state",
            "fg_get_state", "fg_state_device_ptr", "fg_time_derivative", "fg_calc_timestep", "fg_get_dt_elem", "fg_timestep_lserkw2", "fg_run",
            "fg_get_gradients", "fg_get_stream", "fg_launch_count", "fg_debug_array", "fg_profile_enable", "fg_profile_read", "fg_probe_fp64",
-           "fg_time_derivative_noalloc", "fg_set_elem_mu_scale", "fg_rhs_vjp", "fg_adjoint_forward", "fg_adjoint_reverse",
-           "fg_set_body_force_field", "fg_wall_shear"]
+           "fg_time_derivative_noalloc", "fg_set_elem_mu_scale", "fg_vjp_time_derivative", "fg_adjoint_forward", "fg_adjoint_reverse",
+           "fg_set_body_force_field", "fg_wall_shear", "fg_jvp_time_derivative"]
 
 
 class FgDeviceMesh(ctypes.Structure):
@@ -71,7 +71,8 @@ def load(path=None):
     L.fg_profile_read.argtypes = [P, P, P]
     L.fg_probe_fp64.argtypes = [ctypes.POINTER(D)]
     L.fg_set_elem_mu_scale.argtypes = [P, P]
-    L.fg_rhs_vjp.argtypes = [P, P, P, P]
+    L.fg_vjp_time_derivative.argtypes = [P, D, P, P, P]
+    L.fg_jvp_time_derivative.argtypes = [P, D, P, P, I, I, D]
     L.fg_adjoint_forward.argtypes = [P, I, D, I]
     L.fg_adjoint_reverse.argtypes = [P, P, P, P, P]
     L.fg_set_body_force_field.argtypes = [P, P]

@@ -2,7 +2,7 @@
 
 For gradient checks and loss-driven studies: tensors are CPU float64 in the layout of U
 (nElems, N+1, N+1, N+1, 5); the solver keeps its own device state. The backward passes call the
-hand-written adjoint kernels through the C ABI (fg_rhs_vjp, fg_adjoint_forward/fg_adjoint_reverse);
+hand-written adjoint kernels through the C ABI (fg_vjp_time_derivative, fg_adjoint_forward/fg_adjoint_reverse);
 nothing is differentiated by torch itself.
 """
 import numpy as np
@@ -26,7 +26,7 @@ class TimeDerivative(torch.autograd.Function):
     def backward(ctx, gUt):
         (U,) = ctx.saved_tensors
         ctx.solver.U = U.detach().cpu().numpy()
-        V, _ = ctx.solver.rhs_vjp(np.ascontiguousarray(gUt.detach().cpu().numpy()))
+        V, _ = ctx.solver.vjp_time_derivative(np.ascontiguousarray(gUt.detach().cpu().numpy()))
         return torch.from_numpy(V), None
 
 

@@ -139,6 +139,27 @@ __global__ void k_wall_shear(const Dev d, const Basis B, int n2, double* terms, 
     for (int c = 0; c < 12; ++c) gradMb[((size_t)s * 12 + c) * n2 + pq] = gb[c];
   }
 }
+// finite-difference JVP helpers: out = x + alpha y; out = (a - b) s; per-block partial sums of x.x
+__global__ void k_axpy_out(double* __restrict__ out, const double* __restrict__ x, double alpha, const double* __restrict__ y, long long count) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) out[i] = fma(alpha, y[i], x[i]);
+}
+__global__ void k_fd_diff(double* out, const double* a, const double* b, double s, long long count) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) out[i] = (a[i] - b[i]) * s;
+}
+__global__ void k_sumsq_partial(const double* __restrict__ x, long long count, double* __restrict__ partial) {
+  __shared__ double red[256];
+  double s = 0.;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x) s = fma(x[i], x[i], s);
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
 // layout conversion between FLEXI's U(v,i,j,k,e) and [e][v][ijk]
 __global__ void k_fortran_to_dev(const double* __restrict__ f, double* __restrict__ d, int nv, int n3, long long total) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -200,7 +221,7 @@ struct fg_handle {
   long long launches = 0;
   std::string err;
   std::vector<double> instMu0;
-  // adjoint buffers (allocated on the first fg_rhs_vjp)
+  // adjoint buffers (allocated on the first fg_vjp_time_derivative)
   AdjDev a{};
   bool haveAdj = false;
   // LSERK adjoint: U checkpoints of the last fg_adjoint_forward, stage states of one segment, the
@@ -219,6 +240,11 @@ struct fg_handle {
   double* adjPartial = nullptr;   // [nElems] element shares of the bulk-velocity cotangent of the current step
   double* adjBulkBar = nullptr;   // [nInst]
   double* adjFbar = nullptr;      // [e][n3] cotangent of the body-force field
+  // finite-difference JVP (fg_jvp_time_derivative): saved state, perturbation, result, reduction partials
+  double* jvpXk = nullptr;
+  double* jvpV = nullptr;
+  double* jvpR = nullptr;
+  double* jvpPartial = nullptr;
   int adjSteps = 0, adjEvery = 0;
   double adjDt = 0.;
   // per-kernel event timing (fg_profile_enable)
@@ -283,6 +309,7 @@ void free_device(fg_handle* h) {
   h->haveMesh = false;
   h->haveAdj = false;
   h->a = AdjDev{};
+  h->jvpXk = h->jvpV = h->jvpR = h->jvpPartial = nullptr;
 }
 
 void init_basis(fg_handle* h) {
@@ -813,7 +840,65 @@ int fg_set_elem_mu_scale(fg_handle* h, const double* scale) {
   return FG_OK;
 }
 
-int fg_rhs_vjp(fg_handle* h, const double* W, double* V, double* muScaleBar) {
+int fg_jvp_time_derivative(fg_handle* h, double t, const double* V, double* JV, int fdOrder, int epsMethod, double scaleps) {
+  (void)t;  // no time-dependent source on this path
+  if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
+  if (!V || !JV) return fail(h, FG_ERR_CONFIG, "null vector");
+  if ((fdOrder != 1 && fdOrder != 2) || (epsMethod != 1 && epsMethod != 2) || !(scaleps > 0.))
+    return fail(h, FG_ERR_CONFIG, "fdOrder 1/2, epsMethod 1/2 and scaleps > 0 required");
+  const int n3 = h->M.n * h->M.n * h->M.n;
+  const long long cnt = (long long)h->M.nElems * 5 * n3;
+  const size_t bytes = (size_t)cnt * sizeof(double);
+  const unsigned grid = (unsigned)((cnt + 255) / 256);
+  const int nPart = 1024;
+  if (!h->jvpXk) {
+    int r = 0;
+    if ((r = dalloc(h, h->jvpXk, (size_t)cnt)) || (r = dalloc(h, h->jvpV, (size_t)cnt)) || (r = dalloc(h, h->jvpR, (size_t)cnt)) ||
+        (r = dalloc(h, h->jvpPartial, (size_t)nPart))) return r;
+  }
+  h->launches = 0;
+  // step size of InitImplicit / MatrixVector: |V| from the host vector, |Xk| from the device state
+  double Vabs = 0.;
+  for (long long i = 0; i < cnt; ++i) Vabs += V[i] * V[i];
+  if (!(Vabs > 0.)) return fail(h, FG_ERR_CONFIG, "zero direction");
+  double normXk = 0.;
+  if (epsMethod == 2) {
+    k_sumsq_partial<<<nPart, 256, 0, h->st>>>(h->d.U, cnt, h->jvpPartial);
+    std::vector<double> part(nPart);
+    CUDA_TRY(cudaMemcpyAsync(part.data(), h->jvpPartial, sizeof(double) * nPart, cudaMemcpyDeviceToHost, h->st));
+    CUDA_TRY(cudaStreamSynchronize(h->st));
+    for (double p : part) normXk += p;
+    normXk = std::sqrt(normXk);
+  }
+  const double mach = 2.220446049250313e-16;
+  const double rEps0 = fdOrder == 1 ? scaleps * std::sqrt(mach) : std::cbrt(scaleps * scaleps * 0.5 * mach);
+  double eps = rEps0 / std::sqrt(Vabs);
+  if (epsMethod == 2) eps *= std::sqrt(1. + normXk);
+  CUDA_TRY(cudaMemcpyAsync(h->dStage, V, bytes, cudaMemcpyHostToDevice, h->st));
+  k_fortran_to_dev<<<grid, 256, 0, h->st>>>(h->dStage, h->jvpV, 5, n3, cnt);
+  CUDA_TRY(cudaMemcpyAsync(h->jvpXk, h->d.U, bytes, cudaMemcpyDeviceToDevice, h->st));
+  launch_step_setup(h, 2, 0., false);  // bulk velocity of Xk, held for every evaluation
+  if (fdOrder == 1) {
+    launch_rhs(h, 0, 0., 0.);
+    CUDA_TRY(cudaMemcpyAsync(h->jvpR, h->d.Ut, bytes, cudaMemcpyDeviceToDevice, h->st));
+  }
+  k_axpy_out<<<grid, 256, 0, h->st>>>(h->d.U, h->jvpXk, eps, h->jvpV, cnt);
+  launch_rhs(h, 0, 0., 0.);
+  if (fdOrder == 1) {
+    k_fd_diff<<<grid, 256, 0, h->st>>>(h->jvpR, h->d.Ut, h->jvpR, 1. / eps, cnt);
+  } else {
+    CUDA_TRY(cudaMemcpyAsync(h->jvpR, h->d.Ut, bytes, cudaMemcpyDeviceToDevice, h->st));
+    k_axpy_out<<<grid, 256, 0, h->st>>>(h->d.U, h->jvpXk, -eps, h->jvpV, cnt);
+    launch_rhs(h, 0, 0., 0.);
+    k_fd_diff<<<grid, 256, 0, h->st>>>(h->jvpR, h->jvpR, h->d.Ut, 1. / (2. * eps), cnt);
+  }
+  CUDA_TRY(cudaMemcpyAsync(h->d.U, h->jvpXk, bytes, cudaMemcpyDeviceToDevice, h->st));
+  CUDA_TRY(cudaGetLastError());
+  return export_field(h, h->jvpR, 5, 0, 5, JV);
+}
+
+int fg_vjp_time_derivative(fg_handle* h, double t, const double* W, double* V, double* muScaleBar) {
+  (void)t;  // no time-dependent source on this path
   if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
   if (!W) return fail(h, FG_ERR_CONFIG, "null cotangent");
   if (const char* why = adjoint_unsupported(h->cfg)) return fail(h, FG_ERR_CONFIG, why);

@@ -219,13 +219,22 @@ class Flexi:
         s = np.ascontiguousarray(scale, np.float64).reshape(self.n_elems)
         self._check(self.L.fg_set_elem_mu_scale(self.h, _p(s)), "fg_set_elem_mu_scale")
 
-    def rhs_vjp(self, W):
+    def vjp_time_derivative(self, W, t=0.0):
         """(V, mu_bar): V = (dUt/dU)^T W at the current state, mu_bar = d<W, Ut>/d(viscosity multipliers)."""
         W = np.ascontiguousarray(W, np.float64).reshape(self.ushape)
         V = np.empty(self.ushape)
         mub = np.empty(self.n_elems)
-        self._check(self.L.fg_rhs_vjp(self.h, _p(W), _p(V), _p(mub)), "fg_rhs_vjp")
+        self._check(self.L.fg_vjp_time_derivative(self.h, float(t), _p(W), _p(V), _p(mub)), "fg_vjp_time_derivative")
         return V, mub
+
+    def jvp_time_derivative(self, V, t=0.0, fd_order=1, eps_method=2, scaleps=1.0):
+        """J V at the current state by the reference's matrix-free finite difference (implicit.f90:MatrixVector);
+        the defaults are the reference's (FD_Order 1, Eps_Method 2, scaleps 1)."""
+        V = np.ascontiguousarray(V, np.float64).reshape(self.ushape)
+        JV = np.empty(self.ushape)
+        self._check(self.L.fg_jvp_time_derivative(self.h, float(t), _p(V), _p(JV), int(fd_order), int(eps_method), float(scaleps)),
+                    "fg_jvp_time_derivative")
+        return JV
 
     def adjoint_forward(self, n_steps, dt, ckpt_every):
         """Advances n_steps LSERK steps of fixed dt, keeping a checkpoint every ckpt_every steps."""

@@ -178,9 +178,17 @@ int fg_set_elem_mu_scale(fg_handle* h, const double* scale);
 /* Adjoint of DGTimeDerivative_weakForm (dg.f90:221) at the current state: V = (dUt/dU)^T W, with W and V
  * in the layout of U (host arrays), and optionally muScaleBar[nElems] = d<W, Ut>/d(scale). The transposed
  * Jacobian is that of the discrete operator the GPU evaluates (the reference's implicit solver only forms
- * J V by finite differences, implicit.f90:MatrixVector). The bulk velocity of a channel body force is
- * held fixed. Supported: weak form and split form PI, LF/Roe/RoeEntropyFix, BR1/BR2, walls 3/4. */
-int fg_rhs_vjp(fg_handle* h, const double* W, double* V, double* muScaleBar);
+ * J V by finite differences, implicit.f90:MatrixVector). t is unused (no time-dependent source on this
+ * path). The bulk velocity of a channel body force is held fixed. Supported: weak form and split form PI,
+ * LF/Roe/RoeEntropyFix, BR1/BR2, walls 3/4. */
+int fg_vjp_time_derivative(fg_handle* h, double t, const double* W, double* V, double* muScaleBar);
+
+/* J V of DGTimeDerivative_weakForm at the current state by the matrix-free finite difference of the
+ * reference's implicit solver (implicit.f90:483-531, MatrixVector without its V - alpha dt term; step size
+ * of InitImplicit, implicit.f90:141-163): fdOrder 1 (one-sided) or 2 (central), epsMethod 1 (Qin, Ludlow,
+ * Shaw: sqrt(eps) scaleps/|V|) or 2 (Knoll, Keyes: additionally sqrt(1+|U|)); the reference defaults are
+ * fdOrder 1, epsMethod 2, scaleps 1. V and JV have the layout of U; the state is left unchanged. */
+int fg_jvp_time_derivative(fg_handle* h, double t, const double* V, double* JV, int fdOrder, int epsMethod, double scaleps);
 
 /* Adjoint of TimeStepByLSERKW2 (timestep.f90:82) over nSteps steps of fixed dt (the time step is not
  * differentiated), in two calls. fg_adjoint_forward advances the state by nSteps steps and keeps a device

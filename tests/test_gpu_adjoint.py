@@ -1,4 +1,4 @@
-"""Adjoint of the right-hand side (fg_rhs_vjp) against the oracle's Jacobian-vector products.
+"""Adjoint of the right-hand side (fg_vjp_time_derivative) against the oracle's Jacobian-vector products.
 
 Dot-product test <J V, W> = <V, J^T W>: J V comes from the oracle, exactly by its dual-number
 instantiation of the restated algorithm and approximately by the matrix-free finite difference of the
@@ -71,7 +71,7 @@ def test_dot_product_against_exact_jvp(name):
         V = rng.standard_normal(U.shape) * np.abs(U).max(axis=(0, 1, 2, 3))
         W = rng.standard_normal(U.shape)
         JV = o.jvp(V)
-        JTW, _ = f.rhs_vjp(W)
+        JTW, _ = f.vjp_time_derivative(W)
         lhs = float((JV * W).sum())
         rhs = float((V * JTW).sum())
         scale_ = float(np.abs(JV * W).sum())
@@ -84,7 +84,7 @@ def test_dot_product_against_reference_fd_jvp(name):
     V = rng.standard_normal(U.shape) * np.abs(U).max(axis=(0, 1, 2, 3))
     W = rng.standard_normal(U.shape)
     JV = o.fd_jvp(V, fd_order=2, eps_method=1)
-    JTW, _ = f.rhs_vjp(W)
+    JTW, _ = f.vjp_time_derivative(W)
     lhs, rhs = float((JV * W).sum()), float((V * JTW).sum())
     assert abs(lhs - rhs) <= 1e-8 * float(np.abs(JV * W).sum()), (lhs, rhs)
 
@@ -93,7 +93,7 @@ def test_dot_product_against_reference_fd_jvp(name):
 def test_viscosity_multiplier_cotangent(name):
     f, o, U, scale, rng = _setup(name, seed=2)
     W = rng.standard_normal(U.shape)
-    _, mub = f.rhs_vjp(W)
+    _, mub = f.vjp_time_derivative(W)
     ds = rng.standard_normal(f.n_elems)
     h = 1e-5
 
@@ -112,4 +112,21 @@ def test_vjp_rejects_unsupported():
     f = Flexi(c, fmesh.tgv_box(2))
     f.U = testcases.tgv_state(f.elem_xgp(), mach=0.1)
     with pytest.raises(Exception, match="LF, Roe and RoeEntropyFix"):
-        f.rhs_vjp(np.zeros(f.ushape))
+        f.vjp_time_derivative(np.zeros(f.ushape))
+
+
+@pytest.mark.parametrize("name", ["gauss3_weak_roeef_br1", "gl7_split_pi_roe_br1", "channel_gl7_split_pi_roe_br1"])
+@pytest.mark.parametrize("fd_order,eps_method,tol", [(2, 1, 1e-7), (1, 2, 1e-4)])
+def test_fd_jvp_on_gpu(name, fd_order, eps_method, tol):
+    """fg_jvp_time_derivative (the reference's MatrixVector finite difference, on the GPU) against the exact
+    JVP (within the FD truncation error of the recipe: 1e-7 central, 1e-4 one-sided, of max |JV|) and
+    against the same recipe on the oracle; the state is left unchanged."""
+    f, o, U, scale, rng = _setup(name, seed=3)
+    V = rng.standard_normal(U.shape) * np.abs(U).max(axis=(0, 1, 2, 3))
+    JVg = f.jvp_time_derivative(V, fd_order=fd_order, eps_method=eps_method)
+    assert np.array_equal(f.U, U)
+    JVx = o.jvp(V)
+    JVo = o.fd_jvp(V, fd_order=fd_order, eps_method=eps_method)
+    nrm = np.abs(JVx).max()
+    assert np.abs(JVg - JVx).max() <= tol * nrm
+    assert np.abs(JVg - JVo).max() <= tol * nrm
