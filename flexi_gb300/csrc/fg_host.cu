@@ -247,6 +247,12 @@ struct fg_handle {
   double* jvpPartial = nullptr;
   int adjSteps = 0, adjEvery = 0;
   double adjDt = 0.;
+  // binomial schedule: snapshot slots (slot 0 = U at t_0) and the steps whose states the forward pass
+  // already stored (the schedule's first right spine) with their slots
+  bool adjBinomial = false;
+  std::vector<double*> adjSlots;
+  std::vector<std::pair<int, int>> adjSpine;
+  long long adjRecomputed = 0;  // forward steps the last reverse sweep re-ran
   // per-kernel event timing (fg_profile_enable)
   bool profiling = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> evPool;
@@ -298,6 +304,9 @@ void free_adjoint_store(fg_handle* h) {
   h->adjGbar = h->adjUbar = h->adjUfinal = nullptr;
   h->adjBulkHist = h->adjPartial = h->adjBulkBar = h->adjFbar = nullptr;
   h->adjSteps = h->adjEvery = 0;
+  h->adjBinomial = false;
+  h->adjSlots.clear();
+  h->adjSpine.clear();
 }
 void free_device(fg_handle* h) {
   free_adjoint_store(h);
@@ -918,60 +927,206 @@ int fg_vjp_time_derivative(fg_handle* h, double t, const double* W, double* V, d
   return FG_OK;
 }
 
+// buffers of the reverse sweep for segments of up to segSteps steps: stage states (and, when they fit
+// in half of the free device memory, the stage intermediates), running cotangents, final state
+static int adjoint_alloc_common(fg_handle* h, int segSteps) {
+  const int n3 = h->M.n * h->M.n * h->M.n, n2 = h->M.n * h->M.n;
+  const size_t cnt = (size_t)h->M.nElems * 5 * n3;
+  h->adjStage.assign((size_t)segSteps * 5, nullptr);
+  for (auto& p : h->adjStage) if (int r = adj_alloc(h, p, cnt)) return r;
+  const size_t perStage = (size_t)h->M.nElems * (VP_NF + 12) * n3 + (size_t)h->M.nSides * (2 * FS_NF + 24) * n2;
+  size_t freeB = 0, totalB = 0;
+  cudaMemGetInfo(&freeB, &totalB);
+  const char* env = std::getenv("FLEXI_GB300_ADJOINT_RECOMPUTE");
+  const bool forceRecompute = env && env[0] == '1';
+  if (!forceRecompute && perStage * sizeof(double) * h->adjStage.size() < freeB / 2) {
+    h->adjKeepInter = true;
+    h->adjInter.assign(h->adjStage.size(), h->d);
+    for (size_t i = 0; i < h->adjStage.size(); ++i) {
+      Dev& v = h->adjInter[i];
+      v.U = h->adjStage[i];
+      int r = 0;
+      if ((r = adj_alloc(h, v.prim, (size_t)h->M.nElems * VP_NF * n3)) || (r = adj_alloc(h, v.grad, (size_t)h->M.nElems * 12 * n3)) ||
+          (r = adj_alloc(h, v.faceM, (size_t)h->M.nSides * FS_NF * n2)) || (r = adj_alloc(h, v.faceS, (size_t)h->M.nSides * FS_NF * n2)) ||
+          (r = adj_alloc(h, v.gradM, (size_t)h->M.nSides * 12 * n2)) || (r = adj_alloc(h, v.gradS, (size_t)h->M.nSides * 12 * n2)))
+        return r;
+    }
+  }
+  int r = 0;
+  if ((r = adj_alloc(h, h->adjGbar, cnt)) || (r = adj_alloc(h, h->adjUbar, cnt)) || (r = adj_alloc(h, h->adjUfinal, cnt)) ||
+      (r = adj_alloc(h, h->adjBulkHist, (size_t)segSteps * h->d.nInst)) || (r = adj_alloc(h, h->adjPartial, (size_t)h->M.nElems)) ||
+      (r = adj_alloc(h, h->adjBulkBar, (size_t)h->d.nInst)) || (r = adj_alloc(h, h->adjFbar, (size_t)h->M.nElems * n3)))
+    return r;
+  return 0;
+}
+
+// ns fixed-dt steps forward from the state in d.U (nothing recorded)
+static void adjoint_advance(fg_handle* h, int ns) {
+  for (int s = 0; s < ns; ++s) {
+    launch_step_setup(h, 1, h->adjDt, false);
+    launch_lserk(h);
+  }
+}
+
+// reverse ns steps that start from the state Ustart (device; may be d.U itself): recompute their stage
+// states (and intermediates), then run the transposed stages in reverse, accumulating into a.Ub (the
+// running state cotangent), a.muElemb, adjFbar
+static int adjoint_reverse_segment(fg_handle* h, const double* Ustart, int ns, const AdjDev& a, bool bulkAdj) {
+  const int n3 = h->M.n * h->M.n * h->M.n;
+  const long long cnt = (long long)h->M.nElems * 5 * n3;
+  const size_t bytes = (size_t)cnt * sizeof(double);
+  const unsigned gridAx = (unsigned)((cnt + 255) / 256);
+  const double dt = h->adjDt;
+  const int nI = h->d.nInst;
+  if (Ustart != h->d.U) CUDA_TRY(cudaMemcpyAsync(h->d.U, Ustart, bytes, cudaMemcpyDeviceToDevice, h->st));
+  for (int s = 0; s < ns; ++s) {
+    launch_step_setup(h, 1, dt, false);
+    CUDA_TRY(cudaMemcpyAsync(h->adjBulkHist + (size_t)s * nI, h->d.bulkVel, sizeof(double) * nI, cudaMemcpyDeviceToDevice, h->st));
+    for (int k = 1; k <= 5; ++k) {
+      const size_t slot = (size_t)s * 5 + k - 1;
+      CUDA_TRY(cudaMemcpyAsync(h->adjStage[slot], h->d.U, bytes, cudaMemcpyDeviceToDevice, h->st));
+      if (h->adjKeepInter) {
+        // the stage writes its intermediates into the slot; the state is updated in place as usual
+        Dev dv = h->adjInter[slot];
+        dv.U = h->d.U;
+        launch_rhs_dev(h, dv, k == 1 ? 1 : 2, k == 1 ? 0. : h->RKA[k], h->RKb[k]);
+      } else {
+        launch_rhs(h, k == 1 ? 1 : 2, k == 1 ? 0. : h->RKA[k], h->RKb[k]);
+      }
+    }
+  }
+  // Gbar_k = -A_{k+1} Gbar_{k+1} + b_k dt Ubar; Ubar += J(U_{k-1})^T Gbar_k
+  for (int s = ns - 1; s >= 0; --s) {
+    for (int k = 5; k >= 1; --k) {
+      k_adj_axpby<<<gridAx, 256, 0, h->st>>>(h->adjGbar, h->adjUbar, k == 5 ? 0. : -h->RKA[k + 1], h->RKb[k] * dt, cnt);
+      k_adj_source<<<h->M.nElems, 128, 0, h->st>>>(h->d, h->adjGbar, h->adjFbar, h->adjPartial, h->adjBulkHist + (size_t)s * nI, n3);
+      h->launches += 2;
+      const size_t slot = (size_t)s * 5 + k - 1;
+      if (h->adjKeepInter) {
+        launch_vjp_kept(h, h->adjInter[slot], a);
+      } else {
+        Dev dv = h->d;
+        dv.U = h->adjStage[slot];
+        launch_vjp(h, dv, a);
+      }
+    }
+    if (bulkAdj) {
+      // the step's bulk velocity depends on its start state (stage 1 input)
+      k_adj_bulk_reduce<<<(nI + 127) / 128, 128, 0, h->st>>>(nI, h->dInstStart, h->adjPartial, h->adjBulkBar);
+      k_adj_bulk_apply<<<gridAx, 256, 0, h->st>>>(h->d, h->adjUbar, h->adjStage[(size_t)s * 5], h->adjBulkBar, h->dWVol, h->dInstVol, n3);
+      h->launches += 2;
+    }
+  }
+  CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+// binomial checkpointing (Griewank): beta(s, r) = C(s + r, s) steps are reversible with s free snapshot
+// slots and r forward repetitions. For t steps and s >= 1 free slots, the next snapshot is placed so that
+// the part after it is the longest reversible with s - 1 slots at the smallest sufficient r.
+static double binom_d(int n, int k) {
+  double b = 1.;
+  for (int i = 1; i <= k; ++i) b = b * (n - k + i) / i;
+  return b;
+}
+static int revolve_split(int t, int s) {
+  int r = 0;
+  while (binom_d(s + r, s) < t) ++r;
+  const double right = std::min((double)(t - 1), binom_d(s - 1 + r, s - 1));
+  return t - (int)right;
+}
+
+struct RevolveRun {
+  fg_handle* h;
+  AdjDev a;
+  bool bulkAdj;
+  std::vector<int> freeSlots;
+  size_t bytes;
+};
+
+// reverse steps [l, r) with U_l in slot slotL and s free slots
+static int revolve_reverse(RevolveRun& R, int l, int r, int slotL, int s) {
+  fg_handle* h = R.h;
+  if (r - l == 1) {
+    h->adjRecomputed += 1;
+    return adjoint_reverse_segment(h, h->adjSlots[slotL], 1, R.a, R.bulkAdj);
+  }
+  if (s == 0) {  // no free slot: restart from U_l for every step
+    for (int i = r - 1; i >= l; --i) {
+      CUDA_TRY(cudaMemcpyAsync(h->d.U, h->adjSlots[slotL], R.bytes, cudaMemcpyDeviceToDevice, h->st));
+      adjoint_advance(h, i - l);
+      h->adjRecomputed += i - l + 1;
+      if (int e = adjoint_reverse_segment(h, h->d.U, 1, R.a, R.bulkAdj)) return e;
+    }
+    return 0;
+  }
+  const int m = l + revolve_split(r - l, s);
+  int slotM = -1;
+  for (auto it = h->adjSpine.begin(); it != h->adjSpine.end(); ++it)
+    if (it->first == m) { slotM = it->second; h->adjSpine.erase(it); break; }
+  if (slotM < 0) {
+    slotM = R.freeSlots.back();
+    R.freeSlots.pop_back();
+    CUDA_TRY(cudaMemcpyAsync(h->d.U, h->adjSlots[slotL], R.bytes, cudaMemcpyDeviceToDevice, h->st));
+    adjoint_advance(h, m - l);
+    h->adjRecomputed += m - l;
+    CUDA_TRY(cudaMemcpyAsync(h->adjSlots[slotM], h->d.U, R.bytes, cudaMemcpyDeviceToDevice, h->st));
+  }
+  if (int e = revolve_reverse(R, m, r, slotM, s - 1)) return e;
+  R.freeSlots.push_back(slotM);
+  return revolve_reverse(R, l, m, slotL, s);
+}
+
 int fg_adjoint_forward(fg_handle* h, int nSteps, double dt, int ckptEvery) {
   if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
   if (const char* why = adjoint_unsupported(h->cfg)) return fail(h, FG_ERR_CONFIG, why);
-  if (nSteps < 1 || ckptEvery < 1 || !(dt > 0.) || !std::isfinite(dt)) return fail(h, FG_ERR_CONFIG, "nSteps, ckptEvery >= 1 and dt > 0 required");
+  if (nSteps < 1 || ckptEvery == 0 || !(dt > 0.) || !std::isfinite(dt))
+    return fail(h, FG_ERR_CONFIG, "nSteps >= 1, ckptEvery != 0 and dt > 0 required");
   if (int r = ensure_adjoint(h)) return r;
   free_adjoint_store(h);
   const int n3 = h->M.n * h->M.n * h->M.n;
   const size_t cnt = (size_t)h->M.nElems * 5 * n3, bytes = cnt * sizeof(double);
-  const int nCk = (nSteps + ckptEvery - 1) / ckptEvery;
-  h->adjCkpt.assign(nCk, nullptr);
-  h->adjStage.assign((size_t)ckptEvery * 5, nullptr);
-  for (auto& p : h->adjCkpt) if (int r = adj_alloc(h, p, cnt)) { free_adjoint_store(h); return r; }
-  for (auto& p : h->adjStage) if (int r = adj_alloc(h, p, cnt)) { free_adjoint_store(h); return r; }
-  {
-    // keep the stage intermediates of a segment when they take at most half of the free device memory
-    const int n2 = h->M.n * h->M.n;
-    const size_t perStage = (size_t)h->M.nElems * (VP_NF + 12) * n3 + (size_t)h->M.nSides * (2 * FS_NF + 24) * n2;
-    size_t freeB = 0, totalB = 0;
-    cudaMemGetInfo(&freeB, &totalB);
-    const char* env = std::getenv("FLEXI_GB300_ADJOINT_RECOMPUTE");
-    const bool forceRecompute = env && env[0] == '1';
-    if (!forceRecompute && perStage * sizeof(double) * h->adjStage.size() < freeB / 2) {
-      h->adjKeepInter = true;
-      h->adjInter.assign(h->adjStage.size(), h->d);
-      for (size_t i = 0; i < h->adjStage.size(); ++i) {
-        Dev& v = h->adjInter[i];
-        v.U = h->adjStage[i];
-        int r = 0;
-        if ((r = adj_alloc(h, v.prim, (size_t)h->M.nElems * VP_NF * n3)) || (r = adj_alloc(h, v.grad, (size_t)h->M.nElems * 12 * n3)) ||
-            (r = adj_alloc(h, v.faceM, (size_t)h->M.nSides * FS_NF * n2)) || (r = adj_alloc(h, v.faceS, (size_t)h->M.nSides * FS_NF * n2)) ||
-            (r = adj_alloc(h, v.gradM, (size_t)h->M.nSides * 12 * n2)) || (r = adj_alloc(h, v.gradS, (size_t)h->M.nSides * 12 * n2))) {
-          free_adjoint_store(h);
-          return r;
-        }
-      }
+  const bool binomial = ckptEvery < 0;
+  h->adjDt = dt;
+  if (binomial) {
+    const int nSnap = -ckptEvery;
+    h->adjSlots.assign(nSnap, nullptr);
+    for (auto& p : h->adjSlots) if (int r = adj_alloc(h, p, cnt)) { free_adjoint_store(h); return r; }
+    if (int r = adjoint_alloc_common(h, 1)) { free_adjoint_store(h); return r; }
+    // the schedule's first right spine: where the reverse sweep's first snapshots go
+    int l = 0, sFree = nSnap - 1;
+    while (nSteps - l > 1 && sFree > 0) {
+      l += revolve_split(nSteps - l, sFree);
+      h->adjSpine.push_back({l, nSnap - sFree});
+      --sFree;
     }
+  } else {
+    const int nCk = (nSteps + ckptEvery - 1) / ckptEvery;
+    h->adjCkpt.assign(nCk, nullptr);
+    for (auto& p : h->adjCkpt) if (int r = adj_alloc(h, p, cnt)) { free_adjoint_store(h); return r; }
+    if (int r = adjoint_alloc_common(h, ckptEvery)) { free_adjoint_store(h); return r; }
   }
-  if (int r = adj_alloc(h, h->adjGbar, cnt)) { free_adjoint_store(h); return r; }
-  if (int r = adj_alloc(h, h->adjUbar, cnt)) { free_adjoint_store(h); return r; }
-  if (int r = adj_alloc(h, h->adjUfinal, cnt)) { free_adjoint_store(h); return r; }
-  if (int r = adj_alloc(h, h->adjBulkHist, (size_t)ckptEvery * h->d.nInst)) { free_adjoint_store(h); return r; }
-  if (int r = adj_alloc(h, h->adjPartial, (size_t)h->M.nElems)) { free_adjoint_store(h); return r; }
-  if (int r = adj_alloc(h, h->adjBulkBar, (size_t)h->d.nInst)) { free_adjoint_store(h); return r; }
-  if (int r = adj_alloc(h, h->adjFbar, (size_t)h->M.nElems * n3)) { free_adjoint_store(h); return r; }
   h->launches = 0;
+  size_t spineIdx = 0;
   for (int step = 0; step < nSteps; ++step) {
-    if (step % ckptEvery == 0) CUDA_TRY(cudaMemcpyAsync(h->adjCkpt[step / ckptEvery], h->d.U, bytes, cudaMemcpyDeviceToDevice, h->st));
+    if (binomial) {
+      if (step == 0) CUDA_TRY(cudaMemcpyAsync(h->adjSlots[0], h->d.U, bytes, cudaMemcpyDeviceToDevice, h->st));
+      if (spineIdx < h->adjSpine.size() && h->adjSpine[spineIdx].first == step) {
+        CUDA_TRY(cudaMemcpyAsync(h->adjSlots[h->adjSpine[spineIdx].second], h->d.U, bytes, cudaMemcpyDeviceToDevice, h->st));
+        ++spineIdx;
+      }
+    } else if (step % ckptEvery == 0) {
+      CUDA_TRY(cudaMemcpyAsync(h->adjCkpt[step / ckptEvery], h->d.U, bytes, cudaMemcpyDeviceToDevice, h->st));
+    }
     launch_step_setup(h, 1, dt, true);
     launch_lserk(h);
   }
   CUDA_TRY(cudaMemcpyAsync(h->adjUfinal, h->d.U, bytes, cudaMemcpyDeviceToDevice, h->st));
   CUDA_TRY(cudaGetLastError());
   if (int r = check_err(h)) { free_adjoint_store(h); return r; }
-  h->adjSteps = nSteps; h->adjEvery = ckptEvery; h->adjDt = dt;
+  h->adjSteps = nSteps;
+  h->adjEvery = binomial ? 0 : ckptEvery;
+  h->adjBinomial = binomial;
   return FG_OK;
 }
 
@@ -983,8 +1138,8 @@ int fg_adjoint_reverse(fg_handle* h, const double* UbarT, double* Ubar0, double*
   const long long cnt = (long long)h->M.nElems * 5 * n3;
   const size_t bytes = (size_t)cnt * sizeof(double);
   const unsigned gridAx = (unsigned)((cnt + 255) / 256);
-  const double dt = h->adjDt;
   h->launches = 0;
+  h->adjRecomputed = 0;
   CUDA_TRY(cudaMemcpyAsync(h->dStage, UbarT, bytes, cudaMemcpyHostToDevice, h->st));
   k_fortran_to_dev<<<gridAx, 256, 0, h->st>>>(h->dStage, h->adjUbar, 5, n3, cnt);
   CUDA_TRY(cudaMemsetAsync(h->a.muElemb, 0, sizeof(double) * h->M.nElems, h->st));
@@ -993,54 +1148,27 @@ int fg_adjoint_reverse(fg_handle* h, const double* UbarT, double* Ubar0, double*
   // with the channel forcing, each step's bulk velocity is a function of its start state, and the energy
   // source of the body force (uniform and/or field) couples to it
   const bool bulkAdj = h->cfg.doTCSource != 0;
-  const int nI = h->d.nInst;
   AdjDev a = h->a;
   a.accumulate = 1;
   a.Ub = h->adjUbar;
   a.W = h->adjGbar;
-  const int nCk = (int)h->adjCkpt.size();
-  for (int seg = nCk - 1; seg >= 0; --seg) {
-    const int s0 = seg * h->adjEvery, ns = std::min(h->adjEvery, h->adjSteps - s0);
-    // recompute the segment's stage states from its checkpoint
-    CUDA_TRY(cudaMemcpyAsync(h->d.U, h->adjCkpt[seg], bytes, cudaMemcpyDeviceToDevice, h->st));
-    for (int s = 0; s < ns; ++s) {
-      launch_step_setup(h, 1, dt, false);
-      CUDA_TRY(cudaMemcpyAsync(h->adjBulkHist + (size_t)s * nI, h->d.bulkVel, sizeof(double) * nI, cudaMemcpyDeviceToDevice, h->st));
-      for (int k = 1; k <= 5; ++k) {
-        const size_t slot = (size_t)s * 5 + k - 1;
-        CUDA_TRY(cudaMemcpyAsync(h->adjStage[slot], h->d.U, bytes, cudaMemcpyDeviceToDevice, h->st));
-        if (h->adjKeepInter) {
-          // the stage writes its intermediates into the slot; the state is updated in place as usual
-          Dev dv = h->adjInter[slot];
-          dv.U = h->d.U;
-          launch_rhs_dev(h, dv, k == 1 ? 1 : 2, k == 1 ? 0. : h->RKA[k], h->RKb[k]);
-        } else {
-          launch_rhs(h, k == 1 ? 1 : 2, k == 1 ? 0. : h->RKA[k], h->RKb[k]);
-        }
-      }
-    }
-    // reverse the segment: Gbar_k = -A_{k+1} Gbar_{k+1} + b_k dt Ubar; Ubar += J(U_{k-1})^T Gbar_k
-    for (int s = ns - 1; s >= 0; --s) {
-      for (int k = 5; k >= 1; --k) {
-        k_adj_axpby<<<gridAx, 256, 0, h->st>>>(h->adjGbar, h->adjUbar, k == 5 ? 0. : -h->RKA[k + 1], h->RKb[k] * dt, cnt);
-        k_adj_source<<<h->M.nElems, 128, 0, h->st>>>(h->d, h->adjGbar, h->adjFbar, h->adjPartial, h->adjBulkHist + (size_t)s * nI, n3);
-        h->launches += 1;
-        const size_t slot = (size_t)s * 5 + k - 1;
-        if (h->adjKeepInter) {
-          launch_vjp_kept(h, h->adjInter[slot], a);
-        } else {
-          Dev dv = h->d;
-          dv.U = h->adjStage[slot];
-          launch_vjp(h, dv, a);
-        }
-        h->launches += 1;
-      }
-      if (bulkAdj) {
-        // the step's bulk velocity depends on its start state (stage 1 input)
-        k_adj_bulk_reduce<<<(nI + 127) / 128, 128, 0, h->st>>>(nI, h->dInstStart, h->adjPartial, h->adjBulkBar);
-        k_adj_bulk_apply<<<gridAx, 256, 0, h->st>>>(h->d, h->adjUbar, h->adjStage[(size_t)s * 5], h->adjBulkBar, h->dWVol, h->dInstVol, n3);
-        h->launches += 2;
-      }
+  if (h->adjBinomial) {
+    RevolveRun R{h, a, bulkAdj, {}, bytes};
+    const int nSnap = (int)h->adjSlots.size();
+    std::vector<bool> used(nSnap, false);
+    used[0] = true;
+    for (auto& sp : h->adjSpine) used[sp.second] = true;
+    for (int i = nSnap - 1; i >= 1; --i) if (!used[i]) R.freeSlots.push_back(i);
+    const auto spineCopy = h->adjSpine;
+    const int e = revolve_reverse(R, 0, h->adjSteps, 0, nSnap - 1);
+    h->adjSpine = spineCopy;  // the forward's snapshots stay valid for another reverse sweep only if untouched
+    if (e) return e;
+  } else {
+    const int nCk = (int)h->adjCkpt.size();
+    for (int seg = nCk - 1; seg >= 0; --seg) {
+      const int s0 = seg * h->adjEvery, ns = std::min(h->adjEvery, h->adjSteps - s0);
+      h->adjRecomputed += ns;
+      if (int e = adjoint_reverse_segment(h, h->adjCkpt[seg], ns, a, bulkAdj)) return e;
     }
   }
   CUDA_TRY(cudaGetLastError());
@@ -1050,8 +1178,12 @@ int fg_adjoint_reverse(fg_handle* h, const double* UbarT, double* Ubar0, double*
   if (muScaleBar) CUDA_TRY(cudaMemcpyAsync(muScaleBar, h->a.muElemb, sizeof(double) * h->M.nElems, cudaMemcpyDeviceToHost, h->st));
   if (forceBar) { if (int r = export_field(h, h->adjFbar, 1, 0, 1, forceBar)) return r; }
   CUDA_TRY(cudaStreamSynchronize(h->st));
+  // a binomial sweep overwrites snapshot slots it reused: another sweep needs a new forward
+  if (h->adjBinomial) h->adjSteps = 0;
   return FG_OK;
 }
+
+long long fg_adjoint_recomputed_steps(const fg_handle* h) { return h ? h->adjRecomputed : -1; }
 
 int fg_set_body_force_field(fg_handle* h, const double* F) {
   if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");

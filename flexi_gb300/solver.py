@@ -236,9 +236,17 @@ class Flexi:
                     "fg_jvp_time_derivative")
         return JV
 
-    def adjoint_forward(self, n_steps, dt, ckpt_every):
-        """Advances n_steps LSERK steps of fixed dt, keeping a checkpoint every ckpt_every steps."""
-        self._check(self.L.fg_adjoint_forward(self.h, int(n_steps), float(dt), int(ckpt_every)), "fg_adjoint_forward")
+    def adjoint_forward(self, n_steps, dt, ckpt_every=None, snapshots=None):
+        """Advances n_steps LSERK steps of fixed dt, keeping a checkpoint every ckpt_every steps, or, with
+        snapshots=s, the snapshots of a binomial (revolve) schedule with s snapshot states."""
+        if (ckpt_every is None) == (snapshots is None):
+            raise ValueError("give either ckpt_every or snapshots")
+        code = int(ckpt_every) if snapshots is None else -int(snapshots)
+        self._check(self.L.fg_adjoint_forward(self.h, int(n_steps), float(dt), code), "fg_adjoint_forward")
+
+    def adjoint_recomputed_steps(self):
+        """Forward steps the last adjoint_reverse re-ran."""
+        return int(self.L.fg_adjoint_recomputed_steps(self.h))
 
     def adjoint_reverse(self, UbarT, force_bar=False):
         """(Ubar0, mu_bar[, force_bar]) for the cotangent UbarT of the final state of the last adjoint_forward."""

@@ -201,6 +201,12 @@ int fg_jvp_time_derivative(fg_handle* h, double t, const double* V, double* JV, 
  * FLEXI_GB300_ADJOINT_RECOMPUTE=1 forces the recomputing path). The state is left at t_end. No counterpart
  * in the reference. */
 int fg_adjoint_forward(fg_handle* h, int nSteps, double dt, int ckptEvery);
+/* ckptEvery < 0 selects binomial checkpointing (Griewank's revolve schedule) with -ckptEvery snapshot
+ * states in device memory instead of uniform checkpoints: horizons of C(s + r, s) steps need s + 1
+ * snapshots and r forward repetitions, so long horizons fit in a fixed memory budget. A binomial reverse
+ * sweep reuses the snapshot slots and needs a new fg_adjoint_forward before the next sweep. */
+/* Forward steps the last fg_adjoint_reverse re-ran (the recomputation cost of its schedule). */
+long long fg_adjoint_recomputed_steps(const fg_handle* h);
 /* forceBar(0:N,0:N,0:N,nElems) (optional) = dL/d(body-force field of fg_set_body_force_field). With the channel
  * body force or a body-force field, the dependence of each step's bulk velocity on its start state is
  * included. */

@@ -124,3 +124,69 @@ def test_autograd_kinetic_energy_loss():
     fds = _rich(lambda s: L(U0, s), scale, ds, 1e-3)
     assert abs(float((U0_t.grad.numpy() * V).sum()) - fdU) <= 1e-7 * abs(fdU)
     assert abs(float(s_t.grad.numpy() @ ds) - fds) <= 1e-7 * abs(fds)
+
+
+def _binomial_recomputations(n, nsnap):
+    """Forward steps the binomial schedule of fg_adjoint_reverse re-runs (a model of the same rule:
+    snapshot so that the part after it is the longest reversible with one slot less, at the smallest
+    sufficient repetition count; the forward pass stores the first right spine)."""
+    from math import comb
+
+    def split(t, s):
+        r = 0
+        while comb(s + r, s) < t:
+            r += 1
+        return t - min(t - 1, comb(s - 1 + r, s - 1))
+
+    spine, l, s = set(), 0, nsnap - 1
+    while n - l > 1 and s > 0:
+        l += split(n - l, s)
+        spine.add(l)
+        s -= 1
+    count = 0
+
+    def rev(l, r, s):
+        nonlocal count
+        if r - l == 1:
+            count += 1
+            return
+        if s == 0:
+            count += sum(i - l + 1 for i in range(l, r))
+            return
+        m = l + split(r - l, s)
+        if m in spine:
+            spine.discard(m)
+        else:
+            count += m - l
+        rev(m, r, s - 1)
+        rev(l, m, s)
+
+    rev(0, n, nsnap - 1)
+    return count
+
+
+def test_binomial_checkpointing_matches_uniform():
+    """Binomial (revolve) schedules with 1..n+1 snapshots give the gradient of uniform checkpointing, leave
+    the state at t_end, and re-run exactly the forward steps of the schedule (n(n+1)/2 with one snapshot,
+    n with n snapshots or more); a second reverse sweep needs a new forward."""
+    f, U0, scale, dt, rng = _setup("gauss3_weak_roeef_br1", seed=6)
+    n = 13
+    w = rng.standard_normal(U0.shape)
+    f.U = U0
+    f.adjoint_forward(n, dt, ckpt_every=n)
+    UT = f.U
+    ref, mref = f.adjoint_reverse(w)
+    assert f.adjoint_recomputed_steps() == n
+    for nsnap in (1, 2, 3, 5, n + 1):
+        f.U = U0
+        f.adjoint_forward(n, dt, snapshots=nsnap)
+        assert np.array_equal(f.U, UT)
+        Ub0, mub = f.adjoint_reverse(w)
+        assert np.array_equal(f.U, UT)
+        assert np.abs(Ub0 - ref).max() <= 1e-13 * np.abs(ref).max(), nsnap
+        assert np.abs(mub - mref).max() <= 1e-13 * np.abs(mref).max(), nsnap
+        assert f.adjoint_recomputed_steps() == _binomial_recomputations(n, nsnap), nsnap
+        with pytest.raises(Exception):
+            f.adjoint_reverse(w)
+    assert _binomial_recomputations(n, 1) == n * (n + 1) // 2
+    assert _binomial_recomputations(n, n + 1) == n
