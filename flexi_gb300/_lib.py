@@ -21,7 +21,8 @@ EXPORTS = ["fg_config_default", "fg_config_from_ini", "fg_create", "fg_destroy",
            "fg_get_gradients", "fg_get_stream", "fg_launch_count", "fg_debug_array", "fg_profile_enable", "fg_profile_read", "fg_probe_fp64",
            "fg_time_derivative_noalloc", "fg_set_elem_mu_scale", "fg_vjp_time_derivative", "fg_adjoint_forward", "fg_adjoint_reverse",
            "fg_set_body_force_field", "fg_wall_shear", "fg_jvp_time_derivative",
-           "fg_adjoint_recomputed_steps"]
+           "fg_adjoint_recomputed_steps", "fg_autotune", "fg_autotune_choice",
+           "fg_set_launch_shapes"]
 
 
 class FgDeviceMesh(ctypes.Structure):
@@ -77,6 +78,9 @@ def load(path=None):
     L.fg_adjoint_forward.argtypes = [P, I, D, I]
     L.fg_adjoint_reverse.argtypes = [P, P, P, P, P]
     L.fg_adjoint_recomputed_steps.argtypes = [P]
+    L.fg_autotune.argtypes = [P, I, P]
+    L.fg_autotune_choice.argtypes = [P, P]
+    L.fg_set_launch_shapes.argtypes = [P, I, I, I, I]
     L.fg_adjoint_recomputed_steps.restype = ctypes.c_longlong
     L.fg_set_body_force_field.argtypes = [P, P]
     L.fg_wall_shear.argtypes = [P, P, P]

@@ -200,7 +200,8 @@ struct DevBuf {
 struct fg_handle {
   fg_config cfg{};
   Basis B{};
-  KernelSet K{};
+  KernelSet K{};      // kernels in use (after autotuning)
+  KernelSet Kdef{};   // the default kernel set of this (N, node type)
   fgh::HostMesh M;
   Dev d{};
   bool haveMesh = false;      // device arrays ready
@@ -479,7 +480,7 @@ struct ProfScope {
 void launch_rhs_dev(fg_handle* h, const Dev& d, int mode, double rkA, double rkB) {
   { ProfScope p(h, 0); h->K.prep(d, h->B, h->st); }
   { ProfScope p(h, 1); h->K.lift(d, h->B, h->st); }
-  { ProfScope p(h, 2); h->K.flux(d, h->B, h->st); }
+  { ProfScope p(h, 2); h->K.flux_block(d, h->B, h->K.fluxBlock, h->st); }
   {
     ProfScope p(h, 3);
     if (h->cfg.SplitDG >= 0) h->K.vol_split(d, h->B, mode, rkA, rkB, h->st);
@@ -692,6 +693,7 @@ int fg_create(const fg_config* cfg, fg_handle** out) {
   else if (c.TimeDiscMethod != 0) why = "TimeDiscMethod must be CarpenterRK4-5";
   if (!why.empty()) { delete h; return fail(nullptr, FG_ERR_CONFIG, why); }
   h->K = get_kernel_set(c.N + 1, c.NodeType == FG_NODE_GAUSS_LOBATTO);
+  h->Kdef = h->K;
   if (h->K.n == 0) { delete h; return fail(nullptr, FG_ERR_CONFIG, "no kernels for this N"); }
   init_basis(h);
   *out = h;
@@ -1247,6 +1249,91 @@ int fg_wall_shear(fg_handle* h, double* J, double* dJdU) {
   h->launches += 6;
   CUDA_TRY(cudaGetLastError());
   return export_field(h, a.Ub, 5, 0, 5, dJdU);
+}
+
+// mean time per launch of fn over reps launches on the handle's stream (ms), after one untimed launch
+extern "C++" {
+template <class F>
+static double time_launches(fg_handle* h, int reps, F fn) {
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  fn();
+  cudaEventRecord(a, h->st);
+  for (int i = 0; i < reps; ++i) fn();
+  cudaEventRecord(b, h->st);
+  cudaEventSynchronize(b);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return ms / reps;
+}
+}  // extern "C++"
+
+int fg_autotune(fg_handle* h, int reps, double* report) {
+  if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
+  if (reps < 1) return fail(h, FG_ERR_CONFIG, "reps >= 1 required");
+  double rep[9];
+  for (double& v : rep) v = NAN;
+  const Dev& d = h->d;
+  KernelSet& K = h->K;
+  const KernelSet& D = h->Kdef;
+  // valid intermediates for every candidate (prep, lift and the side kernel only write intermediates, the
+  // volume kernel in mode 0 only Ut: the state is not changed)
+  D.prep(d, h->B, h->st);
+  D.lift(d, h->B, h->st);
+  D.flux_block(d, h->B, 128, h->st);
+  CUDA_TRY(cudaGetLastError());
+  K.prep = D.prep; K.lift = D.lift; K.vol_weak = D.vol_weak;
+  if (D.altEPB > 0) {
+    rep[0] = time_launches(h, reps, [&] { D.prep(d, h->B, h->st); });
+    rep[1] = time_launches(h, reps, [&] { D.prep_alt(d, h->B, h->st); });
+    rep[2] = time_launches(h, reps, [&] { D.lift(d, h->B, h->st); });
+    rep[3] = time_launches(h, reps, [&] { D.lift_alt(d, h->B, h->st); });
+    if (rep[1] < rep[0]) K.prep = D.prep_alt;
+    if (rep[3] < rep[2]) K.lift = D.lift_alt;
+    if (h->cfg.SplitDG < 0) {
+      rep[4] = time_launches(h, reps, [&] { D.vol_weak(d, h->B, 0, 0., 0., h->st); });
+      rep[5] = time_launches(h, reps, [&] { D.vol_weak_alt(d, h->B, 0, 0., 0., h->st); });
+      if (rep[5] < rep[4]) K.vol_weak = D.vol_weak_alt;
+    }
+  }
+  const int blocks[3] = {64, 128, 256};
+  int best = 1;
+  for (int i = 0; i < 3; ++i) {
+    rep[6 + i] = time_launches(h, reps, [&] { D.flux_block(d, h->B, blocks[i], h->st); });
+    if (rep[6 + i] < rep[6 + best]) best = i;
+  }
+  K.fluxBlock = blocks[best];
+  CUDA_TRY(cudaGetLastError());
+  // the captured time loop holds the kernels it was captured with
+  if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+  if (report) std::copy(rep, rep + 9, report);
+  return FG_OK;
+}
+
+int fg_set_launch_shapes(fg_handle* h, int epbPrep, int epbLift, int epbVol, int fluxBlock) {
+  if (!h) return FG_ERR_STATE;
+  const KernelSet& D = h->Kdef;
+  auto ok = [&](int e) { return e == D.defEPB || (D.altEPB > 0 && e == D.altEPB); };
+  if (!ok(epbPrep) || !ok(epbLift) || !ok(epbVol) || (fluxBlock != 64 && fluxBlock != 128 && fluxBlock != 256))
+    return fail(h, FG_ERR_CONFIG, "elements per CTA must be the default or the alternative of this N, the side block 64/128/256");
+  h->K.prep = epbPrep == D.defEPB ? D.prep : D.prep_alt;
+  h->K.lift = epbLift == D.defEPB ? D.lift : D.lift_alt;
+  h->K.vol_weak = epbVol == D.defEPB ? D.vol_weak : D.vol_weak_alt;
+  h->K.fluxBlock = fluxBlock;
+  if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+  return FG_OK;
+}
+
+int fg_autotune_choice(const fg_handle* h, int* out) {
+  if (!h || !out) return FG_ERR_STATE;
+  out[0] = h->K.prep == h->Kdef.prep ? h->Kdef.defEPB : h->Kdef.altEPB;
+  out[1] = h->K.lift == h->Kdef.lift ? h->Kdef.defEPB : h->Kdef.altEPB;
+  out[2] = h->K.vol_weak == h->Kdef.vol_weak ? h->Kdef.defEPB : h->Kdef.altEPB;
+  out[3] = h->K.fluxBlock;
+  return FG_OK;
 }
 
 int fg_calc_timestep(fg_handle* h, double* dt, int* errType) {

@@ -20,6 +20,42 @@ struct Inst {
   static size_t smem_split_adj() { return sizeof(double) * (SBasis<n>::SIZE + 2 * S::n2 + S::EPB * 26 * S::n3 + S::THREADS); }
   static size_t smem_lift_adj() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * (13 * S::n3 + 6 * S::n2 * 19)); }
   static size_t smem_prep_adj() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * (5 * S::n3 + 6 * S::n2 * 6)); }
+  // elements per CTA of the autotuner's alternative element kernels (N=5: 2, N=3: 4; 0: none)
+  static constexpr int ALT_E = (n == 6) ? 2 : ((n == 4) ? 4 : 0);
+  template <int E>
+  static size_t smem_prep_E() {
+    using SE = Shape<n, E>;
+    return sizeof(double) * (SBasis<n>::SIZE + SE::EPB * (5 + VP_NF) * SE::n3);
+  }
+  template <int E>
+  static size_t smem_lift_E() {
+    using SE = Shape<n, E>;
+    return sizeof(double) * (SBasis<n>::SIZE + SE::EPB * (4 * SE::n3 + 6 * SE::n2 * 7 + 12 * SE::n3 + SE::n3));
+  }
+  template <int E>
+  static size_t smem_weak_E() {
+    using SE = Shape<n, E>;
+    return sizeof(double) * (SBasis<n>::SIZE + SE::EPB * (15 * SE::n3 + 6 * SE::n2 * 5));
+  }
+  template <int E>
+  static void prep_E(const Dev& d, const Basis& B, cudaStream_t st) {
+    using SE = Shape<n, E>;
+    k_prep<n, GL, E><<<(d.nElems + SE::EPB - 1) / SE::EPB, SE::THREADS, smem_prep_E<E>(), st>>>(d, B);
+  }
+  template <int E>
+  static void lift_E(const Dev& d, const Basis& B, cudaStream_t st) {
+    using SE = Shape<n, E>;
+    k_lift<n, GL, E><<<(d.nElems + SE::EPB - 1) / SE::EPB, SE::THREADS, smem_lift_E<E>(), st>>>(d, B);
+  }
+  template <int E>
+  static void vol_weak_E(const Dev& d, const Basis& B, int mode, double rkA, double rkB, cudaStream_t st) {
+    using SE = Shape<n, E>;
+    k_vol_weak<n, GL, E><<<(d.nElems + SE::EPB - 1) / SE::EPB, SE::THREADS, smem_weak_E<E>(), st>>>(d, B, Stage{mode, rkA, rkB});
+  }
+  static void flux_block(const Dev& d, const Basis& B, int block, cudaStream_t st) {
+    const long long pts = (long long)d.nSides * S::n2;
+    k_flux<n><<<(unsigned)((pts + block - 1) / block), block, 0, st>>>(d, B);
+  }
   template <class K>
   static void set_smem(K kern, size_t bytes) {
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
@@ -33,6 +69,11 @@ struct Inst {
     set_smem(k_lift_adj<n, GL>, smem_lift_adj());
     set_smem(k_prep_adj<n, GL>, smem_prep_adj());
     if constexpr (GL && (n == 2 || n == 4 || n == 8)) set_smem(k_vol_split_adj<n>, smem_split_adj());
+    if constexpr (ALT_E > 0) {
+      set_smem(k_prep<n, GL, ALT_E>, smem_prep_E<ALT_E>());
+      set_smem(k_lift<n, GL, ALT_E>, smem_lift_E<ALT_E>());
+      set_smem(k_vol_weak<n, GL, ALT_E>, smem_weak_E<ALT_E>());
+    }
   }
   static void vol_adj(const Dev& d, const AdjDev& a, const Basis& B, cudaStream_t st) {
     if constexpr (GL && (n == 2 || n == 4 || n == 8)) {
@@ -82,6 +123,14 @@ struct Inst {
     k.prep = &prep; k.lift = &lift; k.flux = &flux; k.vol_weak = &vol_weak; k.dt = &dt;
     if (GL && (n == 2 || n == 4 || n == 8)) k.vol_split = &vol_split;
     k.vol_adj = &vol_adj; k.flux_adj = &flux_adj; k.lift_adj = &lift_adj; k.prep_adj = &prep_adj;
+    k.defEPB = S::EPB;
+    k.flux_block = &flux_block;
+    if constexpr (ALT_E > 0) {
+      k.altEPB = ALT_E;
+      k.prep_alt = &prep_E<ALT_E>;
+      k.lift_alt = &lift_E<ALT_E>;
+      k.vol_weak_alt = &vol_weak_E<ALT_E>;
+    }
     return k;
   }
 };

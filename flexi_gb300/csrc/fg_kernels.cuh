@@ -16,10 +16,11 @@
 
 namespace fg {
 
-template <int n> struct Shape {
+// E = elements per CTA; E = 0 selects the default, which fills at least ~128 threads for small n (the
+// autotuner may pick another E for the element kernels that have variants)
+template <int n, int E = 0> struct Shape {
   static constexpr int N = n - 1, n2 = n * n, n3 = n * n * n;
-  // elements per CTA: fill at least ~128 threads for small n
-  static constexpr int EPB = (n3 >= 128) ? 1 : (128 + n3 - 1) / n3;
+  static constexpr int EPB = E > 0 ? E : ((n3 >= 128) ? 1 : (128 + n3 - 1) / n3);
   static constexpr int THREADS = ((EPB * n3 + 31) / 32) * 32;
 };
 
@@ -53,9 +54,9 @@ template <int n> struct SBasis {
 // =====================================================================================================
 // k_prep: eos.f90:ConsToPrim (volume), prolongtoface.t90:ProlongToFace, equation.f90:GetPrimitiveStateSurface
 // =====================================================================================================
-template <int n, bool GL>
-__global__ void __launch_bounds__(Shape<n>::THREADS) k_prep(Dev d, Basis B) {
-  using S = Shape<n>;
+template <int n, bool GL, int E = 0>
+__global__ void __launch_bounds__(Shape<n, E>::THREADS) k_prep(Dev d, Basis B) {
+  using S = Shape<n, E>;
   constexpr int n2 = S::n2, n3 = S::n3, EPB = S::EPB, N = S::N;
   extern __shared__ double smem[];
   double* sD = smem;
@@ -127,10 +128,10 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_prep(Dev d, Basis B) {
 
 // ProlongToFaceLifting of the gradients in sG (+ BR2: eta * lifting contribution of this face,
 // lifting_br2.t90:Lifting_SurfInt_BR2) for the six faces of the CTA's elements
-template <int n, bool GL>
+template <int n, bool GL, int E = 0>
 __device__ __forceinline__ void lift_prolong_faces(const Dev& d, const Basis& B, const SBasis<n>& Bs, const double* sG, const double* sF,
                                                    const double* sN, const double* sJs, int e0, bool br2) {
-  constexpr int n2 = n * n, n3 = n2 * n, EPB = Shape<n>::EPB, N = n - 1;
+  constexpr int n2 = n * n, n3 = n2 * n, EPB = Shape<n, E>::EPB, N = n - 1;
   for (int t = threadIdx.x; t < EPB * 6 * n2; t += blockDim.x) {
     const int es = t / (6 * n2), r = t - es * 6 * n2, lsi = r / n2, pq = r - lsi * n2;
     const int e = e0 + es;
@@ -190,9 +191,9 @@ __device__ __forceinline__ void lift_prolong_faces(const Dev& d, const Basis& B,
 // only the face nodes: it is added face-parallel, one direction (two opposite faces, disjoint node
 // sets) at a time, so that no warp runs it for interior nodes.
 // =====================================================================================================
-template <int n, bool GL>
-__global__ void __launch_bounds__(Shape<n>::THREADS, (n == 8 && GL ? 2 : 1)) k_lift(Dev d, Basis B) {
-  using S = Shape<n>;
+template <int n, bool GL, int E = 0>
+__global__ void __launch_bounds__(Shape<n, E>::THREADS, (n == 8 && GL ? 2 : 1)) k_lift(Dev d, Basis B) {
+  using S = Shape<n, E>;
   constexpr int n2 = S::n2, n3 = S::n3, EPB = S::EPB, N = S::N;
   extern __shared__ double smem[];
   double* sD = smem;
@@ -326,7 +327,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS, (n == 8 && GL ? 2 : 1)) k_l
   if constexpr (GL) {
     // BR2 prolongs the volume part, before the surface part is added
     if (br2) {
-      lift_prolong_faces<n, GL>(d, B, Bs, sG, sF, sN, sJs, e0, true);
+      lift_prolong_faces<n, GL, E>(d, B, Bs, sG, sF, sN, sJs, e0, true);
       __syncthreads();
     }
     // surface part (DoSurfIntLifting) on the face nodes l = 0 and l = N of one direction at a time
@@ -353,7 +354,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS, (n == 8 && GL ? 2 : 1)) k_l
       __syncthreads();
     }
     // BR1 prolongs the full gradient
-    if (!br2) lift_prolong_faces<n, GL>(d, B, Bs, sG, sF, sN, sJs, e0, false);
+    if (!br2) lift_prolong_faces<n, GL, E>(d, B, Bs, sG, sF, sN, sJs, e0, false);
     for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
       const int es = t / n3, x = t - es * n3, e = e0 + es;
       if (e >= d.nElems) continue;
@@ -361,7 +362,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS, (n == 8 && GL ? 2 : 1)) k_l
       for (int c = 0; c < 12; ++c) d.grad[((size_t)e * 12 + c) * n3 + x] = sG[(es * 12 + c) * n3 + x];
     }
   } else {
-    lift_prolong_faces<n, GL>(d, B, Bs, sG, sF, sN, sJs, e0, br2);
+    lift_prolong_faces<n, GL, E>(d, B, Bs, sG, sF, sN, sJs, e0, br2);
   }
 }
 
@@ -370,7 +371,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS, (n == 8 && GL ? 2 : 1)) k_l
 // getboundaryflux.f90:GetBoundaryFlux (no-slip walls) on BC sides, times SurfElem.
 // =====================================================================================================
 template <int n>
-__global__ void __launch_bounds__(128) k_flux(Dev d, Basis B) {
+__global__ void __launch_bounds__(256) k_flux(Dev d, Basis B) {
   constexpr int n2 = n * n;
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   const int s = idx / n2, pq = idx - s * n2;
@@ -501,9 +502,9 @@ __device__ __forceinline__ void finish_node(const Dev& d, const SBasis<n>& Bs, c
 
 // loads the six sides' numerical fluxes into shared memory in this element's face order,
 // with the sign of the slave side (surfint.t90: -Flux_slave)
-template <int n>
+template <int n, int E = 0>
 __device__ __forceinline__ void load_face_fluxes(const Dev& d, double* sFl, int e0) {
-  constexpr int n2 = n * n, EPB = Shape<n>::EPB, N = n - 1;
+  constexpr int n2 = n * n, EPB = Shape<n, E>::EPB, N = n - 1;
   for (int t = threadIdx.x; t < EPB * 6 * n2; t += blockDim.x) {
     const int es = t / (6 * n2), r = t - es * 6 * n2, lsi = r / n2, pq = r - lsi * n2;
     const int e = e0 + es;
@@ -523,9 +524,9 @@ __device__ __forceinline__ void load_face_fluxes(const Dev& d, double* sFl, int 
 // k_vol_weak: volint.f90:VolInt_weakForm (advective + viscous fluxes, VolInt_Metrics, D_Hat^T sweeps),
 // surfint.t90:SurfInt, Ut=-Ut, ApplyJacobian, and the LSERK stage update.
 // =====================================================================================================
-template <int n, bool GL>
-__global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_weak(Dev d, Basis B, Stage st) {
-  using S = Shape<n>;
+template <int n, bool GL, int E = 0>
+__global__ void __launch_bounds__(Shape<n, E>::THREADS) k_vol_weak(Dev d, Basis B, Stage st) {
+  using S = Shape<n, E>;
   constexpr int n2 = S::n2, n3 = S::n3, EPB = S::EPB;
   extern __shared__ double smem[];
   double* sD = smem;
@@ -534,7 +535,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_weak(Dev d, Basis B, 
   load_basis_smem<n>(B, sD);
   SBasis<n> Bs{sD};
   const int e0 = blockIdx.x * EPB;
-  load_face_fluxes<n>(d, sFl, e0);
+  load_face_fluxes<n, E>(d, sFl, e0);
   for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
     const int es = t / n3, x = t - es * n3, e = e0 + es;
     if (e >= d.nElems) continue;

@@ -20,6 +20,14 @@ struct KernelSet {
   void (*flux_adj)(const Dev&, const AdjDev&, const Basis&, cudaStream_t) = nullptr;
   void (*lift_adj)(const Dev&, const AdjDev&, const Basis&, cudaStream_t) = nullptr;
   void (*prep_adj)(const Dev&, const AdjDev&, const Basis&, cudaStream_t) = nullptr;
+  // autotuner candidates: element kernels with another number of elements per CTA (altEPB = 0: none) and
+  // the side kernel with a given block size (64, 128 or 256 threads); fluxBlock is the block size in use
+  int defEPB = 0, altEPB = 0;
+  void (*prep_alt)(const Dev&, const Basis&, cudaStream_t) = nullptr;
+  void (*lift_alt)(const Dev&, const Basis&, cudaStream_t) = nullptr;
+  void (*vol_weak_alt)(const Dev&, const Basis&, int, double, double, cudaStream_t) = nullptr;
+  void (*flux_block)(const Dev&, const Basis&, int, cudaStream_t) = nullptr;
+  int fluxBlock = 128;
   // sets the dynamic shared-memory limits of all kernels; must run before any stream capture
   void (*prepare)() = nullptr;
 };

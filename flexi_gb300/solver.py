@@ -272,6 +272,21 @@ class Flexi:
         self._check(self.L.fg_wall_shear(self.h, ctypes.byref(J), _p(g) if grad else None), "fg_wall_shear")
         return (J.value, g) if grad else J.value
 
+    def autotune(self, reps=10):
+        """Times the candidate launch shapes on this mesh and state and keeps the fastest; returns the
+        per-launch times (ms) and the shapes in use."""
+        rep = np.full(9, np.nan)
+        self._check(self.L.fg_autotune(self.h, int(reps), _p(rep)), "fg_autotune")
+        ch = np.zeros(4, np.int32)
+        self._check(self.L.fg_autotune_choice(self.h, _p(ch)), "fg_autotune_choice")
+        names = ("prep_default", "prep_alt", "lift_default", "lift_alt", "vol_default", "vol_alt", "flux_64", "flux_128", "flux_256")
+        return {"ms_per_launch": {k: (None if np.isnan(v) else float(v)) for k, v in zip(names, rep)},
+                "elements_per_cta": {"prep": int(ch[0]), "lift": int(ch[1]), "vol_weak": int(ch[2])}, "flux_block": int(ch[3])}
+
+    def set_launch_shapes(self, prep, lift, vol_weak, flux_block):
+        """Explicit launch shapes (elements per CTA of prep/lift/weak volume, side-kernel block size)."""
+        self._check(self.L.fg_set_launch_shapes(self.h, int(prep), int(lift), int(vol_weak), int(flux_block)), "fg_set_launch_shapes")
+
     def stream(self):
         s = ctypes.c_void_p()
         self._check(self.L.fg_get_stream(self.h, ctypes.byref(s)), "fg_get_stream")

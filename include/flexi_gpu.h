@@ -223,6 +223,19 @@ int fg_set_body_force_field(fg_handle* h, const double* F);
  * reference. */
 int fg_wall_shear(fg_handle* h, double* J, double* dJdU);
 
+/* Autotuner (no counterpart in the reference): times, on the handle's mesh and current state with CUDA
+ * events over reps launches each, the candidate launch shapes -- elements per CTA of the prep, lifting and
+ * weak-form volume kernels (default and one alternative, N=3 and N=5) and the block size of the side
+ * kernel (64/128/256) -- and keeps the fastest for all later launches (the captured time loop is captured
+ * again). report[9] (optional) = ms per launch of prep default/alternative, lift default/alternative,
+ * volume default/alternative, side kernel 64/128/256 (NaN where not a candidate); the state is unchanged. */
+int fg_autotune(fg_handle* h, int reps, double* report);
+/* Shapes in use: out[0..2] = elements per CTA of prep, lifting, weak-form volume; out[3] = side-kernel block. */
+int fg_autotune_choice(const fg_handle* h, int* out);
+/* Sets the shapes explicitly (each element count the default or the alternative of this N, as
+ * fg_autotune_choice reports them; side block 64/128/256), e.g. to reproduce a tuned run. */
+int fg_set_launch_shapes(fg_handle* h, int epbPrep, int epbLift, int epbVol, int fluxBlock);
+
 /* FP64 FMA throughput probe (TFLOP/s, 2 flop per FMA) of the current device, used for the roofline. */
 int fg_probe_fp64(double* tflops);
 
