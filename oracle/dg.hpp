@@ -39,7 +39,11 @@ inline bool operator>=(FD a, FD b) { return a.v >= b.v; }
 inline FD sqrt(FD a) { ++flop_counter(); return FD(std::sqrt(a.v)); }
 inline FD fabs(FD a) { return FD(std::fabs(a.v)); }
 inline FD pow(FD a, FD b) { ++flop_counter(); return FD(std::pow(a.v, b.v)); }
+inline FD log(FD a) { ++flop_counter(); return FD(std::log(a.v)); }
+inline FD exp(FD a) { ++flop_counter(); return FD(std::exp(a.v)); }
 inline double sqrt(double a) { return std::sqrt(a); }
+inline double log(double a) { return std::log(a); }
+inline double exp(double a) { return std::exp(a); }
 inline double fabs(double a) { return std::fabs(a); }
 inline double pow(double a, double b) { return std::pow(a, b); }
 inline double val(double x) { return x; }
@@ -71,6 +75,8 @@ inline DD pow(DD a, DD b) {
   const double r = std::pow(a.v, b.v);
   return DD(r, r * (b.v * a.d / a.v) + (b.d != 0. ? r * b.d * std::log(a.v) : 0.));
 }
+inline DD log(DD a) { return DD(std::log(a.v), a.d / a.v); }
+inline DD exp(DD a) { const double r = std::exp(a.v); return DD(r, r * a.d); }
 inline double val(DD x) { return x.v; }
 template <class R> inline R rmax(R a, R b) { return a < b ? b : a; }
 template <class R> inline R rmin(R a, R b) { return a < b ? a : b; }
@@ -98,6 +104,65 @@ struct Config {
 static const int NLIFT = 4;
 static const int PRIM_LIFT[4] = {1, 2, 3, 5};  // 0-based prim indices: v1,v2,v3,T
 
+// splitflux.f90:SplitVolumeFluxPI / SplitVolumeFluxSD (factor 2 of the split form included): two-point
+// flux between (u, p) states "R" and "L" with the mean of the two metric vectors
+template <class R>
+void split_volume_flux_t(int splitDG, const R* uR, const R* pR, const R* u, const R* p, const R* mR, const R* m, R* F) {
+  R ft[5], gt[5], ht[5];
+  if (splitDG == SPLIT_PI) {
+    R HR = (uR[4] + pR[4]) / uR[0], H = (u[4] + p[4]) / u[0];
+    R rs = uR[0] + u[0], us = pR[1] + p[1], vs = pR[2] + p[2], ws = pR[3] + p[3], ps = pR[4] + p[4], Hs = HR + H;
+    ft[0] = R(0.5) * rs * us; ft[1] = R(0.25) * rs * us * us + ps; ft[2] = R(0.25) * rs * us * vs; ft[3] = R(0.25) * rs * us * ws; ft[4] = R(0.25) * rs * us * Hs;
+    gt[0] = R(0.5) * rs * vs; gt[1] = ft[2]; gt[2] = R(0.25) * rs * vs * vs + ps; gt[3] = R(0.25) * rs * vs * ws; gt[4] = R(0.25) * rs * vs * Hs;
+    ht[0] = R(0.5) * rs * ws; ht[1] = ft[3]; ht[2] = gt[3]; ht[3] = R(0.25) * rs * ws * ws + ps; ht[4] = R(0.25) * rs * ws * Hs;
+  } else {  // SD
+    R eR = uR[4] + pR[4], e = u[4] + p[4];
+    ft[0] = uR[1] + u[1]; ft[1] = uR[1] * pR[1] + pR[4] + u[1] * p[1] + p[4]; ft[2] = uR[1] * pR[2] + u[1] * p[2]; ft[3] = uR[1] * pR[3] + u[1] * p[3]; ft[4] = eR * pR[1] + e * p[1];
+    gt[0] = uR[2] + u[2]; gt[1] = uR[1] * pR[2] + u[1] * p[2]; gt[2] = uR[2] * pR[2] + pR[4] + u[2] * p[2] + p[4]; gt[3] = uR[2] * pR[3] + u[2] * p[3]; gt[4] = eR * pR[2] + e * p[2];
+    ht[0] = uR[3] + u[3]; ht[1] = uR[1] * pR[3] + u[1] * p[3]; ht[2] = uR[2] * pR[3] + u[2] * p[3]; ht[3] = uR[3] * pR[3] + pR[4] + u[3] * p[3] + p[4]; ht[4] = eR * pR[3] + e * p[3];
+  }
+  R m1 = R(0.5) * (mR[0] + m[0]), m2 = R(0.5) * (mR[1] + m[1]), m3 = R(0.5) * (mR[2] + m[2]);
+  for (int v = 0; v < 5; ++v) F[v] = m1 * ft[v] + m3 * ht[v] + m2 * gt[v];
+}
+
+// surfint.t90:SurfInt, split-Gauss branch (master part surfint.t90:90-140, slave part 177-215; the
+// formulation of Mateo-Gabin, JCP 2023, eq. 5): adds the surface integral of one side of an element to the
+// element's Ut(5,0:N,0:N,0:N). Fside(5,p,q): +Flux_master or -Flux_slave. vol(i,j,k,u,up,m) yields the
+// node's U, UPrim and metric vector of the side's normal direction; face(p,q,u,up,ja) the face state of
+// this side of the element (U_master/UPrim_master or U_slave/UPrim_slave) and its Ja_Face/Ja_slave row.
+// Along the normal line through (p,q): FluxB(l) = SplitDGVolume(U(l), U_face, Metrics(l), Ja_face),
+// Ut(l) += (F - 1/2 (sum_k Leg(k) FluxB(k) - FluxB(l)) NormalSign) LegHat(l).
+template <class R, class VolFn, class FaceFn>
+void split_gauss_surf_side(int splitDG, int N, int ls, int flip, const DGBasis& B, const R* Fside, VolFn vol, FaceFn face, R* Ut) {
+  const int n = N + 1;
+  const bool minus = (ls == XI_MINUS || ls == ETA_MINUS || ls == ZETA_MINUS);
+  const int idx = (ls == XI_MINUS || ls == XI_PLUS) ? 0 : ((ls == ETA_MINUS || ls == ETA_PLUS) ? 1 : 2);
+  const std::vector<double>& Leg = minus ? B.Lm : B.Lp;
+  const std::vector<double>& LegHat = minus ? B.LhatM : B.LhatP;
+  const R NS = R(NormalSigns[ls]);
+  std::vector<R> FluxB((size_t)n * 5);
+  for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
+    const R *uf, *pf, *jf;
+    face(p, q, uf, pf, jf);
+    R sum[5] = {R(0.), R(0.), R(0.), R(0.), R(0.)};
+    for (int l = 0; l <= N; ++l) {
+      auto ijk = side_to_vol(N, l, p, q, flip, ls);
+      const R *uv, *pv, *mv;
+      vol(ijk[0], ijk[1], ijk[2], uv, pv, mv);
+      R* fb = &FluxB[(size_t)ijk[idx] * 5];
+      split_volume_flux_t<R>(splitDG, uv, pv, uf, pf, mv, jf, fb);
+      for (int v = 0; v < 5; ++v) sum[v] = sum[v] + fb[v] * R(Leg[ijk[idx]]);
+    }
+    for (int l = 0; l <= N; ++l) {
+      auto ijk = side_to_vol(N, l, p, q, flip, ls);
+      const R* fb = &FluxB[(size_t)ijk[idx] * 5];
+      R* ut = &Ut[((((size_t)ijk[2] * n + ijk[1]) * n + ijk[0])) * 5];
+      for (int v = 0; v < 5; ++v)
+        ut[v] = ut[v] + (Fside[((size_t)q * n + p) * 5 + v] - R(0.5) * (sum[v] - fb[v]) * NS) * R(LegHat[ijk[idx]]);
+    }
+  }
+}
+
 template <class R>
 struct DG {
   Config C;
@@ -110,6 +175,9 @@ struct DG {
   std::vector<R> LiftFlux, FluxX, FluxY, FluxZ;  // lifting side fluxes
   std::vector<R> Flux_master, Flux_slave;
   std::vector<R> Ut_tmp;
+  // entropy variables (PP_EntropyVars: split form on Gauss nodes, src/CMakeLists.txt:66-71)
+  bool entropyVars = false;
+  std::vector<R> V, V_master, V_slave;
   R BulkVel = R(0.);
   // additional per-node x-momentum body force (an extension of the channel source for the differentiation
   // study: energy source F * BulkVel as for the uniform one; empty = none)
@@ -147,6 +215,8 @@ struct DG {
     gradUx_s = gradUx_m; gradUy_s = gradUx_m; gradUz_s = gradUx_m;
     LiftFlux = gradUx_m; FluxX = gradUx_m; FluxY = gradUx_m; FluxZ = gradUx_m;
     Flux_master.assign(5 * ns2 * nS, R(0.)); Flux_slave = Flux_master;
+    entropyVars = C.splitDG != SPLIT_NONE && C.nodeType == NT_GAUSS;
+    if (entropyVars) { V.assign(5 * nv3 * nE, R(0.)); V_master = U_master; V_slave = U_master; }
     // Carpenter-Kennedy RK4-5 (timedisc_vars.f90:199-214), 1-based stage index
     RKA[2] = 567301805773.0 / 1357537059087.0; RKA[3] = 2404267990393.0 / 2016746695238.0;
     RKA[4] = 3550918686646.0 / 2091501179385.0; RKA[5] = 1275806237668.0 / 842570457699.0;
@@ -195,6 +265,26 @@ struct DG {
     c[0] = p[0];
     c[1] = p[1] * p[0]; c[2] = p[2] * p[0]; c[3] = p[3] * p[0];
     c[4] = sKappaM1 * p[4] + R(0.5) * (c[1] * p[1] + c[2] * p[2] + c[3] * p[3]);
+  }
+
+  // eos.f90:PrimToEntropy -- entropy variables dS/dU of S = -rho s / (kappa-1), s = ln p - kappa ln rho
+  void prim_to_entropy(const R* p, R* w) const {
+    R s = log(p[4]) - kappa * log(p[0]);
+    R rho_p = p[0] / p[4];
+    w[0] = (kappa - s) * sKappaM1 - rho_p * R(0.5) * (p[1] * p[1] + p[2] * p[2] + p[3] * p[3]);
+    w[1] = rho_p * p[1]; w[2] = rho_p * p[2]; w[3] = rho_p * p[3];
+    w[4] = -rho_p;
+  }
+  // eos.f90:EntropyToCons
+  void entropy_to_cons(const R* w, R* c) const {
+    R e2[5];
+    for (int v = 0; v < 5; ++v) e2[v] = w[v] * kappaM1;
+    R ekin = R(0.5) * (e2[1] * e2[1] + e2[2] * e2[2] + e2[3] * e2[3]) / e2[4];
+    R s = kappa - e2[0] + ekin;
+    R rhoe = pow(kappaM1, sKappaM1) * pow(-e2[4], -(kappa / kappaM1)) * exp(-s * sKappaM1);
+    c[0] = -rhoe * e2[4];
+    c[1] = rhoe * e2[1]; c[2] = rhoe * e2[2]; c[3] = rhoe * e2[3];
+    c[4] = rhoe * (R(1.) - ekin);
   }
 
   // ---------------- prolongtoface.t90:ProlongToFace ----------------
@@ -280,6 +370,40 @@ struct DG {
             FluxTmp[((size_t)ab[1] * n + ab[0]) * NV + v] = master ? Fm[si(v, p, q, s, NV)] : slaveSign * Fs[si(v, p, q, s, NV)];
         }
         do_surf_int<NV>(FluxTmp.data(), ls, Uout, e);
+      }
+    }
+  }
+
+  // surfint.t90:SurfInt with SPLIT_DG on Gauss nodes (side loop restated as an element loop over the
+  // element's six sides)
+  void surf_int_split_gauss() {
+    const size_t nv3 = (size_t)n * n * n, ns2 = (size_t)n * n;
+#pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
+    for (int e = 0; e < nE; ++e) {
+      std::vector<R> Fside(ns2 * 5);
+      for (int ls = 1; ls <= 6; ++ls) {
+        const int s = M.ElemToSide[((size_t)e * 6 + ls - 1) * 2 + 0] - 1;
+        const bool master = (s2e(0, s) == e + 1 && s2e(2, s) == ls);
+        const int flip = master ? 0 : M.ElemToSide[((size_t)e * 6 + ls - 1) * 2 + 1];
+        const std::vector<double>& Mx = (ls == XI_MINUS || ls == XI_PLUS) ? M.Mf : ((ls == ETA_MINUS || ls == ETA_PLUS) ? M.Mg : M.Mh);
+        for (size_t x = 0; x < ns2; ++x)
+          for (int v = 0; v < 5; ++v) Fside[x * 5 + v] = master ? Flux_master[(size_t)s * ns2 * 5 + x * 5 + v] : -Flux_slave[(size_t)s * ns2 * 5 + x * 5 + v];
+        R mvol[3], jface[3];
+        auto vol = [&](int i, int j, int k, const R*& u, const R*& up, const R*& m) {
+          const size_t g = (size_t)e * nv3 + ((size_t)k * n + j) * n + i;
+          u = &U[g * 5]; up = &UPrim[g * 6];
+          for (int c = 0; c < 3; ++c) mvol[c] = R(Mx[g * 3 + c]);
+          m = mvol;
+        };
+        auto face = [&](int p, int q, const R*& u, const R*& up, const R*& ja) {
+          const size_t sx = M.sidx(p, q, s);
+          u = master ? &U_master[sx * 5] : &U_slave[sx * 5];
+          up = master ? &UPrim_master[sx * 6] : &UPrim_slave[sx * 6];
+          const std::vector<double>& J = master ? M.JaN_master : M.JaN_slave;
+          for (int c = 0; c < 3; ++c) jface[c] = R(J[sx * 3 + c]);
+          ja = jface;
+        };
+        split_gauss_surf_side<R>(C.splitDG, N, ls, flip, B, Fside.data(), vol, face, &Ut[(size_t)e * nv3 * 5]);
       }
     }
   }
@@ -511,21 +635,7 @@ struct DG {
   }
   // splitflux.f90:SplitVolumeFluxPI / SplitVolumeFluxSD (factor 2 of the split form included)
   void split_volume_flux(const R* uR, const R* pR, const R* u, const R* p, const R* mR, const R* m, R* F) const {
-    R ft[5], gt[5], ht[5];
-    if (C.splitDG == SPLIT_PI) {
-      R HR = (uR[4] + pR[4]) / uR[0], H = (u[4] + p[4]) / u[0];
-      R rs = uR[0] + u[0], us = pR[1] + p[1], vs = pR[2] + p[2], ws = pR[3] + p[3], ps = pR[4] + p[4], Hs = HR + H;
-      ft[0] = R(0.5) * rs * us; ft[1] = R(0.25) * rs * us * us + ps; ft[2] = R(0.25) * rs * us * vs; ft[3] = R(0.25) * rs * us * ws; ft[4] = R(0.25) * rs * us * Hs;
-      gt[0] = R(0.5) * rs * vs; gt[1] = ft[2]; gt[2] = R(0.25) * rs * vs * vs + ps; gt[3] = R(0.25) * rs * vs * ws; gt[4] = R(0.25) * rs * vs * Hs;
-      ht[0] = R(0.5) * rs * ws; ht[1] = ft[3]; ht[2] = gt[3]; ht[3] = R(0.25) * rs * ws * ws + ps; ht[4] = R(0.25) * rs * ws * Hs;
-    } else {  // SD
-      R eR = uR[4] + pR[4], e = u[4] + p[4];
-      ft[0] = uR[1] + u[1]; ft[1] = uR[1] * pR[1] + pR[4] + u[1] * p[1] + p[4]; ft[2] = uR[1] * pR[2] + u[1] * p[2]; ft[3] = uR[1] * pR[3] + u[1] * p[3]; ft[4] = eR * pR[1] + e * p[1];
-      gt[0] = uR[2] + u[2]; gt[1] = uR[1] * pR[2] + u[1] * p[2]; gt[2] = uR[2] * pR[2] + pR[4] + u[2] * p[2] + p[4]; gt[3] = uR[2] * pR[3] + u[2] * p[3]; gt[4] = eR * pR[2] + e * p[2];
-      ht[0] = uR[3] + u[3]; ht[1] = uR[1] * pR[3] + u[1] * p[3]; ht[2] = uR[2] * pR[3] + u[2] * p[3]; ht[3] = uR[3] * pR[3] + pR[4] + u[3] * p[3] + p[4]; ht[4] = eR * pR[3] + e * p[3];
-    }
-    R m1 = R(0.5) * (mR[0] + m[0]), m2 = R(0.5) * (mR[1] + m[1]), m3 = R(0.5) * (mR[2] + m[2]);
-    for (int v = 0; v < 5; ++v) F[v] = m1 * ft[v] + m3 * ht[v] + m2 * gt[v];
+    split_volume_flux_t<R>(C.splitDG, uR, pR, u, p, mR, m, F);
   }
   // splitflux.f90:SplitSurfaceFluxPI / SD on rotated extended states UE(11): 0..4 cons, 5 srho, 6..8 vel, 9 p, 10 T
   void split_surface_flux(const R* L, const R* Rr, R* F) const {
@@ -789,13 +899,23 @@ struct DG {
   // ---------------- dg.f90:DGTimeDerivative_weakForm ----------------
   void time_derivative(double t) {
     const size_t nv3 = (size_t)n * n * n;
-    if (C.splitDG != SPLIT_NONE && C.nodeType != NT_GL)
-      throw std::runtime_error("split form with Gauss nodes needs the split-Gauss surface correction (not restated)");
     long long& fc = flop_counter();
     phase[0] = fc;
 #pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
     for (int e = 0; e < nE; ++e) for (size_t x = 0; x < nv3; ++x) cons_to_prim(&U[((size_t)e * nv3 + x) * 5], &UPrim[((size_t)e * nv3 + x) * 6]);
-    prolong_to_face<5>(U, U_master, U_slave);
+    if (!entropyVars) prolong_to_face<5>(U, U_master, U_slave);
+    else {
+      // eos.f90:ConsToPrimToEntropy, prolongtoface.t90:ProlongToFaceEntropy (EntropyToCons on every side
+      // of an existing element)
+#pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
+      for (int e = 0; e < nE; ++e) for (size_t x = 0; x < nv3; ++x) prim_to_entropy(&UPrim[((size_t)e * nv3 + x) * 6], &V[((size_t)e * nv3 + x) * 5]);
+      prolong_to_face<5>(V, V_master, V_slave);
+      const size_t ns2 = (size_t)n * n;
+      for (int s = 0; s < nS; ++s) for (size_t x = 0; x < ns2; ++x) {
+        if (s2e(0, s) > 0) entropy_to_cons(&V_master[((size_t)s * ns2 + x) * 5], &U_master[((size_t)s * ns2 + x) * 5]);
+        if (s2e(1, s) > 0) entropy_to_cons(&V_slave[((size_t)s * ns2 + x) * 5], &U_slave[((size_t)s * ns2 + x) * 5]);
+      }
+    }
     // equation.f90:GetPrimitiveStateSurface
     for (int s = 0; s < nS; ++s) for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
       cons_to_prim(&U_master[si(0, p, q, s, 5)], &UPrim_master[si(0, p, q, s, 6)]);
@@ -808,7 +928,8 @@ struct DG {
     phase[3] = fc;
     fill_flux(t);
     phase[4] = fc;
-    surf_int<5>(Flux_master, Flux_slave, Ut, R(-1.));
+    if (entropyVars) surf_int_split_gauss();
+    else surf_int<5>(Flux_master, Flux_slave, Ut, R(-1.));
     // Ut = -Ut ; TestcaseSource (channel) ; ApplyJacobianCons
 #pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
     for (int e = 0; e < nE; ++e) for (size_t x = 0; x < nv3; ++x) {

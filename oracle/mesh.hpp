@@ -93,6 +93,9 @@ struct Mesh {
   std::vector<double> Mf, Mg, Mh;  // Metrics_f/g/hTilde (3,0:N,0:N,0:N,nElems)
   std::vector<double> sJ;          // (0:N,0:N,0:N,nElems)
   std::vector<double> NormVec, TangVec1, TangVec2, Face_xGP;  // (3,0:N,0:N,nSides)
+  // row NormalDir of the face metrics Ja_Face (master, flip 0) and Ja_slave (slave, its own flip), in side
+  // orientation (3,0:N,0:N,nSides): used by the split-Gauss surface integral (surfint.t90:90-140)
+  std::vector<double> JaN_master, JaN_slave;
   std::vector<double> SurfElem;    // (0:N,0:N,nSides)
   std::vector<double> Elem_xGP;    // (3,0:N,0:N,0:N,nElems)
   double Vol = 0.;
@@ -213,6 +216,7 @@ inline void build_mesh(const MeshInput& in, int N, int nodeType, Mesh& M) {
   M.sJ.assign(nv3 * nE, 0.); M.Elem_xGP.assign(3 * nv3 * nE, 0.);
   const size_t nsp = (size_t)n * n;
   M.NormVec.assign(3 * nsp * M.nSides, 0.); M.TangVec1 = M.NormVec; M.TangVec2 = M.NormVec; M.Face_xGP = M.NormVec;
+  M.JaN_master = M.NormVec; M.JaN_slave = M.NormVec;
   M.SurfElem.assign(nsp * M.nSides, 0.);
   const int nr = NGeoRef + 1;
 
@@ -307,7 +311,6 @@ inline void build_mesh(const MeshInput& in, int N, int nodeType, Mesh& M) {
           for (int c = 0; c < 3; ++c) M.Face_xGP[M.sidx(p, q, SideID) * 3 + c] = tmp2[((size_t)pq[1] * n + pq[0]) * 3 + c];
         }
       }
-      if (flip != 0) continue;
       std::vector<double> JaF(nsp * 9);
       for (int dd = 0; dd < 3; ++dd) {
         std::vector<double> tmp(nsp * 3), tmp2(nsp * 3);
@@ -321,8 +324,13 @@ inline void build_mesh(const MeshInput& in, int N, int nodeType, Mesh& M) {
           for (int c = 0; c < 3; ++c) JaF[((size_t)q * n + p) * 9 + dd * 3 + c] = tmp2[((size_t)pq[1] * n + pq[0]) * 3 + c];
         }
       }
-      // SurfMetricsFromJa
       int nd = NormalDirs[ls] - 1, td = TangDirs[ls] - 1; double ns = NormalSigns[ls];
+      // Ja_Face / Ja_slave (metrics.f90:704-705), row nd only
+      std::vector<double>& JaN = flip == 0 ? M.JaN_master : M.JaN_slave;
+      for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p)
+        for (int c = 0; c < 3; ++c) JaN[M.sidx(p, q, SideID) * 3 + c] = JaF[((size_t)q * n + p) * 9 + nd * 3 + c];
+      if (flip != 0) continue;
+      // SurfMetricsFromJa
       for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
         const double* J = &JaF[((size_t)q * n + p) * 9];
         size_t si = M.sidx(p, q, SideID);

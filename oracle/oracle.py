@@ -66,6 +66,7 @@ def lib():
         _lib.orc_mappings.argtypes = [ctypes.c_int, P, P]
         _lib.orc_prolong_unittest.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P]
         _lib.orc_surfint_unittest.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P]
+        _lib.orc_surfint_split_unittest.argtypes = [ctypes.c_int, ctypes.c_int, P, P, P, P, P, P, P]
         _lib.orc_tgv_exact.argtypes = [ctypes.c_int, P, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int, P]
         _lib.orc_tgv_analysis.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P, P, P, ctypes.c_int,
                                           ctypes.c_double, ctypes.c_double, ctypes.c_double, P]
@@ -289,6 +290,17 @@ def surfint_unittest(N, node_type, side_to_elem, s2v2, LhM, LhP, Flux):
     Ut = np.zeros((n, n, n))
     lib().orc_surfint_unittest(N, node_type, nS, _p(s2e), _p(s2v2), _p(np.ascontiguousarray(LhM)), _p(np.ascontiguousarray(LhP)),
                                _p(np.ascontiguousarray(Flux)), _p(Ut))
+    return Ut
+
+
+def surfint_split_unittest(N, side_to_elem, Lm, Lp, LhM, LhP, Flux):
+    """Split-Gauss SurfInt of the reference's unit test (unit states and metrics, SD split flux)."""
+    n = N + 1
+    nS = side_to_elem.shape[0]
+    s2e = np.ascontiguousarray(side_to_elem, np.int32)
+    Ut = np.zeros((n, n, n))
+    args = [np.ascontiguousarray(a, np.float64) for a in (Lm, Lp, LhM, LhP, Flux)]
+    lib().orc_surfint_split_unittest(N, nS, _p(s2e), *[_p(a) for a in args], _p(Ut))
     return Ut
 
 

@@ -342,6 +342,34 @@ void orc_surfint_unittest(int N, int nodeType, int nSides, const int* SideToElem
   }
 }
 
+// SurfInt with SPLIT_DG on Gauss nodes for the unit-test element as the reference's unit test sets it up
+// (unitTests/SurfInt.f90:130-150): U, UPrim, U_master, UPrim_master, metrics and face metrics all 1,
+// SplitVolumeFluxSD; Flux_master = Flux_slave = Flux in every variable. Returns Ut of the first variable.
+void orc_surfint_split_unittest(int N, int nSides, const int* SideToElem, const double* Lm, const double* Lp, const double* LhM,
+                                const double* LhP, const double* Flux, double* Ut1) {
+  const int n = N + 1;
+  const size_t n3 = (size_t)n * n * n, n2 = (size_t)n * n;
+  DGBasis B;
+  B.init(N, NT_GAUSS);
+  for (int l = 0; l < n; ++l) { B.Lm[l] = Lm[l]; B.Lp[l] = Lp[l]; B.LhatM[l] = LhM[l]; B.LhatP[l] = LhP[l]; }
+  std::vector<double> Ut(5 * n3, 0.), Fside(5 * n2);
+  const double ones[6] = {1., 1., 1., 1., 1., 1.};
+  auto vol = [&](int, int, int, const double*& u, const double*& up, const double*& m) { u = ones; up = ones; m = ones; };
+  auto face = [&](int, int, const double*& u, const double*& up, const double*& ja) { u = ones; up = ones; ja = ones; };
+  for (int s = 0; s < nSides; ++s) {
+    const int e = SideToElem[s * 5 + 0], ne = SideToElem[s * 5 + 1];
+    if (e > 0) {
+      for (size_t x = 0; x < n2; ++x) for (int v = 0; v < 5; ++v) Fside[x * 5 + v] = Flux[(size_t)s * n2 + x];
+      split_gauss_surf_side<double>(SPLIT_SD, N, SideToElem[s * 5 + 2], 0, B, Fside.data(), vol, face, Ut.data());
+    }
+    if (ne > 0) {
+      for (size_t x = 0; x < n2; ++x) for (int v = 0; v < 5; ++v) Fside[x * 5 + v] = -Flux[(size_t)s * n2 + x];
+      split_gauss_surf_side<double>(SPLIT_SD, N, SideToElem[s * 5 + 3], SideToElem[s * 5 + 4], B, Fside.data(), vol, face, Ut.data());
+    }
+  }
+  for (size_t x = 0; x < n3; ++x) Ut1[x] = Ut[x * 5];
+}
+
 // --------------------------------------------------------------------------------------------
 // Taylor-Green vortex: taylorgreenvortex/testcase.f90:ExactFuncTestcase and AnalyzeTestcase
 // --------------------------------------------------------------------------------------------

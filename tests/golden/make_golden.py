@@ -2,8 +2,9 @@
 
 Reads FLEXI v25.10's unit-test data (unitTests/*.bin, Fortran unformatted sequential records:
 4-byte length marker, little-endian payload, closing marker) and the Taylor-Green regression
-reference (regressioncheck/checks/tgv/split/TGV_Re1600_Split_TGVAnalysis_Reference.csv), and
-stores the arrays the parity tests need in reference_unittests.npz / tgv_split_reference.npz.
+references (regressioncheck/checks/tgv/{split,splitGauss}/TGV_Re1600_Split_TGVAnalysis_Reference.csv),
+and stores the arrays the parity tests need in reference_unittests.npz, tgv_split_reference.npz and
+tgv_splitgauss_reference.npz.
 
 Run from the repository root in a container that has the reference mounted:
     python tests/golden/make_golden.py /root/reference
@@ -81,13 +82,15 @@ def main(ref):
     out["dmat_D"], _ = f64(rec, 0, (11, 11, 40))
     np.savez_compressed(os.path.join(os.path.dirname(__file__), "reference_unittests.npz"), **out)
 
-    csv = os.path.join(ref, "regressioncheck/checks/tgv/split/TGV_Re1600_Split_TGVAnalysis_Reference.csv")
-    lines = open(csv).read().strip().splitlines()
-    header = [h.strip() for h in lines[0].split(",")]
-    rows = np.array([[float(v) for v in ln.split(",")] for ln in lines[1:]])
-    np.savez_compressed(os.path.join(os.path.dirname(__file__), "tgv_split_reference.npz"),
-                        header=np.array(header), rows=rows)
-    print("wrote fixtures:", sorted(out.keys()), rows.shape)
+    # tgv/split (Gauss-Lobatto, N=7) and tgv/splitGauss (Gauss, N=5, entropy-variable prolongation)
+    for case, name in (("split", "tgv_split_reference.npz"), ("splitGauss", "tgv_splitgauss_reference.npz")):
+        csv = os.path.join(ref, f"regressioncheck/checks/tgv/{case}/TGV_Re1600_Split_TGVAnalysis_Reference.csv")
+        lines = open(csv).read().strip().splitlines()
+        header = [h.strip() for h in lines[0].split(",")]
+        rows = np.array([[float(v) for v in ln.split(",")] for ln in lines[1:]])
+        np.savez_compressed(os.path.join(os.path.dirname(__file__), name), header=np.array(header), rows=rows)
+        print("wrote", name, rows.shape)
+    print("wrote fixtures:", sorted(out.keys()))
 
 
 if __name__ == "__main__":

@@ -64,3 +64,16 @@ def test_surf_int(golden, tag, node_type):
     Ut = orc.surfint_unittest(N, node_type, s2e, s2v2, golden["elem_L_HatMinus"], golden["elem_L_HatPlus"], flux)
     ref = np.transpose(golden[f"surfint_{tag}"][..., 0], (2, 1, 0))
     assert almost_equal_abs_or_rel(Ut, ref, 100 * EPS).all()
+
+
+def test_surf_int_split_gauss(golden):
+    """unitTests/SurfInt.f90 with SPLIT_DG on Gauss nodes: the split-Gauss surface integral of a random flux
+    with unit states and metrics (its correction vanishes for a constant state); the reference compares at
+    200 x PP_RealTolerance."""
+    N = 9
+    s2e = golden["elem_SideToElem"].T.copy()
+    flux = np.transpose(golden["surfint_Flux"], (2, 1, 0)).copy()
+    Ut = orc.surfint_split_unittest(N, s2e, golden["elem_L_Minus"], golden["elem_L_Plus"], golden["elem_L_HatMinus"],
+                                    golden["elem_L_HatPlus"], flux)
+    ref = np.transpose(golden["surfint_G3D_Split"][..., 0], (2, 1, 0))
+    assert almost_equal_abs_or_rel(Ut, ref, 200 * EPS).all()

@@ -1,8 +1,10 @@
-"""End-to-end pin of the CPU oracle: FLEXI's Taylor-Green regression reference
-(regressioncheck/checks/tgv/split: GL N=7, split PI, RoeEntropyFix, BR1, 8^3 periodic, CFL=DFL=0.8,
-Re=1600, Ma=0.1, R=71.42857), whose TGVAnalysis CSV rows are written every 10 steps and compared by
-the reference at 1e-4 relative (analyze.ini). Checks the t=0 row and the first rows after stepping
-with the reference's time-step control (UpdateTimeStep/CALCTIMESTEP), including the time column."""
+"""End-to-end pin of the CPU oracle: FLEXI's Taylor-Green regression references
+regressioncheck/checks/tgv/split (GL N=7) and tgv/splitGauss (Gauss N=5: split form with
+entropy-variable prolongation and the split-Gauss surface integral), both split PI, RoeEntropyFix, BR1,
+8^3 periodic, CFL=DFL=0.8, Re=1600, Ma=0.1, R=71.42857. Their TGVAnalysis CSV rows are written every 10
+steps and compared by the reference at 1e-4 relative (analyze.ini). Checks the t=0 row and the first rows
+after stepping with the reference's time-step control (UpdateTimeStep/CALCTIMESTEP), including the time
+column."""
 import numpy as np
 import pytest
 
@@ -12,7 +14,9 @@ from oracle import oracle as orc
 TGV_CFG = dict(N=7, nodeType=orc.NT_GL, riemann=33, riemannBC=-1, lifting=1, weakLifting=0, consLifting=0, splitDG=4,
                etaBR2=2.0, etaBR2_wall=-1.0, kappa=1.4, R=71.42857, Pr=0.72, mu0=6.25e-4, CFLScale=0.8, DFLScale=0.8,
                doTCSource=0, dpdx=-1.0)
+TGV_GAUSS_CFG = dict(TGV_CFG, N=5, nodeType=orc.NT_GAUSS)
 REL = 1e-4
+CASES = {"split": ("tgv_reference", TGV_CFG), "splitGauss": ("tgv_splitgauss_reference", TGV_GAUSS_CFG)}
 
 
 def tgv_oracle(n=8, cfg=TGV_CFG):
@@ -37,19 +41,23 @@ def compare_row(row, ref, scale):
             assert abs(row[c]) <= 1e-9 * scale[c], (c, row[c], ref[c])
 
 
-def test_tgv_t0_row(tgv_reference):
-    _, rows = tgv_reference
-    o = tgv_oracle()
+@pytest.mark.parametrize("case", list(CASES))
+def test_tgv_t0_row(case, request):
+    fixture, cfg = CASES[case]
+    _, rows = request.getfixturevalue(fixture)
+    o = tgv_oracle(cfg=cfg)
     o.time_derivative(0.0)
-    a = analysis(o)
+    a = analysis(o, cfg)
     scale = np.abs(rows[:, 1:]).max(axis=0)
     compare_row(a, rows[0, 1:], scale)
 
 
 @pytest.mark.timeout(900)
-def test_tgv_first_rows(tgv_reference):
-    _, rows = tgv_reference
-    o = tgv_oracle()
+@pytest.mark.parametrize("case", list(CASES))
+def test_tgv_first_rows(case, request):
+    fixture, cfg = CASES[case]
+    _, rows = request.getfixturevalue(fixture)
+    o = tgv_oracle(cfg=cfg)
     scale = np.abs(rows[:, 1:]).max(axis=0)
     t = 0.0
     o.time_derivative(0.0)
@@ -59,4 +67,4 @@ def test_tgv_first_rows(tgv_reference):
             assert err == 0
             t = o.timestep(t, dt)
         assert abs(t - rows[r, 0]) <= 1e-10 * rows[r, 0], (t, rows[r, 0])
-        compare_row(analysis(o), rows[r, 1:], scale)
+        compare_row(analysis(o, cfg), rows[r, 1:], scale)
