@@ -35,6 +35,7 @@ struct Basis {
   double Lm[FG_MAXN], Lp[FG_MAXN], LhM[FG_MAXN], LhP[FG_MAXN];
   double kappa, kappaM1, sKappaM1, Rgas, sR, lambdaFac, etaBR2, etaBR2_wall;
   double kappaFac, sKappaP1;
+  double kappaM1_sKappaM1, kappa_kappaM1;  // (kappa-1)^(1/(kappa-1)), kappa/(kappa-1): eos.f90:EntropyToCons
 };
 
 // Device arrays of one solver handle (all sizes in units of doubles / ints).
@@ -56,6 +57,7 @@ struct Dev {
   double* faceS;   // [s][FS_NF][n2]
   double* gradM;   // [s][12][n2]
   double* gradS;   // [s][12][n2]
+  double* faceJa;  // [e][6][3][n2]: normal row of the element's own face metrics (split form on Gauss nodes; else null)
   double* geo;     // [s][FG_NF][n2]
   double* flux;    // [s][5][n2] numerical flux times SurfElem, master orientation
   int* sideElem;   // [s][4]: master elem, master locSide, slave elem (-1: BC side), 8*slave locSide + flip

@@ -361,6 +361,8 @@ void init_basis(fg_handle* h) {
   B.etaBR2 = c.etaBR2; B.etaBR2_wall = (c.etaBR2_wall == -1.) ? c.etaBR2 : c.etaBR2_wall;
   B.kappaFac = 2. * c.kappa / (c.kappa - 1.);
   B.sKappaP1 = 1. / (c.kappa + 1.);
+  B.kappaM1_sKappaM1 = std::pow(c.kappa - 1., 1. / (c.kappa - 1.));
+  B.kappa_kappaM1 = c.kappa / (c.kappa - 1.);
   // Carpenter-Kennedy RK4-5, timedisc_vars.f90:199-214
   double* A = h->RKA; double* b = h->RKb; double* cc = h->RKc;
   A[2] = 567301805773.0 / 1357537059087.0; A[3] = 2404267990393.0 / 2016746695238.0;
@@ -419,6 +421,8 @@ int upload_mesh(fg_handle* h) {
   if ((r = dalloc(h, d.gradM, (size_t)nS * 12 * n2))) return r;
   if ((r = dalloc(h, d.gradS, (size_t)nS * 12 * n2))) return r;
   if ((r = upload(h, d.geo, M.geo))) return r;
+  if (h->cfg.SplitDG >= 0 && h->cfg.NodeType == FG_NODE_GAUSS)
+    if ((r = upload(h, d.faceJa, M.faceJa))) return r;
   if ((r = dalloc(h, d.flux, (size_t)nS * 5 * n2))) return r;
   if ((r = upload(h, d.sideElem, M.sideElem))) return r;
   if ((r = upload(h, d.sideInst, M.sideInst))) return r;
@@ -550,6 +554,8 @@ namespace {
 // the adjoint kernels cover: weak form and split form PI, LF/Roe/RoeEntropyFix, BR1/BR2
 const char* adjoint_unsupported(const fg_config& c) {
   if (c.SplitDG != FG_SPLIT_NONE && c.SplitDG != FG_SPLIT_PI) return "the adjoint supports the weak form and the split form PI";
+  if (c.SplitDG != FG_SPLIT_NONE && (c.NodeType != FG_NODE_GAUSS_LOBATTO || (c.N != 1 && c.N != 3 && c.N != 7)))
+    return "the adjoint of the split form supports Gauss-Lobatto nodes with N = 1, 3, 7";
   if (c.Riemann != FG_RIEMANN_LF && c.Riemann != FG_RIEMANN_ROE && c.Riemann != FG_RIEMANN_ROEENTROPYFIX)
     return "the adjoint supports the LF, Roe and RoeEntropyFix surface fluxes";
   return nullptr;
@@ -688,8 +694,6 @@ int fg_create(const fg_config* cfg, fg_handle** out) {
   else if (c.doConservativeLifting) why = "doConservativeLifting is not supported";
   else if (c.doWeakLifting) why = "doWeakLifting is not supported (the volume part needs the conservative form)";
   else if (c.SplitDG != FG_SPLIT_NONE && c.SplitDG != FG_SPLIT_SD && c.SplitDG != FG_SPLIT_PI) why = "SplitDG must be -1 (weak), 0 (SD) or 4 (PI)";
-  else if (c.SplitDG != FG_SPLIT_NONE && c.NodeType != FG_NODE_GAUSS_LOBATTO) why = "the split form is supported with Gauss-Lobatto nodes";
-  else if (c.SplitDG != FG_SPLIT_NONE && c.N != 1 && c.N != 3 && c.N != 7) why = "the split form supports N = 1, 3, 7";
   else if (c.TimeDiscMethod != 0) why = "TimeDiscMethod must be CarpenterRK4-5";
   if (!why.empty()) { delete h; return fail(nullptr, FG_ERR_CONFIG, why); }
   h->K = get_kernel_set(c.N + 1, c.NodeType == FG_NODE_GAUSS_LOBATTO);
@@ -737,6 +741,29 @@ int fg_set_mesh(fg_handle* h, int nElems, int nSides, int nBCSides, const int* S
     return fail(h, FG_ERR_MESH, e.what());
   }
   return upload_mesh(h);
+}
+
+int fg_set_face_metrics(fg_handle* h, const double* Ja_Face, const double* Ja_slave) {
+  if (!h || !h->haveHostMesh) return fail(h, FG_ERR_STATE, "fg_set_face_metrics needs a mesh");
+  if (!Ja_Face || !Ja_slave) return fail(h, FG_ERR_CONFIG, "Ja_Face and Ja_slave are required");
+  fgh::HostMesh& M = h->M;
+  const int n = M.n, n2 = n * n, N = M.N;
+  static const int normalDir[7] = {0, 2, 1, 0, 1, 0, 2};  // 0-based row, mesh_vars.f90:105-111
+  for (int e = 0; e < M.nElems; ++e)
+    for (int ls = 1; ls <= 6; ++ls) {
+      const int code = M.elemSide[e * 6 + ls - 1], s = code >> 3, flip = code & 7;
+      const double* J = flip == 0 ? Ja_Face : Ja_slave;
+      for (int q = 0; q < n; ++q)
+        for (int p = 0; p < n; ++p) {
+          int a, b;
+          side_to_vol2(N, p, q, flip, ls, a, b);
+          for (int c = 0; c < 3; ++c)
+            M.faceJa[(((size_t)e * 6 + ls - 1) * 3 + c) * n2 + a + n * b] = J[((((size_t)s * n + q) * n + p) * 3 + c) * 3 + normalDir[ls]];
+        }
+    }
+  if (h->haveMesh && h->d.faceJa)
+    CUDA_TRY(cudaMemcpy(h->d.faceJa, M.faceJa.data(), sizeof(double) * M.faceJa.size(), cudaMemcpyHostToDevice));
+  return FG_OK;
 }
 
 int fg_set_instance_mu0(fg_handle* h, int nInst, const double* mu0) {

@@ -16,6 +16,12 @@ struct Inst {
   }
   static size_t smem_weak() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * (15 * S::n3 + 6 * S::n2 * 5)); }
   static size_t smem_split() { return sizeof(double) * (SBasis<n>::SIZE + 2 * S::n2 + S::EPB * (20 * S::n3 + 6 * S::n2 * 5)); }
+  // the tuned shuffle-pair kernel for Gauss-Lobatto lines of 2, 4 or 8 nodes; k_vol_split_gen otherwise
+  static constexpr bool SPLIT_POW2 = GL && (n == 2 || n == 4 || n == 8);
+  static size_t smem_split_gen() {
+    using SS = SplitShape<n>;
+    return sizeof(double) * (SBasis<n>::SIZE + 2 * S::n2 + S::EPB * (20 * S::n3 + 6 * S::n2 * 5) + (GL ? 0 : S::EPB * 6 * SS::FACE_NF * S::n2));
+  }
   static size_t smem_weak_adj() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * 5 * S::n3 + S::THREADS); }
   static size_t smem_split_adj() { return sizeof(double) * (SBasis<n>::SIZE + 2 * S::n2 + S::EPB * 26 * S::n3 + S::THREADS); }
   static size_t smem_lift_adj() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * (13 * S::n3 + 6 * S::n2 * 19)); }
@@ -64,7 +70,8 @@ struct Inst {
     set_smem(k_prep<n, GL>, smem_prep());
     set_smem(k_lift<n, GL>, smem_lift());
     set_smem(k_vol_weak<n, GL>, smem_weak());
-    if constexpr (GL && (n == 2 || n == 4 || n == 8)) set_smem(k_vol_split<n>, smem_split());
+    if constexpr (SPLIT_POW2) set_smem(k_vol_split<n>, smem_split());
+    else set_smem(k_vol_split_gen<n, GL>, smem_split_gen());
     set_smem(k_vol_weak_adj<n, GL>, smem_weak_adj());
     set_smem(k_lift_adj<n, GL>, smem_lift_adj());
     set_smem(k_prep_adj<n, GL>, smem_prep_adj());
@@ -108,9 +115,8 @@ struct Inst {
     k_vol_weak<n, GL><<<blocks(d), S::THREADS, smem_weak(), st>>>(d, B, Stage{mode, rkA, rkB});
   }
   static void vol_split(const Dev& d, const Basis& B, int mode, double rkA, double rkB, cudaStream_t st) {
-    if constexpr (GL && (n == 2 || n == 4 || n == 8)) {
-      k_vol_split<n><<<blocks(d), S::THREADS, smem_split(), st>>>(d, B, Stage{mode, rkA, rkB});
-    }
+    if constexpr (SPLIT_POW2) k_vol_split<n><<<blocks(d), S::THREADS, smem_split(), st>>>(d, B, Stage{mode, rkA, rkB});
+    else k_vol_split_gen<n, GL><<<blocks(d), SplitShape<n>::THREADS, smem_split_gen(), st>>>(d, B, Stage{mode, rkA, rkB});
   }
   static void dt(const Dev& d, const Basis& B, const double* ma, const double* mv, double cfl, double dfl, double* bulk, const double* wv,
                  cudaStream_t st) {
@@ -121,7 +127,7 @@ struct Inst {
     k.n = n; k.gl = GL;
     k.prepare = &prepare;
     k.prep = &prep; k.lift = &lift; k.flux = &flux; k.vol_weak = &vol_weak; k.dt = &dt;
-    if (GL && (n == 2 || n == 4 || n == 8)) k.vol_split = &vol_split;
+    k.vol_split = &vol_split;
     k.vol_adj = &vol_adj; k.flux_adj = &flux_adj; k.lift_adj = &lift_adj; k.prep_adj = &prep_adj;
     k.defEPB = S::EPB;
     k.flux_block = &flux_block;

@@ -52,7 +52,10 @@ template <int n> struct SBasis {
 };
 
 // =====================================================================================================
-// k_prep: eos.f90:ConsToPrim (volume), prolongtoface.t90:ProlongToFace, equation.f90:GetPrimitiveStateSurface
+// k_prep: eos.f90:ConsToPrim (volume), prolongtoface.t90:ProlongToFace, equation.f90:GetPrimitiveStateSurface.
+// Split form on Gauss nodes (PP_EntropyVars): the entropy variables are prolonged instead of U and turned
+// back into conservative face states (eos.f90:ConsToPrimToEntropy, prolongtoface.t90:ProlongToFaceEntropy,
+// eos.f90:EntropyToCons).
 // =====================================================================================================
 template <int n, bool GL, int E = 0>
 __global__ void __launch_bounds__(Shape<n, E>::THREADS) k_prep(Dev d, Basis B) {
@@ -60,10 +63,11 @@ __global__ void __launch_bounds__(Shape<n, E>::THREADS) k_prep(Dev d, Basis B) {
   constexpr int n2 = S::n2, n3 = S::n3, EPB = S::EPB, N = S::N;
   extern __shared__ double smem[];
   double* sD = smem;
-  double* sU = smem + SBasis<n>::SIZE;         // [EPB][5][n3]
+  double* sU = smem + SBasis<n>::SIZE;         // [EPB][5][n3] U, or the entropy variables
   double* sP = sU + EPB * 5 * n3;              // [EPB][VP_NF][n3]
   load_basis_smem<n>(B, sD);
   SBasis<n> Bs{sD};
+  const bool entropy = !GL && B.splitDG >= 0;
   const int e0 = blockIdx.x * EPB;
   for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
     const int es = t / n3, x = t - es * n3, e = e0 + es;
@@ -80,6 +84,14 @@ __global__ void __launch_bounds__(Shape<n, E>::THREADS) k_prep(Dev d, Basis B) {
     for (int f = 0; f < VP_NF; ++f) {
       d.prim[((size_t)e * VP_NF + f) * n3 + x] = pr[f];
       sP[(es * VP_NF + f) * n3 + x] = pr[f];
+    }
+    if (entropy) {
+      // PrimToEntropy: s = ln p - kappa ln rho; W = ((kappa - s)/(kappa-1) - rho/p |v|^2/2, rho/p v, -rho/p)
+      const double sEnt = log(p) - B.kappa * log(u[0]);
+      const double rho_p = u[0] / p;
+      u[0] = (B.kappa - sEnt) * B.sKappaM1 - rho_p * 0.5 * (vx * vx + vy * vy + vz * vz);
+      u[1] = rho_p * vx; u[2] = rho_p * vy; u[3] = rho_p * vz;
+      u[4] = -rho_p;
     }
 #pragma unroll
     for (int v = 0; v < 5; ++v) sU[(es * 5 + v) * n3 + x] = u[v];
@@ -113,6 +125,16 @@ __global__ void __launch_bounds__(Shape<n, E>::THREADS) k_prep(Dev d, Basis B) {
         const double L = minus ? Bs.Lm(l) : Bs.Lp(l);
 #pragma unroll
         for (int v = 0; v < 5; ++v) c[v] = fma(sU[(es * 5 + v) * n3 + x], L, c[v]);
+      }
+      if (entropy) {
+        // EntropyToCons: rho e = (kappa-1)^(1/(kappa-1)) (-W5')^(-kappa/(kappa-1)) exp(-s/(kappa-1)), W' = (kappa-1) W
+        const double w0 = c[0] * B.kappaM1, w1 = c[1] * B.kappaM1, w2 = c[2] * B.kappaM1, w3 = c[3] * B.kappaM1, w4 = c[4] * B.kappaM1;
+        const double ekin = 0.5 * (w1 * w1 + w2 * w2 + w3 * w3) / w4;
+        const double sEnt = B.kappa - w0 + ekin;
+        const double rhoe = B.kappaM1_sKappaM1 * pow(-w4, -B.kappa_kappaM1) * exp(-sEnt * B.sKappaM1);
+        c[0] = -rhoe * w4;
+        c[1] = rhoe * w1; c[2] = rhoe * w2; c[3] = rhoe * w3;
+        c[4] = rhoe * (1.0 - ekin);
       }
       const double srho = 1.0 / c[0];
       const double vx = c[1] * srho, vy = c[2] * srho, vz = c[3] * srho;
@@ -788,6 +810,232 @@ __global__ void __launch_bounds__(Shape<n>::THREADS, (n == 8 ? 2 : 1)) k_vol_spl
     }
     finish_node<n, true>(d, Bs, st, sFl, es, e, x, ut);
   }
+}
+
+// =====================================================================================================
+// k_vol_split_gen: volint.f90:VolInt_splitForm for any number of nodes per line, Gauss or Gauss-Lobatto.
+// The lines of one direction are packed SEG = 32/n to a warp (n lanes each, the last 32 - SEG*n lanes of a
+// warp idle); a lane evaluates the pairs (a, a+dd mod n) for dd = 1..n/2 and hands the unscaled flux to its
+// partner by shuffle as in k_vol_split (for odd n every pair is evaluated once).
+// Gauss nodes (surfint.t90:90-140, 177-215, split-Gauss surface integral): in the same pass each lane
+// evaluates the two-point flux FluxB between its node and the element's own face state at both ends of the
+// line (metric: its node's metric vector plus the face metric row Ja_Face / Ja_slave), the segment forms
+// FluxB_sum = sum_k Leg(k) FluxB(k) with shuffles, and the lane adds -1/2 NormalSign LegHat(a)
+// (FluxB_sum - FluxB(a)); the numerical-flux part is the Gauss surface integral of finish_node.
+// =====================================================================================================
+template <int n> struct SplitShape {
+  static constexpr int EPB = Shape<n>::EPB, n2 = n * n, n3 = n * n * n;
+  static constexpr int SEG = 32 / n;                       // lines per warp
+  static constexpr int LINES = EPB * n2;                   // lines per direction per CTA
+  static constexpr int LINE_THREADS = ((LINES + SEG - 1) / SEG) * 32;
+  static constexpr int NODE_THREADS = ((EPB * n3 + 31) / 32) * 32;
+  static constexpr int THREADS = LINE_THREADS > NODE_THREADS ? LINE_THREADS : NODE_THREADS;
+  static constexpr int FACE_NF = 9;  // rho, u, v, w, p-term, H-term, face metric row (3)
+};
+
+template <int n, bool GL>
+__global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d, Basis B, Stage st) {
+  using SS = SplitShape<n>;
+  constexpr int n2 = SS::n2, n3 = SS::n3, EPB = SS::EPB, N = n - 1, SEG = SS::SEG, FNF = SS::FACE_NF;
+  extern __shared__ double smem[];
+  double* sD = smem;
+  double* sC = sD + SBasis<n>::SIZE;   // [2][n2]: DVolSurf(l,i) x density factor, x factor of the other components
+  double* sR = sC + 2 * n2;            // [EPB][15][n3]: rho, u, v, w, p-term, H-term, metrics(9); later viscous fluxes(12)
+  double* sA = sR + EPB * 15 * n3;     // [EPB][5][n3] split-flux divergence
+  double* sFl = sA + EPB * 5 * n3;     // [EPB][6][n2][5]
+  double* sFS = sFl + EPB * 6 * n2 * 5;  // Gauss: [EPB][6][FNF][n2] own face states and face metric rows
+  load_basis_smem<n>(B, sD);
+  SBasis<n> Bs{sD};
+  const bool pi = B.splitDG == 4;
+  const double f0 = pi ? 0.25 : 0.5, f1 = pi ? 0.125 : 0.5;
+  for (int t = threadIdx.x; t < n2; t += blockDim.x) { sC[t] = B.DVS[t] * f0; sC[n2 + t] = B.DVS[t] * f1; }
+  const int e0 = blockIdx.x * EPB;
+  load_face_fluxes<n>(d, sFl, e0);
+  for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
+    const int es = t / n3, x = t - es * n3, e = e0 + es;
+    if (e >= d.nElems) continue;
+    double* Q = sR + es * 15 * n3;
+    const double u0 = d.U[((size_t)e * 5 + 0) * n3 + x], u4 = d.U[((size_t)e * 5 + 4) * n3 + x];
+    const double srho = d.prim[((size_t)e * VP_NF + VP_SRHO) * n3 + x];
+    const double p = d.prim[((size_t)e * VP_NF + VP_P) * n3 + x];
+    Q[x] = u0;
+    Q[n3 + x] = d.prim[((size_t)e * VP_NF + VP_U) * n3 + x];
+    Q[2 * n3 + x] = d.prim[((size_t)e * VP_NF + VP_V) * n3 + x];
+    Q[3 * n3 + x] = d.prim[((size_t)e * VP_NF + VP_W) * n3 + x];
+    Q[4 * n3 + x] = pi ? 4.0 * p : p;
+    Q[5 * n3 + x] = pi ? (u4 + p) * srho : u4 + p;
+#pragma unroll
+    for (int c = 0; c < 9; ++c) Q[(6 + c) * n3 + x] = d.metr[((size_t)e * 9 + c) * n3 + x];
+  }
+  if (!GL) {
+    // this element's face states (U_master/U_slave of its own sides) and face metric rows, in face order
+    for (int t = threadIdx.x; t < EPB * 6 * n2; t += blockDim.x) {
+      const int es = t / (6 * n2), r = t - es * 6 * n2, lsi = r / n2, pq = r - lsi * n2;
+      const int e = e0 + es;
+      if (e >= d.nElems) continue;
+      const int ls = lsi + 1, p = pq % n, q = pq / n;
+      const int code = d.elemSide[e * 6 + lsi], sd = code >> 3, flip = code & 7;
+      int a, b;
+      side_to_vol2(N, p, q, flip, ls, a, b);
+      const double* src = (flip == 0 ? d.faceM : d.faceS) + (size_t)sd * FS_NF * n2 + pq;
+      const double rho = src[FS_RHO * n2], E = src[FS_E * n2], pr = src[FS_P * n2], sr = src[FS_SRHO * n2];
+      double* dst = sFS + (es * 6 + lsi) * FNF * n2;
+      const int o = a + n * b;
+      dst[o] = rho;
+      dst[n2 + o] = src[FS_U * n2];
+      dst[2 * n2 + o] = src[FS_V * n2];
+      dst[3 * n2 + o] = src[FS_W * n2];
+      dst[4 * n2 + o] = pi ? 4.0 * pr : pr;
+      dst[5 * n2 + o] = pi ? (E + pr) * sr : E + pr;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) dst[(6 + c) * n2 + o] = d.faceJa[(((size_t)e * 6 + lsi) * 3 + c) * n2 + o];
+    }
+  }
+  __syncthreads();
+  // two-point flux G (unscaled; density factor f0, others f1) between state a and state b with metric sum ms
+  auto two_point = [pi](double ra, double ua, double va, double wa, double pa, double ha, double rb, double ub, double vb, double wb,
+                        double pb, double hb, double ms0, double ms1, double ms2, double* G) {
+    if (pi) {
+      const double rs = ra + rb, us = ua + ub, vs = va + vb, ws = wa + wb, ps4 = pa + pb, hs = ha + hb;
+      const double qs = us * ms0 + vs * ms1 + ws * ms2;
+      const double A = rs * qs;
+      G[0] = A;
+      G[1] = fma(A, us, ps4 * ms0);
+      G[2] = fma(A, vs, ps4 * ms1);
+      G[3] = fma(A, ws, ps4 * ms2);
+      G[4] = A * hs;
+    } else {
+      const double qa = ua * ms0 + va * ms1 + wa * ms2, qb = ub * ms0 + vb * ms1 + wb * ms2;
+      const double mqa = ra * qa, mqb = rb * qb;
+      G[0] = mqa + mqb;
+      G[1] = fma(mqa, ua, mqb * ub) + (pa + pb) * ms0;
+      G[2] = fma(mqa, va, mqb * vb) + (pa + pb) * ms1;
+      G[3] = fma(mqa, wa, mqb * wb) + (pa + pb) * ms2;
+      G[4] = fma(ha, qa, hb * qb);
+    }
+  };
+  const int lane = threadIdx.x & 31;
+  const int seg = lane / n, a = lane - seg * n, segBase = seg * n;
+#pragma unroll 1
+  for (int dir = 0; dir < 3; ++dir) {
+    if (threadIdx.x < SS::LINE_THREADS) {  // whole warps
+      const int line = (threadIdx.x >> 5) * SEG + seg;
+      const bool valid = seg < SEG && line < SS::LINES;
+      const int lineC = valid ? line : 0;  // idle lanes compute on line 0 and store nothing
+      const int es = lineC / n2, lr = lineC - es * n2, c1 = lr % n, c2 = lr / n;
+      const bool store = valid && e0 + es < d.nElems;
+      const int stride = dir == 0 ? 1 : (dir == 1 ? n : n2);
+      const int xline = dir == 0 ? n * (c1 + n * c2) : (dir == 1 ? c1 + n2 * c2 : c1 + n * c2);
+      const int xa = xline + a * stride;
+      const double* Q = sR + es * 15 * n3;
+      const double* Mm = Q + (6 + 3 * dir) * n3;
+      const double ra = Q[xa], ua = Q[n3 + xa], va = Q[2 * n3 + xa], wa = Q[3 * n3 + xa], pa = Q[4 * n3 + xa], ha = Q[5 * n3 + xa];
+      const double ma0 = Mm[xa], ma1 = Mm[n3 + xa], ma2 = Mm[2 * n3 + xa];
+      double acc[5];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) acc[v] = (dir == 0) ? 0. : sA[(es * 5 + v) * n3 + xa];
+#pragma unroll
+      for (int dd = 1; dd <= n / 2; ++dd) {
+        const int bI = a + dd < n ? a + dd : a + dd - n;
+        const int xb = xline + bI * stride;
+        double G[5];
+        two_point(ra, ua, va, wa, pa, ha, Q[xb], Q[n3 + xb], Q[2 * n3 + xb], Q[3 * n3 + xb], Q[4 * n3 + xb], Q[5 * n3 + xb],
+                  ma0 + Mm[xb], ma1 + Mm[n3 + xb], ma2 + Mm[2 * n3 + xb], G);
+        const double o0 = sC[bI * n + a], o1 = sC[n2 + bI * n + a];
+        acc[0] = fma(o0, G[0], acc[0]);
+#pragma unroll
+        for (int v = 1; v < 5; ++v) acc[v] = fma(o1, G[v], acc[v]);
+        if (2 * dd != n) {
+          // receive the flux of the pair (a-dd, a) from lane a-dd of this segment
+          const int aS = a - dd >= 0 ? a - dd : a - dd + n;
+          const int src = valid ? segBase + aS : lane;
+          const double r0 = sC[aS * n + a], r1 = sC[n2 + aS * n + a];
+          acc[0] = fma(r0, __shfl_sync(0xffffffffu, G[0], src), acc[0]);
+#pragma unroll
+          for (int v = 1; v < 5; ++v) acc[v] = fma(r1, __shfl_sync(0xffffffffu, G[v], src), acc[v]);
+        }
+      }
+      if (!GL) {
+        const int fo = c1 + n * c2;  // face coordinate of this line on both end faces
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+          const int ls = side == 0 ? (dir == 0 ? XI_MINUS : (dir == 1 ? ETA_MINUS : ZETA_MINUS))
+                                   : (dir == 0 ? XI_PLUS : (dir == 1 ? ETA_PLUS : ZETA_PLUS));
+          const double* F = sFS + (es * 6 + ls - 1) * FNF * n2 + fo;
+          double G[5];
+          two_point(ra, ua, va, wa, pa, ha, F[0], F[n2], F[2 * n2], F[3 * n2], F[4 * n2], F[5 * n2], ma0 + F[6 * n2], ma1 + F[7 * n2],
+                    ma2 + F[8 * n2], G);
+          const double leg = side == 0 ? Bs.Lm(a) : Bs.Lp(a);
+          // -1/2 NormalSign LegHat(a): NormalSign = -1 on the minus, +1 on the plus side
+          const double cs = side == 0 ? 0.5 * Bs.LhM(a) : -0.5 * Bs.LhP(a);
+#pragma unroll
+          for (int v = 0; v < 5; ++v) {
+            const double gl = G[v] * leg;
+            double sum = 0.;
+#pragma unroll
+            for (int m = 0; m < n; ++m) sum += __shfl_sync(0xffffffffu, gl, valid ? segBase + m : lane);
+            acc[v] = fma(cs * (v == 0 ? f0 : f1), sum - G[v], acc[v]);
+          }
+        }
+      }
+      if (store) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) sA[(es * 5 + v) * n3 + xa] = acc[v];
+      }
+    }
+    __syncthreads();
+  }
+  // viscous fluxes (weak form): transformed fluxes of this node from the metrics still in sR, written over
+  // sR once every thread has finished reading it
+  const int t = threadIdx.x;
+  const bool hasNode = t < EPB * n3;
+  const int es = hasNode ? t / n3 : 0, x = t - es * n3, e = e0 + es;
+  const bool live = hasNode && e < d.nElems;
+  {
+    double Fv[12];
+    if (live) {
+      const double* Q = sR + es * 15 * n3;
+      const double vx = Q[n3 + x], vy = Q[2 * n3 + x], vz = Q[3 * n3 + x];
+      double m[9], g[12];
+#pragma unroll
+      for (int c = 0; c < 9; ++c) m[c] = Q[(6 + c) * n3 + x];
+#pragma unroll
+      for (int c = 0; c < 12; ++c) g[c] = d.grad[((size_t)e * 12 + c) * n3 + x];
+      const double mu = elem_mu(d, e);
+      const double lam = mu * B.lambdaFac;
+#pragma unroll
+      for (int dd = 0; dd < 3; ++dd) {
+        double F[5];
+        visc_flux_dir(mu, lam, vx, vy, vz, g, m[3 * dd], m[3 * dd + 1], m[3 * dd + 2], F);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) Fv[4 * dd + v] = F[1 + v];
+      }
+    }
+    __syncthreads();
+    if (live) {
+#pragma unroll
+      for (int c = 0; c < 12; ++c) sR[(es * 15 + c) * n3 + x] = Fv[c];
+    }
+  }
+  __syncthreads();
+  if (!live) return;
+  const int i = x % n, j = (x / n) % n, k = x / n2;
+  double ut[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) ut[v] = sA[(es * 5 + v) * n3 + x];
+  const double* V = sR + es * 15 * n3;
+#pragma unroll
+  for (int l = 0; l < n; ++l) {
+    const double ci = Bs.DhT(l, i), cj = Bs.DhT(l, j), ck = Bs.DhT(l, k);
+    const int xi = l + n * (j + n * k), xj = i + n * (l + n * k), xk = i + n * (j + n * l);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      ut[1 + v] = fma(ci, V[v * n3 + xi], ut[1 + v]);
+      ut[1 + v] = fma(cj, V[(4 + v) * n3 + xj], ut[1 + v]);
+      ut[1 + v] = fma(ck, V[(8 + v) * n3 + xk], ut[1 + v]);
+    }
+  }
+  finish_node<n, GL>(d, Bs, st, sFl, es, e, x, ut);
 }
 
 // =====================================================================================================

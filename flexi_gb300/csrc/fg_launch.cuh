@@ -13,7 +13,7 @@ struct KernelSet {
   void (*lift)(const Dev&, const Basis&, cudaStream_t) = nullptr;
   void (*flux)(const Dev&, const Basis&, cudaStream_t) = nullptr;
   void (*vol_weak)(const Dev&, const Basis&, int, double, double, cudaStream_t) = nullptr;
-  void (*vol_split)(const Dev&, const Basis&, int, double, double, cudaStream_t) = nullptr;  // null if unsupported
+  void (*vol_split)(const Dev&, const Basis&, int, double, double, cudaStream_t) = nullptr;
   void (*dt)(const Dev&, const Basis&, const double*, const double*, double, double, double*, const double*, cudaStream_t) = nullptr;
   // adjoint (vector-Jacobian product) of the right-hand side; vol_adj is null where unsupported
   void (*vol_adj)(const Dev&, const AdjDev&, const Basis&, cudaStream_t) = nullptr;

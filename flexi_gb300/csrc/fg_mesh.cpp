@@ -199,6 +199,7 @@ void build_from_raw(const RawMesh& R, int N, int nodeType, HostMesh& M) {
   M.sJ.assign((size_t)nE * n3, 0.);
   M.elemX.assign((size_t)nE * 3 * n3, 0.);
   M.geo.assign((size_t)M.nSides * 10 * n2, 0.);
+  M.faceJa.assign((size_t)nE * 6 * 3 * n2, 0.);
   std::string err;
 #pragma omp parallel
   {
@@ -258,15 +259,19 @@ void build_from_raw(const RawMesh& R, int N, int nodeType, HostMesh& M) {
         }
       }
       tensor3(V_CLN_N, Ja.data(), &M.metr[(size_t)e * 9 * n3], 9);
-      // surface metrics of the sides this element is master of (metrics.f90:CalcSurfMetrics/SurfMetricsFromJa)
+      // surface metrics (metrics.f90:CalcSurfMetrics/SurfMetricsFromJa): the normal row of every side of the
+      // element (Ja_Face / Ja_slave), the normal vectors and surface elements of the sides it is master of
       for (int ls = 1; ls <= 6; ++ls) {
         const int code = M.elemSide[e * 6 + ls - 1];
-        if ((code & 7) != 0) continue;
         const int s = code >> 3;
         const int lf = minus_side(ls) ? 0 : N;
         const int nd = kNormalDir[ls], td = kTangDir[ls];
         // Ja rows nd and td on the face (CL points), interpolated to the solution nodes
         for (int row = 0; row < 2; ++row) {
+          if (row == 1) {
+            std::copy(tmp3.begin(), tmp3.end(), M.faceJa.begin() + ((size_t)e * 6 + ls - 1) * 3 * n2);
+            if ((code & 7) != 0) break;
+          }
           const int mrow = row == 0 ? nd : td;
           for (int c = 0; c < 3; ++c)
             for (int b = 0; b < n; ++b) for (int a = 0; a < n; ++a) {
@@ -276,6 +281,7 @@ void build_from_raw(const RawMesh& R, int N, int nodeType, HostMesh& M) {
             }
           tensor2(V_CLN_N, tmp2.data(), row == 0 ? tmp3.data() : ja_out.data(), 3);
         }
+        if ((code & 7) != 0) continue;
         for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
           int a, b;
           s2v2(N, p, q, 0, ls, a, b);
@@ -357,6 +363,31 @@ void build_from_flexi(int N, int nodeType, int nElems, int nSides, int nBCSides,
       for (int c = 0; c < 3; ++c) { G[c * n2] = NormVec[g * 3 + c]; G[(3 + c) * n2] = TangVec1[g * 3 + c]; G[(6 + c) * n2] = TangVec2[g * 3 + c]; }
       G[9 * n2] = SurfElem[g];
     }
+  // face metrics of every element side: the normal-direction volume metrics evaluated at the face (GL: the
+  // face node; Gauss: interpolated with L(-1) / L(+1)); equal to FLEXI's Ja_Face / Ja_slave up to round-off
+  // (fg_set_face_metrics can hand over FLEXI's own arrays instead)
+  {
+    Vec x, w;
+    nodes(N, nodeType, x, w);
+    const Vec wb = bary_weights(x);
+    const Vec Lm = lagrange_at(-1.0, x, wb), Lp = lagrange_at(1.0, x, wb);
+    M.faceJa.assign((size_t)nElems * 6 * 3 * n2, 0.);
+    for (int e = 0; e < nElems; ++e)
+      for (int ls = 1; ls <= 6; ++ls) {
+        const int nd = kNormalDir[ls];
+        const Vec& L = minus_side(ls) ? Lm : Lp;
+        for (int c = 0; c < 3; ++c)
+          for (int b = 0; b < n; ++b) for (int a = 0; a < n; ++a) {
+            double acc = 0.;
+            for (int l = 0; l < n; ++l) {
+              int i, j, k;
+              face_ijk(ls, a, b, l, i, j, k);
+              acc += L[l] * M.metr[((size_t)e * 9 + 3 * nd + c) * n3 + i + n * (j + n * k)];
+            }
+            M.faceJa[(((size_t)e * 6 + ls - 1) * 3 + c) * n2 + b * n + a] = acc;
+          }
+      }
+  }
   M.elemX.clear();
 }
 

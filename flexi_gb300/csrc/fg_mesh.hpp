@@ -4,6 +4,7 @@
 //   metr [e][9][n3]  Metrics_fTilde(3), Metrics_gTilde(3), Metrics_hTilde(3) per volume node
 //   sJ   [e][n3]     inverse Jacobian
 //   geo  [s][10][n2] NormVec(3), TangVec1(3), TangVec2(3), SurfElem per side point (master orientation)
+//   faceJa [e][6][3][n2] normal-direction row of each element's own face metrics (split form, Gauss nodes)
 // Two entry points: from raw element node coordinates and element connectivity (the content of a HOPR
 // mesh file: NodeCoords on equidistant NGeo points, neighbour ids), or from the arrays FLEXI itself has
 // built (the drop-in path, where FLEXI keeps doing its own InitMesh and hands the result over).
@@ -32,6 +33,10 @@ struct HostMesh {
   std::vector<int> bcType;      // [nBCSides]
   std::vector<double> bcTwall;  // [nBCSides]
   std::vector<double> metr, sJ, geo;
+  // [e][6][3][n2]: row NormalDir of the element's own face metrics on each of its sides (Ja_Face for the
+  // master, Ja_slave for the slave side, metrics.f90:CalcSurfMetrics), indexed by the element's face
+  // coordinates (a + n*b); used by the split form on Gauss nodes
+  std::vector<double> faceJa;
   std::vector<double> elemX;    // [e][3][n3] solution point coordinates (Elem_xGP)
   std::vector<double> wVol;     // [n3] tensor-product quadrature weights
   std::vector<double> metAdv, metVisc;  // [e][3][n3] calctimestep.f90:InitCalctimestep

@@ -124,6 +124,13 @@ class Flexi:
                                        *[_p(x) for x in a]), "fg_set_mesh")
         self._sizes()
 
+    def set_face_metrics(self, Ja_Face, Ja_slave):
+        """Drop-in path, split form on Gauss nodes: FLEXI's Ja_Face / Ja_slave (nSides, 0:N, 0:N, 3, 3) in C
+        order of the Fortran (3,3,0:N,0:N,nSides) arrays."""
+        a = np.ascontiguousarray(Ja_Face, np.float64)
+        b = np.ascontiguousarray(Ja_slave, np.float64)
+        self._check(self.L.fg_set_face_metrics(self.h, _p(a), _p(b)), "fg_set_face_metrics")
+
     def _sizes(self):
         s = np.zeros(5, np.int32)
         self._check(self.L.fg_get_sizes(self.h, _p(s)), "fg_get_sizes")

@@ -104,6 +104,12 @@ int fg_set_mesh(fg_handle* h, int nElems, int nSides, int nBCSides, const int* S
                 const double* Metrics_gTilde, const double* Metrics_hTilde, const double* sJ, const double* NormVec,
                 const double* TangVec1, const double* TangVec2, const double* SurfElem);
 
+/* Face metrics of the split form on Gauss nodes, FLEXI's Ja_Face(3,3,0:N,0:N,nSides) and
+ * Ja_slave(3,3,0:N,0:N,nSides) (MOD_Mesh_Vars, filled by metrics.f90:CalcSurfMetrics; used by
+ * surfint.t90:90-140). Optional after fg_set_mesh, which otherwise evaluates the normal-direction volume
+ * metrics at the faces (identical up to round-off). Only row NormalDir of each side is read. */
+int fg_set_face_metrics(fg_handle* h, const double* Ja_Face, const double* Ja_slave);
+
 /* Per-instance viscosity (ensembles); default: cfg.mu0 for every instance. */
 int fg_set_instance_mu0(fg_handle* h, int nInst, const double* mu0);
 

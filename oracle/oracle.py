@@ -193,7 +193,7 @@ class Oracle:
         lib().orc_set_bulk_velocity(self.h, v)
 
     _MESH_ARRAYS = {"Mf": 0, "Mg": 1, "Mh": 2, "sJ": 3, "NormVec": 4, "TangVec1": 5, "TangVec2": 6, "SurfElem": 7,
-                    "Face_xGP": 8, "Elem_xGP": 9, "wGPVol": 10}
+                    "Face_xGP": 8, "Elem_xGP": 9, "wGPVol": 10, "JaN_master": 12, "JaN_slave": 13}
 
     def mesh_array(self, name):
         w = self._MESH_ARRAYS[name]
@@ -204,7 +204,8 @@ class Oracle:
         shapes = {"Mf": (self.n_elems, n, n, n, 3), "Mg": (self.n_elems, n, n, n, 3), "Mh": (self.n_elems, n, n, n, 3),
                   "sJ": (self.n_elems, n, n, n), "NormVec": (self.n_sides, n, n, 3), "TangVec1": (self.n_sides, n, n, 3),
                   "TangVec2": (self.n_sides, n, n, 3), "SurfElem": (self.n_sides, n, n), "Face_xGP": (self.n_sides, n, n, 3),
-                  "Elem_xGP": (self.n_elems, n, n, n, 3), "wGPVol": (n, n, n)}
+                  "Elem_xGP": (self.n_elems, n, n, n, 3), "wGPVol": (n, n, n), "JaN_master": (self.n_sides, n, n, 3),
+                  "JaN_slave": (self.n_sides, n, n, 3)}
         return out.reshape(shapes[name])
 
     def volume(self):

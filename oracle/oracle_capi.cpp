@@ -196,6 +196,7 @@ long long orc_mesh_array(void* hp, int which, double* out) {
     case 4: a = &M.NormVec; break; case 5: a = &M.TangVec1; break; case 6: a = &M.TangVec2; break;
     case 7: a = &M.SurfElem; break; case 8: a = &M.Face_xGP; break; case 9: a = &M.Elem_xGP; break;
     case 10: a = &M.wGPVol; break;
+    case 12: a = &M.JaN_master; break; case 13: a = &M.JaN_slave; break;
     case 11: if (out) out[0] = M.Vol; return 1;
     default: return -1;
   }

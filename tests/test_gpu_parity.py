@@ -38,6 +38,21 @@ RHS_CASES = {
     "gl7_split_sd_roe": dict(N=7, NodeType="gauss-lobatto", SplitDG="sd", Riemann="roe"),
     "gl3_split_pi_lf": dict(N=3, NodeType="gauss-lobatto", SplitDG="pi", Riemann="lf"),
     "gl1_split_pi": dict(N=1, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roe"),
+    # split forms on Gauss-Lobatto lines of 3, 5, 6, 7 nodes (k_vol_split_gen)
+    "gl2_split_pi_roe": dict(N=2, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roe"),
+    "gl4_split_sd_lf": dict(N=4, NodeType="gauss-lobatto", SplitDG="sd", Riemann="lf"),
+    "gl5_split_pi_roeef_br2": dict(N=5, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roeentropyfix", Lifting="br2"),
+    "gl6_split_pi_hllc": dict(N=6, NodeType="gauss-lobatto", SplitDG="pi", Riemann="hllc"),
+    # split forms on Gauss nodes: entropy-variable prolongation and the split-Gauss surface integral
+    "gauss5_split_pi_roeef_br1": dict(N=5, NodeType="gauss", SplitDG="pi", Riemann="roeentropyfix", Lifting="br1"),
+    "gauss5_split_pi_hllc_br2": dict(N=5, NodeType="gauss", SplitDG="pi", Riemann="hllc", Lifting="br2"),
+    "gauss3_split_pi_roe_br2": dict(N=3, NodeType="gauss", SplitDG="pi", Riemann="roe", Lifting="br2", etaBR2=2.5),
+    "gauss3_split_sd_lf": dict(N=3, NodeType="gauss", SplitDG="sd", Riemann="lf"),
+    "gauss1_split_pi": dict(N=1, NodeType="gauss", SplitDG="pi", Riemann="roe"),
+    "gauss2_split_pi_roeef": dict(N=2, NodeType="gauss", SplitDG="pi", Riemann="roeentropyfix"),
+    "gauss4_split_sd_roe": dict(N=4, NodeType="gauss", SplitDG="sd", Riemann="roe"),
+    "gauss6_split_pi_lf": dict(N=6, NodeType="gauss", SplitDG="pi", Riemann="lf"),
+    "gauss7_split_pi_roeef": dict(N=7, NodeType="gauss", SplitDG="pi", Riemann="roeentropyfix"),
 }
 COMMON = dict(kappa=1.4, R=71.42857, Pr=0.72, mu0=6.25e-4, CFLScale=0.9, DFLScale=0.9)
 
@@ -51,7 +66,8 @@ def test_rhs_parity_tgv(name):
     assert err <= UT_TOL, err
 
 
-@pytest.mark.parametrize("name", ["c1_gauss3_weak_roe_br1", "gl7_split_pi_roeef_br2", "gauss5_weak_roeef"])
+@pytest.mark.parametrize("name", ["c1_gauss3_weak_roe_br1", "gl7_split_pi_roeef_br2", "gauss5_weak_roeef", "gauss5_split_pi_roeef_br1",
+                                  "gauss3_split_sd_lf", "gl5_split_pi_roeef_br2"])
 def test_rhs_parity_curved(name):
     c = product_cfg(**RHS_CASES[name], **COMMON)
     f, o, _ = tgv_pair(c, n_elem=3, ngeo=3, perturb=0.2, seed=3)
@@ -60,9 +76,10 @@ def test_rhs_parity_curved(name):
     assert err <= UT_TOL, err
 
 
-@pytest.mark.parametrize("variant", ["split_pi_roe_br1", "split_pi_roeef_br2", "gauss3_weak_lf_br1"])
+@pytest.mark.parametrize("variant", ["split_pi_roe_br1", "split_pi_roeef_br2", "gauss3_weak_lf_br1", "gauss5_split_pi_roeef_br2"])
 def test_rhs_parity_channel_walls(variant):
     kw = {"split_pi_roe_br1": dict(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roe", Lifting="br1"),
+          "gauss5_split_pi_roeef_br2": dict(N=5, NodeType="gauss", SplitDG="pi", Riemann="roeentropyfix", Lifting="br2"),
           "split_pi_roeef_br2": dict(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roeentropyfix", Lifting="br2", etaBR2_wall=1.5),
           "gauss3_weak_lf_br1": dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="lf", Lifting="br1")}[variant]
     c = product_cfg(**kw, kappa=1.4, R=1.0, Pr=0.72, mu0=1.0 / 2800.0, doTCSource=1, dpdx=-1.0)
@@ -74,7 +91,7 @@ def test_rhs_parity_channel_walls(variant):
     assert err <= UT_TOL, err
 
 
-@pytest.mark.parametrize("name", ["c1_gauss3_weak_roe_br1", "gl7_split_pi_roeef_br1", "gauss3_weak_br2"])
+@pytest.mark.parametrize("name", ["c1_gauss3_weak_roe_br1", "gl7_split_pi_roeef_br1", "gauss3_weak_br2", "gauss5_split_pi_roeef_br1"])
 def test_lserk_steps_fixed_dt(name):
     c = product_cfg(**RHS_CASES[name], **COMMON)
     f, o, _ = tgv_pair(c, n_elem=3)
@@ -178,3 +195,38 @@ def test_ensemble_matches_separate_instances():
         assert abs(t[i] - to) <= 1e-12 * to
         assert rel_err(Uf[off:off + m.n_elems], o.get_state()) <= STATE_TOL
         off += m.n_elems
+
+
+# 0-based row NormalDir of each local side 1..6 (mesh_vars.f90:105-111)
+_NORMAL_DIR = {1: 2, 2: 1, 3: 0, 4: 1, 5: 0, 6: 2}
+
+
+@pytest.mark.parametrize("face_metrics", [False, True])
+def test_dropin_gauss_split_face_metrics(face_metrics):
+    """Drop-in path for the split form on Gauss nodes: fg_set_mesh alone (face metrics evaluated from the
+    volume metrics) and with FLEXI's Ja_Face / Ja_slave handed over by fg_set_face_metrics (here the
+    oracle's; the rows other than NormalDir are NaN, so reading one would show)."""
+    c = product_cfg(**RHS_CASES["gauss5_split_pi_roeef_br1"], **COMMON)
+    m = fmesh.tgv_box(3, ngeo=3, perturb=0.2, seed=6)
+    o = orc.Oracle(__import__("_cases").oracle_cfg(c), m)
+    f = Flexi(c)
+    s2e = o.mesh_iarray("SideToElem")
+    f.set_mesh(s2e, o.mesh_iarray("ElemToSide"), o.mesh_iarray("BC"), m.boundary_type, m.ref_state_prim,
+               o.mesh_array("Mf"), o.mesh_array("Mg"), o.mesh_array("Mh"), o.mesh_array("sJ"), o.mesh_array("NormVec"),
+               o.mesh_array("TangVec1"), o.mesh_array("TangVec2"), o.mesh_array("SurfElem"))
+    if face_metrics:
+        jm, js = o.mesh_array("JaN_master"), o.mesh_array("JaN_slave")
+        n_s, n = jm.shape[0], jm.shape[1]
+        JaF = np.full((n_s, n, n, 3, 3), np.nan)
+        JaS = np.full((n_s, n, n, 3, 3), np.nan)
+        for s_ in range(n_s):
+            JaF[s_, :, :, :, _NORMAL_DIR[int(s2e[s_, 2])]] = jm[s_]
+            if s2e[s_, 1] > 0:
+                JaS[s_, :, :, :, _NORMAL_DIR[int(s2e[s_, 3])]] = js[s_]
+        f.set_face_metrics(JaF, JaS)
+    U0 = __import__("_cases").perturb_state(testcases.tgv_state(o.mesh_array("Elem_xGP"), kappa=c.kappa, R=c.R), seed=8)
+    f.U = U0
+    o.set_state(U0)
+    err = rel_err(f.DGTimeDerivative_weakForm(0.0), o.time_derivative(0.0))
+    f.close()
+    assert err <= UT_TOL, err

@@ -1,9 +1,10 @@
-"""FLEXI's Taylor-Green regression test run on the GPU path: regressioncheck/checks/tgv/split
-(8^3 periodic box, N=7 Gauss-Lobatto, split PI, RoeEntropyFix, BR1, Re=1600, Ma=0.1, CFL=DFL=0.8,
-tEnd=13). The reference writes the 15 TGVAnalysis columns every 10 time steps and compares them at
-1e-4 relative (analyze.ini); here every row up to tEnd is compared, including the time column that
-results from the CALCTIMESTEP-controlled time steps. The analysis integrals are evaluated by the oracle
-from the GPU state and the GPU's lifted gradients of the last stage, as AnalyzeTestcase does."""
+"""FLEXI's Taylor-Green regression tests run on the GPU path: regressioncheck/checks/tgv/split (8^3
+periodic box, N=7 Gauss-Lobatto, split PI) and tgv/splitGauss (N=5 Gauss, split PI with entropy-variable
+prolongation and the split-Gauss surface integral), both RoeEntropyFix, BR1, Re=1600, Ma=0.1,
+CFL=DFL=0.8, tEnd=13. The reference writes the 15 TGVAnalysis columns every 10 time steps and compares
+them at 1e-4 relative (analyze.ini); here every row up to tEnd is compared, including the time column
+that results from the CALCTIMESTEP-controlled time steps. The analysis integrals are evaluated by the
+oracle from the GPU state and the GPU's lifted gradients of the last stage, as AnalyzeTestcase does."""
 import numpy as np
 import pytest
 
@@ -13,11 +14,15 @@ from oracle import oracle as orc
 
 pytestmark = pytest.mark.gpu
 
+CASES = {"split": ("tgv_reference", 7, "gauss-lobatto", orc.NT_GL), "splitGauss": ("tgv_splitgauss_reference", 5, "gauss", orc.NT_GAUSS)}
+
 
 @pytest.mark.timeout(1200)
-def test_tgv_split_regression_all_rows(tgv_reference):
-    _, rows = tgv_reference
-    c = make_config(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roeentropyfix", Lifting="br1", kappa=1.4, R=71.42857,
+@pytest.mark.parametrize("case", list(CASES))
+def test_tgv_split_regression_all_rows(case, request):
+    fixture, N, node_type, nt = CASES[case]
+    _, rows = request.getfixturevalue(fixture)
+    c = make_config(N=N, NodeType=node_type, SplitDG="pi", Riemann="roeentropyfix", Lifting="br1", kappa=1.4, R=71.42857,
                     Pr=0.72, mu0=6.25e-4, CFLScale=0.8, DFLScale=0.8)
     m = fmesh.tgv_box(8, ngeo=1)
     f = Flexi(c, m)
@@ -32,7 +37,7 @@ def test_tgv_split_regression_all_rows(tgv_reference):
         if r > 0:
             t = f.TimeDisc(10)[0]
             assert abs(t - rows[r, 0]) <= 1e-4 * rows[r, 0], (r, t, rows[r, 0])
-        a = orc.tgv_analysis(7, orc.NT_GL, sJ, f.U, f.gradients(), 10, 1.4, 71.42857, 6.25e-4)
+        a = orc.tgv_analysis(N, nt, sJ, f.U, f.gradients(), 10, 1.4, 71.42857, 6.25e-4)
         ref = rows[r, 1:]
         for col in range(15):
             if abs(ref[col]) > 1e-9 * scale[col]:
@@ -44,4 +49,4 @@ def test_tgv_split_regression_all_rows(tgv_reference):
                 worst = max(worst, rel if tol == 1e-4 else 0.0)
                 assert rel <= tol, (r, col, a[col], ref[col])
     f.close()
-    print(f"TGV regression: {n_rows} rows, worst relative deviation {worst:.2e}")
+    print(f"TGV regression {case}: {n_rows} rows, worst relative deviation {worst:.2e}")

@@ -39,7 +39,7 @@ def test_config_defaults_and_validation(lib):
     with pytest.raises(FlexiError):
         Flexi(make_config(N=12))
     with pytest.raises(FlexiError):
-        Flexi(make_config(N=5, NodeType="gauss", SplitDG="pi"))  # split form needs Gauss-Lobatto nodes
+        Flexi(make_config(N=5, SplitDG=2))  # split fluxes other than SD (0) and PI (4)
     with pytest.raises(FlexiError):
         Flexi(make_config(N=3, doConservativeLifting=1))
 
