@@ -12,6 +12,9 @@ value  : DOF*stage/s on the device, inputs resident in HBM, K steps bracketed by
          solver's stream (barrier + synchronize on both sides, max over ranks).
 e2e    : the same metric through the public C ABI with the state in pinned host memory: each step
          uploads U (fg_set_state), advances one step (fg_run), downloads U (fg_get_state).
+--workload tgv-splitgauss : the discretisation of the reference's tgv/splitGauss regression (N=5 Gauss, split
+         PI with entropy-variable prolongation and the split-Gauss surface integral, BR1, RoeEntropyFix) on a
+         curved 40^3 mesh (13.8 M DOF), same metric and timing.
 --impl reference : the CPU implementation of the path (the C++ restatement of FLEXI's Fortran solver,
          FLEXI itself cannot be built here: Fortran/MPI/HDF5) on all host threads, bounded sample per step.
 Multi-GPU: the path does not shard on this setup (no halo exchange is built); N ranks run N replicas.
@@ -38,7 +41,15 @@ RIEMANN_IDS = {"hllc": 2, "roeentropyfix": 33}
 RIEMANN_NAMES = {"hllc": "HLLC", "roeentropyfix": "RoeEntropyFix"}
 
 
-def flops_per_dof_stage(riemann):
+# the Gauss split form (N=5, split PI with entropy-variable prolongation and the split-Gauss surface
+# integral, BR1, RoeEntropyFix: the discretisation of the reference's tgv/splitGauss regression)
+SPLITGAUSS_METRIC = "FP64 DOF*stage/s (N=5 TGV, Gauss split form)"
+SPLITGAUSS_FLOPS_PER_DOF_STAGE = {"prep": 128.0, "lift": 500.0, "flux": 194.0, "vol": 1750.5}
+
+
+def flops_per_dof_stage(riemann, kind="tgv"):
+    if kind == "tgv-splitgauss":
+        return dict(SPLITGAUSS_FLOPS_PER_DOF_STAGE)
     return dict(FLOPS_PER_DOF_STAGE, flux=FLUX_FLOPS_PER_DOF_STAGE[riemann])
 # compulsory HBM traffic per DOF and stage: U read+write, Ut_tmp read+write, 9 metric terms + sJ
 BYTES_ALG_PER_DOF_STAGE = 240.0
@@ -50,36 +61,65 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--elems", type=int, default=32, help="elements per direction")
+    p.add_argument("--elems", type=int, default=None, help="elements per direction (tgv: 32, tgv-splitgauss: 40)")
     p.add_argument("--riemann", default="hllc", choices=sorted(RIEMANN_IDS), help="surface Riemann solver")
-    p.add_argument("--workload", default="tgv", choices=["tgv", "ensemble", "adjoint", "adjoint-channel"],
-                   help="tgv: the single-case N=7 TGV; ensemble: 256 independent TGV/vortex instances at N=5 against a loop over "
+    p.add_argument("--workload", default="tgv", choices=["tgv", "tgv-splitgauss", "ensemble", "adjoint", "adjoint-channel"],
+                   help="tgv: the single-case N=7 TGV; tgv-splitgauss: the N=5 Gauss split form of the reference's tgv/splitGauss "
+                        "regression on a curved 40^3 mesh; ensemble: 256 independent TGV/vortex instances at N=5 against a loop over "
                         "instances; adjoint: gradient of a kinetic-energy loss over a 200-step TGV solve (16^3, N=5)")
     p.add_argument("--ckpt", type=int, default=20, help="adjoint: checkpoint interval in steps")
     p.add_argument("--fd-dirs", type=int, default=20, help="adjoint: random directions of the finite-difference check")
     p.add_argument("--instances", type=int, default=256, help="ensemble size")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline leg (profiling runs)")
-    return p.parse_args()
+    a = p.parse_args()
+    if a.elems is None:
+        a.elems = 40 if a.workload == "tgv-splitgauss" else 32
+    if a.workload == "tgv-splitgauss":
+        a.riemann = "roeentropyfix"
+    return a
 
 
-def workload_config(n, riemann):
+def workload_config(n, riemann, kind="tgv"):
+    if kind == "tgv-splitgauss":
+        dof = n ** 3 * 216
+        return {"workload": f"TGV {n}^3 curved (perturbation 0.05, NGeo=3), N=5 Gauss, split PI with entropy-variable prolongation "
+                            f"and the split-Gauss surface integral, BR1, RoeEntropyFix, FP64",
+                "n_elems": n ** 3, "N": 5, "dof": dof, "Re": 1600, "Ma": 0.1, "CFLScale": 0.8, "DFLScale": 0.8,
+                "time_integration": "CarpenterRK4-5, 5 stages/step, CFL/DFL dt each step",
+                "l2": f"inputs larger than L2 (state {dof * 40 / 1e6:.0f} MB)", "parallelism": "replicas"}
     return {"workload": f"TGV {n}^3 curved (perturbation 0.05, NGeo=3), N=7 Gauss-Lobatto, split PI, BR2, {RIEMANN_NAMES[riemann]}, FP64",
             "n_elems": n ** 3, "N": 7, "dof": n ** 3 * 512, "Re": 1600, "Ma": 0.1, "CFLScale": 0.8, "DFLScale": 0.8,
             "time_integration": "CarpenterRK4-5, 5 stages/step, CFL/DFL dt each step",
             "l2": "inputs larger than L2 (state 671 MB at 32^3)", "parallelism": "replicas"}
 
 
-def solver_config(riemann):
+def solver_config(riemann, kind="tgv"):
     from flexi_gb300.solver import make_config
+    if kind == "tgv-splitgauss":
+        return make_config(N=5, NodeType="gauss", SplitDG="pi", Riemann="roeentropyfix", Lifting="br1", kappa=1.4, R=71.42857,
+                           Pr=0.72, mu0=6.25e-4, CFLScale=0.8, DFLScale=0.8)
     return make_config(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann=riemann, Lifting="br2", kappa=1.4, R=71.42857,
                        Pr=0.72, mu0=6.25e-4, CFLScale=0.8, DFLScale=0.8)
 
 
-def oracle_config(riemann):
+def oracle_config(riemann, kind="tgv"):
     """The same discretisation for the CPU restatement."""
+    if kind == "tgv-splitgauss":
+        return dict(N=5, nodeType=1, riemann=33, riemannBC=-1, lifting=1, weakLifting=0, consLifting=0, splitDG=4, etaBR2=2.0,
+                    etaBR2_wall=-1.0, kappa=1.4, R=71.42857, Pr=0.72, mu0=6.25e-4, CFLScale=0.8, DFLScale=0.8, doTCSource=0, dpdx=-1.0)
     return dict(N=7, nodeType=2, riemann=RIEMANN_IDS[riemann], riemannBC=-1, lifting=2, weakLifting=0, consLifting=0, splitDG=4, etaBR2=2.0,
                 etaBR2_wall=-1.0, kappa=1.4, R=71.42857, Pr=0.72, mu0=6.25e-4, CFLScale=0.8, DFLScale=0.8, doTCSource=0, dpdx=-1.0)
+
+
+def metric_name(kind):
+    return SPLITGAUSS_METRIC if kind == "tgv-splitgauss" else METRIC
+
+
+def kernel_names(kind):
+    if kind == "tgv-splitgauss":
+        return {"vol": "k_vol_split_gen<6,Gauss>", "lift": "k_lift<6,Gauss>", "flux": "k_flux<6>", "prep": "k_prep<6,Gauss>"}
+    return {"vol": "k_vol_split<8>", "lift": "k_lift<8,GL>", "flux": "k_flux<8>", "prep": "k_prep<8,GL>"}
 
 
 def dist_info():
@@ -145,25 +185,27 @@ def measured_peaks():
         return {}
 
 
-def ncu_traffic():
+def ncu_traffic(kind="tgv"):
+    """DRAM bytes per DOF of each kernel class from the committed ncu summary (key: workload)."""
     try:
-        return json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
+        t = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
     except Exception:
         return {}
+    return t.get(kind, {}) if kind != "tgv" else {k: v for k, v in t.items() if not isinstance(v, dict)}
 
 
-def cpu_baseline_sample(riemann, n_elems_dir=8, budget_s=12.0):
+def cpu_baseline_sample(riemann, n_elems_dir=8, budget_s=12.0, kind="tgv"):
     """Oracle (C++ restatement of FLEXI's operator) on all host threads: TGV sample of the same
     discretisation, timed RK steps until the budget is used. Returns (DOF*stage/s, threads, sample)."""
     import numpy as np
     from flexi_gb300 import mesh as fmesh, testcases
     from oracle import oracle as orc
     orc.set_threads(os.cpu_count() or 1)
-    cfg = oracle_config(riemann)
+    cfg = oracle_config(riemann, kind)
     m = fmesh.tgv_box(n_elems_dir, ngeo=3, perturb=0.05, seed=0)
     o = orc.Oracle(cfg, m)
     o.set_state(testcases.tgv_state(o.mesh_array("Elem_xGP"), mach=0.1, kappa=1.4, R=71.42857))
-    dof = m.n_elems * 512
+    dof = m.n_elems * (cfg["N"] + 1) ** 3
     t = 0.0
     dt, _ = o.calc_timestep()
     t = o.timestep(t, dt)  # warm-up
@@ -188,12 +230,12 @@ def run_reference(args):
     from oracle import oracle as orc
     threads = os.cpu_count() or 1
     orc.set_threads(threads)
-    cfg = oracle_config(args.riemann)
+    cfg = oracle_config(args.riemann, args.workload)
     ns = 6  # bounded sample: 6^3 elements of the same discretisation per step
     m = fmesh.tgv_box(ns, ngeo=3, perturb=0.05, seed=0)
     o = orc.Oracle(cfg, m)
     o.set_state(testcases.tgv_state(o.mesh_array("Elem_xGP"), mach=0.1, kappa=1.4, R=71.42857))
-    dof = m.n_elems * 512
+    dof = m.n_elems * (cfg["N"] + 1) ** 3
     t = 0.0
     for _ in range(args.warmup):
         dt, _ = o.calc_timestep()
@@ -205,9 +247,9 @@ def run_reference(args):
     el = time.perf_counter() - t0
     value = dof * 5 * args.steps / el
     sample = f"TGV {ns}^3 of the workload's discretisation ({dof} DOF) per step, {args.steps} RK steps, {el:.2f} s"
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+    line = {"impl": "reference", "metric": metric_name(args.workload), "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(args.elems, args.riemann),
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(args.elems, args.riemann, args.workload),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "C++ restatement of FLEXI's Fortran path (FLEXI needs Fortran, MPI and HDF5, absent here)"}
@@ -229,8 +271,9 @@ def run_gb300(args):
     from flexi_gb300.solver import Flexi, probe_fp64_tflops
 
     n = args.elems
-    cfgd = workload_config(n, args.riemann)
-    c = solver_config(args.riemann)
+    kind = args.workload
+    cfgd = workload_config(n, args.riemann, kind)
+    c = solver_config(args.riemann, kind)
     m = fmesh.tgv_box(n, ngeo=3, perturb=0.05, seed=rank)
     f = Flexi(c, m)
     U0 = testcases.tgv_state(f.elem_xgp(), mach=0.1, kappa=1.4, R=71.42857)
@@ -298,11 +341,11 @@ def run_gb300(args):
     dom = max(("prep", "lift", "flux", "vol"), key=lambda k: prof[k][0])
     dom_ms, dom_cnt = prof[dom]
     avg_ms = dom_ms / max(dom_cnt, 1)
-    flops = flops_per_dof_stage(args.riemann)
+    flops = flops_per_dof_stage(args.riemann, kind)
     achieved = flops[dom] * dof / (avg_ms * 1e-3) / 1e12
     peaks = measured_peaks()
-    traffic = ncu_traffic().get(dom)
-    roofline = {"bound": "fp64", "kernel": {"vol": "k_vol_split<8>", "lift": "k_lift<8,GL>", "flux": "k_flux<8>", "prep": "k_prep<8,GL>"}[dom],
+    traffic = ncu_traffic(kind).get(dom)
+    roofline = {"bound": "fp64", "kernel": kernel_names(kind)[dom],
                 "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved / fp64_peak,
                 "peak_source": "own DFMA probe (fg_probe_fp64), MEASURED_PEAKS.json has no FP64 figure",
                 "traffic": (traffic * dof if traffic is not None else None),
@@ -315,16 +358,16 @@ def run_gb300(args):
     try:
         if args.no_cpu_baseline:
             raise RuntimeError("skipped (--no-cpu-baseline)")
-        cpu_val, cores, sample = cpu_baseline_sample(args.riemann)
+        cpu_val, cores, sample = cpu_baseline_sample(args.riemann, kind=kind)
         cpu = {"value": cpu_val, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
     except Exception as ex:  # reported, never substituted for the GPU path
         cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port", "sample": f"failed: {ex}"}
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+    line = {"metric": metric_name(kind), "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": cfgd, "e2e": e2e, "gpu_launches": launches_per_step * args.steps, "clocks": clk,
             "roofline": roofline, "cpu_baseline": cpu}
     f.close()
-    if args.riemann == "hllc":
+    if args.riemann == "hllc" and kind == "tgv":
         # the same workload with the surface flux of the reference's split-form TGV regression (the parity setting)
         c2 = solver_config("roeentropyfix")
         g = Flexi(c2, m)

@@ -35,7 +35,7 @@ struct Basis {
   double Lm[FG_MAXN], Lp[FG_MAXN], LhM[FG_MAXN], LhP[FG_MAXN];
   double kappa, kappaM1, sKappaM1, Rgas, sR, lambdaFac, etaBR2, etaBR2_wall;
   double kappaFac, sKappaP1;
-  double kappaM1_sKappaM1, kappa_kappaM1;  // (kappa-1)^(1/(kappa-1)), kappa/(kappa-1): eos.f90:EntropyToCons
+  double logEntC, kappa_kappaM1;  // ln((kappa-1)^(1/(kappa-1))), kappa/(kappa-1): eos.f90:EntropyToCons
 };
 
 // Device arrays of one solver handle (all sizes in units of doubles / ints).

@@ -361,7 +361,7 @@ void init_basis(fg_handle* h) {
   B.etaBR2 = c.etaBR2; B.etaBR2_wall = (c.etaBR2_wall == -1.) ? c.etaBR2 : c.etaBR2_wall;
   B.kappaFac = 2. * c.kappa / (c.kappa - 1.);
   B.sKappaP1 = 1. / (c.kappa + 1.);
-  B.kappaM1_sKappaM1 = std::pow(c.kappa - 1., 1. / (c.kappa - 1.));
+  B.logEntC = std::log(c.kappa - 1.) / (c.kappa - 1.);
   B.kappa_kappaM1 = c.kappa / (c.kappa - 1.);
   // Carpenter-Kennedy RK4-5, timedisc_vars.f90:199-214
   double* A = h->RKA; double* b = h->RKb; double* cc = h->RKc;

@@ -20,7 +20,8 @@ struct Inst {
   static constexpr bool SPLIT_POW2 = GL && (n == 2 || n == 4 || n == 8);
   static size_t smem_split_gen() {
     using SS = SplitShape<n>;
-    return sizeof(double) * (SBasis<n>::SIZE + 2 * S::n2 + S::EPB * (20 * S::n3 + 6 * S::n2 * 5) + (GL ? 0 : S::EPB * 6 * SS::FACE_NF * S::n2));
+    return sizeof(double) * (SBasis<n>::SIZE + 2 * S::n2 + S::EPB * (20 * S::n3 + 6 * S::n2 * 5) +
+                             (GL ? 0 : S::EPB * 6 * SS::FACE_NF * S::n2 + SS::SCRATCH));
   }
   static size_t smem_weak_adj() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * 5 * S::n3 + S::THREADS); }
   static size_t smem_split_adj() { return sizeof(double) * (SBasis<n>::SIZE + 2 * S::n2 + S::EPB * 26 * S::n3 + S::THREADS); }

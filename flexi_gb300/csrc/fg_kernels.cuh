@@ -127,11 +127,12 @@ __global__ void __launch_bounds__(Shape<n, E>::THREADS) k_prep(Dev d, Basis B) {
         for (int v = 0; v < 5; ++v) c[v] = fma(sU[(es * 5 + v) * n3 + x], L, c[v]);
       }
       if (entropy) {
-        // EntropyToCons: rho e = (kappa-1)^(1/(kappa-1)) (-W5')^(-kappa/(kappa-1)) exp(-s/(kappa-1)), W' = (kappa-1) W
+        // EntropyToCons: rho e = (kappa-1)^(1/(kappa-1)) (-W5')^(-kappa/(kappa-1)) exp(-s/(kappa-1)), W' = (kappa-1) W;
         const double w0 = c[0] * B.kappaM1, w1 = c[1] * B.kappaM1, w2 = c[2] * B.kappaM1, w3 = c[3] * B.kappaM1, w4 = c[4] * B.kappaM1;
         const double ekin = 0.5 * (w1 * w1 + w2 * w2 + w3 * w3) / w4;
         const double sEnt = B.kappa - w0 + ekin;
-        const double rhoe = B.kappaM1_sKappaM1 * pow(-w4, -B.kappa_kappaM1) * exp(-sEnt * B.sKappaM1);
+        // (kappa-1)^(1/(kappa-1)) (-W5')^(-kappa/(kappa-1)) exp(-s/(kappa-1)) as one exponential
+        const double rhoe = exp(B.logEntC - B.kappa_kappaM1 * log(-w4) - sEnt * B.sKappaM1);
         c[0] = -rhoe * w4;
         c[1] = rhoe * w1; c[2] = rhoe * w2; c[3] = rhoe * w3;
         c[4] = rhoe * (1.0 - ekin);
@@ -831,6 +832,7 @@ template <int n> struct SplitShape {
   static constexpr int NODE_THREADS = ((EPB * n3 + 31) / 32) * 32;
   static constexpr int THREADS = LINE_THREADS > NODE_THREADS ? LINE_THREADS : NODE_THREADS;
   static constexpr int FACE_NF = 9;  // rho, u, v, w, p-term, H-term, face metric row (3)
+  static constexpr int SCRATCH = (LINE_THREADS / 32) * 32 * 5;  // Gauss: per-lane Leg*FluxB of the segment sums
 };
 
 template <int n, bool GL>
@@ -844,6 +846,7 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
   double* sA = sR + EPB * 15 * n3;     // [EPB][5][n3] split-flux divergence
   double* sFl = sA + EPB * 5 * n3;     // [EPB][6][n2][5]
   double* sFS = sFl + EPB * 6 * n2 * 5;  // Gauss: [EPB][6][FNF][n2] own face states and face metric rows
+  double* sScr = sFS + EPB * 6 * FNF * n2;  // Gauss: [warp][lane][5]
   load_basis_smem<n>(B, sD);
   SBasis<n> Bs{sD};
   const bool pi = B.splitDG == 4;
@@ -957,6 +960,8 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
       }
       if (!GL) {
         const int fo = c1 + n * c2;  // face coordinate of this line on both end faces
+        double* scr = sScr + (threadIdx.x >> 5) * 160;
+        constexpr int ROUNDS = (5 + n - 1) / n;  // components summed per lane
 #pragma unroll
         for (int side = 0; side < 2; ++side) {
           const int ls = side == 0 ? (dir == 0 ? XI_MINUS : (dir == 1 ? ETA_MINUS : ZETA_MINUS))
@@ -968,12 +973,26 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
           const double leg = side == 0 ? Bs.Lm(a) : Bs.Lp(a);
           // -1/2 NormalSign LegHat(a): NormalSign = -1 on the minus, +1 on the plus side
           const double cs = side == 0 ? 0.5 * Bs.LhM(a) : -0.5 * Bs.LhP(a);
+          // FluxB_sum of the segment: every lane stores Leg(a) G(a); lane a sums components a, a+n, ... over
+          // the segment's n lanes (in lane order); the sums are broadcast back by shuffles
+          __syncwarp();
+#pragma unroll
+          for (int v = 0; v < 5; ++v) scr[lane * 5 + v] = G[v] * leg;
+          __syncwarp();
+          double S[ROUNDS];
+#pragma unroll
+          for (int r = 0; r < ROUNDS; ++r) {
+            const int c = a + r * n;
+            S[r] = 0.;
+            if (seg < SEG && c < 5) {
+              S[r] = scr[segBase * 5 + c];
+#pragma unroll
+              for (int m = 1; m < n; ++m) S[r] += scr[(segBase + m) * 5 + c];
+            }
+          }
 #pragma unroll
           for (int v = 0; v < 5; ++v) {
-            const double gl = G[v] * leg;
-            double sum = 0.;
-#pragma unroll
-            for (int m = 0; m < n; ++m) sum += __shfl_sync(0xffffffffu, gl, valid ? segBase + m : lane);
+            const double sum = __shfl_sync(0xffffffffu, S[v / n], valid ? segBase + v % n : lane);
             acc[v] = fma(cs * (v == 0 ? f0 : f1), sum - G[v], acc[v]);
           }
         }
