@@ -9,7 +9,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#define FG_MAXN 10  // maximum number of nodes per direction (N <= 9)
+#define FG_MAXN 12  // maximum number of nodes per direction (N <= 11)
 
 namespace fg {
 
@@ -71,6 +71,9 @@ struct Dev {
   double* dpdx;    // [nInst] (0 when no body force)
   double* muScale; // [nElems] viscosity multiplier of each element (null: 1)
   double* forceField;  // [e][n3] additional x-momentum body force per node, energy source F * bulkVel (null: none)
+  double* scratch;  // element kernels whose per-element arrays exceed shared memory (lines of 9..12 nodes):
+                    // [block][scratchStride] (null otherwise)
+  long long scratchStride;
   int* err;        // [1] sticky error word
   double* dtElem;  // [2][nElems] convective and viscous element time-step limits of the last CALCTIMESTEP
 };

@@ -29,6 +29,10 @@ KernelSet kernel_set_n5(bool);
 KernelSet kernel_set_n6(bool);
 KernelSet kernel_set_n7(bool);
 KernelSet kernel_set_n8(bool);
+KernelSet kernel_set_n9(bool);
+KernelSet kernel_set_n10(bool);
+KernelSet kernel_set_n11(bool);
+KernelSet kernel_set_n12(bool);
 KernelSet get_kernel_set(int n, bool gl) {
   switch (n) {
     case 2: return kernel_set_n2(gl);
@@ -38,6 +42,10 @@ KernelSet get_kernel_set(int n, bool gl) {
     case 6: return kernel_set_n6(gl);
     case 7: return kernel_set_n7(gl);
     case 8: return kernel_set_n8(gl);
+    case 9: return kernel_set_n9(gl);
+    case 10: return kernel_set_n10(gl);
+    case 11: return kernel_set_n11(gl);
+    case 12: return kernel_set_n12(gl);
     default: return KernelSet{};
   }
 }
@@ -437,6 +445,11 @@ int upload_mesh(fg_handle* h) {
   if ((r = upload(h, d.err, std::vector<int>(1, 0)))) return r;
   if ((r = upload(h, d.muScale, std::vector<double>(nE, 1.0)))) return r;
   if ((r = dalloc(h, d.dtElem, (size_t)2 * nE))) return r;
+  if (h->K.scratchPerBlock > 0) {
+    // per-CTA slices of the element kernels whose arrays exceed shared memory (one element per CTA here)
+    d.scratchStride = h->K.scratchPerBlock;
+    if ((r = dalloc(h, d.scratch, (size_t)nE * (size_t)d.scratchStride))) return r;
+  }
   if ((r = upload(h, h->dMetAdv, M.metAdv))) return r;
   if ((r = upload(h, h->dMetVisc, M.metVisc))) return r;
   if ((r = upload(h, h->dWVol, M.wVol))) return r;
@@ -553,6 +566,7 @@ namespace {
 
 // the adjoint kernels cover: weak form and split form PI, LF/Roe/RoeEntropyFix, BR1/BR2
 const char* adjoint_unsupported(const fg_config& c) {
+  if (c.N > 7) return "the adjoint supports N = 1..7";
   if (c.SplitDG != FG_SPLIT_NONE && c.SplitDG != FG_SPLIT_PI) return "the adjoint supports the weak form and the split form PI";
   if (c.SplitDG != FG_SPLIT_NONE && (c.NodeType != FG_NODE_GAUSS_LOBATTO || (c.N != 1 && c.N != 3 && c.N != 7)))
     return "the adjoint of the split form supports Gauss-Lobatto nodes with N = 1, 3, 7";
@@ -686,7 +700,7 @@ int fg_create(const fg_config* cfg, fg_handle** out) {
   h->cfg = *cfg;
   const fg_config& c = h->cfg;
   std::string why;
-  if (c.N < 1 || c.N > 7) why = "N must be in 1..7";
+  if (c.N < 1 || c.N > 11) why = "N must be in 1..11";
   else if (c.NodeType != FG_NODE_GAUSS && c.NodeType != FG_NODE_GAUSS_LOBATTO) why = "NodeType must be 1 (Gauss) or 2 (Gauss-Lobatto)";
   else if (c.Riemann != FG_RIEMANN_LF && c.Riemann != FG_RIEMANN_HLLC && c.Riemann != FG_RIEMANN_ROE && c.Riemann != FG_RIEMANN_ROEENTROPYFIX)
     why = "Riemann must be LF, HLLC, Roe or RoeEntropyFix";

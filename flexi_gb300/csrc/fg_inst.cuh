@@ -10,19 +10,19 @@ template <int n, bool GL>
 struct Inst {
   using S = Shape<n>;
   static int blocks(const Dev& d) { return (d.nElems + S::EPB - 1) / S::EPB; }
-  static size_t smem_prep() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * (5 + VP_NF) * S::n3); }
-  static size_t smem_lift() {
-    return sizeof(double) * (SBasis<n>::SIZE + S::EPB * (4 * S::n3 + 6 * S::n2 * 7 + 12 * S::n3 + S::n3));
-  }
-  static size_t smem_weak() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * (15 * S::n3 + 6 * S::n2 * 5)); }
+  static size_t smem_prep() { return dyn_smem_bytes<n>(Big<n>::prep); }
+  static size_t smem_lift() { return dyn_smem_bytes<n>(Big<n>::lift); }
+  static size_t smem_weak() { return dyn_smem_bytes<n>(Big<n>::weak); }
   static size_t smem_split() { return sizeof(double) * (SBasis<n>::SIZE + 2 * S::n2 + S::EPB * (20 * S::n3 + 6 * S::n2 * 5)); }
   // the tuned shuffle-pair kernel for Gauss-Lobatto lines of 2, 4 or 8 nodes; k_vol_split_gen otherwise
   static constexpr bool SPLIT_POW2 = GL && (n == 2 || n == 4 || n == 8);
-  static size_t smem_split_gen() {
-    using SS = SplitShape<n>;
-    return sizeof(double) * (SBasis<n>::SIZE + 2 * S::n2 + S::EPB * (20 * S::n3 + 6 * S::n2 * 5) +
-                             (GL ? 0 : S::EPB * 6 * SS::FACE_NF * S::n2 + SS::SCRATCH));
-  }
+  static size_t smem_split_gen() { return dyn_smem_bytes<n>(SplitShape<n>::template big<GL>()); }
+  // doubles per CTA of the global scratch array: the largest per-element array set that does not fit in
+  // shared memory (0: every kernel of this instantiation stages in shared memory)
+  static constexpr long long gs(long long big) { return big_in_global<n>(big) ? big : 0; }
+  static constexpr long long mx(long long a, long long b) { return a > b ? a : b; }
+  static constexpr long long SCRATCH_PER_BLOCK =
+      mx(mx(gs(Big<n>::prep), gs(Big<n>::lift)), mx(gs(Big<n>::weak), gs(SplitShape<n>::template big<GL>())));
   static size_t smem_weak_adj() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * 5 * S::n3 + S::THREADS); }
   static size_t smem_split_adj() { return sizeof(double) * (SBasis<n>::SIZE + 2 * S::n2 + S::EPB * 26 * S::n3 + S::THREADS); }
   static size_t smem_lift_adj() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * (13 * S::n3 + 6 * S::n2 * 19)); }
@@ -30,20 +30,11 @@ struct Inst {
   // elements per CTA of the autotuner's alternative element kernels (N=5: 2, N=3: 4; 0: none)
   static constexpr int ALT_E = (n == 6) ? 2 : ((n == 4) ? 4 : 0);
   template <int E>
-  static size_t smem_prep_E() {
-    using SE = Shape<n, E>;
-    return sizeof(double) * (SBasis<n>::SIZE + SE::EPB * (5 + VP_NF) * SE::n3);
-  }
+  static size_t smem_prep_E() { return dyn_smem_bytes<n>(Big<n, E>::prep); }
   template <int E>
-  static size_t smem_lift_E() {
-    using SE = Shape<n, E>;
-    return sizeof(double) * (SBasis<n>::SIZE + SE::EPB * (4 * SE::n3 + 6 * SE::n2 * 7 + 12 * SE::n3 + SE::n3));
-  }
+  static size_t smem_lift_E() { return dyn_smem_bytes<n>(Big<n, E>::lift); }
   template <int E>
-  static size_t smem_weak_E() {
-    using SE = Shape<n, E>;
-    return sizeof(double) * (SBasis<n>::SIZE + SE::EPB * (15 * SE::n3 + 6 * SE::n2 * 5));
-  }
+  static size_t smem_weak_E() { return dyn_smem_bytes<n>(Big<n, E>::weak); }
   template <int E>
   static void prep_E(const Dev& d, const Basis& B, cudaStream_t st) {
     using SE = Shape<n, E>;
@@ -73,9 +64,11 @@ struct Inst {
     set_smem(k_vol_weak<n, GL>, smem_weak());
     if constexpr (SPLIT_POW2) set_smem(k_vol_split<n>, smem_split());
     else set_smem(k_vol_split_gen<n, GL>, smem_split_gen());
-    set_smem(k_vol_weak_adj<n, GL>, smem_weak_adj());
-    set_smem(k_lift_adj<n, GL>, smem_lift_adj());
-    set_smem(k_prep_adj<n, GL>, smem_prep_adj());
+    if constexpr (ADJ) {
+      set_smem(k_vol_weak_adj<n, GL>, smem_weak_adj());
+      set_smem(k_lift_adj<n, GL>, smem_lift_adj());
+      set_smem(k_prep_adj<n, GL>, smem_prep_adj());
+    }
     if constexpr (GL && (n == 2 || n == 4 || n == 8)) set_smem(k_vol_split_adj<n>, smem_split_adj());
     if constexpr (ALT_E > 0) {
       set_smem(k_prep<n, GL, ALT_E>, smem_prep_E<ALT_E>());
@@ -83,6 +76,8 @@ struct Inst {
       set_smem(k_vol_weak<n, GL, ALT_E>, smem_weak_E<ALT_E>());
     }
   }
+  // adjoint kernels: lines of up to 8 nodes (one thread per node, shared-memory staging)
+  static constexpr bool ADJ = n <= 8;
   static void vol_adj(const Dev& d, const AdjDev& a, const Basis& B, cudaStream_t st) {
     if constexpr (GL && (n == 2 || n == 4 || n == 8)) {
       if (B.splitDG >= 0) {
@@ -90,17 +85,17 @@ struct Inst {
         return;
       }
     }
-    k_vol_weak_adj<n, GL><<<blocks(d), S::THREADS, smem_weak_adj(), st>>>(d, a, B);
+    if constexpr (ADJ) k_vol_weak_adj<n, GL><<<blocks(d), S::THREADS, smem_weak_adj(), st>>>(d, a, B);
   }
   static void flux_adj(const Dev& d, const AdjDev& a, const Basis& B, cudaStream_t st) {
     const long long pts = (long long)d.nSides * S::n2;
-    k_flux_adj<n><<<(unsigned)((pts + 127) / 128), 128, 0, st>>>(d, a, B);
+    if constexpr (ADJ) k_flux_adj<n><<<(unsigned)((pts + 127) / 128), 128, 0, st>>>(d, a, B);
   }
   static void lift_adj(const Dev& d, const AdjDev& a, const Basis& B, cudaStream_t st) {
-    k_lift_adj<n, GL><<<blocks(d), S::THREADS, smem_lift_adj(), st>>>(d, a, B);
+    if constexpr (ADJ) k_lift_adj<n, GL><<<blocks(d), S::THREADS, smem_lift_adj(), st>>>(d, a, B);
   }
   static void prep_adj(const Dev& d, const AdjDev& a, const Basis& B, cudaStream_t st) {
-    k_prep_adj<n, GL><<<blocks(d), S::THREADS, smem_prep_adj(), st>>>(d, a, B);
+    if constexpr (ADJ) k_prep_adj<n, GL><<<blocks(d), S::THREADS, smem_prep_adj(), st>>>(d, a, B);
   }
   static void prep(const Dev& d, const Basis& B, cudaStream_t st) {
     k_prep<n, GL><<<blocks(d), S::THREADS, smem_prep(), st>>>(d, B);
@@ -129,8 +124,9 @@ struct Inst {
     k.prepare = &prepare;
     k.prep = &prep; k.lift = &lift; k.flux = &flux; k.vol_weak = &vol_weak; k.dt = &dt;
     k.vol_split = &vol_split;
-    k.vol_adj = &vol_adj; k.flux_adj = &flux_adj; k.lift_adj = &lift_adj; k.prep_adj = &prep_adj;
+    if constexpr (ADJ) { k.vol_adj = &vol_adj; k.flux_adj = &flux_adj; k.lift_adj = &lift_adj; k.prep_adj = &prep_adj; }
     k.defEPB = S::EPB;
+    k.scratchPerBlock = SCRATCH_PER_BLOCK;
     k.flux_block = &flux_block;
     if constexpr (ALT_E > 0) {
       k.altEPB = ALT_E;

@@ -17,11 +17,33 @@
 namespace fg {
 
 // E = elements per CTA; E = 0 selects the default, which fills at least ~128 threads for small n (the
-// autotuner may pick another E for the element kernels that have variants)
+// autotuner may pick another E for the element kernels that have variants). One thread per volume node
+// up to 512 threads; larger elements (lines of 9..12 nodes) give each thread several nodes.
 template <int n, int E = 0> struct Shape {
   static constexpr int N = n - 1, n2 = n * n, n3 = n * n * n;
   static constexpr int EPB = E > 0 ? E : ((n3 >= 128) ? 1 : (128 + n3 - 1) / n3);
-  static constexpr int THREADS = ((EPB * n3 + 31) / 32) * 32;
+  static constexpr int THREADS = ((EPB * n3 + 31) / 32) * 32 > 512 ? 512 : ((EPB * n3 + 31) / 32) * 32;
+};
+
+// Shared-memory plan of an element kernel: the basis matrices always live in shared memory, the kernel's
+// per-element arrays ("big", in doubles per CTA) too unless basis + big exceed FG_SMEM_LIMIT; then they
+// live in the CTA's slice of the global array Dev::scratch (L1/L2-cached; lines of 10..12 nodes).
+constexpr long long FG_SMEM_LIMIT = 220 * 1024;
+template <int n> struct SBasisSize { static constexpr int value = 3 * n * n + 4 * n; };
+template <int n>
+__host__ __device__ constexpr bool big_in_global(long long big) { return (SBasisSize<n>::value + big) * 8 > FG_SMEM_LIMIT; }
+template <int n>
+constexpr size_t dyn_smem_bytes(long long big) { return 8 * (size_t)(SBasisSize<n>::value + (big_in_global<n>(big) ? 0 : big)); }
+template <int n>
+__device__ __forceinline__ double* big_base(const Dev& d, double* smem, long long big) {
+  return big_in_global<n>(big) ? d.scratch + (size_t)blockIdx.x * d.scratchStride : smem + SBasisSize<n>::value;
+}
+// per-element arrays of the element kernels (doubles per CTA)
+template <int n, int E = 0> struct Big {
+  using S = Shape<n, E>;
+  static constexpr long long prep = (long long)S::EPB * (5 + VP_NF) * S::n3;
+  static constexpr long long lift = (long long)S::EPB * (17 * S::n3 + 42 * S::n2);
+  static constexpr long long weak = (long long)S::EPB * (15 * S::n3 + 30 * S::n2);
 };
 
 // copies the basis matrices a kernel indexes with thread-dependent indices into shared memory
@@ -63,7 +85,7 @@ __global__ void __launch_bounds__(Shape<n, E>::THREADS) k_prep(Dev d, Basis B) {
   constexpr int n2 = S::n2, n3 = S::n3, EPB = S::EPB, N = S::N;
   extern __shared__ double smem[];
   double* sD = smem;
-  double* sU = smem + SBasis<n>::SIZE;         // [EPB][5][n3] U, or the entropy variables
+  double* sU = big_base<n>(d, smem, Big<n, E>::prep);  // [EPB][5][n3] U, or the entropy variables
   double* sP = sU + EPB * 5 * n3;              // [EPB][VP_NF][n3]
   load_basis_smem<n>(B, sD);
   SBasis<n> Bs{sD};
@@ -220,7 +242,7 @@ __global__ void __launch_bounds__(Shape<n, E>::THREADS, (n == 8 && GL ? 2 : 1)) 
   constexpr int n2 = S::n2, n3 = S::n3, EPB = S::EPB, N = S::N;
   extern __shared__ double smem[];
   double* sD = smem;
-  double* sL = smem + SBasis<n>::SIZE;   // [EPB][4][n3] lifting variables u,v,w,T
+  double* sL = big_base<n>(d, smem, Big<n, E>::lift);  // [EPB][4][n3] lifting variables u,v,w,T
   double* sF = sL + EPB * 4 * n3;        // [EPB][6][n2][4] surface lifting flux (times SurfElem), local face order
   double* sN = sF + EPB * 6 * n2 * 4;    // [EPB][6][n2][3] face normal of the side point mapped to local face order
   double* sG = sN + EPB * 6 * n2 * 3;    // [EPB][12][n3] gradients
@@ -553,7 +575,7 @@ __global__ void __launch_bounds__(Shape<n, E>::THREADS) k_vol_weak(Dev d, Basis 
   constexpr int n2 = S::n2, n3 = S::n3, EPB = S::EPB;
   extern __shared__ double smem[];
   double* sD = smem;
-  double* sT = smem + SBasis<n>::SIZE;   // [EPB][15][n3] transformed fluxes f~(5) g~(5) h~(5)
+  double* sT = big_base<n>(d, smem, Big<n, E>::weak);  // [EPB][15][n3] transformed fluxes f~(5) g~(5) h~(5)
   double* sFl = sT + EPB * 15 * n3;      // [EPB][6][n2][5]
   load_basis_smem<n>(B, sD);
   SBasis<n> Bs{sD};
@@ -821,8 +843,9 @@ __global__ void __launch_bounds__(Shape<n>::THREADS, (n == 8 ? 2 : 1)) k_vol_spl
 // Gauss nodes (surfint.t90:90-140, 177-215, split-Gauss surface integral): in the same pass each lane
 // evaluates the two-point flux FluxB between its node and the element's own face state at both ends of the
 // line (metric: its node's metric vector plus the face metric row Ja_Face / Ja_slave), the segment forms
-// FluxB_sum = sum_k Leg(k) FluxB(k) with shuffles, and the lane adds -1/2 NormalSign LegHat(a)
-// (FluxB_sum - FluxB(a)); the numerical-flux part is the Gauss surface integral of finish_node.
+// FluxB_sum = sum_k Leg(k) FluxB(k) once per face point (shared-memory slot of the warp), and the lane adds
+// -1/2 NormalSign LegHat(a) (FluxB_sum - FluxB(a)); the numerical-flux part is the Gauss surface integral
+// of finish_node. Up to 512 threads: larger elements loop over groups of lines and over nodes.
 // =====================================================================================================
 template <int n> struct SplitShape {
   static constexpr int EPB = Shape<n>::EPB, n2 = n * n, n3 = n * n * n;
@@ -830,9 +853,18 @@ template <int n> struct SplitShape {
   static constexpr int LINES = EPB * n2;                   // lines per direction per CTA
   static constexpr int LINE_THREADS = ((LINES + SEG - 1) / SEG) * 32;
   static constexpr int NODE_THREADS = ((EPB * n3 + 31) / 32) * 32;
-  static constexpr int THREADS = LINE_THREADS > NODE_THREADS ? LINE_THREADS : NODE_THREADS;
+  static constexpr int WANT = LINE_THREADS > NODE_THREADS ? LINE_THREADS : NODE_THREADS;
+  static constexpr int THREADS = WANT > 512 ? 512 : WANT;
+  static constexpr int NPT = (EPB * n3 + THREADS - 1) / THREADS;  // volume nodes per thread
   static constexpr int FACE_NF = 9;  // rho, u, v, w, p-term, H-term, face metric row (3)
-  static constexpr int SCRATCH = (LINE_THREADS / 32) * 32 * 5;  // Gauss: per-lane Leg*FluxB of the segment sums
+  static constexpr int SCRATCH = (THREADS / 32) * 32 * 5;  // Gauss: per-lane Leg*FluxB of the segment sums
+  // per-CTA arrays: coefficients, split-flux inputs, divergence, face fluxes (+ Gauss: face states,
+  // segment-sum slots) (+ several nodes per thread: a separate viscous-flux array)
+  template <bool GL>
+  __host__ __device__ static constexpr long long big() {
+    return 2LL * n2 + (long long)EPB * (20 * n3 + 30 * n2) + (GL ? 0LL : (long long)EPB * 6 * FACE_NF * n2 + SCRATCH) +
+           (NPT > 1 ? (long long)EPB * 12 * n3 : 0LL);
+  }
 };
 
 template <int n, bool GL>
@@ -841,12 +873,13 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
   constexpr int n2 = SS::n2, n3 = SS::n3, EPB = SS::EPB, N = n - 1, SEG = SS::SEG, FNF = SS::FACE_NF;
   extern __shared__ double smem[];
   double* sD = smem;
-  double* sC = sD + SBasis<n>::SIZE;   // [2][n2]: DVolSurf(l,i) x density factor, x factor of the other components
+  double* sC = big_base<n>(d, smem, SS::template big<GL>());  // [2][n2]: DVolSurf(l,i) x density factor, x factor of the others
   double* sR = sC + 2 * n2;            // [EPB][15][n3]: rho, u, v, w, p-term, H-term, metrics(9); later viscous fluxes(12)
   double* sA = sR + EPB * 15 * n3;     // [EPB][5][n3] split-flux divergence
   double* sFl = sA + EPB * 5 * n3;     // [EPB][6][n2][5]
   double* sFS = sFl + EPB * 6 * n2 * 5;  // Gauss: [EPB][6][FNF][n2] own face states and face metric rows
-  double* sScr = sFS + EPB * 6 * FNF * n2;  // Gauss: [warp][lane][5]
+  double* sScr = sFS + (GL ? 0 : EPB * 6 * FNF * n2);  // Gauss: [warp][lane][5]
+  double* sV = SS::NPT > 1 ? sScr + (GL ? 0 : SS::SCRATCH) : sR;  // viscous fluxes [EPB][12][n3]
   load_basis_smem<n>(B, sD);
   SBasis<n> Bs{sD};
   const bool pi = B.splitDG == 4;
@@ -921,8 +954,11 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
   const int seg = lane / n, a = lane - seg * n, segBase = seg * n;
 #pragma unroll 1
   for (int dir = 0; dir < 3; ++dir) {
-    if (threadIdx.x < SS::LINE_THREADS) {  // whole warps
-      const int line = (threadIdx.x >> 5) * SEG + seg;
+#pragma unroll 1
+   for (int base = 0; base < SS::LINE_THREADS; base += SS::THREADS) {
+    const int tt = base + threadIdx.x;
+    if (tt < SS::LINE_THREADS) {  // whole warps
+      const int line = (tt >> 5) * SEG + seg;
       const bool valid = seg < SEG && line < SS::LINES;
       const int lineC = valid ? line : 0;  // idle lanes compute on line 0 and store nothing
       const int es = lineC / n2, lr = lineC - es * n2, c1 = lr % n, c2 = lr / n;
@@ -1002,15 +1038,15 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
         for (int v = 0; v < 5; ++v) sA[(es * 5 + v) * n3 + xa] = acc[v];
       }
     }
+   }
     __syncthreads();
   }
-  // viscous fluxes (weak form): transformed fluxes of this node from the metrics still in sR, written over
-  // sR once every thread has finished reading it
-  const int t = threadIdx.x;
-  const bool hasNode = t < EPB * n3;
-  const int es = hasNode ? t / n3 : 0, x = t - es * n3, e = e0 + es;
-  const bool live = hasNode && e < d.nElems;
-  {
+  // viscous fluxes (weak form): transformed fluxes of each node from the metrics still in sR; with one node
+  // per thread they are written over sR once every thread has finished reading it, else into sV
+  constexpr int VS = SS::NPT > 1 ? 12 : 15;  // field stride of the viscous-flux array
+  for (int t = threadIdx.x; t < SS::NPT * SS::THREADS; t += blockDim.x) {
+    const int es = t < EPB * n3 ? t / n3 : 0, x = t - es * n3, e = e0 + es;
+    const bool live = t < EPB * n3 && e < d.nElems;
     double Fv[12];
     if (live) {
       const double* Q = sR + es * 15 * n3;
@@ -1030,31 +1066,34 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
         for (int v = 0; v < 4; ++v) Fv[4 * dd + v] = F[1 + v];
       }
     }
-    __syncthreads();
+    if (SS::NPT == 1) __syncthreads();  // one pass: every thread reaches it
     if (live) {
 #pragma unroll
-      for (int c = 0; c < 12; ++c) sR[(es * 15 + c) * n3 + x] = Fv[c];
+      for (int c = 0; c < 12; ++c) sV[(es * VS + c) * n3 + x] = Fv[c];
     }
   }
   __syncthreads();
-  if (!live) return;
-  const int i = x % n, j = (x / n) % n, k = x / n2;
-  double ut[5];
+  for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
+    const int es = t / n3, x = t - es * n3, e = e0 + es;
+    if (e >= d.nElems) continue;
+    const int i = x % n, j = (x / n) % n, k = x / n2;
+    double ut[5];
 #pragma unroll
-  for (int v = 0; v < 5; ++v) ut[v] = sA[(es * 5 + v) * n3 + x];
-  const double* V = sR + es * 15 * n3;
+    for (int v = 0; v < 5; ++v) ut[v] = sA[(es * 5 + v) * n3 + x];
+    const double* V = sV + es * VS * n3;
 #pragma unroll
-  for (int l = 0; l < n; ++l) {
-    const double ci = Bs.DhT(l, i), cj = Bs.DhT(l, j), ck = Bs.DhT(l, k);
-    const int xi = l + n * (j + n * k), xj = i + n * (l + n * k), xk = i + n * (j + n * l);
+    for (int l = 0; l < n; ++l) {
+      const double ci = Bs.DhT(l, i), cj = Bs.DhT(l, j), ck = Bs.DhT(l, k);
+      const int xi = l + n * (j + n * k), xj = i + n * (l + n * k), xk = i + n * (j + n * l);
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      ut[1 + v] = fma(ci, V[v * n3 + xi], ut[1 + v]);
-      ut[1 + v] = fma(cj, V[(4 + v) * n3 + xj], ut[1 + v]);
-      ut[1 + v] = fma(ck, V[(8 + v) * n3 + xk], ut[1 + v]);
+      for (int v = 0; v < 4; ++v) {
+        ut[1 + v] = fma(ci, V[v * n3 + xi], ut[1 + v]);
+        ut[1 + v] = fma(cj, V[(4 + v) * n3 + xj], ut[1 + v]);
+        ut[1 + v] = fma(ck, V[(8 + v) * n3 + xk], ut[1 + v]);
+      }
     }
+    finish_node<n, GL>(d, Bs, st, sFl, es, e, x, ut);
   }
-  finish_node<n, GL>(d, Bs, st, sFl, es, e, x, ut);
 }
 
 // =====================================================================================================
@@ -1071,41 +1110,49 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_dt(Dev d, Basis B, const 
                                                           double* bulkPart /* [nElems] or null */, const double* wVol) {
   using S = Shape<n>;
   constexpr int n3 = S::n3, EPB = S::EPB;
+  // nodes handled by one thread: one, or (elements larger than the block) n3 / THREADS rounded up
+  constexpr int NPT = (EPB * n3 + S::THREADS - 1) / S::THREADS;
+  constexpr int NR = NPT > 1 ? S::THREADS : n3;  // entries reduced per element
   // per-thread values: convective bound per direction (3), viscous bound per direction (3), bulk-velocity part
   __shared__ double sred[7][S::THREADS];
   const int e0 = blockIdx.x * EPB;
   const int t = threadIdx.x;
-  const int es = t / n3, x = t - es * n3, e = e0 + es;
+  const int es = NPT > 1 ? 0 : t / n3, x = NPT > 1 ? t : t - es * n3, e = e0 + es;
   const bool active = es < EPB && e < d.nElems;
   double v7[7] = {0., 0., 0., 0., 0., 0., 0.};
   if (active) {
-    double u[5];
+#pragma unroll 1
+    for (int xn = x; xn < n3; xn += (NPT > 1 ? S::THREADS : n3)) {
+      double u[5];
 #pragma unroll
-    for (int v = 0; v < 5; ++v) u[v] = d.U[((size_t)e * 5 + v) * n3 + x];
-    if (u[0] != u[0]) set_error(d.err, 1);
-    const double srho = 1.0 / u[0];
-    const double vx = u[1] * srho, vy = u[2] * srho, vz = u[3] * srho;
-    const double p = B.kappaM1 * (u[4] - 0.5 * (vx * u[1] + vy * u[2] + vz * u[3]));
-    const double c = sqrt(B.kappa * p * srho);
-    const double sj = d.sJ[(size_t)e * n3 + x];
-    const double lv = elem_mu(d, e) * srho;
+      for (int v = 0; v < 5; ++v) u[v] = d.U[((size_t)e * 5 + v) * n3 + xn];
+      if (u[0] != u[0]) set_error(d.err, 1);
+      const double srho = 1.0 / u[0];
+      const double vx = u[1] * srho, vy = u[2] * srho, vz = u[3] * srho;
+      const double p = B.kappaM1 * (u[4] - 0.5 * (vx * u[1] + vy * u[2] + vz * u[3]));
+      const double c = sqrt(B.kappa * p * srho);
+      const double sj = d.sJ[(size_t)e * n3 + xn];
+      const double lv = elem_mu(d, e) * srho;
 #pragma unroll
-    for (int dd = 0; dd < 3; ++dd) {
-      const double* mm = d.metr + ((size_t)e * 9 + 3 * dd) * n3 + x;
-      const double q = (mm[0] * vx + mm[n3] * vy + mm[2 * n3] * vz) * sj;
-      v7[dd] = fabs(q) + c * metAdv[((size_t)e * 3 + dd) * n3 + x];
-      v7[3 + dd] = lv * metVisc[((size_t)e * 3 + dd) * n3 + x];
+      for (int dd = 0; dd < 3; ++dd) {
+        const double* mm = d.metr + ((size_t)e * 9 + 3 * dd) * n3 + xn;
+        const double q = (mm[0] * vx + mm[n3] * vy + mm[2 * n3] * vz) * sj;
+        const double lc = fabs(q) + c * metAdv[((size_t)e * 3 + dd) * n3 + xn];
+        const double lvd = lv * metVisc[((size_t)e * 3 + dd) * n3 + xn];
+        v7[dd] = NPT > 1 ? fmax(v7[dd], lc) : lc;
+        v7[3 + dd] = NPT > 1 ? fmax(v7[3 + dd], lvd) : lvd;
+      }
+      if (bulkPart) v7[6] += vx * wVol[xn] / sj;
     }
-    if (bulkPart) v7[6] = vx * wVol[x] / sj;
   }
 #pragma unroll
   for (int c = 0; c < 7; ++c) sred[c][t] = v7[c];
   __syncthreads();
-  // tree reduction inside each element's thread range [es*n3, es*n3+n3): max for the bounds, sum for the bulk part
-  constexpr int P2 = (n3 <= 1) ? 1 : (1 << (32 - __builtin_clz(n3 - 1)));
+  // tree reduction inside each element's thread range [es*NR, es*NR+NR): max for the bounds, sum for the bulk part
+  constexpr int P2 = (NR <= 1) ? 1 : (1 << (32 - __builtin_clz(NR - 1)));
 #pragma unroll 1
   for (int st = P2 / 2; st > 0; st >>= 1) {
-    if (es < EPB && x < st && x + st < n3) {
+    if (es < EPB && x < st && x + st < NR) {
 #pragma unroll
       for (int c = 0; c < 6; ++c) sred[c][t] = fmax(sred[c][t], sred[c][t + st]);
       sred[6][t] += sred[6][t + st];

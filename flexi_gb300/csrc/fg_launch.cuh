@@ -28,6 +28,8 @@ struct KernelSet {
   void (*vol_weak_alt)(const Dev&, const Basis&, int, double, double, cudaStream_t) = nullptr;
   void (*flux_block)(const Dev&, const Basis&, int, cudaStream_t) = nullptr;
   int fluxBlock = 128;
+  // doubles per CTA of Dev::scratch needed by element kernels whose arrays exceed shared memory (0: none)
+  long long scratchPerBlock = 0;
   // sets the dynamic shared-memory limits of all kernels; must run before any stream capture
   void (*prepare)() = nullptr;
 };

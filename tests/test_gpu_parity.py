@@ -53,6 +53,14 @@ RHS_CASES = {
     "gauss4_split_sd_roe": dict(N=4, NodeType="gauss", SplitDG="sd", Riemann="roe"),
     "gauss6_split_pi_lf": dict(N=6, NodeType="gauss", SplitDG="pi", Riemann="lf"),
     "gauss7_split_pi_roeef": dict(N=7, NodeType="gauss", SplitDG="pi", Riemann="roeentropyfix"),
+    # lines of 9..12 nodes: several nodes per thread; per-element arrays in the global scratch where they
+    # exceed shared memory
+    "gauss8_weak_roe_br2": dict(N=8, NodeType="gauss", SplitDG="weak", Riemann="roe", Lifting="br2"),
+    "gl9_weak_lf": dict(N=9, NodeType="gauss-lobatto", SplitDG="weak", Riemann="lf"),
+    "gauss11_weak_roeef_br1": dict(N=11, NodeType="gauss", SplitDG="weak", Riemann="roeentropyfix", Lifting="br1"),
+    "gl11_split_pi_roeef_br2": dict(N=11, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roeentropyfix", Lifting="br2"),
+    "gauss8_split_pi_hllc": dict(N=8, NodeType="gauss", SplitDG="pi", Riemann="hllc"),
+    "gauss10_split_sd_roe_br2": dict(N=10, NodeType="gauss", SplitDG="sd", Riemann="roe", Lifting="br2"),
 }
 COMMON = dict(kappa=1.4, R=71.42857, Pr=0.72, mu0=6.25e-4, CFLScale=0.9, DFLScale=0.9)
 
@@ -67,7 +75,7 @@ def test_rhs_parity_tgv(name):
 
 
 @pytest.mark.parametrize("name", ["c1_gauss3_weak_roe_br1", "gl7_split_pi_roeef_br2", "gauss5_weak_roeef", "gauss5_split_pi_roeef_br1",
-                                  "gauss3_split_sd_lf", "gl5_split_pi_roeef_br2"])
+                                  "gauss3_split_sd_lf", "gl5_split_pi_roeef_br2", "gauss11_weak_roeef_br1", "gl11_split_pi_roeef_br2"])
 def test_rhs_parity_curved(name):
     c = product_cfg(**RHS_CASES[name], **COMMON)
     f, o, _ = tgv_pair(c, n_elem=3, ngeo=3, perturb=0.2, seed=3)
@@ -91,7 +99,8 @@ def test_rhs_parity_channel_walls(variant):
     assert err <= UT_TOL, err
 
 
-@pytest.mark.parametrize("name", ["c1_gauss3_weak_roe_br1", "gl7_split_pi_roeef_br1", "gauss3_weak_br2", "gauss5_split_pi_roeef_br1"])
+@pytest.mark.parametrize("name", ["c1_gauss3_weak_roe_br1", "gl7_split_pi_roeef_br1", "gauss3_weak_br2", "gauss5_split_pi_roeef_br1",
+                                  "gauss11_weak_roeef_br1"])
 def test_lserk_steps_fixed_dt(name):
     c = product_cfg(**RHS_CASES[name], **COMMON)
     f, o, _ = tgv_pair(c, n_elem=3)
@@ -106,7 +115,7 @@ def test_lserk_steps_fixed_dt(name):
     assert abs(tf - to) < 1e-14 and e <= STATE_TOL, e
 
 
-@pytest.mark.parametrize("name", ["c1_gauss3_weak_roe_br1", "gl7_split_pi_roeef_br2"])
+@pytest.mark.parametrize("name", ["c1_gauss3_weak_roe_br1", "gl7_split_pi_roeef_br2", "gauss11_weak_roeef_br1"])
 def test_timedisc_dt_control(name):
     c = product_cfg(**RHS_CASES[name], **COMMON)
     f, o, _ = tgv_pair(c, n_elem=3)
