@@ -97,7 +97,32 @@ struct Config {
   double CFLScale = 0.9, DFLScale = 0.9;
   int doTCSource = 0;  // channel body force
   double dpdx = -1.;
+  int overintType = 0;  // overintegration.f90: 0 none, 1 modal cut-off of J u_t, 2 conservative cut-off
+  int NUnder = -1;      // cut-off degree (-1: N)
 };
+
+// changebasis.t90:ChangeBasisVolume on an element block X(nv, 0:Ni, 0:Ni, 0:Ni) -> (nv, 0:No, 0:No, 0:No),
+// V (No+1)x(Ni+1) row-major; xi, then eta, then zeta, each sum in increasing input index
+template <class R>
+void change_basis_volume(int nv, int Ni, int No, const std::vector<double>& V, const R* Xin, R* Xout) {
+  const int ni = Ni + 1, no = No + 1;
+  std::vector<R> t1((size_t)nv * no * ni * ni), t2((size_t)nv * no * no * ni);
+  for (int k = 0; k < ni; ++k) for (int j = 0; j < ni; ++j) for (int a = 0; a < no; ++a) for (int c = 0; c < nv; ++c) {
+    R acc = R(V[a * ni]) * Xin[(((size_t)k * ni + j) * ni + 0) * nv + c];
+    for (int i = 1; i < ni; ++i) acc = acc + R(V[a * ni + i]) * Xin[(((size_t)k * ni + j) * ni + i) * nv + c];
+    t1[(((size_t)k * ni + j) * no + a) * nv + c] = acc;
+  }
+  for (int k = 0; k < ni; ++k) for (int b = 0; b < no; ++b) for (int a = 0; a < no; ++a) for (int c = 0; c < nv; ++c) {
+    R acc = R(V[b * ni]) * t1[(((size_t)k * ni + 0) * no + a) * nv + c];
+    for (int j = 1; j < ni; ++j) acc = acc + R(V[b * ni + j]) * t1[(((size_t)k * ni + j) * no + a) * nv + c];
+    t2[(((size_t)k * no + b) * no + a) * nv + c] = acc;
+  }
+  for (int cc = 0; cc < no; ++cc) for (int b = 0; b < no; ++b) for (int a = 0; a < no; ++a) for (int c = 0; c < nv; ++c) {
+    R acc = R(V[cc * ni]) * t2[(((size_t)0 * no + b) * no + a) * nv + c];
+    for (int k = 1; k < ni; ++k) acc = acc + R(V[cc * ni + k]) * t2[(((size_t)k * no + b) * no + a) * nv + c];
+    Xout[(((size_t)cc * no + b) * no + a) * nv + c] = acc;
+  }
+}
 
 // lifting variables (PP_OPTLIFT=1 set): velocity and temperature. The lifted density gradient of the
 // default build never enters Ut for a constant viscosity, so Ut is identical.
@@ -190,6 +215,10 @@ struct DG {
   int nRKStages = 5;
   double CFLScaleEff = 0., DFLScaleEff = 0.;
   std::vector<double> MetricsAdv, MetricsVisc;
+  // overintegration (overintegration.f90:InitOverintegration): filter matrix (type 1), Vandermonde N->NUnder
+  // and NUnder->N and 1/J on NUnder (type 2)
+  std::vector<double> OverintegrationMat, Vdm_N_NUnder, Vdm_NUnder_N, sJNUnder;
+  int NU = 0;
 
   size_t vi(int v, int i, int j, int k, int e, int nv) const { return ((((size_t)e * n + k) * n + j) * n + i) * nv + v; }
   size_t si(int v, int p, int q, int s, int nv) const { return (((size_t)s * n + q) * n + p) * nv + v; }
@@ -205,6 +234,7 @@ struct DG {
     lambdaFac = val(cp) / C.Pr;  // THERMAL_CONDUCTIVITY_H(mu) = mu*cp/Pr
     s23 = 2. / 3.; s43 = 4. / 3.;
     if (C.etaBR2_wall == -1.) C.etaBR2_wall = C.etaBR2;
+    init_overintegration();
     const size_t nv3 = (size_t)n * n * n, ns2 = (size_t)n * n;
     U.assign(5 * nv3 * nE, R(0.)); Ut = U; Ut_tmp = U;
     UPrim.assign(6 * nv3 * nE, R(0.));
@@ -232,8 +262,12 @@ struct DG {
     static const double dflGL[10] = {4.50, 1.95, 1.18, 0.79, 0.56, 0.42, 0.32, 0.25, 0.20, 0.17};
     const double* ct = C.nodeType == NT_GL ? cflGL : cflG;
     const double* dtab = C.nodeType == NT_GL ? dflGL : dflG;
-    double alpha = ct[std::min(15, N) - 1];
-    CFLScaleEff = C.CFLScale * alpha / (2. * N + 1.);
+    // timedisc_func.f90:142-144: the CFL uses NEff = MIN(N, NUnder); with overintegration Gauss-Lobatto
+    // nodes take the Gauss table (timedisc_vars.f90:183-190)
+    if (C.overintType > 0) ct = cflG;
+    const int NEff = std::min(N, NU);
+    double alpha = ct[std::min(15, NEff) - 1];
+    CFLScaleEff = C.CFLScale * alpha / (2. * NEff + 1.);
     double RelativeDFL = 1.853;
     alpha = dtab[std::min(10, N) - 1] * RelativeDFL;
     DFLScaleEff = C.DFLScale * alpha / ((2. * N + 1.) * (2. * N + 1.));
@@ -248,6 +282,64 @@ struct DG {
         MetricsAdv[((size_t)e * nv3 + x) * 3 + d] = sj * nrm;
         double s2 = (mm[d][0] * sj) * (mm[d][0] * sj) + (mm[d][1] * sj) * (mm[d][1] * sj) + (mm[d][2] * sj) * (mm[d][2] * sj);
         MetricsVisc[((size_t)e * nv3 + x) * 3 + d] = KappasPr_max * s2;
+      }
+    }
+  }
+
+  // overintegration.f90:InitOverintegration
+  void init_overintegration() {
+    NU = C.NUnder < 0 ? N : C.NUnder;
+    if (C.overintType == 2 && !(NU < N)) C.overintType = 0;  // "Overintegration is disabled for NUnder >= N"
+    if (C.overintType == 1) {
+      // Vdm_Leg * diag(1 up to NUnder, 0 above) * sVdm_Leg
+      std::vector<double> V, sV;
+      legendre_vdm(N, B.xGP.data(), V, sV);
+      OverintegrationMat.assign((size_t)n * n, 0.);
+      for (int i = 0; i < n; ++i) for (int l = 0; l < n; ++l) {
+        double acc = 0.;
+        for (int m = 0; m <= std::min(NU, N); ++m) acc += V[i * n + m] * sV[m * n + l];
+        OverintegrationMat[i * n + l] = acc;
+      }
+    } else if (C.overintType == 2) {
+      const int nu = NU + 1;
+      Vdm_N_NUnder = get_vandermonde(N, C.nodeType, NU, C.nodeType, true);
+      Vdm_NUnder_N = get_vandermonde(NU, C.nodeType, N, C.nodeType, true);
+      const int NGR = M.NGeoRef, nr = NGR + 1;
+      auto V_Ref_NU = get_vandermonde(NGR, C.nodeType, NU, C.nodeType, true);
+      sJNUnder.assign((size_t)nu * nu * nu * nE, 0.);
+      std::vector<double> dNU((size_t)nu * nu * nu);
+      for (int e = 0; e < nE; ++e) {
+        change_basis_3d(1, NGR, NU, V_Ref_NU, &M.DetJac_Ref[(size_t)e * nr * nr * nr], dNU.data());
+        for (size_t x = 0; x < dNU.size(); ++x) sJNUnder[(size_t)e * dNU.size() + x] = 1. / dNU[x];
+      }
+    }
+  }
+  // overintegration.f90:FilterConservative on one element block (5, 0:N, 0:N, 0:N): J u -> u
+  void filter_conservative(R* u, int e) const {
+    const int nu = NU + 1;
+    const size_t nu3 = (size_t)nu * nu * nu;
+    std::vector<R> loc(5 * nu3);
+    change_basis_volume<R>(5, N, NU, Vdm_N_NUnder, u, loc.data());
+    for (size_t x = 0; x < nu3; ++x)
+      for (int v = 0; v < 5; ++v) loc[x * 5 + v] = loc[x * 5 + v] * R(sJNUnder[(size_t)e * nu3 + x]);
+    change_basis_volume<R>(5, NU, N, Vdm_NUnder_N, loc.data(), u);
+  }
+  // timedisc.f90:115-123, the overintegration of the state before the first time step (type 1: filter U;
+  // type 2: ApplyJacobianCons(toPhysical=.FALSE.), then FilterConservative)
+  void overintegrate_state() {
+    const size_t nv3 = (size_t)n * n * n;
+    if (C.overintType == 0) return;
+#pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
+    for (int e = 0; e < nE; ++e) {
+      R* u = &U[(size_t)e * nv3 * 5];
+      if (C.overintType == 1) {
+        std::vector<R> tmp(5 * nv3);
+        change_basis_volume<R>(5, N, N, OverintegrationMat, u, tmp.data());
+        std::copy(tmp.begin(), tmp.end(), u);
+      } else {
+        for (size_t x = 0; x < nv3; ++x)
+          for (int v = 0; v < 5; ++v) u[x * 5 + v] = u[x * 5 + v] / R(M.sJ[(size_t)e * nv3 + x]);
+        filter_conservative(u, e);
       }
     }
   }
@@ -932,20 +1024,32 @@ struct DG {
     else surf_int<5>(Flux_master, Flux_slave, Ut, R(-1.));
     // Ut = -Ut ; TestcaseSource (channel) ; ApplyJacobianCons
 #pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
-    for (int e = 0; e < nE; ++e) for (size_t x = 0; x < nv3; ++x) {
-      double sj = M.sJ[(size_t)e * nv3 + x];
-      R* ut = &Ut[((size_t)e * nv3 + x) * 5];
-      for (int v = 0; v < 5; ++v) ut[v] = -ut[v];
-      if (C.doTCSource) {
-        ut[1] = ut[1] - R(C.dpdx) / R(sj);
-        ut[4] = ut[4] - R(C.dpdx) / R(sj) * BulkVel;
+    for (int e = 0; e < nE; ++e) {
+      for (size_t x = 0; x < nv3; ++x) {
+        double sj = M.sJ[(size_t)e * nv3 + x];
+        R* ut = &Ut[((size_t)e * nv3 + x) * 5];
+        for (int v = 0; v < 5; ++v) ut[v] = -ut[v];
+        if (C.doTCSource) {
+          ut[1] = ut[1] - R(C.dpdx) / R(sj);
+          ut[4] = ut[4] - R(C.dpdx) / R(sj) * BulkVel;
+        }
+        if (!forceField.empty()) {
+          const R F = forceField[(size_t)e * nv3 + x];
+          ut[1] = ut[1] + F / R(sj);
+          ut[4] = ut[4] + F / R(sj) * BulkVel;
+        }
+        if (C.overintType == 0) for (int v = 0; v < 5; ++v) ut[v] = ut[v] * R(sj);
       }
-      if (!forceField.empty()) {
-        const R F = forceField[(size_t)e * nv3 + x];
-        ut[1] = ut[1] + F / R(sj);
-        ut[4] = ut[4] + F / R(sj) * BulkVel;
+      // dg.f90:663-675: overintegration, then ApplyJacobianCons (the conservative cut-off includes it)
+      R* ue = &Ut[(size_t)e * nv3 * 5];
+      if (C.overintType == 1) {
+        std::vector<R> tmp(5 * nv3);
+        change_basis_volume<R>(5, N, N, OverintegrationMat, ue, tmp.data());
+        for (size_t x = 0; x < nv3; ++x)
+          for (int v = 0; v < 5; ++v) ue[x * 5 + v] = tmp[x * 5 + v] * R(M.sJ[(size_t)e * nv3 + x]);
+      } else if (C.overintType == 2) {
+        filter_conservative(ue, e);
       }
-      for (int v = 0; v < 5; ++v) ut[v] = ut[v] * R(sj);
     }
     phase[5] = fc;
   }

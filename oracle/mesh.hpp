@@ -96,6 +96,10 @@ struct Mesh {
   // row NormalDir of the face metrics Ja_Face (master, flip 0) and Ja_slave (slave, its own flip), in side
   // orientation (3,0:N,0:N,nSides): used by the split-Gauss surface integral (surfint.t90:90-140)
   std::vector<double> JaN_master, JaN_slave;
+  // Jacobian determinant on the NGeoRef = 3 NGeo points of the solution node type (metrics.f90, DetJac_Ref),
+  // (0:NGeoRef,0:NGeoRef,0:NGeoRef,nElems): the conservative cut-off of overintegration.f90 projects it
+  std::vector<double> DetJac_Ref;
+  int NGeoRef = 0;
   std::vector<double> SurfElem;    // (0:N,0:N,nSides)
   std::vector<double> Elem_xGP;    // (3,0:N,0:N,0:N,nElems)
   double Vol = 0.;
@@ -219,6 +223,8 @@ inline void build_mesh(const MeshInput& in, int N, int nodeType, Mesh& M) {
   M.JaN_master = M.NormVec; M.JaN_slave = M.NormVec;
   M.SurfElem.assign(nsp * M.nSides, 0.);
   const int nr = NGeoRef + 1;
+  M.NGeoRef = NGeoRef;
+  M.DetJac_Ref.assign((size_t)nr * nr * nr * nE, 0.);
 
   for (int e = 0; e < nE; ++e) {
     const double* NC = &in.NodeCoords[(size_t)e * ng * ng * ng * 3];
@@ -247,6 +253,7 @@ inline void build_mesh(const MeshInput& in, int N, int nodeType, Mesh& M) {
                   dd(3, 1) * (dd(1, 2) * dd(2, 3) - dd(2, 2) * dd(1, 3));
     }
     change_basis_3d(1, NGeoRef, N, V_Ref_N, detRef.data(), detN.data());
+    std::copy(detRef.begin(), detRef.end(), M.DetJac_Ref.begin() + (size_t)e * nr * nr * nr);
     for (size_t x = 0; x < nv3; ++x) M.sJ[(size_t)e * nv3 + x] = 1. / detN[x];
     // dXCL_N
     std::vector<double> dX_N(nv3 * 9, 0.);

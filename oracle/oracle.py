@@ -23,7 +23,10 @@ class OrcConfig(ctypes.Structure):
                 ("lifting", ctypes.c_int), ("weakLifting", ctypes.c_int), ("consLifting", ctypes.c_int), ("splitDG", ctypes.c_int),
                 ("etaBR2", ctypes.c_double), ("etaBR2_wall", ctypes.c_double), ("kappa", ctypes.c_double), ("R", ctypes.c_double),
                 ("Pr", ctypes.c_double), ("mu0", ctypes.c_double), ("CFLScale", ctypes.c_double), ("DFLScale", ctypes.c_double),
-                ("doTCSource", ctypes.c_int), ("dpdx", ctypes.c_double)]
+                ("doTCSource", ctypes.c_int), ("dpdx", ctypes.c_double), ("overintType", ctypes.c_int), ("NUnder", ctypes.c_int)]
+
+# keys a configuration may leave out (defaults of the reference: no overintegration, NUnder = N)
+_OPTIONAL = {"overintType": 0, "NUnder": -1}
 
 
 def lib():
@@ -67,6 +70,7 @@ def lib():
         _lib.orc_prolong_unittest.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P]
         _lib.orc_surfint_unittest.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P]
         _lib.orc_surfint_split_unittest.argtypes = [ctypes.c_int, ctypes.c_int, P, P, P, P, P, P, P]
+        _lib.orc_overintegrate_state.argtypes = [P]
         _lib.orc_tgv_exact.argtypes = [ctypes.c_int, P, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int, P]
         _lib.orc_tgv_analysis.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P, P, P, ctypes.c_int,
                                           ctypes.c_double, ctypes.c_double, ctypes.c_double, P]
@@ -80,7 +84,7 @@ def _p(a):
 def make_config(cfg: dict) -> OrcConfig:
     c = OrcConfig()
     for name, _ in OrcConfig._fields_:
-        setattr(c, name, cfg[name])
+        setattr(c, name, cfg[name] if name in cfg else _OPTIONAL[name])
     return c
 
 
@@ -231,6 +235,10 @@ class Oracle:
         for d in range(3):
             lib().orc_get_gradients(self.h, d, _p(g[d]))
         return g
+
+    def overintegrate_state(self):
+        """timedisc.f90:115-123: the overintegration of U before the first time step."""
+        lib().orc_overintegrate_state(self.h)
 
     def flops_per_dof_stage(self):
         return lib().orc_flops_per_dof_stage(self.h)

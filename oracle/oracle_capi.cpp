@@ -15,6 +15,7 @@ struct orc_config {
   double etaBR2, etaBR2_wall, kappa, R, Pr, mu0, CFLScale, DFLScale;
   int doTCSource;
   double dpdx;
+  int overintType, NUnder;
 };
 
 static Config to_cfg(const orc_config* c) {
@@ -23,6 +24,7 @@ static Config to_cfg(const orc_config* c) {
   C.lifting = c->lifting; C.weakLifting = c->weakLifting; C.consLifting = c->consLifting; C.splitDG = c->splitDG;
   C.etaBR2 = c->etaBR2; C.etaBR2_wall = c->etaBR2_wall; C.kappa = c->kappa; C.R = c->R; C.Pr = c->Pr; C.mu0 = c->mu0;
   C.CFLScale = c->CFLScale; C.DFLScale = c->DFLScale; C.doTCSource = c->doTCSource; C.dpdx = c->dpdx;
+  C.overintType = c->overintType; C.NUnder = c->NUnder;
   return C;
 }
 
@@ -92,6 +94,8 @@ int orc_timestep(void* hp, double* t, double dt) {
   return 0;
 }
 double orc_calc_timestep(void* hp, int* err) { return ((OrcHandle*)hp)->dg.calc_timestep(*err); }
+// timedisc.f90:115-123: overintegration of the state before the first time step
+void orc_overintegrate_state(void* hp) { ((OrcHandle*)hp)->dg.overintegrate_state(); }
 
 // additional per-node x-momentum body force, layout of U without the variable index (NULL: none)
 void orc_set_force_field(void* hp, const double* F) {

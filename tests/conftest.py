@@ -30,3 +30,10 @@ def tgv_splitgauss_reference():
     import numpy as np
     d = np.load(os.path.join(ROOT, "tests", "golden", "tgv_splitgauss_reference.npz"))
     return d["header"], d["rows"]
+
+
+@pytest.fixture(scope="session")
+def tgv_oint_reference():
+    import numpy as np
+    d = np.load(os.path.join(ROOT, "tests", "golden", "tgv_oint_reference.npz"))
+    return d["header"], d["rows"]

@@ -2,9 +2,9 @@
 
 Reads FLEXI v25.10's unit-test data (unitTests/*.bin, Fortran unformatted sequential records:
 4-byte length marker, little-endian payload, closing marker) and the Taylor-Green regression
-references (regressioncheck/checks/tgv/{split,splitGauss}/TGV_Re1600_Split_TGVAnalysis_Reference.csv),
-and stores the arrays the parity tests need in reference_unittests.npz, tgv_split_reference.npz and
-tgv_splitgauss_reference.npz.
+references (regressioncheck/checks/tgv/{split,splitGauss,oInt}/TGV_Re1600_*_TGVAnalysis_Reference.csv),
+and stores the arrays the parity tests need in reference_unittests.npz, tgv_split_reference.npz,
+tgv_splitgauss_reference.npz and tgv_oint_reference.npz.
 
 Run from the repository root in a container that has the reference mounted:
     python tests/golden/make_golden.py /root/reference
@@ -83,8 +83,10 @@ def main(ref):
     np.savez_compressed(os.path.join(os.path.dirname(__file__), "reference_unittests.npz"), **out)
 
     # tgv/split (Gauss-Lobatto, N=7) and tgv/splitGauss (Gauss, N=5, entropy-variable prolongation)
-    for case, name in (("split", "tgv_split_reference.npz"), ("splitGauss", "tgv_splitgauss_reference.npz")):
-        csv = os.path.join(ref, f"regressioncheck/checks/tgv/{case}/TGV_Re1600_Split_TGVAnalysis_Reference.csv")
+    for case, name, fname in (("split", "tgv_split_reference.npz", "TGV_Re1600_Split_TGVAnalysis_Reference.csv"),
+                              ("splitGauss", "tgv_splitgauss_reference.npz", "TGV_Re1600_Split_TGVAnalysis_Reference.csv"),
+                              ("oInt", "tgv_oint_reference.npz", "TGV_Re1600_OInt_TGVAnalysis_Reference.csv")):
+        csv = os.path.join(ref, f"regressioncheck/checks/tgv/{case}/{fname}")
         lines = open(csv).read().strip().splitlines()
         header = [h.strip() for h in lines[0].split(",")]
         rows = np.array([[float(v) for v in ln.split(",")] for ln in lines[1:]])

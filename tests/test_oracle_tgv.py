@@ -1,7 +1,8 @@
 """End-to-end pin of the CPU oracle: FLEXI's Taylor-Green regression references
 regressioncheck/checks/tgv/split (GL N=7) and tgv/splitGauss (Gauss N=5: split form with
 entropy-variable prolongation and the split-Gauss surface integral), both split PI, RoeEntropyFix, BR1,
-8^3 periodic, CFL=DFL=0.8, Re=1600, Ma=0.1, R=71.42857. Their TGVAnalysis CSV rows are written every 10
+8^3 periodic, CFL=DFL=0.8, and tgv/oInt (Gauss N=11, weak form, overintegration by the modal cut-off
+filter to NUnder=7, 4^3, CFL=DFL=0.9), all at Re=1600, Ma=0.1, R=71.42857. Their TGVAnalysis CSV rows are written every 10
 steps and compared by the reference at 1e-4 relative (analyze.ini). Checks the t=0 row and the first rows
 after stepping with the reference's time-step control (UpdateTimeStep/CALCTIMESTEP), including the time
 column."""
@@ -16,7 +17,10 @@ TGV_CFG = dict(N=7, nodeType=orc.NT_GL, riemann=33, riemannBC=-1, lifting=1, wea
                doTCSource=0, dpdx=-1.0)
 TGV_GAUSS_CFG = dict(TGV_CFG, N=5, nodeType=orc.NT_GAUSS)
 REL = 1e-4
-CASES = {"split": ("tgv_reference", TGV_CFG), "splitGauss": ("tgv_splitgauss_reference", TGV_GAUSS_CFG)}
+# tgv/oInt: N=11 Gauss, weak form, overintegration by the modal cut-off filter to NUnder=7, 4^3, CFL=DFL=0.9
+TGV_OINT_CFG = dict(TGV_CFG, N=11, nodeType=orc.NT_GAUSS, splitDG=-1, CFLScale=0.9, DFLScale=0.9, overintType=1, NUnder=7)
+CASES = {"split": ("tgv_reference", TGV_CFG, 8), "splitGauss": ("tgv_splitgauss_reference", TGV_GAUSS_CFG, 8),
+         "oInt": ("tgv_oint_reference", TGV_OINT_CFG, 4)}
 
 
 def tgv_oracle(n=8, cfg=TGV_CFG):
@@ -24,6 +28,7 @@ def tgv_oracle(n=8, cfg=TGV_CFG):
     o = orc.Oracle(cfg, m)
     x = o.mesh_array("Elem_xGP")
     o.set_state(orc.tgv_exact(x, mach=0.1, kappa=cfg["kappa"], R=cfg["R"]))
+    o.overintegrate_state()  # timedisc.f90:115-123 (no-op without overintegration)
     return o
 
 
@@ -43,9 +48,9 @@ def compare_row(row, ref, scale):
 
 @pytest.mark.parametrize("case", list(CASES))
 def test_tgv_t0_row(case, request):
-    fixture, cfg = CASES[case]
+    fixture, cfg, ne = CASES[case]
     _, rows = request.getfixturevalue(fixture)
-    o = tgv_oracle(cfg=cfg)
+    o = tgv_oracle(ne, cfg=cfg)
     o.time_derivative(0.0)
     a = analysis(o, cfg)
     scale = np.abs(rows[:, 1:]).max(axis=0)
@@ -55,9 +60,9 @@ def test_tgv_t0_row(case, request):
 @pytest.mark.timeout(900)
 @pytest.mark.parametrize("case", list(CASES))
 def test_tgv_first_rows(case, request):
-    fixture, cfg = CASES[case]
+    fixture, cfg, ne = CASES[case]
     _, rows = request.getfixturevalue(fixture)
-    o = tgv_oracle(cfg=cfg)
+    o = tgv_oracle(ne, cfg=cfg)
     scale = np.abs(rows[:, 1:]).max(axis=0)
     t = 0.0
     o.time_derivative(0.0)
