@@ -12,10 +12,11 @@ class FgConfig(ctypes.Structure):
                 ("Lifting", ctypes.c_int), ("doWeakLifting", ctypes.c_int), ("doConservativeLifting", ctypes.c_int),
                 ("SplitDG", ctypes.c_int), ("etaBR2", ctypes.c_double), ("etaBR2_wall", ctypes.c_double), ("kappa", ctypes.c_double),
                 ("R", ctypes.c_double), ("Pr", ctypes.c_double), ("mu0", ctypes.c_double), ("CFLScale", ctypes.c_double),
-                ("DFLScale", ctypes.c_double), ("doTCSource", ctypes.c_int), ("dpdx", ctypes.c_double), ("TimeDiscMethod", ctypes.c_int)]
+                ("DFLScale", ctypes.c_double), ("doTCSource", ctypes.c_int), ("dpdx", ctypes.c_double), ("TimeDiscMethod", ctypes.c_int),
+                ("OverintegrationType", ctypes.c_int), ("NUnder", ctypes.c_int)]
 
 
-EXPORTS = ["fg_config_default", "fg_config_from_ini", "fg_create", "fg_destroy", "fg_last_error", "fg_build_mesh", "fg_set_mesh", "fg_set_face_metrics",
+EXPORTS = ["fg_config_default", "fg_config_from_ini", "fg_create", "fg_destroy", "fg_last_error", "fg_build_mesh", "fg_set_mesh", "fg_set_face_metrics", "fg_overintegrate_state",
            "fg_set_instance_mu0", "fg_get_elem_xgp", "fg_get_sizes", "fg_get_mesh_array", "fg_get_side_to_elem", "fg_set_state",
            "fg_get_state", "fg_state_device_ptr", "fg_time_derivative", "fg_calc_timestep", "fg_get_dt_elem", "fg_timestep_lserkw2", "fg_run",
            "fg_get_gradients", "fg_get_stream", "fg_launch_count", "fg_debug_array", "fg_profile_enable", "fg_profile_read", "fg_probe_fp64",
@@ -52,6 +53,7 @@ def load(path=None):
     L.fg_build_mesh.argtypes = [P, I, I, P, P, I, P, I, P, P]
     L.fg_set_mesh.argtypes = [P, I, I, I, P, P, P, I, P, I, P, P, P, P, P, P, P, P, P]
     L.fg_set_face_metrics.argtypes = [P, P, P]
+    L.fg_overintegrate_state.argtypes = [P]
     L.fg_set_instance_mu0.argtypes = [P, I, P]
     L.fg_get_elem_xgp.argtypes = [P, P]
     L.fg_get_sizes.argtypes = [P, P]

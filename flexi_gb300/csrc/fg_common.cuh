@@ -78,6 +78,16 @@ struct Dev {
   double* dtElem;  // [2][nElems] convective and viscous element time-step limits of the last CALCTIMESTEP
 };
 
+// Overintegration (overintegration.f90): type 1 the modal cut-off filter F = Vdm_Leg diag(1..1,0..0) sVdm_Leg
+// on J u_t; type 2 the conservative cut-off (project J u_t to NUnder, times 1/J on NUnder, back to N).
+struct OverintDev {
+  int type, nu;         // 0/1/2, NUnder + 1
+  const double* F;      // [n][n]: F[i*n+l] = OverintegrationMat(i,l)
+  const double* VNU;    // [nu][n]: Vdm_N_NUnder(iU,i)
+  const double* VUN;    // [n][nu]: Vdm_NUnder_N(i,iU)
+  const double* sJNU;   // [e][nu^3]: 1/J on the NUnder nodes
+};
+
 // viscosity of element e: its instance's mu0 times its multiplier
 __host__ __device__ inline double elem_mu(const Dev& d, int e) {
   const double m = d.mu0[d.elemInst[e]];

@@ -226,6 +226,9 @@ struct fg_handle {
   double* dStage = nullptr;  // staging for layout conversion (size nElems*5*n3)
   double RKA[6]{}, RKb[6]{}, RKc[6]{};
   double cflEff = 0., dflEff = 0.;
+  // overintegration in use (type 2 is off when NUnder >= N, overintegration.f90:139-141) and its matrices
+  OverintDev ov{};
+  int NU = 0;
   cudaGraphExec_t graph = nullptr;
   long long launches = 0;
   std::string err;
@@ -390,8 +393,18 @@ void init_basis(fg_handle* h) {
   // non-literal subscript mis-compiles with the host compiler in use here (g++ 13 returns 0)
   const double* cflTab = gl ? cflGL : cflG;
   const double* dflTab = gl ? dflGL : dflG;
-  const int iC = (N < 15 ? N : 15) - 1, iD = (N < 10 ? N : 10) - 1;
-  h->cflEff = c.CFLScale * cflTab[iC] / (2. * N + 1.);
+  // overintegration (overintegration.f90:99-141): NUnder defaults to N; the conservative cut-off is off
+  // for NUnder >= N; the CFL uses NEff = MIN(N, NUnder) (timedisc_func.f90:142-144), and Gauss-Lobatto
+  // nodes take the Gauss table (timedisc_vars.f90:183-190)
+  h->NU = c.NUnder < 0 ? N : c.NUnder;
+  h->ov = OverintDev{};
+  h->ov.type = c.OverintegrationType;
+  if (h->ov.type == 2 && !(h->NU < N)) h->ov.type = 0;
+  h->ov.nu = (h->NU < N ? h->NU : N) + 1;
+  if (h->ov.type > 0) cflTab = cflG;
+  const int NEff = h->NU < N ? h->NU : N;
+  const int iC = (NEff < 15 ? NEff : 15) - 1, iD = (N < 10 ? N : 10) - 1;
+  h->cflEff = c.CFLScale * cflTab[iC] / (2. * NEff + 1.);
   h->dflEff = c.DFLScale * dflTab[iD] * 1.853 / ((2. * N + 1.) * (2. * N + 1.));
 }
 
@@ -453,6 +466,61 @@ int upload_mesh(fg_handle* h) {
   if ((r = upload(h, h->dMetAdv, M.metAdv))) return r;
   if ((r = upload(h, h->dMetVisc, M.metVisc))) return r;
   if ((r = upload(h, h->dWVol, M.wVol))) return r;
+  if (h->ov.type > 0) {
+    // overintegration.f90:InitOverintegration
+    const int N = M.N, nu = h->ov.nu, NU = nu - 1;
+    const int type = M.nodeType;
+    fgh::Vec x, w;
+    fgh::nodes(N, type, x, w);
+    if (h->ov.type == 1) {
+      fgh::Mat V(n, n);
+      double dL;
+      for (int i = 0; i < n; ++i) for (int m = 0; m < n; ++m) fgh::legendre(m, x[i], V(i, m), dL);
+      const fgh::Mat sV = fgh::inverse(V);
+      std::vector<double> F((size_t)n * n, 0.);
+      for (int i = 0; i < n; ++i)
+        for (int l = 0; l < n; ++l) {
+          double acc = 0.;
+          for (int m = 0; m < nu; ++m) acc += V(i, m) * sV(m, l);
+          F[(size_t)i * n + l] = acc;
+        }
+      double* dF = nullptr;
+      if ((r = upload(h, dF, F))) return r;
+      h->ov.F = dF;
+    } else {
+      const fgh::Mat Vd = fgh::vandermonde(N, type, NU, type, true), Vu = fgh::vandermonde(NU, type, N, type, true);
+      std::vector<double> VNU((size_t)nu * n), VUN((size_t)n * nu);
+      for (int a = 0; a < nu; ++a) for (int i = 0; i < n; ++i) VNU[(size_t)a * n + i] = Vd(a, i);
+      for (int i = 0; i < n; ++i) for (int a = 0; a < nu; ++a) VUN[(size_t)i * nu + a] = Vu(i, a);
+      // 1/J on NUnder: the modal projection of J = 1/sJ (equal to the projection of DetJac_Ref that
+      // overintegration.f90:129-137 forms, up to round-off: both keep the Legendre modes up to NUnder)
+      const int nu3 = nu * nu * nu;
+      std::vector<double> sJNU((size_t)nE * nu3), t1((size_t)nu * n2), t2((size_t)nu * nu * n);
+      for (int e = 0; e < nE; ++e) {
+        const double* sj = &M.sJ[(size_t)e * n3];
+        for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int a = 0; a < nu; ++a) {
+          double acc = 0.;
+          for (int i = 0; i < n; ++i) acc += VNU[(size_t)a * n + i] / sj[i + n * (j + n * k)];
+          t1[a + nu * (j + n * k)] = acc;
+        }
+        for (int k = 0; k < n; ++k) for (int b = 0; b < nu; ++b) for (int a = 0; a < nu; ++a) {
+          double acc = 0.;
+          for (int j = 0; j < n; ++j) acc += VNU[(size_t)b * n + j] * t1[a + nu * (j + n * k)];
+          t2[a + nu * (b + nu * k)] = acc;
+        }
+        for (int c = 0; c < nu; ++c) for (int b = 0; b < nu; ++b) for (int a = 0; a < nu; ++a) {
+          double acc = 0.;
+          for (int k = 0; k < n; ++k) acc += VNU[(size_t)c * n + k] * t2[a + nu * (b + nu * k)];
+          sJNU[(size_t)e * nu3 + a + nu * (b + nu * c)] = 1. / acc;
+        }
+      }
+      double *dV = nullptr, *dW = nullptr, *dS = nullptr;
+      if ((r = upload(h, dV, VNU))) return r;
+      if ((r = upload(h, dW, VUN))) return r;
+      if ((r = upload(h, dS, sJNU))) return r;
+      h->ov.VNU = dV; h->ov.VUN = dW; h->ov.sJNU = dS;
+    }
+  }
   if ((r = dalloc(h, h->dBulkPart, (size_t)nE))) return r;
   // instances must be contiguous element ranges
   std::vector<int> start(M.nInst + 1, 0);
@@ -500,8 +568,11 @@ void launch_rhs_dev(fg_handle* h, const Dev& d, int mode, double rkA, double rkB
   { ProfScope p(h, 2); h->K.flux_block(d, h->B, h->K.fluxBlock, h->st); }
   {
     ProfScope p(h, 3);
-    if (h->cfg.SplitDG >= 0) h->K.vol_split(d, h->B, mode, rkA, rkB, h->st);
-    else h->K.vol_weak(d, h->B, mode, rkA, rkB, h->st);
+    // with overintegration the volume kernel writes Ut and k_overint filters it and updates the registers
+    const bool oi = h->ov.type > 0;
+    if (h->cfg.SplitDG >= 0) h->K.vol_split(d, h->B, oi ? 0 : mode, rkA, rkB, h->st);
+    else h->K.vol_weak(d, h->B, oi ? 0 : mode, rkA, rkB, h->st);
+    if (oi) { h->K.overint(d, h->ov, mode, rkA, rkB, 0, h->st); h->launches += 1; }
   }
   h->launches += 4;
 }
@@ -567,6 +638,7 @@ namespace {
 // the adjoint kernels cover: weak form and split form PI, LF/Roe/RoeEntropyFix, BR1/BR2
 const char* adjoint_unsupported(const fg_config& c) {
   if (c.N > 7) return "the adjoint supports N = 1..7";
+  if (c.OverintegrationType != 0) return "the adjoint does not support overintegration";
   if (c.SplitDG != FG_SPLIT_NONE && c.SplitDG != FG_SPLIT_PI) return "the adjoint supports the weak form and the split form PI";
   if (c.SplitDG != FG_SPLIT_NONE && (c.NodeType != FG_NODE_GAUSS_LOBATTO || (c.N != 1 && c.N != 3 && c.N != 7)))
     return "the adjoint of the split form supports Gauss-Lobatto nodes with N = 1, 3, 7";
@@ -644,6 +716,7 @@ int fg_config_default(fg_config* c) {
   c->Lifting = 1; c->doWeakLifting = 0; c->doConservativeLifting = 0; c->SplitDG = FG_SPLIT_PI;
   c->etaBR2 = 2.; c->etaBR2_wall = -1.; c->kappa = 1.4; c->R = 287.058; c->Pr = 0.72; c->mu0 = 0.;
   c->CFLScale = 0.9; c->DFLScale = 0.9; c->doTCSource = 0; c->dpdx = -1.; c->TimeDiscMethod = 0;
+  c->OverintegrationType = 0; c->NUnder = -1;
   return FG_OK;
 }
 
@@ -686,6 +759,12 @@ int fg_config_from_ini(const char* text, fg_config* c) {
       else if (key == "cflscale") c->CFLScale = std::stod(val);
       else if (key == "dflscale") c->DFLScale = std::stod(val);
       else if (key == "timediscmethod") c->TimeDiscMethod = (lv == "carpenterrk4-5") ? 0 : -1;
+      else if (key == "overintegrationtype") {
+        if (lv == "none") c->OverintegrationType = 0;
+        else if (lv == "cutoff") c->OverintegrationType = 1;
+        else if (lv == "conscutoff") c->OverintegrationType = 2;
+        else c->OverintegrationType = std::stoi(val);
+      } else if (key == "nunder") c->NUnder = std::stoi(val);
     } catch (...) {
       return FG_ERR_CONFIG;
     }
@@ -709,6 +788,8 @@ int fg_create(const fg_config* cfg, fg_handle** out) {
   else if (c.doWeakLifting) why = "doWeakLifting is not supported (the volume part needs the conservative form)";
   else if (c.SplitDG != FG_SPLIT_NONE && c.SplitDG != FG_SPLIT_SD && c.SplitDG != FG_SPLIT_PI) why = "SplitDG must be -1 (weak), 0 (SD) or 4 (PI)";
   else if (c.TimeDiscMethod != 0) why = "TimeDiscMethod must be CarpenterRK4-5";
+  else if (c.OverintegrationType < 0 || c.OverintegrationType > 2) why = "OverintegrationType must be 0 (none), 1 (cutoff) or 2 (conscutoff)";
+  else if (c.OverintegrationType > 0 && c.NUnder < -1) why = "NUnder must be >= 0";
   if (!why.empty()) { delete h; return fail(nullptr, FG_ERR_CONFIG, why); }
   h->K = get_kernel_set(c.N + 1, c.NodeType == FG_NODE_GAUSS_LOBATTO);
   h->Kdef = h->K;
@@ -777,6 +858,15 @@ int fg_set_face_metrics(fg_handle* h, const double* Ja_Face, const double* Ja_sl
     }
   if (h->haveMesh && h->d.faceJa)
     CUDA_TRY(cudaMemcpy(h->d.faceJa, M.faceJa.data(), sizeof(double) * M.faceJa.size(), cudaMemcpyHostToDevice));
+  return FG_OK;
+}
+
+int fg_overintegrate_state(fg_handle* h) {
+  if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "fg_overintegrate_state needs a mesh");
+  if (h->ov.type == 0) return FG_OK;
+  h->K.overint(h->d, h->ov, 0, 0., 0., 1, h->st);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(h->st));
   return FG_OK;
 }
 

@@ -64,6 +64,7 @@ struct Inst {
     set_smem(k_vol_weak<n, GL>, smem_weak());
     if constexpr (SPLIT_POW2) set_smem(k_vol_split<n>, smem_split());
     else set_smem(k_vol_split_gen<n, GL>, smem_split_gen());
+    set_smem(k_overint<n>, smem_overint());
     if constexpr (ADJ) {
       set_smem(k_vol_weak_adj<n, GL>, smem_weak_adj());
       set_smem(k_lift_adj<n, GL>, smem_lift_adj());
@@ -114,6 +115,10 @@ struct Inst {
     if constexpr (SPLIT_POW2) k_vol_split<n><<<blocks(d), S::THREADS, smem_split(), st>>>(d, B, Stage{mode, rkA, rkB});
     else k_vol_split_gen<n, GL><<<blocks(d), SplitShape<n>::THREADS, smem_split_gen(), st>>>(d, B, Stage{mode, rkA, rkB});
   }
+  static size_t smem_overint() { return sizeof(double) * (10 * S::n3 + 2 * S::n2); }
+  static void overint(const Dev& d, const OverintDev& o, int mode, double rkA, double rkB, int state, cudaStream_t st) {
+    k_overint<n><<<d.nElems, OverintShape<n>::THREADS, smem_overint(), st>>>(d, o, Stage{mode, rkA, rkB}, state);
+  }
   static void dt(const Dev& d, const Basis& B, const double* ma, const double* mv, double cfl, double dfl, double* bulk, const double* wv,
                  cudaStream_t st) {
     k_dt<n><<<blocks(d), S::THREADS, 0, st>>>(d, B, ma, mv, cfl, dfl, bulk, wv);
@@ -124,6 +129,7 @@ struct Inst {
     k.prepare = &prepare;
     k.prep = &prep; k.lift = &lift; k.flux = &flux; k.vol_weak = &vol_weak; k.dt = &dt;
     k.vol_split = &vol_split;
+    k.overint = &overint;
     if constexpr (ADJ) { k.vol_adj = &vol_adj; k.flux_adj = &flux_adj; k.lift_adj = &lift_adj; k.prep_adj = &prep_adj; }
     k.defEPB = S::EPB;
     k.scratchPerBlock = SCRATCH_PER_BLOCK;

@@ -1097,6 +1097,100 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
 }
 
 // =====================================================================================================
+// k_overint: overintegration.f90 -- dg.f90:663-675 after the volume kernel has written Ut (mode 0):
+// J u_t = Ut / sJ is filtered (type 1: OverintegrationMat in xi, eta, zeta, then ApplyJacobianCons;
+// type 2: FilterConservative, whose result is u_t), then the LSERK register update of the stage.
+// With state = 1 it is the overintegration of U before the first time step (timedisc.f90:115-123: type 1
+// filters U, type 2 applies FilterConservative to J U). One CTA per element, both buffers in shared memory.
+// =====================================================================================================
+template <int n> struct OverintShape {
+  static constexpr int n3 = n * n * n;
+  static constexpr int T = ((n3 + 31) / 32) * 32;
+  static constexpr int THREADS = T < 64 ? 64 : (T > 512 ? 512 : T);
+};
+
+// one ChangeBasis sweep along axis ax of X(5, d0, d1, d2) -> Y with extent nout along ax; M row a holds the
+// weights of output index a (leading dimension ldm)
+__device__ __forceinline__ void overint_sweep(const double* X, double* Y, const double* M, int ldm, int ax, int d0, int d1, int d2,
+                                              int nout) {
+  const int o0 = ax == 0 ? nout : d0, o1 = ax == 1 ? nout : d1, o2 = ax == 2 ? nout : d2;
+  const int On = o0 * o1 * o2, In = d0 * d1 * d2;
+  const int nin = ax == 0 ? d0 : (ax == 1 ? d1 : d2);
+  const int sIn = ax == 0 ? 1 : (ax == 1 ? d0 : d0 * d1);
+  for (int t = threadIdx.x; t < 5 * On; t += blockDim.x) {
+    const int v = t / On, r = t - v * On;
+    const int i = r % o0, j = (r / o0) % o1, k = r / (o0 * o1);
+    const int a = ax == 0 ? i : (ax == 1 ? j : k);
+    const int base = v * In + (ax == 0 ? 0 : i) + d0 * ((ax == 1 ? 0 : j) + d1 * (ax == 2 ? 0 : k));
+    const double* m = M + a * ldm;
+    double acc = m[0] * X[base];
+    for (int l = 1; l < nin; ++l) acc = fma(m[l], X[base + l * sIn], acc);
+    Y[v * On + r] = acc;
+  }
+  __syncthreads();
+}
+
+template <int n>
+__global__ void __launch_bounds__(OverintShape<n>::THREADS) k_overint(Dev d, OverintDev o, Stage st, int state) {
+  constexpr int n3 = n * n * n;
+  extern __shared__ double smem[];
+  double* A = smem;           // [5][n3]
+  double* Bf = A + 5 * n3;    // [5][n3]
+  double* sM = Bf + 5 * n3;   // type 1: F [n][n]; type 2: VNU [nu][n], VUN [n][nu]
+  const int e = blockIdx.x;
+  const int nu = o.nu;
+  if (o.type == 1) {
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) sM[t] = o.F[t];
+  } else {
+    for (int t = threadIdx.x; t < nu * n; t += blockDim.x) { sM[t] = o.VNU[t]; sM[nu * n + t] = o.VUN[t]; }
+  }
+  const double* src = state ? d.U : d.Ut;
+  const bool toRef = !(state && o.type == 1);  // J u = u / sJ, except for the state filter of type 1
+  for (int t = threadIdx.x; t < 5 * n3; t += blockDim.x) {
+    const int v = t / n3, x = t - v * n3;
+    const double val = src[((size_t)e * 5 + v) * n3 + x];
+    A[t] = toRef ? val / d.sJ[(size_t)e * n3 + x] : val;
+  }
+  __syncthreads();
+  const double* R;
+  if (o.type == 1) {
+    overint_sweep(A, Bf, sM, n, 0, n, n, n, n);
+    overint_sweep(Bf, A, sM, n, 1, n, n, n, n);
+    overint_sweep(A, Bf, sM, n, 2, n, n, n, n);
+    R = Bf;
+  } else {
+    const double* V = sM;
+    const double* W = sM + nu * n;
+    overint_sweep(A, Bf, V, n, 0, n, n, n, nu);
+    overint_sweep(Bf, A, V, n, 1, nu, n, n, nu);
+    overint_sweep(A, Bf, V, n, 2, nu, nu, n, nu);
+    const int nu3 = nu * nu * nu;
+    for (int t = threadIdx.x; t < 5 * nu3; t += blockDim.x) {
+      const int r = t % nu3;
+      Bf[t] *= o.sJNU[(size_t)e * nu3 + r];
+    }
+    __syncthreads();
+    overint_sweep(Bf, A, W, nu, 0, nu, nu, nu, n);
+    overint_sweep(A, Bf, W, nu, 1, n, nu, nu, n);
+    overint_sweep(Bf, A, W, nu, 2, n, n, nu, n);
+    R = A;
+  }
+  const int inst = d.elemInst[e];
+  const double bdt = st.rkB * d.dt[inst];
+  for (int t = threadIdx.x; t < 5 * n3; t += blockDim.x) {
+    const int x = t % n3;
+    const size_t g = (size_t)e * 5 * n3 + t;
+    double r = R[t];
+    if (o.type == 1 && !state) r *= d.sJ[(size_t)e * n3 + x];  // ApplyJacobianCons
+    if (state) { d.U[g] = r; continue; }
+    if (st.mode == 0) { d.Ut[g] = r; continue; }
+    if (st.mode == 2) r = fma(-st.rkA, d.Ut_tmp[g], r);
+    d.Ut_tmp[g] = r;
+    d.U[g] = fma(bdt, r, d.U[g]);
+  }
+}
+
+// =====================================================================================================
 // k_dt: calctimestep.f90:CALCTIMESTEP per element (convective and viscous eigenvalue bounds with the
 // precomputed MetricsAdv / MetricsVisc), reduced per instance with an atomic minimum on the bit pattern
 // of the (positive) time step; plus the channel bulk velocity partial sums (testcase.f90:CalcForcing).

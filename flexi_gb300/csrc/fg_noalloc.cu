@@ -192,6 +192,7 @@ void prepare_all_sets() {
 
 bool config_ok(const fg_config& c) {
   if (c.N < 1 || c.N > 7) return false;
+  if (c.OverintegrationType != 0) return false;
   if (c.NodeType != FG_NODE_GAUSS && c.NodeType != FG_NODE_GAUSS_LOBATTO) return false;
   if (c.Riemann != FG_RIEMANN_LF && c.Riemann != FG_RIEMANN_HLLC && c.Riemann != FG_RIEMANN_ROE && c.Riemann != FG_RIEMANN_ROEENTROPYFIX) return false;
   if (c.Lifting != 1 && c.Lifting != 2) return false;
@@ -210,7 +211,7 @@ extern "C" int fg_time_derivative_noalloc(const fg_config* cfg, const fg_device_
   if (!cfg || !mesh) return reject(FG_ERR_CONFIG, "fg_time_derivative_noalloc: null config or mesh");
   if (!config_ok(*cfg))
     return reject(FG_ERR_CONFIG, "fg_time_derivative_noalloc: unsupported configuration (N 1..7, strong non-conservative "
-                                 "lifting, no body force; split form only on Gauss-Lobatto nodes with N in {1,3,7})");
+                                 "lifting, no body force, no overintegration; split form only on Gauss-Lobatto nodes with N in {1,3,7})");
   const long long n = cfg->N + 1, n2 = n * n, n3 = n2 * n;
   const long long nE = mesh->nElems, nS = mesh->nSides;
   if (nE <= 0 || nS <= 0 || mesh->nBCSides < 0 || mesh->nBCSides > nS)

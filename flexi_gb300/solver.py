@@ -44,6 +44,8 @@ def make_config(**kw) -> _lib.FgConfig:
             v = SPLIT[v.lower()]
         elif k == "Lifting" and isinstance(v, str):
             v = {"br1": 1, "br2": 2}[v.lower()]
+        elif k == "OverintegrationType" and isinstance(v, str):
+            v = {"none": 0, "cutoff": 1, "conscutoff": 2}[v.lower()]
         if not hasattr(c, k):
             raise KeyError(k)
         setattr(c, k, type(getattr(c, k))(v))
@@ -130,6 +132,10 @@ class Flexi:
         a = np.ascontiguousarray(Ja_Face, np.float64)
         b = np.ascontiguousarray(Ja_slave, np.float64)
         self._check(self.L.fg_set_face_metrics(self.h, _p(a), _p(b)), "fg_set_face_metrics")
+
+    def overintegrate_state(self):
+        """timedisc.f90:115-123: the overintegration of U before the first time step (no-op without it)."""
+        self._check(self.L.fg_overintegrate_state(self.h), "fg_overintegrate_state")
 
     def _sizes(self):
         s = np.zeros(5, np.int32)

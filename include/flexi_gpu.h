@@ -66,17 +66,19 @@ typedef struct fg_config {
   int doTCSource;
   double dpdx;
   int TimeDiscMethod;
+  int OverintegrationType;  /* overintegration.f90: 0 none, 1 cut-off filter of J u_t, 2 conservative cut-off */
+  int NUnder;               /* filter degree of OverintegrationType 1/2 (-1: N) */
 } fg_config;
 
 typedef struct fg_handle fg_handle;
 
 /* Defaults of the reference (Riemann=RoeEntropyFix, SplitDG=PI, Lifting=BR1, etaBR2=2, kappa=1.4,
- * R=287.058, Pr=0.72, mu0=0, CFLScale=DFLScale=0.9, CarpenterRK4-5). */
+ * R=287.058, Pr=0.72, mu0=0, CFLScale=DFLScale=0.9, CarpenterRK4-5, no overintegration). */
 int fg_config_default(fg_config* cfg);
 
 /* Parses the keys above from parameter_flexi.ini text (readintools.f90:read_options syntax:
  * "key = value", "!" comments, case-insensitive keys, string values for Riemann/SplitDG/NodeType/
- * TimeDiscMethod). Unknown keys are ignored. */
+ * TimeDiscMethod/OverintegrationType). Unknown keys are ignored. */
 int fg_config_from_ini(const char* ini_text, fg_config* cfg);
 
 /* Creates a solver on the current CUDA device. Replaces InitDG/InitLifting/InitTimeDisc
@@ -109,6 +111,11 @@ int fg_set_mesh(fg_handle* h, int nElems, int nSides, int nBCSides, const int* S
  * surfint.t90:90-140). Optional after fg_set_mesh, which otherwise evaluates the normal-direction volume
  * metrics at the faces (identical up to round-off). Only row NormalDir of each side is read. */
 int fg_set_face_metrics(fg_handle* h, const double* Ja_Face, const double* Ja_slave);
+
+/* Overintegration of the state before the first time step (timedisc.f90:115-123; InitTimeDisc/TimeDisc do
+ * it once after the initial condition or restart): OverintegrationType 1 filters U with the modal cut-off,
+ * 2 applies the conservative cut-off to J U. No-op without overintegration. */
+int fg_overintegrate_state(fg_handle* h);
 
 /* Per-instance viscosity (ensembles); default: cfg.mu0 for every instance. */
 int fg_set_instance_mu0(fg_handle* h, int nInst, const double* mu0);
@@ -274,8 +281,8 @@ typedef struct fg_device_mesh {
  * device, with that device current, looks up the scratch address and sets the kernels' shared-memory
  * limits: make it before any stream capture. Calls that overlap on the GPU (other streams, or host
  * threads without ordering) race on the shared scratch. Meshes needing more scratch, and configurations
- * the kernels do not cover (N > 7, weak or conservative lifting, body force, split form off
- * Gauss-Lobatto nodes or with N not in {1,3,7}), are rejected before any launch, with the reason in
+ * the kernels do not cover (N > 7, weak or conservative lifting, body force, overintegration, split form
+ * off Gauss-Lobatto nodes or with N not in {1,3,7}), are rejected before any launch, with the reason in
  * fg_last_error(NULL). No cudaMalloc, cudaFree or other device allocation is made. */
 int fg_time_derivative_noalloc(const fg_config* cfg, const fg_device_mesh* mesh, const double* U, double* Ut, void* stream);
 

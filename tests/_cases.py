@@ -18,7 +18,8 @@ def oracle_cfg(c):
     return dict(N=d["N"], nodeType=d["NodeType"], riemann=d["Riemann"], riemannBC=d["RiemannBC"], lifting=d["Lifting"],
                 weakLifting=d["doWeakLifting"], consLifting=d["doConservativeLifting"], splitDG=d["SplitDG"], etaBR2=d["etaBR2"],
                 etaBR2_wall=d["etaBR2_wall"], kappa=d["kappa"], R=d["R"], Pr=d["Pr"], mu0=d["mu0"], CFLScale=d["CFLScale"],
-                DFLScale=d["DFLScale"], doTCSource=d["doTCSource"], dpdx=d["dpdx"])
+                DFLScale=d["DFLScale"], doTCSource=d["doTCSource"], dpdx=d["dpdx"], overintType=d["OverintegrationType"],
+                NUnder=d["NUnder"])
 
 
 def perturb_state(U, seed=0, amp=0.05):

@@ -1,7 +1,8 @@
 """FLEXI's Taylor-Green regression tests run on the GPU path: regressioncheck/checks/tgv/split (8^3
-periodic box, N=7 Gauss-Lobatto, split PI) and tgv/splitGauss (N=5 Gauss, split PI with entropy-variable
-prolongation and the split-Gauss surface integral), both RoeEntropyFix, BR1, Re=1600, Ma=0.1,
-CFL=DFL=0.8, tEnd=13. The reference writes the 15 TGVAnalysis columns every 10 time steps and compares
+periodic box, N=7 Gauss-Lobatto, split PI, CFL=DFL=0.8), tgv/splitGauss (8^3, N=5 Gauss, split PI with
+entropy-variable prolongation and the split-Gauss surface integral, CFL=DFL=0.8) and tgv/oInt (4^3,
+N=11 Gauss, weak form, overintegration by the modal cut-off to NUnder=7, CFL=DFL=0.9), all RoeEntropyFix,
+BR1, Re=1600, Ma=0.1, tEnd=13. The reference writes the 15 TGVAnalysis columns every 10 time steps and compares
 them at 1e-4 relative (analyze.ini); here every row up to tEnd is compared, including the time column
 that results from the CALCTIMESTEP-controlled time steps. The analysis integrals are evaluated by the
 oracle from the GPU state and the GPU's lifted gradients of the last stage, as AnalyzeTestcase does."""
@@ -14,20 +15,25 @@ from oracle import oracle as orc
 
 pytestmark = pytest.mark.gpu
 
-CASES = {"split": ("tgv_reference", 7, "gauss-lobatto", orc.NT_GL), "splitGauss": ("tgv_splitgauss_reference", 5, "gauss", orc.NT_GAUSS)}
+SPLIT = dict(SplitDG="pi", CFLScale=0.8, DFLScale=0.8)
+# fixture, N, node type (solver, oracle), elements per direction, further settings of the case
+CASES = {"split": ("tgv_reference", 7, "gauss-lobatto", orc.NT_GL, 8, SPLIT),
+         "splitGauss": ("tgv_splitgauss_reference", 5, "gauss", orc.NT_GAUSS, 8, SPLIT),
+         "oInt": ("tgv_oint_reference", 11, "gauss", orc.NT_GAUSS, 4,
+                  dict(SplitDG="weak", CFLScale=0.9, DFLScale=0.9, OverintegrationType="cutoff", NUnder=7))}
 
 
 @pytest.mark.timeout(1200)
 @pytest.mark.parametrize("case", list(CASES))
 def test_tgv_split_regression_all_rows(case, request):
-    fixture, N, node_type, nt = CASES[case]
+    fixture, N, node_type, nt, ne, extra = CASES[case]
     _, rows = request.getfixturevalue(fixture)
-    c = make_config(N=N, NodeType=node_type, SplitDG="pi", Riemann="roeentropyfix", Lifting="br1", kappa=1.4, R=71.42857,
-                    Pr=0.72, mu0=6.25e-4, CFLScale=0.8, DFLScale=0.8)
-    m = fmesh.tgv_box(8, ngeo=1)
+    c = make_config(N=N, NodeType=node_type, Riemann="roeentropyfix", Lifting="br1", kappa=1.4, R=71.42857, Pr=0.72, mu0=6.25e-4,
+                    **extra)
+    m = fmesh.tgv_box(ne, ngeo=1)
     f = Flexi(c, m)
     f.U = testcases.tgv_state(f.elem_xgp(), mach=0.1, kappa=1.4, R=71.42857)
-    o_sJ = None
+    f.overintegrate_state()  # timedisc.f90:115-123 (no-op without overintegration)
     scale = np.abs(rows[:, 1:]).max(axis=0)
     f.DGTimeDerivative_weakForm(0.0)
     sJ = f.mesh_array("sJ")
