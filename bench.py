@@ -15,6 +15,9 @@ e2e    : the same metric through the public C ABI with the state in pinned host 
 --workload tgv-splitgauss : the discretisation of the reference's tgv/splitGauss regression (N=5 Gauss, split
          PI with entropy-variable prolongation and the split-Gauss surface integral, BR1, RoeEntropyFix) on a
          curved 40^3 mesh (13.8 M DOF), same metric and timing.
+--workload tgv-oint : the discretisation of the reference's tgv/oInt regression (N=11 Gauss, weak form,
+         overintegration by the modal cut-off of J u_t to NUnder=7, BR1, RoeEntropyFix, CFL=DFL=0.9) on a
+         curved 16^3 mesh (7.1 M DOF), same metric and timing.
 --impl reference : the CPU implementation of the path (the C++ restatement of FLEXI's Fortran solver,
          FLEXI itself cannot be built here: Fortran/MPI/HDF5) on all host threads, bounded sample per step.
 Multi-GPU: the path does not shard on this setup (no halo exchange is built); N ranks run N replicas.
@@ -45,11 +48,17 @@ RIEMANN_NAMES = {"hllc": "HLLC", "roeentropyfix": "RoeEntropyFix"}
 # integral, BR1, RoeEntropyFix: the discretisation of the reference's tgv/splitGauss regression)
 SPLITGAUSS_METRIC = "FP64 DOF*stage/s (N=5 TGV, Gauss split form)"
 SPLITGAUSS_FLOPS_PER_DOF_STAGE = {"prep": 128.0, "lift": 500.0, "flux": 194.0, "vol": 1750.5}
+# overintegration (the discretisation of the reference's tgv/oInt regression: N=11 Gauss, weak form, BR1,
+# RoeEntropyFix, modal cut-off filter of J u_t to NUnder=7); "vol" includes the filter
+OINT_METRIC = "FP64 DOF*stage/s (N=11 TGV, overintegration cut-off to NUnder=7)"
+OINT_FLOPS_PER_DOF_STAGE = {"prep": 78.5, "lift": 640.0, "flux": 94.75, "vol": 935.25}
 
 
 def flops_per_dof_stage(riemann, kind="tgv"):
     if kind == "tgv-splitgauss":
         return dict(SPLITGAUSS_FLOPS_PER_DOF_STAGE)
+    if kind == "tgv-oint":
+        return dict(OINT_FLOPS_PER_DOF_STAGE)
     return dict(FLOPS_PER_DOF_STAGE, flux=FLUX_FLOPS_PER_DOF_STAGE[riemann])
 # compulsory HBM traffic per DOF and stage: U read+write, Ut_tmp read+write, 9 metric terms + sJ
 BYTES_ALG_PER_DOF_STAGE = 240.0
@@ -61,11 +70,11 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--elems", type=int, default=None, help="elements per direction (tgv: 32, tgv-splitgauss: 40)")
+    p.add_argument("--elems", type=int, default=None, help="elements per direction (tgv: 32, tgv-splitgauss: 40, tgv-oint: 16)")
     p.add_argument("--riemann", default="hllc", choices=sorted(RIEMANN_IDS), help="surface Riemann solver")
-    p.add_argument("--workload", default="tgv", choices=["tgv", "tgv-splitgauss", "ensemble", "adjoint", "adjoint-channel"],
+    p.add_argument("--workload", default="tgv", choices=["tgv", "tgv-splitgauss", "tgv-oint", "ensemble", "adjoint", "adjoint-channel"],
                    help="tgv: the single-case N=7 TGV; tgv-splitgauss: the N=5 Gauss split form of the reference's tgv/splitGauss "
-                        "regression on a curved 40^3 mesh; ensemble: 256 independent TGV/vortex instances at N=5 against a loop over "
+                        "regression on a curved 40^3 mesh; tgv-oint: the N=11 overintegration of tgv/oInt on a curved 16^3 mesh; ensemble: 256 independent TGV/vortex instances at N=5 against a loop over "
                         "instances; adjoint: gradient of a kinetic-energy loss over a 200-step TGV solve (16^3, N=5)")
     p.add_argument("--ckpt", type=int, default=20, help="adjoint: checkpoint interval in steps")
     p.add_argument("--fd-dirs", type=int, default=20, help="adjoint: random directions of the finite-difference check")
@@ -74,13 +83,20 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline leg (profiling runs)")
     a = p.parse_args()
     if a.elems is None:
-        a.elems = 40 if a.workload == "tgv-splitgauss" else 32
-    if a.workload == "tgv-splitgauss":
+        a.elems = {"tgv-splitgauss": 40, "tgv-oint": 16}.get(a.workload, 32)
+    if a.workload in ("tgv-splitgauss", "tgv-oint"):
         a.riemann = "roeentropyfix"
     return a
 
 
 def workload_config(n, riemann, kind="tgv"):
+    if kind == "tgv-oint":
+        dof = n ** 3 * 1728
+        return {"workload": f"TGV {n}^3 curved (perturbation 0.05, NGeo=3), N=11 Gauss, weak form, overintegration by the modal "
+                            f"cut-off filter of J u_t to NUnder=7, BR1, RoeEntropyFix, FP64",
+                "n_elems": n ** 3, "N": 11, "dof": dof, "Re": 1600, "Ma": 0.1, "CFLScale": 0.9, "DFLScale": 0.9,
+                "time_integration": "CarpenterRK4-5, 5 stages/step, CFL (on NUnder) / DFL dt each step",
+                "l2": f"inputs larger than L2 (state {dof * 40 / 1e6:.0f} MB)", "parallelism": "replicas"}
     if kind == "tgv-splitgauss":
         dof = n ** 3 * 216
         return {"workload": f"TGV {n}^3 curved (perturbation 0.05, NGeo=3), N=5 Gauss, split PI with entropy-variable prolongation "
@@ -96,6 +112,9 @@ def workload_config(n, riemann, kind="tgv"):
 
 def solver_config(riemann, kind="tgv"):
     from flexi_gb300.solver import make_config
+    if kind == "tgv-oint":
+        return make_config(N=11, NodeType="gauss", SplitDG="weak", Riemann="roeentropyfix", Lifting="br1", kappa=1.4, R=71.42857,
+                           Pr=0.72, mu0=6.25e-4, CFLScale=0.9, DFLScale=0.9, OverintegrationType=1, NUnder=7)
     if kind == "tgv-splitgauss":
         return make_config(N=5, NodeType="gauss", SplitDG="pi", Riemann="roeentropyfix", Lifting="br1", kappa=1.4, R=71.42857,
                            Pr=0.72, mu0=6.25e-4, CFLScale=0.8, DFLScale=0.8)
@@ -105,6 +124,10 @@ def solver_config(riemann, kind="tgv"):
 
 def oracle_config(riemann, kind="tgv"):
     """The same discretisation for the CPU restatement."""
+    if kind == "tgv-oint":
+        return dict(N=11, nodeType=1, riemann=33, riemannBC=-1, lifting=1, weakLifting=0, consLifting=0, splitDG=-1, etaBR2=2.0,
+                    etaBR2_wall=-1.0, kappa=1.4, R=71.42857, Pr=0.72, mu0=6.25e-4, CFLScale=0.9, DFLScale=0.9, doTCSource=0, dpdx=-1.0,
+                    overintType=1, NUnder=7)
     if kind == "tgv-splitgauss":
         return dict(N=5, nodeType=1, riemann=33, riemannBC=-1, lifting=1, weakLifting=0, consLifting=0, splitDG=4, etaBR2=2.0,
                     etaBR2_wall=-1.0, kappa=1.4, R=71.42857, Pr=0.72, mu0=6.25e-4, CFLScale=0.8, DFLScale=0.8, doTCSource=0, dpdx=-1.0)
@@ -113,10 +136,12 @@ def oracle_config(riemann, kind="tgv"):
 
 
 def metric_name(kind):
-    return SPLITGAUSS_METRIC if kind == "tgv-splitgauss" else METRIC
+    return {"tgv-splitgauss": SPLITGAUSS_METRIC, "tgv-oint": OINT_METRIC}.get(kind, METRIC)
 
 
 def kernel_names(kind):
+    if kind == "tgv-oint":
+        return {"vol": "k_vol_weak<12,Gauss> + k_overint<12>", "lift": "k_lift<12,Gauss>", "flux": "k_flux<12>", "prep": "k_prep<12,Gauss>"}
     if kind == "tgv-splitgauss":
         return {"vol": "k_vol_split_gen<6,Gauss>", "lift": "k_lift<6,Gauss>", "flux": "k_flux<6>", "prep": "k_prep<6,Gauss>"}
     return {"vol": "k_vol_split<8>", "lift": "k_lift<8,GL>", "flux": "k_flux<8>", "prep": "k_prep<8,GL>"}
@@ -205,6 +230,7 @@ def cpu_baseline_sample(riemann, n_elems_dir=8, budget_s=12.0, kind="tgv"):
     m = fmesh.tgv_box(n_elems_dir, ngeo=3, perturb=0.05, seed=0)
     o = orc.Oracle(cfg, m)
     o.set_state(testcases.tgv_state(o.mesh_array("Elem_xGP"), mach=0.1, kappa=1.4, R=71.42857))
+    o.overintegrate_state()  # timedisc.f90:115-123 (no-op without overintegration)
     dof = m.n_elems * (cfg["N"] + 1) ** 3
     t = 0.0
     dt, _ = o.calc_timestep()
@@ -235,6 +261,7 @@ def run_reference(args):
     m = fmesh.tgv_box(ns, ngeo=3, perturb=0.05, seed=0)
     o = orc.Oracle(cfg, m)
     o.set_state(testcases.tgv_state(o.mesh_array("Elem_xGP"), mach=0.1, kappa=1.4, R=71.42857))
+    o.overintegrate_state()  # timedisc.f90:115-123 (no-op without overintegration)
     dof = m.n_elems * (cfg["N"] + 1) ** 3
     t = 0.0
     for _ in range(args.warmup):
@@ -278,6 +305,7 @@ def run_gb300(args):
     f = Flexi(c, m)
     U0 = testcases.tgv_state(f.elem_xgp(), mach=0.1, kappa=1.4, R=71.42857)
     f.U = U0
+    f.overintegrate_state()  # timedisc.f90:115-123 (no-op without overintegration)
     dof = f.n_elems * f.n ** 3
     stream = torch.cuda.ExternalStream(f.stream())
     fp64_peak = probe_fp64_tflops()

@@ -568,10 +568,10 @@ void launch_rhs_dev(fg_handle* h, const Dev& d, int mode, double rkA, double rkB
   { ProfScope p(h, 2); h->K.flux_block(d, h->B, h->K.fluxBlock, h->st); }
   {
     ProfScope p(h, 3);
-    // with overintegration the volume kernel writes Ut and k_overint filters it and updates the registers
+    // with overintegration the volume kernel writes J u_t and k_overint filters it and updates the registers
     const bool oi = h->ov.type > 0;
-    if (h->cfg.SplitDG >= 0) h->K.vol_split(d, h->B, oi ? 0 : mode, rkA, rkB, h->st);
-    else h->K.vol_weak(d, h->B, oi ? 0 : mode, rkA, rkB, h->st);
+    if (h->cfg.SplitDG >= 0) h->K.vol_split(d, h->B, oi ? 3 : mode, rkA, rkB, h->st);
+    else h->K.vol_weak(d, h->B, oi ? 3 : mode, rkA, rkB, h->st);
     if (oi) { h->K.overint(d, h->ov, mode, rkA, rkB, 0, h->st); h->launches += 1; }
   }
   h->launches += 4;

@@ -482,7 +482,8 @@ __global__ void __launch_bounds__(256) k_flux(Dev d, Basis B) {
 
 // stage parameters of the fused LSERK update
 struct Stage {
-  int mode;        // 0: write Ut only (fg_time_derivative); 1: first RK stage; 2: later RK stage
+  int mode;        // 0: write Ut only (fg_time_derivative); 1: first RK stage; 2: later RK stage;
+                   // 3: write J u_t (before ApplyJacobianCons) for the overintegration kernel
   double rkA;      // RKA(stage) (stage >= 2)
   double rkB;      // RKb(stage)
 };
@@ -517,6 +518,20 @@ __device__ __forceinline__ void finish_node(const Dev& d, const SBasis<n>& Bs, c
   const double sj = d.sJ[(size_t)e * n3 + x];
   const int inst = d.elemInst[e];
   const double dpdx = d.dpdx[inst];
+  if (st.mode == 3) {
+    // dg.f90:656-662: Ut = -Ut, sources in reference space (divided by sJ); the Jacobian follows the filter
+#pragma unroll
+    for (int v = 0; v < 5; ++v) ut[v] = -ut[v];
+    if (dpdx != 0.) { ut[1] -= dpdx / sj; ut[4] -= dpdx / sj * d.bulkVel[inst]; }
+    if (d.forceField) {
+      const double F = d.forceField[(size_t)e * n3 + x];
+      ut[1] += F / sj;
+      ut[4] += F / sj * d.bulkVel[inst];
+    }
+#pragma unroll
+    for (int v = 0; v < 5; ++v) d.Ut[((size_t)e * 5 + v) * n3 + x] = ut[v];
+    return;
+  }
   const double msj = -sj;
 #pragma unroll
   for (int v = 0; v < 5; ++v) ut[v] *= msj;
@@ -1097,9 +1112,9 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
 }
 
 // =====================================================================================================
-// k_overint: overintegration.f90 -- dg.f90:663-675 after the volume kernel has written Ut (mode 0):
-// J u_t = Ut / sJ is filtered (type 1: OverintegrationMat in xi, eta, zeta, then ApplyJacobianCons;
-// type 2: FilterConservative, whose result is u_t), then the LSERK register update of the stage.
+// k_overint: overintegration.f90 -- dg.f90:663-675 after the volume kernel has written J u_t to Ut (stage
+// mode 3): type 1 filters it with OverintegrationMat in xi, eta, zeta and applies ApplyJacobianCons; type 2
+// applies FilterConservative, whose result is u_t; then the LSERK register update of the stage.
 // With state = 1 it is the overintegration of U before the first time step (timedisc.f90:115-123: type 1
 // filters U, type 2 applies FilterConservative to J U). One CTA per element, both buffers in shared memory.
 // =====================================================================================================
@@ -1145,7 +1160,7 @@ __global__ void __launch_bounds__(OverintShape<n>::THREADS) k_overint(Dev d, Ove
     for (int t = threadIdx.x; t < nu * n; t += blockDim.x) { sM[t] = o.VNU[t]; sM[nu * n + t] = o.VUN[t]; }
   }
   const double* src = state ? d.U : d.Ut;
-  const bool toRef = !(state && o.type == 1);  // J u = u / sJ, except for the state filter of type 1
+  const bool toRef = state && o.type == 2;  // the state's conservative cut-off acts on J U = U / sJ
   for (int t = threadIdx.x; t < 5 * n3; t += blockDim.x) {
     const int v = t / n3, x = t - v * n3;
     const double val = src[((size_t)e * 5 + v) * n3 + x];

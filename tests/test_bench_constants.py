@@ -37,3 +37,13 @@ def test_splitgauss_flops_per_dof_stage_match_oracle_count():
     counted = o.flops_breakdown()
     for k, v in bench.flops_per_dof_stage("roeentropyfix", "tgv-splitgauss").items():
         assert v == pytest.approx(counted[k], rel=2e-3), (k, v, counted[k])
+
+
+def test_oint_flops_per_dof_stage_match_oracle_count():
+    bench = _bench()
+    m = fmesh.tgv_box(2, ngeo=3, perturb=0.05)
+    o = orc.Oracle(bench.oracle_config("roeentropyfix", "tgv-oint"), m)
+    o.set_state(testcases.tgv_state(o.mesh_array("Elem_xGP"), mach=0.1, kappa=1.4, R=71.42857))
+    counted = o.flops_breakdown()
+    for k, v in bench.flops_per_dof_stage("roeentropyfix", "tgv-oint").items():
+        assert v == pytest.approx(counted[k], rel=2e-3), (k, v, counted[k])
