@@ -16,8 +16,8 @@ LIB = os.path.join(OUT, "libflexigpu.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU = ["fg_host.cu", "fg_noalloc.cu"] + [f"fg_inst_n{n}.cu" for n in range(2, 13)]
-CPP = ["fg_mesh.cpp"]
-HEADERS = ["fg_common.cuh", "fg_kernels.cuh", "fg_launch.cuh", "fg_inst.cuh", "fg_basis.hpp", "fg_mesh.hpp", "fg_adjoint_point.cuh", "fg_adjoint.cuh"]
+CPP = ["fg_mesh.cpp", "fg_io.cpp"]
+HEADERS = ["fg_common.cuh", "fg_kernels.cuh", "fg_launch.cuh", "fg_inst.cuh", "fg_basis.hpp", "fg_mesh.hpp", "fg_adjoint_point.cuh", "fg_adjoint.cuh", "fg_h5.hpp"]
 # host-only harness of the point-wise physics and its adjoints, for the CPU tests
 POINT_SRC = "fg_point_test.cu"
 POINT_LIB = os.path.join(OUT, "libfgpoint.so")

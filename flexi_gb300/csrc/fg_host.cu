@@ -880,6 +880,12 @@ int fg_set_instance_mu0(fg_handle* h, int nInst, const double* mu0) {
   return FG_OK;
 }
 
+int fg_get_config(const fg_handle* h, fg_config* out) {
+  if (!h || !out) return FG_ERR_STATE;
+  *out = h->cfg;
+  return FG_OK;
+}
+
 int fg_get_sizes(const fg_handle* h, int* out) {
   if (!h || !out) return FG_ERR_STATE;
   out[0] = h->M.nElems; out[1] = h->M.nSides; out[2] = h->M.nBCSides; out[3] = h->cfg.N; out[4] = h->M.nInst;

@@ -137,6 +137,20 @@ class Flexi:
         """timedisc.f90:115-123: the overintegration of U before the first time step (no-op without it)."""
         self._check(self.L.fg_overintegrate_state(self.h), "fg_overintegrate_state")
 
+    def write_state(self, path, project="", mesh_file="", t=0.0):
+        """WriteState (hdf5_output.f90:60-188): DG_Solution and the header attributes of a FLEXI state file."""
+        rc = self.L.fg_write_state(self.h, str(path).encode(), project.encode(), mesh_file.encode(), float(t))
+        if rc != 0:
+            raise FlexiError(f"fg_write_state: {self.L.fg_io_last_error().decode()}")
+
+    def read_state(self, path):
+        """DG_Solution of a FLEXI state file with this solver's N, node type and element count; returns its Time."""
+        t = ctypes.c_double(0.0)
+        rc = self.L.fg_read_state(self.h, str(path).encode(), ctypes.byref(t))
+        if rc != 0:
+            raise FlexiError(f"fg_read_state: {self.L.fg_io_last_error().decode()}")
+        return t.value
+
     def _sizes(self):
         s = np.zeros(5, np.int32)
         self._check(self.L.fg_get_sizes(self.h, _p(s)), "fg_get_sizes")

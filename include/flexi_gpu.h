@@ -117,6 +117,29 @@ int fg_set_face_metrics(fg_handle* h, const double* Ja_Face, const double* Ja_sl
  * 2 applies the conservative cut-off to J U. No-op without overintegration. */
 int fg_overintegrate_state(fg_handle* h);
 
+/* The configuration the handle was created with. */
+int fg_get_config(const fg_handle* h, fg_config* out);
+
+/* HOPR mesh files (the file part of mesh_readin.f90:ReadMesh/ReadBCs, datasets ElemInfo, SideInfo,
+ * NodeCoords, BCType, BCNames, attribute Ngeo), read without the HDF5 library (contiguous datasets of the
+ * classic file format, as HOPR writes them). fg_hopr_sizes: out[0]=nElems, out[1]=NGeo, out[2]=nBCs.
+ * fg_hopr_read fills the inputs of fg_build_mesh: NodeCoords(3,0:NGeo,0:NGeo,0:NGeo,nElems),
+ * ElemNb(3,6,nElems) (neighbour element, its local side, BC index; BC sides of types other than 0/1/100
+ * are boundaries, mesh_readin.f90:398-456), BoundaryType(2,nBCs) = (BCType(1), BCType(3)) and BCNames
+ * (nBCs x 256 chars, NUL-terminated; may be NULL). Hexahedra only, no mortar interfaces. Errors in
+ * fg_io_last_error(). */
+int fg_hopr_sizes(const char* path, int* out);
+int fg_hopr_read(const char* path, double* NodeCoords, int* ElemNb, int* BoundaryType, char* BCNames);
+
+/* FLEXI state files (hdf5_output.f90:WriteState): dataset DG_Solution(1:5,0:N,0:N,0:N,nElems) and the
+ * header attributes (VarNames, Program, File_Type, Project_Name, File_Version, N, Dimension, Time,
+ * MeshFile, NextFile, NodeType, NComputation, TIME). fg_read_state loads DG_Solution of a file with the
+ * same N, node type and element count (the restart of restart.f90 without interpolation) and returns its
+ * Time. Errors in fg_io_last_error(). */
+int fg_write_state(fg_handle* h, const char* path, const char* projectName, const char* meshFile, double time);
+int fg_read_state(fg_handle* h, const char* path, double* time);
+const char* fg_io_last_error(void);
+
 /* Per-instance viscosity (ensembles); default: cfg.mu0 for every instance. */
 int fg_set_instance_mu0(fg_handle* h, int nInst, const double* mu0);
 

@@ -4,7 +4,8 @@ Reads FLEXI v25.10's unit-test data (unitTests/*.bin, Fortran unformatted sequen
 4-byte length marker, little-endian payload, closing marker) and the Taylor-Green regression
 references (regressioncheck/checks/tgv/{split,splitGauss,oInt}/TGV_Re1600_*_TGVAnalysis_Reference.csv),
 and stores the arrays the parity tests need in reference_unittests.npz, tgv_split_reference.npz,
-tgv_splitgauss_reference.npz and tgv_oint_reference.npz.
+tgv_splitgauss_reference.npz and tgv_oint_reference.npz; copies five small HOPR mesh / FLEXI state files of
+the reference's test cases to hopr/ for the HDF5 reader.
 
 Run from the repository root in a container that has the reference mounted:
     python tests/golden/make_golden.py /root/reference
@@ -92,6 +93,16 @@ def main(ref):
         rows = np.array([[float(v) for v in ln.split(",")] for ln in lines[1:]])
         np.savez_compressed(os.path.join(os.path.dirname(__file__), name), header=np.array(header), rows=rows)
         print("wrote", name, rows.shape)
+    # HOPR mesh and FLEXI state files of the reference's test cases, for the HDF5 reader and the mesh
+    # read-in (copied unchanged)
+    import shutil
+    hdir = os.path.join(os.path.dirname(__file__), "hopr")
+    os.makedirs(hdir, exist_ok=True)
+    for src in ("regressioncheck/checks/tgv/oInt/CART_HEX_PERIODIC_004_mesh.h5", "tutorials/channel/CHANNEL_004_mesh.h5",
+                "regressioncheck/checks/convtest/p_3D_mortar/CART_HEX_PERIODIC_MORTAR_002_mesh.h5",
+                "regressioncheck/checks/timedisc/freestream_3D/cartbox3D_mesh.h5",
+                "regressioncheck/checks/timedisc/freestream_3D/cartbox_State_0000000.000000000.h5"):
+        shutil.copyfile(os.path.join(ref, src), os.path.join(hdir, os.path.basename(src)))
     print("wrote fixtures:", sorted(out.keys()))
 
 

@@ -6,6 +6,8 @@ BR1, Re=1600, Ma=0.1, tEnd=13. The reference writes the 15 TGVAnalysis columns e
 them at 1e-4 relative (analyze.ini); here every row up to tEnd is compared, including the time column
 that results from the CALCTIMESTEP-controlled time steps. The analysis integrals are evaluated by the
 oracle from the GPU state and the GPU's lifted gradients of the last stage, as AnalyzeTestcase does."""
+import os
+
 import numpy as np
 import pytest
 
@@ -21,6 +23,8 @@ CASES = {"split": ("tgv_reference", 7, "gauss-lobatto", orc.NT_GL, 8, SPLIT),
          "splitGauss": ("tgv_splitgauss_reference", 5, "gauss", orc.NT_GAUSS, 8, SPLIT),
          "oInt": ("tgv_oint_reference", 11, "gauss", orc.NT_GAUSS, 4,
                   dict(SplitDG="weak", CFLScale=0.9, DFLScale=0.9, OverintegrationType="cutoff", NUnder=7))}
+# oInt runs on the reference's own mesh file of the case (regressioncheck/checks/tgv/oInt, [0, 2 pi]^3)
+MESH_FILE = {"oInt": os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "hopr", "CART_HEX_PERIODIC_004_mesh.h5")}
 
 
 @pytest.mark.timeout(1200)
@@ -30,7 +34,7 @@ def test_tgv_split_regression_all_rows(case, request):
     _, rows = request.getfixturevalue(fixture)
     c = make_config(N=N, NodeType=node_type, Riemann="roeentropyfix", Lifting="br1", kappa=1.4, R=71.42857, Pr=0.72, mu0=6.25e-4,
                     **extra)
-    m = fmesh.tgv_box(ne, ngeo=1)
+    m = fmesh.read_hopr(MESH_FILE[case]) if case in MESH_FILE else fmesh.tgv_box(ne, ngeo=1)
     f = Flexi(c, m)
     f.U = testcases.tgv_state(f.elem_xgp(), mach=0.1, kappa=1.4, R=71.42857)
     f.overintegrate_state()  # timedisc.f90:115-123 (no-op without overintegration)
