@@ -4,7 +4,7 @@ Reads FLEXI v25.10's unit-test data (unitTests/*.bin, Fortran unformatted sequen
 4-byte length marker, little-endian payload, closing marker) and the Taylor-Green regression
 references (regressioncheck/checks/tgv/{split,splitGauss,oInt}/TGV_Re1600_*_TGVAnalysis_Reference.csv),
 and stores the arrays the parity tests need in reference_unittests.npz, tgv_split_reference.npz,
-tgv_splitgauss_reference.npz and tgv_oint_reference.npz; copies five small HOPR mesh / FLEXI state files of
+tgv_splitgauss_reference.npz and tgv_oint_reference.npz; copies six HOPR mesh / FLEXI state files of
 the reference's test cases to hopr/ for the HDF5 reader.
 
 Run from the repository root in a container that has the reference mounted:
@@ -101,7 +101,8 @@ def main(ref):
     for src in ("regressioncheck/checks/tgv/oInt/CART_HEX_PERIODIC_004_mesh.h5", "tutorials/channel/CHANNEL_004_mesh.h5",
                 "regressioncheck/checks/convtest/p_3D_mortar/CART_HEX_PERIODIC_MORTAR_002_mesh.h5",
                 "regressioncheck/checks/timedisc/freestream_3D/cartbox3D_mesh.h5",
-                "regressioncheck/checks/timedisc/freestream_3D/cartbox_State_0000000.000000000.h5"):
+                "regressioncheck/checks/timedisc/freestream_3D/cartbox_State_0000000.000000000.h5",
+                "tutorials/naca0012/NACA0012_652_Ng2_mesh.h5"):
         shutil.copyfile(os.path.join(ref, src), os.path.join(hdir, os.path.basename(src)))
     print("wrote fixtures:", sorted(out.keys()))
 

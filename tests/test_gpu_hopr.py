@@ -1,7 +1,8 @@
 """GPU path on HOPR mesh files and FLEXI state files (mesh_readin.f90, hdf5_output.f90:WriteState, restart).
 
-- Ut on the reference's periodic TGV mesh and channel mesh (isothermal walls) against the oracle on the
-  same file, 1e-12 as in test_gpu_parity.py.
+- Ut on the reference's periodic TGV mesh, channel mesh (isothermal walls) and curved NACA0012 mesh
+  (NGeo=2, adiabatic walls) against the oracle on the same file, 1e-12 as in test_gpu_parity.py; a fluid
+  at rest on the curved mesh stays at rest on the GPU too.
 - fg_write_state / fg_read_state: a written state reads back bit for bit with its Time; a state of another
   N is refused; the reference's own freestream state file (tests/golden/hopr/, N=3 Gauss) reads as the
   constant state (1, 1, 1, 1, 4) it holds.
@@ -87,3 +88,25 @@ def test_reads_reference_state_file():
     f.close()
     assert t == 0.0
     assert np.array_equal(U, np.broadcast_to(np.array([1.0, 1.0, 1.0, 1.0, 4.0]), U.shape))
+
+
+def test_curved_airfoil_file():
+    c = product_cfg(N=4, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roe", Lifting="br2", kappa=1.4, R=1.0, Pr=0.72, mu0=1e-3)
+    m = fmesh.read_hopr(os.path.join(HOPR, "NACA0012_652_Ng2_mesh.h5"), boundary={"BC_inflow": (3, 0), "BC_outflow": (3, 0)})
+    f = Flexi(c, m)
+    x = f.elem_xgp()
+    rest = np.zeros(x.shape[:-1] + (5,))
+    rest[..., 0] = 1.0
+    rest[..., 4] = 1.0 / 0.4
+    f.U = rest
+    assert np.abs(f.DGTimeDerivative_weakForm(0.0)).max() <= 1e-10
+    rng = np.random.default_rng(5)
+    U0 = rest.copy()
+    U0[..., 1] = 0.2 * np.sin(x[..., 0]) + 0.02 * rng.standard_normal(x.shape[:-1])
+    U0[..., 2] = 0.1 * np.cos(x[..., 1])
+    U0[..., 4] += 0.5 * (U0[..., 1] ** 2 + U0[..., 2] ** 2)
+    f.close()
+    f, o = _pair(c, m, U0)
+    err = rel_err(f.DGTimeDerivative_weakForm(0.0), o.time_derivative(0.0))
+    f.close()
+    assert err <= 1e-12, err

@@ -5,7 +5,9 @@ tests/golden/make_golden.py). Checks: sizes, connectivity and BCs as mesh_readin
 the reference's periodic 4^3 TGV mesh gives the same operator as the synthetic box (the oracle's time
 derivative agrees to round-off after matching elements by their barycentres); a fluid at rest between
 isothermal walls of the reference's channel mesh is a steady state (Ut at round-off, which a wrongly
-read wall would break); BC overrides by name; mortar meshes, truncated and non-HDF5 files give errors.
+read wall would break), and likewise on the curved (NGeo=2) NACA0012 mesh, whose free-stream preservation
+needs the curved metrics built from the file's nodes; BC overrides by name; mortar meshes, truncated and
+non-HDF5 files give errors.
 """
 import os
 import shutil
@@ -112,3 +114,20 @@ def test_unsupported_and_corrupt_files(tmp_path):
     p = tmp_path / "copy.h5"
     shutil.copyfile(_path("CART_HEX_PERIODIC_004_mesh.h5"), p)
     assert fmesh.read_hopr(p).n_elems == 64
+
+
+def test_curved_airfoil_mesh_at_rest_is_steady():
+    """NACA0012, 652 curved elements (NGeo=2), inflow/outflow replaced by adiabatic walls: a fluid at rest is
+    steady to round-off (|Ut| against O(100) for a moving fluid)."""
+    m = fmesh.read_hopr(_path("NACA0012_652_Ng2_mesh.h5"), boundary={"BC_inflow": (3, 0), "BC_outflow": (3, 0)})
+    assert m.n_elems == 652 and m.ngeo == 2
+    o = orc.Oracle(dict(CFG, riemann=3, R=1.0, mu0=1e-3), m)
+    x = o.mesh_array("Elem_xGP")
+    U = np.zeros(x.shape[:-1] + (5,))
+    U[..., 0] = 1.0
+    U[..., 4] = 1.0 / 0.4
+    o.set_state(U)
+    assert np.abs(o.time_derivative(0.0)).max() <= 1e-10
+    U[..., 1] = 0.3
+    o.set_state(U)
+    assert np.abs(o.time_derivative(0.0)).max() > 1.0
