@@ -57,7 +57,7 @@ def load(path=None):
     L.fg_overintegrate_state.argtypes = [P]
     L.fg_get_config.argtypes = [P, P]
     L.fg_hopr_sizes.argtypes = [ctypes.c_char_p, P]
-    L.fg_hopr_read.argtypes = [ctypes.c_char_p, P, P, P, P]
+    L.fg_hopr_read.argtypes = [ctypes.c_char_p, P, P, P, P, P]
     L.fg_write_state.argtypes = [P, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_double]
     L.fg_read_state.argtypes = [P, ctypes.c_char_p, P]
     L.fg_io_last_error.restype = ctypes.c_char_p

@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstring>
 #include <ctime>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -54,14 +55,12 @@ Hopr read_hopr(const char* path) {
   for (long long e = 0; e < h.nElems; ++e) {
     const long long* ei = &h.elemInfo[(size_t)e * 6];
     if (!is_hexa(ei[0])) throw std::runtime_error("element " + std::to_string(e + 1) + " is not a hexahedron (type " + std::to_string(ei[0]) + ")");
-    if (ei[3] - ei[2] != 6) throw std::runtime_error("element " + std::to_string(e + 1) + ": mortar interfaces are not supported");
-    if (ei[2] < 0 || ei[3] > nSides) throw std::runtime_error("ElemInfo side range out of bounds");
+    if (ei[3] - ei[2] < 6 || ei[2] < 0 || ei[3] > nSides) throw std::runtime_error("ElemInfo side range out of bounds");
     if (ei[5] - ei[4] != ng3 || ei[4] < 0 || ei[5] > nNodes) throw std::runtime_error("ElemInfo node range does not match Ngeo");
   }
   for (long long s = 0; s < nSides; ++s) {
     const long long* si = &h.sideInfo[(size_t)s * 5];
-    if (si[2] < 0 || si[0] < 0) throw std::runtime_error("mortar interfaces are not supported");
-    if (si[2] > h.nElems) throw std::runtime_error("SideInfo neighbour element out of range");
+    if (si[2] < -3 || si[2] > h.nElems) throw std::runtime_error("SideInfo neighbour element out of range");
     if (si[4] < 0 || si[4] > h.nBCs) throw std::runtime_error("SideInfo BC index out of range");
   }
   return h;
@@ -80,13 +79,16 @@ int fg_hopr_sizes(const char* path, int* out) {
     out[0] = (int)h.nElems;
     out[1] = (int)h.NGeo;
     out[2] = (int)h.nBCs;
+    int nm = 0;
+    for (size_t r = 0; r < h.sideInfo.size() / 5; ++r) nm += h.sideInfo[r * 5 + 2] < 0;
+    out[3] = nm;
   } catch (std::exception& e) {
     return io_fail(FG_ERR_MESH, e.what());
   }
   return FG_OK;
 }
 
-int fg_hopr_read(const char* path, double* NodeCoords, int* ElemNb, int* BoundaryType, char* BCNames) {
+int fg_hopr_read(const char* path, double* NodeCoords, int* ElemNb, int* BoundaryType, char* BCNames, int* Mortars) {
   if (!path || !NodeCoords || !ElemNb) return io_fail(FG_ERR_CONFIG, "fg_hopr_read: null argument");
   try {
     const Hopr h = read_hopr(path);
@@ -107,13 +109,54 @@ int fg_hopr_read(const char* path, double* NodeCoords, int* ElemNb, int* Boundar
         std::memcpy(BCNames + b * 256, h.bcNames[b].data(), std::min<size_t>(h.bcNames[b].size(), 255));
       }
     }
-    // connections (mesh_readin.f90:398-456): an inner side, or a BC side of type 0, 1 (periodic) or 100, is
-    // connected to its neighbour element's side 10*nbLocSide+flip / 10; other BC sides become boundaries
+    // connections (mesh_readin.f90:310-456): an inner side, or a BC side of type 0, 1 (periodic) or 100, is
+    // connected to its neighbour element's side 10*nbLocSide+flip / 10; other BC sides become boundaries.
+    // A side with neighbour -type is a big mortar side, followed by its 2 or 4 small virtual sides
+    int nMortar = 0;
+    std::vector<std::pair<long long, int>> smallSides;  // (element, local side) of the small elements
+    // element side of each slave side id (a small element's side of a mortar is found by its side id)
+    std::map<long long, std::pair<long long, int>> slaveOf;
     for (long long e = 0; e < h.nElems; ++e) {
-      const long long first = h.elemInfo[(size_t)e * 6 + 2];
-      for (int ls = 1; ls <= 6; ++ls) {
-        const long long* si = &h.sideInfo[(size_t)(first + ls - 1) * 5];
+      long long row = h.elemInfo[(size_t)e * 6 + 2];
+      for (int ls = 1; ls <= 6; ++ls, ++row) {
+        const long long* si = &h.sideInfo[(size_t)row * 5];
+        if (si[1] < 0) slaveOf[-si[1]] = {e, ls};
+        if (si[2] < 0) row += si[2] == -1 ? 4 : 2;
+      }
+    }
+    for (long long e = 0; e < h.nElems; ++e) {
+      long long row = h.elemInfo[(size_t)e * 6 + 2];
+      const long long last = h.elemInfo[(size_t)e * 6 + 3];
+      for (int ls = 1; ls <= 6; ++ls, ++row) {
+        if (row >= last) throw std::runtime_error("element " + std::to_string(e + 1) + ": fewer than six sides");
+        const long long* si = &h.sideInfo[(size_t)row * 5];
         int* nb = &ElemNb[((size_t)e * 6 + ls - 1) * 3];
+        if (si[2] < 0) {
+          const int type = (int)-si[2], nm = type == 1 ? 4 : 2;
+          if (row + nm >= last) throw std::runtime_error("mortar side without its small sides");
+          if (Mortars) {
+            int* mo = &Mortars[(size_t)nMortar * 15];
+            for (int k = 0; k < 15; ++k) mo[k] = 0;
+            mo[0] = (int)(e + 1); mo[1] = ls; mo[2] = type;
+            for (int im = 0; im < nm; ++im) {
+              const long long* sm = &h.sideInfo[(size_t)(row + 1 + im) * 5];
+              auto it = slaveOf.find(sm[1] < 0 ? -sm[1] : sm[1]);
+              if (sm[2] <= 0 || it == slaveOf.end() || it->second.first != sm[2] - 1)
+                throw std::runtime_error("mortar small side without its small element side");
+              mo[3 + 3 * im] = (int)sm[2];
+              mo[4 + 3 * im] = it->second.second;
+              smallSides.push_back(it->second);
+            }
+          }
+          ++nMortar;
+          row += nm;
+          nb[0] = -1; nb[1] = 0; nb[2] = 0;
+          continue;
+        }
+        if (si[0] < 0) {  // a small element's side of a mortar (negative side type, mesh_readin.f90:354)
+          nb[0] = -1; nb[1] = 0; nb[2] = 0;
+          continue;
+        }
         const long long bc = si[4];
         bool connected = si[2] != 0;
         if (bc > 0) {
@@ -126,6 +169,11 @@ int fg_hopr_read(const char* path, double* NodeCoords, int* ElemNb, int* Boundar
         if (connected && (nb[1] < 1 || nb[1] > 6)) throw std::runtime_error("SideInfo neighbour side out of range");
         if (!connected && bc == 0) throw std::runtime_error("side without neighbour and without BC");
       }
+    }
+    for (const auto& sm : smallSides) {
+      if (sm.first < 0 || sm.first >= h.nElems) throw std::runtime_error("mortar small element out of range");
+      int* nb = &ElemNb[((size_t)sm.first * 6 + sm.second - 1) * 3];
+      nb[0] = -1; nb[1] = 0; nb[2] = 0;
     }
   } catch (std::exception& e) {
     return io_fail(FG_ERR_MESH, e.what());

@@ -123,6 +123,7 @@ void build_from_raw(const RawMesh& R, int N, int nodeType, HostMesh& M) {
     for (int ls = 1; ls <= 6; ++ls) {
       const int ne = nb(0, ls, e);
       if (ne == 0) { bcs.push_back({e, ls, -1, 0, nb(2, ls, e)}); continue; }
+      if (ne < 0 || ne > nE) throw std::runtime_error("neighbour element out of range (mortar sides need the Mortars table)");
       const int oe = ne - 1, ols = nb(1, ls, e);
       if (e < oe || (e == oe && ls < ols)) inner.push_back({e, ls, oe, ols, 0});
     }

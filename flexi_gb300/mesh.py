@@ -33,6 +33,10 @@ class BoxMesh:
     elem_inst: np.ndarray = None
     description: str = ""
     bc_names: list = None
+    # mortar interfaces (nMortars, 15) int32: big element (1-based), its local side, type (1: 1->4, 2: 1->2 in
+    # eta, 3: 1->2 in xi), then per small side: small element (1-based), its local side, 0; the elem_nb
+    # entries of these sides are -1
+    mortars: np.ndarray = None
 
 
 def cartesian_box(nelems, lower, upper, ngeo=1, periodic=(True, True, True), mapping=None, wall_bc=None, ref_state_prim=None):
@@ -151,7 +155,7 @@ def concatenate(meshes):
 
 def read_hopr(path, ref_state_prim=None, boundary=None):
     """A HOPR mesh file (HDF5) as FLEXI's ReadMesh/ReadBCs read it (mesh_readin.f90:125-500), through the
-    library's own reader (fg_hopr_sizes / fg_hopr_read): hexahedra, conforming (no mortar) interfaces.
+    library's own reader (fg_hopr_sizes / fg_hopr_read): hexahedra, conforming and mortar interfaces.
 
     boundary: optional {BC name: (BC_TYPE, BC_STATE)} overrides, as the BoundaryName / BoundaryType
     keys of the parameter file replace the types stored in the mesh (mesh_readin.f90:150-172).
@@ -161,16 +165,18 @@ def read_hopr(path, ref_state_prim=None, boundary=None):
     from . import _lib
     L = _lib.load()
     b = str(path).encode()
-    sizes = np.zeros(3, np.int32)
+    sizes = np.zeros(4, np.int32)
     if L.fg_hopr_sizes(b, sizes.ctypes.data) != 0:
         raise ValueError(L.fg_io_last_error().decode())
-    ne, ng, nbc = (int(v) for v in sizes)
+    ne, ng, nbc, nmo = (int(v) for v in sizes)
+    mortars = np.zeros((max(nmo, 1), 15), np.int32)
     nc = np.zeros((ne, ng + 1, ng + 1, ng + 1, 3))
     nb = np.zeros((ne, 6, 3), np.int32)
     bt = np.zeros((max(nbc, 1), 2), np.int32)
     names = ctypes.create_string_buffer(256 * max(nbc, 1))
-    if L.fg_hopr_read(b, nc.ctypes.data, nb.ctypes.data, bt.ctypes.data, names) != 0:
+    if L.fg_hopr_read(b, nc.ctypes.data, nb.ctypes.data, bt.ctypes.data, names, mortars.ctypes.data) != 0:
         raise ValueError(L.fg_io_last_error().decode())
+    mortars = mortars[:nmo]
     bc_names = [names.raw[i * 256:(i + 1) * 256].split(b"\0")[0].decode() for i in range(nbc)]
     bt = bt[:nbc]
     for name, (t, st) in (boundary or {}).items():
@@ -179,4 +185,4 @@ def read_hopr(path, ref_state_prim=None, boundary=None):
             raise KeyError(f"no boundary {name!r} in {path} (boundaries: {bc_names})")
         bt[matches[0]] = (t, st)
     rs = np.zeros((0, 6)) if ref_state_prim is None else np.asarray(ref_state_prim, np.float64).reshape(-1, 6)
-    return BoxMesh(ne, ng, nc, nb, bt, rs, description=f"HOPR mesh {path}", bc_names=bc_names)
+    return BoxMesh(ne, ng, nc, nb, bt, rs, description=f"HOPR mesh {path}", bc_names=bc_names, mortars=mortars if nmo else None)

@@ -79,3 +79,17 @@ def channel_state(x, mach=0.1, kappa=1.4, R=1.0, t_wall=1.0, noise=0.05, seed=0)
     prim[..., 3] = noise * u * rng.standard_normal(y.shape)
     prim[..., 4] = p0
     return prim_to_cons(prim, kappa)
+
+
+def sine_wave_state(x, t=0.0, adv_vel=(0.3, 0.3, 0.3), frequency=1.0, amplitude=0.1):
+    """exactfunc.f90 CASE(4), the oblique sine wave of the convergence tests (3D): rho = m1 = m2 = m3 =
+    2 + A sin(omega (x+y+z) - a t), E = rho^2, omega = pi * frequency, a = 2 pi adv_vel[0]. With its source
+    term (CalcSource CASE(4)) it solves the Navier-Stokes equations exactly."""
+    x = np.asarray(x, np.float64)
+    om = np.pi * frequency
+    a = adv_vel[0] * 2.0 * np.pi
+    g = 2.0 + amplitude * np.sin(om * x.sum(axis=-1) - a * t)
+    U = np.empty(x.shape[:-1] + (5,))
+    U[..., 0:4] = g[..., None]
+    U[..., 4] = g * g
+    return U

@@ -122,14 +122,16 @@ int fg_get_config(const fg_handle* h, fg_config* out);
 
 /* HOPR mesh files (the file part of mesh_readin.f90:ReadMesh/ReadBCs, datasets ElemInfo, SideInfo,
  * NodeCoords, BCType, BCNames, attribute Ngeo), read without the HDF5 library (contiguous datasets of the
- * classic file format, as HOPR writes them). fg_hopr_sizes: out[0]=nElems, out[1]=NGeo, out[2]=nBCs.
- * fg_hopr_read fills the inputs of fg_build_mesh: NodeCoords(3,0:NGeo,0:NGeo,0:NGeo,nElems),
+ * classic file format, as HOPR writes them). fg_hopr_sizes: out[0]=nElems, out[1]=NGeo, out[2]=nBCs,
+ * out[3]=nMortars. fg_hopr_read fills the inputs of fg_build_mesh: NodeCoords(3,0:NGeo,0:NGeo,0:NGeo,nElems),
  * ElemNb(3,6,nElems) (neighbour element, its local side, BC index; BC sides of types other than 0/1/100
- * are boundaries, mesh_readin.f90:398-456), BoundaryType(2,nBCs) = (BCType(1), BCType(3)) and BCNames
- * (nBCs x 256 chars, NUL-terminated; may be NULL). Hexahedra only, no mortar interfaces. Errors in
- * fg_io_last_error(). */
+ * are boundaries, mesh_readin.f90:398-456; -1 for the big and small sides of a mortar),
+ * BoundaryType(2,nBCs) = (BCType(1), BCType(3)), BCNames (nBCs x 256 chars, NUL-terminated; may be NULL)
+ * and Mortars(15,nMortars) (big element, its local side, mortar type 1: 1->4, 2: 1->2 in eta, 3: 1->2 in
+ * xi, then per small side: small element, its local side, 0; may be NULL without mortars). Hexahedra only.
+ * Errors in fg_io_last_error(). */
 int fg_hopr_sizes(const char* path, int* out);
-int fg_hopr_read(const char* path, double* NodeCoords, int* ElemNb, int* BoundaryType, char* BCNames);
+int fg_hopr_read(const char* path, double* NodeCoords, int* ElemNb, int* BoundaryType, char* BCNames, int* Mortars);
 
 /* FLEXI state files (hdf5_output.f90:WriteState): dataset DG_Solution(1:5,0:N,0:N,0:N,nElems) and the
  * header attributes (VarNames, Program, File_Type, Project_Name, File_Version, N, Dimension, Time,

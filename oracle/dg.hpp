@@ -99,6 +99,11 @@ struct Config {
   double dpdx = -1.;
   int overintType = 0;  // overintegration.f90: 0 none, 1 modal cut-off of J u_t, 2 conservative cut-off
   int NUnder = -1;      // cut-off degree (-1: N)
+  // exact function with a source term (exactfunc.f90: IniExactFunc 4, the oblique sine wave of the
+  // convergence tests; 0: no source), AdvVel, IniFrequency, IniAmplitude
+  int iniExactFunc = 0;
+  double advVel[3] = {0., 0., 0.};
+  double iniFrequency = 1.0, iniAmplitude = 0.1;
 };
 
 // changebasis.t90:ChangeBasisVolume on an element block X(nv, 0:Ni, 0:Ni, 0:Ni) -> (nv, 0:No, 0:No, 0:No),
@@ -219,6 +224,11 @@ struct DG {
   // and NUnder->N and 1/J on NUnder (type 2)
   std::vector<double> OverintegrationMat, Vdm_N_NUnder, Vdm_NUnder_N, sJNUnder;
   int NU = 0;
+  // mortar operators (mortar.f90:InitMortar), (n x n) with X[l*n+p] = X(l,p): big-to-small interpolation
+  // M_0_1/M_0_2 (U_Mortar), small-to-big projection M_1_0/M_2_0 (Flux_Mortar); the element whose data a
+  // small mortar side's master slot carries (the big element)
+  std::vector<double> M_0_1, M_0_2, M_1_0, M_2_0;
+  std::vector<int> sideMasterElem;  // [nSides] 0-based element of the master data (-1: none)
 
   size_t vi(int v, int i, int j, int k, int e, int nv) const { return ((((size_t)e * n + k) * n + j) * n + i) * nv + v; }
   size_t si(int v, int p, int q, int s, int nv) const { return (((size_t)s * n + q) * n + p) * nv + v; }
@@ -235,6 +245,7 @@ struct DG {
     s23 = 2. / 3.; s43 = 4. / 3.;
     if (C.etaBR2_wall == -1.) C.etaBR2_wall = C.etaBR2;
     init_overintegration();
+    init_mortar();
     const size_t nv3 = (size_t)n * n * n, ns2 = (size_t)n * n;
     U.assign(5 * nv3 * nE, R(0.)); Ut = U; Ut_tmp = U;
     UPrim.assign(6 * nv3 * nE, R(0.));
@@ -285,6 +296,169 @@ struct DG {
       }
     }
   }
+
+  // exactfunc.f90:CalcSource CASE(4) (3D): source of the oblique sine wave rho = m_i = 2 + A sin(omega sum(x) - a t),
+  // E = rho^2, with omega = pi IniFrequency, a = 2 pi AdvVel(1)
+  void sine_wave_source(const double* x, double t, double* src) const {
+    const double om = M_PI * C.iniFrequency, A = C.iniAmplitude, a = C.advVel[0] * 2. * M_PI;
+    const double k = val(kappa), km1 = val(kappaM1);
+    double tmp[6];
+    tmp[0] = -a + 3. * om;
+    tmp[1] = -a + 0.5 * om * (1. + k * 5.);
+    tmp[2] = A * om * km1;
+    tmp[3] = 0.5 * ((9. + k * 15.) * om - 8. * a);
+    tmp[4] = A * (3. * om * k - a);
+    tmp[5] = 3. * val(mu0) * k * om * om / C.Pr;
+    for (double& v : tmp) v *= A;
+    const double ph = om * (x[0] + x[1] + x[2]) - a * t;
+    const double c = std::cos(ph), sn = std::sin(ph), s2 = 2. * sn * c;
+    src[0] = tmp[0] * c;
+    src[1] = src[2] = src[3] = tmp[1] * c + tmp[2] * s2;
+    src[4] = tmp[3] * c + tmp[4] * s2 + tmp[5] * sn;
+  }
+
+  // mortar.f90:InitMortar -- MortarBasis_BigToSmall / MortarBasis_SmallToBig
+  void init_mortar() {
+    sideMasterElem.assign(nS, -1);
+    for (int s = 0; s < nS; ++s) sideMasterElem[s] = s2e(0, s) - 1;
+    if (M.nMortars == 0) return;
+    if (C.lifting == 2) throw std::runtime_error("mortar interfaces with BR2 lifting are not restated");
+    if (C.splitDG != SPLIT_NONE && C.nodeType == NT_GAUSS) throw std::runtime_error("mortar interfaces with the split form on Gauss nodes are not restated");
+    for (int s = 0; s < nS; ++s)
+      if (M.MortarType[(size_t)s * 2] > 0) {
+        const int m = M.MortarType[(size_t)s * 2 + 1] - 1, nm = M.MortarType[(size_t)s * 2] == 1 ? 4 : 2;
+        for (int i = 0; i < nm; ++i) sideMasterElem[M.MortarInfo[((size_t)m * 4 + i) * 2] - 1] = s2e(0, s) - 1;
+      }
+    M_0_1.assign((size_t)n * n, 0.); M_0_2 = M_0_1; M_1_0 = M_0_1; M_2_0 = M_0_1;
+    for (int p = 0; p < n; ++p) {
+      std::vector<double> L1(n), L2(n);
+      lagrange_polys(0.5 * (B.xGP[p] - 1.), N, B.xGP.data(), B.wBary.data(), L1.data());
+      lagrange_polys(0.5 * (B.xGP[p] + 1.), N, B.xGP.data(), B.wBary.data(), L2.data());
+      for (int l = 0; l < n; ++l) { M_0_1[(size_t)l * n + p] = L1[l]; M_0_2[(size_t)l * n + p] = L2[l]; }
+    }
+    // M_1_0 = (Vdm_Leg Vphi1^T W VGP)^T, VGP: nodes -> Gauss, W: Gauss weights, Vphi1/2: normalised Legendre
+    // polynomials at the Gauss nodes mapped to [-1,0] / [0,1]
+    std::vector<double> xg(n), wg(n), wbg(n);
+    nodes_and_weights(N, NT_GAUSS, xg.data(), wg.data(), wbg.data());
+    auto VGP = get_vandermonde(N, C.nodeType, N, NT_GAUSS, false);  // (gauss i, node l)
+    std::vector<double> VL((size_t)n * n), V1((size_t)n * n), V2((size_t)n * n);
+    for (int i = 0; i < n; ++i) for (int j = 0; j < n; ++j) {
+      double d;
+      legendre_poly_and_deriv(j, B.xGP[i], VL[(size_t)i * n + j], d);
+      legendre_poly_and_deriv(j, 0.5 * (xg[i] - 1.), V1[(size_t)i * n + j], d);
+      legendre_poly_and_deriv(j, 0.5 * (xg[i] + 1.), V2[(size_t)i * n + j], d);
+    }
+    for (int p = 0; p < n; ++p) for (int l = 0; l < n; ++l) {
+      double a1 = 0., a2 = 0.;
+      for (int j = 0; j < n; ++j) {
+        double b1 = 0., b2 = 0.;
+        for (int i = 0; i < n; ++i) {
+          const double wv = wg[i] * VGP[(size_t)i * n + l];
+          b1 += V1[(size_t)i * n + j] * wv;
+          b2 += V2[(size_t)i * n + j] * wv;
+        }
+        a1 += VL[(size_t)p * n + j] * b1;
+        a2 += VL[(size_t)p * n + j] * b2;
+      }
+      M_1_0[(size_t)l * n + p] = a1;  // transposed: (small l, big p)
+      M_2_0[(size_t)l * n + p] = a2;
+    }
+  }
+  // fillmortar.t90:U_Mortar -- the big side's master data interpolated to its small sides' master slots
+  template <int NV>
+  void u_mortar(std::vector<R>& Um) const {
+    if (M.nMortars == 0) return;
+    const size_t ns2 = (size_t)n * n;
+    std::vector<R> tmp2(2 * ns2 * NV), tmp(4 * ns2 * NV);
+    auto T2 = [&](int v, int p, int q, int k) -> R& { return tmp2[(((size_t)k * n + q) * n + p) * NV + v]; };
+    auto T = [&](int v, int p, int q, int k) -> R& { return tmp[(((size_t)k * n + q) * n + p) * NV + v]; };
+    auto m01 = [&](int l, int p) { return R(M_0_1[(size_t)l * n + p]); };
+    auto m02 = [&](int l, int p) { return R(M_0_2[(size_t)l * n + p]); };
+    for (int s = 0; s < nS; ++s) {
+      const int type = M.MortarType[(size_t)s * 2];
+      if (type == 0) continue;
+      auto Ub = [&](int v, int p, int q) { return Um[si(v, p, q, s, NV)]; };
+      if (type == 1) {
+        for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) for (int v = 0; v < NV; ++v) {
+          R a = m01(0, q) * Ub(v, p, 0), b = m02(0, q) * Ub(v, p, 0);
+          for (int l = 1; l < n; ++l) { a = a + m01(l, q) * Ub(v, p, l); b = b + m02(l, q) * Ub(v, p, l); }
+          T2(v, p, q, 0) = a; T2(v, p, q, 1) = b;
+        }
+        for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) for (int v = 0; v < NV; ++v) {
+          R a = m01(0, p) * T2(v, 0, q, 0), b = m02(0, p) * T2(v, 0, q, 0), c = m01(0, p) * T2(v, 0, q, 1), d = m02(0, p) * T2(v, 0, q, 1);
+          for (int l = 1; l < n; ++l) {
+            a = a + m01(l, p) * T2(v, l, q, 0); b = b + m02(l, p) * T2(v, l, q, 0);
+            c = c + m01(l, p) * T2(v, l, q, 1); d = d + m02(l, p) * T2(v, l, q, 1);
+          }
+          T(v, p, q, 0) = a; T(v, p, q, 1) = b; T(v, p, q, 2) = c; T(v, p, q, 3) = d;
+        }
+      } else if (type == 2) {  // 1->2 in eta
+        for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) for (int v = 0; v < NV; ++v) {
+          R a = m01(0, q) * Ub(v, p, 0), b = m02(0, q) * Ub(v, p, 0);
+          for (int l = 1; l < n; ++l) { a = a + m01(l, q) * Ub(v, p, l); b = b + m02(l, q) * Ub(v, p, l); }
+          T(v, p, q, 0) = a; T(v, p, q, 1) = b;
+        }
+      } else {  // 1->2 in xi
+        for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) for (int v = 0; v < NV; ++v) {
+          R a = m01(0, p) * Ub(v, 0, q), b = m02(0, p) * Ub(v, 0, q);
+          for (int l = 1; l < n; ++l) { a = a + m01(l, p) * Ub(v, l, q); b = b + m02(l, p) * Ub(v, l, q); }
+          T(v, p, q, 0) = a; T(v, p, q, 1) = b;
+        }
+      }
+      const int m = M.MortarType[(size_t)s * 2 + 1] - 1, nm = type == 1 ? 4 : 2;
+      for (int im = 0; im < nm; ++im) {
+        const int ss = M.MortarInfo[((size_t)m * 4 + im) * 2] - 1;
+        for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p)
+          for (int v = 0; v < NV; ++v) Um[si(v, p, q, ss, NV)] = T(v, p, q, im);
+      }
+    }
+    (void)ns2;
+  }
+  // fillmortar.t90:Flux_Mortar -- the small sides' master fluxes projected onto the big side
+  template <int NV>
+  void flux_mortar(std::vector<R>& Fm) const {
+    if (M.nMortars == 0) return;
+    std::vector<R> tmp2(2 * (size_t)n * n * NV);
+    auto T2 = [&](int v, int p, int q, int k) -> R& { return tmp2[(((size_t)k * n + q) * n + p) * NV + v]; };
+    auto m1 = [&](int l, int p) { return R(M_1_0[(size_t)l * n + p]); };
+    auto m2 = [&](int l, int p) { return R(M_2_0[(size_t)l * n + p]); };
+    for (int s = 0; s < nS; ++s) {
+      const int type = M.MortarType[(size_t)s * 2];
+      if (type == 0) continue;
+      const int m = M.MortarType[(size_t)s * 2 + 1] - 1;
+      int sm[4];
+      for (int im = 0; im < (type == 1 ? 4 : 2); ++im) sm[im] = M.MortarInfo[((size_t)m * 4 + im) * 2] - 1;
+      auto F = [&](int im, int v, int p, int q) { return Fm[si(v, p, q, sm[im], NV)]; };
+      if (type == 1) {
+        for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) for (int v = 0; v < NV; ++v) {
+          R a = m1(0, p) * F(0, v, 0, q) + m2(0, p) * F(1, v, 0, q), b = m1(0, p) * F(2, v, 0, q) + m2(0, p) * F(3, v, 0, q);
+          for (int l = 1; l < n; ++l) {
+            a = a + m1(l, p) * F(0, v, l, q) + m2(l, p) * F(1, v, l, q);
+            b = b + m1(l, p) * F(2, v, l, q) + m2(l, p) * F(3, v, l, q);
+          }
+          T2(v, p, q, 0) = a; T2(v, p, q, 1) = b;
+        }
+        for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) for (int v = 0; v < NV; ++v) {
+          R a = m1(0, q) * T2(v, p, 0, 0) + m2(0, q) * T2(v, p, 0, 1);
+          for (int l = 1; l < n; ++l) a = a + m1(l, q) * T2(v, p, l, 0) + m2(l, q) * T2(v, p, l, 1);
+          Fm[si(v, p, q, s, NV)] = a;
+        }
+      } else if (type == 2) {
+        for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) for (int v = 0; v < NV; ++v) {
+          R a = m1(0, q) * F(0, v, p, 0) + m2(0, q) * F(1, v, p, 0);
+          for (int l = 1; l < n; ++l) a = a + m1(l, q) * F(0, v, p, l) + m2(l, q) * F(1, v, p, l);
+          Fm[si(v, p, q, s, NV)] = a;
+        }
+      } else {
+        for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) for (int v = 0; v < NV; ++v) {
+          R a = m1(0, p) * F(0, v, 0, q) + m2(0, p) * F(1, v, 0, q);
+          for (int l = 1; l < n; ++l) a = a + m1(l, p) * F(0, v, l, q) + m2(l, p) * F(1, v, l, q);
+          Fm[si(v, p, q, s, NV)] = a;
+        }
+      }
+    }
+  }
+  bool big_mortar(int s) const { return !M.MortarType.empty() && M.MortarType[(size_t)s * 2] > 0; }
 
   // overintegration.f90:InitOverintegration
   void init_overintegration() {
@@ -612,6 +786,7 @@ struct DG {
     R sig = C.weakLifting ? R(1.) : R(-1.);  // sig = MERGE(1,-1,doWeakLifting)
     for (int s = M.nBCSides; s < nS; ++s)
       for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
+        if (big_mortar(s)) continue;  // lifting_fillflux.t90:227
         size_t sx = M.sidx(p, q, s);
         for (int v = 0; v < NLIFT; ++v) {
           R f = sig * UPrim_master[si(PRIM_LIFT[v], p, q, s, 6)] + UPrim_slave[si(PRIM_LIFT[v], p, q, s, 6)];
@@ -634,6 +809,10 @@ struct DG {
           gradUz_m[si(v, p, q, s, NLIFT)] = f * R(M.NormVec[sx * 3 + 2]);
         }
       }
+      // lifting_br1.t90:106-109: the small sides' lifting fluxes projected onto the big mortar sides
+      flux_mortar<NLIFT>(gradUx_m);
+      flux_mortar<NLIFT>(gradUy_m);
+      flux_mortar<NLIFT>(gradUz_m);
       R slaveSign = C.weakLifting ? R(-1.) : R(1.);
       surf_int<NLIFT>(gradUx_m, gradUx_m, gradUx, slaveSign);
       surf_int<NLIFT>(gradUy_m, gradUy_m, gradUy, slaveSign);
@@ -642,6 +821,9 @@ struct DG {
       prolong_to_face<NLIFT>(gradUx, gradUx_m, gradUx_s);
       prolong_to_face<NLIFT>(gradUy, gradUy_m, gradUy_s);
       prolong_to_face<NLIFT>(gradUz, gradUz_m, gradUz_s);
+      u_mortar<NLIFT>(gradUx_m);  // lifting_br1.t90:175-178
+      u_mortar<NLIFT>(gradUy_m);
+      u_mortar<NLIFT>(gradUz_m);
     } else {
       apply_jacobian_lift();
       prolong_to_face<NLIFT>(gradUx, gradUx_m, gradUx_s);
@@ -863,6 +1045,7 @@ struct DG {
 #pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
     for (int s = M.nBCSides; s < nS; ++s)
       for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
+        if (big_mortar(s)) continue;  // no slave: the big side's flux is the projection of its small sides'
         size_t sx = M.sidx(p, q, s);
         R F[5];
         riemann_rot(C.riemann, &U_master[si(0, p, q, s, 5)], &UPrim_master[si(0, p, q, s, 6)], &U_slave[si(0, p, q, s, 5)],
@@ -870,7 +1053,7 @@ struct DG {
         // riemann.f90:ViscousFlux_Point
         R fL[5], gL[5], hL[5], fR[5], gR[5], hR[5];
         diff_flux(&UPrim_master[si(0, p, q, s, 6)], &gradUx_m[si(0, p, q, s, NLIFT)], &gradUy_m[si(0, p, q, s, NLIFT)], &gradUz_m[si(0, p, q, s, NLIFT)], fL, gL, hL,
-                  elem_mu_scale(s2e(0, s) - 1));
+                  elem_mu_scale(sideMasterElem[s]));
         diff_flux(&UPrim_slave[si(0, p, q, s, 6)], &gradUx_s[si(0, p, q, s, NLIFT)], &gradUy_s[si(0, p, q, s, NLIFT)], &gradUz_s[si(0, p, q, s, NLIFT)], fR, gR, hR,
                   elem_mu_scale(s2e(1, s) - 1));
         const double* nv = &M.NormVec[sx * 3];
@@ -902,6 +1085,7 @@ struct DG {
       R se = R(M.SurfElem[M.sidx(p, q, s)]);
       for (int v = 0; v < 5; ++v) { Flux_master[si(v, p, q, s, 5)] = Flux_master[si(v, p, q, s, 5)] * se; Flux_slave[si(v, p, q, s, 5)] = Flux_master[si(v, p, q, s, 5)]; }
     }
+    flux_mortar<5>(Flux_master);  // dg.f90:625
   }
 
   // ---------------- volint.f90 ----------------
@@ -995,7 +1179,7 @@ struct DG {
     phase[0] = fc;
 #pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
     for (int e = 0; e < nE; ++e) for (size_t x = 0; x < nv3; ++x) cons_to_prim(&U[((size_t)e * nv3 + x) * 5], &UPrim[((size_t)e * nv3 + x) * 6]);
-    if (!entropyVars) prolong_to_face<5>(U, U_master, U_slave);
+    if (!entropyVars) { prolong_to_face<5>(U, U_master, U_slave); u_mortar<5>(U_master); }  // dg.f90:372-416
     else {
       // eos.f90:ConsToPrimToEntropy, prolongtoface.t90:ProlongToFaceEntropy (EntropyToCons on every side
       // of an existing element)
@@ -1011,7 +1195,7 @@ struct DG {
     // equation.f90:GetPrimitiveStateSurface
     for (int s = 0; s < nS; ++s) for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
       cons_to_prim(&U_master[si(0, p, q, s, 5)], &UPrim_master[si(0, p, q, s, 6)]);
-      if (s >= M.nBCSides) cons_to_prim(&U_slave[si(0, p, q, s, 5)], &UPrim_slave[si(0, p, q, s, 6)]);
+      if (s2e(1, s) > 0) cons_to_prim(&U_slave[si(0, p, q, s, 5)], &UPrim_slave[si(0, p, q, s, 6)]);
     }
     phase[1] = fc;
     lifting();
@@ -1029,6 +1213,12 @@ struct DG {
         double sj = M.sJ[(size_t)e * nv3 + x];
         R* ut = &Ut[((size_t)e * nv3 + x) * 5];
         for (int v = 0; v < 5; ++v) ut[v] = -ut[v];
+        if (C.iniExactFunc == 4) {  // exactfunc.f90:CalcSource, CASE(4)
+          const double* xg = &M.Elem_xGP[((size_t)e * nv3 + x) * 3];
+          double src[5];
+          sine_wave_source(xg, t, src);
+          for (int v = 0; v < 5; ++v) ut[v] = ut[v] + R(src[v]) / R(sj);
+        }
         if (C.doTCSource) {
           ut[1] = ut[1] - R(C.dpdx) / R(sj);
           ut[4] = ut[4] - R(C.dpdx) / R(sj) * BulkVel;

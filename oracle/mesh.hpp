@@ -79,6 +79,10 @@ struct MeshInput {
   int nBCs = 0;
   std::vector<int> BoundaryType;   // (2,nBCs): type, state
   std::vector<double> RefStatePrim;  // (6,nRefStates)
+  // mortar interfaces, 15 per mortar: big element (1-based), its local side, mortar type (1: 1->4, 2: 1->2 in
+  // eta, 3: 1->2 in xi), then for the 2 or 4 small sides: small element (1-based), its local side, unused;
+  // the ElemNb entries of these element sides are -1
+  std::vector<int> Mortars;
 };
 
 // Processed mesh: everything MOD_Mesh_Vars provides to the DG operator.
@@ -88,6 +92,10 @@ struct Mesh {
   std::vector<int> SideToElem;  // (5,nSides) 1-based entries as in FLEXI, -1 if none
   std::vector<int> ElemToSide;  // (2,6,nElems)
   std::vector<int> BC;          // (nBCSides) -> BC index (1-based)
+  // mortars (mesh_vars.f90): MortarType(2,nSides) = type, mortar index (1-based) of a big mortar side;
+  // MortarInfo(2,4,nMortars) = small SideID (1-based), flip (0: the big element is master)
+  int nMortars = 0;
+  std::vector<int> MortarType, MortarInfo;
   std::vector<int> BoundaryType;  // (2,nBCs)
   std::vector<double> RefStatePrim;
   std::vector<double> Mf, Mg, Mh;  // Metrics_f/g/hTilde (3,0:N,0:N,0:N,nElems)
@@ -142,25 +150,32 @@ inline void build_mesh(const MeshInput& in, int N, int nodeType, Mesh& M) {
   auto nc = [&](int d, int i, int j, int k, int e) { return in.NodeCoords[((((size_t)e * ng + k) * ng + j) * ng + i) * 3 + d]; };
   auto nb = [&](int c, int ls, int e) { return in.ElemNb[((size_t)e * 6 + (ls - 1)) * 3 + c]; };
 
-  // ---- sides: BC sides first, then inner sides (prepare_mesh.f90: setLocalSideIDs ordering, no MPI sides) ----
+  // ---- sides: BC sides, big mortar sides, inner sides, small mortar sides (no MPI sides) ----
   std::vector<int> sideOf(6 * nE, -1), flipOf(6 * nE, 0);
   struct S { int e, ls, nbe, nbls, bc; };
   std::vector<S> bcs, inner;
   for (int e = 0; e < nE; ++e)
     for (int ls = 1; ls <= 6; ++ls) {
       int ne = nb(0, ls, e), nls = nb(1, ls, e), bci = nb(2, ls, e);
+      if (ne < 0) continue;  // mortar
       if (ne == 0) { bcs.push_back({e, ls, -1, -1, bci}); continue; }
       int oe = ne - 1;
       // master = element with smaller id (same element: smaller local side id)
       bool iAmMaster = (e < oe) || (e == oe && ls < nls);
       if (iAmMaster) inner.push_back({e, ls, oe, nls, 0});
     }
-  M.nBCSides = (int)bcs.size(); M.nInnerSides = (int)inner.size();
-  M.nSides = M.nBCSides + M.nInnerSides;
-  M.firstInnerSide = M.nBCSides + 1; M.lastInnerSide = M.nSides;
+  const int nMo = (int)in.Mortars.size() / 15;
+  int nSmall = 0;
+  for (int m = 0; m < nMo; ++m) nSmall += in.Mortars[(size_t)m * 15 + 2] == 1 ? 4 : 2;
+  M.nMortars = nMo;
+  M.nBCSides = (int)bcs.size(); M.nInnerSides = (int)inner.size() + nSmall;
+  M.nSides = M.nBCSides + nMo + M.nInnerSides;
+  M.firstInnerSide = M.nBCSides + nMo + 1; M.lastInnerSide = M.nSides;
   M.SideToElem.assign(5 * M.nSides, -1);
   M.ElemToSide.assign(2 * 6 * nE, 0);
   M.BC.assign(M.nBCSides, 0);
+  M.MortarType.assign(2 * M.nSides, 0);
+  M.MortarInfo.assign(2 * 4 * nMo, 0);
   auto s2e = [&](int c, int s) -> int& { return M.SideToElem[(size_t)s * 5 + c]; };
   auto e2s = [&](int c, int ls, int e) -> int& { return M.ElemToSide[((size_t)e * 6 + (ls - 1)) * 2 + c]; };
   for (int s = 0; s < M.nBCSides; ++s) {
@@ -177,28 +192,85 @@ inline void build_mesh(const MeshInput& in, int N, int nodeType, Mesh& M) {
     face_vol_index(ls, ij[0], ij[1], l, NG, i, j, k);
     for (int d = 0; d < 3; ++d) x[d] = nc(d, i, j, k, e);
   };
-  for (int t = 0; t < M.nInnerSides; ++t) {
-    const S& si = inner[t];
-    int s = M.nBCSides + t;
-    int best = -1;
-    for (int f = 0; f <= 4 && best < 0; ++f) {
-      double shift[3]; bool ok = true; bool first = true;
-      for (int q = 0; q <= NG && ok; q += NG) for (int p = 0; p <= NG && ok; p += NG) {
-        double xm[3], xs[3];
-        face_node(si.e, si.ls, p, q, xm);
-        // slave node that pairs with master (p,q): slave side coords Flip_M2S(p,q,f)
+  // flip of the slave whose face corners match the master corners xm(c) (c = p + 2q over the NGeo corners)
+  auto match_flip = [&](const double (*xm)[3], int nbe, int nbls) {
+    for (int f = 1; f <= 4; ++f) {
+      double shift[3]; bool ok = true;
+      for (int c = 0; c < 4 && ok; ++c) {
+        const int p = (c & 1) ? NG : 0, q = (c & 2) ? NG : 0;
+        double xs[3];
         auto ab = flip_s2m(NG, p, q, f);
-        face_node(si.nbe, si.nbls, ab[0], ab[1], xs);
-        double d[3] = {xs[0] - xm[0], xs[1] - xm[1], xs[2] - xm[2]};
-        if (first) { for (int c = 0; c < 3; ++c) shift[c] = d[c]; first = false; }
-        else for (int c = 0; c < 3; ++c) if (std::fabs(d[c] - shift[c]) > 1e-9 * (1. + std::fabs(shift[c]))) ok = false;
+        face_node(nbe, nbls, ab[0], ab[1], xs);
+        double d[3] = {xs[0] - xm[c][0], xs[1] - xm[c][1], xs[2] - xm[c][2]};
+        if (c == 0) { for (int k = 0; k < 3; ++k) shift[k] = d[k]; }
+        else for (int k = 0; k < 3; ++k) if (std::fabs(d[k] - shift[k]) > 1e-9 * (1. + std::fabs(shift[k]))) ok = false;
       }
-      if (ok && f > 0) best = f;  // flip 0 is reserved for master sides
+      if (ok) return f;
     }
+    return -1;
+  };
+  // big mortar sides: master = the big element, no slave (prepare_mesh.f90, MortarType)
+  const int firstBig = M.nBCSides;
+  for (int m = 0; m < nMo; ++m) {
+    const int* r = &in.Mortars[(size_t)m * 15];
+    const int s = firstBig + m;
+    s2e(0, s) = r[0]; s2e(1, s) = -1; s2e(2, s) = r[1]; s2e(3, s) = -1; s2e(4, s) = 0;
+    e2s(0, r[1], r[0] - 1) = s + 1; e2s(1, r[1], r[0] - 1) = 0;
+    M.MortarType[(size_t)s * 2 + 0] = r[2]; M.MortarType[(size_t)s * 2 + 1] = m + 1;
+  }
+  for (int t = 0; t < (int)inner.size(); ++t) {
+    const S& si = inner[t];
+    const int s = firstBig + nMo + t;
+    double xm[4][3];
+    for (int c = 0; c < 4; ++c) face_node(si.e, si.ls, (c & 1) ? NG : 0, (c & 2) ? NG : 0, xm[c]);
+    const int best = match_flip(xm, si.nbe, si.nbls);
     if (best < 0) throw std::runtime_error("could not determine side flip");
     s2e(0, s) = si.e + 1; s2e(1, s) = si.nbe + 1; s2e(2, s) = si.ls; s2e(3, s) = si.nbls; s2e(4, s) = best;
     e2s(0, si.ls, si.e) = s + 1; e2s(1, si.ls, si.e) = 0;
     e2s(0, si.nbls, si.nbe) = s + 1; e2s(1, si.nbls, si.nbe) = best;
+  }
+  // small mortar sides: no master element (its data come from the big side, U_Mortar), the small element is
+  // the slave; orientation of the big side's quadrant, flip found from the quadrant corners
+  {
+    int s = firstBig + nMo + (int)inner.size();
+    std::vector<double> Leq(ng);
+    std::vector<double> xe(ng);
+    for (int a = 0; a < ng; ++a) xe[a] = NG == 0 ? 0. : -1. + 2. * a / NG;
+    auto lag = [&](double x, std::vector<double>& L) {
+      for (int a = 0; a < ng; ++a) {
+        double v = 1.;
+        for (int b = 0; b < ng; ++b) if (b != a) v *= (x - xe[b]) / (xe[a] - xe[b]);
+        L[a] = v;
+      }
+    };
+    std::vector<double> La(ng), Lb(ng);
+    for (int m = 0; m < nMo; ++m) {
+      const int* r = &in.Mortars[(size_t)m * 15];
+      const int be = r[0] - 1, bls = r[1], type = r[2], nm = type == 1 ? 4 : 2;
+      for (int im = 0; im < nm; ++im, ++s) {
+        const int se = r[3 + 3 * im] - 1, sls = r[4 + 3 * im];
+        // quadrant of the big side (p: xi, q: eta of the side) covered by small side im
+        const int iNb = type == 1 ? im % 2 : (type == 3 ? im : -1), jNb = type == 1 ? im / 2 : (type == 2 ? im : -1);
+        double xm[4][3];
+        for (int c = 0; c < 4; ++c) {
+          const double xi = iNb < 0 ? ((c & 1) ? 1. : -1.) : ((c & 1) ? (iNb ? 1. : 0.) : (iNb ? 0. : -1.));
+          const double eta = jNb < 0 ? ((c & 2) ? 1. : -1.) : ((c & 2) ? (jNb ? 1. : 0.) : (jNb ? 0. : -1.));
+          lag(xi, La); lag(eta, Lb);
+          for (int d = 0; d < 3; ++d) xm[c][d] = 0.;
+          for (int b = 0; b < ng; ++b) for (int a = 0; a < ng; ++a) {
+            double x[3];
+            face_node(be, bls, a, b, x);
+            for (int d = 0; d < 3; ++d) xm[c][d] += La[a] * Lb[b] * x[d];
+          }
+        }
+        const int f = match_flip(xm, se, sls);
+        if (f < 0) throw std::runtime_error("mortar: small face does not match its quadrant of the big face");
+        s2e(0, s) = -1; s2e(1, s) = se + 1; s2e(2, s) = -1; s2e(3, s) = sls; s2e(4, s) = f;
+        e2s(0, sls, se) = s + 1; e2s(1, sls, se) = f;
+        M.MortarInfo[((size_t)m * 4 + im) * 2 + 0] = s + 1;
+        M.MortarInfo[((size_t)m * 4 + im) * 2 + 1] = 0;
+      }
+    }
   }
 
   // ---- metrics: metrics.f90:CalcMetrics (curl form, no tree) ----
@@ -338,6 +410,7 @@ inline void build_mesh(const MeshInput& in, int N, int nodeType, Mesh& M) {
         for (int c = 0; c < 3; ++c) JaN[M.sidx(p, q, SideID) * 3 + c] = JaF[((size_t)q * n + p) * 9 + nd * 3 + c];
       if (flip != 0) continue;
       // SurfMetricsFromJa
+      auto surf_metrics = [&](const std::vector<double>& JaF, int SideID) {
       for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
         const double* J = &JaF[((size_t)q * n + p) * 9];
         size_t si = M.sidx(p, q, SideID);
@@ -353,6 +426,60 @@ inline void build_mesh(const MeshInput& in, int N, int nodeType, Mesh& M) {
         t2[1] = nv[2] * t1[0] - nv[0] * t1[2];
         t2[2] = nv[0] * t1[1] - nv[1] * t1[0];
         for (int c = 0; c < 3; ++c) { M.NormVec[si * 3 + c] = nv[c]; M.TangVec1[si * 3 + c] = t1[c]; M.TangVec2[si * 3 + c] = t2[c]; }
+      }
+      };
+      surf_metrics(JaF, SideID);
+      // mortar_metrics.f90:Mortar_CalcSurfMetrics -- small sides: the big side's Ja interpolated to each
+      // quadrant and halved per split direction, coordinates interpolated
+      const int mtype = M.MortarType[(size_t)SideID * 2];
+      if (mtype > 0) {
+        const int m = M.MortarType[(size_t)SideID * 2 + 1] - 1;
+        std::vector<double> M01(nsp), M02(nsp);  // (out, in): L_in(0.5 (xi_out -/+ 1))
+        {
+          DGBasis Bm; Bm.init(N, nodeType);
+          for (int o = 0; o < n; ++o) {
+            std::vector<double> L1(n), L2(n);
+            lagrange_polys(0.5 * (Bm.xGP[o] - 1.), N, Bm.xGP.data(), Bm.wBary.data(), L1.data());
+            lagrange_polys(0.5 * (Bm.xGP[o] + 1.), N, Bm.xGP.data(), Bm.wBary.data(), L2.data());
+            for (int l = 0; l < n; ++l) { M01[(size_t)o * n + l] = L1[l]; M02[(size_t)o * n + l] = L2[l]; }
+          }
+        }
+        const int nm = mtype == 1 ? 4 : 2;
+        std::vector<double> xF((size_t)nsp * 3);
+        for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p)
+          for (int c = 0; c < 3; ++c) xF[((size_t)q * n + p) * 3 + c] = M.Face_xGP[M.sidx(p, q, SideID) * 3 + c];
+        for (int im = 0; im < nm; ++im) {
+          const int iNb = mtype == 1 ? im % 2 : (mtype == 3 ? im : -1), jNb = mtype == 1 ? im / 2 : (mtype == 2 ? im : -1);
+          const std::vector<double>* Mp = iNb < 0 ? nullptr : (iNb ? &M02 : &M01);
+          const std::vector<double>* Mq = jNb < 0 ? nullptr : (jNb ? &M02 : &M01);
+          std::vector<double> Js((size_t)nsp * 9), xs((size_t)nsp * 3);
+          for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
+            for (int c = 0; c < 9; ++c) {
+              double acc = 0.;
+              for (int b = 0; b < n; ++b) for (int a = 0; a < n; ++a) {
+                const double wp = Mp ? 0.5 * (*Mp)[(size_t)p * n + a] : (a == p ? 1. : 0.);
+                const double wq = Mq ? 0.5 * (*Mq)[(size_t)q * n + b] : (b == q ? 1. : 0.);
+                if (wp != 0. && wq != 0.) acc += wp * wq * JaF[((size_t)b * n + a) * 9 + c];
+              }
+              Js[((size_t)q * n + p) * 9 + c] = acc;
+            }
+            for (int c = 0; c < 3; ++c) {
+              double acc = 0.;
+              for (int b = 0; b < n; ++b) for (int a = 0; a < n; ++a) {
+                const double wp = Mp ? (*Mp)[(size_t)p * n + a] : (a == p ? 1. : 0.);
+                const double wq = Mq ? (*Mq)[(size_t)q * n + b] : (b == q ? 1. : 0.);
+                if (wp != 0. && wq != 0.) acc += wp * wq * xF[((size_t)b * n + a) * 3 + c];
+              }
+              xs[((size_t)q * n + p) * 3 + c] = acc;
+            }
+          }
+          const int small = M.MortarInfo[((size_t)m * 4 + im) * 2] - 1;
+          surf_metrics(Js, small);
+          for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
+            for (int c = 0; c < 3; ++c) M.Face_xGP[M.sidx(p, q, small) * 3 + c] = xs[((size_t)q * n + p) * 3 + c];
+            for (int c = 0; c < 3; ++c) M.JaN_master[M.sidx(p, q, small) * 3 + c] = Js[((size_t)q * n + p) * 9 + nd * 3 + c];
+          }
+        }
       }
     }
   }

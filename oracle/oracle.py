@@ -23,10 +23,13 @@ class OrcConfig(ctypes.Structure):
                 ("lifting", ctypes.c_int), ("weakLifting", ctypes.c_int), ("consLifting", ctypes.c_int), ("splitDG", ctypes.c_int),
                 ("etaBR2", ctypes.c_double), ("etaBR2_wall", ctypes.c_double), ("kappa", ctypes.c_double), ("R", ctypes.c_double),
                 ("Pr", ctypes.c_double), ("mu0", ctypes.c_double), ("CFLScale", ctypes.c_double), ("DFLScale", ctypes.c_double),
-                ("doTCSource", ctypes.c_int), ("dpdx", ctypes.c_double), ("overintType", ctypes.c_int), ("NUnder", ctypes.c_int)]
+                ("doTCSource", ctypes.c_int), ("dpdx", ctypes.c_double), ("overintType", ctypes.c_int), ("NUnder", ctypes.c_int),
+                ("iniExactFunc", ctypes.c_int), ("advVel", ctypes.c_double * 3), ("iniFrequency", ctypes.c_double),
+                ("iniAmplitude", ctypes.c_double)]
 
-# keys a configuration may leave out (defaults of the reference: no overintegration, NUnder = N)
-_OPTIONAL = {"overintType": 0, "NUnder": -1}
+# keys a configuration may leave out (defaults of the reference: no overintegration, NUnder = N; no source term,
+# IniFrequency 1, IniAmplitude 0.1 of exact function 4)
+_OPTIONAL = {"overintType": 0, "NUnder": -1, "iniExactFunc": 0, "advVel": (0.0, 0.0, 0.0), "iniFrequency": 1.0, "iniAmplitude": 0.1}
 
 
 def lib():
@@ -36,7 +39,8 @@ def lib():
         _lib = ctypes.CDLL(path)
         P = ctypes.c_void_p
         _lib.orc_create.restype = P
-        _lib.orc_create.argtypes = [ctypes.POINTER(OrcConfig), ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int, P, ctypes.c_int, P]
+        _lib.orc_create.argtypes = [ctypes.POINTER(OrcConfig), ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int, P, ctypes.c_int, P,
+                                    ctypes.c_int, P]
         _lib.orc_destroy.argtypes = [P]
         _lib.orc_last_error.restype = ctypes.c_char_p
         for f in ("orc_set_state", "orc_get_state"):
@@ -84,7 +88,10 @@ def _p(a):
 def make_config(cfg: dict) -> OrcConfig:
     c = OrcConfig()
     for name, _ in OrcConfig._fields_:
-        setattr(c, name, cfg[name] if name in cfg else _OPTIONAL[name])
+        v = cfg[name] if name in cfg else _OPTIONAL[name]
+        if name == "advVel":
+            v = (ctypes.c_double * 3)(*v)
+        setattr(c, name, v)
     return c
 
 
@@ -101,7 +108,10 @@ class Oracle:
         bt = np.ascontiguousarray(mesh.boundary_type, dtype=np.int32).reshape(-1)
         rs = np.ascontiguousarray(mesh.ref_state_prim, dtype=np.float64).reshape(-1)
         self._keep = (nc, nb, bt, rs)
-        self.h = L.orc_create(ctypes.byref(self._c), mesh.n_elems, mesh.ngeo, _p(nc), _p(nb), len(bt) // 2, _p(bt), len(rs) // 6, _p(rs))
+        mo = getattr(mesh, "mortars", None)
+        mo = np.zeros((0, 15), np.int32) if mo is None else np.ascontiguousarray(mo, np.int32).reshape(-1, 15)
+        self.h = L.orc_create(ctypes.byref(self._c), mesh.n_elems, mesh.ngeo, _p(nc), _p(nb), len(bt) // 2, _p(bt), len(rs) // 6, _p(rs),
+                              len(mo), _p(mo) if len(mo) else None)
         if not self.h:
             raise RuntimeError("oracle: " + L.orc_last_error().decode())
         s = np.zeros(4, np.int32)

@@ -16,6 +16,8 @@ struct orc_config {
   int doTCSource;
   double dpdx;
   int overintType, NUnder;
+  int iniExactFunc;
+  double advVel[3], iniFrequency, iniAmplitude;
 };
 
 static Config to_cfg(const orc_config* c) {
@@ -25,6 +27,9 @@ static Config to_cfg(const orc_config* c) {
   C.etaBR2 = c->etaBR2; C.etaBR2_wall = c->etaBR2_wall; C.kappa = c->kappa; C.R = c->R; C.Pr = c->Pr; C.mu0 = c->mu0;
   C.CFLScale = c->CFLScale; C.DFLScale = c->DFLScale; C.doTCSource = c->doTCSource; C.dpdx = c->dpdx;
   C.overintType = c->overintType; C.NUnder = c->NUnder;
+  C.iniExactFunc = c->iniExactFunc;
+  for (int d = 0; d < 3; ++d) C.advVel[d] = c->advVel[d];
+  C.iniFrequency = c->iniFrequency; C.iniAmplitude = c->iniAmplitude;
   return C;
 }
 
@@ -40,10 +45,11 @@ static thread_local std::string g_err;
 const char* orc_last_error() { return g_err.c_str(); }
 
 void* orc_create(const orc_config* cfg, int nElems, int NGeo, const double* NodeCoords, const int* ElemNb, int nBCs,
-                 const int* BoundaryType, int nRefStates, const double* RefStatePrim) {
+                 const int* BoundaryType, int nRefStates, const double* RefStatePrim, int nMortars, const int* Mortars) {
   try {
     auto* h = new OrcHandle();
     MeshInput& mi = h->mi;
+    if (nMortars > 0) mi.Mortars.assign(Mortars, Mortars + (size_t)15 * nMortars);
     mi.nElems = nElems; mi.NGeo = NGeo; mi.nBCs = nBCs;
     size_t nnc = (size_t)3 * (NGeo + 1) * (NGeo + 1) * (NGeo + 1) * nElems;
     mi.NodeCoords.assign(NodeCoords, NodeCoords + nnc);

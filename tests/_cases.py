@@ -64,3 +64,26 @@ def rel_err(a, b):
     num = np.abs(a - b).reshape(-1, 5).max(axis=0)
     den = np.abs(b).reshape(-1, 5).max(axis=0)
     return float((num / np.maximum(den, 1e-300)).max())
+
+
+def _lagrange(xs, x):
+    L = np.ones((len(x), len(xs)))
+    for j in range(len(xs)):
+        for m in range(len(xs)):
+            if m != j:
+                L[:, j] *= (x - xs[m]) / (xs[j] - xs[m])
+    return L
+
+
+def l2_error(N, node_type, x, sJ, U, U_exact_fn, n_analyze=10):
+    """analyze.f90:CalcErrors on affine elements: the state interpolated from the N solution nodes to
+    n_analyze+1 Gauss-Lobatto points, L2 = sqrt(sum w J |U - U_exact|^2 / volume) per variable. x, U with
+    reversed axes (nElems, n, n, n, 3|5), sJ (nElems, n, n, n)."""
+    xs = orc.nodes_and_weights(N, node_type)[0]
+    xa, wa = orc.nodes_and_weights(n_analyze, orc.NT_GL)[:2]
+    I = _lagrange(np.asarray(xs), np.asarray(xa))
+    ip = lambda A: np.einsum('ai,bj,ck,eijkv->eabcv', I, I, I, A)
+    J = ip((1.0 / sJ)[..., None])[..., 0]
+    W = np.einsum('a,b,c->abc', wa, wa, wa) * J
+    err = ip(U) - U_exact_fn(ip(x))
+    return np.sqrt((err ** 2 * W[..., None]).sum(axis=(0, 1, 2, 3)) / W.sum())

@@ -4,8 +4,8 @@ Reads FLEXI v25.10's unit-test data (unitTests/*.bin, Fortran unformatted sequen
 4-byte length marker, little-endian payload, closing marker) and the Taylor-Green regression
 references (regressioncheck/checks/tgv/{split,splitGauss,oInt}/TGV_Re1600_*_TGVAnalysis_Reference.csv),
 and stores the arrays the parity tests need in reference_unittests.npz, tgv_split_reference.npz,
-tgv_splitgauss_reference.npz and tgv_oint_reference.npz; copies six HOPR mesh / FLEXI state files of
-the reference's test cases to hopr/ for the HDF5 reader.
+tgv_splitgauss_reference.npz and tgv_oint_reference.npz; copies eleven HOPR mesh / FLEXI state files
+of the reference's test cases to hopr/ for the HDF5 reader.
 
 Run from the repository root in a container that has the reference mounted:
     python tests/golden/make_golden.py /root/reference
@@ -102,7 +102,9 @@ def main(ref):
                 "regressioncheck/checks/convtest/p_3D_mortar/CART_HEX_PERIODIC_MORTAR_002_mesh.h5",
                 "regressioncheck/checks/timedisc/freestream_3D/cartbox3D_mesh.h5",
                 "regressioncheck/checks/timedisc/freestream_3D/cartbox_State_0000000.000000000.h5",
-                "tutorials/naca0012/NACA0012_652_Ng2_mesh.h5"):
+                "tutorials/naca0012/NACA0012_652_Ng2_mesh.h5",
+                "regressioncheck/checks/run_basic/freestream_3D/cartbox3D_mortar_mesh.h5") + tuple(
+                f"regressioncheck/checks/convtest/h_3D_mortar/CART_HEX_PERIODIC_MORTAR_FLIPPED_{k:03d}_mesh.h5" for k in (1, 2, 4, 8)):
         shutil.copyfile(os.path.join(ref, src), os.path.join(hdir, os.path.basename(src)))
     print("wrote fixtures:", sorted(out.keys()))
 
