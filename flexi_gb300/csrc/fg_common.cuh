@@ -74,6 +74,10 @@ struct Dev {
   double* scratch;  // element kernels whose per-element arrays exceed shared memory (lines of 9..12 nodes):
                     // [block][scratchStride] (null otherwise)
   long long scratchStride;
+  // mortar interfaces (mortar.f90): sides are ordered BC | conforming inner | small mortar | big mortar;
+  // k_flux handles the first nFluxSides, the mortar kernels the rest
+  int nFluxSides, nMortars;
+  double* mortarLift;  // [m][12][n2] BR1 lifting flux times normal (4*dir + var) projected onto big side m
   int* err;        // [1] sticky error word
   double* dtElem;  // [2][nElems] convective and viscous element time-step limits of the last CALCTIMESTEP
 };
@@ -86,6 +90,16 @@ struct OverintDev {
   const double* VNU;    // [nu][n]: Vdm_N_NUnder(iU,i)
   const double* VUN;    // [n][nu]: Vdm_NUnder_N(i,iU)
   const double* sJNU;   // [e][nu^3]: 1/J on the NUnder nodes
+};
+
+// Mortar operators and table (mortar.f90:InitMortar, fillmortar.t90), passed to the mortar kernels only.
+// Big mortar side m is side nSides - nMortars + m, its small sides are listed in info.
+struct MortarDev {
+  const int* info;                // [m][6]: type (1: 1->4, 2: 1->2 in eta, 3: 1->2 in xi), big side, small sides (-1: unused)
+  double M01[FG_MAXN * FG_MAXN];  // [l*n+p] = M_0_1(l,p): big-side node l -> small-side node p, first half
+  double M02[FG_MAXN * FG_MAXN];  // second half
+  double M10[FG_MAXN * FG_MAXN];  // [l*n+p] = M_1_0(l,p): small-side node l (first half) -> big-side node p (L2 projection)
+  double M20[FG_MAXN * FG_MAXN];  // second half
 };
 
 // viscosity of element e: its instance's mu0 times its multiplier

@@ -229,6 +229,8 @@ struct fg_handle {
   // overintegration in use (type 2 is off when NUnder >= N, overintegration.f90:139-141) and its matrices
   OverintDev ov{};
   int NU = 0;
+  // mortar interfaces: operators and the device copy of the mortar table (Dev::nMortars > 0)
+  MortarDev mort{};
   cudaGraphExec_t graph = nullptr;
   long long launches = 0;
   std::string err;
@@ -411,6 +413,11 @@ void init_basis(fg_handle* h) {
 int upload_mesh(fg_handle* h) {
   fgh::HostMesh& M = h->M;
   fgh::finish_mesh(M, h->cfg.kappa, h->cfg.Pr);
+  if (M.nMortars > 0) {
+    if (h->cfg.Lifting != 1) return fail(h, FG_ERR_CONFIG, "mortar interfaces need BR1 lifting");
+    if (h->cfg.SplitDG >= 0 && h->cfg.NodeType == FG_NODE_GAUSS)
+      return fail(h, FG_ERR_CONFIG, "mortar interfaces with the split form need Gauss-Lobatto nodes");
+  }
   h->haveHostMesh = true;
   free_device(h);
   if (!h->st) CUDA_TRY(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
@@ -420,7 +427,43 @@ int upload_mesh(fg_handle* h) {
   Dev& d = h->d;
   d = Dev{};
   d.nElems = nE; d.nSides = nS; d.nBCSides = M.nBCSides; d.nInst = M.nInst;
+  d.nFluxSides = M.nFluxSides; d.nMortars = M.nMortars;
   int r = 0;
+  if (M.nMortars > 0) {
+    // mortar.f90:InitMortar: M_0_1/M_0_2 interpolate to the halves [-1,0]/[0,1]; M_1_0/M_2_0 = (Vdm_Leg
+    // Vphi^T W VGP)^T project back, with Vphi the orthonormal Legendre polynomials at the Gauss points mapped
+    // to each half, W the Gauss weights and VGP the interpolation from the solution nodes to the Gauss points
+    const int N = M.N;
+    fgh::Vec x, w, xg, wg, x1, x2;
+    fgh::nodes(N, M.nodeType, x, w);
+    fgh::nodes(N, fgh::GAUSS, xg, wg);
+    for (double v : x) { x1.push_back(0.5 * (v - 1.)); x2.push_back(0.5 * (v + 1.)); }
+    const fgh::Mat I1 = fgh::interp_matrix(x, x1), I2 = fgh::interp_matrix(x, x2), VGP = fgh::interp_matrix(x, xg);
+    MortarDev& mo = h->mort;
+    mo = MortarDev{};
+    double dL;
+    for (int l = 0; l < n; ++l)
+      for (int p = 0; p < n; ++p) { mo.M01[l * n + p] = I1(p, l); mo.M02[l * n + p] = I2(p, l); }
+    for (int p = 0; p < n; ++p)
+      for (int l = 0; l < n; ++l) {
+        double a1 = 0., a2 = 0.;
+        for (int j = 0; j < n; ++j) {
+          double vl, b1 = 0., b2 = 0.;
+          fgh::legendre(j, x[p], vl, dL);
+          for (int i = 0; i < n; ++i) {
+            double v1, v2;
+            fgh::legendre(j, 0.5 * (xg[i] - 1.), v1, dL);
+            fgh::legendre(j, 0.5 * (xg[i] + 1.), v2, dL);
+            b1 += v1 * wg[i] * VGP(i, l);
+            b2 += v2 * wg[i] * VGP(i, l);
+          }
+          a1 += vl * b1;
+          a2 += vl * b2;
+        }
+        mo.M10[l * n + p] = a1;
+        mo.M20[l * n + p] = a2;
+      }
+  }
   if ((r = dalloc(h, d.U, (size_t)nE * 5 * n3))) return r;
   if ((r = dalloc(h, d.Ut, (size_t)nE * 5 * n3))) return r;
   if ((r = dalloc(h, d.Ut_tmp, (size_t)nE * 5 * n3))) return r;
@@ -449,6 +492,12 @@ int upload_mesh(fg_handle* h) {
   if ((r = upload(h, d.sideInst, M.sideInst))) return r;
   if ((r = upload(h, d.bcType, M.bcType))) return r;
   if ((r = upload(h, d.bcTwall, M.bcTwall))) return r;
+  if (M.nMortars > 0) {
+    int* info = nullptr;
+    if ((r = upload(h, info, M.mortarInfo))) return r;
+    h->mort.info = info;
+    if ((r = dalloc(h, d.mortarLift, (size_t)M.nMortars * 12 * n2))) return r;
+  }
   std::vector<double> mu(M.nInst, h->cfg.mu0), zero(M.nInst, 0.), dp(M.nInst, h->cfg.doTCSource ? h->cfg.dpdx : 0.);
   if (h->instMu0.size() == (size_t)M.nInst) mu = h->instMu0;
   if ((r = upload(h, d.mu0, mu))) return r;
@@ -563,9 +612,12 @@ struct ProfScope {
 
 // state sequence of one right-hand side evaluation plus the RK register update
 void launch_rhs_dev(fg_handle* h, const Dev& d, int mode, double rkA, double rkB) {
+  const bool mortars = d.nMortars > 0;
   { ProfScope p(h, 0); h->K.prep(d, h->B, h->st); }
-  { ProfScope p(h, 1); h->K.lift(d, h->B, h->st); }
-  { ProfScope p(h, 2); h->K.flux_block(d, h->B, h->K.fluxBlock, h->st); }
+  if (mortars) { ProfScope p(h, 5); h->K.mortar_pre(d, h->B, h->mort, h->st); h->launches += 1; }
+  { ProfScope p(h, 1); (mortars ? h->K.lift_mortar : h->K.lift)(d, h->B, h->st); }
+  if (d.nFluxSides > 0) { ProfScope p(h, 2); h->K.flux_block(d, h->B, h->K.fluxBlock, h->st); }
+  if (mortars) { ProfScope p(h, 5); h->K.mortar_face(d, h->B, h->mort, h->st); h->launches += 1; }
   {
     ProfScope p(h, 3);
     // with overintegration the volume kernel writes J u_t and k_overint filters it and updates the registers
@@ -649,6 +701,7 @@ const char* adjoint_unsupported(const fg_config& c) {
 
 int ensure_adjoint(fg_handle* h) {
   if (h->haveAdj) return 0;
+  if (h->d.nMortars > 0) return fail(h, FG_ERR_CONFIG, "the adjoint does not support mortar interfaces");
   const int n = h->M.n, n2 = n * n, n3 = n2 * n, nE = h->M.nElems, nS = h->M.nSides;
   AdjDev& a = h->a;
   double* W = nullptr;
@@ -811,12 +864,19 @@ const char* fg_last_error(const fg_handle* h) { return h ? h->err.c_str() : g_er
 
 int fg_build_mesh(fg_handle* h, int nElems, int NGeo, const double* NodeCoords, const int* ElemNb, int nBCs, const int* BoundaryType,
                   int nRefStates, const double* RefStatePrim, const int* ElemInst) {
+  return fg_build_mesh_mortar(h, nElems, NGeo, NodeCoords, ElemNb, nBCs, BoundaryType, nRefStates, RefStatePrim, ElemInst, 0, nullptr);
+}
+
+int fg_build_mesh_mortar(fg_handle* h, int nElems, int NGeo, const double* NodeCoords, const int* ElemNb, int nBCs, const int* BoundaryType,
+                         int nRefStates, const double* RefStatePrim, const int* ElemInst, int nMortars, const int* Mortars) {
   if (!h) return FG_ERR_STATE;
   if (nElems <= 0 || NGeo < 1 || !NodeCoords || !ElemNb) return fail(h, FG_ERR_MESH, "invalid mesh arguments");
+  if (nMortars < 0 || (nMortars > 0 && !Mortars)) return fail(h, FG_ERR_MESH, "invalid mortar table");
   try {
     fgh::RawMesh R;
     R.nElems = nElems; R.NGeo = NGeo; R.nodeCoords = NodeCoords; R.elemNb = ElemNb; R.nBCs = nBCs; R.boundaryType = BoundaryType;
     R.nRefStates = nRefStates; R.refStatePrim = RefStatePrim; R.elemInst = ElemInst;
+    R.nMortars = nMortars; R.mortars = Mortars;
     fgh::build_from_raw(R, h->cfg.N, h->cfg.NodeType == FG_NODE_GAUSS_LOBATTO ? fgh::LOBATTO : fgh::GAUSS, h->M);
   } catch (std::exception& e) {
     return fail(h, FG_ERR_MESH, e.what());

@@ -22,7 +22,7 @@ struct Inst {
   static constexpr long long gs(long long big) { return big_in_global<n>(big) ? big : 0; }
   static constexpr long long mx(long long a, long long b) { return a > b ? a : b; }
   static constexpr long long SCRATCH_PER_BLOCK =
-      mx(mx(gs(Big<n>::prep), gs(Big<n>::lift)), mx(gs(Big<n>::weak), gs(SplitShape<n>::template big<GL>())));
+      mx(mx(mx(gs(Big<n>::prep), gs(Big<n>::lift)), mx(gs(Big<n>::weak), gs(SplitShape<n>::template big<GL>()))), gs(Big<n>::liftMortar));
   static size_t smem_weak_adj() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * 5 * S::n3 + S::THREADS); }
   static size_t smem_split_adj() { return sizeof(double) * (SBasis<n>::SIZE + 2 * S::n2 + S::EPB * 26 * S::n3 + S::THREADS); }
   static size_t smem_lift_adj() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * (13 * S::n3 + 6 * S::n2 * 19)); }
@@ -51,7 +51,7 @@ struct Inst {
     k_vol_weak<n, GL, E><<<(d.nElems + SE::EPB - 1) / SE::EPB, SE::THREADS, smem_weak_E<E>(), st>>>(d, B, Stage{mode, rkA, rkB});
   }
   static void flux_block(const Dev& d, const Basis& B, int block, cudaStream_t st) {
-    const long long pts = (long long)d.nSides * S::n2;
+    const long long pts = (long long)d.nFluxSides * S::n2;
     k_flux<n><<<(unsigned)((pts + block - 1) / block), block, 0, st>>>(d, B);
   }
   template <class K>
@@ -65,6 +65,9 @@ struct Inst {
     if constexpr (SPLIT_POW2) set_smem(k_vol_split<n>, smem_split());
     else set_smem(k_vol_split_gen<n, GL>, smem_split_gen());
     set_smem(k_overint<n>, smem_overint());
+    set_smem(k_lift<n, GL, 0, true>, smem_lift_mortar());
+    set_smem(k_mortar_pre<n>, smem_mortar_pre());
+    set_smem(k_mortar_face<n>, smem_mortar_face());
     if constexpr (ADJ) {
       set_smem(k_vol_weak_adj<n, GL>, smem_weak_adj());
       set_smem(k_lift_adj<n, GL>, smem_lift_adj());
@@ -105,7 +108,7 @@ struct Inst {
     k_lift<n, GL><<<blocks(d), S::THREADS, smem_lift(), st>>>(d, B);
   }
   static void flux(const Dev& d, const Basis& B, cudaStream_t st) {
-    const long long pts = (long long)d.nSides * S::n2;
+    const long long pts = (long long)d.nFluxSides * S::n2;
     k_flux<n><<<(unsigned)((pts + 127) / 128), 128, 0, st>>>(d, B);
   }
   static void vol_weak(const Dev& d, const Basis& B, int mode, double rkA, double rkB, cudaStream_t st) {
@@ -114,6 +117,19 @@ struct Inst {
   static void vol_split(const Dev& d, const Basis& B, int mode, double rkA, double rkB, cudaStream_t st) {
     if constexpr (SPLIT_POW2) k_vol_split<n><<<blocks(d), S::THREADS, smem_split(), st>>>(d, B, Stage{mode, rkA, rkB});
     else k_vol_split_gen<n, GL><<<blocks(d), SplitShape<n>::THREADS, smem_split_gen(), st>>>(d, B, Stage{mode, rkA, rkB});
+  }
+  // mortar interfaces (one CTA of 256 threads per big mortar side)
+  static size_t smem_lift_mortar() { return dyn_smem_bytes<n>(Big<n>::liftMortar); }
+  static size_t smem_mortar_pre() { return sizeof(double) * 97 * S::n2; }
+  static size_t smem_mortar_face() { return sizeof(double) * 104 * S::n2; }
+  static void mortar_pre(const Dev& d, const Basis& B, const MortarDev& M, cudaStream_t st) {
+    k_mortar_pre<n><<<d.nMortars, 256, smem_mortar_pre(), st>>>(d, B, M);
+  }
+  static void lift_mortar(const Dev& d, const Basis& B, cudaStream_t st) {
+    k_lift<n, GL, 0, true><<<blocks(d), S::THREADS, smem_lift_mortar(), st>>>(d, B);
+  }
+  static void mortar_face(const Dev& d, const Basis& B, const MortarDev& M, cudaStream_t st) {
+    k_mortar_face<n><<<d.nMortars, 256, smem_mortar_face(), st>>>(d, B, M);
   }
   static size_t smem_overint() { return sizeof(double) * (10 * S::n3 + 2 * S::n2); }
   static void overint(const Dev& d, const OverintDev& o, int mode, double rkA, double rkB, int state, cudaStream_t st) {
@@ -130,6 +146,7 @@ struct Inst {
     k.prep = &prep; k.lift = &lift; k.flux = &flux; k.vol_weak = &vol_weak; k.dt = &dt;
     k.vol_split = &vol_split;
     k.overint = &overint;
+    k.mortar_pre = &mortar_pre; k.lift_mortar = &lift_mortar; k.mortar_face = &mortar_face;
     if constexpr (ADJ) { k.vol_adj = &vol_adj; k.flux_adj = &flux_adj; k.lift_adj = &lift_adj; k.prep_adj = &prep_adj; }
     k.defEPB = S::EPB;
     k.scratchPerBlock = SCRATCH_PER_BLOCK;

@@ -43,6 +43,7 @@ template <int n, int E = 0> struct Big {
   using S = Shape<n, E>;
   static constexpr long long prep = (long long)S::EPB * (5 + VP_NF) * S::n3;
   static constexpr long long lift = (long long)S::EPB * (17 * S::n3 + 42 * S::n2);
+  static constexpr long long liftMortar = (long long)S::EPB * (17 * S::n3 + 72 * S::n2);
   static constexpr long long weak = (long long)S::EPB * (15 * S::n3 + 30 * S::n2);
 };
 
@@ -235,22 +236,26 @@ __device__ __forceinline__ void lift_prolong_faces(const Dev& d, const Basis& B,
 // them (Dev::metrJ), else forms the products itself. On Gauss-Lobatto nodes the surface part reaches
 // only the face nodes: it is added face-parallel, one direction (two opposite faces, disjoint node
 // sets) at a time, so that no warp runs it for interior nodes.
+// MORTAR (meshes with mortar interfaces, BR1): the surface flux is kept as the 12 products F_v n_c per face
+// point, so that a big mortar side can take the projection of its small sides' products
+// (lifting_br1.t90: Flux_Mortar on gradUx/y/z_master), which k_mortar_pre leaves in Dev::mortarLift.
 // =====================================================================================================
-template <int n, bool GL, int E = 0>
+template <int n, bool GL, int E = 0, bool MORTAR = false>
 __global__ void __launch_bounds__(Shape<n, E>::THREADS, (n == 8 && GL ? 2 : 1)) k_lift(Dev d, Basis B) {
   using S = Shape<n, E>;
   constexpr int n2 = S::n2, n3 = S::n3, EPB = S::EPB, N = S::N;
+  constexpr int NFN = MORTAR ? 12 : 4;  // values per face point in sF
   extern __shared__ double smem[];
   double* sD = smem;
-  double* sL = big_base<n>(d, smem, Big<n, E>::lift);  // [EPB][4][n3] lifting variables u,v,w,T
-  double* sF = sL + EPB * 4 * n3;        // [EPB][6][n2][4] surface lifting flux (times SurfElem), local face order
-  double* sN = sF + EPB * 6 * n2 * 4;    // [EPB][6][n2][3] face normal of the side point mapped to local face order
-  double* sG = sN + EPB * 6 * n2 * 3;    // [EPB][12][n3] gradients
+  double* sL = big_base<n>(d, smem, MORTAR ? Big<n, E>::liftMortar : Big<n, E>::lift);  // [EPB][4][n3] lifting variables u,v,w,T
+  double* sF = sL + EPB * 4 * n3;        // [EPB][6][n2][NFN] surface lifting flux (times SurfElem), local face order
+  double* sN = sF + EPB * 6 * n2 * NFN;  // [EPB][6][n2][3] face normal of the side point mapped to local face order (not MORTAR)
+  double* sG = sN + (MORTAR ? 0 : EPB * 6 * n2 * 3);  // [EPB][12][n3] gradients
   double* sJs = sG + EPB * 12 * n3;      // [EPB][n3]
   load_basis_smem<n>(B, sD);
   SBasis<n> Bs{sD};
   const int e0 = blockIdx.x * EPB;
-  const bool br2 = B.lifting == 2;
+  const bool br2 = !MORTAR && B.lifting == 2;
   for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
     const int es = t / n3, x = t - es * n3, e = e0 + es;
     if (e >= d.nElems) continue;
@@ -268,6 +273,16 @@ __global__ void __launch_bounds__(Shape<n, E>::THREADS, (n == 8 && GL ? 2 : 1)) 
     const int code = d.elemSide[e * 6 + lsi], s = code >> 3, flip = code & 7;
     int a, b;
     side_to_vol2(N, p, q, flip, ls, a, b);
+    const int o = ((es * 6 + lsi) * n2 + a + n * b);
+    if constexpr (MORTAR) {
+      const int mb = s - (d.nSides - d.nMortars);
+      if (mb >= 0) {  // big mortar side (this element is its master): the projected products
+        const double* ml = d.mortarLift + (size_t)mb * 12 * n2 + pq;
+#pragma unroll
+        for (int c = 0; c < 12; ++c) sF[o * 12 + c] = ml[c * n2];
+        continue;
+      }
+    }
     const double* gm = d.geo + (size_t)s * FG_NF * n2 + pq;
     const double se = gm[FG_SURF * n2];
     const double* fm = d.faceM + (size_t)s * FS_NF * n2 + pq;
@@ -294,11 +309,19 @@ __global__ void __launch_bounds__(Shape<n, E>::THREADS, (n == 8 && GL ? 2 : 1)) 
       // slave side of a weak lifting integrates -Flux
       if (flip != 0 && B.weakLifting) for (int v = 0; v < 4; ++v) F[v] = -F[v];
     }
-    const int o = ((es * 6 + lsi) * n2 + a + n * b);
+    if constexpr (MORTAR) {
 #pragma unroll
-    for (int v = 0; v < 4; ++v) sF[o * 4 + v] = F[v];
+      for (int c = 0; c < 3; ++c) {
+        const double nc = gm[(FG_NX + c) * n2];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) sN[o * 3 + c] = gm[(FG_NX + c) * n2];
+        for (int v = 0; v < 4; ++v) sF[o * 12 + 4 * c + v] = F[v] * nc;
+      }
+    } else {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) sF[o * 4 + v] = F[v];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) sN[o * 3 + c] = gm[(FG_NX + c) * n2];
+    }
   }
   __syncthreads();
   // volume gradient: d/dxi via D_T sweeps, contravariant -> Cartesian with the metrics times sJ
@@ -352,11 +375,16 @@ __global__ void __launch_bounds__(Shape<n, E>::THREADS, (n == 8 && GL ? 2 : 1)) 
         const int l = idx3[dir];
         const double wM = Bs.LhM(l), wP = Bs.LhP(l);
         const int oM = (es * 6 + lsM - 1) * n2 + a + n * b, oP = (es * 6 + lsP - 1) * n2 + a + n * b;
+        if constexpr (MORTAR) {
 #pragma unroll
-        for (int v = 0; v < 4; ++v) {
-          const double fM = sF[oM * 4 + v] * wM, fP = sF[oP * 4 + v] * wP;
+          for (int c = 0; c < 12; ++c) sg[c] = fma(sF[oP * 12 + c], wP, fma(sF[oM * 12 + c], wM, sg[c]));
+        } else {
 #pragma unroll
-          for (int c = 0; c < 3; ++c) sg[4 * c + v] = fma(fP, sN[oP * 3 + c], fma(fM, sN[oM * 3 + c], sg[4 * c + v]));
+          for (int v = 0; v < 4; ++v) {
+            const double fM = sF[oM * 4 + v] * wM, fP = sF[oP * 4 + v] * wP;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) sg[4 * c + v] = fma(fP, sN[oP * 3 + c], fma(fM, sN[oM * 3 + c], sg[4 * c + v]));
+          }
         }
       }
       // BR1: face gradients are prolonged from the full gradient; BR2: from the volume part only
@@ -389,11 +417,16 @@ __global__ void __launch_bounds__(Shape<n, E>::THREADS, (n == 8 && GL ? 2 : 1)) 
         const double w = (plus ? Bs.LhP(N) : Bs.LhM(0)) * sJs[es * n3 + x];
         const int o = (es * 6 + ls - 1) * n2 + a + n * b;
         double* G = sG + es * 12 * n3 + x;
+        if constexpr (MORTAR) {
 #pragma unroll
-        for (int v = 0; v < 4; ++v) {
-          const double f = sF[o * 4 + v] * w;
+          for (int c = 0; c < 12; ++c) G[c * n3] = fma(sF[o * 12 + c], w, G[c * n3]);
+        } else {
 #pragma unroll
-          for (int c = 0; c < 3; ++c) G[(4 * c + v) * n3] = fma(f, sN[o * 3 + c], G[(4 * c + v) * n3]);
+          for (int v = 0; v < 4; ++v) {
+            const double f = sF[o * 4 + v] * w;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) G[(4 * c + v) * n3] = fma(f, sN[o * 3 + c], G[(4 * c + v) * n3]);
+          }
         }
       }
       __syncthreads();
@@ -413,14 +446,13 @@ __global__ void __launch_bounds__(Shape<n, E>::THREADS, (n == 8 && GL ? 2 : 1)) 
 
 // =====================================================================================================
 // k_flux: fillflux.f90:FillFlux -- riemann.f90:Riemann_Side + ViscousFlux_Side on inner sides,
-// getboundaryflux.f90:GetBoundaryFlux (no-slip walls) on BC sides, times SurfElem.
+// getboundaryflux.f90:GetBoundaryFlux (no-slip walls) on BC sides, times SurfElem; conforming sides only
+// (the mortar sides are k_mortar_face's).
 // =====================================================================================================
+// numerical flux times SurfElem of point pq of side s, with the master's face gradients gL (12 values)
 template <int n>
-__global__ void __launch_bounds__(256) k_flux(Dev d, Basis B) {
+__device__ __forceinline__ void side_flux(const Dev& d, const Basis& B, int s, int pq, const double* gL, double* Fout) {
   constexpr int n2 = n * n;
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  const int s = idx / n2, pq = idx - s * n2;
-  if (s >= d.nSides) return;
   const double* gm = d.geo + (size_t)s * FG_NF * n2 + pq;
   double nv[3], t1[3], t2[3];
 #pragma unroll
@@ -431,9 +463,6 @@ __global__ void __launch_bounds__(256) k_flux(Dev d, Basis B) {
   const double mu = d.muScale ? mu0s * d.muScale[d.sideElem[s * 4 + 0]] : mu0s;
   const double lam = mu * B.lambdaFac;
   const double* fm = d.faceM + (size_t)s * FS_NF * n2 + pq;
-  double gL[12];
-#pragma unroll
-  for (int c = 0; c < 12; ++c) gL[c] = d.gradM[((size_t)s * 12 + c) * n2 + pq];
   double F[5];
   if (s < d.nBCSides) {
     const int bt = d.bcType[s];
@@ -477,7 +506,198 @@ __global__ void __launch_bounds__(256) k_flux(Dev d, Basis B) {
     for (int v = 1; v < 5; ++v) F[v] += 0.5 * (FvL[v] + FvR[v]);
   }
 #pragma unroll
-  for (int v = 0; v < 5; ++v) d.flux[((size_t)s * 5 + v) * n2 + pq] = F[v] * se;
+  for (int v = 0; v < 5; ++v) Fout[v] = F[v] * se;
+}
+
+template <int n>
+__global__ void __launch_bounds__(256) k_flux(Dev d, Basis B) {
+  constexpr int n2 = n * n;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = idx / n2, pq = idx - s * n2;
+  if (s >= d.nFluxSides) return;
+  double gL[12], F[5];
+#pragma unroll
+  for (int c = 0; c < 12; ++c) gL[c] = d.gradM[((size_t)s * 12 + c) * n2 + pq];
+  side_flux<n>(d, B, s, pq, gL, F);
+#pragma unroll
+  for (int v = 0; v < 5; ++v) d.flux[((size_t)s * 5 + v) * n2 + pq] = F[v];
+}
+
+// =====================================================================================================
+// Mortar interfaces (mortar.f90, fillmortar.t90), one CTA per big mortar side m. Small side im covers the
+// quadrant iNb = im % 2, jNb = im / 2 of the big side (type 1), the half jNb = im (type 2, split in eta)
+// or iNb = im (type 3, split in xi), in the big side's master orientation.
+// =====================================================================================================
+// fillmortar.t90:U_Mortar: nv fields in[v][p + n*q] of the big side interpolated to out[im][v][n2];
+// tmp holds [2][nv][n2]. Ends with a barrier.
+template <int n>
+__device__ void mortar_interp(const MortarDev& M, int type, int nv, const double* in, double* tmp, double* out) {
+  constexpr int n2 = n * n;
+  if (type == 1) {
+    for (int t = threadIdx.x; t < 2 * nv * n2; t += blockDim.x) {  // eta: tmp[jNb]
+      const int k = t / (nv * n2), r = t - k * nv * n2, v = r / n2, pq = r - v * n2, p = pq % n, q = pq / n;
+      const double* Mq = k ? M.M02 : M.M01;
+      double acc = 0.;
+#pragma unroll
+      for (int l = 0; l < n; ++l) acc = fma(Mq[l * n + q], in[v * n2 + p + n * l], acc);
+      tmp[t] = acc;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < 4 * nv * n2; t += blockDim.x) {  // xi
+      const int im = t / (nv * n2), r = t - im * nv * n2, v = r / n2, pq = r - v * n2, p = pq % n, q = pq / n;
+      const double* Mp = (im & 1) ? M.M02 : M.M01;
+      const double* T = tmp + ((im >> 1) * nv + v) * n2;
+      double acc = 0.;
+#pragma unroll
+      for (int l = 0; l < n; ++l) acc = fma(Mp[l * n + p], T[l + n * q], acc);
+      out[t] = acc;
+    }
+  } else {
+    for (int t = threadIdx.x; t < 2 * nv * n2; t += blockDim.x) {
+      const int im = t / (nv * n2), r = t - im * nv * n2, v = r / n2, pq = r - v * n2, p = pq % n, q = pq / n;
+      const double* Mx = im ? M.M02 : M.M01;
+      double acc = 0.;
+      if (type == 2) {
+#pragma unroll
+        for (int l = 0; l < n; ++l) acc = fma(Mx[l * n + q], in[v * n2 + p + n * l], acc);
+      } else {
+#pragma unroll
+        for (int l = 0; l < n; ++l) acc = fma(Mx[l * n + p], in[v * n2 + l + n * q], acc);
+      }
+      out[t] = acc;
+    }
+  }
+  __syncthreads();
+}
+
+// fillmortar.t90:Flux_Mortar: nv fields in[im][v][n2] of the small sides projected onto the big side,
+// out[v][p + n*q]; tmp holds [2][nv][n2]
+template <int n>
+__device__ void mortar_project(const MortarDev& M, int type, int nv, const double* in, double* tmp, double* out) {
+  constexpr int n2 = n * n;
+  if (type == 1) {
+    for (int t = threadIdx.x; t < 2 * nv * n2; t += blockDim.x) {  // xi: tmp[jNb]
+      const int k = t / (nv * n2), r = t - k * nv * n2, v = r / n2, pq = r - v * n2, p = pq % n, q = pq / n;
+      const double* F1 = in + ((2 * k) * nv + v) * n2;
+      const double* F2 = in + ((2 * k + 1) * nv + v) * n2;
+      double acc = 0.;
+#pragma unroll
+      for (int l = 0; l < n; ++l) acc = fma(M.M10[l * n + p], F1[l + n * q], fma(M.M20[l * n + p], F2[l + n * q], acc));
+      tmp[t] = acc;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < nv * n2; t += blockDim.x) {  // eta
+      const int v = t / n2, pq = t - v * n2, p = pq % n, q = pq / n;
+      const double* T1 = tmp + v * n2;
+      const double* T2 = tmp + (nv + v) * n2;
+      double acc = 0.;
+#pragma unroll
+      for (int l = 0; l < n; ++l) acc = fma(M.M10[l * n + q], T1[p + n * l], fma(M.M20[l * n + q], T2[p + n * l], acc));
+      out[t] = acc;
+    }
+  } else {
+    for (int t = threadIdx.x; t < nv * n2; t += blockDim.x) {
+      const int v = t / n2, pq = t - v * n2, p = pq % n, q = pq / n;
+      const double* F1 = in + v * n2;
+      const double* F2 = in + (nv + v) * n2;
+      double acc = 0.;
+      if (type == 2) {
+#pragma unroll
+        for (int l = 0; l < n; ++l) acc = fma(M.M10[l * n + q], F1[p + n * l], fma(M.M20[l * n + q], F2[p + n * l], acc));
+      } else {
+#pragma unroll
+        for (int l = 0; l < n; ++l) acc = fma(M.M10[l * n + p], F1[l + n * q], fma(M.M20[l * n + p], F2[l + n * q], acc));
+      }
+      out[t] = acc;
+    }
+  }
+}
+
+// between k_prep and k_lift: the big side's conservative face state interpolated to its small sides' master
+// slots, turned into face primitives (dg.f90:372-416, U_Mortar before GetPrimitiveStateSurface), and the
+// small sides' BR1 lifting fluxes times normal (lifting_fillflux.t90) projected onto the big side
+// (lifting_br1.t90:106-109) for k_lift<MORTAR>.
+template <int n>
+__global__ void __launch_bounds__(256) k_mortar_pre(Dev d, Basis B, MortarDev M) {
+  constexpr int n2 = n * n;
+  extern __shared__ double smem[];
+  double* sUb = smem;          // [5][n2] big side U
+  double* sT = sUb + 5 * n2;   // [2][12][n2]
+  double* sUs = sT + 24 * n2;  // [4][5][n2] small sides' U
+  double* sFN = sUs + 20 * n2; // [4][12][n2] small sides' lifting flux times normal
+  const int m = blockIdx.x;
+  const int* info = M.info + 6 * m;
+  const int type = info[0], sb = info[1], nm = type == 1 ? 4 : 2;
+  for (int pq = threadIdx.x; pq < n2; pq += blockDim.x) {
+    const double* fm = d.faceM + (size_t)sb * FS_NF * n2 + pq;
+    const double rho = fm[FS_RHO * n2];
+    sUb[pq] = rho;
+    sUb[n2 + pq] = rho * fm[FS_U * n2];
+    sUb[2 * n2 + pq] = rho * fm[FS_V * n2];
+    sUb[3 * n2 + pq] = rho * fm[FS_W * n2];
+    sUb[4 * n2 + pq] = fm[FS_E * n2];
+  }
+  __syncthreads();
+  mortar_interp<n>(M, type, 5, sUb, sT, sUs);
+  const double sig = B.weakLifting ? 1.0 : -1.0;
+  for (int t = threadIdx.x; t < nm * n2; t += blockDim.x) {
+    const int im = t / n2, pq = t - im * n2, ss = info[2 + im];
+    double c[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) c[v] = sUs[(im * 5 + v) * n2 + pq];
+    const double srho = 1.0 / c[0];
+    const double vx = c[1] * srho, vy = c[2] * srho, vz = c[3] * srho;
+    const double pp = B.kappaM1 * (c[4] - 0.5 * (c[1] * vx + c[2] * vy + c[3] * vz));
+    const double T = pp * srho * B.sR;
+    double* dst = d.faceM + (size_t)ss * FS_NF * n2 + pq;
+    dst[FS_RHO * n2] = c[0]; dst[FS_E * n2] = c[4]; dst[FS_SRHO * n2] = srho;
+    dst[FS_U * n2] = vx; dst[FS_V * n2] = vy; dst[FS_W * n2] = vz; dst[FS_P * n2] = pp; dst[FS_T * n2] = T;
+    const double* fsl = d.faceS + (size_t)ss * FS_NF * n2 + pq;
+    const double* gm = d.geo + (size_t)ss * FG_NF * n2 + pq;
+    const double hs = 0.5 * gm[FG_SURF * n2];
+    const double um[4] = {vx, vy, vz, T};
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const double F = (sig * um[v] + fsl[(v < 3 ? FS_U + v : FS_T) * n2]) * hs;
+#pragma unroll
+      for (int cc = 0; cc < 3; ++cc) sFN[(im * 12 + 4 * cc + v) * n2 + pq] = F * gm[(FG_NX + cc) * n2];
+    }
+  }
+  __syncthreads();
+  mortar_project<n>(M, type, 12, sFN, sT, d.mortarLift + (size_t)m * 12 * n2);
+}
+
+// between k_flux and the volume kernel: the big side's face gradients interpolated to its small sides
+// (lifting_br1.t90:175-178), the small sides' numerical fluxes (fillflux.f90, master viscosity of the big
+// element), and their projection onto the big side (dg.f90:625, Flux_Mortar)
+template <int n>
+__global__ void __launch_bounds__(256) k_mortar_face(Dev d, Basis B, MortarDev M) {
+  constexpr int n2 = n * n;
+  extern __shared__ double smem[];
+  double* sGb = smem;           // [12][n2] big side gradients
+  double* sT = sGb + 12 * n2;   // [2][12][n2]
+  double* sGs = sT + 24 * n2;   // [4][12][n2]
+  double* sF = sGs + 48 * n2;   // [4][5][n2]
+  const int m = blockIdx.x;
+  const int* info = M.info + 6 * m;
+  const int type = info[0], sb = info[1], nm = type == 1 ? 4 : 2;
+  for (int t = threadIdx.x; t < 12 * n2; t += blockDim.x) sGb[t] = d.gradM[(size_t)sb * 12 * n2 + t];
+  __syncthreads();
+  mortar_interp<n>(M, type, 12, sGb, sT, sGs);
+  for (int t = threadIdx.x; t < nm * n2; t += blockDim.x) {
+    const int im = t / n2, pq = t - im * n2, ss = info[2 + im];
+    double gL[12], F[5];
+#pragma unroll
+    for (int c = 0; c < 12; ++c) gL[c] = sGs[(im * 12 + c) * n2 + pq];
+    side_flux<n>(d, B, ss, pq, gL, F);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      d.flux[((size_t)ss * 5 + v) * n2 + pq] = F[v];
+      sF[(im * 5 + v) * n2 + pq] = F[v];
+    }
+  }
+  __syncthreads();
+  mortar_project<n>(M, type, 5, sF, sT, d.flux + (size_t)sb * 5 * n2);
 }
 
 // stage parameters of the fused LSERK update

@@ -17,6 +17,10 @@ struct KernelSet {
   void (*dt)(const Dev&, const Basis&, const double*, const double*, double, double, double*, const double*, cudaStream_t) = nullptr;
   // overintegration of Ut (state = 0, after a volume kernel in mode 0, with the stage's register update) or of U
   void (*overint)(const Dev&, const OverintDev&, int, double, double, int, cudaStream_t) = nullptr;
+  // mortar interfaces: k_mortar_pre, k_lift<MORTAR> (BR1) and k_mortar_face
+  void (*mortar_pre)(const Dev&, const Basis&, const MortarDev&, cudaStream_t) = nullptr;
+  void (*lift_mortar)(const Dev&, const Basis&, cudaStream_t) = nullptr;
+  void (*mortar_face)(const Dev&, const Basis&, const MortarDev&, cudaStream_t) = nullptr;
   // adjoint (vector-Jacobian product) of the right-hand side; vol_adj is null where unsupported
   void (*vol_adj)(const Dev&, const AdjDev&, const Basis&, cudaStream_t) = nullptr;
   void (*flux_adj)(const Dev&, const AdjDev&, const Basis&, cudaStream_t) = nullptr;

@@ -108,6 +108,24 @@ void deriv3(const Mat& D, const double* X, double* out, int dir) {
       }
 }
 
+// metrics.f90:SurfMetricsFromJa at one side point: unit normal (sign of local side ls), tangents and surface
+// element from the normal row jn and the tangential row jt of the face metrics; G = field 0 of the point
+// in a [10][n2] side block
+void surf_point(const double* jn, const double* jt, int ls, double* G, int n2) {
+  const double se = std::sqrt(jn[0] * jn[0] + jn[1] * jn[1] + jn[2] * jn[2]);
+  double nv[3], t1[3], t2[3];
+  for (int c = 0; c < 3; ++c) nv[c] = kNormalSign[ls] * jn[c] / se;
+  const double dt = jt[0] * nv[0] + jt[1] * nv[1] + jt[2] * nv[2];
+  for (int c = 0; c < 3; ++c) t1[c] = jt[c] - dt * nv[c];
+  const double tl = std::sqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
+  for (int c = 0; c < 3; ++c) t1[c] /= tl;
+  t2[0] = nv[1] * t1[2] - nv[2] * t1[1];
+  t2[1] = nv[2] * t1[0] - nv[0] * t1[2];
+  t2[2] = nv[0] * t1[1] - nv[1] * t1[0];
+  for (int c = 0; c < 3; ++c) { G[c * n2] = nv[c]; G[(3 + c) * n2] = t1[c]; G[(6 + c) * n2] = t2[c]; }
+  G[9 * n2] = se;
+}
+
 }  // namespace
 
 void build_from_raw(const RawMesh& R, int N, int nodeType, HostMesh& M) {
@@ -116,19 +134,31 @@ void build_from_raw(const RawMesh& R, int N, int nodeType, HostMesh& M) {
   auto nb = [&](int c, int ls, int e) { return R.elemNb[((size_t)e * 6 + (ls - 1)) * 3 + c]; };
   auto X = [&](int d, int i, int j, int k, int e) { return R.nodeCoords[((((size_t)e * ng + k) * ng + j) * ng + i) * 3 + d]; };
 
-  // ---------------- sides ----------------
+  // ---------------- sides: BC | conforming inner | small mortar | big mortar ----------------
   struct SideRec { int e, ls, ne, nls, bc; };
   std::vector<SideRec> bcs, inner;
+  int nMortarSides = 0;  // element sides with neighbour -1 (big and small mortar sides)
   for (int e = 0; e < nE; ++e)
     for (int ls = 1; ls <= 6; ++ls) {
       const int ne = nb(0, ls, e);
       if (ne == 0) { bcs.push_back({e, ls, -1, 0, nb(2, ls, e)}); continue; }
-      if (ne < 0 || ne > nE) throw std::runtime_error("neighbour element out of range (mortar sides need the Mortars table)");
+      if (ne == -1) { ++nMortarSides; continue; }
+      if (ne < 0 || ne > nE) throw std::runtime_error("neighbour element out of range");
       const int oe = ne - 1, ols = nb(1, ls, e);
       if (e < oe || (e == oe && ls < ols)) inner.push_back({e, ls, oe, ols, 0});
     }
+  const int nMo = R.nMortars;
+  int nSmall = 0;
+  for (int m = 0; m < nMo; ++m) {
+    const int type = R.mortars[(size_t)m * 15 + 2];
+    if (type < 1 || type > 3) throw std::runtime_error("mortar type must be 1, 2 or 3");
+    nSmall += type == 1 ? 4 : 2;
+  }
+  if (nMortarSides != nMo + nSmall) throw std::runtime_error("mortar sides (neighbour -1) do not match the Mortars table");
   M.nBCSides = (int)bcs.size();
-  M.nSides = M.nBCSides + (int)inner.size();
+  M.nFluxSides = M.nBCSides + (int)inner.size();
+  M.nMortars = nMo;
+  M.nSides = M.nFluxSides + nSmall + nMo;
   M.sideElem.assign((size_t)M.nSides * 4, -1);
   M.elemSide.assign((size_t)nE * 6, 0);
   M.bcType.assign(M.nBCSides, 0);
@@ -153,32 +183,88 @@ void build_from_raw(const RawMesh& R, int N, int nodeType, HostMesh& M) {
     face_ijk(ls, a, b, minus_side(ls) ? 0 : NG, i, j, k);
     for (int d = 0; d < 3; ++d) x[d] = X(d, i, j, k, e);
   };
-  for (size_t t = 0; t < inner.size(); ++t) {
-    const SideRec& r = inner[t];
-    const int s = M.nBCSides + (int)t;
-    int found = -1;
-    for (int f = 1; f <= 4 && found < 0; ++f) {
+  // flip of the slave face (ne, nls) whose corners coincide with the master corners xm[c] (c = p + 2q over
+  // the side's corner nodes) up to one constant (periodic) shift; -1 if none does
+  auto match_flip = [&](const double (*xm)[3], int ne, int nls) {
+    for (int f = 1; f <= 4; ++f) {
       bool ok = true;
       double sh[3] = {0., 0., 0.};
       for (int c = 0; c < 4 && ok; ++c) {
         const int p = (c & 1) ? NG : 0, q = (c & 2) ? NG : 0;
-        double xm[3], xs[3];
-        corner(r.e, r.ls, p, q, xm);
+        double xs[3];
         int pa, qa;
         flip_map(NG, p, q, f, pa, qa);
-        corner(r.ne, r.nls, pa, qa, xs);
+        corner(ne, nls, pa, qa, xs);
         for (int dd = 0; dd < 3; ++dd) {
-          const double dv = xs[dd] - xm[dd];
+          const double dv = xs[dd] - xm[c][dd];
           if (c == 0) sh[dd] = dv;
           else if (std::fabs(dv - sh[dd]) > 1e-9 * (1. + std::fabs(sh[dd]))) ok = false;
         }
       }
-      if (ok) found = f;
+      if (ok) return f;
     }
+    return -1;
+  };
+  for (size_t t = 0; t < inner.size(); ++t) {
+    const SideRec& r = inner[t];
+    const int s = M.nBCSides + (int)t;
+    double xm[4][3];
+    for (int c = 0; c < 4; ++c) corner(r.e, r.ls, (c & 1) ? NG : 0, (c & 2) ? NG : 0, xm[c]);
+    const int found = match_flip(xm, r.ne, r.nls);
     if (found < 0) throw std::runtime_error("neighbouring faces do not match geometrically");
     M.sideElem[s * 4 + 0] = r.e; M.sideElem[s * 4 + 1] = r.ls; M.sideElem[s * 4 + 2] = r.ne; M.sideElem[s * 4 + 3] = 8 * r.nls + found;
     M.elemSide[r.e * 6 + r.ls - 1] = 8 * s;
     M.elemSide[r.ne * 6 + r.nls - 1] = 8 * s + found;
+  }
+  // mortar sides (mesh_readin.f90 / prepare_mesh.f90: MortarType, MortarInfo). The big side has the big
+  // element as master and no slave. Small side im covers quadrant (iNb, jNb) of the big side in its master
+  // orientation; its master slot is filled from the big side (U_Mortar), so its master element is the big
+  // element (viscosity, instance) and the small element is the slave, flip from the quadrant corners.
+  M.mortarInfo.assign((size_t)6 * nMo, -1);
+  {
+    const int firstBig = M.nSides - nMo;
+    Vec xe(ng);
+    for (int a = 0; a < ng; ++a) xe[a] = -1. + 2. * a / NG;
+    const Vec wbe = bary_weights(xe);
+    std::vector<char> used((size_t)6 * nE, 0);
+    auto take = [&](int e, int ls) {
+      if (e < 0 || e >= nE || ls < 1 || ls > 6 || nb(0, ls, e) != -1 || used[(size_t)e * 6 + ls - 1])
+        throw std::runtime_error("mortar table names a side that is not an unused mortar side");
+      used[(size_t)e * 6 + ls - 1] = 1;
+    };
+    int s = M.nFluxSides;
+    for (int m = 0; m < nMo; ++m) {
+      const int* r = &R.mortars[(size_t)m * 15];
+      const int be = r[0] - 1, bls = r[1], type = r[2], nm = type == 1 ? 4 : 2, sb = firstBig + m;
+      take(be, bls);
+      M.sideElem[sb * 4 + 0] = be; M.sideElem[sb * 4 + 1] = bls; M.sideElem[sb * 4 + 2] = -1; M.sideElem[sb * 4 + 3] = 0;
+      M.elemSide[be * 6 + bls - 1] = 8 * sb;
+      M.mortarInfo[(size_t)m * 6 + 0] = type;
+      M.mortarInfo[(size_t)m * 6 + 1] = sb;
+      for (int im = 0; im < nm; ++im, ++s) {
+        const int se = r[3 + 3 * im] - 1, sls = r[4 + 3 * im];
+        take(se, sls);
+        const int iNb = type == 1 ? im % 2 : (type == 3 ? im : -1), jNb = type == 1 ? im / 2 : (type == 2 ? im : -1);
+        double xm[4][3];
+        for (int c = 0; c < 4; ++c) {
+          const double xi = iNb < 0 ? ((c & 1) ? 1. : -1.) : ((c & 1) ? (iNb ? 1. : 0.) : (iNb ? 0. : -1.));
+          const double eta = jNb < 0 ? ((c & 2) ? 1. : -1.) : ((c & 2) ? (jNb ? 1. : 0.) : (jNb ? 0. : -1.));
+          const Vec La = lagrange_at(xi, xe, wbe), Lb = lagrange_at(eta, xe, wbe);
+          for (int dd = 0; dd < 3; ++dd) xm[c][dd] = 0.;
+          for (int b = 0; b < ng; ++b)
+            for (int a = 0; a < ng; ++a) {
+              double x[3];
+              corner(be, bls, a, b, x);
+              for (int dd = 0; dd < 3; ++dd) xm[c][dd] += La[a] * Lb[b] * x[dd];
+            }
+        }
+        const int f = match_flip(xm, se, sls);
+        if (f < 0) throw std::runtime_error("mortar: small face does not match its part of the big face");
+        M.sideElem[s * 4 + 0] = be; M.sideElem[s * 4 + 1] = bls; M.sideElem[s * 4 + 2] = se; M.sideElem[s * 4 + 3] = 8 * sls + f;
+        M.elemSide[se * 6 + sls - 1] = 8 * s + f;
+        M.mortarInfo[(size_t)m * 6 + 2 + im] = s;
+      }
+    }
   }
   // instances
   M.elemInst.assign(nE, 0);
@@ -201,12 +287,21 @@ void build_from_raw(const RawMesh& R, int N, int nodeType, HostMesh& M) {
   M.elemX.assign((size_t)nE * 3 * n3, 0.);
   M.geo.assign((size_t)M.nSides * 10 * n2, 0.);
   M.faceJa.assign((size_t)nE * 6 * 3 * n2, 0.);
+  // mortar.f90:InitMortar interpolation to the two halves, MI[h](p, l) = L_l(0.5 (x_p -/+ 1))
+  Mat MI[2];
+  {
+    Vec x, w, x1, x2;
+    nodes(N, nodeType, x, w);
+    for (double v : x) { x1.push_back(0.5 * (v - 1.)); x2.push_back(0.5 * (v + 1.)); }
+    MI[0] = interp_matrix(x, x1);
+    MI[1] = interp_matrix(x, x2);
+  }
   std::string err;
 #pragma omp parallel
   {
     std::vector<double> nc((size_t)3 * ng * ng * ng), xcl_ng(nc.size()), xcl_n((size_t)3 * n3), dng((size_t)9 * ng * ng * ng),
         dref((size_t)9 * nr * nr * nr), detRef((size_t)nr * nr * nr), detN(n3), dn((size_t)9 * n3), Rc((size_t)9 * n3), Ja((size_t)9 * n3),
-        tmp(n3), tmp2((size_t)3 * n2), tmp3((size_t)3 * n2), ja_out((size_t)3 * n3);
+        tmp(n3), tmp2((size_t)3 * n2), tmp3((size_t)3 * n2), ja_out((size_t)3 * n3), sjn((size_t)3 * n2), sjt((size_t)3 * n2);
 #pragma omp for schedule(dynamic, 16)
     for (int e = 0; e < nE; ++e) {
       // component-major copy of the element's node coordinates
@@ -283,25 +378,39 @@ void build_from_raw(const RawMesh& R, int N, int nodeType, HostMesh& M) {
           tensor2(V_CLN_N, tmp2.data(), row == 0 ? tmp3.data() : ja_out.data(), 3);
         }
         if ((code & 7) != 0) continue;
+        // normal and tangential rows in side coordinates (p + n q, master orientation)
         for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
           int a, b;
           s2v2(N, p, q, 0, ls, a, b);
           const int o = b * n + a;
-          const double jn[3] = {tmp3[o], tmp3[n2 + o], tmp3[2 * n2 + o]};
-          const double jt[3] = {ja_out[o], ja_out[n2 + o], ja_out[2 * n2 + o]};
-          const double se = std::sqrt(jn[0] * jn[0] + jn[1] * jn[1] + jn[2] * jn[2]);
-          double nv[3], t1[3], t2[3];
-          for (int c = 0; c < 3; ++c) nv[c] = kNormalSign[ls] * jn[c] / se;
-          const double dt = jt[0] * nv[0] + jt[1] * nv[1] + jt[2] * nv[2];
-          for (int c = 0; c < 3; ++c) t1[c] = jt[c] - dt * nv[c];
-          const double tl = std::sqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
-          for (int c = 0; c < 3; ++c) t1[c] /= tl;
-          t2[0] = nv[1] * t1[2] - nv[2] * t1[1];
-          t2[1] = nv[2] * t1[0] - nv[0] * t1[2];
-          t2[2] = nv[0] * t1[1] - nv[1] * t1[0];
-          double* G = &M.geo[(size_t)s * 10 * n2 + q * n + p];
-          for (int c = 0; c < 3; ++c) { G[c * n2] = nv[c]; G[(3 + c) * n2] = t1[c]; G[(6 + c) * n2] = t2[c]; }
-          G[9 * n2] = se;
+          for (int c = 0; c < 3; ++c) { sjn[(size_t)c * n2 + q * n + p] = tmp3[(size_t)c * n2 + o]; sjt[(size_t)c * n2 + q * n + p] = ja_out[(size_t)c * n2 + o]; }
+        }
+        for (int pq = 0; pq < n2; ++pq) {
+          const double jn[3] = {sjn[pq], sjn[n2 + pq], sjn[2 * n2 + pq]};
+          const double jt[3] = {sjt[pq], sjt[n2 + pq], sjt[2 * n2 + pq]};
+          surf_point(jn, jt, ls, &M.geo[(size_t)s * 10 * n2 + pq], n2);
+        }
+        // mortar_metrics.f90:Mortar_CalcSurfMetrics: each small side's rows are the big side's interpolated to
+        // its part and halved per split direction
+        const int mb = s - (M.nSides - M.nMortars);
+        if (mb < 0) continue;
+        const int type = M.mortarInfo[(size_t)mb * 6];
+        for (int im = 0; im < (type == 1 ? 4 : 2); ++im) {
+          const int iNb = type == 1 ? im % 2 : (type == 3 ? im : -1), jNb = type == 1 ? im / 2 : (type == 2 ? im : -1);
+          const int ss = M.mortarInfo[(size_t)mb * 6 + 2 + im];
+          for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
+            double jn[3] = {0., 0., 0.}, jt[3] = {0., 0., 0.};
+            for (int b = 0; b < n; ++b) {
+              const double wq = jNb < 0 ? (b == q ? 1. : 0.) : 0.5 * MI[jNb](q, b);
+              if (wq == 0.) continue;
+              for (int a = 0; a < n; ++a) {
+                const double w = wq * (iNb < 0 ? (a == p ? 1. : 0.) : 0.5 * MI[iNb](p, a));
+                if (w == 0.) continue;
+                for (int c = 0; c < 3; ++c) { jn[c] += w * sjn[(size_t)c * n2 + b * n + a]; jt[c] += w * sjt[(size_t)c * n2 + b * n + a]; }
+              }
+            }
+            surf_point(jn, jt, ls, &M.geo[(size_t)ss * 10 * n2 + q * n + p], n2);
+          }
         }
       }
     }
@@ -315,6 +424,7 @@ void build_from_flexi(int N, int nodeType, int nElems, int nSides, int nBCSides,
                       const double* SurfElem, HostMesh& M) {
   const int n = N + 1, n2 = n * n, n3 = n2 * n;
   M.N = N; M.n = n; M.nodeType = nodeType; M.nElems = nElems; M.nSides = nSides; M.nBCSides = nBCSides;
+  M.nFluxSides = nSides; M.nMortars = 0; M.mortarInfo.clear();
   M.sideElem.assign((size_t)nSides * 4, -1);
   M.elemSide.assign((size_t)nElems * 6, -1);
   for (int s = 0; s < nSides; ++s) {

@@ -23,10 +23,17 @@ struct RawMesh {
   int nRefStates = 0;
   const double* refStatePrim = nullptr;  // (6,nRefStates)
   const int* elemInst = nullptr;       // optional instance id per element (ensembles)
+  // mortar interfaces (elemNb neighbour -1), 15 per mortar: big element (1-based), its local side, type
+  // (1: 1->4, 2: 1->2 in eta, 3: 1->2 in xi), then per small side: element (1-based), local side, unused
+  int nMortars = 0;
+  const int* mortars = nullptr;
 };
 
 struct HostMesh {
   int N = 0, n = 0, nodeType = 2, nElems = 0, nSides = 0, nBCSides = 0;
+  // sides are ordered BC | conforming inner | small mortar | big mortar; nFluxSides = BC + conforming inner
+  int nFluxSides = 0, nMortars = 0;
+  std::vector<int> mortarInfo;  // [m][6]: type, big side, small sides (-1: unused)
   std::vector<int> sideElem;    // [s][4]
   std::vector<int> elemSide;    // [e][6]
   std::vector<int> sideInst, elemInst;

@@ -266,6 +266,7 @@ extern "C" int fg_time_derivative_noalloc(const fg_config* cfg, const fg_device_
   stack_basis(*cfg, B);
   Dev d{};
   d.nElems = (int)nE; d.nSides = (int)nS; d.nBCSides = mesh->nBCSides; d.nInst = 1;
+  d.nFluxSides = (int)nS; d.nMortars = 0;
   d.U = const_cast<double*>(U);
   d.Ut = Ut;
   d.Ut_tmp = nullptr;

@@ -98,15 +98,20 @@ class Flexi:
 
     # ---------------------------------------------------------------- mesh
     def build_mesh(self, m: BoxMesh, host_only_ok=False):
-        """fg_build_mesh. host_only_ok: accept a failed device upload (no GPU) once the host-side
-        preparation succeeded, so that the set-up can be inspected on a machine without a GPU."""
+        """fg_build_mesh (fg_build_mesh_mortar when the mesh has mortar interfaces). host_only_ok: accept a
+        failed device upload (no GPU) once the host-side preparation succeeded, so that the set-up can be
+        inspected on a machine without a GPU."""
         nc = np.ascontiguousarray(m.node_coords, np.float64)
         nb = np.ascontiguousarray(m.elem_nb, np.int32)
         bt = np.ascontiguousarray(m.boundary_type, np.int32).reshape(-1)
         rs = np.ascontiguousarray(m.ref_state_prim, np.float64).reshape(-1)
         inst = None if m.elem_inst is None else np.ascontiguousarray(m.elem_inst, np.int32)
-        rc = self.L.fg_build_mesh(self.h, m.n_elems, m.ngeo, _p(nc), _p(nb), len(bt) // 2, _p(bt) if len(bt) else None,
-                                  len(rs) // 6, _p(rs) if len(rs) else None, _p(inst) if inst is not None else None)
+        mo = getattr(m, "mortars", None)
+        mo = None if mo is None or len(mo) == 0 else np.ascontiguousarray(mo, np.int32).reshape(-1, 15)
+        self._mesh_keep = (nc, nb, bt, rs, inst, mo)
+        rc = self.L.fg_build_mesh_mortar(self.h, m.n_elems, m.ngeo, _p(nc), _p(nb), len(bt) // 2, _p(bt) if len(bt) else None,
+                                         len(rs) // 6, _p(rs) if len(rs) else None, _p(inst) if inst is not None else None,
+                                         0 if mo is None else len(mo), _p(mo) if mo is not None else None)
         if not (host_only_ok and rc == 3):  # FG_ERR_CUDA after a complete host-side set-up
             self._check(rc, "fg_build_mesh")
         self._sizes()

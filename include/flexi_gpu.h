@@ -97,6 +97,15 @@ const char* fg_last_error(const fg_handle* h);
 int fg_build_mesh(fg_handle* h, int nElems, int NGeo, const double* NodeCoords, const int* ElemNb, int nBCs, const int* BoundaryType,
                   int nRefStates, const double* RefStatePrim, const int* ElemInst);
 
+/* fg_build_mesh for meshes with mortar interfaces (non-conforming 1->4 / 1->2 element faces): ElemNb holds
+ * -1 for every big and small mortar side, and Mortars(15,nMortars) = (big element 1-based, its local side,
+ * MortarType 1: 1->4, 2: 1->2 in eta, 3: 1->2 in xi, then per small side: element, local side, 0) as
+ * fg_hopr_read returns it -- the content of mesh_readin.f90:ReadMesh's MortarType/MortarInfo
+ * (mesh_vars.f90:122-126), with the small-side metrics of mortar_metrics.f90:Mortar_CalcSurfMetrics and
+ * the operators of mortar.f90:InitMortar. BR1 lifting; the split form needs Gauss-Lobatto nodes. */
+int fg_build_mesh_mortar(fg_handle* h, int nElems, int NGeo, const double* NodeCoords, const int* ElemNb, int nBCs, const int* BoundaryType,
+                         int nRefStates, const double* RefStatePrim, const int* ElemInst, int nMortars, const int* Mortars);
+
 /* Drop-in mesh: the arrays of MOD_Mesh_Vars (mesh_vars.f90:34-160) after FLEXI's own InitMesh,
  * SideToElem(5,nSides), ElemToSide(2,6,nElems), BC(nBCSides), Metrics_fTilde/gTilde/hTilde
  * (3,0:N,0:N,0:N,nElems), sJ(0:N,0:N,0:N,nElems), NormVec/TangVec1/TangVec2(3,0:N,0:N,nSides),
@@ -203,7 +212,7 @@ int fg_debug_array(fg_handle* h, const char* name, void* out, long long* count);
 /* Per-kernel CUDA-event timing of later launches on the handle's stream; while enabled, fg_run issues
  * the kernels directly instead of replaying the captured graph. fg_profile_read returns, per kernel
  * class (0 prep, 1 lift, 2 flux, 3 volume+update, 4 time step, 5 other), the summed milliseconds and
- * the launch counts since the previous read, and resets them. */
+ * the launch counts since the previous read, and resets them (class 5 includes the mortar kernels). */
 int fg_profile_enable(fg_handle* h, int on);
 int fg_profile_read(fg_handle* h, double* ms, long long* counts);
 

@@ -1,0 +1,116 @@
+"""Mortar interfaces on the GPU (k_mortar_pre, k_lift<MORTAR>, k_mortar_face; mortar.f90, fillmortar.t90)
+against the oracle on the reference's own mortar meshes (tests/golden/hopr/).
+
+- Ut parity at 1e-12 (as test_gpu_parity.py) on the periodic p_3D_mortar mesh (mortar types 1, 2, 3),
+  the flipped h_3D_mortar meshes (type 3) and the run_basic/freestream_3D mortar box (types 1, 2, its
+  Dirichlet sides replaced by adiabatic walls); Gauss and Gauss-Lobatto weak form, the Gauss-Lobatto split
+  form, lines of up to 11 nodes (the kernels whose arrays live in global scratch).
+- a constant state is preserved on the periodic mortar meshes and a fluid at rest on the walled box.
+- ten LSERK steps with the CFL time step agree with the oracle's (states at 1e-11), on the sine-wave
+  convergence case of convtest/h_3D_mortar (no source term: the operator only).
+- the adjoint refuses mortar meshes.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from _cases import oracle_cfg, perturb_state, product_cfg, rel_err
+from flexi_gb300 import mesh as fmesh, testcases
+from flexi_gb300.solver import Flexi, FlexiError
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+HOPR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "hopr")
+COMMON = dict(kappa=1.4, R=287.058, Pr=0.72, mu0=1e-3)
+MESHES = ["CART_HEX_PERIODIC_MORTAR_002_mesh.h5", "CART_HEX_PERIODIC_MORTAR_FLIPPED_004_mesh.h5", "cartbox3D_mortar_mesh.h5"]
+
+
+def _mesh(name):
+    m0 = fmesh.read_hopr(os.path.join(HOPR, name))
+    if name.startswith("cartbox"):
+        return fmesh.read_hopr(os.path.join(HOPR, name), boundary={nm: (3, 0) for nm in m0.bc_names if nm != "inner"})
+    return m0
+
+
+def _state(x, seed):
+    return perturb_state(testcases.sine_wave_state(x, 0.0, (0.3, 0.3, 0.3)), seed=seed, amp=0.1)
+
+
+@pytest.mark.parametrize("name", MESHES)
+@pytest.mark.parametrize("kw", [dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="roeentropyfix"),
+                                dict(N=4, NodeType="gauss-lobatto", SplitDG="weak", Riemann="roe"),
+                                dict(N=5, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roeentropyfix")])
+def test_rhs_parity_mortar(name, kw):
+    c = product_cfg(**kw, **COMMON)
+    m = _mesh(name)
+    f = Flexi(c, m)
+    o = orc.Oracle(oracle_cfg(c), m)
+    U0 = _state(f.elem_xgp(), seed=5)
+    f.U = U0
+    o.set_state(U0)
+    err = rel_err(f.DGTimeDerivative_weakForm(0.0), o.time_derivative(0.0))
+    f.close()
+    assert err <= 1e-12, err
+
+
+@pytest.mark.parametrize("kw", [dict(N=8, NodeType="gauss", SplitDG="weak", Riemann="roe"),
+                                dict(N=10, NodeType="gauss", SplitDG="weak", Riemann="roeentropyfix"),
+                                dict(N=9, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roeentropyfix")])
+def test_rhs_parity_mortar_high_order(kw):
+    c = product_cfg(**kw, **COMMON)
+    m = _mesh("CART_HEX_PERIODIC_MORTAR_002_mesh.h5")
+    f = Flexi(c, m)
+    o = orc.Oracle(oracle_cfg(c), m)
+    U0 = _state(f.elem_xgp(), seed=6)
+    f.U = U0
+    o.set_state(U0)
+    err = rel_err(f.DGTimeDerivative_weakForm(0.0), o.time_derivative(0.0))
+    f.close()
+    assert err <= 1e-12, err
+
+
+@pytest.mark.parametrize("name", MESHES)
+def test_free_stream_mortar(name):
+    c = product_cfg(N=4, NodeType="gauss", SplitDG="weak", Riemann="roe", **COMMON)
+    f = Flexi(c, _mesh(name))
+    x = f.elem_xgp()
+    U = np.empty(x.shape[:-1] + (5,))
+    if name.startswith("cartbox"):
+        U[...] = [1.0, 0.0, 0.0, 0.0, 2.5]
+    else:
+        U[...] = [1.2, 0.3, -0.2, 0.5, 3.1]
+    f.U = U
+    Ut = f.DGTimeDerivative_weakForm(0.0)
+    f.close()
+    assert np.abs(Ut).max() <= 1e-12
+
+
+def test_lserk_steps_mortar():
+    c = product_cfg(N=3, NodeType="gauss", SplitDG="weak", Riemann="roeentropyfix", CFLScale=0.9, DFLScale=0.9, **COMMON)
+    m = _mesh("CART_HEX_PERIODIC_MORTAR_FLIPPED_004_mesh.h5")
+    f = Flexi(c, m)
+    o = orc.Oracle(oracle_cfg(c), m)
+    U0 = testcases.sine_wave_state(f.elem_xgp(), 0.0, (0.3, 0.3, 0.3))
+    f.U = U0
+    o.set_state(U0)
+    t_f = t_o = 0.0
+    for _ in range(10):
+        dt_f = f.CalcTimeStep()[0]
+        dt_o = o.calc_timestep()[0]
+        assert abs(dt_f / dt_o - 1.0) <= 1e-12
+        t_f = f.TimeStepByLSERKW2(t_f, dt_f)
+        t_o = o.timestep(t_o, dt_o)
+    err = rel_err(f.U, o.get_state())
+    f.close()
+    assert err <= 1e-11, err
+
+
+def test_adjoint_refuses_mortars():
+    c = product_cfg(N=3, NodeType="gauss", SplitDG="weak", Riemann="roe", **COMMON)
+    f = Flexi(c, _mesh("CART_HEX_PERIODIC_MORTAR_002_mesh.h5"))
+    f.U = _state(f.elem_xgp(), seed=1)
+    with pytest.raises(FlexiError, match="mortar"):
+        f.vjp_time_derivative(np.ones_like(f.U))
+    f.close()

@@ -2,6 +2,7 @@
 mesh preparation (sides, flips, curl-form metrics, surface metrics) against the oracle's restatement
 of FLEXI's InitMesh/CalcMetrics. No GPU work is issued here."""
 import ctypes
+import dataclasses
 import os
 import re
 
@@ -94,3 +95,61 @@ def test_mesh_preparation_matches_oracle(lib, mesh_name, N, node_type):
         a, b = f.mesh_array(name), o.mesh_array(name)
         assert np.abs(a - b).max() <= 1e-13 * max(1.0, np.abs(b).max()), name
     f.close()
+
+
+HOPR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "hopr")
+
+
+def _side_keys(s2e):
+    """side -> (slave element, slave local side) where there is a slave, else (master element, its local side)"""
+    return [("s", int(r[1]), int(r[3])) if r[1] > 0 else ("m", int(r[0]), int(r[2])) for r in s2e]
+
+
+@pytest.mark.parametrize("mesh_file", ["CART_HEX_PERIODIC_MORTAR_002_mesh.h5", "CART_HEX_PERIODIC_MORTAR_FLIPPED_002_mesh.h5",
+                                       "cartbox3D_mortar_mesh.h5"])
+@pytest.mark.parametrize("N,node_type", [(3, 1), (4, 2)])
+def test_mortar_mesh_preparation_matches_oracle(lib, mesh_file, N, node_type):
+    """Mortar sides (mesh_readin.f90 MortarType/MortarInfo, mortar_metrics.f90:Mortar_CalcSurfMetrics): the
+    library orders sides BC | conforming | small | big, the oracle BC | big | conforming | small; matched by
+    (slave element, its local side), or (master element, its local side) for sides without a slave, every
+    side has the same flip and the same normals, tangents and surface elements. Small sides carry the big
+    element as master in the library (its viscosity), none in the oracle."""
+    m0 = fmesh.read_hopr(os.path.join(HOPR, mesh_file))
+    m = fmesh.read_hopr(os.path.join(HOPR, mesh_file), boundary={nm: (3, 0) for nm in m0.bc_names if nm != "inner"})
+    o = orc.Oracle(_oracle_cfg(N, node_type), m)
+    f = Flexi(make_config(N=N, NodeType=node_type, SplitDG=-1))
+    f.build_mesh(m, host_only_ok=True)
+    assert (f.n_elems, f.n_sides, f.n_bc_sides) == (o.n_elems, o.n_sides, o.n_bc_sides)
+    fs, os_ = f.side_to_elem(), o.mesh_iarray("SideToElem")
+    ko = {k: i for i, k in enumerate(_side_keys(os_))}
+    perm = np.array([ko[k] for k in _side_keys(fs)])
+    assert len(set(perm.tolist())) == f.n_sides
+    assert np.array_equal(fs[:, [1, 3, 4]], os_[perm][:, [1, 3, 4]])  # slave, its local side, flip
+    small = os_[perm, 0] == -1
+    assert small.sum() == sum(4 if t == 1 else 2 for t in m.mortars[:, 2])
+    assert np.array_equal(fs[~small][:, [0, 2]], os_[perm[~small]][:, [0, 2]])
+    for name in ("NormVec", "TangVec1", "TangVec2", "SurfElem"):
+        a, b = f.mesh_array(name), o.mesh_array(name)[perm]
+        assert np.abs(a - b).max() <= 1e-13 * max(1.0, np.abs(b).max()), name
+    f.close()
+
+
+def test_mortar_mesh_errors(lib):
+    m = fmesh.read_hopr(os.path.join(HOPR, "CART_HEX_PERIODIC_MORTAR_002_mesh.h5"))
+    f = Flexi(make_config(N=3, NodeType=1, SplitDG=-1))
+    bad = dataclasses.replace(m, mortars=m.mortars[:-1])
+    with pytest.raises(FlexiError, match="do not match the Mortars table"):
+        f.build_mesh(bad, host_only_ok=True)
+    swapped = m.mortars.copy()
+    swapped[0, 3] = swapped[1, 3]  # a small side named twice
+    with pytest.raises(FlexiError, match="mortar"):
+        f.build_mesh(dataclasses.replace(m, mortars=swapped), host_only_ok=True)
+    f.close()
+    g = Flexi(make_config(N=3, NodeType=2, SplitDG="pi", Lifting="br2"))
+    with pytest.raises(FlexiError, match="BR1"):
+        g.build_mesh(m, host_only_ok=True)
+    g.close()
+    g = Flexi(make_config(N=3, NodeType=1, SplitDG="pi"))
+    with pytest.raises(FlexiError, match="Gauss-Lobatto"):
+        g.build_mesh(m, host_only_ok=True)
+    g.close()
