@@ -18,6 +18,10 @@ e2e    : the same metric through the public C ABI with the state in pinned host 
 --workload tgv-oint : the discretisation of the reference's tgv/oInt regression (N=11 Gauss, weak form,
          overintegration by the modal cut-off of J u_t to NUnder=7, BR1, RoeEntropyFix, CFL=DFL=0.9) on a
          curved 16^3 mesh (7.1 M DOF), same metric and timing.
+--workload tgv-mortar : TGV on a periodic box with mortar interfaces (24^3 cells whose z-layers alternate
+         between one element per cell and 2x2 elements, 34560 elements, 13824 mortars 1->4, perturbed,
+         NGeo=1), N=7 Gauss-Lobatto, split PI, BR1 (the lifting the mortar path supports), RoeEntropyFix
+         (17.7 M DOF), same metric and timing.
 --impl reference : the CPU implementation of the path (the C++ restatement of FLEXI's Fortran solver,
          FLEXI itself cannot be built here: Fortran/MPI/HDF5) on all host threads, bounded sample per step.
 Multi-GPU: the path does not shard on this setup (no halo exchange is built); N ranks run N replicas.
@@ -52,6 +56,11 @@ SPLITGAUSS_FLOPS_PER_DOF_STAGE = {"prep": 128.0, "lift": 500.0, "flux": 194.0, "
 # RoeEntropyFix, modal cut-off filter of J u_t to NUnder=7); "vol" includes the filter
 OINT_METRIC = "FP64 DOF*stage/s (N=11 TGV, overintegration cut-off to NUnder=7)"
 OINT_FLOPS_PER_DOF_STAGE = {"prep": 78.5, "lift": 640.0, "flux": 94.75, "vol": 935.25}
+# mortar interfaces (N=7 Gauss-Lobatto, split PI, BR1, RoeEntropyFix on the periodic mortar box); the
+# oracle books U_Mortar in prep, the lifting projections in lift and the small-side fluxes with Flux_Mortar
+# in flux, the GPU runs them in k_mortar_pre / k_mortar_face
+MORTAR_METRIC = "FP64 DOF*stage/s (N=7 TGV, mortar box)"
+MORTAR_FLOPS_PER_DOF_STAGE = {"prep": 49.8, "lift": 398.4, "flux": 198.2, "vol": 1409.25}
 
 
 def flops_per_dof_stage(riemann, kind="tgv"):
@@ -59,6 +68,8 @@ def flops_per_dof_stage(riemann, kind="tgv"):
         return dict(SPLITGAUSS_FLOPS_PER_DOF_STAGE)
     if kind == "tgv-oint":
         return dict(OINT_FLOPS_PER_DOF_STAGE)
+    if kind == "tgv-mortar":
+        return dict(MORTAR_FLOPS_PER_DOF_STAGE)
     return dict(FLOPS_PER_DOF_STAGE, flux=FLUX_FLOPS_PER_DOF_STAGE[riemann])
 # compulsory HBM traffic per DOF and stage: U read+write, Ut_tmp read+write, 9 metric terms + sJ
 BYTES_ALG_PER_DOF_STAGE = 240.0
@@ -72,9 +83,11 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--elems", type=int, default=None, help="elements per direction (tgv: 32, tgv-splitgauss: 40, tgv-oint: 16)")
     p.add_argument("--riemann", default="hllc", choices=sorted(RIEMANN_IDS), help="surface Riemann solver")
-    p.add_argument("--workload", default="tgv", choices=["tgv", "tgv-splitgauss", "tgv-oint", "ensemble", "adjoint", "adjoint-channel"],
+    p.add_argument("--workload", default="tgv", choices=["tgv", "tgv-splitgauss", "tgv-oint", "tgv-mortar", "ensemble", "adjoint",
+                                                        "adjoint-channel"],
                    help="tgv: the single-case N=7 TGV; tgv-splitgauss: the N=5 Gauss split form of the reference's tgv/splitGauss "
-                        "regression on a curved 40^3 mesh; tgv-oint: the N=11 overintegration of tgv/oInt on a curved 16^3 mesh; ensemble: 256 independent TGV/vortex instances at N=5 against a loop over "
+                        "regression on a curved 40^3 mesh; tgv-oint: the N=11 overintegration of tgv/oInt on a curved 16^3 mesh; "
+                        "tgv-mortar: N=7 on a 24^3-cell box with 1->4 mortar interfaces; ensemble: 256 independent TGV/vortex instances at N=5 against a loop over "
                         "instances; adjoint: gradient of a kinetic-energy loss over a 200-step TGV solve (16^3, N=5)")
     p.add_argument("--ckpt", type=int, default=20, help="adjoint: checkpoint interval in steps")
     p.add_argument("--fd-dirs", type=int, default=20, help="adjoint: random directions of the finite-difference check")
@@ -83,13 +96,22 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline leg (profiling runs)")
     a = p.parse_args()
     if a.elems is None:
-        a.elems = {"tgv-splitgauss": 40, "tgv-oint": 16}.get(a.workload, 32)
-    if a.workload in ("tgv-splitgauss", "tgv-oint"):
+        a.elems = {"tgv-splitgauss": 40, "tgv-oint": 16, "tgv-mortar": 24}.get(a.workload, 32)
+    if a.workload in ("tgv-splitgauss", "tgv-oint", "tgv-mortar"):
         a.riemann = "roeentropyfix"
     return a
 
 
 def workload_config(n, riemann, kind="tgv"):
+    if kind == "tgv-mortar":
+        ne = 5 * n ** 3 // 2
+        dof = ne * 512
+        return {"workload": f"TGV on the periodic mortar box of {n}^3 cells (z-layers alternating 1 and 2x2 elements per cell, "
+                            f"{ne} elements, {n ** 3} mortars 1->4, perturbation 0.05, NGeo=1), N=7 Gauss-Lobatto, split PI, BR1, "
+                            f"RoeEntropyFix, FP64",
+                "n_elems": ne, "n_mortars": n ** 3, "N": 7, "dof": dof, "Re": 1600, "Ma": 0.1, "CFLScale": 0.8, "DFLScale": 0.8,
+                "time_integration": "CarpenterRK4-5, 5 stages/step, CFL/DFL dt each step",
+                "l2": f"inputs larger than L2 (state {dof * 40 / 1e6:.0f} MB)", "parallelism": "replicas"}
     if kind == "tgv-oint":
         dof = n ** 3 * 1728
         return {"workload": f"TGV {n}^3 curved (perturbation 0.05, NGeo=3), N=11 Gauss, weak form, overintegration by the modal "
@@ -112,6 +134,9 @@ def workload_config(n, riemann, kind="tgv"):
 
 def solver_config(riemann, kind="tgv"):
     from flexi_gb300.solver import make_config
+    if kind == "tgv-mortar":
+        return make_config(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roeentropyfix", Lifting="br1", kappa=1.4, R=71.42857,
+                           Pr=0.72, mu0=6.25e-4, CFLScale=0.8, DFLScale=0.8)
     if kind == "tgv-oint":
         return make_config(N=11, NodeType="gauss", SplitDG="weak", Riemann="roeentropyfix", Lifting="br1", kappa=1.4, R=71.42857,
                            Pr=0.72, mu0=6.25e-4, CFLScale=0.9, DFLScale=0.9, OverintegrationType=1, NUnder=7)
@@ -124,6 +149,9 @@ def solver_config(riemann, kind="tgv"):
 
 def oracle_config(riemann, kind="tgv"):
     """The same discretisation for the CPU restatement."""
+    if kind == "tgv-mortar":
+        return dict(N=7, nodeType=2, riemann=33, riemannBC=-1, lifting=1, weakLifting=0, consLifting=0, splitDG=4, etaBR2=2.0,
+                    etaBR2_wall=-1.0, kappa=1.4, R=71.42857, Pr=0.72, mu0=6.25e-4, CFLScale=0.8, DFLScale=0.8, doTCSource=0, dpdx=-1.0)
     if kind == "tgv-oint":
         return dict(N=11, nodeType=1, riemann=33, riemannBC=-1, lifting=1, weakLifting=0, consLifting=0, splitDG=-1, etaBR2=2.0,
                     etaBR2_wall=-1.0, kappa=1.4, R=71.42857, Pr=0.72, mu0=6.25e-4, CFLScale=0.9, DFLScale=0.9, doTCSource=0, dpdx=-1.0,
@@ -136,7 +164,15 @@ def oracle_config(riemann, kind="tgv"):
 
 
 def metric_name(kind):
-    return {"tgv-splitgauss": SPLITGAUSS_METRIC, "tgv-oint": OINT_METRIC}.get(kind, METRIC)
+    return {"tgv-splitgauss": SPLITGAUSS_METRIC, "tgv-oint": OINT_METRIC, "tgv-mortar": MORTAR_METRIC}.get(kind, METRIC)
+
+
+def workload_mesh(kind, n, seed=0):
+    """The workload's mesh: the curved TGV box, or the periodic mortar box."""
+    from flexi_gb300 import mesh as fmesh
+    if kind == "tgv-mortar":
+        return fmesh.mortar_box(n, perturb=0.05, seed=seed)
+    return fmesh.tgv_box(n, ngeo=3, perturb=0.05, seed=seed)
 
 
 def kernel_names(kind):
@@ -144,6 +180,9 @@ def kernel_names(kind):
         return {"vol": "k_vol_weak<12,Gauss> + k_overint<12>", "lift": "k_lift<12,Gauss>", "flux": "k_flux<12>", "prep": "k_prep<12,Gauss>"}
     if kind == "tgv-splitgauss":
         return {"vol": "k_vol_split_gen<6,Gauss>", "lift": "k_lift<6,Gauss>", "flux": "k_flux<6>", "prep": "k_prep<6,Gauss>"}
+    if kind == "tgv-mortar":
+        return {"vol": "k_vol_split<8>", "lift": "k_lift<8,GL,MORTAR>", "flux": "k_flux<8>", "prep": "k_prep<8,GL>",
+                "other": "k_mortar_pre<8> + k_mortar_face<8>"}
     return {"vol": "k_vol_split<8>", "lift": "k_lift<8,GL>", "flux": "k_flux<8>", "prep": "k_prep<8,GL>"}
 
 
@@ -227,7 +266,9 @@ def cpu_baseline_sample(riemann, n_elems_dir=8, budget_s=12.0, kind="tgv"):
     from oracle import oracle as orc
     orc.set_threads(os.cpu_count() or 1)
     cfg = oracle_config(riemann, kind)
-    m = fmesh.tgv_box(n_elems_dir, ngeo=3, perturb=0.05, seed=0)
+    if kind == "tgv-mortar":
+        n_elems_dir = 4
+    m = workload_mesh(kind, n_elems_dir)
     o = orc.Oracle(cfg, m)
     o.set_state(testcases.tgv_state(o.mesh_array("Elem_xGP"), mach=0.1, kappa=1.4, R=71.42857))
     o.overintegrate_state()  # timedisc.f90:115-123 (no-op without overintegration)
@@ -244,7 +285,7 @@ def cpu_baseline_sample(riemann, n_elems_dir=8, budget_s=12.0, kind="tgv"):
         if el >= budget_s or steps >= 200:
             break
     rate = dof * 5 * steps / el
-    return rate, orc.max_threads(), f"TGV {n_elems_dir}^3 same discretisation ({dof} DOF), {steps} RK steps with dt control, {el:.1f} s"
+    return rate, orc.max_threads(), f"{m.description}, same discretisation ({dof} DOF), {steps} RK steps with dt control, {el:.1f} s"
 
 
 def run_reference(args):
@@ -257,8 +298,8 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     orc.set_threads(threads)
     cfg = oracle_config(args.riemann, args.workload)
-    ns = 6  # bounded sample: 6^3 elements of the same discretisation per step
-    m = fmesh.tgv_box(ns, ngeo=3, perturb=0.05, seed=0)
+    ns = 4 if args.workload == "tgv-mortar" else 6  # bounded sample of the same discretisation per step
+    m = workload_mesh(args.workload, ns)
     o = orc.Oracle(cfg, m)
     o.set_state(testcases.tgv_state(o.mesh_array("Elem_xGP"), mach=0.1, kappa=1.4, R=71.42857))
     o.overintegrate_state()  # timedisc.f90:115-123 (no-op without overintegration)
@@ -273,7 +314,7 @@ def run_reference(args):
         t = o.timestep(t, dt)
     el = time.perf_counter() - t0
     value = dof * 5 * args.steps / el
-    sample = f"TGV {ns}^3 of the workload's discretisation ({dof} DOF) per step, {args.steps} RK steps, {el:.2f} s"
+    sample = f"{m.description}, the workload's discretisation ({dof} DOF) per step, {args.steps} RK steps, {el:.2f} s"
     line = {"impl": "reference", "metric": metric_name(args.workload), "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(args.elems, args.riemann, args.workload),
@@ -301,7 +342,7 @@ def run_gb300(args):
     kind = args.workload
     cfgd = workload_config(n, args.riemann, kind)
     c = solver_config(args.riemann, kind)
-    m = fmesh.tgv_box(n, ngeo=3, perturb=0.05, seed=rank)
+    m = workload_mesh(kind, n, seed=rank)
     f = Flexi(c, m)
     U0 = testcases.tgv_state(f.elem_xgp(), mach=0.1, kappa=1.4, R=71.42857)
     f.U = U0

@@ -115,6 +115,90 @@ def tgv_box(n_per_dir, ngeo=1, perturb=0.0, seed=0):
     return m
 
 
+def mortar_box(n_per_dir, perturb=0.0, seed=0):
+    """Periodic [-pi, pi]^3 box of n^3 cells (n even) with mortar interfaces: the z-layers of cells alternate
+    between one element per cell (even layers) and four elements of half the width in x and y (odd
+    layers), so that both zeta faces of every coarse element are big mortar sides of type 1 (1->4) and the
+    fine elements meet conformingly among themselves. 2.5 n^3 elements, n^3 mortars, NGeo=1.
+    perturb > 0 displaces x and y by perturb * (2 pi / n) * prod_j sin(x_j + phi_ij) (phases seeded, periodic),
+    evaluated at the coarse grid's corners and interpolated bilinearly in x and y to the fine nodes, so that
+    the small faces still tile their big faces exactly."""
+    n = int(n_per_dir)
+    if n < 2 or n % 2:
+        raise ValueError("mortar_box needs an even number of cells per direction")
+    h = 2.0 * np.pi / n
+    coarse, fine = {}, {}
+    boxes = []  # (x0, y0, z0, hx, hy) per element, z-height h
+    for k in range(n):
+        for j in range(n):
+            for i in range(n):
+                if k % 2 == 0:
+                    coarse[(i, j, k)] = len(boxes)
+                    boxes.append((-np.pi + i * h, -np.pi + j * h, -np.pi + k * h, h, h))
+                else:
+                    for b in range(2):
+                        for a in range(2):
+                            fine[(2 * i + a, 2 * j + b, k)] = len(boxes)
+                            boxes.append((-np.pi + (2 * i + a) * h / 2, -np.pi + (2 * j + b) * h / 2, -np.pi + k * h, h / 2, h / 2))
+    ne = len(boxes)
+    B = np.array(boxes)
+    xi = np.array([0.0, 1.0])
+    X = B[:, 0, None, None, None] + xi[None, None, None, :] * B[:, 3, None, None, None]
+    Y = B[:, 1, None, None, None] + xi[None, None, :, None] * B[:, 4, None, None, None]
+    Z = B[:, 2, None, None, None] + xi[None, :, None, None] * h
+    X, Y, Z = np.broadcast_arrays(X, Y, Z)
+    X, Y = X.copy(), Y.copy()
+    if perturb:
+        rng = np.random.default_rng(seed)
+        phi = rng.uniform(0.0, 2.0 * np.pi, size=(2, 3))
+        amp = perturb * h
+
+        def disp(x, y, z, c):
+            return amp * np.sin(x + phi[c, 0]) * np.sin(y + phi[c, 1]) * np.sin(z + phi[c, 2])
+        # displacement of the coarse grid's corner nodes, interpolated bilinearly in x and y at the fine nodes
+        gx = (X + np.pi) / h
+        gy = (Y + np.pi) / h
+        x0, y0 = np.floor(gx + 1e-9), np.floor(gy + 1e-9)
+        fx, fy = gx - x0, gy - y0
+        for c, A in ((0, X), (1, Y)):
+            d = 0.0
+            for dx, wx in ((0, 1 - fx), (1, fx)):
+                for dy, wy in ((0, 1 - fy), (1, fy)):
+                    d = d + wx * wy * disp(-np.pi + (x0 + dx) * h, -np.pi + (y0 + dy) * h, Z, c)
+            A += d
+    node_coords = np.stack([X, Y, Z], axis=-1).astype(np.float64)
+    nb = np.zeros((ne, 6, 3), np.int32)
+    mortars = []
+    for (i, j, k), e in coarse.items():
+        nb[e, XI_MINUS - 1] = (coarse[((i - 1) % n, j, k)] + 1, XI_PLUS, 0)
+        nb[e, XI_PLUS - 1] = (coarse[((i + 1) % n, j, k)] + 1, XI_MINUS, 0)
+        nb[e, ETA_MINUS - 1] = (coarse[(i, (j - 1) % n, k)] + 1, ETA_PLUS, 0)
+        nb[e, ETA_PLUS - 1] = (coarse[(i, (j + 1) % n, k)] + 1, ETA_MINUS, 0)
+        nb[e, ZETA_MINUS - 1] = (-1, 0, 0)
+        nb[e, ZETA_PLUS - 1] = (-1, 0, 0)
+        # zeta+ side: p ~ x, q ~ y (small side im = a + 2b); zeta- side: p ~ y, q ~ x (im = b + 2a)
+        up = [0] * 4
+        dn = [0] * 4
+        for b in range(2):
+            for a in range(2):
+                up[a + 2 * b] = fine[(2 * i + a, 2 * j + b, (k + 1) % n)]
+                dn[b + 2 * a] = fine[(2 * i + a, 2 * j + b, (k - 1) % n)]
+        mortars.append([e + 1, ZETA_PLUS, 1] + sum(([s + 1, ZETA_MINUS, 0] for s in up), []))
+        mortars.append([e + 1, ZETA_MINUS, 1] + sum(([s + 1, ZETA_PLUS, 0] for s in dn), []))
+    m2 = 2 * n
+    for (I, J, k), e in fine.items():
+        nb[e, XI_MINUS - 1] = (fine[((I - 1) % m2, J, k)] + 1, XI_PLUS, 0)
+        nb[e, XI_PLUS - 1] = (fine[((I + 1) % m2, J, k)] + 1, XI_MINUS, 0)
+        nb[e, ETA_MINUS - 1] = (fine[(I, (J - 1) % m2, k)] + 1, ETA_PLUS, 0)
+        nb[e, ETA_PLUS - 1] = (fine[(I, (J + 1) % m2, k)] + 1, ETA_MINUS, 0)
+        nb[e, ZETA_MINUS - 1] = (-1, 0, 0)
+        nb[e, ZETA_PLUS - 1] = (-1, 0, 0)
+    m = BoxMesh(ne, 1, node_coords, nb, np.zeros((0, 2), np.int32), np.zeros((0, 6)),
+                description=f"periodic mortar box {n}^3 cells ({ne} elements, {len(mortars)} mortars), perturbation={perturb}",
+                mortars=np.array(mortars, np.int32))
+    return m
+
+
 def channel_box(nelems=(24, 12, 12), beta=1.5, ngeo=None, t_wall=1.0, rho_wall=1.0, p_wall=1.0):
     """Channel [0,2pi]x[-1,1]x[0,pi] with isothermal no-slip walls (BC type 4) at y=+-1, periodic in x and z,
     y-stretched by y = tanh(beta*eta)/tanh(beta) (elements cluster at the walls)."""

@@ -47,3 +47,13 @@ def test_oint_flops_per_dof_stage_match_oracle_count():
     counted = o.flops_breakdown()
     for k, v in bench.flops_per_dof_stage("roeentropyfix", "tgv-oint").items():
         assert v == pytest.approx(counted[k], rel=2e-3), (k, v, counted[k])
+
+
+def test_mortar_flops_per_dof_stage_match_oracle_count():
+    bench = _bench()
+    m = fmesh.mortar_box(2, perturb=0.05)
+    o = orc.Oracle(bench.oracle_config("roeentropyfix", "tgv-mortar"), m)
+    o.set_state(testcases.tgv_state(o.mesh_array("Elem_xGP"), mach=0.1, kappa=1.4, R=71.42857))
+    counted = o.flops_breakdown()
+    for k, v in bench.flops_per_dof_stage("roeentropyfix", "tgv-mortar").items():
+        assert v == pytest.approx(counted[k], rel=2e-3), (k, v, counted[k])

@@ -5,6 +5,7 @@ against the oracle on the reference's own mortar meshes (tests/golden/hopr/).
   the flipped h_3D_mortar meshes (type 3) and the run_basic/freestream_3D mortar box (types 1, 2, its
   Dirichlet sides replaced by adiabatic walls); Gauss and Gauss-Lobatto weak form, the Gauss-Lobatto split
   form, lines of up to 11 nodes (the kernels whose arrays live in global scratch).
+- the same on the library's synthetic mortar box (the mortar bench mesh) at 160 elements.
 - a constant state is preserved on the periodic mortar meshes and a fluid at rest on the walled box.
 - ten LSERK steps with the CFL time step agree with the oracle's (states at 1e-11), on the sine-wave
   convergence case of convtest/h_3D_mortar (no source term: the operator only).
@@ -48,6 +49,23 @@ def test_rhs_parity_mortar(name, kw):
     f = Flexi(c, m)
     o = orc.Oracle(oracle_cfg(c), m)
     U0 = _state(f.elem_xgp(), seed=5)
+    f.U = U0
+    o.set_state(U0)
+    err = rel_err(f.DGTimeDerivative_weakForm(0.0), o.time_derivative(0.0))
+    f.close()
+    assert err <= 1e-12, err
+
+
+@pytest.mark.parametrize("kw", [dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="roeentropyfix"),
+                                dict(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roeentropyfix"),
+                                dict(N=5, NodeType="gauss-lobatto", SplitDG="sd", Riemann="hllc")])
+def test_rhs_parity_synthetic_mortar_box(kw):
+    """The bench's mortar mesh (perturbed periodic mortar box, both big-side orientations) at a small size."""
+    c = product_cfg(**kw, **COMMON)
+    m = fmesh.mortar_box(4, perturb=0.05, seed=1)
+    f = Flexi(c, m)
+    o = orc.Oracle(oracle_cfg(c), m)
+    U0 = perturb_state(testcases.tgv_state(f.elem_xgp(), mach=0.1, kappa=1.4, R=287.058), seed=7)
     f.U = U0
     o.set_state(U0)
     err = rel_err(f.DGTimeDerivative_weakForm(0.0), o.time_derivative(0.0))

@@ -87,6 +87,28 @@ def test_free_stream_and_conservation(name, form):
     assert (np.abs(total) <= 1e-13 * scale).all(), (total, scale)
 
 
+@pytest.mark.parametrize("perturb", [0.0, 0.1])
+@pytest.mark.parametrize("form", list(FORMS))
+def test_synthetic_mortar_box(perturb, form):
+    """The library's periodic mortar box (flexi_gb300.mesh.mortar_box, both zeta faces of every coarse element
+    1->4 mortars, the small sides on both orientations of the big side): free stream and conservation."""
+    m = fmesh.mortar_box(4, perturb=perturb, seed=2)
+    assert m.n_elems == 160 and len(m.mortars) == 64
+    o = orc.Oracle(dict(BASE, N=4, **FORMS[form]), m)
+    x = o.mesh_array("Elem_xGP")
+    U = np.empty(x.shape[:-1] + (5,))
+    U[...] = [1.2, 0.3, -0.2, 0.5, 3.1]
+    o.set_state(U)
+    assert np.abs(o.time_derivative(0.0)).max() <= 2e-12
+    o.set_state(perturb_state(testcases.sine_wave_state(x, 0.0, (0.3, 0.3, 0.3)), seed=3, amp=0.1))
+    Ut = o.time_derivative(0.0)
+    w = orc.nodes_and_weights(4, FORMS[form]["nodeType"])[1]
+    W = np.einsum('a,b,c->abc', w, w, w) / o.mesh_array("sJ")
+    total = (Ut * W[..., None]).sum(axis=(0, 1, 2, 3))
+    scale = (np.abs(Ut) * W[..., None]).sum(axis=(0, 1, 2, 3))
+    assert (np.abs(total) <= 1e-13 * scale).all(), (total, scale)
+
+
 def _sine_wave_run(name, N, adv, t_end=1.0):
     cfg = dict(BASE, N=N, iniExactFunc=4, advVel=adv, **FORMS["gauss-weak"])
     o = orc.Oracle(cfg, _mesh(name))
