@@ -887,11 +887,19 @@ int fg_build_mesh_mortar(fg_handle* h, int nElems, int NGeo, const double* NodeC
 int fg_set_mesh(fg_handle* h, int nElems, int nSides, int nBCSides, const int* SideToElem, const int* ElemToSide, const int* BC, int nBCs,
                 const int* BoundaryType, int nRefStates, const double* RefStatePrim, const double* Mf, const double* Mg, const double* Mh,
                 const double* sJ, const double* NormVec, const double* TangVec1, const double* TangVec2, const double* SurfElem) {
+  return fg_set_mesh_mortar(h, nElems, nSides, nBCSides, SideToElem, ElemToSide, BC, nBCs, BoundaryType, nRefStates, RefStatePrim, Mf, Mg,
+                            Mh, sJ, NormVec, TangVec1, TangVec2, SurfElem, 0, nullptr, nullptr);
+}
+
+int fg_set_mesh_mortar(fg_handle* h, int nElems, int nSides, int nBCSides, const int* SideToElem, const int* ElemToSide, const int* BC,
+                       int nBCs, const int* BoundaryType, int nRefStates, const double* RefStatePrim, const double* Mf, const double* Mg,
+                       const double* Mh, const double* sJ, const double* NormVec, const double* TangVec1, const double* TangVec2,
+                       const double* SurfElem, int nMortars, const int* MortarType, const int* MortarInfo) {
   if (!h) return FG_ERR_STATE;
   try {
     fgh::build_from_flexi(h->cfg.N, h->cfg.NodeType == FG_NODE_GAUSS_LOBATTO ? fgh::LOBATTO : fgh::GAUSS, nElems, nSides, nBCSides,
                           SideToElem, ElemToSide, BC, nBCs, BoundaryType, nRefStates, RefStatePrim, Mf, Mg, Mh, sJ, NormVec, TangVec1,
-                          TangVec2, SurfElem, h->M);
+                          TangVec2, SurfElem, nMortars, MortarType, MortarInfo, h->M);
   } catch (std::exception& e) {
     return fail(h, FG_ERR_MESH, e.what());
   }
@@ -906,7 +914,8 @@ int fg_set_face_metrics(fg_handle* h, const double* Ja_Face, const double* Ja_sl
   static const int normalDir[7] = {0, 2, 1, 0, 1, 0, 2};  // 0-based row, mesh_vars.f90:105-111
   for (int e = 0; e < M.nElems; ++e)
     for (int ls = 1; ls <= 6; ++ls) {
-      const int code = M.elemSide[e * 6 + ls - 1], s = code >> 3, flip = code & 7;
+      const int code = M.elemSide[e * 6 + ls - 1], flip = code & 7;
+      const int s = M.flexiSide.empty() ? code >> 3 : M.flexiSide[code >> 3];  // FLEXI's side numbering
       const double* J = flip == 0 ? Ja_Face : Ja_slave;
       for (int q = 0; q < n; ++q)
         for (int p = 0; p < n; ++p) {

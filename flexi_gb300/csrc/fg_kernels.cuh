@@ -618,7 +618,7 @@ __device__ void mortar_project(const MortarDev& M, int type, int nv, const doubl
 // small sides' BR1 lifting fluxes times normal (lifting_fillflux.t90) projected onto the big side
 // (lifting_br1.t90:106-109) for k_lift<MORTAR>.
 template <int n>
-__global__ void __launch_bounds__(256) k_mortar_pre(Dev d, Basis B, MortarDev M) {
+__global__ void __launch_bounds__(256, 2) k_mortar_pre(Dev d, Basis B, MortarDev M) {
   constexpr int n2 = n * n;
   extern __shared__ double smem[];
   double* sUb = smem;          // [5][n2] big side U
@@ -671,7 +671,7 @@ __global__ void __launch_bounds__(256) k_mortar_pre(Dev d, Basis B, MortarDev M)
 // (lifting_br1.t90:175-178), the small sides' numerical fluxes (fillflux.f90, master viscosity of the big
 // element), and their projection onto the big side (dg.f90:625, Flux_Mortar)
 template <int n>
-__global__ void __launch_bounds__(256) k_mortar_face(Dev d, Basis B, MortarDev M) {
+__global__ void __launch_bounds__(256, 2) k_mortar_face(Dev d, Basis B, MortarDev M) {
   constexpr int n2 = n * n;
   extern __shared__ double smem[];
   double* sGb = smem;           // [12][n2] big side gradients

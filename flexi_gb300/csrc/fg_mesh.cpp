@@ -158,6 +158,7 @@ void build_from_raw(const RawMesh& R, int N, int nodeType, HostMesh& M) {
   M.nBCSides = (int)bcs.size();
   M.nFluxSides = M.nBCSides + (int)inner.size();
   M.nMortars = nMo;
+  M.flexiSide.clear();
   M.nSides = M.nFluxSides + nSmall + nMo;
   M.sideElem.assign((size_t)M.nSides * 4, -1);
   M.elemSide.assign((size_t)nE * 6, 0);
@@ -421,23 +422,78 @@ void build_from_raw(const RawMesh& R, int N, int nodeType, HostMesh& M) {
 void build_from_flexi(int N, int nodeType, int nElems, int nSides, int nBCSides, const int* SideToElem, const int* ElemToSide, const int* BC,
                       int nBCs, const int* BoundaryType, int nRefStates, const double* RefStatePrim, const double* Mf, const double* Mg,
                       const double* Mh, const double* sJ, const double* NormVec, const double* TangVec1, const double* TangVec2,
-                      const double* SurfElem, HostMesh& M) {
+                      const double* SurfElem, int nMortars, const int* MortarType, const int* MortarInfo, HostMesh& M) {
   const int n = N + 1, n2 = n * n, n3 = n2 * n;
   M.N = N; M.n = n; M.nodeType = nodeType; M.nElems = nElems; M.nSides = nSides; M.nBCSides = nBCSides;
-  M.nFluxSides = nSides; M.nMortars = 0; M.mortarInfo.clear();
+  if (nMortars < 0 || (nMortars > 0 && (!MortarType || !MortarInfo))) throw std::runtime_error("invalid mortar arrays");
+  // side order of the library: BC | conforming inner | small mortar | big mortar. FLEXI's big mortar sides
+  // carry MortarType(1,SideID) > 0 and the small sides of mortar MortarType(2,SideID) in MortarInfo
+  // (mesh_vars.f90:158-159); a small side has no master element (its data come from the big side).
+  std::vector<int> newId(nSides, -1), order;
+  order.reserve(nSides);
+  std::vector<int> bigOf(nMortars, -1);
+  for (int s = 0; s < nSides; ++s) {
+    const int type = nMortars ? MortarType[(size_t)s * 2] : 0;
+    if (type < 0 || type > 3) throw std::runtime_error("MortarType must be 0..3 (no MPI mortars)");
+    if (type > 0) {
+      const int m = MortarType[(size_t)s * 2 + 1] - 1;
+      if (m < 0 || m >= nMortars || bigOf[m] >= 0) throw std::runtime_error("invalid mortar index in MortarType");
+      bigOf[m] = s;
+    }
+  }
+  for (int m = 0; m < nMortars; ++m) if (bigOf[m] < 0) throw std::runtime_error("mortar without big side");
+  std::vector<char> isSmall(nSides, 0);
+  for (int m = 0; m < nMortars; ++m) {
+    const int nm = MortarType[(size_t)bigOf[m] * 2] == 1 ? 4 : 2;
+    for (int im = 0; im < nm; ++im) {
+      const int ss = MortarInfo[((size_t)m * 4 + im) * 2] - 1;
+      if (ss < nBCSides || ss >= nSides || isSmall[ss] || SideToElem[(size_t)ss * 5] > 0 || SideToElem[(size_t)ss * 5 + 1] <= 0)
+        throw std::runtime_error("MortarInfo names a side that is not a small mortar side");
+      isSmall[ss] = 1;
+    }
+  }
+  for (int s = 0; s < nSides; ++s)
+    if (!isSmall[s] && !(nMortars && MortarType[(size_t)s * 2] > 0)) order.push_back(s);
+  M.nFluxSides = (int)order.size();
+  M.nMortars = nMortars;
+  for (int m = 0; m < nMortars; ++m) {
+    const int nm = MortarType[(size_t)bigOf[m] * 2] == 1 ? 4 : 2;
+    for (int im = 0; im < nm; ++im) order.push_back(MortarInfo[((size_t)m * 4 + im) * 2] - 1);
+  }
+  for (int m = 0; m < nMortars; ++m) order.push_back(bigOf[m]);
+  if ((int)order.size() != nSides) throw std::runtime_error("small mortar sides counted twice or missing");
+  for (int t = 0; t < nSides; ++t) newId[order[t]] = t;
+  M.flexiSide = order;
+  M.mortarInfo.assign((size_t)6 * nMortars, -1);
   M.sideElem.assign((size_t)nSides * 4, -1);
   M.elemSide.assign((size_t)nElems * 6, -1);
-  for (int s = 0; s < nSides; ++s) {
+  for (int t = 0; t < nSides; ++t) {
+    const int s = order[t];
     const int* r = &SideToElem[(size_t)s * 5];
-    if (r[0] <= 0) throw std::runtime_error("side without master element (mortar/MPI sides are not supported)");
-    M.sideElem[s * 4 + 0] = r[0] - 1; M.sideElem[s * 4 + 1] = r[2];
-    if (r[1] > 0) { M.sideElem[s * 4 + 2] = r[1] - 1; M.sideElem[s * 4 + 3] = 8 * r[3] + r[4]; }
-    else if (s >= nBCSides) throw std::runtime_error("inner side without slave element");
+    if (isSmall[s]) continue;  // below, with its mortar
+    if (r[0] <= 0) throw std::runtime_error("side without master element (MPI sides are not supported)");
+    M.sideElem[t * 4 + 0] = r[0] - 1; M.sideElem[t * 4 + 1] = r[2];
+    if (r[1] > 0) { M.sideElem[t * 4 + 2] = r[1] - 1; M.sideElem[t * 4 + 3] = 8 * r[3] + r[4]; }
+    else if (s >= nBCSides && !(nMortars && MortarType[(size_t)s * 2] > 0)) throw std::runtime_error("inner side without slave element");
+  }
+  for (int m = 0; m < nMortars; ++m) {
+    const int sb = bigOf[m], type = MortarType[(size_t)sb * 2], nm = type == 1 ? 4 : 2;
+    const int* rb = &SideToElem[(size_t)sb * 5];
+    M.mortarInfo[(size_t)m * 6 + 0] = type;
+    M.mortarInfo[(size_t)m * 6 + 1] = newId[sb];
+    for (int im = 0; im < nm; ++im) {
+      const int ss = MortarInfo[((size_t)m * 4 + im) * 2] - 1, t = newId[ss];
+      const int* r = &SideToElem[(size_t)ss * 5];
+      M.sideElem[t * 4 + 0] = rb[0] - 1; M.sideElem[t * 4 + 1] = rb[2];
+      M.sideElem[t * 4 + 2] = r[1] - 1; M.sideElem[t * 4 + 3] = 8 * r[3] + r[4];
+      M.mortarInfo[(size_t)m * 6 + 2 + im] = t;
+    }
   }
   for (int e = 0; e < nElems; ++e)
     for (int ls = 1; ls <= 6; ++ls) {
       const int sid = ElemToSide[((size_t)e * 6 + ls - 1) * 2] - 1, flip = ElemToSide[((size_t)e * 6 + ls - 1) * 2 + 1];
-      M.elemSide[e * 6 + ls - 1] = 8 * sid + flip;
+      if (sid < 0 || sid >= nSides) throw std::runtime_error("invalid ElemToSide");
+      M.elemSide[e * 6 + ls - 1] = 8 * newId[sid] + flip;
     }
   M.bcType.assign(nBCSides, 0);
   M.bcTwall.assign(nBCSides, 0.);
@@ -467,10 +523,10 @@ void build_from_flexi(int N, int nodeType, int nElems, int nSides, int nBCSides,
       M.sJ[g] = sJ[g];
     }
   M.geo.assign((size_t)nSides * 10 * n2, 0.);
-  for (int s = 0; s < nSides; ++s)
+  for (int t = 0; t < nSides; ++t)
     for (int pq = 0; pq < n2; ++pq) {
-      const size_t g = (size_t)s * n2 + pq;
-      double* G = &M.geo[(size_t)s * 10 * n2 + pq];
+      const size_t g = (size_t)order[t] * n2 + pq;
+      double* G = &M.geo[(size_t)t * 10 * n2 + pq];
       for (int c = 0; c < 3; ++c) { G[c * n2] = NormVec[g * 3 + c]; G[(3 + c) * n2] = TangVec1[g * 3 + c]; G[(6 + c) * n2] = TangVec2[g * 3 + c]; }
       G[9 * n2] = SurfElem[g];
     }

@@ -34,6 +34,7 @@ struct HostMesh {
   // sides are ordered BC | conforming inner | small mortar | big mortar; nFluxSides = BC + conforming inner
   int nFluxSides = 0, nMortars = 0;
   std::vector<int> mortarInfo;  // [m][6]: type, big side, small sides (-1: unused)
+  std::vector<int> flexiSide;   // drop-in meshes: FLEXI's SideID - 1 of each side (empty: identity)
   std::vector<int> sideElem;    // [s][4]
   std::vector<int> elemSide;    // [e][6]
   std::vector<int> sideInst, elemInst;
@@ -57,7 +58,8 @@ void build_from_raw(const RawMesh& raw, int N, int nodeType, HostMesh& M);
 void build_from_flexi(int N, int nodeType, int nElems, int nSides, int nBCSides, const int* SideToElem, const int* ElemToSide,
                       const int* BC, int nBCs, const int* BoundaryType, int nRefStates, const double* RefStatePrim, const double* Mf,
                       const double* Mg, const double* Mh, const double* sJ, const double* NormVec, const double* TangVec1,
-                      const double* TangVec2, const double* SurfElem, HostMesh& M);
+                      const double* TangVec2, const double* SurfElem, int nMortars, const int* MortarType, const int* MortarInfo,
+                      HostMesh& M);
 // derived per-node quantities (time-step metrics, quadrature weights, instance volumes)
 void finish_mesh(HostMesh& M, double kappa, double Pr);
 

@@ -116,8 +116,10 @@ class Flexi:
             self._check(rc, "fg_build_mesh")
         self._sizes()
 
-    def set_mesh(self, side_to_elem, elem_to_side, bc, boundary_type, ref_state_prim, Mf, Mg, Mh, sJ, NormVec, TangVec1, TangVec2, SurfElem):
-        """Drop-in path: FLEXI's own processed mesh arrays (MOD_Mesh_Vars)."""
+    def set_mesh(self, side_to_elem, elem_to_side, bc, boundary_type, ref_state_prim, Mf, Mg, Mh, sJ, NormVec, TangVec1, TangVec2, SurfElem,
+                 mortar_type=None, mortar_info=None, host_only_ok=False):
+        """Drop-in path: FLEXI's own processed mesh arrays (MOD_Mesh_Vars); with mortar interfaces also
+        MortarType (nSides, 2) and MortarInfo (nMortars, 4, 2) (fg_set_mesh_mortar)."""
         a = [np.ascontiguousarray(x) for x in (Mf, Mg, Mh, sJ, NormVec, TangVec1, TangVec2, SurfElem)]
         s2e = np.ascontiguousarray(side_to_elem, np.int32)
         e2s = np.ascontiguousarray(elem_to_side, np.int32)
@@ -126,9 +128,15 @@ class Flexi:
         rs = np.ascontiguousarray(ref_state_prim, np.float64).reshape(-1)
         n_elems = a[3].shape[0]
         n_sides = s2e.shape[0]
-        self._check(self.L.fg_set_mesh(self.h, n_elems, n_sides, len(bcv), _p(s2e), _p(e2s), _p(bcv) if len(bcv) else None,
+        mt = None if mortar_type is None else np.ascontiguousarray(mortar_type, np.int32)
+        mi = None if mortar_info is None else np.ascontiguousarray(mortar_info, np.int32).reshape(-1, 4, 2)
+        n_mortars = 0 if mi is None else len(mi)
+        self._mesh_keep = (a, s2e, e2s, bcv, bt, rs, mt, mi)
+        rc = self.L.fg_set_mesh_mortar(self.h, n_elems, n_sides, len(bcv), _p(s2e), _p(e2s), _p(bcv) if len(bcv) else None,
                                        len(bt) // 2, _p(bt) if len(bt) else None, len(rs) // 6, _p(rs) if len(rs) else None,
-                                       *[_p(x) for x in a]), "fg_set_mesh")
+                                       *[_p(x) for x in a], n_mortars, _p(mt) if n_mortars else None, _p(mi) if n_mortars else None)
+        if not (host_only_ok and rc == 3):  # FG_ERR_CUDA after a complete host-side set-up
+            self._check(rc, "fg_set_mesh")
         self._sizes()
 
     def set_face_metrics(self, Ja_Face, Ja_slave):

@@ -115,6 +115,16 @@ int fg_set_mesh(fg_handle* h, int nElems, int nSides, int nBCSides, const int* S
                 const double* Metrics_gTilde, const double* Metrics_hTilde, const double* sJ, const double* NormVec,
                 const double* TangVec1, const double* TangVec2, const double* SurfElem);
 
+/* fg_set_mesh for meshes with mortar interfaces: also MortarType(2,nSides) and MortarInfo(2,4,nMortars)
+ * (mesh_vars.f90:158-159, nMortars = nMortarInnerSides; single rank, no MPI mortars). The small sides'
+ * metrics are FLEXI's own (mortar_metrics.f90). The library renumbers the sides (conforming, then small,
+ * then big: fg_get_side_to_elem reports its order); fg_set_face_metrics still takes FLEXI's numbering. */
+int fg_set_mesh_mortar(fg_handle* h, int nElems, int nSides, int nBCSides, const int* SideToElem, const int* ElemToSide, const int* BC,
+                       int nBCs, const int* BoundaryType, int nRefStates, const double* RefStatePrim, const double* Metrics_fTilde,
+                       const double* Metrics_gTilde, const double* Metrics_hTilde, const double* sJ, const double* NormVec,
+                       const double* TangVec1, const double* TangVec2, const double* SurfElem, int nMortars, const int* MortarType,
+                       const int* MortarInfo);
+
 /* Face metrics of the split form on Gauss nodes, FLEXI's Ja_Face(3,3,0:N,0:N,nSides) and
  * Ja_slave(3,3,0:N,0:N,nSides) (MOD_Mesh_Vars, filled by metrics.f90:CalcSurfMetrics; used by
  * surfint.t90:90-140). Optional after fg_set_mesh, which otherwise evaluates the normal-direction volume

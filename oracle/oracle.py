@@ -228,7 +228,7 @@ class Oracle:
         return float(out[0])
 
     def mesh_iarray(self, name):
-        w = {"SideToElem": 0, "ElemToSide": 1, "BC": 2}[name]
+        w = {"SideToElem": 0, "ElemToSide": 1, "BC": 2, "MortarType": 3, "MortarInfo": 4}[name]
         cnt = lib().orc_mesh_iarray(self.h, w, None)
         out = np.empty(max(cnt, 1), np.int32)
         lib().orc_mesh_iarray(self.h, w, _p(out))
@@ -237,6 +237,10 @@ class Oracle:
             return out.reshape(self.n_sides, 5)
         if name == "ElemToSide":
             return out.reshape(self.n_elems, 6, 2)
+        if name == "MortarType":
+            return out.reshape(self.n_sides, 2)
+        if name == "MortarInfo":
+            return out.reshape(-1, 4, 2)
         return out
 
     def gradients(self):

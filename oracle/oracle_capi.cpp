@@ -216,7 +216,11 @@ long long orc_mesh_array(void* hp, int which, double* out) {
 // which: 0 SideToElem(5,nSides), 1 ElemToSide(2,6,nElems), 2 BC(nBCSides)
 long long orc_mesh_iarray(void* hp, int which, int* out) {
   auto& M = ((OrcHandle*)hp)->dg.M;
-  const std::vector<int>* a = which == 0 ? &M.SideToElem : (which == 1 ? &M.ElemToSide : &M.BC);
+  const std::vector<int>* a = which == 0 ? &M.SideToElem
+                              : which == 1 ? &M.ElemToSide
+                              : which == 2 ? &M.BC
+                              : which == 3 ? &M.MortarType
+                                           : &M.MortarInfo;
   if (out) std::memcpy(out, a->data(), a->size() * 4);
   return (long long)a->size();
 }

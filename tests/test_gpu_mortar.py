@@ -132,3 +132,22 @@ def test_adjoint_refuses_mortars():
     with pytest.raises(FlexiError, match="mortar"):
         f.vjp_time_derivative(np.ones_like(f.U))
     f.close()
+
+
+@pytest.mark.parametrize("name", ["CART_HEX_PERIODIC_MORTAR_002_mesh.h5", "cartbox3D_mortar_mesh.h5"])
+def test_drop_in_mortar_mesh(name):
+    """fg_set_mesh_mortar: FLEXI's own mesh arrays (SideToElem, ElemToSide, metrics, MortarType, MortarInfo,
+    the small sides' metrics) as the oracle builds them; Ut at 1e-12 of the oracle."""
+    c = product_cfg(N=4, NodeType="gauss", SplitDG="weak", Riemann="roeentropyfix", **COMMON)
+    m = _mesh(name)
+    o = orc.Oracle(oracle_cfg(c), m)
+    f = Flexi(c)
+    f.set_mesh(o.mesh_iarray("SideToElem"), o.mesh_iarray("ElemToSide"), o.mesh_iarray("BC"), m.boundary_type, m.ref_state_prim,
+               *(o.mesh_array(k) for k in ("Mf", "Mg", "Mh", "sJ", "NormVec", "TangVec1", "TangVec2", "SurfElem")),
+               mortar_type=o.mesh_iarray("MortarType"), mortar_info=o.mesh_iarray("MortarInfo"))
+    U0 = _state(o.mesh_array("Elem_xGP"), seed=8)
+    f.U = U0
+    o.set_state(U0)
+    err = rel_err(f.DGTimeDerivative_weakForm(0.0), o.time_derivative(0.0))
+    f.close()
+    assert err <= 1e-12, err

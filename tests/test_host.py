@@ -153,3 +153,30 @@ def test_mortar_mesh_errors(lib):
     with pytest.raises(FlexiError, match="Gauss-Lobatto"):
         g.build_mesh(m, host_only_ok=True)
     g.close()
+
+
+def test_drop_in_mortar_mesh_tables(lib):
+    """fg_set_mesh_mortar takes FLEXI's arrays (here the oracle's): the library's side tables equal those it
+    builds itself from the mesh file (matched by slave / master element side), with the same geometry."""
+    m = fmesh.read_hopr(os.path.join(HOPR, "CART_HEX_PERIODIC_MORTAR_002_mesh.h5"))
+    o = orc.Oracle(_oracle_cfg(3, 1), m)
+    arrays = [o.mesh_array(k) for k in ("Mf", "Mg", "Mh", "sJ", "NormVec", "TangVec1", "TangVec2", "SurfElem")]
+    f = Flexi(make_config(N=3, NodeType=1, SplitDG=-1))
+    f.set_mesh(o.mesh_iarray("SideToElem"), o.mesh_iarray("ElemToSide"), o.mesh_iarray("BC"), m.boundary_type, m.ref_state_prim,
+               *arrays, mortar_type=o.mesh_iarray("MortarType"), mortar_info=o.mesh_iarray("MortarInfo"), host_only_ok=True)
+    g = Flexi(make_config(N=3, NodeType=1, SplitDG=-1))
+    g.build_mesh(m, host_only_ok=True)
+    fs, gs = f.side_to_elem(), g.side_to_elem()
+    kg = {k: i for i, k in enumerate(_side_keys(gs))}
+    perm = np.array([kg[k] for k in _side_keys(fs)])
+    assert np.array_equal(fs, gs[perm])
+    for name in ("NormVec", "SurfElem"):
+        a, b = f.mesh_array(name), g.mesh_array(name)[perm]
+        assert np.abs(a - b).max() <= 1e-13 * max(1.0, np.abs(b).max()), name
+    bad = o.mesh_iarray("MortarInfo").copy()
+    bad[0, 0, 0] = bad[1, 0, 0]
+    with pytest.raises(FlexiError, match="MortarInfo"):
+        f.set_mesh(o.mesh_iarray("SideToElem"), o.mesh_iarray("ElemToSide"), o.mesh_iarray("BC"), m.boundary_type, m.ref_state_prim,
+                   *arrays, mortar_type=o.mesh_iarray("MortarType"), mortar_info=bad, host_only_ok=True)
+    f.close()
+    g.close()
