@@ -13,7 +13,8 @@ class FgConfig(ctypes.Structure):
                 ("SplitDG", ctypes.c_int), ("etaBR2", ctypes.c_double), ("etaBR2_wall", ctypes.c_double), ("kappa", ctypes.c_double),
                 ("R", ctypes.c_double), ("Pr", ctypes.c_double), ("mu0", ctypes.c_double), ("CFLScale", ctypes.c_double),
                 ("DFLScale", ctypes.c_double), ("doTCSource", ctypes.c_int), ("dpdx", ctypes.c_double), ("TimeDiscMethod", ctypes.c_int),
-                ("OverintegrationType", ctypes.c_int), ("NUnder", ctypes.c_int)]
+                ("OverintegrationType", ctypes.c_int), ("NUnder", ctypes.c_int), ("IniExactFunc", ctypes.c_int),
+                ("AdvVel", ctypes.c_double * 3), ("IniFrequency", ctypes.c_double), ("IniAmplitude", ctypes.c_double)]
 
 
 EXPORTS = ["fg_config_default", "fg_config_from_ini", "fg_create", "fg_destroy", "fg_last_error", "fg_build_mesh", "fg_build_mesh_mortar", "fg_set_mesh", "fg_set_mesh_mortar", "fg_set_face_metrics", "fg_overintegrate_state",

@@ -71,6 +71,13 @@ struct Dev {
   double* dpdx;    // [nInst] (0 when no body force)
   double* muScale; // [nElems] viscosity multiplier of each element (null: 1)
   double* forceField;  // [e][n3] additional x-momentum body force per node, energy source F * bulkVel (null: none)
+  // source of an exact function (exactfunc.f90:CalcSource; null: none): srcPar = (omega, a, tmp(1:6)) of
+  // IniExactFunc 4, elemX [e][3][n3] the solution points, tStage [nInst] the time of the current RK stage,
+  // tStep [nInst] the time at the start of the current step
+  const double* srcPar;
+  const double* elemX;
+  double* tStage;
+  double* tStep;
   double* scratch;  // element kernels whose per-element arrays exceed shared memory (lines of 9..12 nodes):
                     // [block][scratchStride] (null otherwise)
   long long scratchStride;

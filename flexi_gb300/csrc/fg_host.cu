@@ -70,7 +70,15 @@ __global__ void k_finish_step(Dev d, const double* bulkPart, const int* instStar
   if (!checkDt) return;
   const double dt = d.dt[i];
   if (!(dt > 0.) || dt > 1e300) set_error(d.err, 2);
-  if (tInst) tInst[i] += dt;
+  if (tInst) {
+    if (d.tStep) d.tStep[i] = tInst[i];
+    tInst[i] += dt;
+  }
+}
+// time of RK stage c of the current step, t_n + c dt, for the time-dependent source
+__global__ void k_stage_time(Dev d, double c) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < d.nInst) d.tStage[i] = fma(c, d.dt[i], d.tStep[i]);
 }
 // LSERK adjoint stage update: G = alpha G + beta U (cotangents of the RK register and of the state);
 // alpha = 0 starts G afresh without reading it
@@ -413,6 +421,8 @@ void init_basis(fg_handle* h) {
 int upload_mesh(fg_handle* h) {
   fgh::HostMesh& M = h->M;
   fgh::finish_mesh(M, h->cfg.kappa, h->cfg.Pr);
+  if (h->cfg.IniExactFunc == 4 && M.elemX.empty())
+    return fail(h, FG_ERR_CONFIG, "the source of exact function 4 needs the solution coordinates (fg_build_mesh)");
   if (M.nMortars > 0) {
     if (h->cfg.Lifting != 1) return fail(h, FG_ERR_CONFIG, "mortar interfaces need BR1 lifting");
     if (h->cfg.SplitDG >= 0 && h->cfg.NodeType == FG_NODE_GAUSS)
@@ -511,6 +521,21 @@ int upload_mesh(fg_handle* h) {
     // per-CTA slices of the element kernels whose arrays exceed shared memory (one element per CTA here)
     d.scratchStride = h->K.scratchPerBlock;
     if ((r = dalloc(h, d.scratch, (size_t)nE * (size_t)d.scratchStride))) return r;
+  }
+  if (h->cfg.IniExactFunc == 4) {
+    // exactfunc.f90:CalcSource CASE(4) (3D) coefficients
+    const fg_config& c = h->cfg;
+    const double om = M_PI * c.IniFrequency, A = c.IniAmplitude, a = c.AdvVel[0] * 2. * M_PI, k = c.kappa, km1 = c.kappa - 1.;
+    std::vector<double> P = {om, a, A * (-a + 3. * om), A * (-a + 0.5 * om * (1. + k * 5.)), A * (A * om * km1),
+                             A * (0.5 * ((9. + k * 15.) * om - 8. * a)), A * (A * (3. * om * k - a)), A * (3. * c.mu0 * k * om * om / c.Pr)};
+    double* dP = nullptr;
+    if ((r = upload(h, dP, P))) return r;
+    d.srcPar = dP;
+    double* dX = nullptr;
+    if ((r = upload(h, dX, M.elemX))) return r;
+    d.elemX = dX;
+    if ((r = upload(h, d.tStage, std::vector<double>(M.nInst, 0.)))) return r;
+    if ((r = upload(h, d.tStep, std::vector<double>(M.nInst, 0.)))) return r;
   }
   if ((r = upload(h, h->dMetAdv, M.metAdv))) return r;
   if ((r = upload(h, h->dMetVisc, M.metVisc))) return r;
@@ -659,7 +684,13 @@ void launch_step_setup(fg_handle* h, int mode, double fixedDt, bool advanceTime)
   h->launches += 1;
 }
 void launch_lserk(fg_handle* h) {
-  for (int s = 1; s <= 5; ++s) launch_rhs(h, s == 1 ? 1 : 2, s == 1 ? 0. : h->RKA[s], h->RKb[s]);
+  for (int s = 1; s <= 5; ++s) {
+    if (h->d.srcPar) {
+      k_stage_time<<<(h->d.nInst + 127) / 128, 128, 0, h->st>>>(h->d, h->RKc[s]);
+      h->launches += 1;
+    }
+    launch_rhs(h, s == 1 ? 1 : 2, s == 1 ? 0. : h->RKA[s], h->RKb[s]);
+  }
 }
 int check_err(fg_handle* h) {
   int e = 0;
@@ -702,6 +733,7 @@ const char* adjoint_unsupported(const fg_config& c) {
 int ensure_adjoint(fg_handle* h) {
   if (h->haveAdj) return 0;
   if (h->d.nMortars > 0) return fail(h, FG_ERR_CONFIG, "the adjoint does not support mortar interfaces");
+  if (h->d.srcPar) return fail(h, FG_ERR_CONFIG, "the adjoint does not support exact-function sources");
   const int n = h->M.n, n2 = n * n, n3 = n2 * n, nE = h->M.nElems, nS = h->M.nSides;
   AdjDev& a = h->a;
   double* W = nullptr;
@@ -770,6 +802,7 @@ int fg_config_default(fg_config* c) {
   c->etaBR2 = 2.; c->etaBR2_wall = -1.; c->kappa = 1.4; c->R = 287.058; c->Pr = 0.72; c->mu0 = 0.;
   c->CFLScale = 0.9; c->DFLScale = 0.9; c->doTCSource = 0; c->dpdx = -1.; c->TimeDiscMethod = 0;
   c->OverintegrationType = 0; c->NUnder = -1;
+  c->IniExactFunc = 0; c->AdvVel[0] = c->AdvVel[1] = c->AdvVel[2] = 0.; c->IniFrequency = 1.; c->IniAmplitude = 0.1;
   return FG_OK;
 }
 
@@ -818,6 +851,16 @@ int fg_config_from_ini(const char* text, fg_config* c) {
         else if (lv == "conscutoff") c->OverintegrationType = 2;
         else c->OverintegrationType = std::stoi(val);
       } else if (key == "nunder") c->NUnder = std::stoi(val);
+      else if (key == "iniexactfunc") c->IniExactFunc = std::stoi(val);
+      else if (key == "inifrequency") c->IniFrequency = std::stod(val);
+      else if (key == "iniamplitude") c->IniAmplitude = std::stod(val);
+      else if (key == "advvel") {  // (/a,b,c/)
+        std::string v = val;
+        for (char& ch : v) if (ch == '(' || ch == ')' || ch == '/' || ch == ',') ch = ' ';
+        std::istringstream vs(v);
+        for (int d = 0; d < 3; ++d)
+          if (!(vs >> c->AdvVel[d])) return FG_ERR_CONFIG;
+      }
     } catch (...) {
       return FG_ERR_CONFIG;
     }
@@ -1033,9 +1076,12 @@ int fg_state_device_ptr(fg_handle* h, double** p) {
 }
 
 int fg_time_derivative(fg_handle* h, double t, double* Ut) {
-  (void)t;  // no time-dependent source or boundary condition on this path
   if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
   h->launches = 0;
+  if (h->d.srcPar) {  // the source is evaluated at t
+    k_fill<<<(h->d.nInst + 127) / 128, 128, 0, h->st>>>(h->d.tStage, t, h->d.nInst);
+    h->launches += 1;
+  }
   launch_step_setup(h, 2, 0., false);
   launch_rhs(h, 0, 0., 0.);
   CUDA_TRY(cudaGetLastError());
@@ -1572,6 +1618,10 @@ int fg_timestep_lserkw2(fg_handle* h, double* t, double dt) {
   if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
   h->launches = 0;
   CUDA_TRY(cudaMemsetAsync(h->d.err, 0, sizeof(int), h->st));
+  if (h->d.srcPar) {  // stage times from the caller's t
+    k_fill<<<(h->d.nInst + 127) / 128, 128, 0, h->st>>>(h->d.tStep, t ? *t : 0., h->d.nInst);
+    h->launches += 1;
+  }
   launch_step_setup(h, 1, dt, false);
   launch_lserk(h);
   CUDA_TRY(cudaGetLastError());

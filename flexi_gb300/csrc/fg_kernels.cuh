@@ -738,11 +738,29 @@ __device__ __forceinline__ void finish_node(const Dev& d, const SBasis<n>& Bs, c
   const double sj = d.sJ[(size_t)e * n3 + x];
   const int inst = d.elemInst[e];
   const double dpdx = d.dpdx[inst];
+  double src[5] = {0., 0., 0., 0., 0.};
+  const bool haveSrc = d.srcPar != nullptr;
+  if (haveSrc) {
+    // exactfunc.f90:CalcSource CASE(4): rho = m_i = 2 + A sin(omega sum(x) - a t), E = rho^2
+    const double* P = d.srcPar;
+    const double* X = d.elemX + (size_t)e * 3 * n3 + x;
+    const double ph = P[0] * (X[0] + X[n3] + X[2 * n3]) - P[1] * d.tStage[inst];
+    double sn, cs;
+    sincos(ph, &sn, &cs);
+    const double s2 = 2. * sn * cs;
+    src[0] = P[2] * cs;
+    src[1] = src[2] = src[3] = fma(P[3], cs, P[4] * s2);
+    src[4] = fma(P[5], cs, fma(P[6], s2, P[7] * sn));
+  }
   if (st.mode == 3) {
     // dg.f90:656-662: Ut = -Ut, sources in reference space (divided by sJ); the Jacobian follows the filter
 #pragma unroll
     for (int v = 0; v < 5; ++v) ut[v] = -ut[v];
     if (dpdx != 0.) { ut[1] -= dpdx / sj; ut[4] -= dpdx / sj * d.bulkVel[inst]; }
+    if (haveSrc) {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) ut[v] += src[v] / sj;
+    }
     if (d.forceField) {
       const double F = d.forceField[(size_t)e * n3 + x];
       ut[1] += F / sj;
@@ -758,6 +776,10 @@ __device__ __forceinline__ void finish_node(const Dev& d, const SBasis<n>& Bs, c
   if (dpdx != 0.) {  // channel testcase.f90:TestcaseSource, applied before ApplyJacobian
     ut[1] -= dpdx;
     ut[4] -= dpdx * d.bulkVel[inst];
+  }
+  if (haveSrc) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) ut[v] += src[v];
   }
   if (d.forceField) {  // additional per-node body force of the same form
     const double F = d.forceField[(size_t)e * n3 + x];

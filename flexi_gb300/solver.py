@@ -48,7 +48,8 @@ def make_config(**kw) -> _lib.FgConfig:
             v = {"none": 0, "cutoff": 1, "conscutoff": 2}[v.lower()]
         if not hasattr(c, k):
             raise KeyError(k)
-        setattr(c, k, type(getattr(c, k))(v))
+        t = type(getattr(c, k))
+        setattr(c, k, t(*v) if issubclass(t, ctypes.Array) else t(v))
     return c
 
 
@@ -62,7 +63,8 @@ def config_from_ini(text: str) -> _lib.FgConfig:
 
 
 def config_dict(c: _lib.FgConfig) -> dict:
-    return {name: getattr(c, name) for name, _ in _lib.FgConfig._fields_}
+    d = {name: getattr(c, name) for name, _ in _lib.FgConfig._fields_}
+    return {k: (tuple(v) if isinstance(v, ctypes.Array) else v) for k, v in d.items()}
 
 
 class Flexi:

@@ -68,6 +68,10 @@ typedef struct fg_config {
   int TimeDiscMethod;
   int OverintegrationType;  /* overintegration.f90: 0 none, 1 cut-off filter of J u_t, 2 conservative cut-off */
   int NUnder;               /* filter degree of OverintegrationType 1/2 (-1: N) */
+  int IniExactFunc;         /* exactfunc.f90: 4 (oblique sine wave) adds its source, CalcSource CASE(4); others: no source */
+  double AdvVel[3];         /* AdvVel of exact function 4 (its wave speed is 2 pi AdvVel(1)) */
+  double IniFrequency;      /* IniFrequency (default 1) */
+  double IniAmplitude;      /* IniAmplitude (default 0.1) */
 } fg_config;
 
 typedef struct fg_handle fg_handle;

@@ -19,7 +19,8 @@ def oracle_cfg(c):
                 weakLifting=d["doWeakLifting"], consLifting=d["doConservativeLifting"], splitDG=d["SplitDG"], etaBR2=d["etaBR2"],
                 etaBR2_wall=d["etaBR2_wall"], kappa=d["kappa"], R=d["R"], Pr=d["Pr"], mu0=d["mu0"], CFLScale=d["CFLScale"],
                 DFLScale=d["DFLScale"], doTCSource=d["doTCSource"], dpdx=d["dpdx"], overintType=d["OverintegrationType"],
-                NUnder=d["NUnder"])
+                NUnder=d["NUnder"], iniExactFunc=d["IniExactFunc"], advVel=d["AdvVel"], iniFrequency=d["IniFrequency"],
+                iniAmplitude=d["IniAmplitude"])
 
 
 def perturb_state(U, seed=0, amp=0.05):

@@ -180,3 +180,20 @@ def test_drop_in_mortar_mesh_tables(lib):
                    *arrays, mortar_type=o.mesh_iarray("MortarType"), mortar_info=bad, host_only_ok=True)
     f.close()
     g.close()
+
+
+def test_ini_exact_function_keys(lib):
+    # keys as written in regressioncheck/checks/convtest/h_3D_mortar/parameter.ini
+    text = """
+    IniExactFunc     = 4
+    AdvVel           = (/0.3,0.2,0.1/)
+    IniFrequency = 2.0
+    IniAmplitude = 0.05
+    """
+    d = config_dict(config_from_ini(text))
+    assert d["IniExactFunc"] == 4 and d["AdvVel"] == (0.3, 0.2, 0.1) and d["IniFrequency"] == 2.0 and d["IniAmplitude"] == 0.05
+    d0 = config_dict(make_config())
+    assert d0["IniExactFunc"] == 0 and d0["IniFrequency"] == 1.0 and d0["IniAmplitude"] == 0.1 and d0["AdvVel"] == (0.0, 0.0, 0.0)
+    assert config_dict(make_config(AdvVel=(1.0, 2.0, 3.0)))["AdvVel"] == (1.0, 2.0, 3.0)
+    with pytest.raises(FlexiError):
+        config_from_ini("AdvVel = (/0.3,0.2/)\n")
