@@ -424,7 +424,6 @@ int upload_mesh(fg_handle* h) {
   if (h->cfg.IniExactFunc == 4 && M.elemX.empty())
     return fail(h, FG_ERR_CONFIG, "the source of exact function 4 needs the solution coordinates (fg_build_mesh)");
   if (M.nMortars > 0) {
-    if (h->cfg.Lifting != 1) return fail(h, FG_ERR_CONFIG, "mortar interfaces need BR1 lifting");
     if (h->cfg.SplitDG >= 0 && h->cfg.NodeType == FG_NODE_GAUSS)
       return fail(h, FG_ERR_CONFIG, "mortar interfaces with the split form need Gauss-Lobatto nodes");
   }

@@ -173,8 +173,9 @@ __global__ void __launch_bounds__(Shape<n, E>::THREADS) k_prep(Dev d, Basis B) {
 }
 
 // ProlongToFaceLifting of the gradients in sG (+ BR2: eta * lifting contribution of this face,
-// lifting_br2.t90:Lifting_SurfInt_BR2) for the six faces of the CTA's elements
-template <int n, bool GL, int E = 0>
+// lifting_br2.t90:Lifting_SurfInt_BR2) for the six faces of the CTA's elements; MORTAR: sF holds the 12
+// products F_v n_c per face point (sN unused)
+template <int n, bool GL, int E = 0, bool MORTAR = false>
 __device__ __forceinline__ void lift_prolong_faces(const Dev& d, const Basis& B, const SBasis<n>& Bs, const double* sG, const double* sF,
                                                    const double* sN, const double* sJs, int e0, bool br2) {
   constexpr int n2 = n * n, n3 = n2 * n, EPB = Shape<n, E>::EPB, N = n - 1;
@@ -216,11 +217,16 @@ __device__ __forceinline__ void lift_prolong_faces(const Dev& d, const Basis& B,
       }
       const int o = (es * 6 + lsi) * n2 + a + n * b;
       const double ew = eta * wsum;
+      if constexpr (MORTAR) {
 #pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        const double f = sF[o * 4 + v] * ew;
+        for (int c = 0; c < 12; ++c) gf[c] = fma(sF[o * 12 + c], ew, gf[c]);
+      } else {
 #pragma unroll
-        for (int c = 0; c < 3; ++c) gf[4 * c + v] = fma(f, sN[o * 3 + c], gf[4 * c + v]);
+        for (int v = 0; v < 4; ++v) {
+          const double f = sF[o * 4 + v] * ew;
+#pragma unroll
+          for (int c = 0; c < 3; ++c) gf[4 * c + v] = fma(f, sN[o * 3 + c], gf[4 * c + v]);
+        }
       }
     }
     double* dst = (flip == 0 ? d.gradM : d.gradS) + (size_t)s * 12 * n2 + pq;
@@ -236,9 +242,10 @@ __device__ __forceinline__ void lift_prolong_faces(const Dev& d, const Basis& B,
 // them (Dev::metrJ), else forms the products itself. On Gauss-Lobatto nodes the surface part reaches
 // only the face nodes: it is added face-parallel, one direction (two opposite faces, disjoint node
 // sets) at a time, so that no warp runs it for interior nodes.
-// MORTAR (meshes with mortar interfaces, BR1): the surface flux is kept as the 12 products F_v n_c per face
+// MORTAR (meshes with mortar interfaces): the surface flux is kept as the 12 products F_v n_c per face
 // point, so that a big mortar side can take the projection of its small sides' products
-// (lifting_br1.t90: Flux_Mortar on gradUx/y/z_master), which k_mortar_pre leaves in Dev::mortarLift.
+// (lifting_br1.t90:106-109, lifting_br2.t90:103-106: Flux_Mortar of the lifting fluxes), which k_mortar_pre
+// leaves in Dev::mortarLift; with BR2 the face penalty uses the same products.
 // =====================================================================================================
 template <int n, bool GL, int E = 0, bool MORTAR = false>
 __global__ void __launch_bounds__(Shape<n, E>::THREADS, (n == 8 && GL ? 2 : 1)) k_lift(Dev d, Basis B) {
@@ -255,7 +262,7 @@ __global__ void __launch_bounds__(Shape<n, E>::THREADS, (n == 8 && GL ? 2 : 1)) 
   load_basis_smem<n>(B, sD);
   SBasis<n> Bs{sD};
   const int e0 = blockIdx.x * EPB;
-  const bool br2 = !MORTAR && B.lifting == 2;
+  const bool br2 = B.lifting == 2;
   for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
     const int es = t / n3, x = t - es * n3, e = e0 + es;
     if (e >= d.nElems) continue;
@@ -400,7 +407,7 @@ __global__ void __launch_bounds__(Shape<n, E>::THREADS, (n == 8 && GL ? 2 : 1)) 
   if constexpr (GL) {
     // BR2 prolongs the volume part, before the surface part is added
     if (br2) {
-      lift_prolong_faces<n, GL, E>(d, B, Bs, sG, sF, sN, sJs, e0, true);
+      lift_prolong_faces<n, GL, E, MORTAR>(d, B, Bs, sG, sF, sN, sJs, e0, true);
       __syncthreads();
     }
     // surface part (DoSurfIntLifting) on the face nodes l = 0 and l = N of one direction at a time
@@ -432,7 +439,7 @@ __global__ void __launch_bounds__(Shape<n, E>::THREADS, (n == 8 && GL ? 2 : 1)) 
       __syncthreads();
     }
     // BR1 prolongs the full gradient
-    if (!br2) lift_prolong_faces<n, GL, E>(d, B, Bs, sG, sF, sN, sJs, e0, false);
+    if (!br2) lift_prolong_faces<n, GL, E, MORTAR>(d, B, Bs, sG, sF, sN, sJs, e0, false);
     for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
       const int es = t / n3, x = t - es * n3, e = e0 + es;
       if (e >= d.nElems) continue;
@@ -440,7 +447,7 @@ __global__ void __launch_bounds__(Shape<n, E>::THREADS, (n == 8 && GL ? 2 : 1)) 
       for (int c = 0; c < 12; ++c) d.grad[((size_t)e * 12 + c) * n3 + x] = sG[(es * 12 + c) * n3 + x];
     }
   } else {
-    lift_prolong_faces<n, GL, E>(d, B, Bs, sG, sF, sN, sJs, e0, br2);
+    lift_prolong_faces<n, GL, E, MORTAR>(d, B, Bs, sG, sF, sN, sJs, e0, br2);
   }
 }
 
@@ -615,8 +622,8 @@ __device__ void mortar_project(const MortarDev& M, int type, int nv, const doubl
 
 // between k_prep and k_lift: the big side's conservative face state interpolated to its small sides' master
 // slots, turned into face primitives (dg.f90:372-416, U_Mortar before GetPrimitiveStateSurface), and the
-// small sides' BR1 lifting fluxes times normal (lifting_fillflux.t90) projected onto the big side
-// (lifting_br1.t90:106-109) for k_lift<MORTAR>.
+// small sides' lifting fluxes times normal (lifting_fillflux.t90) projected onto the big side
+// (lifting_br1.t90:106-109, lifting_br2.t90:103-106) for k_lift<MORTAR>.
 template <int n>
 __global__ void __launch_bounds__(256, 2) k_mortar_pre(Dev d, Basis B, MortarDev M) {
   constexpr int n2 = n * n;
@@ -668,7 +675,7 @@ __global__ void __launch_bounds__(256, 2) k_mortar_pre(Dev d, Basis B, MortarDev
 }
 
 // between k_flux and the volume kernel: the big side's face gradients interpolated to its small sides
-// (lifting_br1.t90:175-178), the small sides' numerical fluxes (fillflux.f90, master viscosity of the big
+// (lifting_br1.t90:175-178, lifting_br2.t90:176-181), the small sides' numerical fluxes (fillflux.f90, master viscosity of the big
 // element), and their projection onto the big side (dg.f90:625, Flux_Mortar)
 template <int n>
 __global__ void __launch_bounds__(256, 2) k_mortar_face(Dev d, Basis B, MortarDev M) {

@@ -322,7 +322,6 @@ struct DG {
     sideMasterElem.assign(nS, -1);
     for (int s = 0; s < nS; ++s) sideMasterElem[s] = s2e(0, s) - 1;
     if (M.nMortars == 0) return;
-    if (C.lifting == 2) throw std::runtime_error("mortar interfaces with BR2 lifting are not restated");
     if (C.splitDG != SPLIT_NONE && C.nodeType == NT_GAUSS) throw std::runtime_error("mortar interfaces with the split form on Gauss nodes are not restated");
     for (int s = 0; s < nS; ++s)
       if (M.MortarType[(size_t)s * 2] > 0) {
@@ -825,6 +824,10 @@ struct DG {
       u_mortar<NLIFT>(gradUy_m);
       u_mortar<NLIFT>(gradUz_m);
     } else {
+      // lifting_br2.t90:103-106: the small sides' fluxes projected onto the big mortar sides
+      flux_mortar<NLIFT>(FluxX);
+      flux_mortar<NLIFT>(FluxY);
+      flux_mortar<NLIFT>(FluxZ);
       apply_jacobian_lift();
       prolong_to_face<NLIFT>(gradUx, gradUx_m, gradUx_s);
       prolong_to_face<NLIFT>(gradUy, gradUy_m, gradUy_s);
@@ -832,6 +835,9 @@ struct DG {
       surf_int_br2(FluxX, gradUx, gradUx_m, gradUx_s);
       surf_int_br2(FluxY, gradUy, gradUy_m, gradUy_s);
       surf_int_br2(FluxZ, gradUz, gradUz_m, gradUz_s);
+      u_mortar<NLIFT>(gradUx_m);  // lifting_br2.t90:176-181
+      u_mortar<NLIFT>(gradUy_m);
+      u_mortar<NLIFT>(gradUz_m);
     }
   }
   void apply_jacobian_lift() {

@@ -145,10 +145,6 @@ def test_mortar_mesh_errors(lib):
     with pytest.raises(FlexiError, match="mortar"):
         f.build_mesh(dataclasses.replace(m, mortars=swapped), host_only_ok=True)
     f.close()
-    g = Flexi(make_config(N=3, NodeType=2, SplitDG="pi", Lifting="br2"))
-    with pytest.raises(FlexiError, match="BR1"):
-        g.build_mesh(m, host_only_ok=True)
-    g.close()
     g = Flexi(make_config(N=3, NodeType=1, SplitDG="pi"))
     with pytest.raises(FlexiError, match="Gauss-Lobatto"):
         g.build_mesh(m, host_only_ok=True)
