@@ -423,10 +423,6 @@ int upload_mesh(fg_handle* h) {
   fgh::finish_mesh(M, h->cfg.kappa, h->cfg.Pr);
   if (h->cfg.IniExactFunc == 4 && M.elemX.empty())
     return fail(h, FG_ERR_CONFIG, "the source of exact function 4 needs the solution coordinates (fg_build_mesh)");
-  if (M.nMortars > 0) {
-    if (h->cfg.SplitDG >= 0 && h->cfg.NodeType == FG_NODE_GAUSS)
-      return fail(h, FG_ERR_CONFIG, "mortar interfaces with the split form need Gauss-Lobatto nodes");
-  }
   h->haveHostMesh = true;
   free_device(h);
   if (!h->st) CUDA_TRY(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));

@@ -106,7 +106,7 @@ int fg_build_mesh(fg_handle* h, int nElems, int NGeo, const double* NodeCoords, 
  * MortarType 1: 1->4, 2: 1->2 in eta, 3: 1->2 in xi, then per small side: element, local side, 0) as
  * fg_hopr_read returns it -- the content of mesh_readin.f90:ReadMesh's MortarType/MortarInfo
  * (mesh_vars.f90:122-126), with the small-side metrics of mortar_metrics.f90:Mortar_CalcSurfMetrics and
- * the operators of mortar.f90:InitMortar. The split form needs Gauss-Lobatto nodes. */
+ * the operators of mortar.f90:InitMortar. */
 int fg_build_mesh_mortar(fg_handle* h, int nElems, int NGeo, const double* NodeCoords, const int* ElemNb, int nBCs, const int* BoundaryType,
                          int nRefStates, const double* RefStatePrim, const int* ElemInst, int nMortars, const int* Mortars);
 

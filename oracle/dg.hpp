@@ -322,7 +322,6 @@ struct DG {
     sideMasterElem.assign(nS, -1);
     for (int s = 0; s < nS; ++s) sideMasterElem[s] = s2e(0, s) - 1;
     if (M.nMortars == 0) return;
-    if (C.splitDG != SPLIT_NONE && C.nodeType == NT_GAUSS) throw std::runtime_error("mortar interfaces with the split form on Gauss nodes are not restated");
     for (int s = 0; s < nS; ++s)
       if (M.MortarType[(size_t)s * 2] > 0) {
         const int m = M.MortarType[(size_t)s * 2 + 1] - 1, nm = M.MortarType[(size_t)s * 2] == 1 ? 4 : 2;
@@ -1197,6 +1196,7 @@ struct DG {
         if (s2e(0, s) > 0) entropy_to_cons(&V_master[((size_t)s * ns2 + x) * 5], &U_master[((size_t)s * ns2 + x) * 5]);
         if (s2e(1, s) > 0) entropy_to_cons(&V_slave[((size_t)s * ns2 + x) * 5], &U_slave[((size_t)s * ns2 + x) * 5]);
       }
+      u_mortar<5>(U_master);  // dg.f90:379/415: U_MortarCons of the conservative face states
     }
     // equation.f90:GetPrimitiveStateSurface
     for (int s = 0; s < nS; ++s) for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {

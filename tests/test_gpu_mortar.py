@@ -3,8 +3,8 @@ against the oracle on the reference's own mortar meshes (tests/golden/hopr/).
 
 - Ut parity at 1e-12 (as test_gpu_parity.py) on the periodic p_3D_mortar mesh (mortar types 1, 2, 3),
   the flipped h_3D_mortar meshes (type 3) and the run_basic/freestream_3D mortar box (types 1, 2, its
-  Dirichlet sides replaced by adiabatic walls); Gauss and Gauss-Lobatto weak form, the Gauss-Lobatto split
-  form, BR1 and BR2 lifting, lines of up to 11 nodes (the kernels whose arrays live in global scratch).
+  Dirichlet sides replaced by adiabatic walls); Gauss and Gauss-Lobatto weak form, the Gauss-Lobatto and
+  the Gauss split form, BR1 and BR2 lifting, lines of up to 11 nodes (the kernels whose arrays live in global scratch).
 - the same on the library's synthetic mortar box (the mortar bench mesh) at 160 elements.
 - a constant state is preserved on the periodic mortar meshes and a fluid at rest on the walled box.
 - ten LSERK steps with the CFL time step agree with the oracle's (states at 1e-11), on the sine-wave
@@ -44,7 +44,8 @@ def _state(x, seed):
                                 dict(N=4, NodeType="gauss-lobatto", SplitDG="weak", Riemann="roe"),
                                 dict(N=5, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roeentropyfix"),
                                 dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="roe", Lifting="br2"),
-                                dict(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="hllc", Lifting="br2")])
+                                dict(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="hllc", Lifting="br2"),
+                                dict(N=5, NodeType="gauss", SplitDG="pi", Riemann="roeentropyfix")])
 def test_rhs_parity_mortar(name, kw):
     c = product_cfg(**kw, **COMMON)
     m = _mesh(name)

@@ -145,10 +145,6 @@ def test_mortar_mesh_errors(lib):
     with pytest.raises(FlexiError, match="mortar"):
         f.build_mesh(dataclasses.replace(m, mortars=swapped), host_only_ok=True)
     f.close()
-    g = Flexi(make_config(N=3, NodeType=1, SplitDG="pi"))
-    with pytest.raises(FlexiError, match="Gauss-Lobatto"):
-        g.build_mesh(m, host_only_ok=True)
-    g.close()
 
 
 def test_drop_in_mortar_mesh_tables(lib):

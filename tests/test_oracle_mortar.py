@@ -6,8 +6,8 @@ in the oracle, on the reference's own mortar meshes (tests/golden/hopr/) and its
   mesh asks for an L2 error below 1e-12.
 - periodic mortar meshes (convtest/p_3D_mortar types 1, 2, 3; convtest/h_3D_mortar type 3, flipped sides): a
   constant moving state is preserved and the volume integral of J Ut vanishes for a perturbed state
-  (the mortar projection conserves mass, momentum and energy), Gauss weak form and Gauss-Lobatto split form,
-  BR1 and BR2 lifting.
+  (the mortar projection conserves mass, momentum and energy), Gauss weak form, Gauss-Lobatto split form and
+  the Gauss split form (entropy-variable prolongation, split-Gauss surface integral), BR1 and BR2 lifting.
 - convtest/h_3D_mortar: N=3, IniExactFunc 4 with its source, AdvVel (0.3, 0.3, 0.3), Riemann 33, mu0 1e-3,
   CFLscale = DFLscale = 0.9, tend 1 with the Carpenter RK4-5 scheme on FLIPPED_001, _002, _004: L2 errors below 0.5
   and the mean order of convergence within 15% of N+1 = 4 for at least 80% of the variables
@@ -30,7 +30,8 @@ BASE = dict(riemannBC=-1, lifting=1, weakLifting=0, consLifting=0, etaBR2=2.0, e
 FORMS = {"gauss-weak": dict(nodeType=orc.NT_GAUSS, splitDG=-1, riemann=33),
          "gl-split-pi": dict(nodeType=orc.NT_GL, splitDG=2, riemann=33),
          "gauss-weak-br2": dict(nodeType=orc.NT_GAUSS, splitDG=-1, riemann=3, lifting=2),
-         "gl-split-br2": dict(nodeType=orc.NT_GL, splitDG=2, riemann=33, lifting=2)}
+         "gl-split-br2": dict(nodeType=orc.NT_GL, splitDG=2, riemann=33, lifting=2),
+         "gauss-split-pi": dict(nodeType=orc.NT_GAUSS, splitDG=4, riemann=33)}
 PERIODIC = ["CART_HEX_PERIODIC_MORTAR_002_mesh.h5", "CART_HEX_PERIODIC_MORTAR_FLIPPED_002_mesh.h5"]
 
 
