@@ -179,6 +179,29 @@ __host__ __device__ __forceinline__ void visc_flux_dir(double mu, double lam, do
   F[4] = -(a1 * u + a2 * v + a3 * w) - lam * qn;
 }
 
+// The same flux in three directions of one node: the stress tensor formed once (tau = txx, tyy, tzz, txy,
+// txz, tyz), then contracted with each direction vector.
+__host__ __device__ __forceinline__ void visc_tau(double mu, const double* g, double* tau) {
+  const double mdiv = (2.0 / 3.0) * (g[0] + g[5] + g[10]);
+  tau[0] = mu * (2.0 * g[0] - mdiv);
+  tau[1] = mu * (2.0 * g[5] - mdiv);
+  tau[2] = mu * (2.0 * g[10] - mdiv);
+  tau[3] = mu * (g[4] + g[1]);
+  tau[4] = mu * (g[8] + g[2]);
+  tau[5] = mu * (g[9] + g[6]);
+}
+__host__ __device__ __forceinline__ void visc_flux_tau(const double* tau, double lam, double u, double v, double w, const double* g,
+                                                       double m1, double m2, double m3, double* F) {
+  const double a1 = tau[0] * m1 + tau[3] * m2 + tau[4] * m3;
+  const double a2 = tau[3] * m1 + tau[1] * m2 + tau[5] * m3;
+  const double a3 = tau[4] * m1 + tau[5] * m2 + tau[2] * m3;
+  const double qn = g[3] * m1 + g[7] * m2 + g[11] * m3;
+  F[1] = -a1;
+  F[2] = -a2;
+  F[3] = -a3;
+  F[4] = -(a1 * u + a2 * v + a3 * w) - lam * qn;
+}
+
 // Rotated extended state (riemann.f90:Riemann_Point): rho, srho, E, p, vn, vt1, vt2.
 struct RotState {
   double rho, srho, E, p, v1, v2, v3;

@@ -914,13 +914,40 @@ __global__ void __launch_bounds__(Shape<n, E>::THREADS) k_vol_weak(Dev d, Basis 
   }
 }
 
+// two-point volume flux of a node pair in contravariant form, without its constant factor (in the scaled
+// DVolSurf): PI (splitflux.f90:SplitVolumeFluxPI): A = rho_s q_s; A u_s + 4 p_s m_s; A H_s, with the node
+// values rho, u, v, w, 4p-term p, H-term h; SD (SplitVolumeFluxSD): m_s . (F(a) + F(b)), p and rho E + p.
+// ms = metric vector sum of the pair.
+__device__ __forceinline__ void split_pair_flux(bool pi, double ra, double ua, double va, double wa, double pa, double ha, double rb,
+                                                double ub, double vb, double wb, double pb, double hb, double ms0, double ms1,
+                                                double ms2, double* G) {
+  if (pi) {
+    const double rs = ra + rb, us = ua + ub, vs = va + vb, ws = wa + wb, ps4 = pa + pb, hs = ha + hb;
+    const double qs = us * ms0 + vs * ms1 + ws * ms2;
+    const double A = rs * qs;
+    G[0] = A;
+    G[1] = fma(A, us, ps4 * ms0);
+    G[2] = fma(A, vs, ps4 * ms1);
+    G[3] = fma(A, ws, ps4 * ms2);
+    G[4] = A * hs;
+  } else {
+    const double qa = ua * ms0 + va * ms1 + wa * ms2, qb = ub * ms0 + vb * ms1 + wb * ms2;
+    const double mqa = ra * qa, mqb = rb * qb;
+    G[0] = mqa + mqb;
+    G[1] = fma(mqa, ua, mqb * ub) + (pa + pb) * ms0;
+    G[2] = fma(mqa, va, mqb * vb) + (pa + pb) * ms1;
+    G[3] = fma(mqa, wa, mqb * wb) + (pa + pb) * ms2;
+    G[4] = fma(ha, qa, hb * qb);
+  }
+}
+
 // =====================================================================================================
 // k_vol_split: volint.f90:VolInt_splitForm with SplitVolumeFluxPI / SD (Gauss-Lobatto nodes, n nodes
 // per line handled by an n-lane segment of a warp), viscous part in weak form, surface integral,
 // Jacobian, LSERK update. Each two-point flux of a line is evaluated once: lane a evaluates the pair
 // (a, a+dd mod n) for dd = 1..n/2-1, applies its own coefficient, and hands the unscaled flux to lane
 // a+dd with a warp shuffle, which applies its coefficient with one FMA per component; the pairs at
-// distance n/2 are evaluated by both lanes. The coefficients DVolSurf(l,i) are pre-scaled in shared
+// distance n/2 follow in a pass of their own, one thread per pair (half the warps). The coefficients DVolSurf(l,i) are pre-scaled in shared
 // memory by the split flux's constant factors (exact: powers of two).
 // Shared memory: one region holds the split-flux inputs (rho, u, v, w, p-term, H-term and the metrics)
 // and afterwards the transformed viscous fluxes, so that two CTAs of 8^3 nodes fit on one SM.
@@ -992,38 +1019,19 @@ __global__ void __launch_bounds__(Shape<n>::THREADS, (n == 8 ? 2 : 1)) k_vol_spl
 #pragma unroll
       for (int v = 0; v < 5; ++v) acc[v] = (dir == 0) ? 0. : sA[(es * 5 + v) * n3 + xa];
 #pragma unroll
-      for (int dd = 1; dd <= n / 2; ++dd) {
+      for (int dd = 1; dd < n / 2; ++dd) {
         const int bI = (a + dd) & (n - 1);
         const int xb = xline + bI * stride;
         const double rb = Q[xb], ub = Q[n3 + xb], vb = Q[2 * n3 + xb], wb = Q[3 * n3 + xb], pb = Q[4 * n3 + xb], hb = Q[5 * n3 + xb];
         const double ms0 = ma0 + Mm[xb], ms1 = ma1 + Mm[n3 + xb], ms2 = ma2 + Mm[2 * n3 + xb];
         double G[5];
-        if (pi) {
-          // SplitVolumeFluxPI in contravariant form (factors in sC): A = rho_s q_s; A u_s + 4 p_s m_s; A H_s
-          const double rs = ra + rb, us = ua + ub, vs = va + vb, ws = wa + wb, ps4 = pa + pb, hs = ha + hb;
-          const double qs = us * ms0 + vs * ms1 + ws * ms2;
-          const double A = rs * qs;
-          G[0] = A;
-          G[1] = fma(A, us, ps4 * ms0);
-          G[2] = fma(A, vs, ps4 * ms1);
-          G[3] = fma(A, ws, ps4 * ms2);
-          G[4] = A * hs;
-        } else {
-          // SplitVolumeFluxSD: m_s . (F(a) + F(b)) (factor 1/2 in sC); Q holds p and rho*E+p
-          const double qa = ua * ms0 + va * ms1 + wa * ms2, qb = ub * ms0 + vb * ms1 + wb * ms2;
-          const double mqa = ra * qa, mqb = rb * qb;
-          G[0] = mqa + mqb;
-          G[1] = fma(mqa, ua, mqb * ub) + (pa + pb) * ms0;
-          G[2] = fma(mqa, va, mqb * vb) + (pa + pb) * ms1;
-          G[3] = fma(mqa, wa, mqb * wb) + (pa + pb) * ms2;
-          G[4] = fma(ha, qa, hb * qb);
-        }
+        split_pair_flux(pi, ra, ua, va, wa, pa, ha, rb, ub, vb, wb, pb, hb, ms0, ms1, ms2, G);
         // contribution to node i from its partner l: DVolSurf(l, i)
         const double o0 = sC[bI * n + a], o1 = sC[n2 + bI * n + a];
         acc[0] = fma(o0, G[0], acc[0]);
 #pragma unroll
         for (int v = 1; v < 5; ++v) acc[v] = fma(o1, G[v], acc[v]);
-        if (dd < n / 2) {
+        {
           // receive the flux of the pair (a-dd, a) from lane a-dd
           const int aS = (a - dd) & (n - 1);
           const int src = segBase | aS;
@@ -1044,6 +1052,38 @@ __global__ void __launch_bounds__(Shape<n>::THREADS, (n == 8 ? 2 : 1)) k_vol_spl
     }
     __syncthreads();
   }
+  // the pairs at distance n/2, (a, a+n/2) with a < n/2: each evaluated once, by one thread that adds it to
+  // both nodes; one direction at a time (every node is in exactly one such pair per direction)
+  {
+    constexpr int HP = n / 2, NPAIR = n2 * HP;
+#pragma unroll 1
+    for (int dir = 0; dir < 3; ++dir) {
+      for (int t = threadIdx.x; t < EPB * NPAIR; t += blockDim.x) {
+        const int es = t / NPAIR, r = t - es * NPAIR;
+        if (e0 + es >= d.nElems) continue;
+        const int a = r % HP, c1 = (r / HP) % n, c2 = r / (HP * n);
+        const int stride = dir == 0 ? 1 : (dir == 1 ? n : n2);
+        const int xline = dir == 0 ? n * (c1 + n * c2) : (dir == 1 ? c1 + n2 * c2 : c1 + n * c2);
+        const int xa = xline + a * stride, xb = xa + HP * stride, b = a + HP;
+        const double* Q = sR + es * 15 * n3;
+        const double* Mm = Q + (6 + 3 * dir) * n3;
+        double G[5];
+        split_pair_flux(pi, Q[xa], Q[n3 + xa], Q[2 * n3 + xa], Q[3 * n3 + xa], Q[4 * n3 + xa], Q[5 * n3 + xa], Q[xb], Q[n3 + xb],
+                        Q[2 * n3 + xb], Q[3 * n3 + xb], Q[4 * n3 + xb], Q[5 * n3 + xb], Mm[xa] + Mm[xb], Mm[n3 + xa] + Mm[n3 + xb],
+                        Mm[2 * n3 + xa] + Mm[2 * n3 + xb], G);
+        double* A = sA + es * 5 * n3;
+        // node a from partner b: DVolSurf(b, a); node b from partner a: DVolSurf(a, b)
+        A[xa] = fma(sC[b * n + a], G[0], A[xa]);
+        A[xb] = fma(sC[a * n + b], G[0], A[xb]);
+#pragma unroll
+        for (int v = 1; v < 5; ++v) {
+          A[v * n3 + xa] = fma(sC[n2 + b * n + a], G[v], A[v * n3 + xa]);
+          A[v * n3 + xb] = fma(sC[n2 + a * n + b], G[v], A[v * n3 + xb]);
+        }
+      }
+      __syncthreads();
+    }
+  }
   // viscous fluxes (weak form): transformed fluxes of this node from the metrics still in sR, written
   // over sR once every thread has finished reading it (one node per thread: EPB * n3 == THREADS)
   static_assert(EPB * n3 == S::THREADS, "one node per thread");
@@ -1061,10 +1101,12 @@ __global__ void __launch_bounds__(Shape<n>::THREADS, (n == 8 ? 2 : 1)) k_vol_spl
       for (int c = 0; c < 12; ++c) g[c] = d.grad[((size_t)e * 12 + c) * n3 + x];
       const double mu = elem_mu(d, e);
       const double lam = mu * B.lambdaFac;
+      double tau[6];
+      visc_tau(mu, g, tau);
 #pragma unroll
       for (int dd = 0; dd < 3; ++dd) {
         double F[5];
-        visc_flux_dir(mu, lam, vx, vy, vz, g, m[3 * dd], m[3 * dd + 1], m[3 * dd + 2], F);
+        visc_flux_tau(tau, lam, vx, vy, vz, g, m[3 * dd], m[3 * dd + 1], m[3 * dd + 2], F);
 #pragma unroll
         for (int v = 0; v < 4; ++v) Fv[4 * dd + v] = F[1 + v];
       }
@@ -1322,10 +1364,12 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
       for (int c = 0; c < 12; ++c) g[c] = d.grad[((size_t)e * 12 + c) * n3 + x];
       const double mu = elem_mu(d, e);
       const double lam = mu * B.lambdaFac;
+      double tau[6];
+      visc_tau(mu, g, tau);
 #pragma unroll
       for (int dd = 0; dd < 3; ++dd) {
         double F[5];
-        visc_flux_dir(mu, lam, vx, vy, vz, g, m[3 * dd], m[3 * dd + 1], m[3 * dd + 2], F);
+        visc_flux_tau(tau, lam, vx, vy, vz, g, m[3 * dd], m[3 * dd + 1], m[3 * dd + 2], F);
 #pragma unroll
         for (int v = 0; v < 4; ++v) Fv[4 * dd + v] = F[1 + v];
       }
