@@ -35,8 +35,8 @@ def _mesh(name):
     return m0
 
 
-def _state(x, seed):
-    return perturb_state(testcases.sine_wave_state(x, 0.0, (0.3, 0.3, 0.3)), seed=seed, amp=0.1)
+def _state(x, seed, amp=0.1):
+    return perturb_state(testcases.sine_wave_state(x, 0.0, (0.3, 0.3, 0.3)), seed=seed, amp=amp)
 
 
 @pytest.mark.parametrize("name", MESHES)
@@ -51,7 +51,9 @@ def test_rhs_parity_mortar(name, kw):
     m = _mesh(name)
     f = Flexi(c, m)
     o = orc.Oracle(oracle_cfg(c), m)
-    U0 = _state(f.elem_xgp(), seed=5)
+    # 5 % noise: with 10 % the Gauss split form's face entropy variable -rho/p, extrapolated from noisy nodes
+    # at N=5, changes sign on FLIPPED_004 and EntropyToCons (a logarithm of it) is undefined, in both codes
+    U0 = _state(f.elem_xgp(), seed=5, amp=0.05)
     f.U = U0
     o.set_state(U0)
     err = rel_err(f.DGTimeDerivative_weakForm(0.0), o.time_derivative(0.0))
