@@ -1144,8 +1144,9 @@ __global__ void __launch_bounds__(Shape<n>::THREADS, (n == 8 ? 2 : 1)) k_vol_spl
 // =====================================================================================================
 // k_vol_split_gen: volint.f90:VolInt_splitForm for any number of nodes per line, Gauss or Gauss-Lobatto.
 // The lines of one direction are packed SEG = 32/n to a warp (n lanes each, the last 32 - SEG*n lanes of a
-// warp idle); a lane evaluates the pairs (a, a+dd mod n) for dd = 1..n/2 and hands the unscaled flux to its
-// partner by shuffle as in k_vol_split (for odd n every pair is evaluated once).
+// warp idle); a lane evaluates the pairs (a, a+dd mod n) for dd = 1..(n-1)/2 and hands the unscaled flux to
+// its partner by shuffle as in k_vol_split; for even n the pairs at distance n/2 follow in a pass of their
+// own, one thread per pair.
 // Gauss nodes (surfint.t90:90-140, 177-215, split-Gauss surface integral): in the same pass each lane
 // evaluates the two-point flux FluxB between its node and the element's own face state at both ends of the
 // line (metric: its node's metric vector plus the face metric row Ja_Face / Ja_slave), the segment forms
@@ -1280,7 +1281,7 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
 #pragma unroll
       for (int v = 0; v < 5; ++v) acc[v] = (dir == 0) ? 0. : sA[(es * 5 + v) * n3 + xa];
 #pragma unroll
-      for (int dd = 1; dd <= n / 2; ++dd) {
+      for (int dd = 1; dd <= (n - 1) / 2; ++dd) {
         const int bI = a + dd < n ? a + dd : a + dd - n;
         const int xb = xline + bI * stride;
         double G[5];
@@ -1290,7 +1291,7 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
         acc[0] = fma(o0, G[0], acc[0]);
 #pragma unroll
         for (int v = 1; v < 5; ++v) acc[v] = fma(o1, G[v], acc[v]);
-        if (2 * dd != n) {
+        {
           // receive the flux of the pair (a-dd, a) from lane a-dd of this segment
           const int aS = a - dd >= 0 ? a - dd : a - dd + n;
           const int src = valid ? segBase + aS : lane;
@@ -1346,6 +1347,37 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
     }
    }
     __syncthreads();
+  }
+  if constexpr (n % 2 == 0) {
+    // even n: the pairs at distance n/2, (a, a+n/2) with a < n/2, each evaluated once by one thread that adds
+    // it to both nodes; one direction at a time (every node is in exactly one such pair per direction)
+    constexpr int HP = n / 2, NPAIR = n2 * HP;
+#pragma unroll 1
+    for (int dir = 0; dir < 3; ++dir) {
+      for (int t = threadIdx.x; t < EPB * NPAIR; t += blockDim.x) {
+        const int es = t / NPAIR, r = t - es * NPAIR;
+        if (e0 + es >= d.nElems) continue;
+        const int a = r % HP, c1 = (r / HP) % n, c2 = r / (HP * n);
+        const int stride = dir == 0 ? 1 : (dir == 1 ? n : n2);
+        const int xline = dir == 0 ? n * (c1 + n * c2) : (dir == 1 ? c1 + n2 * c2 : c1 + n * c2);
+        const int xa = xline + a * stride, xb = xa + HP * stride, b = a + HP;
+        const double* Q = sR + es * 15 * n3;
+        const double* Mm = Q + (6 + 3 * dir) * n3;
+        double G[5];
+        split_pair_flux(pi, Q[xa], Q[n3 + xa], Q[2 * n3 + xa], Q[3 * n3 + xa], Q[4 * n3 + xa], Q[5 * n3 + xa], Q[xb], Q[n3 + xb],
+                        Q[2 * n3 + xb], Q[3 * n3 + xb], Q[4 * n3 + xb], Q[5 * n3 + xb], Mm[xa] + Mm[xb], Mm[n3 + xa] + Mm[n3 + xb],
+                        Mm[2 * n3 + xa] + Mm[2 * n3 + xb], G);
+        double* A = sA + es * 5 * n3;
+        A[xa] = fma(sC[b * n + a], G[0], A[xa]);
+        A[xb] = fma(sC[a * n + b], G[0], A[xb]);
+#pragma unroll
+        for (int v = 1; v < 5; ++v) {
+          A[v * n3 + xa] = fma(sC[n2 + b * n + a], G[v], A[v * n3 + xa]);
+          A[v * n3 + xb] = fma(sC[n2 + a * n + b], G[v], A[v * n3 + xb]);
+        }
+      }
+      __syncthreads();
+    }
   }
   // viscous fluxes (weak form): transformed fluxes of each node from the metrics still in sR; with one node
   // per thread they are written over sR once every thread has finished reading it, else into sV
