@@ -388,11 +388,19 @@ def run_gb300(args):
         hout = torch.empty(dof * 5, dtype=torch.float64).pin_memory()
         f.get_state_ptr(hin.data_ptr())
         barrier()
+        phase = [0.0, 0.0, 0.0]  # upload, step, download (each call returns after its work has finished)
         t0 = time.perf_counter()
         for _ in range(args.steps):
+            ta = time.perf_counter()
             f.set_state_ptr(hin.data_ptr())
+            tb = time.perf_counter()
             f.TimeDisc(1)
+            tc = time.perf_counter()
             f.get_state_ptr(hout.data_ptr())
+            td = time.perf_counter()
+            phase[0] += tb - ta
+            phase[1] += tc - tb
+            phase[2] += td - tc
             hin, hout = hout, hin
         barrier()
         el = time.perf_counter() - t0
@@ -401,7 +409,8 @@ def run_gb300(args):
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             el = float(t.item())
         e2e = {"value": dof * 5 * args.steps * ws / el, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
-               "ms_per_step": el / args.steps * 1e3}
+               "ms_per_step": el / args.steps * 1e3,
+               "ms_per_step_upload_step_download": [round(x / args.steps * 1e3, 3) for x in phase]}
 
     if rank != 0:
         f.close()

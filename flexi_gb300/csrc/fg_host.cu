@@ -19,6 +19,7 @@
 #include "fg_adjoint.cuh"
 #include "fg_common.cuh"
 #include "fg_launch.cuh"
+#include "fg_lserk.hpp"
 #include "fg_mesh.hpp"
 
 namespace fg {
@@ -232,7 +233,8 @@ struct fg_handle {
   double* dInstVol = nullptr;
   double* dTime = nullptr;
   double* dStage = nullptr;  // staging for layout conversion (size nElems*5*n3)
-  double RKA[6]{}, RKb[6]{}, RKc[6]{};
+  double RKA[21]{}, RKb[21]{}, RKc[21]{};
+  int nStages = 5;
   double cflEff = 0., dflEff = 0.;
   // overintegration in use (type 2 is off when NUnder >= N, overintegration.f90:139-141) and its matrices
   OverintDev ov{};
@@ -384,18 +386,13 @@ void init_basis(fg_handle* h) {
   B.sKappaP1 = 1. / (c.kappa + 1.);
   B.logEntC = std::log(c.kappa - 1.) / (c.kappa - 1.);
   B.kappa_kappaM1 = c.kappa / (c.kappa - 1.);
-  // Carpenter-Kennedy RK4-5, timedisc_vars.f90:199-214
-  double* A = h->RKA; double* b = h->RKb; double* cc = h->RKc;
-  A[2] = 567301805773.0 / 1357537059087.0; A[3] = 2404267990393.0 / 2016746695238.0;
-  A[4] = 3550918686646.0 / 2091501179385.0; A[5] = 1275806237668.0 / 842570457699.0;
-  b[1] = 1432997174477.0 / 9575080441755.0; b[2] = 5161836677717.0 / 13612068292357.0;
-  b[3] = 1720146321549.0 / 2090206949498.0; b[4] = 3134564353537.0 / 4481467310338.0;
-  b[5] = 2277821191437.0 / 14882151754819.0;
-  cc[2] = 1432997174477.0 / 9575080441755.0; cc[3] = 2526269341429.0 / 6820363962896.0;
-  cc[4] = 2006345519317.0 / 3224310063776.0; cc[5] = 2802321613138.0 / 2924317926251.0;
+  // the low-storage scheme of TimeDiscMethod (timedisc_vars.f90:137-457)
+  const fgh::LSERKScheme* sch = fgh::lserk_scheme(c.TimeDiscMethod);
+  h->nStages = sch->stages;
+  for (int s = 0; s <= sch->stages; ++s) { h->RKA[s] = sch->A[s]; h->RKb[s] = sch->b[s]; h->RKc[s] = sch->c[s]; }
   // FillCFL_DFL (timedisc_func.f90:463-527)
-  static const double cflG[15] = {2.0351, 1.7595, 1.5401, 1.3702, 1.2375, 1.1318, 1.0440, 0.9709, 0.9079, 0.8539, 0.8066, 0.7650, 0.7290, 0.6952, 0.6660};
-  static const double cflGL[15] = {4.7497, 3.4144, 2.8451, 2.4739, 2.2027, 1.9912, 1.8225, 1.6830, 1.5682, 1.4692, 1.3849, 1.3106, 1.2454, 1.1880, 1.1362};
+  const double* cflG = sch->cflGauss;
+  const double* cflGL = sch->cflGL;
   static const double dflG[10] = {1.12, 0.76, 0.55, 0.41, 0.32, 0.25, 0.20, 0.17, 0.14, 0.12};
   static const double dflGL[10] = {4.50, 1.95, 1.18, 0.79, 0.56, 0.42, 0.32, 0.25, 0.20, 0.17};
   const bool gl = c.NodeType == FG_NODE_GAUSS_LOBATTO;
@@ -415,7 +412,7 @@ void init_basis(fg_handle* h) {
   const int NEff = h->NU < N ? h->NU : N;
   const int iC = (NEff < 15 ? NEff : 15) - 1, iD = (N < 10 ? N : 10) - 1;
   h->cflEff = c.CFLScale * cflTab[iC] / (2. * NEff + 1.);
-  h->dflEff = c.DFLScale * dflTab[iD] * 1.853 / ((2. * N + 1.) * (2. * N + 1.));
+  h->dflEff = c.DFLScale * dflTab[iD] * sch->relativeDFL / ((2. * N + 1.) * (2. * N + 1.));
 }
 
 int upload_mesh(fg_handle* h) {
@@ -679,7 +676,7 @@ void launch_step_setup(fg_handle* h, int mode, double fixedDt, bool advanceTime)
   h->launches += 1;
 }
 void launch_lserk(fg_handle* h) {
-  for (int s = 1; s <= 5; ++s) {
+  for (int s = 1; s <= h->nStages; ++s) {
     if (h->d.srcPar) {
       k_stage_time<<<(h->d.nInst + 127) / 128, 128, 0, h->st>>>(h->d, h->RKc[s]);
       h->launches += 1;
@@ -839,7 +836,7 @@ int fg_config_from_ini(const char* text, fg_config* c) {
       else if (key == "mu0") c->mu0 = std::stod(val);
       else if (key == "cflscale") c->CFLScale = std::stod(val);
       else if (key == "dflscale") c->DFLScale = std::stod(val);
-      else if (key == "timediscmethod") c->TimeDiscMethod = (lv == "carpenterrk4-5") ? 0 : -1;
+      else if (key == "timediscmethod") c->TimeDiscMethod = fgh::lserk_method(lv.c_str());
       else if (key == "overintegrationtype") {
         if (lv == "none") c->OverintegrationType = 0;
         else if (lv == "cutoff") c->OverintegrationType = 1;
@@ -878,7 +875,9 @@ int fg_create(const fg_config* cfg, fg_handle** out) {
   else if (c.doConservativeLifting) why = "doConservativeLifting is not supported";
   else if (c.doWeakLifting) why = "doWeakLifting is not supported (the volume part needs the conservative form)";
   else if (c.SplitDG != FG_SPLIT_NONE && c.SplitDG != FG_SPLIT_SD && c.SplitDG != FG_SPLIT_PI) why = "SplitDG must be -1 (weak), 0 (SD) or 4 (PI)";
-  else if (c.TimeDiscMethod != 0) why = "TimeDiscMethod must be CarpenterRK4-5";
+  else if (!fgh::lserk_scheme(c.TimeDiscMethod))
+    why = "TimeDiscMethod must be one of the low-storage schemes 0..5 (carpenterrk4-5, standardrk3-3, niegemannrk4-14, "
+          "toulorgerk4-8c, toulorgerk3-7c, toulorgerk4-8f)";
   else if (c.OverintegrationType < 0 || c.OverintegrationType > 2) why = "OverintegrationType must be 0 (none), 1 (cutoff) or 2 (conscutoff)";
   else if (c.OverintegrationType > 0 && c.NUnder < -1) why = "NUnder must be >= 0";
   if (!why.empty()) { delete h; return fail(nullptr, FG_ERR_CONFIG, why); }
@@ -984,6 +983,21 @@ int fg_set_instance_mu0(fg_handle* h, int nInst, const double* mu0) {
     if (nInst != h->d.nInst) return fail(h, FG_ERR_CONFIG, "instance count mismatch");
     CUDA_TRY(cudaMemcpy(h->d.mu0, mu0, sizeof(double) * nInst, cudaMemcpyHostToDevice));
   }
+  return FG_OK;
+}
+
+int fg_lserk_table(int method, int* stages, double* A, double* b, double* c, double* cflAlpha, double* relativeDFL) {
+  const fgh::LSERKScheme* s = fgh::lserk_scheme(method);
+  if (!s || !stages) return FG_ERR_CONFIG;
+  *stages = s->stages;
+  for (int i = 0; i < 21; ++i) {
+    if (A) A[i] = s->A[i];
+    if (b) b[i] = s->b[i];
+    if (c) c[i] = s->c[i];
+  }
+  if (cflAlpha)
+    for (int i = 0; i < 15; ++i) { cflAlpha[i] = s->cflGauss[i]; cflAlpha[15 + i] = s->cflGL[i]; }
+  if (relativeDFL) *relativeDFL = s->relativeDFL;
   return FG_OK;
 }
 
@@ -1329,6 +1343,7 @@ static int revolve_reverse(RevolveRun& R, int l, int r, int slotL, int s) {
 int fg_adjoint_forward(fg_handle* h, int nSteps, double dt, int ckptEvery) {
   if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
   if (const char* why = adjoint_unsupported(h->cfg)) return fail(h, FG_ERR_CONFIG, why);
+  if (h->cfg.TimeDiscMethod != 0) return fail(h, FG_ERR_CONFIG, "the LSERK adjoint is built for CarpenterRK4-5 (TimeDiscMethod 0)");
   if (nSteps < 1 || ckptEvery == 0 || !(dt > 0.) || !std::isfinite(dt))
     return fail(h, FG_ERR_CONFIG, "nSteps >= 1, ckptEvery != 0 and dt > 0 required");
   if (int r = ensure_adjoint(h)) return r;

@@ -44,7 +44,7 @@ extern "C" {
  *   N (interpolation.f90:59), NodeType (CMake FLEXI_NODETYPE), Riemann/RiemannBC (riemann.f90:91-115),
  *   Lifting 1=BR1 / 2=BR2 (CMake FLEXI_LIFTING), doWeakLifting, doConservativeLifting, etaBR2,
  *   etaBR2_wall (lifting.f90:61-83), SplitDG (splitflux.f90:77), kappa, R, Pr, mu0 (eos.f90:84-90),
- *   CFLScale, DFLScale (timedisc_func.f90:463-527), TimeDiscMethod (0 = CarpenterRK4-5),
+ *   CFLScale, DFLScale (timedisc_func.f90:463-527), TimeDiscMethod (0 = CarpenterRK4-5, 1..5 the other low-storage schemes),
  *   and the channel body force of testcase/channel (doTCSource, dpdx). */
 typedef struct fg_config {
   int N;
@@ -65,7 +65,8 @@ typedef struct fg_config {
   double DFLScale;
   int doTCSource;
   double dpdx;
-  int TimeDiscMethod;
+  int TimeDiscMethod;       /* timedisc_vars.f90 low-storage schemes (TimeStepByLSERKW2): 0 carpenterrk4-5, 1 standardrk3-3,
+                               2 niegemannrk4-14, 3 toulorgerk4-8c, 4 toulorgerk3-7c, 5 toulorgerk4-8f */
   int OverintegrationType;  /* overintegration.f90: 0 none, 1 cut-off filter of J u_t, 2 conservative cut-off */
   int NUnder;               /* filter degree of OverintegrationType 1/2 (-1: N) */
   int IniExactFunc;         /* exactfunc.f90: 4 (oblique sine wave) adds its source, CalcSource CASE(4); others: no source */
@@ -139,6 +140,11 @@ int fg_set_face_metrics(fg_handle* h, const double* Ja_Face, const double* Ja_sl
  * it once after the initial condition or restart): OverintegrationType 1 filters U with the modal cut-off,
  * 2 applies the conservative cut-off to J U. No-op without overintegration. */
 int fg_overintegrate_state(fg_handle* h);
+
+/* The coefficients of low-storage scheme `method` (TimeDiscMethod code, timedisc_vars.f90:137-457): stage count,
+ * RKA(2:s), RKb(1:s), RKc(2:s) at 1-based indices of 21-element arrays, CFLScaleAlpha(1:15) for Gauss then
+ * Gauss-Lobatto nodes (30 values) and RelativeDFL; any output may be NULL but `stages`. */
+int fg_lserk_table(int method, int* stages, double* A, double* b, double* c, double* cflAlpha, double* relativeDFL);
 
 /* The configuration the handle was created with. */
 int fg_get_config(const fg_handle* h, fg_config* out);

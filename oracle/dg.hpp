@@ -5,6 +5,7 @@
 // (src/timedisc/timestep.f90:82-152). Templated on the scalar type so that a flop-counting scalar can
 // measure the algorithmic flops per DOF and stage. All arrays use FLEXI's Fortran layouts.
 #pragma once
+#include "lserk.hpp"
 #include "mesh.hpp"
 #include <atomic>
 #include <type_traits>
@@ -98,6 +99,7 @@ struct Config {
   int doTCSource = 0;  // channel body force
   double dpdx = -1.;
   int overintType = 0;  // overintegration.f90: 0 none, 1 modal cut-off of J u_t, 2 conservative cut-off
+  int timeDisc = 0;     // TimeDiscMethod code of the low-storage scheme (lserk.hpp)
   int NUnder = -1;      // cut-off degree (-1: N)
   // exact function with a source term (exactfunc.f90: IniExactFunc 4, the oblique sine wave of the
   // convergence tests; 0: no source), AdvVel, IniFrequency, IniAmplitude
@@ -216,7 +218,7 @@ struct DG {
   std::vector<double> muScale;
   std::vector<R> muScaleR;
   // time discretisation (timedisc_vars.f90:175-216, CarpenterRK4-5)
-  double RKA[6], RKb[6], RKc[6];
+  double RKA[21], RKb[21], RKc[21];
   int nRKStages = 5;
   double CFLScaleEff = 0., DFLScaleEff = 0.;
   std::vector<double> MetricsAdv, MetricsVisc;
@@ -258,17 +260,14 @@ struct DG {
     Flux_master.assign(5 * ns2 * nS, R(0.)); Flux_slave = Flux_master;
     entropyVars = C.splitDG != SPLIT_NONE && C.nodeType == NT_GAUSS;
     if (entropyVars) { V.assign(5 * nv3 * nE, R(0.)); V_master = U_master; V_slave = U_master; }
-    // Carpenter-Kennedy RK4-5 (timedisc_vars.f90:199-214), 1-based stage index
-    RKA[2] = 567301805773.0 / 1357537059087.0; RKA[3] = 2404267990393.0 / 2016746695238.0;
-    RKA[4] = 3550918686646.0 / 2091501179385.0; RKA[5] = 1275806237668.0 / 842570457699.0;
-    RKb[1] = 1432997174477.0 / 9575080441755.0; RKb[2] = 5161836677717.0 / 13612068292357.0;
-    RKb[3] = 1720146321549.0 / 2090206949498.0; RKb[4] = 3134564353537.0 / 4481467310338.0;
-    RKb[5] = 2277821191437.0 / 14882151754819.0;
-    RKc[2] = 1432997174477.0 / 9575080441755.0; RKc[3] = 2526269341429.0 / 6820363962896.0;
-    RKc[4] = 2006345519317.0 / 3224310063776.0; RKc[5] = 2802321613138.0 / 2924317926251.0;
+    // the low-storage scheme (timedisc_vars.f90:137-457), 1-based stage index
+    const LserkTable* lt = lserk_table(C.timeDisc);
+    if (!lt) throw std::runtime_error("unknown low-storage time scheme");
+    nRKStages = lt->stages;
+    for (int s = 0; s <= nRKStages; ++s) { RKA[s] = lt->A[s]; RKb[s] = lt->b[s]; RKc[s] = lt->c[s]; }
     // FillCFL_DFL (timedisc_func.f90:463-527) with CFLScaleAlpha/DFLScaleAlpha tables (timedisc_vars.f90)
-    static const double cflG[15] = {2.0351, 1.7595, 1.5401, 1.3702, 1.2375, 1.1318, 1.0440, 0.9709, 0.9079, 0.8539, 0.8066, 0.7650, 0.7290, 0.6952, 0.6660};
-    static const double cflGL[15] = {4.7497, 3.4144, 2.8451, 2.4739, 2.2027, 1.9912, 1.8225, 1.6830, 1.5682, 1.4692, 1.3849, 1.3106, 1.2454, 1.1880, 1.1362};
+    const double* cflG = lt->alphaG;
+    const double* cflGL = lt->alphaGL;
     static const double dflG[10] = {1.12, 0.76, 0.55, 0.41, 0.32, 0.25, 0.20, 0.17, 0.14, 0.12};
     static const double dflGL[10] = {4.50, 1.95, 1.18, 0.79, 0.56, 0.42, 0.32, 0.25, 0.20, 0.17};
     const double* ct = C.nodeType == NT_GL ? cflGL : cflG;
@@ -279,7 +278,7 @@ struct DG {
     const int NEff = std::min(N, NU);
     double alpha = ct[std::min(15, NEff) - 1];
     CFLScaleEff = C.CFLScale * alpha / (2. * NEff + 1.);
-    double RelativeDFL = 1.853;
+    double RelativeDFL = lt->relDFL;
     alpha = dtab[std::min(10, N) - 1] * RelativeDFL;
     DFLScaleEff = C.DFLScale * alpha / ((2. * N + 1.) * (2. * N + 1.));
     // InitCalctimestep (calctimestep.f90:42-83)

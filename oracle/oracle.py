@@ -25,11 +25,12 @@ class OrcConfig(ctypes.Structure):
                 ("Pr", ctypes.c_double), ("mu0", ctypes.c_double), ("CFLScale", ctypes.c_double), ("DFLScale", ctypes.c_double),
                 ("doTCSource", ctypes.c_int), ("dpdx", ctypes.c_double), ("overintType", ctypes.c_int), ("NUnder", ctypes.c_int),
                 ("iniExactFunc", ctypes.c_int), ("advVel", ctypes.c_double * 3), ("iniFrequency", ctypes.c_double),
-                ("iniAmplitude", ctypes.c_double)]
+                ("iniAmplitude", ctypes.c_double), ("timeDisc", ctypes.c_int)]
 
 # keys a configuration may leave out (defaults of the reference: no overintegration, NUnder = N; no source term,
 # IniFrequency 1, IniAmplitude 0.1 of exact function 4)
-_OPTIONAL = {"overintType": 0, "NUnder": -1, "iniExactFunc": 0, "advVel": (0.0, 0.0, 0.0), "iniFrequency": 1.0, "iniAmplitude": 0.1}
+_OPTIONAL = {"overintType": 0, "NUnder": -1, "iniExactFunc": 0, "advVel": (0.0, 0.0, 0.0), "iniFrequency": 1.0, "iniAmplitude": 0.1,
+             "timeDisc": 0}
 
 
 def lib():
@@ -66,6 +67,7 @@ def lib():
         _lib.orc_flops_per_dof_stage.argtypes = [P]
         _lib.orc_flops_per_dof_stage.restype = ctypes.c_double
         _lib.orc_flops_breakdown.argtypes = [P, P]
+        _lib.orc_lserk_table.argtypes = [ctypes.c_int, P, P, P, P]
         _lib.orc_set_threads.argtypes = [ctypes.c_int]
         _lib.orc_max_threads.restype = ctypes.c_int
         _lib.orc_nodes_and_weights.argtypes = [ctypes.c_int, ctypes.c_int, P, P, P]
@@ -271,6 +273,15 @@ def set_threads(n):
 
 def max_threads():
     return lib().orc_max_threads()
+
+
+def lserk_table(code):
+    """(stages, A, b, c) of the oracle's low-storage scheme `code` (1-based stage arrays of length 21)."""
+    st = ctypes.c_int(0)
+    A, b, c = np.zeros(21), np.zeros(21), np.zeros(21)
+    if lib().orc_lserk_table(int(code), ctypes.byref(st), _p(A), _p(b), _p(c)) != 0:
+        raise ValueError(f"no low-storage scheme {code}")
+    return st.value, A, b, c
 
 
 def nodes_and_weights(N, node_type):

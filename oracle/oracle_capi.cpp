@@ -18,6 +18,7 @@ struct orc_config {
   int overintType, NUnder;
   int iniExactFunc;
   double advVel[3], iniFrequency, iniAmplitude;
+  int timeDisc;
 };
 
 static Config to_cfg(const orc_config* c) {
@@ -27,6 +28,7 @@ static Config to_cfg(const orc_config* c) {
   C.etaBR2 = c->etaBR2; C.etaBR2_wall = c->etaBR2_wall; C.kappa = c->kappa; C.R = c->R; C.Pr = c->Pr; C.mu0 = c->mu0;
   C.CFLScale = c->CFLScale; C.DFLScale = c->DFLScale; C.doTCSource = c->doTCSource; C.dpdx = c->dpdx;
   C.overintType = c->overintType; C.NUnder = c->NUnder;
+  C.timeDisc = c->timeDisc;
   C.iniExactFunc = c->iniExactFunc;
   for (int d = 0; d < 3; ++d) C.advVel[d] = c->advVel[d];
   C.iniFrequency = c->iniFrequency; C.iniAmplitude = c->iniAmplitude;
@@ -229,6 +231,15 @@ void orc_get_gradients(void* hp, int which, double* out) {
   auto& d = ((OrcHandle*)hp)->dg;
   auto& g = which == 0 ? d.gradUx : (which == 1 ? d.gradUy : d.gradUz);
   std::memcpy(out, g.data(), g.size() * 8);
+}
+
+// the oracle's low-storage scheme tables: stages, RKA(2..s), RKb(1..s), RKc(2..s) (1-based, length 21)
+int orc_lserk_table(int code, int* stages, double* A, double* b, double* c) {
+  const LserkTable* t = lserk_table(code);
+  if (!t) return 1;
+  *stages = t->stages;
+  for (int s = 0; s < 21; ++s) { A[s] = t->A[s]; b[s] = t->b[s]; c[s] = t->c[s]; }
+  return 0;
 }
 
 // algorithmic flops of one right-hand side evaluation (flop-counting scalar), divided by the DOF count
