@@ -1195,7 +1195,7 @@ int fg_vjp_time_derivative(fg_handle* h, double t, const double* W, double* V, d
 static int adjoint_alloc_common(fg_handle* h, int segSteps) {
   const int n3 = h->M.n * h->M.n * h->M.n, n2 = h->M.n * h->M.n;
   const size_t cnt = (size_t)h->M.nElems * 5 * n3;
-  h->adjStage.assign((size_t)segSteps * 5, nullptr);
+  h->adjStage.assign((size_t)segSteps * h->nStages, nullptr);
   for (auto& p : h->adjStage) if (int r = adj_alloc(h, p, cnt)) return r;
   const size_t perStage = (size_t)h->M.nElems * (VP_NF + 12) * n3 + (size_t)h->M.nSides * (2 * FS_NF + 24) * n2;
   size_t freeB = 0, totalB = 0;
@@ -1245,8 +1245,8 @@ static int adjoint_reverse_segment(fg_handle* h, const double* Ustart, int ns, c
   for (int s = 0; s < ns; ++s) {
     launch_step_setup(h, 1, dt, false);
     CUDA_TRY(cudaMemcpyAsync(h->adjBulkHist + (size_t)s * nI, h->d.bulkVel, sizeof(double) * nI, cudaMemcpyDeviceToDevice, h->st));
-    for (int k = 1; k <= 5; ++k) {
-      const size_t slot = (size_t)s * 5 + k - 1;
+    for (int k = 1; k <= h->nStages; ++k) {
+      const size_t slot = (size_t)s * h->nStages + k - 1;
       CUDA_TRY(cudaMemcpyAsync(h->adjStage[slot], h->d.U, bytes, cudaMemcpyDeviceToDevice, h->st));
       if (h->adjKeepInter) {
         // the stage writes its intermediates into the slot; the state is updated in place as usual
@@ -1260,11 +1260,11 @@ static int adjoint_reverse_segment(fg_handle* h, const double* Ustart, int ns, c
   }
   // Gbar_k = -A_{k+1} Gbar_{k+1} + b_k dt Ubar; Ubar += J(U_{k-1})^T Gbar_k
   for (int s = ns - 1; s >= 0; --s) {
-    for (int k = 5; k >= 1; --k) {
-      k_adj_axpby<<<gridAx, 256, 0, h->st>>>(h->adjGbar, h->adjUbar, k == 5 ? 0. : -h->RKA[k + 1], h->RKb[k] * dt, cnt);
+    for (int k = h->nStages; k >= 1; --k) {
+      k_adj_axpby<<<gridAx, 256, 0, h->st>>>(h->adjGbar, h->adjUbar, k == h->nStages ? 0. : -h->RKA[k + 1], h->RKb[k] * dt, cnt);
       k_adj_source<<<h->M.nElems, 128, 0, h->st>>>(h->d, h->adjGbar, h->adjFbar, h->adjPartial, h->adjBulkHist + (size_t)s * nI, n3);
       h->launches += 2;
-      const size_t slot = (size_t)s * 5 + k - 1;
+      const size_t slot = (size_t)s * h->nStages + k - 1;
       if (h->adjKeepInter) {
         launch_vjp_kept(h, h->adjInter[slot], a);
       } else {
@@ -1276,7 +1276,7 @@ static int adjoint_reverse_segment(fg_handle* h, const double* Ustart, int ns, c
     if (bulkAdj) {
       // the step's bulk velocity depends on its start state (stage 1 input)
       k_adj_bulk_reduce<<<(nI + 127) / 128, 128, 0, h->st>>>(nI, h->dInstStart, h->adjPartial, h->adjBulkBar);
-      k_adj_bulk_apply<<<gridAx, 256, 0, h->st>>>(h->d, h->adjUbar, h->adjStage[(size_t)s * 5], h->adjBulkBar, h->dWVol, h->dInstVol, n3);
+      k_adj_bulk_apply<<<gridAx, 256, 0, h->st>>>(h->d, h->adjUbar, h->adjStage[(size_t)s * h->nStages], h->adjBulkBar, h->dWVol, h->dInstVol, n3);
       h->launches += 2;
     }
   }
@@ -1343,7 +1343,6 @@ static int revolve_reverse(RevolveRun& R, int l, int r, int slotL, int s) {
 int fg_adjoint_forward(fg_handle* h, int nSteps, double dt, int ckptEvery) {
   if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
   if (const char* why = adjoint_unsupported(h->cfg)) return fail(h, FG_ERR_CONFIG, why);
-  if (h->cfg.TimeDiscMethod != 0) return fail(h, FG_ERR_CONFIG, "the LSERK adjoint is built for CarpenterRK4-5 (TimeDiscMethod 0)");
   if (nSteps < 1 || ckptEvery == 0 || !(dt > 0.) || !std::isfinite(dt))
     return fail(h, FG_ERR_CONFIG, "nSteps >= 1, ckptEvery != 0 and dt > 0 required");
   if (int r = ensure_adjoint(h)) return r;
