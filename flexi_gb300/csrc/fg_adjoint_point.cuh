@@ -172,10 +172,93 @@ FG_HD void entropy_fix_adj(double a, double al, double ar, double eb, double& ab
   }
 }
 
-// Transposed Jacobian of riemann_rotated (LF, Roe, RoeEntropyFix; split or not): Fb[5] given, adds to the
+// Transposed Jacobian of the HLLC flux of riemann_rotated (riemann.f90:594-663, Roe-Einfeldt wave speeds;
+// its split and non-split forms are the same): Fb[5] given, adds to the bars of both rotated states,
+// retracing the forward's branch (supersonic left / right, left or right star state).
+FG_HD void hllc_adj(const Basis& B, const RotState& L, const RotState& R, const double* Fb, RotState& Lb, RotState& Rb) {
+  const double HL = (L.E + L.p) * L.srho, HR = (R.E + R.p) * R.srho;
+  const double sqL = sqrt(L.rho), sqR = sqrt(R.rho);
+  const double ssq = 1.0 / (sqL + sqR);
+  const double r1v = (sqR * R.v1 + sqL * L.v1) * ssq;
+  const double r2v = (sqR * R.v2 + sqL * L.v2) * ssq;
+  const double r3v = (sqR * R.v3 + sqL * L.v3) * ssq;
+  const double rH = (sqR * HR + sqL * HL) * ssq;
+  const double absVel = r1v * r1v + r2v * r2v + r3v * r3v;
+  const double rc = sqrt(B.kappaM1 * (rH - 0.5 * absVel));
+  const double Ssl = r1v - rc, Ssr = r1v + rc;
+  if (Ssl >= 0.0) { euler_flux_1d_adj(L, Fb, Lb); return; }
+  if (Ssr <= 0.0) { euler_flux_1d_adj(R, Fb, Rb); return; }
+  const double sMuL = Ssl - L.v1, sMuR = Ssr - R.v1;
+  const double mL = L.rho * L.v1, mR = R.rho * R.v1;
+  const double num = R.p - L.p + mL * sMuL - mR * sMuR, den = L.rho * sMuL - R.rho * sMuR;
+  const double SStar = num / den;
+  double Sslb = 0, Ssrb = 0, SStarb = 0, sMuLb = 0, sMuRb = 0, mLb = 0, mRb = 0;
+  // star state of side X (left: sign s = Ssl, right: Ssr): F = F_X + S (Us - Uc)
+  auto star = [&](const RotState& X, RotState& Xb, double S, double sMu, double m, double& Sb, double& sMub, double& mb) {
+    euler_flux_1d_adj(X, Fb, Xb);
+    const double Z = X.p * X.srho / sMu;
+    const double EStar = X.E * X.srho + (SStar - X.v1) * (SStar + Z);
+    const double d = S - SStar;
+    const double fac = X.rho * sMu / d;
+    const double Us[5] = {fac, fac * SStar, fac * X.v2, fac * X.v3, fac * EStar};
+    const double Uc[5] = {X.rho, m, X.rho * X.v2, X.rho * X.v3, X.E};
+    for (int v = 0; v < 5; ++v) Sb += Fb[v] * (Us[v] - Uc[v]);
+    // Uc
+    Xb.rho -= S * (Fb[0] + Fb[2] * X.v2 + Fb[3] * X.v3);
+    mb -= S * Fb[1];
+    Xb.v2 -= S * Fb[2] * X.rho;
+    Xb.v3 -= S * Fb[3] * X.rho;
+    Xb.E -= S * Fb[4];
+    // Us
+    const double facb = S * (Fb[0] + Fb[1] * SStar + Fb[2] * X.v2 + Fb[3] * X.v3 + Fb[4] * EStar);
+    SStarb += S * Fb[1] * fac;
+    Xb.v2 += S * Fb[2] * fac;
+    Xb.v3 += S * Fb[3] * fac;
+    const double EStarb = S * Fb[4] * fac;
+    // fac = X.rho sMu / d
+    const double qb = facb / d, db = -facb * fac / d;
+    Xb.rho += qb * sMu; sMub += qb * X.rho;
+    Sb += db; SStarb -= db;
+    // EStar = X.E X.srho + (SStar - X.v1) (SStar + Z), Z = X.p X.srho / sMu
+    Xb.E += EStarb * X.srho; Xb.srho += EStarb * X.E;
+    const double Xdb = EStarb * (SStar + Z), Ydb = EStarb * (SStar - X.v1);
+    SStarb += Xdb + Ydb; Xb.v1 -= Xdb;
+    Xb.p += Ydb * X.srho / sMu; Xb.srho += Ydb * X.p / sMu; sMub -= Ydb * Z / sMu;
+  };
+  if (Ssl <= 0.0 && SStar >= 0.0) star(L, Lb, Ssl, sMuL, mL, Sslb, sMuLb, mLb);
+  else star(R, Rb, Ssr, sMuR, mR, Ssrb, sMuRb, mRb);
+  // SStar = num / den
+  const double numb = SStarb / den, denb = -SStarb * SStar / den;
+  Rb.p += numb; Lb.p -= numb;
+  mLb += numb * sMuL; sMuLb += numb * mL; mRb -= numb * sMuR; sMuRb -= numb * mR;
+  Lb.rho += denb * sMuL; sMuLb += denb * L.rho; Rb.rho -= denb * sMuR; sMuRb -= denb * R.rho;
+  Lb.rho += mLb * L.v1; Lb.v1 += mLb * L.rho; Rb.rho += mRb * R.v1; Rb.v1 += mRb * R.rho;
+  Sslb += sMuLb; Lb.v1 -= sMuLb; Ssrb += sMuRb; Rb.v1 -= sMuRb;
+  // wave speeds from the Roe averages
+  double r1vb = Sslb + Ssrb, rcb = Ssrb - Sslb, r2vb = 0, r3vb = 0, rHb = 0, absb = 0, HLb = 0, HRb = 0;
+  const double Zb = rcb / (2.0 * rc);
+  rHb += B.kappaM1 * Zb;
+  absb -= 0.5 * B.kappaM1 * Zb;
+  r1vb += 2.0 * r1v * absb; r2vb += 2.0 * r2v * absb; r3vb += 2.0 * r3v * absb;
+  const double ssqb = rHb * (sqR * HR + sqL * HL) + r1vb * (sqR * R.v1 + sqL * L.v1) + r2vb * (sqR * R.v2 + sqL * L.v2) +
+                      r3vb * (sqR * R.v3 + sqL * L.v3);
+  double sqRb = (rHb * HR + r1vb * R.v1 + r2vb * R.v2 + r3vb * R.v3) * ssq;
+  double sqLb = (rHb * HL + r1vb * L.v1 + r2vb * L.v2 + r3vb * L.v3) * ssq;
+  HRb += rHb * sqR * ssq; HLb += rHb * sqL * ssq;
+  Rb.v1 += r1vb * sqR * ssq; Lb.v1 += r1vb * sqL * ssq;
+  Rb.v2 += r2vb * sqR * ssq; Lb.v2 += r2vb * sqL * ssq;
+  Rb.v3 += r3vb * sqR * ssq; Lb.v3 += r3vb * sqL * ssq;
+  sqLb -= ssqb * ssq * ssq; sqRb -= ssqb * ssq * ssq;
+  Lb.rho += sqLb / (2.0 * sqL); Rb.rho += sqRb / (2.0 * sqR);
+  enthalpy_adj(L, HLb, Lb);
+  enthalpy_adj(R, HRb, Rb);
+}
+
+// Transposed Jacobian of riemann_rotated (LF, HLLC, Roe, RoeEntropyFix; split or not): Fb[5] given, adds to the
 // bars of both rotated states (all seven fields of each are independent inputs).
 FG_HD void riemann_rotated_adj(int solver, int splitDG, const Basis& B, const RotState& L, const RotState& R, const double* Fb, RotState& Lb,
                                RotState& Rb) {
+  if (solver == RIEMANN_HLLC) { hllc_adj(B, L, R, Fb, Lb, Rb); return; }
   const bool split = splitDG >= 0;
   const double HL = (L.E + L.p) * L.srho, HR = (R.E + R.p) * R.srho;
   double HLb = 0.0, HRb = 0.0;

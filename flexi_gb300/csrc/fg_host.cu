@@ -717,8 +717,6 @@ const char* adjoint_unsupported(const fg_config& c) {
   if (c.SplitDG != FG_SPLIT_NONE && c.SplitDG != FG_SPLIT_PI) return "the adjoint supports the weak form and the split form PI";
   if (c.SplitDG != FG_SPLIT_NONE && (c.NodeType != FG_NODE_GAUSS_LOBATTO || (c.N != 1 && c.N != 3 && c.N != 7)))
     return "the adjoint of the split form supports Gauss-Lobatto nodes with N = 1, 3, 7";
-  if (c.Riemann != FG_RIEMANN_LF && c.Riemann != FG_RIEMANN_ROE && c.Riemann != FG_RIEMANN_ROEENTROPYFIX)
-    return "the adjoint supports the LF, Roe and RoeEntropyFix surface fluxes";
   return nullptr;
 }
 

@@ -129,7 +129,7 @@ def test_physical_viscous_flux_adjoint(pt):
         assert err is not None and err < TOL, err
 
 
-@pytest.mark.parametrize("solver", [1, 3, 33])
+@pytest.mark.parametrize("solver", [1, 2, 3, 33])
 @pytest.mark.parametrize("split", [-1, 4, 0])
 def test_riemann_adjoint(pt, solver, split):
     rng = np.random.default_rng(10 * solver + split + 5)

@@ -24,6 +24,9 @@ CASES = {
     "gl7_split_pi_roe_br1": (dict(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roe", Lifting="br1"), "tgv"),
     "gl7_split_pi_roeef_br2": (dict(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roeentropyfix", Lifting="br2"), "tgv"),
     "gl3_split_pi_lf_br2": (dict(N=3, NodeType="gauss-lobatto", SplitDG="pi", Riemann="lf", Lifting="br2"), "tgv"),
+    # HLLC: the surface flux of the N=7 TGV benchmark
+    "gl7_split_pi_hllc_br2": (dict(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="hllc", Lifting="br2"), "tgv"),
+    "gauss3_weak_hllc_br1": (dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="hllc", Lifting="br1"), "tgv"),
     "channel_gauss3_weak_roe_br1": (dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="roe", Lifting="br1"), "channel"),
     "channel_gl7_split_pi_roe_br1": (dict(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roe", Lifting="br1"), "channel"),
     "channel_gl3_split_pi_roeef_br2_adiabatic": (dict(N=3, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roeentropyfix", Lifting="br2"),
@@ -108,10 +111,10 @@ def test_viscosity_multiplier_cotangent(name):
 
 
 def test_vjp_rejects_unsupported():
-    c = make_config(N=3, NodeType="gauss-lobatto", SplitDG="pi", Riemann="hllc")
+    c = make_config(N=3, NodeType="gauss-lobatto", SplitDG="sd", Riemann="hllc")
     f = Flexi(c, fmesh.tgv_box(2))
     f.U = testcases.tgv_state(f.elem_xgp(), mach=0.1)
-    with pytest.raises(Exception, match="LF, Roe and RoeEntropyFix"):
+    with pytest.raises(Exception, match="split form PI"):
         f.vjp_time_derivative(np.zeros(f.ushape))
 
 

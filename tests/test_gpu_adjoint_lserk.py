@@ -30,6 +30,8 @@ CASES = {
                                               TimeDiscMethod=2),
     "gl3_split_pi_roeef_br1_rk33": dict(N=3, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roeentropyfix", Lifting="br1",
                                         TimeDiscMethod=1),
+    # the discretisation of the N=7 TGV benchmark (split PI, HLLC, BR2) at N=3
+    "gl3_split_pi_hllc_br2": dict(N=3, NodeType="gauss-lobatto", SplitDG="pi", Riemann="hllc", Lifting="br2"),
 }
 N_STEPS = 7
 
