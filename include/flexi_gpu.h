@@ -247,7 +247,7 @@ int fg_set_elem_mu_scale(fg_handle* h, const double* scale);
  * Jacobian is that of the discrete operator the GPU evaluates (the reference's implicit solver only forms
  * J V by finite differences, implicit.f90:MatrixVector). t is unused (no time-dependent source on this
  * path). The bulk velocity of a channel body force is held fixed. Supported: weak form and split form PI,
- * LF/Roe/RoeEntropyFix, BR1/BR2, walls 3/4. */
+ * LF/HLLC/Roe/RoeEntropyFix, BR1/BR2, walls 3/4. */
 int fg_vjp_time_derivative(fg_handle* h, double t, const double* W, double* V, double* muScaleBar);
 
 /* J V of DGTimeDerivative_weakForm at the current state by the matrix-free finite difference of the
