@@ -268,34 +268,29 @@ __host__ __device__ __forceinline__ void riemann_rotated(int solver, int splitDG
   const double absVel = r1v * r1v + r2v * r2v + r3v * r3v;
   const double rc = sqrt(B.kappaM1 * (rH - 0.5 * absVel));
   if (solver == RIEMANN_HLLC) {
-    double FL[5], FR[5];
-    euler_flux_1d(L, FL); euler_flux_1d(R, FR);
+    // the side X whose flux (and, subsonic, whose star state) the interface takes is selected first, so
+    // that a warp evaluates one Euler flux and one star state whatever mix of sides its points take
     const double Ssl = r1v - rc, Ssr = r1v + rc;
-    if (Ssl >= 0.0) {
+    const bool supL = Ssl >= 0.0, supR = !supL && Ssr <= 0.0;
+    const double sMuL = Ssl - L.v1, sMuR = Ssr - R.v1;
+    const double mL = L.rho * L.v1, mR = R.rho * R.v1;
+    double SStar = 0.0;
+    if (!supL && !supR) SStar = (R.p - L.p + mL * sMuL - mR * sMuR) / (L.rho * sMuL - R.rho * sMuR);
+    const bool useL = supL || (!supR && SStar >= 0.0);  // subsonic: Ssl < 0, the left star state for SStar >= 0
+    const RotState& X = useL ? L : R;
+    double FX[5];
+    euler_flux_1d(X, FX);
+    if (supL || supR) {
 #pragma unroll
-      for (int v = 0; v < 5; ++v) F[v] = FL[v];
-    } else if (Ssr <= 0.0) {
-#pragma unroll
-      for (int v = 0; v < 5; ++v) F[v] = FR[v];
+      for (int v = 0; v < 5; ++v) F[v] = FX[v];
     } else {
-      const double sMuL = Ssl - L.v1, sMuR = Ssr - R.v1;
-      const double mL = L.rho * L.v1, mR = R.rho * R.v1;
-      const double SStar = (R.p - L.p + mL * sMuL - mR * sMuR) / (L.rho * sMuL - R.rho * sMuR);
-      if (Ssl <= 0.0 && SStar >= 0.0) {
-        const double EStar = L.E * L.srho + (SStar - L.v1) * (SStar + L.p * L.srho / sMuL);
-        const double fac = L.rho * sMuL / (Ssl - SStar);
-        const double Us[5] = {fac, fac * SStar, fac * L.v2, fac * L.v3, fac * EStar};
-        const double Uc[5] = {L.rho, mL, L.rho * L.v2, L.rho * L.v3, L.E};
+      const double S = useL ? Ssl : Ssr, sMu = useL ? sMuL : sMuR, m = useL ? mL : mR;
+      const double EStar = X.E * X.srho + (SStar - X.v1) * (SStar + X.p * X.srho / sMu);
+      const double fac = X.rho * sMu / (S - SStar);
+      const double Us[5] = {fac, fac * SStar, fac * X.v2, fac * X.v3, fac * EStar};
+      const double Uc[5] = {X.rho, m, X.rho * X.v2, X.rho * X.v3, X.E};
 #pragma unroll
-        for (int v = 0; v < 5; ++v) F[v] = FL[v] + Ssl * (Us[v] - Uc[v]);
-      } else {
-        const double EStar = R.E * R.srho + (SStar - R.v1) * (SStar + R.p * R.srho / sMuR);
-        const double fac = R.rho * sMuR / (Ssr - SStar);
-        const double Us[5] = {fac, fac * SStar, fac * R.v2, fac * R.v3, fac * EStar};
-        const double Uc[5] = {R.rho, mR, R.rho * R.v2, R.rho * R.v3, R.E};
-#pragma unroll
-        for (int v = 0; v < 5; ++v) F[v] = FR[v] + Ssr * (Us[v] - Uc[v]);
-      }
+      for (int v = 0; v < 5; ++v) F[v] = FX[v] + S * (Us[v] - Uc[v]);
     }
     return;
   }
