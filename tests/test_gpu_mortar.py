@@ -156,3 +156,28 @@ def test_drop_in_mortar_mesh(name):
     err = rel_err(f.DGTimeDerivative_weakForm(0.0), o.time_derivative(0.0))
     f.close()
     assert err <= 1e-12, err
+
+
+@pytest.mark.parametrize("kw", [dict(N=5, NodeType="gauss", SplitDG="weak", OverintegrationType=1, NUnder=3),
+                                dict(N=5, NodeType="gauss-lobatto", SplitDG="pi", OverintegrationType=2, NUnder=3)])
+def test_overintegration_and_source_on_mortar_mesh(kw):
+    """Overintegration (the filter of J u_t, overintegration.f90) and the exact-function source on a mortar
+    mesh: Ut at t = 0.3 and five LSERK steps against the oracle."""
+    c = product_cfg(Riemann="roeentropyfix", IniExactFunc=4, AdvVel=(0.3, 0.3, 0.3), **kw, **COMMON)
+    m = _mesh("CART_HEX_PERIODIC_MORTAR_FLIPPED_004_mesh.h5")
+    f = Flexi(c, m)
+    o = orc.Oracle(oracle_cfg(c), m)
+    U0 = _state(f.elem_xgp(), seed=9, amp=0.05)
+    f.U = U0
+    o.set_state(U0)
+    err = rel_err(f.DGTimeDerivative_weakForm(0.3), o.time_derivative(0.3))
+    assert err <= 1e-12, err
+    t_f = t_o = 0.3
+    for _ in range(5):
+        dt_f, dt_o = f.CalcTimeStep()[0], o.calc_timestep()[0]
+        assert abs(dt_f / dt_o - 1.0) <= 1e-12
+        t_f = f.TimeStepByLSERKW2(t_f, dt_f)
+        t_o = o.timestep(t_o, dt_o)
+    err = rel_err(f.U, o.get_state())
+    f.close()
+    assert err <= 1e-11, err
