@@ -632,7 +632,11 @@ void launch_rhs_dev(fg_handle* h, const Dev& d, int mode, double rkA, double rkB
   const bool mortars = d.nMortars > 0;
   { ProfScope p(h, 0); h->K.prep(d, h->B, h->st); }
   if (mortars) { ProfScope p(h, 5); h->K.mortar_pre(d, h->B, h->mort, h->st); h->launches += 1; }
-  { ProfScope p(h, 1); (mortars ? h->K.lift_mortar : h->K.lift)(d, h->B, h->st); }
+  {
+    ProfScope p(h, 1);
+    const bool cons = h->cfg.doConservativeLifting || h->cfg.doWeakLifting;
+    (mortars ? (cons ? h->K.lift_mortar_cons : h->K.lift_mortar) : (cons ? h->K.lift_cons : h->K.lift))(d, h->B, h->st);
+  }
   if (d.nFluxSides > 0) { ProfScope p(h, 2); h->K.flux_block(d, h->B, h->K.fluxBlock, h->st); }
   if (mortars) { ProfScope p(h, 5); h->K.mortar_face(d, h->B, h->mort, h->st); h->launches += 1; }
   {
@@ -713,6 +717,7 @@ namespace {
 // the adjoint kernels cover: weak form and split form PI, LF/Roe/RoeEntropyFix, BR1/BR2
 const char* adjoint_unsupported(const fg_config& c) {
   if (c.N > 7) return "the adjoint supports N = 1..7";
+  if (c.doWeakLifting || c.doConservativeLifting) return "the adjoint supports the strong, non-conservative lifting";
   if (c.OverintegrationType != 0) return "the adjoint does not support overintegration";
   if (c.SplitDG != FG_SPLIT_NONE && c.SplitDG != FG_SPLIT_PI) return "the adjoint supports the weak form and the split form PI";
   if (c.SplitDG != FG_SPLIT_NONE && (c.NodeType != FG_NODE_GAUSS_LOBATTO || (c.N != 1 && c.N != 3 && c.N != 7)))
@@ -863,6 +868,7 @@ int fg_create(const fg_config* cfg, fg_handle** out) {
   *out = nullptr;
   fg_handle* h = new fg_handle();
   h->cfg = *cfg;
+  if (h->cfg.Lifting == 2) h->cfg.doWeakLifting = 0;  // lifting.f90:137-139: BR2 lifts in strong form
   const fg_config& c = h->cfg;
   std::string why;
   if (c.N < 1 || c.N > 11) why = "N must be in 1..11";
@@ -870,8 +876,6 @@ int fg_create(const fg_config* cfg, fg_handle** out) {
   else if (c.Riemann != FG_RIEMANN_LF && c.Riemann != FG_RIEMANN_HLLC && c.Riemann != FG_RIEMANN_ROE && c.Riemann != FG_RIEMANN_ROEENTROPYFIX)
     why = "Riemann must be LF, HLLC, Roe or RoeEntropyFix";
   else if (c.Lifting != 1 && c.Lifting != 2) why = "Lifting must be 1 (BR1) or 2 (BR2)";
-  else if (c.doConservativeLifting) why = "doConservativeLifting is not supported";
-  else if (c.doWeakLifting) why = "doWeakLifting is not supported (the volume part needs the conservative form)";
   else if (c.SplitDG != FG_SPLIT_NONE && c.SplitDG != FG_SPLIT_SD && c.SplitDG != FG_SPLIT_PI) why = "SplitDG must be -1 (weak), 0 (SD) or 4 (PI)";
   else if (!fgh::lserk_scheme(c.TimeDiscMethod))
     why = "TimeDiscMethod must be one of the low-storage schemes 0..5 (carpenterrk4-5, standardrk3-3, niegemannrk4-14, "

@@ -22,7 +22,7 @@ struct Inst {
   static constexpr long long gs(long long big) { return big_in_global<n>(big) ? big : 0; }
   static constexpr long long mx(long long a, long long b) { return a > b ? a : b; }
   static constexpr long long SCRATCH_PER_BLOCK =
-      mx(mx(mx(gs(Big<n>::prep), gs(Big<n>::lift)), mx(gs(Big<n>::weak), gs(SplitShape<n>::template big<GL>()))), gs(Big<n>::liftMortar));
+      mx(mx(mx(gs(Big<n>::prep), gs(Big<n>::lift)), mx(gs(Big<n>::weak), gs(SplitShape<n>::template big<GL>()))), gs(Big<n>::liftVariant(true, true)));
   static size_t smem_weak_adj() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * 5 * S::n3 + S::THREADS); }
   static size_t smem_split_adj() { return sizeof(double) * (SBasis<n>::SIZE + 2 * S::n2 + S::EPB * 26 * S::n3 + S::THREADS); }
   static size_t smem_lift_adj() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * (13 * S::n3 + 6 * S::n2 * 19)); }
@@ -66,6 +66,8 @@ struct Inst {
     else set_smem(k_vol_split_gen<n, GL>, smem_split_gen());
     set_smem(k_overint<n>, smem_overint());
     set_smem(k_lift<n, GL, 0, true>, smem_lift_mortar());
+    set_smem(k_lift<n, GL, 0, false, true>, smem_lift_v(false, true));
+    set_smem(k_lift<n, GL, 0, true, true>, smem_lift_v(true, true));
     set_smem(k_mortar_pre<n>, smem_mortar_pre());
     set_smem(k_mortar_face<n>, smem_mortar_face());
     if constexpr (ADJ) {
@@ -120,6 +122,14 @@ struct Inst {
   }
   // mortar interfaces (one CTA of 256 threads per big mortar side)
   static size_t smem_lift_mortar() { return dyn_smem_bytes<n>(Big<n>::liftMortar); }
+  static size_t smem_lift_v(bool mortar, bool cons) { return dyn_smem_bytes<n>(Big<n>::liftVariant(mortar, cons)); }
+  // conservative / weak volume part of the lifting (doConservativeLifting, doWeakLifting), without and with mortars
+  static void lift_cons(const Dev& d, const Basis& B, cudaStream_t st) {
+    k_lift<n, GL, 0, false, true><<<blocks(d), S::THREADS, smem_lift_v(false, true), st>>>(d, B);
+  }
+  static void lift_mortar_cons(const Dev& d, const Basis& B, cudaStream_t st) {
+    k_lift<n, GL, 0, true, true><<<blocks(d), S::THREADS, smem_lift_v(true, true), st>>>(d, B);
+  }
   static size_t smem_mortar_pre() { return sizeof(double) * 97 * S::n2; }
   static size_t smem_mortar_face() { return sizeof(double) * 104 * S::n2; }
   static void mortar_pre(const Dev& d, const Basis& B, const MortarDev& M, cudaStream_t st) {
@@ -147,6 +157,7 @@ struct Inst {
     k.vol_split = &vol_split;
     k.overint = &overint;
     k.mortar_pre = &mortar_pre; k.lift_mortar = &lift_mortar; k.mortar_face = &mortar_face;
+    k.lift_cons = &lift_cons; k.lift_mortar_cons = &lift_mortar_cons;
     if constexpr (ADJ) { k.vol_adj = &vol_adj; k.flux_adj = &flux_adj; k.lift_adj = &lift_adj; k.prep_adj = &prep_adj; }
     k.defEPB = S::EPB;
     k.scratchPerBlock = SCRATCH_PER_BLOCK;

@@ -44,6 +44,8 @@ template <int n, int E = 0> struct Big {
   static constexpr long long prep = (long long)S::EPB * (5 + VP_NF) * S::n3;
   static constexpr long long lift = (long long)S::EPB * (17 * S::n3 + 42 * S::n2);
   static constexpr long long liftMortar = (long long)S::EPB * (17 * S::n3 + 72 * S::n2);
+  // k_lift variants: MORTAR keeps 12 products per face point, CONS stages the 9 metric terms
+  __host__ __device__ static constexpr long long liftVariant(bool mortar, bool cons) { return (mortar ? liftMortar : lift) + (cons ? (long long)S::EPB * 9 * S::n3 : 0); }
   static constexpr long long weak = (long long)S::EPB * (15 * S::n3 + 30 * S::n2);
 };
 
@@ -247,18 +249,19 @@ __device__ __forceinline__ void lift_prolong_faces(const Dev& d, const Basis& B,
 // (lifting_br1.t90:106-109, lifting_br2.t90:103-106: Flux_Mortar of the lifting fluxes), which k_mortar_pre
 // leaves in Dev::mortarLift; with BR2 the face penalty uses the same products.
 // =====================================================================================================
-template <int n, bool GL, int E = 0, bool MORTAR = false>
+template <int n, bool GL, int E = 0, bool MORTAR = false, bool CONS = false>
 __global__ void __launch_bounds__(Shape<n, E>::THREADS, (n == 8 && GL ? 2 : 1)) k_lift(Dev d, Basis B) {
   using S = Shape<n, E>;
   constexpr int n2 = S::n2, n3 = S::n3, EPB = S::EPB, N = S::N;
   constexpr int NFN = MORTAR ? 12 : 4;  // values per face point in sF
   extern __shared__ double smem[];
   double* sD = smem;
-  double* sL = big_base<n>(d, smem, MORTAR ? Big<n, E>::liftMortar : Big<n, E>::lift);  // [EPB][4][n3] lifting variables u,v,w,T
+  double* sL = big_base<n>(d, smem, Big<n, E>::liftVariant(MORTAR, CONS));  // [EPB][4][n3] lifting variables u,v,w,T
   double* sF = sL + EPB * 4 * n3;        // [EPB][6][n2][NFN] surface lifting flux (times SurfElem), local face order
   double* sN = sF + EPB * 6 * n2 * NFN;  // [EPB][6][n2][3] face normal of the side point mapped to local face order (not MORTAR)
   double* sG = sN + (MORTAR ? 0 : EPB * 6 * n2 * 3);  // [EPB][12][n3] gradients
   double* sJs = sG + EPB * 12 * n3;      // [EPB][n3]
+  double* sMc = sJs + EPB * n3;          // CONS: [EPB][9][n3] metrics (not times sJ) of the conservative volume part
   load_basis_smem<n>(B, sD);
   SBasis<n> Bs{sD};
   const int e0 = blockIdx.x * EPB;
@@ -269,6 +272,10 @@ __global__ void __launch_bounds__(Shape<n, E>::THREADS, (n == 8 && GL ? 2 : 1)) 
 #pragma unroll
     for (int v = 0; v < 4; ++v) sL[(es * 4 + v) * n3 + x] = d.prim[((size_t)e * VP_NF + (v < 3 ? VP_U + v : VP_T)) * n3 + x];
     sJs[es * n3 + x] = d.sJ[(size_t)e * n3 + x];
+    if constexpr (CONS) {
+#pragma unroll
+      for (int c = 0; c < 9; ++c) sMc[(es * 9 + c) * n3 + x] = d.metr[((size_t)e * 9 + c) * n3 + x];
+    }
   }
   // surface lifting fluxes of the six sides (lifting_fillflux.t90), stored in this element's face order
   const double sig = B.weakLifting ? 1.0 : -1.0;
@@ -337,33 +344,59 @@ __global__ void __launch_bounds__(Shape<n, E>::THREADS, (n == 8 && GL ? 2 : 1)) 
     if (e >= d.nElems) continue;
     const int i = x % n, j = (x / n) % n, k = x / n2;
     const double* L = sL + es * 4 * n3;
-    double gx[4], ge[4], gz[4];
+    double g[12];
+    if constexpr (CONS) {
+      // lifting_volint.t90:Lifting_VolInt_Conservative: d/dx_c (v) = sJ sum_d sum_l DMat(l, i_d) Ja_d,c(l) v(l), DMat = D_T
+      // (doConservativeLifting) or D_Hat_T (doWeakLifting)
+      const double* Mc = sMc + es * 9 * n3;
 #pragma unroll
-    for (int v = 0; v < 4; ++v) { gx[v] = 0.; ge[v] = 0.; gz[v] = 0.; }
+      for (int c = 0; c < 12; ++c) g[c] = 0.;
+      const int idx3[3] = {i, j, k};
 #pragma unroll
-    for (int l = 0; l < n; ++l) {
-      const double dxi = Bs.DT(l, i), deta = Bs.DT(l, j), dzeta = Bs.DT(l, k);
+      for (int dir = 0; dir < 3; ++dir) {
 #pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        gx[v] = fma(dxi, L[v * n3 + l + n * (j + n * k)], gx[v]);
-        ge[v] = fma(deta, L[v * n3 + i + n * (l + n * k)], ge[v]);
-        gz[v] = fma(dzeta, L[v * n3 + i + n * (j + n * l)], gz[v]);
+        for (int l = 0; l < n; ++l) {
+          const double cf = B.weakLifting ? Bs.DhT(l, idx3[dir]) : Bs.DT(l, idx3[dir]);
+          const int xl = dir == 0 ? l + n * (j + n * k) : (dir == 1 ? i + n * (l + n * k) : i + n * (j + n * l));
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const double f = cf * Mc[(3 * dir + c) * n3 + xl];
+#pragma unroll
+            for (int v = 0; v < 4; ++v) g[4 * c + v] = fma(f, L[v * n3 + xl], g[4 * c + v]);
+          }
+        }
       }
-    }
-    double mJ[9];
-    if (d.metrJ) {
-#pragma unroll
-      for (int c = 0; c < 9; ++c) mJ[c] = d.metrJ[((size_t)e * 9 + c) * n3 + x];
-    } else {
       const double sj = sJs[es * n3 + x];
 #pragma unroll
-      for (int c = 0; c < 9; ++c) mJ[c] = d.metr[((size_t)e * 9 + c) * n3 + x] * sj;
+      for (int c = 0; c < 12; ++c) g[c] *= sj;
+    } else {
+      double gx[4], ge[4], gz[4];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) { gx[v] = 0.; ge[v] = 0.; gz[v] = 0.; }
+#pragma unroll
+      for (int l = 0; l < n; ++l) {
+        const double dxi = Bs.DT(l, i), deta = Bs.DT(l, j), dzeta = Bs.DT(l, k);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          gx[v] = fma(dxi, L[v * n3 + l + n * (j + n * k)], gx[v]);
+          ge[v] = fma(deta, L[v * n3 + i + n * (l + n * k)], ge[v]);
+          gz[v] = fma(dzeta, L[v * n3 + i + n * (j + n * l)], gz[v]);
+        }
+      }
+      double mJ[9];
+      if (d.metrJ) {
+#pragma unroll
+        for (int c = 0; c < 9; ++c) mJ[c] = d.metrJ[((size_t)e * 9 + c) * n3 + x];
+      } else {
+        const double sj = sJs[es * n3 + x];
+#pragma unroll
+        for (int c = 0; c < 9; ++c) mJ[c] = d.metr[((size_t)e * 9 + c) * n3 + x] * sj;
+      }
+#pragma unroll
+      for (int dd = 0; dd < 3; ++dd)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) g[4 * dd + v] = mJ[dd] * gx[v] + mJ[3 + dd] * ge[v] + mJ[6 + dd] * gz[v];
     }
-    double g[12];
-#pragma unroll
-    for (int dd = 0; dd < 3; ++dd)
-#pragma unroll
-      for (int v = 0; v < 4; ++v) g[4 * dd + v] = mJ[dd] * gx[v] + mJ[3 + dd] * ge[v] + mJ[6 + dd] * gz[v];
     if constexpr (GL) {
 #pragma unroll
       for (int c = 0; c < 12; ++c) sG[(es * 12 + c) * n3 + x] = g[c];

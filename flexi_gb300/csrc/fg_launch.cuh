@@ -21,6 +21,9 @@ struct KernelSet {
   void (*mortar_pre)(const Dev&, const Basis&, const MortarDev&, cudaStream_t) = nullptr;
   void (*lift_mortar)(const Dev&, const Basis&, cudaStream_t) = nullptr;
   void (*mortar_face)(const Dev&, const Basis&, const MortarDev&, cudaStream_t) = nullptr;
+  // lifting with the conservative (doConservativeLifting) or weak (doWeakLifting) volume part
+  void (*lift_cons)(const Dev&, const Basis&, cudaStream_t) = nullptr;
+  void (*lift_mortar_cons)(const Dev&, const Basis&, cudaStream_t) = nullptr;
   // adjoint (vector-Jacobian product) of the right-hand side; vol_adj is null where unsupported
   void (*vol_adj)(const Dev&, const AdjDev&, const Basis&, cudaStream_t) = nullptr;
   void (*flux_adj)(const Dev&, const AdjDev&, const Basis&, cudaStream_t) = nullptr;

@@ -148,6 +148,12 @@ class Flexi:
         b = np.ascontiguousarray(Ja_slave, np.float64)
         self._check(self.L.fg_set_face_metrics(self.h, _p(a), _p(b)), "fg_set_face_metrics")
 
+    def get_config(self):
+        """fg_get_config: the configuration the handle runs with (BR2 turns doWeakLifting off, lifting.f90:137-139)."""
+        c = _lib.FgConfig()
+        self._check(self.L.fg_get_config(self.h, ctypes.byref(c)), "fg_get_config")
+        return c
+
     def overintegrate_state(self):
         """timedisc.f90:115-123: the overintegration of U before the first time step (no-op without it)."""
         self._check(self.L.fg_overintegrate_state(self.h), "fg_overintegrate_state")

@@ -42,7 +42,12 @@ def test_config_defaults_and_validation(lib):
     with pytest.raises(FlexiError):
         Flexi(make_config(N=5, SplitDG=2))  # split fluxes other than SD (0) and PI (4)
     with pytest.raises(FlexiError):
-        Flexi(make_config(N=3, doConservativeLifting=1))
+        Flexi(make_config(N=5, OverintegrationType=3))
+    # lifting.f90:137-139: BR2 lifts in strong form, doWeakLifting is dropped; doConservativeLifting stays
+    f = Flexi(make_config(N=3, Lifting="br2", doWeakLifting=1, doConservativeLifting=1))
+    d = config_dict(f.get_config())
+    assert d["doWeakLifting"] == 0 and d["doConservativeLifting"] == 1
+    f.close()
 
 
 def test_ini_parser(lib):
