@@ -1271,24 +1271,7 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
   // two-point flux G (unscaled; density factor f0, others f1) between state a and state b with metric sum ms
   auto two_point = [pi](double ra, double ua, double va, double wa, double pa, double ha, double rb, double ub, double vb, double wb,
                         double pb, double hb, double ms0, double ms1, double ms2, double* G) {
-    if (pi) {
-      const double rs = ra + rb, us = ua + ub, vs = va + vb, ws = wa + wb, ps4 = pa + pb, hs = ha + hb;
-      const double qs = us * ms0 + vs * ms1 + ws * ms2;
-      const double A = rs * qs;
-      G[0] = A;
-      G[1] = fma(A, us, ps4 * ms0);
-      G[2] = fma(A, vs, ps4 * ms1);
-      G[3] = fma(A, ws, ps4 * ms2);
-      G[4] = A * hs;
-    } else {
-      const double qa = ua * ms0 + va * ms1 + wa * ms2, qb = ub * ms0 + vb * ms1 + wb * ms2;
-      const double mqa = ra * qa, mqb = rb * qb;
-      G[0] = mqa + mqb;
-      G[1] = fma(mqa, ua, mqb * ub) + (pa + pb) * ms0;
-      G[2] = fma(mqa, va, mqb * vb) + (pa + pb) * ms1;
-      G[3] = fma(mqa, wa, mqb * wb) + (pa + pb) * ms2;
-      G[4] = fma(ha, qa, hb * qb);
-    }
+    split_pair_flux(pi, ra, ua, va, wa, pa, ha, rb, ub, vb, wb, pb, hb, ms0, ms1, ms2, G);
   };
   const int lane = threadIdx.x & 31;
   const int seg = lane / n, a = lane - seg * n, segBase = seg * n;
