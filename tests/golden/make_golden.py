@@ -4,7 +4,7 @@ Reads FLEXI v25.10's unit-test data (unitTests/*.bin, Fortran unformatted sequen
 4-byte length marker, little-endian payload, closing marker) and the Taylor-Green regression
 references (regressioncheck/checks/tgv/{split,splitGauss,oInt}/TGV_Re1600_*_TGVAnalysis_Reference.csv),
 and stores the arrays the parity tests need in reference_unittests.npz, tgv_split_reference.npz,
-tgv_splitgauss_reference.npz and tgv_oint_reference.npz; copies eleven HOPR mesh / FLEXI state files
+tgv_splitgauss_reference.npz and tgv_oint_reference.npz; copies fifteen HOPR mesh / FLEXI state files
 of the reference's test cases to hopr/ for the HDF5 reader.
 
 Run from the repository root in a container that has the reference mounted:
@@ -104,7 +104,8 @@ def main(ref):
                 "regressioncheck/checks/timedisc/freestream_3D/cartbox_State_0000000.000000000.h5",
                 "tutorials/naca0012/NACA0012_652_Ng2_mesh.h5",
                 "regressioncheck/checks/run_basic/freestream_3D/cartbox3D_mortar_mesh.h5") + tuple(
-                f"regressioncheck/checks/convtest/h_3D_mortar/CART_HEX_PERIODIC_MORTAR_FLIPPED_{k:03d}_mesh.h5" for k in (1, 2, 4, 8)):
+                f"regressioncheck/checks/convtest/h_3D_mortar/CART_HEX_PERIODIC_MORTAR_FLIPPED_{k:03d}_mesh.h5" for k in (1, 2, 4, 8)) + tuple(
+                f"regressioncheck/checks/convtest/h_3D/CART_HEX_PERIODIC_{k:03d}_3D_mesh.h5" for k in (1, 2, 4, 8)):
         shutil.copyfile(os.path.join(ref, src), os.path.join(hdir, os.path.basename(src)))
     print("wrote fixtures:", sorted(out.keys()))
 

@@ -1,5 +1,5 @@
 """The reference's convergence tests on the GPU: exact function 4 (the oblique sine wave) with its source
-(exactfunc.f90:CalcSource CASE(4)) on the mortar meshes of regressioncheck/checks/convtest.
+(exactfunc.f90:CalcSource CASE(4)) on the conforming and mortar meshes of regressioncheck/checks/convtest.
 
 - Ut with the source at t = 0.37 against the oracle (1e-12), on a conforming box and a mortar mesh; ten
   LSERK steps (stage times t + c_i dt in the source) against the oracle (1e-11); the captured time loop
@@ -11,6 +11,9 @@
   increment of N up to 8 lowers the error of every variable, and the algebraic rate
   log(e_N / e_N+1) / log((N+1) / N), averaged over the variables, exceeds 0.6 on at least 75 % of the
   increments (this file's reading of analyze_Convtest_p_rate = 0.6, analyze_Convtest_p_percentage = 0.75).
+- convtest/h_3D and p_3D (conforming periodic meshes CART_HEX_PERIODIC_001..008_3D, AdvVel (0.3, 0.3, 0.3),
+  p-rate 0.8) and their parabolic_off variants (Euler: mu0 = 0; h-tolerance 0.7, L2 below 0.8): the same
+  criteria.
 """
 import os
 
@@ -30,7 +33,7 @@ CONV = dict(Riemann="roeentropyfix", Lifting="br1", kappa=1.4, R=287.058, Pr=0.7
 
 
 def _cfg(N, adv, **kw):
-    return product_cfg(N=N, NodeType="gauss", SplitDG="weak", AdvVel=adv, **CONV, **kw)
+    return product_cfg(**dict(dict(N=N, NodeType="gauss", SplitDG="weak", AdvVel=adv, **CONV), **kw))
 
 
 @pytest.mark.parametrize("mesh", ["box", "CART_HEX_PERIODIC_MORTAR_FLIPPED_002_mesh.h5"])
@@ -74,8 +77,8 @@ def test_captured_time_loop_matches_single_steps():
     assert err <= 1e-13, err
 
 
-def _run(name, N, adv, t_end=1.0):
-    f = Flexi(_cfg(N, adv), fmesh.read_hopr(os.path.join(HOPR, name)))
+def _run(name, N, adv, t_end=1.0, **kw):
+    f = Flexi(_cfg(N, adv, **kw), fmesh.read_hopr(os.path.join(HOPR, name)))
     x = f.elem_xgp()
     f.U = testcases.sine_wave_state(x, 0.0, adv)
     t = 0.0
@@ -104,3 +107,19 @@ def test_p_convergence_mortar_gpu():
     assert (errs[1:8] < errs[:7]).all(), errs
     rate = np.log(errs[:-1] / errs[1:]) / np.log(np.arange(2, 11) / np.arange(1, 10))[:, None]
     assert (rate.mean(axis=1) > 0.6).mean() >= 0.75, rate
+
+
+@pytest.mark.parametrize("mu0,tol,l2max", [(1e-3, 0.15, 0.5), (0.0, 0.7, 0.8)])
+def test_h_convergence_conforming_gpu(mu0, tol, l2max):
+    errs = np.array([_run(f"CART_HEX_PERIODIC_{k:03d}_3D_mesh.h5", 3, (0.3, 0.3, 0.3), mu0=mu0) for k in (1, 2, 4, 8)])
+    assert (errs < l2max).all()
+    order = np.log2(errs[:-1] / errs[1:]).mean(axis=0)
+    assert (np.abs(order / 4.0 - 1.0) <= tol).mean() >= 0.8, order
+
+
+@pytest.mark.parametrize("mu0", [1e-3, 0.0])
+def test_p_convergence_conforming_gpu(mu0):
+    errs = np.array([_run("CART_HEX_PERIODIC_002_3D_mesh.h5", N, (0.3, 0.3, 0.3), mu0=mu0) for N in range(1, 11)])
+    assert (errs < 5.0).all()
+    rate = np.log(errs[:-1] / errs[1:]) / np.log(np.arange(2, 11) / np.arange(1, 10))[:, None]
+    assert (rate.mean(axis=1) > 0.8).mean() >= 0.75, rate
