@@ -76,6 +76,14 @@ __global__ void k_finish_step(Dev d, const double* bulkPart, const int* instStar
     tInst[i] += dt;
   }
 }
+// out = in * sJ (mul = 1) or in / sJ (mul = 0), per node of [e][5][n3] arrays
+__global__ void k_scale_by_sj(const double* __restrict__ in, const double* __restrict__ sJ, double* out, int n3, long long cnt, int mul) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cnt) return;
+  const long long e = i / (5LL * n3);
+  const double s = sJ[e * n3 + i % n3];
+  out[i] = mul ? in[i] * s : in[i] / s;
+}
 // time of RK stage c of the current step, t_n + c dt, for the time-dependent source
 __global__ void k_stage_time(Dev d, double c) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -238,6 +246,8 @@ struct fg_handle {
   double cflEff = 0., dflEff = 0.;
   // overintegration in use (type 2 is off when NUnder >= N, overintegration.f90:139-141) and its matrices
   OverintDev ov{};
+  OverintDev ovT{};  // the transposed filter (adjoint of overintegration): F^T, or VUN^T / VNU^T in the roles of VNU / VUN
+  double* adjWov = nullptr;  // [e][5][n3] cotangent of Ut carried through the transposed filter
   int NU = 0;
   // mortar interfaces: operators and the device copy of the mortar table (Dev::nMortars > 0)
   MortarDev mort{};
@@ -553,6 +563,12 @@ int upload_mesh(fg_handle* h) {
       double* dF = nullptr;
       if ((r = upload(h, dF, F))) return r;
       h->ov.F = dF;
+      std::vector<double> FT((size_t)n * n);
+      for (int i = 0; i < n; ++i) for (int l = 0; l < n; ++l) FT[(size_t)l * n + i] = F[(size_t)i * n + l];
+      double* dFT = nullptr;
+      if ((r = upload(h, dFT, FT))) return r;
+      h->ovT = h->ov;
+      h->ovT.F = dFT;
     } else {
       const fgh::Mat Vd = fgh::vandermonde(N, type, NU, type, true), Vu = fgh::vandermonde(NU, type, N, type, true);
       std::vector<double> VNU((size_t)nu * n), VUN((size_t)n * nu);
@@ -585,6 +601,14 @@ int upload_mesh(fg_handle* h) {
       if ((r = upload(h, dW, VUN))) return r;
       if ((r = upload(h, dS, sJNU))) return r;
       h->ov.VNU = dV; h->ov.VUN = dW; h->ov.sJNU = dS;
+      // transposes: VUN^T [nu][n] takes the role of VNU, VNU^T [n][nu] that of VUN
+      std::vector<double> VUNT((size_t)nu * n), VNUT((size_t)n * nu);
+      for (int i = 0; i < n; ++i) for (int a = 0; a < nu; ++a) { VUNT[(size_t)a * n + i] = VUN[(size_t)i * nu + a]; VNUT[(size_t)i * nu + a] = VNU[(size_t)a * n + i]; }
+      double *dVT = nullptr, *dWT = nullptr;
+      if ((r = upload(h, dVT, VUNT))) return r;
+      if ((r = upload(h, dWT, VNUT))) return r;
+      h->ovT = h->ov;
+      h->ovT.VNU = dVT; h->ovT.VUN = dWT;
     }
   }
   if ((r = dalloc(h, h->dBulkPart, (size_t)nE))) return r;
@@ -718,7 +742,6 @@ namespace {
 const char* adjoint_unsupported(const fg_config& c) {
   if (c.N > 7) return "the adjoint supports N = 1..7";
   if (c.doWeakLifting || c.doConservativeLifting) return "the adjoint supports the strong, non-conservative lifting";
-  if (c.OverintegrationType != 0) return "the adjoint does not support overintegration";
   if (c.SplitDG != FG_SPLIT_NONE && c.SplitDG != FG_SPLIT_PI) return "the adjoint supports the weak form and the split form PI";
   if (c.SplitDG != FG_SPLIT_NONE && (c.NodeType != FG_NODE_GAUSS_LOBATTO || (c.N != 1 && c.N != 3 && c.N != 7)))
     return "the adjoint of the split form supports Gauss-Lobatto nodes with N = 1, 3, 7";
@@ -736,6 +759,7 @@ int ensure_adjoint(fg_handle* h) {
   if ((r = dalloc(h, W, (size_t)nE * 5 * n3))) return r;
   a.W = W;
   if ((r = dalloc(h, a.Ub, (size_t)nE * 5 * n3))) return r;
+  if (h->ov.type > 0 && (r = dalloc(h, h->adjWov, (size_t)nE * 5 * n3))) return r;
   if ((r = dalloc(h, a.gb, (size_t)nE * 12 * n3))) return r;
   if ((r = dalloc(h, a.fluxb, (size_t)nS * 2 * 5 * n2))) return r;
   if ((r = dalloc(h, a.faceMb, (size_t)nS * FS_NF * n2))) return r;
@@ -757,7 +781,27 @@ int ensure_adjoint(fg_handle* h) {
 
 // V = (dUt/dU)^T W at the state d.U, W in a.W; leaves V in a.Ub and the viscosity-multiplier
 // cotangent in a.muElemb (added to them when a.accumulate)
-void launch_vjp(fg_handle* h, const Dev& d, const AdjDev& a) {
+// overintegration.f90 transposed: the cotangent W of Ut = G(J u_t) becomes W' = G^T(W) / sJ, which the
+// adjoint volume kernel (that multiplies by -sJ, the transposed Jacobian) then carries into J u_t; G^T is the
+// state-mode filter kernel run with the transposed matrices on sJ W (type 1: G = sJ F3, G^T W = F3^T (sJ W);
+// type 2: G = VUN sJNU VNU, G^T W = VNU^T sJNU VUN^T W, the state mode dividing its input by sJ first)
+AdjDev overint_adj_cotangent(fg_handle* h, const Dev& d, const AdjDev& a) {
+  if (h->ov.type == 0) return a;
+  const int n3 = h->M.n * h->M.n * h->M.n;
+  const long long cnt = (long long)d.nElems * 5 * n3;
+  k_scale_by_sj<<<(unsigned)((cnt + 255) / 256), 256, 0, h->st>>>(a.W, d.sJ, h->adjWov, n3, cnt, 1);
+  Dev dv = d;
+  dv.U = h->adjWov;
+  h->K.overint(dv, h->ovT, 0, 0., 0., 1, h->st);
+  k_scale_by_sj<<<(unsigned)((cnt + 255) / 256), 256, 0, h->st>>>(h->adjWov, d.sJ, h->adjWov, n3, cnt, 0);
+  h->launches += 3;
+  AdjDev b = a;
+  b.W = h->adjWov;
+  return b;
+}
+
+void launch_vjp(fg_handle* h, const Dev& d, const AdjDev& a0) {
+  const AdjDev a = overint_adj_cotangent(h, d, a0);
   h->K.prep(d, h->B, h->st);
   h->K.lift(d, h->B, h->st);
   h->K.vol_adj(d, a, h->B, h->st);
@@ -768,7 +812,8 @@ void launch_vjp(fg_handle* h, const Dev& d, const AdjDev& a) {
 }
 
 // adjoint right-hand side on forward intermediates the caller kept (no prep/lift recomputation)
-void launch_vjp_kept(fg_handle* h, const Dev& d, const AdjDev& a) {
+void launch_vjp_kept(fg_handle* h, const Dev& d, const AdjDev& a0) {
+  const AdjDev a = overint_adj_cotangent(h, d, a0);
   h->K.vol_adj(d, a, h->B, h->st);
   h->K.flux_adj(d, a, h->B, h->st);
   h->K.lift_adj(d, a, h->B, h->st);

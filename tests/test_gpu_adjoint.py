@@ -27,6 +27,11 @@ CASES = {
     # HLLC: the surface flux of the N=7 TGV benchmark
     "gl7_split_pi_hllc_br2": (dict(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="hllc", Lifting="br2"), "tgv"),
     "gauss3_weak_hllc_br1": (dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="hllc", Lifting="br1"), "tgv"),
+    # overintegration (the transposed filter): modal cut-off and conservative cut-off
+    "gauss5_weak_roeef_br1_cutoff": (dict(N=5, NodeType="gauss", SplitDG="weak", Riemann="roeentropyfix", Lifting="br1",
+                                          OverintegrationType=1, NUnder=3), "tgv"),
+    "gl7_split_pi_roeef_br2_conscutoff": (dict(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roeentropyfix", Lifting="br2",
+                                               OverintegrationType=2, NUnder=4), "tgv"),
     "channel_gauss3_weak_roe_br1": (dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="roe", Lifting="br1"), "channel"),
     "channel_gl7_split_pi_roe_br1": (dict(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roe", Lifting="br1"), "channel"),
     "channel_gl3_split_pi_roeef_br2_adiabatic": (dict(N=3, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roeentropyfix", Lifting="br2"),

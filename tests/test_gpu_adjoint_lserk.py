@@ -34,6 +34,9 @@ CASES = {
                                         TimeDiscMethod=1),
     # the discretisation of the N=7 TGV benchmark (split PI, HLLC, BR2) at N=3
     "gl3_split_pi_hllc_br2": dict(N=3, NodeType="gauss-lobatto", SplitDG="pi", Riemann="hllc", Lifting="br2"),
+    # overintegration: the stage right-hand sides carry the cut-off filter, the reverse sweep its transpose
+    "gauss3_weak_roeef_br1_cutoff": dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="roeentropyfix", Lifting="br1",
+                                         OverintegrationType=1, NUnder=2),
 }
 N_STEPS = 7
 
