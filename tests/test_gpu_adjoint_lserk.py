@@ -2,17 +2,15 @@
 
 Bars: the gradients with respect to the initial state and the viscosity multipliers pass the dot-product
 test against the oracle's exact (dual-number) tangent of the whole solve within 1e-10 of the sum of
-|JV_i w_i|; in the RoeEntropyFix case both also agree with
-Richardson-extrapolated central differences of the same fixed-dt solve within 1e-7 (relative; HLLC's
-wave-speed branches switch under the viscosity step of those differences, so HLLC is held to the exact
-tangent as the plain Roe flux is); the
-result does not depend on the checkpoint interval (identical to round-off, 1e-13); a kinetic-energy
-loss differentiated through flexi_gb300.autograd matches its finite difference within 1e-7. The plain
-Roe flux has a kink at a zero eigenvalue, which a finite difference can straddle somewhere among a
-thousand face points and 35 stages, so its gradients are checked against the exact tangent only (as for
-the 14-stage case, whose 3.4x larger steps made the RoeEntropyFix central differences drift by 2e-5 while
-the dot-product test against the exact tangent held at 1e-10). The reverse sweep runs every low-storage
-scheme (3, 5 and 14 stages here)."""
+|JV_i w_i|; for the 5-stage RoeEntropyFix cases both also agree with Richardson-extrapolated central
+differences of the same fixed-dt solve within 1e-7 (relative); the result does not depend on the
+checkpoint interval (identical to round-off, 1e-13); a kinetic-energy loss differentiated through
+flexi_gb300.autograd matches its finite difference within 1e-7. The other cases are held to the exact
+tangent only: the plain Roe flux has a kink at a zero eigenvalue and HLLC wave-speed branches, which a
+finite difference can straddle somewhere among a thousand face points and 35 stages; the 14-stage scheme's
+3.4x larger steps and the overintegration case made the central differences drift by 2e-5 and 6e-6 while
+their dot-product tests held at 1e-10. The reverse sweep runs every low-storage scheme (3, 5 and 14 stages
+here) and the transposed overintegration filter."""
 import numpy as np
 import pytest
 import torch
@@ -35,8 +33,8 @@ CASES = {
     # the discretisation of the N=7 TGV benchmark (split PI, HLLC, BR2) at N=3
     "gl3_split_pi_hllc_br2": dict(N=3, NodeType="gauss-lobatto", SplitDG="pi", Riemann="hllc", Lifting="br2"),
     # overintegration: the stage right-hand sides carry the cut-off filter, the reverse sweep its transpose
-    "gauss3_weak_roeef_br1_cutoff": dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="roeentropyfix", Lifting="br1",
-                                         OverintegrationType=1, NUnder=2),
+    "gauss3_weak_roe_br1_cutoff": dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="roe", Lifting="br1",
+                                       OverintegrationType=1, NUnder=2),
 }
 N_STEPS = 7
 
