@@ -220,18 +220,23 @@ def concatenate(meshes):
     ngeo = meshes[0].ngeo
     if any(m.ngeo != ngeo for m in meshes):
         raise ValueError("all instances need the same NGeo")
-    coords, nbs, inst = [], [], []
+    coords, nbs, inst, mortars = [], [], [], []
     off = 0
     for i, m in enumerate(meshes):
         if len(m.boundary_type):
             raise ValueError("ensembles of periodic instances only")
         coords.append(m.node_coords)
         nb = m.elem_nb.copy()
-        nb[:, :, 0] = np.where(nb[:, :, 0] > 0, nb[:, :, 0] + off, 0)
+        nb[:, :, 0] = np.where(nb[:, :, 0] > 0, nb[:, :, 0] + off, nb[:, :, 0])  # 0 boundary, -1 mortar side
         nbs.append(nb)
+        if m.mortars is not None and len(m.mortars):
+            mo = np.array(m.mortars, np.int32).copy()
+            for c in (0, 3, 6, 9, 12):  # element ids of the big side and the small sides
+                mo[:, c] = np.where(mo[:, c] > 0, mo[:, c] + off, mo[:, c])
+            mortars.append(mo)
         inst.append(np.full(m.n_elems, i, np.int32))
         off += m.n_elems
-    out = BoxMesh(off, ngeo, np.concatenate(coords), np.concatenate(nbs))
+    out = BoxMesh(off, ngeo, np.concatenate(coords), np.concatenate(nbs), mortars=np.concatenate(mortars) if mortars else None)
     out.elem_inst = np.concatenate(inst)
     out.description = f"ensemble of {len(meshes)} instances, {off} elements"
     return out

@@ -181,3 +181,24 @@ def test_overintegration_and_source_on_mortar_mesh(kw):
     err = rel_err(f.U, o.get_state())
     f.close()
     assert err <= 1e-11, err
+
+
+def test_ensemble_with_mortar_instance():
+    """An ensemble of a mortar box and a conforming box (concatenate) gives each instance the time derivative
+    of its own handle."""
+    c = product_cfg(N=3, NodeType="gauss", SplitDG="weak", Riemann="roeentropyfix", **COMMON)
+    a, b = fmesh.mortar_box(2, perturb=0.05, seed=1), fmesh.tgv_box(2, ngeo=2, perturb=0.05, seed=2)
+    fe = Flexi(c, fmesh.concatenate([a, b]))
+    xe = fe.elem_xgp()
+    Ue = perturb_state(testcases.tgv_state(xe, mach=0.1, kappa=1.4, R=287.058), seed=3)
+    fe.U = Ue
+    Ute = fe.DGTimeDerivative_weakForm(0.0)
+    off = 0
+    for m in (a, b):
+        f = Flexi(c, m)
+        f.U = Ue[off:off + m.n_elems]
+        ut = f.DGTimeDerivative_weakForm(0.0)
+        assert rel_err(Ute[off:off + m.n_elems], ut) <= 1e-14
+        off += m.n_elems
+        f.close()
+    fe.close()

@@ -194,3 +194,21 @@ def test_ini_exact_function_keys(lib):
     assert config_dict(make_config(AdvVel=(1.0, 2.0, 3.0)))["AdvVel"] == (1.0, 2.0, 3.0)
     with pytest.raises(FlexiError):
         config_from_ini("AdvVel = (/0.3,0.2/)\n")
+
+
+def test_ensemble_of_mortar_instances(lib):
+    """concatenate() keeps mortar sides (-1) and offsets the Mortars table: an ensemble of a mortar box and a
+    plain box prepares the same sides as the two meshes separately."""
+    a, b = fmesh.mortar_box(2, perturb=0.05, seed=1), fmesh.tgv_box(2)
+    e = fmesh.concatenate([a, b])
+    assert len(e.mortars) == len(a.mortars) and (e.elem_nb[:, :, 0] == -1).sum() == (a.elem_nb[:, :, 0] == -1).sum()
+    fe = Flexi(make_config(N=3, NodeType=1, SplitDG=-1))
+    fe.build_mesh(e, host_only_ok=True)
+    sizes = []
+    for m in (a, b):
+        f = Flexi(make_config(N=3, NodeType=1, SplitDG=-1))
+        f.build_mesh(m, host_only_ok=True)
+        sizes.append(f.n_sides)
+        f.close()
+    assert fe.n_sides == sum(sizes)
+    fe.close()
