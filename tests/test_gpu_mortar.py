@@ -187,7 +187,7 @@ def test_ensemble_with_mortar_instance():
     """An ensemble of a mortar box and a conforming box (concatenate) gives each instance the time derivative
     of its own handle."""
     c = product_cfg(N=3, NodeType="gauss", SplitDG="weak", Riemann="roeentropyfix", **COMMON)
-    a, b = fmesh.mortar_box(2, perturb=0.05, seed=1), fmesh.tgv_box(2, ngeo=2, perturb=0.05, seed=2)
+    a, b = fmesh.mortar_box(2, perturb=0.05, seed=1), fmesh.tgv_box(2, ngeo=1, perturb=0.05, seed=2)
     fe = Flexi(c, fmesh.concatenate([a, b]))
     xe = fe.elem_xgp()
     Ue = perturb_state(testcases.tgv_state(xe, mach=0.1, kappa=1.4, R=287.058), seed=3)
