@@ -18,7 +18,7 @@ class FgConfig(ctypes.Structure):
 
 
 EXPORTS = ["fg_config_default", "fg_config_from_ini", "fg_create", "fg_destroy", "fg_last_error", "fg_build_mesh", "fg_build_mesh_mortar", "fg_set_mesh", "fg_set_mesh_mortar", "fg_set_face_metrics", "fg_overintegrate_state",
-           "fg_get_config", "fg_lserk_table", "fg_hopr_sizes", "fg_hopr_read", "fg_write_state", "fg_read_state", "fg_io_last_error",
+           "fg_get_config", "fg_lserk_table", "fg_set_time", "fg_hopr_sizes", "fg_hopr_read", "fg_write_state", "fg_read_state", "fg_io_last_error",
            "fg_set_instance_mu0", "fg_get_elem_xgp", "fg_get_sizes", "fg_get_mesh_array", "fg_get_side_to_elem", "fg_set_state",
            "fg_get_state", "fg_state_device_ptr", "fg_time_derivative", "fg_calc_timestep", "fg_get_dt_elem", "fg_timestep_lserkw2", "fg_run",
            "fg_get_gradients", "fg_get_stream", "fg_launch_count", "fg_debug_array", "fg_profile_enable", "fg_profile_read", "fg_probe_fp64",
@@ -60,6 +60,7 @@ def load(path=None):
     L.fg_overintegrate_state.argtypes = [P]
     L.fg_get_config.argtypes = [P, P]
     L.fg_lserk_table.argtypes = [I, P, P, P, P, P, P]
+    L.fg_set_time.argtypes = [P, P]
     L.fg_hopr_sizes.argtypes = [ctypes.c_char_p, P]
     L.fg_hopr_read.argtypes = [ctypes.c_char_p, P, P, P, P, P]
     L.fg_write_state.argtypes = [P, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_double]

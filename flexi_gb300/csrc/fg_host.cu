@@ -84,6 +84,11 @@ __global__ void k_scale_by_sj(const double* __restrict__ in, const double* __res
   const double s = sJ[e * n3 + i % n3];
   out[i] = mul ? in[i] * s : in[i] / s;
 }
+// start time of step k of an adjoint solve, t0 + k dt (recomputed steps of the reverse sweep)
+__global__ void k_step_time(Dev d, const double* t0, double off) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < d.nInst) d.tStep[i] = t0[i] + off;
+}
 // time of RK stage c of the current step, t_n + c dt, for the time-dependent source
 __global__ void k_stage_time(Dev d, double c) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -248,6 +253,7 @@ struct fg_handle {
   OverintDev ov{};
   OverintDev ovT{};  // the transposed filter (adjoint of overintegration): F^T, or VUN^T / VNU^T in the roles of VNU / VUN
   double* adjWov = nullptr;  // [e][5][n3] cotangent of Ut carried through the transposed filter
+  double* adjT0 = nullptr;   // [nInst] time at the start of the last fg_adjoint_forward (time-dependent source)
   int NU = 0;
   // mortar interfaces: operators and the device copy of the mortar table (Dev::nMortars > 0)
   MortarDev mort{};
@@ -751,7 +757,6 @@ const char* adjoint_unsupported(const fg_config& c) {
 int ensure_adjoint(fg_handle* h) {
   if (h->haveAdj) return 0;
   if (h->d.nMortars > 0) return fail(h, FG_ERR_CONFIG, "the adjoint does not support mortar interfaces");
-  if (h->d.srcPar) return fail(h, FG_ERR_CONFIG, "the adjoint does not support exact-function sources");
   const int n = h->M.n, n2 = n * n, n3 = n2 * n, nE = h->M.nElems, nS = h->M.nSides;
   AdjDev& a = h->a;
   double* W = nullptr;
@@ -1271,8 +1276,17 @@ static int adjoint_alloc_common(fg_handle* h, int segSteps) {
 }
 
 // ns fixed-dt steps forward from the state in d.U (nothing recorded)
-static void adjoint_advance(fg_handle* h, int ns) {
+// stage times of step k of the adjoint solve for the source (no-op without one)
+static void adjoint_step_time(fg_handle* h, int k) {
+  if (!h->d.srcPar) return;
+  k_step_time<<<(h->d.nInst + 127) / 128, 128, 0, h->st>>>(h->d, h->adjT0, k * h->adjDt);
+  h->launches += 1;
+}
+
+// ns forward steps from step firstStep of the adjoint solve
+static void adjoint_advance(fg_handle* h, int ns, int firstStep) {
   for (int s = 0; s < ns; ++s) {
+    adjoint_step_time(h, firstStep + s);
     launch_step_setup(h, 1, h->adjDt, false);
     launch_lserk(h);
   }
@@ -1281,7 +1295,7 @@ static void adjoint_advance(fg_handle* h, int ns) {
 // reverse ns steps that start from the state Ustart (device; may be d.U itself): recompute their stage
 // states (and intermediates), then run the transposed stages in reverse, accumulating into a.Ub (the
 // running state cotangent), a.muElemb, adjFbar
-static int adjoint_reverse_segment(fg_handle* h, const double* Ustart, int ns, const AdjDev& a, bool bulkAdj) {
+static int adjoint_reverse_segment(fg_handle* h, const double* Ustart, int ns, const AdjDev& a, bool bulkAdj, int firstStep) {
   const int n3 = h->M.n * h->M.n * h->M.n;
   const long long cnt = (long long)h->M.nElems * 5 * n3;
   const size_t bytes = (size_t)cnt * sizeof(double);
@@ -1290,10 +1304,12 @@ static int adjoint_reverse_segment(fg_handle* h, const double* Ustart, int ns, c
   const int nI = h->d.nInst;
   if (Ustart != h->d.U) CUDA_TRY(cudaMemcpyAsync(h->d.U, Ustart, bytes, cudaMemcpyDeviceToDevice, h->st));
   for (int s = 0; s < ns; ++s) {
+    adjoint_step_time(h, firstStep + s);
     launch_step_setup(h, 1, dt, false);
     CUDA_TRY(cudaMemcpyAsync(h->adjBulkHist + (size_t)s * nI, h->d.bulkVel, sizeof(double) * nI, cudaMemcpyDeviceToDevice, h->st));
     for (int k = 1; k <= h->nStages; ++k) {
       const size_t slot = (size_t)s * h->nStages + k - 1;
+      if (h->d.srcPar) { k_stage_time<<<(nI + 127) / 128, 128, 0, h->st>>>(h->d, h->RKc[k]); h->launches += 1; }
       CUDA_TRY(cudaMemcpyAsync(h->adjStage[slot], h->d.U, bytes, cudaMemcpyDeviceToDevice, h->st));
       if (h->adjKeepInter) {
         // the stage writes its intermediates into the slot; the state is updated in place as usual
@@ -1359,14 +1375,14 @@ static int revolve_reverse(RevolveRun& R, int l, int r, int slotL, int s) {
   fg_handle* h = R.h;
   if (r - l == 1) {
     h->adjRecomputed += 1;
-    return adjoint_reverse_segment(h, h->adjSlots[slotL], 1, R.a, R.bulkAdj);
+    return adjoint_reverse_segment(h, h->adjSlots[slotL], 1, R.a, R.bulkAdj, l);
   }
   if (s == 0) {  // no free slot: restart from U_l for every step
     for (int i = r - 1; i >= l; --i) {
       CUDA_TRY(cudaMemcpyAsync(h->d.U, h->adjSlots[slotL], R.bytes, cudaMemcpyDeviceToDevice, h->st));
-      adjoint_advance(h, i - l);
+      adjoint_advance(h, i - l, l);
       h->adjRecomputed += i - l + 1;
-      if (int e = adjoint_reverse_segment(h, h->d.U, 1, R.a, R.bulkAdj)) return e;
+      if (int e = adjoint_reverse_segment(h, h->d.U, 1, R.a, R.bulkAdj, i)) return e;
     }
     return 0;
   }
@@ -1378,7 +1394,7 @@ static int revolve_reverse(RevolveRun& R, int l, int r, int slotL, int s) {
     slotM = R.freeSlots.back();
     R.freeSlots.pop_back();
     CUDA_TRY(cudaMemcpyAsync(h->d.U, h->adjSlots[slotL], R.bytes, cudaMemcpyDeviceToDevice, h->st));
-    adjoint_advance(h, m - l);
+    adjoint_advance(h, m - l, l);
     h->adjRecomputed += m - l;
     CUDA_TRY(cudaMemcpyAsync(h->adjSlots[slotM], h->d.U, R.bytes, cudaMemcpyDeviceToDevice, h->st));
   }
@@ -1417,6 +1433,11 @@ int fg_adjoint_forward(fg_handle* h, int nSteps, double dt, int ckptEvery) {
     if (int r = adjoint_alloc_common(h, ckptEvery)) { free_adjoint_store(h); return r; }
   }
   h->launches = 0;
+  if (h->d.srcPar) {  // the source's stage times in the reverse sweep start from the solve's start time
+    if (!h->adjT0)
+      if (int r = dalloc(h, h->adjT0, (size_t)h->d.nInst)) return r;
+    CUDA_TRY(cudaMemcpyAsync(h->adjT0, h->dTime, sizeof(double) * h->d.nInst, cudaMemcpyDeviceToDevice, h->st));
+  }
   size_t spineIdx = 0;
   for (int step = 0; step < nSteps; ++step) {
     if (binomial) {
@@ -1478,7 +1499,7 @@ int fg_adjoint_reverse(fg_handle* h, const double* UbarT, double* Ubar0, double*
     for (int seg = nCk - 1; seg >= 0; --seg) {
       const int s0 = seg * h->adjEvery, ns = std::min(h->adjEvery, h->adjSteps - s0);
       h->adjRecomputed += ns;
-      if (int e = adjoint_reverse_segment(h, h->adjCkpt[seg], ns, a, bulkAdj)) return e;
+      if (int e = adjoint_reverse_segment(h, h->adjCkpt[seg], ns, a, bulkAdj, s0)) return e;
     }
   }
   CUDA_TRY(cudaGetLastError());
@@ -1720,6 +1741,12 @@ int fg_run(fg_handle* h, int nSteps, double* t) {
   if (t) CUDA_TRY(cudaMemcpy(t, h->dTime, sizeof(double) * h->d.nInst, cudaMemcpyDeviceToHost));
   h->launches = perStep;
   (void)perStep;
+  return FG_OK;
+}
+
+int fg_set_time(fg_handle* h, const double* t) {
+  if (!h || !h->haveMesh || !t) return fail(h, FG_ERR_STATE, "fg_set_time needs a mesh and times");
+  CUDA_TRY(cudaMemcpy(h->dTime, t, sizeof(double) * h->d.nInst, cudaMemcpyHostToDevice));
   return FG_OK;
 }
 

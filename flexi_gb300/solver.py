@@ -148,6 +148,11 @@ class Flexi:
         b = np.ascontiguousarray(Ja_slave, np.float64)
         self._check(self.L.fg_set_face_metrics(self.h, _p(a), _p(b)), "fg_set_face_metrics")
 
+    def set_time(self, t):
+        """fg_set_time: the device-side time of every instance (start of fg_run / fg_adjoint_forward)."""
+        tt = np.ascontiguousarray(np.broadcast_to(np.asarray(t, np.float64), (max(1, getattr(self, "n_inst", 1)),)))
+        self._check(self.L.fg_set_time(self.h, _p(tt)), "fg_set_time")
+
     def get_config(self):
         """fg_get_config: the configuration the handle runs with (BR2 turns doWeakLifting off, lifting.f90:137-139)."""
         c = _lib.FgConfig()

@@ -214,6 +214,10 @@ int fg_timestep_lserkw2(fg_handle* h, double* t, double dt);
  * per-instance times, which start at 0 on the first call and continue on later calls. */
 int fg_run(fg_handle* h, int nSteps, double* t);
 
+/* Sets the device-side time of every instance (t[nInst]), the time fg_run and fg_adjoint_forward start from
+ * (the restart time of a FLEXI run); it matters only with a time-dependent source (IniExactFunc 4). */
+int fg_set_time(fg_handle* h, const double* t);
+
 /* Lifted gradients of the last right-hand side, gradUx/gradUy/gradUz(4,0:N,0:N,0:N,nElems) of the
  * lifting variables (v1,v2,v3,T) (lifting_vars.f90, PP_OPTLIFT layout). */
 int fg_get_gradients(fg_handle* h, double* gx, double* gy, double* gz);

@@ -203,3 +203,31 @@ def test_binomial_checkpointing_matches_uniform():
             f.adjoint_reverse(w)
     assert _binomial_recomputations(n, 1) == n * (n + 1) // 2
     assert _binomial_recomputations(n, n + 1) == n
+
+
+def test_lserk_adjoint_with_time_dependent_source():
+    """Exact function 4 with its source (stage times t + RKc dt): the reverse sweep recomputes its steps at
+    the times of the forward solve (started at fg_set_time's t = 0, as the oracle's tangent solve starts);
+    the dot-product test against the oracle's exact tangent of the solve holds at 1e-10."""
+    adv = (0.3, 0.3, 0.3)
+    c = make_config(N=3, NodeType="gauss", SplitDG="weak", Riemann="roeentropyfix", Lifting="br1", mu0=5e-3, R=287.058,
+                    CFLScale=0.5, DFLScale=0.5, IniExactFunc=4, AdvVel=adv)
+    m = fmesh.cartesian_box((3, 3, 3), (-1.0,) * 3, (1.0,) * 3)
+    f = Flexi(c, m)
+    U0 = perturb_state(testcases.sine_wave_state(f.elem_xgp(), 0.0, adv), seed=1, amp=0.05)
+    f.U = U0
+    dt = float(np.atleast_1d(f.CalcTimeStep()[0])[0])
+    rng = np.random.default_rng(9)
+    w = rng.standard_normal(U0.shape)
+    for every in (3, N_STEPS):
+        f.set_time(0.0)
+        f.U = U0
+        f.adjoint_forward(N_STEPS, dt, every)
+        Ub0, _ = f.adjoint_reverse(w)
+        V = rng.standard_normal(U0.shape) * np.abs(U0).max(axis=(0, 1, 2, 3))
+        o = orc.Oracle(oracle_cfg(f.cfg), m)
+        o.set_state(U0)
+        JV = o.jvp_solve(V, N_STEPS, dt)
+        lhs, rhs = float((JV * w).sum()), float((Ub0 * V).sum())
+        assert abs(lhs - rhs) <= 1e-10 * float(np.abs(JV * w).sum()), (every, lhs, rhs)
+    f.close()
