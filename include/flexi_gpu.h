@@ -250,7 +250,8 @@ int fg_set_elem_mu_scale(fg_handle* h, const double* scale);
  * in the layout of U (host arrays), and optionally muScaleBar[nElems] = d<W, Ut>/d(scale). The transposed
  * Jacobian is that of the discrete operator the GPU evaluates (the reference's implicit solver only forms
  * J V by finite differences, implicit.f90:MatrixVector). t is unused (the exact-function source does not
- * depend on U; handles with it are refused). The bulk velocity of a channel body force is held fixed.
+ * depend on U; the LSERK adjoint recomputes its steps at the forward's stage times). The bulk velocity of a
+ * channel body force is held fixed.
  * Supported: weak form and split form PI (Gauss-Lobatto, N = 1, 3, 7), N <= 7, LF/HLLC/Roe/RoeEntropyFix,
  * strong BR1/BR2 lifting, both overintegration types (the transposed filter), walls 3/4; no mortars. */
 int fg_vjp_time_derivative(fg_handle* h, double t, const double* W, double* V, double* muScaleBar);
