@@ -327,7 +327,9 @@ __host__ __device__ __forceinline__ void riemann_rotated(int solver, int splitDG
     auto fix = [](double a, double al, double ar) {
       const double da = fmax(0.0, fmax(a - al, ar - a));
       const double aa = fabs(a);
-      return (aa < da) ? 0.5 * (a * a / da + da) : aa;
+      double e = aa;
+      if (aa < da) e = 0.5 * (a * a / da + da);  // a branch: the division only where the fix applies
+      return e;
     };
     e0 = fix(a0, L.v1 - cL, R.v1 - cR);
     e1 = fix(a1, L.v1, R.v1);
