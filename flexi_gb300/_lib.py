@@ -14,14 +14,22 @@ class FgConfig(ctypes.Structure):
                 ("R", ctypes.c_double), ("Pr", ctypes.c_double), ("mu0", ctypes.c_double), ("CFLScale", ctypes.c_double),
                 ("DFLScale", ctypes.c_double), ("doTCSource", ctypes.c_int), ("dpdx", ctypes.c_double), ("TimeDiscMethod", ctypes.c_int),
                 ("OverintegrationType", ctypes.c_int), ("NUnder", ctypes.c_int), ("IniExactFunc", ctypes.c_int),
-                ("AdvVel", ctypes.c_double * 3), ("IniFrequency", ctypes.c_double), ("IniAmplitude", ctypes.c_double)]
+                ("AdvVel", ctypes.c_double * 3), ("IniFrequency", ctypes.c_double), ("IniAmplitude", ctypes.c_double),
+                ("TEnd", ctypes.c_double), ("Analyze_dt", ctypes.c_double), ("dtmin", ctypes.c_double), ("dtkill", ctypes.c_double),
+                ("nCalcTimeStepMax", ctypes.c_int), ("maxIter", ctypes.c_int)]
+
+
+class FgTimeDiscState(ctypes.Structure):
+    """fg_timedisc_state: per-instance state of the time loop."""
+    _fields_ = [("t", ctypes.c_double), ("dt", ctypes.c_double), ("dtMin", ctypes.c_double), ("iter", ctypes.c_longlong),
+                ("atAnalyze", ctypes.c_int), ("finished", ctypes.c_int), ("nDtLimited", ctypes.c_int)]
 
 
 EXPORTS = ["fg_config_default", "fg_config_from_ini", "fg_create", "fg_destroy", "fg_last_error", "fg_build_mesh", "fg_build_mesh_mortar", "fg_set_mesh", "fg_set_mesh_mortar", "fg_set_face_metrics", "fg_overintegrate_state",
            "fg_get_config", "fg_lserk_table", "fg_set_time", "fg_hopr_sizes", "fg_hopr_read", "fg_write_state", "fg_read_state", "fg_io_last_error",
            "fg_set_instance_mu0", "fg_get_elem_xgp", "fg_get_sizes", "fg_get_mesh_array", "fg_get_side_to_elem", "fg_set_state",
            "fg_get_state", "fg_state_device_ptr", "fg_time_derivative", "fg_calc_timestep", "fg_get_dt_elem", "fg_timestep_lserkw2", "fg_run",
-           "fg_get_gradients", "fg_get_stream", "fg_launch_count", "fg_debug_array", "fg_profile_enable", "fg_profile_read", "fg_probe_fp64",
+           "fg_get_gradients", "fg_get_stream", "fg_launch_count", "fg_get_timedisc_state", "fg_debug_array", "fg_profile_enable", "fg_profile_read", "fg_probe_fp64",
            "fg_time_derivative_noalloc", "fg_set_elem_mu_scale", "fg_vjp_time_derivative", "fg_adjoint_forward", "fg_adjoint_reverse",
            "fg_set_body_force_field", "fg_wall_shear", "fg_jvp_time_derivative",
            "fg_adjoint_recomputed_steps", "fg_autotune", "fg_autotune_choice",
@@ -80,6 +88,7 @@ def load(path=None):
     L.fg_get_dt_elem.argtypes = [P, P, P]
     L.fg_timestep_lserkw2.argtypes = [P, ctypes.POINTER(D), D]
     L.fg_run.argtypes = [P, I, P]
+    L.fg_get_timedisc_state.argtypes = [P, I, P]
     L.fg_get_gradients.argtypes = [P, P, P, P]
     L.fg_get_stream.argtypes = [P, ctypes.POINTER(P)]
     L.fg_launch_count.argtypes = [P]

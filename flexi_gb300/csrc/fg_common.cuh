@@ -87,6 +87,7 @@ struct Dev {
   double* mortarLift;  // [m][12][n2] BR1 lifting flux times normal (4*dir + var) projected onto big side m
   int* err;        // [1] sticky error word
   double* dtElem;  // [2][nElems] convective and viscous element time-step limits of the last CALCTIMESTEP
+  const int* dtSkip;  // [nInst] nonzero: the instance needs no CALCTIMESTEP in this step (null: every instance does)
 };
 
 // Overintegration (overintegration.f90): type 1 the modal cut-off filter F = Vdm_Leg diag(1..1,0..0) sVdm_Leg

@@ -76,6 +76,121 @@ __global__ void k_finish_step(Dev d, const double* bulkPart, const int* instStar
     tInst[i] += dt;
   }
 }
+// Time-loop bookkeeping of fg_run per instance (timedisc_vars.f90: tAnalyze, dt_minOld, dt, dt_Min(DT_MIN),
+// nCalcTimeStep, doAnalyze/doFinalize, iter, nDtLimited) and the parameters of InitTimeDisc.
+enum { TD_HOLD = 1, TD_DONE = 2 };  // flags: the last step ended on an analysis time / at TEnd or maxIter
+struct TimeDiscDev {
+  double* tAnalyze;
+  double* dtMinOld;
+  double* dtPrev;  // the time step of the last step (reused while nCalc >= 1)
+  double* dtMin;   // dt_Min(DT_MIN) of the last CALCTIMESTEP
+  int* nCalc;
+  int* flags;
+  int* skip;       // Dev::dtSkip of the next step
+  int* nDtLimited;
+  long long* iter;
+  double tEnd, analyzeDt, dtmin, dtkill;
+  int nCalcMax;
+  long long maxIter;
+};
+// InitTimeStep state at the instance times t (timedisc.f90:105-112, timedisc_func.f90:194-195)
+__global__ void k_timedisc_reset(TimeDiscDev td, const double* t, int nInst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nInst) return;
+  td.tAnalyze[i] = fmin(t[i] + td.analyzeDt, td.tEnd);
+  td.dtMinOld[i] = -999.;
+  td.dtPrev[i] = 0.;
+  td.dtMin[i] = 0.;
+  td.nCalc[i] = 0;
+  td.flags[i] = 0;
+  td.skip[i] = 0;
+  td.nDtLimited[i] = 0;
+  td.iter[i] = 0;
+}
+// start of an fg_run call: instances held at an analysis time continue (AnalyzeTimeStep has run on the host)
+__global__ void k_timedisc_release(TimeDiscDev td, int nInst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nInst) return;
+  const int f = td.flags[i] & ~TD_HOLD;
+  td.flags[i] = f;
+  td.skip[i] = (f != 0) || td.nCalc[i] >= 1;
+}
+// UpdateTimeStep (timedisc_func.f90:215-268) with EvalTimeStep (:433-454) and the step counting of TimeDisc /
+// AnalyzeTimeStep (timedisc.f90:190-212, timedisc_func.f90:316-380), one thread per instance, after k_dt has
+// written CALCTIMESTEP's dt (unless the instance skips it). Also the bulk velocity of CalcForcing.
+__global__ void k_update_timestep(Dev d, TimeDiscDev td, const double* bulkPart, const int* instStart, const double* instVol, double* tInst,
+                                  int doBulk) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.nInst) return;
+  if (doBulk) {
+    double s = 0.;
+    for (int e = instStart[i]; e < instStart[i + 1]; ++e) s += bulkPart[e];
+    d.bulkVel[i] = s / instVol[i];
+  }
+  const double t = tInst[i];
+  if (d.tStep) d.tStep[i] = t;
+  const int fl = td.flags[i];
+  // held, finished, or the run stopped on an error: the stages run with dt = 0 and leave the state as it is
+  if ((fl & (TD_HOLD | TD_DONE)) || *(volatile int*)d.err != 0) {
+    d.dt[i] = 0.;
+    td.skip[i] = 1;
+    return;
+  }
+  double dt;
+  bool ana = false, fin = false;
+  if (td.nCalc[i] >= 1) {  // no time-step update in this step
+    td.nCalc[i] -= 1;
+    dt = td.dtPrev[i];
+  } else {
+    double dtm = d.dt[i];  // CALCTIMESTEP
+    if (!(dtm > 0.) || dtm > 1e300) {
+      set_error(d.err, 2);
+      d.dt[i] = 0.;
+      td.skip[i] = 1;
+      return;
+    }
+    if (dtm < td.dtmin) {
+      dtm = td.dtmin;
+      td.nDtLimited[i] += 1;
+    }
+    td.dtMin[i] = dtm;
+    if (dtm < td.dtkill) {  // "Critical Kill timestep reached": keep the state of time t
+      set_error(d.err, 4);
+      d.dt[i] = 0.;
+      td.skip[i] = 1;
+      return;
+    }
+    const double dA = td.tAnalyze[i] - t, dE = td.tEnd - t;
+    const double m = fmin(dtm, fmin(dA, dE));
+    if (m == dA) ana = true;
+    if (m == dE) ana = fin = true;
+    dt = dtm;  // MINVAL(dt_min, MASK=dt_min > 0); dtm > 0 here
+    if (dA > 0.) dt = fmin(dt, dA);
+    if (dE > 0.) dt = fmin(dt, dE);
+    // steps until the next update: fewer the more dt changed since the last update
+    const double q = td.dtMinOld[i] / dt - 1.;
+    const double lg = fabs(log10(q * q * 100. + 2.220446049250313e-16));
+    td.nCalc[i] = (lg >= (double)td.nCalcMax ? td.nCalcMax : (int)floor(lg)) - 1;
+    td.dtMinOld[i] = dt;
+    // stretch the step if the next analysis / the end would otherwise follow after less than dt/100
+    if (dA - dt < dt / 100. && dA > 0.) { dt = dA; ana = true; }
+    if (dE - dt < dt / 100. && dE > 0.) { dt = dE; ana = fin = true; }
+    td.dtPrev[i] = dt;
+  }
+  d.dt[i] = dt;
+  tInst[i] = t + dt;
+  const long long it = td.iter[i] + 1;
+  td.iter[i] = it;
+  if (it == td.maxIter) ana = fin = true;
+  int nf = fl;
+  if (ana) {
+    td.tAnalyze[i] = fmin(td.tAnalyze[i] + td.analyzeDt, td.tEnd);
+    nf |= TD_HOLD;
+  }
+  if (fin) nf |= TD_DONE;
+  td.flags[i] = nf;
+  td.skip[i] = (nf != 0) || td.nCalc[i] >= 1;
+}
 // out = in * sJ (mul = 1) or in / sJ (mul = 0), per node of [e][5][n3] arrays
 __global__ void k_scale_by_sj(const double* __restrict__ in, const double* __restrict__ sJ, double* out, int n3, long long cnt, int mul) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -245,6 +360,7 @@ struct fg_handle {
   int* dInstStart = nullptr;
   double* dInstVol = nullptr;
   double* dTime = nullptr;
+  TimeDiscDev td{};  // time-loop bookkeeping of fg_run
   double* dStage = nullptr;  // staging for layout conversion (size nElems*5*n3)
   double RKA[21]{}, RKb[21]{}, RKc[21]{};
   int nStages = 5;
@@ -628,6 +744,24 @@ int upload_mesh(fg_handle* h) {
   if ((r = upload(h, h->dInstStart, start))) return r;
   if ((r = upload(h, h->dInstVol, M.instVol))) return r;
   if ((r = upload(h, h->dTime, zero))) return r;
+  {
+    TimeDiscDev& td = h->td;
+    const int nI = M.nInst;
+    if ((r = dalloc(h, td.tAnalyze, nI)) || (r = dalloc(h, td.dtMinOld, nI)) || (r = dalloc(h, td.dtPrev, nI)) || (r = dalloc(h, td.dtMin, nI)) ||
+        (r = dalloc(h, td.nCalc, nI)) || (r = dalloc(h, td.flags, nI)) || (r = dalloc(h, td.skip, nI)) || (r = dalloc(h, td.nDtLimited, nI)) ||
+        (r = dalloc(h, td.iter, nI)))
+      return r;
+    const fg_config& c = h->cfg;
+    td.tEnd = c.TEnd;
+    td.analyzeDt = c.Analyze_dt > 0. ? c.Analyze_dt : c.TEnd;  // analyze.f90:127-130
+    td.dtmin = c.dtmin;
+    td.dtkill = c.dtkill;
+    td.nCalcMax = c.nCalcTimeStepMax;
+    td.maxIter = c.maxIter;
+    CUDA_TRY(cudaDeviceSynchronize());
+    k_timedisc_reset<<<(nI + 127) / 128, 128>>>(td, h->dTime, nI);
+    CUDA_TRY(cudaGetLastError());
+  }
   if ((r = dalloc(h, h->dStage, (size_t)nE * 12 * n3))) return r;
   // the uploads above run on the legacy default stream, which the solver's non-blocking stream does not
   // order against: finish them before any kernel can read the arrays
@@ -695,6 +829,14 @@ void launch_step_setup(fg_handle* h, int mode, double fixedDt, bool advanceTime)
   }
   if (computeDt) {
     k_fill<<<(nI + 127) / 128, 128, 0, h->st>>>(d.dt, INFINITY, nI);
+    if (advanceTime) {  // the TimeDisc loop: CALCTIMESTEP only for instances that update dt, then UpdateTimeStep
+      Dev dd = d;
+      dd.dtSkip = h->td.skip;
+      { ProfScope p(h, 4); h->K.dt(dd, h->B, h->dMetAdv, h->dMetVisc, h->cflEff, h->dflEff, doBulk ? h->dBulkPart : nullptr, h->dWVol, h->st); }
+      k_update_timestep<<<(nI + 127) / 128, 128, 0, h->st>>>(d, h->td, h->dBulkPart, h->dInstStart, h->dInstVol, h->dTime, doBulk);
+      h->launches += 3;
+      return;
+    }
     { ProfScope p(h, 4); h->K.dt(d, h->B, h->dMetAdv, h->dMetVisc, h->cflEff, h->dflEff, h->dBulkPart, h->dWVol, h->st); }
     h->launches += 2;
   } else {
@@ -723,6 +865,7 @@ int check_err(fg_handle* h) {
   CUDA_TRY(cudaMemcpyAsync(&e, h->d.err, sizeof(int), cudaMemcpyDeviceToHost, h->st));
   CUDA_TRY(cudaStreamSynchronize(h->st));
   if (e == 1) return fail(h, FG_ERR_NAN, "NaN density found");
+  if (e == 4) return fail(h, FG_ERR_DTKILL, "time step below dtkill (critical kill time step reached)");
   if (e) return fail(h, FG_ERR_DT, "non-finite or non-positive time step");
   return 0;
 }
@@ -848,6 +991,7 @@ int fg_config_default(fg_config* c) {
   c->CFLScale = 0.9; c->DFLScale = 0.9; c->doTCSource = 0; c->dpdx = -1.; c->TimeDiscMethod = 0;
   c->OverintegrationType = 0; c->NUnder = -1;
   c->IniExactFunc = 0; c->AdvVel[0] = c->AdvVel[1] = c->AdvVel[2] = 0.; c->IniFrequency = 1.; c->IniAmplitude = 0.1;
+  c->TEnd = INFINITY; c->Analyze_dt = 0.; c->dtmin = -1.; c->dtkill = -1.; c->nCalcTimeStepMax = 1; c->maxIter = -1;
   return FG_OK;
 }
 
@@ -899,6 +1043,12 @@ int fg_config_from_ini(const char* text, fg_config* c) {
       else if (key == "iniexactfunc") c->IniExactFunc = std::stoi(val);
       else if (key == "inifrequency") c->IniFrequency = std::stod(val);
       else if (key == "iniamplitude") c->IniAmplitude = std::stod(val);
+      else if (key == "tend") c->TEnd = std::stod(val);
+      else if (key == "analyze_dt") c->Analyze_dt = std::stod(val);
+      else if (key == "dtmin") c->dtmin = std::stod(val);
+      else if (key == "dtkill") c->dtkill = std::stod(val);
+      else if (key == "ncalctimestepmax") c->nCalcTimeStepMax = std::stoi(val);
+      else if (key == "maxiter") c->maxIter = std::stoi(val);
       else if (key == "advvel") {  // (/a,b,c/)
         std::string v = val;
         for (char& ch : v) if (ch == '(' || ch == ')' || ch == '/' || ch == ',') ch = ' ';
@@ -932,6 +1082,8 @@ int fg_create(const fg_config* cfg, fg_handle** out) {
           "toulorgerk4-8c, toulorgerk3-7c, toulorgerk4-8f)";
   else if (c.OverintegrationType < 0 || c.OverintegrationType > 2) why = "OverintegrationType must be 0 (none), 1 (cutoff) or 2 (conscutoff)";
   else if (c.OverintegrationType > 0 && c.NUnder < -1) why = "NUnder must be >= 0";
+  else if (c.nCalcTimeStepMax < 1) why = "nCalcTimeStepMax must be >= 1";
+  else if (!(c.TEnd > 0.)) why = "TEnd must be > 0";
   if (!why.empty()) { delete h; return fail(nullptr, FG_ERR_CONFIG, why); }
   h->K = get_kernel_set(c.N + 1, c.NodeType == FG_NODE_GAUSS_LOBATTO);
   h->Kdef = h->K;
@@ -1711,6 +1863,7 @@ int fg_run(fg_handle* h, int nSteps, double* t) {
   if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
   if (nSteps < 0) return fail(h, FG_ERR_CONFIG, "nSteps < 0");
   CUDA_TRY(cudaMemsetAsync(h->d.err, 0, sizeof(int), h->st));
+  k_timedisc_release<<<(h->d.nInst + 127) / 128, 128, 0, h->st>>>(h->td, h->d.nInst);
   if (h->profiling) {  // direct launches with per-kernel events
     h->launches = 0;
     for (int s = 0; s < nSteps; ++s) {
@@ -1746,7 +1899,36 @@ int fg_run(fg_handle* h, int nSteps, double* t) {
 
 int fg_set_time(fg_handle* h, const double* t) {
   if (!h || !h->haveMesh || !t) return fail(h, FG_ERR_STATE, "fg_set_time needs a mesh and times");
-  CUDA_TRY(cudaMemcpy(h->dTime, t, sizeof(double) * h->d.nInst, cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpyAsync(h->dTime, t, sizeof(double) * h->d.nInst, cudaMemcpyHostToDevice, h->st));
+  k_timedisc_reset<<<(h->d.nInst + 127) / 128, 128, 0, h->st>>>(h->td, h->dTime, h->d.nInst);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(h->st));
+  return FG_OK;
+}
+
+int fg_get_timedisc_state(fg_handle* h, int nInst, fg_timedisc_state* out) {
+  if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
+  if (!out || nInst < 1 || nInst > h->d.nInst) return fail(h, FG_ERR_CONFIG, "fg_get_timedisc_state: nInst must be in 1..number of instances");
+  const int n = nInst;
+  std::vector<double> t(n), dt(n), dtMin(n);
+  std::vector<long long> it(n);
+  std::vector<int> fl(n), lim(n);
+  CUDA_TRY(cudaStreamSynchronize(h->st));
+  CUDA_TRY(cudaMemcpy(t.data(), h->dTime, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(dt.data(), h->td.dtPrev, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(dtMin.data(), h->td.dtMin, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(it.data(), h->td.iter, sizeof(long long) * n, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(fl.data(), h->td.flags, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(lim.data(), h->td.nDtLimited, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < n; ++i) {
+    out[i].t = t[i];
+    out[i].dt = dt[i];
+    out[i].dtMin = dtMin[i];
+    out[i].iter = it[i];
+    out[i].atAnalyze = (fl[i] & TD_HOLD) ? 1 : 0;
+    out[i].finished = (fl[i] & TD_DONE) ? 1 : 0;
+    out[i].nDtLimited = lim[i];
+  }
   return FG_OK;
 }
 

@@ -1568,7 +1568,9 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_dt(Dev d, Basis B, const 
   const int e0 = blockIdx.x * EPB;
   const int t = threadIdx.x;
   const int es = NPT > 1 ? 0 : t / n3, x = NPT > 1 ? t : t - es * n3, e = e0 + es;
-  const bool active = es < EPB && e < d.nElems;
+  // elements of instances that reuse their time step (nCalcTimeStep >= 1, held or finished) are skipped
+  // unless the bulk velocity needs their nodes
+  const bool active = es < EPB && e < d.nElems && (bulkPart || !d.dtSkip || !d.dtSkip[d.elemInst[e]]);
   double v7[7] = {0., 0., 0., 0., 0., 0., 0.};
   if (active) {
 #pragma unroll 1

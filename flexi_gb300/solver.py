@@ -22,7 +22,11 @@ SPLIT = {"none": -1, "weak": -1, "sd": 0, "pi": 4}
 
 
 class FlexiError(RuntimeError):
-    pass
+    """A failed call of the C ABI; `code` is its FG_ERR_* status (0 where no call failed)."""
+
+    def __init__(self, msg, code=0):
+        super().__init__(msg)
+        self.code = code
 
 
 def _p(a):
@@ -85,7 +89,7 @@ class Flexi:
 
     def _check(self, rc, what):
         if rc != 0:
-            raise FlexiError(f"{what} failed ({rc}): {self.L.fg_last_error(self.h).decode()}")
+            raise FlexiError(f"{what} failed ({rc}): {self.L.fg_last_error(self.h).decode()}", rc)
 
     def close(self):
         if getattr(self, "h", None):
@@ -256,6 +260,14 @@ class Flexi:
         t = np.zeros(self.n_inst)
         self._check(self.L.fg_run(self.h, int(n_steps), _p(t)), "fg_run")
         return t
+
+    def timedisc_state(self):
+        """Per-instance state of the time loop (fg_get_timedisc_state): list of dicts with t, dt, dtMin, iter,
+        atAnalyze, finished, nDtLimited."""
+        n = max(1, getattr(self, "n_inst", 1))
+        arr = (_lib.FgTimeDiscState * n)()
+        self._check(self.L.fg_get_timedisc_state(self.h, n, arr), "fg_get_timedisc_state")
+        return [{k: getattr(a, k) for k, _ in _lib.FgTimeDiscState._fields_} for a in arr]
 
     def gradients(self):
         n = self.n

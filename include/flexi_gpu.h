@@ -26,6 +26,7 @@ extern "C" {
 #define FG_ERR_STATE 4     /* call order violated (e.g. no mesh yet) */
 #define FG_ERR_NAN 5       /* NaN density found (calctimestep.f90 errType 1) */
 #define FG_ERR_DT 6        /* non-finite time step (errType 2/3) */
+#define FG_ERR_DTKILL 7    /* time step below dtkill (timedisc_func.f90:EvalTimeStep, "Critical Kill timestep reached") */
 
 /* Riemann solver ids: the integer values of riemann.f90:44-58 */
 #define FG_RIEMANN_SAME (-1)
@@ -45,7 +46,8 @@ extern "C" {
  *   Lifting 1=BR1 / 2=BR2 (CMake FLEXI_LIFTING), doWeakLifting, doConservativeLifting, etaBR2,
  *   etaBR2_wall (lifting.f90:61-83), SplitDG (splitflux.f90:77), kappa, R, Pr, mu0 (eos.f90:84-90),
  *   CFLScale, DFLScale (timedisc_func.f90:463-527), TimeDiscMethod (0 = CarpenterRK4-5, 1..5 the other low-storage schemes),
- *   and the channel body force of testcase/channel (doTCSource, dpdx). */
+ *   the channel body force of testcase/channel (doTCSource, dpdx), and the time-loop control of TimeDisc
+ *   (TEnd, Analyze_dt, dtmin, dtkill, nCalcTimeStepMax, maxIter: timedisc_func.f90:51-61, analyze.f90:49-52). */
 typedef struct fg_config {
   int N;
   int NodeType;
@@ -73,12 +75,20 @@ typedef struct fg_config {
   double AdvVel[3];         /* AdvVel of exact function 4 (its wave speed is 2 pi AdvVel(1)) */
   double IniFrequency;      /* IniFrequency (default 1) */
   double IniAmplitude;      /* IniAmplitude (default 0.1) */
+  /* time-loop control of fg_run (timedisc_func.f90:UpdateTimeStep/EvalTimeStep, timedisc.f90:190-212) */
+  double TEnd;              /* end time: the step that reaches it is clipped to it, later steps do not advance (default +inf: none) */
+  double Analyze_dt;        /* analysis interval: steps are clipped to the analysis times t0 + k Analyze_dt (<= 0: TEnd, analyze.f90:127) */
+  double dtmin;             /* time steps below dtmin are raised to it (default -1: off) */
+  double dtkill;            /* a time step below dtkill stops the run with FG_ERR_DTKILL (default -1: off) */
+  int nCalcTimeStepMax;     /* NCalcTimeStepMax: CALCTIMESTEP at least every nCalcTimeStepMax steps, fewer when dt varies (default 1) */
+  int maxIter;              /* maxIter: an instance stops after this many steps (default -1: no limit) */
 } fg_config;
 
 typedef struct fg_handle fg_handle;
 
 /* Defaults of the reference (Riemann=RoeEntropyFix, SplitDG=PI, Lifting=BR1, etaBR2=2, kappa=1.4,
- * R=287.058, Pr=0.72, mu0=0, CFLScale=DFLScale=0.9, CarpenterRK4-5, no overintegration). */
+ * R=287.058, Pr=0.72, mu0=0, CFLScale=DFLScale=0.9, CarpenterRK4-5, no overintegration, Analyze_dt=0,
+ * dtmin=dtkill=-1, nCalcTimeStepMax=1, maxIter=-1); TEnd (mandatory in the reference) defaults to +inf. */
 int fg_config_default(fg_config* cfg);
 
 /* Parses the keys above from parameter_flexi.ini text (readintools.f90:read_options syntax:
@@ -203,19 +213,38 @@ int fg_calc_timestep(fg_handle* h, double* dt, int* errType);
  * CFL*2/sum(lambda_conv) and viscous limit DFL*4/sum(lambda_visc) (+inf when mu0 = 0), nElems each. */
 int fg_get_dt_elem(fg_handle* h, double* dtConv, double* dtVisc);
 
-/* TimeStepByLSERKW2 (timestep.f90:82) with CarpenterRK4-5 (timedisc_vars.f90:199-214): advances the
- * state by dt (all instances use the same dt here); t is advanced by dt. Includes CalcForcing
+/* TimeStepByLSERKW2 (timestep.f90:82) with the low-storage scheme of cfg.TimeDiscMethod (timedisc_vars.f90:137-457):
+ * advances the state by dt (all instances use the same dt here); t is advanced by dt. Includes CalcForcing
  * (testcase/channel/testcase.f90:262) when the channel body force is active. */
 int fg_timestep_lserkw2(fg_handle* h, double* t, double dt);
 
 /* TimeDisc loop body (timedisc.f90:190-212) for nSteps steps without host synchronisation:
- * UpdateTimeStep (dt from CALCTIMESTEP, per instance), CalcForcing, TimeStepByLSERKW2; the step
- * sequence is captured once into a CUDA graph and replayed. t[inst] (nullable) receives the
+ * UpdateTimeStep (timedisc_func.f90:215-268, per instance, on the device: CALCTIMESTEP, dtmin/dtkill of
+ * EvalTimeStep :433-454, clipping to the next analysis time and to TEnd with the dt/100 stretch, the
+ * nCalcTimeStepMax reuse of dt), CalcForcing, TimeStepByLSERKW2; the step sequence is captured once into a
+ * CUDA graph and replayed. An instance whose step ends on an analysis time (doAnalyze) holds there for the
+ * rest of the call and continues on the next call; one that reached TEnd or maxIter (doFinalize) no longer
+ * advances (fg_set_time starts a new run); fg_get_timedisc_state reports which. A time step below dtkill stops the
+ * instance that found it at its state then, the other instances after at most one more step, and returns FG_ERR_DTKILL. t[inst] (nullable) receives the
  * per-instance times, which start at 0 on the first call and continue on later calls. */
 int fg_run(fg_handle* h, int nSteps, double* t);
 
+/* Per-instance state of the time loop (the reference's t, dt, dt_Min(DT_MIN), iter, doAnalyze, doFinalize,
+ * nDtLimited of timedisc_vars.f90). */
+typedef struct fg_timedisc_state {
+  double t;          /* time */
+  double dt;         /* time step of the last step */
+  double dtMin;      /* dt_Min(DT_MIN): the last CALCTIMESTEP time step, after dtmin */
+  long long iter;    /* steps since the handle's creation or the last fg_set_time */
+  int atAnalyze;     /* the last step ended on an analysis time (the next fg_run continues) */
+  int finished;      /* TEnd or maxIter reached (doFinalize) */
+  int nDtLimited;    /* steps whose time step was raised to dtmin */
+} fg_timedisc_state;
+int fg_get_timedisc_state(fg_handle* h, int nInst, fg_timedisc_state* out);
+
 /* Sets the device-side time of every instance (t[nInst]), the time fg_run and fg_adjoint_forward start from
- * (the restart time of a FLEXI run); it matters only with a time-dependent source (IniExactFunc 4). */
+ * (the restart time of a FLEXI run), and starts the time loop afresh there (InitTimeStep, timedisc.f90:105-112:
+ * next analysis time min(t + Analyze_dt, TEnd), step counter 0, no held or finished instance). */
 int fg_set_time(fg_handle* h, const double* t);
 
 /* Lifted gradients of the last right-hand side, gradUx/gradUy/gradUz(4,0:N,0:N,0:N,nElems) of the

@@ -32,8 +32,9 @@ MESH_FILE = {"oInt": os.path.join(os.path.dirname(os.path.abspath(__file__)), "g
 def test_tgv_split_regression_all_rows(case, request):
     fixture, N, node_type, nt, ne, extra = CASES[case]
     _, rows = request.getfixturevalue(fixture)
+    # tEnd = Analyze_dt = 13 as in the cases' parameter files: the last time step is clipped to tEnd
     c = make_config(N=N, NodeType=node_type, Riemann="roeentropyfix", Lifting="br1", kappa=1.4, R=71.42857, Pr=0.72, mu0=6.25e-4,
-                    **extra)
+                    TEnd=13.0, Analyze_dt=13.0, **extra)
     m = fmesh.read_hopr(MESH_FILE[case]) if case in MESH_FILE else fmesh.tgv_box(ne, ngeo=1)
     f = Flexi(c, m)
     f.U = testcases.tgv_state(f.elem_xgp(), mach=0.1, kappa=1.4, R=71.42857)
@@ -42,10 +43,17 @@ def test_tgv_split_regression_all_rows(case, request):
     f.DGTimeDerivative_weakForm(0.0)
     sJ = f.mesh_array("sJ")
     worst = 0.0
-    n_rows = rows.shape[0] - 1  # the last row is written at the clipped final time step
+    n_rows = rows.shape[0]
     for r in range(n_rows):
         if r > 0:
+            # rows every 10 steps (nAnalyzeTestCase); the last one after the step clipped to tEnd, where
+            # AnalyzeTimeStep evaluates the operator at the final state before the analysis (doAnalyze)
             t = f.TimeDisc(10)[0]
+            st = f.timedisc_state()[0]
+            assert st["finished"] == (r == n_rows - 1), (r, st)
+            if st["finished"]:
+                assert t == 13.0, t
+                f.DGTimeDerivative_weakForm(t)
             assert abs(t - rows[r, 0]) <= 1e-4 * rows[r, 0], (r, t, rows[r, 0])
         a = orc.tgv_analysis(N, nt, sJ, f.U, f.gradients(), 10, 1.4, 71.42857, 6.25e-4)
         ref = rows[r, 1:]
