@@ -324,14 +324,25 @@ __global__ void k_dev_to_fortran(const double* __restrict__ d, double* __restric
   const long long e = r / n3;
   f[t] = d[(e * nvDev + v0 + v) * n3 + x];
 }
-// FP64 FMA throughput probe
-__global__ void k_probe_dfma(double* out, double a, double b, int iters) {
-  double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+// FP64 pipe throughput probe: 8 independent chains per thread of one FP64 operation (OP 0 DFMA, 1 DADD, 2 DMUL) or of
+// the three mixed (OP 3: chain c uses operation c mod 3); every grid shape from 4 to 32 chains and 128 to 512 threads,
+// and every mix, gives the same rate on GB300
+template <int OP>
+__global__ void k_probe_fp64(double* out, double a, double b, int iters) {
+  double x[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) x[c] = threadIdx.x * 1e-3 + c;
   for (int i = 0; i < iters; ++i) {
-    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
-    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const int op = OP < 3 ? OP : c % 3;
+      x[c] = op == 0 ? fma(x[c], a, b) : op == 1 ? x[c] + b : x[c] * a;
+    }
   }
-  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+  double s = 0.;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) s += x[c];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 }  // namespace fg
 
@@ -2001,8 +2012,9 @@ int fg_profile_read(fg_handle* h, double* ms, long long* counts) {
   return FG_OK;
 }
 
-int fg_probe_fp64(double* tflops) {
+int fg_probe_fp64_pipe(double* rates) {
   fg_handle* h = nullptr;
+  if (!rates) return fail(h, FG_ERR_CONFIG, "fg_probe_fp64_pipe: rates is NULL");
   int dev = 0;
   cudaDeviceProp p;
   CUDA_TRY(cudaGetDevice(&dev));
@@ -2012,21 +2024,31 @@ int fg_probe_fp64(double* tflops) {
   CUDA_TRY(cudaMalloc(&out, sizeof(double) * blocks * threads));
   cudaEvent_t a, b;
   cudaEventCreate(&a); cudaEventCreate(&b);
-  k_probe_dfma<<<blocks, threads>>>(out, 0.999, 1e-3, 256);
-  float best = 1e30f;
-  for (int r = 0; r < 3; ++r) {
-    cudaEventRecord(a);
-    k_probe_dfma<<<blocks, threads>>>(out, 0.999, 1e-3, iters);
-    cudaEventRecord(b);
-    cudaEventSynchronize(b);
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, a, b);
-    best = std::min(best, ms);
+  void (*kern[4])(double*, double, double, int) = {k_probe_fp64<0>, k_probe_fp64<1>, k_probe_fp64<2>, k_probe_fp64<3>};
+  for (int op = 0; op < 4; ++op) {
+    kern[op]<<<blocks, threads>>>(out, 0.999, 1e-3, 256);
+    float best = 1e30f;
+    for (int r = 0; r < 3; ++r) {
+      cudaEventRecord(a);
+      kern[op]<<<blocks, threads>>>(out, 0.999, 1e-3, iters);
+      cudaEventRecord(b);
+      cudaEventSynchronize(b);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, a, b);
+      best = std::min(best, ms);
+    }
+    rates[op] = (double)blocks * threads * iters * 8 / (best * 1e-3) / 1e12;
   }
   cudaEventDestroy(a); cudaEventDestroy(b);
   cudaFree(out);
   CUDA_TRY(cudaGetLastError());
-  *tflops = (double)blocks * threads * iters * 8 * 2 / (best * 1e-3) / 1e12;
+  return FG_OK;
+}
+
+int fg_probe_fp64(double* tflops) {
+  double r[4];
+  if (int e = fg_probe_fp64_pipe(r)) return e;
+  *tflops = 2. * r[0];
   return FG_OK;
 }
 

@@ -387,3 +387,13 @@ def probe_fp64_tflops():
     if L.fg_probe_fp64(ctypes.byref(v)) != 0:
         raise FlexiError("fg_probe_fp64 failed: " + L.fg_last_error(None).decode())
     return v.value
+
+
+def probe_fp64_pipe():
+    """fg_probe_fp64_pipe: DFMA, DADD, DMUL and mixed throughput of the device's FP64 pipe (T thread-instructions/s)."""
+    L = _lib.load()
+    r = np.zeros(4)
+    if L.fg_probe_fp64_pipe(_p(r)) != 0:
+        raise FlexiError("fg_probe_fp64_pipe failed: " + L.fg_last_error(None).decode())
+    return {"dfma": float(r[0]), "dadd": float(r[1]), "dmul": float(r[2]), "mixed": float(r[3])}
+

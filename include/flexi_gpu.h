@@ -338,7 +338,11 @@ int fg_autotune_choice(const fg_handle* h, int* out);
  * fg_autotune_choice reports them; side block 64/128/256), e.g. to reproduce a tuned run. */
 int fg_set_launch_shapes(fg_handle* h, int epbPrep, int epbLift, int epbVol, int fluxBlock);
 
-/* FP64 FMA throughput probe (TFLOP/s, 2 flop per FMA) of the current device, used for the roofline. */
+/* FP64 pipe probes of the current device (no counterpart in the reference): the rate an arithmetic FP64 instruction
+ * stream attains, next to which the roofline of these FP64-bound kernels is read. fg_probe_fp64_pipe: rates[0..3] = DFMA,
+ * DADD, DMUL alone and the three mixed, in T thread-instructions per second (independent chains on every SM).
+ * fg_probe_fp64: 2 x the DFMA rate (TFLOP/s). */
+int fg_probe_fp64_pipe(double* rates);
 int fg_probe_fp64(double* tflops);
 
 /* ---- Allocation-free right-hand side (no counterpart in the reference) ----------------------------

@@ -8,7 +8,7 @@ tgv_splitgauss_reference.npz and tgv_oint_reference.npz; copies fifteen HOPR mes
 of the reference's test cases to hopr/ for the HDF5 reader.
 
 Run from the repository root in a container that has the reference mounted:
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path of the FLEXI source tree>
 """
 import os
 import sys
@@ -111,4 +111,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the FLEXI source tree>")
+    main(sys.argv[1])
