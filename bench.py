@@ -577,6 +577,7 @@ def run_ensemble(args):
     f = Flexi(c, m)
     xgp = f.elem_xgp()
     starts = np.concatenate([[0], np.cumsum(sizes.astype(np.int64) ** 3)])
+    f_n3 = (c.N + 1) ** 3
     U0 = np.concatenate([instance_state(xgp[starts[i]:starts[i + 1]], int(kind[i]), float(mach[i])) for i in range(len(sizes))])
     mu = 1.0 / re
     f.U = U0
@@ -632,8 +633,10 @@ def run_ensemble(args):
                "d2h_bytes_per_step": nbytes, "ms_per_step": el / args.steps * 1e3}
     f.close()
 
-    # the same instances, one plain solver after another (same kernels, same steps, graph-replayed per instance)
+    # the same instances, one plain solver after another (same kernels, same steps, graph-replayed per instance),
+    # with the time per instance size
     loop_ms, max_diff = 0.0, 0.0
+    per_size = {}
     for i in range(len(sizes)):
         g = Flexi(c, boxes[int(sizes[i])])
         g.U = U0[starts[i]:starts[i + 1]]
@@ -646,11 +649,29 @@ def run_ensemble(args):
         g.TimeDisc(args.steps)
         b.record(gs)
         torch.cuda.synchronize()
-        loop_ms += a.elapsed_time(b)
+        ms_i = a.elapsed_time(b)
+        loop_ms += ms_i
+        ps = per_size.setdefault(int(sizes[i]), {"instances": 0, "ms": 0.0, "dof": 0})
+        ps["instances"] += 1
+        ps["ms"] += ms_i
+        ps["dof"] += int(sizes[i]) ** 3 * f_n3
         ref = U_ens[starts[i]:starts[i + 1]]
         max_diff = max(max_diff, float(np.abs(g.U - ref).max() / np.abs(ref).max()))
         g.close()
     loop_value = len(sizes) * args.steps / (loop_ms * 1e-3)
+    ens_rate = dof * 5 * args.steps / (ms * 1e-3)
+    # per instance size: share of the loop's time and of the DOF, DOF*stage/s of an instance of that size run alone
+    # against the ensemble's rate (instances too small to fill the GPU run below it)
+    loop_breakdown = {f"{k}^3": {"instances": v["instances"], "elements": k ** 3, "dof_share": v["dof"] / dof,
+                                  "loop_time_share": v["ms"] / loop_ms,
+                                  "ms_per_step_all_instances": v["ms"] / args.steps,
+                                  "dof_stage_per_s_alone": v["dof"] * 5 * args.steps / (v["ms"] * 1e-3),
+                                  "rate_vs_ensemble": v["dof"] * 5 * args.steps / (v["ms"] * 1e-3) / ens_rate}
+                      for k, v in sorted(per_size.items())}
+    # Amdahl bound of batching: the ensemble cannot beat the loop by more than running every size class at the rate of
+    # the best-filled one
+    best = max(v["dof_stage_per_s_alone"] for v in loop_breakdown.values())
+    amdahl = loop_ms * 1e-3 / sum(v["dof"] * 5 * args.steps / best for v in per_size.values())
 
     if rank != 0:
         return
@@ -680,7 +701,11 @@ def run_ensemble(args):
             "gpu_launches": launches_per_step * args.steps, "clocks": clk, "roofline": roofline, "cpu_baseline": cpu,
             "dof_stage_per_s": dof * 5 * args.steps * ws / (ms * 1e-3),
             "loop_baseline": {"value": loop_value, "unit": "instance-steps/s", "ms_per_step": loop_ms / args.steps,
-                              "what": "the same instances advanced one after another by the plain solver (one handle per instance)"},
+                              "what": "the same instances advanced one after another by the plain solver (one handle per instance)",
+                              "per_instance_size": loop_breakdown,
+                              "batching_bound": amdahl,
+                              "batching_bound_note": "largest speed-up over the loop that batching can give: every size class "
+                                                     "run at the DOF*stage/s of the best-filled size alone"},
             "speedup_vs_loop": value / ws / loop_value, "max_rel_state_diff_vs_loop": max_diff,
             "autotune": tuned}
     print(json.dumps(line), flush=True)
@@ -799,15 +824,23 @@ def run_adjoint(args):
     (Ub0, mub), ms_rev = timed(lambda: f.adjoint_reverse(UbarT))
     clk = clocks.stop()
     L0 = 0.5 * (KE - target) ** 2
-    # central finite differences (eps = 1e-6) of the loss in seeded random directions of (U0, multipliers)
-    errs = []
+    # finite differences of the loss in seeded random directions of (U0, multipliers): the central difference with
+    # eps = 1e-6, and a Richardson-extrapolated central difference with h = 1e-4 (fourth order: truncation ~h^4, round-off
+    # of the loss / h ~1e-11), whose distance from the eps = 1e-6 quotient is that quotient's own error
+    errs, errs_rich, fd_own = [], [], []
     for k in range(args.fd_dirs):
         dU = rng.standard_normal(U0.shape) * np.abs(U0).max(axis=(0, 1, 2, 3))
         ds = rng.standard_normal(f.n_elems)
         eps = 1e-6
         fd = (loss(U0 + eps * dU, scale + eps * ds) - loss(U0 - eps * dU, scale - eps * ds)) / (2 * eps)
+        h = 1e-4
+        d1 = (loss(U0 + h * dU, scale + h * ds) - loss(U0 - h * dU, scale - h * ds)) / (2 * h)
+        d2 = (loss(U0 + 2 * h * dU, scale + 2 * h * ds) - loss(U0 - 2 * h * dU, scale - 2 * h * ds)) / (4 * h)
+        rich = (4 * d1 - d2) / 3
         ad = float((Ub0 * dU).sum() + mub @ ds)
         errs.append(abs(ad - fd) / max(abs(fd), 1e-300))
+        errs_rich.append(abs(ad - rich) / max(abs(rich), 1e-300))
+        fd_own.append(abs(fd - rich) / max(abs(rich), 1e-300))
     # dot-product test at t_end against the reference's matrix-free FD JVP (FD_Order 2) on the oracle
     o = orc.Oracle(dict(N=5, nodeType=1, riemann=33, riemannBC=-1, lifting=1, weakLifting=0, consLifting=0, splitDG=-1, etaBR2=2.0,
                         etaBR2_wall=-1.0, kappa=1.4, R=71.42857, Pr=0.72, mu0=1.0 / 1600.0, CFLScale=0.9, DFLScale=0.9, doTCSource=0,
@@ -839,7 +872,12 @@ def run_adjoint(args):
             "adjoint_device_memory_gb": adj_bytes / 1e9, "checkpoint_and_stage_states_gb": mem_states_gb,
             "stage_intermediates_kept": adj_bytes / 1e9 > 1.5 * mem_states_gb, "loss": L0,
             "fd_check": {"directions": args.fd_dirs, "eps": 1e-6, "max_rel_err": max(errs) if errs else None,
-                         "median_rel_err": float(np.median(errs)) if errs else None},
+                         "median_rel_err": float(np.median(errs)) if errs else None,
+                         "richardson_h": 1e-4, "max_rel_err_vs_richardson": max(errs_rich) if errs_rich else None,
+                         "median_rel_err_vs_richardson": float(np.median(errs_rich)) if errs_rich else None,
+                         "eps_1e-6_quotient_own_error_max": max(fd_own) if fd_own else None,
+                         "note": "central FD at eps=1e-6 as the configuration states, and a Richardson-extrapolated central FD "
+                                 "(h=1e-4, 2h) whose distance from the eps=1e-6 quotient measures that quotient's own error"},
             "dot_product_vs_reference_fd_jvp": {"rel_err": dot_err, "fd": "implicit.f90:MatrixVector FD_Order 2, Eps_Method 1, on the oracle"},
             "e2e": {"value": ms_rev / ms_plain, "unit": "reverse time / forward time", "h2d_bytes_per_step": dof * 5 * 8 / n_steps,
                     "d2h_bytes_per_step": (dof * 5 * 8 + f.n_elems * 8) / n_steps},

@@ -15,7 +15,10 @@ namespace fg {
 
 // local side ids of FLEXI (src/flexi.h:90-95)
 enum { ZETA_MINUS = 1, ETA_MINUS = 2, XI_PLUS = 3, ETA_PLUS = 4, XI_MINUS = 5, ZETA_PLUS = 6 };
-enum { RIEMANN_LF = 1, RIEMANN_HLLC = 2, RIEMANN_ROE = 3, RIEMANN_ROEENTROPYFIX = 33 };
+// riemann.f90:44-58 and splitflux.f90:63-69
+enum { RIEMANN_LF = 1, RIEMANN_HLLC = 2, RIEMANN_ROE = 3, RIEMANN_ROEL2 = 32, RIEMANN_ROEENTROPYFIX = 33, RIEMANN_ROEENTROPYGSHOCKFIX = 34,
+       RIEMANN_HLL = 4, RIEMANN_HLLE = 5, RIEMANN_HLLEM = 6, RIEMANN_CH = 7, RIEMANN_IR = 8, RIEMANN_AVERAGE = 0 };
+enum { SPLIT_SD = 0, SPLIT_MO = 1, SPLIT_DU = 2, SPLIT_KG = 3, SPLIT_PI = 4, SPLIT_CH = 5, SPLIT_IR = 6 };
 enum { NODE_GAUSS = 1, NODE_GL = 2 };
 
 // face state fields, stored [side][field][p + n*q] for the master and for the slave (in master orientation)
@@ -36,6 +39,7 @@ struct Basis {
   double kappa, kappaM1, sKappaM1, Rgas, sR, lambdaFac, etaBR2, etaBR2_wall;
   double kappaFac, sKappaP1;
   double logEntC, kappa_kappaM1;  // ln((kappa-1)^(1/(kappa-1))), kappa/(kappa-1): eos.f90:EntropyToCons
+  double riemannPhi;              // RiemannPhiFactor of RoeEntropyGShockFix
 };
 
 // Device arrays of one solver handle (all sizes in units of doubles / ints).
@@ -207,6 +211,78 @@ __host__ __device__ __forceinline__ void visc_flux_tau(const double* tau, double
 struct RotState {
   double rho, srho, E, p, v1, v2, v3;
 };
+
+// splitflux.f90:GetLogMean (Ismail and Roe): (a + b) / g, g = log(chi) / f or its series 2 + 2/3 u + 2/5 u^2 + 2/7 u^3
+// (u = f^2) for |f| < 0.1, chi = a / b, f = (chi - 1) / (chi + 1)
+__host__ __device__ __forceinline__ double log_mean(double a, double b) {
+  const double chi = a / b;
+  const double f = (chi - 1.0) / (chi + 1.0);
+  double g;
+  if (fabs(f) < 0.1) {
+    const double u = f * f;
+    g = 2.0 + u * ((2.0 / 3.0) + u * (0.4 + u * (2.0 / 7.0)));
+  } else {
+    g = log(chi) / f;
+  }
+  return (a + b) / g;
+}
+
+// Central split surface flux (splitflux.f90:SplitSurfaceFlux*) on rotated states: SD, MO, DU, KG, PI, CH, IR.
+__host__ __device__ __forceinline__ void split_surface_flux_more(int splitDG, const Basis& B, const RotState& L, const RotState& R,
+                                                                 double* F) {
+  const double mL = L.rho * L.v1, mR = R.rho * R.v1;
+  if (splitDG == SPLIT_MO) {
+    const double rhoepL = L.E - 0.5 * L.rho * (L.v1 * L.v1 + L.v2 * L.v2 + L.v3 * L.v3) + L.p;
+    const double rhoepR = R.E - 0.5 * R.rho * (R.v1 * R.v1 + R.v2 * R.v2 + R.v3 * R.v3) + R.p;
+    const double ms = mL + mR;
+    F[0] = 0.5 * ms;
+    F[1] = 0.25 * ms * (L.v1 + R.v1) + 0.5 * (L.p + R.p);
+    F[2] = 0.25 * ms * (L.v2 + R.v2);
+    F[3] = 0.25 * ms * (L.v3 + R.v3);
+    // {rho u v_k}{v_k} - 1/2 {rho u v_k^2} summed over k = 1/4 (mL + mR) ... as (mL vL.vR + mR vL.vR) / 4
+    const double vv = L.v1 * R.v1 + L.v2 * R.v2 + L.v3 * R.v3;
+    F[4] = 0.5 * (rhoepL * L.v1 + rhoepR * R.v1) + 0.25 * ms * vv;
+  } else if (splitDG == SPLIT_DU) {
+    const double us = L.v1 + R.v1;
+    F[0] = 0.25 * (L.rho + R.rho) * us;
+    F[1] = 0.25 * (mL + mR) * us + 0.5 * (L.p + R.p);
+    F[2] = 0.25 * (L.rho * L.v2 + R.rho * R.v2) * us;
+    F[3] = 0.25 * (L.rho * L.v3 + R.rho * R.v3) * us;
+    F[4] = 0.25 * (L.E + R.E + L.p + R.p) * us;
+  } else if (splitDG == SPLIT_KG) {
+    const double rs = L.rho + R.rho, us = L.v1 + R.v1;
+    const double b = 0.125 * rs * us;
+    F[0] = 0.25 * rs * us;
+    F[1] = b * us + 0.5 * (L.p + R.p);
+    F[2] = b * (L.v2 + R.v2);
+    F[3] = b * (L.v3 + R.v3);
+    F[4] = b * (L.E * L.srho + R.E * R.srho) + 0.25 * (L.p + R.p) * us;
+  } else if (splitDG == SPLIT_CH) {
+    const double bL = 0.5 * L.rho / L.p, bR = 0.5 * R.rho / R.p;
+    const double rhoLog = log_mean(L.rho, R.rho), betaLog = log_mean(bL, bR);
+    const double pHat = 0.5 * (L.rho + R.rho) / (bL + bR);
+    const double H = 0.5 * B.sKappaM1 / betaLog + pHat / rhoLog + 0.5 * (L.v1 * R.v1 + L.v2 * R.v2 + L.v3 * R.v3);
+    F[0] = rhoLog * 0.5 * (L.v1 + R.v1);
+    F[1] = F[0] * 0.5 * (L.v1 + R.v1) + pHat;
+    F[2] = F[0] * 0.5 * (L.v2 + R.v2);
+    F[3] = F[0] * 0.5 * (L.v3 + R.v3);
+    F[4] = F[0] * H;
+  } else {  // IR
+    const double zL1 = sqrt(L.rho / L.p), zL5 = sqrt(L.rho * L.p), zR1 = sqrt(R.rho / R.p), zR5 = sqrt(R.rho * R.p);
+    const double z1Log = log_mean(zL1, zR1), z5Log = log_mean(zL5, zR5);
+    const double z1s = zL1 + zR1;  // 2 z1Mean
+    const double rhoHat = 0.5 * z1s * z5Log;
+    const double pHat = (zL5 + zR5) / z1s;
+    const double p2Hat = 0.5 / B.kappa * ((B.kappa + 1.0) * z5Log / z1Log + B.kappaM1 * pHat);
+    const double uHat = (zL1 * L.v1 + zR1 * R.v1) / z1s, vHat = (zL1 * L.v2 + zR1 * R.v2) / z1s, wHat = (zL1 * L.v3 + zR1 * R.v3) / z1s;
+    const double hHat = B.kappa * p2Hat / (rhoHat * B.kappaM1) + 0.5 * (uHat * uHat + vHat * vHat + wHat * wHat);
+    F[0] = rhoHat * uHat;
+    F[1] = F[0] * uHat + pHat;
+    F[2] = F[0] * vHat;
+    F[3] = F[0] * wHat;
+    F[4] = F[0] * hHat;
+  }
+}
 
 // Central split surface flux (splitflux.f90:SplitSurfaceFluxPI / SD) on rotated states.
 __host__ __device__ __forceinline__ void split_surface_flux(int splitDG, const RotState& L, const RotState& R, double HL, double HR, double* F) {

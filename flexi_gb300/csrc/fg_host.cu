@@ -1981,7 +1981,11 @@ int fg_debug_array(fg_handle* h, const char* name, void* out, long long* count) 
   else if (k == "elemInst") { src = h->d.elemInst; cnt = nE; esz = sizeof(int); }
   else if (k == "elemSide") { src = h->d.elemSide; cnt = nE * 6; esz = sizeof(int); }
   else if (k == "sideElem") { src = h->d.sideElem; cnt = nS * 4; esz = sizeof(int); }
+  else if (k == "geo") { src = h->d.geo; cnt = nS * FG_NF * (long long)h->M.n * h->M.n; }
+  else if (k == "bcType") { src = h->d.bcType; cnt = h->d.nBCSides; esz = sizeof(int); }
+  else if (k == "bcTwall") { src = h->d.bcTwall; cnt = h->d.nBCSides; }
   else return fail(h, FG_ERR_CONFIG, "unknown array " + k);
+  if (cnt == 0) { *count = 0; return FG_OK; }
   *count = cnt;
   if (out) {
     CUDA_TRY(cudaStreamSynchronize(h->st));

@@ -11,7 +11,11 @@ struct Inst {
   using S = Shape<n>;
   static int blocks(const Dev& d) { return (d.nElems + S::EPB - 1) / S::EPB; }
   static size_t smem_prep() { return dyn_smem_bytes<n>(Big<n>::prep); }
-  static size_t smem_lift() { return dyn_smem_bytes<n>(Big<n>::lift); }
+  // Gauss nodes (lines of up to 8): the lifting keeps the 12 products F_v n_c per face point (the mortar layout, inert
+  // without mortar sides): the surface part then costs 2 FMA per gradient component and direction at every node of
+  // the normal lines, instead of forming F_v w and three normal products there
+  static constexpr bool LIFT12 = !GL && n <= 8;
+  static size_t smem_lift() { return dyn_smem_bytes<n>(LIFT12 ? Big<n>::liftMortar : Big<n>::lift); }
   static size_t smem_weak() { return dyn_smem_bytes<n>(Big<n>::weak); }
   static size_t smem_split() { return sizeof(double) * (SBasis<n>::SIZE + 2 * S::n2 + S::EPB * (20 * S::n3 + 6 * S::n2 * 5)); }
   // the tuned shuffle-pair kernel for Gauss-Lobatto lines of 2, 4 or 8 nodes; k_vol_split_gen otherwise
@@ -32,7 +36,7 @@ struct Inst {
   template <int E>
   static size_t smem_prep_E() { return dyn_smem_bytes<n>(Big<n, E>::prep); }
   template <int E>
-  static size_t smem_lift_E() { return dyn_smem_bytes<n>(Big<n, E>::lift); }
+  static size_t smem_lift_E() { return dyn_smem_bytes<n>(LIFT12 ? Big<n, E>::liftMortar : Big<n, E>::lift); }
   template <int E>
   static size_t smem_weak_E() { return dyn_smem_bytes<n>(Big<n, E>::weak); }
   template <int E>
@@ -43,7 +47,7 @@ struct Inst {
   template <int E>
   static void lift_E(const Dev& d, const Basis& B, cudaStream_t st) {
     using SE = Shape<n, E>;
-    k_lift<n, GL, E><<<(d.nElems + SE::EPB - 1) / SE::EPB, SE::THREADS, smem_lift_E<E>(), st>>>(d, B);
+    k_lift<n, GL, E, LIFT12><<<(d.nElems + SE::EPB - 1) / SE::EPB, SE::THREADS, smem_lift_E<E>(), st>>>(d, B);
   }
   template <int E>
   static void vol_weak_E(const Dev& d, const Basis& B, int mode, double rkA, double rkB, cudaStream_t st) {
@@ -60,7 +64,7 @@ struct Inst {
   }
   static void prepare() {
     set_smem(k_prep<n, GL>, smem_prep());
-    set_smem(k_lift<n, GL>, smem_lift());
+    set_smem(k_lift<n, GL, 0, LIFT12>, smem_lift());
     set_smem(k_vol_weak<n, GL>, smem_weak());
     if constexpr (SPLIT_POW2) set_smem(k_vol_split<n>, smem_split());
     else set_smem(k_vol_split_gen<n, GL>, smem_split_gen());
@@ -78,7 +82,7 @@ struct Inst {
     if constexpr (GL && (n == 2 || n == 4 || n == 8)) set_smem(k_vol_split_adj<n>, smem_split_adj());
     if constexpr (ALT_E > 0) {
       set_smem(k_prep<n, GL, ALT_E>, smem_prep_E<ALT_E>());
-      set_smem(k_lift<n, GL, ALT_E>, smem_lift_E<ALT_E>());
+      set_smem(k_lift<n, GL, ALT_E, LIFT12>, smem_lift_E<ALT_E>());
       set_smem(k_vol_weak<n, GL, ALT_E>, smem_weak_E<ALT_E>());
     }
   }
@@ -107,7 +111,7 @@ struct Inst {
     k_prep<n, GL><<<blocks(d), S::THREADS, smem_prep(), st>>>(d, B);
   }
   static void lift(const Dev& d, const Basis& B, cudaStream_t st) {
-    k_lift<n, GL><<<blocks(d), S::THREADS, smem_lift(), st>>>(d, B);
+    k_lift<n, GL, 0, LIFT12><<<blocks(d), S::THREADS, smem_lift(), st>>>(d, B);
   }
   static void flux(const Dev& d, const Basis& B, cudaStream_t st) {
     const long long pts = (long long)d.nFluxSides * S::n2;

@@ -12,17 +12,21 @@
 // Rules of use:
 //  * The first call on a device resolves the device address of the scratch array with
 //    cudaGetSymbolAddress (host code may only use that address, never the array's name) and sets the
-//    kernels' shared-memory limits; make that first call on each device before any stream capture.
+//    kernels' shared-memory limits; make that first call on each device before any stream capture. The
+//    set-up is kept per device and per CUDA context: a call in a context created after it (e.g. after
+//    cudaDeviceReset) does it again. Host threads making their first calls together are serialised on it.
 //  * All calls share the array, which keeps the last call's contents; calls that overlap on the GPU
 //    (on different streams, or from different host threads without ordering) race on it.
 //  * Meshes whose intermediates need more than FG_NOALLOC_SCRATCH_BYTES are rejected with
 //    FG_ERR_CONFIG before anything is launched.
 //  * The call is asynchronous on the caller's stream and calls no cudaMalloc, cudaFree or other
 //    allocating routine, on the device or on the host.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
 #include <cstdio>
+#include <mutex>
 
 #include "../../include/flexi_gpu.h"
 #include "fg_common.cuh"
@@ -43,7 +47,38 @@ int reject(int code, const char* msg) {
 static __device__ __align__(256) double g_noalloc_scratch[FG_NOALLOC_SCRATCH_BYTES / sizeof(double)];
 
 constexpr int kMaxDevices = 64;
-double* g_scratch_addr[kMaxDevices] = {nullptr};
+// per-device set-up: the scratch array's device address in the context it was resolved in
+struct DeviceSetup {
+  std::mutex m;
+  unsigned long long ctxId = 0;
+  double* scratch = nullptr;
+};
+DeviceSetup g_setup[kMaxDevices];
+
+// unique id of the calling thread's current CUDA context (driver cuCtxGetCurrent / cuCtxGetId through the runtime's
+// entry-point query, no link to the driver library); 0 when there is none or the query is unavailable
+unsigned long long current_context_id() {
+  using PfnGetCurrent = CUresult (*)(CUcontext*);
+  using PfnGetId = CUresult (*)(CUcontext, unsigned long long*);
+  static PfnGetCurrent getCurrent = nullptr;
+  static PfnGetId getId = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      getCurrent = (PfnGetCurrent)p;
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess && q == cudaDriverEntryPointSuccess)
+      getId = (PfnGetId)p;
+  });
+  if (!getCurrent || !getId) return 0;
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (getCurrent(&c) != CUDA_SUCCESS || !c || getId(c, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 // per-call constants of the scratch: one instance, no body force
 __global__ void k_noalloc_init(double* perInst, int* err, int* elemInst, int nE, int* sideInst, int nS, double mu0) {
@@ -239,29 +274,43 @@ extern "C" int fg_time_derivative_noalloc(const fg_config* cfg, const fg_device_
       (mesh->nBCSides > 0 && (!mesh->bcType || !mesh->bcTwall)))
     return reject(FG_ERR_MESH, "fg_time_derivative_noalloc: null device pointer");
 
+  // an error left by earlier work of the caller stays where it is, for the caller's own check
+  const cudaError_t pending = cudaPeekAtLastError();
+  if (pending != cudaSuccess) {
+    std::snprintf(msg, sizeof msg, "fg_time_derivative_noalloc: a CUDA error from earlier work is pending (%s); nothing launched",
+                  cudaGetErrorString(pending));
+    return reject(FG_ERR_CUDA, msg);
+  }
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
     return reject(FG_ERR_CUDA, "fg_time_derivative_noalloc: no usable current device");
   KernelSet K = get_kernel_set((int)n, cfg->NodeType == FG_NODE_GAUSS_LOBATTO);
   if (K.n == 0 || (cfg->SplitDG >= 0 && !K.vol_split))
     return reject(FG_ERR_CONFIG, "fg_time_derivative_noalloc: no kernels for this N and node type");
-  if (!g_scratch_addr[dev]) {
-    // first call on this device (the current one): device address of the scratch array, kernel limits
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) {
-      std::snprintf(msg, sizeof msg, "fg_time_derivative_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
-      return reject(FG_ERR_CUDA, msg);
+  double* S = nullptr;
+  {
+    DeviceSetup& su = g_setup[dev];
+    std::lock_guard<std::mutex> lock(su.m);
+    const unsigned long long ctx = current_context_id();
+    if (!su.scratch || ctx == 0 || ctx != su.ctxId) {
+      // first call on this device in this context (the current one): device address of the scratch array, kernel limits
+      void* p = nullptr;
+      const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess || !p) {
+        std::snprintf(msg, sizeof msg, "fg_time_derivative_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+        return reject(FG_ERR_CUDA, msg);
+      }
+      prepare_all_sets();
+      const cudaError_t e2 = cudaGetLastError();
+      if (e2 != cudaSuccess) {
+        std::snprintf(msg, sizeof msg, "fg_time_derivative_noalloc: kernel set-up: %s", cudaGetErrorString(e2));
+        return reject(FG_ERR_CUDA, msg);
+      }
+      su.scratch = (double*)p;
+      su.ctxId = current_context_id();  // the look-up has made the primary context current if none was
     }
-    prepare_all_sets();
-    const cudaError_t e2 = cudaGetLastError();
-    if (e2 != cudaSuccess) {
-      std::snprintf(msg, sizeof msg, "fg_time_derivative_noalloc: kernel set-up: %s", cudaGetErrorString(e2));
-      return reject(FG_ERR_CUDA, msg);
-    }
-    g_scratch_addr[dev] = (double*)p;
+    S = su.scratch;
   }
-  double* S = g_scratch_addr[dev];
   Basis B{};
   stack_basis(*cfg, B);
   Dev d{};

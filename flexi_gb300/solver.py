@@ -364,7 +364,7 @@ class Flexi:
         """Copy of a device array in the device layout (inspection only)."""
         cnt = ctypes.c_longlong(0)
         self._check(self.L.fg_debug_array(self.h, name.encode(), None, ctypes.byref(cnt)), "fg_debug_array")
-        dtype = np.int32 if name in ("elemInst", "elemSide", "sideElem") else np.float64
+        dtype = np.int32 if name in ("elemInst", "elemSide", "sideElem", "bcType") else np.float64
         out = np.empty(cnt.value, dtype)
         self._check(self.L.fg_debug_array(self.h, name.encode(), _p(out), ctypes.byref(cnt)), "fg_debug_array")
         return out

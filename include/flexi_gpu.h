@@ -258,8 +258,8 @@ int fg_get_stream(fg_handle* h, void** stream);
 long long fg_launch_count(const fg_handle* h);
 
 /* Copies one of the handle's device arrays to host memory for inspection, in the device layout:
- * "U","Ut","prim","grad","metr","sJ","metAdv","metVisc","mu0","dt","dtElem" (double), "elemInst",
- * "elemSide","sideElem" (int). *count receives the number of elements; out may be NULL to query it. */
+ * "U","Ut","prim","grad","metr","sJ","metAdv","metVisc","mu0","dt","dtElem","geo","bcTwall" (double), "elemInst",
+ * "elemSide","sideElem","bcType" (int). *count receives the number of elements; out may be NULL to query it. */
 int fg_debug_array(fg_handle* h, const char* name, void* out, long long* count);
 
 /* Per-kernel CUDA-event timing of later launches on the handle's stream; while enabled, fg_run issues
@@ -349,8 +349,8 @@ int fg_probe_fp64(double* tflops);
  * For callers that cannot allocate device memory: host codes whose device memory all comes from their
  * own pool or caching allocator, and time loops that must not allocate once they run. Everything is
  * caller-owned DEVICE memory in the library's device layouts (n = N+1 nodes per direction, n2 = n*n,
- * n3 = n*n*n); the layouts are those fg_debug_array returns for "U", "metr", "sJ", "elemSide",
- * "sideElem". BC sides are sides 0..nBCSides-1, as in FLEXI. */
+ * n3 = n*n*n); the layouts are those fg_debug_array returns for "U", "metr", "sJ", "geo", "elemSide",
+ * "sideElem", "bcType", "bcTwall". BC sides are sides 0..nBCSides-1, as in FLEXI. */
 typedef struct fg_device_mesh {
   int nElems, nSides, nBCSides;
   const int* elemSide;    /* [nElems][6]: 8*sideID + flip per local side ZETA-,ETA-,XI+,ETA+,XI-,ZETA+ (flip 0: master) */
@@ -358,9 +358,13 @@ typedef struct fg_device_mesh {
   const double* metr;     /* [nElems][9][n3]: Metrics_fTilde(1:3), Metrics_gTilde(1:3), Metrics_hTilde(1:3) */
   const double* sJ;       /* [nElems][n3]: 1/J */
   const double* geo;      /* [nSides][10][n2]: NormVec(3), TangVec1(3), TangVec2(3), SurfElem */
-  const int* bcType;      /* [nBCSides]: FLEXI BC type of each BC side (3 adiabatic, 4 isothermal wall) */
+  const int* bcType;      /* [nBCSides]: FLEXI BC type of each BC side, 3 (adiabatic wall) or 4 (isothermal wall) */
   const double* bcTwall;  /* [nBCSides]: wall temperature of each BC side (isothermal walls) */
 } fg_device_mesh;
+
+/* The device tables of fg_device_mesh are not checked: they must describe a valid mesh as this library builds it (as
+ * fg_debug_array returns them from a handle), with side and element ids in range and bcType 3 or 4 only; other values
+ * make the kernels read or write out of bounds or apply neither wall condition. */
 
 /* Largest scratch the allocation-free call can use: 64 MiB of static device memory, held by every
  * device that loads the library (e.g. 343 elements at N=7, ~2500 elements at N=3). */
@@ -372,8 +376,12 @@ typedef struct fg_device_mesh {
  * arrays live in one static __device__ scratch array of FG_NOALLOC_SCRATCH_BYTES; the call clears what
  * must start at zero (sticky error word, instance ids) itself on the stream. The first call on each
  * device, with that device current, looks up the scratch address and sets the kernels' shared-memory
- * limits: make it before any stream capture. Calls that overlap on the GPU (other streams, or host
- * threads without ordering) race on the shared scratch. Meshes needing more scratch, and configurations
+ * limits: make it before any stream capture. That set-up belongs to the CUDA context it ran in and is
+ * redone by the first call in a later context of the device (e.g. after cudaDeviceReset); host threads
+ * making first calls together are serialised on it. Calls that overlap on the GPU (other streams, or host
+ * threads without ordering) race on the shared scratch. The call reports no NaN (it runs no CALCTIMESTEP)
+ * and no asynchronous kernel fault (check the stream); it refuses to run, leaving the error in place, when a
+ * CUDA error of earlier work is pending on the calling thread. Meshes needing more scratch, and configurations
  * the kernels do not cover (N > 7, weak or conservative lifting, body force, overintegration, split form
  * off Gauss-Lobatto nodes or with N not in {1,3,7}), are rejected before any launch, with the reason in
  * fg_last_error(NULL). No cudaMalloc, cudaFree or other device allocation is made. */

@@ -85,8 +85,10 @@ template <class R> inline R rmin(R a, R b) { return a < b ? a : b; }
 // ---------------------------------------------------------------------------------------------
 // configuration (ini keys of parameter_flexi.ini; integer codes as in the reference)
 // ---------------------------------------------------------------------------------------------
-enum { RIEMANN_LF = 1, RIEMANN_HLLC = 2, RIEMANN_ROE = 3, RIEMANN_ROEENTROPYFIX = 33, RIEMANN_SAME = -1 };
-enum { SPLIT_NONE = -1, SPLIT_SD = 0, SPLIT_PI = 4 };
+// riemann.f90:44-58 and splitflux.f90:63-69
+enum { RIEMANN_LF = 1, RIEMANN_HLLC = 2, RIEMANN_ROE = 3, RIEMANN_ROEL2 = 32, RIEMANN_ROEENTROPYFIX = 33, RIEMANN_ROEENTROPYGSHOCKFIX = 34,
+       RIEMANN_HLL = 4, RIEMANN_HLLE = 5, RIEMANN_HLLEM = 6, RIEMANN_CH = 7, RIEMANN_IR = 8, RIEMANN_AVERAGE = 0, RIEMANN_SAME = -1 };
+enum { SPLIT_NONE = -1, SPLIT_SD = 0, SPLIT_MO = 1, SPLIT_DU = 2, SPLIT_KG = 3, SPLIT_PI = 4, SPLIT_CH = 5, SPLIT_IR = 6 };
 struct Config {
   int N = 3, nodeType = NT_GAUSS;
   int riemann = RIEMANN_ROEENTROPYFIX, riemannBC = RIEMANN_SAME;
@@ -106,7 +108,24 @@ struct Config {
   int iniExactFunc = 0;
   double advVel[3] = {0., 0., 0.};
   double iniFrequency = 1.0, iniAmplitude = 0.1;
+  double riemannPhi = 5.0;  // RiemannPhiFactor of Riemann_RoeEntropyGShockFix (riemann.f90:131, default 5)
 };
+
+// splitflux.f90:GetLogMean (Ismail and Roe, appendix B): (U_L + U_R) / g with g = log(chi)/f, or its series
+// 2 + 2/3 u + 2/5 u^2 + 2/7 u^3 (u = f^2) for |f| < 0.1, chi = U_L/U_R, f = (chi-1)/(chi+1)
+template <class R>
+R log_mean(R uL, R uR) {
+  R chi = uL / uR;
+  R f = (chi - R(1.)) / (chi + R(1.));
+  R g;
+  if (fabs(f) < R(0.1)) {
+    R u = f * f;
+    g = R(2.) + R(2. / 3.) * u + R(0.4) * u * u + R(2. / 7.) * u * u * u;
+  } else {
+    g = log(chi) / f;
+  }
+  return (uL + uR) / g;
+}
 
 // changebasis.t90:ChangeBasisVolume on an element block X(nv, 0:Ni, 0:Ni, 0:Ni) -> (nv, 0:No, 0:No, 0:No),
 // V (No+1)x(Ni+1) row-major; xi, then eta, then zeta, each sum in increasing input index
@@ -139,9 +158,95 @@ static const int PRIM_LIFT[4] = {1, 2, 3, 5};  // 0-based prim indices: v1,v2,v3
 // splitflux.f90:SplitVolumeFluxPI / SplitVolumeFluxSD (factor 2 of the split form included): two-point
 // flux between (u, p) states "R" and "L" with the mean of the two metric vectors
 template <class R>
-void split_volume_flux_t(int splitDG, const R* uR, const R* pR, const R* u, const R* p, const R* mR, const R* m, R* F) {
+void split_volume_flux_t(int splitDG, const R* uR, const R* pR, const R* u, const R* p, const R* mR, const R* m, R* F, double kappa = 1.4) {
   R ft[5], gt[5], ht[5];
-  if (splitDG == SPLIT_PI) {
+  if (splitDG == SPLIT_IR) {
+    // SplitVolumeFluxIR (splitflux.f90, the Ismail-Roe flux): no factor 2, as the reference has it
+    const R kP1 = R(kappa + 1.), kM1 = R(kappa - 1.), kap = R(kappa);
+    R z1 = sqrt(u[0] / p[4]), z5 = sqrt(u[0] * p[4]);
+    R z[5] = {z1, z1 * p[1], z1 * p[2], z1 * p[3], z5};
+    R zr1 = sqrt(uR[0] / pR[4]), zr5 = sqrt(uR[0] * pR[4]);
+    R zr[5] = {zr1, zr1 * pR[1], zr1 * pR[2], zr1 * pR[3], zr5};
+    R z1Log = log_mean(z[0], zr[0]), z5Log = log_mean(z[4], zr[4]);
+    R z1Mean = R(0.5) * (z[0] + zr[0]);
+    R rhoHat = z1Mean * z5Log;
+    R pHat = R(0.5) * (z[4] + zr[4]) / z1Mean;
+    R p2Hat = R(1.) / (R(2.) * kap) * (kP1 * z5Log / z1Log + kM1 * pHat);
+    R uHat = R(0.5) * (z[1] + zr[1]) / z1Mean, vHat = R(0.5) * (z[2] + zr[2]) / z1Mean, wHat = R(0.5) * (z[3] + zr[3]) / z1Mean;
+    R hHat = kap * p2Hat / (rhoHat * kM1) + R(0.5) * (uHat * uHat + vHat * vHat + wHat * wHat);
+    R me[3] = {R(0.5) * (mR[0] + m[0]), R(0.5) * (mR[1] + m[1]), R(0.5) * (mR[2] + m[2])};
+    R qeff = rhoHat * (uHat * me[0] + vHat * me[1] + wHat * me[2]);
+    F[0] = qeff;
+    F[1] = qeff * uHat + pHat * me[0];
+    F[2] = qeff * vHat + pHat * me[1];
+    F[3] = qeff * wHat + pHat * me[2];
+    F[4] = qeff * hHat;
+    return;
+  }
+  if (splitDG == SPLIT_MO) {
+    // SplitVolumeFluxMO (Morinishi)
+    R rhoepR = uR[4] - R(0.5) * uR[0] * (pR[1] * pR[1] + pR[2] * pR[2] + pR[3] * pR[3]) + pR[4];
+    R rhoep = u[4] - R(0.5) * u[0] * (p[1] * p[1] + p[2] * p[2] + p[3] * p[3]) + p[4];
+    R* T[3] = {ft, gt, ht};
+    for (int d = 0; d < 3; ++d) {
+      R* t = T[d];
+      R ms = uR[1 + d] + u[1 + d];
+      t[0] = ms;
+      for (int k = 0; k < 3; ++k) t[1 + k] = R(0.5) * ms * (pR[1 + k] + p[1 + k]) + (k == d ? pR[4] + p[4] : R(0.));
+      t[4] = (rhoepR * pR[1 + d] + rhoep * p[1 + d]);
+      for (int k = 0; k < 3; ++k) t[4] = t[4] + R(0.5) * (uR[1 + d] * pR[1 + k] + u[1 + d] * p[1 + k]) * (pR[1 + k] + p[1 + k]);
+      for (int k = 0; k < 3; ++k) t[4] = t[4] - R(0.5) * (uR[1 + d] * pR[1 + k] * pR[1 + k] + u[1 + d] * p[1 + k] * p[1 + k]);
+    }
+  } else if (splitDG == SPLIT_DU) {
+    // SplitVolumeFluxDU (Ducros)
+    R* T[3] = {ft, gt, ht};
+    for (int d = 0; d < 3; ++d) {
+      R* t = T[d];
+      R vs = pR[1 + d] + p[1 + d];
+      t[0] = R(0.5) * (uR[0] + u[0]) * vs;
+      for (int k = 0; k < 3; ++k) t[1 + k] = R(0.5) * (uR[1 + k] + u[1 + k]) * vs + (k == d ? pR[4] + p[4] : R(0.));
+      t[4] = R(0.5) * (uR[4] + u[4] + pR[4] + p[4]) * vs;
+    }
+  } else if (splitDG == SPLIT_KG) {
+    // SplitVolumeFluxKG (Kennedy and Gruber)
+    R ERef = uR[4] / uR[0], E = u[4] / u[0];
+    R rs = uR[0] + u[0], ps = pR[4] + p[4];
+    R vs[3] = {pR[1] + p[1], pR[2] + p[2], pR[3] + p[3]};
+    ft[0] = R(0.5) * rs * vs[0];
+    ft[1] = R(0.25) * rs * vs[0] * vs[0] + ps;
+    ft[2] = R(0.25) * rs * vs[0] * vs[1];
+    ft[3] = R(0.25) * rs * vs[0] * vs[2];
+    ft[4] = R(0.25) * rs * vs[0] * (ERef + E) + R(0.5) * ps * vs[0];
+    gt[0] = R(0.5) * rs * vs[1];
+    gt[1] = ft[2];
+    gt[2] = R(0.25) * rs * vs[1] * vs[1] + ps;
+    gt[3] = R(0.25) * rs * vs[1] * vs[2];
+    gt[4] = R(0.25) * rs * vs[1] * (ERef + E) + R(0.5) * ps * vs[1];
+    ht[0] = R(0.5) * rs * vs[2];
+    ht[1] = ft[3];
+    ht[2] = gt[3];
+    ht[3] = R(0.25) * rs * vs[2] * vs[2] + ps;
+    ht[4] = R(0.25) * rs * vs[2] * (ERef + E) + R(0.5) * ps * vs[2];
+  } else if (splitDG == SPLIT_CH) {
+    // SplitVolumeFluxCH (Chandrashekar), times 2 as the reference has it
+    const R sKappaM1 = R(1. / (kappa - 1.));
+    R um[3] = {R(0.5) * (pR[1] + p[1]), R(0.5) * (pR[2] + p[2]), R(0.5) * (pR[3] + p[3])};
+    R betaRef = R(0.5) * uR[0] / pR[4], beta = R(0.5) * u[0] / p[4];
+    R rhoLog = log_mean(uR[0], u[0]);
+    R betaLog = log_mean(betaRef, beta);
+    R pHat = R(0.5) * (uR[0] + u[0]) / (betaRef + beta);
+    R HMean = R(0.5) * sKappaM1 / betaLog + pHat / rhoLog + R(0.5) * (pR[1] * p[1] + pR[2] * p[2] + pR[3] * p[3]);
+    R* T[3] = {ft, gt, ht};
+    for (int d = 0; d < 3; ++d) {
+      R* t = T[d];
+      t[0] = rhoLog * um[d];
+      for (int k = 0; k < 3; ++k) t[1 + k] = rhoLog * um[d] * um[k] + (k == d ? pHat : R(0.));
+      t[4] = rhoLog * HMean * um[d];
+    }
+    R m1 = R(0.5) * (mR[0] + m[0]), m2 = R(0.5) * (mR[1] + m[1]), m3 = R(0.5) * (mR[2] + m[2]);
+    for (int v = 0; v < 5; ++v) F[v] = (m1 * ft[v] + m3 * ht[v] + m2 * gt[v]) * R(2.);
+    return;
+  } else if (splitDG == SPLIT_PI) {
     R HR = (uR[4] + pR[4]) / uR[0], H = (u[4] + p[4]) / u[0];
     R rs = uR[0] + u[0], us = pR[1] + p[1], vs = pR[2] + p[2], ws = pR[3] + p[3], ps = pR[4] + p[4], Hs = HR + H;
     ft[0] = R(0.5) * rs * us; ft[1] = R(0.25) * rs * us * us + ps; ft[2] = R(0.25) * rs * us * vs; ft[3] = R(0.25) * rs * us * ws; ft[4] = R(0.25) * rs * us * Hs;
@@ -165,7 +270,8 @@ void split_volume_flux_t(int splitDG, const R* uR, const R* pR, const R* u, cons
 // Along the normal line through (p,q): FluxB(l) = SplitDGVolume(U(l), U_face, Metrics(l), Ja_face),
 // Ut(l) += (F - 1/2 (sum_k Leg(k) FluxB(k) - FluxB(l)) NormalSign) LegHat(l).
 template <class R, class VolFn, class FaceFn>
-void split_gauss_surf_side(int splitDG, int N, int ls, int flip, const DGBasis& B, const R* Fside, VolFn vol, FaceFn face, R* Ut) {
+void split_gauss_surf_side(int splitDG, int N, int ls, int flip, const DGBasis& B, const R* Fside, VolFn vol, FaceFn face, R* Ut,
+                           double kappa = 1.4) {
   const int n = N + 1;
   const bool minus = (ls == XI_MINUS || ls == ETA_MINUS || ls == ZETA_MINUS);
   const int idx = (ls == XI_MINUS || ls == XI_PLUS) ? 0 : ((ls == ETA_MINUS || ls == ETA_PLUS) ? 1 : 2);
@@ -182,7 +288,7 @@ void split_gauss_surf_side(int splitDG, int N, int ls, int flip, const DGBasis& 
       const R *uv, *pv, *mv;
       vol(ijk[0], ijk[1], ijk[2], uv, pv, mv);
       R* fb = &FluxB[(size_t)ijk[idx] * 5];
-      split_volume_flux_t<R>(splitDG, uv, pv, uf, pf, mv, jf, fb);
+      split_volume_flux_t<R>(splitDG, uv, pv, uf, pf, mv, jf, fb, kappa);
       for (int v = 0; v < 5; ++v) sum[v] = sum[v] + fb[v] * R(Leg[ijk[idx]]);
     }
     for (int l = 0; l <= N; ++l) {
@@ -666,7 +772,7 @@ struct DG {
           for (int c = 0; c < 3; ++c) jface[c] = R(J[sx * 3 + c]);
           ja = jface;
         };
-        split_gauss_surf_side<R>(C.splitDG, N, ls, flip, B, Fside.data(), vol, face, &Ut[(size_t)e * nv3 * 5]);
+        split_gauss_surf_side<R>(C.splitDG, N, ls, flip, B, Fside.data(), vol, face, &Ut[(size_t)e * nv3 * 5], C.kappa);
       }
     }
   }
@@ -913,11 +1019,74 @@ struct DG {
   }
   // splitflux.f90:SplitVolumeFluxPI / SplitVolumeFluxSD (factor 2 of the split form included)
   void split_volume_flux(const R* uR, const R* pR, const R* u, const R* p, const R* mR, const R* m, R* F) const {
-    split_volume_flux_t<R>(C.splitDG, uR, pR, u, p, mR, m, F);
+    split_volume_flux_t<R>(C.splitDG, uR, pR, u, p, mR, m, F, C.kappa);
   }
   // splitflux.f90:SplitSurfaceFluxPI / SD on rotated extended states UE(11): 0..4 cons, 5 srho, 6..8 vel, 9 p, 10 T
   void split_surface_flux(const R* L, const R* Rr, R* F) const {
-    if (C.splitDG == SPLIT_PI) {
+    const int sd = C.splitDG;
+    if (sd == SPLIT_MO) {  // SplitSurfaceFluxMO
+      R rhoepL = L[4] - R(0.5) * L[0] * (L[6] * L[6] + L[7] * L[7] + L[8] * L[8]) + L[9];
+      R rhoepR = Rr[4] - R(0.5) * Rr[0] * (Rr[6] * Rr[6] + Rr[7] * Rr[7] + Rr[8] * Rr[8]) + Rr[9];
+      F[0] = R(0.5) * (L[1] + Rr[1]);
+      F[1] = R(0.25) * (L[1] + Rr[1]) * (L[6] + Rr[6]) + R(0.5) * (L[9] + Rr[9]);
+      F[2] = R(0.25) * (L[1] + Rr[1]) * (L[7] + Rr[7]);
+      F[3] = R(0.25) * (L[1] + Rr[1]) * (L[8] + Rr[8]);
+      F[4] = R(0.5) * (rhoepL * L[6] + rhoepR * Rr[6]);
+      for (int k = 0; k < 3; ++k) F[4] = F[4] + R(0.25) * (L[1] * L[6 + k] + Rr[1] * Rr[6 + k]) * (L[6 + k] + Rr[6 + k]);
+      for (int k = 0; k < 3; ++k) F[4] = F[4] - R(0.25) * (L[1] * L[6 + k] * L[6 + k] + Rr[1] * Rr[6 + k] * Rr[6 + k]);
+      return;
+    }
+    if (sd == SPLIT_DU) {  // SplitSurfaceFluxDU
+      R us = L[6] + Rr[6];
+      F[0] = R(0.25) * (L[0] + Rr[0]) * us;
+      F[1] = R(0.25) * (L[1] + Rr[1]) * us + R(0.5) * (L[9] + Rr[9]);
+      F[2] = R(0.25) * (L[2] + Rr[2]) * us;
+      F[3] = R(0.25) * (L[3] + Rr[3]) * us;
+      F[4] = R(0.25) * (L[4] + Rr[4] + L[9] + Rr[9]) * us;
+      return;
+    }
+    if (sd == SPLIT_KG) {  // SplitSurfaceFluxKG
+      R EL = L[4] / L[0], ER = Rr[4] / Rr[0];
+      R rs = L[0] + Rr[0], us = L[6] + Rr[6];
+      F[0] = R(0.25) * rs * us;
+      F[1] = R(0.125) * rs * us * us + R(0.5) * (L[9] + Rr[9]);
+      F[2] = R(0.125) * rs * us * (L[7] + Rr[7]);
+      F[3] = R(0.125) * rs * us * (L[8] + Rr[8]);
+      F[4] = R(0.125) * rs * (EL + ER) * us + R(0.25) * (L[9] + Rr[9]) * us;
+      return;
+    }
+    if (sd == SPLIT_CH) {  // SplitSurfaceFluxCH
+      R uM = R(0.5) * (L[6] + Rr[6]), vM = R(0.5) * (L[7] + Rr[7]), wM = R(0.5) * (L[8] + Rr[8]);
+      R bL = R(0.5) * L[0] / L[9], bR = R(0.5) * Rr[0] / Rr[9];
+      R rhoLog = log_mean(L[0], Rr[0]), betaLog = log_mean(bL, bR);
+      R pHat = R(0.5) * (L[0] + Rr[0]) / (bL + bR);
+      R HMean = R(0.5) * R(sKappaM1) / betaLog + pHat / rhoLog + R(0.5) * (L[6] * Rr[6] + L[7] * Rr[7] + L[8] * Rr[8]);
+      F[0] = rhoLog * uM;
+      F[1] = F[0] * uM + pHat;
+      F[2] = F[0] * vM;
+      F[3] = F[0] * wM;
+      F[4] = F[0] * HMean;
+      return;
+    }
+    if (sd == SPLIT_IR) {  // SplitSurfaceFluxIR
+      R zL1 = sqrt(L[0] / L[9]), zL5 = sqrt(L[0] * L[9]), zR1 = sqrt(Rr[0] / Rr[9]), zR5 = sqrt(Rr[0] * Rr[9]);
+      R z1Log = log_mean(zL1, zR1), z5Log = log_mean(zL5, zR5);
+      R z1Mean = R(0.5) * (zL1 + zR1);
+      R rhoHat = z1Mean * z5Log;
+      R pHat = R(0.5) * (zL5 + zR5) / z1Mean;
+      R p2Hat = R(1.) / (R(2.) * kappa) * (R(kappa + 1.) * z5Log / z1Log + kappaM1 * pHat);
+      R uHat = R(0.5) * (zL1 * L[6] + zR1 * Rr[6]) / z1Mean;
+      R vHat = R(0.5) * (zL1 * L[7] + zR1 * Rr[7]) / z1Mean;
+      R wHat = R(0.5) * (zL1 * L[8] + zR1 * Rr[8]) / z1Mean;
+      R hHat = kappa * p2Hat / (rhoHat * kappaM1) + R(0.5) * (uHat * uHat + vHat * vHat + wHat * wHat);
+      F[0] = rhoHat * uHat;
+      F[1] = F[0] * uHat + pHat;
+      F[2] = F[0] * vHat;
+      F[3] = F[0] * wHat;
+      F[4] = F[0] * hHat;
+      return;
+    }
+    if (sd == SPLIT_PI) {
       R HL = (L[4] + L[9]) / L[0], HR = (Rr[4] + Rr[9]) / Rr[0];
       R rs = L[0] + Rr[0], us = L[6] + Rr[6];
       F[0] = R(0.25) * rs * us;
@@ -938,11 +1107,72 @@ struct DG {
   void euler_flux_1d(const R* U, R* F) const {
     F[0] = U[1]; F[1] = U[1] * U[6] + U[9]; F[2] = U[1] * U[7]; F[3] = U[1] * U[8]; F[4] = (U[4] + U[9]) * U[6];
   }
-  // riemann.f90: Riemann_LF/HLLC/Roe/RoeEntropyFix
+  // riemann.f90: Riemann_LF/HLLC/Roe/RoeEntropyFix/RoeL2/RoeEntropyGShockFix/HLL/HLLE/HLLEM/CH/IR/FluxAverage
   void riemann_point(int solver, const R* L, const R* Rr, R* F) const {
     const bool split = C.splitDG != SPLIT_NONE;
     R FL[5], FR[5];
-    if (!split || solver == RIEMANN_HLLC) { euler_flux_1d(L, FL); euler_flux_1d(Rr, FR); }
+    const bool hllFamily = solver == RIEMANN_HLLC || solver == RIEMANN_HLL || solver == RIEMANN_HLLE || solver == RIEMANN_HLLEM;
+    if (!split || hllFamily) { euler_flux_1d(L, FL); euler_flux_1d(Rr, FR); }
+    if (solver == RIEMANN_AVERAGE) {  // Riemann_FluxAverage
+      split_surface_flux(L, Rr, F);
+      return;
+    }
+    if (solver == RIEMANN_CH) {  // Riemann_CH: entropy-stable dissipation of Chandrashekar
+      R cL = sqrt(kappa * L[9] * L[5]), cR = sqrt(kappa * Rr[9] * Rr[5]);
+      R lmax = rmax(fabs(Rr[6]), fabs(L[6])) + rmax(cL, cR);
+      R rhoMean = R(0.5) * (L[0] + Rr[0]);
+      R uM = R(0.5) * (L[6] + Rr[6]), vM = R(0.5) * (L[7] + Rr[7]), wM = R(0.5) * (L[8] + Rr[8]);
+      R bL = R(0.5) * L[0] / L[9], bR = R(0.5) * Rr[0] / Rr[9];
+      R betaLog = log_mean(bL, bR);
+      split_surface_flux(L, Rr, F);
+      for (int v = 0; v < 4; ++v) F[v] = F[v] - R(0.5) * lmax * (Rr[v] - L[v]);
+      F[4] = F[4] - R(0.5) * lmax * ((Rr[0] - L[0]) * (R(0.5) * R(sKappaM1) / betaLog + R(0.5) * (Rr[6] * L[6] + Rr[7] * L[7] + Rr[8] * L[8])) +
+                                     rhoMean * uM * (Rr[6] - L[6]) + rhoMean * vM * (Rr[7] - L[7]) + rhoMean * wM * (Rr[8] - L[8]) +
+                                     R(0.5) * rhoMean * R(sKappaM1) * (R(1.) / bR - R(1.) / bL));
+      return;
+    }
+    if (solver == RIEMANN_IR) {  // Riemann_IR: dissipation in entropy variables with the Ismail-Roe averages
+      R sR = log(Rr[9]) - kappa * log(Rr[0]), sL = log(L[9]) - kappa * log(L[0]);
+      R rpR = Rr[0] / Rr[9], rpL = L[0] / L[9];
+      R vR[5], vL[5];
+      vR[0] = (kappa - sR) / kappaM1 - R(0.5) * rpR * (Rr[6] * Rr[6] + Rr[7] * Rr[7] + Rr[8] * Rr[8]);
+      vL[0] = (kappa - sL) / kappaM1 - R(0.5) * rpL * (L[6] * L[6] + L[7] * L[7] + L[8] * L[8]);
+      for (int k = 0; k < 3; ++k) { vR[1 + k] = rpR * Rr[6 + k]; vL[1 + k] = rpL * L[6 + k]; }
+      vR[4] = -rpR; vL[4] = -rpL;
+      R zL1 = sqrt(L[0] / L[9]), zL5 = sqrt(L[0] * L[9]), zR1 = sqrt(Rr[0] / Rr[9]), zR5 = sqrt(Rr[0] * Rr[9]);
+      R z1Log = log_mean(zL1, zR1), z5Log = log_mean(zL5, zR5);
+      R z1Mean = R(0.5) * (zL1 + zR1);
+      R rhoHat = z1Mean * z5Log;
+      R uHat = R(0.5) * (zL1 * L[6] + zR1 * Rr[6]) / z1Mean;
+      R vHat = R(0.5) * (zL1 * L[7] + zR1 * Rr[7]) / z1Mean;
+      R wHat = R(0.5) * (zL1 * L[8] + zR1 * Rr[8]) / z1Mean;
+      R pHat = R(0.5) * (zL5 + zR5) / z1Mean;
+      R p2Hat = R(1.) / (R(2.) * kappa) * (R(kappa + 1.) * z5Log / z1Log + kappaM1 * pHat);
+      R aHat = sqrt(kappa * p2Hat / rhoHat);
+      R hHat = kappa * p2Hat / (rhoHat * kappaM1) + R(0.5) * (uHat * uHat + vHat * vHat + wHat * wHat);
+      // RHat rows (reference RHat(row,:)), DHat, dissipation RHat diag(DHat) RHat^T vJump
+      R Rh[5][5] = {{R(1.), R(1.), R(0.), R(0.), R(1.)},
+                    {uHat - aHat, uHat, R(0.), R(0.), uHat + aHat},
+                    {vHat, vHat, R(1.), R(0.), vHat},
+                    {wHat, wHat, R(0.), R(1.), wHat},
+                    {hHat - uHat * aHat, R(0.5) * (uHat * uHat + vHat * vHat + wHat * wHat), vHat, wHat, hHat + uHat * aHat}};
+      R Dh[5];
+      Dh[0] = R(0.5) * fabs(uHat - aHat) * rhoHat / kappa;
+      Dh[1] = fabs(uHat) * (kappaM1 / kappa) * rhoHat;
+      Dh[2] = fabs(uHat) * pHat;
+      Dh[3] = Dh[2];
+      Dh[4] = R(0.5) * fabs(uHat + aHat) * rhoHat / kappa;
+      R vJ[5], diss[5], out[5];
+      for (int k = 0; k < 5; ++k) vJ[k] = vR[k] - vL[k];
+      // diss = RHat(1,:)*vJump(1) + ... + RHat(5,:)*vJump(5)   (rows weighted by the jump: RHat^T vJump)
+      for (int c = 0; c < 5; ++c) diss[c] = Rh[0][c] * vJ[0] + Rh[1][c] * vJ[1] + Rh[2][c] * vJ[2] + Rh[3][c] * vJ[3] + Rh[4][c] * vJ[4];
+      for (int c = 0; c < 5; ++c) diss[c] = Dh[c] * diss[c];
+      // diss = RHat(:,1)*diss(1) + ... (columns)
+      for (int r = 0; r < 5; ++r) out[r] = Rh[r][0] * diss[0] + Rh[r][1] * diss[1] + Rh[r][2] * diss[2] + Rh[r][3] * diss[3] + Rh[r][4] * diss[4];
+      split_surface_flux(L, Rr, F);
+      for (int v = 0; v < 5; ++v) F[v] = F[v] - R(0.5) * out[v];
+      return;
+    }
     if (solver == RIEMANN_LF) {
       R cL = sqrt(kappa * L[9] * L[5]), cR = sqrt(kappa * Rr[9] * Rr[5]);
       R lmax = rmax(fabs(Rr[6]), fabs(L[6])) + rmax(cL, cR);
@@ -956,6 +1186,34 @@ struct DG {
     R rv[3] = {(sqR * Rr[6] + sqL * L[6]) * ssq, (sqR * Rr[7] + sqL * L[7]) * ssq, (sqR * Rr[8] + sqL * L[8]) * ssq};
     R rH = (sqR * HR + sqL * HL) * ssq;
     R absVel = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
+    if (solver == RIEMANN_HLL || solver == RIEMANN_HLLE || solver == RIEMANN_HLLEM) {
+      R rc = sqrt(kappaM1 * (rH - R(0.5) * absVel));
+      R Ssl, Ssr;
+      if (solver == RIEMANN_HLL) {  // Riemann_HLL: Roe-averaged signal speeds
+        Ssl = rv[0] - rc;
+        Ssr = rv[0] + rc;
+      } else {  // Riemann_HLLE / HLLEM: Einfeldt's speeds, BETA_RIEMANN_H = sqrt(0.5 (kappa-1)/kappa)
+        R beta = sqrt(R(0.5) * kappaM1 / kappa);
+        Ssl = rmin(rmin(rv[0] - rc, L[6] - beta * sqrt(kappa * L[9] * L[5])), R(0.));
+        Ssr = rmax(rmax(rv[0] + rc, Rr[6] + beta * sqrt(kappa * Rr[9] * Rr[5])), R(0.));
+      }
+      if (Ssl >= R(0.)) { for (int v = 0; v < 5; ++v) F[v] = FL[v]; }
+      else if (Ssr <= R(0.)) { for (int v = 0; v < 5; ++v) F[v] = FR[v]; }
+      else if (solver != RIEMANN_HLLEM) {
+        for (int v = 0; v < 5; ++v) F[v] = (Ssr * FL[v] - Ssl * FR[v] + Ssl * Ssr * (Rr[v] - L[v])) / (Ssr - Ssl);
+      } else {
+        R RoeDens = sqrt(L[0] * Rr[0]);
+        R delta = rc / (rc + fabs(R(0.5) * (Ssl + Ssr)));
+        R A2 = (Rr[0] - L[0]) - (Rr[9] - L[9]) / (rc * rc);
+        R A3 = RoeDens * (Rr[7] - L[7]), A4 = RoeDens * (Rr[8] - L[8]);
+        R r2[5] = {R(1.), rv[0], rv[1], rv[2], R(0.5) * absVel};
+        R r3[5] = {R(0.), R(0.), R(1.), R(0.), rv[1]};
+        R r4[5] = {R(0.), R(0.), R(0.), R(1.), rv[2]};
+        for (int v = 0; v < 5; ++v)
+          F[v] = (Ssr * FL[v] - Ssl * FR[v] + Ssl * Ssr * (Rr[v] - L[v] - delta * (r2[v] * A2 + r3[v] * A3 + r4[v] * A4))) / (Ssr - Ssl);
+      }
+      return;
+    }
     if (solver == RIEMANN_HLLC) {
       R rc = sqrt(kappaM1 * (rH - R(0.5) * absVel));
       R Ssl = rv[0] - rc, Ssr = rv[0] + rc;
@@ -986,7 +1244,41 @@ struct DG {
     R r4[5] = {R(0.), R(0.), R(0.), R(1.), rv[2]};
     R r5[5] = {R(1.), a[4], rv[1], rv[2], rH + rv[0] * rc};
     R Alpha[5];
-    if (solver == RIEMANN_ROE) {
+    if (solver == RIEMANN_ROEL2) {  // Riemann_RoeL2: velocity jumps scaled by the local Mach number
+      R dU[6];
+      for (int v = 0; v < 5; ++v) dU[v] = Rr[v] - L[v];
+      dU[5] = dU[4] - (dU[2] - rv[1] * dU[0]) * rv[1] - (dU[3] - rv[2] * dU[0]) * rv[2];
+      R Ma = sqrt(absVel) / (rc * sqrt(R(kappa)));
+      dU[1] = dU[1] * Ma; dU[2] = dU[2] * Ma; dU[3] = dU[3] * Ma;
+      Alpha[2] = dU[2] - rv[1] * dU[0];
+      Alpha[3] = dU[3] - rv[2] * dU[0];
+      Alpha[1] = kappaM1 / (rc * rc) * (dU[0] * (rH - rv[0] * rv[0]) - dU[5] + rv[0] * dU[1]);
+      Alpha[0] = R(0.5) / rc * (dU[0] * (rv[0] + rc) - dU[1] - rc * Alpha[1]);
+      Alpha[4] = dU[0] - Alpha[0] - Alpha[1];
+      for (int v = 0; v < 5; ++v) a[v] = fabs(a[v]);
+    } else if (solver == RIEMANN_ROEENTROPYGSHOCKFIX) {
+      // Riemann_RoeEntropyGShockFix: wave speeds limited from below by c/RiemannPhi, then the Harten-Hyman fix
+      R cL = sqrt(kappa * L[9] * L[5]), cR = sqrt(kappa * Rr[9] * Rr[5]);
+      R RoeDens = sqrt(L[0] * Rr[0]);
+      R dU[5] = {Rr[0] - L[0], Rr[6] - L[6], Rr[7] - L[7], Rr[8] - L[8], Rr[9] - L[9]};
+      R sg = rv[0] < R(0.) ? R(-1.) : R(1.);
+      R am = sg * rmax(rc / R(C.riemannPhi), fabs(rv[0]));
+      a[0] = am - rc; a[1] = am; a[2] = am; a[3] = am; a[4] = am + rc;
+      r1[1] = a[0]; r5[1] = a[4];
+      R tmp = R(0.5) / (rc * rc);
+      Alpha[0] = tmp * (dU[4] - RoeDens * rc * dU[1]);
+      Alpha[1] = dU[0] - dU[4] * R(2.) * tmp;
+      Alpha[2] = RoeDens * dU[2];
+      Alpha[3] = RoeDens * dU[3];
+      Alpha[4] = tmp * (dU[4] + RoeDens * rc * dU[1]);
+      R al[5] = {L[6] - cL, L[6], L[6], L[6], L[6] + cL};
+      R ar[5] = {Rr[6] - cR, Rr[6], Rr[6], Rr[6], Rr[6] + cR};
+      for (int v = 0; v < 5; ++v) {
+        R da = rmax(R(0.), rmax(a[v] - al[v], ar[v] - a[v]));
+        if (fabs(a[v]) < da) a[v] = R(0.5) * (a[v] * a[v] / da + da);
+        else a[v] = fabs(a[v]);
+      }
+    } else if (solver == RIEMANN_ROE) {
       R dU[6];
       for (int v = 0; v < 5; ++v) dU[v] = Rr[v] - L[v];
       dU[5] = dU[4] - (dU[2] - rv[1] * dU[0]) * rv[1] - (dU[3] - rv[2] * dU[0]) * rv[2];

@@ -25,12 +25,12 @@ class OrcConfig(ctypes.Structure):
                 ("Pr", ctypes.c_double), ("mu0", ctypes.c_double), ("CFLScale", ctypes.c_double), ("DFLScale", ctypes.c_double),
                 ("doTCSource", ctypes.c_int), ("dpdx", ctypes.c_double), ("overintType", ctypes.c_int), ("NUnder", ctypes.c_int),
                 ("iniExactFunc", ctypes.c_int), ("advVel", ctypes.c_double * 3), ("iniFrequency", ctypes.c_double),
-                ("iniAmplitude", ctypes.c_double), ("timeDisc", ctypes.c_int)]
+                ("iniAmplitude", ctypes.c_double), ("timeDisc", ctypes.c_int), ("riemannPhi", ctypes.c_double)]
 
 # keys a configuration may leave out (defaults of the reference: no overintegration, NUnder = N; no source term,
 # IniFrequency 1, IniAmplitude 0.1 of exact function 4)
 _OPTIONAL = {"overintType": 0, "NUnder": -1, "iniExactFunc": 0, "advVel": (0.0, 0.0, 0.0), "iniFrequency": 1.0, "iniAmplitude": 0.1,
-             "timeDisc": 0}
+             "timeDisc": 0, "riemannPhi": 5.0}
 
 
 def lib():

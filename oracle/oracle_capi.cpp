@@ -19,6 +19,7 @@ struct orc_config {
   int iniExactFunc;
   double advVel[3], iniFrequency, iniAmplitude;
   int timeDisc;
+  double riemannPhi;
 };
 
 static Config to_cfg(const orc_config* c) {
@@ -32,6 +33,7 @@ static Config to_cfg(const orc_config* c) {
   C.iniExactFunc = c->iniExactFunc;
   for (int d = 0; d < 3; ++d) C.advVel[d] = c->advVel[d];
   C.iniFrequency = c->iniFrequency; C.iniAmplitude = c->iniAmplitude;
+  C.riemannPhi = c->riemannPhi;
   return C;
 }
 

@@ -1,40 +1,41 @@
-"""fg_time_derivative_noalloc (allocation-free right-hand side) against fg_time_derivative.
+"""fg_time_derivative_noalloc (allocation-free right-hand side) against fg_time_derivative and the oracle.
 
-The allocation-free entry point takes caller-owned device arrays and keeps its intermediates in a static
-device scratch array. Each case evaluates it twice in a row on two different states and compares each
-result with the handle-based fg_time_derivative on the same state: max abs difference per conservative
-variable, normalised by that variable's max |Ut|, within 1e-12 (both run the same kernels, so the
-results are expected to agree to the last bit). This file is collected last so that it also runs after
-every other GPU test in one process; it passes alone in a fresh process as well."""
+The allocation-free entry point exists for callers that cannot let a library allocate device memory: host codes whose
+device memory all comes from their own pool or caching allocator, and time loops that must not allocate once they run.
+It takes caller-owned device arrays and keeps its intermediates in a static device scratch array. Each case evaluates it
+twice in a row on two different states and compares each result with the handle-based fg_time_derivative on the same
+state and with the CPU oracle: max abs difference per conservative variable, normalised by that variable's max |Ut|,
+within 1e-12. The allocation-free path forms the metric x 1/J products inside its kernels where the handle uses products
+formed at mesh upload, so the two differ by round-off and the oracle is the common reference. This file is collected last
+so that it also runs after every other GPU test in one process; it passes alone in a fresh process as well."""
 import ctypes
 
 import numpy as np
 import pytest
 
-from _cases import perturb_state, rel_err
+from _cases import oracle_cfg, perturb_state, rel_err
 from flexi_gb300 import _lib, mesh as fmesh, testcases
 from flexi_gb300.solver import Flexi, make_config
+from oracle import oracle as orc
 
 UT_TOL = 1e-12
 
 
-def _device_mesh(f, t_wall):
-    """fg_device_mesh of a Flexi handle's mesh, in caller-owned torch device memory."""
+def _device_mesh(f):
+    """fg_device_mesh of a Flexi handle's mesh (its own device tables copied out), in caller-owned torch device memory."""
     import torch
 
-    n2 = f.n * f.n
-    geo = np.empty((f.n_sides, 10, n2))
-    for k, name in enumerate(("NormVec", "TangVec1", "TangVec2")):
-        geo[:, 3 * k:3 * k + 3, :] = f.mesh_array(name).reshape(f.n_sides, n2, 3).transpose(0, 2, 1)
-    geo[:, 9, :] = f.mesh_array("SurfElem").reshape(f.n_sides, n2)
+    nb = max(f.n_bc_sides, 1)
+    bct = f.debug_array("bcType") if f.n_bc_sides else np.full(1, 4, np.int32)
+    bcw = f.debug_array("bcTwall") if f.n_bc_sides else np.ones(1)
     keep = {
         "elemSide": torch.from_numpy(f.debug_array("elemSide")).cuda(),
         "sideElem": torch.from_numpy(f.debug_array("sideElem")).cuda(),
         "metr": torch.from_numpy(f.debug_array("metr")).cuda(),
         "sJ": torch.from_numpy(f.debug_array("sJ")).cuda(),
-        "geo": torch.from_numpy(geo).cuda(),
-        "bcType": torch.full((max(f.n_bc_sides, 1),), 4, dtype=torch.int32, device="cuda"),
-        "bcTwall": torch.full((max(f.n_bc_sides, 1),), t_wall, dtype=torch.float64, device="cuda"),
+        "geo": torch.from_numpy(f.debug_array("geo")).cuda(),
+        "bcType": torch.from_numpy(np.ascontiguousarray(bct[:nb])).cuda(),
+        "bcTwall": torch.from_numpy(np.ascontiguousarray(bcw[:nb])).cuda(),
     }
     m = _lib.FgDeviceMesh(f.n_elems, f.n_sides, f.n_bc_sides, *[keep[k].data_ptr() for k in
                                                                   ("elemSide", "sideElem", "metr", "sJ", "geo", "bcType", "bcTwall")])
@@ -46,11 +47,23 @@ def _to_dev_layout(U, n_elems, n3):
     return np.ascontiguousarray(U.reshape(n_elems, n3, 5).transpose(0, 2, 1))
 
 
+def _channel_mixed_walls(t_wall):
+    """Channel box whose lower wall is isothermal (BC type 4) and upper wall adiabatic (BC type 3)."""
+    m = fmesh.channel_box((3, 4, 2), beta=1.5, ngeo=2, t_wall=t_wall)
+    m.boundary_type = np.array([[4, 1], [3, 1]], np.int32)
+    upper = m.elem_nb[:, 3, 2] == 1  # local side ETA_PLUS (4) of the top elements
+    m.elem_nb[upper, 3, 2] = 2
+    return m
+
+
 CASES = {
     # benchmark discretisation on a curved periodic box: N=7 Gauss-Lobatto, split form (Pirozzoli), BR2
     "gl7_split_pi_br2_curved": (dict(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roeentropyfix", Lifting="br2"), "tgv"),
     # weak form on Gauss nodes with isothermal no-slip walls, BR1
     "gauss3_weak_br1_channel": (dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="roe", Lifting="br1"), "channel"),
+    # split form SD on Gauss-Lobatto nodes, BR2 with its wall penalty, an isothermal and an adiabatic wall
+    "gl3_split_sd_br2_mixed_walls": (dict(N=3, NodeType="gauss-lobatto", SplitDG="sd", Riemann="hllc", Lifting="br2", etaBR2_wall=1.5),
+                                     "mixed"),
 }
 
 
@@ -64,8 +77,10 @@ def test_noalloc_matches_handle_two_calls(name):
     t_wall = 1.0
     if kind == "tgv":
         m = fmesh.tgv_box(3, ngeo=2, perturb=0.05, seed=3)
-    else:
+    elif kind == "channel":
         m = fmesh.channel_box((4, 4, 2), beta=1.5, ngeo=2, t_wall=t_wall)
+    else:
+        m = _channel_mixed_walls(t_wall)
     f = Flexi(c, m)
     xgp = f.elem_xgp()
     if kind == "tgv":
@@ -73,15 +88,20 @@ def test_noalloc_matches_handle_two_calls(name):
     else:
         base = testcases.channel_state(xgp, mach=0.1, kappa=c.kappa, R=c.R, t_wall=t_wall, noise=0.0, seed=0)
     states = [perturb_state(base, seed=21, amp=0.05), perturb_state(base, seed=22, amp=0.05)]
-    if kind == "channel":
+    if kind != "tgv":
         assert f.n_bc_sides > 0
+    if kind == "mixed":
+        assert set(f.debug_array("bcType").tolist()) == {3, 4}
     n3 = f.n ** 3
     L = _lib.load()
-    dmesh, keep = _device_mesh(f, t_wall)
-    refs = []
+    dmesh, keep = _device_mesh(f)
+    o = orc.Oracle(oracle_cfg(c), m)
+    refs, orcs = [], []
     for U in states:
         f.U = U
         refs.append(f.DGTimeDerivative_weakForm(0.0))
+        o.set_state(U)
+        orcs.append(o.time_derivative(0.0))
     U_devs = [torch.from_numpy(_to_dev_layout(U, f.n_elems, n3)).cuda() for U in states]
     Ut_devs = [torch.full_like(u, float("nan")) for u in U_devs]
     stream = torch.cuda.current_stream()
@@ -94,11 +114,13 @@ def test_noalloc_matches_handle_two_calls(name):
         assert rc == 0, L.fg_last_error(None)
         torch.cuda.synchronize()
         free.append((before, torch.cuda.mem_get_info()[0]))
-    for call, (ref, Ut_dev) in enumerate(zip(refs, Ut_devs)):
+    for call, (ref, ref_o, Ut_dev) in enumerate(zip(refs, orcs, Ut_devs)):
         got = Ut_dev.cpu().numpy().reshape(f.n_elems, 5, n3).transpose(0, 2, 1).reshape(ref.shape)
         assert np.isfinite(got).all(), f"call {call}: output not fully written"
         err = rel_err(got, ref)
-        assert err <= UT_TOL, f"call {call}: rel err {err:.3e}"
+        err_o = rel_err(got, ref_o)
+        assert err <= UT_TOL and err_o <= UT_TOL, f"call {call}: rel err {err:.3e} (handle), {err_o:.3e} (oracle)"
+        assert rel_err(ref, ref_o) <= UT_TOL
     # the second call (past the first-call set-up) left the device's free memory unchanged
     assert free[1][0] == free[1][1]
     del keep
