@@ -16,7 +16,7 @@ class FgConfig(ctypes.Structure):
                 ("OverintegrationType", ctypes.c_int), ("NUnder", ctypes.c_int), ("IniExactFunc", ctypes.c_int),
                 ("AdvVel", ctypes.c_double * 3), ("IniFrequency", ctypes.c_double), ("IniAmplitude", ctypes.c_double),
                 ("TEnd", ctypes.c_double), ("Analyze_dt", ctypes.c_double), ("dtmin", ctypes.c_double), ("dtkill", ctypes.c_double),
-                ("nCalcTimeStepMax", ctypes.c_int), ("maxIter", ctypes.c_int)]
+                ("nCalcTimeStepMax", ctypes.c_int), ("maxIter", ctypes.c_int), ("RiemannPhiFactor", ctypes.c_double)]
 
 
 class FgTimeDiscState(ctypes.Structure):

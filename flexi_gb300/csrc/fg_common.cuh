@@ -314,8 +314,17 @@ __host__ __device__ __forceinline__ void euler_flux_1d(const RotState& S, double
   F[4] = (S.E + S.p) * S.v1;
 }
 
+// central flux of the split form for any SplitDG (GEN) or for PI / SD only
+template <bool GEN>
+__host__ __device__ __forceinline__ void central_flux(int splitDG, const Basis& B, const RotState& L, const RotState& R, double HL, double HR,
+                                                      double* F) {
+  if (GEN && splitDG != SPLIT_PI && splitDG != SPLIT_SD) split_surface_flux_more(splitDG, B, L, R, F);
+  else split_surface_flux(splitDG, L, R, HL, HR, F);
+}
+
 // Riemann solvers of riemann.f90 (LF :558, HLLC :594, Roe :668, RoeEntropyFix :748) on rotated states.
-// split != 0: central part from the split surface flux (SPLIT_DG builds), as the reference does.
+// split != 0: central part from the split surface flux (SPLIT_DG builds), as the reference does; GEN: any SplitDG.
+template <bool GEN = false>
 __host__ __device__ __forceinline__ void riemann_rotated(int solver, int splitDG, const Basis& B, const RotState& L, const RotState& R, double* F) {
   const bool split = splitDG >= 0;
   const double HL = (L.E + L.p) * L.srho, HR = (R.E + R.p) * R.srho;
@@ -329,7 +338,7 @@ __host__ __device__ __forceinline__ void riemann_rotated(int solver, int splitDG
 #pragma unroll
       for (int v = 0; v < 5; ++v) F[v] = 0.5 * ((FL[v] + FR[v]) - lmax * dU[v]);
     } else {
-      split_surface_flux(splitDG, L, R, HL, HR, F);
+      central_flux<GEN>(splitDG, B, L, R, HL, HR, F);
       const double h = 0.5 * lmax;
 #pragma unroll
       for (int v = 0; v < 5; ++v) F[v] = F[v] - h * dU[v];
@@ -426,7 +435,174 @@ __host__ __device__ __forceinline__ void riemann_rotated(int solver, int splitDG
 #pragma unroll
     for (int v = 0; v < 5; ++v) F[v] = 0.5 * ((FL[v] + FR[v]) - D[v]);
   } else {
-    split_surface_flux(splitDG, L, R, HL, HR, F);
+    central_flux<GEN>(splitDG, B, L, R, HL, HR, F);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) F[v] = F[v] - 0.5 * D[v];
+  }
+}
+
+// The other Riemann solvers of riemann.f90 -- RoeL2 (:983), RoeEntropyGShockFix (:866), HLL (:1067), HLLE (:1119),
+// HLLEM (:1170), and with the split form the flux average (:1236), CH (:1261) and IR (:1315) -- and every solver with
+// the split fluxes MO, DU, KG, CH, IR, on rotated states.
+__host__ __device__ inline void riemann_rotated_more(int solver, int splitDG, const Basis& B, const RotState& L, const RotState& R, double* F) {
+  if (solver == RIEMANN_LF || solver == RIEMANN_HLLC || solver == RIEMANN_ROE || solver == RIEMANN_ROEENTROPYFIX) {
+    riemann_rotated<true>(solver, splitDG, B, L, R, F);
+    return;
+  }
+  const bool split = splitDG >= 0;
+  const double HL = (L.E + L.p) * L.srho, HR = (R.E + R.p) * R.srho;
+  if (solver == RIEMANN_AVERAGE) {
+    central_flux<true>(splitDG, B, L, R, HL, HR, F);
+    return;
+  }
+  const double cL = sqrt(B.kappa * L.p * L.srho), cR = sqrt(B.kappa * R.p * R.srho);
+  if (solver == RIEMANN_CH) {
+    const double lmax = fmax(fabs(R.v1), fabs(L.v1)) + fmax(cL, cR);
+    const double rhoMean = 0.5 * (L.rho + R.rho);
+    const double bL = 0.5 * L.rho / L.p, bR = 0.5 * R.rho / R.p;
+    const double betaLog = log_mean(bL, bR);
+    central_flux<true>(splitDG, B, L, R, HL, HR, F);
+    const double h = 0.5 * lmax;
+    const double dU[4] = {R.rho - L.rho, R.rho * R.v1 - L.rho * L.v1, R.rho * R.v2 - L.rho * L.v2, R.rho * R.v3 - L.rho * L.v3};
+#pragma unroll
+    for (int v = 0; v < 4; ++v) F[v] -= h * dU[v];
+    F[4] -= h * (dU[0] * (0.5 * B.sKappaM1 / betaLog + 0.5 * (R.v1 * L.v1 + R.v2 * L.v2 + R.v3 * L.v3)) +
+                 rhoMean * (0.5 * (L.v1 + R.v1) * (R.v1 - L.v1) + 0.5 * (L.v2 + R.v2) * (R.v2 - L.v2) + 0.5 * (L.v3 + R.v3) * (R.v3 - L.v3)) +
+                 0.5 * rhoMean * B.sKappaM1 * (1.0 / bR - 1.0 / bL));
+    return;
+  }
+  if (solver == RIEMANN_IR) {
+    const double sR = log(R.p) - B.kappa * log(R.rho), sL = log(L.p) - B.kappa * log(L.rho);
+    const double rpR = R.rho / R.p, rpL = L.rho / L.p;
+    double vJ[5];
+    vJ[0] = ((B.kappa - sR) - (B.kappa - sL)) * B.sKappaM1 - 0.5 * (rpR * (R.v1 * R.v1 + R.v2 * R.v2 + R.v3 * R.v3) -
+                                                                    rpL * (L.v1 * L.v1 + L.v2 * L.v2 + L.v3 * L.v3));
+    vJ[1] = rpR * R.v1 - rpL * L.v1;
+    vJ[2] = rpR * R.v2 - rpL * L.v2;
+    vJ[3] = rpR * R.v3 - rpL * L.v3;
+    vJ[4] = rpL - rpR;
+    const double zL1 = sqrt(rpL), zL5 = sqrt(L.rho * L.p), zR1 = sqrt(rpR), zR5 = sqrt(R.rho * R.p);
+    const double z1Log = log_mean(zL1, zR1), z5Log = log_mean(zL5, zR5);
+    const double z1s = zL1 + zR1;
+    const double rhoHat = 0.5 * z1s * z5Log;
+    const double uH = (zL1 * L.v1 + zR1 * R.v1) / z1s, vH = (zL1 * L.v2 + zR1 * R.v2) / z1s, wH = (zL1 * L.v3 + zR1 * R.v3) / z1s;
+    const double pHat = (zL5 + zR5) / z1s;
+    const double p2Hat = 0.5 / B.kappa * ((B.kappa + 1.0) * z5Log / z1Log + B.kappaM1 * pHat);
+    const double aH = sqrt(B.kappa * p2Hat / rhoHat);
+    const double ek = 0.5 * (uH * uH + vH * vH + wH * wH);
+    const double hH = B.kappa * p2Hat / (rhoHat * B.kappaM1) + ek;
+    // R = [r1 .. r5] (columns): r1 = (1, u-a, v, w, h-ua), r2 = (1, u, v, w, ek), r3 = e3 + v e5, r4 = e4 + w e5,
+    // r5 = (1, u+a, v, w, h+ua); dissipation R diag(D) R^T vJump
+    const double c0 = vJ[0] + (uH - aH) * vJ[1] + vH * vJ[2] + wH * vJ[3] + (hH - uH * aH) * vJ[4];
+    const double c1 = vJ[0] + uH * vJ[1] + vH * vJ[2] + wH * vJ[3] + ek * vJ[4];
+    const double c2 = vJ[2] + vH * vJ[4];
+    const double c3 = vJ[3] + wH * vJ[4];
+    const double c4 = vJ[0] + (uH + aH) * vJ[1] + vH * vJ[2] + wH * vJ[3] + (hH + uH * aH) * vJ[4];
+    const double d0 = 0.5 * fabs(uH - aH) * rhoHat / B.kappa * c0;
+    const double d1 = fabs(uH) * (B.kappaM1 / B.kappa) * rhoHat * c1;
+    const double d2 = fabs(uH) * pHat * c2;
+    const double d3 = fabs(uH) * pHat * c3;
+    const double d4 = 0.5 * fabs(uH + aH) * rhoHat / B.kappa * c4;
+    const double sum014 = d0 + d1 + d4;
+    double Dd[5];
+    Dd[0] = sum014;
+    Dd[1] = (uH - aH) * d0 + uH * d1 + (uH + aH) * d4;
+    Dd[2] = vH * sum014 + d2;
+    Dd[3] = wH * sum014 + d3;
+    Dd[4] = (hH - uH * aH) * d0 + ek * d1 + vH * d2 + wH * d3 + (hH + uH * aH) * d4;
+    central_flux<true>(splitDG, B, L, R, HL, HR, F);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) F[v] -= 0.5 * Dd[v];
+    return;
+  }
+  double FL[5], FR[5];
+  euler_flux_1d(L, FL);
+  euler_flux_1d(R, FR);
+  const double sqL = sqrt(L.rho), sqR = sqrt(R.rho);
+  const double ssq = 1.0 / (sqL + sqR);
+  const double r1v = (sqR * R.v1 + sqL * L.v1) * ssq;
+  const double r2v = (sqR * R.v2 + sqL * L.v2) * ssq;
+  const double r3v = (sqR * R.v3 + sqL * L.v3) * ssq;
+  const double rH = (sqR * HR + sqL * HL) * ssq;
+  const double absVel = r1v * r1v + r2v * r2v + r3v * r3v;
+  const double rc = sqrt(B.kappaM1 * (rH - 0.5 * absVel));
+  const double dU[5] = {R.rho - L.rho, R.rho * R.v1 - L.rho * L.v1, R.rho * R.v2 - L.rho * L.v2, R.rho * R.v3 - L.rho * L.v3, R.E - L.E};
+  if (solver == RIEMANN_HLL || solver == RIEMANN_HLLE || solver == RIEMANN_HLLEM) {
+    double Ssl = r1v - rc, Ssr = r1v + rc;
+    if (solver != RIEMANN_HLL) {
+      const double beta = sqrt(0.5 * B.kappaM1 / B.kappa);
+      Ssl = fmin(fmin(Ssl, L.v1 - beta * cL), 0.0);
+      Ssr = fmax(fmax(Ssr, R.v1 + beta * cR), 0.0);
+    }
+    if (Ssl >= 0.0) {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) F[v] = FL[v];
+    } else if (Ssr <= 0.0) {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) F[v] = FR[v];
+    } else {
+      double J[5] = {dU[0], dU[1], dU[2], dU[3], dU[4]};
+      if (solver == RIEMANN_HLLEM) {
+        const double RoeDens = sqL * sqR;
+        const double delta = rc / (rc + fabs(0.5 * (Ssl + Ssr)));
+        const double A2 = (R.rho - L.rho) - (R.p - L.p) / (rc * rc);
+        const double A3 = RoeDens * (R.v2 - L.v2), A4 = RoeDens * (R.v3 - L.v3);
+        J[0] -= delta * A2;
+        J[1] -= delta * r1v * A2;
+        J[2] -= delta * (r2v * A2 + A3);
+        J[3] -= delta * (r3v * A2 + A4);
+        J[4] -= delta * (0.5 * absVel * A2 + r2v * A3 + r3v * A4);
+      }
+      const double sd = 1.0 / (Ssr - Ssl), ss = Ssl * Ssr;
+#pragma unroll
+      for (int v = 0; v < 5; ++v) F[v] = (Ssr * FL[v] - Ssl * FR[v] + ss * J[v]) * sd;
+    }
+    return;
+  }
+  // RoeL2 / RoeEntropyGShockFix: Roe-type dissipation sum_k Alpha_k |a_k| r_k
+  double a0 = r1v - rc, a1 = r1v, a4 = r1v + rc;
+  double A0, A1, A2, A3, A4, e0, e1, e4;
+  if (solver == RIEMANN_ROEL2) {
+    const double d5 = dU[4] - (dU[2] - r2v * dU[0]) * r2v - (dU[3] - r3v * dU[0]) * r3v;
+    const double Ma = sqrt(absVel) / (rc * sqrt(B.kappa));
+    const double d1 = dU[1] * Ma, d2 = dU[2] * Ma, d3 = dU[3] * Ma;
+    A2 = d2 - r2v * dU[0];
+    A3 = d3 - r3v * dU[0];
+    A1 = B.kappaM1 / (rc * rc) * (dU[0] * (rH - r1v * r1v) - d5 + r1v * d1);
+    A0 = 0.5 / rc * (dU[0] * (r1v + rc) - d1 - rc * A1);
+    A4 = dU[0] - A0 - A1;
+    e0 = fabs(a0); e1 = fabs(a1); e4 = fabs(a4);
+  } else {  // RoeEntropyGShockFix
+    const double am = (r1v < 0.0 ? -1.0 : 1.0) * fmax(rc / B.riemannPhi, fabs(r1v));
+    a0 = am - rc; a1 = am; a4 = am + rc;
+    const double RoeDens = sqL * sqR;
+    const double dr = R.rho - L.rho, du = R.v1 - L.v1, dv = R.v2 - L.v2, dw = R.v3 - L.v3, dp = R.p - L.p;
+    const double tmp = 0.5 / (rc * rc);
+    A0 = tmp * (dp - RoeDens * rc * du);
+    A1 = dr - dp * (2.0 * tmp);
+    A2 = RoeDens * dv;
+    A3 = RoeDens * dw;
+    A4 = tmp * (dp + RoeDens * rc * du);
+    auto fix = [](double a, double al, double ar) {
+      const double da = fmax(0.0, fmax(a - al, ar - a));
+      return fabs(a) < da ? 0.5 * (a * a / da + da) : fabs(a);
+    };
+    e0 = fix(a0, L.v1 - cL, R.v1 - cR);
+    e1 = fix(a1, L.v1, R.v1);
+    e4 = fix(a4, L.v1 + cL, R.v1 + cR);
+  }
+  const double w0 = A0 * e0, w1 = A1 * e1, w2 = A2 * e1, w3 = A3 * e1, w4 = A4 * e4;
+  double D[5];
+  D[0] = w0 + w1 + w4;
+  D[1] = w0 * a0 + w1 * r1v + w4 * a4;
+  D[2] = (w0 + w1 + w4) * r2v + w2;
+  D[3] = (w0 + w1 + w4) * r3v + w3;
+  D[4] = w0 * (rH - r1v * rc) + w1 * (0.5 * absVel) + w2 * r2v + w3 * r3v + w4 * (rH + r1v * rc);
+  if (!split) {
+#pragma unroll
+    for (int v = 0; v < 5; ++v) F[v] = 0.5 * ((FL[v] + FR[v]) - D[v]);
+  } else {
+    central_flux<true>(splitDG, B, L, R, HL, HR, F);
 #pragma unroll
     for (int v = 0; v < 5; ++v) F[v] = F[v] - 0.5 * D[v];
   }
@@ -443,6 +619,113 @@ __host__ __device__ __forceinline__ double pressure_riemann(const Basis& B, doub
   return p + vn / ar * 0.5 * (vn + sqrt(vn * vn + 4.0 * ar * (p + br)));
 }
 
+// Two-point volume fluxes of the split form in contravariant form (split kernels; the point harness checks them on
+// the CPU): SplitVolumeFluxPI / SD and, for the other kinds, their per-node inputs, constant factors and pair flux.
+__host__ __device__ __forceinline__ void split_pair_flux(bool pi, double ra, double ua, double va, double wa, double pa, double ha, double rb,
+                                                double ub, double vb, double wb, double pb, double hb, double ms0, double ms1,
+                                                double ms2, double* G) {
+  if (pi) {
+    const double rs = ra + rb, us = ua + ub, vs = va + vb, ws = wa + wb, ps4 = pa + pb, hs = ha + hb;
+    const double qs = us * ms0 + vs * ms1 + ws * ms2;
+    const double A = rs * qs;
+    G[0] = A;
+    G[1] = fma(A, us, ps4 * ms0);
+    G[2] = fma(A, vs, ps4 * ms1);
+    G[3] = fma(A, ws, ps4 * ms2);
+    G[4] = A * hs;
+  } else {
+    const double qa = ua * ms0 + va * ms1 + wa * ms2, qb = ub * ms0 + vb * ms1 + wb * ms2;
+    const double mqa = ra * qa, mqb = rb * qb;
+    G[0] = mqa + mqb;
+    G[1] = fma(mqa, ua, mqb * ub) + (pa + pb) * ms0;
+    G[2] = fma(mqa, va, mqb * vb) + (pa + pb) * ms1;
+    G[3] = fma(mqa, wa, mqb * wb) + (pa + pb) * ms2;
+    G[4] = fma(ha, qa, hb * qb);
+  }
+}
+
+// The other two-point volume fluxes of splitflux.f90 (MO :445, DU :225, KG :327, CH :703, IR :822) in the same
+// contravariant form, on the per-node inputs of split_node_inputs (q0, u, v, w, q4, q5); the constant factors of
+// split_factors are applied by the kernels' pre-scaled coefficients. IR carries no factor 2, as in the reference.
+__host__ __device__ __forceinline__ void split_node_inputs(int sd, double rho, double u, double v, double w, double p, double E, double srho, double& q0,
+                                                  double& q4, double& q5) {
+  q0 = rho;
+  switch (sd) {
+    case SPLIT_PI: q4 = 4.0 * p; q5 = (E + p) * srho; break;
+    case SPLIT_DU: q4 = 2.0 * p; q5 = E + p; break;
+    case SPLIT_KG: q4 = 4.0 * p; q5 = E * srho; break;
+    case SPLIT_MO: q4 = 2.0 * p; q5 = 2.0 * (E - 0.5 * rho * (u * u + v * v + w * w) + p); break;
+    case SPLIT_CH: q4 = 0.5 * rho / p; q5 = 0.; break;
+    case SPLIT_IR: q0 = sqrt(rho / p); q4 = sqrt(rho * p); q5 = 0.; break;
+    default: q4 = p; q5 = E + p; break;  // SD
+  }
+}
+__host__ __device__ __forceinline__ void split_factors(int sd, double& f0, double& f1) {
+  switch (sd) {
+    case SPLIT_PI: f0 = 0.25; f1 = 0.125; break;
+    case SPLIT_DU: f0 = 0.25; f1 = 0.25; break;
+    case SPLIT_KG: f0 = 0.25; f1 = 0.125; break;
+    case SPLIT_MO: f0 = 0.5; f1 = 0.25; break;
+    default: f0 = 0.5; f1 = 0.5; break;  // SD, CH, IR
+  }
+}
+__host__ __device__ __forceinline__ void split_pair_flux_gen(int sd, const Basis& B, double ra, double ua, double va, double wa, double pa, double ha,
+                                                    double rb, double ub, double vb, double wb, double pb, double hb, double ms0, double ms1,
+                                                    double ms2, double* G) {
+  if (sd == SPLIT_PI || sd == SPLIT_SD) {
+    split_pair_flux(sd == SPLIT_PI, ra, ua, va, wa, pa, ha, rb, ub, vb, wb, pb, hb, ms0, ms1, ms2, G);
+    return;
+  }
+  const double us = ua + ub, vs = va + vb, ws = wa + wb;
+  const double qs = us * ms0 + vs * ms1 + ws * ms2;
+  if (sd == SPLIT_DU) {
+    const double ps = pa + pb;
+    G[0] = (ra + rb) * qs;
+    G[1] = fma(ra * ua + rb * ub, qs, ps * ms0);
+    G[2] = fma(ra * va + rb * vb, qs, ps * ms1);
+    G[3] = fma(ra * wa + rb * wb, qs, ps * ms2);
+    G[4] = (ha + hb) * qs;
+  } else if (sd == SPLIT_KG) {
+    const double A = (ra + rb) * qs, ps = pa + pb;
+    G[0] = A;
+    G[1] = fma(A, us, ps * ms0);
+    G[2] = fma(A, vs, ps * ms1);
+    G[3] = fma(A, ws, ps * ms2);
+    G[4] = fma(A, ha + hb, 0.5 * ps * qs);
+  } else if (sd == SPLIT_MO) {
+    const double qa = ua * ms0 + va * ms1 + wa * ms2, qb = ub * ms0 + vb * ms1 + wb * ms2;
+    const double mq = ra * qa + rb * qb, ps = pa + pb;
+    G[0] = mq;
+    G[1] = fma(mq, us, ps * ms0);
+    G[2] = fma(mq, vs, ps * ms1);
+    G[3] = fma(mq, ws, ps * ms2);
+    G[4] = fma(ha, qa, fma(hb, qb, mq * (ua * ub + va * vb + wa * wb)));
+  } else if (sd == SPLIT_CH) {
+    const double rhoLog = log_mean(ra, rb), betaLog = log_mean(pa, pb);
+    const double pHat = 0.5 * (ra + rb) / (pa + pb);
+    const double H = 0.5 * B.sKappaM1 / betaLog + pHat / rhoLog + 0.5 * (ua * ub + va * vb + wa * wb);
+    const double A = rhoLog * qs, hA = 0.5 * A, p2 = 2.0 * pHat;
+    G[0] = A;
+    G[1] = fma(hA, us, p2 * ms0);
+    G[2] = fma(hA, vs, p2 * ms1);
+    G[3] = fma(hA, ws, p2 * ms2);
+    G[4] = A * H;
+  } else {  // IR: q0 = sqrt(rho/p), q4 = sqrt(rho p)
+    const double z1Log = log_mean(ra, rb), z5Log = log_mean(pa, pb);
+    const double z1s = ra + rb;
+    const double rhoHat = 0.5 * z1s * z5Log;
+    const double pHat = (pa + pb) / z1s;
+    const double p2Hat = 0.5 / B.kappa * ((B.kappa + 1.0) * z5Log / z1Log + B.kappaM1 * pHat);
+    const double uH = (ra * ua + rb * ub) / z1s, vH = (ra * va + rb * vb) / z1s, wH = (ra * wa + rb * wb) / z1s;
+    const double hH = B.kappa * p2Hat / (rhoHat * B.kappaM1) + 0.5 * (uH * uH + vH * vH + wH * wH);
+    const double A = rhoHat * (uH * ms0 + vH * ms1 + wH * ms2);
+    G[0] = A;
+    G[1] = fma(A, uH, pHat * ms0);
+    G[2] = fma(A, vH, pHat * ms1);
+    G[3] = fma(A, wH, pHat * ms2);
+    G[4] = A * hH;
+  }
+}
 __device__ __forceinline__ void set_error(int* err, int code) { atomicCAS(err, 0, code); }
 
 }  // namespace fg

@@ -529,6 +529,7 @@ void init_basis(fg_handle* h) {
   B.sKappaP1 = 1. / (c.kappa + 1.);
   B.logEntC = std::log(c.kappa - 1.) / (c.kappa - 1.);
   B.kappa_kappaM1 = c.kappa / (c.kappa - 1.);
+  B.riemannPhi = c.RiemannPhiFactor;
   // the low-storage scheme of TimeDiscMethod (timedisc_vars.f90:137-457)
   const fgh::LSERKScheme* sch = fgh::lserk_scheme(c.TimeDiscMethod);
   h->nStages = sch->stages;
@@ -575,6 +576,11 @@ int upload_mesh(fg_handle* h) {
   d.nFluxSides = M.nFluxSides; d.nMortars = M.nMortars;
   int r = 0;
   if (M.nMortars > 0) {
+    const fg_config& c = h->cfg;
+    const bool baseRiemann = c.Riemann == FG_RIEMANN_LF || c.Riemann == FG_RIEMANN_HLLC || c.Riemann == FG_RIEMANN_ROE ||
+                             c.Riemann == FG_RIEMANN_ROEENTROPYFIX;
+    if (!baseRiemann || (c.SplitDG != FG_SPLIT_NONE && c.SplitDG != FG_SPLIT_SD && c.SplitDG != FG_SPLIT_PI))
+      return fail(h, FG_ERR_CONFIG, "mortar interfaces support the Riemann solvers LF, HLLC, Roe, RoeEntropyFix and SplitDG SD or PI");
     // mortar.f90:InitMortar: M_0_1/M_0_2 interpolate to the halves [-1,0]/[0,1]; M_1_0/M_2_0 = (Vdm_Leg
     // Vphi^T W VGP)^T project back, with Vphi the orthonormal Legendre polynomials at the Gauss points mapped
     // to each half, W the Gauss weights and VGP the interpolation from the solution nodes to the Gauss points
@@ -881,6 +887,15 @@ int check_err(fg_handle* h) {
   return 0;
 }
 
+bool riemann_known(int r) {
+  switch (r) {
+    case FG_RIEMANN_LF: case FG_RIEMANN_HLLC: case FG_RIEMANN_ROE: case FG_RIEMANN_ROEENTROPYFIX: case FG_RIEMANN_ROEL2:
+    case FG_RIEMANN_ROEENTROPYGSHOCKFIX: case FG_RIEMANN_HLL: case FG_RIEMANN_HLLE: case FG_RIEMANN_HLLEM: case FG_RIEMANN_CH:
+    case FG_RIEMANN_IR: case FG_RIEMANN_AVERAGE: return true;
+    default: return false;
+  }
+}
+
 std::string lower(std::string s) {
   for (char& c : s) c = (char)std::tolower((unsigned char)c);
   return s;
@@ -898,9 +913,11 @@ void set_error_without_handle(const char* msg) { g_err = msg; }
 
 namespace {
 
-// the adjoint kernels cover: weak form and split form PI, LF/Roe/RoeEntropyFix, BR1/BR2
+// the adjoint kernels cover: weak form and split form PI, LF/HLLC/Roe/RoeEntropyFix, BR1/BR2
 const char* adjoint_unsupported(const fg_config& c) {
   if (c.N > 7) return "the adjoint supports N = 1..7";
+  if (c.Riemann != FG_RIEMANN_LF && c.Riemann != FG_RIEMANN_HLLC && c.Riemann != FG_RIEMANN_ROE && c.Riemann != FG_RIEMANN_ROEENTROPYFIX)
+    return "the adjoint supports the Riemann solvers LF, HLLC, Roe and RoeEntropyFix";
   if (c.doWeakLifting || c.doConservativeLifting) return "the adjoint supports the strong, non-conservative lifting";
   if (c.SplitDG != FG_SPLIT_NONE && c.SplitDG != FG_SPLIT_PI) return "the adjoint supports the weak form and the split form PI";
   if (c.SplitDG != FG_SPLIT_NONE && (c.NodeType != FG_NODE_GAUSS_LOBATTO || (c.N != 1 && c.N != 3 && c.N != 7)))
@@ -1003,6 +1020,7 @@ int fg_config_default(fg_config* c) {
   c->OverintegrationType = 0; c->NUnder = -1;
   c->IniExactFunc = 0; c->AdvVel[0] = c->AdvVel[1] = c->AdvVel[2] = 0.; c->IniFrequency = 1.; c->IniAmplitude = 0.1;
   c->TEnd = INFINITY; c->Analyze_dt = 0.; c->dtmin = -1.; c->dtkill = -1.; c->nCalcTimeStepMax = 1; c->maxIter = -1;
+  c->RiemannPhiFactor = 5.;
   return FG_OK;
 }
 
@@ -1025,12 +1043,25 @@ int fg_config_from_ini(const char* text, fg_config* c) {
         else if (lv == "hllc") id = FG_RIEMANN_HLLC;
         else if (lv == "roe") id = FG_RIEMANN_ROE;
         else if (lv == "roeentropyfix") id = FG_RIEMANN_ROEENTROPYFIX;
+        else if (lv == "roel2") id = FG_RIEMANN_ROEL2;
+        else if (lv == "roeentropygshockfix") id = FG_RIEMANN_ROEENTROPYGSHOCKFIX;
+        else if (lv == "hll") id = FG_RIEMANN_HLL;
+        else if (lv == "hlle") id = FG_RIEMANN_HLLE;
+        else if (lv == "hllem") id = FG_RIEMANN_HLLEM;
+        else if (lv == "ch") id = FG_RIEMANN_CH;
+        else if (lv == "ir") id = FG_RIEMANN_IR;
+        else if (lv == "avg") id = FG_RIEMANN_AVERAGE;
         else if (lv == "same") id = FG_RIEMANN_SAME;
         else id = std::stoi(val);
         (key == "riemann" ? c->Riemann : c->RiemannBC) = id;
       } else if (key == "splitdg") {
         if (lv == "sd") c->SplitDG = FG_SPLIT_SD;
+        else if (lv == "mo") c->SplitDG = FG_SPLIT_MO;
+        else if (lv == "du") c->SplitDG = FG_SPLIT_DU;
+        else if (lv == "kg") c->SplitDG = FG_SPLIT_KG;
         else if (lv == "pi") c->SplitDG = FG_SPLIT_PI;
+        else if (lv == "ch") c->SplitDG = FG_SPLIT_CH;
+        else if (lv == "ir") c->SplitDG = FG_SPLIT_IR;
         else if (lv == "none" || lv == "off") c->SplitDG = FG_SPLIT_NONE;
         else c->SplitDG = std::stoi(val);
       } else if (key == "lifting") c->Lifting = (lv == "br2" || lv == "2") ? 2 : 1;
@@ -1060,6 +1091,7 @@ int fg_config_from_ini(const char* text, fg_config* c) {
       else if (key == "dtkill") c->dtkill = std::stod(val);
       else if (key == "ncalctimestepmax") c->nCalcTimeStepMax = std::stoi(val);
       else if (key == "maxiter") c->maxIter = std::stoi(val);
+      else if (key == "riemannphifactor") c->RiemannPhiFactor = std::stod(val);
       else if (key == "advvel") {  // (/a,b,c/)
         std::string v = val;
         for (char& ch : v) if (ch == '(' || ch == ')' || ch == '/' || ch == ',') ch = ' ';
@@ -1084,10 +1116,14 @@ int fg_create(const fg_config* cfg, fg_handle** out) {
   std::string why;
   if (c.N < 1 || c.N > 11) why = "N must be in 1..11";
   else if (c.NodeType != FG_NODE_GAUSS && c.NodeType != FG_NODE_GAUSS_LOBATTO) why = "NodeType must be 1 (Gauss) or 2 (Gauss-Lobatto)";
-  else if (c.Riemann != FG_RIEMANN_LF && c.Riemann != FG_RIEMANN_HLLC && c.Riemann != FG_RIEMANN_ROE && c.Riemann != FG_RIEMANN_ROEENTROPYFIX)
-    why = "Riemann must be LF, HLLC, Roe or RoeEntropyFix";
+  else if (!riemann_known(c.Riemann))
+    why = "Riemann must be one of LF, HLLC, Roe, RoeEntropyFix, RoeL2, RoeEntropyGShockFix, HLL, HLLE, HLLEM (and with the split form CH, IR, avg)";
+  else if (c.SplitDG == FG_SPLIT_NONE && (c.Riemann == FG_RIEMANN_CH || c.Riemann == FG_RIEMANN_IR || c.Riemann == FG_RIEMANN_AVERAGE))
+    why = "the Riemann solvers CH, IR and avg need the split form (riemann.f90:204-223)";
+  else if (c.RiemannBC != FG_RIEMANN_SAME && !riemann_known(c.RiemannBC)) why = "RiemannBC must be Same or one of the Riemann solvers";
   else if (c.Lifting != 1 && c.Lifting != 2) why = "Lifting must be 1 (BR1) or 2 (BR2)";
-  else if (c.SplitDG != FG_SPLIT_NONE && c.SplitDG != FG_SPLIT_SD && c.SplitDG != FG_SPLIT_PI) why = "SplitDG must be -1 (weak), 0 (SD) or 4 (PI)";
+  else if (c.SplitDG < FG_SPLIT_NONE || c.SplitDG > FG_SPLIT_IR) why = "SplitDG must be -1 (weak), 0 SD, 1 MO, 2 DU, 3 KG, 4 PI, 5 CH or 6 IR";
+  else if (c.Riemann == FG_RIEMANN_ROEENTROPYGSHOCKFIX && !(c.RiemannPhiFactor > 0.)) why = "RiemannPhiFactor must be > 0";
   else if (!fgh::lserk_scheme(c.TimeDiscMethod))
     why = "TimeDiscMethod must be one of the low-storage schemes 0..5 (carpenterrk4-5, standardrk3-3, niegemannrk4-14, "
           "toulorgerk4-8c, toulorgerk3-7c, toulorgerk4-8f)";

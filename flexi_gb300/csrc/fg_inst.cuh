@@ -54,9 +54,16 @@ struct Inst {
     using SE = Shape<n, E>;
     k_vol_weak<n, GL, E><<<(d.nElems + SE::EPB - 1) / SE::EPB, SE::THREADS, smem_weak_E<E>(), st>>>(d, B, Stage{mode, rkA, rkB});
   }
+  // the Riemann solvers and split fluxes beyond LF/HLLC/Roe/RoeEntropyFix with the weak form, SD or PI
+  static bool flux_more(const Basis& B) {
+    const bool base = B.riemann == RIEMANN_LF || B.riemann == RIEMANN_HLLC || B.riemann == RIEMANN_ROE || B.riemann == RIEMANN_ROEENTROPYFIX;
+    return !base || (B.splitDG >= 0 && B.splitDG != SPLIT_SD && B.splitDG != SPLIT_PI);
+  }
+  static bool split_more(const Basis& B) { return B.splitDG != SPLIT_SD && B.splitDG != SPLIT_PI; }
   static void flux_block(const Dev& d, const Basis& B, int block, cudaStream_t st) {
     const long long pts = (long long)d.nFluxSides * S::n2;
-    k_flux<n><<<(unsigned)((pts + block - 1) / block), block, 0, st>>>(d, B);
+    if (flux_more(B)) k_flux<n, true><<<(unsigned)((pts + block - 1) / block), block, 0, st>>>(d, B);
+    else k_flux<n><<<(unsigned)((pts + block - 1) / block), block, 0, st>>>(d, B);
   }
   template <class K>
   static void set_smem(K kern, size_t bytes) {
@@ -66,8 +73,13 @@ struct Inst {
     set_smem(k_prep<n, GL>, smem_prep());
     set_smem(k_lift<n, GL, 0, LIFT12>, smem_lift());
     set_smem(k_vol_weak<n, GL>, smem_weak());
-    if constexpr (SPLIT_POW2) set_smem(k_vol_split<n>, smem_split());
-    else set_smem(k_vol_split_gen<n, GL>, smem_split_gen());
+    if constexpr (SPLIT_POW2) {
+      set_smem(k_vol_split<n>, smem_split());
+      set_smem(k_vol_split<n, true>, smem_split());
+    } else {
+      set_smem(k_vol_split_gen<n, GL>, smem_split_gen());
+      set_smem(k_vol_split_gen<n, GL, true>, smem_split_gen());
+    }
     set_smem(k_overint<n>, smem_overint());
     set_smem(k_lift<n, GL, 0, true>, smem_lift_mortar());
     set_smem(k_lift<n, GL, 0, false, true>, smem_lift_v(false, true));
@@ -115,14 +127,21 @@ struct Inst {
   }
   static void flux(const Dev& d, const Basis& B, cudaStream_t st) {
     const long long pts = (long long)d.nFluxSides * S::n2;
-    k_flux<n><<<(unsigned)((pts + 127) / 128), 128, 0, st>>>(d, B);
+    if (flux_more(B)) k_flux<n, true><<<(unsigned)((pts + 127) / 128), 128, 0, st>>>(d, B);
+    else k_flux<n><<<(unsigned)((pts + 127) / 128), 128, 0, st>>>(d, B);
   }
   static void vol_weak(const Dev& d, const Basis& B, int mode, double rkA, double rkB, cudaStream_t st) {
     k_vol_weak<n, GL><<<blocks(d), S::THREADS, smem_weak(), st>>>(d, B, Stage{mode, rkA, rkB});
   }
   static void vol_split(const Dev& d, const Basis& B, int mode, double rkA, double rkB, cudaStream_t st) {
-    if constexpr (SPLIT_POW2) k_vol_split<n><<<blocks(d), S::THREADS, smem_split(), st>>>(d, B, Stage{mode, rkA, rkB});
-    else k_vol_split_gen<n, GL><<<blocks(d), SplitShape<n>::THREADS, smem_split_gen(), st>>>(d, B, Stage{mode, rkA, rkB});
+    const Stage sg{mode, rkA, rkB};
+    if (split_more(B)) {
+      if constexpr (SPLIT_POW2) k_vol_split<n, true><<<blocks(d), S::THREADS, smem_split(), st>>>(d, B, sg);
+      else k_vol_split_gen<n, GL, true><<<blocks(d), SplitShape<n>::THREADS, smem_split_gen(), st>>>(d, B, sg);
+      return;
+    }
+    if constexpr (SPLIT_POW2) k_vol_split<n><<<blocks(d), S::THREADS, smem_split(), st>>>(d, B, sg);
+    else k_vol_split_gen<n, GL><<<blocks(d), SplitShape<n>::THREADS, smem_split_gen(), st>>>(d, B, sg);
   }
   // mortar interfaces (one CTA of 256 threads per big mortar side)
   static size_t smem_lift_mortar() { return dyn_smem_bytes<n>(Big<n>::liftMortar); }

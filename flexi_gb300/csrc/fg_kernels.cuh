@@ -490,7 +490,8 @@ __global__ void __launch_bounds__(Shape<n, E>::THREADS, (n == 8 && GL ? 2 : 1)) 
 // (the mortar sides are k_mortar_face's).
 // =====================================================================================================
 // numerical flux times SurfElem of point pq of side s, with the master's face gradients gL (12 values)
-template <int n>
+// MORE: the Riemann solvers and split central fluxes beyond LF/HLLC/Roe/RoeEntropyFix with SD/PI (riemann_rotated_more)
+template <int n, bool MORE = false>
 __device__ __forceinline__ void side_flux(const Dev& d, const Basis& B, int s, int pq, const double* gL, double* Fout) {
   constexpr int n2 = n * n;
   const double* gm = d.geo + (size_t)s * FG_NF * n2 + pq;
@@ -530,7 +531,8 @@ __device__ __forceinline__ void side_flux(const Dev& d, const Basis& B, int s, i
     R.v2 = uR * t1[0] + vR * t1[1] + wR * t1[2];
     R.v3 = uR * t2[0] + vR * t2[1] + wR * t2[2];
     double Fr[5];
-    riemann_rotated(B.riemann, B.splitDG, B, L, R, Fr);
+    if constexpr (MORE) riemann_rotated_more(B.riemann, B.splitDG, B, L, R, Fr);
+    else riemann_rotated(B.riemann, B.splitDG, B, L, R, Fr);
     F[0] = Fr[0];
 #pragma unroll
     for (int c = 0; c < 3; ++c) F[1 + c] = nv[c] * Fr[1] + t1[c] * Fr[2] + t2[c] * Fr[3];
@@ -549,7 +551,7 @@ __device__ __forceinline__ void side_flux(const Dev& d, const Basis& B, int s, i
   for (int v = 0; v < 5; ++v) Fout[v] = F[v] * se;
 }
 
-template <int n>
+template <int n, bool MORE = false>
 __global__ void __launch_bounds__(256) k_flux(Dev d, Basis B) {
   constexpr int n2 = n * n;
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
@@ -558,7 +560,7 @@ __global__ void __launch_bounds__(256) k_flux(Dev d, Basis B) {
   double gL[12], F[5];
 #pragma unroll
   for (int c = 0; c < 12; ++c) gL[c] = d.gradM[((size_t)s * 12 + c) * n2 + pq];
-  side_flux<n>(d, B, s, pq, gL, F);
+  side_flux<n, MORE>(d, B, s, pq, gL, F);
 #pragma unroll
   for (int v = 0; v < 5; ++v) d.flux[((size_t)s * 5 + v) * n2 + pq] = F[v];
 }
@@ -948,30 +950,13 @@ __global__ void __launch_bounds__(Shape<n, E>::THREADS) k_vol_weak(Dev d, Basis 
 }
 
 // two-point volume flux of a node pair in contravariant form, without its constant factor (in the scaled
-// DVolSurf): PI (splitflux.f90:SplitVolumeFluxPI): A = rho_s q_s; A u_s + 4 p_s m_s; A H_s, with the node
-// values rho, u, v, w, 4p-term p, H-term h; SD (SplitVolumeFluxSD): m_s . (F(a) + F(b)), p and rho E + p.
-// ms = metric vector sum of the pair.
-__device__ __forceinline__ void split_pair_flux(bool pi, double ra, double ua, double va, double wa, double pa, double ha, double rb,
-                                                double ub, double vb, double wb, double pb, double hb, double ms0, double ms1,
-                                                double ms2, double* G) {
-  if (pi) {
-    const double rs = ra + rb, us = ua + ub, vs = va + vb, ws = wa + wb, ps4 = pa + pb, hs = ha + hb;
-    const double qs = us * ms0 + vs * ms1 + ws * ms2;
-    const double A = rs * qs;
-    G[0] = A;
-    G[1] = fma(A, us, ps4 * ms0);
-    G[2] = fma(A, vs, ps4 * ms1);
-    G[3] = fma(A, ws, ps4 * ms2);
-    G[4] = A * hs;
-  } else {
-    const double qa = ua * ms0 + va * ms1 + wa * ms2, qb = ub * ms0 + vb * ms1 + wb * ms2;
-    const double mqa = ra * qa, mqb = rb * qb;
-    G[0] = mqa + mqb;
-    G[1] = fma(mqa, ua, mqb * ub) + (pa + pb) * ms0;
-    G[2] = fma(mqa, va, mqb * vb) + (pa + pb) * ms1;
-    G[3] = fma(mqa, wa, mqb * wb) + (pa + pb) * ms2;
-    G[4] = fma(ha, qa, hb * qb);
-  }
+// DVolSurf): PI or SD (split_pair_flux) in the PI/SD kernels, any SplitDG (split_pair_flux_gen) in the GEN ones.
+template <bool GEN>
+__device__ __forceinline__ void split_pair(int sd, bool pi, const Basis& B, double ra, double ua, double va, double wa, double pa, double ha,
+                                           double rb, double ub, double vb, double wb, double pb, double hb, double ms0, double ms1, double ms2,
+                                           double* G) {
+  if constexpr (GEN) split_pair_flux_gen(sd, B, ra, ua, va, wa, pa, ha, rb, ub, vb, wb, pb, hb, ms0, ms1, ms2, G);
+  else split_pair_flux(pi, ra, ua, va, wa, pa, ha, rb, ub, vb, wb, pb, hb, ms0, ms1, ms2, G);
 }
 
 // =====================================================================================================
@@ -985,7 +970,9 @@ __device__ __forceinline__ void split_pair_flux(bool pi, double ra, double ua, d
 // Shared memory: one region holds the split-flux inputs (rho, u, v, w, p-term, H-term and the metrics)
 // and afterwards the transformed viscous fluxes, so that two CTAs of 8^3 nodes fit on one SM.
 // =====================================================================================================
-template <int n>
+// GEN: any SplitDG (MO, DU, KG, CH, IR as well as SD, PI), with the kind chosen at run time; the PI/SD kernel
+// stays free of the other kinds' code.
+template <int n, bool GEN = false>
 __global__ void __launch_bounds__(Shape<n>::THREADS, (n == 8 ? 2 : 1)) k_vol_split(Dev d, Basis B, Stage st) {
   using S = Shape<n>;
   constexpr int n2 = S::n2, n3 = S::n3, EPB = S::EPB;
@@ -999,9 +986,11 @@ __global__ void __launch_bounds__(Shape<n>::THREADS, (n == 8 ? 2 : 1)) k_vol_spl
   load_basis_smem<n>(B, sD);
   SBasis<n> Bs{sD};
   const bool pi = B.splitDG == 4;
+  const int skind = B.splitDG;
   {
     // SplitVolumeFluxPI: 1/4 (density), 1/8 (others) of the contravariant sums below; SD: 1/2
-    const double f0 = pi ? 0.25 : 0.5, f1 = pi ? 0.125 : 0.5;
+    double f0 = pi ? 0.25 : 0.5, f1 = pi ? 0.125 : 0.5;
+    if constexpr (GEN) split_factors(skind, f0, f1);
     for (int t = threadIdx.x; t < n2; t += blockDim.x) { sC[t] = B.DVS[t] * f0; sC[n2 + t] = B.DVS[t] * f1; }
   }
   const int e0 = blockIdx.x * EPB;
@@ -1017,7 +1006,9 @@ __global__ void __launch_bounds__(Shape<n>::THREADS, (n == 8 ? 2 : 1)) k_vol_spl
     Q[n3 + x] = d.prim[((size_t)e * VP_NF + VP_U) * n3 + x];
     Q[2 * n3 + x] = d.prim[((size_t)e * VP_NF + VP_V) * n3 + x];
     Q[3 * n3 + x] = d.prim[((size_t)e * VP_NF + VP_W) * n3 + x];
-    if (pi) {
+    if constexpr (GEN) {
+      split_node_inputs(skind, u0, Q[n3 + x], Q[2 * n3 + x], Q[3 * n3 + x], p, u4, srho, Q[x], Q[4 * n3 + x], Q[5 * n3 + x]);
+    } else if (pi) {
       Q[4 * n3 + x] = 4.0 * p;
       Q[5 * n3 + x] = (u4 + p) * srho;
     } else {
@@ -1058,7 +1049,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS, (n == 8 ? 2 : 1)) k_vol_spl
         const double rb = Q[xb], ub = Q[n3 + xb], vb = Q[2 * n3 + xb], wb = Q[3 * n3 + xb], pb = Q[4 * n3 + xb], hb = Q[5 * n3 + xb];
         const double ms0 = ma0 + Mm[xb], ms1 = ma1 + Mm[n3 + xb], ms2 = ma2 + Mm[2 * n3 + xb];
         double G[5];
-        split_pair_flux(pi, ra, ua, va, wa, pa, ha, rb, ub, vb, wb, pb, hb, ms0, ms1, ms2, G);
+        split_pair<GEN>(skind, pi, B, ra, ua, va, wa, pa, ha, rb, ub, vb, wb, pb, hb, ms0, ms1, ms2, G);
         // contribution to node i from its partner l: DVolSurf(l, i)
         const double o0 = sC[bI * n + a], o1 = sC[n2 + bI * n + a];
         acc[0] = fma(o0, G[0], acc[0]);
@@ -1101,7 +1092,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS, (n == 8 ? 2 : 1)) k_vol_spl
         const double* Q = sR + es * 15 * n3;
         const double* Mm = Q + (6 + 3 * dir) * n3;
         double G[5];
-        split_pair_flux(pi, Q[xa], Q[n3 + xa], Q[2 * n3 + xa], Q[3 * n3 + xa], Q[4 * n3 + xa], Q[5 * n3 + xa], Q[xb], Q[n3 + xb],
+        split_pair<GEN>(skind, pi, B, Q[xa], Q[n3 + xa], Q[2 * n3 + xa], Q[3 * n3 + xa], Q[4 * n3 + xa], Q[5 * n3 + xa], Q[xb], Q[n3 + xb],
                         Q[2 * n3 + xb], Q[3 * n3 + xb], Q[4 * n3 + xb], Q[5 * n3 + xb], Mm[xa] + Mm[xb], Mm[n3 + xa] + Mm[n3 + xb],
                         Mm[2 * n3 + xa] + Mm[2 * n3 + xb], G);
         double* A = sA + es * 5 * n3;
@@ -1207,7 +1198,7 @@ template <int n> struct SplitShape {
   }
 };
 
-template <int n, bool GL>
+template <int n, bool GL, bool GEN = false>
 __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d, Basis B, Stage st) {
   using SS = SplitShape<n>;
   constexpr int n2 = SS::n2, n3 = SS::n3, EPB = SS::EPB, N = n - 1, SEG = SS::SEG, FNF = SS::FACE_NF;
@@ -1223,7 +1214,9 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
   load_basis_smem<n>(B, sD);
   SBasis<n> Bs{sD};
   const bool pi = B.splitDG == 4;
-  const double f0 = pi ? 0.25 : 0.5, f1 = pi ? 0.125 : 0.5;
+  const int skind = B.splitDG;
+  double f0 = pi ? 0.25 : 0.5, f1 = pi ? 0.125 : 0.5;
+  if constexpr (GEN) split_factors(skind, f0, f1);
   for (int t = threadIdx.x; t < n2; t += blockDim.x) { sC[t] = B.DVS[t] * f0; sC[n2 + t] = B.DVS[t] * f1; }
   const int e0 = blockIdx.x * EPB;
   load_face_fluxes<n>(d, sFl, e0);
@@ -1238,8 +1231,12 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
     Q[n3 + x] = d.prim[((size_t)e * VP_NF + VP_U) * n3 + x];
     Q[2 * n3 + x] = d.prim[((size_t)e * VP_NF + VP_V) * n3 + x];
     Q[3 * n3 + x] = d.prim[((size_t)e * VP_NF + VP_W) * n3 + x];
-    Q[4 * n3 + x] = pi ? 4.0 * p : p;
-    Q[5 * n3 + x] = pi ? (u4 + p) * srho : u4 + p;
+    if constexpr (GEN) {
+      split_node_inputs(skind, u0, Q[n3 + x], Q[2 * n3 + x], Q[3 * n3 + x], p, u4, srho, Q[x], Q[4 * n3 + x], Q[5 * n3 + x]);
+    } else {
+      Q[4 * n3 + x] = pi ? 4.0 * p : p;
+      Q[5 * n3 + x] = pi ? (u4 + p) * srho : u4 + p;
+    }
 #pragma unroll
     for (int c = 0; c < 9; ++c) Q[(6 + c) * n3 + x] = d.metr[((size_t)e * 9 + c) * n3 + x];
   }
@@ -1261,17 +1258,21 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
       dst[n2 + o] = src[FS_U * n2];
       dst[2 * n2 + o] = src[FS_V * n2];
       dst[3 * n2 + o] = src[FS_W * n2];
-      dst[4 * n2 + o] = pi ? 4.0 * pr : pr;
-      dst[5 * n2 + o] = pi ? (E + pr) * sr : E + pr;
+      if constexpr (GEN) {
+        split_node_inputs(skind, rho, dst[n2 + o], dst[2 * n2 + o], dst[3 * n2 + o], pr, E, sr, dst[o], dst[4 * n2 + o], dst[5 * n2 + o]);
+      } else {
+        dst[4 * n2 + o] = pi ? 4.0 * pr : pr;
+        dst[5 * n2 + o] = pi ? (E + pr) * sr : E + pr;
+      }
 #pragma unroll
       for (int c = 0; c < 3; ++c) dst[(6 + c) * n2 + o] = d.faceJa[(((size_t)e * 6 + lsi) * 3 + c) * n2 + o];
     }
   }
   __syncthreads();
   // two-point flux G (unscaled; density factor f0, others f1) between state a and state b with metric sum ms
-  auto two_point = [pi](double ra, double ua, double va, double wa, double pa, double ha, double rb, double ub, double vb, double wb,
-                        double pb, double hb, double ms0, double ms1, double ms2, double* G) {
-    split_pair_flux(pi, ra, ua, va, wa, pa, ha, rb, ub, vb, wb, pb, hb, ms0, ms1, ms2, G);
+  auto two_point = [pi, skind, &B](double ra, double ua, double va, double wa, double pa, double ha, double rb, double ub, double vb, double wb,
+                                double pb, double hb, double ms0, double ms1, double ms2, double* G) {
+    split_pair<GEN>(skind, pi, B, ra, ua, va, wa, pa, ha, rb, ub, vb, wb, pb, hb, ms0, ms1, ms2, G);
   };
   const int lane = threadIdx.x & 31;
   const int seg = lane / n, a = lane - seg * n, segBase = seg * n;
@@ -1380,7 +1381,7 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
         const double* Q = sR + es * 15 * n3;
         const double* Mm = Q + (6 + 3 * dir) * n3;
         double G[5];
-        split_pair_flux(pi, Q[xa], Q[n3 + xa], Q[2 * n3 + xa], Q[3 * n3 + xa], Q[4 * n3 + xa], Q[5 * n3 + xa], Q[xb], Q[n3 + xb],
+        split_pair<GEN>(skind, pi, B, Q[xa], Q[n3 + xa], Q[2 * n3 + xa], Q[3 * n3 + xa], Q[4 * n3 + xa], Q[5 * n3 + xa], Q[xb], Q[n3 + xb],
                         Q[2 * n3 + xb], Q[3 * n3 + xb], Q[4 * n3 + xb], Q[5 * n3 + xb], Mm[xa] + Mm[xb], Mm[n3 + xa] + Mm[n3 + xb],
                         Mm[2 * n3 + xa] + Mm[2 * n3 + xb], G);
         double* A = sA + es * 5 * n3;

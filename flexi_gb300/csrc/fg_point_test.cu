@@ -77,6 +77,30 @@ void fgpt_riemann_adj(int solver, int splitDG, double kappa, double R, const dou
   rs_out(lb, Lb); rs_out(rb, Rb);
 }
 
+// every Riemann solver with any SplitDG (-1: weak form): riemann_rotated_more
+void fgpt_riemann_more(int solver, int splitDG, double kappa, double R, double riemannPhi, const double* L, const double* Rr, double* F) {
+  Basis B = gas(kappa, R);
+  B.riemannPhi = riemannPhi;
+  riemann_rotated_more(solver, splitDG, B, rs(L), rs(Rr), F);
+}
+// two-point volume flux of the split form as the split kernels form it: per-node inputs, pair flux with the metric sum,
+// constant factors; uR/u conservative (5), pR/p primitive (rho, u, v, w, p, T), mR/m metric vectors (3)
+void fgpt_split_volume(int splitDG, double kappa, const double* uR, const double* pR, const double* u, const double* p, const double* mR,
+                       const double* m, double* F) {
+  Basis B = gas(kappa, 1.0);
+  double qa[6], qb[6];
+  qa[1] = pR[1]; qa[2] = pR[2]; qa[3] = pR[3];
+  qb[1] = p[1]; qb[2] = p[2]; qb[3] = p[3];
+  split_node_inputs(splitDG, uR[0], pR[1], pR[2], pR[3], pR[4], uR[4], 1.0 / uR[0], qa[0], qa[4], qa[5]);
+  split_node_inputs(splitDG, u[0], p[1], p[2], p[3], p[4], u[4], 1.0 / u[0], qb[0], qb[4], qb[5]);
+  double G[5], f0, f1;
+  split_pair_flux_gen(splitDG, B, qa[0], qa[1], qa[2], qa[3], qa[4], qa[5], qb[0], qb[1], qb[2], qb[3], qb[4], qb[5], mR[0] + m[0],
+                      mR[1] + m[1], mR[2] + m[2], G);
+  split_factors(splitDG, f0, f1);
+  F[0] = f0 * G[0];
+  for (int v = 1; v < 5; ++v) F[v] = f1 * G[v];
+}
+
 // x = (rho, vn, p) -> boundary pressure
 double fgpt_pressure_riemann(double kappa, double R, const double* x) {
   const Basis B = gas(kappa, R);

@@ -35,6 +35,7 @@ TYPE, BIND(C), PUBLIC :: fg_config
   REAL(C_DOUBLE)  :: AdvVel(3), IniFrequency, IniAmplitude
   REAL(C_DOUBLE)  :: TEnd, Analyze_dt, dtmin, dtkill
   INTEGER(C_INT)  :: nCalcTimeStepMax, maxIter
+  REAL(C_DOUBLE)  :: RiemannPhiFactor
 END TYPE fg_config
 
 TYPE, BIND(C), PUBLIC :: fg_timedisc_state

@@ -17,8 +17,9 @@ from . import _lib
 from .mesh import BoxMesh
 
 NODE_TYPES = {"gauss": 1, "gauss-lobatto": 2}
-RIEMANN = {"lf": 1, "hllc": 2, "roe": 3, "roeentropyfix": 33, "same": -1}
-SPLIT = {"none": -1, "weak": -1, "sd": 0, "pi": 4}
+RIEMANN = {"avg": 0, "lf": 1, "hllc": 2, "roe": 3, "hll": 4, "hlle": 5, "hllem": 6, "ch": 7, "ir": 8, "roel2": 32, "roeentropyfix": 33,
+           "roeentropygshockfix": 34, "same": -1}
+SPLIT = {"none": -1, "weak": -1, "sd": 0, "mo": 1, "du": 2, "kg": 3, "pi": 4, "ch": 5, "ir": 6}
 
 
 class FlexiError(RuntimeError):

@@ -28,16 +28,30 @@ extern "C" {
 #define FG_ERR_DT 6        /* non-finite time step (errType 2/3) */
 #define FG_ERR_DTKILL 7    /* time step below dtkill (timedisc_func.f90:EvalTimeStep, "Critical Kill timestep reached") */
 
-/* Riemann solver ids: the integer values of riemann.f90:44-58 */
+/* Riemann solver ids: the integer values of riemann.f90:44-58 (CH, IR and AVERAGE need the split form; the other
+ * solvers run with both forms, the HLL family with the split form as an extension of the reference) */
 #define FG_RIEMANN_SAME (-1)
+#define FG_RIEMANN_AVERAGE 0
 #define FG_RIEMANN_LF 1
 #define FG_RIEMANN_HLLC 2
 #define FG_RIEMANN_ROE 3
+#define FG_RIEMANN_HLL 4
+#define FG_RIEMANN_HLLE 5
+#define FG_RIEMANN_HLLEM 6
+#define FG_RIEMANN_CH 7
+#define FG_RIEMANN_IR 8
+#define FG_RIEMANN_ROEL2 32
 #define FG_RIEMANN_ROEENTROPYFIX 33
+#define FG_RIEMANN_ROEENTROPYGSHOCKFIX 34
 /* SplitDG ids: splitflux.f90:63-69; -1 selects the weak (non-split) form */
 #define FG_SPLIT_NONE (-1)
 #define FG_SPLIT_SD 0
+#define FG_SPLIT_MO 1
+#define FG_SPLIT_DU 2
+#define FG_SPLIT_KG 3
 #define FG_SPLIT_PI 4
+#define FG_SPLIT_CH 5
+#define FG_SPLIT_IR 6
 #define FG_NODE_GAUSS 1
 #define FG_NODE_GAUSS_LOBATTO 2
 
@@ -82,6 +96,7 @@ typedef struct fg_config {
   double dtkill;            /* a time step below dtkill stops the run with FG_ERR_DTKILL (default -1: off) */
   int nCalcTimeStepMax;     /* NCalcTimeStepMax: CALCTIMESTEP at least every nCalcTimeStepMax steps, fewer when dt varies (default 1) */
   int maxIter;              /* maxIter: an instance stops after this many steps (default -1: no limit) */
+  double RiemannPhiFactor;  /* RiemannPhiFactor of RoeEntropyGShockFix (riemann.f90:131, default 5) */
 } fg_config;
 
 typedef struct fg_handle fg_handle;

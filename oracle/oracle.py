@@ -50,6 +50,8 @@ def lib():
         _lib.orc_timestep.argtypes = [P, P, ctypes.c_double]
         _lib.orc_calc_timestep.argtypes = [P, P]
         _lib.orc_calc_timestep.restype = ctypes.c_double
+        _lib.orc_point_riemann.argtypes = [P, ctypes.c_int, P, P, P]
+        _lib.orc_point_split_volume.argtypes = [P, P, P, P, P, P, P, P]
         _lib.orc_bulk_velocity.argtypes = [P]
         _lib.orc_bulk_velocity.restype = ctypes.c_double
         _lib.orc_set_bulk_velocity.argtypes = [P, ctypes.c_double]
@@ -201,6 +203,21 @@ class Oracle:
         err = ctypes.c_int(0)
         dt = lib().orc_calc_timestep(self.h, ctypes.byref(err))
         return dt, err.value
+
+    def point_riemann(self, solver, L, R):
+        """riemann.f90 solver `solver` on extended rotated states (11 values each) with this oracle's configuration."""
+        L = np.ascontiguousarray(L, np.float64)
+        R = np.ascontiguousarray(R, np.float64)
+        F = np.empty(5)
+        lib().orc_point_riemann(self.h, int(solver), _p(L), _p(R), _p(F))
+        return F
+
+    def point_split_volume(self, uR, pR, u, p, mR, m):
+        """splitflux.f90 two-point volume flux of this oracle's SplitDG (node states U(5), UPrim(6), metric vectors(3))."""
+        a = [np.ascontiguousarray(x, np.float64) for x in (uR, pR, u, p, mR, m)]
+        F = np.empty(5)
+        lib().orc_point_split_volume(self.h, *[_p(x) for x in a], _p(F))
+        return F
 
     def bulk_velocity(self):
         return lib().orc_bulk_velocity(self.h)

@@ -37,6 +37,7 @@ static Config to_cfg(const orc_config* c) {
   return C;
 }
 
+
 struct OrcHandle {
   DG<double> dg;
   MeshInput mi;
@@ -196,6 +197,16 @@ int orc_fd_jvp(void* hp, const double* V, int fdOrder, int epsMethod, double sca
     d.U = Xk;
     return 0;
   } catch (std::exception& e) { g_err = e.what(); return 1; }
+}
+// point-wise fluxes of the restated reference with the handle's configuration, for the CPU tests of the GPU's point
+// functions: riemann.f90:Riemann_Point's solver call on extended rotated states UE(11) (0..4 cons, 5 srho, 6..8 vel,
+// 9 p, 10 T), and splitflux.f90's two-point volume flux (U(5), UPrim(6), metric vectors(3) of both nodes)
+void orc_point_riemann(void* hp, int solver, const double* L, const double* R, double* F) {
+  ((OrcHandle*)hp)->dg.riemann_point(solver, L, R, F);
+}
+void orc_point_split_volume(void* hp, const double* uR, const double* pR, const double* u, const double* p, const double* mR, const double* m,
+                            double* F) {
+  ((OrcHandle*)hp)->dg.split_volume_flux(uR, pR, u, p, mR, m, F);
 }
 double orc_bulk_velocity(void* hp) { auto& d = ((OrcHandle*)hp)->dg; d.calc_forcing(); return val(d.BulkVel); }
 void orc_set_bulk_velocity(void* hp, double bv) { ((OrcHandle*)hp)->dg.BulkVel = bv; }

@@ -20,7 +20,7 @@ def oracle_cfg(c):
                 etaBR2_wall=d["etaBR2_wall"], kappa=d["kappa"], R=d["R"], Pr=d["Pr"], mu0=d["mu0"], CFLScale=d["CFLScale"],
                 DFLScale=d["DFLScale"], doTCSource=d["doTCSource"], dpdx=d["dpdx"], overintType=d["OverintegrationType"],
                 NUnder=d["NUnder"], iniExactFunc=d["IniExactFunc"], advVel=d["AdvVel"], iniFrequency=d["IniFrequency"],
-                iniAmplitude=d["IniAmplitude"], timeDisc=d["TimeDiscMethod"])
+                iniAmplitude=d["IniAmplitude"], timeDisc=d["TimeDiscMethod"], riemannPhi=d["RiemannPhiFactor"])
 
 
 def perturb_state(U, seed=0, amp=0.05):

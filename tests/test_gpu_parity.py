@@ -61,8 +61,31 @@ RHS_CASES = {
     "gl11_split_pi_roeef_br2": dict(N=11, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roeentropyfix", Lifting="br2"),
     "gauss8_split_pi_hllc": dict(N=8, NodeType="gauss", SplitDG="pi", Riemann="hllc"),
     "gauss10_split_sd_roe_br2": dict(N=10, NodeType="gauss", SplitDG="sd", Riemann="roe", Lifting="br2"),
+    # the other SplitDG fluxes (MO, DU, KG, CH, IR) and Riemann solvers (RoeL2, RoeEntropyGShockFix, HLL, HLLE, HLLEM, and the
+    # split-only CH, IR, avg) of splitflux.f90 / riemann.f90
+    "gl7_split_mo_roe": dict(N=7, NodeType="gauss-lobatto", SplitDG="mo", Riemann="roe"),
+    "gl7_split_du_roel2_br2": dict(N=7, NodeType="gauss-lobatto", SplitDG="du", Riemann="roel2", Lifting="br2"),
+    "gl7_split_kg_gshock": dict(N=7, NodeType="gauss-lobatto", SplitDG="kg", Riemann="roeentropygshockfix", RiemannPhiFactor=3.0),
+    "gl7_split_ch_ch_br2": dict(N=7, NodeType="gauss-lobatto", SplitDG="ch", Riemann="ch", Lifting="br2"),
+    "gl7_split_ir_ir": dict(N=7, NodeType="gauss-lobatto", SplitDG="ir", Riemann="ir"),
+    "gl7_split_pi_avg": dict(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="avg"),
+    "gl7_split_pi_hllem": dict(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="hllem"),
+    "gl5_split_kg_avg": dict(N=5, NodeType="gauss-lobatto", SplitDG="kg", Riemann="avg"),
+    "gl4_split_ch_roeef": dict(N=4, NodeType="gauss-lobatto", SplitDG="ch", Riemann="roeentropyfix"),
+    "gl3_split_mo_ir": dict(N=3, NodeType="gauss-lobatto", SplitDG="mo", Riemann="ir"),
+    "gauss5_split_ch_ch": dict(N=5, NodeType="gauss", SplitDG="ch", Riemann="ch"),
+    "gauss3_split_ir_lf_br2": dict(N=3, NodeType="gauss", SplitDG="ir", Riemann="lf", Lifting="br2"),
+    "gauss4_split_du_roel2": dict(N=4, NodeType="gauss", SplitDG="du", Riemann="roel2"),
+    "gauss6_split_mo_gshock": dict(N=6, NodeType="gauss", SplitDG="mo", Riemann="roeentropygshockfix"),
+    "gauss3_weak_roel2": dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="roel2"),
+    "gauss3_weak_hll": dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="hll"),
+    "gauss5_weak_hlle_br2": dict(N=5, NodeType="gauss", SplitDG="weak", Riemann="hlle", Lifting="br2"),
+    "gauss3_weak_hllem": dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="hllem"),
+    "gl3_weak_gshock": dict(N=3, NodeType="gauss-lobatto", SplitDG="weak", Riemann="roeentropygshockfix"),
+    "gauss9_weak_hllem": dict(N=9, NodeType="gauss", SplitDG="weak", Riemann="hllem"),
 }
 COMMON = dict(kappa=1.4, R=71.42857, Pr=0.72, mu0=6.25e-4, CFLScale=0.9, DFLScale=0.9)
+HALF_DT = {"gl7_split_ch_ch_br2": 0.5, "gl7_split_ir_ir": 0.5}
 
 
 @pytest.mark.parametrize("name", list(RHS_CASES))
@@ -75,7 +98,8 @@ def test_rhs_parity_tgv(name):
 
 
 @pytest.mark.parametrize("name", ["c1_gauss3_weak_roe_br1", "gl7_split_pi_roeef_br2", "gauss5_weak_roeef", "gauss5_split_pi_roeef_br1",
-                                  "gauss3_split_sd_lf", "gl5_split_pi_roeef_br2", "gauss11_weak_roeef_br1", "gl11_split_pi_roeef_br2"])
+                                  "gauss3_split_sd_lf", "gl5_split_pi_roeef_br2", "gauss11_weak_roeef_br1", "gl11_split_pi_roeef_br2",
+                                  "gl7_split_ch_ch_br2", "gauss5_split_ch_ch", "gl7_split_mo_roe", "gauss3_weak_hllem"])
 def test_rhs_parity_curved(name):
     c = product_cfg(**RHS_CASES[name], **COMMON)
     f, o, _ = tgv_pair(c, n_elem=3, ngeo=3, perturb=0.2, seed=3)
@@ -100,12 +124,16 @@ def test_rhs_parity_channel_walls(variant):
 
 
 @pytest.mark.parametrize("name", ["c1_gauss3_weak_roe_br1", "gl7_split_pi_roeef_br1", "gauss3_weak_br2", "gauss5_split_pi_roeef_br1",
-                                  "gauss11_weak_roeef_br1"])
+                                  "gauss11_weak_roeef_br1", "gl7_split_ch_ch_br2", "gl7_split_ir_ir", "gauss5_split_ch_ch", "gauss3_weak_hllem",
+                                  "gl5_split_kg_avg"])
 def test_lserk_steps_fixed_dt(name):
     c = product_cfg(**RHS_CASES[name], **COMMON)
     f, o, _ = tgv_pair(c, n_elem=3)
     dt, err = o.calc_timestep()
     assert err == 0
+    # the CH dissipation (like LF's) and the IR volume flux leave the N=7 split operator unstable at CFLScale 0.9 on this
+    # noisy state within two steps, on the oracle as on the GPU; half the time step keeps ten steps finite
+    dt *= HALF_DT.get(name, 1.0)
     tf = to = 0.0
     for _ in range(10):
         tf = f.TimeStepByLSERKW2(tf, dt)

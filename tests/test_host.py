@@ -40,7 +40,11 @@ def test_config_defaults_and_validation(lib):
     with pytest.raises(FlexiError):
         Flexi(make_config(N=12))
     with pytest.raises(FlexiError):
-        Flexi(make_config(N=5, SplitDG=2))  # split fluxes other than SD (0) and PI (4)
+        Flexi(make_config(N=5, SplitDG=7))  # splitflux.f90:63-69 defines SplitDG 0..6
+    with pytest.raises(FlexiError):
+        Flexi(make_config(N=5, SplitDG="weak", Riemann="ch"))  # CH, IR and avg need the split form
+    with pytest.raises(FlexiError):
+        Flexi(make_config(N=5, Riemann=9))  # no solver 9 in riemann.f90:44-58
     with pytest.raises(FlexiError):
         Flexi(make_config(N=5, OverintegrationType=3))
     # lifting.f90:137-139: BR2 lifts in strong form, doWeakLifting is dropped; doConservativeLifting stays
