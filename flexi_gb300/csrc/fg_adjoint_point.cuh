@@ -504,4 +504,113 @@ FG_HD void pressure_riemann_adj(const Basis& B, double rho, double vn, double p,
   rhob -= arb * 2.0 * B.sKappaP1 / (rho * rho);
 }
 
+// Two-point volume flux of the split form (split_pair_flux, PI or SD) between the per-node inputs qa, qb
+// (q0, u, v, w, q4, q5) with metric sum ms: given Gb[5], adds the bars of both nodes' inputs. PI depends on
+// the sums of the inputs only, so both nodes get the same bars.
+FG_HD void split_pair_flux_adj(bool pi, const double* qa, const double* qb, const double* ms, const double* Gb, double* qab, double* qbb) {
+  if (pi) {
+    const double rs = qa[0] + qb[0], us = qa[1] + qb[1], vs = qa[2] + qb[2], ws = qa[3] + qb[3], hs = qa[5] + qb[5];
+    const double qs = us * ms[0] + vs * ms[1] + ws * ms[2];
+    const double A = rs * qs;
+    const double Ab = Gb[0] + Gb[1] * us + Gb[2] * vs + Gb[3] * ws + Gb[4] * hs;
+    const double qsb = Ab * rs;
+    const double bar[6] = {Ab * qs, Gb[1] * A + qsb * ms[0], Gb[2] * A + qsb * ms[1], Gb[3] * A + qsb * ms[2],
+                           Gb[1] * ms[0] + Gb[2] * ms[1] + Gb[3] * ms[2], Gb[4] * A};
+#pragma unroll
+    for (int c = 0; c < 6; ++c) { qab[c] += bar[c]; qbb[c] += bar[c]; }
+    return;
+  }
+  const double pb = Gb[1] * ms[0] + Gb[2] * ms[1] + Gb[3] * ms[2];
+  const double* q[2] = {qa, qb};
+  double* o[2] = {qab, qbb};
+#pragma unroll
+  for (int side = 0; side < 2; ++side) {
+    const double* s = q[side];
+    // G0 = sum m q, G1..3 = sum m q u_c + p_s ms_c, G4 = sum h q (q = u . ms, m = rho)
+    const double qn = s[1] * ms[0] + s[2] * ms[1] + s[3] * ms[2];
+    const double mq = s[0] * qn;
+    const double mqb = Gb[0] + Gb[1] * s[1] + Gb[2] * s[2] + Gb[3] * s[3];
+    const double qnb = mqb * s[0] + Gb[4] * s[5];
+    o[side][0] += mqb * qn;
+    o[side][1] += qnb * ms[0] + Gb[1] * mq;
+    o[side][2] += qnb * ms[1] + Gb[2] * mq;
+    o[side][3] += qnb * ms[2] + Gb[3] * mq;
+    o[side][4] += pb;
+    o[side][5] += Gb[4] * qn;
+  }
+}
+
+// split_node_inputs (PI or SD) transposed to the bars of the face-state fields rho, u, v, w, p, E, 1/rho
+// (PI: q4 = 4p, q5 = (E+p)/rho; SD: q4 = p, q5 = E+p); adds into fb[FS_NF]
+FG_HD void split_inputs_to_face_adj(bool pi, double E, double p, double srho, const double* qb, double* fb) {
+  fb[FS_RHO] += qb[0];
+  fb[FS_U] += qb[1]; fb[FS_V] += qb[2]; fb[FS_W] += qb[3];
+  if (pi) {
+    fb[FS_P] += 4.0 * qb[4] + qb[5] * srho;
+    fb[FS_E] += qb[5] * srho;
+    fb[FS_SRHO] += qb[5] * (E + p);
+  } else {
+    fb[FS_P] += qb[4] + qb[5];
+    fb[FS_E] += qb[5];
+  }
+}
+
+// the entropy-variable transforms of k_prep, in place on one point (the adjoint's linearisation point)
+FG_HD void cons_to_entropy(const Basis& B, double* u) {
+  const double srho = 1.0 / u[0];
+  const double vx = u[1] * srho, vy = u[2] * srho, vz = u[3] * srho;
+  const double p = B.kappaM1 * (u[4] - 0.5 * (u[1] * vx + u[2] * vy + u[3] * vz));
+  const double sEnt = log(p) - B.kappa * log(u[0]);
+  const double rho_p = u[0] / p;
+  u[0] = (B.kappa - sEnt) * B.sKappaM1 - rho_p * 0.5 * (vx * vx + vy * vy + vz * vz);
+  u[1] = rho_p * vx; u[2] = rho_p * vy; u[3] = rho_p * vz;
+  u[4] = -rho_p;
+}
+FG_HD void entropy_to_cons(const Basis& B, double* c) {
+  const double w0 = c[0] * B.kappaM1, w1 = c[1] * B.kappaM1, w2 = c[2] * B.kappaM1, w3 = c[3] * B.kappaM1, w4 = c[4] * B.kappaM1;
+  const double ekin = 0.5 * (w1 * w1 + w2 * w2 + w3 * w3) / w4;
+  const double sEnt = B.kappa - w0 + ekin;
+  const double rhoe = exp(B.logEntC - B.kappa_kappaM1 * log(-w4) - sEnt * B.sKappaM1);
+  c[0] = -rhoe * w4;
+  c[1] = rhoe * w1; c[2] = rhoe * w2; c[3] = rhoe * w3;
+  c[4] = rhoe * (1.0 - ekin);
+}
+
+// eos.f90:ConsToEntropy (the form of k_prep): W =((kappa - s)/(kappa-1) - rho/p |v|^2/2, rho/p v, -rho/p) with
+// s = ln p - kappa ln rho. Given Wb[5], adds the conservative bars into Ub[5].
+FG_HD void cons_to_entropy_adj(const Basis& B, const double* U, const double* Wb, double* Ub) {
+  const double srho = 1.0 / U[0];
+  const double vx = U[1] * srho, vy = U[2] * srho, vz = U[3] * srho;
+  const double p = B.kappaM1 * (U[4] - 0.5 * (U[1] * vx + U[2] * vy + U[3] * vz));
+  const double rho_p = U[0] / p;
+  const double v2 = vx * vx + vy * vy + vz * vz;
+  const double rpb = -Wb[0] * 0.5 * v2 + Wb[1] * vx + Wb[2] * vy + Wb[3] * vz - Wb[4];
+  const double sb = -Wb[0] * B.sKappaM1;
+  const double vxb = (Wb[1] - Wb[0] * vx) * rho_p, vyb = (Wb[2] - Wb[0] * vy) * rho_p, vzb = (Wb[3] - Wb[0] * vz) * rho_p;
+  // s = ln p - kappa ln rho, rho_p = rho / p
+  const double pb = sb / p - rpb * rho_p / p;
+  const double rhob = -B.kappa * sb * srho + rpb / p;
+  cons_to_prim_adj(B, U, 0.0, vxb, vyb, vzb, pb, 0.0, rhob, 0.0, Ub);
+}
+
+// eos.f90:EntropyToCons (the form of k_prep, one exponential): given the entropy variables W[5] of a face point
+// and the bars cb[5] of the conservative result, adds the bars of W into Wb[5]
+FG_HD void entropy_to_cons_adj(const Basis& B, const double* W, const double* cb, double* Wb) {
+  const double w0 = W[0] * B.kappaM1, w1 = W[1] * B.kappaM1, w2 = W[2] * B.kappaM1, w3 = W[3] * B.kappaM1, w4 = W[4] * B.kappaM1;
+  const double ekin = 0.5 * (w1 * w1 + w2 * w2 + w3 * w3) / w4;
+  const double sEnt = B.kappa - w0 + ekin;
+  const double rhoe = exp(B.logEntC - B.kappa_kappaM1 * log(-w4) - sEnt * B.sKappaM1);
+  // c = rhoe (-w4, w1, w2, w3, 1 - ekin)
+  const double rhoeb = -cb[0] * w4 + cb[1] * w1 + cb[2] * w2 + cb[3] * w3 + cb[4] * (1.0 - ekin);
+  const double Xb = rhoeb * rhoe;  // rhoe = exp(X)
+  const double sEntb = -Xb * B.sKappaM1;
+  const double ekinb = -cb[4] * rhoe + sEntb;
+  double w1b = cb[1] * rhoe + ekinb * w1 / w4;
+  double w2b = cb[2] * rhoe + ekinb * w2 / w4;
+  double w3b = cb[3] * rhoe + ekinb * w3 / w4;
+  double w4b = -cb[0] * rhoe - Xb * B.kappa_kappaM1 / w4 - ekinb * ekin / w4;
+  const double w0b = -sEntb;
+  Wb[0] += w0b * B.kappaM1; Wb[1] += w1b * B.kappaM1; Wb[2] += w2b * B.kappaM1; Wb[3] += w3b * B.kappaM1; Wb[4] += w4b * B.kappaM1;
+}
+
 }  // namespace fg

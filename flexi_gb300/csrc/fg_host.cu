@@ -913,21 +913,19 @@ void set_error_without_handle(const char* msg) { g_err = msg; }
 
 namespace {
 
-// the adjoint kernels cover: weak form and split form PI, LF/HLLC/Roe/RoeEntropyFix, BR1/BR2
+// the adjoint kernels cover: weak form and split forms PI and SD (Gauss, Gauss-Lobatto), LF/HLLC/Roe/RoeEntropyFix, BR1/BR2
 const char* adjoint_unsupported(const fg_config& c) {
   if (c.N > 7) return "the adjoint supports N = 1..7";
   if (c.Riemann != FG_RIEMANN_LF && c.Riemann != FG_RIEMANN_HLLC && c.Riemann != FG_RIEMANN_ROE && c.Riemann != FG_RIEMANN_ROEENTROPYFIX)
     return "the adjoint supports the Riemann solvers LF, HLLC, Roe and RoeEntropyFix";
   if (c.doWeakLifting || c.doConservativeLifting) return "the adjoint supports the strong, non-conservative lifting";
-  if (c.SplitDG != FG_SPLIT_NONE && c.SplitDG != FG_SPLIT_PI) return "the adjoint supports the weak form and the split form PI";
-  if (c.SplitDG != FG_SPLIT_NONE && (c.NodeType != FG_NODE_GAUSS_LOBATTO || (c.N != 1 && c.N != 3 && c.N != 7)))
-    return "the adjoint of the split form supports Gauss-Lobatto nodes with N = 1, 3, 7";
+  if (c.SplitDG != FG_SPLIT_NONE && c.SplitDG != FG_SPLIT_PI && c.SplitDG != FG_SPLIT_SD)
+    return "the adjoint supports the weak form and the split forms PI and SD";
   return nullptr;
 }
 
 int ensure_adjoint(fg_handle* h) {
   if (h->haveAdj) return 0;
-  if (h->d.nMortars > 0) return fail(h, FG_ERR_CONFIG, "the adjoint does not support mortar interfaces");
   const int n = h->M.n, n2 = n * n, n3 = n2 * n, nE = h->M.nElems, nS = h->M.nSides;
   AdjDev& a = h->a;
   double* W = nullptr;
@@ -945,6 +943,16 @@ int ensure_adjoint(fg_handle* h) {
   if ((r = dalloc(h, a.liftb, (size_t)nS * 2 * 4 * n2))) return r;
   if ((r = dalloc(h, a.muSideb, (size_t)nS * 2 * n2))) return r;
   if ((r = dalloc(h, a.muElemb, (size_t)nE))) return r;
+  a.liftMortarb = nullptr;
+  if (h->d.nMortars > 0) {
+    if ((r = dalloc(h, a.liftMortarb, (size_t)h->d.nMortars * 12 * n2))) return r;
+    CUDA_TRY(cudaMemset(a.liftMortarb, 0, sizeof(double) * h->d.nMortars * 12 * n2));
+  }
+  a.faceVolb = nullptr;
+  if (h->cfg.SplitDG != FG_SPLIT_NONE && h->cfg.NodeType == FG_NODE_GAUSS) {
+    if ((r = dalloc(h, a.faceVolb, (size_t)nS * 2 * FS_NF * n2))) return r;
+    CUDA_TRY(cudaMemset(a.faceVolb, 0, sizeof(double) * nS * 2 * FS_NF * n2));
+  }
   // entries no kernel writes (slave slots of boundary sides) stay zero
   CUDA_TRY(cudaMemset(a.faceSb, 0, sizeof(double) * nS * FS_NF * n2));
   CUDA_TRY(cudaMemset(a.gradSb, 0, sizeof(double) * nS * 12 * n2));
@@ -976,25 +984,35 @@ AdjDev overint_adj_cotangent(fg_handle* h, const Dev& d, const AdjDev& a) {
   return b;
 }
 
+// the transposed kernels in reverse order of the forward's (prep, mortar_pre, lift, flux, mortar_face, volume)
+static void launch_vjp_sweep(fg_handle* h, const Dev& d, const AdjDev& a) {
+  const bool mortars = d.nMortars > 0;
+  h->K.vol_adj(d, a, h->B, h->st);
+  h->K.flux_adj(d, a, h->B, h->st);
+  if (mortars) h->K.mortar_face_adj(d, a, h->B, h->mort, h->st);
+  (mortars ? h->K.lift_mortar_adj : h->K.lift_adj)(d, a, h->B, h->st);
+  if (mortars) h->K.mortar_pre_adj(d, a, h->B, h->mort, h->st);
+  h->K.prep_adj(d, a, h->B, h->st);
+  h->launches += mortars ? 6 : 4;
+}
+
 void launch_vjp(fg_handle* h, const Dev& d, const AdjDev& a0) {
   const AdjDev a = overint_adj_cotangent(h, d, a0);
   h->K.prep(d, h->B, h->st);
-  h->K.lift(d, h->B, h->st);
-  h->K.vol_adj(d, a, h->B, h->st);
-  h->K.flux_adj(d, a, h->B, h->st);
-  h->K.lift_adj(d, a, h->B, h->st);
-  h->K.prep_adj(d, a, h->B, h->st);
-  h->launches += 6;
+  if (d.nMortars > 0) {
+    h->K.mortar_pre(d, h->B, h->mort, h->st);
+    h->K.lift_mortar(d, h->B, h->st);
+    h->launches += 1;
+  } else {
+    h->K.lift(d, h->B, h->st);
+  }
+  h->launches += 2;
+  launch_vjp_sweep(h, d, a);
 }
 
 // adjoint right-hand side on forward intermediates the caller kept (no prep/lift recomputation)
 void launch_vjp_kept(fg_handle* h, const Dev& d, const AdjDev& a0) {
-  const AdjDev a = overint_adj_cotangent(h, d, a0);
-  h->K.vol_adj(d, a, h->B, h->st);
-  h->K.flux_adj(d, a, h->B, h->st);
-  h->K.lift_adj(d, a, h->B, h->st);
-  h->K.prep_adj(d, a, h->B, h->st);
-  h->launches += 4;
+  launch_vjp_sweep(h, d, overint_adj_cotangent(h, d, a0));
 }
 
 int adj_alloc(fg_handle* h, double*& p, size_t count) {

@@ -29,8 +29,14 @@ struct Inst {
       mx(mx(mx(gs(Big<n>::prep), gs(Big<n>::lift)), mx(gs(Big<n>::weak), gs(SplitShape<n>::template big<GL>()))), gs(Big<n>::liftVariant(true, true)));
   static size_t smem_weak_adj() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * 5 * S::n3 + S::THREADS); }
   static size_t smem_split_adj() { return sizeof(double) * (SBasis<n>::SIZE + 2 * S::n2 + S::EPB * 26 * S::n3 + S::THREADS); }
+  static size_t smem_split_gen_adj() {
+    return sizeof(double) * (SBasis<n>::SIZE + 2 * S::n2 + S::EPB * 20 * S::n3 + S::THREADS + (GL ? 0 : S::EPB * 6 * S::n2 * 14));
+  }
   static size_t smem_lift_adj() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * (13 * S::n3 + 6 * S::n2 * 19)); }
   static size_t smem_prep_adj() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * (5 * S::n3 + 6 * S::n2 * 6)); }
+  static size_t smem_lift_mortar_adj() { return sizeof(double) * (SBasis<n>::SIZE + S::EPB * (13 * S::n3 + 6 * S::n2 * 27)); }
+  static size_t smem_mortar_face_adj() { return sizeof(double) * 113 * S::n2; }
+  static size_t smem_mortar_pre_adj() { return sizeof(double) * 109 * S::n2; }
   // elements per CTA of the autotuner's alternative element kernels (N=5: 2, N=3: 4; 0: none)
   static constexpr int ALT_E = (n == 6) ? 2 : ((n == 4) ? 4 : 0);
   template <int E>
@@ -90,6 +96,10 @@ struct Inst {
       set_smem(k_vol_weak_adj<n, GL>, smem_weak_adj());
       set_smem(k_lift_adj<n, GL>, smem_lift_adj());
       set_smem(k_prep_adj<n, GL>, smem_prep_adj());
+      set_smem(k_vol_split_gen_adj<n, GL>, smem_split_gen_adj());
+      set_smem(k_lift_adj<n, GL, true>, smem_lift_mortar_adj());
+      set_smem(k_mortar_face_adj<n>, smem_mortar_face_adj());
+      set_smem(k_mortar_pre_adj<n>, smem_mortar_pre_adj());
     }
     if constexpr (GL && (n == 2 || n == 4 || n == 8)) set_smem(k_vol_split_adj<n>, smem_split_adj());
     if constexpr (ALT_E > 0) {
@@ -100,24 +110,40 @@ struct Inst {
   }
   // adjoint kernels: lines of up to 8 nodes (one thread per node, shared-memory staging)
   static constexpr bool ADJ = n <= 8;
+  // split form: the shuffle-pair kernel for PI on Gauss-Lobatto lines of 2, 4 or 8 nodes, the per-node kernel
+  // otherwise (SD, other line lengths, Gauss nodes)
   static void vol_adj(const Dev& d, const AdjDev& a, const Basis& B, cudaStream_t st) {
     if constexpr (GL && (n == 2 || n == 4 || n == 8)) {
-      if (B.splitDG >= 0) {
+      if (B.splitDG == SPLIT_PI) {
         k_vol_split_adj<n><<<blocks(d), S::THREADS, smem_split_adj(), st>>>(d, a, B);
         return;
       }
     }
-    if constexpr (ADJ) k_vol_weak_adj<n, GL><<<blocks(d), S::THREADS, smem_weak_adj(), st>>>(d, a, B);
+    if constexpr (ADJ) {
+      if (B.splitDG >= 0) k_vol_split_gen_adj<n, GL><<<blocks(d), S::THREADS, smem_split_gen_adj(), st>>>(d, a, B);
+      else k_vol_weak_adj<n, GL><<<blocks(d), S::THREADS, smem_weak_adj(), st>>>(d, a, B);
+    }
   }
   static void flux_adj(const Dev& d, const AdjDev& a, const Basis& B, cudaStream_t st) {
-    const long long pts = (long long)d.nSides * S::n2;
-    if constexpr (ADJ) k_flux_adj<n><<<(unsigned)((pts + 127) / 128), 128, 0, st>>>(d, a, B);
+    const long long pts = (long long)d.nFluxSides * S::n2;
+    if constexpr (ADJ) {
+      if (pts > 0) k_flux_adj<n><<<(unsigned)((pts + 127) / 128), 128, 0, st>>>(d, a, B);
+    }
   }
   static void lift_adj(const Dev& d, const AdjDev& a, const Basis& B, cudaStream_t st) {
     if constexpr (ADJ) k_lift_adj<n, GL><<<blocks(d), S::THREADS, smem_lift_adj(), st>>>(d, a, B);
   }
   static void prep_adj(const Dev& d, const AdjDev& a, const Basis& B, cudaStream_t st) {
     if constexpr (ADJ) k_prep_adj<n, GL><<<blocks(d), S::THREADS, smem_prep_adj(), st>>>(d, a, B);
+  }
+  static void mortar_face_adj(const Dev& d, const AdjDev& a, const Basis& B, const MortarDev& M, cudaStream_t st) {
+    if constexpr (ADJ) k_mortar_face_adj<n><<<d.nMortars, 256, smem_mortar_face_adj(), st>>>(d, a, B, M);
+  }
+  static void lift_mortar_adj(const Dev& d, const AdjDev& a, const Basis& B, cudaStream_t st) {
+    if constexpr (ADJ) k_lift_adj<n, GL, true><<<blocks(d), S::THREADS, smem_lift_mortar_adj(), st>>>(d, a, B);
+  }
+  static void mortar_pre_adj(const Dev& d, const AdjDev& a, const Basis& B, const MortarDev& M, cudaStream_t st) {
+    if constexpr (ADJ) k_mortar_pre_adj<n><<<d.nMortars, 256, smem_mortar_pre_adj(), st>>>(d, a, B, M);
   }
   static void prep(const Dev& d, const Basis& B, cudaStream_t st) {
     k_prep<n, GL><<<blocks(d), S::THREADS, smem_prep(), st>>>(d, B);
@@ -181,7 +207,10 @@ struct Inst {
     k.overint = &overint;
     k.mortar_pre = &mortar_pre; k.lift_mortar = &lift_mortar; k.mortar_face = &mortar_face;
     k.lift_cons = &lift_cons; k.lift_mortar_cons = &lift_mortar_cons;
-    if constexpr (ADJ) { k.vol_adj = &vol_adj; k.flux_adj = &flux_adj; k.lift_adj = &lift_adj; k.prep_adj = &prep_adj; }
+    if constexpr (ADJ) {
+      k.vol_adj = &vol_adj; k.flux_adj = &flux_adj; k.lift_adj = &lift_adj; k.prep_adj = &prep_adj;
+      k.mortar_face_adj = &mortar_face_adj; k.lift_mortar_adj = &lift_mortar_adj; k.mortar_pre_adj = &mortar_pre_adj;
+    }
     k.defEPB = S::EPB;
     k.scratchPerBlock = SCRATCH_PER_BLOCK;
     k.flux_block = &flux_block;

@@ -29,6 +29,10 @@ struct KernelSet {
   void (*flux_adj)(const Dev&, const AdjDev&, const Basis&, cudaStream_t) = nullptr;
   void (*lift_adj)(const Dev&, const AdjDev&, const Basis&, cudaStream_t) = nullptr;
   void (*prep_adj)(const Dev&, const AdjDev&, const Basis&, cudaStream_t) = nullptr;
+  // adjoint on mortar meshes: k_mortar_face_adj (after flux_adj), k_lift_adj<MORTAR>, k_mortar_pre_adj (before prep_adj)
+  void (*mortar_face_adj)(const Dev&, const AdjDev&, const Basis&, const MortarDev&, cudaStream_t) = nullptr;
+  void (*lift_mortar_adj)(const Dev&, const AdjDev&, const Basis&, cudaStream_t) = nullptr;
+  void (*mortar_pre_adj)(const Dev&, const AdjDev&, const Basis&, const MortarDev&, cudaStream_t) = nullptr;
   // autotuner candidates: element kernels with another number of elements per CTA (altEPB = 0: none) and
   // the side kernel with a given block size (64, 128 or 256 threads); fluxBlock is the block size in use
   int defEPB = 0, altEPB = 0;

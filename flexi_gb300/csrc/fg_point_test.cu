@@ -3,6 +3,8 @@
 // Exposes the __host__ __device__ functions of fg_common.cuh and fg_adjoint_point.cuh through plain C
 // entry points so that the CPU test suite can check every transposed Jacobian against central finite
 // differences of the very same forward code. Not part of the solver library.
+#include <cmath>
+
 #include "fg_adjoint_point.cuh"
 
 using namespace fg;
@@ -14,6 +16,8 @@ Basis gas(double kappa, double R) {
   B.Rgas = R; B.sR = 1.0 / R;
   B.kappaFac = 2.0 * kappa / (kappa - 1.0);
   B.sKappaP1 = 1.0 / (kappa + 1.0);
+  B.logEntC = std::log(kappa - 1.0) / (kappa - 1.0);
+  B.kappa_kappaM1 = kappa / (kappa - 1.0);
   return B;
 }
 RotState rs(const double* a) { RotState S; S.rho = a[0]; S.srho = a[1]; S.E = a[2]; S.p = a[3]; S.v1 = a[4]; S.v2 = a[5]; S.v3 = a[6]; return S; }
@@ -110,6 +114,47 @@ void fgpt_pressure_riemann_adj(double kappa, double R, const double* x, double p
   const Basis B = gas(kappa, R);
   xb[0] = xb[1] = xb[2] = 0.0;
   pressure_riemann_adj(B, x[0], x[1], x[2], pbb, xb[0], xb[1], xb[2]);
+}
+
+// split_pair_flux (PI: pi = 1, SD: pi = 0) on the per-node inputs x = (qa[6], qb[6]) with the metric sum ms[3]: G[5]
+void fgpt_split_pair(int pi, const double* x, const double* ms, double* G) {
+  split_pair_flux(pi != 0, x[0], x[1], x[2], x[3], x[4], x[5], x[6], x[7], x[8], x[9], x[10], x[11], ms[0], ms[1], ms[2], G);
+}
+void fgpt_split_pair_adj(int pi, const double* x, const double* ms, const double* Gb, double* xb) {
+  for (int c = 0; c < 12; ++c) xb[c] = 0.0;
+  split_pair_flux_adj(pi != 0, x, x + 6, ms, Gb, xb, xb + 6);
+}
+// face-state fields x = (rho, E, u, v, w, p, srho) -> split inputs (q0, u, v, w, q4, q5) as the kernels form them
+void fgpt_split_inputs(int pi, const double* x, double* q) {
+  q[0] = x[0]; q[1] = x[2]; q[2] = x[3]; q[3] = x[4];
+  q[4] = pi ? 4.0 * x[5] : x[5];
+  q[5] = pi ? (x[1] + x[5]) * x[6] : x[1] + x[5];
+}
+void fgpt_split_inputs_adj(int pi, const double* x, const double* qb, double* xb) {
+  double fb[FS_NF] = {0., 0., 0., 0., 0., 0., 0., 0.};
+  split_inputs_to_face_adj(pi != 0, x[1], x[5], x[6], qb, fb);
+  xb[0] = fb[FS_RHO]; xb[1] = fb[FS_E]; xb[2] = fb[FS_U]; xb[3] = fb[FS_V]; xb[4] = fb[FS_W]; xb[5] = fb[FS_P]; xb[6] = fb[FS_SRHO];
+}
+// ConsToEntropy / EntropyToCons of k_prep and their adjoints
+void fgpt_cons_to_entropy(double kappa, const double* U, double* W) {
+  const Basis B = gas(kappa, 1.0);
+  for (int v = 0; v < 5; ++v) W[v] = U[v];
+  cons_to_entropy(B, W);
+}
+void fgpt_cons_to_entropy_adj(double kappa, const double* U, const double* Wb, double* Ub) {
+  const Basis B = gas(kappa, 1.0);
+  for (int v = 0; v < 5; ++v) Ub[v] = 0.0;
+  cons_to_entropy_adj(B, U, Wb, Ub);
+}
+void fgpt_entropy_to_cons(double kappa, const double* W, double* U) {
+  const Basis B = gas(kappa, 1.0);
+  for (int v = 0; v < 5; ++v) U[v] = W[v];
+  entropy_to_cons(B, U);
+}
+void fgpt_entropy_to_cons_adj(double kappa, const double* W, const double* Ub, double* Wb) {
+  const Basis B = gas(kappa, 1.0);
+  for (int v = 0; v < 5; ++v) Wb[v] = 0.0;
+  entropy_to_cons_adj(B, W, Ub, Wb);
 }
 
 }  // extern "C"

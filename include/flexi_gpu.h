@@ -296,8 +296,10 @@ int fg_set_elem_mu_scale(fg_handle* h, const double* scale);
  * J V by finite differences, implicit.f90:MatrixVector). t is unused (the exact-function source does not
  * depend on U; the LSERK adjoint recomputes its steps at the forward's stage times). The bulk velocity of a
  * channel body force is held fixed.
- * Supported: weak form and split form PI (Gauss-Lobatto, N = 1, 3, 7), N <= 7, LF/HLLC/Roe/RoeEntropyFix,
- * strong BR1/BR2 lifting, both overintegration types (the transposed filter), walls 3/4; no mortars. */
+ * Supported: weak form and the split forms PI and SD on Gauss and Gauss-Lobatto nodes (on Gauss nodes with the
+ * transposed entropy-variable prolongation and split-Gauss surface term), N <= 7, LF/HLLC/Roe/RoeEntropyFix,
+ * strong BR1/BR2 lifting, both overintegration types (the transposed filter), walls 3/4, mortar interfaces
+ * (transposed U_Mortar and Flux_Mortar, fillmortar.t90). */
 int fg_vjp_time_derivative(fg_handle* h, double t, const double* W, double* V, double* muScaleBar);
 
 /* J V of DGTimeDerivative_weakForm at the current state by the matrix-free finite difference of the

@@ -34,6 +34,13 @@ def pt():
     L.fgpt_pressure_riemann.argtypes = [D, D, P]
     L.fgpt_pressure_riemann.restype = D
     L.fgpt_pressure_riemann_adj.argtypes = [D, D, P, D, P]
+    L.fgpt_split_pair.argtypes = [I, P, P, P]
+    L.fgpt_split_pair_adj.argtypes = [I, P, P, P, P]
+    L.fgpt_split_inputs.argtypes = [I, P, P]
+    L.fgpt_split_inputs_adj.argtypes = [I, P, P, P]
+    for nm in ("fgpt_cons_to_entropy", "fgpt_entropy_to_cons"):
+        getattr(L, nm).argtypes = [D, P, P]
+        getattr(L, nm + "_adj").argtypes = [D, P, P, P]
     return L
 
 
@@ -179,3 +186,74 @@ def test_pressure_riemann_adjoint(pt):
         kept += 1
         assert err < TOL, (it, err)
     assert kept >= 90
+
+
+@pytest.mark.parametrize("pi", [1, 0])
+def test_split_pair_flux_adjoint(pt, pi):
+    """Two-point volume flux of the split form (PI, SD) transposed, w.r.t. both nodes' inputs."""
+    rng = np.random.default_rng(20 + pi)
+    for _ in range(50):
+        x = np.concatenate([rng.uniform(0.5, 2.0, 1), rng.uniform(-1, 1, 3), rng.uniform(0.5, 3.0, 2),
+                            rng.uniform(0.5, 2.0, 1), rng.uniform(-1, 1, 3), rng.uniform(0.5, 3.0, 2)])
+        ms = rng.standard_normal(3)
+
+        def f(x):
+            G = np.empty(5)
+            pt.fgpt_split_pair(pi, _p(np.ascontiguousarray(x)), _p(ms), _p(G))
+            return G
+
+        def fadj(x, yb):
+            xb = np.empty(12)
+            pt.fgpt_split_pair_adj(pi, _p(np.ascontiguousarray(x)), _p(ms), _p(np.ascontiguousarray(yb)), _p(xb))
+            return xb
+
+        err = _check(f, fadj, x, 5, rng)
+        assert err is not None and err < TOL, err
+
+
+@pytest.mark.parametrize("pi", [1, 0])
+def test_split_inputs_adjoint(pt, pi):
+    rng = np.random.default_rng(30 + pi)
+    for _ in range(30):
+        s = _state(rng)
+        x = np.array([s[0], s[2], s[4], s[5], s[6], s[3], s[1]])  # rho, E, u, v, w, p, 1/rho as independent fields
+
+        def f(x):
+            q = np.empty(6)
+            pt.fgpt_split_inputs(pi, _p(np.ascontiguousarray(x)), _p(q))
+            return q
+
+        def fadj(x, yb):
+            xb = np.empty(7)
+            pt.fgpt_split_inputs_adj(pi, _p(np.ascontiguousarray(x)), _p(np.ascontiguousarray(yb)), _p(xb))
+            return xb
+
+        err = _check(f, fadj, x, 6, rng)
+        assert err is not None and err < TOL, err
+
+
+def test_entropy_variable_transforms_adjoint(pt):
+    """ConsToEntropy and EntropyToCons of the Gauss split-form prolongation, transposed; EntropyToCons
+    inverts ConsToEntropy."""
+    rng = np.random.default_rng(40)
+    for _ in range(50):
+        s = _state(rng)
+        U = np.array([s[0], s[0] * s[4], s[0] * s[5], s[0] * s[6], s[2]])
+        W = np.empty(5)
+        pt.fgpt_cons_to_entropy(KAPPA, _p(U), _p(W))
+        back = np.empty(5)
+        pt.fgpt_entropy_to_cons(KAPPA, _p(W), _p(back))
+        assert np.allclose(back, U, rtol=1e-13, atol=1e-13)
+        for fwd, adj, x in (("fgpt_cons_to_entropy", "fgpt_cons_to_entropy_adj", U), ("fgpt_entropy_to_cons", "fgpt_entropy_to_cons_adj", W)):
+            def f(x, fwd=fwd):
+                out = np.empty(5)
+                getattr(pt, fwd)(KAPPA, _p(np.ascontiguousarray(x)), _p(out))
+                return out
+
+            def fadj(x, yb, adj=adj):
+                xb = np.empty(5)
+                getattr(pt, adj)(KAPPA, _p(np.ascontiguousarray(x)), _p(np.ascontiguousarray(yb)), _p(xb))
+                return xb
+
+            err = _check(f, fadj, x, 5, rng)
+            assert err is not None and err < TOL, (fwd, err)

@@ -32,7 +32,16 @@ CASES = {
                                           OverintegrationType=1, NUnder=3), "tgv"),
     "gl7_split_pi_roeef_br2_conscutoff": (dict(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roeentropyfix", Lifting="br2",
                                                OverintegrationType=2, NUnder=4), "tgv"),
+    # split form on Gauss nodes (entropy-variable prolongation, split-Gauss surface term): the discretisation of the
+    # reference's tgv/splitGauss regression at N=5, and SD at N=3 with BR2
+    "gauss5_split_pi_roeef_br1": (dict(N=5, NodeType="gauss", SplitDG="pi", Riemann="roeentropyfix", Lifting="br1"), "tgv"),
+    "gauss3_split_sd_hllc_br2": (dict(N=3, NodeType="gauss", SplitDG="sd", Riemann="hllc", Lifting="br2"), "tgv"),
+    "gauss4_split_pi_lf_br2": (dict(N=4, NodeType="gauss", SplitDG="pi", Riemann="lf", Lifting="br2"), "tgv"),
+    # split form on Gauss-Lobatto lines the shuffle-pair kernel does not take: SD, and PI with odd node counts
+    "gl3_split_sd_roe_br1": (dict(N=3, NodeType="gauss-lobatto", SplitDG="sd", Riemann="roe", Lifting="br1"), "tgv"),
+    "gl4_split_pi_roeef_br2": (dict(N=4, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roeentropyfix", Lifting="br2"), "tgv"),
     "channel_gauss3_weak_roe_br1": (dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="roe", Lifting="br1"), "channel"),
+    "channel_gauss3_split_pi_roe_br2": (dict(N=3, NodeType="gauss", SplitDG="pi", Riemann="roe", Lifting="br2"), "channel"),
     "channel_gl7_split_pi_roe_br1": (dict(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roe", Lifting="br1"), "channel"),
     "channel_gl3_split_pi_roeef_br2_adiabatic": (dict(N=3, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roeentropyfix", Lifting="br2"),
                                                  "adiabatic"),
@@ -86,7 +95,8 @@ def test_dot_product_against_exact_jvp(name):
         assert abs(lhs - rhs) <= 1e-11 * scale_, (k, lhs, rhs, abs(lhs - rhs) / scale_)
 
 
-@pytest.mark.parametrize("name", ["gauss3_weak_roeef_br1", "gl7_split_pi_roe_br1", "channel_gl7_split_pi_roe_br1"])
+@pytest.mark.parametrize("name", ["gauss3_weak_roeef_br1", "gl7_split_pi_roe_br1", "channel_gl7_split_pi_roe_br1",
+                                  "gauss5_split_pi_roeef_br1"])
 def test_dot_product_against_reference_fd_jvp(name):
     f, o, U, scale, rng = _setup(name, seed=1)
     V = rng.standard_normal(U.shape) * np.abs(U).max(axis=(0, 1, 2, 3))
@@ -97,7 +107,8 @@ def test_dot_product_against_reference_fd_jvp(name):
     assert abs(lhs - rhs) <= 1e-8 * float(np.abs(JV * W).sum()), (lhs, rhs)
 
 
-@pytest.mark.parametrize("name", ["gauss3_weak_roeef_br1", "gl7_split_pi_roeef_br2", "channel_gauss3_weak_roe_br1"])
+@pytest.mark.parametrize("name", ["gauss3_weak_roeef_br1", "gl7_split_pi_roeef_br2", "channel_gauss3_weak_roe_br1",
+                                  "gauss3_split_sd_hllc_br2"])
 def test_viscosity_multiplier_cotangent(name):
     f, o, U, scale, rng = _setup(name, seed=2)
     W = rng.standard_normal(U.shape)
@@ -116,10 +127,10 @@ def test_viscosity_multiplier_cotangent(name):
 
 
 def test_vjp_rejects_unsupported():
-    c = make_config(N=3, NodeType="gauss-lobatto", SplitDG="sd", Riemann="hllc")
+    c = make_config(N=3, NodeType="gauss-lobatto", SplitDG="kg", Riemann="hllc")
     f = Flexi(c, fmesh.tgv_box(2))
     f.U = testcases.tgv_state(f.elem_xgp(), mach=0.1)
-    with pytest.raises(Exception, match="split form PI"):
+    with pytest.raises(Exception, match="split forms PI and SD"):
         f.vjp_time_derivative(np.zeros(f.ushape))
 
 

@@ -9,7 +9,7 @@ against the oracle on the reference's own mortar meshes (tests/golden/hopr/).
 - a constant state is preserved on the periodic mortar meshes and a fluid at rest on the walled box.
 - ten LSERK steps with the CFL time step agree with the oracle's (states at 1e-11), on the sine-wave
   convergence case of convtest/h_3D_mortar (no source term: the operator only).
-- the adjoint refuses mortar meshes.
+- the adjoint (right-hand side and LSERK reverse sweep) against the oracle's exact JVP on mortar meshes.
 """
 import os
 
@@ -18,7 +18,7 @@ import pytest
 
 from _cases import oracle_cfg, perturb_state, product_cfg, rel_err
 from flexi_gb300 import mesh as fmesh, testcases
-from flexi_gb300.solver import Flexi, FlexiError
+from flexi_gb300.solver import Flexi
 from oracle import oracle as orc
 
 pytestmark = pytest.mark.gpu
@@ -130,13 +130,77 @@ def test_lserk_steps_mortar():
     assert err <= 1e-11, err
 
 
-def test_adjoint_refuses_mortars():
-    c = product_cfg(N=3, NodeType="gauss", SplitDG="weak", Riemann="roe", **COMMON)
-    f = Flexi(c, _mesh("CART_HEX_PERIODIC_MORTAR_002_mesh.h5"))
-    f.U = _state(f.elem_xgp(), seed=1)
-    with pytest.raises(FlexiError, match="mortar"):
-        f.vjp_time_derivative(np.ones_like(f.U))
+ADJ_MORTAR = {
+    "p002_gauss3_weak_roe_br1": ("CART_HEX_PERIODIC_MORTAR_002_mesh.h5", dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="roe",
+                                                                               Lifting="br1")),
+    "flipped004_gl3_split_pi_roeef_br2": ("CART_HEX_PERIODIC_MORTAR_FLIPPED_004_mesh.h5",
+                                          dict(N=3, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roeentropyfix", Lifting="br2")),
+    "cartbox_gauss4_weak_hllc_br2": ("cartbox3D_mortar_mesh.h5", dict(N=4, NodeType="gauss", SplitDG="weak", Riemann="hllc", Lifting="br2")),
+    "p002_gauss3_split_pi_roeef_br1": ("CART_HEX_PERIODIC_MORTAR_002_mesh.h5",
+                                       dict(N=3, NodeType="gauss", SplitDG="pi", Riemann="roeentropyfix", Lifting="br1")),
+}
+
+
+@pytest.mark.parametrize("name", list(ADJ_MORTAR))
+def test_adjoint_dot_product_mortar(name):
+    """Adjoint on mortar meshes (transposed U_Mortar, Flux_Mortar of the numerical and the lifting fluxes, and
+    the gradient interpolation): <J V, W> with J V the oracle's exact dual-number JVP against <V, J^T W> from
+    the GPU adjoint, within 1e-11 of sum |JV_i W_i|; the viscosity-multiplier cotangent against a fourth-order
+    Richardson quotient of <W, Ut> (1e-8)."""
+    mesh_name, kw = ADJ_MORTAR[name]
+    c = product_cfg(**kw, **COMMON)
+    m = _mesh(mesh_name)
+    f = Flexi(c, m)
+    o = orc.Oracle(oracle_cfg(c), m)
+    U0 = _state(f.elem_xgp(), seed=11, amp=0.05)
+    rng = np.random.default_rng(12)
+    scale = rng.uniform(0.8, 1.2, f.n_elems)
+    f.U = U0
+    f.set_elem_mu_scale(scale)
+    o.set_state(U0)
+    o.set_mu_scale(scale)
+    assert rel_err(f.DGTimeDerivative_weakForm(0.0), o.time_derivative(0.0)) <= 1e-12
+    for _ in range(2):
+        V = rng.standard_normal(U0.shape) * np.abs(U0).max(axis=(0, 1, 2, 3))
+        W = rng.standard_normal(U0.shape)
+        JV = o.jvp(V)
+        JTW, mub = f.vjp_time_derivative(W)
+        lhs, rhs = float((JV * W).sum()), float((V * JTW).sum())
+        assert abs(lhs - rhs) <= 1e-11 * float(np.abs(JV * W).sum()), (lhs, rhs)
+    ds = rng.standard_normal(f.n_elems)
+    h = 1e-3
+
+    def J(s):
+        f.set_elem_mu_scale(s)
+        return float((f.DGTimeDerivative_weakForm(0.0) * W).sum())
+
+    d1 = (J(scale + h * ds) - J(scale - h * ds)) / (2 * h)
+    d2 = (J(scale + 2 * h * ds) - J(scale - 2 * h * ds)) / (4 * h)
+    rich = (4 * d1 - d2) / 3
     f.close()
+    assert abs(float(mub @ ds) - rich) <= 1e-8 * abs(rich), (float(mub @ ds), rich)
+
+
+def test_lserk_adjoint_mortar():
+    """Seven LSERK steps reversed on a mortar mesh (fg_adjoint_forward / fg_adjoint_reverse) against the oracle's
+    exact tangent of the same steps (dual numbers), 1e-10 of sum |JV_i w_i|."""
+    c = product_cfg(N=3, NodeType="gauss", SplitDG="weak", Riemann="roe", Lifting="br2", CFLScale=0.5, DFLScale=0.5, **COMMON)
+    m = _mesh("CART_HEX_PERIODIC_MORTAR_FLIPPED_004_mesh.h5")
+    f = Flexi(c, m)
+    U0 = _state(f.elem_xgp(), seed=13, amp=0.05)
+    f.U = U0
+    dt = float(np.atleast_1d(f.CalcTimeStep()[0])[0])
+    f.adjoint_forward(7, dt, 3)
+    rng = np.random.default_rng(14)
+    w = rng.standard_normal(U0.shape)
+    Ub0, _ = f.adjoint_reverse(w)
+    f.close()
+    o = orc.Oracle(oracle_cfg(c), m)
+    o.set_state(U0)
+    V = rng.standard_normal(U0.shape) * np.abs(U0).max(axis=(0, 1, 2, 3))
+    JV = o.jvp_solve(V, 7, dt)
+    lhs, rhs = float((JV * w).sum()), float((Ub0 * V).sum())
+    assert abs(lhs - rhs) <= 1e-10 * float(np.abs(JV * w).sum()), (lhs, rhs)
 
 
 @pytest.mark.parametrize("name", ["CART_HEX_PERIODIC_MORTAR_002_mesh.h5", "cartbox3D_mortar_mesh.h5"])
