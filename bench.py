@@ -93,6 +93,8 @@ def parse():
                         "instances; adjoint: gradient of a kinetic-energy loss over a 200-step TGV solve (16^3, N=5)")
     p.add_argument("--ckpt", type=int, default=20, help="adjoint: checkpoint interval in steps")
     p.add_argument("--fd-dirs", type=int, default=20, help="adjoint: random directions of the finite-difference check")
+    p.add_argument("--exact-dirs", type=int, default=3, help="adjoint: directions (the first of the FD check) whose exact tangent "
+                                                              "the oracle also computes (dual numbers, host threads)")
     p.add_argument("--instances", type=int, default=256, help="ensemble size")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline leg (profiling runs)")
@@ -359,7 +361,7 @@ def run_gb300(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from flexi_gb300 import mesh as fmesh, testcases
-    from flexi_gb300.solver import Flexi, probe_fp64_pipe
+    from flexi_gb300.solver import Flexi, probe_fp64_pipe, probe_fp64_tensor
 
     n = args.elems
     kind = args.workload
@@ -373,6 +375,7 @@ def run_gb300(args):
     dof = f.n_elems * f.n ** 3
     stream = torch.cuda.ExternalStream(f.stream())
     pipe_rates = probe_fp64_pipe()
+    tensor_rates = probe_fp64_tensor()
 
     def barrier():
         torch.cuda.synchronize()
@@ -463,6 +466,8 @@ def run_gb300(args):
                               % (rf.get("attainable_frac_of_nominal") or float("nan"), pipe_rates["dfma"], pipe_rates["dadd"], pipe_rates["dmul"],
                                  pipe_rates["mixed"]),
                 "frac_of_attainable": rf.get("frac_of_attainable"), "sm_clock_hz": sm_hz, "sms": props.multi_processor_count,
+                "fp64_tensor_tflops": dict(tensor_rates, note="mma.sync m8n8k4 f64 alone, and interleaved with DFMA (both "
+                                           "counted): not above the DFMA pipe's own rate, the FP64 tensor path shares the FP64 units"),
                 "fp64_instr_per_dof": instr, "ncu_fp64_pipe_active_pct": instr.get("pipe_active_pct") if instr else None,
                 "traffic": (traffic * dof if traffic is not None else None),
                 "traffic_unit": "bytes per launch (ncu dram read+write, scaled per DOF)" if traffic is not None else None,
@@ -747,6 +752,8 @@ def ensemble_cpu_baseline(budget_s=10.0):
 # Differentiation workload: adjoint of a checkpointed fixed-dt solve
 # ---------------------------------------------------------------------------------------------------------
 ADJOINT_METRIC = "adjoint/forward cost ratio (TGV 16^3, N=5 Gauss, 200 LSERK steps)"
+ORACLE_ADJ_CFG = dict(N=5, nodeType=1, riemann=33, riemannBC=-1, lifting=1, weakLifting=0, consLifting=0, splitDG=-1, etaBR2=2.0, etaBR2_wall=-1.0,
+                      kappa=1.4, R=71.42857, Pr=0.72, mu0=1.0 / 1600.0, CFLScale=0.9, DFLScale=0.9, doTCSource=0, dpdx=-1.0)
 
 
 def run_adjoint(args):
@@ -830,13 +837,14 @@ def run_adjoint(args):
     clk = clocks.stop()
     L0 = 0.5 * (KE - target) ** 2
     # finite differences of the loss in seeded random directions of (U0, multipliers): the central difference with
-    # eps = 1e-6, and central differences at h, 2h, 4h (h = 2e-5) extrapolated twice (Richardson: fourth order from h, 2h,
-    # sixth order from all three). On this loss the central quotient's error is round-off (~4e-9 of the derivative) at
-    # 1e-6 and truncation (~170 h^2 relative) above 1e-5, which the extrapolation removes; the distance between the
-    # fourth- and sixth-order values estimates the fourth-order one's error, and that of the eps = 1e-6 quotient from
-    # the sixth-order value is that quotient's own error.
-    errs, errs_rich, fd_own, rich_own = [], [], [], []
-    h = 2e-5
+    # eps = 1e-6, and central differences at h, 2h, 4h (h = 1e-4) extrapolated twice (Richardson: fourth order from h, 2h,
+    # sixth order from all three). On this loss the central quotient's error is round-off (~4e-9 of the derivative at
+    # 1e-6, falling as 1/h) and truncation (~170 h^2 relative) above 1e-5, which the extrapolation removes; the distance
+    # between the fourth- and sixth-order values estimates the fourth-order one's error, and that of the eps = 1e-6
+    # quotient from the sixth-order value is that quotient's own error.
+    errs, errs_rich, fd_own, rich_own, exact = [], [], [], [], []
+    o_ex = None
+    h = 1e-4
     for k in range(args.fd_dirs):
         dU = rng.standard_normal(U0.shape) * np.abs(U0).max(axis=(0, 1, 2, 3))
         ds = rng.standard_normal(f.n_elems)
@@ -851,10 +859,21 @@ def run_adjoint(args):
         errs_rich.append(abs(ad - rich) / den)
         fd_own.append(abs(fd - rich) / den)
         rich_own.append(abs(r4[0] - rich) / den)
+        if k < args.exact_dirs:
+            # the exact tangent of the oracle's own solve of the same steps along the same direction (dual numbers):
+            # the FD quotients' error against it, and the adjoint's
+            if o_ex is None:
+                orc.set_threads(os.cpu_count() or 1)
+                o_ex = orc.Oracle(ORACLE_ADJ_CFG, m)
+            o_ex.set_state(U0)
+            o_ex.set_mu_scale(scale)
+            t0 = time.perf_counter()
+            JV = o_ex.jvp_solve(dU, n_steps, dt, d_scale=ds)
+            ex = float((UbarT * JV).sum())
+            exact.append({"direction": k, "adjoint_vs_exact": abs(ad - ex) / abs(ex), "richardson_vs_exact": abs(rich - ex) / abs(ex),
+                          "eps_1e-6_vs_exact": abs(fd - ex) / abs(ex), "oracle_s": time.perf_counter() - t0})
     # dot-product test at t_end against the reference's matrix-free FD JVP (FD_Order 2) on the oracle
-    o = orc.Oracle(dict(N=5, nodeType=1, riemann=33, riemannBC=-1, lifting=1, weakLifting=0, consLifting=0, splitDG=-1, etaBR2=2.0,
-                        etaBR2_wall=-1.0, kappa=1.4, R=71.42857, Pr=0.72, mu0=1.0 / 1600.0, CFLScale=0.9, DFLScale=0.9, doTCSource=0,
-                        dpdx=-1.0), m)
+    o = orc.Oracle(ORACLE_ADJ_CFG, m)
     o.set_state(UT)
     o.set_mu_scale(scale)
     V = rng.standard_normal(UT.shape) * np.abs(UT).max(axis=(0, 1, 2, 3))
@@ -887,7 +906,8 @@ def run_adjoint(args):
                          "median_rel_err_vs_richardson": float(np.median(errs_rich)) if errs_rich else None,
                          "eps_1e-6_quotient_own_error_max": max(fd_own) if fd_own else None,
                          "richardson_4th_order_own_error_max": max(rich_own) if rich_own else None,
-                         "note": "central FD at eps=1e-6 as the configuration states, and central FDs at h=2e-5, 2h, 4h extrapolated to "
+                         "exact_tangent": exact,
+                         "note": "central FD at eps=1e-6 as the configuration states, and central FDs at h=1e-4, 2h, 4h extrapolated to "
                                  "sixth order; the sixth-order value's distance from the eps=1e-6 quotient is that quotient's own error, "
                                  "its distance from the fourth-order value (h, 2h) bounds the fourth-order value's"},
             "dot_product_vs_reference_fd_jvp": {"rel_err": dot_err, "fd": "implicit.f90:MatrixVector FD_Order 2, Eps_Method 1, on the oracle"},

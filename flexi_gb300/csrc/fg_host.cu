@@ -344,6 +344,35 @@ __global__ void k_probe_fp64(double* out, double a, double b, int iters) {
   for (int c = 0; c < 8; ++c) s += x[c];
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
+
+// FP64 tensor-core MMA (mma.sync m8n8k4, 8x8x4 per warp instruction = 512 flops) in NM independent accumulator
+// chains per warp; WITH_FMA adds eight independent DFMA chains per thread to every iteration, to see whether the two
+// share the FP64 units (register operands only; one store per thread at the end)
+template <int NM, bool WITH_FMA>
+__global__ void k_probe_dmma(double* out, double a, double b, int iters) {
+  double c[NM][2], x[8];
+#pragma unroll
+  for (int m = 0; m < NM; ++m) { c[m][0] = threadIdx.x * 1e-4 + m; c[m][1] = 0.5 * m; }
+#pragma unroll
+  for (int i = 0; i < 8; ++i) x[i] = threadIdx.x * 1e-3 + i;
+  const double av = 1e-3 * (threadIdx.x & 7), bv = 2e-3 * (threadIdx.x & 3);
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int m = 0; m < NM; ++m)
+      asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
+                   : "+d"(c[m][0]), "+d"(c[m][1]) : "d"(av), "d"(bv));
+    if (WITH_FMA) {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) x[i] = fma(x[i], a, b);
+    }
+  }
+  double s = 0.;
+#pragma unroll
+  for (int m = 0; m < NM; ++m) s += c[m][0] + c[m][1];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) s += x[i];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
 }  // namespace fg
 
 using namespace fg;
@@ -2097,6 +2126,43 @@ int fg_probe_fp64_pipe(double* rates) {
     }
     rates[op] = (double)blocks * threads * iters * 8 / (best * 1e-3) / 1e12;
   }
+  cudaEventDestroy(a); cudaEventDestroy(b);
+  cudaFree(out);
+  CUDA_TRY(cudaGetLastError());
+  return FG_OK;
+}
+
+int fg_probe_fp64_tensor(double* rates) {
+  fg_handle* h = nullptr;
+  if (!rates) return fail(h, FG_ERR_CONFIG, "fg_probe_fp64_tensor: rates is NULL");
+  int dev = 0;
+  cudaDeviceProp p;
+  CUDA_TRY(cudaGetDevice(&dev));
+  CUDA_TRY(cudaGetDeviceProperties(&p, dev));
+  const int blocks = p.multiProcessorCount * 4, threads = 256, iters = 4096;
+  double* out = nullptr;
+  CUDA_TRY(cudaMalloc(&out, sizeof(double) * blocks * threads));
+  cudaEvent_t a, b;
+  cudaEventCreate(&a); cudaEventCreate(&b);
+  auto best_ms = [&](void (*k)(double*, double, double, int)) {
+    k<<<blocks, threads>>>(out, 0.999, 1e-3, 64);
+    float best = 1e30f;
+    for (int r = 0; r < 3; ++r) {
+      cudaEventRecord(a);
+      k<<<blocks, threads>>>(out, 0.999, 1e-3, iters);
+      cudaEventRecord(b);
+      cudaEventSynchronize(b);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, a, b);
+      best = std::min(best, ms);
+    }
+    return (double)best * 1e-3;
+  };
+  const double warps = (double)blocks * threads / 32.;
+  const double t0 = best_ms(k_probe_dmma<2, false>);
+  rates[0] = warps * iters * 2 * 512. / t0 / 1e12;
+  const double t1 = best_ms(k_probe_dmma<2, true>);
+  rates[1] = (warps * iters * 2 * 512. + (double)blocks * threads * iters * 8 * 2.) / t1 / 1e12;
   cudaEventDestroy(a); cudaEventDestroy(b);
   cudaFree(out);
   CUDA_TRY(cudaGetLastError());

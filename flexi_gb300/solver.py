@@ -398,3 +398,12 @@ def probe_fp64_pipe():
         raise FlexiError("fg_probe_fp64_pipe failed: " + L.fg_last_error(None).decode())
     return {"dfma": float(r[0]), "dadd": float(r[1]), "dmul": float(r[2]), "mixed": float(r[3])}
 
+
+def probe_fp64_tensor():
+    """fg_probe_fp64_tensor: FP64 tensor-core MMA throughput alone and interleaved with DFMA (TFLOP/s)."""
+    L = _lib.load()
+    r = np.zeros(2)
+    if L.fg_probe_fp64_tensor(_p(r)) != 0:
+        raise FlexiError("fg_probe_fp64_tensor failed: " + L.fg_last_error(None).decode())
+    return {"dmma": float(r[0]), "dmma_with_dfma": float(r[1])}
+

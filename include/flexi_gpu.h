@@ -361,6 +361,11 @@ int fg_set_launch_shapes(fg_handle* h, int epbPrep, int epbLift, int epbVol, int
  * fg_probe_fp64: 2 x the DFMA rate (TFLOP/s). */
 int fg_probe_fp64_pipe(double* rates);
 int fg_probe_fp64(double* tflops);
+/* FP64 tensor-core throughput of the current device, TFLOP/s: rates[0] = mma.sync m8n8k4 f64 alone (two independent
+ * accumulator chains per warp), rates[1] = the same interleaved with eight independent DFMA chains per thread (MMA
+ * and DFMA flops together). If rates[1] is not above the larger of rates[0] and 2 x the DFMA rate, the two share the
+ * FP64 units. No counterpart in the reference. */
+int fg_probe_fp64_tensor(double* rates);
 
 /* ---- Allocation-free right-hand side (no counterpart in the reference) ----------------------------
  * For callers that cannot allocate device memory: host codes whose device memory all comes from their

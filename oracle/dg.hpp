@@ -606,7 +606,7 @@ struct DG {
   void overintegrate_state() {
     const size_t nv3 = (size_t)n * n * n;
     if (C.overintType == 0) return;
-#pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
+#pragma omp parallel for schedule(static) if (!std::is_same<R, FD>::value)
     for (int e = 0; e < nE; ++e) {
       R* u = &U[(size_t)e * nv3 * 5];
       if (C.overintType == 1) {
@@ -681,7 +681,7 @@ struct DG {
         for (int v = 0; v < NV; ++v) Uface[((size_t)b * n + a) * NV + v] = acc[v];
       }
     };
-#pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
+#pragma omp parallel for schedule(static) if (!std::is_same<R, FD>::value)
     for (int s = 0; s < nS; ++s) {
       std::vector<R> Uface((size_t)n * n * NV);
       int e = s2e(0, s), ne = s2e(1, s);
@@ -726,7 +726,7 @@ struct DG {
   // slaveSign: -1 for the conservative flux, +1/-1 for strong/weak lifting
   template <int NV>
   void surf_int(const std::vector<R>& Fm, const std::vector<R>& Fs, std::vector<R>& Uout, R slaveSign) const {
-#pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
+#pragma omp parallel for schedule(static) if (!std::is_same<R, FD>::value)
     for (int e = 0; e < nE; ++e) {
       std::vector<R> FluxTmp((size_t)n * n * NV);
       for (int ls = 1; ls <= 6; ++ls) {
@@ -747,7 +747,7 @@ struct DG {
   // element's six sides)
   void surf_int_split_gauss() {
     const size_t nv3 = (size_t)n * n * n, ns2 = (size_t)n * n;
-#pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
+#pragma omp parallel for schedule(static) if (!std::is_same<R, FD>::value)
     for (int e = 0; e < nE; ++e) {
       std::vector<R> Fside(ns2 * 5);
       for (int ls = 1; ls <= 6; ++ls) {
@@ -816,7 +816,7 @@ struct DG {
       const std::vector<double>& DMat = C.weakLifting ? B.Dhat_T : B.D_T;
       for (int dir = 0; dir < 3; ++dir) {
         std::vector<R>& g = dir == 0 ? gradUx : (dir == 1 ? gradUy : gradUz);
-#pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
+#pragma omp parallel for schedule(static) if (!std::is_same<R, FD>::value)
         for (int e = 0; e < nE; ++e) {
           std::vector<R> Ef(NLIFT * nv3), Eg(NLIFT * nv3), Eh(NLIFT * nv3);
           for (size_t x = 0; x < nv3; ++x) for (int v = 0; v < NLIFT; ++v) {
@@ -837,7 +837,7 @@ struct DG {
         }
       }
     } else {
-#pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
+#pragma omp parallel for schedule(static) if (!std::is_same<R, FD>::value)
       for (int e = 0; e < nE; ++e)
         for (int k = 0; k < n; ++k) for (int j = 0; j < n; ++j) for (int i = 0; i < n; ++i) {
           R gxi[NLIFT], geta[NLIFT], gzeta[NLIFT];
@@ -1338,7 +1338,7 @@ struct DG {
   // ---------------- fillflux.f90:FillFlux ----------------
   void fill_flux(double t) {
     (void)t;
-#pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
+#pragma omp parallel for schedule(static) if (!std::is_same<R, FD>::value)
     for (int s = M.nBCSides; s < nS; ++s)
       for (int q = 0; q < n; ++q) for (int p = 0; p < n; ++p) {
         if (big_mortar(s)) continue;  // no slave: the big side's flux is the projection of its small sides'
@@ -1388,7 +1388,7 @@ struct DG {
   void vol_int() {
     const size_t nv3 = (size_t)n * n * n;
     const bool split = C.splitDG != SPLIT_NONE;
-#pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
+#pragma omp parallel for schedule(static) if (!std::is_same<R, FD>::value)
     for (int e = 0; e < nE; ++e) {
       std::vector<R> f(5 * nv3), g(5 * nv3), h(5 * nv3);
       // viscous fluxes fv,gv,hv (EvalDiffFlux3D) and, for the weak form, advective fluxes
@@ -1473,13 +1473,13 @@ struct DG {
     const size_t nv3 = (size_t)n * n * n;
     long long& fc = flop_counter();
     phase[0] = fc;
-#pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
+#pragma omp parallel for schedule(static) if (!std::is_same<R, FD>::value)
     for (int e = 0; e < nE; ++e) for (size_t x = 0; x < nv3; ++x) cons_to_prim(&U[((size_t)e * nv3 + x) * 5], &UPrim[((size_t)e * nv3 + x) * 6]);
     if (!entropyVars) { prolong_to_face<5>(U, U_master, U_slave); u_mortar<5>(U_master); }  // dg.f90:372-416
     else {
       // eos.f90:ConsToPrimToEntropy, prolongtoface.t90:ProlongToFaceEntropy (EntropyToCons on every side
       // of an existing element)
-#pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
+#pragma omp parallel for schedule(static) if (!std::is_same<R, FD>::value)
       for (int e = 0; e < nE; ++e) for (size_t x = 0; x < nv3; ++x) prim_to_entropy(&UPrim[((size_t)e * nv3 + x) * 6], &V[((size_t)e * nv3 + x) * 5]);
       prolong_to_face<5>(V, V_master, V_slave);
       const size_t ns2 = (size_t)n * n;
@@ -1504,7 +1504,7 @@ struct DG {
     if (entropyVars) surf_int_split_gauss();
     else surf_int<5>(Flux_master, Flux_slave, Ut, R(-1.));
     // Ut = -Ut ; TestcaseSource (channel) ; ApplyJacobianCons
-#pragma omp parallel for schedule(static) if (std::is_same<R, double>::value)
+#pragma omp parallel for schedule(static) if (!std::is_same<R, FD>::value)
     for (int e = 0; e < nE; ++e) {
       for (size_t x = 0; x < nv3; ++x) {
         double sj = M.sJ[(size_t)e * nv3 + x];
