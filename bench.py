@@ -837,14 +837,15 @@ def run_adjoint(args):
     clk = clocks.stop()
     L0 = 0.5 * (KE - target) ** 2
     # finite differences of the loss in seeded random directions of (U0, multipliers): the central difference with
-    # eps = 1e-6, and central differences at h, 2h, 4h (h = 1e-4) extrapolated twice (Richardson: fourth order from h, 2h,
+    # eps = 1e-6, and central differences at h, 2h, 4h (h = 2e-5) extrapolated twice (Richardson: fourth order from h, 2h,
     # sixth order from all three). On this loss the central quotient's error is round-off (~4e-9 of the derivative at
-    # 1e-6, falling as 1/h) and truncation (~170 h^2 relative) above 1e-5, which the extrapolation removes; the distance
-    # between the fourth- and sixth-order values estimates the fourth-order one's error, and that of the eps = 1e-6
-    # quotient from the sixth-order value is that quotient's own error.
+    # 1e-6, falling as 1/h) and truncation (~170 h^2 relative) above 1e-5, which the extrapolation removes; from h = 1e-4
+    # on the extrapolated values drift again (2e-8 against the exact tangent). The distance between the fourth- and
+    # sixth-order values estimates the fourth-order one's truncation error, and that of the eps = 1e-6 quotient from the
+    # sixth-order value is that quotient's own error; the exact tangent (--exact-dirs) measures both FD values' errors.
     errs, errs_rich, fd_own, rich_own, exact = [], [], [], [], []
     o_ex = None
-    h = 1e-4
+    h = 2e-5
     for k in range(args.fd_dirs):
         dU = rng.standard_normal(U0.shape) * np.abs(U0).max(axis=(0, 1, 2, 3))
         ds = rng.standard_normal(f.n_elems)
@@ -907,7 +908,9 @@ def run_adjoint(args):
                          "eps_1e-6_quotient_own_error_max": max(fd_own) if fd_own else None,
                          "richardson_4th_order_own_error_max": max(rich_own) if rich_own else None,
                          "exact_tangent": exact,
-                         "note": "central FD at eps=1e-6 as the configuration states, and central FDs at h=1e-4, 2h, 4h extrapolated to "
+                         "adjoint_vs_exact_max": max((x["adjoint_vs_exact"] for x in exact), default=None),
+                         "richardson_vs_exact_max": max((x["richardson_vs_exact"] for x in exact), default=None),
+                         "note": "central FD at eps=1e-6 as the configuration states, and central FDs at h=2e-5, 2h, 4h extrapolated to "
                                  "sixth order; the sixth-order value's distance from the eps=1e-6 quotient is that quotient's own error, "
                                  "its distance from the fourth-order value (h, 2h) bounds the fourth-order value's"},
             "dot_product_vs_reference_fd_jvp": {"rel_err": dot_err, "fd": "implicit.f90:MatrixVector FD_Order 2, Eps_Method 1, on the oracle"},

@@ -1,5 +1,9 @@
 """Adjoint of the right-hand side (fg_vjp_time_derivative) against the oracle's Jacobian-vector products.
 
+Cases: the weak form and the split forms PI and SD on Gauss-Lobatto nodes (the shuffle-pair kernel for PI on lines
+of 2, 4 or 8 nodes, the per-node kernel otherwise) and on Gauss nodes (entropy-variable prolongation and split-Gauss
+surface term transposed), every supported Riemann solver, BR1/BR2, both overintegration types, walls.
+
 Dot-product test <J V, W> = <V, J^T W>: J V comes from the oracle, exactly by its dual-number
 instantiation of the restated algorithm and approximately by the matrix-free finite difference of the
 reference's implicit solver (src/implicit/implicit.f90:MatrixVector, FD_Order 2); J^T W comes from the
