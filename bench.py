@@ -361,7 +361,7 @@ def run_gb300(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from flexi_gb300 import mesh as fmesh, testcases
-    from flexi_gb300.solver import Flexi, probe_fp64_pipe, probe_fp64_tensor
+    from flexi_gb300.solver import Flexi, probe_fp64_lanes, probe_fp64_pipe, probe_fp64_tensor
 
     n = args.elems
     kind = args.workload
@@ -376,6 +376,7 @@ def run_gb300(args):
     stream = torch.cuda.ExternalStream(f.stream())
     pipe_rates = probe_fp64_pipe()
     tensor_rates = probe_fp64_tensor()
+    lane_ms = probe_fp64_lanes()
 
     def barrier():
         torch.cuda.synchronize()
@@ -468,6 +469,8 @@ def run_gb300(args):
                 "frac_of_attainable": rf.get("frac_of_attainable"), "sm_clock_hz": sm_hz, "sms": props.multi_processor_count,
                 "fp64_tensor_tflops": dict(tensor_rates, note="mma.sync m8n8k4 f64 alone, and interleaved with DFMA (both "
                                            "counted): not above the DFMA pipe's own rate, the FP64 tensor path shares the FP64 units"),
+                "fp64_idle_lanes_ms": dict(lane_ms, note="the same DFMA chains with 32/16/8/4/1 active lanes per warp: equal "
+                                           "times, so idle lanes of FP64 code cost pipe time like active ones"),
                 "fp64_instr_per_dof": instr, "ncu_fp64_pipe_active_pct": instr.get("pipe_active_pct") if instr else None,
                 "traffic": (traffic * dof if traffic is not None else None),
                 "traffic_unit": "bytes per launch (ncu dram read+write, scaled per DOF)" if traffic is not None else None,

@@ -373,6 +373,25 @@ __global__ void k_probe_dmma(double* out, double a, double b, int iters) {
   for (int i = 0; i < 8; ++i) s += x[i];
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
+
+// the DFMA chains of k_probe_fp64<0> run by the first K lanes of every warp only: whether the FP64 pipe's issue
+// time for a warp instruction depends on its active lanes
+template <int K>
+__global__ void k_probe_fp64_lanes(double* out, double a, double b, int iters) {
+  double x[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) x[c] = threadIdx.x * 1e-3 + c;
+  if ((threadIdx.x & 31) < K) {
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+      for (int c = 0; c < 8; ++c) x[c] = fma(x[c], a, b);
+    }
+  }
+  double s = 0.;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) s += x[c];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
 }  // namespace fg
 
 using namespace fg;
@@ -2163,6 +2182,40 @@ int fg_probe_fp64_tensor(double* rates) {
   rates[0] = warps * iters * 2 * 512. / t0 / 1e12;
   const double t1 = best_ms(k_probe_dmma<2, true>);
   rates[1] = (warps * iters * 2 * 512. + (double)blocks * threads * iters * 8 * 2.) / t1 / 1e12;
+  cudaEventDestroy(a); cudaEventDestroy(b);
+  cudaFree(out);
+  CUDA_TRY(cudaGetLastError());
+  return FG_OK;
+}
+
+int fg_probe_fp64_lanes(double* ms) {
+  fg_handle* h = nullptr;
+  if (!ms) return fail(h, FG_ERR_CONFIG, "fg_probe_fp64_lanes: ms is NULL");
+  int dev = 0;
+  cudaDeviceProp p;
+  CUDA_TRY(cudaGetDevice(&dev));
+  CUDA_TRY(cudaGetDeviceProperties(&p, dev));
+  const int blocks = p.multiProcessorCount * 8, threads = 256, iters = 4096;
+  double* out = nullptr;
+  CUDA_TRY(cudaMalloc(&out, sizeof(double) * blocks * threads));
+  cudaEvent_t a, b;
+  cudaEventCreate(&a); cudaEventCreate(&b);
+  void (*kern[5])(double*, double, double, int) = {k_probe_fp64_lanes<32>, k_probe_fp64_lanes<16>, k_probe_fp64_lanes<8>,
+                                                   k_probe_fp64_lanes<4>, k_probe_fp64_lanes<1>};
+  for (int v = 0; v < 5; ++v) {
+    kern[v]<<<blocks, threads>>>(out, 0.999, 1e-3, 64);
+    float best = 1e30f;
+    for (int r = 0; r < 3; ++r) {
+      cudaEventRecord(a);
+      kern[v]<<<blocks, threads>>>(out, 0.999, 1e-3, iters);
+      cudaEventRecord(b);
+      cudaEventSynchronize(b);
+      float t = 0.f;
+      cudaEventElapsedTime(&t, a, b);
+      best = std::min(best, t);
+    }
+    ms[v] = best;
+  }
   cudaEventDestroy(a); cudaEventDestroy(b);
   cudaFree(out);
   CUDA_TRY(cudaGetLastError());

@@ -751,14 +751,15 @@ struct Stage {
 };
 
 // surface integral + Jacobian + source + RK update for the node owned by this thread
-template <int n, bool GL>
+// SURF = false: the surface integral was added face-parallel before (gl_surface_faces)
+template <int n, bool GL, bool SURF = true>
 __device__ __forceinline__ void finish_node(const Dev& d, const SBasis<n>& Bs, const Stage& st, const double* sFl, int es, int e, int x,
                                             double* ut) {
   constexpr int n2 = n * n, n3 = n * n * n, N = n - 1;
   const int i = x % n, j = (x / n) % n, k = x / n2;
   const int idx3[3] = {i, j, k};
 #pragma unroll
-  for (int dir = 0; dir < 3; ++dir) {
+  for (int dir = 0; dir < (SURF ? 3 : 0); ++dir) {
     const int lsM = dir == 0 ? XI_MINUS : (dir == 1 ? ETA_MINUS : ZETA_MINUS);
     const int lsP = dir == 0 ? XI_PLUS : (dir == 1 ? ETA_PLUS : ZETA_PLUS);
     const int a = dir == 0 ? j : i, b = dir == 2 ? j : k;
@@ -861,6 +862,31 @@ __device__ __forceinline__ void load_face_fluxes(const Dev& d, double* sFl, int 
     const double sg = flip == 0 ? 1.0 : -1.0;
 #pragma unroll
     for (int v = 0; v < 5; ++v) sFl[o * 5 + v] = sg * d.flux[((size_t)s * 5 + v) * n2 + pq];
+  }
+}
+
+// surfint.t90:SurfInt on Gauss-Lobatto nodes, face-parallel: the flux of each face point times L_HatMinus(0) /
+// L_HatPlus(N) added to its face node's entry of sA ([EPB][5][n3]), one direction (two opposite faces, disjoint node
+// sets) at a time, so that no lane of a warp idles on interior nodes (the FP64 pipe pays for idle lanes). Ends with
+// a barrier.
+template <int n, int E = 0>
+__device__ __forceinline__ void gl_surface_faces(const SBasis<n>& Bs, const double* sFl, double* sA, int e0, int nElems) {
+  constexpr int n2 = n * n, n3 = n2 * n, EPB = Shape<n, E>::EPB, N = n - 1;
+#pragma unroll 1
+  for (int dir = 0; dir < 3; ++dir) {
+    for (int t = threadIdx.x; t < EPB * 2 * n2; t += blockDim.x) {
+      const int es = t / (2 * n2), r = t - es * 2 * n2, side = r / n2, ab = r - side * n2;
+      if (e0 + es >= nElems) continue;
+      const int ls = side == 0 ? (dir == 0 ? XI_MINUS : (dir == 1 ? ETA_MINUS : ZETA_MINUS))
+                               : (dir == 0 ? XI_PLUS : (dir == 1 ? ETA_PLUS : ZETA_PLUS));
+      const int x = face_node(ls, ab % n, ab / n, side == 0 ? 0 : N, n);
+      const double w = side == 0 ? Bs.LhM(0) : Bs.LhP(N);
+      const double* F = sFl + ((es * 6 + ls - 1) * n2 + ab) * 5;
+      double* A = sA + es * 5 * n3 + x;
+#pragma unroll
+      for (int v = 0; v < 5; ++v) A[v * n3] = fma(F[v], w, A[v * n3]);
+    }
+    __syncthreads();
   }
 }
 
@@ -1108,6 +1134,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS, (n == 8 ? 2 : 1)) k_vol_spl
       __syncthreads();
     }
   }
+  gl_surface_faces<n>(Bs, sFl, sA, e0, d.nElems);
   // viscous fluxes (weak form): transformed fluxes of this node from the metrics still in sR, written
   // over sR once every thread has finished reading it (one node per thread: EPB * n3 == THREADS)
   static_assert(EPB * n3 == S::THREADS, "one node per thread");
@@ -1161,7 +1188,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS, (n == 8 ? 2 : 1)) k_vol_spl
         ut[1 + v] = fma(ck, V[(8 + v) * n3 + xk], ut[1 + v]);
       }
     }
-    finish_node<n, true>(d, Bs, st, sFl, es, e, x, ut);
+    finish_node<n, true, false>(d, Bs, st, sFl, es, e, x, ut);
   }
 }
 
@@ -1396,6 +1423,7 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
       __syncthreads();
     }
   }
+  if constexpr (GL) gl_surface_faces<n>(Bs, sFl, sA, e0, d.nElems);
   // viscous fluxes (weak form): transformed fluxes of each node from the metrics still in sR; with one node
   // per thread they are written over sR once every thread has finished reading it, else into sV
   constexpr int VS = SS::NPT > 1 ? 12 : 15;  // field stride of the viscous-flux array
@@ -1449,7 +1477,7 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
         ut[1 + v] = fma(ck, V[(8 + v) * n3 + xk], ut[1 + v]);
       }
     }
-    finish_node<n, GL>(d, Bs, st, sFl, es, e, x, ut);
+    finish_node<n, GL, !GL>(d, Bs, st, sFl, es, e, x, ut);
   }
 }
 

@@ -239,6 +239,9 @@ INTERFACE
   INTEGER(C_INT) FUNCTION fg_probe_fp64_tensor(rates) BIND(C,NAME='fg_probe_fp64_tensor')
     IMPORT; REAL(C_DOUBLE) :: rates(*)
   END FUNCTION
+  INTEGER(C_INT) FUNCTION fg_probe_fp64_lanes(ms) BIND(C,NAME='fg_probe_fp64_lanes')
+    IMPORT; REAL(C_DOUBLE) :: ms(*)
+  END FUNCTION
   INTEGER(C_INT) FUNCTION fg_time_derivative_noalloc(cfg, mesh, U, Ut, stream) BIND(C,NAME='fg_time_derivative_noalloc')
     IMPORT; TYPE(fg_config) :: cfg; TYPE(fg_device_mesh) :: mesh; TYPE(C_PTR), VALUE :: U, Ut, stream
   END FUNCTION
@@ -256,7 +259,7 @@ PUBLIC :: fg_time_derivative, fg_calc_timestep, fg_get_dt_elem, fg_timestep_lser
 PUBLIC :: fg_get_gradients, fg_get_stream, fg_launch_count, fg_debug_array, fg_profile_enable, fg_profile_read
 PUBLIC :: fg_set_elem_mu_scale, fg_vjp_time_derivative, fg_jvp_time_derivative, fg_adjoint_forward, fg_adjoint_recomputed_steps
 PUBLIC :: fg_adjoint_reverse, fg_set_body_force_field, fg_wall_shear, fg_autotune, fg_autotune_choice, fg_set_launch_shapes
-PUBLIC :: fg_probe_fp64_pipe, fg_probe_fp64, fg_probe_fp64_tensor, fg_time_derivative_noalloc
+PUBLIC :: fg_probe_fp64_pipe, fg_probe_fp64, fg_probe_fp64_tensor, fg_probe_fp64_lanes, fg_time_derivative_noalloc
 
 !----------------------------------------------------------------------------------------------------------------------------------
 ! Part 2: the FLEXI shim

@@ -407,3 +407,12 @@ def probe_fp64_tensor():
         raise FlexiError("fg_probe_fp64_tensor failed: " + L.fg_last_error(None).decode())
     return {"dmma": float(r[0]), "dmma_with_dfma": float(r[1])}
 
+
+def probe_fp64_lanes():
+    """fg_probe_fp64_lanes: time (ms) of the same DFMA chains with 32, 16, 8, 4 and 1 active lanes per warp."""
+    L = _lib.load()
+    r = np.zeros(5)
+    if L.fg_probe_fp64_lanes(_p(r)) != 0:
+        raise FlexiError("fg_probe_fp64_lanes failed: " + L.fg_last_error(None).decode())
+    return {str(k): float(v) for k, v in zip((32, 16, 8, 4, 1), r)}
+

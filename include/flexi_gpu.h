@@ -366,6 +366,10 @@ int fg_probe_fp64(double* tflops);
  * and DFMA flops together). If rates[1] is not above the larger of rates[0] and 2 x the DFMA rate, the two share the
  * FP64 units. No counterpart in the reference. */
 int fg_probe_fp64_tensor(double* rates);
+/* Time (ms) of the same DFMA chains run by 32, 16, 8, 4 and 1 active lanes of every warp (ms[0..4]): equal times mean
+ * the FP64 pipe spends the same issue time on a warp instruction whatever its active lanes, so idle lanes of FP64 code
+ * are lost pipe time. No counterpart in the reference. */
+int fg_probe_fp64_lanes(double* ms);
 
 /* ---- Allocation-free right-hand side (no counterpart in the reference) ----------------------------
  * For callers that cannot allocate device memory: host codes whose device memory all comes from their
