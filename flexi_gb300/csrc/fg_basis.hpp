@@ -37,14 +37,14 @@ inline Mat matmul(const Mat& A, const Mat& B) {
 
 // Legendre polynomial of degree m at x, scaled by sqrt(m+1/2), and its derivative
 inline void legendre(int m, double x, double& L, double& dL) {
-  double l0 = 1., l1 = x, d0 = 0., d1 = 1.;
+  double l0 = 1., l1 = x, d1 = 1.;
   if (m == 0) { L = 1.; dL = 0.; }
   else if (m == 1) { L = x; dL = 1.; }
   else {
     for (int k = 2; k <= m; ++k) {
       const double lk = ((2. * k - 1.) * x * l1 - (k - 1.) * l0) / k;
       const double dk = k * l1 + x * d1;
-      l0 = l1; l1 = lk; d0 = d1; d1 = dk;
+      l0 = l1; l1 = lk; d1 = dk;
     }
     L = l1; dL = d1;
   }

@@ -324,6 +324,34 @@ __global__ void k_dev_to_fortran(const double* __restrict__ d, double* __restric
   const long long e = r / n3;
   f[t] = d[(e * nvDev + v0 + v) * n3 + x];
 }
+// One CTA per element: the element's nv x n3 block between the Fortran layout (variable fastest) and the device layout
+// (variable-major), staged through shared memory so that the global reads and writes are both contiguous and the
+// index arithmetic is 32-bit (the element-wise kernels above serve blocks larger than the tile limit)
+__global__ void k_fortran_to_dev_tiled(const double* __restrict__ f, double* __restrict__ d, int nv, int n3) {
+  extern __shared__ double s[];
+  const int m = nv * n3;
+  const size_t base = (size_t)blockIdx.x * m;
+  for (int t = threadIdx.x; t < m; t += blockDim.x) s[t] = f[base + t];
+  __syncthreads();
+  for (int t = threadIdx.x; t < m; t += blockDim.x) {
+    const int v = t / n3, x = t - v * n3;
+    d[base + t] = s[x * nv + v];
+  }
+}
+__global__ void k_dev_to_fortran_tiled(const double* __restrict__ d, double* __restrict__ f, int nvDev, int v0, int nv, int n3) {
+  extern __shared__ double s[];
+  const int m = nv * n3;
+  const double* src = d + ((size_t)blockIdx.x * nvDev + v0) * n3;
+  for (int t = threadIdx.x; t < m; t += blockDim.x) s[t] = src[t];
+  __syncthreads();
+  double* dst = f + (size_t)blockIdx.x * m;
+  for (int t = threadIdx.x; t < m; t += blockDim.x) {
+    const int x = t / nv, v = t - x * nv;
+    dst[t] = s[v * n3 + x];
+  }
+}
+constexpr size_t FG_TILE_SMEM_MAX = 96 * 1024;
+
 // FP64 pipe throughput probe: 8 independent chains per thread of one FP64 operation (OP 0 DFMA, 1 DADD, 2 DMUL) or of
 // the three mixed (OP 3: chain c uses operation c mod 3); every grid shape from 4 to 32 chains and 128 to 512 threads,
 // and every mix, gives the same rate on GB300
@@ -1369,12 +1397,37 @@ int fg_get_side_to_elem(fg_handle* h, int* out) {
   return FG_OK;
 }
 
+// Fortran layout (nv, n, n, n, nElems) in device memory -> device layout [e][nv][n3], on the handle's stream
+static void fortran_to_dev(fg_handle* h, const double* f, double* d, int nv) {
+  const int n3 = h->M.n * h->M.n * h->M.n;
+  const size_t bytes = sizeof(double) * nv * n3;
+  if (bytes <= FG_TILE_SMEM_MAX) {
+    cudaFuncSetAttribute(k_fortran_to_dev_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    k_fortran_to_dev_tiled<<<(unsigned)h->M.nElems, 256, bytes, h->st>>>(f, d, nv, n3);
+  } else {
+    const long long total = (long long)h->M.nElems * nv * n3;
+    k_fortran_to_dev<<<(unsigned)((total + 255) / 256), 256, 0, h->st>>>(f, d, nv, n3, total);
+  }
+}
+// device layout [e][nvDev][n3], variables v0 .. v0+nv-1 -> Fortran layout (nv, n, n, n, nElems) in device memory
+static void dev_to_fortran(fg_handle* h, const double* d, double* f, int nvDev, int v0, int nv) {
+  const int n3 = h->M.n * h->M.n * h->M.n;
+  const size_t bytes = sizeof(double) * nv * n3;
+  if (bytes <= FG_TILE_SMEM_MAX) {
+    cudaFuncSetAttribute(k_dev_to_fortran_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    k_dev_to_fortran_tiled<<<(unsigned)h->M.nElems, 256, bytes, h->st>>>(d, f, nvDev, v0, nv, n3);
+  } else {
+    const long long total = (long long)h->M.nElems * nv * n3;
+    k_dev_to_fortran<<<(unsigned)((total + 255) / 256), 256, 0, h->st>>>(d, f, nvDev, v0, nv, n3, total);
+  }
+}
+
 int fg_set_state(fg_handle* h, const double* U) {
   if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
   const int n3 = h->M.n * h->M.n * h->M.n;
   const long long total = (long long)h->M.nElems * 5 * n3;
   CUDA_TRY(cudaMemcpyAsync(h->dStage, U, total * sizeof(double), cudaMemcpyHostToDevice, h->st));
-  k_fortran_to_dev<<<(unsigned)((total + 255) / 256), 256, 0, h->st>>>(h->dStage, h->d.U, 5, n3, total);
+  fortran_to_dev(h, h->dStage, h->d.U, 5);
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaStreamSynchronize(h->st));
   return FG_OK;
@@ -1383,7 +1436,7 @@ int fg_set_state(fg_handle* h, const double* U) {
 static int export_field(fg_handle* h, const double* dsrc, int nvDev, int v0, int nv, double* out) {
   const int n3 = h->M.n * h->M.n * h->M.n;
   const long long total = (long long)h->M.nElems * nv * n3;
-  k_dev_to_fortran<<<(unsigned)((total + 255) / 256), 256, 0, h->st>>>(dsrc, h->dStage, nvDev, v0, nv, n3, total);
+  dev_to_fortran(h, dsrc, h->dStage, nvDev, v0, nv);
   CUDA_TRY(cudaGetLastError());
   CUDA_TRY(cudaMemcpyAsync(out, h->dStage, total * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   CUDA_TRY(cudaStreamSynchronize(h->st));
@@ -1464,7 +1517,7 @@ int fg_jvp_time_derivative(fg_handle* h, double t, const double* V, double* JV, 
   double eps = rEps0 / std::sqrt(Vabs);
   if (epsMethod == 2) eps *= std::sqrt(1. + normXk);
   CUDA_TRY(cudaMemcpyAsync(h->dStage, V, bytes, cudaMemcpyHostToDevice, h->st));
-  k_fortran_to_dev<<<grid, 256, 0, h->st>>>(h->dStage, h->jvpV, 5, n3, cnt);
+  fortran_to_dev(h, h->dStage, h->jvpV, 5);
   CUDA_TRY(cudaMemcpyAsync(h->jvpXk, h->d.U, bytes, cudaMemcpyDeviceToDevice, h->st));
   launch_step_setup(h, 2, 0., false);  // bulk velocity of Xk, held for every evaluation
   if (fdOrder == 1) {
@@ -1496,7 +1549,7 @@ int fg_vjp_time_derivative(fg_handle* h, double t, const double* W, double* V, d
   const long long total = (long long)h->M.nElems * 5 * n3;
   h->launches = 0;
   CUDA_TRY(cudaMemcpyAsync(h->dStage, W, total * sizeof(double), cudaMemcpyHostToDevice, h->st));
-  k_fortran_to_dev<<<(unsigned)((total + 255) / 256), 256, 0, h->st>>>(h->dStage, const_cast<double*>(h->a.W), 5, n3, total);
+  fortran_to_dev(h, h->dStage, const_cast<double*>(h->a.W), 5);
   AdjDev a = h->a;
   a.accumulate = 0;
   launch_vjp(h, h->d, a);
@@ -1733,11 +1786,10 @@ int fg_adjoint_reverse(fg_handle* h, const double* UbarT, double* Ubar0, double*
   const int n3 = h->M.n * h->M.n * h->M.n;
   const long long cnt = (long long)h->M.nElems * 5 * n3;
   const size_t bytes = (size_t)cnt * sizeof(double);
-  const unsigned gridAx = (unsigned)((cnt + 255) / 256);
   h->launches = 0;
   h->adjRecomputed = 0;
   CUDA_TRY(cudaMemcpyAsync(h->dStage, UbarT, bytes, cudaMemcpyHostToDevice, h->st));
-  k_fortran_to_dev<<<gridAx, 256, 0, h->st>>>(h->dStage, h->adjUbar, 5, n3, cnt);
+  fortran_to_dev(h, h->dStage, h->adjUbar, 5);
   CUDA_TRY(cudaMemsetAsync(h->a.muElemb, 0, sizeof(double) * h->M.nElems, h->st));
   CUDA_TRY(cudaMemsetAsync(h->adjPartial, 0, sizeof(double) * h->M.nElems, h->st));
   CUDA_TRY(cudaMemsetAsync(h->adjFbar, 0, sizeof(double) * h->M.nElems * n3, h->st));
@@ -1793,7 +1845,7 @@ int fg_set_body_force_field(fg_handle* h, const double* F) {
   }
   if (F) {
     CUDA_TRY(cudaMemcpyAsync(h->dStage, F, total * sizeof(double), cudaMemcpyHostToDevice, h->st));
-    k_fortran_to_dev<<<(unsigned)((total + 255) / 256), 256, 0, h->st>>>(h->dStage, h->d.forceField, 1, n3, total);
+    fortran_to_dev(h, h->dStage, h->d.forceField, 1);
   } else {
     k_fill<<<(unsigned)((total + 255) / 256), 256, 0, h->st>>>(h->d.forceField, 0., (int)total);
   }

@@ -1209,7 +1209,12 @@ template <int n> struct SplitShape {
   static constexpr int EPB = Shape<n>::EPB, n2 = n * n, n3 = n * n * n;
   static constexpr int SEG = 32 / n;                       // lines per warp
   static constexpr int LINES = EPB * n2;                   // lines per direction per CTA
-  static constexpr int LINE_THREADS = ((LINES + SEG - 1) / SEG) * 32;
+  // each direction's pass runs whole warps of SEG lines; the LO lines of each direction left over go to one joint
+  // pass over the three directions (a warp with a single line would issue its FP64 work for 32 lanes)
+  static constexpr int MAIN_WARPS = LINES / SEG;
+  static constexpr int LO = LINES - MAIN_WARPS * SEG;
+  static constexpr int LO_WARPS = (3 * LO + SEG - 1) / SEG;
+  static constexpr int LINE_THREADS = (MAIN_WARPS > LO_WARPS ? MAIN_WARPS : LO_WARPS) * 32;
   static constexpr int NODE_THREADS = ((EPB * n3 + 31) / 32) * 32;
   static constexpr int WANT = LINE_THREADS > NODE_THREADS ? LINE_THREADS : NODE_THREADS;
   static constexpr int THREADS = WANT > 512 ? 512 : WANT;
@@ -1221,7 +1226,7 @@ template <int n> struct SplitShape {
   template <bool GL>
   __host__ __device__ static constexpr long long big() {
     return 2LL * n2 + (long long)EPB * (20 * n3 + 30 * n2) + (GL ? 0LL : (long long)EPB * 6 * FACE_NF * n2 + SCRATCH) +
-           (NPT > 1 ? (long long)EPB * 12 * n3 : 0LL);
+           (NPT > 1 ? (long long)EPB * 12 * n3 : 0LL) + 3LL * LO * n * 5;
   }
 };
 
@@ -1238,6 +1243,7 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
   double* sFS = sFl + EPB * 6 * n2 * 5;  // Gauss: [EPB][6][FNF][n2] own face states and face metric rows
   double* sScr = sFS + (GL ? 0 : EPB * 6 * FNF * n2);  // Gauss: [warp][lane][5]
   double* sV = SS::NPT > 1 ? sScr + (GL ? 0 : SS::SCRATCH) : sR;  // viscous fluxes [EPB][12][n3]
+  double* sX = sScr + (GL ? 0 : SS::SCRATCH) + (SS::NPT > 1 ? EPB * 12 * n3 : 0);  // [3][LO][n][5] joint-pass line sums
   load_basis_smem<n>(B, sD);
   SBasis<n> Bs{sD};
   const bool pi = B.splitDG == 4;
@@ -1266,6 +1272,11 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
     }
 #pragma unroll
     for (int c = 0; c < 9; ++c) Q[(6 + c) * n3 + x] = d.metr[((size_t)e * 9 + c) * n3 + x];
+    if constexpr (SS::LO > 0) {
+      // nodes of lines left over in the first direction get that direction's sum only at the end
+#pragma unroll
+      for (int v = 0; v < 5; ++v) sA[(es * 5 + v) * n3 + x] = 0.;
+    }
   }
   if (!GL) {
     // this element's face states (U_master/U_slave of its own sides) and face metric rows, in face order
@@ -1303,93 +1314,114 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
   };
   const int lane = threadIdx.x & 31;
   const int seg = lane / n, a = lane - seg * n, segBase = seg * n;
+  // node a of line `line` of direction dir for this lane: its pairs and, on Gauss nodes, the split-Gauss surface
+  // term. carry: added to the previous directions' sums in sA and stored there; else the line's own contribution
+  // is stored into out[a][5]. Lanes of invalid segments compute on line 0 and store nothing.
+  auto line_pass = [&](int dir, int line, bool valid, bool carry, double* out) {
+    const int lineC = valid ? line : 0;  // idle lanes compute on line 0 and store nothing
+    const int es = lineC / n2, lr = lineC - es * n2, c1 = lr % n, c2 = lr / n;
+    const bool store = valid && e0 + es < d.nElems;
+    const int stride = dir == 0 ? 1 : (dir == 1 ? n : n2);
+    const int xline = dir == 0 ? n * (c1 + n * c2) : (dir == 1 ? c1 + n2 * c2 : c1 + n * c2);
+    const int xa = xline + a * stride;
+    const double* Q = sR + es * 15 * n3;
+    const double* Mm = Q + (6 + 3 * dir) * n3;
+    const double ra = Q[xa], ua = Q[n3 + xa], va = Q[2 * n3 + xa], wa = Q[3 * n3 + xa], pa = Q[4 * n3 + xa], ha = Q[5 * n3 + xa];
+    const double ma0 = Mm[xa], ma1 = Mm[n3 + xa], ma2 = Mm[2 * n3 + xa];
+    double acc[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) acc[v] = (carry && dir > 0) ? sA[(es * 5 + v) * n3 + xa] : 0.;
+#pragma unroll
+    for (int dd = 1; dd <= (n - 1) / 2; ++dd) {
+      const int bI = a + dd < n ? a + dd : a + dd - n;
+      const int xb = xline + bI * stride;
+      double G[5];
+      two_point(ra, ua, va, wa, pa, ha, Q[xb], Q[n3 + xb], Q[2 * n3 + xb], Q[3 * n3 + xb], Q[4 * n3 + xb], Q[5 * n3 + xb],
+                ma0 + Mm[xb], ma1 + Mm[n3 + xb], ma2 + Mm[2 * n3 + xb], G);
+      const double o0 = sC[bI * n + a], o1 = sC[n2 + bI * n + a];
+      acc[0] = fma(o0, G[0], acc[0]);
+#pragma unroll
+      for (int v = 1; v < 5; ++v) acc[v] = fma(o1, G[v], acc[v]);
+      {
+        // receive the flux of the pair (a-dd, a) from lane a-dd of this segment
+        const int aS = a - dd >= 0 ? a - dd : a - dd + n;
+        const int src = valid ? segBase + aS : lane;
+        const double r0 = sC[aS * n + a], r1 = sC[n2 + aS * n + a];
+        acc[0] = fma(r0, __shfl_sync(0xffffffffu, G[0], src), acc[0]);
+#pragma unroll
+        for (int v = 1; v < 5; ++v) acc[v] = fma(r1, __shfl_sync(0xffffffffu, G[v], src), acc[v]);
+      }
+    }
+    if (!GL) {
+      const int fo = c1 + n * c2;  // face coordinate of this line on both end faces
+      double* scr = sScr + (threadIdx.x >> 5) * 160;
+      constexpr int ROUNDS = (5 + n - 1) / n;  // components summed per lane
+#pragma unroll
+      for (int side = 0; side < 2; ++side) {
+        const int ls = side == 0 ? (dir == 0 ? XI_MINUS : (dir == 1 ? ETA_MINUS : ZETA_MINUS))
+                                 : (dir == 0 ? XI_PLUS : (dir == 1 ? ETA_PLUS : ZETA_PLUS));
+        const double* F = sFS + (es * 6 + ls - 1) * FNF * n2 + fo;
+        double G[5];
+        two_point(ra, ua, va, wa, pa, ha, F[0], F[n2], F[2 * n2], F[3 * n2], F[4 * n2], F[5 * n2], ma0 + F[6 * n2], ma1 + F[7 * n2],
+                  ma2 + F[8 * n2], G);
+        const double leg = side == 0 ? Bs.Lm(a) : Bs.Lp(a);
+        // -1/2 NormalSign LegHat(a): NormalSign = -1 on the minus, +1 on the plus side
+        const double cs = side == 0 ? 0.5 * Bs.LhM(a) : -0.5 * Bs.LhP(a);
+        // FluxB_sum of the segment: every lane stores Leg(a) G(a); lane a sums components a, a+n, ... over
+        // the segment's n lanes (in lane order); the sums are broadcast back by shuffles
+        __syncwarp();
+#pragma unroll
+        for (int v = 0; v < 5; ++v) scr[lane * 5 + v] = G[v] * leg;
+        __syncwarp();
+        double S[ROUNDS];
+#pragma unroll
+        for (int r = 0; r < ROUNDS; ++r) {
+          const int c = a + r * n;
+          S[r] = 0.;
+          if (seg < SEG && c < 5) {
+            S[r] = scr[segBase * 5 + c];
+#pragma unroll
+            for (int m = 1; m < n; ++m) S[r] += scr[(segBase + m) * 5 + c];
+          }
+        }
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+          const double sum = __shfl_sync(0xffffffffu, S[v / n], valid ? segBase + v % n : lane);
+          acc[v] = fma(cs * (v == 0 ? f0 : f1), sum - G[v], acc[v]);
+        }
+      }
+    }
+    if (store) {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        if (carry) sA[(es * 5 + v) * n3 + xa] = acc[v];
+        else out[a * 5 + v] = acc[v];
+      }
+    }
+  };
 #pragma unroll 1
   for (int dir = 0; dir < 3; ++dir) {
 #pragma unroll 1
-   for (int base = 0; base < SS::LINE_THREADS; base += SS::THREADS) {
-    const int tt = base + threadIdx.x;
-    if (tt < SS::LINE_THREADS) {  // whole warps
-      const int line = (tt >> 5) * SEG + seg;
-      const bool valid = seg < SEG && line < SS::LINES;
-      const int lineC = valid ? line : 0;  // idle lanes compute on line 0 and store nothing
-      const int es = lineC / n2, lr = lineC - es * n2, c1 = lr % n, c2 = lr / n;
-      const bool store = valid && e0 + es < d.nElems;
-      const int stride = dir == 0 ? 1 : (dir == 1 ? n : n2);
-      const int xline = dir == 0 ? n * (c1 + n * c2) : (dir == 1 ? c1 + n2 * c2 : c1 + n * c2);
-      const int xa = xline + a * stride;
-      const double* Q = sR + es * 15 * n3;
-      const double* Mm = Q + (6 + 3 * dir) * n3;
-      const double ra = Q[xa], ua = Q[n3 + xa], va = Q[2 * n3 + xa], wa = Q[3 * n3 + xa], pa = Q[4 * n3 + xa], ha = Q[5 * n3 + xa];
-      const double ma0 = Mm[xa], ma1 = Mm[n3 + xa], ma2 = Mm[2 * n3 + xa];
-      double acc[5];
-#pragma unroll
-      for (int v = 0; v < 5; ++v) acc[v] = (dir == 0) ? 0. : sA[(es * 5 + v) * n3 + xa];
-#pragma unroll
-      for (int dd = 1; dd <= (n - 1) / 2; ++dd) {
-        const int bI = a + dd < n ? a + dd : a + dd - n;
-        const int xb = xline + bI * stride;
-        double G[5];
-        two_point(ra, ua, va, wa, pa, ha, Q[xb], Q[n3 + xb], Q[2 * n3 + xb], Q[3 * n3 + xb], Q[4 * n3 + xb], Q[5 * n3 + xb],
-                  ma0 + Mm[xb], ma1 + Mm[n3 + xb], ma2 + Mm[2 * n3 + xb], G);
-        const double o0 = sC[bI * n + a], o1 = sC[n2 + bI * n + a];
-        acc[0] = fma(o0, G[0], acc[0]);
-#pragma unroll
-        for (int v = 1; v < 5; ++v) acc[v] = fma(o1, G[v], acc[v]);
-        {
-          // receive the flux of the pair (a-dd, a) from lane a-dd of this segment
-          const int aS = a - dd >= 0 ? a - dd : a - dd + n;
-          const int src = valid ? segBase + aS : lane;
-          const double r0 = sC[aS * n + a], r1 = sC[n2 + aS * n + a];
-          acc[0] = fma(r0, __shfl_sync(0xffffffffu, G[0], src), acc[0]);
-#pragma unroll
-          for (int v = 1; v < 5; ++v) acc[v] = fma(r1, __shfl_sync(0xffffffffu, G[v], src), acc[v]);
-        }
-      }
-      if (!GL) {
-        const int fo = c1 + n * c2;  // face coordinate of this line on both end faces
-        double* scr = sScr + (threadIdx.x >> 5) * 160;
-        constexpr int ROUNDS = (5 + n - 1) / n;  // components summed per lane
-#pragma unroll
-        for (int side = 0; side < 2; ++side) {
-          const int ls = side == 0 ? (dir == 0 ? XI_MINUS : (dir == 1 ? ETA_MINUS : ZETA_MINUS))
-                                   : (dir == 0 ? XI_PLUS : (dir == 1 ? ETA_PLUS : ZETA_PLUS));
-          const double* F = sFS + (es * 6 + ls - 1) * FNF * n2 + fo;
-          double G[5];
-          two_point(ra, ua, va, wa, pa, ha, F[0], F[n2], F[2 * n2], F[3 * n2], F[4 * n2], F[5 * n2], ma0 + F[6 * n2], ma1 + F[7 * n2],
-                    ma2 + F[8 * n2], G);
-          const double leg = side == 0 ? Bs.Lm(a) : Bs.Lp(a);
-          // -1/2 NormalSign LegHat(a): NormalSign = -1 on the minus, +1 on the plus side
-          const double cs = side == 0 ? 0.5 * Bs.LhM(a) : -0.5 * Bs.LhP(a);
-          // FluxB_sum of the segment: every lane stores Leg(a) G(a); lane a sums components a, a+n, ... over
-          // the segment's n lanes (in lane order); the sums are broadcast back by shuffles
-          __syncwarp();
-#pragma unroll
-          for (int v = 0; v < 5; ++v) scr[lane * 5 + v] = G[v] * leg;
-          __syncwarp();
-          double S[ROUNDS];
-#pragma unroll
-          for (int r = 0; r < ROUNDS; ++r) {
-            const int c = a + r * n;
-            S[r] = 0.;
-            if (seg < SEG && c < 5) {
-              S[r] = scr[segBase * 5 + c];
-#pragma unroll
-              for (int m = 1; m < n; ++m) S[r] += scr[(segBase + m) * 5 + c];
-            }
-          }
-#pragma unroll
-          for (int v = 0; v < 5; ++v) {
-            const double sum = __shfl_sync(0xffffffffu, S[v / n], valid ? segBase + v % n : lane);
-            acc[v] = fma(cs * (v == 0 ? f0 : f1), sum - G[v], acc[v]);
-          }
-        }
-      }
-      if (store) {
-#pragma unroll
-        for (int v = 0; v < 5; ++v) sA[(es * 5 + v) * n3 + xa] = acc[v];
+    for (int base = 0; base < SS::MAIN_WARPS * 32; base += SS::THREADS) {
+      const int tt = base + threadIdx.x;
+      if (tt < SS::MAIN_WARPS * 32) line_pass(dir, (tt >> 5) * SEG + seg, seg < SEG, true, nullptr);  // whole warps
+    }
+    __syncthreads();
+  }
+  if constexpr (SS::LO > 0) {
+    // the LO lines left over in each direction, the three directions in one pass; their sums are added per node
+    // at the end (sX)
+#pragma unroll 1
+    for (int base = 0; base < SS::LO_WARPS * 32; base += SS::THREADS) {
+      const int tt = base + threadIdx.x;
+      if (tt < SS::LO_WARPS * 32) {
+        const int kk = (tt >> 5) * SEG + seg;
+        const bool valid = seg < SEG && kk < 3 * SS::LO;
+        const int kc = valid ? kk : 0;
+        const int dir = kc / SS::LO;
+        line_pass(dir, SS::MAIN_WARPS * SEG + kc - dir * SS::LO, valid, false, sX + kc * n * 5);
       }
     }
-   }
     __syncthreads();
   }
   if constexpr (n % 2 == 0) {
@@ -1465,6 +1497,20 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
     double ut[5];
 #pragma unroll
     for (int v = 0; v < 5; ++v) ut[v] = sA[(es * 5 + v) * n3 + x];
+    if constexpr (SS::LO > 0) {
+      // contributions of the joint pass: the node's line in each direction, if that line was left over
+      const int lines[3] = {es * n2 + j + n * k, es * n2 + i + n * k, es * n2 + i + n * j};
+      const int pos[3] = {i, j, k};
+#pragma unroll
+      for (int dir = 0; dir < 3; ++dir) {
+        const int l = lines[dir] - SS::MAIN_WARPS * SEG;
+        if (l >= 0) {
+          const double* X = sX + ((dir * SS::LO + l) * n + pos[dir]) * 5;
+#pragma unroll
+          for (int v = 0; v < 5; ++v) ut[v] += X[v];
+        }
+      }
+    }
     const double* V = sV + es * VS * n3;
 #pragma unroll
     for (int l = 0; l < n; ++l) {
