@@ -822,11 +822,13 @@ def run_adjoint(args):
     f.TimeDisc(2)
     f.U = U0
     _, ms_plain = timed(lambda: f.TimeDisc(n_steps))
+    plain_launches = f.launch_count() * n_steps  # per step of the captured loop
     # forward with checkpoints, then the reverse sweep
     f.U = U0
     clocks = ClockSampler(local)
     clocks.start()
     _, ms_fwd = timed(lambda: f.adjoint_forward(n_steps, dt, args.ckpt))
+    fwd_launches = f.launch_count()
     adj_bytes = free0 - torch.cuda.mem_get_info()[0]
     UT = f.U
     KE = kinetic(UT)
@@ -837,6 +839,7 @@ def run_adjoint(args):
         UbarT[..., c_] = UT[..., c_] / rho * wq
     UbarT *= KE - target
     (Ub0, mub), ms_rev = timed(lambda: f.adjoint_reverse(UbarT))
+    rev_launches = f.launch_count()
     clk = clocks.stop()
     L0 = 0.5 * (KE - target) ** 2
     # finite differences of the loss in seeded random directions of (U0, multipliers): the central difference with
@@ -919,7 +922,8 @@ def run_adjoint(args):
             "dot_product_vs_reference_fd_jvp": {"rel_err": dot_err, "fd": "implicit.f90:MatrixVector FD_Order 2, Eps_Method 1, on the oracle"},
             "e2e": {"value": ms_rev / ms_plain, "unit": "reverse time / forward time", "h2d_bytes_per_step": dof * 5 * 8 / n_steps,
                     "d2h_bytes_per_step": (dof * 5 * 8 + f.n_elems * 8) / n_steps},
-            "gpu_launches": None, "clocks": clk}
+            "gpu_launches": rev_launches, "gpu_launches_forward_checkpointed": fwd_launches, "gpu_launches_forward_plain": plain_launches,
+            "clocks": clk}
     print(json.dumps(line), flush=True)
 
 
@@ -967,13 +971,16 @@ def run_adjoint_channel(args):
     f.TimeDisc(2)
     f.U = U0
     _, ms_plain = timed(lambda: f.TimeDisc(n_steps))
+    plain_launches = f.launch_count() * n_steps
     f.U = U0
     clocks = ClockSampler(local)
     clocks.start()
     _, ms_fwd = timed(lambda: f.adjoint_forward(n_steps, dt, args.ckpt))
+    fwd_launches = f.launch_count()
     adj_bytes = free0 - torch.cuda.mem_get_info()[0]
     (J, dJdU), ms_seed = timed(lambda: f.wall_shear(grad=True))
     (Ub0, mub, Fbar), ms_rev = timed(lambda: f.adjoint_reverse(dJdU, force_bar=True))
+    rev_launches = f.launch_count()
     clk = clocks.stop()
     # directional check along one smooth body-force mode with a Richardson-extrapolated central difference
     # of the same fixed-dt solve (approximate: the Roe flux has kinks a difference quotient can straddle)
@@ -1010,7 +1017,8 @@ def run_adjoint_channel(args):
                          "rel_err": abs(ad - fd) / max(abs(fd), 1e-300)},
             "e2e": {"value": ms_rev / ms_plain, "unit": "reverse time / forward time", "h2d_bytes_per_step": dof * 5 * 8 / n_steps,
                     "d2h_bytes_per_step": dof * 6 * 8 / n_steps},
-            "gpu_launches": None, "clocks": clk}
+            "gpu_launches": rev_launches, "gpu_launches_forward_checkpointed": fwd_launches, "gpu_launches_forward_plain": plain_launches,
+            "clocks": clk}
     print(json.dumps(line), flush=True)
 
 
