@@ -36,6 +36,8 @@ CASES = {
                                           OverintegrationType=1, NUnder=3), "tgv"),
     "gl7_split_pi_roeef_br2_conscutoff": (dict(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roeentropyfix", Lifting="br2",
                                                OverintegrationType=2, NUnder=4), "tgv"),
+    "gauss3_split_pi_roeef_br1_conscutoff": (dict(N=3, NodeType="gauss", SplitDG="pi", Riemann="roeentropyfix", Lifting="br1",
+                                                  OverintegrationType=2, NUnder=2), "tgv"),
     # split form on Gauss nodes (entropy-variable prolongation, split-Gauss surface term): the discretisation of the
     # reference's tgv/splitGauss regression at N=5, and SD at N=3 with BR2
     "gauss5_split_pi_roeef_br1": (dict(N=5, NodeType="gauss", SplitDG="pi", Riemann="roeentropyfix", Lifting="br1"), "tgv"),
