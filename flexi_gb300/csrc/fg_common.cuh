@@ -40,6 +40,13 @@ struct Basis {
   double kappaFac, sKappaP1;
   double logEntC, kappa_kappaM1;  // ln((kappa-1)^(1/(kappa-1))), kappa/(kappa-1): eos.f90:EntropyToCons
   double riemannPhi;              // RiemannPhiFactor of RoeEntropyGShockFix
+  // even-odd form of D (eoD) and D_Hat (eoDh), row a = node a of a line, 8 columns: for a < n/2 the
+  // coefficients 1/2 (M(a,l) + M(a,N-l)) (l < n/2) on the sums s_l = u_l + u_{N-l}; for a past the middle
+  // 1/2 (M(N-a,l) - M(N-a,N-l)) on the differences d_l = u_l - u_{N-l}; for the middle node of odd n M(m,l) on d_l;
+  // column n/2: M(a,m) (odd n, a < n/2), column n/2+1: the sign (+1, -1, 0 middle) that combines a lane's sum
+  // with its mirror lane's (eo_line_derivative)
+  double eoD[FG_MAXN * 8];
+  double eoDh[FG_MAXN * 8];
 };
 
 // Device arrays of one solver handle (all sizes in units of doubles / ints).

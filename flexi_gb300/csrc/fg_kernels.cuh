@@ -76,6 +76,96 @@ template <int n> struct SBasis {
   __device__ double LhP(int l) const { return s[3 * n * n + 3 * n + l]; }
 };
 
+// Line sweeps in the even-odd form: lines of n nodes are held one node per lane, SEG = 32/n lines to a warp
+// (lane a of segment seg = node a); for lines of 6 nodes and more this takes fewer FP64 instructions than
+// n FMAs per node
+template <int n> struct EOShape {
+  static constexpr bool ON = n >= 6;    // lifting: three direction sweeps per variable, no sum across directions
+  static constexpr bool VOL = n >= 8;   // volume kernels: the three directions' results are summed per node
+                                        // afterwards (one FP64 add each), which offsets the gain below n = 8
+  static constexpr int SEG = 32 / n;
+};
+// this lane's row of an even-odd table (Basis::eoD, or eoDh when DHAT) into registers
+template <int n, bool DHAT>
+__device__ __forceinline__ void eo_row(const Basis& B, double* eo) {
+  const int lane = threadIdx.x & 31, a = lane - n * (lane / n);
+#pragma unroll
+  for (int c = 0; c < 8; ++c) eo[c] = DHAT ? B.eoDh[a * 8 + c] : B.eoD[a * 8 + c];
+}
+
+// derivative along a line held one node per lane (lane a = node a of the segment starting at lane segBase) with a
+// centro-antisymmetric matrix M (M(N-i,N-l) = -M(i,l): D and D_Hat on symmetric nodes), by its even-odd form: with
+// s_l = u_l + u_{N-l}, d_l = u_l - u_{N-l} (l < n/2) and the middle node m of odd n,
+//   du_i + du_{N-i} = sum_l (M(i,l) - M(i,N-l)) d_l,   du_i - du_{N-i} = sum_l (M(i,l) + M(i,N-l)) s_l + 2 M(i,m) u_m,
+// du_m = sum_l M(m,l) d_l: n/2 + 2 FP64 operations per output (+1 for odd n) instead of n. eo: this lane's row of the
+// basis table (Basis::eoD / eoDh); every lane of the warp takes part (lanes outside a segment pass their own values).
+template <int n, int NV>
+__device__ __forceinline__ void eo_line_derivative(const double* eo, int a, int segBase, const double* u, double* du) {
+  constexpr int N = n - 1, h = n / 2, m = N / 2;
+  const int lane = threadIdx.x & 31;
+  const bool inSeg = a < n && segBase + n <= 32;
+  const int mirror = inSeg ? segBase + N - a : lane;
+  const double sgnA = a < h ? 1.0 : -1.0;
+  double sd[NV], acc[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) sd[v] = fma(sgnA, u[v], __shfl_sync(0xffffffffu, u[v], mirror));  // s_a or d_{N-a}
+#pragma unroll
+  for (int c = 0; c < h; ++c) {
+    const int src = inSeg ? segBase + (a < h ? c : N - c) : lane;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      const double x = __shfl_sync(0xffffffffu, sd[v], src);
+      acc[v] = c == 0 ? eo[0] * x : fma(eo[c], x, acc[v]);
+    }
+  }
+  if constexpr (n % 2 == 1) {
+    const int srcM = inSeg ? segBase + m : lane;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) acc[v] = fma(eo[h], __shfl_sync(0xffffffffu, u[v], srcM), acc[v]);
+  }
+#pragma unroll
+  for (int v = 0; v < NV; ++v) du[v] = fma(eo[h + 1], __shfl_sync(0xffffffffu, acc[v], mirror), acc[v]);
+}
+
+
+// even-odd sweeps of NV components of a [EPB][*][n3] shared array along each direction: input component
+// inC0 + inDirStep*dir + v (v < NV) differentiated along direction dir with a row of Basis::eoD or eoDh into
+// output component outC0 + 4*dir + v (in place when both name the same entries: each line and component belongs to
+// one work item, and a warp reads its lines before it writes them). The lines of all three directions run in one
+// flat loop of whole warps. Ends with a barrier.
+// (eo: the row of the table for this lane's node a = (lane % 32) - n * ((lane % 32) / n), loaded by the caller)
+template <int n, int NV, int E = 0>
+__device__ __forceinline__ void eo_sweep_all(const double* eo, const double* in, int inStride, int inC0, int inDirStep, double* out,
+                                             int outStride, int outC0, int e0, int nElems) {
+  constexpr int n2 = n * n, n3 = n2 * n, EPB = Shape<n, E>::EPB, SEG = EOShape<n>::SEG;
+  constexpr int LINES = EPB * n2, L3 = 3 * LINES, W = (L3 + SEG - 1) / SEG;
+  const int lane = threadIdx.x & 31, seg = lane / n, a = lane - seg * n, segBase = seg * n;
+  for (int base = 0; base < W * 32; base += blockDim.x) {
+    const int tt = base + threadIdx.x;
+    if (tt < W * 32) {  // whole warps
+      const int k = (tt >> 5) * SEG + seg;
+      const bool valid = seg < SEG && k < L3;
+      const int kc = valid ? k : 0;
+      const int dir = kc / LINES, line = kc - dir * LINES;
+      const int es = line / n2, lr = line - es * n2, c1 = lr % n, c2 = lr / n;
+      const int stride = dir == 0 ? 1 : (dir == 1 ? n : n2);
+      const int xline = dir == 0 ? n * (c1 + n * c2) : (dir == 1 ? c1 + n2 * c2 : c1 + n * c2);
+      const int x = xline + a * stride;
+      const double* I = in + ((size_t)es * inStride + inC0 + inDirStep * dir) * n3 + x;
+      double u[NV], du[NV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) u[v] = I[v * n3];
+      eo_line_derivative<n, NV>(eo, a, segBase, u, du);
+      if (valid && e0 + es < nElems) {
+        double* O = out + ((size_t)es * outStride + outC0 + 4 * dir) * n3 + x;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) O[v * n3] = du[v];
+      }
+    }
+  }
+  __syncthreads();
+}
+
 // =====================================================================================================
 // k_prep: eos.f90:ConsToPrim (volume), prolongtoface.t90:ProlongToFace, equation.f90:GetPrimitiveStateSurface.
 // Split form on Gauss nodes (PP_EntropyVars): the entropy variables are prolonged instead of U and turned
@@ -338,6 +428,14 @@ __global__ void __launch_bounds__(Shape<n, E>::THREADS, (n == 8 && GL ? 2 : 1)) 
     }
   }
   __syncthreads();
+  constexpr bool EO = EOShape<n>::ON && !CONS;
+  if constexpr (EO) {
+    // reference derivatives of the four lifting variables along each direction, line by line in the even-odd
+    // form, into sG[es][4 dir + v]
+    double eo[8];
+    eo_row<n, false>(B, eo);
+    eo_sweep_all<n, 4, E>(eo, sL, 4, 0, 0, sG, 12, 0, e0, d.nElems);
+  }
   // volume gradient: d/dxi via D_T sweeps, contravariant -> Cartesian with the metrics times sJ
   for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
     const int es = t / n3, x = t - es * n3, e = e0 + es;
@@ -371,16 +469,25 @@ __global__ void __launch_bounds__(Shape<n, E>::THREADS, (n == 8 && GL ? 2 : 1)) 
       for (int c = 0; c < 12; ++c) g[c] *= sj;
     } else {
       double gx[4], ge[4], gz[4];
-#pragma unroll
-      for (int v = 0; v < 4; ++v) { gx[v] = 0.; ge[v] = 0.; gz[v] = 0.; }
-#pragma unroll
-      for (int l = 0; l < n; ++l) {
-        const double dxi = Bs.DT(l, i), deta = Bs.DT(l, j), dzeta = Bs.DT(l, k);
+      if constexpr (EO) {
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
-          gx[v] = fma(dxi, L[v * n3 + l + n * (j + n * k)], gx[v]);
-          ge[v] = fma(deta, L[v * n3 + i + n * (l + n * k)], ge[v]);
-          gz[v] = fma(dzeta, L[v * n3 + i + n * (j + n * l)], gz[v]);
+          gx[v] = sG[(es * 12 + v) * n3 + x];
+          ge[v] = sG[(es * 12 + 4 + v) * n3 + x];
+          gz[v] = sG[(es * 12 + 8 + v) * n3 + x];
+        }
+      } else {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) { gx[v] = 0.; ge[v] = 0.; gz[v] = 0.; }
+#pragma unroll
+        for (int l = 0; l < n; ++l) {
+          const double dxi = Bs.DT(l, i), deta = Bs.DT(l, j), dzeta = Bs.DT(l, k);
+#pragma unroll
+          for (int v = 0; v < 4; ++v) {
+            gx[v] = fma(dxi, L[v * n3 + l + n * (j + n * k)], gx[v]);
+            ge[v] = fma(deta, L[v * n3 + i + n * (l + n * k)], ge[v]);
+            gz[v] = fma(dzeta, L[v * n3 + i + n * (j + n * l)], gz[v]);
+          }
         }
       }
       double mJ[9];
@@ -1169,6 +1276,14 @@ __global__ void __launch_bounds__(Shape<n>::THREADS, (n == 8 ? 2 : 1)) k_vol_spl
     }
   }
   __syncthreads();
+  constexpr bool EO = EOShape<n>::VOL;
+  if constexpr (EO) {
+    // D_Hat sweeps of the viscous fluxes in the even-odd form, in place: component 4 dir + v becomes its
+    // contribution to Ut
+    double eo[8];
+    eo_row<n, true>(B, eo);
+    eo_sweep_all<n, 4>(eo, sR, 15, 0, 4, sR, 15, 0, e0, d.nElems);
+  }
   for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
     const int es = t / n3, x = t - es * n3, e = e0 + es;
     if (e >= d.nElems) continue;
@@ -1177,15 +1292,20 @@ __global__ void __launch_bounds__(Shape<n>::THREADS, (n == 8 ? 2 : 1)) k_vol_spl
 #pragma unroll
     for (int v = 0; v < 5; ++v) ut[v] = sA[(es * 5 + v) * n3 + x];
     const double* V = sR + es * 15 * n3;
+    if constexpr (EO) {
 #pragma unroll
-    for (int l = 0; l < n; ++l) {
-      const double ci = Bs.DhT(l, i), cj = Bs.DhT(l, j), ck = Bs.DhT(l, k);
-      const int xi = l + n * (j + n * k), xj = i + n * (l + n * k), xk = i + n * (j + n * l);
+      for (int v = 0; v < 4; ++v) ut[1 + v] += (V[v * n3 + x] + V[(4 + v) * n3 + x]) + V[(8 + v) * n3 + x];
+    } else {
 #pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        ut[1 + v] = fma(ci, V[v * n3 + xi], ut[1 + v]);
-        ut[1 + v] = fma(cj, V[(4 + v) * n3 + xj], ut[1 + v]);
-        ut[1 + v] = fma(ck, V[(8 + v) * n3 + xk], ut[1 + v]);
+      for (int l = 0; l < n; ++l) {
+        const double ci = Bs.DhT(l, i), cj = Bs.DhT(l, j), ck = Bs.DhT(l, k);
+        const int xi = l + n * (j + n * k), xj = i + n * (l + n * k), xk = i + n * (j + n * l);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          ut[1 + v] = fma(ci, V[v * n3 + xi], ut[1 + v]);
+          ut[1 + v] = fma(cj, V[(4 + v) * n3 + xj], ut[1 + v]);
+          ut[1 + v] = fma(ck, V[(8 + v) * n3 + xk], ut[1 + v]);
+        }
       }
     }
     finish_node<n, true, false>(d, Bs, st, sFl, es, e, x, ut);
@@ -1490,6 +1610,14 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
     }
   }
   __syncthreads();
+  constexpr bool EO = EOShape<n>::VOL;
+  if constexpr (EO) {
+    // D_Hat sweeps of the viscous fluxes in the even-odd form, in place (component 4 dir + v becomes its
+    // contribution to Ut)
+    double eo[8];
+    eo_row<n, true>(B, eo);
+    eo_sweep_all<n, 4>(eo, sV, VS, 0, 4, sV, VS, 0, e0, d.nElems);
+  }
   for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
     const int es = t / n3, x = t - es * n3, e = e0 + es;
     if (e >= d.nElems) continue;
@@ -1512,15 +1640,20 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
       }
     }
     const double* V = sV + es * VS * n3;
+    if constexpr (EO) {
 #pragma unroll
-    for (int l = 0; l < n; ++l) {
-      const double ci = Bs.DhT(l, i), cj = Bs.DhT(l, j), ck = Bs.DhT(l, k);
-      const int xi = l + n * (j + n * k), xj = i + n * (l + n * k), xk = i + n * (j + n * l);
+      for (int v = 0; v < 4; ++v) ut[1 + v] += (V[v * n3 + x] + V[(4 + v) * n3 + x]) + V[(8 + v) * n3 + x];
+    } else {
 #pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        ut[1 + v] = fma(ci, V[v * n3 + xi], ut[1 + v]);
-        ut[1 + v] = fma(cj, V[(4 + v) * n3 + xj], ut[1 + v]);
-        ut[1 + v] = fma(ck, V[(8 + v) * n3 + xk], ut[1 + v]);
+      for (int l = 0; l < n; ++l) {
+        const double ci = Bs.DhT(l, i), cj = Bs.DhT(l, j), ck = Bs.DhT(l, k);
+        const int xi = l + n * (j + n * k), xj = i + n * (l + n * k), xk = i + n * (j + n * l);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          ut[1 + v] = fma(ci, V[v * n3 + xi], ut[1 + v]);
+          ut[1 + v] = fma(cj, V[(4 + v) * n3 + xj], ut[1 + v]);
+          ut[1 + v] = fma(ck, V[(8 + v) * n3 + xk], ut[1 + v]);
+        }
       }
     }
     finish_node<n, GL, !GL>(d, Bs, st, sFl, es, e, x, ut);
