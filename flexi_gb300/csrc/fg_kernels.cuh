@@ -130,13 +130,13 @@ __device__ __forceinline__ void eo_line_derivative(const double* eo, int a, int 
 
 // even-odd sweeps of NV components of a [EPB][*][n3] shared array along each direction: input component
 // inC0 + inDirStep*dir + v (v < NV) differentiated along direction dir with a row of Basis::eoD or eoDh into
-// output component outC0 + 4*dir + v (in place when both name the same entries: each line and component belongs to
+// output component outC0 + outDirStep*dir + v (in place when both name the same entries: each line and component belongs to
 // one work item, and a warp reads its lines before it writes them). The lines of all three directions run in one
 // flat loop of whole warps. Ends with a barrier.
 // (eo: the row of the table for this lane's node a = (lane % 32) - n * ((lane % 32) / n), loaded by the caller)
 template <int n, int NV, int E = 0>
 __device__ __forceinline__ void eo_sweep_all(const double* eo, const double* in, int inStride, int inC0, int inDirStep, double* out,
-                                             int outStride, int outC0, int e0, int nElems) {
+                                             int outStride, int outC0, int outDirStep, int e0, int nElems) {
   constexpr int n2 = n * n, n3 = n2 * n, EPB = Shape<n, E>::EPB, SEG = EOShape<n>::SEG;
   constexpr int LINES = EPB * n2, L3 = 3 * LINES, W = (L3 + SEG - 1) / SEG;
   const int lane = threadIdx.x & 31, seg = lane / n, a = lane - seg * n, segBase = seg * n;
@@ -157,7 +157,7 @@ __device__ __forceinline__ void eo_sweep_all(const double* eo, const double* in,
       for (int v = 0; v < NV; ++v) u[v] = I[v * n3];
       eo_line_derivative<n, NV>(eo, a, segBase, u, du);
       if (valid && e0 + es < nElems) {
-        double* O = out + ((size_t)es * outStride + outC0 + 4 * dir) * n3 + x;
+        double* O = out + ((size_t)es * outStride + outC0 + outDirStep * dir) * n3 + x;
 #pragma unroll
         for (int v = 0; v < NV; ++v) O[v * n3] = du[v];
       }
@@ -434,7 +434,7 @@ __global__ void __launch_bounds__(Shape<n, E>::THREADS, (n == 8 && GL ? 2 : 1)) 
     // form, into sG[es][4 dir + v]
     double eo[8];
     eo_row<n, false>(B, eo);
-    eo_sweep_all<n, 4, E>(eo, sL, 4, 0, 0, sG, 12, 0, e0, d.nElems);
+    eo_sweep_all<n, 4, E>(eo, sL, 4, 0, 0, sG, 12, 0, 4, e0, d.nElems);
   }
   // volume gradient: d/dxi via D_T sweeps, contravariant -> Cartesian with the metrics times sJ
   for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
@@ -1282,7 +1282,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS, (n == 8 ? 2 : 1)) k_vol_spl
     // contribution to Ut
     double eo[8];
     eo_row<n, true>(B, eo);
-    eo_sweep_all<n, 4>(eo, sR, 15, 0, 4, sR, 15, 0, e0, d.nElems);
+    eo_sweep_all<n, 4>(eo, sR, 15, 0, 4, sR, 15, 0, 4, e0, d.nElems);
   }
   for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
     const int es = t / n3, x = t - es * n3, e = e0 + es;
@@ -1437,6 +1437,13 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
   // node a of line `line` of direction dir for this lane: its pairs and, on Gauss nodes, the split-Gauss surface
   // term. carry: added to the previous directions' sums in sA and stored there; else the line's own contribution
   // is stored into out[a][5]. Lanes of invalid segments compute on line 0 and store nothing.
+  // Gauss: this lane's weights of the split-Gauss surface term, -1/2 NormalSign LegHat(a) times the density factor
+  // and the others' (minus side, plus side), formed once
+  double csW[4] = {0., 0., 0., 0.};
+  if (!GL) {
+    const double hM = 0.5 * Bs.LhM(a), hP = -0.5 * Bs.LhP(a);
+    csW[0] = hM * f0; csW[1] = hM * f1; csW[2] = hP * f0; csW[3] = hP * f1;
+  }
   auto line_pass = [&](int dir, int line, bool valid, bool carry, double* out) {
     const int lineC = valid ? line : 0;  // idle lanes compute on line 0 and store nothing
     const int es = lineC / n2, lr = lineC - es * n2, c1 = lr % n, c2 = lr / n;
@@ -1486,7 +1493,7 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
                   ma2 + F[8 * n2], G);
         const double leg = side == 0 ? Bs.Lm(a) : Bs.Lp(a);
         // -1/2 NormalSign LegHat(a): NormalSign = -1 on the minus, +1 on the plus side
-        const double cs = side == 0 ? 0.5 * Bs.LhM(a) : -0.5 * Bs.LhP(a);
+        const double cw0 = csW[2 * side], cw1 = csW[2 * side + 1];
         // FluxB_sum of the segment: every lane stores Leg(a) G(a); lane a sums components a, a+n, ... over
         // the segment's n lanes (in lane order); the sums are broadcast back by shuffles
         __syncwarp();
@@ -1507,7 +1514,7 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
 #pragma unroll
         for (int v = 0; v < 5; ++v) {
           const double sum = __shfl_sync(0xffffffffu, S[v / n], valid ? segBase + v % n : lane);
-          acc[v] = fma(cs * (v == 0 ? f0 : f1), sum - G[v], acc[v]);
+          acc[v] = fma(v == 0 ? cw0 : cw1, sum - G[v], acc[v]);
         }
       }
     }
@@ -1616,7 +1623,7 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
     // contribution to Ut)
     double eo[8];
     eo_row<n, true>(B, eo);
-    eo_sweep_all<n, 4>(eo, sV, VS, 0, 4, sV, VS, 0, e0, d.nElems);
+    eo_sweep_all<n, 4>(eo, sV, VS, 0, 4, sV, VS, 0, 4, e0, d.nElems);
   }
   for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
     const int es = t / n3, x = t - es * n3, e = e0 + es;
