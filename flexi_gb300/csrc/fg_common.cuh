@@ -49,6 +49,30 @@ struct Basis {
   double eoDh[FG_MAXN * 8];
 };
 
+// Basis::eoD and eoDh from D_T and Dhat_T (both must be filled): D(i,l) = D_T[l*n+i], D_Hat(i,l) = Dhat_T[l*n+i].
+inline void fill_even_odd(Basis& B) {
+  const int n = B.n, N = n - 1, h = n / 2, m = N / 2;
+  auto fill = [&](double* T, const double* MT) {
+    auto M = [&](int i, int l) { return MT[l * n + i]; };
+    for (int a = 0; a < n; ++a) {
+      double* r = T + a * 8;
+      for (int c = 0; c < 8; ++c) r[c] = 0.;
+      if (a < h) {
+        for (int c = 0; c < h; ++c) r[c] = 0.5 * (M(a, c) + M(a, N - c));
+        r[h] = (n % 2) ? M(a, m) : 0.;
+        r[h + 1] = 1.;
+      } else if (n % 2 && a == m) {
+        for (int c = 0; c < h; ++c) r[c] = M(m, c);
+      } else {
+        for (int c = 0; c < h; ++c) r[c] = 0.5 * (M(N - a, c) - M(N - a, N - c));
+        r[h + 1] = -1.;
+      }
+    }
+  };
+  fill(B.eoD, B.D_T);
+  fill(B.eoDh, B.Dhat_T);
+}
+
 // Device arrays of one solver handle (all sizes in units of doubles / ints).
 struct Dev {
   int nElems, nSides, nBCSides, nInst;

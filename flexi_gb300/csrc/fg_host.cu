@@ -596,29 +596,8 @@ void init_basis(fg_handle* h) {
       B.DVS[l * n + i] = v;
     }
   for (int i = 0; i < n; ++i) { B.Lm[i] = Lm[i]; B.Lp[i] = Lp[i]; B.LhM[i] = Lm[i] / w[i]; B.LhP[i] = Lp[i] / w[i]; }
-  // even-odd tables of D(i,l) and D_Hat(i,l) = -w_i^-1 D(l,i) w_l; both are centro-antisymmetric on symmetric nodes,
-  // M(N-i,N-l) = -M(i,l)
-  {
-    const int h = n / 2, m = N / 2;
-    auto fill = [&](double* T, auto M) {
-      for (int a = 0; a < n; ++a) {
-        double* r = T + a * 8;
-        for (int c = 0; c < 8; ++c) r[c] = 0.;
-        if (a < h) {
-          for (int c = 0; c < h; ++c) r[c] = 0.5 * (M(a, c) + M(a, N - c));
-          r[h] = (n % 2) ? M(a, m) : 0.;
-          r[h + 1] = 1.;
-        } else if (n % 2 && a == m) {
-          for (int c = 0; c < h; ++c) r[c] = M(m, c);
-        } else {
-          for (int c = 0; c < h; ++c) r[c] = 0.5 * (M(N - a, c) - M(N - a, N - c));
-          r[h + 1] = -1.;
-        }
-      }
-    };
-    fill(B.eoD, [&](int i, int l) { return D(i, l); });
-    fill(B.eoDh, [&](int i, int l) { return -(1. / w[i]) * D(l, i) * w[l]; });
-  }
+  // even-odd tables of D and D_Hat; both are centro-antisymmetric on symmetric nodes, M(N-i,N-l) = -M(i,l)
+  fill_even_odd(B);
   B.kappa = c.kappa; B.kappaM1 = c.kappa - 1.; B.sKappaM1 = 1. / (c.kappa - 1.);
   B.Rgas = c.R; B.sR = 1. / c.R;
   const double cp = c.R * c.kappa / (c.kappa - 1.);

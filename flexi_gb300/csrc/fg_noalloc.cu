@@ -207,6 +207,7 @@ void stack_basis(const fg_config& c, Basis& B) {
       B.DVS[l * n + i] = v;
     }
   for (int i = 0; i < n; ++i) { B.Lm[i] = Lm[i]; B.Lp[i] = Lp[i]; B.LhM[i] = Lm[i] / w[i]; B.LhP[i] = Lp[i] / w[i]; }
+  fill_even_odd(B);
   B.kappa = c.kappa; B.kappaM1 = c.kappa - 1.; B.sKappaM1 = 1. / (c.kappa - 1.);
   B.Rgas = c.R; B.sR = 1. / c.R;
   const double cp = c.R * c.kappa / (c.kappa - 1.);
@@ -214,6 +215,9 @@ void stack_basis(const fg_config& c, Basis& B) {
   B.etaBR2 = c.etaBR2; B.etaBR2_wall = (c.etaBR2_wall == -1.) ? c.etaBR2 : c.etaBR2_wall;
   B.kappaFac = 2. * c.kappa / (c.kappa - 1.);
   B.sKappaP1 = 1. / (c.kappa + 1.);
+  B.logEntC = std::log(c.kappa - 1.) / (c.kappa - 1.);
+  B.kappa_kappaM1 = c.kappa / (c.kappa - 1.);
+  B.riemannPhi = c.RiemannPhiFactor;
 }
 
 // kernel shared-memory limits of every kernel set, once per device (they are per-device settings)
