@@ -28,7 +28,7 @@ class FgTimeDiscState(ctypes.Structure):
 EXPORTS = ["fg_config_default", "fg_config_from_ini", "fg_create", "fg_destroy", "fg_last_error", "fg_build_mesh", "fg_build_mesh_mortar", "fg_set_mesh", "fg_set_mesh_mortar", "fg_set_face_metrics", "fg_overintegrate_state",
            "fg_get_config", "fg_lserk_table", "fg_set_time", "fg_hopr_sizes", "fg_hopr_read", "fg_write_state", "fg_read_state", "fg_io_last_error",
            "fg_set_instance_mu0", "fg_get_elem_xgp", "fg_get_sizes", "fg_get_mesh_array", "fg_get_side_to_elem", "fg_set_state",
-           "fg_get_state", "fg_state_device_ptr", "fg_time_derivative", "fg_calc_timestep", "fg_get_dt_elem", "fg_timestep_lserkw2", "fg_run",
+           "fg_get_state", "fg_state_device_ptr", "fg_time_derivative", "fg_calc_timestep", "fg_get_dt_elem", "fg_timestep_lserkw2", "fg_run", "fg_run_to_host",
            "fg_get_gradients", "fg_get_stream", "fg_launch_count", "fg_get_timedisc_state", "fg_debug_array", "fg_profile_enable", "fg_profile_read", "fg_probe_fp64", "fg_probe_fp64_pipe", "fg_probe_fp64_tensor", "fg_probe_fp64_lanes",
            "fg_time_derivative_noalloc", "fg_set_elem_mu_scale", "fg_vjp_time_derivative", "fg_adjoint_forward", "fg_adjoint_reverse",
            "fg_set_body_force_field", "fg_wall_shear", "fg_jvp_time_derivative",
@@ -88,6 +88,7 @@ def load(path=None):
     L.fg_get_dt_elem.argtypes = [P, P, P]
     L.fg_timestep_lserkw2.argtypes = [P, ctypes.POINTER(D), D]
     L.fg_run.argtypes = [P, I, P]
+    L.fg_run_to_host.argtypes = [P, I, P, P]
     L.fg_get_timedisc_state.argtypes = [P, I, P]
     L.fg_probe_fp64_pipe.argtypes = [P]
     L.fg_probe_fp64_tensor.argtypes = [P]

@@ -1,6 +1,6 @@
 // flexi_gb300 -- device data layout and point-wise physics of the DGSEM Navier-Stokes operator.
 //
-// Everything is FP64. GB300's FP64 pipe (measured 0.50 T instr/s, 1.0 TFLOP/s FMA) is ~70x slower than
+// Everything is FP64. GB300's FP64 pipe (a pure DFMA stream attains 0.53 T instr/s, 1.06 TFLOP/s) is ~70x slower than
 // its FP32 pipe and ~30x below what this operator needs to be HBM-bound, so the kernels are organised to
 // minimise FP64 instructions: reciprocals are formed once and reused, constant factors are folded, face
 // values are computed once per side and read by both neighbours, and integer/shared-memory work (which
@@ -123,6 +123,9 @@ struct Dev {
   int* err;        // [1] sticky error word
   double* dtElem;  // [2][nElems] convective and viscous element time-step limits of the last CALCTIMESTEP
   const int* dtSkip;  // [nInst] nonzero: the instance needs no CALCTIMESTEP in this step (null: every instance does)
+  // element range of one volume-kernel launch: elements volBegin .. volBegin + volCount - 1 (volCount 0: all);
+  // volBegin is a multiple of the kernel's elements per CTA
+  int volBegin, volCount;
 };
 
 // Overintegration (overintegration.f90): type 1 the modal cut-off filter F = Vdm_Leg diag(1..1,0..0) sVdm_Leg

@@ -429,6 +429,9 @@ struct DevBuf {
   size_t bytes = 0;
 };
 
+// element chunks of the last stage's volume kernel in fg_run_to_host
+constexpr int FG_OUT_CHUNKS = 6;
+
 struct fg_handle {
   fg_config cfg{};
   Basis B{};
@@ -461,6 +464,11 @@ struct fg_handle {
   // mortar interfaces: operators and the device copy of the mortar table (Dev::nMortars > 0)
   MortarDev mort{};
   cudaGraphExec_t graph = nullptr;
+  long long launchesPerStep = 0;  // kernel launches of one captured TimeDisc step
+  // fg_run_to_host: the stream of the state download that overlaps the last stage, and its events
+  cudaStream_t stOut = nullptr;
+  cudaEvent_t evOut[FG_OUT_CHUNKS] = {};
+  cudaEvent_t evOutDone = nullptr;
   long long launches = 0;
   std::string err;
   std::vector<double> instMu0;
@@ -886,8 +894,8 @@ struct ProfScope {
   }
 };
 
-// state sequence of one right-hand side evaluation plus the RK register update
-void launch_rhs_dev(fg_handle* h, const Dev& d, int mode, double rkA, double rkB) {
+// state sequence of one right-hand side evaluation up to the volume kernel
+void launch_rhs_front(fg_handle* h, const Dev& d) {
   const bool mortars = d.nMortars > 0;
   { ProfScope p(h, 0); h->K.prep(d, h->B, h->st); }
   if (mortars) { ProfScope p(h, 5); h->K.mortar_pre(d, h->B, h->mort, h->st); h->launches += 1; }
@@ -898,6 +906,10 @@ void launch_rhs_dev(fg_handle* h, const Dev& d, int mode, double rkA, double rkB
   }
   if (d.nFluxSides > 0) { ProfScope p(h, 2); h->K.flux_block(d, h->B, h->K.fluxBlock, h->st); }
   if (mortars) { ProfScope p(h, 5); h->K.mortar_face(d, h->B, h->mort, h->st); h->launches += 1; }
+}
+// state sequence of one right-hand side evaluation plus the RK register update
+void launch_rhs_dev(fg_handle* h, const Dev& d, int mode, double rkA, double rkB) {
+  launch_rhs_front(h, d);
   {
     ProfScope p(h, 3);
     // with overintegration the volume kernel writes J u_t and k_overint filters it and updates the registers
@@ -1239,6 +1251,10 @@ int fg_create(const fg_config* cfg, fg_handle** out) {
 int fg_destroy(fg_handle* h) {
   if (!h) return FG_OK;
   free_device(h);
+  for (auto& e : h->evOut)
+    if (e) cudaEventDestroy(e);
+  if (h->evOutDone) cudaEventDestroy(h->evOutDone);
+  if (h->stOut) cudaStreamDestroy(h->stOut);
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
   return FG_OK;
@@ -1412,15 +1428,19 @@ static void fortran_to_dev(fg_handle* h, const double* f, double* d, int nv) {
   }
 }
 // device layout [e][nvDev][n3], variables v0 .. v0+nv-1 -> Fortran layout (nv, n, n, n, nElems) in device memory
-static void dev_to_fortran(fg_handle* h, const double* d, double* f, int nvDev, int v0, int nv) {
+// nElems elements (all: -1) from the device layout at d to the Fortran layout at f, on stream st (null: the handle's)
+static void dev_to_fortran(fg_handle* h, const double* d, double* f, int nvDev, int v0, int nv, int nElems = -1, cudaStream_t st = nullptr) {
   const int n3 = h->M.n * h->M.n * h->M.n;
   const size_t bytes = sizeof(double) * nv * n3;
+  if (nElems < 0) nElems = h->M.nElems;
+  if (!st) st = h->st;
+  if (nElems == 0) return;
   if (bytes <= FG_TILE_SMEM_MAX) {
     cudaFuncSetAttribute(k_dev_to_fortran_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    k_dev_to_fortran_tiled<<<(unsigned)h->M.nElems, 256, bytes, h->st>>>(d, f, nvDev, v0, nv, n3);
+    k_dev_to_fortran_tiled<<<(unsigned)nElems, 256, bytes, st>>>(d, f, nvDev, v0, nv, n3);
   } else {
-    const long long total = (long long)h->M.nElems * nv * n3;
-    k_dev_to_fortran<<<(unsigned)((total + 255) / 256), 256, 0, h->st>>>(d, f, nvDev, v0, nv, n3, total);
+    const long long total = (long long)nElems * nv * n3;
+    k_dev_to_fortran<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(d, f, nvDev, v0, nv, n3, total);
   }
 }
 
@@ -2026,6 +2046,68 @@ int fg_timestep_lserkw2(fg_handle* h, double* t, double dt) {
   return FG_OK;
 }
 
+// nSteps replays of the captured TimeDisc step (captured on first use) on the handle's stream; h->launches = launches
+// per step
+static int launch_steps_graph(fg_handle* h, int nSteps) {
+  if (!h->graph) {
+    cudaGraph_t g;
+    const long long before = h->launches;
+    CUDA_TRY(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+    launch_step_setup(h, 0, 0., true);
+    launch_lserk(h);
+    CUDA_TRY(cudaStreamEndCapture(h->st, &g));
+    CUDA_TRY(cudaGraphInstantiate(&h->graph, g, 0));
+    cudaGraphDestroy(g);
+    h->launchesPerStep = h->launches - before;
+  }
+  for (int s = 0; s < nSteps; ++s) CUDA_TRY(cudaGraphLaunch(h->graph, h->st));
+  h->launches = h->launchesPerStep;
+  return 0;
+}
+
+// elements per CTA of the volume kernel in use (chunks of its grid start at multiples of it)
+static int vol_epb(const fg_handle* h) {
+  if (h->cfg.SplitDG >= 0) return h->Kdef.defEPB;
+  return h->K.vol_weak == h->Kdef.vol_weak ? h->Kdef.defEPB : h->Kdef.altEPB;
+}
+
+// The last LSERK stage of fg_run_to_host. Its volume kernel writes each element's final state, so it runs over
+// element chunks: four of a fifth of the elements, then 15 % and the last 5 %. Once a chunk is done, the second
+// stream converts its elements to the Fortran layout and copies them to Uhost while the later chunks run. The copy of
+// a fifth of the state takes less time than the kernel's work on the next fifth down to about 45 GB/s of link rate
+// (the link runs at 190 GB/s device-to-host when nothing else loads it, but far slower at times), so the copies keep
+// pace and only the last chunk's is left when the kernel ends. Overintegration is excluded by the caller.
+static int launch_last_stage_to_host(fg_handle* h, int mode, double rkA, double rkB, double* Uhost) {
+  static const double ends[FG_OUT_CHUNKS] = {0.2, 0.4, 0.6, 0.8, 0.95, 1.0};
+  const Dev& d = h->d;
+  launch_rhs_front(h, d);
+  h->launches += d.nFluxSides > 0 ? 3 : 2;  // prep, lifting, side kernel
+  const int nE = d.nElems, epb = vol_epb(h);
+  const long long per = 5LL * h->M.n * h->M.n * h->M.n;  // doubles per element
+  int begin = 0;
+  for (int c = 0; c < FG_OUT_CHUNKS && begin < nE; ++c) {
+    // chunk ends at multiples of the elements per CTA (the last at nElems)
+    const long long want = (long long)std::ceil(ends[c] * nE);
+    const int end = c == FG_OUT_CHUNKS - 1 ? nE : (int)std::min<long long>(nE, (want + epb - 1) / epb * epb);
+    if (end <= begin) continue;
+    const int cnt = end - begin;
+    Dev dc = d;
+    dc.volBegin = begin;
+    dc.volCount = cnt;
+    if (h->cfg.SplitDG >= 0) h->K.vol_split(dc, h->B, mode, rkA, rkB, h->st);
+    else h->K.vol_weak(dc, h->B, mode, rkA, rkB, h->st);
+    CUDA_TRY(cudaEventRecord(h->evOut[c], h->st));
+    CUDA_TRY(cudaStreamWaitEvent(h->stOut, h->evOut[c], 0));
+    dev_to_fortran(h, d.U + begin * per, h->dStage + begin * per, 5, 0, 5, cnt, h->stOut);
+    CUDA_TRY(cudaMemcpyAsync(Uhost + begin * per, h->dStage + begin * per, sizeof(double) * cnt * per, cudaMemcpyDeviceToHost, h->stOut));
+    h->launches += 2;
+    begin = end;
+  }
+  CUDA_TRY(cudaEventRecord(h->evOutDone, h->stOut));
+  CUDA_TRY(cudaStreamWaitEvent(h->st, h->evOutDone, 0));
+  return 0;
+}
+
 int fg_run(fg_handle* h, int nSteps, double* t) {
   if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
   if (nSteps < 0) return fail(h, FG_ERR_CONFIG, "nSteps < 0");
@@ -2043,24 +2125,53 @@ int fg_run(fg_handle* h, int nSteps, double* t) {
     if (nSteps > 0) h->launches /= nSteps;
     return FG_OK;
   }
-  if (!h->graph) {
-    cudaGraph_t g;
-    const long long before = h->launches;
-    CUDA_TRY(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
-    launch_step_setup(h, 0, 0., true);
-    launch_lserk(h);
-    CUDA_TRY(cudaStreamEndCapture(h->st, &g));
-    CUDA_TRY(cudaGraphInstantiate(&h->graph, g, 0));
-    cudaGraphDestroy(g);
-    h->launches = h->launches - before;  // launches per step
-  }
+  if (int r = launch_steps_graph(h, nSteps)) return r;
   const long long perStep = h->launches;
-  for (int s = 0; s < nSteps; ++s) CUDA_TRY(cudaGraphLaunch(h->graph, h->st));
   CUDA_TRY(cudaGetLastError());
   if (int r = check_err(h)) return r;
   if (t) CUDA_TRY(cudaMemcpy(t, h->dTime, sizeof(double) * h->d.nInst, cudaMemcpyDeviceToHost));
   h->launches = perStep;
-  (void)perStep;
+  return FG_OK;
+}
+
+int fg_run_to_host(fg_handle* h, int nSteps, double* t, double* U) {
+  if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
+  if (!U) return fail(h, FG_ERR_CONFIG, "fg_run_to_host: null state pointer");
+  if (nSteps < 0) return fail(h, FG_ERR_CONFIG, "nSteps < 0");
+  // per-kernel profiling, and overintegration (whose filter kernel writes U after the volume kernel), take the
+  // plain sequence
+  if (nSteps == 0 || h->profiling || h->ov.type > 0) {
+    if (int r = fg_run(h, nSteps, t)) return r;
+    return fg_get_state(h, U);
+  }
+  if (!h->stOut) {
+    // the highest priority: at each chunk boundary the conversion of the finished chunk gets the SMs before the next
+    // volume chunk (whose CTAs fill the register files while they run)
+    int least = 0, greatest = 0;
+    CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    CUDA_TRY(cudaStreamCreateWithPriority(&h->stOut, cudaStreamNonBlocking, greatest));
+    for (auto& e : h->evOut) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&h->evOutDone, cudaEventDisableTiming));
+  }
+  CUDA_TRY(cudaMemsetAsync(h->d.err, 0, sizeof(int), h->st));
+  k_timedisc_release<<<(h->d.nInst + 127) / 128, 128, 0, h->st>>>(h->td, h->d.nInst);
+  if (int r = launch_steps_graph(h, nSteps - 1)) return r;
+  // the last step as direct launches: the sequence of the graph with the last stage's volume kernel in chunks
+  h->launches = 0;
+  launch_step_setup(h, 0, 0., true);
+  for (int s = 1; s <= h->nStages; ++s) {
+    if (h->d.srcPar) {
+      k_stage_time<<<(h->d.nInst + 127) / 128, 128, 0, h->st>>>(h->d, h->RKc[s]);
+      h->launches += 1;
+    }
+    const int mode = s == 1 ? 1 : 2;
+    const double rkA = s == 1 ? 0. : h->RKA[s];
+    if (s < h->nStages) launch_rhs(h, mode, rkA, h->RKb[s]);
+    else if (int r = launch_last_stage_to_host(h, mode, rkA, h->RKb[s], U)) return r;
+  }
+  CUDA_TRY(cudaGetLastError());
+  if (int r = check_err(h)) return r;
+  if (t) CUDA_TRY(cudaMemcpy(t, h->dTime, sizeof(double) * h->d.nInst, cudaMemcpyDeviceToHost));
   return FG_OK;
 }
 

@@ -10,6 +10,8 @@ template <int n, bool GL>
 struct Inst {
   using S = Shape<n>;
   static int blocks(const Dev& d) { return (d.nElems + S::EPB - 1) / S::EPB; }
+  // CTAs of a volume-kernel launch over Dev::volCount elements from Dev::volBegin (all elements when volCount is 0)
+  static int vol_blocks(const Dev& d, int epb) { return ((d.volCount > 0 ? d.volCount : d.nElems) + epb - 1) / epb; }
   static size_t smem_prep() { return dyn_smem_bytes<n>(Big<n>::prep); }
   // Gauss nodes (lines of up to 8): the lifting keeps the 12 products F_v n_c per face point (the mortar layout, inert
   // without mortar sides): the surface part then costs 2 FMA per gradient component and direction at every node of
@@ -58,7 +60,7 @@ struct Inst {
   template <int E>
   static void vol_weak_E(const Dev& d, const Basis& B, int mode, double rkA, double rkB, cudaStream_t st) {
     using SE = Shape<n, E>;
-    k_vol_weak<n, GL, E><<<(d.nElems + SE::EPB - 1) / SE::EPB, SE::THREADS, smem_weak_E<E>(), st>>>(d, B, Stage{mode, rkA, rkB});
+    k_vol_weak<n, GL, E><<<vol_blocks(d, SE::EPB), SE::THREADS, smem_weak_E<E>(), st>>>(d, B, Stage{mode, rkA, rkB});
   }
   // the Riemann solvers and split fluxes beyond LF/HLLC/Roe/RoeEntropyFix with the weak form, SD or PI
   static bool flux_more(const Basis& B) {
@@ -157,17 +159,17 @@ struct Inst {
     else k_flux<n><<<(unsigned)((pts + 127) / 128), 128, 0, st>>>(d, B);
   }
   static void vol_weak(const Dev& d, const Basis& B, int mode, double rkA, double rkB, cudaStream_t st) {
-    k_vol_weak<n, GL><<<blocks(d), S::THREADS, smem_weak(), st>>>(d, B, Stage{mode, rkA, rkB});
+    k_vol_weak<n, GL><<<vol_blocks(d, S::EPB), S::THREADS, smem_weak(), st>>>(d, B, Stage{mode, rkA, rkB});
   }
   static void vol_split(const Dev& d, const Basis& B, int mode, double rkA, double rkB, cudaStream_t st) {
     const Stage sg{mode, rkA, rkB};
     if (split_more(B)) {
-      if constexpr (SPLIT_POW2) k_vol_split<n, true><<<blocks(d), S::THREADS, smem_split(), st>>>(d, B, sg);
-      else k_vol_split_gen<n, GL, true><<<blocks(d), SplitShape<n>::THREADS, smem_split_gen(), st>>>(d, B, sg);
+      if constexpr (SPLIT_POW2) k_vol_split<n, true><<<vol_blocks(d, S::EPB), S::THREADS, smem_split(), st>>>(d, B, sg);
+      else k_vol_split_gen<n, GL, true><<<vol_blocks(d, S::EPB), SplitShape<n>::THREADS, smem_split_gen(), st>>>(d, B, sg);
       return;
     }
-    if constexpr (SPLIT_POW2) k_vol_split<n><<<blocks(d), S::THREADS, smem_split(), st>>>(d, B, sg);
-    else k_vol_split_gen<n, GL><<<blocks(d), SplitShape<n>::THREADS, smem_split_gen(), st>>>(d, B, sg);
+    if constexpr (SPLIT_POW2) k_vol_split<n><<<vol_blocks(d, S::EPB), S::THREADS, smem_split(), st>>>(d, B, sg);
+    else k_vol_split_gen<n, GL><<<vol_blocks(d, S::EPB), SplitShape<n>::THREADS, smem_split_gen(), st>>>(d, B, sg);
   }
   // mortar interfaces (one CTA of 256 threads per big mortar side)
   static size_t smem_lift_mortar() { return dyn_smem_bytes<n>(Big<n>::liftMortar); }

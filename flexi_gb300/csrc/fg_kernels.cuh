@@ -1011,7 +1011,7 @@ __global__ void __launch_bounds__(Shape<n, E>::THREADS) k_vol_weak(Dev d, Basis 
   double* sFl = sT + EPB * 15 * n3;      // [EPB][6][n2][5]
   load_basis_smem<n>(B, sD);
   SBasis<n> Bs{sD};
-  const int e0 = blockIdx.x * EPB;
+  const int e0 = d.volBegin + blockIdx.x * EPB;
   load_face_fluxes<n, E>(d, sFl, e0);
   for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
     const int es = t / n3, x = t - es * n3, e = e0 + es;
@@ -1126,7 +1126,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS, (n == 8 ? 2 : 1)) k_vol_spl
     if constexpr (GEN) split_factors(skind, f0, f1);
     for (int t = threadIdx.x; t < n2; t += blockDim.x) { sC[t] = B.DVS[t] * f0; sC[n2 + t] = B.DVS[t] * f1; }
   }
-  const int e0 = blockIdx.x * EPB;
+  const int e0 = d.volBegin + blockIdx.x * EPB;
   load_face_fluxes<n>(d, sFl, e0);
   for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
     const int es = t / n3, x = t - es * n3, e = e0 + es;
@@ -1371,7 +1371,7 @@ __global__ void __launch_bounds__(SplitShape<n>::THREADS) k_vol_split_gen(Dev d,
   double f0 = pi ? 0.25 : 0.5, f1 = pi ? 0.125 : 0.5;
   if constexpr (GEN) split_factors(skind, f0, f1);
   for (int t = threadIdx.x; t < n2; t += blockDim.x) { sC[t] = B.DVS[t] * f0; sC[n2 + t] = B.DVS[t] * f1; }
-  const int e0 = blockIdx.x * EPB;
+  const int e0 = d.volBegin + blockIdx.x * EPB;
   load_face_fluxes<n>(d, sFl, e0);
   for (int t = threadIdx.x; t < EPB * n3; t += blockDim.x) {
     const int es = t / n3, x = t - es * n3, e = e0 + es;

@@ -83,23 +83,25 @@ INTERFACE
     INTEGER(C_INT), VALUE :: nMortars; INTEGER(C_INT), OPTIONAL :: Mortars(*)
   END FUNCTION
   INTEGER(C_INT) FUNCTION fg_set_mesh(h, nElems, nSides, nBCSides, SideToElem, ElemToSide, BC, nBCs, BoundaryType, nRefStates, &
-                                      RefStatePrim, Metrics_fTilde, Metrics_gTilde, Metrics_hTilde, sJ, NormVec, TangVec1, TangVec2, &
-                                      SurfElem) BIND(C,NAME='fg_set_mesh')
+                                      RefStatePrim, Metrics_fTilde, Metrics_gTilde, Metrics_hTilde, sJ, NormVec, TangVec1, &
+                                      TangVec2, SurfElem) BIND(C,NAME='fg_set_mesh')
     IMPORT; TYPE(C_PTR), VALUE :: h; INTEGER(C_INT), VALUE :: nElems, nSides, nBCSides
     INTEGER(C_INT) :: SideToElem(*), ElemToSide(*), BC(*)
     INTEGER(C_INT), VALUE :: nBCs; INTEGER(C_INT) :: BoundaryType(*)
     INTEGER(C_INT), VALUE :: nRefStates; REAL(C_DOUBLE) :: RefStatePrim(*)
-    REAL(C_DOUBLE) :: Metrics_fTilde(*), Metrics_gTilde(*), Metrics_hTilde(*), sJ(*), NormVec(*), TangVec1(*), TangVec2(*), SurfElem(*)
+    REAL(C_DOUBLE) :: Metrics_fTilde(*), Metrics_gTilde(*), Metrics_hTilde(*), sJ(*)
+    REAL(C_DOUBLE) :: NormVec(*), TangVec1(*), TangVec2(*), SurfElem(*)
   END FUNCTION
   INTEGER(C_INT) FUNCTION fg_set_mesh_mortar(h, nElems, nSides, nBCSides, SideToElem, ElemToSide, BC, nBCs, BoundaryType, &
-                                             nRefStates, RefStatePrim, Metrics_fTilde, Metrics_gTilde, Metrics_hTilde, sJ, NormVec, &
-                                             TangVec1, TangVec2, SurfElem, nMortars, MortarType, MortarInfo) &
+                                             nRefStates, RefStatePrim, Metrics_fTilde, Metrics_gTilde, Metrics_hTilde, sJ, &
+                                             NormVec, TangVec1, TangVec2, SurfElem, nMortars, MortarType, MortarInfo) &
                                              BIND(C,NAME='fg_set_mesh_mortar')
     IMPORT; TYPE(C_PTR), VALUE :: h; INTEGER(C_INT), VALUE :: nElems, nSides, nBCSides
     INTEGER(C_INT) :: SideToElem(*), ElemToSide(*), BC(*)
     INTEGER(C_INT), VALUE :: nBCs; INTEGER(C_INT) :: BoundaryType(*)
     INTEGER(C_INT), VALUE :: nRefStates; REAL(C_DOUBLE) :: RefStatePrim(*)
-    REAL(C_DOUBLE) :: Metrics_fTilde(*), Metrics_gTilde(*), Metrics_hTilde(*), sJ(*), NormVec(*), TangVec1(*), TangVec2(*), SurfElem(*)
+    REAL(C_DOUBLE) :: Metrics_fTilde(*), Metrics_gTilde(*), Metrics_hTilde(*), sJ(*)
+    REAL(C_DOUBLE) :: NormVec(*), TangVec1(*), TangVec2(*), SurfElem(*)
     INTEGER(C_INT), VALUE :: nMortars; INTEGER(C_INT) :: MortarType(*), MortarInfo(*)
   END FUNCTION
   INTEGER(C_INT) FUNCTION fg_set_face_metrics(h, Ja_Face, Ja_slave) BIND(C,NAME='fg_set_face_metrics')
@@ -170,6 +172,9 @@ INTERFACE
   INTEGER(C_INT) FUNCTION fg_run(h, nSteps, t) BIND(C,NAME='fg_run')
     IMPORT; TYPE(C_PTR), VALUE :: h; INTEGER(C_INT), VALUE :: nSteps; REAL(C_DOUBLE), OPTIONAL :: t(*)
   END FUNCTION
+  INTEGER(C_INT) FUNCTION fg_run_to_host(h, nSteps, t, U) BIND(C,NAME='fg_run_to_host')
+    IMPORT; TYPE(C_PTR), VALUE :: h; INTEGER(C_INT), VALUE :: nSteps; REAL(C_DOUBLE) :: t(*); REAL(C_DOUBLE) :: U(*)
+  END FUNCTION
   INTEGER(C_INT) FUNCTION fg_get_timedisc_state(h, nInst, state) BIND(C,NAME='fg_get_timedisc_state')
     IMPORT; TYPE(C_PTR), VALUE :: h; INTEGER(C_INT), VALUE :: nInst; TYPE(fg_timedisc_state) :: state(*)
   END FUNCTION
@@ -206,7 +211,8 @@ INTERFACE
     INTEGER(C_INT), VALUE :: fdOrder, epsMethod; REAL(C_DOUBLE), VALUE :: scaleps
   END FUNCTION
   INTEGER(C_INT) FUNCTION fg_adjoint_forward(h, nSteps, dt, ckptEvery) BIND(C,NAME='fg_adjoint_forward')
-    IMPORT; TYPE(C_PTR), VALUE :: h; INTEGER(C_INT), VALUE :: nSteps; REAL(C_DOUBLE), VALUE :: dt; INTEGER(C_INT), VALUE :: ckptEvery
+    IMPORT; TYPE(C_PTR), VALUE :: h; INTEGER(C_INT), VALUE :: nSteps; REAL(C_DOUBLE), VALUE :: dt
+    INTEGER(C_INT), VALUE :: ckptEvery
   END FUNCTION
   INTEGER(C_LONG_LONG) FUNCTION fg_adjoint_recomputed_steps(h) BIND(C,NAME='fg_adjoint_recomputed_steps')
     IMPORT; TYPE(C_PTR), VALUE :: h
@@ -255,7 +261,8 @@ PUBLIC :: fg_config_default, fg_config_from_ini, fg_create, fg_destroy, fg_last_
 PUBLIC :: fg_set_mesh, fg_set_mesh_mortar, fg_set_face_metrics, fg_overintegrate_state, fg_lserk_table, fg_get_config
 PUBLIC :: fg_hopr_sizes, fg_hopr_read, fg_write_state, fg_read_state, fg_io_last_error, fg_set_instance_mu0, fg_get_elem_xgp
 PUBLIC :: fg_get_sizes, fg_get_mesh_array, fg_get_side_to_elem, fg_set_state, fg_get_state, fg_state_device_ptr
-PUBLIC :: fg_time_derivative, fg_calc_timestep, fg_get_dt_elem, fg_timestep_lserkw2, fg_run, fg_get_timedisc_state, fg_set_time
+PUBLIC :: fg_time_derivative, fg_calc_timestep, fg_get_dt_elem, fg_timestep_lserkw2, fg_run, fg_run_to_host, fg_get_timedisc_state
+PUBLIC :: fg_set_time
 PUBLIC :: fg_get_gradients, fg_get_stream, fg_launch_count, fg_debug_array, fg_profile_enable, fg_profile_read
 PUBLIC :: fg_set_elem_mu_scale, fg_vjp_time_derivative, fg_jvp_time_derivative, fg_adjoint_forward, fg_adjoint_recomputed_steps
 PUBLIC :: fg_adjoint_reverse, fg_set_body_force_field, fg_wall_shear, fg_autotune, fg_autotune_choice, fg_set_launch_shapes
@@ -267,7 +274,8 @@ PUBLIC :: fg_probe_fp64_pipe, fg_probe_fp64, fg_probe_fp64_tensor, fg_probe_fp64
 TYPE(C_PTR)    :: gpu = C_NULL_PTR   !< the solver handle (one rank, one GPU)
 LOGICAL,PUBLIC :: useGPU = .FALSE.   !< set by InitDG_GPU once the handle holds mesh and state
 
-PUBLIC :: InitDG_GPU, DGTimeDerivative_GPU, TimeStepByLSERKW2_GPU, CalcTimeStep_GPU, TimeDiscSteps_GPU, GetState_GPU
+PUBLIC :: InitDG_GPU, DGTimeDerivative_GPU, TimeStepByLSERKW2_GPU, CalcTimeStep_GPU, TimeDiscSteps_GPU, TimeDiscStepsToHost_GPU
+PUBLIC :: GetState_GPU
 PUBLIC :: FinalizeDG_GPU, GPUErrorMessage
 
 CONTAINS
@@ -438,6 +446,25 @@ iter       = st(1)%iter
 doAnalyze  = st(1)%atAnalyze.NE.0
 doFinalize = st(1)%finished.NE.0
 END SUBROUTINE TimeDiscSteps_GPU
+
+!==================================================================================================================================
+!> TimeDiscSteps_GPU and GetState_GPU in one call: the copy of the state into U overlaps the last stage of the last step
+!==================================================================================================================================
+SUBROUTINE TimeDiscStepsToHost_GPU(nSteps, doAnalyze, doFinalize)
+USE MOD_DG_Vars,       ONLY: U
+USE MOD_TimeDisc_Vars, ONLY: t, dt, iter
+INTEGER,INTENT(IN)      :: nSteps
+LOGICAL,INTENT(OUT)     :: doAnalyze, doFinalize
+TYPE(fg_timedisc_state) :: st(1)
+REAL(C_DOUBLE)          :: tInst(1)
+CALL CheckGPU(fg_run_to_host(gpu, INT(nSteps, C_INT), tInst, U), 'TimeDisc')
+CALL CheckGPU(fg_get_timedisc_state(gpu, 1_C_INT, st), 'TimeDisc state')
+t          = st(1)%t
+dt         = st(1)%dt
+iter       = st(1)%iter
+doAnalyze  = st(1)%atAnalyze.NE.0
+doFinalize = st(1)%finished.NE.0
+END SUBROUTINE TimeDiscStepsToHost_GPU
 
 !==================================================================================================================================
 !> Copies the device state into U (before WriteState / Analyze) and, optionally, the lifted gradients

@@ -262,6 +262,13 @@ class Flexi:
         self._check(self.L.fg_run(self.h, int(n_steps), _p(t)), "fg_run")
         return t
 
+    def TimeDisc_to_host_ptr(self, n_steps, host_ptr):
+        """TimeDisc(n_steps), then U(t_end) into the host memory at host_ptr (Fortran layout), the copy overlapped with
+        the last stage (fg_run_to_host); returns the times."""
+        t = np.zeros(self.n_inst)
+        self._check(self.L.fg_run_to_host(self.h, int(n_steps), _p(t), ctypes.c_void_p(host_ptr)), "fg_run_to_host")
+        return t
+
     def timedisc_state(self):
         """Per-instance state of the time loop (fg_get_timedisc_state): list of dicts with t, dt, dtMin, iter,
         atAnalyze, finished, nDtLimited."""

@@ -244,6 +244,13 @@ int fg_timestep_lserkw2(fg_handle* h, double* t, double dt);
  * per-instance times, which start at 0 on the first call and continue on later calls. */
 int fg_run(fg_handle* h, int nSteps, double* t);
 
+/* fg_run followed by fg_get_state: nSteps steps of the TimeDisc loop, then U(t_end) into the host array U in the
+ * Fortran layout (the reference's state after the loop, e.g. for WriteStateToHDF5 at an analysis time). The copy
+ * overlaps the last stage: its volume kernel, which writes the final state, runs over element chunks, and each
+ * chunk is copied to U while the later ones compute. Results are bitwise those of fg_run + fg_get_state; U is
+ * written only up to the return (pinned host memory gives the full copy rate). */
+int fg_run_to_host(fg_handle* h, int nSteps, double* t, double* U);
+
 /* Per-instance state of the time loop (the reference's t, dt, dt_Min(DT_MIN), iter, doAnalyze, doFinalize,
  * nDtLimited of timedisc_vars.f90). */
 typedef struct fg_timedisc_state {
