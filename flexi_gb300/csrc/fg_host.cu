@@ -2076,7 +2076,8 @@ static int vol_epb(const fg_handle* h) {
 // stream converts its elements to the Fortran layout and copies them to Uhost while the later chunks run. The copy of
 // a fifth of the state takes less time than the kernel's work on the next fifth down to about 45 GB/s of link rate
 // (the link runs at 190 GB/s device-to-host when nothing else loads it, but far slower at times), so the copies keep
-// pace and only the last chunk's is left when the kernel ends. Overintegration is excluded by the caller.
+// pace and only the last chunk's is left when the kernel ends. With overintegration each chunk is followed by its
+// elements' filter kernel (which writes their final state).
 static int launch_last_stage_to_host(fg_handle* h, int mode, double rkA, double rkB, double* Uhost) {
   static const double ends[FG_OUT_CHUNKS] = {0.2, 0.4, 0.6, 0.8, 0.95, 1.0};
   const Dev& d = h->d;
@@ -2094,8 +2095,11 @@ static int launch_last_stage_to_host(fg_handle* h, int mode, double rkA, double 
     Dev dc = d;
     dc.volBegin = begin;
     dc.volCount = cnt;
-    if (h->cfg.SplitDG >= 0) h->K.vol_split(dc, h->B, mode, rkA, rkB, h->st);
-    else h->K.vol_weak(dc, h->B, mode, rkA, rkB, h->st);
+    // with overintegration the volume kernel writes J u_t and k_overint filters it and updates the registers
+    const bool oi = h->ov.type > 0;
+    if (h->cfg.SplitDG >= 0) h->K.vol_split(dc, h->B, oi ? 3 : mode, rkA, rkB, h->st);
+    else h->K.vol_weak(dc, h->B, oi ? 3 : mode, rkA, rkB, h->st);
+    if (oi) { h->K.overint(dc, h->ov, mode, rkA, rkB, 0, h->st); h->launches += 1; }
     CUDA_TRY(cudaEventRecord(h->evOut[c], h->st));
     CUDA_TRY(cudaStreamWaitEvent(h->stOut, h->evOut[c], 0));
     dev_to_fortran(h, d.U + begin * per, h->dStage + begin * per, 5, 0, 5, cnt, h->stOut);
@@ -2138,9 +2142,8 @@ int fg_run_to_host(fg_handle* h, int nSteps, double* t, double* U) {
   if (!h || !h->haveMesh) return fail(h, FG_ERR_STATE, "no mesh");
   if (!U) return fail(h, FG_ERR_CONFIG, "fg_run_to_host: null state pointer");
   if (nSteps < 0) return fail(h, FG_ERR_CONFIG, "nSteps < 0");
-  // per-kernel profiling, and overintegration (whose filter kernel writes U after the volume kernel), take the
-  // plain sequence
-  if (nSteps == 0 || h->profiling || h->ov.type > 0) {
+  // per-kernel profiling takes the plain sequence
+  if (nSteps == 0 || h->profiling) {
     if (int r = fg_run(h, nSteps, t)) return r;
     return fg_get_state(h, U);
   }

@@ -194,7 +194,7 @@ struct Inst {
   }
   static size_t smem_overint() { return sizeof(double) * (10 * S::n3 + 2 * S::n2); }
   static void overint(const Dev& d, const OverintDev& o, int mode, double rkA, double rkB, int state, cudaStream_t st) {
-    k_overint<n><<<d.nElems, OverintShape<n>::THREADS, smem_overint(), st>>>(d, o, Stage{mode, rkA, rkB}, state);
+    k_overint<n><<<d.volCount > 0 ? d.volCount : d.nElems, OverintShape<n>::THREADS, smem_overint(), st>>>(d, o, Stage{mode, rkA, rkB}, state);
   }
   static void dt(const Dev& d, const Basis& B, const double* ma, const double* mv, double cfl, double dfl, double* bulk, const double* wv,
                  cudaStream_t st) {

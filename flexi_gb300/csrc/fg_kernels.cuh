@@ -1708,7 +1708,7 @@ __global__ void __launch_bounds__(OverintShape<n>::THREADS) k_overint(Dev d, Ove
   double* A = smem;           // [5][n3]
   double* Bf = A + 5 * n3;    // [5][n3]
   double* sM = Bf + 5 * n3;   // type 1: F [n][n]; type 2: VNU [nu][n], VUN [n][nu]
-  const int e = blockIdx.x;
+  const int e = d.volBegin + blockIdx.x;
   const int nu = o.nu;
   if (o.type == 1) {
     for (int t = threadIdx.x; t < n * n; t += blockDim.x) sM[t] = o.F[t];

@@ -3,8 +3,9 @@ last stage over element chunks, each copied while the later ones compute) gives 
 followed by fg_get_state. Cases cover every volume-kernel family and chunk shape: the shuffle-pair split kernel
 (lines of 2 and 8 nodes: 16 and 1 elements per CTA, element counts that leave a partial last CTA), the per-node split
 kernel on Gauss nodes, the weak-form kernel with 5 elements per CTA and the autotuner's 2-element variant, mortar
-meshes, wall boundaries with the channel body force, an ensemble of two instances, and overintegration (which takes
-the unchunked sequence); calls of 1 and 3 steps, a call that continues the loop, and pinned host memory."""
+meshes, wall boundaries with the channel body force, an ensemble of two instances, and overintegration (each chunk
+followed by its elements' filter kernel); calls of 1 and 3 steps, a call that continues the loop, and pinned host
+memory."""
 import numpy as np
 import pytest
 
@@ -27,6 +28,10 @@ CASES = {
     "gauss3_weak_ensemble": (dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="roe", Lifting="br1"), "ensemble", None),
     "gauss5_overint_cutoff": (dict(N=5, NodeType="gauss", SplitDG="weak", Riemann="roe", Lifting="br1", OverintegrationType=1, NUnder=3),
                               "tgv3", None),
+    "gauss4_overint_conservative": (dict(N=4, NodeType="gauss", SplitDG="weak", Riemann="roeentropyfix", Lifting="br1",
+                                         OverintegrationType=2, NUnder=2), "tgv4", None),
+    "gauss11_overint_cutoff": (dict(N=11, NodeType="gauss", SplitDG="weak", Riemann="roeentropyfix", Lifting="br1", OverintegrationType=1,
+                                    NUnder=7), "tgv2", None),
 }
 
 
