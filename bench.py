@@ -798,19 +798,28 @@ def run_adjoint(args):
     _, w1, _ = orc.nodes_and_weights(5, 1)
     wq = np.einsum("k,j,i->kji", w1, w1, w1)[None] / f.mesh_array("sJ")  # quadrature weight x Jacobian
 
+    def kinetic_terms(U):
+        return 0.5 * (U[..., 1] ** 2 + U[..., 2] ** 2 + U[..., 3] ** 2) / U[..., 0] * wq
+
     def kinetic(U):
-        return float((0.5 * (U[..., 1] ** 2 + U[..., 2] ** 2 + U[..., 3] ** 2) / U[..., 0] * wq).sum())
+        return float(kinetic_terms(U).sum())
 
     target = kinetic(U0) * rng.uniform(0.9, 0.95)
 
-    def loss(U0_, s_):
+    def final_state(U0_, s_):
         # the same fixed-dt solve through the reference-facing step entry (TimeStepByLSERKW2)
         f.U = U0_
         f.set_elem_mu_scale(s_)
         t = 0.0
         for _ in range(n_steps):
             t = f.TimeStepByLSERKW2(t, dt)
-        return 0.5 * (kinetic(f.U) - target) ** 2
+        return f.U
+
+    def loss_difference(Up, Um):
+        # L(Up) - L(Um) = 1/2 (K+ - K-) (K+ + K- - 2 target), with K+ - K- summed from the nodes' differences: two
+        # separately rounded sums K+ and K- would leave about 1e-16 K of round-off in their difference
+        kp, km = kinetic_terms(Up), kinetic_terms(Um)
+        return 0.5 * float((kp - km).sum()) * (float(kp.sum()) + float(km.sum()) - 2.0 * target)
 
     stream = torch.cuda.ExternalStream(f.stream())
 
@@ -858,11 +867,10 @@ def run_adjoint(args):
     L0 = 0.5 * (KE - target) ** 2
     # finite differences of the loss in seeded random directions of (U0, multipliers): the central difference with
     # eps = 1e-6, and central differences at h, 2h, 4h (h = 2e-5) extrapolated twice (Richardson: fourth order from h, 2h,
-    # sixth order from all three). On this loss the central quotient's error is round-off (~4e-9 of the derivative at
-    # 1e-6, falling as 1/h) and truncation (~170 h^2 relative) above 1e-5, which the extrapolation removes; from h = 1e-4
-    # on the extrapolated values drift again (2e-8 against the exact tangent). The distance between the fourth- and
-    # sixth-order values estimates the fourth-order one's truncation error, and that of the eps = 1e-6 quotient from the
-    # sixth-order value is that quotient's own error; the exact tangent (--exact-dirs) measures both FD values' errors.
+    # sixth order from all three). Each quotient differences the two final states node by node before summing
+    # (loss_difference). The distance between the fourth- and sixth-order values estimates the fourth-order one's
+    # truncation error, and that of the eps = 1e-6 quotient from the sixth-order value is that quotient's own error; the
+    # exact tangent (--exact-dirs) measures both FD values' errors.
     errs, errs_rich, fd_own, rich_own, exact = [], [], [], [], []
     o_ex = None
     h = 2e-5
@@ -870,8 +878,9 @@ def run_adjoint(args):
         dU = rng.standard_normal(U0.shape) * np.abs(U0).max(axis=(0, 1, 2, 3))
         ds = rng.standard_normal(f.n_elems)
         eps = 1e-6
-        fd = (loss(U0 + eps * dU, scale + eps * ds) - loss(U0 - eps * dU, scale - eps * ds)) / (2 * eps)
-        D = [(loss(U0 + k_ * h * dU, scale + k_ * h * ds) - loss(U0 - k_ * h * dU, scale - k_ * h * ds)) / (2 * k_ * h) for k_ in (1, 2, 4)]
+        fd = loss_difference(final_state(U0 + eps * dU, scale + eps * ds), final_state(U0 - eps * dU, scale - eps * ds)) / (2 * eps)
+        D = [loss_difference(final_state(U0 + k_ * h * dU, scale + k_ * h * ds), final_state(U0 - k_ * h * dU, scale - k_ * h * ds)) /
+             (2 * k_ * h) for k_ in (1, 2, 4)]
         r4 = [(4 * D[0] - D[1]) / 3, (4 * D[1] - D[2]) / 3]
         rich = (16 * r4[0] - r4[1]) / 15
         ad = float((Ub0 * dU).sum() + mub @ ds)
@@ -931,7 +940,8 @@ def run_adjoint(args):
                          "adjoint_vs_exact_max": max((x["adjoint_vs_exact"] for x in exact), default=None),
                          "richardson_vs_exact_max": max((x["richardson_vs_exact"] for x in exact), default=None),
                          "note": "central FD at eps=1e-6 as the configuration states, and central FDs at h=2e-5, 2h, 4h extrapolated to "
-                                 "sixth order; the sixth-order value's distance from the eps=1e-6 quotient is that quotient's own error, "
+                                 "sixth order; each quotient sums the node-by-node differences of the two final states' kinetic "
+                                 "energies; the sixth-order value's distance from the eps=1e-6 quotient is that quotient's own error, "
                                  "its distance from the fourth-order value (h, 2h) bounds the fourth-order value's"},
             "dot_product_vs_reference_fd_jvp": {"rel_err": dot_err, "fd": "implicit.f90:MatrixVector FD_Order 2, Eps_Method 1, on the oracle"},
             "e2e": {"value": ms_rev / ms_plain, "unit": "reverse time / forward time", "h2d_bytes_per_step": dof * 5 * 8 / n_steps,
