@@ -650,7 +650,8 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_split_gen_adj(Dev d, 
 // SurfElem factor; gL[12] the master's face gradients (on a small mortar side: the big side's, interpolated).
 // Writes the slave face-state, slave face-gradient and slave multiplier cotangents of the point, and adds the
 // master face-state, master face-gradient and master multiplier (times mu0) cotangents into fbM, gLb, muLb.
-template <int n>
+// MORE: the Riemann solvers beyond LF/HLLC/Roe/RoeEntropyFix (riemann_rotated_more_adj)
+template <int n, bool MORE = false>
 __device__ __forceinline__ void inner_flux_adj(const Dev& d, const AdjDev& a, const Basis& B, int s, int pq, const double* Fb,
                                                const double* gL, double* gLb, double* fbM, double& muLb) {
   constexpr int n2 = n * n;
@@ -681,7 +682,8 @@ __device__ __forceinline__ void inner_flux_adj(const Dev& d, const AdjDev& a, co
   Frb[4] = Fb[4];
   RotState Lb, Rb;
   rot_zero(Lb); rot_zero(Rb);
-  riemann_rotated_adj(B.riemann, B.splitDG, B, L, R, Frb, Lb, Rb);
+  if constexpr (MORE) riemann_rotated_more_adj(B.riemann, B.splitDG, B, L, R, Frb, Lb, Rb);
+  else riemann_rotated_adj(B.riemann, B.splitDG, B, L, R, Frb, Lb, Rb);
   double uLb = Lb.v1 * nv[0] + Lb.v2 * t1[0] + Lb.v3 * t2[0];
   double vLb = Lb.v1 * nv[1] + Lb.v2 * t1[1] + Lb.v3 * t2[1];
   double wLb = Lb.v1 * nv[2] + Lb.v2 * t1[2] + Lb.v3 * t2[2];
@@ -708,7 +710,7 @@ __device__ __forceinline__ void inner_flux_adj(const Dev& d, const AdjDev& a, co
   a.muSideb[((size_t)s * 2 + 1) * n2 + pq] = muRb * mu0s;
 }
 
-template <int n>
+template <int n, bool MORE = false>
 __global__ void __launch_bounds__(128) k_flux_adj(Dev d, AdjDev a, Basis B) {
   constexpr int n2 = n * n;
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -747,7 +749,7 @@ __global__ void __launch_bounds__(128) k_flux_adj(Dev d, AdjDev a, Basis B) {
     visc_flux_dir_adj(muL, B.lambdaFac, 0., 0., 0., gL, nv[0], nv[1], nv[2], Fv, zu, zv, zw, gLb, mub);
     muLb = mub * mu0s;
   } else {
-    inner_flux_adj<n>(d, a, B, s, pq, Fb, gL, gLb, fbM, muLb);
+    inner_flux_adj<n, MORE>(d, a, B, s, pq, Fb, gL, gLb, fbM, muLb);
   }
   double* dM = a.faceMb + (size_t)s * FS_NF * n2 + pq;
 #pragma unroll

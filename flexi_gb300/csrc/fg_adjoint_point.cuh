@@ -467,6 +467,299 @@ FG_HD void riemann_rotated_adj(int solver, int splitDG, const Basis& B, const Ro
   enthalpy_adj(R, HRb, Rb);
 }
 
+// ---- the Riemann solvers of riemann_rotated_more: HLL, HLLE, HLLEM, RoeL2, RoeEntropyGShockFix, the flux average ----
+
+// transposed Roe averages (square-root-density weights of v1..v3 and H; rc = sqrt(kappaM1 (rH - absVel/2)), absVel =
+// r1v^2 + r2v^2 + r3v^2): given the bars of the averages, of rc and absVel, and of the square roots of the densities,
+// adds to the states' bars and to the enthalpy bars HLb, HRb (the caller applies enthalpy_adj)
+FG_HD void roe_average_adj(const Basis& B, const RotState& L, const RotState& R, double HL, double HR, double sqL, double sqR, double ssq,
+                           double r1v, double r2v, double r3v, double rc, double r1vb, double r2vb, double r3vb, double rHb, double rcb,
+                           double absb, double sqLb, double sqRb, RotState& Lb, RotState& Rb, double& HLb, double& HRb) {
+  const double Zb = rcb / (2.0 * rc);
+  rHb += B.kappaM1 * Zb;
+  absb -= 0.5 * B.kappaM1 * Zb;
+  r1vb += 2.0 * r1v * absb; r2vb += 2.0 * r2v * absb; r3vb += 2.0 * r3v * absb;
+  const double ssqb = rHb * (sqR * HR + sqL * HL) + r1vb * (sqR * R.v1 + sqL * L.v1) + r2vb * (sqR * R.v2 + sqL * L.v2) +
+                      r3vb * (sqR * R.v3 + sqL * L.v3);
+  sqRb += (rHb * HR + r1vb * R.v1 + r2vb * R.v2 + r3vb * R.v3) * ssq;
+  sqLb += (rHb * HL + r1vb * L.v1 + r2vb * L.v2 + r3vb * L.v3) * ssq;
+  HRb += rHb * sqR * ssq; HLb += rHb * sqL * ssq;
+  Rb.v1 += r1vb * sqR * ssq; Lb.v1 += r1vb * sqL * ssq;
+  Rb.v2 += r2vb * sqR * ssq; Lb.v2 += r2vb * sqL * ssq;
+  Rb.v3 += r3vb * sqR * ssq; Lb.v3 += r3vb * sqL * ssq;
+  sqLb -= ssqb * ssq * ssq; sqRb -= ssqb * ssq * ssq;
+  Lb.rho += sqLb / (2.0 * sqL); Rb.rho += sqRb / (2.0 * sqR);
+}
+
+// c = sqrt(kappa p srho): adds the bars of p and srho for the bar of c
+FG_HD void sound_speed_adj(const Basis& B, const RotState& S, double c, double cb, RotState& Sb) {
+  Sb.p += cb * B.kappa * S.srho / (2.0 * c);
+  Sb.srho += cb * B.kappa * S.p / (2.0 * c);
+}
+
+// dU = U_R - U_L of the conservative variables (rho, rho v1, rho v2, rho v3, E): adds the states' bars for dUb[5]
+FG_HD void jump_adj(const RotState& L, const RotState& R, const double* dUb, RotState& Lb, RotState& Rb) {
+  Rb.rho += dUb[0] + dUb[1] * R.v1 + dUb[2] * R.v2 + dUb[3] * R.v3;
+  Lb.rho -= dUb[0] + dUb[1] * L.v1 + dUb[2] * L.v2 + dUb[3] * L.v3;
+  Rb.v1 += dUb[1] * R.rho; Lb.v1 -= dUb[1] * L.rho;
+  Rb.v2 += dUb[2] * R.rho; Lb.v2 -= dUb[2] * L.rho;
+  Rb.v3 += dUb[3] * R.rho; Lb.v3 -= dUb[3] * L.rho;
+  Rb.E += dUb[4]; Lb.E -= dUb[4];
+}
+
+// bars of the Roe-type dissipation D = sum_k A_k e_k r_k (w_k = A_k e_k; a0, a4 the outer eigenvalues in D[1], r1v the
+// averaged normal velocity in the other rows): given Db[5], sets the bars of A0..A4, e0, e1, e4, a0, a4 and adds those of
+// r1v, r2v, r3v, rH, rc and absVel
+struct RoeDissBars {
+  double A[5], e0, e1, e4, a0, a4;
+};
+FG_HD void roe_dissipation_adj(const double* Db, const double* A, double e0, double e1, double e4, double a0, double a4, double r1v, double r2v,
+                               double r3v, double rH, double rc, double absVel, RoeDissBars& o, double& r1vb, double& r2vb, double& r3vb,
+                               double& rHb, double& rcb, double& absb) {
+  const double w0 = A[0] * e0, w1 = A[1] * e1, w2 = A[2] * e1, w3 = A[3] * e1, w4 = A[4] * e4;
+  const double S = w0 + w1 + w4;
+  double w0b = 0, w1b = 0, w2b = 0, w3b = 0, w4b = 0;
+  double Sb = Db[0];
+  w0b += Db[1] * a0; o.a0 = Db[1] * w0; w1b += Db[1] * r1v; r1vb += Db[1] * w1; w4b += Db[1] * a4; o.a4 = Db[1] * w4;
+  Sb += Db[2] * r2v; r2vb += Db[2] * S; w2b += Db[2];
+  Sb += Db[3] * r3v; r3vb += Db[3] * S; w3b += Db[3];
+  w0b += Db[4] * (rH - r1v * rc); rHb += Db[4] * (w0 + w4); r1vb += Db[4] * rc * (w4 - w0); rcb += Db[4] * r1v * (w4 - w0);
+  w1b += Db[4] * (0.5 * absVel); absb += Db[4] * 0.5 * w1;
+  w2b += Db[4] * r2v; r2vb += Db[4] * w2; w3b += Db[4] * r3v; r3vb += Db[4] * w3;
+  w4b += Db[4] * (rH + r1v * rc);
+  w0b += Sb; w1b += Sb; w4b += Sb;
+  o.A[0] = w0b * e0; o.A[1] = w1b * e1; o.A[2] = w2b * e1; o.A[3] = w3b * e1; o.A[4] = w4b * e4;
+  o.e0 = w0b * A[0]; o.e1 = w1b * A[1] + w2b * A[2] + w3b * A[3]; o.e4 = w4b * A[4];
+}
+
+// Transposed Jacobian of riemann_rotated_more for HLL, HLLE, HLLEM (riemann.f90:1067-1235), RoeL2 (:983) and
+// RoeEntropyGShockFix (:866) with the weak form or the split forms PI / SD, and of the flux average (:1236) with PI / SD;
+// LF, HLLC, Roe and RoeEntropyFix go to riemann_rotated_adj. Fb[5] given, adds to the bars of both rotated states.
+FG_HD void riemann_rotated_more_adj(int solver, int splitDG, const Basis& B, const RotState& L, const RotState& R, const double* Fb,
+                                    RotState& Lb, RotState& Rb) {
+  if (solver == RIEMANN_LF || solver == RIEMANN_HLLC || solver == RIEMANN_ROE || solver == RIEMANN_ROEENTROPYFIX) {
+    riemann_rotated_adj(solver, splitDG, B, L, R, Fb, Lb, Rb);
+    return;
+  }
+  const bool split = splitDG >= 0;
+  const double HL = (L.E + L.p) * L.srho, HR = (R.E + R.p) * R.srho;
+  double HLb = 0.0, HRb = 0.0;
+  if (solver == RIEMANN_AVERAGE) {
+    split_surface_flux_adj(splitDG, L, R, HL, HR, Fb, Lb, Rb, HLb, HRb);
+    enthalpy_adj(L, HLb, Lb);
+    enthalpy_adj(R, HRb, Rb);
+    return;
+  }
+  const double cL = sqrt(B.kappa * L.p * L.srho), cR = sqrt(B.kappa * R.p * R.srho);
+  double FL[5], FR[5];
+  euler_flux_1d(L, FL);
+  euler_flux_1d(R, FR);
+  const double sqL = sqrt(L.rho), sqR = sqrt(R.rho);
+  const double ssq = 1.0 / (sqL + sqR);
+  const double r1v = (sqR * R.v1 + sqL * L.v1) * ssq;
+  const double r2v = (sqR * R.v2 + sqL * L.v2) * ssq;
+  const double r3v = (sqR * R.v3 + sqL * L.v3) * ssq;
+  const double rH = (sqR * HR + sqL * HL) * ssq;
+  const double absVel = r1v * r1v + r2v * r2v + r3v * r3v;
+  const double rc = sqrt(B.kappaM1 * (rH - 0.5 * absVel));
+  const double dU[5] = {R.rho - L.rho, R.rho * R.v1 - L.rho * L.v1, R.rho * R.v2 - L.rho * L.v2, R.rho * R.v3 - L.rho * L.v3, R.E - L.E};
+  double r1vb = 0, r2vb = 0, r3vb = 0, rHb = 0, rcb = 0, absb = 0, sqLb = 0, sqRb = 0, cLb = 0, cRb = 0;
+  double dUb[5] = {0, 0, 0, 0, 0};
+  if (solver == RIEMANN_HLL || solver == RIEMANN_HLLE || solver == RIEMANN_HLLEM) {
+    // signal speeds and which argument of each min / max the forward took
+    const double Ssl0 = r1v - rc, Ssr0 = r1v + rc;
+    double Ssl = Ssl0, Ssr = Ssr0, xl = 0.0, xr = 0.0, beta = 0.0;
+    bool lRoe = true, rRoe = true;
+    if (solver != RIEMANN_HLL) {
+      beta = sqrt(0.5 * B.kappaM1 / B.kappa);
+      xl = L.v1 - beta * cL;
+      xr = R.v1 + beta * cR;
+      lRoe = !(xl < Ssl0);
+      rRoe = !(xr > Ssr0);
+      Ssl = fmin(fmin(Ssl0, xl), 0.0);
+      Ssr = fmax(fmax(Ssr0, xr), 0.0);
+    }
+    if (Ssl >= 0.0) { euler_flux_1d_adj(L, Fb, Lb); return; }
+    if (Ssr <= 0.0) { euler_flux_1d_adj(R, Fb, Rb); return; }
+    // F = (Ssr FL - Ssl FR + Ssl Ssr J) / (Ssr - Ssl), J = dU (HLLEM: minus the anti-diffusion of the contact and shear waves)
+    double J[5] = {dU[0], dU[1], dU[2], dU[3], dU[4]};
+    double delta = 0, A2 = 0, A3 = 0, A4 = 0, RoeDens = 0, K[5] = {0, 0, 0, 0, 0};
+    if (solver == RIEMANN_HLLEM) {
+      RoeDens = sqL * sqR;
+      delta = rc / (rc + fabs(0.5 * (Ssl + Ssr)));
+      A2 = (R.rho - L.rho) - (R.p - L.p) / (rc * rc);
+      A3 = RoeDens * (R.v2 - L.v2);
+      A4 = RoeDens * (R.v3 - L.v3);
+      K[0] = A2; K[1] = r1v * A2; K[2] = r2v * A2 + A3; K[3] = r3v * A2 + A4; K[4] = 0.5 * absVel * A2 + r2v * A3 + r3v * A4;
+      for (int v = 0; v < 5; ++v) J[v] -= delta * K[v];
+    }
+    const double sd = 1.0 / (Ssr - Ssl), ss = Ssl * Ssr;
+    double FLb[5], FRb[5], Jb[5], sdb = 0, ssb = 0, Sslb = 0, Ssrb = 0;
+    for (int v = 0; v < 5; ++v) {
+      FLb[v] = Fb[v] * Ssr * sd;
+      FRb[v] = -Fb[v] * Ssl * sd;
+      Jb[v] = Fb[v] * ss * sd;
+      sdb += Fb[v] * (Ssr * FL[v] - Ssl * FR[v] + ss * J[v]);
+      ssb += Fb[v] * J[v] * sd;
+      Ssrb += Fb[v] * FL[v] * sd;
+      Sslb -= Fb[v] * FR[v] * sd;
+    }
+    Ssrb += ssb * Ssl - sdb * sd * sd;
+    Sslb += ssb * Ssr + sdb * sd * sd;
+    euler_flux_1d_adj(L, FLb, Lb);
+    euler_flux_1d_adj(R, FRb, Rb);
+    for (int v = 0; v < 5; ++v) dUb[v] += Jb[v];
+    if (solver == RIEMANN_HLLEM) {
+      double Kb[5], deltab = 0;
+      for (int v = 0; v < 5; ++v) { Kb[v] = -delta * Jb[v]; deltab -= Jb[v] * K[v]; }
+      const double A2b = Kb[0] + Kb[1] * r1v + Kb[2] * r2v + Kb[3] * r3v + Kb[4] * 0.5 * absVel;
+      const double A3b = Kb[2] + Kb[4] * r2v, A4b = Kb[3] + Kb[4] * r3v;
+      r1vb += Kb[1] * A2; r2vb += Kb[2] * A2 + Kb[4] * A3; r3vb += Kb[3] * A2 + Kb[4] * A4; absb += Kb[4] * 0.5 * A2;
+      // delta = rc / (rc + |m|), m = (Ssl + Ssr) / 2
+      const double m = 0.5 * (Ssl + Ssr), q = rc + fabs(m);
+      rcb += deltab * fabs(m) / (q * q);
+      const double mb = -deltab * rc / (q * q) * sgn1(m);
+      Sslb += 0.5 * mb; Ssrb += 0.5 * mb;
+      // A2 = drho - dp / rc^2, A3 = RoeDens dv2, A4 = RoeDens dv3, RoeDens = sqL sqR
+      const double dp = R.p - L.p;
+      Rb.rho += A2b; Lb.rho -= A2b;
+      Rb.p -= A2b / (rc * rc); Lb.p += A2b / (rc * rc);
+      rcb += A2b * 2.0 * dp / (rc * rc * rc);
+      const double RoeDensb = A3b * (R.v2 - L.v2) + A4b * (R.v3 - L.v3);
+      Rb.v2 += A3b * RoeDens; Lb.v2 -= A3b * RoeDens;
+      Rb.v3 += A4b * RoeDens; Lb.v3 -= A4b * RoeDens;
+      sqLb += RoeDensb * sqR; sqRb += RoeDensb * sqL;
+    }
+    jump_adj(L, R, dUb, Lb, Rb);
+    // signal speeds (in the subsonic case neither min nor max took 0)
+    if (lRoe) { r1vb += Sslb; rcb -= Sslb; } else { Lb.v1 += Sslb; cLb -= beta * Sslb; }
+    if (rRoe) { r1vb += Ssrb; rcb += Ssrb; } else { Rb.v1 += Ssrb; cRb += beta * Ssrb; }
+    sound_speed_adj(B, L, cL, cLb, Lb);
+    sound_speed_adj(B, R, cR, cRb, Rb);
+    roe_average_adj(B, L, R, HL, HR, sqL, sqR, ssq, r1v, r2v, r3v, rc, r1vb, r2vb, r3vb, rHb, rcb, absb, sqLb, sqRb, Lb, Rb, HLb, HRb);
+    enthalpy_adj(L, HLb, Lb);
+    enthalpy_adj(R, HRb, Rb);
+    return;
+  }
+  // RoeL2 / RoeEntropyGShockFix: F = central - D/2 with the Roe-type dissipation D
+  if (!split) {
+    double Fh[5];
+    for (int v = 0; v < 5; ++v) Fh[v] = 0.5 * Fb[v];
+    euler_flux_1d_adj(L, Fh, Lb);
+    euler_flux_1d_adj(R, Fh, Rb);
+  } else {
+    split_surface_flux_adj(splitDG, L, R, HL, HR, Fb, Lb, Rb, HLb, HRb);
+  }
+  double Db[5];
+  for (int v = 0; v < 5; ++v) Db[v] = -0.5 * Fb[v];
+  RoeDissBars o;
+  if (solver == RIEMANN_ROEL2) {
+    const double a0 = r1v - rc, a1 = r1v, a4 = r1v + rc;
+    const double P2 = dU[2] - r2v * dU[0], P3 = dU[3] - r3v * dU[0];
+    const double d5 = dU[4] - P2 * r2v - P3 * r3v;
+    const double sa = sqrt(absVel), sk = sqrt(B.kappa);
+    const double Ma = sa / (rc * sk);
+    const double d1 = dU[1] * Ma, d2 = dU[2] * Ma, d3 = dU[3] * Ma;
+    const double src = 1.0 / rc;
+    double A[5];
+    A[2] = d2 - r2v * dU[0];
+    A[3] = d3 - r3v * dU[0];
+    const double Y = dU[0] * (rH - r1v * r1v) - d5 + r1v * d1;
+    A[1] = B.kappaM1 * (src * src) * Y;
+    const double X = dU[0] * (r1v + rc) - d1 - rc * A[1];
+    A[0] = 0.5 * src * X;
+    A[4] = dU[0] - A[0] - A[1];
+    const double e0 = fabs(a0), e1 = fabs(a1), e4 = fabs(a4);
+    roe_dissipation_adj(Db, A, e0, e1, e4, a0, a4, r1v, r2v, r3v, rH, rc, absVel, o, r1vb, r2vb, r3vb, rHb, rcb, absb);
+    double a0b = o.a0 + o.e0 * sgn1(a0), a1b = o.e1 * sgn1(a1), a4b = o.a4 + o.e4 * sgn1(a4);
+    double A0b = o.A[0], A1b = o.A[1], A2b = o.A[2], A3b = o.A[3], A4b = o.A[4];
+    double d1b = 0, d5b = 0, srcb = 0, Mab = 0;
+    // A4 = dU0 - A0 - A1
+    dUb[0] += A4b; A0b -= A4b; A1b -= A4b;
+    // A0 = src X / 2
+    srcb += A0b * 0.5 * X;
+    const double Xb = A0b * 0.5 * src;
+    dUb[0] += Xb * (r1v + rc); r1vb += Xb * dU[0]; rcb += Xb * (dU[0] - A[1]); d1b -= Xb; A1b -= Xb * rc;
+    // A1 = kappaM1 src^2 Y
+    srcb += A1b * B.kappaM1 * 2.0 * src * Y;
+    const double Yb = A1b * B.kappaM1 * src * src;
+    dUb[0] += Yb * (rH - r1v * r1v); rHb += Yb * dU[0]; r1vb += Yb * (d1 - 2.0 * r1v * dU[0]); d5b -= Yb; d1b += Yb * r1v;
+    rcb -= srcb * src * src;
+    // A2 = Ma dU2 - r2v dU0, A3 = Ma dU3 - r3v dU0, d1 = Ma dU1
+    Mab += A2b * dU[2] + A3b * dU[3] + d1b * dU[1];
+    dUb[2] += A2b * Ma; r2vb -= A2b * dU[0]; dUb[0] -= A2b * r2v;
+    dUb[3] += A3b * Ma; r3vb -= A3b * dU[0]; dUb[0] -= A3b * r3v;
+    dUb[1] += d1b * Ma;
+    // d5 = dU4 - P2 r2v - P3 r3v, P2 = dU2 - r2v dU0, P3 = dU3 - r3v dU0
+    dUb[4] += d5b;
+    const double P2b = -d5b * r2v, P3b = -d5b * r3v;
+    r2vb -= d5b * P2; r3vb -= d5b * P3;
+    dUb[2] += P2b; r2vb -= P2b * dU[0]; dUb[0] -= P2b * r2v;
+    dUb[3] += P3b; r3vb -= P3b * dU[0]; dUb[0] -= P3b * r3v;
+    // Ma = sqrt(absVel) / (rc sqrt(kappa))
+    if (sa > 0.0) absb += Mab / (rc * sk) / (2.0 * sa);
+    rcb -= Mab * Ma / rc;
+    jump_adj(L, R, dUb, Lb, Rb);
+    r1vb += a0b + a1b + a4b;
+    rcb += a4b - a0b;
+  } else {  // RoeEntropyGShockFix
+    const double sg = r1v < 0.0 ? -1.0 : 1.0;
+    const double lim = rc / B.riemannPhi, ar1 = fabs(r1v);
+    const bool limTaken = !(lim < ar1);  // fmax(lim, |r1v|): the first argument on a tie
+    const double am = sg * fmax(lim, ar1);
+    const double a0 = am - rc, a1 = am, a4 = am + rc;
+    const double RoeDens = sqL * sqR;
+    const double dr = R.rho - L.rho, du = R.v1 - L.v1, dv = R.v2 - L.v2, dw = R.v3 - L.v3, dp = R.p - L.p;
+    const double tmp = 0.5 / (rc * rc);
+    const double rdc = RoeDens * rc * du;
+    double A[5];
+    A[0] = tmp * (dp - rdc);
+    A[1] = dr - dp * (2.0 * tmp);
+    A[2] = RoeDens * dv;
+    A[3] = RoeDens * dw;
+    A[4] = tmp * (dp + rdc);
+    auto fix = [](double a, double al, double ar) {
+      const double da = fmax(0.0, fmax(a - al, ar - a));
+      return fabs(a) < da ? 0.5 * (a * a / da + da) : fabs(a);
+    };
+    const double e0 = fix(a0, L.v1 - cL, R.v1 - cR), e1 = fix(a1, L.v1, R.v1), e4 = fix(a4, L.v1 + cL, R.v1 + cR);
+    roe_dissipation_adj(Db, A, e0, e1, e4, a0, a4, r1v, r2v, r3v, rH, rc, absVel, o, r1vb, r2vb, r3vb, rHb, rcb, absb);
+    double a0b = o.a0, a1b = 0.0, a4b = o.a4, alb = 0, arb = 0;
+    entropy_fix_adj(a0, L.v1 - cL, R.v1 - cR, o.e0, a0b, alb, arb);
+    Lb.v1 += alb; cLb -= alb; Rb.v1 += arb; cRb -= arb;
+    alb = arb = 0;
+    entropy_fix_adj(a1, L.v1, R.v1, o.e1, a1b, alb, arb);
+    Lb.v1 += alb; Rb.v1 += arb;
+    alb = arb = 0;
+    entropy_fix_adj(a4, L.v1 + cL, R.v1 + cR, o.e4, a4b, alb, arb);
+    Lb.v1 += alb; cLb += alb; Rb.v1 += arb; cRb += arb;
+    // strengths
+    const double A0b = o.A[0], A1b = o.A[1], A2b = o.A[2], A3b = o.A[3], A4b = o.A[4];
+    const double tmpb = A0b * (dp - rdc) - 2.0 * A1b * dp + A4b * (dp + rdc);
+    const double dpb = (A0b - 2.0 * A1b + A4b) * tmp;
+    const double rdcb = (A4b - A0b) * tmp;
+    const double RoeDensb = A2b * dv + A3b * dw + rdcb * rc * du;
+    rcb += rdcb * RoeDens * du - tmpb / (rc * rc * rc);
+    const double dub = rdcb * RoeDens * rc;
+    Rb.rho += A1b; Lb.rho -= A1b;
+    Rb.v1 += dub; Lb.v1 -= dub;
+    Rb.v2 += A2b * RoeDens; Lb.v2 -= A2b * RoeDens;
+    Rb.v3 += A3b * RoeDens; Lb.v3 -= A3b * RoeDens;
+    Rb.p += dpb; Lb.p -= dpb;
+    sqLb += RoeDensb * sqR; sqRb += RoeDensb * sqL;
+    // eigenvalues a0 = am - rc, a1 = am, a4 = am + rc; am = sg max(rc / phi, |r1v|)
+    const double amb = a0b + a1b + a4b;
+    rcb += a4b - a0b;
+    if (limTaken) rcb += amb * sg / B.riemannPhi;
+    else r1vb += amb;  // sg |r1v| = r1v
+  }
+  sound_speed_adj(B, L, cL, cLb, Lb);
+  sound_speed_adj(B, R, cR, cRb, Rb);
+  roe_average_adj(B, L, R, HL, HR, sqL, sqR, ssq, r1v, r2v, r3v, rc, r1vb, r2vb, r3vb, rHb, rcb, absb, sqLb, sqRb, Lb, Rb, HLb, HRb);
+  enthalpy_adj(L, HLb, Lb);
+  enthalpy_adj(R, HRb, Rb);
+}
+
 // eos.f90:PRESSURE_RIEMANN: adds the bars of rho, vn, p for the bar of the boundary pressure
 FG_HD void pressure_riemann_adj(const Basis& B, double rho, double vn, double p, double pbb, double& rhob, double& vnb, double& pb) {
   if (vn <= 0.0) {

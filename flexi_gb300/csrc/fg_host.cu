@@ -1003,11 +1003,13 @@ void set_error_without_handle(const char* msg) { g_err = msg; }
 
 namespace {
 
-// the adjoint kernels cover: weak form and split forms PI and SD (Gauss, Gauss-Lobatto), LF/HLLC/Roe/RoeEntropyFix, BR1/BR2
+// the adjoint kernels cover: weak form and split forms PI and SD (Gauss, Gauss-Lobatto), every Riemann solver but CH and IR,
+// BR1/BR2
 const char* adjoint_unsupported(const fg_config& c) {
   if (c.N > 7) return "the adjoint supports N = 1..7";
-  if (c.Riemann != FG_RIEMANN_LF && c.Riemann != FG_RIEMANN_HLLC && c.Riemann != FG_RIEMANN_ROE && c.Riemann != FG_RIEMANN_ROEENTROPYFIX)
-    return "the adjoint supports the Riemann solvers LF, HLLC, Roe and RoeEntropyFix";
+  if (c.Riemann == FG_RIEMANN_CH || c.Riemann == FG_RIEMANN_IR)
+    return "the adjoint supports the Riemann solvers LF, HLLC, Roe, RoeEntropyFix, RoeL2, RoeEntropyGShockFix, HLL, HLLE, HLLEM and "
+           "the flux average (not CH or IR)";
   if (c.doWeakLifting || c.doConservativeLifting) return "the adjoint supports the strong, non-conservative lifting";
   if (c.SplitDG != FG_SPLIT_NONE && c.SplitDG != FG_SPLIT_PI && c.SplitDG != FG_SPLIT_SD)
     return "the adjoint supports the weak form and the split forms PI and SD";

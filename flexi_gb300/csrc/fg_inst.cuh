@@ -129,7 +129,10 @@ struct Inst {
   static void flux_adj(const Dev& d, const AdjDev& a, const Basis& B, cudaStream_t st) {
     const long long pts = (long long)d.nFluxSides * S::n2;
     if constexpr (ADJ) {
-      if (pts > 0) k_flux_adj<n><<<(unsigned)((pts + 127) / 128), 128, 0, st>>>(d, a, B);
+      if (pts > 0) {
+        if (flux_more(B)) k_flux_adj<n, true><<<(unsigned)((pts + 127) / 128), 128, 0, st>>>(d, a, B);
+        else k_flux_adj<n><<<(unsigned)((pts + 127) / 128), 128, 0, st>>>(d, a, B);
+      }
     }
   }
   static void lift_adj(const Dev& d, const AdjDev& a, const Basis& B, cudaStream_t st) {
@@ -139,6 +142,7 @@ struct Inst {
     if constexpr (ADJ) k_prep_adj<n, GL><<<blocks(d), S::THREADS, smem_prep_adj(), st>>>(d, a, B);
   }
   static void mortar_face_adj(const Dev& d, const AdjDev& a, const Basis& B, const MortarDev& M, cudaStream_t st) {
+    // mortar meshes take LF, HLLC, Roe and RoeEntropyFix only (fg_build_mesh)
     if constexpr (ADJ) k_mortar_face_adj<n><<<d.nMortars, 256, smem_mortar_face_adj(), st>>>(d, a, B, M);
   }
   static void lift_mortar_adj(const Dev& d, const AdjDev& a, const Basis& B, cudaStream_t st) {

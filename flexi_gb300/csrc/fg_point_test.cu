@@ -87,6 +87,15 @@ void fgpt_riemann_more(int solver, int splitDG, double kappa, double R, double r
   B.riemannPhi = riemannPhi;
   riemann_rotated_more(solver, splitDG, B, rs(L), rs(Rr), F);
 }
+void fgpt_riemann_more_adj(int solver, int splitDG, double kappa, double R, double riemannPhi, const double* L, const double* Rr, const double* Fb,
+                           double* Lb, double* Rb) {
+  Basis B = gas(kappa, R);
+  B.riemannPhi = riemannPhi;
+  RotState lb, rb;
+  rot_zero(lb); rot_zero(rb);
+  riemann_rotated_more_adj(solver, splitDG, B, rs(L), rs(Rr), Fb, lb, rb);
+  rs_out(lb, Lb); rs_out(rb, Rb);
+}
 // two-point volume flux of the split form as the split kernels form it: per-node inputs, pair flux with the metric sum,
 // constant factors; uR/u conservative (5), pR/p primitive (rho, u, v, w, p, T), mR/m metric vectors (3)
 void fgpt_split_volume(int splitDG, double kappa, const double* uR, const double* pR, const double* u, const double* p, const double* mR,

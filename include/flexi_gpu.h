@@ -304,8 +304,9 @@ int fg_set_elem_mu_scale(fg_handle* h, const double* scale);
  * depend on U; the LSERK adjoint recomputes its steps at the forward's stage times). The bulk velocity of a
  * channel body force is held fixed.
  * Supported: weak form and the split forms PI and SD on Gauss and Gauss-Lobatto nodes (on Gauss nodes with the
- * transposed entropy-variable prolongation and split-Gauss surface term), N <= 7, LF/HLLC/Roe/RoeEntropyFix,
- * strong BR1/BR2 lifting, both overintegration types (the transposed filter), walls 3/4, mortar interfaces
+ * transposed entropy-variable prolongation and split-Gauss surface term), N <= 7, every Riemann solver but the split
+ * form's CH and IR surface fluxes (LF, HLLC, Roe, RoeEntropyFix, RoeL2, RoeEntropyGShockFix, HLL, HLLE, HLLEM, the flux
+ * average), strong BR1/BR2 lifting, both overintegration types (the transposed filter), walls 3/4, mortar interfaces
  * (transposed U_Mortar and Flux_Mortar, fillmortar.t90). */
 int fg_vjp_time_derivative(fg_handle* h, double t, const double* W, double* V, double* muScaleBar);
 

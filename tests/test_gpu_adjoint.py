@@ -2,7 +2,8 @@
 
 Cases: the weak form and the split forms PI and SD on Gauss-Lobatto nodes (the shuffle-pair kernel for PI on lines
 of 2, 4 or 8 nodes, the per-node kernel otherwise) and on Gauss nodes (entropy-variable prolongation and split-Gauss
-surface term transposed), every supported Riemann solver, BR1/BR2, both overintegration types, walls.
+surface term transposed), every supported Riemann solver (all of riemann.f90 but the split form's CH and IR surface
+fluxes), BR1/BR2, both overintegration types, walls.
 
 Dot-product test <J V, W> = <V, J^T W>: J V comes from the oracle, exactly by its dual-number
 instantiation of the restated algorithm and approximately by the matrix-free finite difference of the
@@ -46,6 +47,19 @@ CASES = {
     # split form on Gauss-Lobatto lines the shuffle-pair kernel does not take: SD, and PI with odd node counts
     "gl3_split_sd_roe_br1": (dict(N=3, NodeType="gauss-lobatto", SplitDG="sd", Riemann="roe", Lifting="br1"), "tgv"),
     "gl4_split_pi_roeef_br2": (dict(N=4, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roeentropyfix", Lifting="br2"), "tgv"),
+    # the other Riemann solvers: HLL, HLLE, HLLEM (physical fluxes, Roe or Einfeldt signal speeds), RoeL2 (Mach-scaled jumps),
+    # RoeEntropyGShockFix (wave speeds limited by c / RiemannPhiFactor), and the split form's flux average
+    "gauss3_weak_hll_br1": (dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="hll", Lifting="br1"), "tgv"),
+    "gl3_weak_hlle_br2": (dict(N=3, NodeType="gauss-lobatto", SplitDG="weak", Riemann="hlle", Lifting="br2"), "tgv"),
+    "gauss4_weak_hllem_br1": (dict(N=4, NodeType="gauss", SplitDG="weak", Riemann="hllem", Lifting="br1"), "tgv"),
+    "gl3_split_pi_hllem_br2": (dict(N=3, NodeType="gauss-lobatto", SplitDG="pi", Riemann="hllem", Lifting="br2"), "tgv"),
+    "gauss3_weak_roel2_br1": (dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="roel2", Lifting="br1"), "tgv"),
+    "gl7_split_pi_roel2_br1": (dict(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roel2", Lifting="br1"), "tgv"),
+    "gauss3_weak_gshock_br2": (dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="roeentropygshockfix", Lifting="br2"), "tgv"),
+    "gl3_split_sd_gshock_br1": (dict(N=3, NodeType="gauss-lobatto", SplitDG="sd", Riemann="roeentropygshockfix", Lifting="br1"), "tgv"),
+    "gl7_split_pi_avg_br2": (dict(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="avg", Lifting="br2"), "tgv"),
+    "gauss3_split_sd_avg_br1": (dict(N=3, NodeType="gauss", SplitDG="sd", Riemann="avg", Lifting="br1"), "tgv"),
+    "channel_gauss3_weak_hlle_br2": (dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="hlle", Lifting="br2"), "channel"),
     "channel_gauss3_weak_roe_br1": (dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="roe", Lifting="br1"), "channel"),
     "channel_gauss3_split_pi_roe_br2": (dict(N=3, NodeType="gauss", SplitDG="pi", Riemann="roe", Lifting="br2"), "channel"),
     "channel_gl7_split_pi_roe_br1": (dict(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roe", Lifting="br1"), "channel"),
@@ -130,6 +144,16 @@ def test_viscosity_multiplier_cotangent(name):
     fd2 = (J(scale + 2 * h * ds) - J(scale - 2 * h * ds)) / (4 * h)
     rich = (4 * fd - fd2) / 3
     assert abs(float(mub @ ds) - rich) <= 1e-8 * abs(rich), (float(mub @ ds), rich)
+
+
+def test_vjp_rejects_ch_and_ir_surface_fluxes():
+    for riemann in ("ch", "ir"):
+        c = make_config(N=3, NodeType="gauss-lobatto", SplitDG="pi", Riemann=riemann)
+        f = Flexi(c, fmesh.tgv_box(2))
+        f.U = testcases.tgv_state(f.elem_xgp(), mach=0.1)
+        with pytest.raises(Exception, match="not CH or IR"):
+            f.vjp_time_derivative(np.zeros(f.ushape))
+        f.close()
 
 
 def test_vjp_rejects_unsupported():
