@@ -420,8 +420,9 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_split_gen_adj(Dev d, 
   double* sT = sFS + (GL ? 0 : EPB * 6 * 9 * n2);  // Gauss: [EPB][6][n2][5] line sums T_v
   load_basis_smem<n>(B, sD);
   SBasis<n> Bs{sD};
-  const bool pi = B.splitDG == SPLIT_PI;
-  const double f0 = pi ? 0.25 : 0.5, f1 = pi ? 0.125 : 0.5;
+  const int sd = B.splitDG;  // SD, PI, MO, DU or KG
+  double f0, f1;
+  split_factors(sd, f0, f1);
   for (int t = threadIdx.x; t < n2; t += blockDim.x) { sC[t] = B.DVS[t] * f0; sC[n2 + t] = B.DVS[t] * f1; }
   const int e0 = blockIdx.x * EPB;
   adj_load_ubar_and_surface<n, GL>(d, a, Bs, sUb, e0);
@@ -432,12 +433,16 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_split_gen_adj(Dev d, 
     const double u0 = d.U[((size_t)e * 5 + 0) * n3 + x], u4 = d.U[((size_t)e * 5 + 4) * n3 + x];
     const double srho = d.prim[((size_t)e * VP_NF + VP_SRHO) * n3 + x];
     const double p = d.prim[((size_t)e * VP_NF + VP_P) * n3 + x];
-    Q[x] = u0;
-    Q[n3 + x] = d.prim[((size_t)e * VP_NF + VP_U) * n3 + x];
-    Q[2 * n3 + x] = d.prim[((size_t)e * VP_NF + VP_V) * n3 + x];
-    Q[3 * n3 + x] = d.prim[((size_t)e * VP_NF + VP_W) * n3 + x];
-    Q[4 * n3 + x] = pi ? 4.0 * p : p;
-    Q[5 * n3 + x] = pi ? (u4 + p) * srho : u4 + p;
+    const double vx = d.prim[((size_t)e * VP_NF + VP_U) * n3 + x], vy = d.prim[((size_t)e * VP_NF + VP_V) * n3 + x],
+                 vz = d.prim[((size_t)e * VP_NF + VP_W) * n3 + x];
+    double q0, q4, q5;
+    split_node_inputs(sd, u0, vx, vy, vz, p, u4, srho, q0, q4, q5);
+    Q[x] = q0;
+    Q[n3 + x] = vx;
+    Q[2 * n3 + x] = vy;
+    Q[3 * n3 + x] = vz;
+    Q[4 * n3 + x] = q4;
+    Q[5 * n3 + x] = q5;
 #pragma unroll
     for (int c = 0; c < 9; ++c) Q[(6 + c) * n3 + x] = d.metr[((size_t)e * 9 + c) * n3 + x];
   }
@@ -454,12 +459,15 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_split_gen_adj(Dev d, 
       const double pr = src[FS_P * n2];
       double* dst = sFS + (es * 6 + lsi) * 9 * n2;
       const int o = aa + n * bb;
-      dst[o] = src[FS_RHO * n2];
+      double q0, q4, q5;
+      split_node_inputs(sd, src[FS_RHO * n2], src[FS_U * n2], src[FS_V * n2], src[FS_W * n2], pr, src[FS_E * n2], src[FS_SRHO * n2], q0, q4,
+                        q5);
+      dst[o] = q0;
       dst[n2 + o] = src[FS_U * n2];
       dst[2 * n2 + o] = src[FS_V * n2];
       dst[3 * n2 + o] = src[FS_W * n2];
-      dst[4 * n2 + o] = pi ? 4.0 * pr : pr;
-      dst[5 * n2 + o] = pi ? (src[FS_E * n2] + pr) * src[FS_SRHO * n2] : src[FS_E * n2] + pr;
+      dst[4 * n2 + o] = q4;
+      dst[5 * n2 + o] = q5;
 #pragma unroll
       for (int c = 0; c < 3; ++c) dst[(6 + c) * n2 + o] = d.faceJa[(((size_t)e * 6 + lsi) * 3 + c) * n2 + o];
     }
@@ -518,7 +526,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_split_gen_adj(Dev d, 
         Gb[0] = sC[bI * n + aI] * uba[0] + sC[aI * n + bI] * Ub[xb];
 #pragma unroll
         for (int v = 1; v < 5; ++v) Gb[v] = sC[n2 + bI * n + aI] * uba[v] + sC[n2 + aI * n + bI] * Ub[v * n3 + xb];
-        split_pair_flux_adj(pi, qa, qb, ms, Gb, qbar, dummy);
+        split_pair_flux_gen_adj(sd, qa, qb, ms, Gb, qbar, dummy);
       }
       if (!GL) {
         const int fo = dir == 0 ? j + n * k : (dir == 1 ? i + n * k : i + n * j);
@@ -537,7 +545,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_split_gen_adj(Dev d, 
           double Gb[5];
 #pragma unroll
           for (int v = 0; v < 5; ++v) Gb[v] = leg * T[v] - cs * (v == 0 ? f0 : f1) * uba[v];
-          split_pair_flux_adj(pi, qa, qf, ms, Gb, qbar, dummy);
+          split_pair_flux_gen_adj(sd, qa, qf, ms, Gb, qbar, dummy);
         }
       }
     }
@@ -573,12 +581,10 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_split_gen_adj(Dev d, 
     for (int v = 0; v < 5; ++v) u[v] = d.U[((size_t)e * 5 + v) * n3 + x];
     const double vx = qa[1], vy = qa[2], vz = qa[3];
     const double srho = 1.0 / u[0];
-    const double p = pi ? qa[4] * 0.25 : qa[4];
-    double vxb = qbar[1], vyb = qbar[2], vzb = qbar[3];
-    // PI: 4p and H = (E + p) srho; SD: p and E + p
-    const double pb = pi ? 4.0 * qbar[4] + qbar[5] * srho : qbar[4] + qbar[5];
-    const double Eb = pi ? qbar[5] * srho : qbar[5];
-    const double sb = pi ? qbar[5] * (u[4] + p) : 0.;
+    const double p = d.prim[((size_t)e * VP_NF + VP_P) * n3 + x];
+    // the split inputs (split_node_inputs) transposed to the bars of rho, v, p, E and 1/rho
+    double rhob = 0., vxb = 0., vyb = 0., vzb = 0., pb = 0., Eb = 0., sb = 0.;
+    split_node_inputs_adj(sd, u[0], vx, vy, vz, p, u[4], srho, qbar, rhob, vxb, vyb, vzb, pb, Eb, sb);
     double g[12], gb[12];
 #pragma unroll
     for (int c = 0; c < 12; ++c) { g[c] = d.grad[((size_t)e * 12 + c) * n3 + x]; gb[c] = 0.; }
@@ -586,7 +592,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_split_gen_adj(Dev d, 
     visc_flux_phys_adj(mu, B.lambdaFac, vx, vy, vz, g, fb, gyb, hb, vxb, vyb, vzb, gb, mub);
     mub *= d.mu0[d.elemInst[e]];
     double ubar[5] = {0., 0., 0., 0., 0.};
-    cons_to_prim_adj(B, u, sb, vxb, vyb, vzb, pb, 0., qbar[0], Eb, ubar);
+    cons_to_prim_adj(B, u, sb, vxb, vyb, vzb, pb, 0., rhob, Eb, ubar);
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
       double* o = a.Ub + ((size_t)e * 5 + v) * n3 + x;
@@ -627,13 +633,14 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_split_gen_adj(Dev d, 
         double Gb[5];
 #pragma unroll
         for (int v = 0; v < 5; ++v) Gb[v] = leg * T[v] - cs * (v == 0 ? f0 : f1) * Ub[v * n3 + xn];
-        split_pair_flux_adj(pi, qn, qf, ms, Gb, dummy, qfb);
+        split_pair_flux_gen_adj(sd, qn, qf, ms, Gb, dummy, qfb);
       }
       const double* src = (flip == 0 ? d.faceM : d.faceS) + (size_t)s * FS_NF * n2 + pq;
       double fb[FS_NF];
 #pragma unroll
       for (int f = 0; f < FS_NF; ++f) fb[f] = 0.;
-      split_inputs_to_face_adj(pi, src[FS_E * n2], src[FS_P * n2], src[FS_SRHO * n2], qfb, fb);
+      split_node_inputs_adj(sd, src[FS_RHO * n2], src[FS_U * n2], src[FS_V * n2], src[FS_W * n2], src[FS_P * n2], src[FS_E * n2],
+                            src[FS_SRHO * n2], qfb, fb[FS_RHO], fb[FS_U], fb[FS_V], fb[FS_W], fb[FS_P], fb[FS_E], fb[FS_SRHO]);
       double* dst = a.faceVolb + ((size_t)s * 2 + (flip == 0 ? 0 : 1)) * FS_NF * n2 + pq;
 #pragma unroll
       for (int f = 0; f < FS_NF; ++f) dst[f * n2] = fb[f];

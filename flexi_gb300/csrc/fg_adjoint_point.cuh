@@ -467,6 +467,71 @@ FG_HD void riemann_rotated_adj(int solver, int splitDG, const Basis& B, const Ro
   enthalpy_adj(R, HRb, Rb);
 }
 
+// ---- the split fluxes MO, DU and KG (splitflux.f90: SplitVolumeFluxMO :445, DU :225, KG :327 and their surface forms) ----
+
+// split_surface_flux_more transposed for MO, DU, KG on rotated states: Fb[5] given, adds to both states' bars
+FG_HD void split_surface_flux_more_adj(int sd, const RotState& L, const RotState& R, const double* Fb, RotState& Lb, RotState& Rb) {
+  if (sd == SPLIT_DU) {
+    const double us = L.v1 + R.v1;
+    const double mL = L.rho * L.v1, mR = R.rho * R.v1;
+    const double usb = 0.25 * (Fb[0] * (L.rho + R.rho) + Fb[1] * (mL + mR) + Fb[2] * (L.rho * L.v2 + R.rho * R.v2) +
+                               Fb[3] * (L.rho * L.v3 + R.rho * R.v3) + Fb[4] * (L.E + R.E + L.p + R.p));
+    const double q = 0.25 * us;
+    Lb.rho += q * (Fb[0] + Fb[1] * L.v1 + Fb[2] * L.v2 + Fb[3] * L.v3);
+    Rb.rho += q * (Fb[0] + Fb[1] * R.v1 + Fb[2] * R.v2 + Fb[3] * R.v3);
+    Lb.v1 += q * Fb[1] * L.rho + usb; Rb.v1 += q * Fb[1] * R.rho + usb;
+    Lb.v2 += q * Fb[2] * L.rho; Rb.v2 += q * Fb[2] * R.rho;
+    Lb.v3 += q * Fb[3] * L.rho; Rb.v3 += q * Fb[3] * R.rho;
+    Lb.p += 0.5 * Fb[1] + q * Fb[4]; Rb.p += 0.5 * Fb[1] + q * Fb[4];
+    Lb.E += q * Fb[4]; Rb.E += q * Fb[4];
+  } else if (sd == SPLIT_KG) {
+    const double rs = L.rho + R.rho, us = L.v1 + R.v1, b = 0.125 * rs * us;
+    const double eL = L.E * L.srho, eR = R.E * R.srho;
+    const double bb = Fb[1] * us + Fb[2] * (L.v2 + R.v2) + Fb[3] * (L.v3 + R.v3) + Fb[4] * (eL + eR);
+    const double rsb = 0.25 * Fb[0] * us + 0.125 * bb * us;
+    const double usb = 0.25 * Fb[0] * rs + Fb[1] * b + 0.125 * bb * rs + 0.25 * Fb[4] * (L.p + R.p);
+    Lb.rho += rsb; Rb.rho += rsb;
+    Lb.v1 += usb; Rb.v1 += usb;
+    Lb.v2 += Fb[2] * b; Rb.v2 += Fb[2] * b;
+    Lb.v3 += Fb[3] * b; Rb.v3 += Fb[3] * b;
+    Lb.E += Fb[4] * b * L.srho; Lb.srho += Fb[4] * b * L.E;
+    Rb.E += Fb[4] * b * R.srho; Rb.srho += Fb[4] * b * R.E;
+    Lb.p += 0.5 * Fb[1] + 0.25 * Fb[4] * us; Rb.p += 0.5 * Fb[1] + 0.25 * Fb[4] * us;
+  } else {  // MO
+    const double mL = L.rho * L.v1, mR = R.rho * R.v1, ms = mL + mR;
+    const double kL = L.v1 * L.v1 + L.v2 * L.v2 + L.v3 * L.v3, kR = R.v1 * R.v1 + R.v2 * R.v2 + R.v3 * R.v3;
+    const double rhoepL = L.E - 0.5 * L.rho * kL + L.p, rhoepR = R.E - 0.5 * R.rho * kR + R.p;
+    const double vv = L.v1 * R.v1 + L.v2 * R.v2 + L.v3 * R.v3;
+    const double msb = 0.5 * Fb[0] + 0.25 * (Fb[1] * (L.v1 + R.v1) + Fb[2] * (L.v2 + R.v2) + Fb[3] * (L.v3 + R.v3) + Fb[4] * vv);
+    const double q = 0.25 * ms;
+    Lb.v1 += q * Fb[1]; Rb.v1 += q * Fb[1];
+    Lb.v2 += q * Fb[2]; Rb.v2 += q * Fb[2];
+    Lb.v3 += q * Fb[3]; Rb.v3 += q * Fb[3];
+    Lb.p += 0.5 * Fb[1]; Rb.p += 0.5 * Fb[1];
+    const double vvb = q * Fb[4];
+    Lb.v1 += vvb * R.v1; Rb.v1 += vvb * L.v1;
+    Lb.v2 += vvb * R.v2; Rb.v2 += vvb * L.v2;
+    Lb.v3 += vvb * R.v3; Rb.v3 += vvb * L.v3;
+    // F4's (rho e + p) v1 / 2 terms, rho e + p = E - rho |v|^2 / 2 + p
+    const double eLb = 0.5 * Fb[4] * L.v1, eRb = 0.5 * Fb[4] * R.v1;
+    Lb.v1 += 0.5 * Fb[4] * rhoepL; Rb.v1 += 0.5 * Fb[4] * rhoepR;
+    Lb.E += eLb; Lb.p += eLb; Lb.rho -= 0.5 * eLb * kL;
+    Lb.v1 -= eLb * L.rho * L.v1; Lb.v2 -= eLb * L.rho * L.v2; Lb.v3 -= eLb * L.rho * L.v3;
+    Rb.E += eRb; Rb.p += eRb; Rb.rho -= 0.5 * eRb * kR;
+    Rb.v1 -= eRb * R.rho * R.v1; Rb.v2 -= eRb * R.rho * R.v2; Rb.v3 -= eRb * R.rho * R.v3;
+    // ms = rho_L v1_L + rho_R v1_R
+    Lb.rho += msb * L.v1; Lb.v1 += msb * L.rho;
+    Rb.rho += msb * R.v1; Rb.v1 += msb * R.rho;
+  }
+}
+
+// the split form's central surface flux transposed: PI / SD (split_surface_flux_adj) or MO, DU, KG
+FG_HD void central_flux_adj(int sd, const RotState& L, const RotState& R, double HL, double HR, const double* Fb, RotState& Lb, RotState& Rb,
+                            double& HLb, double& HRb) {
+  if (sd == SPLIT_PI || sd == SPLIT_SD) split_surface_flux_adj(sd, L, R, HL, HR, Fb, Lb, Rb, HLb, HRb);
+  else split_surface_flux_more_adj(sd, L, R, Fb, Lb, Rb);
+}
+
 // ---- the Riemann solvers of riemann_rotated_more: HLL, HLLE, HLLEM, RoeL2, RoeEntropyGShockFix, the flux average ----
 
 // transposed Roe averages (square-root-density weights of v1..v3 and H; rc = sqrt(kappaM1 (rH - absVel/2)), absVel =
@@ -533,11 +598,24 @@ FG_HD void roe_dissipation_adj(const double* Db, const double* A, double e0, dou
 }
 
 // Transposed Jacobian of riemann_rotated_more for HLL, HLLE, HLLEM (riemann.f90:1067-1235), RoeL2 (:983) and
-// RoeEntropyGShockFix (:866) with the weak form or the split forms PI / SD, and of the flux average (:1236) with PI / SD;
-// LF, HLLC, Roe and RoeEntropyFix go to riemann_rotated_adj. Fb[5] given, adds to the bars of both rotated states.
+// RoeEntropyGShockFix (:866) with the weak form or the split forms SD, PI, MO, DU, KG, of the flux average (:1236) with
+// those split forms, and of LF, HLLC, Roe and RoeEntropyFix (riemann_rotated_adj) with MO, DU, KG. Fb[5] given, adds to
+// the bars of both rotated states.
 FG_HD void riemann_rotated_more_adj(int solver, int splitDG, const Basis& B, const RotState& L, const RotState& R, const double* Fb,
                                     RotState& Lb, RotState& Rb) {
   if (solver == RIEMANN_LF || solver == RIEMANN_HLLC || solver == RIEMANN_ROE || solver == RIEMANN_ROEENTROPYFIX) {
+    if (splitDG >= 0 && splitDG != SPLIT_PI && splitDG != SPLIT_SD && solver != RIEMANN_HLLC) {
+      // central part MO / DU / KG: F = central - dissipation/2, the weak form's F = (F_L + F_R)/2 - the same dissipation/2,
+      // so the transpose is the weak form's, minus that of (F_L + F_R)/2, plus that of the central flux (HLLC has no
+      // central part)
+      riemann_rotated_adj(solver, -1, B, L, R, Fb, Lb, Rb);
+      double Fh[5];
+      for (int v = 0; v < 5; ++v) Fh[v] = -0.5 * Fb[v];
+      euler_flux_1d_adj(L, Fh, Lb);
+      euler_flux_1d_adj(R, Fh, Rb);
+      split_surface_flux_more_adj(splitDG, L, R, Fb, Lb, Rb);
+      return;
+    }
     riemann_rotated_adj(solver, splitDG, B, L, R, Fb, Lb, Rb);
     return;
   }
@@ -545,7 +623,7 @@ FG_HD void riemann_rotated_more_adj(int solver, int splitDG, const Basis& B, con
   const double HL = (L.E + L.p) * L.srho, HR = (R.E + R.p) * R.srho;
   double HLb = 0.0, HRb = 0.0;
   if (solver == RIEMANN_AVERAGE) {
-    split_surface_flux_adj(splitDG, L, R, HL, HR, Fb, Lb, Rb, HLb, HRb);
+    central_flux_adj(splitDG, L, R, HL, HR, Fb, Lb, Rb, HLb, HRb);
     enthalpy_adj(L, HLb, Lb);
     enthalpy_adj(R, HRb, Rb);
     return;
@@ -648,7 +726,7 @@ FG_HD void riemann_rotated_more_adj(int solver, int splitDG, const Basis& B, con
     euler_flux_1d_adj(L, Fh, Lb);
     euler_flux_1d_adj(R, Fh, Rb);
   } else {
-    split_surface_flux_adj(splitDG, L, R, HL, HR, Fb, Lb, Rb, HLb, HRb);
+    central_flux_adj(splitDG, L, R, HL, HR, Fb, Lb, Rb, HLb, HRb);
   }
   double Db[5];
   for (int v = 0; v < 5; ++v) Db[v] = -0.5 * Fb[v];
@@ -846,6 +924,88 @@ FG_HD void split_inputs_to_face_adj(bool pi, double E, double p, double srho, co
     fb[FS_P] += qb[4] + qb[5];
     fb[FS_E] += qb[5];
   }
+}
+
+// split_node_inputs transposed (SD, PI, MO, DU, KG): given the bars qb[6] of (q0, u, v, w, q4, q5), adds the bars of the
+// point's rho, u, v, w, p, E and 1/rho, each an independent input
+FG_HD void split_node_inputs_adj(int sd, double rho, double u, double v, double w, double p, double E, double srho, const double* qb,
+                                 double& rhob, double& ub, double& vb, double& wb, double& pb, double& Eb, double& srhob) {
+  rhob += qb[0];
+  ub += qb[1]; vb += qb[2]; wb += qb[3];
+  switch (sd) {
+    case SPLIT_PI: pb += 4.0 * qb[4] + qb[5] * srho; Eb += qb[5] * srho; srhob += qb[5] * (E + p); break;
+    case SPLIT_DU: pb += 2.0 * qb[4] + qb[5]; Eb += qb[5]; break;
+    case SPLIT_KG: pb += 4.0 * qb[4]; Eb += qb[5] * srho; srhob += qb[5] * E; break;
+    case SPLIT_MO:  // q4 = 2p, q5 = 2 (E - rho |v|^2 / 2 + p)
+      pb += 2.0 * qb[4] + 2.0 * qb[5]; Eb += 2.0 * qb[5];
+      rhob -= qb[5] * (u * u + v * v + w * w);
+      ub -= 2.0 * qb[5] * rho * u; vb -= 2.0 * qb[5] * rho * v; wb -= 2.0 * qb[5] * rho * w;
+      break;
+    default: pb += qb[4] + qb[5]; Eb += qb[5]; break;  // SD
+  }
+}
+
+// split_pair_flux_gen transposed (SD, PI, MO, DU, KG): given Gb[5], adds the bars of both nodes' inputs
+// (q0, u, v, w, q4, q5); the metric sum ms is not an input
+FG_HD void split_pair_flux_gen_adj(int sd, const double* qa, const double* qb, const double* ms, const double* Gb, double* qab, double* qbb) {
+  if (sd == SPLIT_PI || sd == SPLIT_SD) {
+    split_pair_flux_adj(sd == SPLIT_PI, qa, qb, ms, Gb, qab, qbb);
+    return;
+  }
+  const double us = qa[1] + qb[1], vs = qa[2] + qb[2], ws = qa[3] + qb[3];
+  const double qs = us * ms[0] + vs * ms[1] + ws * ms[2];
+  const double psb0 = Gb[1] * ms[0] + Gb[2] * ms[1] + Gb[3] * ms[2];
+  double usb = 0.0, vsb = 0.0, wsb = 0.0;
+  if (sd == SPLIT_DU) {
+    // G0 = (ra + rb) qs, G1..3 = (ra u_a + rb u_b)_c qs + ps ms_c, G4 = (ha + hb) qs
+    const double Rs = qa[0] + qb[0], Hs = qa[5] + qb[5];
+    const double M[3] = {qa[0] * qa[1] + qb[0] * qb[1], qa[0] * qa[2] + qb[0] * qb[2], qa[0] * qa[3] + qb[0] * qb[3]};
+    const double qsb = Gb[0] * Rs + Gb[1] * M[0] + Gb[2] * M[1] + Gb[3] * M[2] + Gb[4] * Hs;
+    const double Rb = Gb[0] * qs, Hsb = Gb[4] * qs;
+    qab[0] += Rb; qbb[0] += Rb;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const double Mb = Gb[1 + c] * qs;
+      qab[0] += Mb * qa[1 + c]; qbb[0] += Mb * qb[1 + c];
+      qab[1 + c] += Mb * qa[0]; qbb[1 + c] += Mb * qb[0];
+    }
+    qab[4] += psb0; qbb[4] += psb0;
+    qab[5] += Hsb; qbb[5] += Hsb;
+    usb = qsb * ms[0]; vsb = qsb * ms[1]; wsb = qsb * ms[2];
+  } else if (sd == SPLIT_KG) {
+    // A = (ra + rb) qs; G0 = A, G1..3 = A (u_a + u_b)_c + ps ms_c, G4 = A (ha + hb) + ps qs / 2
+    const double Rs = qa[0] + qb[0], A = Rs * qs, Hs = qa[5] + qb[5], ps = qa[4] + qb[4];
+    const double Ab = Gb[0] + Gb[1] * us + Gb[2] * vs + Gb[3] * ws + Gb[4] * Hs;
+    usb = Gb[1] * A; vsb = Gb[2] * A; wsb = Gb[3] * A;
+    const double Hsb = Gb[4] * A;
+    const double psb = psb0 + Gb[4] * 0.5 * qs;
+    const double qsb = Ab * Rs + Gb[4] * 0.5 * ps;
+    const double Rb = Ab * qs;
+    usb += qsb * ms[0]; vsb += qsb * ms[1]; wsb += qsb * ms[2];
+    qab[0] += Rb; qbb[0] += Rb;
+    qab[4] += psb; qbb[4] += psb;
+    qab[5] += Hsb; qbb[5] += Hsb;
+  } else {  // MO: qn = u . ms per node, mq = ra qn_a + rb qn_b; G0 = mq, G1..3 = mq (u_a + u_b)_c + ps ms_c,
+            // G4 = ha qn_a + hb qn_b + mq (u_a . u_b)
+    const double qna = qa[1] * ms[0] + qa[2] * ms[1] + qa[3] * ms[2], qnb = qb[1] * ms[0] + qb[2] * ms[1] + qb[3] * ms[2];
+    const double mq = qa[0] * qna + qb[0] * qnb;
+    const double vv = qa[1] * qb[1] + qa[2] * qb[2] + qa[3] * qb[3];
+    const double mqb = Gb[0] + Gb[1] * us + Gb[2] * vs + Gb[3] * ws + Gb[4] * vv;
+    usb = Gb[1] * mq; vsb = Gb[2] * mq; wsb = Gb[3] * mq;
+    const double vvb = Gb[4] * mq;
+    qab[5] += Gb[4] * qna; qbb[5] += Gb[4] * qnb;
+    const double qnab = Gb[4] * qa[5] + mqb * qa[0], qnbb = Gb[4] * qb[5] + mqb * qb[0];
+    qab[0] += mqb * qna; qbb[0] += mqb * qnb;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      qab[1 + c] += vvb * qb[1 + c] + qnab * ms[c];
+      qbb[1 + c] += vvb * qa[1 + c] + qnbb * ms[c];
+    }
+    qab[4] += psb0; qbb[4] += psb0;
+  }
+  qab[1] += usb; qbb[1] += usb;
+  qab[2] += vsb; qbb[2] += vsb;
+  qab[3] += wsb; qbb[3] += wsb;
 }
 
 // the entropy-variable transforms of k_prep, in place on one point (the adjoint's linearisation point)

@@ -144,6 +144,34 @@ void fgpt_split_inputs_adj(int pi, const double* x, const double* qb, double* xb
   split_inputs_to_face_adj(pi != 0, x[1], x[5], x[6], qb, fb);
   xb[0] = fb[FS_RHO]; xb[1] = fb[FS_E]; xb[2] = fb[FS_U]; xb[3] = fb[FS_V]; xb[4] = fb[FS_W]; xb[5] = fb[FS_P]; xb[6] = fb[FS_SRHO];
 }
+// the general split fluxes (SD, PI, MO, DU, KG) as the GEN kernels form them: pair flux of two nodes' inputs
+// x = (q0, u, v, w, q4, q5) x 2 with metric sum ms; node inputs from x = (rho, E, u, v, w, p, srho); surface flux
+void fgpt_split_pair_gen(int sd, const double* x, const double* ms, double* G) {
+  const Basis B = gas(1.4, 1.0);
+  split_pair_flux_gen(sd, B, x[0], x[1], x[2], x[3], x[4], x[5], x[6], x[7], x[8], x[9], x[10], x[11], ms[0], ms[1], ms[2], G);
+}
+void fgpt_split_pair_gen_adj(int sd, const double* x, const double* ms, const double* Gb, double* xb) {
+  for (int c = 0; c < 12; ++c) xb[c] = 0.0;
+  split_pair_flux_gen_adj(sd, x, x + 6, ms, Gb, xb, xb + 6);
+}
+void fgpt_split_node_inputs(int sd, const double* x, double* q) {
+  q[1] = x[2]; q[2] = x[3]; q[3] = x[4];
+  split_node_inputs(sd, x[0], x[2], x[3], x[4], x[5], x[1], x[6], q[0], q[4], q[5]);
+}
+void fgpt_split_node_inputs_adj(int sd, const double* x, const double* qb, double* xb) {
+  for (int c = 0; c < 7; ++c) xb[c] = 0.0;
+  split_node_inputs_adj(sd, x[0], x[2], x[3], x[4], x[5], x[1], x[6], qb, xb[0], xb[2], xb[3], xb[4], xb[5], xb[1], xb[6]);
+}
+void fgpt_split_surface_more(int sd, const double* L, const double* Rr, double* F) {
+  const Basis B = gas(1.4, 1.0);
+  split_surface_flux_more(sd, B, rs(L), rs(Rr), F);
+}
+void fgpt_split_surface_more_adj(int sd, const double* L, const double* Rr, const double* Fb, double* Lb, double* Rb) {
+  RotState lb, rb;
+  rot_zero(lb); rot_zero(rb);
+  split_surface_flux_more_adj(sd, rs(L), rs(Rr), Fb, lb, rb);
+  rs_out(lb, Lb); rs_out(rb, Rb);
+}
 // ConsToEntropy / EntropyToCons of k_prep and their adjoints
 void fgpt_cons_to_entropy(double kappa, const double* U, double* W) {
   const Basis B = gas(kappa, 1.0);

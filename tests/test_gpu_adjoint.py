@@ -1,7 +1,7 @@
 """Adjoint of the right-hand side (fg_vjp_time_derivative) against the oracle's Jacobian-vector products.
 
-Cases: the weak form and the split forms PI and SD on Gauss-Lobatto nodes (the shuffle-pair kernel for PI on lines
-of 2, 4 or 8 nodes, the per-node kernel otherwise) and on Gauss nodes (entropy-variable prolongation and split-Gauss
+Cases: the weak form and the split forms SD, PI, MO, DU, KG on Gauss-Lobatto nodes (the shuffle-pair kernel for PI on
+lines of 2, 4 or 8 nodes, the per-node kernel otherwise) and on Gauss nodes (entropy-variable prolongation and split-Gauss
 surface term transposed), every supported Riemann solver (all of riemann.f90 but the split form's CH and IR surface
 fluxes), BR1/BR2, both overintegration types, walls.
 
@@ -60,6 +60,15 @@ CASES = {
     "gl7_split_pi_avg_br2": (dict(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="avg", Lifting="br2"), "tgv"),
     "gauss3_split_sd_avg_br1": (dict(N=3, NodeType="gauss", SplitDG="sd", Riemann="avg", Lifting="br1"), "tgv"),
     "channel_gauss3_weak_hlle_br2": (dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="hlle", Lifting="br2"), "channel"),
+    # the split fluxes MO, DU, KG (per-node kernel; on Gauss nodes with the entropy-variable prolongation) with the surface
+    # fluxes of both kernel variants
+    "gl3_split_mo_roe_br1": (dict(N=3, NodeType="gauss-lobatto", SplitDG="mo", Riemann="roe", Lifting="br1"), "tgv"),
+    "gl4_split_du_lf_br2": (dict(N=4, NodeType="gauss-lobatto", SplitDG="du", Riemann="lf", Lifting="br2"), "tgv"),
+    "gl7_split_kg_hllc_br2": (dict(N=7, NodeType="gauss-lobatto", SplitDG="kg", Riemann="hllc", Lifting="br2"), "tgv"),
+    "gauss3_split_kg_roeef_br1": (dict(N=3, NodeType="gauss", SplitDG="kg", Riemann="roeentropyfix", Lifting="br1"), "tgv"),
+    "gauss4_split_du_avg_br1": (dict(N=4, NodeType="gauss", SplitDG="du", Riemann="avg", Lifting="br1"), "tgv"),
+    "gl3_split_mo_roel2_br2": (dict(N=3, NodeType="gauss-lobatto", SplitDG="mo", Riemann="roel2", Lifting="br2"), "tgv"),
+    "channel_gauss3_split_mo_hll_br1": (dict(N=3, NodeType="gauss", SplitDG="mo", Riemann="hll", Lifting="br1"), "channel"),
     "channel_gauss3_weak_roe_br1": (dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="roe", Lifting="br1"), "channel"),
     "channel_gauss3_split_pi_roe_br2": (dict(N=3, NodeType="gauss", SplitDG="pi", Riemann="roe", Lifting="br2"), "channel"),
     "channel_gl7_split_pi_roe_br1": (dict(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roe", Lifting="br1"), "channel"),
@@ -157,10 +166,10 @@ def test_vjp_rejects_ch_and_ir_surface_fluxes():
 
 
 def test_vjp_rejects_unsupported():
-    c = make_config(N=3, NodeType="gauss-lobatto", SplitDG="kg", Riemann="hllc")
+    c = make_config(N=3, NodeType="gauss-lobatto", SplitDG="ch", Riemann="hllc")
     f = Flexi(c, fmesh.tgv_box(2))
     f.U = testcases.tgv_state(f.elem_xgp(), mach=0.1)
-    with pytest.raises(Exception, match="split forms PI and SD"):
+    with pytest.raises(Exception, match="split forms SD, PI, MO, DU and KG"):
         f.vjp_time_derivative(np.zeros(f.ushape))
 
 
