@@ -303,7 +303,7 @@ int fg_set_elem_mu_scale(fg_handle* h, const double* scale);
  * J V by finite differences, implicit.f90:MatrixVector). t is unused (the exact-function source does not
  * depend on U; the LSERK adjoint recomputes its steps at the forward's stage times). The bulk velocity of a
  * channel body force is held fixed.
- * Supported: weak form and the split forms PI and SD on Gauss and Gauss-Lobatto nodes (on Gauss nodes with the
+ * Supported: weak form and the split forms SD, PI, MO, DU and KG on Gauss and Gauss-Lobatto nodes (on Gauss nodes with the
  * transposed entropy-variable prolongation and split-Gauss surface term), N <= 7, every Riemann solver but the split
  * form's CH and IR surface fluxes (LF, HLLC, Roe, RoeEntropyFix, RoeL2, RoeEntropyGShockFix, HLL, HLLE, HLLEM, the flux
  * average), strong BR1/BR2 lifting, both overintegration types (the transposed filter), walls 3/4, mortar interfaces
