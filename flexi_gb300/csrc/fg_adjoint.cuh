@@ -405,7 +405,8 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_split_adj(Dev d, AdjD
 // line sum T_v = sum_a C_v(a) ubar_v(a). The node takes the node share of each G_k; one thread per face point
 // sums the face-state share over its line into a.faceVolb (k_prep_adj adds it to the face cotangent).
 // -----------------------------------------------------------------------------------------------------
-template <int n, bool GL>
+// LM: the split forms CH and IR (logarithmic means), in a variant of their own
+template <int n, bool GL, bool LM = false>
 __global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_split_gen_adj(Dev d, AdjDev a, Basis B) {
   using S = Shape<n>;
   constexpr int n2 = S::n2, n3 = S::n3, EPB = S::EPB, N = n - 1;
@@ -526,7 +527,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_split_gen_adj(Dev d, 
         Gb[0] = sC[bI * n + aI] * uba[0] + sC[aI * n + bI] * Ub[xb];
 #pragma unroll
         for (int v = 1; v < 5; ++v) Gb[v] = sC[n2 + bI * n + aI] * uba[v] + sC[n2 + aI * n + bI] * Ub[v * n3 + xb];
-        split_pair_flux_gen_adj(sd, qa, qb, ms, Gb, qbar, dummy);
+        split_pair_flux_gen_adj<LM>(sd, B, qa, qb, ms, Gb, qbar, dummy);
       }
       if (!GL) {
         const int fo = dir == 0 ? j + n * k : (dir == 1 ? i + n * k : i + n * j);
@@ -545,7 +546,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_split_gen_adj(Dev d, 
           double Gb[5];
 #pragma unroll
           for (int v = 0; v < 5; ++v) Gb[v] = leg * T[v] - cs * (v == 0 ? f0 : f1) * uba[v];
-          split_pair_flux_gen_adj(sd, qa, qf, ms, Gb, qbar, dummy);
+          split_pair_flux_gen_adj<LM>(sd, B, qa, qf, ms, Gb, qbar, dummy);
         }
       }
     }
@@ -633,7 +634,7 @@ __global__ void __launch_bounds__(Shape<n>::THREADS) k_vol_split_gen_adj(Dev d, 
         double Gb[5];
 #pragma unroll
         for (int v = 0; v < 5; ++v) Gb[v] = leg * T[v] - cs * (v == 0 ? f0 : f1) * Ub[v * n3 + xn];
-        split_pair_flux_gen_adj(sd, qn, qf, ms, Gb, dummy, qfb);
+        split_pair_flux_gen_adj<LM>(sd, B, qn, qf, ms, Gb, dummy, qfb);
       }
       const double* src = (flip == 0 ? d.faceM : d.faceS) + (size_t)s * FS_NF * n2 + pq;
       double fb[FS_NF];

@@ -14,6 +14,34 @@ namespace fg {
 
 FG_HD double sgn1(double x) { return x >= 0.0 ? 1.0 : -1.0; }
 
+// log_mean transposed (splitflux.f90:GetLogMean, the branch the forward took): given the bar Lb of the mean of a and b,
+// adds the bars of a and b
+FG_HD void log_mean_adj(double a, double b, double Lb, double& ab, double& bb) {
+  const double chi = a / b;
+  const double f = (chi - 1.0) / (chi + 1.0);
+  double g, gu = 0.0;  // g and, on the series branch, dg/du
+  const bool series = fabs(f) < 0.1;
+  const double u = f * f;
+  if (series) {
+    g = 2.0 + u * ((2.0 / 3.0) + u * (0.4 + u * (2.0 / 7.0)));
+    gu = (2.0 / 3.0) + u * (0.8 + u * (6.0 / 7.0));
+  } else {
+    g = log(chi) / f;
+  }
+  const double sb = Lb / g;                // bar of a + b
+  const double gb = -Lb * (a + b) / (g * g);
+  double fb = 0.0, chib = 0.0;
+  if (series) {
+    fb = gb * gu * 2.0 * f;
+  } else {
+    chib = gb / (chi * f);
+    fb = -gb * log(chi) / (f * f);
+  }
+  chib += fb * 2.0 / ((chi + 1.0) * (chi + 1.0));
+  ab += sb + chib / b;
+  bb += sb - chib * a / (b * b);
+}
+
 // eos.f90:ConsToPrim: (rho, m, E) -> (1/rho, v, p, T). Given the bars of 1/rho, v (3), p, T and direct bars
 // of rho and E (face states store both), accumulates the conservative bars into Ub[5].
 FG_HD void cons_to_prim_adj(const Basis& B, const double* U, double sb, double ub, double vb, double wb, double pb, double Tb,
@@ -469,8 +497,92 @@ FG_HD void riemann_rotated_adj(int solver, int splitDG, const Basis& B, const Ro
 
 // ---- the split fluxes MO, DU and KG (splitflux.f90: SplitVolumeFluxMO :445, DU :225, KG :327 and their surface forms) ----
 
-// split_surface_flux_more transposed for MO, DU, KG on rotated states: Fb[5] given, adds to both states' bars
-FG_HD void split_surface_flux_more_adj(int sd, const RotState& L, const RotState& R, const double* Fb, RotState& Lb, RotState& Rb) {
+// IR's means of two states (splitflux.f90:SplitSurfaceFluxIR, riemann.f90:Riemann_IR): z1 = sqrt(rho/p), z5 = sqrt(rho p)
+struct IRMeans {
+  double zL1, zL5, zR1, zR5, z1Log, z5Log, z1s, rhoHat, pHat, p2Hat, uH, vH, wH;
+};
+FG_HD IRMeans ir_means(const Basis& B, const RotState& L, const RotState& R) {
+  IRMeans m;
+  m.zL1 = sqrt(L.rho / L.p); m.zL5 = sqrt(L.rho * L.p); m.zR1 = sqrt(R.rho / R.p); m.zR5 = sqrt(R.rho * R.p);
+  m.z1Log = log_mean(m.zL1, m.zR1); m.z5Log = log_mean(m.zL5, m.zR5);
+  m.z1s = m.zL1 + m.zR1;
+  m.rhoHat = 0.5 * m.z1s * m.z5Log;
+  m.pHat = (m.zL5 + m.zR5) / m.z1s;
+  m.p2Hat = 0.5 / B.kappa * ((B.kappa + 1.0) * m.z5Log / m.z1Log + B.kappaM1 * m.pHat);
+  m.uH = (m.zL1 * L.v1 + m.zR1 * R.v1) / m.z1s;
+  m.vH = (m.zL1 * L.v2 + m.zR1 * R.v2) / m.z1s;
+  m.wH = (m.zL1 * L.v3 + m.zR1 * R.v3) / m.z1s;
+  return m;
+}
+// the means transposed: given the bars of rhoHat, pHat, p2Hat, uH, vH, wH, adds to both states' bars
+FG_HD void ir_means_adj(const Basis& B, const RotState& L, const RotState& R, const IRMeans& m, double rhoHatb, double pHatb, double p2Hatb,
+                        double uHb, double vHb, double wHb, RotState& Lb, RotState& Rb) {
+  double z5Logb = p2Hatb * 0.5 / B.kappa * (B.kappa + 1.0) / m.z1Log;
+  const double z1Logb = -p2Hatb * 0.5 / B.kappa * (B.kappa + 1.0) * m.z5Log / (m.z1Log * m.z1Log);
+  pHatb += p2Hatb * 0.5 * B.kappaM1 / B.kappa;
+  double zL1b = 0.0, zR1b = 0.0, zL5b = pHatb / m.z1s, zR5b = pHatb / m.z1s;
+  double z1sb = -pHatb * m.pHat / m.z1s;
+  zL1b += (uHb * L.v1 + vHb * L.v2 + wHb * L.v3) / m.z1s;
+  zR1b += (uHb * R.v1 + vHb * R.v2 + wHb * R.v3) / m.z1s;
+  Lb.v1 += uHb * m.zL1 / m.z1s; Rb.v1 += uHb * m.zR1 / m.z1s;
+  Lb.v2 += vHb * m.zL1 / m.z1s; Rb.v2 += vHb * m.zR1 / m.z1s;
+  Lb.v3 += wHb * m.zL1 / m.z1s; Rb.v3 += wHb * m.zR1 / m.z1s;
+  z1sb -= (uHb * m.uH + vHb * m.vH + wHb * m.wH) / m.z1s;
+  z1sb += rhoHatb * 0.5 * m.z5Log;
+  z5Logb += rhoHatb * 0.5 * m.z1s;
+  zL1b += z1sb; zR1b += z1sb;
+  log_mean_adj(m.zL1, m.zR1, z1Logb, zL1b, zR1b);
+  log_mean_adj(m.zL5, m.zR5, z5Logb, zL5b, zR5b);
+  // z1 = sqrt(rho / p), z5 = sqrt(rho p)
+  Lb.rho += zL1b * m.zL1 / (2.0 * L.rho) + zL5b * m.zL5 / (2.0 * L.rho);
+  Lb.p += -zL1b * m.zL1 / (2.0 * L.p) + zL5b * m.zL5 / (2.0 * L.p);
+  Rb.rho += zR1b * m.zR1 / (2.0 * R.rho) + zR5b * m.zR5 / (2.0 * R.rho);
+  Rb.p += -zR1b * m.zR1 / (2.0 * R.p) + zR5b * m.zR5 / (2.0 * R.p);
+}
+
+// split_surface_flux_more transposed for MO, DU, KG, CH, IR on rotated states: Fb[5] given, adds to both states' bars
+FG_HD void split_surface_flux_more_adj(int sd, const Basis& B, const RotState& L, const RotState& R, const double* Fb, RotState& Lb,
+                                       RotState& Rb) {
+  if (sd == SPLIT_CH) {
+    const double bL = 0.5 * L.rho / L.p, bR = 0.5 * R.rho / R.p;
+    const double rhoLog = log_mean(L.rho, R.rho), betaLog = log_mean(bL, bR);
+    const double pHat = 0.5 * (L.rho + R.rho) / (bL + bR);
+    const double H = 0.5 * B.sKappaM1 / betaLog + pHat / rhoLog + 0.5 * (L.v1 * R.v1 + L.v2 * R.v2 + L.v3 * R.v3);
+    const double us = L.v1 + R.v1;
+    const double F0 = rhoLog * 0.5 * us;
+    const double F0b = Fb[0] + Fb[1] * 0.5 * us + Fb[2] * 0.5 * (L.v2 + R.v2) + Fb[3] * 0.5 * (L.v3 + R.v3) + Fb[4] * H;
+    const double usb = Fb[1] * F0 * 0.5 + F0b * rhoLog * 0.5;
+    Lb.v1 += usb; Rb.v1 += usb;
+    Lb.v2 += Fb[2] * F0 * 0.5; Rb.v2 += Fb[2] * F0 * 0.5;
+    Lb.v3 += Fb[3] * F0 * 0.5; Rb.v3 += Fb[3] * F0 * 0.5;
+    const double Hb = Fb[4] * F0;
+    const double pHatb = Fb[1] + Hb / rhoLog;
+    const double rhoLogb = F0b * 0.5 * us - Hb * pHat / (rhoLog * rhoLog);
+    const double betaLogb = -Hb * 0.5 * B.sKappaM1 / (betaLog * betaLog);
+    Lb.v1 += 0.5 * Hb * R.v1; Rb.v1 += 0.5 * Hb * L.v1;
+    Lb.v2 += 0.5 * Hb * R.v2; Rb.v2 += 0.5 * Hb * L.v2;
+    Lb.v3 += 0.5 * Hb * R.v3; Rb.v3 += 0.5 * Hb * L.v3;
+    Lb.rho += pHatb * 0.5 / (bL + bR); Rb.rho += pHatb * 0.5 / (bL + bR);
+    double bLb = -pHatb * pHat / (bL + bR), bRb = bLb;
+    log_mean_adj(L.rho, R.rho, rhoLogb, Lb.rho, Rb.rho);
+    log_mean_adj(bL, bR, betaLogb, bLb, bRb);
+    Lb.rho += bLb * 0.5 / L.p; Lb.p -= bLb * 0.5 * L.rho / (L.p * L.p);
+    Rb.rho += bRb * 0.5 / R.p; Rb.p -= bRb * 0.5 * R.rho / (R.p * R.p);
+    return;
+  }
+  if (sd == SPLIT_IR) {
+    const IRMeans m = ir_means(B, L, R);
+    const double hH = B.kappa * m.p2Hat / (m.rhoHat * B.kappaM1) + 0.5 * (m.uH * m.uH + m.vH * m.vH + m.wH * m.wH);
+    const double F0 = m.rhoHat * m.uH;
+    const double F0b = Fb[0] + Fb[1] * m.uH + Fb[2] * m.vH + Fb[3] * m.wH + Fb[4] * hH;
+    const double hHb = Fb[4] * F0;
+    const double uHb = Fb[1] * F0 + F0b * m.rhoHat + hHb * m.uH;
+    const double vHb = Fb[2] * F0 + hHb * m.vH, wHb = Fb[3] * F0 + hHb * m.wH;
+    const double p2Hatb = hHb * B.kappa / (m.rhoHat * B.kappaM1);
+    const double rhoHatb = F0b * m.uH - hHb * B.kappa * m.p2Hat / (m.rhoHat * m.rhoHat * B.kappaM1);
+    ir_means_adj(B, L, R, m, rhoHatb, Fb[1], p2Hatb, uHb, vHb, wHb, Lb, Rb);
+    return;
+  }
   if (sd == SPLIT_DU) {
     const double us = L.v1 + R.v1;
     const double mL = L.rho * L.v1, mR = R.rho * R.v1;
@@ -525,11 +637,11 @@ FG_HD void split_surface_flux_more_adj(int sd, const RotState& L, const RotState
   }
 }
 
-// the split form's central surface flux transposed: PI / SD (split_surface_flux_adj) or MO, DU, KG
-FG_HD void central_flux_adj(int sd, const RotState& L, const RotState& R, double HL, double HR, const double* Fb, RotState& Lb, RotState& Rb,
-                            double& HLb, double& HRb) {
+// the split form's central surface flux transposed: PI / SD (split_surface_flux_adj) or MO, DU, KG, CH, IR
+FG_HD void central_flux_adj(int sd, const Basis& B, const RotState& L, const RotState& R, double HL, double HR, const double* Fb, RotState& Lb,
+                            RotState& Rb, double& HLb, double& HRb) {
   if (sd == SPLIT_PI || sd == SPLIT_SD) split_surface_flux_adj(sd, L, R, HL, HR, Fb, Lb, Rb, HLb, HRb);
-  else split_surface_flux_more_adj(sd, L, R, Fb, Lb, Rb);
+  else split_surface_flux_more_adj(sd, B, L, R, Fb, Lb, Rb);
 }
 
 // ---- the Riemann solvers of riemann_rotated_more: HLL, HLLE, HLLEM, RoeL2, RoeEntropyGShockFix, the flux average ----
@@ -598,9 +710,9 @@ FG_HD void roe_dissipation_adj(const double* Db, const double* A, double e0, dou
 }
 
 // Transposed Jacobian of riemann_rotated_more for HLL, HLLE, HLLEM (riemann.f90:1067-1235), RoeL2 (:983) and
-// RoeEntropyGShockFix (:866) with the weak form or the split forms SD, PI, MO, DU, KG, of the flux average (:1236) with
-// those split forms, and of LF, HLLC, Roe and RoeEntropyFix (riemann_rotated_adj) with MO, DU, KG. Fb[5] given, adds to
-// the bars of both rotated states.
+// RoeEntropyGShockFix (:866) with the weak form or any split form, of the split form's flux average (:1236), CH (:1261) and
+// IR (:1315) surface fluxes, and of LF, HLLC, Roe and RoeEntropyFix (riemann_rotated_adj) with MO, DU, KG, CH, IR. Fb[5]
+// given, adds to the bars of both rotated states.
 FG_HD void riemann_rotated_more_adj(int solver, int splitDG, const Basis& B, const RotState& L, const RotState& R, const double* Fb,
                                     RotState& Lb, RotState& Rb) {
   if (solver == RIEMANN_LF || solver == RIEMANN_HLLC || solver == RIEMANN_ROE || solver == RIEMANN_ROEENTROPYFIX) {
@@ -613,7 +725,7 @@ FG_HD void riemann_rotated_more_adj(int solver, int splitDG, const Basis& B, con
       for (int v = 0; v < 5; ++v) Fh[v] = -0.5 * Fb[v];
       euler_flux_1d_adj(L, Fh, Lb);
       euler_flux_1d_adj(R, Fh, Rb);
-      split_surface_flux_more_adj(splitDG, L, R, Fb, Lb, Rb);
+      split_surface_flux_more_adj(splitDG, B, L, R, Fb, Lb, Rb);
       return;
     }
     riemann_rotated_adj(solver, splitDG, B, L, R, Fb, Lb, Rb);
@@ -623,12 +735,139 @@ FG_HD void riemann_rotated_more_adj(int solver, int splitDG, const Basis& B, con
   const double HL = (L.E + L.p) * L.srho, HR = (R.E + R.p) * R.srho;
   double HLb = 0.0, HRb = 0.0;
   if (solver == RIEMANN_AVERAGE) {
-    central_flux_adj(splitDG, L, R, HL, HR, Fb, Lb, Rb, HLb, HRb);
+    central_flux_adj(splitDG, B, L, R, HL, HR, Fb, Lb, Rb, HLb, HRb);
     enthalpy_adj(L, HLb, Lb);
     enthalpy_adj(R, HRb, Rb);
     return;
   }
   const double cL = sqrt(B.kappa * L.p * L.srho), cR = sqrt(B.kappa * R.p * R.srho);
+  if (solver == RIEMANN_CH) {
+    // F = central - (lmax / 2) (dU_0..3, X4), X4 = drho T1 + rhoMean T2 + rhoMean sKappaM1 (1/bR - 1/bL) / 2,
+    // T1 = sKappaM1 / (2 betaLog) + vL . vR / 2, T2 = (|vR|^2 - |vL|^2) / 2, b = rho / (2p)
+    central_flux_adj(splitDG, B, L, R, HL, HR, Fb, Lb, Rb, HLb, HRb);
+    const double aL = fabs(L.v1), aR = fabs(R.v1);
+    const double lmax = fmax(aR, aL) + fmax(cL, cR), h = 0.5 * lmax;
+    const double rhoMean = 0.5 * (L.rho + R.rho);
+    const double bL = 0.5 * L.rho / L.p, bR = 0.5 * R.rho / R.p;
+    const double betaLog = log_mean(bL, bR);
+    const double dU[4] = {R.rho - L.rho, R.rho * R.v1 - L.rho * L.v1, R.rho * R.v2 - L.rho * L.v2, R.rho * R.v3 - L.rho * L.v3};
+    const double T1 = 0.5 * B.sKappaM1 / betaLog + 0.5 * (R.v1 * L.v1 + R.v2 * L.v2 + R.v3 * L.v3);
+    const double T2 = 0.5 * (L.v1 + R.v1) * (R.v1 - L.v1) + 0.5 * (L.v2 + R.v2) * (R.v2 - L.v2) + 0.5 * (L.v3 + R.v3) * (R.v3 - L.v3);
+    const double X4 = dU[0] * T1 + rhoMean * T2 + 0.5 * rhoMean * B.sKappaM1 * (1.0 / bR - 1.0 / bL);
+    double hb = 0.0, dUb[5] = {0., 0., 0., 0., 0.};
+    for (int v = 0; v < 4; ++v) { hb -= Fb[v] * dU[v]; dUb[v] = -h * Fb[v]; }
+    hb -= Fb[4] * X4;
+    const double X4b = -h * Fb[4];
+    dUb[0] += X4b * T1;
+    const double T1b = X4b * dU[0], T2b = X4b * rhoMean;
+    const double rhoMeanb = X4b * (T2 + 0.5 * B.sKappaM1 * (1.0 / bR - 1.0 / bL));
+    double bLb = X4b * 0.5 * rhoMean * B.sKappaM1 / (bL * bL), bRb = -X4b * 0.5 * rhoMean * B.sKappaM1 / (bR * bR);
+    const double betaLogb = -T1b * 0.5 * B.sKappaM1 / (betaLog * betaLog);
+    Rb.v1 += 0.5 * T1b * L.v1 + T2b * R.v1; Lb.v1 += 0.5 * T1b * R.v1 - T2b * L.v1;
+    Rb.v2 += 0.5 * T1b * L.v2 + T2b * R.v2; Lb.v2 += 0.5 * T1b * R.v2 - T2b * L.v2;
+    Rb.v3 += 0.5 * T1b * L.v3 + T2b * R.v3; Lb.v3 += 0.5 * T1b * R.v3 - T2b * L.v3;
+    log_mean_adj(bL, bR, betaLogb, bLb, bRb);
+    Lb.rho += bLb * 0.5 / L.p + 0.5 * rhoMeanb; Lb.p -= bLb * 0.5 * L.rho / (L.p * L.p);
+    Rb.rho += bRb * 0.5 / R.p + 0.5 * rhoMeanb; Rb.p -= bRb * 0.5 * R.rho / (R.p * R.p);
+    jump_adj(L, R, dUb, Lb, Rb);
+    const double lb = 0.5 * hb;
+    if (aR >= aL) Rb.v1 += lb * sgn1(R.v1); else Lb.v1 += lb * sgn1(L.v1);
+    if (cL >= cR) sound_speed_adj(B, L, cL, lb, Lb); else sound_speed_adj(B, R, cR, lb, Rb);
+    enthalpy_adj(L, HLb, Lb);
+    enthalpy_adj(R, HRb, Rb);
+    return;
+  }
+  if (solver == RIEMANN_IR) {
+    // F = central - Dd/2, Dd = R |Lambda| T R^T vJ with the jump vJ of the entropy variables and the eigenvectors at IR's means
+    central_flux_adj(splitDG, B, L, R, HL, HR, Fb, Lb, Rb, HLb, HRb);
+    const double sR = log(R.p) - B.kappa * log(R.rho), sL = log(L.p) - B.kappa * log(L.rho);
+    const double rpR = R.rho / R.p, rpL = L.rho / L.p;
+    const double kR = R.v1 * R.v1 + R.v2 * R.v2 + R.v3 * R.v3, kL = L.v1 * L.v1 + L.v2 * L.v2 + L.v3 * L.v3;
+    double vJ[5];
+    vJ[0] = ((B.kappa - sR) - (B.kappa - sL)) * B.sKappaM1 - 0.5 * (rpR * kR - rpL * kL);
+    vJ[1] = rpR * R.v1 - rpL * L.v1;
+    vJ[2] = rpR * R.v2 - rpL * L.v2;
+    vJ[3] = rpR * R.v3 - rpL * L.v3;
+    vJ[4] = rpL - rpR;
+    const IRMeans m = ir_means(B, L, R);
+    const double uH = m.uH, vH = m.vH, wH = m.wH, rhoHat = m.rhoHat, pHat = m.pHat, p2Hat = m.p2Hat;
+    const double aH = sqrt(B.kappa * p2Hat / rhoHat);
+    const double ek = 0.5 * (uH * uH + vH * vH + wH * wH);
+    const double hH = B.kappa * p2Hat / (rhoHat * B.kappaM1) + ek;
+    const double c0 = vJ[0] + (uH - aH) * vJ[1] + vH * vJ[2] + wH * vJ[3] + (hH - uH * aH) * vJ[4];
+    const double c1 = vJ[0] + uH * vJ[1] + vH * vJ[2] + wH * vJ[3] + ek * vJ[4];
+    const double c2 = vJ[2] + vH * vJ[4];
+    const double c3 = vJ[3] + wH * vJ[4];
+    const double c4 = vJ[0] + (uH + aH) * vJ[1] + vH * vJ[2] + wH * vJ[3] + (hH + uH * aH) * vJ[4];
+    const double am = uH - aH, ap = uH + aH;
+    const double Am = fabs(am), Ap = fabs(ap), Au = fabs(uH);
+    const double d0 = 0.5 * Am * rhoHat / B.kappa * c0;
+    const double d1 = Au * (B.kappaM1 / B.kappa) * rhoHat * c1;
+    const double d2 = Au * pHat * c2;
+    const double d3 = Au * pHat * c3;
+    const double d4 = 0.5 * Ap * rhoHat / B.kappa * c4;
+    const double sum014 = d0 + d1 + d4;
+    double Ddb[5];
+    for (int v = 0; v < 5; ++v) Ddb[v] = -0.5 * Fb[v];
+    // Dd0 = sum014, Dd1 = (uH - aH) d0 + uH d1 + (uH + aH) d4, Dd2 = vH sum014 + d2, Dd3 = wH sum014 + d3,
+    // Dd4 = (hH - uH aH) d0 + ek d1 + vH d2 + wH d3 + (hH + uH aH) d4
+    const double sumb = Ddb[0] + Ddb[2] * vH + Ddb[3] * wH;
+    const double d0b = sumb + Ddb[1] * am + Ddb[4] * (hH - uH * aH);
+    const double d1b = sumb + Ddb[1] * uH + Ddb[4] * ek;
+    const double d4b = sumb + Ddb[1] * ap + Ddb[4] * (hH + uH * aH);
+    const double d2b = Ddb[2] + Ddb[4] * vH, d3b = Ddb[3] + Ddb[4] * wH;
+    double uHb = Ddb[1] * (d0 + d1 + d4) + Ddb[4] * aH * (d4 - d0);
+    double aHb = Ddb[1] * (d4 - d0) + Ddb[4] * uH * (d4 - d0);
+    double vHb = Ddb[2] * sum014 + Ddb[4] * d2;
+    double wHb = Ddb[3] * sum014 + Ddb[4] * d3;
+    double hHb = Ddb[4] * (d0 + d4);
+    double ekb = Ddb[4] * d1;
+    // d_k
+    const double Amb = d0b * 0.5 * rhoHat / B.kappa * c0, Apb = d4b * 0.5 * rhoHat / B.kappa * c4;
+    const double Aub = d1b * (B.kappaM1 / B.kappa) * rhoHat * c1 + (d2b * c2 + d3b * c3) * pHat;
+    double rhoHatb = d0b * 0.5 * Am / B.kappa * c0 + d1b * Au * (B.kappaM1 / B.kappa) * c1 + d4b * 0.5 * Ap / B.kappa * c4;
+    double pHatb = Au * (d2b * c2 + d3b * c3);
+    const double c0b = d0b * 0.5 * Am * rhoHat / B.kappa, c1b = d1b * Au * (B.kappaM1 / B.kappa) * rhoHat;
+    const double c2b = d2b * Au * pHat, c3b = d3b * Au * pHat, c4b = d4b * 0.5 * Ap * rhoHat / B.kappa;
+    const double amb = Amb * sgn1(am), apb = Apb * sgn1(ap);
+    uHb += amb + apb + Aub * sgn1(uH);
+    aHb += apb - amb;
+    // c_k
+    double vJb[5];
+    vJb[0] = c0b + c1b + c4b;
+    vJb[1] = c0b * am + c1b * uH + c4b * ap;
+    vJb[2] = c0b * vH + c1b * vH + c2b + c4b * vH;
+    vJb[3] = c0b * wH + c1b * wH + c3b + c4b * wH;
+    vJb[4] = c0b * (hH - uH * aH) + c1b * ek + c2b * vH + c3b * wH + c4b * (hH + uH * aH);
+    uHb += c0b * (vJ[1] - aH * vJ[4]) + c1b * vJ[1] + c4b * (vJ[1] + aH * vJ[4]);
+    aHb += c0b * (-vJ[1] - uH * vJ[4]) + c4b * (vJ[1] + uH * vJ[4]);
+    vHb += (c0b + c1b + c4b) * vJ[2] + c2b * vJ[4];
+    wHb += (c0b + c1b + c4b) * vJ[3] + c3b * vJ[4];
+    hHb += (c0b + c4b) * vJ[4];
+    ekb += c1b * vJ[4];
+    // hH = kappa p2Hat / (rhoHat kappaM1) + ek, ek = |uH|^2 / 2, aH = sqrt(kappa p2Hat / rhoHat)
+    double p2Hatb = hHb * B.kappa / (rhoHat * B.kappaM1);
+    rhoHatb -= hHb * B.kappa * p2Hat / (rhoHat * rhoHat * B.kappaM1);
+    ekb += hHb;
+    uHb += ekb * uH; vHb += ekb * vH; wHb += ekb * wH;
+    const double rb = aHb / (2.0 * aH);
+    p2Hatb += rb * B.kappa / rhoHat;
+    rhoHatb -= rb * B.kappa * p2Hat / (rhoHat * rhoHat);
+    ir_means_adj(B, L, R, m, rhoHatb, pHatb, p2Hatb, uHb, vHb, wHb, Lb, Rb);
+    // vJ
+    const double sLb = vJb[0] * B.sKappaM1, sRb = -vJb[0] * B.sKappaM1;
+    const double rpRb = -0.5 * vJb[0] * kR + vJb[1] * R.v1 + vJb[2] * R.v2 + vJb[3] * R.v3 - vJb[4];
+    const double rpLb = 0.5 * vJb[0] * kL - vJb[1] * L.v1 - vJb[2] * L.v2 - vJb[3] * L.v3 + vJb[4];
+    Rb.v1 += -vJb[0] * rpR * R.v1 + vJb[1] * rpR; Lb.v1 += vJb[0] * rpL * L.v1 - vJb[1] * rpL;
+    Rb.v2 += -vJb[0] * rpR * R.v2 + vJb[2] * rpR; Lb.v2 += vJb[0] * rpL * L.v2 - vJb[2] * rpL;
+    Rb.v3 += -vJb[0] * rpR * R.v3 + vJb[3] * rpR; Lb.v3 += vJb[0] * rpL * L.v3 - vJb[3] * rpL;
+    // s = ln p - kappa ln rho, rp = rho / p
+    Rb.p += sRb / R.p - rpRb * R.rho / (R.p * R.p); Rb.rho += -sRb * B.kappa / R.rho + rpRb / R.p;
+    Lb.p += sLb / L.p - rpLb * L.rho / (L.p * L.p); Lb.rho += -sLb * B.kappa / L.rho + rpLb / L.p;
+    enthalpy_adj(L, HLb, Lb);
+    enthalpy_adj(R, HRb, Rb);
+    return;
+  }
   double FL[5], FR[5];
   euler_flux_1d(L, FL);
   euler_flux_1d(R, FR);
@@ -726,7 +965,7 @@ FG_HD void riemann_rotated_more_adj(int solver, int splitDG, const Basis& B, con
     euler_flux_1d_adj(L, Fh, Lb);
     euler_flux_1d_adj(R, Fh, Rb);
   } else {
-    central_flux_adj(splitDG, L, R, HL, HR, Fb, Lb, Rb, HLb, HRb);
+    central_flux_adj(splitDG, B, L, R, HL, HR, Fb, Lb, Rb, HLb, HRb);
   }
   double Db[5];
   for (int v = 0; v < 5; ++v) Db[v] = -0.5 * Fb[v];
@@ -926,13 +1165,20 @@ FG_HD void split_inputs_to_face_adj(bool pi, double E, double p, double srho, co
   }
 }
 
-// split_node_inputs transposed (SD, PI, MO, DU, KG): given the bars qb[6] of (q0, u, v, w, q4, q5), adds the bars of the
+// split_node_inputs transposed (every split form): given the bars qb[6] of (q0, u, v, w, q4, q5), adds the bars of the
 // point's rho, u, v, w, p, E and 1/rho, each an independent input
 FG_HD void split_node_inputs_adj(int sd, double rho, double u, double v, double w, double p, double E, double srho, const double* qb,
                                  double& rhob, double& ub, double& vb, double& wb, double& pb, double& Eb, double& srhob) {
-  rhob += qb[0];
   ub += qb[1]; vb += qb[2]; wb += qb[3];
+  if (sd == SPLIT_IR) {  // q0 = sqrt(rho / p), q4 = sqrt(rho p)
+    const double z1 = sqrt(rho / p), z5 = sqrt(rho * p);
+    rhob += qb[0] * z1 / (2.0 * rho) + qb[4] * z5 / (2.0 * rho);
+    pb += -qb[0] * z1 / (2.0 * p) + qb[4] * z5 / (2.0 * p);
+    return;
+  }
+  rhob += qb[0];
   switch (sd) {
+    case SPLIT_CH: rhob += qb[4] * 0.5 / p; pb -= qb[4] * 0.5 * rho / (p * p); break;  // q4 = rho / (2p)
     case SPLIT_PI: pb += 4.0 * qb[4] + qb[5] * srho; Eb += qb[5] * srho; srhob += qb[5] * (E + p); break;
     case SPLIT_DU: pb += 2.0 * qb[4] + qb[5]; Eb += qb[5]; break;
     case SPLIT_KG: pb += 4.0 * qb[4]; Eb += qb[5] * srho; srhob += qb[5] * E; break;
@@ -945,9 +1191,12 @@ FG_HD void split_node_inputs_adj(int sd, double rho, double u, double v, double 
   }
 }
 
-// split_pair_flux_gen transposed (SD, PI, MO, DU, KG): given Gb[5], adds the bars of both nodes' inputs
-// (q0, u, v, w, q4, q5); the metric sum ms is not an input
-FG_HD void split_pair_flux_gen_adj(int sd, const double* qa, const double* qb, const double* ms, const double* Gb, double* qab, double* qbb) {
+// split_pair_flux_gen transposed: given Gb[5], adds the bars of both nodes' inputs (q0, u, v, w, q4, q5); the metric sum ms
+// is not an input. LM: CH and IR too (their logarithmic means); without it SD, PI, MO, DU, KG only, which keeps the
+// volume adjoint's registers for those forms where they were
+template <bool LM = true>
+FG_HD void split_pair_flux_gen_adj(int sd, const Basis& B, const double* qa, const double* qb, const double* ms, const double* Gb, double* qab,
+                                   double* qbb) {
   if (sd == SPLIT_PI || sd == SPLIT_SD) {
     split_pair_flux_adj(sd == SPLIT_PI, qa, qb, ms, Gb, qab, qbb);
     return;
@@ -956,7 +1205,71 @@ FG_HD void split_pair_flux_gen_adj(int sd, const double* qa, const double* qb, c
   const double qs = us * ms[0] + vs * ms[1] + ws * ms[2];
   const double psb0 = Gb[1] * ms[0] + Gb[2] * ms[1] + Gb[3] * ms[2];
   double usb = 0.0, vsb = 0.0, wsb = 0.0;
-  if (sd == SPLIT_DU) {
+  if (LM && sd == SPLIT_CH) {
+    // q4 = beta = rho / (2p); rhoLog, betaLog the logarithmic means, pHat = (ra + rb) / (2 (beta_a + beta_b)),
+    // H = sKappaM1 / (2 betaLog) + pHat / rhoLog + (u_a . u_b) / 2, A = rhoLog qs; G0 = A, G1..3 = A/2 (u_a + u_b)_c + 2 pHat ms_c,
+    // G4 = A H
+    const double rhoLog = log_mean(qa[0], qb[0]), betaLog = log_mean(qa[4], qb[4]);
+    const double Rs = qa[0] + qb[0], Bs = qa[4] + qb[4];
+    const double pHat = 0.5 * Rs / Bs;
+    const double H = 0.5 * B.sKappaM1 / betaLog + pHat / rhoLog + 0.5 * (qa[1] * qb[1] + qa[2] * qb[2] + qa[3] * qb[3]);
+    const double A = rhoLog * qs;
+    const double Ab = Gb[0] + Gb[4] * H + 0.5 * (Gb[1] * us + Gb[2] * vs + Gb[3] * ws);
+    usb = 0.5 * Gb[1] * A; vsb = 0.5 * Gb[2] * A; wsb = 0.5 * Gb[3] * A;
+    const double Hb = Gb[4] * A;
+    double pHatb = 2.0 * psb0 + Hb / rhoLog;
+    const double rhoLogb = Ab * qs - Hb * pHat / (rhoLog * rhoLog);
+    const double betaLogb = -Hb * 0.5 * B.sKappaM1 / (betaLog * betaLog);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) { qab[1 + c] += 0.5 * Hb * qb[1 + c]; qbb[1 + c] += 0.5 * Hb * qa[1 + c]; }
+    const double qsb = Ab * rhoLog;
+    usb += qsb * ms[0]; vsb += qsb * ms[1]; wsb += qsb * ms[2];
+    qab[0] += pHatb * 0.5 / Bs; qbb[0] += pHatb * 0.5 / Bs;
+    qab[4] -= pHatb * pHat / Bs; qbb[4] -= pHatb * pHat / Bs;
+    log_mean_adj(qa[0], qb[0], rhoLogb, qab[0], qbb[0]);
+    log_mean_adj(qa[4], qb[4], betaLogb, qab[4], qbb[4]);
+  } else if (LM && sd == SPLIT_IR) {
+    // q0 = z1 = sqrt(rho / p), q4 = z5 = sqrt(rho p); rhoHat = (z1a + z1b) z5Log / 2, pHat = (z5a + z5b) / (z1a + z1b),
+    // p2Hat = ((kappa + 1) z5Log / z1Log + kappaM1 pHat) / (2 kappa), uH = (z1a u_a + z1b u_b) / (z1a + z1b),
+    // hH = kappa p2Hat / (rhoHat kappaM1) + |uH|^2 / 2, A = rhoHat uH . ms; G0 = A, G1..3 = A uH_c + pHat ms_c, G4 = A hH
+    const double z1Log = log_mean(qa[0], qb[0]), z5Log = log_mean(qa[4], qb[4]);
+    const double z1s = qa[0] + qb[0];
+    const double rhoHat = 0.5 * z1s * z5Log;
+    const double pHat = (qa[4] + qb[4]) / z1s;
+    const double p2Hat = 0.5 / B.kappa * ((B.kappa + 1.0) * z5Log / z1Log + B.kappaM1 * pHat);
+    double uH[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) uH[c] = (qa[0] * qa[1 + c] + qb[0] * qb[1 + c]) / z1s;
+    const double hH = B.kappa * p2Hat / (rhoHat * B.kappaM1) + 0.5 * (uH[0] * uH[0] + uH[1] * uH[1] + uH[2] * uH[2]);
+    const double qH = uH[0] * ms[0] + uH[1] * ms[1] + uH[2] * ms[2];
+    const double A = rhoHat * qH;
+    const double Ab = Gb[0] + Gb[1] * uH[0] + Gb[2] * uH[1] + Gb[3] * uH[2] + Gb[4] * hH;
+    double uHb[3] = {Gb[1] * A, Gb[2] * A, Gb[3] * A};
+    double pHatb = psb0;
+    const double hHb = Gb[4] * A;
+    double p2Hatb = hHb * B.kappa / (rhoHat * B.kappaM1);
+    double rhoHatb = -hHb * B.kappa * p2Hat / (rhoHat * rhoHat * B.kappaM1) + Ab * qH;
+    const double qHb = Ab * rhoHat;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) uHb[c] += hHb * uH[c] + qHb * ms[c];
+    double z5Logb = p2Hatb * 0.5 / B.kappa * (B.kappa + 1.0) / z1Log;
+    double z1Logb = -p2Hatb * 0.5 / B.kappa * (B.kappa + 1.0) * z5Log / (z1Log * z1Log);
+    pHatb += p2Hatb * 0.5 * B.kappaM1 / B.kappa;
+    double z1sb = -pHatb * pHat / z1s;
+    qab[4] += pHatb / z1s; qbb[4] += pHatb / z1s;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      qab[0] += uHb[c] * qa[1 + c] / z1s; qbb[0] += uHb[c] * qb[1 + c] / z1s;
+      qab[1 + c] += uHb[c] * qa[0] / z1s; qbb[1 + c] += uHb[c] * qb[0] / z1s;
+      z1sb -= uHb[c] * uH[c] / z1s;
+    }
+    z1sb += rhoHatb * 0.5 * z5Log;
+    z5Logb += rhoHatb * 0.5 * z1s;
+    qab[0] += z1sb; qbb[0] += z1sb;
+    log_mean_adj(qa[0], qb[0], z1Logb, qab[0], qbb[0]);
+    log_mean_adj(qa[4], qb[4], z5Logb, qab[4], qbb[4]);
+    return;
+  } else if (sd == SPLIT_DU) {
     // G0 = (ra + rb) qs, G1..3 = (ra u_a + rb u_b)_c qs + ps ms_c, G4 = (ha + hb) qs
     const double Rs = qa[0] + qb[0], Hs = qa[5] + qb[5];
     const double M[3] = {qa[0] * qa[1] + qb[0] * qb[1], qa[0] * qa[2] + qb[0] * qb[2], qa[0] * qa[3] + qb[0] * qb[3]};

@@ -1003,16 +1003,11 @@ void set_error_without_handle(const char* msg) { g_err = msg; }
 
 namespace {
 
-// the adjoint kernels cover: weak form and split forms SD, PI, MO, DU, KG (Gauss, Gauss-Lobatto), every Riemann solver but
-// CH and IR, BR1/BR2
+// the adjoint kernels cover: the weak form and every split form (Gauss, Gauss-Lobatto), every Riemann solver, strong
+// non-conservative BR1/BR2 lifting, N <= 7
 const char* adjoint_unsupported(const fg_config& c) {
   if (c.N > 7) return "the adjoint supports N = 1..7";
-  if (c.Riemann == FG_RIEMANN_CH || c.Riemann == FG_RIEMANN_IR)
-    return "the adjoint supports the Riemann solvers LF, HLLC, Roe, RoeEntropyFix, RoeL2, RoeEntropyGShockFix, HLL, HLLE, HLLEM and "
-           "the flux average (not CH or IR)";
   if (c.doWeakLifting || c.doConservativeLifting) return "the adjoint supports the strong, non-conservative lifting";
-  if (c.SplitDG == FG_SPLIT_CH || c.SplitDG == FG_SPLIT_IR)
-    return "the adjoint supports the weak form and the split forms SD, PI, MO, DU and KG (not CH or IR)";
   return nullptr;
 }
 

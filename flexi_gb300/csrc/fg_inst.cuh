@@ -99,6 +99,7 @@ struct Inst {
       set_smem(k_lift_adj<n, GL>, smem_lift_adj());
       set_smem(k_prep_adj<n, GL>, smem_prep_adj());
       set_smem(k_vol_split_gen_adj<n, GL>, smem_split_gen_adj());
+      set_smem(k_vol_split_gen_adj<n, GL, true>, smem_split_gen_adj());
       set_smem(k_lift_adj<n, GL, true>, smem_lift_mortar_adj());
       set_smem(k_mortar_face_adj<n>, smem_mortar_face_adj());
       set_smem(k_mortar_pre_adj<n>, smem_mortar_pre_adj());
@@ -122,7 +123,8 @@ struct Inst {
       }
     }
     if constexpr (ADJ) {
-      if (B.splitDG >= 0) k_vol_split_gen_adj<n, GL><<<blocks(d), S::THREADS, smem_split_gen_adj(), st>>>(d, a, B);
+      if (B.splitDG == SPLIT_CH || B.splitDG == SPLIT_IR) k_vol_split_gen_adj<n, GL, true><<<blocks(d), S::THREADS, smem_split_gen_adj(), st>>>(d, a, B);
+      else if (B.splitDG >= 0) k_vol_split_gen_adj<n, GL><<<blocks(d), S::THREADS, smem_split_gen_adj(), st>>>(d, a, B);
       else k_vol_weak_adj<n, GL><<<blocks(d), S::THREADS, smem_weak_adj(), st>>>(d, a, B);
     }
   }

@@ -152,7 +152,8 @@ void fgpt_split_pair_gen(int sd, const double* x, const double* ms, double* G) {
 }
 void fgpt_split_pair_gen_adj(int sd, const double* x, const double* ms, const double* Gb, double* xb) {
   for (int c = 0; c < 12; ++c) xb[c] = 0.0;
-  split_pair_flux_gen_adj(sd, x, x + 6, ms, Gb, xb, xb + 6);
+  const Basis B = gas(1.4, 1.0);
+  split_pair_flux_gen_adj(sd, B, x, x + 6, ms, Gb, xb, xb + 6);
 }
 void fgpt_split_node_inputs(int sd, const double* x, double* q) {
   q[1] = x[2]; q[2] = x[3]; q[3] = x[4];
@@ -169,7 +170,8 @@ void fgpt_split_surface_more(int sd, const double* L, const double* Rr, double* 
 void fgpt_split_surface_more_adj(int sd, const double* L, const double* Rr, const double* Fb, double* Lb, double* Rb) {
   RotState lb, rb;
   rot_zero(lb); rot_zero(rb);
-  split_surface_flux_more_adj(sd, rs(L), rs(Rr), Fb, lb, rb);
+  const Basis B = gas(1.4, 1.0);
+  split_surface_flux_more_adj(sd, B, rs(L), rs(Rr), Fb, lb, rb);
   rs_out(lb, Lb); rs_out(rb, Rb);
 }
 // ConsToEntropy / EntropyToCons of k_prep and their adjoints

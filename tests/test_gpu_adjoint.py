@@ -1,9 +1,8 @@
 """Adjoint of the right-hand side (fg_vjp_time_derivative) against the oracle's Jacobian-vector products.
 
-Cases: the weak form and the split forms SD, PI, MO, DU, KG on Gauss-Lobatto nodes (the shuffle-pair kernel for PI on
-lines of 2, 4 or 8 nodes, the per-node kernel otherwise) and on Gauss nodes (entropy-variable prolongation and split-Gauss
-surface term transposed), every supported Riemann solver (all of riemann.f90 but the split form's CH and IR surface
-fluxes), BR1/BR2, both overintegration types, walls.
+Cases: the weak form and every split form (SD, PI, MO, DU, KG, CH, IR) on Gauss-Lobatto nodes (the shuffle-pair kernel
+for PI on lines of 2, 4 or 8 nodes, the per-node kernel otherwise) and on Gauss nodes (entropy-variable prolongation and split-Gauss
+surface term transposed), every Riemann solver of riemann.f90, BR1/BR2, both overintegration types, walls.
 
 Dot-product test <J V, W> = <V, J^T W>: J V comes from the oracle, exactly by its dual-number
 instantiation of the restated algorithm and approximately by the matrix-free finite difference of the
@@ -69,6 +68,13 @@ CASES = {
     "gauss4_split_du_avg_br1": (dict(N=4, NodeType="gauss", SplitDG="du", Riemann="avg", Lifting="br1"), "tgv"),
     "gl3_split_mo_roel2_br2": (dict(N=3, NodeType="gauss-lobatto", SplitDG="mo", Riemann="roel2", Lifting="br2"), "tgv"),
     "channel_gauss3_split_mo_hll_br1": (dict(N=3, NodeType="gauss", SplitDG="mo", Riemann="hll", Lifting="br1"), "channel"),
+    # the entropy-conserving split fluxes CH and IR (logarithmic means) and the CH and IR surface fluxes
+    "gl3_split_ch_ch_br1": (dict(N=3, NodeType="gauss-lobatto", SplitDG="ch", Riemann="ch", Lifting="br1"), "tgv"),
+    "gl4_split_ir_roeef_br2": (dict(N=4, NodeType="gauss-lobatto", SplitDG="ir", Riemann="roeentropyfix", Lifting="br2"), "tgv"),
+    "gl7_split_ch_lf_br2": (dict(N=7, NodeType="gauss-lobatto", SplitDG="ch", Riemann="lf", Lifting="br2"), "tgv"),
+    "gauss3_split_ir_ir_br1": (dict(N=3, NodeType="gauss", SplitDG="ir", Riemann="ir", Lifting="br1"), "tgv"),
+    "gauss4_split_pi_ir_br2": (dict(N=4, NodeType="gauss", SplitDG="pi", Riemann="ir", Lifting="br2"), "tgv"),
+    "gl3_split_mo_ch_br1": (dict(N=3, NodeType="gauss-lobatto", SplitDG="mo", Riemann="ch", Lifting="br1"), "tgv"),
     "channel_gauss3_weak_roe_br1": (dict(N=3, NodeType="gauss", SplitDG="weak", Riemann="roe", Lifting="br1"), "channel"),
     "channel_gauss3_split_pi_roe_br2": (dict(N=3, NodeType="gauss", SplitDG="pi", Riemann="roe", Lifting="br2"), "channel"),
     "channel_gl7_split_pi_roe_br1": (dict(N=7, NodeType="gauss-lobatto", SplitDG="pi", Riemann="roe", Lifting="br1"), "channel"),
@@ -155,21 +161,11 @@ def test_viscosity_multiplier_cotangent(name):
     assert abs(float(mub @ ds) - rich) <= 1e-8 * abs(rich), (float(mub @ ds), rich)
 
 
-def test_vjp_rejects_ch_and_ir_surface_fluxes():
-    for riemann in ("ch", "ir"):
-        c = make_config(N=3, NodeType="gauss-lobatto", SplitDG="pi", Riemann=riemann)
-        f = Flexi(c, fmesh.tgv_box(2))
-        f.U = testcases.tgv_state(f.elem_xgp(), mach=0.1)
-        with pytest.raises(Exception, match="not CH or IR"):
-            f.vjp_time_derivative(np.zeros(f.ushape))
-        f.close()
-
-
 def test_vjp_rejects_unsupported():
-    c = make_config(N=3, NodeType="gauss-lobatto", SplitDG="ch", Riemann="hllc")
+    c = make_config(N=3, NodeType="gauss", SplitDG="weak", Riemann="roe", doWeakLifting=1)
     f = Flexi(c, fmesh.tgv_box(2))
     f.U = testcases.tgv_state(f.elem_xgp(), mach=0.1)
-    with pytest.raises(Exception, match="split forms SD, PI, MO, DU and KG"):
+    with pytest.raises(Exception, match="strong, non-conservative lifting"):
         f.vjp_time_derivative(np.zeros(f.ushape))
 
 
