@@ -303,10 +303,10 @@ int fg_set_elem_mu_scale(fg_handle* h, const double* scale);
  * J V by finite differences, implicit.f90:MatrixVector). t is unused (the exact-function source does not
  * depend on U; the LSERK adjoint recomputes its steps at the forward's stage times). The bulk velocity of a
  * channel body force is held fixed.
- * Supported: weak form and the split forms SD, PI, MO, DU and KG on Gauss and Gauss-Lobatto nodes (on Gauss nodes with the
- * transposed entropy-variable prolongation and split-Gauss surface term), N <= 7, every Riemann solver but the split
- * form's CH and IR surface fluxes (LF, HLLC, Roe, RoeEntropyFix, RoeL2, RoeEntropyGShockFix, HLL, HLLE, HLLEM, the flux
- * average), strong BR1/BR2 lifting, both overintegration types (the transposed filter), walls 3/4, mortar interfaces
+ * Supported: weak form and every split form (SD, PI, MO, DU, KG, CH, IR) on Gauss and Gauss-Lobatto nodes (on Gauss nodes
+ * with the transposed entropy-variable prolongation and split-Gauss surface term), N <= 7, every Riemann solver (LF, HLLC,
+ * Roe, RoeEntropyFix, RoeL2, RoeEntropyGShockFix, HLL, HLLE, HLLEM; with the split form the flux average, CH and IR),
+ * strong BR1/BR2 lifting, both overintegration types (the transposed filter), walls 3/4, mortar interfaces
  * (transposed U_Mortar and Flux_Mortar, fillmortar.t90). */
 int fg_vjp_time_derivative(fg_handle* h, double t, const double* W, double* V, double* muScaleBar);
 
